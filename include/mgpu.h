@@ -1,0 +1,163 @@
+/*
+ * mgpu.h -- C ABI of the GB300 time-marching library for Multall-open 18.3.
+ *
+ * The library replaces the numeric body of SUBROUTINE LOOP
+ * (multall-open-18.3.f:3664-5463): per step it recovers the primitive
+ * variables, forms the mass / energy / momentum face fluxes, calls the
+ * SCREE/SSS update TSTEP five times (multigrid, negative feedback, corner
+ * scatter, SMOOTH_VAR, periodic / tip-gap / mixing-plane averaging), applies
+ * the inlet and exit boundary conditions, the density and Mach limiters and
+ * NEW_MIXPLAN, runs LOSS every NLOS steps and, every 5 steps, the convergence
+ * monitors and STEPUP.  All flow-field arrays stay resident on one GPU.
+ *
+ * Reference call site replaced: `CALL LOOP` at multall-open-18.3.f:137.  The
+ * reference has no FFI of its own: LOOP takes no arguments and exchanges all
+ * data through COMMON blocks (commall-open-18.3:13-203).  This ABI therefore
+ * binds arrays and scalars BY THEIR COMMON NAMES: a Fortran ISO_C_BINDING
+ * shim passes `C_LOC(AQX)` under the name "AQX" and so on, once, after
+ * SETUP.  Arrays are passed packed, Fortran order, I fastest:
+ *   3-D node/cell arrays  A(I,J,K)  -> IM*JM*KM values
+ *   2-D meridional        A(J,K)    -> JM*KM
+ *   2-D pitch/span        A(I,K)    -> IM*KM      (FBL, FBR, FTL, FTR)
+ *   2-D endwall           A(I,J)    -> IM*JM      (YPLUS_K1, YPLUS_KM)
+ *   per-J / per-I / per-K / per-row 1-D arrays of length JM / IM / KM / NROWS
+ *   STEP1(NIB1,NJB1+1,NKB1), STEP2(NIB2,NJB2+1,NKB2), STEPSBK(NSBLK)
+ * A shim on a compiled-in ID/JD/KD layout passes the sections
+ * RO(1:IM,1:JM,1:KM) etc., which gfortran packs on the call.
+ *
+ * Conventions (all entry points):
+ *   - return 0 on success, a negative MGPU_E_* code on failure; the text of
+ *     the last failure on this thread is available from mgpu_last_error();
+ *   - no C++ exception crosses the ABI; nothing here calls exit();
+ *   - one handle = one flow problem = one CUDA stream owned by the handle;
+ *     calls on one handle are not re-entrant, distinct handles are
+ *     independent;
+ *   - host buffers passed in are only read (set_*) or only written (get_*)
+ *     during the call; the library keeps no host pointer.
+ */
+#ifndef MGPU_H_
+#define MGPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MGPU_ABI_VERSION 1
+
+/* status codes */
+#define MGPU_OK              0
+#define MGPU_E_ARG          -1  /* bad argument, unknown name, size mismatch   */
+#define MGPU_E_STATE        -2  /* call out of order (e.g. step before commit) */
+#define MGPU_E_CUDA         -3  /* CUDA runtime error                          */
+#define MGPU_E_UNSUPPORTED  -4  /* an input option this build does not cover   */
+#define MGPU_E_NONFINITE    -5  /* health check: NaN/Inf or RO <= 0 found      */
+#define MGPU_E_NOMEM        -6  /* device allocation failed                    */
+
+typedef struct mgpu_handle mgpu_handle;
+
+/* Per-step monitors, the quantities LOOP prints every 5 steps
+ * (multall-open-18.3.f:5264-5317, 3840-3864, 9000 FORMAT).  Filled by
+ * mgpu_step()/mgpu_run() on steps where the 5-step tail ran (tail_ran=1). */
+typedef struct mgpu_monitors {
+    int32_t nstep;        /* NSTEP of the step these values belong to       */
+    int32_t tail_ran;     /* 1 if the every-5-step tail ran on this step    */
+    int32_t ifend;        /* convergence / NSTEPS_MAX test after this step  */
+    int32_t health;       /* 0 ok, else count of non-finite or RO<=0 nodes  */
+    float   emax;         /* signed max % change of Vm  (EMAX)              */
+    int32_t imax, jmax, kmax;
+    float   eavg;         /* mean |% change of Vm|      (EAVG)              */
+    float   econt;        /* max |1 - CHECK_FLOW(J)/CHECK_FLOW(1)| (ECONT)  */
+    int32_t jcont;
+    float   vref;         /* SQRT(VRMS*RIJKM)           (VREF)              */
+    float   vmax;         /* max relative speed         (VMAX)              */
+    int32_t ivmax, jvmax, kvmax;
+    double  flow_in;      /* BLADE_FLOW(1)  [kg/s]                          */
+    double  flow_out;     /* BLADE_FLOW(JM) [kg/s]                          */
+} mgpu_monitors;
+
+/* Whole-machine performance, EFICOOL with IFCOOL=0
+ * (multall-open-18.3.f:10662-10849, 11253-11394; SUMFLX 7873-7912). */
+typedef struct mgpu_integrals {
+    double mass_flow_in;   /* BLADE_FLOW(J1)                                */
+    double mass_flow_out;  /* BLADE_FLOW(J2M1)                              */
+    double eta_tt;         /* total-to-total isentropic efficiency ETAIS    */
+    double eta_ts;         /* total-to-static efficiency ETATS              */
+    double po_ratio;       /* PORAT = PO2/POIN                              */
+    double to_ratio;       /* TORAT = TO_OUT/TO_IN                          */
+    int32_t j1, j2m1;      /* stations used                                 */
+} mgpu_integrals;
+
+/* ---- library information --------------------------------------------- */
+int32_t mgpu_abi_version(void);
+/* Copies the text of the last error raised on the calling thread. */
+int32_t mgpu_last_error(char *buf, int32_t len);
+/* Number of CUDA devices visible; negative code if the runtime fails. */
+int32_t mgpu_device_count(void);
+
+/* ---- handle lifetime -------------------------------------------------- */
+/* Creates a problem of IM x JM x KM nodes and NROWS blade rows on the
+ * current CUDA device (replaces the COMMON PARAMETER sizing, commall:4-9).
+ * Allocates the device working set. */
+int32_t mgpu_create(int32_t im, int32_t jm, int32_t km, int32_t nrows,
+                    mgpu_handle **out);
+void    mgpu_destroy(mgpu_handle *h);
+
+/* ---- binding COMMON data (before mgpu_commit) -------------------------- */
+/* Integer / real COMMON scalars by name, e.g. "ITIMST", "CFL". */
+int32_t mgpu_set_int(mgpu_handle *h, const char *name, int32_t value);
+int32_t mgpu_set_real(mgpu_handle *h, const char *name, float value);
+/* Copies a packed COMMON array (float32 for REAL, int32 for INTEGER) to
+ * the device.  nbytes must equal the array's packed size.  State arrays
+ * (RO, ROVX, ... ) may also be set after commit, e.g. on restart. */
+int32_t mgpu_set_array(mgpu_handle *h, const char *name,
+                       const void *host, int64_t nbytes);
+/* Copies a packed COMMON array back from the device into host memory. */
+int32_t mgpu_get_array(mgpu_handle *h, const char *name,
+                       void *host, int64_t nbytes);
+/* Reads back a real / integer scalar the loop updates (e.g. "VISLAM"). */
+int32_t mgpu_get_real(mgpu_handle *h, const char *name, float *value);
+int32_t mgpu_get_int(mgpu_handle *h, const char *name, int32_t *value);
+
+/* Validates that every input LOOP reads has been bound, rejects options
+ * outside the covered set with MGPU_E_UNSUPPORTED, derives the tables
+ * LOSS builds on its first call, and performs the LOOP prologue
+ * (multall-open-18.3.f:3677-3709: RO_REF, ROLIM, PLIM, PREFF, SFXIN/SFTIN
+ * scaled by CFL).  NSTEP starts at 0. */
+int32_t mgpu_commit(mgpu_handle *h);
+
+/* ---- the calls SETUP makes into the hot path --------------------------- */
+/* STEPUP(RELAX), multall-open-18.3.f:7916-8002 (SETUP calls it with 1.0 at
+ * 7057, LOOP with 0.25 at 5349).  Valid after commit. */
+int32_t mgpu_stepup(mgpu_handle *h, float relax);
+/* LOSS called from SETUP with RF_VIS=1, FMIXUP=1, NSTEP=1
+ * (multall-open-18.3.f:7350-7357) to initialise the body forces. */
+int32_t mgpu_loss_init(mgpu_handle *h);
+
+/* ---- time marching ----------------------------------------------------- */
+/* One LOOP iteration, multall-open-18.3.f:5000-5240 plus the every-5-step
+ * tail 8000-5438 (monitors, STEPUP; printing is left to the caller).
+ * force_end=1 marks the final step (IFEND): the tail runs whatever NSTEP.
+ * mon may be NULL.  Returns MGPU_E_NONFINITE if the tail's health check
+ * finds a NaN/Inf or a non-positive density. */
+int32_t mgpu_step(mgpu_handle *h, int32_t force_end, mgpu_monitors *mon);
+/* nsteps LOOP iterations launched back to back (CUDA graph replay), no
+ * host synchronisation in between; mon receives the last tail's values.
+ * Stops early, returning 1, if the reference's convergence test
+ * (multall-open-18.3.f:3762-3764) is met at a tail. */
+int32_t mgpu_run(mgpu_handle *h, int32_t nsteps, mgpu_monitors *mon);
+/* Blocks until all work on the handle's stream has finished. */
+int32_t mgpu_sync(mgpu_handle *h);
+/* EFICOOL's mass averages and efficiencies on the current state, computed
+ * on the device with FP64 accumulation. */
+int32_t mgpu_integrals_compute(mgpu_handle *h, mgpu_integrals *out);
+
+/* ---- instrumentation --------------------------------------------------- */
+/* Number of kernel launches one plain (non-tail) step issues. */
+int32_t mgpu_kernels_per_step(mgpu_handle *h, int32_t tail_step);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MGPU_H_ */

@@ -1,0 +1,731 @@
+// mgpu_api.cu -- the C ABI of include/mgpu.h.
+//
+// A handle owns one flow problem on the current CUDA device: every COMMON
+// array of the loop in HBM, the loop's work arrays, one stream and, after
+// the first step, a CUDA graph holding the whole launch sequence of one
+// LOOP iteration.  Arrays are bound by COMMON name (the table in
+// include/mgpu_common_table.h).  No exception crosses the ABI: every entry
+// point catches, records the message for mgpu_last_error() and returns a
+// negative status.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "mgpu_internal.cuh"
+
+using namespace mgpu;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                     \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) return fail(MGPU_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+enum Shape { SH_IJK, SH_JK, SH_IK, SH_IJ, SH_J, SH_I, SH_K, SH_ROW, SH_MG1, SH_MG2, SH_SB };
+enum Role { RO_GEOM, RO_STATE, RO_OUT };
+
+struct ArrayInfo {
+    const char *name;
+    bool is_int;
+    Shape shape;
+    Role role;
+};
+
+#define T_IS_INT_INT32 true
+#define T_IS_INT_FLOAT32 false
+const ArrayInfo kArrays[] = {
+#define MGPU_AINFO(n, t, s, r) {#n, T_IS_INT_##t, SH_##s, RO_##r},
+    MGPU_ARRAYS(MGPU_AINFO)
+};
+const int kNumArrays = sizeof(kArrays) / sizeof(kArrays[0]);
+
+}  // namespace
+
+struct mgpu_handle {
+    Dev d;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    int sm_count = 0;
+    bool committed = false;
+    bool bound[sizeof(kArrays) / sizeof(kArrays[0])] = {};
+    void *dptr[sizeof(kArrays) / sizeof(kArrays[0])] = {};
+    size_t dbytes[sizeof(kArrays) / sizeof(kArrays[0])] = {};
+    std::vector<void *> allocs;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    size_t graph_nodes = 0;
+    double *d_int = nullptr;     // integrals output (4 x JM)
+    DevCtl *h_ctl = nullptr;     // pinned mirror of the control block
+};
+
+namespace {
+
+size_t shape_count(const mgpu_handle *h, Shape s) {
+    const Dev &d = h->d;
+    switch (s) {
+    case SH_IJK: return (size_t)d.IM * d.JM * d.KM;
+    case SH_JK: return (size_t)d.JM * d.KM;
+    case SH_IK: return (size_t)d.IM * d.KM;
+    case SH_IJ: return (size_t)d.IM * d.JM;
+    case SH_J: return d.JM;
+    case SH_I: return d.IM;
+    case SH_K: return d.KM;
+    case SH_ROW: return d.NROWS;
+    case SH_MG1: return (size_t)d.NIB1 * (d.NJB1 + 1) * d.NKB1;
+    case SH_MG2: return (size_t)d.NIB2 * (d.NJB2 + 1) * d.NKB2;
+    case SH_SB: return d.NSBLK;
+    }
+    return 0;
+}
+
+int find_array(const char *name) {
+    for (int a = 0; a < kNumArrays; ++a)
+        if (!strcmp(kArrays[a].name, name)) return a;
+    return -1;
+}
+
+void **dev_slot(Dev &d, const char *name) {
+#define MGPU_SLOT(n, t, s, r) if (!strcmp(name, #n)) return (void **)&d.n;
+    MGPU_ARRAYS(MGPU_SLOT)
+    return nullptr;
+}
+
+template <typename T>
+int dalloc(mgpu_handle *h, T **p, size_t count) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, count * sizeof(T) + 16);
+    if (e != cudaSuccess) return fail(MGPU_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    e = cudaMemset(q, 0, count * sizeof(T) + 16);
+    if (e != cudaSuccess) return fail(MGPU_E_CUDA, std::string("cudaMemset: ") + cudaGetErrorString(e));
+    h->allocs.push_back(q);
+    *p = (T *)q;
+    return 0;
+}
+
+template <typename T>
+int upload(mgpu_handle *h, T *dst, const std::vector<T> &src) {
+    CK(cudaMemcpy(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return 0;
+}
+
+template <typename T>
+int download(mgpu_handle *h, std::vector<T> &dst, const T *src, size_t n) {
+    dst.resize(n);
+    CK(cudaMemcpy(dst.data(), src, n * sizeof(T), cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+// the tables LOSS builds on its first call (multall-open-18.3.f:8123-8189)
+void loss_tables(const Dev &d, const std::vector<float> &FP, const std::vector<float> &FR,
+                 const std::vector<float> &X, const std::vector<float> &R, const std::vector<int> &NBLADE,
+                 const std::vector<int> &JLE, const std::vector<int> &JTE, const std::vector<float> *XL,
+                 std::vector<float> &FILAM, std::vector<float> &FITURB, std::vector<float> &FIWAKE,
+                 std::vector<float> &FIUP, std::vector<float> &FKLAM, std::vector<float> &FKTURB) {
+    const int IM = d.IM, KM = d.KM, IMM1 = d.IMM1, KMM1 = d.KMM1, JM = d.JM, KMID = d.KMID;
+    FILAM.assign((size_t)d.NROWS * IM, 0.f);
+    FITURB = FIWAKE = FIUP = FILAM;
+    FKLAM.assign((size_t)d.NROWS * KM, 0.f);
+    FKTURB = FKLAM;
+    auto fp = [&](int i) { return FP[i - 1]; };
+    auto fr = [&](int k) { return FR[k - 1]; };
+    auto x2 = [&](int j, int k) { return X[(size_t)(j - 1) + (size_t)JM * (k - 1)]; };
+    auto r2 = [&](int j, int k) { return R[(size_t)(j - 1) + (size_t)JM * (k - 1)]; };
+    for (int nrw = 1; nrw <= d.NROWS; ++nrw) {
+        float XI1 = XL[0][nrw - 1], XIM = XL[1][nrw - 1], XK1 = XL[2][nrw - 1], XKM = XL[3][nrw - 1];
+        float XDWN = XL[4][nrw - 1], XUP = XL[5][nrw - 1];
+        auto at = [&](std::vector<float> &v, int i) -> float & { return v[(size_t)(nrw - 1) * IM + i - 1]; };
+        auto atk = [&](std::vector<float> &v, int k) -> float & { return v[(size_t)(nrw - 1) * KM + k - 1]; };
+        float SUMF = 0.0f;
+        for (int i = 2; i <= IMM1; ++i) {
+            SUMF = SUMF + fp(i - 1);
+            float XLIM = XI1 * (1.0f - SUMF) + XIM * SUMF;
+            float FPITCH = SUMF * (1.0f - SUMF);
+            if (FPITCH > XLIM) FPITCH = XLIM;
+            float DF = fp(i) + fp(i - 1);
+            at(FILAM, i) = fp(i) / DF;
+            at(FITURB, i) = 0.16f * FPITCH * FPITCH / (DF * DF);
+            at(FIWAKE, i) = 0.16f * XDWN * XDWN / (DF * DF);
+            at(FIUP, i) = 0.16f * XUP * XUP / (DF * DF);
+        }
+        float DF = fp(1) + fp(IMM1);
+        at(FILAM, 1) = fp(1) / DF;
+        at(FIWAKE, 1) = 0.16f * XDWN * XDWN / (DF * DF);
+        at(FIUP, 1) = 0.16f * XUP * XUP / (DF * DF);
+        at(FITURB, 1) = at(FITURB, 2);
+        at(FILAM, IM) = fp(IMM1) / DF;
+        at(FIWAKE, IM) = 0.16f * XDWN * XDWN / (DF * DF);
+        at(FIUP, IM) = 0.16f * XUP * XUP / (DF * DF);
+        at(FITURB, IM) = at(FITURB, IMM1);
+        float AVGSPAN = 0.0f;
+        int JMID = (int)(0.5f * (float)(JLE[nrw - 1] + JTE[nrw - 1]));
+        for (int k = 2; k <= KM; ++k) {
+            float XDIF = x2(JMID, k) - x2(JMID, k - 1);
+            float RDIF = r2(JMID, k) - r2(JMID, k - 1);
+            AVGSPAN = AVGSPAN + sqrtf(XDIF * XDIF + RDIF * RDIF);
+        }
+        float AVGPIT = 2.0f * 3.1415926f * r2(JMID, KMID) / (float)NBLADE[JMID - 1];
+        float XLIMH = XK1 * AVGPIT / AVGSPAN;
+        float XLIMT = XKM * AVGPIT / AVGSPAN;
+        SUMF = 0.0f;
+        for (int k = 2; k <= KMM1; ++k) {
+            SUMF = SUMF + fr(k - 1);
+            float XLIM = XLIMH * (1.0f - SUMF) + XLIMT * SUMF;
+            float FCSPAN = SUMF * (1.0f - SUMF);
+            if (FCSPAN > XLIM) FCSPAN = XLIM;
+            float DFk = fr(k) + fr(k - 1);
+            atk(FKLAM, k) = fr(k) / DFk;
+            atk(FKTURB, k) = 0.16f * FCSPAN * FCSPAN / (DFk * DFk);
+        }
+    }
+}
+
+// contiguous extent of each block of a 1-based map over [lo, hi]
+int extents(const std::vector<int> &map, int lo, int hi, int nblk, std::vector<int> &s, std::vector<int> &e,
+            const char *what) {
+    s.assign(nblk, 1 << 30);
+    e.assign(nblk, -1);
+    for (int x = lo; x <= hi; ++x) {
+        int b = map[x - 1];
+        if (b < 1 || b > nblk) continue;
+        if (e[b - 1] >= 0 && e[b - 1] != x - 1)
+            return fail(MGPU_E_ARG, std::string("non-contiguous multigrid block in ") + what);
+        if (s[b - 1] > x) s[b - 1] = x;
+        e[b - 1] = x;
+    }
+    for (int b = 0; b < nblk; ++b)
+        if (e[b] < 0) {
+            s[b] = 1;
+            e[b] = 0;
+        }
+    return 0;
+}
+
+int enqueue_step(mgpu_handle *h) {
+    const Dev &d = h->d;
+    Launch L{h->stream, h->sm_count};
+    launch_step_begin(d, L);
+    launch_prim(d, L);
+    launch_loss(d, L, false);
+    launch_flux_mass(d, L);
+    launch_tstep(d, L, d.RO, d.DRO);
+    launch_flux_energy(d, L);
+    launch_tstep(d, L, d.ROE, d.DROE);
+    launch_bc(d, L);
+    launch_peff(d, L);
+    launch_flux_xmom(d, L);
+    launch_tstep(d, L, d.ROVX, d.DROVX);
+    launch_flux_rvt(d, L);
+    launch_tstep(d, L, d.RORVT, d.DRORVT);
+    launch_flux_rmom(d, L);
+    launch_tstep(d, L, d.ROVR, d.DROVR);
+    launch_limiters(d, L);
+    launch_mixplan(d, L);
+    launch_tail(d, L);
+    launch_stepup(d, L, 0.25f, true);
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int build_graph(mgpu_handle *h) {
+    if (h->gexec) return 0;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_step(h);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(MGPU_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    h->graph = g;
+    CK(cudaGraphGetNodes(g, nullptr, &h->graph_nodes));
+    CK(cudaGraphInstantiate(&h->gexec, g, 0));
+    return 0;
+}
+
+void fill_monitors(const DevCtl &c, mgpu_monitors *m) {
+    memset(m, 0, sizeof(*m));
+    m->nstep = c.nstep;
+    m->tail_ran = c.do_tail;
+    m->ifend = c.ifend;
+    m->health = c.health;
+    m->emax = c.EMAX;
+    m->imax = c.IMAXE;
+    m->jmax = c.JMAXE;
+    m->kmax = c.KMAXE;
+    m->eavg = c.EAVG;
+    m->econt = c.ECONT;
+    m->jcont = c.JCONT;
+    m->vref = c.VREF;
+    m->vmax = c.VMAX;
+    m->ivmax = c.IVMAX;
+    m->jvmax = c.JVMAX;
+    m->kvmax = c.KVMAX;
+    m->flow_in = c.flow_in;
+    m->flow_out = c.flow_out;
+}
+
+int read_ctl(mgpu_handle *h) {
+    CK(cudaMemcpyAsync(h->h_ctl, h->d.ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t mgpu_abi_version(void) { return MGPU_ABI_VERSION; }
+
+int32_t mgpu_last_error(char *buf, int32_t len) {
+    if (!buf || len <= 0) return MGPU_E_ARG;
+    snprintf(buf, (size_t)len, "%s", g_err.c_str());
+    return 0;
+}
+
+int32_t mgpu_device_count(void) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) return fail(MGPU_E_CUDA, cudaGetErrorString(e));
+    return n;
+}
+
+int32_t mgpu_create(int32_t im, int32_t jm, int32_t km, int32_t nrows, mgpu_handle **out) {
+    if (!out) return fail(MGPU_E_ARG, "null handle pointer");
+    *out = nullptr;
+    if (im < 5 || jm < 10 || km < 5 || nrows < 1 || nrows > 64)
+        return fail(MGPU_E_ARG, "dimensions out of range (IM,KM >= 5, JM >= 10, 1 <= NROWS <= 64)");
+    if (im > 160 || km > 160) return fail(MGPU_E_UNSUPPORTED, "IM and KM above 160 are not covered");
+    mgpu_handle *h = new (std::nothrow) mgpu_handle();
+    if (!h) return fail(MGPU_E_NOMEM, "host allocation");
+    Dev &d = h->d;
+    memset(&d, 0, sizeof(d));
+    d.IM = im; d.JM = jm; d.KM = km; d.NROWS = nrows;
+    d.IMM1 = im - 1; d.JMM1 = jm - 1; d.KMM1 = km - 1;
+    d.IMM2 = im - 2; d.JMM2 = jm - 2; d.KMM2 = km - 2;
+    d.IMID = (int)(0.5f * im);
+    d.KMID = (int)(0.5f * km);
+    d.NRWSM1 = nrows - 1;
+#define MGPU_DEF_I(n, v) d.n = v;
+    MGPU_INT_SCALARS(MGPU_DEF_I)
+#define MGPU_DEF_R(n, v) d.n = v;
+    MGPU_REAL_SCALARS(MGPU_DEF_R)
+    int rc = 0;
+    auto bail = [&](int code) {
+        mgpu_destroy(h);
+        return code;
+    };
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e != cudaSuccess) return bail(fail(MGPU_E_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e)));
+    cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(fail(MGPU_E_CUDA, cudaGetErrorString(e)));
+    // arrays whose size is known now
+    for (int a = 0; a < kNumArrays; ++a) {
+        Shape s = kArrays[a].shape;
+        if (s == SH_MG1 || s == SH_MG2 || s == SH_SB) continue;
+        size_t cnt = shape_count(h, s);
+        void **slot = dev_slot(d, kArrays[a].name);
+        if (kArrays[a].is_int) rc = dalloc(h, (int32_t **)slot, cnt);
+        else rc = dalloc(h, (float **)slot, cnt);
+        if (rc) return bail(rc);
+        h->dptr[a] = *slot;
+        h->dbytes[a] = cnt * 4;
+    }
+    size_t N = (size_t)im * jm * km;
+    float **work[] = {&d.XFLUX, &d.TFLUX, &d.RFLUX, &d.SOURCE, &d.FLOWX, &d.FLOWT, &d.FLOWR, &d.STORE, &d.TMP, &d.TEMP1};
+    for (float **w : work)
+        if ((rc = dalloc(h, w, N))) return bail(rc);
+    if ((rc = dalloc(h, &d.PLIM, km))) return bail(rc);
+    float **rowt[] = {&d.FILAM, &d.FITURB, &d.FIWAKE, &d.FIUP};
+    for (float **w : rowt)
+        if ((rc = dalloc(h, w, (size_t)nrows * im))) return bail(rc);
+    if ((rc = dalloc(h, &d.FKLAM, (size_t)nrows * km))) return bail(rc);
+    if ((rc = dalloc(h, &d.FKTURB, (size_t)nrows * km))) return bail(rc);
+    if ((rc = dalloc(h, &d.VLIMIT, nrows))) return bail(rc);
+    if ((rc = dalloc(h, &d.ROLIMIT, nrows))) return bail(rc);
+    if ((rc = dalloc(h, &d.AVG_BLK, nrows))) return bail(rc);
+    if ((rc = dalloc(h, &d.plane_sum, jm))) return bail(rc);
+    if ((rc = dalloc(h, &d.plane_abs, jm))) return bail(rc);
+    if ((rc = dalloc(h, &d.BLADE_FLOW, jm))) return bail(rc);
+    d.nparts = (int)((N + 255) / 256) + 1;
+    if ((rc = dalloc(h, &d.part_sum, d.nparts))) return bail(rc);
+    if ((rc = dalloc(h, &d.part_key, d.nparts))) return bail(rc);
+    if ((rc = dalloc(h, &d.part_cnt, d.nparts))) return bail(rc);
+    if ((rc = dalloc(h, &d.ctl, 1))) return bail(rc);
+    if ((rc = dalloc(h, &h->d_int, (size_t)4 * jm))) return bail(rc);
+    e = cudaMallocHost((void **)&h->h_ctl, sizeof(DevCtl));
+    if (e != cudaSuccess) return bail(fail(MGPU_E_NOMEM, cudaGetErrorString(e)));
+    *out = h;
+    return 0;
+}
+
+void mgpu_destroy(mgpu_handle *h) {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    for (void *p : h->allocs) cudaFree(p);
+    if (h->h_ctl) cudaFreeHost(h->h_ctl);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+int32_t mgpu_set_int(mgpu_handle *h, const char *name, int32_t value) {
+    if (!h || !name) return fail(MGPU_E_ARG, "null argument");
+    if (h->committed) return fail(MGPU_E_STATE, "scalars are fixed after commit");
+#define MGPU_SETI(n, v) if (!strcmp(name, #n)) { h->d.n = value; return 0; }
+    MGPU_INT_SCALARS(MGPU_SETI)
+    return fail(MGPU_E_ARG, std::string("unknown integer scalar ") + name);
+}
+
+int32_t mgpu_set_real(mgpu_handle *h, const char *name, float value) {
+    if (!h || !name) return fail(MGPU_E_ARG, "null argument");
+    if (h->committed) return fail(MGPU_E_STATE, "scalars are fixed after commit");
+#define MGPU_SETR(n, v) if (!strcmp(name, #n)) { h->d.n = value; return 0; }
+    MGPU_REAL_SCALARS(MGPU_SETR)
+    return fail(MGPU_E_ARG, std::string("unknown real scalar ") + name);
+}
+
+int32_t mgpu_get_real(mgpu_handle *h, const char *name, float *value) {
+    if (!h || !name || !value) return fail(MGPU_E_ARG, "null argument");
+    if (h->committed && (!strcmp(name, "VISLAM") || !strcmp(name, "FTCOND") || !strcmp(name, "SFT") ||
+                         !strcmp(name, "SFX") || !strcmp(name, "DAMP") || !strcmp(name, "FMIXUP"))) {
+        int rc = read_ctl(h);
+        if (rc) return rc;
+        const DevCtl &c = *h->h_ctl;
+        if (!strcmp(name, "VISLAM")) *value = c.VISLAM;
+        else if (!strcmp(name, "FTCOND")) *value = c.FTCOND;
+        else if (!strcmp(name, "SFT")) *value = c.SFT;
+        else if (!strcmp(name, "SFX")) *value = c.SFX;
+        else if (!strcmp(name, "DAMP")) *value = c.DAMP;
+        else *value = c.FMIXUP;
+        return 0;
+    }
+    if (!strcmp(name, "PREFF")) { *value = h->d.PREFF; return 0; }
+#define MGPU_GETR(n, v) if (!strcmp(name, #n)) { *value = h->d.n; return 0; }
+    MGPU_REAL_SCALARS(MGPU_GETR)
+    return fail(MGPU_E_ARG, std::string("unknown real scalar ") + name);
+}
+
+int32_t mgpu_get_int(mgpu_handle *h, const char *name, int32_t *value) {
+    if (!h || !name || !value) return fail(MGPU_E_ARG, "null argument");
+    if (!strcmp(name, "NSTEP") && h->committed) {
+        int rc = read_ctl(h);
+        if (rc) return rc;
+        *value = h->h_ctl->nstep;
+        return 0;
+    }
+#define MGPU_GETI(n, v) if (!strcmp(name, #n)) { *value = h->d.n; return 0; }
+    MGPU_INT_SCALARS(MGPU_GETI)
+    return fail(MGPU_E_ARG, std::string("unknown integer scalar ") + name);
+}
+
+int32_t mgpu_set_array(mgpu_handle *h, const char *name, const void *host, int64_t nbytes) {
+    if (!h || !name || !host) return fail(MGPU_E_ARG, "null argument");
+    int a = find_array(name);
+    if (a < 0) return fail(MGPU_E_ARG, std::string("unknown array ") + name);
+    if (kArrays[a].role == RO_OUT) return fail(MGPU_E_ARG, std::string("array is output only: ") + name);
+    if (h->committed && kArrays[a].role != RO_STATE)
+        return fail(MGPU_E_STATE, std::string("geometry is fixed after commit: ") + name);
+    Shape s = kArrays[a].shape;
+    if ((s == SH_MG1 || s == SH_MG2 || s == SH_SB) && !h->dptr[a]) {
+        Dev &d = h->d;
+        if ((s == SH_MG1 && (d.NIB1 <= 0 || d.NJB1 <= 0 || d.NKB1 <= 0)) ||
+            (s == SH_MG2 && (d.NIB2 <= 0 || d.NJB2 <= 0 || d.NKB2 <= 0)) || (s == SH_SB && d.NSBLK <= 0))
+            return fail(MGPU_E_STATE, std::string("set the multigrid block counts before ") + name);
+        size_t cnt = shape_count(h, s);
+        void **slot = dev_slot(d, name);
+        int rc = dalloc(h, (float **)slot, cnt);
+        if (rc) return rc;
+        h->dptr[a] = *slot;
+        h->dbytes[a] = cnt * 4;
+    }
+    size_t want = shape_count(h, s) * 4;
+    if ((size_t)nbytes != want)
+        return fail(MGPU_E_ARG, std::string("size mismatch for ") + name + ": expected " + std::to_string(want) +
+                                    " bytes, got " + std::to_string(nbytes));
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(h->dptr[a], host, want, cudaMemcpyHostToDevice));
+    h->bound[a] = true;
+    return 0;
+}
+
+int32_t mgpu_get_array(mgpu_handle *h, const char *name, void *host, int64_t nbytes) {
+    if (!h || !name || !host) return fail(MGPU_E_ARG, "null argument");
+    int a = find_array(name);
+    const void *src = nullptr;
+    size_t want = 0;
+    if (a >= 0) {
+        src = h->dptr[a];
+        want = shape_count(h, kArrays[a].shape) * 4;
+        if (!src) return fail(MGPU_E_STATE, std::string("array not allocated: ") + name);
+    } else {
+        size_t N = (size_t)h->d.IM * h->d.JM * h->d.KM;
+        if (!strcmp(name, "FLOWX")) src = h->d.FLOWX;
+        else if (!strcmp(name, "STORE")) src = h->d.STORE;
+        else return fail(MGPU_E_ARG, std::string("unknown array ") + name);
+        want = N * 4;
+    }
+    if ((size_t)nbytes != want) return fail(MGPU_E_ARG, std::string("size mismatch for ") + name);
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(host, src, want, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int32_t mgpu_commit(mgpu_handle *h) {
+    if (!h) return fail(MGPU_E_ARG, "null handle");
+    if (h->committed) return fail(MGPU_E_STATE, "already committed");
+    Dev &d = h->d;
+    for (int a = 0; a < kNumArrays; ++a)
+        if (kArrays[a].role != RO_OUT && !h->bound[a])
+            return fail(MGPU_E_ARG, std::string("array not bound: ") + kArrays[a].name);
+#define MGPU_CHKI(n, v) if (d.n == MGPU_REQUIRED_INT) return fail(MGPU_E_ARG, "integer not set: " #n);
+    MGPU_INT_SCALARS(MGPU_CHKI)
+#define MGPU_CHKR(n, v) if (d.n == MGPU_REQUIRED_REAL) return fail(MGPU_E_ARG, "real not set: " #n);
+    MGPU_REAL_SCALARS(MGPU_CHKR)
+    if (d.ITIMST != 3) return fail(MGPU_E_UNSUPPORTED, "ITIMST other than 3 (incompressible 5/6) not covered");
+    if (d.ILOS != 10) return fail(MGPU_E_UNSUPPORTED, "only ILOS=10 (mixing-length LOSS) is covered");
+    if (d.IFGAS != 0) return fail(MGPU_E_UNSUPPORTED, "real-gas IFGAS=1 not covered");
+    if (d.IFCOOL || d.IFBLEED || d.IFSHROUD) return fail(MGPU_E_UNSUPPORTED, "cooling/bleed/shroud not covered");
+    if (d.IN_FLOW != 0 || d.IF_REPEAT != 0) return fail(MGPU_E_UNSUPPORTED, "IN_FLOW/IF_REPEAT not covered");
+    if (d.PLATE_LOSS > 0.001f || d.THROTTLE_EXIT > 0.001f) return fail(MGPU_E_UNSUPPORTED, "plate loss/throttle not covered");
+    if (d.YPLUSWALL <= -10.0f)
+        return fail(MGPU_E_UNSUPPORTED, "YPLUSWALL<=-10 (pressure-gradient wall functions) not covered");
+    if (d.IPOUT == 3 || d.IPOUT < -1) return fail(MGPU_E_UNSUPPORTED, "IPOUT not covered");
+    if (d.NCHANGE <= 0 || d.NMIXUP <= 0 || d.NLOS <= 0) return fail(MGPU_E_ARG, "NCHANGE, NMIXUP, NLOS must be positive");
+    if (d.IR <= 1 && d.JR <= 1 && d.KR <= 1) return fail(MGPU_E_UNSUPPORTED, "runs without multigrid are not covered");
+    if (d.KM > 512) return fail(MGPU_E_UNSUPPORTED, "KM above 512");
+    size_t smem = (size_t)2 * d.IM * d.KM * sizeof(float);
+    if (smem > 200 * 1024) return fail(MGPU_E_UNSUPPORTED, "J-plane does not fit shared memory");
+
+    // host copies of the inputs the derived tables need
+    int rc = 0;
+    auto geti = [&](const char *n, std::vector<int> &v) -> int {
+        int a = find_array(n);
+        return download(h, v, (const int *)h->dptr[a], shape_count(h, kArrays[a].shape));
+    };
+    auto getf = [&](const char *n, std::vector<float> &v) -> int {
+        int a = find_array(n);
+        return download(h, v, (const float *)h->dptr[a], shape_count(h, kArrays[a].shape));
+    };
+    std::vector<int> IF_CUSP, JB1, JB2, JSBLK, IB1, IB2, KB1, KB2, NBLADE, JLE, JTE, NROW, JSTART, JMIX, INDMIX;
+    std::vector<float> FP, FR, X, R, PO1, TO1, P, RO, XL[6];
+    if ((rc = geti("IF_CUSP", IF_CUSP)) || (rc = geti("JB1", JB1)) || (rc = geti("JB2", JB2)) ||
+        (rc = geti("JSBLK", JSBLK)) || (rc = geti("IB1", IB1)) || (rc = geti("IB2", IB2)) || (rc = geti("KB1", KB1)) ||
+        (rc = geti("KB2", KB2)) || (rc = geti("NBLADE", NBLADE)) || (rc = geti("JLE", JLE)) || (rc = geti("JTE", JTE)) ||
+        (rc = geti("NROW", NROW)) || (rc = geti("JSTART", JSTART)) || (rc = geti("JMIX", JMIX)) ||
+        (rc = geti("INDMIX", INDMIX)))
+        return rc;
+    if ((rc = getf("FP", FP)) || (rc = getf("FR", FR)) || (rc = getf("X", X)) || (rc = getf("R", R)) ||
+        (rc = getf("PO1", PO1)) || (rc = getf("TO1", TO1)) || (rc = getf("P", P)) || (rc = getf("RO", RO)) ||
+        (rc = getf("XLLIM_I1", XL[0])) || (rc = getf("XLLIM_IM", XL[1])) || (rc = getf("XLLIM_K1", XL[2])) ||
+        (rc = getf("XLLIM_KM", XL[3])) || (rc = getf("XLLIM_DWN", XL[4])) || (rc = getf("XLLIM_UP", XL[5])))
+        return rc;
+    for (int nr = 0; nr < d.NROWS; ++nr)
+        if (IF_CUSP[nr] >= 2) return fail(MGPU_E_UNSUPPORTED, "IF_CUSP=2 not covered");
+    for (int nr = 0; nr < d.NROWS; ++nr) {
+        if (JSTART[nr] < 1 || JMIX[nr] > d.JM || JMIX[nr] - JSTART[nr] < 8)
+            return fail(MGPU_E_ARG, "row J ranges (JSTART/JMIX) out of range");
+        if (nr < d.NROWS - 1 && JMIX[nr] + 4 > d.JM) return fail(MGPU_E_ARG, "mixing plane too close to the exit");
+    }
+    for (int j = 1; j <= d.JM; ++j)
+        if (NROW[j - 1] < 1 || NROW[j - 1] > d.NROWS) return fail(MGPU_E_ARG, "NROW out of range");
+
+    // gas constants, SETUP 6459-6468
+    d.GA1 = d.GA - 1.0f;
+    d.FGA = d.GA1 / d.GA;
+    d.RFGA = 1.0f / d.FGA;
+    d.RCP = 1.0f / d.CP;
+    d.CV = d.CP / d.GA;
+    d.RCV = 1.0f / d.CV;
+    d.RGAS = d.CP - d.CV;
+    // LOOP prologue, 3677-3709
+    auto P3 = [&](const std::vector<float> &v, int i, int j, int k) {
+        return v[(size_t)(i - 1) + (size_t)d.IM * ((size_t)(j - 1) + (size_t)d.JM * (k - 1))];
+    };
+    d.RO_REF = PO1[d.KMID - 1] / (d.RGAS * TO1[d.KMID - 1]);
+    float ROMIN = fminf(P3(RO, d.IMID, 1, d.KMID), P3(RO, d.IMID, d.JM, d.KMID));
+    d.ROLIM = 0.25f * ROMIN;
+    d.RIJKM = 2.0f / (float)(d.IM * d.JM * d.KM);
+    std::vector<float> PLIM(d.KM);
+    for (int k = 1; k <= d.KM; ++k) PLIM[k - 1] = 0.9f * PO1[k - 1] + 0.1f * P3(P, 1, 1, k);
+    if ((rc = upload(h, d.PLIM, PLIM))) return rc;
+    d.PREFF = 0.5f * (P3(P, d.IMID, 1, d.KMID) + P3(P, d.IMID, d.JM, d.KMID));
+    d.SFXIN = d.SFXIN * d.CFL / 0.5f;
+    d.SFTIN = d.SFTIN * d.CFL / 0.5f;
+    d.RFIN1 = 1.0f - d.RFIN;
+    d.RFIN2 = 2.0f * d.RFIN;
+    d.TCOOL_MIN = 1.0E6f;
+    // the LOSS tables
+    std::vector<float> FILAM, FITURB, FIWAKE, FIUP, FKLAM, FKTURB;
+    loss_tables(d, FP, FR, X, R, NBLADE, JLE, JTE, XL, FILAM, FITURB, FIWAKE, FIUP, FKLAM, FKTURB);
+    if ((rc = upload(h, d.FILAM, FILAM)) || (rc = upload(h, d.FITURB, FITURB)) || (rc = upload(h, d.FIWAKE, FIWAKE)) ||
+        (rc = upload(h, d.FIUP, FIUP)) || (rc = upload(h, d.FKLAM, FKLAM)) || (rc = upload(h, d.FKTURB, FKTURB)))
+        return rc;
+    // multigrid block extents
+    std::vector<int> s, e;
+    struct Ext {
+        const std::vector<int> *map;
+        int lo, hi, n;
+        int **ds, **de;
+        const char *what;
+    } ext[] = {
+        {&JB1, 2, d.JM, d.NJB1, &d.JB1_START, &d.JB1_END, "JB1"},
+        {&JB2, 2, d.JM, d.NJB2, &d.JB2_START, &d.JB2_END, "JB2"},
+        {&IB1, 1, d.IMM1, d.NIB1, &d.IB1_S, &d.IB1_E, "IB1"},
+        {&IB2, 1, d.IMM1, d.NIB2, &d.IB2_S, &d.IB2_E, "IB2"},
+        {&KB1, 1, d.KMM1, d.NKB1, &d.KB1_S, &d.KB1_E, "KB1"},
+        {&KB2, 1, d.KMM1, d.NKB2, &d.KB2_S, &d.KB2_E, "KB2"},
+        {&JSBLK, 2, d.JM, d.NSBLK, &d.SB_START, &d.SB_END, "JSBLK"},
+    };
+    for (auto &x : ext) {
+        if ((rc = extents(*x.map, x.lo, x.hi, x.n, s, e, x.what))) return rc;
+        if ((rc = dalloc(h, x.ds, x.n)) || (rc = dalloc(h, x.de, x.n))) return rc;
+        if ((rc = upload(h, *x.ds, s)) || (rc = upload(h, *x.de, e))) return rc;
+    }
+    for (int j = 2; j <= d.JM; ++j) {
+        if (JB1[j - 1] < 1 || JB1[j - 1] > d.NJB1 + 1 || JB2[j - 1] < 1 || JB2[j - 1] > d.NJB2 + 1 ||
+            JSBLK[j - 1] < 1 || JSBLK[j - 1] > d.NSBLK)
+            return fail(MGPU_E_ARG, "multigrid J map out of range");
+    }
+    if ((rc = dalloc(h, &d.B1CHG, shape_count(h, SH_MG1))) || (rc = dalloc(h, &d.B2CHG, shape_count(h, SH_MG2))))
+        return rc;
+    // the control block
+    DevCtl c;
+    memset(&c, 0, sizeof(c));
+    c.EAVG = 1.0E06f;
+    c.ECONT = 1.0f;
+    c.EMAX = 1.0E06f;
+    c.FMIXUP = 1.0f;
+    c.VISLAM = d.VISLAM;
+    c.FTCOND = d.FTCOND;
+    c.nstep = d.NSTEP;
+    CK(cudaMemcpy(d.ctl, &c, sizeof(c), cudaMemcpyHostToDevice));
+    CK(configure_kernels(d));
+    CK(cudaDeviceSynchronize());
+    h->committed = true;
+    return 0;
+}
+
+int32_t mgpu_stepup(mgpu_handle *h, float relax) {
+    if (!h || !h->committed) return fail(MGPU_E_STATE, "stepup before commit");
+    Launch L{h->stream, h->sm_count};
+    launch_stepup(h->d, L, relax, false);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+int32_t mgpu_loss_init(mgpu_handle *h) {
+    if (!h || !h->committed) return fail(MGPU_E_STATE, "loss_init before commit");
+    Launch L{h->stream, h->sm_count};
+    launch_loss(h->d, L, true);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+int32_t mgpu_step(mgpu_handle *h, int32_t force_end, mgpu_monitors *mon) {
+    if (!h || !h->committed) return fail(MGPU_E_STATE, "step before commit");
+    int rc = build_graph(h);
+    if (rc) return rc;
+    int fe = force_end ? 1 : 0;
+    CK(cudaMemcpyAsync(&h->d.ctl->force_end, &fe, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaGraphLaunch(h->gexec, h->stream));
+    if ((rc = read_ctl(h))) return rc;
+    const DevCtl &c = *h->h_ctl;
+    if (mon) fill_monitors(c, mon);
+    if (c.do_tail && c.health) return fail(MGPU_E_NONFINITE, "non-finite or non-positive density in the flow field");
+    return 0;
+}
+
+int32_t mgpu_run(mgpu_handle *h, int32_t nsteps, mgpu_monitors *mon) {
+    if (!h || !h->committed) return fail(MGPU_E_STATE, "run before commit");
+    if (nsteps < 0) return fail(MGPU_E_ARG, "negative step count");
+    int rc = build_graph(h);
+    if (rc) return rc;
+    const int chunk = 50;
+    int done = 0;
+    while (done < nsteps) {
+        int n = nsteps - done < chunk ? nsteps - done : chunk;
+        for (int s = 0; s < n; ++s) CK(cudaGraphLaunch(h->gexec, h->stream));
+        done += n;
+        if ((rc = read_ctl(h))) return rc;
+        const DevCtl &c = *h->h_ctl;
+        if (mon) fill_monitors(c, mon);
+        if (c.health) return fail(MGPU_E_NONFINITE, "non-finite or non-positive density in the flow field");
+        if (c.converged || c.ifend) return 1;
+    }
+    return 0;
+}
+
+int32_t mgpu_sync(mgpu_handle *h) {
+    if (!h) return fail(MGPU_E_ARG, "null handle");
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+int32_t mgpu_integrals_compute(mgpu_handle *h, mgpu_integrals *out) {
+    if (!h || !h->committed || !out) return fail(MGPU_E_STATE, "integrals before commit");
+    const Dev &d = h->d;
+    Launch L{h->stream, h->sm_count};
+    launch_integrals(d, L, h->d_int);
+    CK(cudaGetLastError());
+    std::vector<double> v((size_t)4 * d.JM);
+    CK(cudaMemcpyAsync(v.data(), h->d_int, v.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    // whole-machine efficiency (11269-11394): for one stage the inlet
+    // station is J=1, otherwise J=2; the exit station is JM-1
+    int J1 = d.NSTAGES == 1 ? 1 : 2, J2M1 = d.JM - 1;
+    auto bf = [&](int j) { return v[(size_t)(j - 1)]; };
+    auto spo = [&](int j) { return v[(size_t)d.JM + j - 1] / bf(j); };
+    auto sto = [&](int j) { return v[(size_t)2 * d.JM + j - 1] / bf(j); };
+    auto sps = [&](int j) { return v[(size_t)3 * d.JM + j - 1] / bf(j); };
+    double PO1M = 0.0;
+    {
+        std::vector<float> po1;
+        int a = find_array("PO1");
+        int rc = download(h, po1, (const float *)h->dptr[a], d.KM);
+        if (rc) return rc;
+        PO1M = po1[d.KMID - 1];
+    }
+    double FGA = (double)d.FGA;
+    double POIN = spo(J1) * PO1M, PO2 = spo(J2M1) * PO1M, PSOUT = sps(J2M1);
+    double TO_IN = sto(J1), TO_OUT = sto(J2M1);
+    double TORAT = TO_OUT / TO_IN, DELTO = TO_OUT - TO_IN, PORAT = PO2 / POIN, PSRAT = PSOUT / POIN;
+    if (PORAT < 0.01) PORAT = 0.01;
+    double TO2IS = pow(PORAT, FGA) * TO_IN, TSTAT2_IS = pow(PSRAT, FGA) * TO_IN;
+    double DELTOIS = TO2IS - TO_IN, DELT_TOT_STAT = TSTAT2_IS - TO_IN;
+    double ETAIS = 1.0, ETATS = 1.0;
+    if (DELTO > 0.0) { ETAIS = DELTOIS / DELTO; ETATS = DELT_TOT_STAT / DELTO; }
+    if (DELTO < 0.0) { ETAIS = DELTO / DELTOIS; ETATS = DELTO / DELT_TOT_STAT; }
+    out->mass_flow_in = bf(J1);
+    out->mass_flow_out = bf(J2M1);
+    out->eta_tt = ETAIS;
+    out->eta_ts = ETATS;
+    out->po_ratio = PORAT;
+    out->to_ratio = TORAT;
+    out->j1 = J1;
+    out->j2m1 = J2M1;
+    return 0;
+}
+
+int32_t mgpu_kernels_per_step(mgpu_handle *h, int32_t tail_step) {
+    (void)tail_step;
+    if (!h || !h->committed) return fail(MGPU_E_STATE, "kernels_per_step before commit");
+    int rc = build_graph(h);
+    if (rc) return rc;
+    return (int32_t)h->graph_nodes;
+}
+
+}  // extern "C"

@@ -1,0 +1,761 @@
+// mgpu_flux.cu -- per-step node kernels of the time-marching loop:
+// step control, primitive recovery, the face fluxes of the five
+// conservation equations, inlet/exit boundary conditions, PEFF, the density
+// and Mach limiters and the mixing-plane relaxation.
+//
+// Each kernel restates one sweep of SUBROUTINE LOOP
+// (multall-open-18.3.f:3664-5463) with one thread per node and the
+// reference's floating-point expression order, so that (built without FMA
+// contraction, as the reference is) the results match REAL*4 arithmetic.
+// Periodic fix-ups that couple I=1 and I=IM are done by both end threads
+// from the same raw values, so no thread waits on another.
+#include "mgpu_internal.cuh"
+
+namespace mgpu {
+
+static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
+
+// ---------------------------------------------------------------------
+// step control: NSTEP, the end test, the smoothing/damping ramp and FMIXUP
+// (multall-open-18.3.f:3759-3815), and the viscosity update LOSS makes on
+// entry (8088-8112).
+// ---------------------------------------------------------------------
+__global__ void k_step_begin(Dev d) {
+    DevCtl *c = d.ctl;
+    int n = c->nstep + 1;
+    c->nstep = n;
+    int ifend = c->ifend;
+    if (n == d.NSTEPS_MAX) ifend = 1;
+    if (c->EAVG < d.CONLIM && c->ECONT < 0.01f) ifend = 1;
+    if (fabsf(c->EMAX) < 4.0f * d.CONLIM && c->ECONT < 0.01f) ifend = 1;
+    if (c->force_end) ifend = 1;
+    c->ifend = ifend;
+    if (!(d.IF_RESTART != 0 && n > 100)) {
+        float FCHANGE = 1.0f - (float)(n - 1) / (float)d.NCHANGE;
+        if (FCHANGE > 0.0f) {
+            c->SFT = d.SFTIN + 0.02f * FCHANGE;
+            c->SFX = d.SFXIN + 0.02f * FCHANGE;
+            c->DAMP = d.DAMPIN * (1.0f - 0.75f * FCHANGE);
+        }
+        float SFT = c->SFT, SFX = c->SFX;
+        c->SFT1 = 1.0f - SFT;
+        c->SFTH = 0.5f * SFT;
+        c->SFX1 = 1.0f - SFX;
+        c->SFXH = 0.5f * SFX;
+        c->SFX14 = 0.25f * SFX;
+        c->SFXB = d.FSMTHB * SFX;
+        c->SFXB1 = 1.0f - c->SFXB;
+        c->SFXBH = 0.5f * c->SFXB;
+        c->SFXHM1 = 1.0f - c->SFXH;
+        float FM = 1.0f + (d.FACMIXUP - 1.0f) * (float)(d.NMIXUP - n) / (float)d.NMIXUP;
+        if (FM < 1.0f) FM = 1.0f;
+        c->FMIXUP = FM * FM;
+    }
+    c->do_tail = (n % 5 == 0) || ifend == 1;
+    c->do_loss = (d.ILOS == 10) && (n % d.NLOS == 0);
+    c->damp_on = !(c->DAMP < 2.0f || c->DAMP > 100.0f);
+    if (c->do_tail) {
+        c->mon.vrms = 0.0;
+        c->mon.vmax_key = 0ull;
+        c->mon.eavg_sum = 0.0;
+        c->mon.emax_key = 0ull;
+        c->mon.health = 0;
+    }
+}
+
+void launch_step_begin(const Dev &d, Launch L) { k_step_begin<<<1, 1, 0, L.s>>>(d); }
+
+// ---------------------------------------------------------------------
+// primitive variables (7450) and P, HO, T (5900); with the 5-step tail
+// also the sum and the maximum of |W|^2 (5910, uses the previous WT).
+// ---------------------------------------------------------------------
+template <int BS>
+__device__ inline void block_reduce_sum_key(double s, unsigned long long key, double *out_s,
+                                            unsigned long long *out_k) {
+    __shared__ double ss[BS / 32];
+    __shared__ unsigned long long sk[BS / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_down_sync(0xffffffffu, s, o);
+        unsigned long long ok = __shfl_down_sync(0xffffffffu, key, o);
+        key = ok > key ? ok : key;
+    }
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) {
+        ss[w] = s;
+        sk[w] = key;
+    }
+    __syncthreads();
+    if (w == 0) {
+        s = l < BS / 32 ? ss[l] : 0.0;
+        key = l < BS / 32 ? sk[l] : 0ull;
+        for (int o = 16; o > 0; o >>= 1) {
+            s += __shfl_down_sync(0xffffffffu, s, o);
+            unsigned long long ok = __shfl_down_sync(0xffffffffu, key, o);
+            key = ok > key ? ok : key;
+        }
+        if (l == 0) {
+            *out_s = s;
+            *out_k = key;
+        }
+    }
+}
+
+constexpr int PRIM_BS = 256;
+
+__global__ void __launch_bounds__(PRIM_BS) k_prim(Dev d) {
+    size_t n = (size_t)blockIdx.x * PRIM_BS + threadIdx.x;
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    int do_tail = d.ctl->do_tail;
+    double eke_s = 0.0;
+    unsigned long long key = 0ull;
+    if (n < N) {
+        int i, j, k;
+        node_ijk(d, n, i, j, k);
+        if (j >= 2) {
+            float RRNOW = 1.0f / A2(d.R, j, k);
+            float RECIP = 1.0f / d.RO[n];
+            float vx = d.ROVX[n] * RECIP;
+            float vr = d.ROVR[n] * RECIP;
+            float rovt = d.RORVT[n] * RRNOW;
+            float vt = rovt * RECIP;
+            d.VX[n] = vx;
+            d.VR[n] = vr;
+            d.ROVT[n] = rovt;
+            d.VT[n] = vt;
+            if (do_tail) {
+                float wt = d.WT[n];
+                float EKE = vr * vr + wt * wt + vx * vx;
+                eke_s = (double)EKE;
+                key = max_key(EKE, n);
+            }
+            if (j <= d.JMM1) {
+                float RONOW = d.RO[n];
+                float EKE = 0.5f * (vr * vr + vt * vt + vx * vx);
+                float TSTATIC = (d.ROE[n] / RONOW - EKE) / d.CV;
+                d.P[n] = RONOW * d.RGAS * TSTATIC;
+                d.HO[n] = d.CP * TSTATIC + EKE;
+                d.T_STATIC[n] = TSTATIC;
+            }
+        }
+    }
+    if (do_tail) block_reduce_sum_key<PRIM_BS>(eke_s, key, &d.part_sum[blockIdx.x], &d.part_key[blockIdx.x]);
+}
+
+void launch_prim(const Dev &d, Launch L) {
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    k_prim<<<grid_for(N, PRIM_BS), PRIM_BS, 0, L.s>>>(d);
+}
+
+// ---------------------------------------------------------------------
+// mass fluxes FLOWX/FLOWT/FLOWR, ROWT and WT (5020-5045)
+// ---------------------------------------------------------------------
+__device__ inline float rowt_at(const Dev &d, int i, int j, int k) {
+    return A3(d.ROVT, i, j, k) - A2(d.UBLADE, j, k) * A3(d.RO, i, j, k);
+}
+
+__device__ inline float flowt_raw(const Dev &d, int i, int j, int k) {
+    float AVGRVX = A3(d.ROVX, i, j, k) + A3(d.ROVX, i, j - 1, k) + A3(d.ROVX, i, j - 1, k + 1) + A3(d.ROVX, i, j, k + 1);
+    float AVGRVT = rowt_at(d, i, j, k) + rowt_at(d, i, j - 1, k) + rowt_at(d, i, j - 1, k + 1) + rowt_at(d, i, j, k + 1);
+    float AVGRVR = A3(d.ROVR, i, j, k) + A3(d.ROVR, i, j - 1, k) + A3(d.ROVR, i, j - 1, k + 1) + A3(d.ROVR, i, j, k + 1);
+    return (AVGRVX * A3(d.ABX, i, j, k) + AVGRVT * A2(d.ABT, j, k) + AVGRVR * A3(d.ABR, i, j, k)) * 0.25f;
+}
+
+__global__ void k_flux_mass(Dev d) {
+    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, n, i, j, k);
+    if (i < d.IM && k < d.KM) {
+        float AVGRVX = A3(d.ROVX, i, j, k) + A3(d.ROVX, i, j, k + 1) + A3(d.ROVX, i + 1, j, k) + A3(d.ROVX, i + 1, j, k + 1);
+        float AVGRVR = A3(d.ROVR, i, j, k) + A3(d.ROVR, i, j, k + 1) + A3(d.ROVR, i + 1, j, k) + A3(d.ROVR, i + 1, j, k + 1);
+        float fx = 0.25f * (AVGRVX * A3(d.AQX, i, j, k) + AVGRVR * A3(d.AQR, i, j, k));
+        d.FLOWX[n] = fx;
+        d.SOURCE[n] = 0.0f;
+        d.XFLUX[n] = fx;
+    }
+    {
+        float rowt = d.ROVT[n] - A2(d.UBLADE, j, k) * d.RO[n];
+        d.ROWT[n] = rowt;
+        d.WT[n] = rowt / d.RO[n];
+    }
+    if (j >= 2 && k < d.KM) {
+        float ft = flowt_raw(d, i, j, k);
+        if (i == 1 || i == d.IM) {
+            if (A1(d.IND, j) != 1) {
+                float f1 = (i == 1) ? ft : flowt_raw(d, 1, j, k);
+                float fm = (i == d.IM) ? ft : flowt_raw(d, d.IM, j, k);
+                ft = 0.5f * (f1 + fm);
+            } else {
+                int nr = A1(d.NROW, j);
+                if (k >= A1(d.KS1, nr) && k <= A1(d.KS2, nr)) ft = 0.0f;
+            }
+        }
+        d.FLOWT[n] = ft;
+        d.TFLUX[n] = ft;
+    }
+    if (i < d.IM && j >= 2) {
+        float fr = 0.0f;
+        if (k >= 2 && k <= d.KMM1) {
+            float AVGRVX = A3(d.ROVX, i, j, k) + A3(d.ROVX, i, j - 1, k) + A3(d.ROVX, i + 1, j - 1, k) + A3(d.ROVX, i + 1, j, k);
+            float AVGRVR = A3(d.ROVR, i, j, k) + A3(d.ROVR, i, j - 1, k) + A3(d.ROVR, i + 1, j - 1, k) + A3(d.ROVR, i + 1, j, k);
+            fr = 0.25f * (AVGRVX * A3(d.ASX, i, j, k) + AVGRVR * A3(d.ASR, i, j, k));
+        }
+        d.FLOWR[n] = fr;
+        d.RFLUX[n] = fr;
+    }
+}
+
+void launch_flux_mass(const Dev &d, Launch L) {
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    k_flux_mass<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+}
+
+// ---------------------------------------------------------------------
+// energy fluxes (5501-5503) and their periodic balance (900)
+// ---------------------------------------------------------------------
+__device__ inline float tflux_energy_raw(const Dev &d, int i, int j, int k) {
+    float AVGHO = A3(d.HO, i, j, k) + A3(d.HO, i, j - 1, k) + A3(d.HO, i, j - 1, k + 1) + A3(d.HO, i, j, k + 1);
+    float AVGPB = A3(d.PEFF, i, j, k) + A3(d.PEFF, i, j - 1, k) + A3(d.PEFF, i, j - 1, k + 1) + A3(d.PEFF, i, j, k + 1);
+    return (A3(d.FLOWT, i, j, k) * AVGHO + A2(d.WRABT, j, k) * AVGPB) * 0.25f;
+}
+
+__global__ void k_flux_energy(Dev d) {
+    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, n, i, j, k);
+    if (i < d.IM && k < d.KM) {
+        float AVGHO = A3(d.HO, i, j, k) + A3(d.HO, i, j, k + 1) + A3(d.HO, i + 1, j, k) + A3(d.HO, i + 1, j, k + 1);
+        d.XFLUX[n] = d.FLOWX[n] * AVGHO * 0.25f;
+        if (j >= 2) d.SOURCE[n] = d.QSOURCE[n];
+    }
+    if (i < d.IM && j >= 2) {
+        float AVGHO = 0.25f * (A3(d.HO, i, j, k) + A3(d.HO, i, j - 1, k) + A3(d.HO, i + 1, j - 1, k) + A3(d.HO, i + 1, j, k));
+        d.RFLUX[n] = d.FLOWR[n] * AVGHO;
+    }
+    if (j >= 2 && k < d.KM) {
+        float tf = tflux_energy_raw(d, i, j, k);
+        if ((i == 1 || i == d.IM) && A1(d.IND, j) != 1) {
+            float t1 = (i == 1) ? tf : tflux_energy_raw(d, 1, j, k);
+            float tm = (i == d.IM) ? tf : tflux_energy_raw(d, d.IM, j, k);
+            tf = 0.5f * (t1 + tm);
+        }
+        d.TFLUX[n] = tf;
+    }
+}
+
+void launch_flux_energy(const Dev &d, Launch L) {
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    k_flux_energy<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+}
+
+// ---------------------------------------------------------------------
+// inlet and exit boundary conditions (4476-4734): one CTA.  The pitchwise
+// sums per K keep the reference's sequential order, and one thread runs
+// the radial-equilibrium recurrence for PD(K) (4533-4541).
+// ---------------------------------------------------------------------
+constexpr int BC_MAXK = 512;
+
+__global__ void __launch_bounds__(1024) k_bc(Dev d) {
+    __shared__ float s_pavg2[BC_MAXK], s_pavg3[BC_MAXK], s_pavgout[BC_MAXK], s_sum[BC_MAXK];
+    for (int k = threadIdx.x + 1; k <= d.KM; k += blockDim.x) {
+        float PAVG2 = 0.0f, PAVG3 = 0.0f, PAVGOUT = 0.0f, SUM = 0.0f;
+        float RJM = A2(d.R, d.JM, k);
+        for (int i = 1; i <= d.IMM1; ++i) {
+            float fp = A1(d.FP, i);
+            PAVG2 = PAVG2 + 0.5f * (A3(d.P, i, 2, k) + A3(d.P, i + 1, 2, k)) * fp;
+            PAVG3 = PAVG3 + 0.5f * (A3(d.P, i, 3, k) + A3(d.P, i + 1, 3, k)) * fp;
+            PAVGOUT = PAVGOUT + 0.5f * (A3(d.P, i, d.JMM1, k) + A3(d.P, i + 1, d.JMM1, k)) * fp;
+            SUM = SUM + 0.5f * fp *
+                            (A3(d.ROVT, i, d.JM, k) * A3(d.VT, i, d.JM, k) + A3(d.ROVT, i + 1, d.JM, k) * A3(d.VT, i + 1, d.JM, k)) /
+                            RJM;
+        }
+        s_pavg2[k - 1] = PAVG2;
+        s_pavg3[k - 1] = PAVG3;
+        s_pavgout[k - 1] = PAVGOUT;
+        s_sum[k - 1] = SUM;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && d.IPOUT <= 0) {
+        float PDIFF = 0.0f;
+        if (d.IPOUT == -1) PDIFF = d.PDOWN_TIP - A1(d.PD, d.KM);
+        float SUMP = 0.0f;
+        for (int k = 1; k <= d.KM; ++k) {
+            A1(d.PD, 1) = d.PDOWN_HUB;
+            if (k != 1) {
+                float DP = (s_sum[k - 1] + SUMP) * 0.5f * (A2(d.R, d.JM, k) - A2(d.R, d.JM, k - 1));
+                A1(d.PD, k) = 0.9f * A1(d.PD, k) + 0.1f * (A1(d.PD, k - 1) + DP);
+            }
+            SUMP = s_sum[k - 1];
+            if (d.IPOUT == -1) A1(d.PD, k) = A1(d.PD, k) + PDIFF;
+        }
+    }
+    __syncthreads();
+    int total = d.IM * d.KM;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        int i = t % d.IM + 1, k = t / d.IM + 1;
+        float PO1 = A1(d.PO1, k), TO1 = A1(d.TO1, k);
+        // inlet, isentropic from the stagnation state
+        float RO_STAG = PO1 / d.RGAS / TO1;
+        float RO_IN = A3(d.RO, i, 1, k);
+        if (RO_IN > 0.9999f * RO_STAG) RO_IN = 0.9999f * RO_STAG;
+        float PNEW = PO1 * powf(RO_IN / RO_STAG, d.GA);
+        float p1 = A3(d.P, i, 1, k);
+        int ip = d.IN_PRESS < 0 ? -d.IN_PRESS : d.IN_PRESS;
+        if (d.IN_PRESS == 0) p1 = d.RFIN1 * p1 + d.RFIN * PNEW;
+        if (ip == 1) p1 = d.RFIN1 * p1 + d.RFIN2 * A3(d.P, i, 2, k) - d.RFIN * A3(d.P, i, 3, k);
+        if (ip == 3) p1 = d.RFIN1 * p1 + d.RFIN2 * s_pavg2[k - 1] - d.RFIN * s_pavg3[k - 1];
+        if (ip == 4) p1 = d.RFIN1 * p1 + d.RFIN2 * A3(d.P, d.IMID, 2, d.KMID) - d.RFIN * A3(d.P, d.IMID, 3, d.KMID);
+        float plim = A1(d.PLIM, k);
+        if (p1 > plim) p1 = 0.9f * p1 + 0.1f * plim;
+        if (p1 > 0.99999f * PO1) p1 = PO1 * 0.99999f;
+        A3(d.P, i, 1, k) = p1;
+        float TSTATIC = TO1 * powf(p1 * A1(d.RPO1, k), d.FGA);
+        float VABSQ = 2.0f * d.CP * (TO1 - TSTATIC);
+        A3(d.T_STATIC, i, 1, k) = TSTATIC;
+        float VABS = sqrtf(VABSQ);
+        float VMER = 0.0f;
+        float vt1 = A3(d.VT, i, 1, k);
+        if (d.IN_VTAN == 0) {
+            VMER = VABS * A1(d.BSCOS, k);
+            vt1 = VABS * A1(d.BSSIN, k);
+        }
+        if (d.IN_VTAN == 1) {
+            float VMERSQ = VABSQ - A1(d.VTIN, k) * A1(d.VTIN, k);
+            if (VMERSQ < 0.01f) VMERSQ = 0.01f;
+            VMER = sqrtf(VMERSQ);
+            vt1 = A1(d.VTIN, k);
+        }
+        if (d.IN_VTAN == 2) {
+            float WR = A2(d.UBLADE, 1, k);
+            float VRELSQ = VABSQ - WR * WR * A1(d.BSCOS, k) * A1(d.BSCOS, k);
+            if (VRELSQ < 0.01f) VRELSQ = 0.01f;
+            float VREL = sqrtf(VRELSQ) - WR * A1(d.BSSIN, k);
+            VMER = VREL * A1(d.BSCOS, k);
+            vt1 = VREL * A1(d.BSSIN, k) + WR;
+        }
+        A3(d.VT, i, 1, k) = vt1;
+        float vx1 = A3(d.VX, i, 1, k), vr1 = A3(d.VR, i, 1, k);
+        float vr2 = A3(d.VR, i, 2, k);
+        if (d.IN_VR > 0) vx1 = VMER * A1(d.BRCOS, k);
+        float VXSQ = VMER * VMER - vr2 * vr2;
+        if (VXSQ < 0.0000001f * TO1 * d.CP) VXSQ = 0.0000001f * TO1 * d.CP;
+        if (d.IN_VR <= 0) vx1 = sqrtf(VXSQ);
+        if (d.IN_VR > 0) vr1 = VMER * A1(d.BRSIN, k);
+        if (d.IN_VR <= 0) vr1 = vr2;
+        A3(d.VX, i, 1, k) = vx1;
+        A3(d.VR, i, 1, k) = vr1;
+        float ro1 = p1 / (d.RGAS * TSTATIC);
+        float rovt1 = ro1 * vt1;
+        A3(d.RO, i, 1, k) = ro1;
+        A3(d.ROVT, i, 1, k) = rovt1;
+        A3(d.ROVR, i, 1, k) = ro1 * vr1;
+        A3(d.RORVT, i, 1, k) = rovt1 * A2(d.R, 1, k);
+        A3(d.ROVX, i, 1, k) = ro1 * vx1;
+        A3(d.ROE, i, 1, k) = p1 / d.GA1 + ro1 * 0.5f * VABSQ;
+        A3(d.HO, i, 1, k) = d.CP * TO1;
+        // exit: pitchwise pressure variation extrapolated from upstream
+        float vr = A3(d.VR, i, d.JM, k), vt = A3(d.VT, i, d.JM, k), vx = A3(d.VX, i, d.JM, k);
+        float EKE = 0.5f * (vr * vr + vt * vt + vx * vx);
+        float pe = A1(d.PD, k) + d.FEXTRAP * (A3(d.P, i, d.JMM1, k) - s_pavgout[k - 1]);
+        float hoe = 2.0f * A3(d.HO, i, d.JMM1, k) - A3(d.HO, i, d.JM - 2, k);
+        float TEXIT = (hoe - EKE) / d.CP;
+        float roe_ = pe / d.RGAS / TEXIT;
+        A3(d.P, i, d.JM, k) = pe;
+        A3(d.HO, i, d.JM, k) = hoe;
+        A3(d.RO, i, d.JM, k) = roe_;
+        A3(d.ROE, i, d.JM, k) = roe_ * (d.CV * TEXIT + EKE);
+    }
+}
+
+void launch_bc(const Dev &d, Launch L) { k_bc<<<1, 1024, 0, L.s>>>(d); }
+
+// ---------------------------------------------------------------------
+// PEFF = P - PREFF + F_PDOWN*(P(J+1)-P(J))  (4321)
+// ---------------------------------------------------------------------
+__global__ void k_peff(Dev d) {
+    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, n, i, j, k);
+    int jp1 = (j == d.JM) ? d.JM : j + 1;
+    float p = d.P[n];
+    d.PEFF[n] = p - d.PREFF + d.F_PDOWN * (A3(d.P, i, jp1, k) - p);
+}
+
+void launch_peff(const Dev &d, Launch L) {
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    k_peff<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+}
+
+// ---------------------------------------------------------------------
+// axial-momentum fluxes (6100-6120) and the cusp balance (6026)
+// ---------------------------------------------------------------------
+__global__ void k_flux_xmom(Dev d) {
+    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, n, i, j, k);
+    const float *PE = d.PEFF, *VX = d.VX;
+    if (i < d.IM && k < d.KM) {
+        d.SOURCE[n] = d.XFORCE[n];
+        float AVGP = A3(PE, i, j, k) + A3(PE, i, j, k + 1) + A3(PE, i + 1, j, k + 1) + A3(PE, i + 1, j, k);
+        float AVGVX = A3(VX, i, j, k) + A3(VX, i, j, k + 1) + A3(VX, i + 1, j, k + 1) + A3(VX, i + 1, j, k);
+        d.XFLUX[n] = 0.25f * (AVGP * A3(d.AQX, i, j, k) + d.FLOWX[n] * AVGVX);
+    }
+    if (i < d.IM && j >= 2) {
+        float AVGP = A3(PE, i, j, k) + A3(PE, i, j - 1, k) + A3(PE, i + 1, j - 1, k) + A3(PE, i + 1, j, k);
+        float AVGVX = A3(VX, i, j, k) + A3(VX, i, j - 1, k) + A3(VX, i + 1, j - 1, k) + A3(VX, i + 1, j, k);
+        d.RFLUX[n] = 0.25f * (AVGP * A3(d.ASX, i, j, k) + d.FLOWR[n] * AVGVX);
+    }
+    if (j >= 2 && k < d.KM) {
+        if ((i == 1 || i == d.IM) && A1(d.IND, j) != 1) {
+            int IM = d.IM;
+            float AVGPCUSP = A3(PE, 1, j, k) + A3(PE, 1, j - 1, k) + A3(PE, 1, j, k + 1) + A3(PE, 1, j - 1, k + 1) +
+                             A3(PE, IM, j, k) + A3(PE, IM, j - 1, k) + A3(PE, IM, j, k + 1) + A3(PE, IM, j - 1, k + 1);
+            float AVGVXCUSP = A3(VX, 1, j, k) + A3(VX, 1, j - 1, k) + A3(VX, 1, j, k + 1) + A3(VX, 1, j - 1, k + 1) +
+                              A3(VX, IM, j, k) + A3(VX, IM, j - 1, k) + A3(VX, IM, j, k + 1) + A3(VX, IM, j - 1, k + 1);
+            d.TFLUX[n] = 0.125f * (d.FLOWT[n] * AVGVXCUSP + AVGPCUSP * d.ABX[n]);
+        } else {
+            float AVGVX = A3(VX, i, j, k) + A3(VX, i, j - 1, k) + A3(VX, i, j - 1, k + 1) + A3(VX, i, j, k + 1);
+            float AVGP = A3(PE, i, j, k) + A3(PE, i, j - 1, k) + A3(PE, i, j - 1, k + 1) + A3(PE, i, j, k + 1);
+            d.TFLUX[n] = 0.25f * (d.FLOWT[n] * AVGVX + d.ABX[n] * AVGP);
+        }
+    }
+}
+
+void launch_flux_xmom(const Dev &d, Launch L) {
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    k_flux_xmom<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+}
+
+// ---------------------------------------------------------------------
+// moment-of-momentum fluxes (6200-6230) and periodic balance (902)
+// ---------------------------------------------------------------------
+__device__ inline float tflux_rvt_raw(const Dev &d, int i, int j, int k, float AVGR) {
+    const float *PE = d.PEFF, *VT = d.VT;
+    float AVGVT = A3(VT, i, j, k) + A3(VT, i, j - 1, k) + A3(VT, i, j - 1, k + 1) + A3(VT, i, j, k + 1);
+    float AVGP = A3(PE, i, j, k) + A3(PE, i, j - 1, k) + A3(PE, i, j - 1, k + 1) + A3(PE, i, j, k + 1);
+    return (A3(d.FLOWT, i, j, k) * AVGVT + A2(d.ABT, j, k) * AVGP) * AVGR;
+}
+
+__global__ void k_flux_rvt(Dev d) {
+    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, n, i, j, k);
+    const float *VT = d.VT;
+    if (i < d.IM && k < d.KM) {
+        float AVGR = 0.125f * (A2(d.R, j, k) + A2(d.R, j, k + 1));
+        float AVGVT = A3(VT, i, j, k) + A3(VT, i, j, k + 1) + A3(VT, i + 1, j, k) + A3(VT, i + 1, j, k + 1);
+        d.SOURCE[n] = d.TFORCE[n];
+        d.XFLUX[n] = d.FLOWX[n] * AVGR * AVGVT;
+    }
+    if (j >= 2 && k < d.KM) {
+        float AVGR = 0.25f * A2(d.RAVG_CELL, j, k);
+        float tf = tflux_rvt_raw(d, i, j, k, AVGR);
+        if ((i == 1 || i == d.IM) && A1(d.IND, j) != 1) {
+            float t1 = (i == 1) ? tf : tflux_rvt_raw(d, 1, j, k, AVGR);
+            float tm = (i == d.IM) ? tf : tflux_rvt_raw(d, d.IM, j, k, AVGR);
+            tf = 0.5f * (t1 + tm);
+        }
+        d.TFLUX[n] = tf;
+    }
+    if (i < d.IM && j >= 2) {
+        float AVGR = (A2(d.R, j, k) + A2(d.R, j - 1, k)) * 0.125f;
+        float AVGVT = A3(VT, i, j, k) + A3(VT, i, j - 1, k) + A3(VT, i + 1, j - 1, k) + A3(VT, i + 1, j, k);
+        d.RFLUX[n] = d.FLOWR[n] * AVGVT * AVGR;
+    }
+}
+
+void launch_flux_rvt(const Dev &d, Launch L) {
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    k_flux_rvt<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+}
+
+// ---------------------------------------------------------------------
+// radial-momentum fluxes and source (6300-6330), periodic balance (6260)
+// ---------------------------------------------------------------------
+__device__ inline float tflux_rmom_raw(const Dev &d, int i, int j, int k, float *avgp4) {
+    const float *PE = d.PEFF, *VR = d.VR;
+    float AVGVR = A3(VR, i, j, k) + A3(VR, i, j - 1, k) + A3(VR, i, j - 1, k + 1) + A3(VR, i, j, k + 1);
+    float AVGP = A3(PE, i, j, k) + A3(PE, i, j - 1, k) + A3(PE, i, j - 1, k + 1) + A3(PE, i, j, k + 1);
+    *avgp4 = AVGP;
+    return 0.25f * (A3(d.FLOWT, i, j, k) * AVGVR + AVGP * A3(d.ABR, i, j, k));
+}
+
+__global__ void k_flux_rmom(Dev d) {
+    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, n, i, j, k);
+    const float *PE = d.PEFF, *VR = d.VR, *VT = d.VT, *RV = d.ROVT;
+    if (i < d.IM && k < d.KM) {
+        float AVGVR = A3(VR, i, j, k) + A3(VR, i, j, k + 1) + A3(VR, i + 1, j, k) + A3(VR, i + 1, j, k + 1);
+        float AVGP = A3(PE, i, j, k) + A3(PE, i, j, k + 1) + A3(PE, i + 1, j, k + 1) + A3(PE, i + 1, j, k);
+        d.XFLUX[n] = 0.25f * (d.FLOWX[n] * AVGVR + A3(d.AQR, i, j, k) * AVGP);
+    }
+    if (j >= 2 && k < d.KM) {
+        float ap;
+        float tf = tflux_rmom_raw(d, i, j, k, &ap);
+        if ((i == 1 || i == d.IM) && A1(d.IND, j) != 1) {
+            int IM = d.IM;
+            float ap1, apm;
+            float t1raw = tflux_rmom_raw(d, 1, j, k, &ap1);
+            float tmraw = tflux_rmom_raw(d, IM, j, k, &apm);
+            float AVGP1 = 0.25f * (A3(PE, 1, j, k) + A3(PE, 1, j - 1, k) + A3(PE, 1, j, k + 1) + A3(PE, 1, j - 1, k + 1));
+            float AVGPM = 0.25f * (A3(PE, IM, j, k) + A3(PE, IM, j - 1, k) + A3(PE, IM, j, k + 1) + A3(PE, IM, j - 1, k + 1));
+            float T1 = t1raw - AVGP1 * A3(d.ABR, 1, j, k);
+            float T2 = tmraw - AVGPM * A3(d.ABR, IM, j, k);
+            tf = 0.5f * ((T1 + T2) + (AVGP1 + AVGPM) * A3(d.ABR, i, j, k));
+        }
+        d.TFLUX[n] = tf;
+    }
+    if (i < d.IM && j >= 2) {
+        float AVGVR = A3(VR, i, j, k) + A3(VR, i, j - 1, k) + A3(VR, i + 1, j - 1, k) + A3(VR, i + 1, j, k);
+        float AVGP = A3(PE, i, j, k) + A3(PE, i, j - 1, k) + A3(PE, i + 1, j - 1, k) + A3(PE, i + 1, j, k);
+        d.RFLUX[n] = 0.25f * (d.FLOWR[n] * AVGVR + A3(d.ASR, i, j, k) * AVGP);
+        if (k < d.KM) {
+            float AVGRVT = A3(RV, i, j, k) + A3(RV, i, j, k + 1) + A3(RV, i, j - 1, k) + A3(RV, i, j - 1, k + 1) +
+                           A3(RV, i + 1, j, k) + A3(RV, i + 1, j, k + 1) + A3(RV, i + 1, j - 1, k) + A3(RV, i + 1, j - 1, k + 1);
+            float AVGVT = 0.125f * (A3(VT, i, j, k) + A3(VT, i, j - 1, k) + A3(VT, i, j - 1, k + 1) + A3(VT, i, j, k + 1) +
+                                    A3(VT, i + 1, j, k) + A3(VT, i + 1, j - 1, k) + A3(VT, i + 1, j - 1, k + 1) +
+                                    A3(VT, i + 1, j, k + 1));
+            float AVGP8 = A3(PE, i, j, k) + A3(PE, i, j - 1, k) + A3(PE, i, j - 1, k + 1) + A3(PE, i, j, k + 1) +
+                          A3(PE, i + 1, j, k) + A3(PE, i + 1, j - 1, k) + A3(PE, i + 1, j - 1, k + 1) + A3(PE, i + 1, j, k + 1);
+            d.SOURCE[n] = d.RFORCE[n] - (AVGRVT * AVGVT + AVGP8) * d.VOLOR[n];
+        }
+    }
+}
+
+void launch_flux_rmom(const Dev &d, Launch L) {
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    k_flux_rmom<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+}
+
+// ---------------------------------------------------------------------
+// density limiter (7200): one thread per (I,K) line walks J in the
+// reference's order, since RO(J-1), RO(J-2) are already limited when RO(J)
+// is tested.  The thread owning (IMID,KMID) then sets the per-row Mach
+// limits VLIMIT/ROLIMIT (7250) from its final densities.
+// ---------------------------------------------------------------------
+__global__ void k_density_limiter(Dev d) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.IM * d.KM) return;
+    int i = t % d.IM + 1, k = t / d.IM + 1;
+    float *RO = d.RO;
+    float ROLIM = d.ROLIM;
+    if (d.JM - 3 >= 3) {
+        float rm2 = A3(RO, i, 1, k), rm1 = A3(RO, i, 2, k), r0 = A3(RO, i, 3, k);
+        float rp1 = A3(RO, i, 4, k);
+        for (int j = 3; j <= d.JM - 3; ++j) {
+            float rp2 = A3(RO, i, j + 2, k);
+            float ROAVG = 0.25f * (rm2 + rm1 + rp1 + rp2);
+            float ro = r0;
+            if (ro < 0.6f * ROAVG) ro = 0.5f * (ro + 0.6f * ROAVG);
+            if (ro > 1.5f * ROAVG) ro = 0.5f * (ro + 1.5f * ROAVG);
+            if (ro < ROLIM) ro = 0.5f * (ro + ROLIM);
+            if (ro != r0) A3(RO, i, j, k) = ro;
+            rm2 = rm1;
+            rm1 = ro;
+            r0 = rp1;
+            rp1 = rp2;
+        }
+    }
+    if (i == d.IMID && k == d.KMID) {
+        float GM1 = d.GA - 1.0f;
+        float TRATIO = 1.0f + d.MACHLIM * d.MACHLIM * 0.5f * GM1;
+        float RFGM1 = 1.0f / GM1;
+        float RORATIO = powf(TRATIO, RFGM1);
+        for (int nr = 1; nr <= d.NROWS; ++nr) {
+            int JREF = A1(d.JLE, nr);
+            float TREF = A3(d.T_STATIC, d.IMID, JREF, d.KMID);
+            float vx = A3(d.VX, d.IMID, JREF, d.KMID), vr = A3(d.VR, d.IMID, JREF, d.KMID), wt = A3(d.WT, d.IMID, JREF, d.KMID);
+            float WREFSQ = vx * vx + vr * vr + wt * wt;
+            float TOREL_REF = TREF + 0.5f * WREFSQ / d.CP;
+            float TLIMIT = TOREL_REF / TRATIO;
+            if (TLIMIT > d.TCOOL_MIN) TLIMIT = d.TCOOL_MIN;
+            A1(d.VLIMIT, nr) = sqrtf(2.0f * d.CP * (TOREL_REF - TLIMIT));
+            float ROSTAG_REL = A3(RO, d.IMID, JREF, d.KMID) * powf(TOREL_REF / TREF, RFGM1);
+            A1(d.ROLIMIT, nr) = ROSTAG_REL / RORATIO;
+        }
+    }
+}
+
+// Mach-number / relative-mass-flux limiter (7100)
+__global__ void k_mach_limiter(Dev d) {
+    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, n, i, j, k);
+    int nr = A1(d.NROW, j);
+    float V_LIMIT = A1(d.VLIMIT, nr), RO_LIMIT = A1(d.ROLIMIT, nr);
+    float ro = d.RO[n];
+    if (ro < RO_LIMIT) {
+        ro = RO_LIMIT;
+        d.RO[n] = ro;
+    }
+    float vx = d.VX[n], vr = d.VR[n], wt = d.WT[n];
+    float WRELSQ = vx * vx + vr * vr + wt * wt;
+    float WREL = sqrtf(WRELSQ);
+    float FACSAFE = V_LIMIT / WREL;
+    if (FACSAFE < 1.0f) {
+        d.ROVX[n] = ro * vx * FACSAFE;
+        d.ROVR[n] = ro * vr * FACSAFE;
+        float ROVTREL = ro * wt * FACSAFE;
+        d.ROWT[n] = ROVTREL;
+        float rovt = ROVTREL + ro * A2(d.UBLADE, j, k);
+        d.ROVT[n] = rovt;
+        d.RORVT[n] = rovt * A2(d.R, j, k);
+    }
+}
+
+void launch_limiters(const Dev &d, Launch L) {
+    int lines = d.IM * d.KM;
+    k_density_limiter<<<(lines + 127) / 128, 128, 0, L.s>>>(d);
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    k_mach_limiter<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+}
+
+// ---------------------------------------------------------------------
+// NEW_MIXPLAN (14922-15251), IFGAS=0: one thread per (row interface, K)
+// runs the reference's I loops in order, including the outward
+// Prandtl-Meyer sweeps for a supersonic relative flow.
+// ---------------------------------------------------------------------
+constexpr int MIX_MAXI = 160;
+
+__global__ void k_mixplan(Dev d) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.NRWSM1 * d.KM) return;
+    int nr = t / d.KM + 1, k = t % d.KM + 1;
+    float ALPHAA[MIX_MAXI], GAMA[MIX_MAXI], WREF_JP2[MIX_MAXI], ROREF_JP2[MIX_MAXI], PISENT[MIX_MAXI];
+    float ROISENT[MIX_MAXI], WMACH_JP2[MIX_MAXI], TISENT[MIX_MAXI], WIS_JP2[MIX_MAXI];
+    const int IM = d.IM;
+    float RFMIX1 = 1.0f - d.RFMIX;
+    int KSUB = (k == d.KM) ? d.KM - 1 : k;
+    int j = A1(d.JMIX, nr);
+    int JP1, JP2, JP3;
+    float F_ANGLE;
+    if (A3(d.FLOWX, d.IMID, j, KSUB) < 0.0f) {
+        JP1 = j + 1; JP2 = j + 2; JP3 = j + 3;
+        F_ANGLE = d.FANGLE;
+    } else {
+        j = A1(d.JMIX, nr) + 1;
+        JP1 = j - 1; JP2 = j - 2; JP3 = j - 3;
+        F_ANGLE = 0.0f;
+    }
+    float F_ANGLE1 = 1.0f - F_ANGLE;
+    float RJP1 = A2(d.R, JP1, k), UJP1 = A2(d.UBLADE, JP1, k);
+    float ROMIX = A3(d.RO, d.IMID, JP1, k);
+    float VXMIX = A3(d.ROVX, d.IMID, JP1, k) / ROMIX;
+    float VRMIX = A3(d.ROVR, d.IMID, JP1, k) / ROMIX;
+    float VTMIX = A3(d.RORVT, d.IMID, JP1, k) / ROMIX / RJP1;
+    float ROEMIX = A3(d.ROE, d.IMID, JP1, k);
+    float VMSQ = VXMIX * VXMIX + VRMIX * VRMIX;
+    float VABSQ = VMSQ + VTMIX * VTMIX;
+    float WTMIX = VTMIX - UJP1;
+    float WMIXSQ = VMSQ + WTMIX * WTMIX;
+    float WMIX = sqrtf(WMIXSQ);
+    float ALPHAMIX = asinf(WTMIX / WMIX);
+    float GAMAMIX = atan2f(VRMIX, VXMIX);
+    float TMIX = (ROEMIX / ROMIX - 0.5f * VABSQ) / d.CV;
+    float ROTHALPY = d.CP * TMIX + 0.5f * (WMIXSQ - UJP1 * UJP1);
+    float GAGAS = d.GA;
+    float PMIX = ROMIX * d.RGAS * TMIX;
+    int NMACH = 0;
+    float RJP2 = A2(d.R, JP2, k), UNOWJP2 = A2(d.UBLADE, JP2, k);
+    float RJP3 = A2(d.R, JP3, k), UNOWJP3 = A2(d.UBLADE, JP3, k);
+    for (int i = 1; i <= IM; ++i) {
+        float ROJP2 = A3(d.RO, i, JP2, k);
+        float XVELJP2 = A3(d.ROVX, i, JP2, k) / ROJP2;
+        float RVELJP2 = A3(d.ROVR, i, JP2, k) / ROJP2;
+        float TVELJP2 = A3(d.RORVT, i, JP2, k) / RJP2 / ROJP2;
+        float WTJP2 = TVELJP2 - UNOWJP2;
+        float VMSQJP2 = XVELJP2 * XVELJP2 + RVELJP2 * RVELJP2;
+        float VELSQJP2 = VMSQJP2 + TVELJP2 * TVELJP2;
+        float WACT_SQ_JP2 = VMSQJP2 + WTJP2 * WTJP2;
+        float WACT_JP2 = sqrtf(WACT_SQ_JP2);
+        float T_ACT_JP2 = (A3(d.ROE, i, JP2, k) / ROJP2 - 0.5f * VELSQJP2) / d.CV;
+        float ROJP3 = A3(d.RO, i, JP3, k);
+        float ROVXJP3 = A3(d.ROVX, i, JP3, k), ROVRJP3 = A3(d.ROVR, i, JP3, k);
+        float ROVTJP3 = A3(d.RORVT, i, JP3, k) / RJP3;
+        float ROWTJP3 = ROVTJP3 - UNOWJP3 * ROJP3;
+        float ROVMSQJP3 = ROVXJP3 * ROVXJP3 + ROVRJP3 * ROVRJP3;
+        float ROWRELSQJP3 = ROVMSQJP3 + ROWTJP3 * ROWTJP3;
+        float ROWRELJP3 = sqrtf(ROWRELSQJP3);
+        float ALPHAJP3 = asinf(ROWTJP3 / ROWRELJP3);
+        float GAMAJP3 = atan2f(ROVRJP3, ROVXJP3);
+        float PSTAT = ROJP2 * d.RGAS * T_ACT_JP2;
+        float TISENT_JP2 = TMIX * powf(PSTAT / PMIX, d.FGA);
+        float WIS_SQ_JP2 = 2.0f * (ROTHALPY - d.CP * TISENT_JP2 + 0.5f * UNOWJP2 * UNOWJP2);
+        ROISENT[i - 1] = PSTAT / d.RGAS / TISENT_JP2;
+        PISENT[i - 1] = PSTAT;
+        TISENT[i - 1] = TISENT_JP2;
+        if (WIS_SQ_JP2 < 1.0f) WIS_SQ_JP2 = 1.0f;
+        WIS_JP2[i - 1] = sqrtf(WIS_SQ_JP2);
+        WREF_JP2[i - 1] = WACT_JP2;
+        ROREF_JP2[i - 1] = ROJP2;
+        WMACH_JP2[i - 1] = WACT_JP2 / sqrtf(GAGAS * d.RGAS * T_ACT_JP2);
+        if (WMACH_JP2[i - 1] > 1.0f) NMACH = NMACH + 1;
+        ALPHAA[i - 1] = F_ANGLE1 * ALPHAMIX + F_ANGLE * ALPHAJP3;
+        GAMA[i - 1] = F_ANGLE1 * GAMAMIX + F_ANGLE * GAMAJP3;
+    }
+    if (NMACH != 0) {
+        float FROTN = 1.0f;
+        if (WTMIX < 0.0f) FROTN = -1.0f;
+        for (int i = d.IMID + 1; i <= IM; ++i) {
+            int a = i - 1, b = i - 2;   // 0-based I and I-1
+            if (WMACH_JP2[a] > 1.001f && WMACH_JP2[b] > 1.001f) {
+                float DELP = PISENT[a] - PISENT[b];
+                float DELTAI = sqrtf(WMACH_JP2[a] * WMACH_JP2[a] - 1.0f) / (ROREF_JP2[a] * WREF_JP2[a] * WREF_JP2[a]);
+                float DELTAIM1 = sqrtf(WMACH_JP2[b] * WMACH_JP2[b] - 1.0f) / (ROREF_JP2[b] * WREF_JP2[b] * WREF_JP2[b]);
+                ALPHAA[a] = ALPHAA[b] + FROTN * DELP * 0.5f * (DELTAI + DELTAIM1);
+            }
+        }
+        for (int i = d.IMID - 1; i >= 1; --i) {
+            int a = i - 1, b = i;       // I and I+1
+            if (WMACH_JP2[a] > 1.001f && WMACH_JP2[b] > 1.001f) {
+                float DELP = PISENT[a] - PISENT[b];
+                float DELTAI = sqrtf(WMACH_JP2[a] * WMACH_JP2[a] - 1.0f) / (ROREF_JP2[a] * WREF_JP2[a] * WREF_JP2[a]);
+                float DELTAIP1 = sqrtf(WMACH_JP2[b] * WMACH_JP2[b] - 1.0f) / (ROREF_JP2[b] * WREF_JP2[b] * WREF_JP2[b]);
+                ALPHAA[a] = ALPHAA[b] + FROTN * DELP * 0.5f * (DELTAI + DELTAIP1);
+            }
+        }
+        float ROTN = ALPHAA[IM - 1] - ALPHAA[0];
+        float SUMFP = 0.0f;
+        for (int i = 1; i <= IM; ++i) {
+            ALPHAA[i - 1] = ALPHAA[i - 1] - ROTN * (SUMFP - 0.5f);
+            SUMFP = SUMFP + A1(d.FP, i);
+        }
+    }
+    for (int i = 1; i <= IM; ++i) {
+        float RO_JP2 = ROISENT[i - 1];
+        float WT_JP2 = WIS_JP2[i - 1] * sinf(ALPHAA[i - 1]);
+        float VM_JP2 = WIS_JP2[i - 1] * cosf(ALPHAA[i - 1]);
+        float VX_JP2 = VM_JP2 * cosf(GAMA[i - 1]);
+        float VR_JP2 = VM_JP2 * sinf(GAMA[i - 1]);
+        float VT_JP2 = WT_JP2 + UNOWJP2;
+        float V_JP2_SQ = VM_JP2 * VM_JP2 + VT_JP2 * VT_JP2;
+        float ROE_JP2 = ROISENT[i - 1] * (d.CV * TISENT[i - 1] + 0.5f * V_JP2_SQ);
+        A3(d.RO, i, JP2, k) = RFMIX1 * A3(d.RO, i, JP2, k) + d.RFMIX * RO_JP2;
+        A3(d.ROVX, i, JP2, k) = RFMIX1 * A3(d.ROVX, i, JP2, k) + d.RFMIX * RO_JP2 * VX_JP2;
+        A3(d.ROVR, i, JP2, k) = RFMIX1 * A3(d.ROVR, i, JP2, k) + d.RFMIX * RO_JP2 * VR_JP2;
+        A3(d.RORVT, i, JP2, k) = RFMIX1 * A3(d.RORVT, i, JP2, k) + d.RFMIX * RO_JP2 * VT_JP2 * RJP2;
+        A3(d.ROE, i, JP2, k) = RFMIX1 * A3(d.ROE, i, JP2, k) + d.RFMIX * ROE_JP2;
+    }
+}
+
+void launch_mixplan(const Dev &d, Launch L) {
+    if (!(d.IFMIX > 0 && d.RFMIX > 1.0e-3f) || d.NRWSM1 <= 0) return;
+    int n = d.NRWSM1 * d.KM;
+    k_mixplan<<<(n + 63) / 64, 64, 0, L.s>>>(d);
+}
+
+}  // namespace mgpu

@@ -1,0 +1,159 @@
+// mgpu_internal.cuh -- device-side description of one Multall flow problem.
+//
+// Every COMMON array of the loop lives in HBM in the reference's packed
+// Fortran order (I fastest, then J, then K), so one node (I,J,K) is
+// element (I-1) + IM*((J-1) + JM*(K-1)) and a warp reads 32 consecutive
+// pitchwise points.  Kernels take the whole description by value (`Dev`,
+// ~1.5 KB of kernel parameters: pointers, dimensions and the constant
+// REAL scalars); the values that change from step to step (smoothing ramp,
+// NSTEP, the 5-step flags, the monitors) live in a small device struct
+// `DevCtl` that the first kernel of each step updates, so a step is a fixed
+// launch sequence that can be captured once in a CUDA graph.
+//
+// Indices in kernel code are the reference's 1-based ones.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/mgpu.h"
+#include "../../include/mgpu_common_table.h"
+
+namespace mgpu {
+
+#define MGPU_T_INT32 int32_t
+#define MGPU_T_FLOAT32 float
+
+// Reduction slots written by the step and read back by the host.
+struct DevMon {
+    double vrms;            // sum of |W|^2 (VRMS)
+    unsigned long long vmax_key;
+    double eavg_sum;
+    unsigned long long emax_key;
+    int health;
+    int pad;
+};
+
+// State that changes from step to step; one per problem, in device memory.
+struct DevCtl {
+    int nstep;        // NSTEP
+    int ifend;        // IFEND after the convergence test of this step
+    int force_end;    // host request: make this the final step
+    int do_tail;      // every-5-step tail runs on this step
+    int do_loss;      // LOSS runs on this step
+    int damp_on;      // negative feedback active (2 <= DAMP <= 100)
+    int converged;    // the reference's convergence test met at a tail
+    int pad0;
+    float SFT, SFX, DAMP, FMIXUP;
+    float SFT1, SFTH, SFX1, SFXH, SFX14, SFXB, SFXB1, SFXBH, SFXHM1;
+    float VISLAM, FTCOND;
+    float EMAX, EAVG, ECONT, VMAX, VREF;
+    int IMAXE, JMAXE, KMAXE, JCONT, IVMAX, JVMAX, KVMAX;
+    int health;
+    double flow_in, flow_out;
+    DevMon mon;
+};
+
+struct Dev {
+    // dimensions
+    int IM, JM, KM, NROWS;
+    int IMM1, JMM1, KMM1, IMM2, JMM2, KMM2, IMID, KMID, NRWSM1;
+    // COMMON integer and real scalars (include/mgpu_common_table.h)
+#define MGPU_DEV_I(n, d) int n;
+    MGPU_INT_SCALARS(MGPU_DEV_I)
+#define MGPU_DEV_R(n, d) float n;
+    MGPU_REAL_SCALARS(MGPU_DEV_R)
+    // gas constants and loop constants (SETUP 6459-6468, LOOP 3677-3709)
+    float GA1, FGA, RFGA, RCP, CV, RCV, RGAS;
+    float RO_REF, ROLIM, RIJKM, PREFF, RFIN1, RFIN2, TCOOL_MIN;
+    // COMMON arrays on the device
+#define MGPU_DEV_A(n, t, s, r) MGPU_T_##t *n;
+    MGPU_ARRAYS(MGPU_DEV_A)
+    // loop work arrays (COMMON scratch of the reference)
+    float *XFLUX, *TFLUX, *RFLUX, *SOURCE, *FLOWX, *FLOWT, *FLOWR;
+    float *STORE, *TMP, *TEMP1;
+    float *PLIM;                       // (KM)
+    float *FILAM, *FITURB, *FIWAKE, *FIUP, *FKLAM, *FKTURB;   // (NROWS, IM|KM)
+    float *VLIMIT, *ROLIMIT;           // (NROWS)
+    float *B1CHG, *B2CHG;              // MG1 / MG2 shaped
+    double *plane_sum;                 // (JM) per-J-plane sums of STORE
+    double *plane_abs;                 // (JM) per-J-plane sums of |STORE|
+    float *AVG_BLK;                    // (NROWS)
+    double *BLADE_FLOW;                // (JM)
+    // per-block reduction partials of the 5-step tail
+    double *part_sum;
+    unsigned long long *part_key;
+    int *part_cnt;
+    int nparts;
+    // multigrid block extents (host-derived from JB1/JB2)
+    int *JB1_START, *JB1_END, *JB2_START, *JB2_END;    // (NJBn)
+    int *IB1_S, *IB1_E, *IB2_S, *IB2_E;                 // (NIBn) I extent of each block
+    int *KB1_S, *KB1_E, *KB2_S, *KB2_E;                 // (NKBn) K extent of each block
+    int *SB_START, *SB_END;                             // (NSBLK)
+    DevCtl *ctl;
+};
+
+__host__ __device__ inline size_t ix3(const Dev &d, int i, int j, int k) {
+    return (size_t)(i - 1) + (size_t)d.IM * ((size_t)(j - 1) + (size_t)d.JM * (size_t)(k - 1));
+}
+__host__ __device__ inline size_t ix2(const Dev &d, int j, int k) {
+    return (size_t)(j - 1) + (size_t)d.JM * (size_t)(k - 1);
+}
+__host__ __device__ inline size_t ixik(const Dev &d, int i, int k) {
+    return (size_t)(i - 1) + (size_t)d.IM * (size_t)(k - 1);
+}
+__host__ __device__ inline size_t ixij(const Dev &d, int i, int j) {
+    return (size_t)(i - 1) + (size_t)d.IM * (size_t)(j - 1);
+}
+
+// 1-based accessors used by the kernels, e.g. A3(d.RO, i, j, k)
+#define A3(p, i, j, k) (p)[ix3(d, (i), (j), (k))]
+#define A2(p, j, k) (p)[ix2(d, (j), (k))]
+#define AIK(p, i, k) (p)[ixik(d, (i), (k))]
+#define AIJ(p, i, j) (p)[ixij(d, (i), (j))]
+#define A1(p, x) (p)[(x) - 1]
+
+// Decomposes a linear node index n (I fastest) into 1-based (i, j, k).
+__device__ inline void node_ijk(const Dev &d, size_t n, int &i, int &j, int &k) {
+    i = (int)(n % (size_t)d.IM) + 1;
+    size_t q = n / (size_t)d.IM;
+    j = (int)(q % (size_t)d.JM) + 1;
+    k = (int)(q / (size_t)d.JM) + 1;
+}
+
+// Order-preserving key for "largest value, earliest index wins": the value
+// must be >= 0 (squares, absolute values); NaN counts as smallest.
+__device__ inline unsigned long long max_key(float v, size_t lin) {
+    if (!(v >= 0.0f)) return 0ull;
+    return ((unsigned long long)__float_as_uint(v) << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)lin);
+}
+
+// ---------------------------------------------------------------------
+// kernel launch wrappers (defined in the .cu files); each enqueues on s
+// ---------------------------------------------------------------------
+struct Launch {
+    cudaStream_t s;
+    int sm_count;
+};
+
+void launch_step_begin(const Dev &d, Launch L);
+void launch_prim(const Dev &d, Launch L);
+void launch_loss(const Dev &d, Launch L, bool init_call);
+void launch_flux_mass(const Dev &d, Launch L);
+void launch_flux_energy(const Dev &d, Launch L);
+void launch_bc(const Dev &d, Launch L);
+void launch_peff(const Dev &d, Launch L);
+void launch_flux_xmom(const Dev &d, Launch L);
+void launch_flux_rvt(const Dev &d, Launch L);
+void launch_flux_rmom(const Dev &d, Launch L);
+void launch_tstep(const Dev &d, Launch L, float *D, float *DIFF);
+void launch_limiters(const Dev &d, Launch L);
+void launch_mixplan(const Dev &d, Launch L);
+void launch_tail(const Dev &d, Launch L);
+void launch_stepup(const Dev &d, Launch L, float relax, bool gated);
+void launch_integrals(const Dev &d, Launch L, double *out8);
+
+// sets per-kernel attributes (dynamic shared memory of the J-plane kernel)
+cudaError_t configure_kernels(const Dev &d);
+
+}  // namespace mgpu

@@ -1,0 +1,179 @@
+"""ctypes binding of libmgpu.so (the C ABI in include/mgpu.h).
+
+`Problem` binds one case's COMMON data to a device handle by name, performs
+the calls SETUP makes into the hot path (STEPUP(1.0), the first LOSS) and
+then marches.  There is no CPU fallback: if the CUDA library cannot be
+loaded, or no GPU is present, the constructor raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import build as _build
+
+MGPU_OK = 0
+
+
+class Monitors(ctypes.Structure):
+    _fields_ = [("nstep", ctypes.c_int32), ("tail_ran", ctypes.c_int32), ("ifend", ctypes.c_int32),
+                ("health", ctypes.c_int32), ("emax", ctypes.c_float), ("imax", ctypes.c_int32),
+                ("jmax", ctypes.c_int32), ("kmax", ctypes.c_int32), ("eavg", ctypes.c_float),
+                ("econt", ctypes.c_float), ("jcont", ctypes.c_int32), ("vref", ctypes.c_float),
+                ("vmax", ctypes.c_float), ("ivmax", ctypes.c_int32), ("jvmax", ctypes.c_int32),
+                ("kvmax", ctypes.c_int32), ("flow_in", ctypes.c_double), ("flow_out", ctypes.c_double)]
+
+
+class Integrals(ctypes.Structure):
+    _fields_ = [("mass_flow_in", ctypes.c_double), ("mass_flow_out", ctypes.c_double),
+                ("eta_tt", ctypes.c_double), ("eta_ts", ctypes.c_double), ("po_ratio", ctypes.c_double),
+                ("to_ratio", ctypes.c_double), ("j1", ctypes.c_int32), ("j2m1", ctypes.c_int32)]
+
+
+# every entry point include/mgpu.h declares
+EXPORTS = ["mgpu_abi_version", "mgpu_last_error", "mgpu_device_count", "mgpu_create", "mgpu_destroy",
+           "mgpu_set_int", "mgpu_set_real", "mgpu_set_array", "mgpu_get_array", "mgpu_get_real", "mgpu_get_int",
+           "mgpu_commit", "mgpu_stepup", "mgpu_loss_init", "mgpu_step", "mgpu_run", "mgpu_sync",
+           "mgpu_integrals_compute", "mgpu_kernels_per_step"]
+
+_lib = None
+
+
+def load(build: bool = True):
+    """Loads libmgpu.so (building it in-tree first if needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build() if build else _build.LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"libmgpu.so not found at {path}; the CUDA library is required")
+    L = ctypes.CDLL(path)
+    vp, cp, i32 = ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int32
+    L.mgpu_abi_version.restype = i32
+    L.mgpu_last_error.argtypes = [ctypes.c_char_p, i32]
+    L.mgpu_device_count.restype = i32
+    L.mgpu_create.argtypes = [i32, i32, i32, i32, ctypes.POINTER(vp)]
+    L.mgpu_destroy.argtypes = [vp]
+    L.mgpu_destroy.restype = None
+    L.mgpu_set_int.argtypes = [vp, cp, i32]
+    L.mgpu_set_real.argtypes = [vp, cp, ctypes.c_float]
+    L.mgpu_set_array.argtypes = [vp, cp, vp, ctypes.c_int64]
+    L.mgpu_get_array.argtypes = [vp, cp, vp, ctypes.c_int64]
+    L.mgpu_get_real.argtypes = [vp, cp, ctypes.POINTER(ctypes.c_float)]
+    L.mgpu_get_int.argtypes = [vp, cp, ctypes.POINTER(i32)]
+    L.mgpu_commit.argtypes = [vp]
+    L.mgpu_stepup.argtypes = [vp, ctypes.c_float]
+    L.mgpu_loss_init.argtypes = [vp]
+    L.mgpu_step.argtypes = [vp, i32, ctypes.POINTER(Monitors)]
+    L.mgpu_run.argtypes = [vp, i32, ctypes.POINTER(Monitors)]
+    L.mgpu_sync.argtypes = [vp]
+    L.mgpu_integrals_compute.argtypes = [vp, ctypes.POINTER(Integrals)]
+    L.mgpu_kernels_per_step.argtypes = [vp, i32]
+    for f in EXPORTS:
+        fn = getattr(L, f)
+        if f != "mgpu_destroy":
+            fn.restype = i32
+    _lib = L
+    return L
+
+
+class MgpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"mgpu error {code}: {msg}")
+        self.code = code
+
+
+def last_error() -> str:
+    buf = ctypes.create_string_buffer(1024)
+    load().mgpu_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def _chk(rc: int) -> int:
+    if rc < 0:
+        raise MgpuError(rc, last_error())
+    return rc
+
+
+class Problem:
+    """One flow problem resident on the current GPU."""
+
+    def __init__(self, cd, setup_calls: bool = True):
+        L = load()
+        n = L.mgpu_device_count()
+        if n <= 0:
+            raise MgpuError(n, "no CUDA device visible: the GPU library has no CPU fallback")
+        self.cd = cd
+        h = ctypes.c_void_p()
+        _chk(L.mgpu_create(cd.im, cd.jm, cd.km, cd.nrows, ctypes.byref(h)))
+        self.h = h
+        for k, v in cd.ints.items():
+            _chk(L.mgpu_set_int(self.h, k.encode(), int(v)))
+        for k, v in cd.reals.items():
+            _chk(L.mgpu_set_real(self.h, k.encode(), float(v)))
+        for k, a in cd.arrays.items():
+            a = np.ascontiguousarray(a)
+            _chk(L.mgpu_set_array(self.h, k.encode(), a.ctypes.data, a.nbytes))
+        _chk(L.mgpu_commit(self.h))
+        if setup_calls:
+            self.setup_calls()
+
+    def setup_calls(self):
+        """STEPUP(1.0) and the first LOSS, as SETUP makes them."""
+        _chk(load().mgpu_stepup(self.h, 1.0))
+        _chk(load().mgpu_loss_init(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().mgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, force_end: bool = False, check: bool = True) -> Monitors:
+        m = Monitors()
+        rc = load().mgpu_step(self.h, 1 if force_end else 0, ctypes.byref(m))
+        if check:
+            _chk(rc)
+        return m
+
+    def run(self, nsteps: int) -> tuple[int, Monitors]:
+        m = Monitors()
+        rc = _chk(load().mgpu_run(self.h, int(nsteps), ctypes.byref(m)))
+        return rc, m
+
+    def sync(self):
+        _chk(load().mgpu_sync(self.h))
+
+    def get(self, name: str) -> np.ndarray:
+        ref = self.cd.arrays.get(name)
+        if ref is not None:
+            out = np.zeros(ref.shape, ref.dtype)
+        else:
+            out = np.zeros((self.cd.km, self.cd.jm, self.cd.im), np.float32)
+        _chk(load().mgpu_get_array(self.h, name.encode(), out.ctypes.data, out.nbytes))
+        return out
+
+    def set(self, name: str, a: np.ndarray):
+        a = np.ascontiguousarray(a)
+        _chk(load().mgpu_set_array(self.h, name.encode(), a.ctypes.data, a.nbytes))
+
+    def get_real(self, name: str) -> float:
+        v = ctypes.c_float()
+        _chk(load().mgpu_get_real(self.h, name.encode(), ctypes.byref(v)))
+        return v.value
+
+    def integrals(self) -> Integrals:
+        o = Integrals()
+        _chk(load().mgpu_integrals_compute(self.h, ctypes.byref(o)))
+        return o
+
+    def kernels_per_step(self) -> int:
+        return _chk(load().mgpu_kernels_per_step(self.h, 0))

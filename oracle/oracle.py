@@ -1,0 +1,144 @@
+"""ctypes driver for the CPU oracle (liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, never by the product path.  The oracle is a
+serial C++ restatement of Multall's LOOP (see multall_oracle.cpp) driven
+through the same COMMON-name interface as the GPU library, so a test binds
+one CommonData to both and compares.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+
+class Monitors(ctypes.Structure):
+    _fields_ = [("nstep", ctypes.c_int32), ("tail_ran", ctypes.c_int32), ("ifend", ctypes.c_int32),
+                ("health", ctypes.c_int32), ("emax", ctypes.c_float), ("imax", ctypes.c_int32),
+                ("jmax", ctypes.c_int32), ("kmax", ctypes.c_int32), ("eavg", ctypes.c_float),
+                ("econt", ctypes.c_float), ("jcont", ctypes.c_int32), ("vref", ctypes.c_float),
+                ("vmax", ctypes.c_float), ("ivmax", ctypes.c_int32), ("jvmax", ctypes.c_int32),
+                ("kvmax", ctypes.c_int32), ("flow_in", ctypes.c_double), ("flow_out", ctypes.c_double)]
+
+
+class Integrals(ctypes.Structure):
+    _fields_ = [("mass_flow_in", ctypes.c_double), ("mass_flow_out", ctypes.c_double),
+                ("eta_tt", ctypes.c_double), ("eta_ts", ctypes.c_double), ("po_ratio", ctypes.c_double),
+                ("to_ratio", ctypes.c_double), ("j1", ctypes.c_int32), ("j2m1", ctypes.c_int32)]
+
+
+def build(force: bool = False) -> str:
+    """Compiles liboracle.so with the recipe in oracle/Makefile."""
+    src = os.path.join(HERE, "multall_oracle.cpp")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        vp, cp = ctypes.c_void_p, ctypes.c_char_p
+        L.oref_create.restype = vp
+        L.oref_create.argtypes = [ctypes.c_int32] * 5
+        L.oref_destroy.argtypes = [vp]
+        L.oref_last_error.restype = cp
+        L.oref_set_int.argtypes = [vp, cp, ctypes.c_int32]
+        L.oref_set_real.argtypes = [vp, cp, ctypes.c_double]
+        L.oref_get_real.argtypes = [vp, cp, ctypes.POINTER(ctypes.c_double)]
+        L.oref_get_int.argtypes = [vp, cp, ctypes.POINTER(ctypes.c_int32)]
+        L.oref_set_array.argtypes = [vp, cp, vp, ctypes.c_int64]
+        L.oref_get_array.argtypes = [vp, cp, vp, ctypes.c_int64, ctypes.c_int32]
+        L.oref_commit.argtypes = [vp]
+        L.oref_stepup.argtypes = [vp, ctypes.c_double]
+        L.oref_loss_init.argtypes = [vp]
+        L.oref_step.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(Monitors)]
+        L.oref_integrals.argtypes = [vp, ctypes.POINTER(Integrals)]
+        for f in ("oref_set_int", "oref_set_real", "oref_get_real", "oref_get_int", "oref_set_array",
+                  "oref_get_array", "oref_commit", "oref_stepup", "oref_loss_init", "oref_step",
+                  "oref_integrals"):
+            getattr(L, f).restype = ctypes.c_int32
+        _lib = L
+    return _lib
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+class Oracle:
+    """One oracle problem (float or double arithmetic)."""
+
+    def __init__(self, cd, double: bool = False):
+        L = lib()
+        self.cd = cd
+        self.double = double
+        self.h = L.oref_create(cd.im, cd.jm, cd.km, cd.nrows, 1 if double else 0)
+        if not self.h:
+            raise OracleError(L.oref_last_error().decode())
+        for k, v in cd.ints.items():
+            self._chk(L.oref_set_int(self.h, k.encode(), int(v)))
+        for k, v in cd.reals.items():
+            self._chk(L.oref_set_real(self.h, k.encode(), float(v)))
+        for k, a in cd.arrays.items():
+            a = np.ascontiguousarray(a)
+            self._chk(L.oref_set_array(self.h, k.encode(), a.ctypes.data, a.nbytes))
+        self._chk(L.oref_commit(self.h))
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise OracleError(f"oracle error {rc}: {lib().oref_last_error().decode()}")
+        return rc
+
+    def close(self):
+        if self.h:
+            lib().oref_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def setup_calls(self):
+        """The two hot-path calls SETUP makes: STEPUP(1.0), then LOSS."""
+        self._chk(lib().oref_stepup(self.h, 1.0))
+        self._chk(lib().oref_loss_init(self.h))
+
+    def step(self, force_end: bool = False, check: bool = True) -> Monitors:
+        m = Monitors()
+        rc = lib().oref_step(self.h, 1 if force_end else 0, ctypes.byref(m))
+        if check:
+            self._chk(rc)
+        return m
+
+    def get(self, name: str, double: bool = True) -> np.ndarray:
+        ref = self.cd.arrays.get(name)
+        shape = ref.shape if ref is not None else (self.cd.km, self.cd.jm, self.cd.im)
+        dt = np.float64 if double else (ref.dtype if ref is not None else np.float32)
+        out = np.zeros(shape, dt)
+        self._chk(lib().oref_get_array(self.h, name.encode(), out.ctypes.data, out.nbytes, 1 if double else 0))
+        return out
+
+    def get_real(self, name: str) -> float:
+        v = ctypes.c_double()
+        self._chk(lib().oref_get_real(self.h, name.encode(), ctypes.byref(v)))
+        return v.value
+
+    def integrals(self) -> Integrals:
+        o = Integrals()
+        self._chk(lib().oref_integrals(self.h, ctypes.byref(o)))
+        return o

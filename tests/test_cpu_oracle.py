@@ -1,0 +1,165 @@
+"""CPU tests: the oracle's own invariants, the host-side setup, and the C
+ABI library's symbol table (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from helpers import rel_linf
+
+
+@pytest.fixture(scope="module")
+def mods():
+    from mgpu import case, common_setup
+    import oracle as O
+    O.build()
+    return case, common_setup, O
+
+
+def test_setup_geometry_closes(mods):
+    """Face areas close each cell: the divergence of a constant field is
+    zero in x (the reference checks this, commented out, at
+    multall-open-18.3.f:6727-6733).  The mixing-plane cell J=JMIX+1 is
+    excluded: its upstream faces use the theta extrapolated from the next
+    row (TEMP1, multall-open-18.3.f:3025-3035), so it does not close."""
+    case, common_setup, O = mods
+    cd = common_setup.build_common(case.small_stage())
+    a = cd.arrays
+    K, J, I = cd.km, cd.jm, cd.im
+    xarea = (a["AQX"][:K - 1, 1:, :I - 1] - a["AQX"][:K - 1, :-1, :I - 1] + a["ABX"][:K - 1, 1:, :I - 1]
+             - a["ABX"][:K - 1, 1:, 1:] + a["ASX"][:K - 1, 1:, :I - 1] - a["ASX"][1:, 1:, :I - 1])
+    scale = np.abs(a["AQX"]).max()
+    for jmix in a["JMIX"][:-1]:
+        xarea[:, int(jmix) + 1 - 2, :] = 0.0
+    assert np.abs(xarea).max() <= 1e-4 * scale
+    assert (a["VOL"][:K - 1, 1:, :I - 1] > 0).all()
+
+
+def test_oracle_float_vs_double_one_step(mods):
+    """REAL*4 and REAL*8 restatements agree to 1e-4 after one step (the
+    FP32 rounding of cancelling face fluxes, not a code difference)."""
+    case, common_setup, O = mods
+    cd = common_setup.build_common(case.small_stage())
+    of, od = O.Oracle(cd), O.Oracle(cd, double=True)
+    of.setup_calls()
+    od.setup_calls()
+    of.step()
+    od.step()
+    for n in ("RO", "ROE", "ROVX", "RORVT", "ROVR"):
+        assert rel_linf(of.get(n), od.get(n)) < 1e-4, n
+
+
+def test_oracle_periodic_and_mixing_plane(mods):
+    """After a step, non-blade J-planes are periodic (D(1)=D(IM)) and the
+    two faces of the mixing plane are pitchwise uniform.  The exit plane
+    J=JM is excluded: the exit condition, applied after TSTEP, rebuilds it
+    from HO(JM-1) of the step's start (multall-open-18.3.f:4701-4728)."""
+    case, common_setup, O = mods
+    cd = common_setup.build_common(case.small_stage())
+    o = O.Oracle(cd)
+    o.setup_calls()
+    o.step()
+    ro = o.get("RO", double=False)
+    ind = cd.arrays["IND"]
+    indle = cd.arrays["INDLE"]
+    for j in range(cd.jm - 1):
+        if ind[j] != 1 and indle[j] != 1:
+            assert np.array_equal(ro[:, j, 0], ro[:, j, -1]), j
+    jmix = int(cd.arrays["JMIX"][0])
+    for jj in (jmix, jmix + 1):
+        plane = ro[:, jj - 1, :]
+        assert np.all(plane == plane[:, :1])
+
+
+def test_oracle_converges(mods):
+    """The small stage converges: continuity error below 1 % and the
+    residual EAVG falls by orders of magnitude."""
+    case, common_setup, O = mods
+    cd = common_setup.build_common(case.small_stage())
+    cd.ints["NCHANGE"] = 200
+    cd.ints["NMIXUP"] = 200
+    o = O.Oracle(cd)
+    o.setup_calls()
+    first = None
+    for n in range(1500):
+        m = o.step()
+        if m.tail_ran and first is None:
+            first = m.eavg
+    assert m.econt < 0.01
+    assert m.eavg < 0.01 * first
+    it = o.integrals()
+    assert 0.5 < it.eta_tt < 1.0
+
+
+def test_oracle_rejects_uncovered_options(mods):
+    case, common_setup, O = mods
+    cd = common_setup.build_common(case.small_nozzle())
+    cd.ints["IFGAS"] = 1
+    with pytest.raises(O.OracleError):
+        O.Oracle(cd)
+
+
+def test_golden_regression(mods):
+    """The oracle reproduces the committed fixture (tests/golden, made by
+    tests/golden/make_golden.py) bit for bit: a guard against unintended
+    changes to the restatement."""
+    case, common_setup, O = mods
+    path = os.path.join(os.path.dirname(__file__), "golden", "small_stage_10steps.npz")
+    g = np.load(path)
+    cd = common_setup.build_common(case.small_stage())
+    o = O.Oracle(cd)
+    o.setup_calls()
+    for _ in range(10):
+        o.step()
+    for n in g.files:
+        assert np.array_equal(o.get(n, double=False), g[n]), n
+
+
+def test_abi_library_exports_every_declared_symbol():
+    """libmgpu.so loads without a GPU and exports each function
+    include/mgpu.h declares."""
+    from mgpu import build, lib
+    path = build.build()
+    L = ctypes.CDLL(path)
+    hdr = open(os.path.join(os.path.dirname(__file__), "..", "include", "mgpu.h")).read()
+    declared = set(re.findall(r"\b(mgpu_[a-z_]+)\s*\(", hdr))
+    assert declared == set(lib.EXPORTS)
+    for name in declared:
+        assert hasattr(L, name), name
+    assert L.mgpu_abi_version() == 1
+
+
+def test_gloo_two_ranks_shard_instances():
+    """Batched instances shard across ranks with no data-path collective:
+    each of two gloo ranks steps its own instance on the CPU oracle and the
+    ranks only gather the per-instance node counts."""
+    import torch.multiprocessing as mp
+    mp.spawn(_rank_main, args=(2,), nprocs=2, join=True)
+
+
+def _rank_main(rank, world):
+    import os
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    sys.path.insert(0, os.path.join(here, "..", "multall-open-18.3_gb300"))
+    sys.path.insert(0, os.path.join(here, "..", "oracle"))
+    import torch
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    os.environ.setdefault("MASTER_PORT", "29533")
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from mgpu import case, common_setup
+    import oracle as O
+    spec = case.small_stage(seed=10 + rank)
+    cd = common_setup.build_common(spec)
+    o = O.Oracle(cd)
+    o.setup_calls()
+    for _ in range(5):
+        m = o.step()
+    t = torch.tensor([float(cd.nodes()), float(m.flow_in)])
+    out = [torch.zeros(2) for _ in range(world)]
+    dist.all_gather(out, t)
+    assert all(x[0] > 0 for x in out)
+    dist.destroy_process_group()

@@ -1,0 +1,161 @@
+"""GPU parity: the sm_103a library, called through its C ABI, against the
+CPU oracle on the same seeded cases.
+
+Tolerance (the stated bar for the plain FP32 path): after one step every
+updated field agrees with the FP32 oracle to an L-infinity relative
+difference <= 1e-5.  Residual differences come only from the order of the
+long reductions (superblock multigrid sums and row averages in FP64 on the
+GPU, sequential REAL*4 in the reference) and from the last-ulp differences of
+CUDA's pow/asin/atan2/sin/cos against the host C library; every other
+expression keeps the reference's evaluation order without FMA.
+"""
+import numpy as np
+import pytest
+
+from helpers import FORCES, STATE, rel_linf
+
+pytestmark = pytest.mark.gpu
+
+STEP1_TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def mods():
+    from mgpu import case, common_setup, lib
+    import oracle as O
+    lib.load()
+    return case, common_setup, lib, O
+
+
+def _pair(mods, spec, **over):
+    case, common_setup, lib, O = mods
+    cd = common_setup.build_common(spec)
+    for k, v in over.items():
+        if k in cd.ints:
+            cd.ints[k] = v
+        else:
+            cd.reals[k] = v
+    gpu = lib.Problem(cd)
+    ref = O.Oracle(cd)
+    ref.setup_calls()
+    return cd, gpu, ref
+
+
+def _compare(gpu, ref, names, tol, label):
+    worst = {}
+    for n in names:
+        g = gpu.get(n)
+        r = ref.get(n, double=False)
+        worst[n] = rel_linf(g, r)
+    bad = {k: v for k, v in worst.items() if not (v <= tol)}
+    assert not bad, f"{label}: fields above {tol}: {bad}"
+    return worst
+
+
+@pytest.mark.parametrize("which", ["small_nozzle", "small_stage"])
+def test_setup_calls_match(mods, which):
+    """STEPUP(1.0) and the first LOSS (SETUP's calls into the hot path)."""
+    case = mods[0]
+    cd, gpu, ref = _pair(mods, getattr(case, which)())
+    _compare(gpu, ref, ["STEP", "RSTEP"] + FORCES, STEP1_TOL, "setup calls")
+
+
+@pytest.mark.parametrize("which", ["small_nozzle", "small_stage"])
+def test_one_step(mods, which):
+    case = mods[0]
+    cd, gpu, ref = _pair(mods, getattr(case, which)())
+    gpu.step()
+    ref.step()
+    _compare(gpu, ref, STATE, STEP1_TOL, "step 1")
+
+
+@pytest.mark.parametrize("which", ["small_nozzle", "small_stage"])
+def test_five_steps_with_loss_and_tail(mods, which):
+    """Step 5 runs LOSS, the monitors and STEPUP(0.25)."""
+    case = mods[0]
+    cd, gpu, ref = _pair(mods, getattr(case, which)())
+    for _ in range(5):
+        mg = gpu.step()
+        mr = ref.step()
+    assert mg.tail_ran == 1 and mr.tail_ran == 1
+    _compare(gpu, ref, STATE + FORCES, 1e-4, "step 5")
+    assert abs(mg.flow_in - mr.flow_in) <= 1e-5 * abs(mr.flow_in)
+    assert abs(mg.econt - mr.econt) <= 1e-4
+    assert abs(mg.vmax - mr.vmax) <= 1e-5 * mr.vmax
+    assert (mg.ivmax, mg.jvmax, mg.kvmax) == (mr.ivmax, mr.jvmax, mr.kvmax)
+
+
+def test_sss_scheme_one_step(mods):
+    """ITIMST=-3 (SSS): F2/F3 history terms and SMOOTH_RESID."""
+    case = mods[0]
+    cd, gpu, ref = _pair(mods, case.small_stage(), NRSMTH=1, F2=-1.65, F3=-0.65)
+    for _ in range(2):
+        gpu.step()
+        ref.step()
+    _compare(gpu, ref, STATE, 1e-5, "SSS step 2")
+
+
+def test_stage_config_one_step(mods):
+    """The single-stage turbine at its full size, 65 x 242 x 49."""
+    case = mods[0]
+    cd, gpu, ref = _pair(mods, case.turbine_stage())
+    gpu.step()
+    ref.step()
+    _compare(gpu, ref, STATE, STEP1_TOL, "stage step 1")
+
+
+def test_converged_mass_flow_and_efficiency(mods):
+    """Converged small stage: mass flow within 1e-4 relative, efficiency
+    within 1e-4 absolute of the FP32 oracle run the same number of steps."""
+    case = mods[0]
+    cd, gpu, ref = _pair(mods, case.small_stage(), NCHANGE=200, NMIXUP=200)
+    n = 1500
+    rc, mg = gpu.run(n)
+    for _ in range(n):
+        mr = ref.step()
+    ig, ir = gpu.integrals(), ref.integrals()
+    assert mg.econt < 0.01 and mr.econt < 0.01
+    assert abs(ig.mass_flow_in - ir.mass_flow_in) <= 1e-4 * abs(ir.mass_flow_in)
+    assert abs(ig.eta_tt - ir.eta_tt) <= 1e-4
+
+
+def test_deterministic(mods):
+    """Two runs of the same case are bitwise identical (no float atomics)."""
+    case = mods[0]
+    outs = []
+    for _ in range(2):
+        cd, gpu, ref = _pair(mods, case.small_stage())
+        gpu.run(20)
+        outs.append([gpu.get(n) for n in ("RO", "ROE", "ROVX")])
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+
+
+def test_health_check_reports_nonfinite(mods):
+    """A NaN planted in the host copy of RO comes back as MGPU_E_NONFINITE
+    from the next tail step; the handle stays usable."""
+    case, common_setup, lib, O = mods
+    cd = common_setup.build_common(case.small_nozzle())
+    gpu = lib.Problem(cd)
+    ro = cd.arrays["RO"].copy()
+    ro[2, 10, 3] = np.nan
+    gpu.set("RO", ro)
+    with pytest.raises(lib.MgpuError) as e:
+        gpu.run(5)
+    assert e.value.code == -5
+    gpu.set("RO", cd.arrays["RO"])          # still usable afterwards
+    assert gpu.get("RO").shape == cd.arrays["RO"].shape
+
+
+def test_api_errors(mods):
+    case, common_setup, lib, O = mods
+    cd = common_setup.build_common(case.small_nozzle())
+    gpu = lib.Problem(cd)
+    with pytest.raises(lib.MgpuError) as e:
+        gpu.set("RO", np.zeros(7, np.float32))
+    assert e.value.code == -1
+    with pytest.raises(lib.MgpuError):
+        gpu.set("NOT_A_COMMON_NAME", np.zeros(7, np.float32))
+    with pytest.raises(lib.MgpuError) as e:
+        gpu.set("AQX", cd.arrays["AQX"])      # geometry is fixed after commit
+    assert e.value.code == -2
