@@ -1,0 +1,314 @@
+#!/usr/bin/env python
+"""Throughput of the Multall time-marching loop on GB300, in Gnode-iter/s.
+
+Workload: the single-stage axial turbine, 65 x 242 x 49 nodes (121 J-points
+per row), 48-vane nozzle + 60-blade rotor at 9000 rpm with 1 % tip gap,
+mixing plane, 3-level multigrid (blocks 3 and 9), SCREE, mixing-length LOSS
+every 5 steps, the 5-step monitor tail and STEPUP -- synthetic seeded
+geometry (no public benchmark suite exists for this solver).  One "step" is
+one full LOOP iteration.  Gnode-iter/s = IM*JM*KM*steps/seconds/1e9.
+
+GPU arm (default): steps are CUDA-graph replays timed with CUDA events on
+the library's stream, with an L2-sized buffer rewritten between steps
+(outside the timed events).  e2e: the same steps through the C ABI call a
+Fortran LOOP replacement would make, mgpu_step() per iteration (host->device
+control word, device->host monitors, synchronous), plus the upload of the
+flow state from host buffers before and the download after, all inside the
+wall-clock region.  Multi-GPU (torchrun): one independent instance per GPU
+(replicas, weak scaling), host-side barrier and max-over-ranks time.
+
+Reference arm (--impl reference): the CPU oracle -- the serial C++
+restatement of the reference's LOOP -- on the same workload, on the box's
+host cores; the reference program is serial, so it uses one thread.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "multall-open-18.3_gb300"))
+
+METRIC = "Gnode-iter/s"
+WORKLOAD = ("single-stage axial turbine 65x242x49 (121 J per row), nozzle 48 vanes + rotor 60 blades "
+            "9000 rpm, 1% tip gap, mixing plane, 3-level multigrid, SCREE, mixing-length LOSS/5 steps")
+# SURVEY-defined compulsory traffic of one LOOP iteration per node (FP32):
+# 5 state arrays r+w, 5 SCREE histories r+w, 9 geometry arrays r, 4 forces r
+B_ALG_STEP = 132
+# compulsory bytes per node of each kernel (arrays read once + written once)
+ALG_BYTES_PER_NODE = {
+    "k_prim": 48, "k_flux_mass": 76, "k_flux_energy": 40, "k_flux_xmom": 52, "k_flux_rvt": 40,
+    "k_flux_rmom": 64, "k_ts_delta": 28, "k_ts_prolong": 16, "k_ts_damp": 8, "k_ts_scatter": 12,
+    "k_sv_stream": 8, "k_sv_plane": 8, "k_ts_plane_sum": 4, "k_ts_restrict": 4, "k_peff": 8,
+    "k_mach_limiter": 16, "k_density_limiter": 4,
+}
+
+
+def env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic_per_launch():
+    """Per-kernel DRAM bytes per launch from the committed ncu summary of
+    this workload (profiles/ncu_stage_traffic.md), if present."""
+    p = os.path.join(ROOT, "profiles", "ncu_stage_traffic.md")
+    out = {}
+    if not os.path.exists(p):
+        return out
+    for line in open(p):
+        cols = [c.strip() for c in line.strip().strip("|").split("|")]
+        if len(cols) >= 3 and cols[0].startswith("k_"):
+            try:
+                out[cols[0]] = float(cols[2])
+            except ValueError:
+                pass
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.rows = []
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(world, rank):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    return dist
+
+
+def dist_max(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def build_case():
+    from mgpu import case, common_setup
+    spec = case.turbine_stage()
+    return common_setup.build_common(spec)
+
+
+def cpu_oracle_rate(cd, seconds, max_steps):
+    """Serial CPU oracle (FP32) on the workload: (Gnode-iter/s, steps, s)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    o = O.Oracle(cd)
+    o.setup_calls()
+    o.step()                                  # warm-up step
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_steps and (n == 0 or time.perf_counter() - t0 < seconds):
+        o.step()
+        n += 1
+    dt = time.perf_counter() - t0
+    o.close()
+    return cd.nodes() * n / dt / 1e9, n, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    cd = build_case()
+    budget = float(os.environ.get("MGPU_REF_SECONDS", "120"))
+    rate, n, dt = cpu_oracle_rate(cd, budget, max(1, args.steps))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": METRIC, "n_gpus": args.gpus,
+        "steps": n, "warmup": 1, "ms_per_step": dt / n * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "nodes": cd.nodes(), "parallelism": "serial CPU (the reference is serial)"},
+        "cpu_baseline": {"value": rate, "unit": METRIC, "cores": 1, "kind": "port",
+                         "sample": f"{n} LOOP iterations of the workload after 1 warm-up, serial C++ restatement "
+                                   f"(oracle) built -O2 -ffp-contract=off, {dt:.1f} s"},
+        "e2e": {"value": rate, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args, rank, world, local_rank):
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local_rank)
+    dist = dist_setup(world, rank)
+    from mgpu import lib
+    import numpy as np
+    cd = build_case()
+    N = cd.nodes()
+    prob = lib.Problem(cd)
+    kps = prob.kernels_per_step()
+    prob.run(max(args.warmup, 3))
+    dist_barrier(dist)
+    with ClockSampler(0) as clk:
+        t_wall0 = time.perf_counter()
+        ms = prob.bench_steps(args.steps, flush_l2=True)
+        t_wall1 = time.perf_counter()
+    dist_barrier(dist)
+    ms_max = dist_max(dist, ms)
+    value = N * args.steps * world / (ms_max / 1e3) / 1e9
+    ms_per_step = ms_max / args.steps
+
+    # per-kernel device times (events around each launch, no graph)
+    prof = prob.profile_steps(10)
+    step_kernels = [p for p in prof if p[0] in ALG_BYTES_PER_NODE]
+    dom = max(step_kernels, key=lambda p: p[2])
+    dom_name, dom_launches, dom_ms = dom
+    avg_s = dom_ms / dom_launches / 1e3
+    alg_bytes = ALG_BYTES_PER_NODE[dom_name] * N
+    achieved = alg_bytes / avg_s / 1e9
+    peak, peak_kind = load_peaks()
+    traffic = ncu_traffic_per_launch().get(dom_name)
+    total_prof = sum(p[2] for p in prof)
+
+    # end to end through the C ABI with host buffers
+    state = ["RO", "ROVX", "ROVR", "RORVT", "ROE"]
+    host = {n: prob.get(n) for n in state}
+    h2d_step, d2h_step = lib.step_io_bytes()
+    ne = max(1, args.steps // 2)
+    dist_barrier(dist)
+    t0 = time.perf_counter()
+    for n in state:
+        prob.set(n, host[n])
+    for _ in range(ne):
+        prob.step()
+    out = {n: prob.get(n) for n in state}
+    t1 = time.perf_counter()
+    dist_barrier(dist)
+    e2e_s = dist_max(dist, t1 - t0)
+    state_bytes = sum(host[n].nbytes for n in state)
+    e2e = {"value": N * ne * world / e2e_s / 1e9, "unit": METRIC,
+           "h2d_bytes_per_step": (state_bytes + h2d_step * ne) / ne,
+           "d2h_bytes_per_step": (state_bytes + d2h_step * ne) / ne,
+           "steps": ne, "how": "per step mgpu_step() (graph launch, control word in, monitors out, sync); "
+                               "flow state uploaded before and downloaded after from pageable host buffers"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, n, dt = cpu_oracle_rate(cd, float(os.environ.get("MGPU_CPU_SECONDS", "15")), 10 ** 6)
+        cpu = {"value": rate, "unit": METRIC, "cores": 1, "kind": "port",
+               "sample": f"{n} LOOP iterations of the same workload after 1 warm-up, serial C++ restatement of "
+                         f"LOOP (oracle), {dt:.1f} s"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "nodes": N, "l2": "flushed between timed steps",
+                       "parallelism": f"replicas: one instance per GPU x{world}",
+                       "reductions": "FP64 tree sums (REDUCE_ORDER=0)"},
+            "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_s * 1e3,
+                         "share_of_step": dom_ms / total_prof,
+                         "step": {"alg_bytes_per_node_iter": B_ALG_STEP,
+                                  "achieved": value / world * B_ALG_STEP, "frac": value / world * B_ALG_STEP / peak}},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "e2e": e2e,
+            "gpu_launches": kps * args.steps,
+            "kernels_per_step": kps,
+            "wall_s_timed_region": t_wall1 - t_wall0,
+        }
+        print(json.dumps(line), flush=True)
+        if args.profile_out:
+            with open(args.profile_out, "w") as f:
+                for name, launches, tot in sorted(prof, key=lambda p: -p[2]):
+                    f.write(f"{name} {launches} {tot:.4f}\n")
+    prob.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-out", default=None)
+    args = ap.parse_args()
+    rank = env_int("RANK", 0)
+    world = env_int("WORLD_SIZE", 1)
+    local_rank = env_int("LOCAL_RANK", 0)
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_gpu(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

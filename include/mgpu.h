@@ -147,6 +147,9 @@ int32_t mgpu_step(mgpu_handle *h, int32_t force_end, mgpu_monitors *mon);
  * Stops early, returning 1, if the reference's convergence test
  * (multall-open-18.3.f:3762-3764) is met at a tail. */
 int32_t mgpu_run(mgpu_handle *h, int32_t nsteps, mgpu_monitors *mon);
+/* Bytes one mgpu_step() call moves between host and device: the
+ * end-of-run flag it sends and the control block (monitors) it reads back. */
+int32_t mgpu_step_io_bytes(int32_t *h2d, int32_t *d2h);
 /* Blocks until all work on the handle's stream has finished. */
 int32_t mgpu_sync(mgpu_handle *h);
 /* EFICOOL's mass averages and efficiencies on the current state, computed
@@ -154,8 +157,27 @@ int32_t mgpu_sync(mgpu_handle *h);
 int32_t mgpu_integrals_compute(mgpu_handle *h, mgpu_integrals *out);
 
 /* ---- instrumentation --------------------------------------------------- */
-/* Number of kernel launches one plain (non-tail) step issues. */
+/* The reference prints "CPU TIME PER STEP" every 50 steps
+ * (multall-open-18.3.f:5404-5414); these are the device-side equivalents. */
+
+/* Number of kernel launches one LOOP iteration issues (graph nodes). */
 int32_t mgpu_kernels_per_step(mgpu_handle *h, int32_t tail_step);
+/* Runs nsteps iterations, each bracketed by CUDA events on the handle's
+ * stream; with flush_l2=1 a buffer larger than L2 is rewritten between the
+ * iterations (outside the events).  *total_ms = sum of the iteration
+ * times. */
+int32_t mgpu_bench_steps(mgpu_handle *h, int32_t nsteps, int32_t flush_l2, double *total_ms);
+
+typedef struct mgpu_kernel_time {
+    char    name[48];
+    int32_t launches;
+    double  total_ms;
+} mgpu_kernel_time;
+/* Runs nsteps iterations launching kernel by kernel (no graph) with a CUDA
+ * event after each launch, and reports per kernel its launch count and
+ * summed duration.  *n_out = entries written (<= max_entries). */
+int32_t mgpu_profile_steps(mgpu_handle *h, int32_t nsteps, mgpu_kernel_time *out, int32_t max_entries,
+                           int32_t *n_out);
 
 #ifdef __cplusplus
 }

@@ -61,7 +61,11 @@
     M_(IFCOOL,   0)                                                       \
     M_(IFBLEED,  0)                                                       \
     M_(IFSHROUD, 0)                                                       \
-    M_(NSTEP,    0)
+    M_(NSTEP,    0)                                                       \
+    /* not a COMMON variable: order of the long reductions on the GPU,   */ \
+    /* 0 = FP64 tree sums (default), 1 = the reference's sequential REAL*4 */ \
+    /* order for the superblock and row-average sums (parity checks)     */ \
+    M_(REDUCE_ORDER, 0)
 
 /* ----- REAL scalars: /BKGAS/, /BKCNTL/, /BKSMTH/, /BKLOSS/, /BKINPT/ ---- */
 #define MGPU_REAL_SCALARS(M_)                                             \

@@ -67,6 +67,8 @@ struct mgpu_handle {
     cudaGraphExec_t gexec = nullptr;
     size_t graph_nodes = 0;
     double *d_int = nullptr;     // integrals output (4 x JM)
+    void *flush_buf = nullptr;   // > L2, rewritten between timed iterations
+    size_t flush_bytes = 0;
     DevCtl *h_ctl = nullptr;     // pinned mirror of the control block
 };
 
@@ -212,9 +214,17 @@ int extents(const std::vector<int> &map, int lo, int hi, int nblk, std::vector<i
     return 0;
 }
 
-int enqueue_step(mgpu_handle *h) {
+// keeps the GPU busy for ~cycles clocks so that a burst of launches queued
+// behind it runs back to back (used only when profiling); always ends
+__global__ void k_delay(long long cycles) {
+    long long t0 = clock64();
+    while (clock64() - t0 < cycles) {
+    }
+}
+
+int enqueue_step(mgpu_handle *h, Prof *prof = nullptr) {
     const Dev &d = h->d;
-    Launch L{h->stream, h->sm_count};
+    Launch L{h->stream, h->sm_count, prof};
     launch_step_begin(d, L);
     launch_prim(d, L);
     launch_loss(d, L, false);
@@ -357,6 +367,8 @@ int32_t mgpu_create(int32_t im, int32_t jm, int32_t km, int32_t nrows, mgpu_hand
     if ((rc = dalloc(h, &d.plane_sum, jm))) return bail(rc);
     if ((rc = dalloc(h, &d.plane_abs, jm))) return bail(rc);
     if ((rc = dalloc(h, &d.BLADE_FLOW, jm))) return bail(rc);
+    if ((rc = dalloc(h, &d.DFLAG, (size_t)im * km))) return bail(rc);
+    if ((rc = dalloc(h, &d.BCBUF, (size_t)3 * km))) return bail(rc);
     d.nparts = (int)((N + 255) / 256) + 1;
     if ((rc = dalloc(h, &d.part_sum, d.nparts))) return bail(rc);
     if ((rc = dalloc(h, &d.part_key, d.nparts))) return bail(rc);
@@ -372,6 +384,7 @@ int32_t mgpu_create(int32_t im, int32_t jm, int32_t km, int32_t nrows, mgpu_hand
 void mgpu_destroy(mgpu_handle *h) {
     if (!h) return;
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->flush_buf) cudaFree(h->flush_buf);
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     if (h->graph) cudaGraphDestroy(h->graph);
     for (void *p : h->allocs) cudaFree(p);
@@ -518,9 +531,9 @@ int32_t mgpu_commit(mgpu_handle *h) {
         int a = find_array(n);
         return download(h, v, (const float *)h->dptr[a], shape_count(h, kArrays[a].shape));
     };
-    std::vector<int> IF_CUSP, JB1, JB2, JSBLK, IB1, IB2, KB1, KB2, NBLADE, JLE, JTE, NROW, JSTART, JMIX, INDMIX;
+    std::vector<int> JLED, IF_CUSP, JB1, JB2, JSBLK, IB1, IB2, KB1, KB2, NBLADE, JLE, JTE, NROW, JSTART, JMIX, INDMIX;
     std::vector<float> FP, FR, X, R, PO1, TO1, P, RO, XL[6];
-    if ((rc = geti("IF_CUSP", IF_CUSP)) || (rc = geti("JB1", JB1)) || (rc = geti("JB2", JB2)) ||
+    if ((rc = geti("JLED", JLED)) || (rc = geti("IF_CUSP", IF_CUSP)) || (rc = geti("JB1", JB1)) || (rc = geti("JB2", JB2)) ||
         (rc = geti("JSBLK", JSBLK)) || (rc = geti("IB1", IB1)) || (rc = geti("IB2", IB2)) || (rc = geti("KB1", KB1)) ||
         (rc = geti("KB2", KB2)) || (rc = geti("NBLADE", NBLADE)) || (rc = geti("JLE", JLE)) || (rc = geti("JTE", JTE)) ||
         (rc = geti("NROW", NROW)) || (rc = geti("JSTART", JSTART)) || (rc = geti("JMIX", JMIX)) ||
@@ -540,6 +553,10 @@ int32_t mgpu_commit(mgpu_handle *h) {
     }
     for (int j = 1; j <= d.JM; ++j)
         if (NROW[j - 1] < 1 || NROW[j - 1] > d.NROWS) return fail(MGPU_E_ARG, "NROW out of range");
+    for (int nr = 0; nr < d.NROWS; ++nr)
+        if (JLED[nr] < 3 || JLED[nr] >= JMIX[nr] || JLE[nr] < 1 || JTE[nr] > d.JM || JTE[nr] <= JLE[nr])
+            return fail(MGPU_E_ARG, "leading/trailing edge indices out of range");
+    if (INDMIX[d.JM - 1] != 0) return fail(MGPU_E_ARG, "INDMIX(JM) must be 0");
 
     // gas constants, SETUP 6459-6468
     d.GA1 = d.GA - 1.0f;
@@ -598,8 +615,11 @@ int32_t mgpu_commit(mgpu_handle *h) {
             JSBLK[j - 1] < 1 || JSBLK[j - 1] > d.NSBLK)
             return fail(MGPU_E_ARG, "multigrid J map out of range");
     }
-    if ((rc = dalloc(h, &d.B1CHG, shape_count(h, SH_MG1))) || (rc = dalloc(h, &d.B2CHG, shape_count(h, SH_MG2))))
+    if ((rc = dalloc(h, &d.B1CHG, shape_count(h, SH_MG1))) || (rc = dalloc(h, &d.B2CHG, shape_count(h, SH_MG2))) ||
+        (rc = dalloc(h, &d.SBSUM, d.NSBLK)) || (rc = dalloc(h, &d.P1, (size_t)d.JM * d.NIB1 * d.NKB1)) ||
+        (rc = dalloc(h, &d.P2, (size_t)d.JM * d.NIB2 * d.NKB2)))
         return rc;
+    if (d.REDUCE_ORDER != 0 && d.REDUCE_ORDER != 1) return fail(MGPU_E_ARG, "REDUCE_ORDER must be 0 or 1");
     // the control block
     DevCtl c;
     memset(&c, 0, sizeof(c));
@@ -669,6 +689,13 @@ int32_t mgpu_run(mgpu_handle *h, int32_t nsteps, mgpu_monitors *mon) {
     return 0;
 }
 
+int32_t mgpu_step_io_bytes(int32_t *h2d, int32_t *d2h) {
+    if (!h2d || !d2h) return fail(MGPU_E_ARG, "null argument");
+    *h2d = (int32_t)sizeof(int);
+    *d2h = (int32_t)sizeof(DevCtl);
+    return 0;
+}
+
 int32_t mgpu_sync(mgpu_handle *h) {
     if (!h) return fail(MGPU_E_ARG, "null handle");
     CK(cudaStreamSynchronize(h->stream));
@@ -717,6 +744,79 @@ int32_t mgpu_integrals_compute(mgpu_handle *h, mgpu_integrals *out) {
     out->to_ratio = TORAT;
     out->j1 = J1;
     out->j2m1 = J2M1;
+    return 0;
+}
+
+int32_t mgpu_bench_steps(mgpu_handle *h, int32_t nsteps, int32_t flush_l2, double *total_ms) {
+    if (!h || !h->committed || !total_ms || nsteps < 0) return fail(MGPU_E_ARG, "bad arguments to mgpu_bench_steps");
+    int rc = build_graph(h);
+    if (rc) return rc;
+    if (flush_l2 && !h->flush_buf) {
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, h->device);
+        h->flush_bytes = (size_t)(l2 > 0 ? l2 : 128 << 20) * 2;
+        CK(cudaMalloc(&h->flush_buf, h->flush_bytes));
+    }
+    std::vector<cudaEvent_t> ev((size_t)2 * nsteps);
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    for (int s = 0; s < nsteps; ++s) {
+        if (flush_l2) CK(cudaMemsetAsync(h->flush_buf, s & 0xff, h->flush_bytes, h->stream));
+        CK(cudaEventRecord(ev[2 * s], h->stream));
+        CK(cudaGraphLaunch(h->gexec, h->stream));
+        CK(cudaEventRecord(ev[2 * s + 1], h->stream));
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    double tot = 0.0;
+    for (int s = 0; s < nsteps; ++s) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ev[2 * s], ev[2 * s + 1]));
+        tot += ms;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    *total_ms = tot;
+    if ((rc = read_ctl(h))) return rc;
+    if (h->h_ctl->health) return fail(MGPU_E_NONFINITE, "non-finite or non-positive density in the flow field");
+    return 0;
+}
+
+int32_t mgpu_profile_steps(mgpu_handle *h, int32_t nsteps, mgpu_kernel_time *out, int32_t max_entries,
+                           int32_t *n_out) {
+    if (!h || !h->committed || !out || !n_out || nsteps < 0) return fail(MGPU_E_ARG, "bad arguments to mgpu_profile_steps");
+    std::map<std::string, std::pair<int, double>> acc;
+    std::vector<std::string> order;
+    for (int s = 0; s < nsteps; ++s) {
+        Prof *p = new (std::nothrow) Prof();
+        if (!p) return fail(MGPU_E_NOMEM, "host allocation");
+        for (int e = 0; e < Prof::MAXEV; ++e) cudaEventCreate(&p->ev[e]);
+        Launch L0{h->stream, h->sm_count, p};
+        k_delay<<<1, 1, 0, h->stream>>>(40000000LL);   // ~20 ms at 2 GHz
+        mark(L0, "start");
+        int rc = enqueue_step(h, p);
+        cudaError_t ce = cudaStreamSynchronize(h->stream);
+        if (!rc && ce == cudaSuccess) {
+            for (int e = 1; e < p->n; ++e) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, p->ev[e - 1], p->ev[e]);
+                std::string nm = p->name[e];
+                if (!acc.count(nm)) order.push_back(nm);
+                acc[nm].first += 1;
+                acc[nm].second += ms;
+            }
+        }
+        for (int e = 0; e < Prof::MAXEV; ++e) cudaEventDestroy(p->ev[e]);
+        delete p;
+        if (rc) return rc;
+        if (ce != cudaSuccess) return fail(MGPU_E_CUDA, cudaGetErrorString(ce));
+    }
+    int n = 0;
+    for (const auto &nm : order) {
+        if (n >= max_entries) break;
+        snprintf(out[n].name, sizeof(out[n].name), "%s", nm.c_str());
+        out[n].launches = acc[nm].first;
+        out[n].total_ms = acc[nm].second;
+        ++n;
+    }
+    *n_out = n;
     return 0;
 }
 

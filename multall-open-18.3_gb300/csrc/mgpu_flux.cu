@@ -63,7 +63,10 @@ __global__ void k_step_begin(Dev d) {
     }
 }
 
-void launch_step_begin(const Dev &d, Launch L) { k_step_begin<<<1, 1, 0, L.s>>>(d); }
+void launch_step_begin(const Dev &d, Launch L) {
+    k_step_begin<<<1, 1, 0, L.s>>>(d);
+    mark(L, "k_step_begin");
+}
 
 // ---------------------------------------------------------------------
 // primitive variables (7450) and P, HO, T (5900); with the 5-step tail
@@ -144,6 +147,7 @@ __global__ void __launch_bounds__(PRIM_BS) k_prim(Dev d) {
 void launch_prim(const Dev &d, Launch L) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
     k_prim<<<grid_for(N, PRIM_BS), PRIM_BS, 0, L.s>>>(d);
+    mark(L, "k_prim");
 }
 
 // ---------------------------------------------------------------------
@@ -209,6 +213,7 @@ __global__ void k_flux_mass(Dev d) {
 void launch_flux_mass(const Dev &d, Launch L) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
     k_flux_mass<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+    mark(L, "k_flux_mass");
 }
 
 // ---------------------------------------------------------------------
@@ -249,33 +254,49 @@ __global__ void k_flux_energy(Dev d) {
 void launch_flux_energy(const Dev &d, Launch L) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
     k_flux_energy<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+    mark(L, "k_flux_energy");
 }
 
 // ---------------------------------------------------------------------
-// inlet and exit boundary conditions (4476-4734): one CTA.  The pitchwise
-// sums per K keep the reference's sequential order, and one thread runs
-// the radial-equilibrium recurrence for PD(K) (4533-4541).
+// inlet and exit boundary conditions (4476-4734).  k_bc_sums: one warp per
+// K line forms the pitchwise sums in the reference's sequential order (the
+// lanes load, lane 0 adds in I order), then one thread runs the radial-
+// equilibrium recurrence for PD(K) (4533-4541).  k_bc_apply: one thread per
+// (I,K) sets the inlet and exit states.
 // ---------------------------------------------------------------------
-constexpr int BC_MAXK = 512;
-
-__global__ void __launch_bounds__(1024) k_bc(Dev d) {
-    __shared__ float s_pavg2[BC_MAXK], s_pavg3[BC_MAXK], s_pavgout[BC_MAXK], s_sum[BC_MAXK];
-    for (int k = threadIdx.x + 1; k <= d.KM; k += blockDim.x) {
+__global__ void __launch_bounds__(1024) k_bc_sums(Dev d) {
+    __shared__ float s_sum[512];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int k = w + 1; k <= d.KM; k += nw) {
         float PAVG2 = 0.0f, PAVG3 = 0.0f, PAVGOUT = 0.0f, SUM = 0.0f;
         float RJM = A2(d.R, d.JM, k);
-        for (int i = 1; i <= d.IMM1; ++i) {
-            float fp = A1(d.FP, i);
-            PAVG2 = PAVG2 + 0.5f * (A3(d.P, i, 2, k) + A3(d.P, i + 1, 2, k)) * fp;
-            PAVG3 = PAVG3 + 0.5f * (A3(d.P, i, 3, k) + A3(d.P, i + 1, 3, k)) * fp;
-            PAVGOUT = PAVGOUT + 0.5f * (A3(d.P, i, d.JMM1, k) + A3(d.P, i + 1, d.JMM1, k)) * fp;
-            SUM = SUM + 0.5f * fp *
-                            (A3(d.ROVT, i, d.JM, k) * A3(d.VT, i, d.JM, k) + A3(d.ROVT, i + 1, d.JM, k) * A3(d.VT, i + 1, d.JM, k)) /
-                            RJM;
+        for (int i0 = 1; i0 <= d.IMM1; i0 += 32) {
+            int i = i0 + l;
+            float t2 = 0.f, t3 = 0.f, to = 0.f, ts = 0.f;
+            if (i <= d.IMM1) {
+                float fp = A1(d.FP, i);
+                t2 = 0.5f * (A3(d.P, i, 2, k) + A3(d.P, i + 1, 2, k)) * fp;
+                t3 = 0.5f * (A3(d.P, i, 3, k) + A3(d.P, i + 1, 3, k)) * fp;
+                to = 0.5f * (A3(d.P, i, d.JMM1, k) + A3(d.P, i + 1, d.JMM1, k)) * fp;
+                ts = 0.5f * fp * (A3(d.ROVT, i, d.JM, k) * A3(d.VT, i, d.JM, k) + A3(d.ROVT, i + 1, d.JM, k) * A3(d.VT, i + 1, d.JM, k)) /
+                     RJM;
+            }
+            int cnt = d.IMM1 - i0 + 1 < 32 ? d.IMM1 - i0 + 1 : 32;
+            for (int q = 0; q < cnt; ++q) {
+                float a2 = __shfl_sync(0xffffffffu, t2, q), a3 = __shfl_sync(0xffffffffu, t3, q);
+                float ao = __shfl_sync(0xffffffffu, to, q), as = __shfl_sync(0xffffffffu, ts, q);
+                PAVG2 = PAVG2 + a2;
+                PAVG3 = PAVG3 + a3;
+                PAVGOUT = PAVGOUT + ao;
+                SUM = SUM + as;
+            }
         }
-        s_pavg2[k - 1] = PAVG2;
-        s_pavg3[k - 1] = PAVG3;
-        s_pavgout[k - 1] = PAVGOUT;
-        s_sum[k - 1] = SUM;
+        if (l == 0) {
+            d.BCBUF[k - 1] = PAVG2;
+            d.BCBUF[d.KM + k - 1] = PAVG3;
+            d.BCBUF[2 * d.KM + k - 1] = PAVGOUT;
+            s_sum[k - 1] = SUM;
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0 && d.IPOUT <= 0) {
@@ -292,85 +313,91 @@ __global__ void __launch_bounds__(1024) k_bc(Dev d) {
             if (d.IPOUT == -1) A1(d.PD, k) = A1(d.PD, k) + PDIFF;
         }
     }
-    __syncthreads();
-    int total = d.IM * d.KM;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        int i = t % d.IM + 1, k = t / d.IM + 1;
-        float PO1 = A1(d.PO1, k), TO1 = A1(d.TO1, k);
-        // inlet, isentropic from the stagnation state
-        float RO_STAG = PO1 / d.RGAS / TO1;
-        float RO_IN = A3(d.RO, i, 1, k);
-        if (RO_IN > 0.9999f * RO_STAG) RO_IN = 0.9999f * RO_STAG;
-        float PNEW = PO1 * powf(RO_IN / RO_STAG, d.GA);
-        float p1 = A3(d.P, i, 1, k);
-        int ip = d.IN_PRESS < 0 ? -d.IN_PRESS : d.IN_PRESS;
-        if (d.IN_PRESS == 0) p1 = d.RFIN1 * p1 + d.RFIN * PNEW;
-        if (ip == 1) p1 = d.RFIN1 * p1 + d.RFIN2 * A3(d.P, i, 2, k) - d.RFIN * A3(d.P, i, 3, k);
-        if (ip == 3) p1 = d.RFIN1 * p1 + d.RFIN2 * s_pavg2[k - 1] - d.RFIN * s_pavg3[k - 1];
-        if (ip == 4) p1 = d.RFIN1 * p1 + d.RFIN2 * A3(d.P, d.IMID, 2, d.KMID) - d.RFIN * A3(d.P, d.IMID, 3, d.KMID);
-        float plim = A1(d.PLIM, k);
-        if (p1 > plim) p1 = 0.9f * p1 + 0.1f * plim;
-        if (p1 > 0.99999f * PO1) p1 = PO1 * 0.99999f;
-        A3(d.P, i, 1, k) = p1;
-        float TSTATIC = TO1 * powf(p1 * A1(d.RPO1, k), d.FGA);
-        float VABSQ = 2.0f * d.CP * (TO1 - TSTATIC);
-        A3(d.T_STATIC, i, 1, k) = TSTATIC;
-        float VABS = sqrtf(VABSQ);
-        float VMER = 0.0f;
-        float vt1 = A3(d.VT, i, 1, k);
-        if (d.IN_VTAN == 0) {
-            VMER = VABS * A1(d.BSCOS, k);
-            vt1 = VABS * A1(d.BSSIN, k);
-        }
-        if (d.IN_VTAN == 1) {
-            float VMERSQ = VABSQ - A1(d.VTIN, k) * A1(d.VTIN, k);
-            if (VMERSQ < 0.01f) VMERSQ = 0.01f;
-            VMER = sqrtf(VMERSQ);
-            vt1 = A1(d.VTIN, k);
-        }
-        if (d.IN_VTAN == 2) {
-            float WR = A2(d.UBLADE, 1, k);
-            float VRELSQ = VABSQ - WR * WR * A1(d.BSCOS, k) * A1(d.BSCOS, k);
-            if (VRELSQ < 0.01f) VRELSQ = 0.01f;
-            float VREL = sqrtf(VRELSQ) - WR * A1(d.BSSIN, k);
-            VMER = VREL * A1(d.BSCOS, k);
-            vt1 = VREL * A1(d.BSSIN, k) + WR;
-        }
-        A3(d.VT, i, 1, k) = vt1;
-        float vx1 = A3(d.VX, i, 1, k), vr1 = A3(d.VR, i, 1, k);
-        float vr2 = A3(d.VR, i, 2, k);
-        if (d.IN_VR > 0) vx1 = VMER * A1(d.BRCOS, k);
-        float VXSQ = VMER * VMER - vr2 * vr2;
-        if (VXSQ < 0.0000001f * TO1 * d.CP) VXSQ = 0.0000001f * TO1 * d.CP;
-        if (d.IN_VR <= 0) vx1 = sqrtf(VXSQ);
-        if (d.IN_VR > 0) vr1 = VMER * A1(d.BRSIN, k);
-        if (d.IN_VR <= 0) vr1 = vr2;
-        A3(d.VX, i, 1, k) = vx1;
-        A3(d.VR, i, 1, k) = vr1;
-        float ro1 = p1 / (d.RGAS * TSTATIC);
-        float rovt1 = ro1 * vt1;
-        A3(d.RO, i, 1, k) = ro1;
-        A3(d.ROVT, i, 1, k) = rovt1;
-        A3(d.ROVR, i, 1, k) = ro1 * vr1;
-        A3(d.RORVT, i, 1, k) = rovt1 * A2(d.R, 1, k);
-        A3(d.ROVX, i, 1, k) = ro1 * vx1;
-        A3(d.ROE, i, 1, k) = p1 / d.GA1 + ro1 * 0.5f * VABSQ;
-        A3(d.HO, i, 1, k) = d.CP * TO1;
-        // exit: pitchwise pressure variation extrapolated from upstream
-        float vr = A3(d.VR, i, d.JM, k), vt = A3(d.VT, i, d.JM, k), vx = A3(d.VX, i, d.JM, k);
-        float EKE = 0.5f * (vr * vr + vt * vt + vx * vx);
-        float pe = A1(d.PD, k) + d.FEXTRAP * (A3(d.P, i, d.JMM1, k) - s_pavgout[k - 1]);
-        float hoe = 2.0f * A3(d.HO, i, d.JMM1, k) - A3(d.HO, i, d.JM - 2, k);
-        float TEXIT = (hoe - EKE) / d.CP;
-        float roe_ = pe / d.RGAS / TEXIT;
-        A3(d.P, i, d.JM, k) = pe;
-        A3(d.HO, i, d.JM, k) = hoe;
-        A3(d.RO, i, d.JM, k) = roe_;
-        A3(d.ROE, i, d.JM, k) = roe_ * (d.CV * TEXIT + EKE);
-    }
 }
 
-void launch_bc(const Dev &d, Launch L) { k_bc<<<1, 1024, 0, L.s>>>(d); }
+__global__ void k_bc_apply(Dev d) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.IM * d.KM) return;
+    int i = t % d.IM + 1, k = t / d.IM + 1;
+    float PO1 = A1(d.PO1, k), TO1 = A1(d.TO1, k);
+    // inlet, isentropic from the stagnation state
+    float RO_STAG = PO1 / d.RGAS / TO1;
+    float RO_IN = A3(d.RO, i, 1, k);
+    if (RO_IN > 0.9999f * RO_STAG) RO_IN = 0.9999f * RO_STAG;
+    float PNEW = PO1 * powf(RO_IN / RO_STAG, d.GA);
+    float p1 = A3(d.P, i, 1, k);
+    int ip = d.IN_PRESS < 0 ? -d.IN_PRESS : d.IN_PRESS;
+    if (d.IN_PRESS == 0) p1 = d.RFIN1 * p1 + d.RFIN * PNEW;
+    if (ip == 1) p1 = d.RFIN1 * p1 + d.RFIN2 * A3(d.P, i, 2, k) - d.RFIN * A3(d.P, i, 3, k);
+    if (ip == 3) p1 = d.RFIN1 * p1 + d.RFIN2 * d.BCBUF[k - 1] - d.RFIN * d.BCBUF[d.KM + k - 1];
+    if (ip == 4) p1 = d.RFIN1 * p1 + d.RFIN2 * A3(d.P, d.IMID, 2, d.KMID) - d.RFIN * A3(d.P, d.IMID, 3, d.KMID);
+    float plim = A1(d.PLIM, k);
+    if (p1 > plim) p1 = 0.9f * p1 + 0.1f * plim;
+    if (p1 > 0.99999f * PO1) p1 = PO1 * 0.99999f;
+    A3(d.P, i, 1, k) = p1;
+    float TSTATIC = TO1 * powf(p1 * A1(d.RPO1, k), d.FGA);
+    float VABSQ = 2.0f * d.CP * (TO1 - TSTATIC);
+    A3(d.T_STATIC, i, 1, k) = TSTATIC;
+    float VABS = sqrtf(VABSQ);
+    float VMER = 0.0f;
+    float vt1 = A3(d.VT, i, 1, k);
+    if (d.IN_VTAN == 0) {
+        VMER = VABS * A1(d.BSCOS, k);
+        vt1 = VABS * A1(d.BSSIN, k);
+    }
+    if (d.IN_VTAN == 1) {
+        float VMERSQ = VABSQ - A1(d.VTIN, k) * A1(d.VTIN, k);
+        if (VMERSQ < 0.01f) VMERSQ = 0.01f;
+        VMER = sqrtf(VMERSQ);
+        vt1 = A1(d.VTIN, k);
+    }
+    if (d.IN_VTAN == 2) {
+        float WR = A2(d.UBLADE, 1, k);
+        float VRELSQ = VABSQ - WR * WR * A1(d.BSCOS, k) * A1(d.BSCOS, k);
+        if (VRELSQ < 0.01f) VRELSQ = 0.01f;
+        float VREL = sqrtf(VRELSQ) - WR * A1(d.BSSIN, k);
+        VMER = VREL * A1(d.BSCOS, k);
+        vt1 = VREL * A1(d.BSSIN, k) + WR;
+    }
+    A3(d.VT, i, 1, k) = vt1;
+    float vx1 = A3(d.VX, i, 1, k), vr1 = A3(d.VR, i, 1, k);
+    float vr2 = A3(d.VR, i, 2, k);
+    if (d.IN_VR > 0) vx1 = VMER * A1(d.BRCOS, k);
+    float VXSQ = VMER * VMER - vr2 * vr2;
+    if (VXSQ < 0.0000001f * TO1 * d.CP) VXSQ = 0.0000001f * TO1 * d.CP;
+    if (d.IN_VR <= 0) vx1 = sqrtf(VXSQ);
+    if (d.IN_VR > 0) vr1 = VMER * A1(d.BRSIN, k);
+    if (d.IN_VR <= 0) vr1 = vr2;
+    A3(d.VX, i, 1, k) = vx1;
+    A3(d.VR, i, 1, k) = vr1;
+    float ro1 = p1 / (d.RGAS * TSTATIC);
+    float rovt1 = ro1 * vt1;
+    A3(d.RO, i, 1, k) = ro1;
+    A3(d.ROVT, i, 1, k) = rovt1;
+    A3(d.ROVR, i, 1, k) = ro1 * vr1;
+    A3(d.RORVT, i, 1, k) = rovt1 * A2(d.R, 1, k);
+    A3(d.ROVX, i, 1, k) = ro1 * vx1;
+    A3(d.ROE, i, 1, k) = p1 / d.GA1 + ro1 * 0.5f * VABSQ;
+    A3(d.HO, i, 1, k) = d.CP * TO1;
+    // exit: pitchwise pressure variation extrapolated from upstream
+    float vr = A3(d.VR, i, d.JM, k), vt = A3(d.VT, i, d.JM, k), vx = A3(d.VX, i, d.JM, k);
+    float EKE = 0.5f * (vr * vr + vt * vt + vx * vx);
+    float pe = A1(d.PD, k) + d.FEXTRAP * (A3(d.P, i, d.JMM1, k) - d.BCBUF[2 * d.KM + k - 1]);
+    float hoe = 2.0f * A3(d.HO, i, d.JMM1, k) - A3(d.HO, i, d.JM - 2, k);
+    float TEXIT = (hoe - EKE) / d.CP;
+    float roe_ = pe / d.RGAS / TEXIT;
+    A3(d.P, i, d.JM, k) = pe;
+    A3(d.HO, i, d.JM, k) = hoe;
+    A3(d.RO, i, d.JM, k) = roe_;
+    A3(d.ROE, i, d.JM, k) = roe_ * (d.CV * TEXIT + EKE);
+}
+
+void launch_bc(const Dev &d, Launch L) {
+    k_bc_sums<<<1, 1024, 0, L.s>>>(d);
+    mark(L, "k_bc_sums");
+    k_bc_apply<<<(d.IM * d.KM + 127) / 128, 128, 0, L.s>>>(d);
+    mark(L, "k_bc_apply");
+}
 
 // ---------------------------------------------------------------------
 // PEFF = P - PREFF + F_PDOWN*(P(J+1)-P(J))  (4321)
@@ -389,6 +416,7 @@ __global__ void k_peff(Dev d) {
 void launch_peff(const Dev &d, Launch L) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
     k_peff<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+    mark(L, "k_peff");
 }
 
 // ---------------------------------------------------------------------
@@ -431,6 +459,7 @@ __global__ void k_flux_xmom(Dev d) {
 void launch_flux_xmom(const Dev &d, Launch L) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
     k_flux_xmom<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+    mark(L, "k_flux_xmom");
 }
 
 // ---------------------------------------------------------------------
@@ -476,6 +505,7 @@ __global__ void k_flux_rvt(Dev d) {
 void launch_flux_rvt(const Dev &d, Launch L) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
     k_flux_rvt<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+    mark(L, "k_flux_rvt");
 }
 
 // ---------------------------------------------------------------------
@@ -537,21 +567,42 @@ __global__ void k_flux_rmom(Dev d) {
 void launch_flux_rmom(const Dev &d, Launch L) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
     k_flux_rmom<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+    mark(L, "k_flux_rmom");
 }
 
 // ---------------------------------------------------------------------
-// density limiter (7200): one thread per (I,K) line walks J in the
-// reference's order, since RO(J-1), RO(J-2) are already limited when RO(J)
-// is tested.  The thread owning (IMID,KMID) then sets the per-row Mach
-// limits VLIMIT/ROLIMIT (7250) from its final densities.
+// density limiter (7200).  The reference walks J in place, so RO(J-1) and
+// RO(J-2) are already limited when RO(J) is tested.  A column's result
+// differs from its input only if some J triggers a limit on the unmodified
+// values (the first trigger is the same in both), so k_density_detect flags
+// those columns in parallel and k_density_fix replays the sequential walk
+// on flagged columns only.  The thread owning (IMID,KMID) then sets the
+// per-row Mach limits VLIMIT/ROLIMIT (7250) from its final densities.
 // ---------------------------------------------------------------------
-__global__ void k_density_limiter(Dev d) {
+__device__ inline bool density_triggers(float ro, float ROAVG, float ROLIM) {
+    return ro < 0.6f * ROAVG || ro > 1.5f * ROAVG || ro < ROLIM;
+}
+
+__global__ void k_density_detect(Dev d) {
+    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, n, i, j, k);
+    if (j < 3 || j > d.JM - 3) return;
+    const float *RO = d.RO;
+    float ROAVG = 0.25f * (A3(RO, i, j - 2, k) + A3(RO, i, j - 1, k) + A3(RO, i, j + 1, k) + A3(RO, i, j + 2, k));
+    if (density_triggers(RO[n], ROAVG, d.ROLIM)) d.DFLAG[(size_t)(k - 1) * d.IM + (i - 1)] = 1;
+}
+
+__global__ void k_density_fix(Dev d) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= d.IM * d.KM) return;
     int i = t % d.IM + 1, k = t / d.IM + 1;
     float *RO = d.RO;
-    float ROLIM = d.ROLIM;
-    if (d.JM - 3 >= 3) {
+    if (d.DFLAG[t]) {
+        d.DFLAG[t] = 0;
+        float ROLIM = d.ROLIM;
         float rm2 = A3(RO, i, 1, k), rm1 = A3(RO, i, 2, k), r0 = A3(RO, i, 3, k);
         float rp1 = A3(RO, i, 4, k);
         for (int j = 3; j <= d.JM - 3; ++j) {
@@ -618,28 +669,34 @@ __global__ void k_mach_limiter(Dev d) {
 }
 
 void launch_limiters(const Dev &d, Launch L) {
+    size_t Nn = (size_t)d.IM * d.JM * d.KM;
+    k_density_detect<<<grid_for(Nn, 256), 256, 0, L.s>>>(d);
+    mark(L, "k_density_detect");
     int lines = d.IM * d.KM;
-    k_density_limiter<<<(lines + 127) / 128, 128, 0, L.s>>>(d);
+    k_density_fix<<<(lines + 127) / 128, 128, 0, L.s>>>(d);
+    mark(L, "k_density_fix");
     size_t N = (size_t)d.IM * d.JM * d.KM;
     k_mach_limiter<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+    mark(L, "k_mach_limiter");
 }
 
 // ---------------------------------------------------------------------
-// NEW_MIXPLAN (14922-15251), IFGAS=0: one thread per (row interface, K)
-// runs the reference's I loops in order, including the outward
-// Prandtl-Meyer sweeps for a supersonic relative flow.
+// NEW_MIXPLAN (14922-15251), IFGAS=0: one CTA per (row interface, K).
+// The threads fill the per-I isentropic states and angles; the outward
+// Prandtl-Meyer sweeps for a supersonic relative flow and the periodicity
+// correction run in the reference's order on one thread; the threads then
+// relax the J=JMIX+2 (or JMIX-1) plane.
 // ---------------------------------------------------------------------
 constexpr int MIX_MAXI = 160;
+constexpr int MIX_BS = 64;
 
-__global__ void k_mixplan(Dev d) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= d.NRWSM1 * d.KM) return;
-    int nr = t / d.KM + 1, k = t % d.KM + 1;
-    float ALPHAA[MIX_MAXI], GAMA[MIX_MAXI], WREF_JP2[MIX_MAXI], ROREF_JP2[MIX_MAXI], PISENT[MIX_MAXI];
-    float ROISENT[MIX_MAXI], WMACH_JP2[MIX_MAXI], TISENT[MIX_MAXI], WIS_JP2[MIX_MAXI];
+__global__ void __launch_bounds__(MIX_BS) k_mixplan(Dev d) {
+    __shared__ float ALPHAA[MIX_MAXI], GAMA[MIX_MAXI], WREF_JP2[MIX_MAXI], ROREF_JP2[MIX_MAXI], PISENT[MIX_MAXI];
+    __shared__ float ROISENT[MIX_MAXI], WMACH_JP2[MIX_MAXI], TISENT[MIX_MAXI], WIS_JP2[MIX_MAXI];
+    const int nr = blockIdx.x / d.KM + 1, k = blockIdx.x % d.KM + 1;
     const int IM = d.IM;
-    float RFMIX1 = 1.0f - d.RFMIX;
-    int KSUB = (k == d.KM) ? d.KM - 1 : k;
+    const float RFMIX1 = 1.0f - d.RFMIX;
+    const int KSUB = (k == d.KM) ? d.KM - 1 : k;
     int j = A1(d.JMIX, nr);
     int JP1, JP2, JP3;
     float F_ANGLE;
@@ -651,28 +708,28 @@ __global__ void k_mixplan(Dev d) {
         JP1 = j - 1; JP2 = j - 2; JP3 = j - 3;
         F_ANGLE = 0.0f;
     }
-    float F_ANGLE1 = 1.0f - F_ANGLE;
-    float RJP1 = A2(d.R, JP1, k), UJP1 = A2(d.UBLADE, JP1, k);
-    float ROMIX = A3(d.RO, d.IMID, JP1, k);
-    float VXMIX = A3(d.ROVX, d.IMID, JP1, k) / ROMIX;
-    float VRMIX = A3(d.ROVR, d.IMID, JP1, k) / ROMIX;
-    float VTMIX = A3(d.RORVT, d.IMID, JP1, k) / ROMIX / RJP1;
-    float ROEMIX = A3(d.ROE, d.IMID, JP1, k);
-    float VMSQ = VXMIX * VXMIX + VRMIX * VRMIX;
-    float VABSQ = VMSQ + VTMIX * VTMIX;
-    float WTMIX = VTMIX - UJP1;
-    float WMIXSQ = VMSQ + WTMIX * WTMIX;
-    float WMIX = sqrtf(WMIXSQ);
-    float ALPHAMIX = asinf(WTMIX / WMIX);
-    float GAMAMIX = atan2f(VRMIX, VXMIX);
-    float TMIX = (ROEMIX / ROMIX - 0.5f * VABSQ) / d.CV;
-    float ROTHALPY = d.CP * TMIX + 0.5f * (WMIXSQ - UJP1 * UJP1);
-    float GAGAS = d.GA;
-    float PMIX = ROMIX * d.RGAS * TMIX;
-    int NMACH = 0;
-    float RJP2 = A2(d.R, JP2, k), UNOWJP2 = A2(d.UBLADE, JP2, k);
-    float RJP3 = A2(d.R, JP3, k), UNOWJP3 = A2(d.UBLADE, JP3, k);
-    for (int i = 1; i <= IM; ++i) {
+    const float F_ANGLE1 = 1.0f - F_ANGLE;
+    const float RJP1 = A2(d.R, JP1, k), UJP1 = A2(d.UBLADE, JP1, k);
+    const float ROMIX = A3(d.RO, d.IMID, JP1, k);
+    const float VXMIX = A3(d.ROVX, d.IMID, JP1, k) / ROMIX;
+    const float VRMIX = A3(d.ROVR, d.IMID, JP1, k) / ROMIX;
+    const float VTMIX = A3(d.RORVT, d.IMID, JP1, k) / ROMIX / RJP1;
+    const float ROEMIX = A3(d.ROE, d.IMID, JP1, k);
+    const float VMSQ = VXMIX * VXMIX + VRMIX * VRMIX;
+    const float VABSQ = VMSQ + VTMIX * VTMIX;
+    const float WTMIX = VTMIX - UJP1;
+    const float WMIXSQ = VMSQ + WTMIX * WTMIX;
+    const float WMIX = sqrtf(WMIXSQ);
+    const float ALPHAMIX = asinf(WTMIX / WMIX);
+    const float GAMAMIX = atan2f(VRMIX, VXMIX);
+    const float TMIX = (ROEMIX / ROMIX - 0.5f * VABSQ) / d.CV;
+    const float ROTHALPY = d.CP * TMIX + 0.5f * (WMIXSQ - UJP1 * UJP1);
+    const float GAGAS = d.GA;
+    const float PMIX = ROMIX * d.RGAS * TMIX;
+    const float RJP2 = A2(d.R, JP2, k), UNOWJP2 = A2(d.UBLADE, JP2, k);
+    const float RJP3 = A2(d.R, JP3, k), UNOWJP3 = A2(d.UBLADE, JP3, k);
+    int nmach = 0;
+    for (int i = threadIdx.x + 1; i <= IM; i += MIX_BS) {
         float ROJP2 = A3(d.RO, i, JP2, k);
         float XVELJP2 = A3(d.ROVX, i, JP2, k) / ROJP2;
         float RVELJP2 = A3(d.ROVR, i, JP2, k) / ROJP2;
@@ -702,12 +759,14 @@ __global__ void k_mixplan(Dev d) {
         WIS_JP2[i - 1] = sqrtf(WIS_SQ_JP2);
         WREF_JP2[i - 1] = WACT_JP2;
         ROREF_JP2[i - 1] = ROJP2;
-        WMACH_JP2[i - 1] = WACT_JP2 / sqrtf(GAGAS * d.RGAS * T_ACT_JP2);
-        if (WMACH_JP2[i - 1] > 1.0f) NMACH = NMACH + 1;
+        float wm = WACT_JP2 / sqrtf(GAGAS * d.RGAS * T_ACT_JP2);
+        WMACH_JP2[i - 1] = wm;
+        if (wm > 1.0f) nmach = 1;
         ALPHAA[i - 1] = F_ANGLE1 * ALPHAMIX + F_ANGLE * ALPHAJP3;
         GAMA[i - 1] = F_ANGLE1 * GAMAMIX + F_ANGLE * GAMAJP3;
     }
-    if (NMACH != 0) {
+    int NMACH = __syncthreads_or(nmach);
+    if (NMACH != 0 && threadIdx.x == 0) {
         float FROTN = 1.0f;
         if (WTMIX < 0.0f) FROTN = -1.0f;
         for (int i = d.IMID + 1; i <= IM; ++i) {
@@ -735,7 +794,8 @@ __global__ void k_mixplan(Dev d) {
             SUMFP = SUMFP + A1(d.FP, i);
         }
     }
-    for (int i = 1; i <= IM; ++i) {
+    __syncthreads();
+    for (int i = threadIdx.x + 1; i <= IM; i += MIX_BS) {
         float RO_JP2 = ROISENT[i - 1];
         float WT_JP2 = WIS_JP2[i - 1] * sinf(ALPHAA[i - 1]);
         float VM_JP2 = WIS_JP2[i - 1] * cosf(ALPHAA[i - 1]);
@@ -754,8 +814,8 @@ __global__ void k_mixplan(Dev d) {
 
 void launch_mixplan(const Dev &d, Launch L) {
     if (!(d.IFMIX > 0 && d.RFMIX > 1.0e-3f) || d.NRWSM1 <= 0) return;
-    int n = d.NRWSM1 * d.KM;
-    k_mixplan<<<(n + 63) / 64, 64, 0, L.s>>>(d);
+    k_mixplan<<<d.NRWSM1 * d.KM, MIX_BS, 0, L.s>>>(d);
+    mark(L, "k_mixplan");
 }
 
 }  // namespace mgpu

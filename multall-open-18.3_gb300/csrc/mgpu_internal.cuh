@@ -79,6 +79,10 @@ struct Dev {
     double *plane_sum;                 // (JM) per-J-plane sums of STORE
     double *plane_abs;                 // (JM) per-J-plane sums of |STORE|
     float *AVG_BLK;                    // (NROWS)
+    float *SBSUM;                      // (NSBLK) superblock sums, reference order
+    float *P1, *P2;                    // (JM, NIB1*NKB1) / (JM, NIB2*NKB2) per-plane block partials
+    int *DFLAG;                        // (IM*KM) density-limiter column flags
+    float *BCBUF;                      // (3, KM) PAVG2, PAVG3, PAVGOUT of the exit/inlet BCs
     double *BLADE_FLOW;                // (JM)
     // per-block reduction partials of the 5-step tail
     double *part_sum;
@@ -131,10 +135,28 @@ __device__ inline unsigned long long max_key(float v, size_t lin) {
 // ---------------------------------------------------------------------
 // kernel launch wrappers (defined in the .cu files); each enqueues on s
 // ---------------------------------------------------------------------
+// Optional per-kernel event trace (mgpu_profile_steps): each launch wrapper
+// calls mark() after a launch, so consecutive events bracket one kernel.
+struct Prof {
+    static constexpr int MAXEV = 4096;
+    cudaEvent_t ev[MAXEV];
+    const char *name[MAXEV];
+    int n = 0;
+};
+
 struct Launch {
     cudaStream_t s;
     int sm_count;
+    Prof *prof = nullptr;
 };
+
+inline void mark(const Launch &L, const char *name) {
+    if (L.prof && L.prof->n < Prof::MAXEV) {
+        cudaEventRecord(L.prof->ev[L.prof->n], L.s);
+        L.prof->name[L.prof->n] = name;
+        L.prof->n++;
+    }
+}
 
 void launch_step_begin(const Dev &d, Launch L);
 void launch_prim(const Dev &d, Launch L);

@@ -14,7 +14,7 @@ namespace mgpu {
 
 static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
 
-constexpr int LMAX = 160;   // longest K or I line LOSS handles
+constexpr int LMAX = 164;   // IM, KM <= 160 plus the 1-based end slots
 
 // viscosity set on entry to LOSS (8088-8112); one thread
 __global__ void k_loss_prologue(Dev d, int init_call) {
@@ -445,10 +445,13 @@ __global__ void __launch_bounds__(128) k_loss_ifaces(Dev d, int init_call) {
 
 void launch_loss(const Dev &d, Launch L, bool init_call) {
     k_loss_prologue<<<1, 1, 0, L.s>>>(d, init_call ? 1 : 0);
+    mark(L, "k_loss_prologue");
     int nk = d.IMM1 * (d.JM - 1);
     k_loss_kfaces<<<grid_for(nk, 128), 128, 0, L.s>>>(d, init_call ? 1 : 0);
+    mark(L, "k_loss_kfaces");
     int ni = (d.JM - 1) * d.KMM1;
     k_loss_ifaces<<<grid_for(ni, 128), 128, 0, L.s>>>(d, init_call ? 1 : 0);
+    mark(L, "k_loss_ifaces");
 }
 
 // ---------------------------------------------------------------------
@@ -651,12 +654,16 @@ __global__ void k_tail_final(Dev d, int nparts) {
 
 void launch_tail(const Dev &d, Launch L) {
     k_tail_flow<<<d.JM, TAIL_BS, 0, L.s>>>(d);
+    mark(L, "k_tail_flow");
     size_t N = (size_t)d.IM * d.JM * d.KM;
     int prim_parts = (int)grid_for(N, 256);
     k_tail_vref<<<1, 1024, 0, L.s>>>(d, prim_parts);
+    mark(L, "k_tail_vref");
     int parts = (int)grid_for(N, TAIL_BS);
     k_tail_dvm<<<parts, TAIL_BS, 0, L.s>>>(d);
+    mark(L, "k_tail_dvm");
     k_tail_final<<<1, 1024, 0, L.s>>>(d, parts);
+    mark(L, "k_tail_final");
 }
 
 // ---------------------------------------------------------------------
@@ -706,7 +713,7 @@ __global__ void k_stepup_cell(Dev d, float RELAX, int gated) {
     if (i >= d.IM || j < 2 || k >= d.KM) return;
     float step = stepup_cell(d, i, j, k, RELAX);
     float rstep = step / d.BSTEP[n];
-    if (A1(d.INDMIX, j - 1) == 1) {     // J = JMIX+1: take the step of JMIX+2
+    if (A1(d.INDMIX, j - 1) == 1 && j < d.JM) {     // J = JMIX+1: take the step of JMIX+2
         step = stepup_cell(d, i, j + 1, k, RELAX);
         rstep = 0.0f;
     }
@@ -733,8 +740,11 @@ void launch_stepup(const Dev &d, Launch L, float relax, bool gated) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
     unsigned g = grid_for(N, 256);
     k_stepup_node<<<g, 256, 0, L.s>>>(d, gated ? 1 : 0);
+    mark(L, "k_stepup_node");
     k_stepup_cell<<<g, 256, 0, L.s>>>(d, relax, gated ? 1 : 0);
+    mark(L, "k_stepup_cell");
     k_stepup_store<<<g, 256, 0, L.s>>>(d, gated ? 1 : 0);
+    mark(L, "k_stepup_store");
 }
 
 // ---------------------------------------------------------------------
@@ -791,7 +801,9 @@ __global__ void __launch_bounds__(TAIL_BS) k_int_sum(Dev d, double *out) {
 void launch_integrals(const Dev &d, Launch L, double *out) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
     k_int_node<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+    mark(L, "k_int_node");
     k_int_sum<<<d.JM, TAIL_BS, 0, L.s>>>(d, out);
+    mark(L, "k_int_sum");
 }
 
 }  // namespace mgpu

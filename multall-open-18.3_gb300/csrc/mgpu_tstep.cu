@@ -1,150 +1,37 @@
 // mgpu_tstep.cu -- SUBROUTINE TSTEP (multall-open-18.3.f:5470-5932) with
 // SMOOTH_VAR (15352-15594) and SMOOTH_RESID (14833-14917) on the GPU.
 //
-// Per call, for one conserved variable D with its SCREE history DIFF:
-//   prep     tip-gap TFLUX balance and mixing-plane flux extrapolation
-//   delta    flux sum -> STORE, DIFF update (one thread per cell)
-//   mp1      pitchwise redistribution of STORE at the mixing planes
-//   restrict level-1/level-2 block sums, one thread per block walking its
-//            cells in the reference's (K,J,I) order; per-J-plane sums (FP64)
-//            for the superblocks
-//   prolong  STORE*STEP + block corrections*RSTEP (one CTA per J-plane;
-//            also the per-plane sum of |STORE| for the negative feedback)
-//   avgblk   per-row mean |STORE| and its row smoothing (AVG_BLK)
-//   damp     negative feedback, then mp2 (plain pitchwise mean at the MP)
-//   scatter  each node gathers its <= 8 cell changes in the order the
-//            reference's scatter loop adds them, so no atomics are needed
-//   smooth   streamwise 2nd+4th order smoothing (gather, J+-2), then one
-//            CTA per J-plane in shared memory: pitchwise and spanwise
-//            smoothing, corners, exit smoothing, periodic, tip-gap and
-//            mixing-plane averaging of D.
+// One call updates one conserved variable D with its SCREE history DIFF in
+// four kernels, each with one CTA per J-plane (a J-plane of the largest
+// configuration, 73 x 57 points, is 16 KB: it lives in shared memory):
+//   cells    tip-gap TFLUX balance, mixing-plane flux extrapolation into
+//            SOURCE, the flux sum DELTA -> STORE and DIFF, the pitchwise
+//            redistribution of STORE on the mixing-plane cells, and this
+//            plane's partial sums for the three multigrid levels
+//   prolong  block sums assembled from the plane partials (level-1 blocks
+//            span <= JR planes, level-2 <= JRBB, superblocks a row part);
+//            STORE*STEP + corrections*RSTEP; per-plane sum of |STORE|
+//   update   per-row mean |STORE| (negative feedback, 1501-1525) applied to
+//            the cell planes J and J+1, the second mixing-plane average
+//            (1850), then every node of plane J gathers its <= 8 cell
+//            changes in the order the reference's scatter loop adds them
+//            (1100) -- no atomics, result written to TMP
+//   smooth   streamwise smoothing of plane J from TMP planes J-2..J+2, then
+//            pitchwise, spanwise, corners, exit smoothing, periodic,
+//            tip-gap and mixing-plane averaging in shared memory -> D
+// With REDUCE_ORDER=1 the level sums and the row mean are instead formed by
+// single threads in the reference's sequential REAL*4 order (parity checks).
 #include "mgpu_internal.cuh"
 
 namespace mgpu {
 
 static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
 
-// ---------------------------------------------------------------------
-// tip-gap flux balance (5503-5510) and mixing-plane extrapolation of the
-// upstream fluxes into SOURCE (5516-5555)
-// ---------------------------------------------------------------------
-__global__ void k_ts_prep(Dev d) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    int ntip = (d.JM - 1) * d.KMM1;
-    if (t < ntip) {
-        int j = t / d.KMM1 + 2, k = t % d.KMM1 + 1;
-        int nr = A1(d.NROW, j);
-        int ks = A1(d.KTIPS, nr);
-        if (ks > 0 && k >= ks && k <= A1(d.KTIPE, nr) - 1) {
-            float a = 0.5f * (A3(d.TFLUX, 1, j, k) + A3(d.TFLUX, d.IM, j, k));
-            A3(d.TFLUX, 1, j, k) = a;
-            A3(d.TFLUX, d.IM, j, k) = a;
-        }
-        return;
-    }
-    t -= ntip;
-    if (t >= d.NRWSM1 * d.KMM1) return;
-    if (d.FEXTRAP < 0.001f) return;
-    int nr = t / d.KMM1 + 1, k = t % d.KMM1 + 1;
-    int j = A1(d.JMIX, nr), jp1 = j + 1, jm1 = j - 1, jp2 = j + 2;
-    float FLOWDIRN = -A3(d.FLOWX, d.IMID, j, k);
-    float AVFLXJM1 = 0.0f, AVFLXJP2 = 0.0f;
-    for (int i = 1; i <= d.IMM1; ++i) {
-        AVFLXJM1 = AVFLXJM1 + A3(d.XFLUX, i, jm1, k);
-        AVFLXJP2 = AVFLXJP2 + A3(d.XFLUX, i, jp2, k);
-    }
-    for (int i = 1; i <= d.IMM1; ++i) {
-        if (FLOWDIRN > 0.0f) {
-            float DFLUX = (A3(d.XFLUX, i, jm1, k) - AVFLXJM1 * A1(d.FP, i)) * d.FEXTRAP;
-            A3(d.SOURCE, i, j, k) = A3(d.SOURCE, i, j, k) - DFLUX;
-        } else {
-            float DFLUX = (A3(d.XFLUX, i, jp2, k) - AVFLXJP2 * A1(d.FP, i)) * d.FEXTRAP;
-            A3(d.SOURCE, i, jp2, k) = A3(d.SOURCE, i, jp2, k) + DFLUX;
-        }
-        A3(d.SOURCE, i, jp1, k) = 0.0f;
-    }
-}
+constexpr int TS_BS = 256;
+constexpr int SV_BS = 512;
 
-// flux sum and SCREE/SSS update (1000)
-__global__ void k_ts_delta(Dev d, float *__restrict__ DIFF) {
-    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t N = (size_t)d.IM * d.JM * d.KM;
-    if (n >= N) return;
-    int i, j, k;
-    node_ijk(d, n, i, j, k);
-    if (i >= d.IM || j < 2 || k >= d.KM) return;
-    float RATPITCH = (float)A1(d.NBLADE, j - 1) / (float)A1(d.NBLADE, j);
-    float DELTA = d.XFLUX[n] - A3(d.XFLUX, i, j - 1, k) * RATPITCH + d.RFLUX[n] - A3(d.RFLUX, i, j, k + 1) + d.TFLUX[n] -
-                  A3(d.TFLUX, i + 1, j, k) - d.SOURCE[n];
-    float df = DIFF[n];
-    d.STORE[n] = d.F1 * DELTA + d.F2 * df;
-    DIFF[n] = DELTA + d.F3 * df;
-}
-
-// pitchwise redistribution of the change at the mixing planes (1750);
-// plain=1 gives the second, plain-mean averaging after the multigrid (1850)
-__global__ void k_ts_mp(Dev d, int plain) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= d.NRWSM1 * d.KMM1) return;
-    int nr = t / d.KMM1 + 1, k = t % d.KMM1 + 1;
-    int j = A1(d.JMIX, nr);
-    float FLOWDIRN = -A3(d.FLOWX, d.IMID, j, k);
-    bool lowx = d.FEXTRAP < 0.001f;
-    for (int pass = 0; pass < 2; ++pass) {
-        bool on = pass == 0 ? (FLOWDIRN > 0.0f || lowx) : (FLOWDIRN < 0.0f || lowx);
-        if (!on) continue;
-        int jj = pass == 0 ? j + 2 : j;
-        float SUM_STORE = 0.0f;
-        for (int i = 1; i <= d.IMM1; ++i) SUM_STORE = SUM_STORE + A3(d.STORE, i, jj, k);
-        if (plain) {
-            SUM_STORE = SUM_STORE / (float)d.IMM1;
-            for (int i = 1; i <= d.IMM1; ++i) A3(d.STORE, i, jj, k) = SUM_STORE;
-        } else {
-            for (int i = 1; i <= d.IMM1; ++i) A3(d.STORE, i, jj, k) = SUM_STORE * A1(d.FP, i);
-        }
-    }
-}
-
-// multigrid restriction (700): level-1 and level-2 block sums.  Each thread
-// owns one block and adds its cells in the reference's (K,J,I) loop order.
-__global__ void k_ts_restrict(Dev d) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    int n1 = d.NIB1 * (d.NJB1 + 1) * d.NKB1;
-    int n2 = d.NIB2 * (d.NJB2 + 1) * d.NKB2;
-    const int *JS, *JE, *IS, *IE, *KS, *KE;
-    int nib, njb;
-    float *out;
-    if (t < n1) {
-        nib = d.NIB1; njb = d.NJB1;
-        JS = d.JB1_START; JE = d.JB1_END; IS = d.IB1_S; IE = d.IB1_E; KS = d.KB1_S; KE = d.KB1_E;
-        out = d.B1CHG;
-    } else if (t < n1 + n2) {
-        t -= n1;
-        nib = d.NIB2; njb = d.NJB2;
-        JS = d.JB2_START; JE = d.JB2_END; IS = d.IB2_S; IE = d.IB2_E; KS = d.KB2_S; KE = d.KB2_E;
-        out = d.B2CHG;
-    } else {
-        return;
-    }
-    int ib = t % nib + 1;
-    int jb = (t / nib) % (njb + 1) + 1;
-    int kb = t / (nib * (njb + 1)) + 1;
-    float s = 0.0f;
-    if (jb <= njb) {
-        int j0 = JS[jb - 1], j1 = JE[jb - 1];
-        int i0 = IS[ib - 1], i1 = IE[ib - 1];
-        int k0 = KS[kb - 1], k1 = KE[kb - 1];
-        for (int k = k0; k <= k1; ++k)
-            for (int j = j0; j <= j1; ++j)
-                for (int i = i0; i <= i1; ++i) s = s + A3(d.STORE, i, j, k);
-    }
-    out[t] = s;
-}
-
-// per-J-plane sums of STORE (abs=0) or |STORE| (abs=1) in FP64
 template <int BS>
-__device__ inline double block_sum(double v) {
-    __shared__ double sh[BS / 32];
+__device__ inline double block_sum(double v, double *sh) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     if (l == 0) sh[w] = v;
@@ -154,73 +41,242 @@ __device__ inline double block_sum(double v) {
         r = l < BS / 32 ? sh[l] : 0.0;
         for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
     }
+    __syncthreads();
     return r;
 }
 
-constexpr int PLANE_BS = 256;
-
-__global__ void __launch_bounds__(PLANE_BS) k_ts_plane_sum(Dev d, int absval, double *out) {
-    int j = blockIdx.x + 2;
-    int ncell = d.IMM1 * d.KMM1;
-    double s = 0.0;
-    for (int c = threadIdx.x; c < ncell; c += PLANE_BS) {
-        int i = c % d.IMM1 + 1, k = c / d.IMM1 + 1;
-        float v = A3(d.STORE, i, j, k);
-        s += absval ? (double)fabsf(v) : (double)v;
+// position of plane j relative to the mixing planes: 1 = JMIX, 2 = JMIX+1,
+// 3 = JMIX+2 (0 otherwise); *nr receives the row interface
+__device__ inline int mp_role(const Dev &d, int j, int *nr) {
+    for (int r = 1; r <= d.NRWSM1; ++r) {
+        int jx = A1(d.JMIX, r);
+        if (j == jx) { *nr = r; return 1; }
+        if (j == jx + 1) { *nr = r; return 2; }
+        if (j == jx + 2) { *nr = r; return 3; }
     }
-    s = block_sum<PLANE_BS>(s);
-    if (threadIdx.x == 0) out[j - 1] = s;
+    *nr = 0;
+    return 0;
 }
 
-// prolongation and time step (1500); with the negative feedback on and no
-// residual smoothing the per-plane sum of |STORE| is formed here too
-__global__ void __launch_bounds__(PLANE_BS) k_ts_prolong(Dev d, int want_abs) {
-    int j = blockIdx.x + 2;
-    __shared__ float s_sb;
-    if (threadIdx.x < 32) {
-        int sb = A1(d.JSBLK, j);
-        int a = A1(d.SB_START, sb), b = A1(d.SB_END, sb);
-        double s = 0.0;
-        for (int jj = a + (int)threadIdx.x; jj <= b; jj += 32) s += d.plane_sum[jj - 1];
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if (threadIdx.x == 0) s_sb = (float)s;
+// ---------------------------------------------------------------------
+// cells: 5503-5510 (tip gap), 5516-5555 (MP extrapolation), 1000 (flux
+// sum), 1750 (MP redistribution) and the multigrid partial sums
+// ---------------------------------------------------------------------
+__global__ void __launch_bounds__(TS_BS) k_ts_cells(Dev d, float *__restrict__ DIFF) {
+    extern __shared__ float sm[];
+    __shared__ double shd[TS_BS / 32];
+    const int j = blockIdx.x + 2;
+    const int IM = d.IM, IMM1 = d.IMM1, KMM1 = d.KMM1;
+    const int nc = IMM1 * KMM1;
+    float *st = sm;              // STORE of this plane, [k-1][i-1]
+    float *lsum = sm + nc;       // per-K line sums
+    int mnr;
+    const int role = mp_role(d, j, &mnr);
+    const bool lowx = d.FEXTRAP < 0.001f;
+    const int jmx = role ? A1(d.JMIX, mnr) : 0;
+    if ((role == 1 || role == 3) && !lowx) {
+        int jj = role == 1 ? j - 1 : j;
+        for (int k = threadIdx.x + 1; k <= KMM1; k += TS_BS) {
+            float s = 0.0f;
+            for (int i = 1; i <= IMM1; ++i) s = s + A3(d.XFLUX, i, jj, k);
+            lsum[k - 1] = s;
+        }
     }
     __syncthreads();
-    float SBCHG = s_sb;
-    int jsb = A1(d.JSBLK, j);
-    float SSB = A1(d.STEPSBK, jsb);
-    int j1 = A1(d.JB1, j), j2 = A1(d.JB2, j);
-    int ncell = d.IMM1 * d.KMM1;
-    double sabs = 0.0;
-    for (int c = threadIdx.x; c < ncell; c += PLANE_BS) {
-        int i = c % d.IMM1 + 1, k = c / d.IMM1 + 1;
-        int i1 = A1(d.IB1, i), i2 = A1(d.IB2, i), k1 = A1(d.KB1, k), k2 = A1(d.KB2, k);
-        size_t b1 = (size_t)(i1 - 1) + (size_t)d.NIB1 * ((size_t)(j1 - 1) + (size_t)(d.NJB1 + 1) * (k1 - 1));
-        size_t b2 = (size_t)(i2 - 1) + (size_t)d.NIB2 * ((size_t)(j2 - 1) + (size_t)(d.NJB2 + 1) * (k2 - 1));
+    const float RATPITCH = (float)A1(d.NBLADE, j - 1) / (float)A1(d.NBLADE, j);
+    const int nr = A1(d.NROW, j);
+    const int kts = A1(d.KTIPS, nr), kte = A1(d.KTIPE, nr);
+    const float F1 = d.F1, F2 = d.F2, F3 = d.F3;
+    for (int c = threadIdx.x; c < nc; c += TS_BS) {
+        int i = c % IMM1 + 1, k = c / IMM1 + 1;
         size_t n = ix3(d, i, j, k);
-        float DELTA = d.STORE[n] * d.STEP[n] +
-                      (d.B1CHG[b1] * d.STEP1[b1] + d.B2CHG[b2] * d.STEP2[b2] + SBCHG * SSB) * d.RSTEP[n];
+        float t0 = d.TFLUX[n], t1 = A3(d.TFLUX, i + 1, j, k);
+        if (kts > 0 && k >= kts && k <= kte - 1) {
+            if (i == 1 || i + 1 == IM) {
+                float tb = 0.5f * (A3(d.TFLUX, 1, j, k) + A3(d.TFLUX, IM, j, k));
+                if (i == 1) t0 = tb;
+                if (i + 1 == IM) t1 = tb;
+            }
+        }
+        float src = d.SOURCE[n];
+        if (role && !lowx) {
+            float FLOWDIRN = -A3(d.FLOWX, d.IMID, jmx, k);
+            if (role == 1 && FLOWDIRN > 0.0f) src = src - (A3(d.XFLUX, i, j - 1, k) - lsum[k - 1] * A1(d.FP, i)) * d.FEXTRAP;
+            if (role == 2) src = 0.0f;
+            if (role == 3 && !(FLOWDIRN > 0.0f)) src = src + (d.XFLUX[n] - lsum[k - 1] * A1(d.FP, i)) * d.FEXTRAP;
+        }
+        float DELTA = d.XFLUX[n] - A3(d.XFLUX, i, j - 1, k) * RATPITCH + d.RFLUX[n] - A3(d.RFLUX, i, j, k + 1) + t0 - t1 - src;
+        float df = DIFF[n];
+        st[c] = F1 * DELTA + F2 * df;
+        DIFF[n] = DELTA + F3 * df;
+    }
+    __syncthreads();
+    if (role == 1 || role == 3) {
+        for (int k = threadIdx.x + 1; k <= KMM1; k += TS_BS) {
+            float FLOWDIRN = -A3(d.FLOWX, d.IMID, jmx, k);
+            bool on = role == 3 ? (FLOWDIRN > 0.0f || lowx) : (FLOWDIRN < 0.0f || lowx);
+            if (!on) continue;
+            float *row = st + (size_t)(k - 1) * IMM1;
+            float s = 0.0f;
+            for (int i = 0; i < IMM1; ++i) s = s + row[i];
+            for (int i = 0; i < IMM1; ++i) row[i] = s * A1(d.FP, i + 1);
+        }
+        __syncthreads();
+    }
+    double ps = 0.0;
+    for (int c = threadIdx.x; c < nc; c += TS_BS) {
+        int i = c % IMM1 + 1, k = c / IMM1 + 1;
+        float v = st[c];
+        A3(d.STORE, i, j, k) = v;
+        ps += (double)v;
+    }
+    ps = block_sum<TS_BS>(ps, shd);
+    if (threadIdx.x == 0) d.plane_sum[j - 1] = ps;
+    // level-1 and level-2 partial sums of this plane
+    const int n1 = d.NIB1 * d.NKB1, n2 = d.NIB2 * d.NKB2;
+    for (int t = threadIdx.x; t < n1 + n2; t += TS_BS) {
+        const bool lv1 = t < n1;
+        int u = lv1 ? t : t - n1;
+        int nib = lv1 ? d.NIB1 : d.NIB2;
+        int ib = u % nib + 1, kb = u / nib + 1;
+        int i0 = lv1 ? A1(d.IB1_S, ib) : A1(d.IB2_S, ib), i1 = lv1 ? A1(d.IB1_E, ib) : A1(d.IB2_E, ib);
+        int k0 = lv1 ? A1(d.KB1_S, kb) : A1(d.KB2_S, kb), k1 = lv1 ? A1(d.KB1_E, kb) : A1(d.KB2_E, kb);
+        float s = 0.0f;
+        for (int k = k0; k <= k1; ++k)
+            for (int i = i0; i <= i1; ++i) s = s + st[(k - 1) * IMM1 + (i - 1)];
+        if (lv1) d.P1[(size_t)(j - 1) * n1 + u] = s;
+        else d.P2[(size_t)(j - 1) * n2 + u] = s;
+    }
+}
+
+// ---------------------------------------------------------------------
+// reference-order level sums (REDUCE_ORDER=1): one thread per block walks
+// its cells in the (K,J,I) loop order of 700; superblocks likewise
+// ---------------------------------------------------------------------
+__global__ void k_ts_restrict_seq(Dev d) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int n1 = d.NIB1 * (d.NJB1 + 1) * d.NKB1;
+    int n2 = d.NIB2 * (d.NJB2 + 1) * d.NKB2;
+    if (t >= n1 + n2 + d.NSBLK) return;
+    if (t >= n1 + n2) {
+        int sb = t - n1 - n2 + 1;
+        int a = A1(d.SB_START, sb), b = A1(d.SB_END, sb);
+        float s = 0.0f;
+        for (int k = 1; k <= d.KMM1; ++k)
+            for (int j = a; j <= b; ++j)
+                for (int i = 1; i <= d.IMM1; ++i) s = s + A3(d.STORE, i, j, k);
+        A1(d.SBSUM, sb) = s;
+        return;
+    }
+    const bool lv1 = t < n1;
+    int u = lv1 ? t : t - n1;
+    int nib = lv1 ? d.NIB1 : d.NIB2, njb = lv1 ? d.NJB1 : d.NJB2;
+    int ib = u % nib + 1;
+    int jb = (u / nib) % (njb + 1) + 1;
+    int kb = u / (nib * (njb + 1)) + 1;
+    float s = 0.0f;
+    if (jb <= njb) {
+        int j0 = lv1 ? A1(d.JB1_START, jb) : A1(d.JB2_START, jb), j1 = lv1 ? A1(d.JB1_END, jb) : A1(d.JB2_END, jb);
+        int i0 = lv1 ? A1(d.IB1_S, ib) : A1(d.IB2_S, ib), i1 = lv1 ? A1(d.IB1_E, ib) : A1(d.IB2_E, ib);
+        int k0 = lv1 ? A1(d.KB1_S, kb) : A1(d.KB2_S, kb), k1 = lv1 ? A1(d.KB1_E, kb) : A1(d.KB2_E, kb);
+        for (int k = k0; k <= k1; ++k)
+            for (int j = j0; j <= j1; ++j)
+                for (int i = i0; i <= i1; ++i) s = s + A3(d.STORE, i, j, k);
+    }
+    (lv1 ? d.B1CHG : d.B2CHG)[u] = s;
+}
+
+// ---------------------------------------------------------------------
+// prolong: 1500, with the block sums assembled from the plane partials
+// ---------------------------------------------------------------------
+__global__ void __launch_bounds__(TS_BS) k_ts_prolong(Dev d, int want_abs) {
+    extern __shared__ float sm[];
+    __shared__ double shd[TS_BS / 32];
+    __shared__ float s_sb;
+    const int j = blockIdx.x + 2;
+    const int IMM1 = d.IMM1, KMM1 = d.KMM1;
+    const int n1 = d.NIB1 * d.NKB1, n2 = d.NIB2 * d.NKB2;
+    float *b1 = sm, *b2 = sm + n1;
+    const int j1 = A1(d.JB1, j), j2 = A1(d.JB2, j), jsb = A1(d.JSBLK, j);
+    if (d.REDUCE_ORDER == 1) {
+        for (int t = threadIdx.x; t < n1; t += TS_BS) {
+            int ib = t % d.NIB1 + 1, kb = t / d.NIB1 + 1;
+            b1[t] = d.B1CHG[(size_t)(ib - 1) + (size_t)d.NIB1 * ((size_t)(j1 - 1) + (size_t)(d.NJB1 + 1) * (kb - 1))];
+        }
+        for (int t = threadIdx.x; t < n2; t += TS_BS) {
+            int ib = t % d.NIB2 + 1, kb = t / d.NIB2 + 1;
+            b2[t] = d.B2CHG[(size_t)(ib - 1) + (size_t)d.NIB2 * ((size_t)(j2 - 1) + (size_t)(d.NJB2 + 1) * (kb - 1))];
+        }
+        if (threadIdx.x == 0) s_sb = A1(d.SBSUM, jsb);
+    } else {
+        for (int t = threadIdx.x; t < n1; t += TS_BS) {
+            float s = 0.0f;
+            if (j1 <= d.NJB1)
+                for (int jj = A1(d.JB1_START, j1); jj <= A1(d.JB1_END, j1); ++jj) s = s + d.P1[(size_t)(jj - 1) * n1 + t];
+            b1[t] = s;
+        }
+        for (int t = threadIdx.x; t < n2; t += TS_BS) {
+            float s = 0.0f;
+            if (j2 <= d.NJB2)
+                for (int jj = A1(d.JB2_START, j2); jj <= A1(d.JB2_END, j2); ++jj) s = s + d.P2[(size_t)(jj - 1) * n2 + t];
+            b2[t] = s;
+        }
+        if (threadIdx.x < 32) {
+            int a = A1(d.SB_START, jsb), b = A1(d.SB_END, jsb);
+            double s = 0.0;
+            for (int jj = a + (int)threadIdx.x; jj <= b; jj += 32) s += d.plane_sum[jj - 1];
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if (threadIdx.x == 0) s_sb = (float)s;
+        }
+    }
+    __syncthreads();
+    const float SBCHG = s_sb, SSB = A1(d.STEPSBK, jsb);
+    const int nc = IMM1 * KMM1;
+    double sabs = 0.0;
+    for (int c = threadIdx.x; c < nc; c += TS_BS) {
+        int i = c % IMM1 + 1, k = c / IMM1 + 1;
+        int i1 = A1(d.IB1, i), i2 = A1(d.IB2, i), k1 = A1(d.KB1, k), k2 = A1(d.KB2, k);
+        size_t s1 = (size_t)(i1 - 1) + (size_t)d.NIB1 * ((size_t)(j1 - 1) + (size_t)(d.NJB1 + 1) * (k1 - 1));
+        size_t s2 = (size_t)(i2 - 1) + (size_t)d.NIB2 * ((size_t)(j2 - 1) + (size_t)(d.NJB2 + 1) * (k2 - 1));
+        size_t n = ix3(d, i, j, k);
+        float B1 = b1[(k1 - 1) * d.NIB1 + (i1 - 1)], B2 = b2[(k2 - 1) * d.NIB2 + (i2 - 1)];
+        float DELTA = d.STORE[n] * d.STEP[n] + (B1 * d.STEP1[s1] + B2 * d.STEP2[s2] + SBCHG * SSB) * d.RSTEP[n];
         d.STORE[n] = DELTA;
         sabs += (double)fabsf(DELTA);
     }
     if (want_abs) {
-        sabs = block_sum<PLANE_BS>(sabs);
+        sabs = block_sum<TS_BS>(sabs, shd);
         if (threadIdx.x == 0) d.plane_abs[j - 1] = sabs;
     }
 }
 
-// per-row average change AVG_CHG and its smoothing AVG_BLK (1501-1515)
-__global__ void k_ts_avgblk(Dev d) {
+// per-J-plane sum of |STORE| (after residual smoothing)
+__global__ void __launch_bounds__(TS_BS) k_ts_plane_abs(Dev d) {
+    __shared__ double shd[TS_BS / 32];
+    int j = blockIdx.x + 2;
+    int nc = d.IMM1 * d.KMM1;
+    double s = 0.0;
+    for (int c = threadIdx.x; c < nc; c += TS_BS) {
+        int i = c % d.IMM1 + 1, k = c / d.IMM1 + 1;
+        s += (double)fabsf(A3(d.STORE, i, j, k));
+    }
+    s = block_sum<TS_BS>(s, shd);
+    if (threadIdx.x == 0) d.plane_abs[j - 1] = s;
+}
+
+// AVG_CHG / AVG_BLK with the reference's sequential REAL*4 sum (1501-1515)
+__global__ void k_ts_avgblk_seq(Dev d) {
     __shared__ float chg[64];
     if (!d.ctl->damp_on) return;
     int NROWS = d.NROWS;
     for (int nr = threadIdx.x + 1; nr <= NROWS; nr += blockDim.x) {
         int JST = A1(d.JSTART, nr) + 1, JEN = A1(d.JMIX, nr) - 1;
-        int JCHANGE = JEN - JST + 1;
-        int NSUM = d.IMM1 * d.KMM1 * JCHANGE;
-        double s = 0.0;
-        for (int j = JST; j <= JEN; ++j) s += d.plane_abs[j - 1];
-        chg[nr - 1] = (float)s / (float)NSUM;
+        int NSUM = d.IMM1 * d.KMM1 * (JEN - JST + 1);
+        float SUMCHG = 0.0f;
+        for (int k = 1; k <= d.KMM1; ++k)
+            for (int j = JST; j <= JEN; ++j)
+                for (int i = 1; i <= d.IMM1; ++i) SUMCHG = SUMCHG + fabsf(A3(d.STORE, i, j, k));
+        chg[nr - 1] = SUMCHG / (float)NSUM;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -238,120 +294,175 @@ __global__ void k_ts_avgblk(Dev d) {
     }
 }
 
-// negative feedback (1525)
-__global__ void k_ts_damp(Dev d) {
-    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t N = (size_t)d.IM * d.JM * d.KM;
-    if (n >= N) return;
-    int i, j, k;
-    node_ijk(d, n, i, j, k);
-    if (i >= d.IM || j < 2 || k >= d.KM) return;
-    if (!d.ctl->damp_on) return;
-    float DAMP = d.ctl->DAMP;
-    int nr = A1(d.NROW, j);
-    float DELTA = d.STORE[n];
-    float ABSCHG = fabsf(DELTA);
-    float FDAMP = ABSCHG / A1(d.AVG_BLK, nr);
-    d.STORE[n] = DELTA / (1.0f + FDAMP / DAMP);
-}
-
-// corner distribution (1100) as a gather: node (I,J,K) adds, in the order
-// the reference's cell loop reaches it, the weighted change of each of its
-// <= 8 neighbouring cells
-__global__ void k_ts_scatter(Dev d, float *__restrict__ D) {
-    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t N = (size_t)d.IM * d.JM * d.KM;
-    if (n >= N) return;
-    int i, j, k;
-    node_ijk(d, n, i, j, k);
-    float v = D[n];
-    for (int kc = k - 1; kc <= k; ++kc) {
-        if (kc < 1 || kc > d.KMM1) continue;
-        for (int jc = j; jc <= j + 1; ++jc) {
-            if (jc < 2 || jc > d.JM) continue;
-            float fac = (jc == j) ? A1(d.FACDWN, jc) : A1(d.FACUP, jc);
-            for (int ic = i - 1; ic <= i; ++ic) {
-                if (ic < 1 || ic > d.IMM1) continue;
-                float w;
-                if (ic == i) w = (kc == k) ? AIK(d.FBL, ic, kc) : AIK(d.FTL, ic, kc);
-                else w = (kc == k) ? AIK(d.FBR, ic, kc) : AIK(d.FTR, ic, kc);
-                v = v + A3(d.STORE, ic, jc, kc) * w * fac;
+// ---------------------------------------------------------------------
+// update: negative feedback, second MP average, corner gather -> TMP
+// ---------------------------------------------------------------------
+__global__ void __launch_bounds__(TS_BS) k_ts_update(Dev d, const float *__restrict__ D) {
+    extern __shared__ float sm[];
+    __shared__ float s_blk[64];
+    __shared__ float chg[64];
+    const int j = blockIdx.x + 1;
+    const int IM = d.IM, IMM1 = d.IMM1, KM = d.KM, KMM1 = d.KMM1;
+    const int nc = IMM1 * KMM1;
+    float *cA = sm, *cB = sm + nc;            // cell planes j and j+1
+    const DevCtl *ctl = d.ctl;
+    const int damp_on = ctl->damp_on;
+    const float DAMP = ctl->DAMP;
+    if (damp_on) {
+        if (d.REDUCE_ORDER == 1) {
+            for (int r = threadIdx.x; r < d.NROWS; r += TS_BS) s_blk[r] = d.AVG_BLK[r];
+        } else {
+            int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+            for (int nr = w + 1; nr <= d.NROWS; nr += TS_BS / 32) {
+                int JST = A1(d.JSTART, nr) + 1, JEN = A1(d.JMIX, nr) - 1;
+                double s = 0.0;
+                for (int jj = JST + l; jj <= JEN; jj += 32) s += d.plane_abs[jj - 1];
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+                if (l == 0) chg[nr - 1] = (float)s / (float)(IMM1 * KMM1 * (JEN - JST + 1));
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int NROWS = d.NROWS;
+                if (NROWS == 1) s_blk[0] = chg[0];
+                if (NROWS == 2) {
+                    s_blk[1] = 0.5f * (chg[0] + chg[1]);
+                    s_blk[0] = s_blk[1];
+                }
+                if (NROWS > 2) {
+                    for (int nr = 2; nr <= NROWS - 1; ++nr)
+                        s_blk[nr - 1] = 0.25f * (chg[nr - 2] + chg[nr]) + 0.5f * chg[nr - 1];
+                    s_blk[NROWS - 1] = 0.5f * (chg[NROWS - 2] + chg[NROWS - 1]);
+                    s_blk[0] = 0.5f * (chg[0] + chg[1]);
+                }
             }
         }
+        __syncthreads();
     }
-    D[n] = v;
+    // damped cell changes of the two planes this node plane touches
+    for (int h = 0; h < 2; ++h) {
+        int jc = j + h;
+        if (jc < 2 || jc > d.JM) continue;
+        float *c = h ? cB : cA;
+        float blk = damp_on ? s_blk[A1(d.NROW, jc) - 1] : 1.0f;
+        for (int t = threadIdx.x; t < nc; t += TS_BS) {
+            int i = t % IMM1 + 1, k = t / IMM1 + 1;
+            float v = A3(d.STORE, i, jc, k);
+            if (damp_on) {
+                float FDAMP = fabsf(v) / blk;
+                v = v / (1.0f + FDAMP / DAMP);
+            }
+            c[t] = v;
+        }
+    }
+    __syncthreads();
+    // second pitchwise average on the mixing-plane cells (1850)
+    const bool lowx = d.FEXTRAP < 0.001f;
+    bool any = false;
+    for (int h = 0; h < 2; ++h) {
+        int jc = j + h;
+        if (jc < 2 || jc > d.JM) continue;
+        int mnr;
+        int role = mp_role(d, jc, &mnr);
+        if (role != 1 && role != 3) continue;
+        any = true;
+        float *c = h ? cB : cA;
+        int jmx = A1(d.JMIX, mnr);
+        for (int k = threadIdx.x + 1; k <= KMM1; k += TS_BS) {
+            float FLOWDIRN = -A3(d.FLOWX, d.IMID, jmx, k);
+            bool on = role == 3 ? (FLOWDIRN > 0.0f || lowx) : (FLOWDIRN < 0.0f || lowx);
+            if (!on) continue;
+            float *row = c + (size_t)(k - 1) * IMM1;
+            float s = 0.0f;
+            for (int i = 0; i < IMM1; ++i) s = s + row[i];
+            s = s / (float)IMM1;
+            for (int i = 0; i < IMM1; ++i) row[i] = s;
+        }
+    }
+    if (any) __syncthreads();
+    // gather (1100): cells (kc, jc, ic) in the reference's loop order
+    const int np = IM * KM;
+    const float fdn = A1(d.FACDWN, j);
+    const float fup = j + 1 <= d.JM ? A1(d.FACUP, j + 1) : 0.0f;
+    for (int t = threadIdx.x; t < np; t += TS_BS) {
+        int i = t % IM + 1, k = t / IM + 1;
+        size_t n = ix3(d, i, j, k);
+        float v = D[n];
+        for (int kc = k - 1; kc <= k; ++kc) {
+            if (kc < 1 || kc > KMM1) continue;
+            for (int h = 0; h < 2; ++h) {
+                int jc = j + h;
+                if (jc < 2 || jc > d.JM) continue;
+                const float *c = h ? cB : cA;
+                float fac = h ? fup : fdn;
+                for (int ic = i - 1; ic <= i; ++ic) {
+                    if (ic < 1 || ic > IMM1) continue;
+                    float w;
+                    if (ic == i) w = (kc == k) ? AIK(d.FBL, ic, kc) : AIK(d.FTL, ic, kc);
+                    else w = (kc == k) ? AIK(d.FBR, ic, kc) : AIK(d.FTR, ic, kc);
+                    v = v + c[(kc - 1) * IMM1 + (ic - 1)] * w * fac;
+                }
+            }
+        }
+        d.TMP[n] = v;
+    }
 }
 
 // ---------------------------------------------------------------------
-// SMOOTH_VAR: streamwise part (3900-4015) as a gather into TMP
+// smooth: SMOOTH_VAR (3900-9000, 8502) + periodic (8000), tip gap (510),
+// mixing-plane average (100): TMP -> D, one CTA per J-plane
 // ---------------------------------------------------------------------
-__global__ void k_sv_stream(Dev d, const float *__restrict__ D) {
-    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t N = (size_t)d.IM * d.JM * d.KM;
-    const DevCtl *c = d.ctl;
-    if (c->SFX < 0.0001f) return;
-    if (n >= N) return;
-    int i, j, k;
-    node_ijk(d, n, i, j, k);
+__device__ inline float stream_value(const Dev &d, const DevCtl *c, const float *__restrict__ S, int i, int j, int k) {
     int nr = A1(d.NROW, j);
     int J1 = A1(d.JSTART, nr), J2 = A1(d.JMIX, nr);
-    float SFX = c->SFX, SFX1 = c->SFX1, SFXB = c->SFXB, SFXB1 = c->SFXB1, SFXBH = c->SFXBH;
-#define DV(jj) A3(D, i, (jj), k)
-    float v = D[n];
+#define DV(jj) A3(S, i, (jj), k)
+    float d0 = DV(j);
+    float v = d0;
+    const float SFX = c->SFX, SFX1 = c->SFX1, SFXB = c->SFXB, SFXB1 = c->SFXB1, SFXBH = c->SFXBH;
     if (j >= J1 + 3 && j <= J2 - 3) {
         float AVERG = 0.5f * (DV(j + 1) + DV(j - 1));
-        float CURV = AVERG - 0.5f * v - 0.25f * (DV(j - 2) + DV(j + 2));
-        v = SFX1 * v + SFX * (AVERG + d.FAC_4TH * CURV);
+        float CURV = AVERG - 0.5f * d0 - 0.25f * (DV(j - 2) + DV(j + 2));
+        v = SFX1 * d0 + SFX * (AVERG + d.FAC_4TH * CURV);
     }
-    if (j == J2) v = D[n];
-    if (j == J1) v = D[n];
-    if (j == J1 + 2) v = SFXB1 * DV(J1 + 2) + SFXBH * (DV(J1 + 3) + DV(J1 + 1));
-    if (j == J1 + 1) v = SFXB1 * DV(J1 + 1) + SFXB * (1.25f * DV(J1 + 2) + 0.5f * DV(J1 + 3) - 0.75f * DV(J1 + 4));
-    if (j == J2 - 2) v = SFXB1 * DV(J2 - 2) + SFXBH * (DV(J2 - 1) + DV(J2 - 3));
-    if (j == J2 - 1) v = SFXB1 * DV(J2 - 1) + SFXB * (1.25f * DV(J2 - 2) + 0.5f * DV(J2 - 3) - 0.75f * DV(J2 - 4));
+    if (j == J2) v = d0;
+    if (j == J1) v = d0;
+    if (j == J1 + 2) v = SFXB1 * d0 + SFXBH * (DV(J1 + 3) + DV(J1 + 1));
+    if (j == J1 + 1) v = SFXB1 * d0 + SFXB * (1.25f * DV(J1 + 2) + 0.5f * DV(J1 + 3) - 0.75f * DV(J1 + 4));
+    if (j == J2 - 2) v = SFXB1 * d0 + SFXBH * (DV(J2 - 1) + DV(J2 - 3));
+    if (j == J2 - 1) v = SFXB1 * d0 + SFXB * (1.25f * DV(J2 - 2) + 0.5f * DV(J2 - 3) - 0.75f * DV(J2 - 4));
 #undef DV
     if (i == 1 || i == d.IM) {
         for (int r = 1; r <= d.NROWS; ++r) {
             int JL = A1(d.JLED, r);
-            if (j == JL - 2 || j == JL - 1)
-                v = c->SFXHM1 * D[n] + c->SFX14 * (A3(D, 2, j, k) + A3(D, d.IMM1, j, k));
+            if (j == JL - 2 || j == JL - 1) v = c->SFXHM1 * d0 + c->SFX14 * (A3(S, 2, j, k) + A3(S, d.IMM1, j, k));
             if (j == JL) {
-                if (i == 1) v = c->SFXHM1 * D[n] + c->SFX14 * (A3(D, 1, j + 1, k) + A3(D, d.IM, j, k));
-                else v = c->SFXHM1 * D[n] + c->SFX14 * (A3(D, d.IM, j + 1, k) + A3(D, 1, j, k));
+                if (i == 1) v = c->SFXHM1 * d0 + c->SFX14 * (A3(S, 1, j + 1, k) + A3(S, d.IM, j, k));
+                else v = c->SFXHM1 * d0 + c->SFX14 * (A3(S, d.IM, j + 1, k) + A3(S, 1, j, k));
             }
         }
     }
-    d.TMP[n] = v;
+    return v;
 }
 
-// ---------------------------------------------------------------------
-// SMOOTH_VAR pitchwise + spanwise + corners + exit smoothing (9000-8602),
-// then TSTEP's periodic (8000), tip-gap (510) and mixing-plane (100)
-// averaging of D: one CTA per J-plane, the plane held in shared memory.
-// ---------------------------------------------------------------------
-constexpr int SV_BS = 512;
-
-__global__ void __launch_bounds__(SV_BS) k_sv_plane(Dev d, float *__restrict__ D) {
+__global__ void __launch_bounds__(SV_BS) k_ts_smooth(Dev d, const float *__restrict__ S, float *__restrict__ D) {
     extern __shared__ float sm[];
     const int IM = d.IM, KM = d.KM, IMM1 = d.IMM1, KMM1 = d.KMM1;
     const int np = IM * KM;
     float *a = sm, *b = sm + np;
     const int j = blockIdx.x + 1;
     const DevCtl *c = d.ctl;
-    const float *src = (c->SFX < 0.0001f) ? D : d.TMP;
+    const bool stream = !(c->SFX < 0.0001f);
     for (int t = threadIdx.x; t < np; t += SV_BS) {
         int i = t % IM + 1, k = t / IM + 1;
-        a[t] = A3(src, i, j, k);
+        a[t] = stream ? stream_value(d, c, S, i, j, k) : A3(S, i, j, k);
     }
     __syncthreads();
 #define P(buf, i, k) buf[((i) - 1) + IM * ((k) - 1)]
     const bool periodic_j = !(A1(d.IND, j) == 1 || A1(d.INDLE, j) == 1);
     if (j >= 2 && !(c->SFT < 0.0001f)) {
         const float SFT = c->SFT, SFT1 = c->SFT1, F4 = d.FAC_4TH;
-        // pitchwise, Jacobi per K line: a -> b
         for (int t = threadIdx.x; t < np; t += SV_BS) {
             int i = t % IM + 1, k = t / IM + 1;
-            auto curve = [&](int ii) -> float {   // CURVE(ii), ii in 1..IM
+            auto curve = [&](int ii) -> float {
                 if (ii == 1 || ii == IM) {
                     if (!periodic_j) return 0.0f;
                     float avg1 = 0.5f * (P(a, 2, k) + P(a, IMM1, k));
@@ -377,7 +488,6 @@ __global__ void __launch_bounds__(SV_BS) k_sv_plane(Dev d, float *__restrict__ D
             P(b, i, k) = SFT1 * P(a, i, k) + SFT * (AVG + F4 * SC);
         }
         __syncthreads();
-        // spanwise, Jacobi per I line: b -> a
         for (int t = threadIdx.x; t < np; t += SV_BS) {
             int i = t % IM + 1, k = t / IM + 1;
             auto curvek = [&](int kk) -> float {
@@ -399,7 +509,6 @@ __global__ void __launch_bounds__(SV_BS) k_sv_plane(Dev d, float *__restrict__ D
             P(a, i, k) = SFT1 * P(b, i, k) + SFT * (AVG + F4 * SC);
         }
         __syncthreads();
-        // the four corners read no corner, so they update together
         float cv = 0.0f;
         if (threadIdx.x < 4) {
             const float SFTH = c->SFTH;
@@ -415,7 +524,6 @@ __global__ void __launch_bounds__(SV_BS) k_sv_plane(Dev d, float *__restrict__ D
         else if (threadIdx.x == 3) P(a, IM, KM) = cv;
         __syncthreads();
     }
-    // exit-flow smoothing (8502), Gauss-Seidel along I then along K
     if (!(d.SFEXIT < 0.0001f) && j >= d.JM + 1 - d.NSFEXIT) {
         const float SE = d.SFEXIT, SE1 = 1.0f - SE, SEH = 0.5f * SE;
         for (int k = threadIdx.x + 1; k <= KM; k += SV_BS) {
@@ -431,7 +539,6 @@ __global__ void __launch_bounds__(SV_BS) k_sv_plane(Dev d, float *__restrict__ D
         }
         __syncthreads();
     }
-    // periodic boundaries and tip-gap periodicity
     int nr = A1(d.NROW, j);
     int K1 = A1(d.KTIPS, nr), K2 = A1(d.KTIPE, nr);
     bool tip = K1 > 0;
@@ -452,7 +559,6 @@ __global__ void __launch_bounds__(SV_BS) k_sv_plane(Dev d, float *__restrict__ D
         }
     }
     __syncthreads();
-    // pitchwise average of D on both faces of each mixing plane
     bool mp = false;
     if (d.IFMIX != 0)
         for (int r = 1; r <= d.NRWSM1; ++r)
@@ -518,41 +624,65 @@ __global__ void k_copy(const float *__restrict__ src, float *__restrict__ dst, s
     if (t < n) dst[t] = src[t];
 }
 
+static size_t cells_smem(const Dev &d) { return ((size_t)d.IMM1 * d.KMM1 + d.KMM1) * sizeof(float); }
+static size_t prolong_smem(const Dev &d) { return ((size_t)d.NIB1 * d.NKB1 + (size_t)d.NIB2 * d.NKB2) * sizeof(float); }
+static size_t update_smem(const Dev &d) { return (size_t)2 * d.IMM1 * d.KMM1 * sizeof(float); }
+static size_t smooth_smem(const Dev &d) { return (size_t)2 * d.IM * d.KM * sizeof(float); }
+
 cudaError_t configure_kernels(const Dev &d) {
-    int smem = 2 * d.IM * d.KM * (int)sizeof(float);
-    return cudaFuncSetAttribute(k_sv_plane, cudaFuncAttributeMaxDynamicSharedMemorySize, smem > 48 * 1024 ? smem : 48 * 1024);
+    struct {
+        const void *f;
+        size_t bytes;
+    } k[] = {{(const void *)k_ts_cells, cells_smem(d)},
+             {(const void *)k_ts_prolong, prolong_smem(d)},
+             {(const void *)k_ts_update, update_smem(d)},
+             {(const void *)k_ts_smooth, smooth_smem(d)}};
+    for (auto &x : k) {
+        if (x.bytes > 200 * 1024) return cudaErrorInvalidValue;
+        int want = (int)(x.bytes > 48 * 1024 ? x.bytes : 48 * 1024);
+        cudaError_t e = cudaFuncSetAttribute(x.f, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 void launch_tstep(const Dev &d, Launch L, float *D, float *DIFF) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
     unsigned gN = grid_for(N, 256);
-    int nprep = (d.JM - 1) * d.KMM1 + d.NRWSM1 * d.KMM1;
-    k_ts_prep<<<grid_for(nprep, 128), 128, 0, L.s>>>(d);
-    k_ts_delta<<<gN, 256, 0, L.s>>>(d, DIFF);
-    if (d.NRWSM1 > 0) k_ts_mp<<<grid_for(d.NRWSM1 * d.KMM1, 64), 64, 0, L.s>>>(d, 0);
-    bool mg = !(d.IR <= 1 && d.JR <= 1 && d.KR <= 1);
-    if (mg) {
-        int nb = d.NIB1 * (d.NJB1 + 1) * d.NKB1 + d.NIB2 * (d.NJB2 + 1) * d.NKB2;
-        k_ts_restrict<<<grid_for(nb, 64), 64, 0, L.s>>>(d);
-        k_ts_plane_sum<<<d.JM - 1, PLANE_BS, 0, L.s>>>(d, 0, d.plane_sum);
+    const bool seq = d.REDUCE_ORDER == 1;
+    k_ts_cells<<<d.JM - 1, TS_BS, cells_smem(d), L.s>>>(d, DIFF);
+    mark(L, "k_ts_cells");
+    if (seq) {
+        int nb = d.NIB1 * (d.NJB1 + 1) * d.NKB1 + d.NIB2 * (d.NJB2 + 1) * d.NKB2 + d.NSBLK;
+        k_ts_restrict_seq<<<grid_for(nb, 64), 64, 0, L.s>>>(d);
+        mark(L, "k_ts_restrict_seq");
     }
-    k_ts_prolong<<<d.JM - 1, PLANE_BS, 0, L.s>>>(d, d.NRSMTH == 0 ? 1 : 0);
+    k_ts_prolong<<<d.JM - 1, TS_BS, prolong_smem(d), L.s>>>(d, (d.NRSMTH == 0 && !seq) ? 1 : 0);
+    mark(L, "k_ts_prolong");
     if (d.NRSMTH > 0) {
         for (int it = 0; it < d.NRSMTH; ++it) {
             k_resid_pass<<<gN, 256, 0, L.s>>>(d, 0, d.RSMTH, d.STORE, d.TMP);
+            mark(L, "k_resid_pass");
             k_resid_pass<<<gN, 256, 0, L.s>>>(d, 1, d.RSMTH, d.TMP, d.STORE);
+            mark(L, "k_resid_pass");
             k_resid_pass<<<gN, 256, 0, L.s>>>(d, 2, d.RSMTH, d.STORE, d.TMP);
+            mark(L, "k_resid_pass");
             k_copy<<<gN, 256, 0, L.s>>>(d.TMP, d.STORE, N);
+            mark(L, "k_copy");
         }
-        k_ts_plane_sum<<<d.JM - 1, PLANE_BS, 0, L.s>>>(d, 1, d.plane_abs);
+        if (!seq) {
+            k_ts_plane_abs<<<d.JM - 1, TS_BS, 0, L.s>>>(d);
+            mark(L, "k_ts_plane_abs");
+        }
     }
-    k_ts_avgblk<<<1, 32, 0, L.s>>>(d);
-    k_ts_damp<<<gN, 256, 0, L.s>>>(d);
-    if (d.NRWSM1 > 0) k_ts_mp<<<grid_for(d.NRWSM1 * d.KMM1, 64), 64, 0, L.s>>>(d, 1);
-    k_ts_scatter<<<gN, 256, 0, L.s>>>(d, D);
-    k_sv_stream<<<gN, 256, 0, L.s>>>(d, D);
-    size_t smem = (size_t)2 * d.IM * d.KM * sizeof(float);
-    k_sv_plane<<<d.JM, SV_BS, smem, L.s>>>(d, D);
+    if (seq) {
+        k_ts_avgblk_seq<<<1, 32, 0, L.s>>>(d);
+        mark(L, "k_ts_avgblk_seq");
+    }
+    k_ts_update<<<d.JM, TS_BS, update_smem(d), L.s>>>(d, D);
+    mark(L, "k_ts_update");
+    k_ts_smooth<<<d.JM, SV_BS, smooth_smem(d), L.s>>>(d, d.TMP, D);
+    mark(L, "k_ts_smooth");
 }
 
 }  // namespace mgpu

@@ -33,11 +33,16 @@ class Integrals(ctypes.Structure):
                 ("to_ratio", ctypes.c_double), ("j1", ctypes.c_int32), ("j2m1", ctypes.c_int32)]
 
 
+class KernelTime(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 48), ("launches", ctypes.c_int32), ("total_ms", ctypes.c_double)]
+
+
 # every entry point include/mgpu.h declares
 EXPORTS = ["mgpu_abi_version", "mgpu_last_error", "mgpu_device_count", "mgpu_create", "mgpu_destroy",
            "mgpu_set_int", "mgpu_set_real", "mgpu_set_array", "mgpu_get_array", "mgpu_get_real", "mgpu_get_int",
            "mgpu_commit", "mgpu_stepup", "mgpu_loss_init", "mgpu_step", "mgpu_run", "mgpu_sync",
-           "mgpu_integrals_compute", "mgpu_kernels_per_step"]
+           "mgpu_integrals_compute", "mgpu_kernels_per_step", "mgpu_bench_steps", "mgpu_profile_steps",
+           "mgpu_step_io_bytes"]
 
 _lib = None
 
@@ -72,6 +77,9 @@ def load(build: bool = True):
     L.mgpu_sync.argtypes = [vp]
     L.mgpu_integrals_compute.argtypes = [vp, ctypes.POINTER(Integrals)]
     L.mgpu_kernels_per_step.argtypes = [vp, i32]
+    L.mgpu_bench_steps.argtypes = [vp, i32, i32, ctypes.POINTER(ctypes.c_double)]
+    L.mgpu_profile_steps.argtypes = [vp, i32, ctypes.POINTER(KernelTime), i32, ctypes.POINTER(i32)]
+    L.mgpu_step_io_bytes.argtypes = [ctypes.POINTER(i32), ctypes.POINTER(i32)]
     for f in EXPORTS:
         fn = getattr(L, f)
         if f != "mgpu_destroy":
@@ -84,6 +92,13 @@ class MgpuError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"mgpu error {code}: {msg}")
         self.code = code
+
+
+def step_io_bytes() -> tuple[int, int]:
+    """(host->device, device->host) bytes of one mgpu_step call."""
+    a, b = ctypes.c_int32(), ctypes.c_int32()
+    _chk(load().mgpu_step_io_bytes(ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value
 
 
 def last_error() -> str:
@@ -177,3 +192,16 @@ class Problem:
 
     def kernels_per_step(self) -> int:
         return _chk(load().mgpu_kernels_per_step(self.h, 0))
+
+    def bench_steps(self, nsteps: int, flush_l2: bool = True) -> float:
+        """Sum of the device times (ms) of nsteps iterations."""
+        ms = ctypes.c_double()
+        _chk(load().mgpu_bench_steps(self.h, int(nsteps), 1 if flush_l2 else 0, ctypes.byref(ms)))
+        return ms.value
+
+    def profile_steps(self, nsteps: int) -> list:
+        """[(kernel name, launches, total ms)] over nsteps iterations."""
+        arr = (KernelTime * 256)()
+        n = ctypes.c_int32()
+        _chk(load().mgpu_profile_steps(self.h, int(nsteps), arr, 256, ctypes.byref(n)))
+        return [(arr[i].name.decode(), arr[i].launches, arr[i].total_ms) for i in range(n.value)]
