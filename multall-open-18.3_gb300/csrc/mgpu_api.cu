@@ -56,6 +56,7 @@ const int kNumArrays = sizeof(kArrays) / sizeof(kArrays[0]);
 struct mgpu_handle {
     Dev d;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;     // captures the bodies of conditional graph nodes
     int device = 0;
     int sm_count = 0;
     bool committed = false;
@@ -222,12 +223,8 @@ __global__ void k_delay(long long cycles) {
     }
 }
 
-int enqueue_step(mgpu_handle *h, Prof *prof = nullptr) {
-    const Dev &d = h->d;
-    Launch L{h->stream, h->sm_count, prof};
-    launch_step_begin(d, L);
-    launch_prim(d, L);
-    launch_loss(d, L, false);
+// the launch sequence of one LOOP iteration
+void enqueue_core(const Dev &d, Launch L) {
     launch_flux_mass(d, L);
     launch_tstep(d, L, d.RO, d.DRO);
     launch_flux_energy(d, L);
@@ -242,19 +239,88 @@ int enqueue_step(mgpu_handle *h, Prof *prof = nullptr) {
     launch_tstep(d, L, d.ROVR, d.DROVR);
     launch_limiters(d, L);
     launch_mixplan(d, L);
+}
+
+void enqueue_tail(const Dev &d, Launch L) {
     launch_tail(d, L);
     launch_stepup(d, L, 0.25f, true);
+}
+
+// kernel by kernel, every kernel present (LOSS and tail kernels return
+// early when their flag is off); used for profiling
+int enqueue_step(mgpu_handle *h, Prof *prof = nullptr) {
+    const Dev &d = h->d;
+    Launch L{h->stream, h->sm_count, prof};
+    launch_step_begin(d, L);
+    launch_prim(d, L);
+    launch_loss(d, L, false);
+    enqueue_core(d, L);
+    enqueue_tail(d, L);
     CK(cudaGetLastError());
     return 0;
 }
 
+// appends an IF conditional node to the graph being captured on h->stream
+// and captures its body (fn) on the side stream
+template <typename F>
+int add_conditional(mgpu_handle *h, cudaGraphConditionalHandle hnd, F fn) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    CK(cudaStreamGetCaptureInfo(h->stream, &st, nullptr, &cg, &deps, nullptr, &ndeps));
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = hnd;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, cg, deps, nullptr, ndeps, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    CK(cudaStreamBeginCaptureToGraph(h->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    fn(Launch{h->side, h->sm_count, nullptr});
+    cudaGraph_t out = nullptr;
+    CK(cudaStreamEndCapture(h->side, &out));
+    CK(cudaStreamUpdateCaptureDependencies(h->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    return 0;
+}
+
+// one LOOP iteration as a CUDA graph: the LOSS and tail kernels sit in
+// conditional bodies that the step-control kernel switches on only on the
+// steps that need them
 int build_graph(mgpu_handle *h) {
     if (h->gexec) return 0;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueue_step(h);
+    int rc = 0;
+    {
+        cudaStreamCaptureStatus st;
+        cudaGraph_t cg = nullptr;
+        cudaError_t e = cudaStreamGetCaptureInfo(h->stream, &st, nullptr, &cg, nullptr, nullptr, nullptr);
+        cudaGraphConditionalHandle hl = 0, ht = 0;
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hl, cg, 0, cudaGraphCondAssignDefault);
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&ht, cg, 0, cudaGraphCondAssignDefault);
+        if (e != cudaSuccess) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(h->stream, &g);
+            if (g) cudaGraphDestroy(g);
+            return fail(MGPU_E_CUDA, std::string("conditional handles: ") + cudaGetErrorString(e));
+        }
+        Dev dg = h->d;
+        dg.use_cond = 1;
+        dg.cond_loss = (unsigned long long)hl;
+        dg.cond_tail = (unsigned long long)ht;
+        Launch L{h->stream, h->sm_count, nullptr};
+        launch_step_begin(dg, L);
+        launch_prim(dg, L);
+        rc = add_conditional(h, hl, [&](Launch L2) { launch_loss(dg, L2, false); });
+        if (!rc) enqueue_core(dg, L);
+        if (!rc) rc = add_conditional(h, ht, [&](Launch L2) { enqueue_tail(dg, L2); });
+    }
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
-    if (rc) return rc;
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
     if (e != cudaSuccess) return fail(MGPU_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
     h->graph = g;
     CK(cudaGraphGetNodes(g, nullptr, &h->graph_nodes));
@@ -339,6 +405,8 @@ int32_t mgpu_create(int32_t im, int32_t jm, int32_t km, int32_t nrows, mgpu_hand
     cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(fail(MGPU_E_CUDA, cudaGetErrorString(e)));
+    e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(fail(MGPU_E_CUDA, cudaGetErrorString(e)));
     // arrays whose size is known now
     for (int a = 0; a < kNumArrays; ++a) {
         Shape s = kArrays[a].shape;
@@ -390,6 +458,7 @@ void mgpu_destroy(mgpu_handle *h) {
     for (void *p : h->allocs) cudaFree(p);
     if (h->h_ctl) cudaFreeHost(h->h_ctl);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->side) cudaStreamDestroy(h->side);
     delete h;
 }
 

@@ -54,6 +54,10 @@ __global__ void k_step_begin(Dev d) {
     c->do_tail = (n % 5 == 0) || ifend == 1;
     c->do_loss = (d.ILOS == 10) && (n % d.NLOS == 0);
     c->damp_on = !(c->DAMP < 2.0f || c->DAMP > 100.0f);
+    if (d.use_cond) {
+        cudaGraphSetConditional((cudaGraphConditionalHandle)d.cond_loss, c->do_loss ? 1u : 0u);
+        cudaGraphSetConditional((cudaGraphConditionalHandle)d.cond_tail, c->do_tail ? 1u : 0u);
+    }
     if (c->do_tail) {
         c->mon.vrms = 0.0;
         c->mon.vmax_key = 0ull;

@@ -95,6 +95,10 @@ struct Dev {
     int *KB1_S, *KB1_E, *KB2_S, *KB2_E;                 // (NKBn) K extent of each block
     int *SB_START, *SB_END;                             // (NSBLK)
     DevCtl *ctl;
+    // graph conditionals selecting the LOSS and 5-step tail bodies (set by
+    // the step-control kernel when the step runs from the CUDA graph)
+    int use_cond;
+    unsigned long long cond_loss, cond_tail;
 };
 
 __host__ __device__ inline size_t ix3(const Dev &d, int i, int j, int k) {

@@ -27,8 +27,8 @@ namespace mgpu {
 
 static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
 
-constexpr int TS_BS = 256;
-constexpr int SV_BS = 512;
+constexpr int TS_BS = 1024;
+constexpr int SV_BS = 1024;
 
 template <int BS>
 __device__ inline double block_sum(double v, double *sh) {
@@ -75,10 +75,18 @@ __global__ void __launch_bounds__(TS_BS) k_ts_cells(Dev d, float *__restrict__ D
     const bool lowx = d.FEXTRAP < 0.001f;
     const int jmx = role ? A1(d.JMIX, mnr) : 0;
     if ((role == 1 || role == 3) && !lowx) {
+        // stage the XFLUX plane in shared memory (coalesced), then add each
+        // I-line in the reference's order
         int jj = role == 1 ? j - 1 : j;
+        for (int c = threadIdx.x; c < nc; c += TS_BS) {
+            int i = c % IMM1 + 1, k = c / IMM1 + 1;
+            st[c] = A3(d.XFLUX, i, jj, k);
+        }
+        __syncthreads();
         for (int k = threadIdx.x + 1; k <= KMM1; k += TS_BS) {
+            const float *row = st + (size_t)(k - 1) * IMM1;
             float s = 0.0f;
-            for (int i = 1; i <= IMM1; ++i) s = s + A3(d.XFLUX, i, jj, k);
+            for (int i = 0; i < IMM1; ++i) s = s + row[i];
             lsum[k - 1] = s;
         }
     }
@@ -87,10 +95,14 @@ __global__ void __launch_bounds__(TS_BS) k_ts_cells(Dev d, float *__restrict__ D
     const int nr = A1(d.NROW, j);
     const int kts = A1(d.KTIPS, nr), kte = A1(d.KTIPE, nr);
     const float F1 = d.F1, F2 = d.F2, F3 = d.F3;
+    const float *__restrict__ XF = d.XFLUX;
+    const float *__restrict__ RF = d.RFLUX;
+    const float *__restrict__ TF = d.TFLUX;
+    const float *__restrict__ SR = d.SOURCE;
     for (int c = threadIdx.x; c < nc; c += TS_BS) {
         int i = c % IMM1 + 1, k = c / IMM1 + 1;
         size_t n = ix3(d, i, j, k);
-        float t0 = d.TFLUX[n], t1 = A3(d.TFLUX, i + 1, j, k);
+        float t0 = TF[n], t1 = TF[n + 1];
         if (kts > 0 && k >= kts && k <= kte - 1) {
             if (i == 1 || i + 1 == IM) {
                 float tb = 0.5f * (A3(d.TFLUX, 1, j, k) + A3(d.TFLUX, IM, j, k));
@@ -98,14 +110,14 @@ __global__ void __launch_bounds__(TS_BS) k_ts_cells(Dev d, float *__restrict__ D
                 if (i + 1 == IM) t1 = tb;
             }
         }
-        float src = d.SOURCE[n];
+        float src = SR[n];
         if (role && !lowx) {
             float FLOWDIRN = -A3(d.FLOWX, d.IMID, jmx, k);
             if (role == 1 && FLOWDIRN > 0.0f) src = src - (A3(d.XFLUX, i, j - 1, k) - lsum[k - 1] * A1(d.FP, i)) * d.FEXTRAP;
             if (role == 2) src = 0.0f;
             if (role == 3 && !(FLOWDIRN > 0.0f)) src = src + (d.XFLUX[n] - lsum[k - 1] * A1(d.FP, i)) * d.FEXTRAP;
         }
-        float DELTA = d.XFLUX[n] - A3(d.XFLUX, i, j - 1, k) * RATPITCH + d.RFLUX[n] - A3(d.RFLUX, i, j, k + 1) + t0 - t1 - src;
+        float DELTA = XF[n] - XF[n - IM] * RATPITCH + RF[n] - RF[n + (size_t)IM * d.JM] + t0 - t1 - src;
         float df = DIFF[n];
         st[c] = F1 * DELTA + F2 * df;
         DIFF[n] = DELTA + F3 * df;
