@@ -156,6 +156,41 @@ int32_t mgpu_sync(mgpu_handle *h);
  * on the device with FP64 accumulation. */
 int32_t mgpu_integrals_compute(mgpu_handle *h, mgpu_integrals *out);
 
+/* The same integrals as mgpu_integrals_compute, through a path that
+ * allocates nothing.  This entry point has no counterpart in the reference
+ * (whose efficiency summary is plain Fortran over COMMON arrays).
+ *
+ * Who needs it: a caller that must not allocate once the solver is
+ * marching -- a Fortran driver that sized the problem to fill the device
+ * from fixed COMMON extents, a monitoring thread that reports the
+ * efficiency during a long run, a host whose own allocator holds the rest
+ * of device memory.  mgpu_integrals_compute allocates host memory on every
+ * call and overwrites the handle's node-sized work arrays; this variant
+ * allocates no device or host memory (no cudaMalloc/cudaFree, no library
+ * routine that allocates; only recording an error message for
+ * mgpu_last_error may take host memory) and writes nothing of the handle's
+ * arrays.  Its scratch is
+ * one fixed array of (4 * MGPU_NOALLOC_MAX_JM + 8) doubles (131,136 bytes)
+ * in the library's static device memory, one copy per device and process.
+ *
+ * Limits and rules:
+ *  - JM (the handle's J extent) must be <= MGPU_NOALLOC_MAX_JM; larger
+ *    problems are rejected with MGPU_E_ARG before any device work.
+ *  - Nothing in the scratch has to start at zero: every slot a call reads
+ *    it has written earlier in the same call.
+ *  - The first call on each device looks up the scratch's device address
+ *    (with the handle's device current, which it must be: otherwise
+ *    MGPU_E_STATE); under CUDA's lazy module loading that lookup also loads
+ *    the library module holding the scratch.  Make that first call before
+ *    any stream capture begins;
+ *    a call with out == NULL performs only this set-up and returns 0.
+ *  - Calls whose executions overlap in time on the same device (two host
+ *    threads, or two handles on one device) share the one scratch array and
+ *    race: serialise them.  The call returns only after its results are on
+ *    the host. */
+#define MGPU_NOALLOC_MAX_JM 4096
+int32_t mgpu_integrals_noalloc(mgpu_handle *h, mgpu_integrals *out);
+
 /* ---- instrumentation --------------------------------------------------- */
 /* The reference prints "CPU TIME PER STEP" every 50 steps
  * (multall-open-18.3.f:5404-5414); these are the device-side equivalents. */

@@ -358,6 +358,14 @@ int read_ctl(mgpu_handle *h) {
 
 }  // namespace
 
+namespace mgpu {
+
+HandleView handle_view(const mgpu_handle *h) { return HandleView{&h->d, h->stream, h->device, h->committed}; }
+
+int api_fail(int code, const char *msg) { return fail(code, msg); }
+
+}  // namespace mgpu
+
 extern "C" {
 
 int32_t mgpu_abi_version(void) { return MGPU_ABI_VERSION; }

@@ -182,4 +182,15 @@ void launch_integrals(const Dev &d, Launch L, double *out8);
 // sets per-kernel attributes (dynamic shared memory of the J-plane kernel)
 cudaError_t configure_kernels(const Dev &d);
 
+// Read-only view of a handle, for entry points defined outside mgpu_api.cu.
+struct HandleView {
+    const Dev *d;
+    cudaStream_t stream;
+    int device;
+    bool committed;
+};
+HandleView handle_view(const mgpu_handle *h);
+// Records msg for mgpu_last_error() and returns code.
+int api_fail(int code, const char *msg);
+
 }  // namespace mgpu

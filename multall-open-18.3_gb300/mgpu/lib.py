@@ -42,7 +42,7 @@ EXPORTS = ["mgpu_abi_version", "mgpu_last_error", "mgpu_device_count", "mgpu_cre
            "mgpu_set_int", "mgpu_set_real", "mgpu_set_array", "mgpu_get_array", "mgpu_get_real", "mgpu_get_int",
            "mgpu_commit", "mgpu_stepup", "mgpu_loss_init", "mgpu_step", "mgpu_run", "mgpu_sync",
            "mgpu_integrals_compute", "mgpu_kernels_per_step", "mgpu_bench_steps", "mgpu_profile_steps",
-           "mgpu_step_io_bytes"]
+           "mgpu_step_io_bytes", "mgpu_integrals_noalloc"]
 
 _lib = None
 
@@ -76,6 +76,7 @@ def load(build: bool = True):
     L.mgpu_run.argtypes = [vp, i32, ctypes.POINTER(Monitors)]
     L.mgpu_sync.argtypes = [vp]
     L.mgpu_integrals_compute.argtypes = [vp, ctypes.POINTER(Integrals)]
+    L.mgpu_integrals_noalloc.argtypes = [vp, ctypes.POINTER(Integrals)]
     L.mgpu_kernels_per_step.argtypes = [vp, i32]
     L.mgpu_bench_steps.argtypes = [vp, i32, i32, ctypes.POINTER(ctypes.c_double)]
     L.mgpu_profile_steps.argtypes = [vp, i32, ctypes.POINTER(KernelTime), i32, ctypes.POINTER(i32)]
@@ -188,6 +189,13 @@ class Problem:
     def integrals(self) -> Integrals:
         o = Integrals()
         _chk(load().mgpu_integrals_compute(self.h, ctypes.byref(o)))
+        return o
+
+    def integrals_noalloc(self) -> Integrals:
+        """The same integrals through mgpu_integrals_noalloc (fixed static
+        device scratch, no allocation; calls on one device must not overlap)."""
+        o = Integrals()
+        _chk(load().mgpu_integrals_noalloc(self.h, ctypes.byref(o)))
         return o
 
     def kernels_per_step(self) -> int:
