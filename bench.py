@@ -36,16 +36,25 @@ sys.path.insert(0, os.path.join(ROOT, "multall-open-18.3_gb300"))
 METRIC = "Gnode-iter/s"
 WORKLOAD = ("single-stage axial turbine 65x242x49 (121 J per row), nozzle 48 vanes + rotor 60 blades "
             "9000 rpm, 1% tip gap, mixing plane, 3-level multigrid, SCREE, mixing-length LOSS/5 steps")
-# SURVEY-defined compulsory traffic of one LOOP iteration per node (FP32):
-# 5 state arrays r+w, 5 SCREE histories r+w, 9 geometry arrays r, 4 forces r
+# Compulsory traffic of one LOOP iteration per node (FP32), every array read
+# once and written once: 5 state arrays r+w (40 B), 5 SCREE histories r+w
+# (40 B), 9 geometry arrays r (36 B), 4 body forces r (16 B).
 B_ALG_STEP = 132
-# compulsory bytes per node of each kernel (arrays read once + written once)
-ALG_BYTES_PER_NODE = {
-    "k_prim": 48, "k_flux_mass": 76, "k_flux_energy": 40, "k_flux_xmom": 52, "k_flux_rvt": 40,
-    "k_flux_rmom": 64, "k_ts_delta": 28, "k_ts_prolong": 16, "k_ts_damp": 8, "k_ts_scatter": 12,
-    "k_sv_stream": 8, "k_sv_plane": 8, "k_ts_plane_sum": 4, "k_ts_restrict": 4, "k_peff": 8,
-    "k_mach_limiter": 16, "k_density_limiter": 4,
+# Per kernel: (compulsory bytes per node for one unit of its work, units per
+# step).  A TSTEP kernel's unit is one variable (5 per step, batched 2 + 3 per
+# launch); LOSS runs every NLOS = 5 steps.
+#   cells   XFLUX, TFLUX, RFLUX, SOURCE, DIFF read; DIFF, STORE written
+#   prolong STORE, STEP, RSTEP read; STORE written
+#   update  STORE, D read; TMP written
+#   smooth  TMP read; D written
+KERNEL_BYTES = {
+    "k_prim": (48, 1), "k_flux_mass": (60, 1), "k_flux_energy": (40, 1), "k_flux_xmom": (52, 1),
+    "k_flux_rvt": (40, 1), "k_flux_rmom": (64, 1), "k_peff": (8, 1), "k_density_detect": (4, 1),
+    "k_mach_limiter": (24, 1),
+    "k_ts_cells": (28, 5), "k_ts_prolong": (16, 5), "k_ts_update": (12, 5), "k_ts_smooth": (8, 5),
+    "k_loss_kfaces": (72, 0.2), "k_loss_ifaces": (84, 0.2),
 }
+PROFILE_STEPS = 10
 
 
 def env_int(name, default):
@@ -210,6 +219,7 @@ def run_gpu(args, rank, world, local_rank):
     N = cd.nodes()
     prob = lib.Problem(cd)
     kps = prob.kernels_per_step()
+    kps_loss, kps_tail = prob.kernels_per_step(loss=True) - kps, prob.kernels_per_step(tail=True) - kps
     prob.run(max(args.warmup, 3))
     dist_barrier(dist)
     with ClockSampler(0) as clk:
@@ -221,14 +231,17 @@ def run_gpu(args, rank, world, local_rank):
     value = N * args.steps * world / (ms_max / 1e3) / 1e9
     ms_per_step = ms_max / args.steps
 
-    # per-kernel device times (events around each launch, no graph)
-    prof = prob.profile_steps(10)
-    step_kernels = [p for p in prof if p[0] in ALG_BYTES_PER_NODE]
-    dom = max(step_kernels, key=lambda p: p[2])
-    dom_name, dom_launches, dom_ms = dom
-    avg_s = dom_ms / dom_launches / 1e3
-    alg_bytes = ALG_BYTES_PER_NODE[dom_name] * N
-    achieved = alg_bytes / avg_s / 1e9
+    # per-kernel device times (events around each launch, no graph); LOSS
+    # and tail kernels are launched every step here and return at once on
+    # the steps that do not need them
+    prof = prob.profile_steps(PROFILE_STEPS)
+    step_kernels = [p for p in prof if p[0] in KERNEL_BYTES]
+    dom_name, dom_launches, dom_ms = max(step_kernels, key=lambda p: p[2])
+    bpn, units = KERNEL_BYTES[dom_name]
+    step_s = dom_ms / PROFILE_STEPS / 1e3                    # this kernel's device time per step
+    alg_step = bpn * N * units                               # its compulsory bytes per step
+    launches_step = dom_launches / PROFILE_STEPS
+    achieved = alg_step / step_s / 1e9
     peak, peak_kind = load_peaks()
     traffic = ncu_traffic_per_launch().get(dom_name)
     total_prof = sum(p[2] for p in prof)
@@ -271,15 +284,19 @@ def run_gpu(args, rank, world, local_rank):
                        "reductions": "FP64 tree sums (REDUCE_ORDER=0)"},
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                         "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_s * 1e3,
+                         "alg_bytes_per_launch": alg_step / launches_step,
+                         "avg_launch_ms": step_s * 1e3 / launches_step,
+                         "alg_bytes_per_node_unit": bpn, "units_per_step": units,
                          "share_of_step": dom_ms / total_prof,
                          "step": {"alg_bytes_per_node_iter": B_ALG_STEP,
                                   "achieved": value / world * B_ALG_STEP, "frac": value / world * B_ALG_STEP / peak}},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "e2e": e2e,
-            "gpu_launches": kps * args.steps,
-            "kernels_per_step": kps,
+            # NSTEP runs on from the warm-up; over a whole number of 5-step
+            # cycles every 5th step runs LOSS (NLOS = 5) and the tail
+            "gpu_launches": kps * args.steps + (kps_loss + kps_tail) * (args.steps // 5),
+            "kernels_per_step": {"plain": kps, "loss_extra": kps_loss, "tail_extra": kps_tail},
             "wall_s_timed_region": t_wall1 - t_wall0,
         }
         print(json.dumps(line), flush=True)

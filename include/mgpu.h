@@ -195,8 +195,10 @@ int32_t mgpu_integrals_noalloc(mgpu_handle *h, mgpu_integrals *out);
 /* The reference prints "CPU TIME PER STEP" every 50 steps
  * (multall-open-18.3.f:5404-5414); these are the device-side equivalents. */
 
-/* Number of kernel launches one LOOP iteration issues (graph nodes). */
-int32_t mgpu_kernels_per_step(mgpu_handle *h, int32_t tail_step);
+/* Number of kernel launches one LOOP iteration issues from the step graph:
+ * which = 0 a plain step, 1 a LOSS step, 2 a tail step (every 5th), 3 a step
+ * that is both. */
+int32_t mgpu_kernels_per_step(mgpu_handle *h, int32_t which);
 /* Runs nsteps iterations, each bracketed by CUDA events on the handle's
  * stream; with flush_l2=1 a buffer larger than L2 is rewritten between the
  * iterations (outside the events).  *total_ms = sum of the iteration

@@ -67,6 +67,7 @@ struct mgpu_handle {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     size_t graph_nodes = 0;
+    size_t loss_nodes = 0, tail_nodes = 0;   // kernels in the conditional bodies
     double *d_int = nullptr;     // integrals output (4 x JM)
     void *flush_buf = nullptr;   // > L2, rewritten between timed iterations
     size_t flush_bytes = 0;
@@ -224,19 +225,22 @@ __global__ void k_delay(long long cycles) {
 }
 
 // the launch sequence of one LOOP iteration
+// The reference updates RO, ROE, ROVX, RORVT, ROVR one after the other,
+// each TSTEP reading only its own fluxes and the start-of-step primitives;
+// the only coupling is the inlet/exit condition, which reads the new RO and
+// ROE and resets the momenta at J=1 before their update.  So the step runs
+// two batched TSTEPs, [RO, ROE] and [ROVX, RORVT, ROVR], with the boundary
+// conditions between them; every value is the same as in the serial order.
 void enqueue_core(const Dev &d, Launch L) {
     launch_flux_mass(d, L);
-    launch_tstep(d, L, d.RO, d.DRO);
     launch_flux_energy(d, L);
-    launch_tstep(d, L, d.ROE, d.DROE);
+    launch_tstep(d, L, V_RO, 2);
     launch_bc(d, L);
     launch_peff(d, L);
     launch_flux_xmom(d, L);
-    launch_tstep(d, L, d.ROVX, d.DROVX);
     launch_flux_rvt(d, L);
-    launch_tstep(d, L, d.RORVT, d.DRORVT);
     launch_flux_rmom(d, L);
-    launch_tstep(d, L, d.ROVR, d.DROVR);
+    launch_tstep(d, L, V_ROVX, 3);
     launch_limiters(d, L);
     launch_mixplan(d, L);
 }
@@ -261,9 +265,9 @@ int enqueue_step(mgpu_handle *h, Prof *prof = nullptr) {
 }
 
 // appends an IF conditional node to the graph being captured on h->stream
-// and captures its body (fn) on the side stream
+// and captures its body (fn) on the side stream; *nbody = the body's nodes
 template <typename F>
-int add_conditional(mgpu_handle *h, cudaGraphConditionalHandle hnd, F fn) {
+int add_conditional(mgpu_handle *h, cudaGraphConditionalHandle hnd, size_t *nbody, F fn) {
     cudaStreamCaptureStatus st;
     cudaGraph_t cg = nullptr;
     const cudaGraphNode_t *deps = nullptr;
@@ -280,6 +284,7 @@ int add_conditional(mgpu_handle *h, cudaGraphConditionalHandle hnd, F fn) {
     fn(Launch{h->side, h->sm_count, nullptr});
     cudaGraph_t out = nullptr;
     CK(cudaStreamEndCapture(h->side, &out));
+    CK(cudaGraphGetNodes(body, nullptr, nbody));
     CK(cudaStreamUpdateCaptureDependencies(h->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
     return 0;
 }
@@ -311,9 +316,9 @@ int build_graph(mgpu_handle *h) {
         Launch L{h->stream, h->sm_count, nullptr};
         launch_step_begin(dg, L);
         launch_prim(dg, L);
-        rc = add_conditional(h, hl, [&](Launch L2) { launch_loss(dg, L2, false); });
+        rc = add_conditional(h, hl, &h->loss_nodes, [&](Launch L2) { launch_loss(dg, L2, false); });
         if (!rc) enqueue_core(dg, L);
-        if (!rc) rc = add_conditional(h, ht, [&](Launch L2) { enqueue_tail(dg, L2); });
+        if (!rc) rc = add_conditional(h, ht, &h->tail_nodes, [&](Launch L2) { enqueue_tail(dg, L2); });
     }
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
@@ -428,9 +433,32 @@ int32_t mgpu_create(int32_t im, int32_t jm, int32_t km, int32_t nrows, mgpu_hand
         h->dbytes[a] = cnt * 4;
     }
     size_t N = (size_t)im * jm * km;
-    float **work[] = {&d.XFLUX, &d.TFLUX, &d.RFLUX, &d.SOURCE, &d.FLOWX, &d.FLOWT, &d.FLOWR, &d.STORE, &d.TMP, &d.TEMP1};
+    float **work[] = {&d.FLOWX, &d.FLOWT, &d.FLOWR, &d.ZERO, &d.TEMP1};
     for (float **w : work)
         if ((rc = dalloc(h, w, N))) return bail(rc);
+    // per-variable TSTEP operands; RO's face fluxes are the mass fluxes
+    float *vd[NVAR] = {d.RO, d.ROE, d.ROVX, d.RORVT, d.ROVR};
+    float *vdiff[NVAR] = {d.DRO, d.DROE, d.DROVX, d.DRORVT, d.DROVR};
+    for (int v = 0; v < NVAR; ++v) {
+        VarSet &V = d.var[v];
+        V.D = vd[v];
+        V.DIFF = vdiff[v];
+        if (v == V_RO) {
+            V.XF = d.FLOWX;
+            V.TF = d.FLOWT;
+            V.RF = d.FLOWR;
+            V.SR = d.ZERO;
+        } else {
+            float **fl[] = {&V.XF, &V.TF, &V.RF, &V.SR};
+            for (float **w : fl)
+                if ((rc = dalloc(h, w, N))) return bail(rc);
+        }
+        if ((rc = dalloc(h, &V.ST, N)) || (rc = dalloc(h, &V.TM, N)) || (rc = dalloc(h, &V.psum, jm)) ||
+            (rc = dalloc(h, &V.pabs, jm)) || (rc = dalloc(h, &V.AVG_BLK, nrows)))
+            return bail(rc);
+    }
+    d.STORE = d.var[V_RO].ST;
+    d.TMP = d.var[V_RO].TM;
     if ((rc = dalloc(h, &d.PLIM, km))) return bail(rc);
     float **rowt[] = {&d.FILAM, &d.FITURB, &d.FIWAKE, &d.FIUP};
     for (float **w : rowt)
@@ -439,9 +467,6 @@ int32_t mgpu_create(int32_t im, int32_t jm, int32_t km, int32_t nrows, mgpu_hand
     if ((rc = dalloc(h, &d.FKTURB, (size_t)nrows * km))) return bail(rc);
     if ((rc = dalloc(h, &d.VLIMIT, nrows))) return bail(rc);
     if ((rc = dalloc(h, &d.ROLIMIT, nrows))) return bail(rc);
-    if ((rc = dalloc(h, &d.AVG_BLK, nrows))) return bail(rc);
-    if ((rc = dalloc(h, &d.plane_sum, jm))) return bail(rc);
-    if ((rc = dalloc(h, &d.plane_abs, jm))) return bail(rc);
     if ((rc = dalloc(h, &d.BLADE_FLOW, jm))) return bail(rc);
     if ((rc = dalloc(h, &d.DFLAG, (size_t)im * km))) return bail(rc);
     if ((rc = dalloc(h, &d.BCBUF, (size_t)3 * km))) return bail(rc);
@@ -692,10 +717,13 @@ int32_t mgpu_commit(mgpu_handle *h) {
             JSBLK[j - 1] < 1 || JSBLK[j - 1] > d.NSBLK)
             return fail(MGPU_E_ARG, "multigrid J map out of range");
     }
-    if ((rc = dalloc(h, &d.B1CHG, shape_count(h, SH_MG1))) || (rc = dalloc(h, &d.B2CHG, shape_count(h, SH_MG2))) ||
-        (rc = dalloc(h, &d.SBSUM, d.NSBLK)) || (rc = dalloc(h, &d.P1, (size_t)d.JM * d.NIB1 * d.NKB1)) ||
-        (rc = dalloc(h, &d.P2, (size_t)d.JM * d.NIB2 * d.NKB2)))
-        return rc;
+    for (int v = 0; v < NVAR; ++v) {
+        VarSet &V = d.var[v];
+        if ((rc = dalloc(h, &V.B1CHG, shape_count(h, SH_MG1))) || (rc = dalloc(h, &V.B2CHG, shape_count(h, SH_MG2))) ||
+            (rc = dalloc(h, &V.SBSUM, d.NSBLK)) || (rc = dalloc(h, &V.P1, (size_t)d.JM * d.NIB1 * d.NKB1)) ||
+            (rc = dalloc(h, &V.P2, (size_t)d.JM * d.NIB2 * d.NKB2)))
+            return rc;
+    }
     if (d.REDUCE_ORDER != 0 && d.REDUCE_ORDER != 1) return fail(MGPU_E_ARG, "REDUCE_ORDER must be 0 or 1");
     // the control block
     DevCtl c;
@@ -897,12 +925,15 @@ int32_t mgpu_profile_steps(mgpu_handle *h, int32_t nsteps, mgpu_kernel_time *out
     return 0;
 }
 
-int32_t mgpu_kernels_per_step(mgpu_handle *h, int32_t tail_step) {
-    (void)tail_step;
+int32_t mgpu_kernels_per_step(mgpu_handle *h, int32_t which) {
     if (!h || !h->committed) return fail(MGPU_E_STATE, "kernels_per_step before commit");
+    if (which < 0 || which > 3) return fail(MGPU_E_ARG, "kernels_per_step: which must be 0..3");
     int rc = build_graph(h);
     if (rc) return rc;
-    return (int32_t)h->graph_nodes;
+    size_t n = h->graph_nodes - 2;   // every top-level node but the two conditionals is a kernel
+    if (which & 1) n += h->loss_nodes;
+    if (which & 2) n += h->tail_nodes;
+    return (int32_t)n;
 }
 
 }  // extern "C"

@@ -179,8 +179,6 @@ __global__ void k_flux_mass(Dev d) {
         float AVGRVR = A3(d.ROVR, i, j, k) + A3(d.ROVR, i, j, k + 1) + A3(d.ROVR, i + 1, j, k) + A3(d.ROVR, i + 1, j, k + 1);
         float fx = 0.25f * (AVGRVX * A3(d.AQX, i, j, k) + AVGRVR * A3(d.AQR, i, j, k));
         d.FLOWX[n] = fx;
-        d.SOURCE[n] = 0.0f;
-        d.XFLUX[n] = fx;
     }
     {
         float rowt = d.ROVT[n] - A2(d.UBLADE, j, k) * d.RO[n];
@@ -200,7 +198,6 @@ __global__ void k_flux_mass(Dev d) {
             }
         }
         d.FLOWT[n] = ft;
-        d.TFLUX[n] = ft;
     }
     if (i < d.IM && j >= 2) {
         float fr = 0.0f;
@@ -210,7 +207,6 @@ __global__ void k_flux_mass(Dev d) {
             fr = 0.25f * (AVGRVX * A3(d.ASX, i, j, k) + AVGRVR * A3(d.ASR, i, j, k));
         }
         d.FLOWR[n] = fr;
-        d.RFLUX[n] = fr;
     }
 }
 
@@ -235,14 +231,15 @@ __global__ void k_flux_energy(Dev d) {
     if (n >= N) return;
     int i, j, k;
     node_ijk(d, n, i, j, k);
+    const VarSet &V = d.var[V_ROE];
     if (i < d.IM && k < d.KM) {
         float AVGHO = A3(d.HO, i, j, k) + A3(d.HO, i, j, k + 1) + A3(d.HO, i + 1, j, k) + A3(d.HO, i + 1, j, k + 1);
-        d.XFLUX[n] = d.FLOWX[n] * AVGHO * 0.25f;
-        if (j >= 2) d.SOURCE[n] = d.QSOURCE[n];
+        V.XF[n] = d.FLOWX[n] * AVGHO * 0.25f;
+        if (j >= 2) V.SR[n] = d.QSOURCE[n];
     }
     if (i < d.IM && j >= 2) {
         float AVGHO = 0.25f * (A3(d.HO, i, j, k) + A3(d.HO, i, j - 1, k) + A3(d.HO, i + 1, j - 1, k) + A3(d.HO, i + 1, j, k));
-        d.RFLUX[n] = d.FLOWR[n] * AVGHO;
+        V.RF[n] = d.FLOWR[n] * AVGHO;
     }
     if (j >= 2 && k < d.KM) {
         float tf = tflux_energy_raw(d, i, j, k);
@@ -251,7 +248,7 @@ __global__ void k_flux_energy(Dev d) {
             float tm = (i == d.IM) ? tf : tflux_energy_raw(d, d.IM, j, k);
             tf = 0.5f * (t1 + tm);
         }
-        d.TFLUX[n] = tf;
+        V.TF[n] = tf;
     }
 }
 
@@ -432,17 +429,18 @@ __global__ void k_flux_xmom(Dev d) {
     if (n >= N) return;
     int i, j, k;
     node_ijk(d, n, i, j, k);
+    const VarSet &V = d.var[V_ROVX];
     const float *PE = d.PEFF, *VX = d.VX;
     if (i < d.IM && k < d.KM) {
-        d.SOURCE[n] = d.XFORCE[n];
+        V.SR[n] = d.XFORCE[n];
         float AVGP = A3(PE, i, j, k) + A3(PE, i, j, k + 1) + A3(PE, i + 1, j, k + 1) + A3(PE, i + 1, j, k);
         float AVGVX = A3(VX, i, j, k) + A3(VX, i, j, k + 1) + A3(VX, i + 1, j, k + 1) + A3(VX, i + 1, j, k);
-        d.XFLUX[n] = 0.25f * (AVGP * A3(d.AQX, i, j, k) + d.FLOWX[n] * AVGVX);
+        V.XF[n] = 0.25f * (AVGP * A3(d.AQX, i, j, k) + d.FLOWX[n] * AVGVX);
     }
     if (i < d.IM && j >= 2) {
         float AVGP = A3(PE, i, j, k) + A3(PE, i, j - 1, k) + A3(PE, i + 1, j - 1, k) + A3(PE, i + 1, j, k);
         float AVGVX = A3(VX, i, j, k) + A3(VX, i, j - 1, k) + A3(VX, i + 1, j - 1, k) + A3(VX, i + 1, j, k);
-        d.RFLUX[n] = 0.25f * (AVGP * A3(d.ASX, i, j, k) + d.FLOWR[n] * AVGVX);
+        V.RF[n] = 0.25f * (AVGP * A3(d.ASX, i, j, k) + d.FLOWR[n] * AVGVX);
     }
     if (j >= 2 && k < d.KM) {
         if ((i == 1 || i == d.IM) && A1(d.IND, j) != 1) {
@@ -451,11 +449,11 @@ __global__ void k_flux_xmom(Dev d) {
                              A3(PE, IM, j, k) + A3(PE, IM, j - 1, k) + A3(PE, IM, j, k + 1) + A3(PE, IM, j - 1, k + 1);
             float AVGVXCUSP = A3(VX, 1, j, k) + A3(VX, 1, j - 1, k) + A3(VX, 1, j, k + 1) + A3(VX, 1, j - 1, k + 1) +
                               A3(VX, IM, j, k) + A3(VX, IM, j - 1, k) + A3(VX, IM, j, k + 1) + A3(VX, IM, j - 1, k + 1);
-            d.TFLUX[n] = 0.125f * (d.FLOWT[n] * AVGVXCUSP + AVGPCUSP * d.ABX[n]);
+            V.TF[n] = 0.125f * (d.FLOWT[n] * AVGVXCUSP + AVGPCUSP * d.ABX[n]);
         } else {
             float AVGVX = A3(VX, i, j, k) + A3(VX, i, j - 1, k) + A3(VX, i, j - 1, k + 1) + A3(VX, i, j, k + 1);
             float AVGP = A3(PE, i, j, k) + A3(PE, i, j - 1, k) + A3(PE, i, j - 1, k + 1) + A3(PE, i, j, k + 1);
-            d.TFLUX[n] = 0.25f * (d.FLOWT[n] * AVGVX + d.ABX[n] * AVGP);
+            V.TF[n] = 0.25f * (d.FLOWT[n] * AVGVX + d.ABX[n] * AVGP);
         }
     }
 }
@@ -482,12 +480,13 @@ __global__ void k_flux_rvt(Dev d) {
     if (n >= N) return;
     int i, j, k;
     node_ijk(d, n, i, j, k);
+    const VarSet &V = d.var[V_RORVT];
     const float *VT = d.VT;
     if (i < d.IM && k < d.KM) {
         float AVGR = 0.125f * (A2(d.R, j, k) + A2(d.R, j, k + 1));
         float AVGVT = A3(VT, i, j, k) + A3(VT, i, j, k + 1) + A3(VT, i + 1, j, k) + A3(VT, i + 1, j, k + 1);
-        d.SOURCE[n] = d.TFORCE[n];
-        d.XFLUX[n] = d.FLOWX[n] * AVGR * AVGVT;
+        V.SR[n] = d.TFORCE[n];
+        V.XF[n] = d.FLOWX[n] * AVGR * AVGVT;
     }
     if (j >= 2 && k < d.KM) {
         float AVGR = 0.25f * A2(d.RAVG_CELL, j, k);
@@ -497,12 +496,12 @@ __global__ void k_flux_rvt(Dev d) {
             float tm = (i == d.IM) ? tf : tflux_rvt_raw(d, d.IM, j, k, AVGR);
             tf = 0.5f * (t1 + tm);
         }
-        d.TFLUX[n] = tf;
+        V.TF[n] = tf;
     }
     if (i < d.IM && j >= 2) {
         float AVGR = (A2(d.R, j, k) + A2(d.R, j - 1, k)) * 0.125f;
         float AVGVT = A3(VT, i, j, k) + A3(VT, i, j - 1, k) + A3(VT, i + 1, j - 1, k) + A3(VT, i + 1, j, k);
-        d.RFLUX[n] = d.FLOWR[n] * AVGVT * AVGR;
+        V.RF[n] = d.FLOWR[n] * AVGVT * AVGR;
     }
 }
 
@@ -529,11 +528,12 @@ __global__ void k_flux_rmom(Dev d) {
     if (n >= N) return;
     int i, j, k;
     node_ijk(d, n, i, j, k);
+    const VarSet &V = d.var[V_ROVR];
     const float *PE = d.PEFF, *VR = d.VR, *VT = d.VT, *RV = d.ROVT;
     if (i < d.IM && k < d.KM) {
         float AVGVR = A3(VR, i, j, k) + A3(VR, i, j, k + 1) + A3(VR, i + 1, j, k) + A3(VR, i + 1, j, k + 1);
         float AVGP = A3(PE, i, j, k) + A3(PE, i, j, k + 1) + A3(PE, i + 1, j, k + 1) + A3(PE, i + 1, j, k);
-        d.XFLUX[n] = 0.25f * (d.FLOWX[n] * AVGVR + A3(d.AQR, i, j, k) * AVGP);
+        V.XF[n] = 0.25f * (d.FLOWX[n] * AVGVR + A3(d.AQR, i, j, k) * AVGP);
     }
     if (j >= 2 && k < d.KM) {
         float ap;
@@ -549,12 +549,12 @@ __global__ void k_flux_rmom(Dev d) {
             float T2 = tmraw - AVGPM * A3(d.ABR, IM, j, k);
             tf = 0.5f * ((T1 + T2) + (AVGP1 + AVGPM) * A3(d.ABR, i, j, k));
         }
-        d.TFLUX[n] = tf;
+        V.TF[n] = tf;
     }
     if (i < d.IM && j >= 2) {
         float AVGVR = A3(VR, i, j, k) + A3(VR, i, j - 1, k) + A3(VR, i + 1, j - 1, k) + A3(VR, i + 1, j, k);
         float AVGP = A3(PE, i, j, k) + A3(PE, i, j - 1, k) + A3(PE, i + 1, j - 1, k) + A3(PE, i + 1, j, k);
-        d.RFLUX[n] = 0.25f * (d.FLOWR[n] * AVGVR + A3(d.ASR, i, j, k) * AVGP);
+        V.RF[n] = 0.25f * (d.FLOWR[n] * AVGVR + A3(d.ASR, i, j, k) * AVGP);
         if (k < d.KM) {
             float AVGRVT = A3(RV, i, j, k) + A3(RV, i, j, k + 1) + A3(RV, i, j - 1, k) + A3(RV, i, j - 1, k + 1) +
                            A3(RV, i + 1, j, k) + A3(RV, i + 1, j, k + 1) + A3(RV, i + 1, j - 1, k) + A3(RV, i + 1, j - 1, k + 1);
@@ -563,7 +563,7 @@ __global__ void k_flux_rmom(Dev d) {
                                     A3(VT, i + 1, j, k + 1));
             float AVGP8 = A3(PE, i, j, k) + A3(PE, i, j - 1, k) + A3(PE, i, j - 1, k + 1) + A3(PE, i, j, k + 1) +
                           A3(PE, i + 1, j, k) + A3(PE, i + 1, j - 1, k) + A3(PE, i + 1, j - 1, k + 1) + A3(PE, i + 1, j, k + 1);
-            d.SOURCE[n] = d.RFORCE[n] - (AVGRVT * AVGVT + AVGP8) * d.VOLOR[n];
+            V.SR[n] = d.RFORCE[n] - (AVGRVT * AVGVT + AVGP8) * d.VOLOR[n];
         }
     }
 }

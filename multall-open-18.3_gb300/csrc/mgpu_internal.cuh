@@ -4,7 +4,7 @@
 // Fortran order (I fastest, then J, then K), so one node (I,J,K) is
 // element (I-1) + IM*((J-1) + JM*(K-1)) and a warp reads 32 consecutive
 // pitchwise points.  Kernels take the whole description by value (`Dev`,
-// ~1.5 KB of kernel parameters: pointers, dimensions and the constant
+// ~2.2 KB of kernel parameters: pointers, dimensions and the constant
 // REAL scalars); the values that change from step to step (smoothing ramp,
 // NSTEP, the 5-step flags, the monitors) live in a small device struct
 // `DevCtl` that the first kernel of each step updates, so a step is a fixed
@@ -54,6 +54,25 @@ struct DevCtl {
     DevMon mon;
 };
 
+// One conserved variable's TSTEP operands and work arrays.  The five
+// variables (RO, ROE, ROVX, RORVT, ROVR) each have their own face fluxes and
+// cell-change arrays, so the TSTEP kernels can update several variables in
+// one launch (blockIdx.y selects the variable): RO and ROE together, then
+// the three momenta after the inlet/exit conditions.
+struct VarSet {
+    float *D, *DIFF;             // the variable and its SCREE history (COMMON)
+    float *XF, *TF, *RF, *SR;    // XFLUX, TFLUX, RFLUX, SOURCE of this variable
+    float *ST;                   // STORE: cell changes
+    float *TM;                   // TMP: node values before SMOOTH_VAR
+    double *psum, *pabs;         // (JM) per-J-plane sums of STORE and |STORE|
+    float *P1, *P2;              // (JM, NIB1*NKB1) / (JM, NIB2*NKB2) per-plane block partials
+    float *B1CHG, *B2CHG;        // MG1 / MG2 block sums, reference order
+    float *SBSUM;                // (NSBLK) superblock sums, reference order
+    float *AVG_BLK;              // (NROWS) row means of |STORE|, reference order
+};
+constexpr int NVAR = 5;
+enum { V_RO = 0, V_ROE = 1, V_ROVX = 2, V_RORVT = 3, V_ROVR = 4 };
+
 struct Dev {
     // dimensions
     int IM, JM, KM, NROWS;
@@ -69,18 +88,16 @@ struct Dev {
     // COMMON arrays on the device
 #define MGPU_DEV_A(n, t, s, r) MGPU_T_##t *n;
     MGPU_ARRAYS(MGPU_DEV_A)
-    // loop work arrays (COMMON scratch of the reference)
-    float *XFLUX, *TFLUX, *RFLUX, *SOURCE, *FLOWX, *FLOWT, *FLOWR;
+    // loop work arrays (COMMON scratch of the reference).  STORE and TMP
+    // alias var[V_RO].ST / .TM (scratch of the tail, STEPUP and integrals);
+    // RO's face fluxes are the mass fluxes FLOWX/FLOWT/FLOWR and its SOURCE
+    // is the all-zero ZERO array.
+    float *FLOWX, *FLOWT, *FLOWR, *ZERO;
     float *STORE, *TMP, *TEMP1;
+    VarSet var[NVAR];
     float *PLIM;                       // (KM)
     float *FILAM, *FITURB, *FIWAKE, *FIUP, *FKLAM, *FKTURB;   // (NROWS, IM|KM)
     float *VLIMIT, *ROLIMIT;           // (NROWS)
-    float *B1CHG, *B2CHG;              // MG1 / MG2 shaped
-    double *plane_sum;                 // (JM) per-J-plane sums of STORE
-    double *plane_abs;                 // (JM) per-J-plane sums of |STORE|
-    float *AVG_BLK;                    // (NROWS)
-    float *SBSUM;                      // (NSBLK) superblock sums, reference order
-    float *P1, *P2;                    // (JM, NIB1*NKB1) / (JM, NIB2*NKB2) per-plane block partials
     int *DFLAG;                        // (IM*KM) density-limiter column flags
     float *BCBUF;                      // (3, KM) PAVG2, PAVG3, PAVGOUT of the exit/inlet BCs
     double *BLADE_FLOW;                // (JM)
@@ -172,7 +189,8 @@ void launch_peff(const Dev &d, Launch L);
 void launch_flux_xmom(const Dev &d, Launch L);
 void launch_flux_rvt(const Dev &d, Launch L);
 void launch_flux_rmom(const Dev &d, Launch L);
-void launch_tstep(const Dev &d, Launch L, float *D, float *DIFF);
+// TSTEP for the nv variables v0 .. v0+nv-1 of d.var
+void launch_tstep(const Dev &d, Launch L, int v0, int nv);
 void launch_limiters(const Dev &d, Launch L);
 void launch_mixplan(const Dev &d, Launch L);
 void launch_tail(const Dev &d, Launch L);

@@ -62,8 +62,10 @@ __device__ inline int mp_role(const Dev &d, int j, int *nr) {
 // cells: 5503-5510 (tip gap), 5516-5555 (MP extrapolation), 1000 (flux
 // sum), 1750 (MP redistribution) and the multigrid partial sums
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(TS_BS) k_ts_cells(Dev d, float *__restrict__ DIFF) {
+__global__ void __launch_bounds__(TS_BS) k_ts_cells(const __grid_constant__ Dev d, int v0) {
     extern __shared__ float sm[];
+    const VarSet &V = d.var[v0 + blockIdx.y];
+    float *__restrict__ DIFF = V.DIFF;
     __shared__ double shd[TS_BS / 32];
     const int j = blockIdx.x + 2;
     const int IM = d.IM, IMM1 = d.IMM1, KMM1 = d.KMM1;
@@ -80,7 +82,7 @@ __global__ void __launch_bounds__(TS_BS) k_ts_cells(Dev d, float *__restrict__ D
         int jj = role == 1 ? j - 1 : j;
         for (int c = threadIdx.x; c < nc; c += TS_BS) {
             int i = c % IMM1 + 1, k = c / IMM1 + 1;
-            st[c] = A3(d.XFLUX, i, jj, k);
+            st[c] = A3(V.XF, i, jj, k);
         }
         __syncthreads();
         for (int k = threadIdx.x + 1; k <= KMM1; k += TS_BS) {
@@ -95,17 +97,17 @@ __global__ void __launch_bounds__(TS_BS) k_ts_cells(Dev d, float *__restrict__ D
     const int nr = A1(d.NROW, j);
     const int kts = A1(d.KTIPS, nr), kte = A1(d.KTIPE, nr);
     const float F1 = d.F1, F2 = d.F2, F3 = d.F3;
-    const float *__restrict__ XF = d.XFLUX;
-    const float *__restrict__ RF = d.RFLUX;
-    const float *__restrict__ TF = d.TFLUX;
-    const float *__restrict__ SR = d.SOURCE;
+    const float *__restrict__ XF = V.XF;
+    const float *__restrict__ RF = V.RF;
+    const float *__restrict__ TF = V.TF;
+    const float *__restrict__ SR = V.SR;
     for (int c = threadIdx.x; c < nc; c += TS_BS) {
         int i = c % IMM1 + 1, k = c / IMM1 + 1;
         size_t n = ix3(d, i, j, k);
         float t0 = TF[n], t1 = TF[n + 1];
         if (kts > 0 && k >= kts && k <= kte - 1) {
             if (i == 1 || i + 1 == IM) {
-                float tb = 0.5f * (A3(d.TFLUX, 1, j, k) + A3(d.TFLUX, IM, j, k));
+                float tb = 0.5f * (A3(TF, 1, j, k) + A3(TF, IM, j, k));
                 if (i == 1) t0 = tb;
                 if (i + 1 == IM) t1 = tb;
             }
@@ -113,9 +115,9 @@ __global__ void __launch_bounds__(TS_BS) k_ts_cells(Dev d, float *__restrict__ D
         float src = SR[n];
         if (role && !lowx) {
             float FLOWDIRN = -A3(d.FLOWX, d.IMID, jmx, k);
-            if (role == 1 && FLOWDIRN > 0.0f) src = src - (A3(d.XFLUX, i, j - 1, k) - lsum[k - 1] * A1(d.FP, i)) * d.FEXTRAP;
+            if (role == 1 && FLOWDIRN > 0.0f) src = src - (A3(XF, i, j - 1, k) - lsum[k - 1] * A1(d.FP, i)) * d.FEXTRAP;
             if (role == 2) src = 0.0f;
-            if (role == 3 && !(FLOWDIRN > 0.0f)) src = src + (d.XFLUX[n] - lsum[k - 1] * A1(d.FP, i)) * d.FEXTRAP;
+            if (role == 3 && !(FLOWDIRN > 0.0f)) src = src + (XF[n] - lsum[k - 1] * A1(d.FP, i)) * d.FEXTRAP;
         }
         float DELTA = XF[n] - XF[n - IM] * RATPITCH + RF[n] - RF[n + (size_t)IM * d.JM] + t0 - t1 - src;
         float df = DIFF[n];
@@ -139,11 +141,11 @@ __global__ void __launch_bounds__(TS_BS) k_ts_cells(Dev d, float *__restrict__ D
     for (int c = threadIdx.x; c < nc; c += TS_BS) {
         int i = c % IMM1 + 1, k = c / IMM1 + 1;
         float v = st[c];
-        A3(d.STORE, i, j, k) = v;
+        A3(V.ST, i, j, k) = v;
         ps += (double)v;
     }
     ps = block_sum<TS_BS>(ps, shd);
-    if (threadIdx.x == 0) d.plane_sum[j - 1] = ps;
+    if (threadIdx.x == 0) V.psum[j - 1] = ps;
     // level-1 and level-2 partial sums of this plane
     const int n1 = d.NIB1 * d.NKB1, n2 = d.NIB2 * d.NKB2;
     for (int t = threadIdx.x; t < n1 + n2; t += TS_BS) {
@@ -156,8 +158,8 @@ __global__ void __launch_bounds__(TS_BS) k_ts_cells(Dev d, float *__restrict__ D
         float s = 0.0f;
         for (int k = k0; k <= k1; ++k)
             for (int i = i0; i <= i1; ++i) s = s + st[(k - 1) * IMM1 + (i - 1)];
-        if (lv1) d.P1[(size_t)(j - 1) * n1 + u] = s;
-        else d.P2[(size_t)(j - 1) * n2 + u] = s;
+        if (lv1) V.P1[(size_t)(j - 1) * n1 + u] = s;
+        else V.P2[(size_t)(j - 1) * n2 + u] = s;
     }
 }
 
@@ -165,7 +167,8 @@ __global__ void __launch_bounds__(TS_BS) k_ts_cells(Dev d, float *__restrict__ D
 // reference-order level sums (REDUCE_ORDER=1): one thread per block walks
 // its cells in the (K,J,I) loop order of 700; superblocks likewise
 // ---------------------------------------------------------------------
-__global__ void k_ts_restrict_seq(Dev d) {
+__global__ void k_ts_restrict_seq(const __grid_constant__ Dev d, int v0) {
+    const VarSet &V = d.var[v0 + blockIdx.y];
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     int n1 = d.NIB1 * (d.NJB1 + 1) * d.NKB1;
     int n2 = d.NIB2 * (d.NJB2 + 1) * d.NKB2;
@@ -176,8 +179,8 @@ __global__ void k_ts_restrict_seq(Dev d) {
         float s = 0.0f;
         for (int k = 1; k <= d.KMM1; ++k)
             for (int j = a; j <= b; ++j)
-                for (int i = 1; i <= d.IMM1; ++i) s = s + A3(d.STORE, i, j, k);
-        A1(d.SBSUM, sb) = s;
+                for (int i = 1; i <= d.IMM1; ++i) s = s + A3(V.ST, i, j, k);
+        A1(V.SBSUM, sb) = s;
         return;
     }
     const bool lv1 = t < n1;
@@ -193,16 +196,17 @@ __global__ void k_ts_restrict_seq(Dev d) {
         int k0 = lv1 ? A1(d.KB1_S, kb) : A1(d.KB2_S, kb), k1 = lv1 ? A1(d.KB1_E, kb) : A1(d.KB2_E, kb);
         for (int k = k0; k <= k1; ++k)
             for (int j = j0; j <= j1; ++j)
-                for (int i = i0; i <= i1; ++i) s = s + A3(d.STORE, i, j, k);
+                for (int i = i0; i <= i1; ++i) s = s + A3(V.ST, i, j, k);
     }
-    (lv1 ? d.B1CHG : d.B2CHG)[u] = s;
+    (lv1 ? V.B1CHG : V.B2CHG)[u] = s;
 }
 
 // ---------------------------------------------------------------------
 // prolong: 1500, with the block sums assembled from the plane partials
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(TS_BS) k_ts_prolong(Dev d, int want_abs) {
+__global__ void __launch_bounds__(TS_BS) k_ts_prolong(const __grid_constant__ Dev d, int v0, int want_abs) {
     extern __shared__ float sm[];
+    const VarSet &V = d.var[v0 + blockIdx.y];
     __shared__ double shd[TS_BS / 32];
     __shared__ float s_sb;
     const int j = blockIdx.x + 2;
@@ -213,30 +217,30 @@ __global__ void __launch_bounds__(TS_BS) k_ts_prolong(Dev d, int want_abs) {
     if (d.REDUCE_ORDER == 1) {
         for (int t = threadIdx.x; t < n1; t += TS_BS) {
             int ib = t % d.NIB1 + 1, kb = t / d.NIB1 + 1;
-            b1[t] = d.B1CHG[(size_t)(ib - 1) + (size_t)d.NIB1 * ((size_t)(j1 - 1) + (size_t)(d.NJB1 + 1) * (kb - 1))];
+            b1[t] = V.B1CHG[(size_t)(ib - 1) + (size_t)d.NIB1 * ((size_t)(j1 - 1) + (size_t)(d.NJB1 + 1) * (kb - 1))];
         }
         for (int t = threadIdx.x; t < n2; t += TS_BS) {
             int ib = t % d.NIB2 + 1, kb = t / d.NIB2 + 1;
-            b2[t] = d.B2CHG[(size_t)(ib - 1) + (size_t)d.NIB2 * ((size_t)(j2 - 1) + (size_t)(d.NJB2 + 1) * (kb - 1))];
+            b2[t] = V.B2CHG[(size_t)(ib - 1) + (size_t)d.NIB2 * ((size_t)(j2 - 1) + (size_t)(d.NJB2 + 1) * (kb - 1))];
         }
-        if (threadIdx.x == 0) s_sb = A1(d.SBSUM, jsb);
+        if (threadIdx.x == 0) s_sb = A1(V.SBSUM, jsb);
     } else {
         for (int t = threadIdx.x; t < n1; t += TS_BS) {
             float s = 0.0f;
             if (j1 <= d.NJB1)
-                for (int jj = A1(d.JB1_START, j1); jj <= A1(d.JB1_END, j1); ++jj) s = s + d.P1[(size_t)(jj - 1) * n1 + t];
+                for (int jj = A1(d.JB1_START, j1); jj <= A1(d.JB1_END, j1); ++jj) s = s + V.P1[(size_t)(jj - 1) * n1 + t];
             b1[t] = s;
         }
         for (int t = threadIdx.x; t < n2; t += TS_BS) {
             float s = 0.0f;
             if (j2 <= d.NJB2)
-                for (int jj = A1(d.JB2_START, j2); jj <= A1(d.JB2_END, j2); ++jj) s = s + d.P2[(size_t)(jj - 1) * n2 + t];
+                for (int jj = A1(d.JB2_START, j2); jj <= A1(d.JB2_END, j2); ++jj) s = s + V.P2[(size_t)(jj - 1) * n2 + t];
             b2[t] = s;
         }
         if (threadIdx.x < 32) {
             int a = A1(d.SB_START, jsb), b = A1(d.SB_END, jsb);
             double s = 0.0;
-            for (int jj = a + (int)threadIdx.x; jj <= b; jj += 32) s += d.plane_sum[jj - 1];
+            for (int jj = a + (int)threadIdx.x; jj <= b; jj += 32) s += V.psum[jj - 1];
             for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
             if (threadIdx.x == 0) s_sb = (float)s;
         }
@@ -252,33 +256,35 @@ __global__ void __launch_bounds__(TS_BS) k_ts_prolong(Dev d, int want_abs) {
         size_t s2 = (size_t)(i2 - 1) + (size_t)d.NIB2 * ((size_t)(j2 - 1) + (size_t)(d.NJB2 + 1) * (k2 - 1));
         size_t n = ix3(d, i, j, k);
         float B1 = b1[(k1 - 1) * d.NIB1 + (i1 - 1)], B2 = b2[(k2 - 1) * d.NIB2 + (i2 - 1)];
-        float DELTA = d.STORE[n] * d.STEP[n] + (B1 * d.STEP1[s1] + B2 * d.STEP2[s2] + SBCHG * SSB) * d.RSTEP[n];
-        d.STORE[n] = DELTA;
+        float DELTA = V.ST[n] * d.STEP[n] + (B1 * d.STEP1[s1] + B2 * d.STEP2[s2] + SBCHG * SSB) * d.RSTEP[n];
+        V.ST[n] = DELTA;
         sabs += (double)fabsf(DELTA);
     }
     if (want_abs) {
         sabs = block_sum<TS_BS>(sabs, shd);
-        if (threadIdx.x == 0) d.plane_abs[j - 1] = sabs;
+        if (threadIdx.x == 0) V.pabs[j - 1] = sabs;
     }
 }
 
 // per-J-plane sum of |STORE| (after residual smoothing)
-__global__ void __launch_bounds__(TS_BS) k_ts_plane_abs(Dev d) {
+__global__ void __launch_bounds__(TS_BS) k_ts_plane_abs(const __grid_constant__ Dev d, int v0) {
     __shared__ double shd[TS_BS / 32];
+    const VarSet &V = d.var[v0 + blockIdx.y];
     int j = blockIdx.x + 2;
     int nc = d.IMM1 * d.KMM1;
     double s = 0.0;
     for (int c = threadIdx.x; c < nc; c += TS_BS) {
         int i = c % d.IMM1 + 1, k = c / d.IMM1 + 1;
-        s += (double)fabsf(A3(d.STORE, i, j, k));
+        s += (double)fabsf(A3(V.ST, i, j, k));
     }
     s = block_sum<TS_BS>(s, shd);
-    if (threadIdx.x == 0) d.plane_abs[j - 1] = s;
+    if (threadIdx.x == 0) V.pabs[j - 1] = s;
 }
 
 // AVG_CHG / AVG_BLK with the reference's sequential REAL*4 sum (1501-1515)
-__global__ void k_ts_avgblk_seq(Dev d) {
+__global__ void k_ts_avgblk_seq(const __grid_constant__ Dev d, int v0) {
     __shared__ float chg[64];
+    const VarSet &V = d.var[v0 + blockIdx.y];
     if (!d.ctl->damp_on) return;
     int NROWS = d.NROWS;
     for (int nr = threadIdx.x + 1; nr <= NROWS; nr += blockDim.x) {
@@ -287,12 +293,12 @@ __global__ void k_ts_avgblk_seq(Dev d) {
         float SUMCHG = 0.0f;
         for (int k = 1; k <= d.KMM1; ++k)
             for (int j = JST; j <= JEN; ++j)
-                for (int i = 1; i <= d.IMM1; ++i) SUMCHG = SUMCHG + fabsf(A3(d.STORE, i, j, k));
+                for (int i = 1; i <= d.IMM1; ++i) SUMCHG = SUMCHG + fabsf(A3(V.ST, i, j, k));
         chg[nr - 1] = SUMCHG / (float)NSUM;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        float *B = d.AVG_BLK;
+        float *B = V.AVG_BLK;
         if (NROWS == 1) B[0] = chg[0];
         if (NROWS == 2) {
             B[1] = 0.5f * (chg[0] + chg[1]);
@@ -309,8 +315,10 @@ __global__ void k_ts_avgblk_seq(Dev d) {
 // ---------------------------------------------------------------------
 // update: negative feedback, second MP average, corner gather -> TMP
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(TS_BS) k_ts_update(Dev d, const float *__restrict__ D) {
+__global__ void __launch_bounds__(TS_BS) k_ts_update(const __grid_constant__ Dev d, int v0) {
     extern __shared__ float sm[];
+    const VarSet &V = d.var[v0 + blockIdx.y];
+    const float *__restrict__ D = V.D;
     __shared__ float s_blk[64];
     __shared__ float chg[64];
     const int j = blockIdx.x + 1;
@@ -322,13 +330,13 @@ __global__ void __launch_bounds__(TS_BS) k_ts_update(Dev d, const float *__restr
     const float DAMP = ctl->DAMP;
     if (damp_on) {
         if (d.REDUCE_ORDER == 1) {
-            for (int r = threadIdx.x; r < d.NROWS; r += TS_BS) s_blk[r] = d.AVG_BLK[r];
+            for (int r = threadIdx.x; r < d.NROWS; r += TS_BS) s_blk[r] = V.AVG_BLK[r];
         } else {
             int w = threadIdx.x >> 5, l = threadIdx.x & 31;
             for (int nr = w + 1; nr <= d.NROWS; nr += TS_BS / 32) {
                 int JST = A1(d.JSTART, nr) + 1, JEN = A1(d.JMIX, nr) - 1;
                 double s = 0.0;
-                for (int jj = JST + l; jj <= JEN; jj += 32) s += d.plane_abs[jj - 1];
+                for (int jj = JST + l; jj <= JEN; jj += 32) s += V.pabs[jj - 1];
                 for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
                 if (l == 0) chg[nr - 1] = (float)s / (float)(IMM1 * KMM1 * (JEN - JST + 1));
             }
@@ -358,7 +366,7 @@ __global__ void __launch_bounds__(TS_BS) k_ts_update(Dev d, const float *__restr
         float blk = damp_on ? s_blk[A1(d.NROW, jc) - 1] : 1.0f;
         for (int t = threadIdx.x; t < nc; t += TS_BS) {
             int i = t % IMM1 + 1, k = t / IMM1 + 1;
-            float v = A3(d.STORE, i, jc, k);
+            float v = A3(V.ST, i, jc, k);
             if (damp_on) {
                 float FDAMP = fabsf(v) / blk;
                 v = v / (1.0f + FDAMP / DAMP);
@@ -415,7 +423,7 @@ __global__ void __launch_bounds__(TS_BS) k_ts_update(Dev d, const float *__restr
                 }
             }
         }
-        d.TMP[n] = v;
+        V.TM[n] = v;
     }
 }
 
@@ -455,8 +463,11 @@ __device__ inline float stream_value(const Dev &d, const DevCtl *c, const float 
     return v;
 }
 
-__global__ void __launch_bounds__(SV_BS) k_ts_smooth(Dev d, const float *__restrict__ S, float *__restrict__ D) {
+__global__ void __launch_bounds__(SV_BS) k_ts_smooth(const __grid_constant__ Dev d, int v0) {
     extern __shared__ float sm[];
+    const VarSet &V = d.var[v0 + blockIdx.y];
+    const float *__restrict__ S = V.TM;
+    float *__restrict__ D = V.D;
     const int IM = d.IM, KM = d.KM, IMM1 = d.IMM1, KMM1 = d.KMM1;
     const int np = IM * KM;
     float *a = sm, *b = sm + np;
@@ -596,7 +607,10 @@ __global__ void __launch_bounds__(SV_BS) k_ts_smooth(Dev d, const float *__restr
 // SMOOTH_RESID (14833-14917): one Jacobi pass along J, I or K of the cell
 // changes inside each row, src -> dst (cells outside every row are copied)
 // ---------------------------------------------------------------------
-__global__ void k_resid_pass(Dev d, int dir, float smfac, const float *__restrict__ src, float *__restrict__ dst) {
+__global__ void k_resid_pass(const __grid_constant__ Dev d, int v0, int dir, float smfac, int st_to_tm) {
+    const VarSet &V = d.var[v0 + blockIdx.y];
+    const float *__restrict__ src = st_to_tm ? V.ST : V.TM;
+    float *__restrict__ dst = st_to_tm ? V.TM : V.ST;
     size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t N = (size_t)d.IM * d.JM * d.KM;
     if (n >= N) return;
@@ -631,9 +645,11 @@ __global__ void k_resid_pass(Dev d, int dir, float smfac, const float *__restric
     dst[n] = v;
 }
 
-__global__ void k_copy(const float *__restrict__ src, float *__restrict__ dst, size_t n) {
+// STORE = TMP after the three SMOOTH_RESID passes
+__global__ void k_copy_tm_st(const __grid_constant__ Dev d, int v0, size_t n) {
+    const VarSet &V = d.var[v0 + blockIdx.y];
     size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) dst[t] = src[t];
+    if (t < n) V.ST[t] = V.TM[t];
 }
 
 static size_t cells_smem(const Dev &d) { return ((size_t)d.IMM1 * d.KMM1 + d.KMM1) * sizeof(float); }
@@ -658,42 +674,43 @@ cudaError_t configure_kernels(const Dev &d) {
     return cudaSuccess;
 }
 
-void launch_tstep(const Dev &d, Launch L, float *D, float *DIFF) {
+void launch_tstep(const Dev &d, Launch L, int v0, int nv) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
     unsigned gN = grid_for(N, 256);
     const bool seq = d.REDUCE_ORDER == 1;
-    k_ts_cells<<<d.JM - 1, TS_BS, cells_smem(d), L.s>>>(d, DIFF);
+    const unsigned jp = (unsigned)(d.JM - 1), ja = (unsigned)d.JM, vy = (unsigned)nv;
+    k_ts_cells<<<dim3(jp, vy), TS_BS, cells_smem(d), L.s>>>(d, v0);
     mark(L, "k_ts_cells");
     if (seq) {
         int nb = d.NIB1 * (d.NJB1 + 1) * d.NKB1 + d.NIB2 * (d.NJB2 + 1) * d.NKB2 + d.NSBLK;
-        k_ts_restrict_seq<<<grid_for(nb, 64), 64, 0, L.s>>>(d);
+        k_ts_restrict_seq<<<dim3(grid_for(nb, 64), vy), 64, 0, L.s>>>(d, v0);
         mark(L, "k_ts_restrict_seq");
     }
-    k_ts_prolong<<<d.JM - 1, TS_BS, prolong_smem(d), L.s>>>(d, (d.NRSMTH == 0 && !seq) ? 1 : 0);
+    k_ts_prolong<<<dim3(jp, vy), TS_BS, prolong_smem(d), L.s>>>(d, v0, (d.NRSMTH == 0 && !seq) ? 1 : 0);
     mark(L, "k_ts_prolong");
     if (d.NRSMTH > 0) {
         for (int it = 0; it < d.NRSMTH; ++it) {
-            k_resid_pass<<<gN, 256, 0, L.s>>>(d, 0, d.RSMTH, d.STORE, d.TMP);
+            k_resid_pass<<<dim3(gN, vy), 256, 0, L.s>>>(d, v0, 0, d.RSMTH, 1);
             mark(L, "k_resid_pass");
-            k_resid_pass<<<gN, 256, 0, L.s>>>(d, 1, d.RSMTH, d.TMP, d.STORE);
+            k_resid_pass<<<dim3(gN, vy), 256, 0, L.s>>>(d, v0, 1, d.RSMTH, 0);
             mark(L, "k_resid_pass");
-            k_resid_pass<<<gN, 256, 0, L.s>>>(d, 2, d.RSMTH, d.STORE, d.TMP);
+            k_resid_pass<<<dim3(gN, vy), 256, 0, L.s>>>(d, v0, 2, d.RSMTH, 1);
             mark(L, "k_resid_pass");
-            k_copy<<<gN, 256, 0, L.s>>>(d.TMP, d.STORE, N);
-            mark(L, "k_copy");
+            k_copy_tm_st<<<dim3(gN, vy), 256, 0, L.s>>>(d, v0, N);
+            mark(L, "k_copy_tm_st");
         }
         if (!seq) {
-            k_ts_plane_abs<<<d.JM - 1, TS_BS, 0, L.s>>>(d);
+            k_ts_plane_abs<<<dim3(jp, vy), TS_BS, 0, L.s>>>(d, v0);
             mark(L, "k_ts_plane_abs");
         }
     }
     if (seq) {
-        k_ts_avgblk_seq<<<1, 32, 0, L.s>>>(d);
+        k_ts_avgblk_seq<<<dim3(1, vy), 32, 0, L.s>>>(d, v0);
         mark(L, "k_ts_avgblk_seq");
     }
-    k_ts_update<<<d.JM, TS_BS, update_smem(d), L.s>>>(d, D);
+    k_ts_update<<<dim3(ja, vy), TS_BS, update_smem(d), L.s>>>(d, v0);
     mark(L, "k_ts_update");
-    k_ts_smooth<<<d.JM, SV_BS, smooth_smem(d), L.s>>>(d, d.TMP, D);
+    k_ts_smooth<<<dim3(ja, vy), SV_BS, smooth_smem(d), L.s>>>(d, v0);
     mark(L, "k_ts_smooth");
 }
 

@@ -198,8 +198,9 @@ class Problem:
         _chk(load().mgpu_integrals_noalloc(self.h, ctypes.byref(o)))
         return o
 
-    def kernels_per_step(self) -> int:
-        return _chk(load().mgpu_kernels_per_step(self.h, 0))
+    def kernels_per_step(self, loss: bool = False, tail: bool = False) -> int:
+        """Kernel launches of one step (LOSS and tail steps launch more)."""
+        return _chk(load().mgpu_kernels_per_step(self.h, (1 if loss else 0) | (2 if tail else 0)))
 
     def bench_steps(self, nsteps: int, flush_l2: bool = True) -> float:
         """Sum of the device times (ms) of nsteps iterations."""
