@@ -197,8 +197,10 @@ void launch_tail(const Dev &d, Launch L);
 void launch_stepup(const Dev &d, Launch L, float relax, bool gated);
 void launch_integrals(const Dev &d, Launch L, double *out8);
 
-// sets per-kernel attributes (dynamic shared memory of the J-plane kernel)
+// sets per-kernel attributes (dynamic shared memory of the J-plane kernels
+// and of the LOSS kernels)
 cudaError_t configure_kernels(const Dev &d);
+cudaError_t configure_loss_kernels(const Dev &d);
 
 // Read-only view of a handle, for entry points defined outside mgpu_api.cu.
 struct HandleView {

@@ -14,7 +14,6 @@ namespace mgpu {
 
 static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
 
-constexpr int LMAX = 164;   // IM, KM <= 160 plus the 1-based end slots
 
 // viscosity set on entry to LOSS (8088-8112); one thread
 __global__ void k_loss_prologue(Dev d, int init_call) {
@@ -100,186 +99,283 @@ __device__ inline float fyplus_of(float yp, float yplam, float ypturb, float pre
 }
 
 // ---------------------------------------------------------------------
-// stresses on the streamwise (K = const) faces, LOSS DO 50
+// stresses on the streamwise (K = const) faces, LOSS DO 50 (8208-8556).
+// One CTA = 32 consecutive I-columns of one J-plane (threadIdx.x = I,
+// threadIdx.y = a K stride of LK_W), every column's K-line staged in shared
+// memory ([K][32] arrays, K rows 1..KM), so each load instruction reads 32
+// consecutive pitchwise points.  The per-column wall functions and the
+// transition scans run one thread per column in the reference's order.
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_loss_kfaces(Dev d, int init_call) {
+constexpr int LK_W = 8;            // warps per CTA (K stride)
+constexpr int LK_NARR = 10;        // [K][32] arrays in shared memory (+ RAVG per K)
+
+__global__ void __launch_bounds__(32 * LK_W) k_loss_kfaces(const __grid_constant__ Dev d, int init_call) {
     const DevCtl *c = d.ctl;
     if (!init_call && !c->do_loss) return;
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= d.IMM1 * (d.JM - 1)) return;
-    int i = t % d.IMM1 + 1, j = t / d.IMM1 + 2;
+    extern __shared__ float lsm[];
+    const int KM = d.KM, KMM1 = d.KMM1, KMID = d.KMID;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i = blockIdx.x * 32 + tx + 1;
+    const int j = blockIdx.y + 2;
+    const bool col = i <= d.IMM1;
+    // [K][32] arrays, row k-1
+    float *AREA = lsm, *VXAVG = AREA + KM * 32, *VRAVG = VXAVG + KM * 32, *VTAVG = VRAVG + KM * 32;
+    float *ROAVG = VTAVG + KM * 32, *TAVG = ROAVG + KM * 32, *WABS = TAVG + KM * 32, *YP = WABS + KM * 32;
+    float *VLAM = YP + KM * 32, *VTURB = VLAM + KM * 32, *RAVGK = VTURB + KM * 32;   // RAVGK: [K] only
+    __shared__ float s_vis[32], s_ftc[32], s_tw1[32], s_twm[32];
+    __shared__ float s_w1[32][4], s_wm[32][4];     // wall-face xs, rs, ts, wv at K=1 and K=KM
+#define LK(a, k) a[((k) - 1) * 32 + tx]
     const float RF_VIS = init_call ? 1.0f : d.RF_VIS;
     const float FMIXUP = init_call ? 1.0f : c->FMIXUP;
-    float VISLAM = c->VISLAM, FTCOND = c->FTCOND;
-    const int KM = d.KM, KMM1 = d.KMM1, KMID = d.KMID;
-    float VXAVG[LMAX], VRAVG[LMAX], VTAVG[LMAX], ROAVG[LMAX], TAVG[LMAX], RAVG[LMAX], WABS[LMAX], WTB[LMAX],
-        WBOUND[LMAX], AREA[LMAX], VLAM[LMAX], VTURB[LMAX];
-    int NRW = A1(d.NROW, j);
-    int JROW = j - A1(d.JSTART, NRW) + 1;
-    int JTRHUB = A1(d.JTRAN_K1, NRW), JTRTIP = A1(d.JTRAN_KM, NRW);
-    float WREL = A1(d.WRAD, j), WHUB = A1(d.WHUB, j), WTIP = A1(d.WTIP, j);
-    for (int k = 1; k <= KM; ++k) {
+    const int NRW = A1(d.NROW, j);
+    const float WREL = A1(d.WRAD, j), WHUB = A1(d.WHUB, j), WTIP = A1(d.WTIP, j);
+    // 1. face averages
+    for (int k = ty + 1; k <= KM; k += LK_W) {
+        float RAVG = 0.5f * (A2(d.R, j, k) + A2(d.R, j - 1, k));
+        if (tx == 0) RAVGK[k - 1] = RAVG;
+        if (!col) continue;
         float asx = A3(d.ASX, i, j, k), asr = A3(d.ASR, i, j, k);
-        AREA[k] = sqrtf(asx * asx + asr * asr);
-        VXAVG[k] = 0.25f * (A3(d.VX, i, j, k) + A3(d.VX, i, j - 1, k) + A3(d.VX, i + 1, j, k) + A3(d.VX, i + 1, j - 1, k));
-        VRAVG[k] = 0.25f * (A3(d.VR, i, j, k) + A3(d.VR, i, j - 1, k) + A3(d.VR, i + 1, j, k) + A3(d.VR, i + 1, j - 1, k));
-        VTAVG[k] = 0.25f * (A3(d.VT, i, j, k) + A3(d.VT, i, j - 1, k) + A3(d.VT, i + 1, j, k) + A3(d.VT, i + 1, j - 1, k));
-        ROAVG[k] = 0.25f * (A3(d.RO, i, j, k) + A3(d.RO, i, j - 1, k) + A3(d.RO, i + 1, j, k) + A3(d.RO, i + 1, j - 1, k));
-        TAVG[k] = 0.25f * (A3(d.T_STATIC, i, j, k) + A3(d.T_STATIC, i, j - 1, k) + A3(d.T_STATIC, i + 1, j, k) +
-                           A3(d.T_STATIC, i + 1, j - 1, k));
-        RAVG[k] = 0.5f * (A2(d.R, j, k) + A2(d.R, j - 1, k));
-        float WTAVG = VTAVG[k] - WREL * RAVG[k];
-        float WABSQ = VXAVG[k] * VXAVG[k] + VRAVG[k] * VRAVG[k] + WTAVG * WTAVG;
-        WABS[k] = sqrtf(WABSQ);
-        WTB[k] = VTAVG[k] - WHUB * RAVG[k];
-        if (k > KMID) WTB[k] = VTAVG[k] - WTIP * RAVG[k];
-        WBOUND[k] = sqrtf(VXAVG[k] * VXAVG[k] + VRAVG[k] * VRAVG[k] + WTB[k] * WTB[k]);
+        float vx = 0.25f * (A3(d.VX, i, j, k) + A3(d.VX, i, j - 1, k) + A3(d.VX, i + 1, j, k) + A3(d.VX, i + 1, j - 1, k));
+        float vr = 0.25f * (A3(d.VR, i, j, k) + A3(d.VR, i, j - 1, k) + A3(d.VR, i + 1, j, k) + A3(d.VR, i + 1, j - 1, k));
+        float vt = 0.25f * (A3(d.VT, i, j, k) + A3(d.VT, i, j - 1, k) + A3(d.VT, i + 1, j, k) + A3(d.VT, i + 1, j - 1, k));
+        LK(AREA, k) = sqrtf(asx * asx + asr * asr);
+        LK(VXAVG, k) = vx;
+        LK(VRAVG, k) = vr;
+        LK(VTAVG, k) = vt;
+        LK(ROAVG, k) = 0.25f * (A3(d.RO, i, j, k) + A3(d.RO, i, j - 1, k) + A3(d.RO, i + 1, j, k) + A3(d.RO, i + 1, j - 1, k));
+        LK(TAVG, k) = 0.25f * (A3(d.T_STATIC, i, j, k) + A3(d.T_STATIC, i, j - 1, k) + A3(d.T_STATIC, i + 1, j, k) +
+                               A3(d.T_STATIC, i + 1, j - 1, k));
+        float WTAVG = vt - WREL * RAVG;
+        float WABSQ = vx * vx + vr * vr + WTAVG * WTAVG;
+        LK(WABS, k) = sqrtf(WABSQ);
     }
-    if (d.REYNO < 0.0001f) {
-        VISLAM = (fabsf(d.REYNO) / 100000.0f) * powf(TAVG[KMID] / 288.0f, 0.62f);
-        float TCOND = d.CP * VISLAM / d.PRANDTL;
-        FTCOND = TCOND / VISLAM;
-    }
-    float TWALLK1, TWALLKM;
-    if (d.YPLUSWALL < -0.001f) {
-        float PERPK1 = A3(d.VOL, i, j, 1) / AREA[1];
-        float ynew;
-        wallfun(PERPK1, ROAVG[1], TWALLK1, AIJ(d.YPLUS_K1, i, j), WBOUND[1], ynew, VISLAM);
-        AIJ(d.YPLUS_K1, i, j) = fminf(1000.0f, ynew);
-    } else if (d.YPLUSWALL < 5.0f) {
-        float PERP = A3(d.VOL, i, j, 1) / AREA[1];
-        float RE = PERP * ROAVG[2] * WBOUND[2] / VISLAM;
-        TWALLK1 = skin_friction(RE, PERP, A1(d.ROUGH_H, NRW), ROAVG[2], WBOUND[2], VISLAM);
-    } else {
-        TWALLK1 = d.CFWALL * ROAVG[1] * WBOUND[1] * WBOUND[1];
-    }
-    if (d.YPLUSWALL < -0.001f) {
-        float PERPKM = A3(d.VOL, i, j, KMM1) / AREA[KM];
-        float ynew;
-        wallfun(PERPKM, ROAVG[KMM1], TWALLKM, AIJ(d.YPLUS_KM, i, j), WBOUND[KMM1], ynew, VISLAM);
-        AIJ(d.YPLUS_KM, i, j) = fminf(1000.0f, ynew);
-    } else if (d.YPLUSWALL < 5.0f) {
-        float PERP = A3(d.VOL, i, j, KMM1) / AREA[KM];
-        float RE = PERP * ROAVG[KMM1] * WBOUND[KMM1] / VISLAM;
-        TWALLKM = skin_friction(RE, PERP, A1(d.ROUGH_T, NRW), ROAVG[KMM1], WBOUND[KMM1], VISLAM);
-    } else {
-        TWALLKM = d.CFWALL * ROAVG[KM] * WBOUND[KM] * WBOUND[KM];
-    }
-    float VSTAR = sqrtf(TWALLK1 / ROAVG[1]);
-    for (int k = 1; k <= KMID; ++k) {
-        float PERP = sqrtf(A3(d.DWALLSQ, i, j, k));
-        float YPLSK1 = VSTAR * PERP * ROAVG[1] / VISLAM;
-        A3(d.Y_PLUS, i, j, k) = fminf(YPLSK1, 1000.0f);
-    }
-    VSTAR = sqrtf(TWALLKM / ROAVG[KM]);
-    for (int k = KMID + 1; k <= KMM1; ++k) {
-        float PERP = sqrtf(A3(d.DWALLSQ, i, j, k));
-        float YPLS = VSTAR * PERP * ROAVG[KM] / VISLAM;
-        A3(d.Y_PLUS, i, j, k) = fminf(YPLS, 1000.0f);
-    }
-    float FYPLUS = 0.0f;
-    for (int k = 2; k <= KMM1; ++k) {
-        FYPLUS = fyplus_of(A3(d.Y_PLUS, i, j, k), d.YPLAM, d.YPTURB, FYPLUS);
-        float DPERP = A3(d.VOL, i, j, k) / AREA[k];
-        VLAM[k] = d.FKLAM[(size_t)(NRW - 1) * KM + k - 1] * VISLAM / DPERP;
-        VTURB[k] = d.FKTURB[(size_t)(NRW - 1) * KM + k - 1] * ROAVG[k] * fabsf(WABS[k + 1] - WABS[k - 1]) * FMIXUP;
-        VTURB[k] = VTURB[k] * FYPLUS;
-    }
-    bool turb = false;
-    if (!(JROW < JTRHUB)) {
-        float RMAX = 0.0f;
-        for (int k = 2; k <= KMID; ++k) {
-            float RATVIS = VTURB[k] / VLAM[k];
-            if (RATVIS < RMAX) continue;
-            RMAX = RATVIS;
+    __syncthreads();
+    // 2. viscosity and wall shear stresses, one thread per column
+    auto wbound = [&](int k) {
+        float WTB = LK(VTAVG, k) - (k > KMID ? WTIP : WHUB) * RAVGK[k - 1];
+        return sqrtf(LK(VXAVG, k) * LK(VXAVG, k) + LK(VRAVG, k) * LK(VRAVG, k) + WTB * WTB);
+    };
+    if (ty == 0 && col) {
+        float VISLAM = c->VISLAM, FTCOND = c->FTCOND;
+        if (d.REYNO < 0.0001f) {
+            VISLAM = (fabsf(d.REYNO) / 100000.0f) * powf(LK(TAVG, KMID) / 288.0f, 0.62f);
+            float TCOND = d.CP * VISLAM / d.PRANDTL;
+            FTCOND = TCOND / VISLAM;
         }
-        turb = RMAX > d.FTRANS;
-    }
-    if (!turb)
-        for (int k = 2; k <= KMID; ++k) VTURB[k] = 0.0f;
-    turb = false;
-    if (!(JROW < JTRTIP)) {
-        float RMAX = 0.0f;
-        for (int k = KMID; k <= KMM1; ++k) {
-            float RATVIS = VTURB[k] / VLAM[k];
-            if (RATVIS < RMAX) continue;
-            RMAX = RATVIS;
-        }
-        turb = RMAX > d.FTRANS;
-    }
-    if (!turb)
-        for (int k = KMID; k <= KMM1; ++k) VTURB[k] = 0.0f;
-    // stresses at the faces K, streamed from K=1 upwards
-    float FMULT = TWALLK1 * AREA[1] / WBOUND[1];
-    if (d.IBOUND == 1 || d.IBOUND > 2) FMULT = 0.0f;
-    float xs_lo = FMULT * VXAVG[1], rs_lo = FMULT * VRAVG[1], ts_lo = FMULT * WTB[1];
-    float qf_lo = 0.0f, wv_lo = ts_lo * WHUB * RAVG[1];
-    float FMULTM = -TWALLKM * AREA[KM] / WBOUND[KM];
-    if (d.IBOUND >= 2) FMULTM = 0.0f;
-    float RF_VIS1 = 1.0f - RF_VIS;
-    for (int k = 1; k <= KMM1; ++k) {
-        int kp = k + 1;
-        float xs_hi, rs_hi, ts_hi, qf_hi, wv_hi;
-        if (kp == KM) {
-            xs_hi = FMULTM * VXAVG[KM];
-            rs_hi = FMULTM * VRAVG[KM];
-            ts_hi = FMULTM * WTB[KM];
-            qf_hi = 0.0f;
-            wv_hi = ts_hi * WTIP * RAVG[KM];
+        float TWALLK1, TWALLKM;
+        if (d.YPLUSWALL < -0.001f) {
+            float PERPK1 = A3(d.VOL, i, j, 1) / LK(AREA, 1);
+            float ynew;
+            wallfun(PERPK1, LK(ROAVG, 1), TWALLK1, AIJ(d.YPLUS_K1, i, j), wbound(1), ynew, VISLAM);
+            AIJ(d.YPLUS_K1, i, j) = fminf(1000.0f, ynew);
+        } else if (d.YPLUSWALL < 5.0f) {
+            float PERP = A3(d.VOL, i, j, 1) / LK(AREA, 1);
+            float RE = PERP * LK(ROAVG, 2) * wbound(2) / VISLAM;
+            TWALLK1 = skin_friction(RE, PERP, A1(d.ROUGH_H, NRW), LK(ROAVG, 2), wbound(2), VISLAM);
         } else {
-            float FM = AREA[kp] * (VLAM[kp] + VTURB[kp]);
-            xs_hi = FM * (VXAVG[kp + 1] - VXAVG[kp - 1]);
-            rs_hi = FM * (VRAVG[kp + 1] - VRAVG[kp - 1]);
-            float VISTOT = VISLAM * (1.0f + VTURB[kp] / VLAM[kp]);
-            ts_hi = FM * (VTAVG[kp + 1] - VTAVG[kp - 1]) - VISTOT * AREA[kp] * VTAVG[kp] / RAVG[kp];
-            qf_hi = FM * FTCOND * (TAVG[kp + 1] - TAVG[kp - 1]);
-            wv_hi = xs_hi * VXAVG[kp] + ts_hi * VTAVG[kp] + rs_hi * VRAVG[kp];
+            float wb = wbound(1);
+            TWALLK1 = d.CFWALL * LK(ROAVG, 1) * wb * wb;
         }
-        size_t n = ix3(d, i, j, k);
-        d.XFORCE[n] = RF_VIS1 * d.XFORCE[n] + RF_VIS * (xs_lo - xs_hi);
-        d.RFORCE[n] = RF_VIS1 * d.RFORCE[n] + RF_VIS * (rs_lo - rs_hi);
-        d.TFORCE[n] = RF_VIS1 * d.TFORCE[n] + RF_VIS * (ts_lo * RAVG[k] - ts_hi * RAVG[kp]);
-        d.QSOURCE[n] = RF_VIS1 * d.QSOURCE[n] + RF_VIS * (qf_lo - qf_hi + wv_lo - wv_hi);
-        xs_lo = xs_hi; rs_lo = rs_hi; ts_lo = ts_hi; qf_lo = qf_hi; wv_lo = wv_hi;
+        if (d.YPLUSWALL < -0.001f) {
+            float PERPKM = A3(d.VOL, i, j, KMM1) / LK(AREA, KM);
+            float ynew;
+            wallfun(PERPKM, LK(ROAVG, KMM1), TWALLKM, AIJ(d.YPLUS_KM, i, j), wbound(KMM1), ynew, VISLAM);
+            AIJ(d.YPLUS_KM, i, j) = fminf(1000.0f, ynew);
+        } else if (d.YPLUSWALL < 5.0f) {
+            float PERP = A3(d.VOL, i, j, KMM1) / LK(AREA, KM);
+            float RE = PERP * LK(ROAVG, KMM1) * wbound(KMM1) / VISLAM;
+            TWALLKM = skin_friction(RE, PERP, A1(d.ROUGH_T, NRW), LK(ROAVG, KMM1), wbound(KMM1), VISLAM);
+        } else {
+            float wb = wbound(KM);
+            TWALLKM = d.CFWALL * LK(ROAVG, KM) * wb * wb;
+        }
+        s_vis[tx] = VISLAM;
+        s_ftc[tx] = FTCOND;
+        s_tw1[tx] = TWALLK1;
+        s_twm[tx] = TWALLKM;
+        // the two wall faces (K=1 hub, K=KM casing)
+        float FMULT = TWALLK1 * LK(AREA, 1) / wbound(1);
+        if (d.IBOUND == 1 || d.IBOUND > 2) FMULT = 0.0f;
+        float WTB1 = LK(VTAVG, 1) - (1 > KMID ? WTIP : WHUB) * RAVGK[0];
+        float ts1 = FMULT * WTB1;
+        s_w1[tx][0] = FMULT * LK(VXAVG, 1);
+        s_w1[tx][1] = FMULT * LK(VRAVG, 1);
+        s_w1[tx][2] = ts1;
+        s_w1[tx][3] = ts1 * WHUB * RAVGK[0];
+        float FMULTM = -TWALLKM * LK(AREA, KM) / wbound(KM);
+        if (d.IBOUND >= 2) FMULTM = 0.0f;
+        float WTBM = LK(VTAVG, KM) - (KM > KMID ? WTIP : WHUB) * RAVGK[KM - 1];
+        float tsm = FMULTM * WTBM;
+        s_wm[tx][0] = FMULTM * LK(VXAVG, KM);
+        s_wm[tx][1] = FMULTM * LK(VRAVG, KM);
+        s_wm[tx][2] = tsm;
+        s_wm[tx][3] = tsm * WTIP * RAVGK[KM - 1];
     }
+    __syncthreads();
+    // 3. Y_PLUS from the wall nearer in K
+    if (col) {
+        const float VISLAM = s_vis[tx];
+        const float VS1 = sqrtf(s_tw1[tx] / LK(ROAVG, 1)), VSM = sqrtf(s_twm[tx] / LK(ROAVG, KM));
+        for (int k = ty + 1; k <= KMM1; k += LK_W) {
+            float PERP = sqrtf(A3(d.DWALLSQ, i, j, k));
+            float y = k <= KMID ? VS1 * PERP * LK(ROAVG, 1) / VISLAM : VSM * PERP * LK(ROAVG, KM) / VISLAM;
+            y = fminf(y, 1000.0f);
+            A3(d.Y_PLUS, i, j, k) = y;
+            LK(YP, k) = y;
+        }
+    }
+    __syncthreads();
+    // 4. laminar and mixing-length viscosities of the interior faces
+    if (col) {
+        const float VISLAM = s_vis[tx];
+        for (int k = ty + 2; k <= KMM1; k += LK_W) {
+            // FYPLUS keeps its previous value where Y_PLUS is NaN
+            int kk = k;
+            while (kk >= 2 && isnan(LK(YP, kk))) --kk;
+            float FYPLUS = kk >= 2 ? fyplus_of(LK(YP, kk), d.YPLAM, d.YPTURB, 0.0f) : 0.0f;
+            float DPERP = A3(d.VOL, i, j, k) / LK(AREA, k);
+            LK(VLAM, k) = d.FKLAM[(size_t)(NRW - 1) * KM + k - 1] * VISLAM / DPERP;
+            float vt = d.FKTURB[(size_t)(NRW - 1) * KM + k - 1] * LK(ROAVG, k) * fabsf(LK(WABS, k + 1) - LK(WABS, k - 1)) *
+                       FMIXUP;
+            LK(VTURB, k) = vt * FYPLUS;
+        }
+    }
+    __syncthreads();
+    // 5. transition, hub half then casing half (the casing scan sees the
+    //    hub half's result at KMID)
+    if (ty == 0 && col) {
+        const int JROW = j - A1(d.JSTART, NRW) + 1;
+        float *vt = VTURB + tx, *vl = VLAM + tx;   // column view, stride 32
+        auto scan = [&](int a, int b) {
+            float RMAX = 0.0f;
+            for (int q = a; q <= b; ++q) {
+                float RATVIS = vt[(q - 1) * 32] / vl[(q - 1) * 32];
+                if (RATVIS < RMAX) continue;
+                RMAX = RATVIS;
+            }
+            return RMAX > d.FTRANS;
+        };
+        bool turb = !(JROW < A1(d.JTRAN_K1, NRW)) && scan(2, KMID);
+        if (!turb)
+            for (int q = 2; q <= KMID; ++q) vt[(q - 1) * 32] = 0.0f;
+        turb = !(JROW < A1(d.JTRAN_KM, NRW)) && scan(KMID, KMM1);
+        if (!turb)
+            for (int q = KMID; q <= KMM1; ++q) vt[(q - 1) * 32] = 0.0f;
+    }
+    __syncthreads();
+    // 6. stresses on faces K and K+1 of each cell, body forces relaxed by RF_VIS
+    if (col) {
+        const float VISLAM = s_vis[tx], FTCOND = s_ftc[tx];
+        const float RF_VIS1 = 1.0f - RF_VIS;
+        auto face = [&](int kp, float &xs, float &rs, float &ts, float &qf, float &wv) {
+            if (kp == 1) {
+                xs = s_w1[tx][0]; rs = s_w1[tx][1]; ts = s_w1[tx][2]; qf = 0.0f; wv = s_w1[tx][3];
+            } else if (kp == KM) {
+                xs = s_wm[tx][0]; rs = s_wm[tx][1]; ts = s_wm[tx][2]; qf = 0.0f; wv = s_wm[tx][3];
+            } else {
+                float vl = LK(VLAM, kp), vtu = LK(VTURB, kp), ar = LK(AREA, kp);
+                float FM = ar * (vl + vtu);
+                xs = FM * (LK(VXAVG, kp + 1) - LK(VXAVG, kp - 1));
+                rs = FM * (LK(VRAVG, kp + 1) - LK(VRAVG, kp - 1));
+                float VISTOT = VISLAM * (1.0f + vtu / vl);
+                ts = FM * (LK(VTAVG, kp + 1) - LK(VTAVG, kp - 1)) - VISTOT * ar * LK(VTAVG, kp) / RAVGK[kp - 1];
+                qf = FM * FTCOND * (LK(TAVG, kp + 1) - LK(TAVG, kp - 1));
+                wv = xs * LK(VXAVG, kp) + ts * LK(VTAVG, kp) + rs * LK(VRAVG, kp);
+            }
+        };
+        for (int k = ty + 1; k <= KMM1; k += LK_W) {
+            float xl, rl, tl, ql, wl, xh, rh, th, qh, wh;
+            face(k, xl, rl, tl, ql, wl);
+            face(k + 1, xh, rh, th, qh, wh);
+            size_t n = ix3(d, i, j, k);
+            d.XFORCE[n] = RF_VIS1 * d.XFORCE[n] + RF_VIS * (xl - xh);
+            d.RFORCE[n] = RF_VIS1 * d.RFORCE[n] + RF_VIS * (rl - rh);
+            d.TFORCE[n] = RF_VIS1 * d.TFORCE[n] + RF_VIS * (tl * RAVGK[k - 1] - th * RAVGK[k]);
+            d.QSOURCE[n] = RF_VIS1 * d.QSOURCE[n] + RF_VIS * (ql - qh + wl - wh);
+        }
+    }
+#undef LK
 }
 
 // ---------------------------------------------------------------------
 // stresses on the bladewise (I = const) faces and the blade surfaces,
-// LOSS DO 100
+// LOSS DO 100 (8566-9044).  One warp per (J,K) line; the lanes cover I (coalesced), the
+// line's arrays sit in this warp's slice of shared memory.
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_loss_ifaces(Dev d, int init_call) {
+constexpr int LI_W = 4;            // warps (lines) per CTA
+constexpr int LI_NARR = 16;        // per-line arrays of IM+1 floats
+
+// Transition test of one wall's mixing-length viscosity (LOSS 8481-8510,
+// 8823-8852): the reference keeps RMAX = the running value of
+// "IF(RATVIS.LT.RMAX) skip, else RMAX = RATVIS" from RMAX = 0 and switches
+// the wall turbulent if RMAX > FTRANS.  Without a NaN that is
+// max(0, ratios) > FTRANS; a NaN ratio resets RMAX, so only the ratios after
+// the last NaN count (and none after it leaves RMAX = NaN: laminar).  The
+// lanes of one warp evaluate it over vt[a..b] / vl[a..b].
+__device__ inline bool transition_warp(const float *vt, const float *vl, int a, int b, float FTRANS) {
+    const int lane = threadIdx.x & 31;
+    int lastnan = a - 1;
+    for (int q0 = a; q0 <= b; q0 += 32) {
+        int q = q0 + lane;
+        float r = q <= b ? vt[q] / vl[q] : 0.0f;
+        bool nan = q <= b && isnan(r);
+        unsigned m = __ballot_sync(0xffffffffu, nan);
+        if (m) lastnan = q0 + 31 - __clz((int)m);
+    }
+    bool t = false;
+    for (int q0 = a; q0 <= b; q0 += 32) {
+        int q = q0 + lane;
+        if (q <= b && q > lastnan) {
+            float r = vt[q] / vl[q];
+            if (r > FTRANS) t = true;
+        }
+    }
+    bool any = __any_sync(0xffffffffu, t);
+    if (lastnan < a) any = any || (0.0f > FTRANS);
+    return any;
+}
+
+__global__ void __launch_bounds__(32 * LI_W) k_loss_ifaces(const __grid_constant__ Dev d, int init_call) {
     const DevCtl *c = d.ctl;
     if (!init_call && !c->do_loss) return;
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (d.JM - 1) * d.KMM1) return;
-    int k = t % d.KMM1 + 1, j = t / d.KMM1 + 2;
+    extern __shared__ float lsm[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int line = blockIdx.x * LI_W + w;
+    if (line >= (d.JM - 1) * d.KMM1) return;     // whole warps leave together
+    const int k = line % d.KMM1 + 1, j = line / d.KMM1 + 2;
+    const int IM = d.IM, IMM1 = d.IMM1, IMID = d.IMID;
+    const int L = IM + 1;
+    float *base = lsm + (size_t)w * LI_NARR * L;
+    float *AREA = base, *VXAVG = AREA + L, *VRAVG = VXAVG + L, *VTAVG = VRAVG + L, *WTAVG = VTAVG + L;
+    float *ROAVG = WTAVG + L, *TAVG = ROAVG + L, *WABS = TAVG + L, *YP = WABS + L, *VLAM = YP + L;
+    float *VTURB = VLAM + L, *XSTRES = VTURB + L, *RSTRES = XSTRES + L, *TSTRES = RSTRES + L;
+    float *QFLOW = TSTRES + L, *WVISC = QFLOW + L;
     const float RF_VIS = init_call ? 1.0f : d.RF_VIS;
     const float FMIXUP = init_call ? 1.0f : c->FMIXUP;
     float VISLAM = c->VISLAM, FTCOND = c->FTCOND;
-    const int IM = d.IM, IMM1 = d.IMM1, IMID = d.IMID;
-    float VXAVG[LMAX], VRAVG[LMAX], VTAVG[LMAX], WTAVG[LMAX], ROAVG[LMAX], TAVG[LMAX], WABS[LMAX], AREA[LMAX];
-    float XSTRES[LMAX], RSTRES[LMAX], TSTRES[LMAX], QFLOW[LMAX], WVISC[LMAX], VLAM[LMAX], VTURB[LMAX];
-    int NRW = A1(d.NROW, j);
-    int JROW = j - A1(d.JSTART, NRW) + 1;
-    int JTRLOW = A1(d.JTRAN_I1, NRW), JTRUP = A1(d.JTRAN_IM, NRW);
-    int JLEDGE = A1(d.JLE, NRW), JTEDGE = A1(d.JTE, NRW);
-    float WREL = A1(d.WRAD, j);
-    float RAVGK = A2(d.RAVG_CELL, j, k);
-    float abt = A2(d.ABT, j, k);
-    for (int i = 1; i <= IM; ++i) {
+    const int NRW = A1(d.NROW, j);
+    const int JROW = j - A1(d.JSTART, NRW) + 1;
+    const int JLEDGE = A1(d.JLE, NRW), JTEDGE = A1(d.JTE, NRW);
+    const float WREL = A1(d.WRAD, j);
+    const float RAVGK = A2(d.RAVG_CELL, j, k);
+    const float abt = A2(d.ABT, j, k);
+    for (int i = lane + 1; i <= IM; i += 32) {
         float abx = A3(d.ABX, i, j, k), abr = A3(d.ABR, i, j, k);
         AREA[i] = sqrtf(abx * abx + abr * abr + abt * abt);
-        VXAVG[i] = 0.25f * (A3(d.VX, i, j, k) + A3(d.VX, i, j - 1, k) + A3(d.VX, i, j - 1, k + 1) + A3(d.VX, i, j, k + 1));
-        VRAVG[i] = 0.25f * (A3(d.VR, i, j, k) + A3(d.VR, i, j - 1, k) + A3(d.VR, i, j - 1, k + 1) + A3(d.VR, i, j, k + 1));
+        float vx = 0.25f * (A3(d.VX, i, j, k) + A3(d.VX, i, j - 1, k) + A3(d.VX, i, j - 1, k + 1) + A3(d.VX, i, j, k + 1));
+        float vr = 0.25f * (A3(d.VR, i, j, k) + A3(d.VR, i, j - 1, k) + A3(d.VR, i, j - 1, k + 1) + A3(d.VR, i, j, k + 1));
+        float wt = 0.25f * (A3(d.WT, i, j, k) + A3(d.WT, i, j - 1, k) + A3(d.WT, i, j - 1, k + 1) + A3(d.WT, i, j, k + 1));
+        VXAVG[i] = vx;
+        VRAVG[i] = vr;
         VTAVG[i] = 0.25f * (A3(d.VT, i, j, k) + A3(d.VT, i, j - 1, k) + A3(d.VT, i, j - 1, k + 1) + A3(d.VT, i, j, k + 1));
-        WTAVG[i] = 0.25f * (A3(d.WT, i, j, k) + A3(d.WT, i, j - 1, k) + A3(d.WT, i, j - 1, k + 1) + A3(d.WT, i, j, k + 1));
+        WTAVG[i] = wt;
         ROAVG[i] = 0.25f * (A3(d.RO, i, j, k) + A3(d.RO, i, j - 1, k) + A3(d.RO, i, j - 1, k + 1) + A3(d.RO, i, j, k + 1));
         TAVG[i] = 0.25f * (A3(d.T_STATIC, i, j, k) + A3(d.T_STATIC, i, j - 1, k) + A3(d.T_STATIC, i, j - 1, k + 1) +
                            A3(d.T_STATIC, i, j, k + 1));
-        float WABSQ = VXAVG[i] * VXAVG[i] + VRAVG[i] * VRAVG[i] + WTAVG[i] * WTAVG[i];
+        float WABSQ = vx * vx + vr * vr + wt * wt;
         WABS[i] = sqrtf(WABSQ);
     }
+    __syncwarp();
     if (d.REYNO < 0.0001f) {
         VISLAM = (fabsf(d.REYNO) / 100000.0f) * powf(TAVG[IMID] / 288.0f, 0.62f);
         float TCOND = d.CP * VISLAM / d.PRANDTL;
@@ -289,102 +385,89 @@ __global__ void __launch_bounds__(128) k_loss_ifaces(Dev d, int init_call) {
     const float *FIT = d.FITURB + (size_t)(NRW - 1) * IM;
     const float *FIW = d.FIWAKE + (size_t)(NRW - 1) * IM;
     const float *FIU = d.FIUP + (size_t)(NRW - 1) * IM;
-    bool in_blade = !(j <= JLEDGE || j > JTEDGE);
-    bool in_gap = (A1(d.KTIPS, NRW) > 0) && (k >= A1(d.KTIPS, NRW)) && (k < A1(d.KTIPE, NRW));
+    const bool in_blade = !(j <= JLEDGE || j > JTEDGE);
+    const bool in_gap = (A1(d.KTIPS, NRW) > 0) && (k >= A1(d.KTIPS, NRW)) && (k < A1(d.KTIPE, NRW));
     if (in_blade) {
         if (!in_gap) {
-            float TWALLI1, TWALLIM;
-            if (d.YPLUSWALL < -0.001f) {
-                float PERPI1 = A3(d.VOL, 1, j, k) / AREA[1];
-                float ynew;
-                wallfun(PERPI1, ROAVG[1], TWALLI1, A2(d.YPLUS_I1, j, k), WABS[2], ynew, VISLAM);
-                A2(d.YPLUS_I1, j, k) = fminf(1000.0f, ynew);
-            } else if (d.YPLUSWALL < 5.0f) {
-                float PERP = A3(d.VOL, 1, j, k) / AREA[1];
-                float RE = ROAVG[2] * WABS[2] * PERP / VISLAM;
-                TWALLI1 = skin_friction(RE, PERP, A1(d.ROUGH_L, NRW), ROAVG[2], WABS[2], VISLAM);
-            } else {
-                TWALLI1 = d.CFWALL * ROAVG[1] * WABS[1] * WABS[1];
+            // wall shear on the two blade surfaces: lane 0 the I=1 side, lane 1 the I=IM side
+            float TW = 0.0f;
+            if (lane < 2) {
+                const bool lo = lane == 0;
+                const int iw = lo ? 1 : IM, ia = lo ? 1 : IMM1, ib = lo ? 2 : IMM1;
+                if (d.YPLUSWALL < -0.001f) {
+                    float PERPW = A3(d.VOL, ia, j, k) / AREA[iw];
+                    float ynew;
+                    float *yw = lo ? &A2(d.YPLUS_I1, j, k) : &A2(d.YPLUS_IM, j, k);
+                    wallfun(PERPW, ROAVG[ia], TW, *yw, WABS[ib], ynew, VISLAM);
+                    *yw = fminf(1000.0f, ynew);
+                } else if (d.YPLUSWALL < 5.0f) {
+                    float PERP = A3(d.VOL, ia, j, k) / AREA[iw];
+                    float RE = ROAVG[ib] * WABS[ib] * PERP / VISLAM;
+                    TW = skin_friction(RE, PERP, lo ? A1(d.ROUGH_L, NRW) : A1(d.ROUGH_U, NRW), ROAVG[ib], WABS[ib], VISLAM);
+                } else {
+                    TW = d.CFWALL * ROAVG[iw] * WABS[iw] * WABS[iw];
+                }
             }
-            if (d.YPLUSWALL < -0.001f) {
-                float PERPIM = A3(d.VOL, IMM1, j, k) / AREA[IM];
-                float ynew;
-                wallfun(PERPIM, ROAVG[IMM1], TWALLIM, A2(d.YPLUS_IM, j, k), WABS[IMM1], ynew, VISLAM);
-                A2(d.YPLUS_IM, j, k) = fminf(1000.0f, ynew);
-            } else if (d.YPLUSWALL < 5.0f) {
-                float PERP = A3(d.VOL, IMM1, j, k) / AREA[IM];
-                float RE = ROAVG[IMM1] * WABS[IMM1] * PERP / VISLAM;
-                TWALLIM = skin_friction(RE, PERP, A1(d.ROUGH_U, NRW), ROAVG[IMM1], WABS[IMM1], VISLAM);
-            } else {
-                TWALLIM = d.CFWALL * ROAVG[IM] * WABS[IM] * WABS[IM];
-            }
-            float VSTAR = sqrtf(TWALLI1 / ROAVG[1]);
-            for (int i = 1; i <= IMID; ++i) {
-                float YPLS = VSTAR * sqrtf(A3(d.DWALLSQ, i, j, k)) * ROAVG[1] / VISLAM;
+            const float TWALLI1 = __shfl_sync(0xffffffffu, TW, 0), TWALLIM = __shfl_sync(0xffffffffu, TW, 1);
+            const float VS1 = sqrtf(TWALLI1 / ROAVG[1]), VSM = sqrtf(TWALLIM / ROAVG[IM]);
+            for (int i = lane + 1; i <= IMM1; i += 32) {
+                float YPLS = i <= IMID ? VS1 * sqrtf(A3(d.DWALLSQ, i, j, k)) * ROAVG[1] / VISLAM
+                                       : VSM * sqrtf(A3(d.DWALLSQ, i, j, k)) * ROAVG[IM] / VISLAM;
                 float YPLSP = A3(d.Y_PLUS, i, j, k);
-                A3(d.Y_PLUS, i, j, k) = fminf(YPLS, YPLSP);
+                float y = fminf(YPLS, YPLSP);
+                A3(d.Y_PLUS, i, j, k) = y;
+                YP[i] = y;
             }
-            VSTAR = sqrtf(TWALLIM / ROAVG[IM]);
-            for (int i = IMID + 1; i <= IMM1; ++i) {
-                float YPLS = VSTAR * sqrtf(A3(d.DWALLSQ, i, j, k)) * ROAVG[IM] / VISLAM;
-                float YPLSP = A3(d.Y_PLUS, i, j, k);
-                A3(d.Y_PLUS, i, j, k) = fminf(YPLS, YPLSP);
+            if (lane == 0) {
+                float FMULT = TWALLI1 * AREA[1] / WABS[1];
+                XSTRES[1] = FMULT * VXAVG[1];
+                RSTRES[1] = FMULT * VRAVG[1];
+                TSTRES[1] = FMULT * WTAVG[1];
+                FMULT = -TWALLIM * AREA[IM] / WABS[IM];
+                XSTRES[IM] = FMULT * VXAVG[IM];
+                RSTRES[IM] = FMULT * VRAVG[IM];
+                TSTRES[IM] = FMULT * WTAVG[IM];
+                QFLOW[1] = 0.0f;
+                WVISC[1] = TSTRES[1] * WREL * RAVGK;
+                QFLOW[IM] = 0.0f;
+                WVISC[IM] = TSTRES[IM] * WREL * RAVGK;
             }
-            float FMULT = TWALLI1 * AREA[1] / WABS[1];
-            XSTRES[1] = FMULT * VXAVG[1];
-            RSTRES[1] = FMULT * VRAVG[1];
-            TSTRES[1] = FMULT * WTAVG[1];
-            FMULT = -TWALLIM * AREA[IM] / WABS[IM];
-            XSTRES[IM] = FMULT * VXAVG[IM];
-            RSTRES[IM] = FMULT * VRAVG[IM];
-            TSTRES[IM] = FMULT * WTAVG[IM];
-            QFLOW[1] = 0.0f;
-            WVISC[1] = TSTRES[1] * WREL * RAVGK;
-            QFLOW[IM] = 0.0f;
-            WVISC[IM] = TSTRES[IM] * WREL * RAVGK;
+        } else {
+            for (int i = lane + 2; i <= IMM1; i += 32) YP[i] = A3(d.Y_PLUS, i, j, k);
         }
-        float FYPLUS = 0.0f;
-        for (int i = 2; i <= IMM1; ++i) {
-            FYPLUS = fyplus_of(A3(d.Y_PLUS, i, j, k), d.YPLAM, d.YPTURB, FYPLUS);
+        __syncwarp();
+        for (int i = lane + 2; i <= IMM1; i += 32) {
+            int ii = i;     // FYPLUS keeps its previous value where Y_PLUS is NaN
+            while (ii >= 2 && isnan(YP[ii])) --ii;
+            float FYPLUS = ii >= 2 ? fyplus_of(YP[ii], d.YPLAM, d.YPTURB, 0.0f) : 0.0f;
             float DPERP = A3(d.VOL, i, j, k) / AREA[i];
             VLAM[i] = FIL[i - 1] * VISLAM / DPERP;
-            VTURB[i] = FIT[i - 1] * ROAVG[i] * fabsf(WABS[i + 1] - WABS[i - 1]) * FMIXUP;
-            VTURB[i] = VTURB[i] * FYPLUS;
+            float vt = FIT[i - 1] * ROAVG[i] * fabsf(WABS[i + 1] - WABS[i - 1]) * FMIXUP;
+            VTURB[i] = vt * FYPLUS;
         }
-        bool turb = false;
-        if (!(JROW < JTRLOW)) {
-            float RMAX = 0.0f;
-            for (int i = 2; i <= IMID; ++i) {
-                float RATVIS = VTURB[i] / VLAM[i];
-                if (RATVIS < RMAX) continue;
-                RMAX = RATVIS;
-            }
-            turb = RMAX > d.FTRANS;
-        }
+        __syncwarp();
+        bool turb = !(JROW < A1(d.JTRAN_I1, NRW)) && transition_warp(VTURB, VLAM, 2, IMID, d.FTRANS);
         if (!turb)
-            for (int i = 2; i <= IMID; ++i) VTURB[i] = 0.0f;
-        turb = false;
-        if (!(JROW < JTRUP)) {
-            float RMAX = 0.0f;
-            for (int i = IMID; i <= IMM1; ++i) {
-                float RATVIS = VTURB[i] / VLAM[i];
-                if (RATVIS < RMAX) continue;
-                RMAX = RATVIS;
-            }
-            turb = RMAX > d.FTRANS;
-        }
+            for (int i = lane + 2; i <= IMID; i += 32) VTURB[i] = 0.0f;
+        __syncwarp();
+        turb = !(JROW < A1(d.JTRAN_IM, NRW)) && transition_warp(VTURB, VLAM, IMID, IMM1, d.FTRANS);
         if (!turb)
-            for (int i = IMID; i <= IMM1; ++i) VTURB[i] = 0.0f;
-        for (int i = 2; i <= IMM1; ++i) {
+            for (int i = lane + IMID; i <= IMM1; i += 32) VTURB[i] = 0.0f;
+        __syncwarp();
+        for (int i = lane + 2; i <= IMM1; i += 32) {
             float FM = (VLAM[i] + VTURB[i]) * AREA[i];
-            XSTRES[i] = FM * (VXAVG[i + 1] - VXAVG[i - 1]);
-            RSTRES[i] = FM * (VRAVG[i + 1] - VRAVG[i - 1]);
-            TSTRES[i] = FM * (WTAVG[i + 1] - WTAVG[i - 1]);
+            float xs = FM * (VXAVG[i + 1] - VXAVG[i - 1]);
+            float rs = FM * (VRAVG[i + 1] - VRAVG[i - 1]);
+            float ts = FM * (WTAVG[i + 1] - WTAVG[i - 1]);
+            XSTRES[i] = xs;
+            RSTRES[i] = rs;
+            TSTRES[i] = ts;
             A3(d.VISC_RAT, i, j, k) = VTURB[i] / VLAM[i];
             QFLOW[i] = FM * FTCOND * (TAVG[i + 1] - TAVG[i - 1]);
-            WVISC[i] = XSTRES[i] * VXAVG[i] + RSTRES[i] * VRAVG[i] + TSTRES[i] * VTAVG[i];
+            WVISC[i] = xs * VXAVG[i] + rs * VRAVG[i] + ts * VTAVG[i];
         }
-        if (in_gap) {
+        __syncwarp();
+        if (in_gap && lane == 0) {
             XSTRES[1] = 0.5f * (XSTRES[2] + XSTRES[IMM1]);
             RSTRES[1] = 0.5f * (RSTRES[2] + RSTRES[IMM1]);
             TSTRES[1] = 0.5f * (TSTRES[2] + TSTRES[IMM1]);
@@ -398,43 +481,51 @@ __global__ void __launch_bounds__(128) k_loss_ifaces(Dev d, int init_call) {
         }
     } else {
         float FACJ = 0.0f;
-        bool wake = j > JTEDGE;
+        const bool wake = j > JTEDGE;
         if (wake) {
             FACJ = 0.1f * (float)(j - JTEDGE);
             if (FACJ > 1.0f) FACJ = 1.0f;
         }
-        for (int i = 1; i <= IM; ++i) {
+        for (int i = lane + 1; i <= IM; i += 32) {
             int ISUB = (i == IM) ? IMM1 : i;
             int IM1 = (i == 1) ? IMM1 : i - 1;
             int IP1 = (i == IM) ? 2 : i + 1;
             float DPERP = A3(d.VOL, ISUB, j, k) / AREA[i];
-            VLAM[i] = FIL[i - 1] * VISLAM / DPERP;
+            float vl = FIL[i - 1] * VISLAM / DPERP;
+            float vt;
             if (wake) {
                 float FBLEND = (FACJ * FIW[i - 1] + (1.0f - FACJ) * FIT[i - 1]) * FMIXUP;
-                VTURB[i] = FBLEND * ROAVG[i] * fabsf(WABS[IP1] - WABS[IM1]);
+                vt = FBLEND * ROAVG[i] * fabsf(WABS[IP1] - WABS[IM1]);
             } else {
-                VTURB[i] = FMIXUP * FIU[i - 1] * ROAVG[i] * fabsf(WABS[IP1] - WABS[IM1]);
+                vt = FMIXUP * FIU[i - 1] * ROAVG[i] * fabsf(WABS[IP1] - WABS[IM1]);
             }
-            A3(d.VISC_RAT, i, j, k) = VTURB[i] / VLAM[i];
-            float FM = AREA[i] * (VLAM[i] + VTURB[i]);
-            XSTRES[i] = FM * (VXAVG[IP1] - VXAVG[IM1]);
-            RSTRES[i] = FM * (VRAVG[IP1] - VRAVG[IM1]);
-            TSTRES[i] = FM * (WTAVG[IP1] - WTAVG[IM1]);
+            A3(d.VISC_RAT, i, j, k) = vt / vl;
+            float FM = AREA[i] * (vl + vt);
+            float xs = FM * (VXAVG[IP1] - VXAVG[IM1]);
+            float rs = FM * (VRAVG[IP1] - VRAVG[IM1]);
+            float ts = FM * (WTAVG[IP1] - WTAVG[IM1]);
+            XSTRES[i] = xs;
+            RSTRES[i] = rs;
+            TSTRES[i] = ts;
             QFLOW[i] = FM * FTCOND * (TAVG[IP1] - TAVG[IM1]);
-            WVISC[i] = XSTRES[i] * VXAVG[i] + TSTRES[i] * VTAVG[i] + RSTRES[i] * VRAVG[i];
+            WVISC[i] = xs * VXAVG[i] + ts * VTAVG[i] + rs * VRAVG[i];
         }
-        XSTRES[1] = 0.5f * (XSTRES[IM] + XSTRES[1]);
-        RSTRES[1] = 0.5f * (RSTRES[IM] + RSTRES[1]);
-        TSTRES[1] = 0.5f * (TSTRES[IM] + TSTRES[1]);
-        XSTRES[IM] = XSTRES[1];
-        RSTRES[IM] = RSTRES[1];
-        TSTRES[IM] = TSTRES[1];
-        QFLOW[1] = 0.5f * (QFLOW[IM] + QFLOW[1]);
-        WVISC[1] = 0.5f * (WVISC[IM] + WVISC[1]);
-        QFLOW[IM] = QFLOW[1];
-        WVISC[IM] = WVISC[1];
+        __syncwarp();
+        if (lane == 0) {
+            XSTRES[1] = 0.5f * (XSTRES[IM] + XSTRES[1]);
+            RSTRES[1] = 0.5f * (RSTRES[IM] + RSTRES[1]);
+            TSTRES[1] = 0.5f * (TSTRES[IM] + TSTRES[1]);
+            XSTRES[IM] = XSTRES[1];
+            RSTRES[IM] = RSTRES[1];
+            TSTRES[IM] = TSTRES[1];
+            QFLOW[1] = 0.5f * (QFLOW[IM] + QFLOW[1]);
+            WVISC[1] = 0.5f * (WVISC[IM] + WVISC[1]);
+            QFLOW[IM] = QFLOW[1];
+            WVISC[IM] = WVISC[1];
+        }
     }
-    for (int i = 1; i <= IMM1; ++i) {
+    __syncwarp();
+    for (int i = lane + 1; i <= IMM1; i += 32) {
         size_t n = ix3(d, i, j, k);
         d.XFORCE[n] = d.XFORCE[n] + RF_VIS * (XSTRES[i] - XSTRES[i + 1]);
         d.RFORCE[n] = d.RFORCE[n] + RF_VIS * (RSTRES[i] - RSTRES[i + 1]);
@@ -443,14 +534,27 @@ __global__ void __launch_bounds__(128) k_loss_ifaces(Dev d, int init_call) {
     }
 }
 
+size_t loss_kfaces_smem(const Dev &d) { return ((size_t)LK_NARR * d.KM * 32 + d.KM) * sizeof(float); }
+size_t loss_ifaces_smem(const Dev &d) { return (size_t)LI_W * LI_NARR * (d.IM + 1) * sizeof(float); }
+
+cudaError_t configure_loss_kernels(const Dev &d) {
+    size_t kb = loss_kfaces_smem(d), ib = loss_ifaces_smem(d);
+    if (kb > 220 * 1024 || ib > 220 * 1024) return cudaErrorInvalidValue;   // KM <= 160: kb <= 201 KB
+    cudaError_t e = cudaFuncSetAttribute((const void *)k_loss_kfaces, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(kb > 48 * 1024 ? kb : 48 * 1024));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute((const void *)k_loss_ifaces, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(ib > 48 * 1024 ? ib : 48 * 1024));
+}
+
 void launch_loss(const Dev &d, Launch L, bool init_call) {
     k_loss_prologue<<<1, 1, 0, L.s>>>(d, init_call ? 1 : 0);
     mark(L, "k_loss_prologue");
-    int nk = d.IMM1 * (d.JM - 1);
-    k_loss_kfaces<<<grid_for(nk, 128), 128, 0, L.s>>>(d, init_call ? 1 : 0);
+    dim3 gk((unsigned)((d.IMM1 + 31) / 32), (unsigned)(d.JM - 1));
+    k_loss_kfaces<<<gk, dim3(32, LK_W), loss_kfaces_smem(d), L.s>>>(d, init_call ? 1 : 0);
     mark(L, "k_loss_kfaces");
-    int ni = (d.JM - 1) * d.KMM1;
-    k_loss_ifaces<<<grid_for(ni, 128), 128, 0, L.s>>>(d, init_call ? 1 : 0);
+    int nl = (d.JM - 1) * d.KMM1;
+    k_loss_ifaces<<<(nl + LI_W - 1) / LI_W, 32 * LI_W, loss_ifaces_smem(d), L.s>>>(d, init_call ? 1 : 0);
     mark(L, "k_loss_ifaces");
 }
 

@@ -671,7 +671,7 @@ cudaError_t configure_kernels(const Dev &d) {
         cudaError_t e = cudaFuncSetAttribute(x.f, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
         if (e != cudaSuccess) return e;
     }
-    return cudaSuccess;
+    return configure_loss_kernels(d);
 }
 
 void launch_tstep(const Dev &d, Launch L, int v0, int nv) {
