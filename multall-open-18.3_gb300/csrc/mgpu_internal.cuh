@@ -4,7 +4,7 @@
 // Fortran order (I fastest, then J, then K), so one node (I,J,K) is
 // element (I-1) + IM*((J-1) + JM*(K-1)) and a warp reads 32 consecutive
 // pitchwise points.  Kernels take the whole description by value (`Dev`,
-// ~2.2 KB of kernel parameters: pointers, dimensions and the constant
+// ~2.3 KB of kernel parameters: pointers, dimensions and the constant
 // REAL scalars); the values that change from step to step (smoothing ramp,
 // NSTEP, the 5-step flags, the monitors) live in a small device struct
 // `DevCtl` that the first kernel of each step updates, so a step is a fixed
