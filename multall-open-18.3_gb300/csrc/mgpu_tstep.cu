@@ -27,8 +27,9 @@ namespace mgpu {
 
 static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
 
-constexpr int TS_BS = 1024;
-constexpr int SV_BS = 1024;
+constexpr int TS_BS = 256;      // threads per J-plane CTA; 4 CTAs resident per SM
+constexpr int TS_U = 3;          // cells per thread whose loads are issued together
+constexpr int SV_BS = 256;
 
 template <int BS>
 __device__ inline double block_sum(double v, double *sh) {
@@ -58,11 +59,31 @@ __device__ inline int mp_role(const Dev &d, int j, int *nr) {
     return 0;
 }
 
+// (i, k) of the points t = start, start + stride, ... of an ni-wide plane,
+// 1-based, advanced without a division per point
+struct Walk2 {
+    int i, k, di, dk, ni;
+    __device__ Walk2(int ni_, int start, int stride) : ni(ni_) {
+        i = start % ni_ + 1;
+        k = start / ni_ + 1;
+        di = stride % ni_;
+        dk = stride / ni_;
+    }
+    __device__ void next() {
+        i += di;
+        k += dk;
+        if (i > ni) {
+            i -= ni;
+            ++k;
+        }
+    }
+};
+
 // ---------------------------------------------------------------------
 // cells: 5503-5510 (tip gap), 5516-5555 (MP extrapolation), 1000 (flux
 // sum), 1750 (MP redistribution) and the multigrid partial sums
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(TS_BS) k_ts_cells(const __grid_constant__ Dev d, int v0) {
+__global__ void __launch_bounds__(TS_BS, 4) k_ts_cells(const __grid_constant__ Dev d, int v0) {
     extern __shared__ float sm[];
     const VarSet &V = d.var[v0 + blockIdx.y];
     float *__restrict__ DIFF = V.DIFF;
@@ -101,28 +122,55 @@ __global__ void __launch_bounds__(TS_BS) k_ts_cells(const __grid_constant__ Dev 
     const float *__restrict__ RF = V.RF;
     const float *__restrict__ TF = V.TF;
     const float *__restrict__ SR = V.SR;
-    for (int c = threadIdx.x; c < nc; c += TS_BS) {
-        int i = c % IMM1 + 1, k = c / IMM1 + 1;
-        size_t n = ix3(d, i, j, k);
-        float t0 = TF[n], t1 = TF[n + 1];
-        if (kts > 0 && k >= kts && k <= kte - 1) {
-            if (i == 1 || i + 1 == IM) {
-                float tb = 0.5f * (A3(TF, 1, j, k) + A3(TF, IM, j, k));
-                if (i == 1) t0 = tb;
-                if (i + 1 == IM) t1 = tb;
+    // each thread first loads the operands of its TS_U cells, then computes:
+    // the loads of all cells are in flight together
+    const size_t ks = (size_t)IM * d.JM, pj = (size_t)IM * (j - 1);
+    Walk2 w(IMM1, threadIdx.x, TS_BS);
+    for (int c0 = threadIdx.x; c0 < nc; c0 += TS_U * TS_BS) {
+        float xf[TS_U], xm[TS_U], rf[TS_U], rk[TS_U], ta[TS_U], tb1[TS_U], sr[TS_U], df[TS_U];
+        int ci[TS_U], ck[TS_U];
+#pragma unroll
+        for (int u = 0; u < TS_U; ++u) {
+            ci[u] = w.i;
+            ck[u] = w.k;
+            w.next();
+            if (c0 + u * TS_BS < nc) {
+                const size_t n = pj + (size_t)(ci[u] - 1) + ks * (ck[u] - 1);
+                xf[u] = XF[n];
+                xm[u] = XF[n - IM];
+                rf[u] = RF[n];
+                rk[u] = RF[n + ks];
+                ta[u] = TF[n];
+                tb1[u] = TF[n + 1];
+                sr[u] = SR[n];
+                df[u] = DIFF[n];
             }
         }
-        float src = SR[n];
-        if (role && !lowx) {
-            float FLOWDIRN = -A3(d.FLOWX, d.IMID, jmx, k);
-            if (role == 1 && FLOWDIRN > 0.0f) src = src - (A3(XF, i, j - 1, k) - lsum[k - 1] * A1(d.FP, i)) * d.FEXTRAP;
-            if (role == 2) src = 0.0f;
-            if (role == 3 && !(FLOWDIRN > 0.0f)) src = src + (XF[n] - lsum[k - 1] * A1(d.FP, i)) * d.FEXTRAP;
+#pragma unroll
+        for (int u = 0; u < TS_U; ++u) {
+            const int c = c0 + u * TS_BS;
+            if (c >= nc) break;
+            const int i = ci[u], k = ck[u];
+            const size_t n = pj + (size_t)(i - 1) + ks * (k - 1);
+            float t0 = ta[u], t1 = tb1[u];
+            if (kts > 0 && k >= kts && k <= kte - 1) {
+                if (i == 1 || i + 1 == IM) {
+                    float tb = 0.5f * (A3(TF, 1, j, k) + A3(TF, IM, j, k));
+                    if (i == 1) t0 = tb;
+                    if (i + 1 == IM) t1 = tb;
+                }
+            }
+            float src = sr[u];
+            if (role && !lowx) {
+                float FLOWDIRN = -A3(d.FLOWX, d.IMID, jmx, k);
+                if (role == 1 && FLOWDIRN > 0.0f) src = src - (xm[u] - lsum[k - 1] * A1(d.FP, i)) * d.FEXTRAP;
+                if (role == 2) src = 0.0f;
+                if (role == 3 && !(FLOWDIRN > 0.0f)) src = src + (xf[u] - lsum[k - 1] * A1(d.FP, i)) * d.FEXTRAP;
+            }
+            float DELTA = xf[u] - xm[u] * RATPITCH + rf[u] - rk[u] + t0 - t1 - src;
+            st[c] = F1 * DELTA + F2 * df[u];
+            DIFF[n] = DELTA + F3 * df[u];
         }
-        float DELTA = XF[n] - XF[n - IM] * RATPITCH + RF[n] - RF[n + (size_t)IM * d.JM] + t0 - t1 - src;
-        float df = DIFF[n];
-        st[c] = F1 * DELTA + F2 * df;
-        DIFF[n] = DELTA + F3 * df;
     }
     __syncthreads();
     if (role == 1 || role == 3) {
@@ -204,7 +252,7 @@ __global__ void k_ts_restrict_seq(const __grid_constant__ Dev d, int v0) {
 // ---------------------------------------------------------------------
 // prolong: 1500, with the block sums assembled from the plane partials
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(TS_BS) k_ts_prolong(const __grid_constant__ Dev d, int v0, int want_abs) {
+__global__ void __launch_bounds__(TS_BS, 4) k_ts_prolong(const __grid_constant__ Dev d, int v0, int want_abs) {
     extern __shared__ float sm[];
     const VarSet &V = d.var[v0 + blockIdx.y];
     __shared__ double shd[TS_BS / 32];
@@ -214,14 +262,38 @@ __global__ void __launch_bounds__(TS_BS) k_ts_prolong(const __grid_constant__ De
     const int n1 = d.NIB1 * d.NKB1, n2 = d.NIB2 * d.NKB2;
     float *b1 = sm, *b2 = sm + n1;
     const int j1 = A1(d.JB1, j), j2 = A1(d.JB2, j), jsb = A1(d.JSBLK, j);
+    const int nc = IMM1 * KMM1;
+    const size_t ks = (size_t)d.IM * d.JM, pj = (size_t)d.IM * (j - 1);
+    const size_t m1 = (size_t)d.NIB1 * (d.NJB1 + 1), m2 = (size_t)d.NIB2 * (d.NJB2 + 1);
+    // operands of this thread's first TS_U cells, loaded before the block
+    // sums so their latency overlaps the assembly below
+    float pst[TS_U], pstp[TS_U], prs[TS_U], ps1[TS_U], ps2[TS_U];
+    int pb1[TS_U], pb2[TS_U];
+    Walk2 w(IMM1, threadIdx.x, TS_BS);
+#pragma unroll
+    for (int u = 0; u < TS_U; ++u) {
+        const int i = w.i, k = w.k;
+        w.next();
+        if (threadIdx.x + u * TS_BS < nc) {
+            const size_t n = pj + (size_t)(i - 1) + ks * (k - 1);
+            const int i1 = A1(d.IB1, i), i2 = A1(d.IB2, i), k1 = A1(d.KB1, k), k2 = A1(d.KB2, k);
+            pst[u] = V.ST[n];
+            pstp[u] = d.STEP[n];
+            prs[u] = d.RSTEP[n];
+            ps1[u] = d.STEP1[(size_t)(i1 - 1) + (size_t)d.NIB1 * (j1 - 1) + m1 * (k1 - 1)];
+            ps2[u] = d.STEP2[(size_t)(i2 - 1) + (size_t)d.NIB2 * (j2 - 1) + m2 * (k2 - 1)];
+            pb1[u] = (k1 - 1) * d.NIB1 + (i1 - 1);
+            pb2[u] = (k2 - 1) * d.NIB2 + (i2 - 1);
+        }
+    }
     if (d.REDUCE_ORDER == 1) {
         for (int t = threadIdx.x; t < n1; t += TS_BS) {
             int ib = t % d.NIB1 + 1, kb = t / d.NIB1 + 1;
-            b1[t] = V.B1CHG[(size_t)(ib - 1) + (size_t)d.NIB1 * ((size_t)(j1 - 1) + (size_t)(d.NJB1 + 1) * (kb - 1))];
+            b1[t] = V.B1CHG[(size_t)(ib - 1) + (size_t)d.NIB1 * (j1 - 1) + m1 * (kb - 1)];
         }
         for (int t = threadIdx.x; t < n2; t += TS_BS) {
             int ib = t % d.NIB2 + 1, kb = t / d.NIB2 + 1;
-            b2[t] = V.B2CHG[(size_t)(ib - 1) + (size_t)d.NIB2 * ((size_t)(j2 - 1) + (size_t)(d.NJB2 + 1) * (kb - 1))];
+            b2[t] = V.B2CHG[(size_t)(ib - 1) + (size_t)d.NIB2 * (j2 - 1) + m2 * (kb - 1)];
         }
         if (threadIdx.x == 0) s_sb = A1(V.SBSUM, jsb);
     } else {
@@ -247,14 +319,25 @@ __global__ void __launch_bounds__(TS_BS) k_ts_prolong(const __grid_constant__ De
     }
     __syncthreads();
     const float SBCHG = s_sb, SSB = A1(d.STEPSBK, jsb);
-    const int nc = IMM1 * KMM1;
     double sabs = 0.0;
-    for (int c = threadIdx.x; c < nc; c += TS_BS) {
-        int i = c % IMM1 + 1, k = c / IMM1 + 1;
-        int i1 = A1(d.IB1, i), i2 = A1(d.IB2, i), k1 = A1(d.KB1, k), k2 = A1(d.KB2, k);
-        size_t s1 = (size_t)(i1 - 1) + (size_t)d.NIB1 * ((size_t)(j1 - 1) + (size_t)(d.NJB1 + 1) * (k1 - 1));
-        size_t s2 = (size_t)(i2 - 1) + (size_t)d.NIB2 * ((size_t)(j2 - 1) + (size_t)(d.NJB2 + 1) * (k2 - 1));
-        size_t n = ix3(d, i, j, k);
+    w = Walk2(IMM1, threadIdx.x, TS_BS);
+#pragma unroll
+    for (int u = 0; u < TS_U; ++u) {
+        const int i = w.i, k = w.k;
+        w.next();
+        if (threadIdx.x + u * TS_BS < nc) {
+            const size_t n = pj + (size_t)(i - 1) + ks * (k - 1);
+            float DELTA = pst[u] * pstp[u] + (b1[pb1[u]] * ps1[u] + b2[pb2[u]] * ps2[u] + SBCHG * SSB) * prs[u];
+            V.ST[n] = DELTA;
+            sabs += (double)fabsf(DELTA);
+        }
+    }
+    for (int c = threadIdx.x + TS_U * TS_BS; c < nc; c += TS_BS, w.next()) {
+        const int i = w.i, k = w.k;
+        const int i1 = A1(d.IB1, i), i2 = A1(d.IB2, i), k1 = A1(d.KB1, k), k2 = A1(d.KB2, k);
+        const size_t s1 = (size_t)(i1 - 1) + (size_t)d.NIB1 * (j1 - 1) + m1 * (k1 - 1);
+        const size_t s2 = (size_t)(i2 - 1) + (size_t)d.NIB2 * (j2 - 1) + m2 * (k2 - 1);
+        const size_t n = pj + (size_t)(i - 1) + ks * (k - 1);
         float B1 = b1[(k1 - 1) * d.NIB1 + (i1 - 1)], B2 = b2[(k2 - 1) * d.NIB2 + (i2 - 1)];
         float DELTA = V.ST[n] * d.STEP[n] + (B1 * d.STEP1[s1] + B2 * d.STEP2[s2] + SBCHG * SSB) * d.RSTEP[n];
         V.ST[n] = DELTA;
@@ -267,7 +350,7 @@ __global__ void __launch_bounds__(TS_BS) k_ts_prolong(const __grid_constant__ De
 }
 
 // per-J-plane sum of |STORE| (after residual smoothing)
-__global__ void __launch_bounds__(TS_BS) k_ts_plane_abs(const __grid_constant__ Dev d, int v0) {
+__global__ void __launch_bounds__(TS_BS, 4) k_ts_plane_abs(const __grid_constant__ Dev d, int v0) {
     __shared__ double shd[TS_BS / 32];
     const VarSet &V = d.var[v0 + blockIdx.y];
     int j = blockIdx.x + 2;
@@ -315,7 +398,7 @@ __global__ void k_ts_avgblk_seq(const __grid_constant__ Dev d, int v0) {
 // ---------------------------------------------------------------------
 // update: negative feedback, second MP average, corner gather -> TMP
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(TS_BS) k_ts_update(const __grid_constant__ Dev d, int v0) {
+__global__ void __launch_bounds__(TS_BS, 4) k_ts_update(const __grid_constant__ Dev d, int v0) {
     extern __shared__ float sm[];
     const VarSet &V = d.var[v0 + blockIdx.y];
     const float *__restrict__ D = V.D;
@@ -363,10 +446,12 @@ __global__ void __launch_bounds__(TS_BS) k_ts_update(const __grid_constant__ Dev
         int jc = j + h;
         if (jc < 2 || jc > d.JM) continue;
         float *c = h ? cB : cA;
-        float blk = damp_on ? s_blk[A1(d.NROW, jc) - 1] : 1.0f;
-        for (int t = threadIdx.x; t < nc; t += TS_BS) {
-            int i = t % IMM1 + 1, k = t / IMM1 + 1;
-            float v = A3(V.ST, i, jc, k);
+        const float blk = damp_on ? s_blk[A1(d.NROW, jc) - 1] : 1.0f;
+        const float *__restrict__ stp = V.ST + (size_t)IM * (jc - 1);     // plane jc, (i, k) at i-1 + IM*JM*(k-1)
+        const size_t kstride = (size_t)IM * d.JM;
+        Walk2 w(IMM1, threadIdx.x, TS_BS);
+        for (int t = threadIdx.x; t < nc; t += TS_BS, w.next()) {
+            float v = stp[(size_t)(w.i - 1) + kstride * (w.k - 1)];
             if (damp_on) {
                 float FDAMP = fabsf(v) / blk;
                 v = v / (1.0f + FDAMP / DAMP);
@@ -403,23 +488,44 @@ __global__ void __launch_bounds__(TS_BS) k_ts_update(const __grid_constant__ Dev
     const int np = IM * KM;
     const float fdn = A1(d.FACDWN, j);
     const float fup = j + 1 <= d.JM ? A1(d.FACUP, j + 1) : 0.0f;
-    for (int t = threadIdx.x; t < np; t += TS_BS) {
-        int i = t % IM + 1, k = t / IM + 1;
-        size_t n = ix3(d, i, j, k);
+    const bool hA = j >= 2, hB = j + 1 <= d.JM;
+    const float *__restrict__ FBL = d.FBL;
+    const float *__restrict__ FBR = d.FBR;
+    const float *__restrict__ FTL = d.FTL;
+    const float *__restrict__ FTR = d.FTR;
+    const size_t nbase = (size_t)IM * (j - 1), kstride = (size_t)IM * d.JM;
+    Walk2 w(IM, threadIdx.x, TS_BS);
+    for (int t = threadIdx.x; t < np; t += TS_BS, w.next()) {
+        const int i = w.i, k = w.k;
+        const size_t n = nbase + (size_t)(i - 1) + kstride * (k - 1);
         float v = D[n];
-        for (int kc = k - 1; kc <= k; ++kc) {
-            if (kc < 1 || kc > KMM1) continue;
-            for (int h = 0; h < 2; ++h) {
-                int jc = j + h;
-                if (jc < 2 || jc > d.JM) continue;
-                const float *c = h ? cB : cA;
-                float fac = h ? fup : fdn;
-                for (int ic = i - 1; ic <= i; ++ic) {
-                    if (ic < 1 || ic > IMM1) continue;
-                    float w;
-                    if (ic == i) w = (kc == k) ? AIK(d.FBL, ic, kc) : AIK(d.FTL, ic, kc);
-                    else w = (kc == k) ? AIK(d.FBR, ic, kc) : AIK(d.FTR, ic, kc);
-                    v = v + c[(kc - 1) * IMM1 + (ic - 1)] * w * fac;
+        if (hA && hB && i >= 2 && i <= IMM1 && k >= 2 && k <= KMM1) {
+            // interior node: all eight cells, weights FTR/FTL of row k-1 and FBR/FBL of row k
+            const int lo = (i - 2) + IMM1 * (k - 2), hi = lo + IMM1;       // cells (i-1, k-1), (i-1, k)
+            const float wtr = FTR[(i - 2) + IM * (k - 2)], wtl = FTL[(i - 1) + IM * (k - 2)];
+            const float wbr = FBR[(i - 2) + IM * (k - 1)], wbl = FBL[(i - 1) + IM * (k - 1)];
+            v = v + cA[lo] * wtr * fdn;
+            v = v + cA[lo + 1] * wtl * fdn;
+            v = v + cB[lo] * wtr * fup;
+            v = v + cB[lo + 1] * wtl * fup;
+            v = v + cA[hi] * wbr * fdn;
+            v = v + cA[hi + 1] * wbl * fdn;
+            v = v + cB[hi] * wbr * fup;
+            v = v + cB[hi + 1] * wbl * fup;
+        } else {
+            for (int kc = k - 1; kc <= k; ++kc) {
+                if (kc < 1 || kc > KMM1) continue;
+                for (int h = 0; h < 2; ++h) {
+                    if (!(h ? hB : hA)) continue;
+                    const float *c = h ? cB : cA;
+                    float fac = h ? fup : fdn;
+                    for (int ic = i - 1; ic <= i; ++ic) {
+                        if (ic < 1 || ic > IMM1) continue;
+                        float wt;
+                        if (ic == i) wt = (kc == k) ? AIK(FBL, ic, kc) : AIK(FTL, ic, kc);
+                        else wt = (kc == k) ? AIK(FBR, ic, kc) : AIK(FTR, ic, kc);
+                        v = v + c[(kc - 1) * IMM1 + (ic - 1)] * wt * fac;
+                    }
                 }
             }
         }
@@ -431,39 +537,36 @@ __global__ void __launch_bounds__(TS_BS) k_ts_update(const __grid_constant__ Dev
 // smooth: SMOOTH_VAR (3900-9000, 8502) + periodic (8000), tip gap (510),
 // mixing-plane average (100): TMP -> D, one CTA per J-plane
 // ---------------------------------------------------------------------
-__device__ inline float stream_value(const Dev &d, const DevCtl *c, const float *__restrict__ S, int i, int j, int k) {
+// Streamwise smoothing case of plane j (SMOOTH_VAR 15375-15406): the
+// reference tests the cases in this order and the last one that holds wins.
+__device__ inline int stream_case(const Dev &d, int j) {
     int nr = A1(d.NROW, j);
     int J1 = A1(d.JSTART, nr), J2 = A1(d.JMIX, nr);
-#define DV(jj) A3(S, i, (jj), k)
-    float d0 = DV(j);
-    float v = d0;
-    const float SFX = c->SFX, SFX1 = c->SFX1, SFXB = c->SFXB, SFXB1 = c->SFXB1, SFXBH = c->SFXBH;
-    if (j >= J1 + 3 && j <= J2 - 3) {
-        float AVERG = 0.5f * (DV(j + 1) + DV(j - 1));
-        float CURV = AVERG - 0.5f * d0 - 0.25f * (DV(j - 2) + DV(j + 2));
-        v = SFX1 * d0 + SFX * (AVERG + d.FAC_4TH * CURV);
-    }
-    if (j == J2) v = d0;
-    if (j == J1) v = d0;
-    if (j == J1 + 2) v = SFXB1 * d0 + SFXBH * (DV(J1 + 3) + DV(J1 + 1));
-    if (j == J1 + 1) v = SFXB1 * d0 + SFXB * (1.25f * DV(J1 + 2) + 0.5f * DV(J1 + 3) - 0.75f * DV(J1 + 4));
-    if (j == J2 - 2) v = SFXB1 * d0 + SFXBH * (DV(J2 - 1) + DV(J2 - 3));
-    if (j == J2 - 1) v = SFXB1 * d0 + SFXB * (1.25f * DV(J2 - 2) + 0.5f * DV(J2 - 3) - 0.75f * DV(J2 - 4));
-#undef DV
-    if (i == 1 || i == d.IM) {
-        for (int r = 1; r <= d.NROWS; ++r) {
-            int JL = A1(d.JLED, r);
-            if (j == JL - 2 || j == JL - 1) v = c->SFXHM1 * d0 + c->SFX14 * (A3(S, 2, j, k) + A3(S, d.IMM1, j, k));
-            if (j == JL) {
-                if (i == 1) v = c->SFXHM1 * d0 + c->SFX14 * (A3(S, 1, j + 1, k) + A3(S, d.IM, j, k));
-                else v = c->SFXHM1 * d0 + c->SFX14 * (A3(S, d.IM, j + 1, k) + A3(S, 1, j, k));
-            }
-        }
-    }
-    return v;
+    int sc = 0;                                   // 0: unchanged
+    if (j >= J1 + 3 && j <= J2 - 3) sc = 1;       // 2nd + 4th order interior
+    if (j == J2) sc = 0;
+    if (j == J1) sc = 0;
+    if (j == J1 + 2) sc = 2;
+    if (j == J1 + 1) sc = 3;
+    if (j == J2 - 2) sc = 4;
+    if (j == J2 - 1) sc = 5;
+    return sc;
 }
 
-__global__ void __launch_bounds__(SV_BS) k_ts_smooth(const __grid_constant__ Dev d, int v0) {
+// Leading-edge periodic smoothing case of plane j (15417-15434): 1 on the
+// two planes before a row's JLED, 2 on JLED itself; the last row that
+// matches wins.
+__device__ inline int le_case(const Dev &d, int j) {
+    int lc = 0;
+    for (int r = 1; r <= d.NROWS; ++r) {
+        int JL = A1(d.JLED, r);
+        if (j == JL - 2 || j == JL - 1) lc = 1;
+        if (j == JL) lc = 2;
+    }
+    return lc;
+}
+
+__global__ void __launch_bounds__(SV_BS, 4) k_ts_smooth(const __grid_constant__ Dev d, int v0) {
     extern __shared__ float sm[];
     const VarSet &V = d.var[v0 + blockIdx.y];
     const float *__restrict__ S = V.TM;
@@ -471,65 +574,113 @@ __global__ void __launch_bounds__(SV_BS) k_ts_smooth(const __grid_constant__ Dev
     const int IM = d.IM, KM = d.KM, IMM1 = d.IMM1, KMM1 = d.KMM1;
     const int np = IM * KM;
     float *a = sm, *b = sm + np;
+    float *cFD = b + np, *cFU = cFD + IM, *cFKD = cFU + IM, *cFKU = cFKD + KM;   // FD, FU, FKD, FKU
     const int j = blockIdx.x + 1;
     const DevCtl *c = d.ctl;
     const bool stream = !(c->SFX < 0.0001f);
-    for (int t = threadIdx.x; t < np; t += SV_BS) {
-        int i = t % IM + 1, k = t / IM + 1;
-        a[t] = stream ? stream_value(d, c, S, i, j, k) : A3(S, i, j, k);
+    for (int t = threadIdx.x; t < IM; t += SV_BS) {
+        cFD[t] = d.FD[t];
+        cFU[t] = d.FU[t];
+    }
+    for (int t = threadIdx.x; t < KM; t += SV_BS) {
+        cFKD[t] = d.FKD[t];
+        cFKU[t] = d.FKU[t];
+    }
+    const size_t ks = (size_t)IM * d.JM;                     // K stride of a node array
+    const float *__restrict__ Sj = S + (size_t)IM * (j - 1);  // plane j: (i, k) at i-1 + ks*(k-1)
+    {
+        const int sc = stream ? stream_case(d, j) : 0;
+        const int lc = stream ? le_case(d, j) : 0;
+        const int nr = A1(d.NROW, j);
+        const int J1 = A1(d.JSTART, nr), J2 = A1(d.JMIX, nr);
+        const float SFX = c->SFX, SFX1 = c->SFX1, SFXB = c->SFXB, SFXB1 = c->SFXB1, SFXBH = c->SFXBH;
+        const float SFXHM1 = c->SFXHM1, SFX14 = c->SFX14, F4 = d.FAC_4TH;
+        // plane offsets (in nodes) of the J neighbours each case reads
+        auto pl = [&](int jj) { return (ptrdiff_t)IM * (jj - j); };
+        Walk2 w(IM, threadIdx.x, SV_BS);
+        for (int t = threadIdx.x; t < np; t += SV_BS, w.next()) {
+            const int i = w.i, k = w.k;
+            const float *p = Sj + (size_t)(i - 1) + ks * (k - 1);
+            const float d0 = p[0];
+            float v = d0;
+            switch (sc) {
+            case 1: {
+                float AVERG = 0.5f * (p[pl(j + 1)] + p[pl(j - 1)]);
+                float CURV = AVERG - 0.5f * d0 - 0.25f * (p[pl(j - 2)] + p[pl(j + 2)]);
+                v = SFX1 * d0 + SFX * (AVERG + F4 * CURV);
+                break;
+            }
+            case 2: v = SFXB1 * d0 + SFXBH * (p[pl(J1 + 3)] + p[pl(J1 + 1)]); break;
+            case 3: v = SFXB1 * d0 + SFXB * (1.25f * p[pl(J1 + 2)] + 0.5f * p[pl(J1 + 3)] - 0.75f * p[pl(J1 + 4)]); break;
+            case 4: v = SFXB1 * d0 + SFXBH * (p[pl(J2 - 1)] + p[pl(J2 - 3)]); break;
+            case 5: v = SFXB1 * d0 + SFXB * (1.25f * p[pl(J2 - 2)] + 0.5f * p[pl(J2 - 3)] - 0.75f * p[pl(J2 - 4)]); break;
+            default: break;
+            }
+            if (lc && (i == 1 || i == IM)) {
+                const float *pk = Sj + ks * (k - 1);
+                if (lc == 1) v = SFXHM1 * d0 + SFX14 * (pk[1] + pk[IMM1 - 1]);
+                else if (i == 1) v = SFXHM1 * d0 + SFX14 * (pk[IM + 0] + pk[IM - 1]);
+                else v = SFXHM1 * d0 + SFX14 * (pk[IM + IM - 1] + pk[0]);
+            }
+            a[t] = v;
+        }
     }
     __syncthreads();
 #define P(buf, i, k) buf[((i) - 1) + IM * ((k) - 1)]
     const bool periodic_j = !(A1(d.IND, j) == 1 || A1(d.INDLE, j) == 1);
     if (j >= 2 && !(c->SFT < 0.0001f)) {
         const float SFT = c->SFT, SFT1 = c->SFT1, F4 = d.FAC_4TH;
-        for (int t = threadIdx.x; t < np; t += SV_BS) {
-            int i = t % IM + 1, k = t / IM + 1;
+        Walk2 w(IM, threadIdx.x, SV_BS);
+        for (int t = threadIdx.x; t < np; t += SV_BS, w.next()) {
+            const int i = w.i, k = w.k;
+            const float *ak = a + IM * (k - 1) - 1;     // ak[i] = P(a, i, k)
             auto curve = [&](int ii) -> float {
                 if (ii == 1 || ii == IM) {
                     if (!periodic_j) return 0.0f;
-                    float avg1 = 0.5f * (P(a, 2, k) + P(a, IMM1, k));
-                    return P(a, 1, k) - avg1;
+                    float avg1 = 0.5f * (ak[2] + ak[IMM1]);
+                    return ak[1] - avg1;
                 }
-                float avg = A1(d.FD, ii) * P(a, ii + 1, k) + A1(d.FU, ii) * P(a, ii - 1, k);
-                return P(a, ii, k) - avg;
+                float avg = cFD[ii - 1] * ak[ii + 1] + cFU[ii - 1] * ak[ii - 1];
+                return ak[ii] - avg;
             };
             float AVG, SC;
             if (i == 1 || i == IM) {
                 if (periodic_j) {
-                    AVG = 0.5f * (P(a, 2, k) + P(a, IMM1, k));
+                    AVG = 0.5f * (ak[2] + ak[IMM1]);
                     SC = 0.5f * (curve(2) + curve(IMM1));
                 } else {
-                    if (i == 1) AVG = P(a, 2, k) + A1(d.FU, 1) * (P(a, 2, k) - P(a, 3, k));
-                    else AVG = P(a, IMM1, k) + A1(d.FU, IM) * (P(a, IMM1, k) - P(a, d.IMM2, k));
+                    if (i == 1) AVG = ak[2] + cFU[0] * (ak[2] - ak[3]);
+                    else AVG = ak[IMM1] + cFU[IM - 1] * (ak[IMM1] - ak[d.IMM2]);
                     SC = 0.0f;
                 }
             } else {
-                AVG = A1(d.FD, i) * P(a, i + 1, k) + A1(d.FU, i) * P(a, i - 1, k);
-                SC = A1(d.FU, i) * curve(i - 1) + A1(d.FD, i) * curve(i + 1);
+                AVG = cFD[i - 1] * ak[i + 1] + cFU[i - 1] * ak[i - 1];
+                SC = cFU[i - 1] * curve(i - 1) + cFD[i - 1] * curve(i + 1);
             }
-            P(b, i, k) = SFT1 * P(a, i, k) + SFT * (AVG + F4 * SC);
+            b[t] = SFT1 * ak[i] + SFT * (AVG + F4 * SC);
         }
         __syncthreads();
-        for (int t = threadIdx.x; t < np; t += SV_BS) {
-            int i = t % IM + 1, k = t / IM + 1;
+        w = Walk2(IM, threadIdx.x, SV_BS);
+        for (int t = threadIdx.x; t < np; t += SV_BS, w.next()) {
+            const int i = w.i, k = w.k;
+            const float *bi = b + (i - 1) - IM;         // bi[IM * kk] = P(b, i, kk)
             auto curvek = [&](int kk) -> float {
                 if (kk == 1 || kk == KM) return 0.0f;
-                float avg = A1(d.FKD, kk) * P(b, i, kk + 1) + A1(d.FKU, kk) * P(b, i, kk - 1);
-                return P(b, i, kk) - avg;
+                float avg = cFKD[kk - 1] * bi[IM * (kk + 1)] + cFKU[kk - 1] * bi[IM * (kk - 1)];
+                return bi[IM * kk] - avg;
             };
             float AVG, SC;
             if (k == 1) {
-                AVG = P(b, i, 2) + 0.5f * A1(d.FKU, 1) * (P(b, i, 2) - P(b, i, 3));
+                AVG = bi[IM * 2] + 0.5f * cFKU[0] * (bi[IM * 2] - bi[IM * 3]);
                 SC = 0.0f;
             } else if (k == KM) {
-                AVG = P(b, i, KMM1) + 0.5f * A1(d.FKU, KM) * (P(b, i, KMM1) - P(b, i, d.KMM2));
+                AVG = bi[IM * KMM1] + 0.5f * cFKU[KM - 1] * (bi[IM * KMM1] - bi[IM * d.KMM2]);
                 SC = 0.0f;
             } else {
-                AVG = A1(d.FKD, k) * P(b, i, k + 1) + A1(d.FKU, k) * P(b, i, k - 1);
-                SC = A1(d.FKU, k) * curvek(k - 1) + A1(d.FKD, k) * curvek(k + 1);
+                AVG = cFKD[k - 1] * bi[IM * (k + 1)] + cFKU[k - 1] * bi[IM * (k - 1)];
+                SC = cFKU[k - 1] * curvek(k - 1) + cFKD[k - 1] * curvek(k + 1);
             }
-            P(a, i, k) = SFT1 * P(b, i, k) + SFT * (AVG + F4 * SC);
+            a[t] = SFT1 * bi[IM * k] + SFT * (AVG + F4 * SC);
         }
         __syncthreads();
         float cv = 0.0f;
@@ -597,10 +748,9 @@ __global__ void __launch_bounds__(SV_BS) k_ts_smooth(const __grid_constant__ Dev
         __syncthreads();
     }
 #undef P
-    for (int t = threadIdx.x; t < np; t += SV_BS) {
-        int i = t % IM + 1, k = t / IM + 1;
-        A3(D, i, j, k) = a[t];
-    }
+    float *Dj = D + (size_t)IM * (j - 1);
+    Walk2 w(IM, threadIdx.x, SV_BS);
+    for (int t = threadIdx.x; t < np; t += SV_BS, w.next()) Dj[(size_t)(w.i - 1) + ks * (w.k - 1)] = a[t];
 }
 
 // ---------------------------------------------------------------------
@@ -655,7 +805,7 @@ __global__ void k_copy_tm_st(const __grid_constant__ Dev d, int v0, size_t n) {
 static size_t cells_smem(const Dev &d) { return ((size_t)d.IMM1 * d.KMM1 + d.KMM1) * sizeof(float); }
 static size_t prolong_smem(const Dev &d) { return ((size_t)d.NIB1 * d.NKB1 + (size_t)d.NIB2 * d.NKB2) * sizeof(float); }
 static size_t update_smem(const Dev &d) { return (size_t)2 * d.IMM1 * d.KMM1 * sizeof(float); }
-static size_t smooth_smem(const Dev &d) { return (size_t)2 * d.IM * d.KM * sizeof(float); }
+static size_t smooth_smem(const Dev &d) { return ((size_t)2 * d.IM * d.KM + 2 * d.IM + 2 * d.KM) * sizeof(float); }
 
 cudaError_t configure_kernels(const Dev &d) {
     struct {
