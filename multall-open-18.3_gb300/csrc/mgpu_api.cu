@@ -394,6 +394,8 @@ int32_t mgpu_create(int32_t im, int32_t jm, int32_t km, int32_t nrows, mgpu_hand
     if (im < 5 || jm < 10 || km < 5 || nrows < 1 || nrows > 64)
         return fail(MGPU_E_ARG, "dimensions out of range (IM,KM >= 5, JM >= 10, 1 <= NROWS <= 64)");
     if (im > 160 || km > 160) return fail(MGPU_E_UNSUPPORTED, "IM and KM above 160 are not covered");
+    if ((int64_t)im * jm * km > (int64_t)1 << 30)
+        return fail(MGPU_E_UNSUPPORTED, "more than 2^30 nodes are not covered (32-bit node indices)");
     mgpu_handle *h = new (std::nothrow) mgpu_handle();
     if (!h) return fail(MGPU_E_NOMEM, "host allocation");
     Dev &d = h->d;

@@ -139,11 +139,13 @@ __host__ __device__ inline size_t ixij(const Dev &d, int i, int j) {
 #define A1(p, x) (p)[(x) - 1]
 
 // Decomposes a linear node index n (I fastest) into 1-based (i, j, k).
+// mgpu_create keeps IM*JM*KM below 2^31, so 32-bit division suffices.
 __device__ inline void node_ijk(const Dev &d, size_t n, int &i, int &j, int &k) {
-    i = (int)(n % (size_t)d.IM) + 1;
-    size_t q = n / (size_t)d.IM;
-    j = (int)(q % (size_t)d.JM) + 1;
-    k = (int)(q / (size_t)d.JM) + 1;
+    const unsigned u = (unsigned)n, im = (unsigned)d.IM, jm = (unsigned)d.JM;
+    const unsigned q = u / im, q2 = q / jm;
+    i = (int)(u - q * im) + 1;
+    j = (int)(q - q2 * jm) + 1;
+    k = (int)q2 + 1;
 }
 
 // Order-preserving key for "largest value, earliest index wins": the value

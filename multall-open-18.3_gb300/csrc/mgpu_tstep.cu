@@ -29,7 +29,9 @@ static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n
 
 constexpr int TS_BS = 256;      // threads per J-plane CTA; 4 CTAs resident per SM
 constexpr int TS_U = 3;          // cells per thread whose loads are issued together
+constexpr int TS_UG = 4;         // the same for the damping and gather phases of update
 constexpr int SV_BS = 256;
+constexpr int SV_U = 3;          // points per thread whose streamwise loads are issued together
 
 template <int BS>
 __device__ inline double block_sum(double v, double *sh) {
@@ -450,13 +452,24 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_update(const __grid_constant__ 
         const float *__restrict__ stp = V.ST + (size_t)IM * (jc - 1);     // plane jc, (i, k) at i-1 + IM*JM*(k-1)
         const size_t kstride = (size_t)IM * d.JM;
         Walk2 w(IMM1, threadIdx.x, TS_BS);
-        for (int t = threadIdx.x; t < nc; t += TS_BS, w.next()) {
-            float v = stp[(size_t)(w.i - 1) + kstride * (w.k - 1)];
-            if (damp_on) {
-                float FDAMP = fabsf(v) / blk;
-                v = v / (1.0f + FDAMP / DAMP);
+        for (int t0 = threadIdx.x; t0 < nc; t0 += TS_UG * TS_BS) {
+            float sv[TS_UG];
+#pragma unroll
+            for (int u = 0; u < TS_UG; ++u) {
+                if (t0 + u * TS_BS < nc) sv[u] = stp[(size_t)(w.i - 1) + kstride * (w.k - 1)];
+                w.next();
             }
-            c[t] = v;
+#pragma unroll
+            for (int u = 0; u < TS_UG; ++u) {
+                const int t = t0 + u * TS_BS;
+                if (t >= nc) break;
+                float v = sv[u];
+                if (damp_on) {
+                    float FDAMP = fabsf(v) / blk;
+                    v = v / (1.0f + FDAMP / DAMP);
+                }
+                c[t] = v;
+            }
         }
     }
     __syncthreads();
@@ -495,41 +508,63 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_update(const __grid_constant__ 
     const float *__restrict__ FTR = d.FTR;
     const size_t nbase = (size_t)IM * (j - 1), kstride = (size_t)IM * d.JM;
     Walk2 w(IM, threadIdx.x, TS_BS);
-    for (int t = threadIdx.x; t < np; t += TS_BS, w.next()) {
-        const int i = w.i, k = w.k;
-        const size_t n = nbase + (size_t)(i - 1) + kstride * (k - 1);
-        float v = D[n];
-        if (hA && hB && i >= 2 && i <= IMM1 && k >= 2 && k <= KMM1) {
-            // interior node: all eight cells, weights FTR/FTL of row k-1 and FBR/FBL of row k
-            const int lo = (i - 2) + IMM1 * (k - 2), hi = lo + IMM1;       // cells (i-1, k-1), (i-1, k)
-            const float wtr = FTR[(i - 2) + IM * (k - 2)], wtl = FTL[(i - 1) + IM * (k - 2)];
-            const float wbr = FBR[(i - 2) + IM * (k - 1)], wbl = FBL[(i - 1) + IM * (k - 1)];
-            v = v + cA[lo] * wtr * fdn;
-            v = v + cA[lo + 1] * wtl * fdn;
-            v = v + cB[lo] * wtr * fup;
-            v = v + cB[lo + 1] * wtl * fup;
-            v = v + cA[hi] * wbr * fdn;
-            v = v + cA[hi + 1] * wbl * fdn;
-            v = v + cB[hi] * wbr * fup;
-            v = v + cB[hi + 1] * wbl * fup;
-        } else {
-            for (int kc = k - 1; kc <= k; ++kc) {
-                if (kc < 1 || kc > KMM1) continue;
-                for (int h = 0; h < 2; ++h) {
-                    if (!(h ? hB : hA)) continue;
-                    const float *c = h ? cB : cA;
-                    float fac = h ? fup : fdn;
-                    for (int ic = i - 1; ic <= i; ++ic) {
-                        if (ic < 1 || ic > IMM1) continue;
-                        float wt;
-                        if (ic == i) wt = (kc == k) ? AIK(FBL, ic, kc) : AIK(FTL, ic, kc);
-                        else wt = (kc == k) ? AIK(FBR, ic, kc) : AIK(FTR, ic, kc);
-                        v = v + c[(kc - 1) * IMM1 + (ic - 1)] * wt * fac;
-                    }
+    for (int t0 = threadIdx.x; t0 < np; t0 += TS_UG * TS_BS) {
+        // loads of TS_UG nodes first: the node value and, for interior nodes,
+        // the four corner weights
+        float dv[TS_UG], wtr[TS_UG], wtl[TS_UG], wbr[TS_UG], wbl[TS_UG];
+        int ni[TS_UG], nk[TS_UG];
+#pragma unroll
+        for (int u = 0; u < TS_UG; ++u) {
+            const int i = w.i, k = w.k;
+            ni[u] = i;
+            nk[u] = k;
+            w.next();
+            if (t0 + u * TS_BS < np) {
+                dv[u] = D[nbase + (size_t)(i - 1) + kstride * (k - 1)];
+                if (hA && hB && i >= 2 && i <= IMM1 && k >= 2 && k <= KMM1) {
+                    wtr[u] = FTR[(i - 2) + IM * (k - 2)];
+                    wtl[u] = FTL[(i - 1) + IM * (k - 2)];
+                    wbr[u] = FBR[(i - 2) + IM * (k - 1)];
+                    wbl[u] = FBL[(i - 1) + IM * (k - 1)];
                 }
             }
         }
-        V.TM[n] = v;
+#pragma unroll
+        for (int u = 0; u < TS_UG; ++u) {
+            if (t0 + u * TS_BS >= np) break;
+            const int i = ni[u], k = nk[u];
+            const size_t n = nbase + (size_t)(i - 1) + kstride * (k - 1);
+            float v = dv[u];
+            if (hA && hB && i >= 2 && i <= IMM1 && k >= 2 && k <= KMM1) {
+                // interior node: all eight cells, weights FTR/FTL of row k-1 and FBR/FBL of row k
+                const int lo = (i - 2) + IMM1 * (k - 2), hi = lo + IMM1;   // cells (i-1, k-1), (i-1, k)
+                v = v + cA[lo] * wtr[u] * fdn;
+                v = v + cA[lo + 1] * wtl[u] * fdn;
+                v = v + cB[lo] * wtr[u] * fup;
+                v = v + cB[lo + 1] * wtl[u] * fup;
+                v = v + cA[hi] * wbr[u] * fdn;
+                v = v + cA[hi + 1] * wbl[u] * fdn;
+                v = v + cB[hi] * wbr[u] * fup;
+                v = v + cB[hi + 1] * wbl[u] * fup;
+            } else {
+                for (int kc = k - 1; kc <= k; ++kc) {
+                    if (kc < 1 || kc > KMM1) continue;
+                    for (int h = 0; h < 2; ++h) {
+                        if (!(h ? hB : hA)) continue;
+                        const float *c = h ? cB : cA;
+                        float fac = h ? fup : fdn;
+                        for (int ic = i - 1; ic <= i; ++ic) {
+                            if (ic < 1 || ic > IMM1) continue;
+                            float wt;
+                            if (ic == i) wt = (kc == k) ? AIK(FBL, ic, kc) : AIK(FTL, ic, kc);
+                            else wt = (kc == k) ? AIK(FBR, ic, kc) : AIK(FTR, ic, kc);
+                            v = v + c[(kc - 1) * IMM1 + (ic - 1)] * wt * fac;
+                        }
+                    }
+                }
+            }
+            V.TM[n] = v;
+        }
     }
 }
 
@@ -595,34 +630,58 @@ __global__ void __launch_bounds__(SV_BS, 4) k_ts_smooth(const __grid_constant__ 
         const int J1 = A1(d.JSTART, nr), J2 = A1(d.JMIX, nr);
         const float SFX = c->SFX, SFX1 = c->SFX1, SFXB = c->SFXB, SFXB1 = c->SFXB1, SFXBH = c->SFXBH;
         const float SFXHM1 = c->SFXHM1, SFX14 = c->SFX14, F4 = d.FAC_4TH;
-        // plane offsets (in nodes) of the J neighbours each case reads
-        auto pl = [&](int jj) { return (ptrdiff_t)IM * (jj - j); };
+        // the J planes each case reads, as node offsets from plane j
+        int nq = 0;
+        ptrdiff_t off[4] = {0, 0, 0, 0};
+        auto add = [&](int jj) { off[nq++] = (ptrdiff_t)IM * (jj - j); };
+        if (sc == 1) { add(j + 1); add(j - 1); add(j - 2); add(j + 2); }
+        if (sc == 2) { add(J1 + 3); add(J1 + 1); }
+        if (sc == 3) { add(J1 + 2); add(J1 + 3); add(J1 + 4); }
+        if (sc == 4) { add(J2 - 1); add(J2 - 3); }
+        if (sc == 5) { add(J2 - 2); add(J2 - 3); add(J2 - 4); }
         Walk2 w(IM, threadIdx.x, SV_BS);
-        for (int t = threadIdx.x; t < np; t += SV_BS, w.next()) {
-            const int i = w.i, k = w.k;
-            const float *p = Sj + (size_t)(i - 1) + ks * (k - 1);
-            const float d0 = p[0];
-            float v = d0;
-            switch (sc) {
-            case 1: {
-                float AVERG = 0.5f * (p[pl(j + 1)] + p[pl(j - 1)]);
-                float CURV = AVERG - 0.5f * d0 - 0.25f * (p[pl(j - 2)] + p[pl(j + 2)]);
-                v = SFX1 * d0 + SFX * (AVERG + F4 * CURV);
-                break;
+        for (int t0 = threadIdx.x; t0 < np; t0 += SV_U * SV_BS) {
+            float d0[SV_U], x[SV_U][4];
+            int pi[SV_U], pk[SV_U];
+#pragma unroll
+            for (int u = 0; u < SV_U; ++u) {
+                pi[u] = w.i;
+                pk[u] = w.k;
+                w.next();
+                if (t0 + u * SV_BS < np) {
+                    const float *p = Sj + (size_t)(pi[u] - 1) + ks * (pk[u] - 1);
+                    d0[u] = p[0];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        if (q < nq) x[u][q] = p[off[q]];
+                }
             }
-            case 2: v = SFXB1 * d0 + SFXBH * (p[pl(J1 + 3)] + p[pl(J1 + 1)]); break;
-            case 3: v = SFXB1 * d0 + SFXB * (1.25f * p[pl(J1 + 2)] + 0.5f * p[pl(J1 + 3)] - 0.75f * p[pl(J1 + 4)]); break;
-            case 4: v = SFXB1 * d0 + SFXBH * (p[pl(J2 - 1)] + p[pl(J2 - 3)]); break;
-            case 5: v = SFXB1 * d0 + SFXB * (1.25f * p[pl(J2 - 2)] + 0.5f * p[pl(J2 - 3)] - 0.75f * p[pl(J2 - 4)]); break;
-            default: break;
+#pragma unroll
+            for (int u = 0; u < SV_U; ++u) {
+                const int t = t0 + u * SV_BS;
+                if (t >= np) break;
+                const int i = pi[u], k = pk[u];
+                const float dd = d0[u];
+                float v = dd;
+                switch (sc) {
+                case 1: {
+                    float AVERG = 0.5f * (x[u][0] + x[u][1]);
+                    float CURV = AVERG - 0.5f * dd - 0.25f * (x[u][2] + x[u][3]);
+                    v = SFX1 * dd + SFX * (AVERG + F4 * CURV);
+                    break;
+                }
+                case 2: case 4: v = SFXB1 * dd + SFXBH * (x[u][0] + x[u][1]); break;
+                case 3: case 5: v = SFXB1 * dd + SFXB * (1.25f * x[u][0] + 0.5f * x[u][1] - 0.75f * x[u][2]); break;
+                default: break;
+                }
+                if (lc && (i == 1 || i == IM)) {
+                    const float *pkk = Sj + ks * (k - 1);
+                    if (lc == 1) v = SFXHM1 * dd + SFX14 * (pkk[1] + pkk[IMM1 - 1]);
+                    else if (i == 1) v = SFXHM1 * dd + SFX14 * (pkk[IM + 0] + pkk[IM - 1]);
+                    else v = SFXHM1 * dd + SFX14 * (pkk[IM + IM - 1] + pkk[0]);
+                }
+                a[t] = v;
             }
-            if (lc && (i == 1 || i == IM)) {
-                const float *pk = Sj + ks * (k - 1);
-                if (lc == 1) v = SFXHM1 * d0 + SFX14 * (pk[1] + pk[IMM1 - 1]);
-                else if (i == 1) v = SFXHM1 * d0 + SFX14 * (pk[IM + 0] + pk[IM - 1]);
-                else v = SFXHM1 * d0 + SFX14 * (pk[IM + IM - 1] + pk[0]);
-            }
-            a[t] = v;
         }
     }
     __syncthreads();
