@@ -48,8 +48,9 @@ B_ALG_STEP = 132
 #   update  STORE, D read; TMP written
 #   smooth  TMP read; D written
 KERNEL_BYTES = {
-    "k_prim": (48, 1), "k_flux_mass": (60, 1), "k_flux_energy": (40, 1), "k_flux_xmom": (52, 1),
-    "k_flux_rvt": (40, 1), "k_flux_rmom": (64, 1), "k_peff": (8, 1), "k_density_detect": (4, 1),
+    "k_prim": (48, 1), "k_flux_mass": (60, 1), "k_flux_energy": (40, 1),
+    # momentum fluxes: 18 arrays read (PEFF, V*, ROVT, FLOW*, 6 areas, VOLOR, 3 forces), 12 written
+    "k_flux_mom": (120, 1), "k_peff": (8, 1), "k_density_detect": (4, 1),
     "k_mach_limiter": (24, 1),
     "k_ts_cells": (28, 5), "k_ts_prolong": (16, 5), "k_ts_update": (12, 5), "k_ts_smooth": (8, 5),
     "k_loss_kfaces": (72, 0.2), "k_loss_ifaces": (84, 0.2),

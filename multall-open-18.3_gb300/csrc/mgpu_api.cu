@@ -232,14 +232,14 @@ __global__ void k_delay(long long cycles) {
 // two batched TSTEPs, [RO, ROE] and [ROVX, RORVT, ROVR], with the boundary
 // conditions between them; every value is the same as in the serial order.
 void enqueue_core(const Dev &d, Launch L) {
-    launch_flux_mass(d, L);
+    Launch L0 = L;        // follows the LOSS conditional node: plain stream order
+    L0.pdl = false;
+    launch_flux_mass(d, L0);
     launch_flux_energy(d, L);
     launch_tstep(d, L, V_RO, 2);
     launch_bc(d, L);
     launch_peff(d, L);
-    launch_flux_xmom(d, L);
-    launch_flux_rvt(d, L);
-    launch_flux_rmom(d, L);
+    launch_flux_mom(d, L);
     launch_tstep(d, L, V_ROVX, 3);
     launch_limiters(d, L);
     launch_mixplan(d, L);
@@ -315,6 +315,7 @@ int build_graph(mgpu_handle *h) {
         dg.cond_tail = (unsigned long long)ht;
         Launch L{h->stream, h->sm_count, nullptr};
         launch_step_begin(dg, L);
+        L.pdl = true;          // kernel-to-kernel edges of the step are programmatic
         launch_prim(dg, L);
         rc = add_conditional(h, hl, &h->loss_nodes, [&](Launch L2) { launch_loss(dg, L2, false); });
         if (!rc) enqueue_core(dg, L);

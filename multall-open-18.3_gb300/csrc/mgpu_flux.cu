@@ -21,6 +21,7 @@ static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n
 // entry (8088-8112).
 // ---------------------------------------------------------------------
 __global__ void k_step_begin(Dev d) {
+    pdl_wait();
     DevCtl *c = d.ctl;
     int n = c->nstep + 1;
     c->nstep = n;
@@ -68,7 +69,7 @@ __global__ void k_step_begin(Dev d) {
 }
 
 void launch_step_begin(const Dev &d, Launch L) {
-    k_step_begin<<<1, 1, 0, L.s>>>(d);
+    launchk(L, k_step_begin, dim3(1), dim3(1), 0, d);
     mark(L, "k_step_begin");
 }
 
@@ -110,6 +111,7 @@ __device__ inline void block_reduce_sum_key(double s, unsigned long long key, do
 constexpr int PRIM_BS = 256;
 
 __global__ void __launch_bounds__(PRIM_BS) k_prim(Dev d) {
+    pdl_wait();
     size_t n = (size_t)blockIdx.x * PRIM_BS + threadIdx.x;
     size_t N = (size_t)d.IM * d.JM * d.KM;
     int do_tail = d.ctl->do_tail;
@@ -150,7 +152,7 @@ __global__ void __launch_bounds__(PRIM_BS) k_prim(Dev d) {
 
 void launch_prim(const Dev &d, Launch L) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
-    k_prim<<<grid_for(N, PRIM_BS), PRIM_BS, 0, L.s>>>(d);
+    launchk(L, k_prim, dim3(grid_for(N, PRIM_BS)), dim3(PRIM_BS), 0, d);
     mark(L, "k_prim");
 }
 
@@ -169,6 +171,7 @@ __device__ inline float flowt_raw(const Dev &d, int i, int j, int k) {
 }
 
 __global__ void k_flux_mass(Dev d) {
+    pdl_wait();
     size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t N = (size_t)d.IM * d.JM * d.KM;
     if (n >= N) return;
@@ -212,7 +215,7 @@ __global__ void k_flux_mass(Dev d) {
 
 void launch_flux_mass(const Dev &d, Launch L) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
-    k_flux_mass<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+    launchk(L, k_flux_mass, dim3(grid_for(N, 256)), dim3(256), 0, d);
     mark(L, "k_flux_mass");
 }
 
@@ -226,6 +229,7 @@ __device__ inline float tflux_energy_raw(const Dev &d, int i, int j, int k) {
 }
 
 __global__ void k_flux_energy(Dev d) {
+    pdl_wait();
     size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t N = (size_t)d.IM * d.JM * d.KM;
     if (n >= N) return;
@@ -254,7 +258,7 @@ __global__ void k_flux_energy(Dev d) {
 
 void launch_flux_energy(const Dev &d, Launch L) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
-    k_flux_energy<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+    launchk(L, k_flux_energy, dim3(grid_for(N, 256)), dim3(256), 0, d);
     mark(L, "k_flux_energy");
 }
 
@@ -266,7 +270,8 @@ void launch_flux_energy(const Dev &d, Launch L) {
 // (I,K) sets the inlet and exit states.
 // ---------------------------------------------------------------------
 __global__ void __launch_bounds__(1024) k_bc_sums(Dev d) {
-    __shared__ float s_sum[512];
+    pdl_wait();
+    __shared__ float s_sum[512], s_pd[512], s_r[512];
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int k = w + 1; k <= d.KM; k += nw) {
         float PAVG2 = 0.0f, PAVG3 = 0.0f, PAVGOUT = 0.0f, SUM = 0.0f;
@@ -299,24 +304,34 @@ __global__ void __launch_bounds__(1024) k_bc_sums(Dev d) {
             s_sum[k - 1] = SUM;
         }
     }
+    if (d.IPOUT > 0) return;
+    // the recurrence runs on shared copies of PD and R(JM, K): one thread,
+    // no global round trip per K
+    for (int k = threadIdx.x; k < d.KM; k += blockDim.x) {
+        s_pd[k] = d.PD[k];
+        s_r[k] = A2(d.R, d.JM, k + 1);
+    }
     __syncthreads();
-    if (threadIdx.x == 0 && d.IPOUT <= 0) {
+    if (threadIdx.x == 0) {
         float PDIFF = 0.0f;
-        if (d.IPOUT == -1) PDIFF = d.PDOWN_TIP - A1(d.PD, d.KM);
+        if (d.IPOUT == -1) PDIFF = d.PDOWN_TIP - s_pd[d.KM - 1];
         float SUMP = 0.0f;
         for (int k = 1; k <= d.KM; ++k) {
-            A1(d.PD, 1) = d.PDOWN_HUB;
+            s_pd[0] = d.PDOWN_HUB;
             if (k != 1) {
-                float DP = (s_sum[k - 1] + SUMP) * 0.5f * (A2(d.R, d.JM, k) - A2(d.R, d.JM, k - 1));
-                A1(d.PD, k) = 0.9f * A1(d.PD, k) + 0.1f * (A1(d.PD, k - 1) + DP);
+                float DP = (s_sum[k - 1] + SUMP) * 0.5f * (s_r[k - 1] - s_r[k - 2]);
+                s_pd[k - 1] = 0.9f * s_pd[k - 1] + 0.1f * (s_pd[k - 2] + DP);
             }
             SUMP = s_sum[k - 1];
-            if (d.IPOUT == -1) A1(d.PD, k) = A1(d.PD, k) + PDIFF;
+            if (d.IPOUT == -1) s_pd[k - 1] = s_pd[k - 1] + PDIFF;
         }
     }
+    __syncthreads();
+    for (int k = threadIdx.x; k < d.KM; k += blockDim.x) d.PD[k] = s_pd[k];
 }
 
 __global__ void k_bc_apply(Dev d) {
+    pdl_wait();
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= d.IM * d.KM) return;
     int i = t % d.IM + 1, k = t / d.IM + 1;
@@ -394,9 +409,9 @@ __global__ void k_bc_apply(Dev d) {
 }
 
 void launch_bc(const Dev &d, Launch L) {
-    k_bc_sums<<<1, 1024, 0, L.s>>>(d);
+    launchk(L, k_bc_sums, dim3(1), dim3(1024), 0, d);
     mark(L, "k_bc_sums");
-    k_bc_apply<<<(d.IM * d.KM + 127) / 128, 128, 0, L.s>>>(d);
+    launchk(L, k_bc_apply, dim3((d.IM * d.KM + 127) / 128), dim3(128), 0, d);
     mark(L, "k_bc_apply");
 }
 
@@ -404,6 +419,7 @@ void launch_bc(const Dev &d, Launch L) {
 // PEFF = P - PREFF + F_PDOWN*(P(J+1)-P(J))  (4321)
 // ---------------------------------------------------------------------
 __global__ void k_peff(Dev d) {
+    pdl_wait();
     size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t N = (size_t)d.IM * d.JM * d.KM;
     if (n >= N) return;
@@ -416,19 +432,14 @@ __global__ void k_peff(Dev d) {
 
 void launch_peff(const Dev &d, Launch L) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
-    k_peff<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+    launchk(L, k_peff, dim3(grid_for(N, 256)), dim3(256), 0, d);
     mark(L, "k_peff");
 }
 
 // ---------------------------------------------------------------------
 // axial-momentum fluxes (6100-6120) and the cusp balance (6026)
 // ---------------------------------------------------------------------
-__global__ void k_flux_xmom(Dev d) {
-    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t N = (size_t)d.IM * d.JM * d.KM;
-    if (n >= N) return;
-    int i, j, k;
-    node_ijk(d, n, i, j, k);
+__device__ __forceinline__ void flux_xmom_node(const Dev &d, size_t n, int i, int j, int k) {
     const VarSet &V = d.var[V_ROVX];
     const float *PE = d.PEFF, *VX = d.VX;
     if (i < d.IM && k < d.KM) {
@@ -458,11 +469,6 @@ __global__ void k_flux_xmom(Dev d) {
     }
 }
 
-void launch_flux_xmom(const Dev &d, Launch L) {
-    size_t N = (size_t)d.IM * d.JM * d.KM;
-    k_flux_xmom<<<grid_for(N, 256), 256, 0, L.s>>>(d);
-    mark(L, "k_flux_xmom");
-}
 
 // ---------------------------------------------------------------------
 // moment-of-momentum fluxes (6200-6230) and periodic balance (902)
@@ -474,12 +480,7 @@ __device__ inline float tflux_rvt_raw(const Dev &d, int i, int j, int k, float A
     return (A3(d.FLOWT, i, j, k) * AVGVT + A2(d.ABT, j, k) * AVGP) * AVGR;
 }
 
-__global__ void k_flux_rvt(Dev d) {
-    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t N = (size_t)d.IM * d.JM * d.KM;
-    if (n >= N) return;
-    int i, j, k;
-    node_ijk(d, n, i, j, k);
+__device__ __forceinline__ void flux_rvt_node(const Dev &d, size_t n, int i, int j, int k) {
     const VarSet &V = d.var[V_RORVT];
     const float *VT = d.VT;
     if (i < d.IM && k < d.KM) {
@@ -505,11 +506,6 @@ __global__ void k_flux_rvt(Dev d) {
     }
 }
 
-void launch_flux_rvt(const Dev &d, Launch L) {
-    size_t N = (size_t)d.IM * d.JM * d.KM;
-    k_flux_rvt<<<grid_for(N, 256), 256, 0, L.s>>>(d);
-    mark(L, "k_flux_rvt");
-}
 
 // ---------------------------------------------------------------------
 // radial-momentum fluxes and source (6300-6330), periodic balance (6260)
@@ -522,12 +518,7 @@ __device__ inline float tflux_rmom_raw(const Dev &d, int i, int j, int k, float 
     return 0.25f * (A3(d.FLOWT, i, j, k) * AVGVR + AVGP * A3(d.ABR, i, j, k));
 }
 
-__global__ void k_flux_rmom(Dev d) {
-    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t N = (size_t)d.IM * d.JM * d.KM;
-    if (n >= N) return;
-    int i, j, k;
-    node_ijk(d, n, i, j, k);
+__device__ __forceinline__ void flux_rmom_node(const Dev &d, size_t n, int i, int j, int k) {
     const VarSet &V = d.var[V_ROVR];
     const float *PE = d.PEFF, *VR = d.VR, *VT = d.VT, *RV = d.ROVT;
     if (i < d.IM && k < d.KM) {
@@ -568,10 +559,26 @@ __global__ void k_flux_rmom(Dev d) {
     }
 }
 
-void launch_flux_rmom(const Dev &d, Launch L) {
+
+// The three momentum equations' fluxes in one pass over the nodes: they
+// read the same PEFF, FLOWX/FLOWT/FLOWR and velocities (L1 serves the
+// repeats) and write disjoint per-variable flux sets.
+__global__ void k_flux_mom(Dev d) {
+    pdl_wait();
+    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t N = (size_t)d.IM * d.JM * d.KM;
-    k_flux_rmom<<<grid_for(N, 256), 256, 0, L.s>>>(d);
-    mark(L, "k_flux_rmom");
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, n, i, j, k);
+    flux_xmom_node(d, n, i, j, k);
+    flux_rvt_node(d, n, i, j, k);
+    flux_rmom_node(d, n, i, j, k);
+}
+
+void launch_flux_mom(const Dev &d, Launch L) {
+    size_t N = (size_t)d.IM * d.JM * d.KM;
+    launchk(L, k_flux_mom, dim3(grid_for(N, 256)), dim3(256), 0, d);
+    mark(L, "k_flux_mom");
 }
 
 // ---------------------------------------------------------------------
@@ -588,6 +595,7 @@ __device__ inline bool density_triggers(float ro, float ROAVG, float ROLIM) {
 }
 
 __global__ void k_density_detect(Dev d) {
+    pdl_wait();
     size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t N = (size_t)d.IM * d.JM * d.KM;
     if (n >= N) return;
@@ -600,6 +608,7 @@ __global__ void k_density_detect(Dev d) {
 }
 
 __global__ void k_density_fix(Dev d) {
+    pdl_wait();
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= d.IM * d.KM) return;
     int i = t % d.IM + 1, k = t / d.IM + 1;
@@ -645,6 +654,7 @@ __global__ void k_density_fix(Dev d) {
 
 // Mach-number / relative-mass-flux limiter (7100)
 __global__ void k_mach_limiter(Dev d) {
+    pdl_wait();
     size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t N = (size_t)d.IM * d.JM * d.KM;
     if (n >= N) return;
@@ -674,13 +684,13 @@ __global__ void k_mach_limiter(Dev d) {
 
 void launch_limiters(const Dev &d, Launch L) {
     size_t Nn = (size_t)d.IM * d.JM * d.KM;
-    k_density_detect<<<grid_for(Nn, 256), 256, 0, L.s>>>(d);
+    launchk(L, k_density_detect, dim3(grid_for(Nn, 256)), dim3(256), 0, d);
     mark(L, "k_density_detect");
     int lines = d.IM * d.KM;
-    k_density_fix<<<(lines + 127) / 128, 128, 0, L.s>>>(d);
+    launchk(L, k_density_fix, dim3((lines + 127) / 128), dim3(128), 0, d);
     mark(L, "k_density_fix");
     size_t N = (size_t)d.IM * d.JM * d.KM;
-    k_mach_limiter<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+    launchk(L, k_mach_limiter, dim3(grid_for(N, 256)), dim3(256), 0, d);
     mark(L, "k_mach_limiter");
 }
 
@@ -695,6 +705,7 @@ constexpr int MIX_MAXI = 160;
 constexpr int MIX_BS = 64;
 
 __global__ void __launch_bounds__(MIX_BS) k_mixplan(Dev d) {
+    pdl_wait();
     __shared__ float ALPHAA[MIX_MAXI], GAMA[MIX_MAXI], WREF_JP2[MIX_MAXI], ROREF_JP2[MIX_MAXI], PISENT[MIX_MAXI];
     __shared__ float ROISENT[MIX_MAXI], WMACH_JP2[MIX_MAXI], TISENT[MIX_MAXI], WIS_JP2[MIX_MAXI];
     const int nr = blockIdx.x / d.KM + 1, k = blockIdx.x % d.KM + 1;
@@ -818,7 +829,7 @@ __global__ void __launch_bounds__(MIX_BS) k_mixplan(Dev d) {
 
 void launch_mixplan(const Dev &d, Launch L) {
     if (!(d.IFMIX > 0 && d.RFMIX > 1.0e-3f) || d.NRWSM1 <= 0) return;
-    k_mixplan<<<d.NRWSM1 * d.KM, MIX_BS, 0, L.s>>>(d);
+    launchk(L, k_mixplan, dim3(d.NRWSM1 * d.KM), dim3(MIX_BS), 0, d);
     mark(L, "k_mixplan");
 }
 

@@ -171,7 +171,31 @@ struct Launch {
     cudaStream_t s;
     int sm_count;
     Prof *prof = nullptr;
+    // programmatic dependent launch: the kernel may be scheduled while its
+    // predecessor in the stream drains; every kernel calls pdl_wait() before
+    // it touches memory, which returns once the predecessor has completed
+    // and its writes are visible
+    bool pdl = false;
 };
+
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline void launchk(const Launch &L, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = L.s;
+    cudaLaunchAttribute at[1];
+    if (L.pdl) {
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+    }
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
 
 inline void mark(const Launch &L, const char *name) {
     if (L.prof && L.prof->n < Prof::MAXEV) {
@@ -188,9 +212,7 @@ void launch_flux_mass(const Dev &d, Launch L);
 void launch_flux_energy(const Dev &d, Launch L);
 void launch_bc(const Dev &d, Launch L);
 void launch_peff(const Dev &d, Launch L);
-void launch_flux_xmom(const Dev &d, Launch L);
-void launch_flux_rvt(const Dev &d, Launch L);
-void launch_flux_rmom(const Dev &d, Launch L);
+void launch_flux_mom(const Dev &d, Launch L);   // XMOM, RVT and RMOM fluxes
 // TSTEP for the nv variables v0 .. v0+nv-1 of d.var
 void launch_tstep(const Dev &d, Launch L, int v0, int nv);
 void launch_limiters(const Dev &d, Launch L);

@@ -17,6 +17,7 @@ static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n
 
 // viscosity set on entry to LOSS (8088-8112); one thread
 __global__ void k_loss_prologue(Dev d, int init_call) {
+    pdl_wait();
     DevCtl *c = d.ctl;
     if (!init_call && !c->do_loss) return;
     int nstep = init_call ? 1 : c->nstep;
@@ -110,6 +111,7 @@ constexpr int LK_W = 8;            // warps per CTA (K stride)
 constexpr int LK_NARR = 10;        // [K][32] arrays in shared memory (+ RAVG per K)
 
 __global__ void __launch_bounds__(32 * LK_W) k_loss_kfaces(const __grid_constant__ Dev d, int init_call) {
+    pdl_wait();
     const DevCtl *c = d.ctl;
     if (!init_call && !c->do_loss) return;
     extern __shared__ float lsm[];
@@ -336,6 +338,7 @@ __device__ inline bool transition_warp(const float *vt, const float *vl, int a, 
 }
 
 __global__ void __launch_bounds__(32 * LI_W) k_loss_ifaces(const __grid_constant__ Dev d, int init_call) {
+    pdl_wait();
     const DevCtl *c = d.ctl;
     if (!init_call && !c->do_loss) return;
     extern __shared__ float lsm[];
@@ -548,13 +551,13 @@ cudaError_t configure_loss_kernels(const Dev &d) {
 }
 
 void launch_loss(const Dev &d, Launch L, bool init_call) {
-    k_loss_prologue<<<1, 1, 0, L.s>>>(d, init_call ? 1 : 0);
+    launchk(L, k_loss_prologue, dim3(1), dim3(1), 0, d, init_call ? 1 : 0);
     mark(L, "k_loss_prologue");
     dim3 gk((unsigned)((d.IMM1 + 31) / 32), (unsigned)(d.JM - 1));
-    k_loss_kfaces<<<gk, dim3(32, LK_W), loss_kfaces_smem(d), L.s>>>(d, init_call ? 1 : 0);
+    launchk(L, k_loss_kfaces, dim3(gk), dim3(32, LK_W), loss_kfaces_smem(d), d, init_call ? 1 : 0);
     mark(L, "k_loss_kfaces");
     int nl = (d.JM - 1) * d.KMM1;
-    k_loss_ifaces<<<(nl + LI_W - 1) / LI_W, 32 * LI_W, loss_ifaces_smem(d), L.s>>>(d, init_call ? 1 : 0);
+    launchk(L, k_loss_ifaces, dim3((nl + LI_W - 1) / LI_W), dim3(32 * LI_W), loss_ifaces_smem(d), d, init_call ? 1 : 0);
     mark(L, "k_loss_ifaces");
 }
 
@@ -565,6 +568,7 @@ void launch_loss(const Dev &d, Launch L, bool init_call) {
 constexpr int TAIL_BS = 256;
 
 __global__ void __launch_bounds__(TAIL_BS) k_tail_flow(Dev d) {
+    pdl_wait();
     if (!d.ctl->do_tail) return;
     int j = blockIdx.x + 1;
     int ncell = d.IMM1 * d.KMM1;
@@ -586,6 +590,7 @@ __global__ void __launch_bounds__(TAIL_BS) k_tail_flow(Dev d) {
 
 // finishes the |W|^2 reduction of k_prim: VREF and VMAX
 __global__ void k_tail_vref(Dev d, int nparts) {
+    pdl_wait();
     DevCtl *c = d.ctl;
     if (!c->do_tail) return;
     double s = 0.0;
@@ -631,6 +636,7 @@ __global__ void k_tail_vref(Dev d, int nparts) {
 }
 
 __global__ void __launch_bounds__(TAIL_BS) k_tail_dvm(Dev d) {
+    pdl_wait();
     const DevCtl *c = d.ctl;
     if (!c->do_tail) return;
     size_t n = (size_t)blockIdx.x * TAIL_BS + threadIdx.x;
@@ -688,6 +694,7 @@ __global__ void __launch_bounds__(TAIL_BS) k_tail_dvm(Dev d) {
 }
 
 __global__ void k_tail_final(Dev d, int nparts) {
+    pdl_wait();
     DevCtl *c = d.ctl;
     if (!c->do_tail) return;
     double s = 0.0;
@@ -757,16 +764,16 @@ __global__ void k_tail_final(Dev d, int nparts) {
 }
 
 void launch_tail(const Dev &d, Launch L) {
-    k_tail_flow<<<d.JM, TAIL_BS, 0, L.s>>>(d);
+    launchk(L, k_tail_flow, dim3(d.JM), dim3(TAIL_BS), 0, d);
     mark(L, "k_tail_flow");
     size_t N = (size_t)d.IM * d.JM * d.KM;
     int prim_parts = (int)grid_for(N, 256);
-    k_tail_vref<<<1, 1024, 0, L.s>>>(d, prim_parts);
+    launchk(L, k_tail_vref, dim3(1), dim3(1024), 0, d, prim_parts);
     mark(L, "k_tail_vref");
     int parts = (int)grid_for(N, TAIL_BS);
-    k_tail_dvm<<<parts, TAIL_BS, 0, L.s>>>(d);
+    launchk(L, k_tail_dvm, dim3(parts), dim3(TAIL_BS), 0, d);
     mark(L, "k_tail_dvm");
-    k_tail_final<<<1, 1024, 0, L.s>>>(d, parts);
+    launchk(L, k_tail_final, dim3(1), dim3(1024), 0, d, parts);
     mark(L, "k_tail_final");
 }
 
@@ -774,6 +781,7 @@ void launch_tail(const Dev &d, Launch L) {
 // STEPUP(RELAX) (7916-8002): local time step ~ c/(|W|+c), relaxed
 // ---------------------------------------------------------------------
 __global__ void k_stepup_node(Dev d, int gated) {
+    pdl_wait();
     if (gated && !d.ctl->do_tail) return;
     size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t N = (size_t)d.IM * d.JM * d.KM;
@@ -808,6 +816,7 @@ __device__ inline float stepup_cell(const Dev &d, int i, int j, int k, float REL
 }
 
 __global__ void k_stepup_cell(Dev d, float RELAX, int gated) {
+    pdl_wait();
     if (gated && !d.ctl->do_tail) return;
     size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t N = (size_t)d.IM * d.JM * d.KM;
@@ -829,6 +838,7 @@ __global__ void k_stepup_cell(Dev d, float RELAX, int gated) {
 }
 
 __global__ void k_stepup_store(Dev d, int gated) {
+    pdl_wait();
     if (gated && !d.ctl->do_tail) return;
     size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t N = (size_t)d.IM * d.JM * d.KM;
@@ -843,11 +853,11 @@ __global__ void k_stepup_store(Dev d, int gated) {
 void launch_stepup(const Dev &d, Launch L, float relax, bool gated) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
     unsigned g = grid_for(N, 256);
-    k_stepup_node<<<g, 256, 0, L.s>>>(d, gated ? 1 : 0);
+    launchk(L, k_stepup_node, dim3(g), dim3(256), 0, d, gated ? 1 : 0);
     mark(L, "k_stepup_node");
-    k_stepup_cell<<<g, 256, 0, L.s>>>(d, relax, gated ? 1 : 0);
+    launchk(L, k_stepup_cell, dim3(g), dim3(256), 0, d, relax, gated ? 1 : 0);
     mark(L, "k_stepup_cell");
-    k_stepup_store<<<g, 256, 0, L.s>>>(d, gated ? 1 : 0);
+    launchk(L, k_stepup_store, dim3(g), dim3(256), 0, d, gated ? 1 : 0);
     mark(L, "k_stepup_store");
 }
 
@@ -855,6 +865,7 @@ void launch_stepup(const Dev &d, Launch L, float relax, bool gated) {
 // EFICOOL node quantities (5610) and SUMFLX mass averages per J, FP64
 // ---------------------------------------------------------------------
 __global__ void k_int_node(Dev d) {
+    pdl_wait();
     size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t N = (size_t)d.IM * d.JM * d.KM;
     if (n >= N) return;
@@ -873,6 +884,7 @@ __global__ void k_int_node(Dev d) {
 }
 
 __global__ void __launch_bounds__(TAIL_BS) k_int_sum(Dev d, double *out) {
+    pdl_wait();
     int j = blockIdx.x + 1;
     int ncell = d.IMM1 * d.KMM1;
     double bf = 0, spo = 0, sto = 0, sps = 0;
@@ -904,9 +916,9 @@ __global__ void __launch_bounds__(TAIL_BS) k_int_sum(Dev d, double *out) {
 
 void launch_integrals(const Dev &d, Launch L, double *out) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
-    k_int_node<<<grid_for(N, 256), 256, 0, L.s>>>(d);
+    launchk(L, k_int_node, dim3(grid_for(N, 256)), dim3(256), 0, d);
     mark(L, "k_int_node");
-    k_int_sum<<<d.JM, TAIL_BS, 0, L.s>>>(d, out);
+    launchk(L, k_int_sum, dim3(d.JM), dim3(TAIL_BS), 0, d, out);
     mark(L, "k_int_sum");
 }
 

@@ -86,6 +86,7 @@ struct Walk2 {
 // sum), 1750 (MP redistribution) and the multigrid partial sums
 // ---------------------------------------------------------------------
 __global__ void __launch_bounds__(TS_BS, 4) k_ts_cells(const __grid_constant__ Dev d, int v0) {
+    pdl_wait();
     extern __shared__ float sm[];
     const VarSet &V = d.var[v0 + blockIdx.y];
     float *__restrict__ DIFF = V.DIFF;
@@ -218,6 +219,7 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_cells(const __grid_constant__ D
 // its cells in the (K,J,I) loop order of 700; superblocks likewise
 // ---------------------------------------------------------------------
 __global__ void k_ts_restrict_seq(const __grid_constant__ Dev d, int v0) {
+    pdl_wait();
     const VarSet &V = d.var[v0 + blockIdx.y];
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     int n1 = d.NIB1 * (d.NJB1 + 1) * d.NKB1;
@@ -255,6 +257,7 @@ __global__ void k_ts_restrict_seq(const __grid_constant__ Dev d, int v0) {
 // prolong: 1500, with the block sums assembled from the plane partials
 // ---------------------------------------------------------------------
 __global__ void __launch_bounds__(TS_BS, 4) k_ts_prolong(const __grid_constant__ Dev d, int v0, int want_abs) {
+    pdl_wait();
     extern __shared__ float sm[];
     const VarSet &V = d.var[v0 + blockIdx.y];
     __shared__ double shd[TS_BS / 32];
@@ -353,6 +356,7 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_prolong(const __grid_constant__
 
 // per-J-plane sum of |STORE| (after residual smoothing)
 __global__ void __launch_bounds__(TS_BS, 4) k_ts_plane_abs(const __grid_constant__ Dev d, int v0) {
+    pdl_wait();
     __shared__ double shd[TS_BS / 32];
     const VarSet &V = d.var[v0 + blockIdx.y];
     int j = blockIdx.x + 2;
@@ -368,6 +372,7 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_plane_abs(const __grid_constant
 
 // AVG_CHG / AVG_BLK with the reference's sequential REAL*4 sum (1501-1515)
 __global__ void k_ts_avgblk_seq(const __grid_constant__ Dev d, int v0) {
+    pdl_wait();
     __shared__ float chg[64];
     const VarSet &V = d.var[v0 + blockIdx.y];
     if (!d.ctl->damp_on) return;
@@ -401,6 +406,7 @@ __global__ void k_ts_avgblk_seq(const __grid_constant__ Dev d, int v0) {
 // update: negative feedback, second MP average, corner gather -> TMP
 // ---------------------------------------------------------------------
 __global__ void __launch_bounds__(TS_BS, 4) k_ts_update(const __grid_constant__ Dev d, int v0) {
+    pdl_wait();
     extern __shared__ float sm[];
     const VarSet &V = d.var[v0 + blockIdx.y];
     const float *__restrict__ D = V.D;
@@ -602,6 +608,7 @@ __device__ inline int le_case(const Dev &d, int j) {
 }
 
 __global__ void __launch_bounds__(SV_BS, 4) k_ts_smooth(const __grid_constant__ Dev d, int v0) {
+    pdl_wait();
     extern __shared__ float sm[];
     const VarSet &V = d.var[v0 + blockIdx.y];
     const float *__restrict__ S = V.TM;
@@ -817,6 +824,7 @@ __global__ void __launch_bounds__(SV_BS, 4) k_ts_smooth(const __grid_constant__ 
 // changes inside each row, src -> dst (cells outside every row are copied)
 // ---------------------------------------------------------------------
 __global__ void k_resid_pass(const __grid_constant__ Dev d, int v0, int dir, float smfac, int st_to_tm) {
+    pdl_wait();
     const VarSet &V = d.var[v0 + blockIdx.y];
     const float *__restrict__ src = st_to_tm ? V.ST : V.TM;
     float *__restrict__ dst = st_to_tm ? V.TM : V.ST;
@@ -856,6 +864,7 @@ __global__ void k_resid_pass(const __grid_constant__ Dev d, int v0, int dir, flo
 
 // STORE = TMP after the three SMOOTH_RESID passes
 __global__ void k_copy_tm_st(const __grid_constant__ Dev d, int v0, size_t n) {
+    pdl_wait();
     const VarSet &V = d.var[v0 + blockIdx.y];
     size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) V.ST[t] = V.TM[t];
@@ -888,38 +897,38 @@ void launch_tstep(const Dev &d, Launch L, int v0, int nv) {
     unsigned gN = grid_for(N, 256);
     const bool seq = d.REDUCE_ORDER == 1;
     const unsigned jp = (unsigned)(d.JM - 1), ja = (unsigned)d.JM, vy = (unsigned)nv;
-    k_ts_cells<<<dim3(jp, vy), TS_BS, cells_smem(d), L.s>>>(d, v0);
+    launchk(L, k_ts_cells, dim3(jp, vy), dim3(TS_BS), cells_smem(d), d, v0);
     mark(L, "k_ts_cells");
     if (seq) {
         int nb = d.NIB1 * (d.NJB1 + 1) * d.NKB1 + d.NIB2 * (d.NJB2 + 1) * d.NKB2 + d.NSBLK;
-        k_ts_restrict_seq<<<dim3(grid_for(nb, 64), vy), 64, 0, L.s>>>(d, v0);
+        launchk(L, k_ts_restrict_seq, dim3(grid_for(nb, 64), vy), dim3(64), 0, d, v0);
         mark(L, "k_ts_restrict_seq");
     }
-    k_ts_prolong<<<dim3(jp, vy), TS_BS, prolong_smem(d), L.s>>>(d, v0, (d.NRSMTH == 0 && !seq) ? 1 : 0);
+    launchk(L, k_ts_prolong, dim3(jp, vy), dim3(TS_BS), prolong_smem(d), d, v0, (d.NRSMTH == 0 && !seq) ? 1 : 0);
     mark(L, "k_ts_prolong");
     if (d.NRSMTH > 0) {
         for (int it = 0; it < d.NRSMTH; ++it) {
-            k_resid_pass<<<dim3(gN, vy), 256, 0, L.s>>>(d, v0, 0, d.RSMTH, 1);
+            launchk(L, k_resid_pass, dim3(gN, vy), dim3(256), 0, d, v0, 0, d.RSMTH, 1);
             mark(L, "k_resid_pass");
-            k_resid_pass<<<dim3(gN, vy), 256, 0, L.s>>>(d, v0, 1, d.RSMTH, 0);
+            launchk(L, k_resid_pass, dim3(gN, vy), dim3(256), 0, d, v0, 1, d.RSMTH, 0);
             mark(L, "k_resid_pass");
-            k_resid_pass<<<dim3(gN, vy), 256, 0, L.s>>>(d, v0, 2, d.RSMTH, 1);
+            launchk(L, k_resid_pass, dim3(gN, vy), dim3(256), 0, d, v0, 2, d.RSMTH, 1);
             mark(L, "k_resid_pass");
-            k_copy_tm_st<<<dim3(gN, vy), 256, 0, L.s>>>(d, v0, N);
+            launchk(L, k_copy_tm_st, dim3(gN, vy), dim3(256), 0, d, v0, N);
             mark(L, "k_copy_tm_st");
         }
         if (!seq) {
-            k_ts_plane_abs<<<dim3(jp, vy), TS_BS, 0, L.s>>>(d, v0);
+            launchk(L, k_ts_plane_abs, dim3(jp, vy), dim3(TS_BS), 0, d, v0);
             mark(L, "k_ts_plane_abs");
         }
     }
     if (seq) {
-        k_ts_avgblk_seq<<<dim3(1, vy), 32, 0, L.s>>>(d, v0);
+        launchk(L, k_ts_avgblk_seq, dim3(1, vy), dim3(32), 0, d, v0);
         mark(L, "k_ts_avgblk_seq");
     }
-    k_ts_update<<<dim3(ja, vy), TS_BS, update_smem(d), L.s>>>(d, v0);
+    launchk(L, k_ts_update, dim3(ja, vy), dim3(TS_BS), update_smem(d), d, v0);
     mark(L, "k_ts_update");
-    k_ts_smooth<<<dim3(ja, vy), SV_BS, smooth_smem(d), L.s>>>(d, v0);
+    launchk(L, k_ts_smooth, dim3(ja, vy), dim3(SV_BS), smooth_smem(d), d, v0);
     mark(L, "k_ts_smooth");
 }
 
