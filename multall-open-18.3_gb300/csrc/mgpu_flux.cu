@@ -271,38 +271,34 @@ void launch_flux_energy(const Dev &d, Launch L) {
 // ---------------------------------------------------------------------
 __global__ void __launch_bounds__(1024) k_bc_sums(Dev d) {
     pdl_wait();
+    // per warp: the four pitchwise terms of one K line, [4][IMM1]
+    extern __shared__ float bsm[];
     __shared__ float s_sum[512], s_pd[512], s_r[512];
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int IMM1 = d.IMM1;
+    float *tt = bsm + (size_t)w * 4 * IMM1;
     for (int k = w + 1; k <= d.KM; k += nw) {
-        float PAVG2 = 0.0f, PAVG3 = 0.0f, PAVGOUT = 0.0f, SUM = 0.0f;
-        float RJM = A2(d.R, d.JM, k);
-        for (int i0 = 1; i0 <= d.IMM1; i0 += 32) {
-            int i = i0 + l;
-            float t2 = 0.f, t3 = 0.f, to = 0.f, ts = 0.f;
-            if (i <= d.IMM1) {
-                float fp = A1(d.FP, i);
-                t2 = 0.5f * (A3(d.P, i, 2, k) + A3(d.P, i + 1, 2, k)) * fp;
-                t3 = 0.5f * (A3(d.P, i, 3, k) + A3(d.P, i + 1, 3, k)) * fp;
-                to = 0.5f * (A3(d.P, i, d.JMM1, k) + A3(d.P, i + 1, d.JMM1, k)) * fp;
-                ts = 0.5f * fp * (A3(d.ROVT, i, d.JM, k) * A3(d.VT, i, d.JM, k) + A3(d.ROVT, i + 1, d.JM, k) * A3(d.VT, i + 1, d.JM, k)) /
-                     RJM;
-            }
-            int cnt = d.IMM1 - i0 + 1 < 32 ? d.IMM1 - i0 + 1 : 32;
-            for (int q = 0; q < cnt; ++q) {
-                float a2 = __shfl_sync(0xffffffffu, t2, q), a3 = __shfl_sync(0xffffffffu, t3, q);
-                float ao = __shfl_sync(0xffffffffu, to, q), as = __shfl_sync(0xffffffffu, ts, q);
-                PAVG2 = PAVG2 + a2;
-                PAVG3 = PAVG3 + a3;
-                PAVGOUT = PAVGOUT + ao;
-                SUM = SUM + as;
-            }
+        const float RJM = A2(d.R, d.JM, k);
+        for (int i = l + 1; i <= IMM1; i += 32) {
+            float fp = A1(d.FP, i);
+            tt[i - 1] = 0.5f * (A3(d.P, i, 2, k) + A3(d.P, i + 1, 2, k)) * fp;
+            tt[IMM1 + i - 1] = 0.5f * (A3(d.P, i, 3, k) + A3(d.P, i + 1, 3, k)) * fp;
+            tt[2 * IMM1 + i - 1] = 0.5f * (A3(d.P, i, d.JMM1, k) + A3(d.P, i + 1, d.JMM1, k)) * fp;
+            tt[3 * IMM1 + i - 1] = 0.5f * fp *
+                                   (A3(d.ROVT, i, d.JM, k) * A3(d.VT, i, d.JM, k) +
+                                    A3(d.ROVT, i + 1, d.JM, k) * A3(d.VT, i + 1, d.JM, k)) /
+                                   RJM;
         }
-        if (l == 0) {
-            d.BCBUF[k - 1] = PAVG2;
-            d.BCBUF[d.KM + k - 1] = PAVG3;
-            d.BCBUF[2 * d.KM + k - 1] = PAVGOUT;
-            s_sum[k - 1] = SUM;
+        __syncwarp();
+        // lanes 0..3 each add one term over I in the reference's order
+        if (l < 4) {
+            const float *t = tt + l * IMM1;
+            float sum = 0.0f;
+            for (int i = 0; i < IMM1; ++i) sum = sum + t[i];
+            if (l < 3) d.BCBUF[l * d.KM + k - 1] = sum;   // PAVG2, PAVG3, PAVGOUT
+            else s_sum[k - 1] = sum;
         }
+        __syncwarp();
     }
     if (d.IPOUT > 0) return;
     // the recurrence runs on shared copies of PD and R(JM, K): one thread,
@@ -408,8 +404,16 @@ __global__ void k_bc_apply(Dev d) {
     A3(d.ROE, i, d.JM, k) = roe_ * (d.CV * TEXIT + EKE);
 }
 
+static size_t bc_sums_smem(const Dev &d) { return (size_t)32 * 4 * d.IMM1 * sizeof(float); }
+
+cudaError_t configure_flux_kernels(const Dev &d) {
+    size_t b = bc_sums_smem(d);
+    return cudaFuncSetAttribute((const void *)k_bc_sums, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(b > 48 * 1024 ? b : 48 * 1024));
+}
+
 void launch_bc(const Dev &d, Launch L) {
-    launchk(L, k_bc_sums, dim3(1), dim3(1024), 0, d);
+    launchk(L, k_bc_sums, dim3(1), dim3(1024), bc_sums_smem(d), d);
     mark(L, "k_bc_sums");
     launchk(L, k_bc_apply, dim3((d.IM * d.KM + 127) / 128), dim3(128), 0, d);
     mark(L, "k_bc_apply");

@@ -118,18 +118,15 @@ struct Dev {
     unsigned long long cond_loss, cond_tail;
 };
 
-__host__ __device__ inline size_t ix3(const Dev &d, int i, int j, int k) {
-    return (size_t)(i - 1) + (size_t)d.IM * ((size_t)(j - 1) + (size_t)d.JM * (size_t)(k - 1));
+// Element offsets in 32-bit int: mgpu_create keeps IM*JM*KM below 2^30,
+// and signed arithmetic lets the compiler share one node's offset among its
+// neighbours (i+1, j-1, k+1 ... differ by constants).
+__host__ __device__ inline int ix3(const Dev &d, int i, int j, int k) {
+    return (i - 1) + d.IM * ((j - 1) + d.JM * (k - 1));
 }
-__host__ __device__ inline size_t ix2(const Dev &d, int j, int k) {
-    return (size_t)(j - 1) + (size_t)d.JM * (size_t)(k - 1);
-}
-__host__ __device__ inline size_t ixik(const Dev &d, int i, int k) {
-    return (size_t)(i - 1) + (size_t)d.IM * (size_t)(k - 1);
-}
-__host__ __device__ inline size_t ixij(const Dev &d, int i, int j) {
-    return (size_t)(i - 1) + (size_t)d.IM * (size_t)(j - 1);
-}
+__host__ __device__ inline int ix2(const Dev &d, int j, int k) { return (j - 1) + d.JM * (k - 1); }
+__host__ __device__ inline int ixik(const Dev &d, int i, int k) { return (i - 1) + d.IM * (k - 1); }
+__host__ __device__ inline int ixij(const Dev &d, int i, int j) { return (i - 1) + d.IM * (j - 1); }
 
 // 1-based accessors used by the kernels, e.g. A3(d.RO, i, j, k)
 #define A3(p, i, j, k) (p)[ix3(d, (i), (j), (k))]
@@ -225,6 +222,7 @@ void launch_integrals(const Dev &d, Launch L, double *out8);
 // and of the LOSS kernels)
 cudaError_t configure_kernels(const Dev &d);
 cudaError_t configure_loss_kernels(const Dev &d);
+cudaError_t configure_flux_kernels(const Dev &d);
 
 // Read-only view of a handle, for entry points defined outside mgpu_api.cu.
 struct HandleView {

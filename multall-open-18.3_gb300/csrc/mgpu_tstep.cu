@@ -889,7 +889,8 @@ cudaError_t configure_kernels(const Dev &d) {
         cudaError_t e = cudaFuncSetAttribute(x.f, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
         if (e != cudaSuccess) return e;
     }
-    return configure_loss_kernels(d);
+    cudaError_t e = configure_loss_kernels(d);
+    return e != cudaSuccess ? e : configure_flux_kernels(d);
 }
 
 void launch_tstep(const Dev &d, Launch L, int v0, int nv) {
