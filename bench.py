@@ -34,8 +34,21 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "multall-open-18.3_gb300"))
 
 METRIC = "Gnode-iter/s"
-WORKLOAD = ("single-stage axial turbine 65x242x49 (121 J per row), nozzle 48 vanes + rotor 60 blades "
-            "9000 rpm, 1% tip gap, mixing plane, 3-level multigrid, SCREE, mixing-length LOSS/5 steps")
+WORKLOADS = {
+    "stage": ("turbine_stage",
+              "single-stage axial turbine 65x242x49 (121 J per row), nozzle 48 vanes + rotor 60 blades "
+              "9000 rpm, 1% tip gap, mixing plane, 3-level multigrid, SCREE, mixing-length LOSS/5 steps"),
+    "compressor": ("compressor_4stage",
+                   "4-stage axial compressor 73x752x57, 8 rows (36..64 blades) 12000 rpm, mixing planes "
+                   "between all rows, 3-level multigrid, SCREE, mixing-length LOSS/5 steps"),
+    "nozzle": ("nozzle_row",
+               "axial turbine nozzle row 37x97x33, 48 vanes, 3-level multigrid (level 2 off), SCREE, "
+               "mixing-length LOSS/5 steps"),
+    "batch64": ("batch_instance",
+                "64 single-stage turbines in one batch graph: I in {33,49,65}, K in {33,49}, J in [97,161], "
+                "exit P/P0 in [0.45,0.70], 7000-10000 rpm (seeded), SCREE, mixing-length LOSS/5 steps"),
+}
+BATCH = 64
 # Compulsory traffic of one LOOP iteration per node (FP32), every array read
 # once and written once: 5 state arrays r+w (40 B), 5 SCREE histories r+w
 # (40 B), 9 geometry arrays r (36 B), 4 body forces r (16 B).
@@ -56,6 +69,7 @@ KERNEL_BYTES = {
     "k_loss_kfaces": (72, 0.2), "k_loss_ifaces": (84, 0.2),
 }
 PROFILE_STEPS = 10
+ARGS_WORKLOAD = "stage"
 
 
 def env_int(name, default):
@@ -168,7 +182,9 @@ def dist_barrier(dist):
 
 def build_case():
     from mgpu import case, common_setup
-    spec = case.turbine_stage()
+    if ARGS_WORKLOAD == "batch64":          # one member stands for the batch on the CPU
+        return common_setup.build_common(case.batch_instance(0))
+    spec = getattr(case, WORKLOADS[ARGS_WORKLOAD][0])()
     return common_setup.build_common(spec)
 
 
@@ -200,13 +216,91 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": rate, "unit": METRIC, "n_gpus": args.gpus,
         "steps": n, "warmup": 1, "ms_per_step": dt / n * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "nodes": cd.nodes(), "parallelism": "serial CPU (the reference is serial)"},
+        "config": {"workload": WORKLOADS[ARGS_WORKLOAD][1], "nodes": cd.nodes(),
+                   "parallelism": "serial CPU (the reference is serial)"},
         "cpu_baseline": {"value": rate, "unit": METRIC, "cores": 1, "kind": "port",
                          "sample": f"{n} LOOP iterations of the workload after 1 warm-up, serial C++ restatement "
                                    f"(oracle) built -O2 -ffp-contract=off, {dt:.1f} s"},
         "e2e": {"value": rate, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+    return 0
+
+
+def _build_instance(seed):
+    from mgpu import case, common_setup
+    return common_setup.build_common(case.batch_instance(seed))
+
+
+def run_batch(args, rank, world, local_rank):
+    """The 64-instance batch: one graph launch steps every instance."""
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local_rank)
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    # host-side set-up of the 64 decks in a spawn pool, before any GPU call
+    with ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn")) as ex:
+        cds = list(ex.map(_build_instance, range(BATCH)))
+    dist = dist_setup(world, rank)
+    from mgpu import lib
+    nodes = sum(cd.nodes() for cd in cds)
+    probs = [lib.Problem(cd) for cd in cds]
+    batch = lib.Batch(probs)
+    batch.run(max(args.warmup, 3))
+    dist_barrier(dist)
+    with ClockSampler(0) as clk:
+        ms = batch.bench_steps(args.steps, flush_l2=True)
+    dist_barrier(dist)
+    ms_max = dist_max(dist, ms)
+    value = nodes * args.steps * world / (ms_max / 1e3) / 1e9
+    # the same instances one after another, each from its own step graph
+    nseq = max(5, args.steps // 10)
+    seq_ms = sum(p.bench_steps(nseq, flush_l2=True) for p in probs)
+    seq_value = nodes * nseq / (seq_ms / 1e3) / 1e9
+    # end to end: flow state of every instance in from host buffers, batch
+    # steps with the control blocks read back, state out
+    state = ["RO", "ROVX", "ROVR", "RORVT", "ROE"]
+    host = [{n: p.get(n) for n in state} for p in probs]
+    ne = max(1, args.steps // 2)
+    dist_barrier(dist)
+    t0 = time.perf_counter()
+    for p, hd in zip(probs, host):
+        for n in state:
+            p.set(n, hd[n])
+    batch.run(ne)
+    for p in probs:
+        for n in state:
+            p.get(n)
+    t1 = time.perf_counter()
+    e2e_s = dist_max(dist, t1 - t0)
+    state_bytes = sum(a.nbytes for hd in host for a in hd.values())
+    peak, peak_kind = load_peaks()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOADS["batch64"][1], "instances": BATCH, "nodes": nodes,
+                       "l2": "flushed between timed steps", "parallelism": f"replicas: one batch per GPU x{world}",
+                       "reductions": "FP64 tree sums (REDUCE_ORDER=0)"},
+            "roofline": {"bound": "hbm", "kernel": None, "peak": peak, "unit": "GB/s", "peak_source": peak_kind,
+                         "step": {"alg_bytes_per_node_iter": B_ALG_STEP, "achieved": value / world * B_ALG_STEP,
+                                  "frac": value / world * B_ALG_STEP / peak}},
+            "sequential": {"value": seq_value, "unit": METRIC, "steps": nseq,
+                           "how": "the same 64 instances stepped one after another, each from its own graph"},
+            "cpu_baseline": None,
+            "clocks": clk.summary(),
+            "e2e": {"value": nodes * ne * world / e2e_s / 1e9, "unit": METRIC,
+                    "h2d_bytes_per_step": state_bytes / ne, "d2h_bytes_per_step": state_bytes / ne,
+                    "steps": ne, "how": "mgpu_batch_run over all steps (control blocks read back every 50), "
+                                        "every instance's flow state uploaded before and downloaded after"},
+        }
+        print(json.dumps(line), flush=True)
+    batch.close()
+    for p in probs:
+        p.close()
+    if dist is not None:
+        dist.destroy_process_group()
     return 0
 
 
@@ -280,7 +374,7 @@ def run_gpu(args, rank, world, local_rank):
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "nodes": N, "l2": "flushed between timed steps",
+            "config": {"workload": WORKLOADS[ARGS_WORKLOAD][1], "nodes": N, "l2": "flushed between timed steps",
                        "parallelism": f"replicas: one instance per GPU x{world}",
                        "reductions": "FP64 tree sums (REDUCE_ORDER=0)"},
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -319,12 +413,18 @@ def main():
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-out", default=None)
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="stage",
+                    help="the headline workload is the single-stage turbine; the others are extra lines")
     args = ap.parse_args()
+    global ARGS_WORKLOAD
+    ARGS_WORKLOAD = args.workload
     rank = env_int("RANK", 0)
     world = env_int("WORLD_SIZE", 1)
     local_rank = env_int("LOCAL_RANK", 0)
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload == "batch64":
+        return run_batch(args, rank, world, local_rank)
     return run_gpu(args, rank, world, local_rank)
 
 

@@ -191,6 +191,28 @@ int32_t mgpu_integrals_compute(mgpu_handle *h, mgpu_integrals *out);
 #define MGPU_NOALLOC_MAX_JM 4096
 int32_t mgpu_integrals_noalloc(mgpu_handle *h, mgpu_integrals *out);
 
+/* ---- batches of independent problems ----------------------------------- */
+/* No counterpart in the reference, which marches one problem per process.
+ * A batch steps several committed handles (operating points, grids of any
+ * size) with one CUDA graph launch per LOOP iteration: the graph holds one
+ * branch per handle, so the kernels of all instances share the GPU at the
+ * same time.  The handles must live on the current device and outlive the
+ * batch; each keeps its own NSTEP, monitors and end test, and every value it
+ * computes is bitwise the same as when the handle is stepped alone.  Do not
+ * step a member on its own while a batch call is running. */
+typedef struct mgpu_batch mgpu_batch;
+int32_t mgpu_batch_create(mgpu_handle *const *handles, int32_t n, mgpu_batch **out);
+void    mgpu_batch_destroy(mgpu_batch *b);
+/* nsteps iterations of every member, launched back to back.  mons (n
+ * entries, or NULL) receives each member's control block after the last
+ * step.  Returns the number of members whose end test (convergence,
+ * NSTEPS_MAX) has been met; they keep marching with the others, so a caller
+ * that wants them stopped builds a new batch without them.  Returns
+ * MGPU_E_NONFINITE if a member's health check fails. */
+int32_t mgpu_batch_run(mgpu_batch *b, int32_t nsteps, mgpu_monitors *mons);
+/* As mgpu_bench_steps, for the whole batch. */
+int32_t mgpu_batch_bench_steps(mgpu_batch *b, int32_t nsteps, int32_t flush_l2, double *total_ms);
+
 /* ---- instrumentation --------------------------------------------------- */
 /* The reference prints "CPU TIME PER STEP" every 50 steps
  * (multall-open-18.3.f:5404-5414); these are the device-side equivalents. */

@@ -74,6 +74,21 @@ struct mgpu_handle {
     DevCtl *h_ctl = nullptr;     // pinned mirror of the control block
 };
 
+// A batch: one CUDA graph whose branches are the step graphs of several
+// handles, forked from and joined back to the batch's own stream.
+struct mgpu_batch {
+    std::vector<mgpu_handle *> hs;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> joins;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    size_t graph_nodes = 0;
+    void *flush_buf = nullptr;
+    size_t flush_bytes = 0;
+};
+
 namespace {
 
 size_t shape_count(const mgpu_handle *h, Shape s) {
@@ -289,38 +304,36 @@ int add_conditional(mgpu_handle *h, cudaGraphConditionalHandle hnd, size_t *nbod
     return 0;
 }
 
-// one LOOP iteration as a CUDA graph: the LOSS and tail kernels sit in
-// conditional bodies that the step-control kernel switches on only on the
-// steps that need them
+// Records one LOOP iteration of h on h->stream, which must be capturing
+// (alone, or as one branch of a batch graph): the LOSS and tail kernels sit
+// in conditional bodies that the step-control kernel switches on only on
+// the steps that need them.
+int capture_step(mgpu_handle *h) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t cg = nullptr;
+    CK(cudaStreamGetCaptureInfo(h->stream, &st, nullptr, &cg, nullptr, nullptr, nullptr));
+    cudaGraphConditionalHandle hl = 0, ht = 0;
+    CK(cudaGraphConditionalHandleCreate(&hl, cg, 0, cudaGraphCondAssignDefault));
+    CK(cudaGraphConditionalHandleCreate(&ht, cg, 0, cudaGraphCondAssignDefault));
+    Dev dg = h->d;
+    dg.use_cond = 1;
+    dg.cond_loss = (unsigned long long)hl;
+    dg.cond_tail = (unsigned long long)ht;
+    Launch L{h->stream, h->sm_count, nullptr};
+    launch_step_begin(dg, L);
+    L.pdl = true;          // kernel-to-kernel edges of the step are programmatic
+    launch_prim(dg, L);
+    int rc = add_conditional(h, hl, &h->loss_nodes, [&](Launch L2) { launch_loss(dg, L2, false); });
+    if (!rc) enqueue_core(dg, L);
+    if (!rc) rc = add_conditional(h, ht, &h->tail_nodes, [&](Launch L2) { enqueue_tail(dg, L2); });
+    return rc;
+}
+
+// one LOOP iteration of h as a CUDA graph
 int build_graph(mgpu_handle *h) {
     if (h->gexec) return 0;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = 0;
-    {
-        cudaStreamCaptureStatus st;
-        cudaGraph_t cg = nullptr;
-        cudaError_t e = cudaStreamGetCaptureInfo(h->stream, &st, nullptr, &cg, nullptr, nullptr, nullptr);
-        cudaGraphConditionalHandle hl = 0, ht = 0;
-        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hl, cg, 0, cudaGraphCondAssignDefault);
-        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&ht, cg, 0, cudaGraphCondAssignDefault);
-        if (e != cudaSuccess) {
-            cudaGraph_t g = nullptr;
-            cudaStreamEndCapture(h->stream, &g);
-            if (g) cudaGraphDestroy(g);
-            return fail(MGPU_E_CUDA, std::string("conditional handles: ") + cudaGetErrorString(e));
-        }
-        Dev dg = h->d;
-        dg.use_cond = 1;
-        dg.cond_loss = (unsigned long long)hl;
-        dg.cond_tail = (unsigned long long)ht;
-        Launch L{h->stream, h->sm_count, nullptr};
-        launch_step_begin(dg, L);
-        L.pdl = true;          // kernel-to-kernel edges of the step are programmatic
-        launch_prim(dg, L);
-        rc = add_conditional(h, hl, &h->loss_nodes, [&](Launch L2) { launch_loss(dg, L2, false); });
-        if (!rc) enqueue_core(dg, L);
-        if (!rc) rc = add_conditional(h, ht, &h->tail_nodes, [&](Launch L2) { enqueue_tail(dg, L2); });
-    }
+    int rc = capture_step(h);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
     if (rc) {
@@ -926,6 +939,137 @@ int32_t mgpu_profile_steps(mgpu_handle *h, int32_t nsteps, mgpu_kernel_time *out
     }
     *n_out = n;
     return 0;
+}
+
+void mgpu_batch_destroy(mgpu_batch *b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->flush_buf) cudaFree(b->flush_buf);
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (cudaEvent_t e : b->joins)
+        if (e) cudaEventDestroy(e);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+int32_t mgpu_batch_create(mgpu_handle *const *handles, int32_t n, mgpu_batch **out) {
+    if (!handles || !out || n < 1) return fail(MGPU_E_ARG, "mgpu_batch_create: need n >= 1 handles and an out pointer");
+    *out = nullptr;
+    int cur = -1;
+    CK(cudaGetDevice(&cur));
+    for (int i = 0; i < n; ++i) {
+        mgpu_handle *h = handles[i];
+        if (!h || !h->committed) return fail(MGPU_E_STATE, "mgpu_batch_create: every handle must be committed");
+        if (h->device != cur) return fail(MGPU_E_STATE, "mgpu_batch_create: every handle must live on the current device");
+        for (int q = 0; q < i; ++q)
+            if (handles[q] == h) return fail(MGPU_E_ARG, "mgpu_batch_create: a handle appears twice");
+    }
+    mgpu_batch *b = new (std::nothrow) mgpu_batch();
+    if (!b) return fail(MGPU_E_NOMEM, "host allocation");
+    b->hs.assign(handles, handles + n);
+    b->device = cur;
+    b->joins.assign((size_t)n, nullptr);
+    auto bail = [&](int code) {
+        mgpu_batch_destroy(b);
+        return code;
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    for (int i = 0; i < n && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&b->joins[i], cudaEventDisableTiming);
+    if (e != cudaSuccess) return bail(fail(MGPU_E_CUDA, std::string("mgpu_batch_create: ") + cudaGetErrorString(e)));
+    e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return bail(fail(MGPU_E_CUDA, std::string("batch capture: ") + cudaGetErrorString(e)));
+    int rc = 0;
+    e = cudaEventRecord(b->fork, b->stream);
+    for (int i = 0; i < n && !rc && e == cudaSuccess; ++i) {
+        mgpu_handle *h = b->hs[i];
+        e = cudaStreamWaitEvent(h->stream, b->fork, 0);
+        if (e != cudaSuccess) break;
+        rc = capture_step(h);
+        if (rc) break;
+        e = cudaEventRecord(b->joins[i], h->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->joins[i], 0);
+    }
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+    if (rc || e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        if (rc) return bail(rc);
+        return bail(fail(MGPU_E_CUDA, std::string("batch capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2)));
+    }
+    b->graph = g;
+    e = cudaGraphGetNodes(g, nullptr, &b->graph_nodes);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->gexec, g, 0);
+    if (e != cudaSuccess) return bail(fail(MGPU_E_CUDA, std::string("batch graph: ") + cudaGetErrorString(e)));
+    *out = b;
+    return 0;
+}
+
+namespace {
+// the control blocks of every instance, read back on the batch stream
+int batch_read(mgpu_batch *b, mgpu_monitors *mons, int *ended) {
+    for (mgpu_handle *h : b->hs)
+        CK(cudaMemcpyAsync(h->h_ctl, h->d.ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    int nend = 0;
+    for (size_t i = 0; i < b->hs.size(); ++i) {
+        const DevCtl &c = *b->hs[i]->h_ctl;
+        if (mons) fill_monitors(c, &mons[i]);
+        if (c.health) {
+            char msg[96];
+            snprintf(msg, sizeof msg, "batch instance %zu: non-finite or non-positive density", i);
+            return fail(MGPU_E_NONFINITE, msg);
+        }
+        if (c.converged || c.ifend) ++nend;
+    }
+    *ended = nend;
+    return 0;
+}
+}  // namespace
+
+int32_t mgpu_batch_run(mgpu_batch *b, int32_t nsteps, mgpu_monitors *mons) {
+    if (!b || nsteps < 0) return fail(MGPU_E_ARG, "bad arguments to mgpu_batch_run");
+    const int chunk = 50;
+    int done = 0, ended = 0, rc = 0;
+    while (done < nsteps) {
+        int m = nsteps - done < chunk ? nsteps - done : chunk;
+        for (int s = 0; s < m; ++s) CK(cudaGraphLaunch(b->gexec, b->stream));
+        done += m;
+        if ((rc = batch_read(b, mons, &ended))) return rc;
+    }
+    if (nsteps == 0 && (rc = batch_read(b, mons, &ended))) return rc;
+    return ended;
+}
+
+int32_t mgpu_batch_bench_steps(mgpu_batch *b, int32_t nsteps, int32_t flush_l2, double *total_ms) {
+    if (!b || !total_ms || nsteps < 0) return fail(MGPU_E_ARG, "bad arguments to mgpu_batch_bench_steps");
+    if (flush_l2 && !b->flush_buf) {
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, b->device);
+        b->flush_bytes = (size_t)(l2 > 0 ? l2 : 128 << 20) * 2;
+        CK(cudaMalloc(&b->flush_buf, b->flush_bytes));
+    }
+    std::vector<cudaEvent_t> ev((size_t)2 * nsteps);
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    for (int s = 0; s < nsteps; ++s) {
+        if (flush_l2) CK(cudaMemsetAsync(b->flush_buf, s & 0xff, b->flush_bytes, b->stream));
+        CK(cudaEventRecord(ev[2 * s], b->stream));
+        CK(cudaGraphLaunch(b->gexec, b->stream));
+        CK(cudaEventRecord(ev[2 * s + 1], b->stream));
+    }
+    CK(cudaStreamSynchronize(b->stream));
+    double tot = 0.0;
+    for (int s = 0; s < nsteps; ++s) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ev[2 * s], ev[2 * s + 1]));
+        tot += ms;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    *total_ms = tot;
+    int ended = 0;
+    return batch_read(b, nullptr, &ended);
 }
 
 int32_t mgpu_kernels_per_step(mgpu_handle *h, int32_t which) {

@@ -42,7 +42,8 @@ EXPORTS = ["mgpu_abi_version", "mgpu_last_error", "mgpu_device_count", "mgpu_cre
            "mgpu_set_int", "mgpu_set_real", "mgpu_set_array", "mgpu_get_array", "mgpu_get_real", "mgpu_get_int",
            "mgpu_commit", "mgpu_stepup", "mgpu_loss_init", "mgpu_step", "mgpu_run", "mgpu_sync",
            "mgpu_integrals_compute", "mgpu_kernels_per_step", "mgpu_bench_steps", "mgpu_profile_steps",
-           "mgpu_step_io_bytes", "mgpu_integrals_noalloc"]
+           "mgpu_step_io_bytes", "mgpu_integrals_noalloc", "mgpu_batch_create", "mgpu_batch_destroy",
+           "mgpu_batch_run", "mgpu_batch_bench_steps"]
 
 _lib = None
 
@@ -81,9 +82,15 @@ def load(build: bool = True):
     L.mgpu_bench_steps.argtypes = [vp, i32, i32, ctypes.POINTER(ctypes.c_double)]
     L.mgpu_profile_steps.argtypes = [vp, i32, ctypes.POINTER(KernelTime), i32, ctypes.POINTER(i32)]
     L.mgpu_step_io_bytes.argtypes = [ctypes.POINTER(i32), ctypes.POINTER(i32)]
+    L.mgpu_batch_create.argtypes = [ctypes.POINTER(vp), i32, ctypes.POINTER(vp)]
+    L.mgpu_batch_destroy.argtypes = [vp]
+    L.mgpu_batch_run.argtypes = [vp, i32, ctypes.POINTER(Monitors)]
+    L.mgpu_batch_bench_steps.argtypes = [vp, i32, i32, ctypes.POINTER(ctypes.c_double)]
     for f in EXPORTS:
         fn = getattr(L, f)
-        if f != "mgpu_destroy":
+        if f in ("mgpu_destroy", "mgpu_batch_destroy"):
+            fn.restype = None
+        else:
             fn.restype = i32
     _lib = L
     return L
@@ -214,3 +221,39 @@ class Problem:
         n = ctypes.c_int32()
         _chk(load().mgpu_profile_steps(self.h, int(nsteps), arr, 256, ctypes.byref(n)))
         return [(arr[i].name.decode(), arr[i].launches, arr[i].total_ms) for i in range(n.value)]
+
+
+class Batch:
+    """Several Problems stepped by one CUDA graph launch per iteration (one
+    graph branch per problem); each problem's results are the same as when
+    it is stepped alone."""
+
+    def __init__(self, problems):
+        L = load()
+        self.problems = list(problems)
+        arr = (ctypes.c_void_p * len(self.problems))(*[p.h.value for p in self.problems])
+        b = ctypes.c_void_p()
+        _chk(L.mgpu_batch_create(arr, len(self.problems), ctypes.byref(b)))
+        self.b = b
+
+    def run(self, nsteps: int):
+        """(members whose end test is met, [Monitors per member])."""
+        mons = (Monitors * len(self.problems))()
+        ended = _chk(load().mgpu_batch_run(self.b, int(nsteps), mons))
+        return ended, list(mons)
+
+    def bench_steps(self, nsteps: int, flush_l2: bool = True) -> float:
+        ms = ctypes.c_double()
+        _chk(load().mgpu_batch_bench_steps(self.b, int(nsteps), 1 if flush_l2 else 0, ctypes.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if getattr(self, "b", None):
+            load().mgpu_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -106,6 +106,59 @@ def test_stage_config_one_step_reference_order(mods):
     _compare(gpu, ref, STATE, STEP1_TOL, "stage step 1 (reference order)")
 
 
+def test_nozzle_config_one_step_reference_order(mods):
+    """The single nozzle row at its full size, 37 x 97 x 33 (one row, JLE=18,
+    JTE=74), long sums in reference order: every field within 1e-5."""
+    case = mods[0]
+    cd, gpu, ref = _pair(mods, case.nozzle_row(), REDUCE_ORDER=1)
+    gpu.step()
+    ref.step()
+    _compare(gpu, ref, STATE, STEP1_TOL, "nozzle step 1 (reference order)")
+
+
+@pytest.fixture(scope="module")
+def compressor(mods):
+    case, common_setup, lib, O = mods
+    return common_setup.build_common(case.compressor_4stage())
+
+
+def test_compressor_config_reference_order(mods, compressor):
+    """The 4-stage compressor, 73 x 752 x 57, 8 rows with a mixing plane at
+    every row interface, sums in reference order.  After one step every field
+    is within 1e-5 of the FP32 oracle, or no farther from the FP64 oracle
+    than the FP32 oracle itself is: at the low-speed inlet the velocity comes
+    from 2*CP*(TO1 - TSTATIC) with TSTATIC = TO1*(P/PO1)**FGA, which turns the
+    last-ulp difference between CUDA's powf and the host's into ~1e-5 of VX,
+    the same size as the FP32 oracle's own error there.  After five steps
+    (LOSS, tail, STEPUP) every field is within 1e-4 of the FP32 oracle."""
+    case, common_setup, lib, O = mods
+    cd = compressor
+    cd.ints["REDUCE_ORDER"] = 1
+    try:
+        gpu = lib.Problem(cd)
+        ref = O.Oracle(cd)
+        ref.setup_calls()
+        ref64 = O.Oracle(cd, double=True)
+        ref64.setup_calls()
+    finally:
+        cd.ints["REDUCE_ORDER"] = 0
+    gpu.step()
+    ref.step()
+    ref64.step()
+    for n in STATE:
+        g, r32, r64 = gpu.get(n), ref.get(n, double=False), ref64.get(n, double=True)
+        e32 = rel_linf(g, r32)
+        if e32 > STEP1_TOL:
+            assert rel_linf(g, r64) <= 1.05 * rel_linf(r32, r64), (n, e32, rel_linf(g, r64), rel_linf(r32, r64))
+    del ref64
+    for _ in range(4):
+        mg = gpu.step()
+        mr = ref.step()
+    assert mg.tail_ran == 1 and mr.tail_ran == 1
+    _compare(gpu, ref, STATE + FORCES, 1e-4, "compressor step 5")
+    assert abs(mg.flow_in - mr.flow_in) <= 1e-5 * abs(mr.flow_in)
+
+
 def test_stage_config_one_step_fp64_sums(mods):
     """Default path (FP64 tree sums for the superblock and row-average
     reductions): against the FP64 oracle it is at least as close as the
@@ -149,6 +202,27 @@ def test_deterministic(mods):
         outs.append([gpu.get(n) for n in ("RO", "ROE", "ROVX")])
     for a, b in zip(*outs):
         assert np.array_equal(a, b)
+
+
+def test_batch_matches_members_stepped_alone(mods):
+    """Three uneven problems in one batch graph: after 12 steps (two tails,
+    two LOSS steps) every member's state is bitwise the state of the same
+    problem stepped on its own, and the monitors agree."""
+    case, common_setup, lib, O = mods
+    specs = [case.small_stage(), case.small_nozzle(), case.small_stage(im=11, jm_row=21, km=9, seed=7)]
+    cds = [common_setup.build_common(sp) for sp in specs]
+    alone = [lib.Problem(cd) for cd in cds]
+    for p in alone:
+        p.run(12)
+    members = [lib.Problem(cd) for cd in cds]
+    batch = lib.Batch(members)
+    ended, mons = batch.run(12)
+    assert ended == 0
+    for p, q, m in zip(alone, members, mons):
+        assert m.nstep == 12
+        for n in ("RO", "ROVX", "ROVR", "RORVT", "ROE", "DRO", "XFORCE", "STEP"):
+            assert np.array_equal(p.get(n), q.get(n)), n
+    batch.close()
 
 
 def test_health_check_reports_nonfinite(mods):
