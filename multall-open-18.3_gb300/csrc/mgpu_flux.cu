@@ -441,41 +441,9 @@ void launch_peff(const Dev &d, Launch L) {
 }
 
 // ---------------------------------------------------------------------
-// axial-momentum fluxes (6100-6120) and the cusp balance (6026)
-// ---------------------------------------------------------------------
-__device__ __forceinline__ void flux_xmom_node(const Dev &d, size_t n, int i, int j, int k) {
-    const VarSet &V = d.var[V_ROVX];
-    const float *PE = d.PEFF, *VX = d.VX;
-    if (i < d.IM && k < d.KM) {
-        V.SR[n] = d.XFORCE[n];
-        float AVGP = A3(PE, i, j, k) + A3(PE, i, j, k + 1) + A3(PE, i + 1, j, k + 1) + A3(PE, i + 1, j, k);
-        float AVGVX = A3(VX, i, j, k) + A3(VX, i, j, k + 1) + A3(VX, i + 1, j, k + 1) + A3(VX, i + 1, j, k);
-        V.XF[n] = 0.25f * (AVGP * A3(d.AQX, i, j, k) + d.FLOWX[n] * AVGVX);
-    }
-    if (i < d.IM && j >= 2) {
-        float AVGP = A3(PE, i, j, k) + A3(PE, i, j - 1, k) + A3(PE, i + 1, j - 1, k) + A3(PE, i + 1, j, k);
-        float AVGVX = A3(VX, i, j, k) + A3(VX, i, j - 1, k) + A3(VX, i + 1, j - 1, k) + A3(VX, i + 1, j, k);
-        V.RF[n] = 0.25f * (AVGP * A3(d.ASX, i, j, k) + d.FLOWR[n] * AVGVX);
-    }
-    if (j >= 2 && k < d.KM) {
-        if ((i == 1 || i == d.IM) && A1(d.IND, j) != 1) {
-            int IM = d.IM;
-            float AVGPCUSP = A3(PE, 1, j, k) + A3(PE, 1, j - 1, k) + A3(PE, 1, j, k + 1) + A3(PE, 1, j - 1, k + 1) +
-                             A3(PE, IM, j, k) + A3(PE, IM, j - 1, k) + A3(PE, IM, j, k + 1) + A3(PE, IM, j - 1, k + 1);
-            float AVGVXCUSP = A3(VX, 1, j, k) + A3(VX, 1, j - 1, k) + A3(VX, 1, j, k + 1) + A3(VX, 1, j - 1, k + 1) +
-                              A3(VX, IM, j, k) + A3(VX, IM, j - 1, k) + A3(VX, IM, j, k + 1) + A3(VX, IM, j - 1, k + 1);
-            V.TF[n] = 0.125f * (d.FLOWT[n] * AVGVXCUSP + AVGPCUSP * d.ABX[n]);
-        } else {
-            float AVGVX = A3(VX, i, j, k) + A3(VX, i, j - 1, k) + A3(VX, i, j - 1, k + 1) + A3(VX, i, j, k + 1);
-            float AVGP = A3(PE, i, j, k) + A3(PE, i, j - 1, k) + A3(PE, i, j - 1, k + 1) + A3(PE, i, j, k + 1);
-            V.TF[n] = 0.25f * (d.FLOWT[n] * AVGVX + d.ABX[n] * AVGP);
-        }
-    }
-}
-
-
-// ---------------------------------------------------------------------
-// moment-of-momentum fluxes (6200-6230) and periodic balance (902)
+// raw TFLUX of the moment-of-momentum (6200-6230) and radial-momentum
+// (6300-6330) equations at one I, used for the periodic balances at I=1
+// and I=IM (902, 6260)
 // ---------------------------------------------------------------------
 __device__ inline float tflux_rvt_raw(const Dev &d, int i, int j, int k, float AVGR) {
     const float *PE = d.PEFF, *VT = d.VT;
@@ -484,36 +452,6 @@ __device__ inline float tflux_rvt_raw(const Dev &d, int i, int j, int k, float A
     return (A3(d.FLOWT, i, j, k) * AVGVT + A2(d.ABT, j, k) * AVGP) * AVGR;
 }
 
-__device__ __forceinline__ void flux_rvt_node(const Dev &d, size_t n, int i, int j, int k) {
-    const VarSet &V = d.var[V_RORVT];
-    const float *VT = d.VT;
-    if (i < d.IM && k < d.KM) {
-        float AVGR = 0.125f * (A2(d.R, j, k) + A2(d.R, j, k + 1));
-        float AVGVT = A3(VT, i, j, k) + A3(VT, i, j, k + 1) + A3(VT, i + 1, j, k) + A3(VT, i + 1, j, k + 1);
-        V.SR[n] = d.TFORCE[n];
-        V.XF[n] = d.FLOWX[n] * AVGR * AVGVT;
-    }
-    if (j >= 2 && k < d.KM) {
-        float AVGR = 0.25f * A2(d.RAVG_CELL, j, k);
-        float tf = tflux_rvt_raw(d, i, j, k, AVGR);
-        if ((i == 1 || i == d.IM) && A1(d.IND, j) != 1) {
-            float t1 = (i == 1) ? tf : tflux_rvt_raw(d, 1, j, k, AVGR);
-            float tm = (i == d.IM) ? tf : tflux_rvt_raw(d, d.IM, j, k, AVGR);
-            tf = 0.5f * (t1 + tm);
-        }
-        V.TF[n] = tf;
-    }
-    if (i < d.IM && j >= 2) {
-        float AVGR = (A2(d.R, j, k) + A2(d.R, j - 1, k)) * 0.125f;
-        float AVGVT = A3(VT, i, j, k) + A3(VT, i, j - 1, k) + A3(VT, i + 1, j - 1, k) + A3(VT, i + 1, j, k);
-        V.RF[n] = d.FLOWR[n] * AVGVT * AVGR;
-    }
-}
-
-
-// ---------------------------------------------------------------------
-// radial-momentum fluxes and source (6300-6330), periodic balance (6260)
-// ---------------------------------------------------------------------
 __device__ inline float tflux_rmom_raw(const Dev &d, int i, int j, int k, float *avgp4) {
     const float *PE = d.PEFF, *VR = d.VR;
     float AVGVR = A3(VR, i, j, k) + A3(VR, i, j - 1, k) + A3(VR, i, j - 1, k + 1) + A3(VR, i, j, k + 1);
@@ -522,19 +460,107 @@ __device__ inline float tflux_rmom_raw(const Dev &d, int i, int j, int k, float 
     return 0.25f * (A3(d.FLOWT, i, j, k) * AVGVR + AVGP * A3(d.ABR, i, j, k));
 }
 
-__device__ __forceinline__ void flux_rmom_node(const Dev &d, size_t n, int i, int j, int k) {
-    const VarSet &V = d.var[V_ROVR];
-    const float *PE = d.PEFF, *VR = d.VR, *VT = d.VT, *RV = d.ROVT;
-    if (i < d.IM && k < d.KM) {
-        float AVGVR = A3(VR, i, j, k) + A3(VR, i, j, k + 1) + A3(VR, i + 1, j, k) + A3(VR, i + 1, j, k + 1);
-        float AVGP = A3(PE, i, j, k) + A3(PE, i, j, k + 1) + A3(PE, i + 1, j, k + 1) + A3(PE, i + 1, j, k);
-        V.XF[n] = 0.25f * (d.FLOWX[n] * AVGVR + A3(d.AQR, i, j, k) * AVGP);
+// The three momentum equations' fluxes in one pass over the nodes
+// (6100-6120, 6200-6230, 6300-6330 with the cusp and periodic balances).
+// Each thread loads its node's neighbour cube of PEFF, VX, VT, VR and ROVT
+// once -- the values at (i+di, j+dj, k+dk), di, dk in {0,1}, dj in {-1,0} --
+// and forms every average from registers, each sum in the order of the
+// reference's expression.  The balances at I=1 and I=IM, which also need the
+// other end's column, keep the direct loads of the helpers above.
+__global__ void __launch_bounds__(256) k_flux_mom(Dev d) {
+    pdl_wait();
+    const int n = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int N = d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, (size_t)n, i, j, k);
+    const int IM = d.IM, sJ = d.IM, sK = d.IM * d.JM;
+    const bool hi = i < IM, hj = j >= 2, hk = k < d.KM;
+    const float *__restrict__ PE = d.PEFF;
+    const float *__restrict__ VX = d.VX;
+    const float *__restrict__ VT = d.VT;
+    const float *__restrict__ VR = d.VR;
+    const float *__restrict__ RV = d.ROVT;
+    // c[di][dj + 1][dk]; positions outside the grid are never used
+    float pe[2][2][2] = {}, vx[2][2][2] = {}, vt[2][2][2] = {}, vr[2][2][2] = {}, rv[2][2][2] = {};
+#pragma unroll
+    for (int di = 0; di < 2; ++di)
+#pragma unroll
+        for (int dj = -1; dj <= 0; ++dj)
+#pragma unroll
+            for (int dk = 0; dk < 2; ++dk) {
+                if ((di && !hi) || (dj && !hj) || (dk && !hk)) continue;
+                const int o = n + di + dj * sJ + dk * sK;
+                pe[di][dj + 1][dk] = PE[o];
+                vt[di][dj + 1][dk] = VT[o];
+                if (!(di && dj && dk)) {
+                    vx[di][dj + 1][dk] = VX[o];
+                    vr[di][dj + 1][dk] = VR[o];
+                }
+                if (hi && hj && hk) rv[di][dj + 1][dk] = RV[o];
+            }
+#define C(a, di, dj, dk) a[di][(dj) + 1][dk]
+    const VarSet &VXm = d.var[V_ROVX], &VTm = d.var[V_RORVT], &VRm = d.var[V_ROVR];
+    const bool edge = (i == 1 || i == IM) && A1(d.IND, j) != 1;
+    // faces K = const (XFLUX) and the axial / tangential sources
+    if (hi && hk) {
+        VXm.SR[n] = d.XFORCE[n];
+        float AVGP = C(pe, 0, 0, 0) + C(pe, 0, 0, 1) + C(pe, 1, 0, 1) + C(pe, 1, 0, 0);
+        float AVGVX = C(vx, 0, 0, 0) + C(vx, 0, 0, 1) + C(vx, 1, 0, 1) + C(vx, 1, 0, 0);
+        VXm.XF[n] = 0.25f * (AVGP * d.AQX[n] + d.FLOWX[n] * AVGVX);
+        float AVGR = 0.125f * (A2(d.R, j, k) + A2(d.R, j, k + 1));
+        float AVGVT = C(vt, 0, 0, 0) + C(vt, 0, 0, 1) + C(vt, 1, 0, 0) + C(vt, 1, 0, 1);
+        VTm.SR[n] = d.TFORCE[n];
+        VTm.XF[n] = d.FLOWX[n] * AVGR * AVGVT;
+        float AVGVR = C(vr, 0, 0, 0) + C(vr, 0, 0, 1) + C(vr, 1, 0, 0) + C(vr, 1, 0, 1);
+        VRm.XF[n] = 0.25f * (d.FLOWX[n] * AVGVR + d.AQR[n] * AVGP);
     }
-    if (j >= 2 && k < d.KM) {
-        float ap;
-        float tf = tflux_rmom_raw(d, i, j, k, &ap);
-        if ((i == 1 || i == d.IM) && A1(d.IND, j) != 1) {
-            int IM = d.IM;
+    // faces J = const (RFLUX) and the radial source
+    if (hi && hj) {
+        float AVGP = C(pe, 0, 0, 0) + C(pe, 0, -1, 0) + C(pe, 1, -1, 0) + C(pe, 1, 0, 0);
+        float AVGVX = C(vx, 0, 0, 0) + C(vx, 0, -1, 0) + C(vx, 1, -1, 0) + C(vx, 1, 0, 0);
+        VXm.RF[n] = 0.25f * (AVGP * d.ASX[n] + d.FLOWR[n] * AVGVX);
+        float AVGR = (A2(d.R, j, k) + A2(d.R, j - 1, k)) * 0.125f;
+        float AVGVT = C(vt, 0, 0, 0) + C(vt, 0, -1, 0) + C(vt, 1, -1, 0) + C(vt, 1, 0, 0);
+        VTm.RF[n] = d.FLOWR[n] * AVGVT * AVGR;
+        float AVGVR = C(vr, 0, 0, 0) + C(vr, 0, -1, 0) + C(vr, 1, -1, 0) + C(vr, 1, 0, 0);
+        VRm.RF[n] = 0.25f * (d.FLOWR[n] * AVGVR + d.ASR[n] * AVGP);
+        if (hk) {
+            float AVGRVT = C(rv, 0, 0, 0) + C(rv, 0, 0, 1) + C(rv, 0, -1, 0) + C(rv, 0, -1, 1) + C(rv, 1, 0, 0) +
+                           C(rv, 1, 0, 1) + C(rv, 1, -1, 0) + C(rv, 1, -1, 1);
+            float AVGVT8 = 0.125f * (C(vt, 0, 0, 0) + C(vt, 0, -1, 0) + C(vt, 0, -1, 1) + C(vt, 0, 0, 1) + C(vt, 1, 0, 0) +
+                                     C(vt, 1, -1, 0) + C(vt, 1, -1, 1) + C(vt, 1, 0, 1));
+            float AVGP8 = C(pe, 0, 0, 0) + C(pe, 0, -1, 0) + C(pe, 0, -1, 1) + C(pe, 0, 0, 1) + C(pe, 1, 0, 0) +
+                          C(pe, 1, -1, 0) + C(pe, 1, -1, 1) + C(pe, 1, 0, 1);
+            VRm.SR[n] = d.RFORCE[n] - (AVGRVT * AVGVT8 + AVGP8) * d.VOLOR[n];
+        }
+    }
+    // faces I = const (TFLUX)
+    if (hj && hk) {
+        const float FT = d.FLOWT[n];
+        float AVGP = C(pe, 0, 0, 0) + C(pe, 0, -1, 0) + C(pe, 0, -1, 1) + C(pe, 0, 0, 1);
+        if (edge) {
+            float AVGPCUSP = A3(PE, 1, j, k) + A3(PE, 1, j - 1, k) + A3(PE, 1, j, k + 1) + A3(PE, 1, j - 1, k + 1) +
+                             A3(PE, IM, j, k) + A3(PE, IM, j - 1, k) + A3(PE, IM, j, k + 1) + A3(PE, IM, j - 1, k + 1);
+            float AVGVXCUSP = A3(VX, 1, j, k) + A3(VX, 1, j - 1, k) + A3(VX, 1, j, k + 1) + A3(VX, 1, j - 1, k + 1) +
+                              A3(VX, IM, j, k) + A3(VX, IM, j - 1, k) + A3(VX, IM, j, k + 1) + A3(VX, IM, j - 1, k + 1);
+            VXm.TF[n] = 0.125f * (FT * AVGVXCUSP + AVGPCUSP * d.ABX[n]);
+        } else {
+            float AVGVX = C(vx, 0, 0, 0) + C(vx, 0, -1, 0) + C(vx, 0, -1, 1) + C(vx, 0, 0, 1);
+            VXm.TF[n] = 0.25f * (FT * AVGVX + d.ABX[n] * AVGP);
+        }
+        const float AVGR = 0.25f * A2(d.RAVG_CELL, j, k);
+        float AVGVT = C(vt, 0, 0, 0) + C(vt, 0, -1, 0) + C(vt, 0, -1, 1) + C(vt, 0, 0, 1);
+        float tf = (FT * AVGVT + A2(d.ABT, j, k) * AVGP) * AVGR;
+        if (edge) {
+            float t1 = (i == 1) ? tf : tflux_rvt_raw(d, 1, j, k, AVGR);
+            float tm = (i == IM) ? tf : tflux_rvt_raw(d, IM, j, k, AVGR);
+            tf = 0.5f * (t1 + tm);
+        }
+        VTm.TF[n] = tf;
+        float AVGVR = C(vr, 0, 0, 0) + C(vr, 0, -1, 0) + C(vr, 0, -1, 1) + C(vr, 0, 0, 1);
+        float tr = 0.25f * (FT * AVGVR + AVGP * d.ABR[n]);
+        if (edge) {
             float ap1, apm;
             float t1raw = tflux_rmom_raw(d, 1, j, k, &ap1);
             float tmraw = tflux_rmom_raw(d, IM, j, k, &apm);
@@ -542,41 +568,11 @@ __device__ __forceinline__ void flux_rmom_node(const Dev &d, size_t n, int i, in
             float AVGPM = 0.25f * (A3(PE, IM, j, k) + A3(PE, IM, j - 1, k) + A3(PE, IM, j, k + 1) + A3(PE, IM, j - 1, k + 1));
             float T1 = t1raw - AVGP1 * A3(d.ABR, 1, j, k);
             float T2 = tmraw - AVGPM * A3(d.ABR, IM, j, k);
-            tf = 0.5f * ((T1 + T2) + (AVGP1 + AVGPM) * A3(d.ABR, i, j, k));
+            tr = 0.5f * ((T1 + T2) + (AVGP1 + AVGPM) * d.ABR[n]);
         }
-        V.TF[n] = tf;
+        VRm.TF[n] = tr;
     }
-    if (i < d.IM && j >= 2) {
-        float AVGVR = A3(VR, i, j, k) + A3(VR, i, j - 1, k) + A3(VR, i + 1, j - 1, k) + A3(VR, i + 1, j, k);
-        float AVGP = A3(PE, i, j, k) + A3(PE, i, j - 1, k) + A3(PE, i + 1, j - 1, k) + A3(PE, i + 1, j, k);
-        V.RF[n] = 0.25f * (d.FLOWR[n] * AVGVR + A3(d.ASR, i, j, k) * AVGP);
-        if (k < d.KM) {
-            float AVGRVT = A3(RV, i, j, k) + A3(RV, i, j, k + 1) + A3(RV, i, j - 1, k) + A3(RV, i, j - 1, k + 1) +
-                           A3(RV, i + 1, j, k) + A3(RV, i + 1, j, k + 1) + A3(RV, i + 1, j - 1, k) + A3(RV, i + 1, j - 1, k + 1);
-            float AVGVT = 0.125f * (A3(VT, i, j, k) + A3(VT, i, j - 1, k) + A3(VT, i, j - 1, k + 1) + A3(VT, i, j, k + 1) +
-                                    A3(VT, i + 1, j, k) + A3(VT, i + 1, j - 1, k) + A3(VT, i + 1, j - 1, k + 1) +
-                                    A3(VT, i + 1, j, k + 1));
-            float AVGP8 = A3(PE, i, j, k) + A3(PE, i, j - 1, k) + A3(PE, i, j - 1, k + 1) + A3(PE, i, j, k + 1) +
-                          A3(PE, i + 1, j, k) + A3(PE, i + 1, j - 1, k) + A3(PE, i + 1, j - 1, k + 1) + A3(PE, i + 1, j, k + 1);
-            V.SR[n] = d.RFORCE[n] - (AVGRVT * AVGVT + AVGP8) * d.VOLOR[n];
-        }
-    }
-}
-
-
-// The three momentum equations' fluxes in one pass over the nodes: they
-// read the same PEFF, FLOWX/FLOWT/FLOWR and velocities (L1 serves the
-// repeats) and write disjoint per-variable flux sets.
-__global__ void k_flux_mom(Dev d) {
-    pdl_wait();
-    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t N = (size_t)d.IM * d.JM * d.KM;
-    if (n >= N) return;
-    int i, j, k;
-    node_ijk(d, n, i, j, k);
-    flux_xmom_node(d, n, i, j, k);
-    flux_rvt_node(d, n, i, j, k);
-    flux_rmom_node(d, n, i, j, k);
+#undef C
 }
 
 void launch_flux_mom(const Dev &d, Launch L) {
