@@ -630,8 +630,8 @@ int32_t mgpu_commit(mgpu_handle *h) {
     if (d.IFCOOL || d.IFBLEED || d.IFSHROUD) return fail(MGPU_E_UNSUPPORTED, "cooling/bleed/shroud not covered");
     if (d.IN_FLOW != 0 || d.IF_REPEAT != 0) return fail(MGPU_E_UNSUPPORTED, "IN_FLOW/IF_REPEAT not covered");
     if (d.PLATE_LOSS > 0.001f || d.THROTTLE_EXIT > 0.001f) return fail(MGPU_E_UNSUPPORTED, "plate loss/throttle not covered");
-    if (d.YPLUSWALL <= -10.0f)
-        return fail(MGPU_E_UNSUPPORTED, "YPLUSWALL<=-10 (pressure-gradient wall functions) not covered");
+    if (d.YPLUSWALL < -10.0f && d.JM > 1700)
+        return fail(MGPU_E_UNSUPPORTED, "YPLUSWALL<-10 with JM > 1700 is not covered (SET_PWALLGRAD column buffer)");
     if (d.IPOUT == 3 || d.IPOUT < -1) return fail(MGPU_E_UNSUPPORTED, "IPOUT not covered");
     if (d.NCHANGE <= 0 || d.NMIXUP <= 0 || d.NLOS <= 0) return fail(MGPU_E_ARG, "NCHANGE, NMIXUP, NLOS must be positive");
     if (d.IR <= 1 && d.JR <= 1 && d.KR <= 1) return fail(MGPU_E_UNSUPPORTED, "runs without multigrid are not covered");

@@ -467,7 +467,8 @@ __device__ inline float tflux_rmom_raw(const Dev &d, int i, int j, int k, float 
 // and forms every average from registers, each sum in the order of the
 // reference's expression.  The balances at I=1 and I=IM, which also need the
 // other end's column, keep the direct loads of the helpers above.
-__global__ void __launch_bounds__(256) k_flux_mom(Dev d) {
+
+__global__ void __launch_bounds__(256, 4) k_flux_mom(Dev d) {
     pdl_wait();
     const int n = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int N = d.IM * d.JM * d.KM;

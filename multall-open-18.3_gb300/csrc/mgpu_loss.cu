@@ -1,13 +1,12 @@
 // mgpu_loss.cu -- the viscous body forces of SUBROUTINE LOSS (ILOS=10,
 // multall-open-18.3.f:8058-9066) with the Shih wall functions WALLFUN
-// (15980-16047, YPLUSWALL in (-10,-0.001)); the every-5-step tail of LOOP
-// (monitors 5264-5317 and STEPUP 7916-8002); and the EFICOOL/SUMFLX mass
-// averages (10662-10849, 7873-7912).
+// (15980-16047) and, for YPLUSWALL < -10, the pressure gradients of
+// SET_PWALLGRAD (16052-16114); the every-5-step tail of LOOP (monitors
+// 5264-5317 and STEPUP 7916-8002); and the EFICOOL/SUMFLX mass averages
+// (10662-10849, 7873-7912).
 //
-// LOSS is two passes over the grid.  The streamwise-face pass takes one
-// thread per (I,J) column of cells and walks K (the transition test needs
-// the maximum of mu_t/mu over half the span before any stress is formed);
-// the bladewise-face pass takes one thread per (J,K) line and walks I.
+// LOSS is two passes over the grid: the streamwise (K) faces for every
+// (I,J) column, then the bladewise (I) faces for every (J,K) line.
 #include "mgpu_internal.cuh"
 
 namespace mgpu {
@@ -40,16 +39,34 @@ __global__ void k_loss_prologue(Dev d, int init_call) {
     }
 }
 
-// Shih et al. wall function without the pressure-gradient term
-__device__ inline void wallfun(float PERP, float DENSITY, float &TWALL, float YPLUS_OLD, float WREL_WALL,
-                               float &YPLUS_NEW, float VISLAM) {
+// Shih et al. wall function (WALLFUN).  DPDS is the caller's DPDS_CELL
+// element: with YPLUSWALL <= -10 the pressure-gradient term is added and,
+// as the Fortran argument does, |DPDS| < 1 is raised to 1.0 in place.
+__device__ inline void wallfun(float PERP, float &DPDS, float DENSITY, float &TWALL, float YPLUS_OLD, float WREL_WALL,
+                               float &YPLUS_NEW, float VISLAM, float YPLUSWALL) {
+    float SGN_DPDS = 0.0f, VPRES = 0.0f, VSTAR_P = 0.0f, FYPLUSP = 0.0f;
+    const bool pres = !(YPLUSWALL > -10.0f);
+    if (pres) {
+        if (fabsf(DPDS) < 1.0f) DPDS = 1.0f;
+        SGN_DPDS = fabsf(DPDS) / DPDS;
+        VPRES = powf(VISLAM / DENSITY / DENSITY * fabsf(DPDS), 0.33333f);
+        VSTAR_P = YPLUS_OLD * VISLAM / (DENSITY * PERP);
+        if (SGN_DPDS < 0.0f && VPRES > 0.33f * VSTAR_P) VPRES = 0.33f * VSTAR_P;
+        if (SGN_DPDS > 0.0f && VPRES > 2.0f * VSTAR_P) VPRES = 2.0f * VSTAR_P;
+        float YPLUS_PRES = VPRES * PERP * DENSITY / VISLAM;
+        float P1 = YPLUS_PRES, P2 = P1 * P1, P3 = P2 * P1, P4 = P2 * P2;
+        if (P1 <= 4.0f) FYPLUSP = 0.5f * P2 - 7.31E-3f * P3;
+        if (P1 > 4.0f && P1 <= 15.0f) FYPLUSP = -15.138f + 8.4688f * P1 - 0.81976f * P2 + 3.7292E-2f * P3 - 6.3866E-4f * P4;
+        if (P1 > 15.0f && P1 <= 30.0f) FYPLUSP = 11.925f + 0.934f * P1 - 2.7805E-2f * P2 + 4.6262E-4f * P3 - 3.1442E-6f * P4;
+        if (P1 > 30.0f) FYPLUSP = 5.0f * logf(P1) + 8.0f;
+    }
     float YP1 = YPLUS_OLD, YP2 = YP1 * YP1, YP3 = YP2 * YP1, YP4 = YP2 * YP2;
     float FYPLUS = 0.0f;
     if (YP1 <= 5.0f) FYPLUS = YP1 + 1.0E-2f * YP2 - 2.9E-03f * YP3;
     if (YP1 > 5.0f && YP1 <= 30.0f) FYPLUS = -0.872f + 1.465f * YP1 - 7.02E-2f * YP2 + 1.66E-03f * YP3 - 1.495E-5f * YP4;
     if (YP1 > 30.0f && YP1 <= 140.0f) FYPLUS = 8.6f + 0.1864f * YP1 - 2.006E-3f * YP2 + 1.144E-5f * YP3 - 2.551E-8f * YP4;
     if (YP1 > 140.0f) FYPLUS = 2.439f * logf(YP1) + 5.0f;
-    float FRACP = 0.0f;
+    float FRACP = pres ? SGN_DPDS * (VPRES / VSTAR_P) * FYPLUSP / FYPLUS : 0.0f;
     float VPLUS = FYPLUS * (1.0f + FRACP);
     float VSTAR = WREL_WALL / VPLUS;
     TWALL = DENSITY * VSTAR * VSTAR;
@@ -97,6 +114,103 @@ __device__ inline float fyplus_of(float yp, float yplam, float ypturb, float pre
         f = XFAC * XFAC * (3.0f - 2.0f * XFAC);
     }
     return f;
+}
+
+// ---------------------------------------------------------------------
+// SET_PWALLGRAD (16052-16114), run at the start of LOSS when YPLUSWALL <
+// -10.  k_pwallgrad_cells: one thread per cell, the streamwise pressure
+// gradient from GRADVEL (13468-13508) of PEFF along the cell's relative
+// velocity, limited by DPDS_LIM.  k_pwallgrad_smooth: the smoothing along J
+// within each row, sequential in J and across rows as the reference runs it;
+// one warp takes 32 (I,K) columns staged in shared memory.  The last row
+// reaches J = JM+1 .. JM+4, storage the reference never writes otherwise:
+// those reads give 0 and the writes are dropped.
+// ---------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_pwallgrad_cells(const __grid_constant__ Dev d, int init_call) {
+    pdl_wait();
+    if (!init_call && !d.ctl->do_loss) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int IMM1 = d.IMM1, KMM1 = d.KMM1;
+    if (t >= IMM1 * KMM1 * (d.JM - 1)) return;
+    const int i = t % IMM1 + 1, q = t / IMM1, k = q % KMM1 + 1, j = q / KMM1 + 2;
+    float PDIV = 0.5f * (d.PDOWN_HUB + d.PDOWN_TIP);
+    PDIV = PDIV / (float)d.NROWS;
+    PDIV = PDIV / (A1(d.CHORD, 1) + A1(d.CHORD, d.NROWS));
+    const float DPDS_LIM = fabsf(20.0f * (A1(d.PO1, d.KMID) - PDIV));
+    const int sJ = d.IM, sK = d.IM * d.JM;
+    const int n = ix3(d, i, j, k);
+    // node offsets of the cell's corners: (i | i+1, j-1 | j, k | k+1)
+    const int o000 = n, o100 = n + 1, o0m0 = n - sJ, o1m0 = n + 1 - sJ;
+    const int o001 = n + sK, o101 = n + 1 + sK, o0m1 = n - sJ + sK, o1m1 = n + 1 - sJ + sK;
+    const float *V = d.PEFF;
+    const float RVOL = 0.25f / d.VOL[n];
+    const float VAVGJ1 = V[o0m0] + V[o1m0] + V[o1m1] + V[o0m1];
+    const float VAVGJ2 = V[o000] + V[o100] + V[o101] + V[o001];
+    const float VAVGI1 = V[o000] + V[o0m0] + V[o0m1] + V[o001];
+    const float VAVGI2 = V[o100] + V[o1m0] + V[o1m1] + V[o101];
+    const float VAVGK1 = V[o000] + V[o100] + V[o1m0] + V[o0m0];
+    const float VAVGK2 = V[o001] + V[o101] + V[o1m1] + V[o0m1];
+    const float VAVGCELL = 0.125f * (VAVGJ1 + VAVGJ2);
+    const float DPDX = -((VAVGJ2 * d.AQX[n] - VAVGJ1 * d.AQX[n - sJ] + VAVGI1 * d.ABX[n] - VAVGI2 * d.ABX[n + 1] +
+                          VAVGK1 * d.ASX[n] - VAVGK2 * d.ASX[n + sK]) *
+                         RVOL);
+    const float DPDR = -((VAVGJ2 * d.AQR[n] - VAVGJ1 * d.AQR[n - sJ] + VAVGI1 * d.ABR[n] - VAVGI2 * d.ABR[n + 1] +
+                          VAVGK1 * d.ASR[n] - VAVGK2 * d.ASR[n + sK]) *
+                         RVOL) -
+                       VAVGCELL / A2(d.RAVG_CELL, j, k);
+    const float DPDT = -((VAVGI1 - VAVGI2) * A2(d.ABT, j, k) * RVOL);
+    auto c8 = [&](const float *A) {
+        return A[o000] + A[o0m0] + A[o100] + A[o1m0] + A[o001] + A[o0m1] + A[o101] + A[o1m1];
+    };
+    const float VXCELL = c8(d.VX), VRCELL = c8(d.VR), WTCELL = c8(d.WT);
+    const float WREL_CELL = sqrtf(VXCELL * VXCELL + VRCELL * VRCELL + WTCELL * WTCELL);
+    float DPDS = (DPDX * VXCELL + DPDR * VRCELL + DPDT * WTCELL) / WREL_CELL;
+    if (fabsf(DPDS) > DPDS_LIM) DPDS = DPDS_LIM * DPDS / fabsf(DPDS);
+    d.DPDS_CELL[n] = DPDS;
+}
+
+__global__ void __launch_bounds__(32) k_pwallgrad_smooth(const __grid_constant__ Dev d, int init_call) {
+    pdl_wait();
+    if (!init_call && !d.ctl->do_loss) return;
+    extern __shared__ float col[];                 // [JM + 4][32], plane J at row J-1
+    const int lane = threadIdx.x;
+    const int i = blockIdx.x * 32 + lane + 1, k = blockIdx.y + 1;
+    const bool act = i <= d.IMM1;
+    const int JM = d.JM;
+    const int sK = d.IM * JM;
+    float *base = d.DPDS_CELL + (i - 1) + sK * (k - 1);
+#define CJ(jj) col[((jj) - 1) * 32 + lane]
+    for (int jj = 1; jj <= JM + 4; ++jj) CJ(jj) = (act && jj <= JM) ? base[(jj - 1) * d.IM] : 0.0f;
+    if (act) {
+        for (int nr = 1; nr <= d.NROWS; ++nr) {
+            const int J1 = A1(d.JSTART, nr), J2 = A1(d.JMIX, nr);
+            auto ends = [&]() {
+                CJ(J2 + 1) = 0.0f;
+                CJ(J2 + 2) = 2.0f * CJ(J2 + 3) - CJ(J2 + 4);
+                CJ(J2) = 2.0f * CJ(J2 - 1) - CJ(J2 - 2);
+            };
+            ends();
+            // TEMPP(J) = 0.5 D(J) + 0.25 (D(J-1) + D(J+1)) for J1+2..J2-1 from the
+            // unsmoothed values, then D(J) = 0.5 T(J) + 0.25 (T(J-1) + T(J+1)) for
+            // J1+3..J2-2: one pass with TEMPP in three registers, each D(J)
+            // overwritten only after TEMPP(J+1) has read it
+            if (J2 - 2 >= J1 + 3) {
+                float tm = 0.5f * CJ(J1 + 2) + 0.25f * (CJ(J1 + 1) + CJ(J1 + 3));
+                float tc = 0.5f * CJ(J1 + 3) + 0.25f * (CJ(J1 + 2) + CJ(J1 + 4));
+                for (int jj = J1 + 3; jj <= J2 - 2; ++jj) {
+                    float tp = 0.5f * CJ(jj + 1) + 0.25f * (CJ(jj) + CJ(jj + 2));
+                    CJ(jj) = 0.5f * tc + 0.25f * (tm + tp);
+                    tm = tc;
+                    tc = tp;
+                }
+            }
+            ends();
+        }
+    }
+    __syncwarp();
+    if (act)
+        for (int jj = 1; jj <= JM; ++jj) base[(jj - 1) * d.IM] = CJ(jj);
+#undef CJ
 }
 
 // ---------------------------------------------------------------------
@@ -168,7 +282,8 @@ __global__ void __launch_bounds__(32 * LK_W) k_loss_kfaces(const __grid_constant
         if (d.YPLUSWALL < -0.001f) {
             float PERPK1 = A3(d.VOL, i, j, 1) / LK(AREA, 1);
             float ynew;
-            wallfun(PERPK1, LK(ROAVG, 1), TWALLK1, AIJ(d.YPLUS_K1, i, j), wbound(1), ynew, VISLAM);
+            wallfun(PERPK1, A3(d.DPDS_CELL, i, j, 1), LK(ROAVG, 1), TWALLK1, AIJ(d.YPLUS_K1, i, j), wbound(1), ynew, VISLAM,
+                    d.YPLUSWALL);
             AIJ(d.YPLUS_K1, i, j) = fminf(1000.0f, ynew);
         } else if (d.YPLUSWALL < 5.0f) {
             float PERP = A3(d.VOL, i, j, 1) / LK(AREA, 1);
@@ -181,7 +296,8 @@ __global__ void __launch_bounds__(32 * LK_W) k_loss_kfaces(const __grid_constant
         if (d.YPLUSWALL < -0.001f) {
             float PERPKM = A3(d.VOL, i, j, KMM1) / LK(AREA, KM);
             float ynew;
-            wallfun(PERPKM, LK(ROAVG, KMM1), TWALLKM, AIJ(d.YPLUS_KM, i, j), wbound(KMM1), ynew, VISLAM);
+            wallfun(PERPKM, A3(d.DPDS_CELL, i, j, KMM1), LK(ROAVG, KMM1), TWALLKM, AIJ(d.YPLUS_KM, i, j), wbound(KMM1), ynew,
+                    VISLAM, d.YPLUSWALL);
             AIJ(d.YPLUS_KM, i, j) = fminf(1000.0f, ynew);
         } else if (d.YPLUSWALL < 5.0f) {
             float PERP = A3(d.VOL, i, j, KMM1) / LK(AREA, KM);
@@ -401,7 +517,7 @@ __global__ void __launch_bounds__(32 * LI_W) k_loss_ifaces(const __grid_constant
                     float PERPW = A3(d.VOL, ia, j, k) / AREA[iw];
                     float ynew;
                     float *yw = lo ? &A2(d.YPLUS_I1, j, k) : &A2(d.YPLUS_IM, j, k);
-                    wallfun(PERPW, ROAVG[ia], TW, *yw, WABS[ib], ynew, VISLAM);
+                    wallfun(PERPW, A3(d.DPDS_CELL, ia, j, k), ROAVG[ia], TW, *yw, WABS[ib], ynew, VISLAM, d.YPLUSWALL);
                     *yw = fminf(1000.0f, ynew);
                 } else if (d.YPLUSWALL < 5.0f) {
                     float PERP = A3(d.VOL, ia, j, k) / AREA[iw];
@@ -537,11 +653,18 @@ __global__ void __launch_bounds__(32 * LI_W) k_loss_ifaces(const __grid_constant
     }
 }
 
+size_t pwallgrad_smem(const Dev &d) { return (size_t)(d.JM + 4) * 32 * sizeof(float); }
 size_t loss_kfaces_smem(const Dev &d) { return ((size_t)LK_NARR * d.KM * 32 + d.KM) * sizeof(float); }
 size_t loss_ifaces_smem(const Dev &d) { return (size_t)LI_W * LI_NARR * (d.IM + 1) * sizeof(float); }
 
 cudaError_t configure_loss_kernels(const Dev &d) {
-    size_t kb = loss_kfaces_smem(d), ib = loss_ifaces_smem(d);
+    size_t kb = loss_kfaces_smem(d), ib = loss_ifaces_smem(d), pb = pwallgrad_smem(d);
+    if (d.YPLUSWALL < -10.0f) {
+        if (pb > 220 * 1024) return cudaErrorInvalidValue;
+        cudaError_t e = cudaFuncSetAttribute((const void *)k_pwallgrad_smooth, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(pb > 48 * 1024 ? pb : 48 * 1024));
+        if (e != cudaSuccess) return e;
+    }
     if (kb > 220 * 1024 || ib > 220 * 1024) return cudaErrorInvalidValue;   // KM <= 160: kb <= 201 KB
     cudaError_t e = cudaFuncSetAttribute((const void *)k_loss_kfaces, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(kb > 48 * 1024 ? kb : 48 * 1024));
@@ -553,6 +676,14 @@ cudaError_t configure_loss_kernels(const Dev &d) {
 void launch_loss(const Dev &d, Launch L, bool init_call) {
     launchk(L, k_loss_prologue, dim3(1), dim3(1), 0, d, init_call ? 1 : 0);
     mark(L, "k_loss_prologue");
+    if (d.YPLUSWALL < -10.0f) {
+        int nc = d.IMM1 * d.KMM1 * (d.JM - 1);
+        launchk(L, k_pwallgrad_cells, dim3((nc + 255) / 256), dim3(256), 0, d, init_call ? 1 : 0);
+        mark(L, "k_pwallgrad_cells");
+        launchk(L, k_pwallgrad_smooth, dim3((unsigned)((d.IMM1 + 31) / 32), (unsigned)d.KMM1), dim3(32),
+                pwallgrad_smem(d), d, init_call ? 1 : 0);
+        mark(L, "k_pwallgrad_smooth");
+    }
     dim3 gk((unsigned)((d.IMM1 + 31) / 32), (unsigned)(d.JM - 1));
     launchk(L, k_loss_kfaces, dim3(gk), dim3(32, LK_W), loss_kfaces_smem(d), d, init_call ? 1 : 0);
     mark(L, "k_loss_kfaces");

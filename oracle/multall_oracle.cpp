@@ -28,7 +28,9 @@
  * Options covered (the rest are rejected at commit): ITIMST=3 (SCREE, or
  * SSS through F1,F2,F3,NRSMTH), ILOS=10, IFGAS=0, no cooling, bleed or
  * shroud, IN_FLOW=0, IF_REPEAT=0, IF_CUSP<2, IM>2, KM>2, no throttle or
- * plate loss, YPLUSWALL > -10.
+ * plate loss.  Wall treatments: YPLUSWALL > 5 (fixed Y+), in [-0.001, 5) (log-law
+ * skin friction), in (-10, -0.001) (Shih wall functions) and <= -10 (Shih
+ * with the SET_PWALLGRAD pressure-gradient term).
  */
 #include <cmath>
 #include <cstdint>
@@ -228,7 +230,6 @@ struct Oracle : OracleBase {
         if (IFCOOL || IFBLEED || IFSHROUD) return fail(MGPU_E_UNSUPPORTED, "cooling/bleed/shroud not covered");
         if (IN_FLOW != 0 || IF_REPEAT != 0) return fail(MGPU_E_UNSUPPORTED, "IN_FLOW/IF_REPEAT not covered");
         if (PLATE_LOSS > R(0.001) || THROTTLE_EXIT > R(0.001)) return fail(MGPU_E_UNSUPPORTED, "plate loss/throttle not covered");
-        if (YPLUSWALL <= R(-10.0)) return fail(MGPU_E_UNSUPPORTED, "YPLUSWALL<=-10 (pressure-gradient wall functions) not covered");
         if (IPOUT == 3 || IPOUT < -1) return fail(MGPU_E_UNSUPPORTED, "IPOUT not covered");
         for (int nr = 1; nr <= NROWS; ++nr)
             if (F1(IF_CUSP, nr) >= 2) return fail(MGPU_E_UNSUPPORTED, "IF_CUSP=2 not covered");
@@ -708,9 +709,107 @@ struct Oracle : OracleBase {
     }
 
     /* ================================================================== */
-    /*  WALLFUN   multall-open-18.3.f:15980-16047  (YPLUSWALL > -10)        */
+    /*  GRADVEL   multall-open-18.3.f:13468-13508: cell gradient of a node  */
+    /*  quantity by Gauss' theorem (corner storage)                        */
     /* ================================================================== */
-    void wallfun(R PERP, R DENSITY, R &TWALL, R YPLUS_OLD, R WREL_WALL, R &YPLUS_NEW) {
+    void gradvel(int i, int j, int k, const std::vector<R> &V, R &DVDX, R &DVDR, R &DVDT) {
+        int ip1 = i + 1, jm1 = j - 1, kp1 = k + 1;
+        auto v = [&](int a, int b, int c) { return V[ijk(a, b, c)]; };
+        R RVOL = R(0.25) / F3(VOL, i, j, k);
+        R VAVGJ1 = v(i, jm1, k) + v(ip1, jm1, k) + v(ip1, jm1, kp1) + v(i, jm1, kp1);
+        R VAVGJ2 = v(i, j, k) + v(ip1, j, k) + v(ip1, j, kp1) + v(i, j, kp1);
+        R VAVGI1 = v(i, j, k) + v(i, jm1, k) + v(i, jm1, kp1) + v(i, j, kp1);
+        R VAVGI2 = v(ip1, j, k) + v(ip1, jm1, k) + v(ip1, jm1, kp1) + v(ip1, j, kp1);
+        R VAVGK1 = v(i, j, k) + v(ip1, j, k) + v(ip1, jm1, k) + v(i, jm1, k);
+        R VAVGK2 = v(i, j, kp1) + v(ip1, j, kp1) + v(ip1, jm1, kp1) + v(i, jm1, kp1);
+        R VAVGCELL = R(0.125) * (VAVGJ1 + VAVGJ2);
+        DVDX = -((VAVGJ2 * F3(AQX, i, j, k) - VAVGJ1 * F3(AQX, i, jm1, k) + VAVGI1 * F3(ABX, i, j, k) -
+                  VAVGI2 * F3(ABX, ip1, j, k) + VAVGK1 * F3(ASX, i, j, k) - VAVGK2 * F3(ASX, i, j, kp1)) *
+                 RVOL);
+        DVDR = -((VAVGJ2 * F3(AQR, i, j, k) - VAVGJ1 * F3(AQR, i, jm1, k) + VAVGI1 * F3(ABR, i, j, k) -
+                  VAVGI2 * F3(ABR, ip1, j, k) + VAVGK1 * F3(ASR, i, j, k) - VAVGK2 * F3(ASR, i, j, kp1)) *
+                 RVOL) -
+               VAVGCELL / F2(RAVG_CELL, j, k);
+        DVDT = -((VAVGI1 - VAVGI2) * F2(ABT, j, k) * RVOL);
+    }
+
+    /* ================================================================== */
+    /*  SET_PWALLGRAD   multall-open-18.3.f:16052-16114: streamwise        */
+    /*  pressure gradient per cell for the Shih wall functions, limited    */
+    /*  and smoothed along J within each row.  The last row's smoothing    */
+    /*  touches J = JM+1 .. JM+4, outside the grid: storage the reference  */
+    /*  never writes otherwise (zero), so those reads give 0 here and the  */
+    /*  writes are dropped.                                                 */
+    /* ================================================================== */
+    void set_pwallgrad() {
+        R t = R(0.5) * (PDOWN_HUB + PDOWN_TIP);
+        t = t / R(NROWS);
+        t = t / (F1(CHORD, 1) + F1(CHORD, NROWS));
+        R DPDS_LIM = std::fabs(R(20.0) * (F1(PO1, KMID) - t));
+        for (int j = 2; j <= JM; ++j)
+            for (int k = 1; k <= KMM1; ++k)
+                for (int i = 1; i <= IMM1; ++i) {
+                    R DPDX, DPDR, DPDT;
+                    gradvel(i, j, k, PEFF_v, DPDX, DPDR, DPDT);
+                    auto c8 = [&](const std::vector<R> &A) {
+                        return A[ijk(i, j, k)] + A[ijk(i, j - 1, k)] + A[ijk(i + 1, j, k)] + A[ijk(i + 1, j - 1, k)] +
+                               A[ijk(i, j, k + 1)] + A[ijk(i, j - 1, k + 1)] + A[ijk(i + 1, j, k + 1)] +
+                               A[ijk(i + 1, j - 1, k + 1)];
+                    };
+                    R VXCELL = c8(VX_v), VRCELL = c8(VR_v), WTCELL = c8(WT_v);
+                    R WREL_CELL = std::sqrt(VXCELL * VXCELL + VRCELL * VRCELL + WTCELL * WTCELL);
+                    R DPDS = (DPDX * VXCELL + DPDR * VRCELL + DPDT * WTCELL) / WREL_CELL;
+                    if (std::fabs(DPDS) > DPDS_LIM) DPDS = DPDS_LIM * DPDS / std::fabs(DPDS);
+                    F3(DPDS_CELL, i, j, k) = DPDS;
+                }
+        std::vector<R> TEMPP((size_t)JM + 8);
+        for (int nr = 1; nr <= NROWS; ++nr) {
+            int J1 = F1(JSTART, nr), J2 = F1(JMIX, nr);
+            for (int k = 1; k <= KMM1; ++k)
+                for (int i = 1; i <= IMM1; ++i) {
+                    auto D = [&](int jj) -> R { return jj <= JM ? F3(DPDS_CELL, i, jj, k) : R(0); };
+                    auto setD = [&](int jj, R v) {
+                        if (jj <= JM) F3(DPDS_CELL, i, jj, k) = v;
+                    };
+                    auto ends = [&]() {
+                        setD(J2 + 1, R(0.0));
+                        setD(J2 + 2, R(2) * D(J2 + 3) - D(J2 + 4));
+                        setD(J2, R(2) * D(J2 - 1) - D(J2 - 2));
+                    };
+                    ends();
+                    for (int jj = J1 + 2; jj <= J2 - 1; ++jj) TEMPP[jj] = R(0.5) * D(jj) + R(0.25) * (D(jj - 1) + D(jj + 1));
+                    TEMPP[J2 + 1] = R(0.0);
+                    for (int jj = J1 + 3; jj <= J2 - 2; ++jj)
+                        setD(jj, R(0.5) * TEMPP[jj] + R(0.25) * (TEMPP[jj - 1] + TEMPP[jj + 1]));
+                    ends();
+                }
+        }
+    }
+
+    /* ================================================================== */
+    /*  WALLFUN   multall-open-18.3.f:15980-16047.  DPDS is the caller's    */
+    /*  DPDS_CELL element: the pressure-gradient branch (YPLUSWALL <= -10)  */
+    /*  raises |DPDS| < 1 to 1.0 in place, as the Fortran argument does.    */
+    /* ================================================================== */
+    void wallfun(R PERP, R &DPDS, R DENSITY, R &TWALL, R YPLUS_OLD, R WREL_WALL, R &YPLUS_NEW) {
+        R SGN_DPDS = R(0), VPRES = R(0), VSTAR_P = R(0), FYPLUSP = R(0);
+        const bool pres = !(YPLUSWALL > R(-10.0));
+        if (pres) {
+            if (std::fabs(DPDS) < R(1.0)) DPDS = R(1.0);
+            SGN_DPDS = std::fabs(DPDS) / DPDS;
+            VPRES = std::pow(VISLAM / DENSITY / DENSITY * std::fabs(DPDS), R(0.33333));
+            VSTAR_P = YPLUS_OLD * VISLAM / (DENSITY * PERP);
+            if (SGN_DPDS < R(0.0) && VPRES > R(0.33) * VSTAR_P) VPRES = R(0.33) * VSTAR_P;
+            if (SGN_DPDS > R(0.0) && VPRES > R(2.0) * VSTAR_P) VPRES = R(2.0) * VSTAR_P;
+            R YPLUS_PRES = VPRES * PERP * DENSITY / VISLAM;
+            R P1 = YPLUS_PRES, P2 = P1 * P1, P3 = P2 * P1, P4 = P2 * P2;
+            if (P1 <= R(4.0)) FYPLUSP = R(0.5) * P2 - R(7.31E-3) * P3;
+            if (P1 > R(4.0) && P1 <= R(15.0))
+                FYPLUSP = R(-15.138) + R(8.4688) * P1 - R(0.81976) * P2 + R(3.7292E-2) * P3 - R(6.3866E-4) * P4;
+            if (P1 > R(15.0) && P1 <= R(30.0))
+                FYPLUSP = R(11.925) + R(0.934) * P1 - R(2.7805E-2) * P2 + R(4.6262E-4) * P3 - R(3.1442E-6) * P4;
+            if (P1 > R(30.0)) FYPLUSP = R(5) * std::log(P1) + R(8.0);
+        }
         R YP1 = YPLUS_OLD, YP2 = YP1 * YP1, YP3 = YP2 * YP1, YP4 = YP2 * YP2;
         R FYPLUS = R(0);
         if (YP1 <= R(5.0)) FYPLUS = YP1 + R(1.0E-2) * YP2 - R(2.9E-03) * YP3;
@@ -719,7 +818,7 @@ struct Oracle : OracleBase {
         if (YP1 > R(30) && YP1 <= R(140.0))
             FYPLUS = R(8.6) + R(0.1864) * YP1 - R(2.006E-3) * YP2 + R(1.144E-5) * YP3 - R(2.551E-8) * YP4;
         if (YP1 > R(140.0)) FYPLUS = R(2.439) * std::log(YP1) + R(5.0);
-        R FRACP = R(0.0);
+        R FRACP = pres ? SGN_DPDS * (VPRES / VSTAR_P) * FYPLUSP / FYPLUS : R(0.0);
         R VPLUS = FYPLUS * (R(1.0) + FRACP);
         R VSTAR = WREL_WALL / VPLUS;
         TWALL = DENSITY * VSTAR * VSTAR;
@@ -792,6 +891,7 @@ struct Oracle : OracleBase {
             FTCOND = TCOND / VISLAM;
         }
         if (NSTEP <= NLOS) loss_tables();
+        if (YPLUSWALL < R(-10.0)) set_pwallgrad();
 
         int LEN = std::max(IM, KM) + 2;
         std::vector<R> VXAVG(LEN), VRAVG(LEN), WTAVG(LEN), WABS(LEN), ROAVG(LEN), XSTRES(LEN), RAVG(LEN),
@@ -833,7 +933,7 @@ struct Oracle : OracleBase {
                 if (YPLUSWALL < R(-0.001)) {
                     R PERPK1 = F3(VOL, i, j, 1) / AREA[1];
                     R YPLUS_NEW;
-                    wallfun(PERPK1, ROAVG[1], TWALLK1, FIJ(YPLUS_K1, i, j), WBOUND[1], YPLUS_NEW);
+                    wallfun(PERPK1, F3(DPDS_CELL, i, j, 1), ROAVG[1], TWALLK1, FIJ(YPLUS_K1, i, j), WBOUND[1], YPLUS_NEW);
                     FIJ(YPLUS_K1, i, j) = std::min(R(1000.0), YPLUS_NEW);
                 } else if (YPLUSWALL < R(5.)) {
                     R PERP = F3(VOL, i, j, 1) / AREA[1];
@@ -845,7 +945,7 @@ struct Oracle : OracleBase {
                 if (YPLUSWALL < R(-0.001)) {
                     R PERPKM = F3(VOL, i, j, KMM1) / AREA[KM];
                     R YPLUS_NEW;
-                    wallfun(PERPKM, ROAVG[KMM1], TWALLKM, FIJ(YPLUS_KM, i, j), WBOUND[KMM1], YPLUS_NEW);
+                    wallfun(PERPKM, F3(DPDS_CELL, i, j, KMM1), ROAVG[KMM1], TWALLKM, FIJ(YPLUS_KM, i, j), WBOUND[KMM1], YPLUS_NEW);
                     FIJ(YPLUS_KM, i, j) = std::min(R(1000.0), YPLUS_NEW);
                 } else if (YPLUSWALL < R(5.)) {
                     R PERP = F3(VOL, i, j, KMM1) / AREA[KM];
@@ -967,7 +1067,7 @@ struct Oracle : OracleBase {
                         if (YPLUSWALL < R(-0.001)) {
                             R PERPI1 = F3(VOL, 1, j, k) / AREA[1];
                             R YPLUS_NEW;
-                            wallfun(PERPI1, ROAVG[1], TWALLI1, F2(YPLUS_I1, j, k), WBOUND[2], YPLUS_NEW);
+                            wallfun(PERPI1, F3(DPDS_CELL, 1, j, k), ROAVG[1], TWALLI1, F2(YPLUS_I1, j, k), WBOUND[2], YPLUS_NEW);
                             F2(YPLUS_I1, j, k) = std::min(R(1000.0), YPLUS_NEW);
                         } else if (YPLUSWALL < R(5.)) {
                             R PERP = F3(VOL, 1, j, k) / AREA[1];
@@ -979,7 +1079,7 @@ struct Oracle : OracleBase {
                         if (YPLUSWALL < R(-0.001)) {
                             R PERPIM = F3(VOL, IMM1, j, k) / AREA[IM];
                             R YPLUS_NEW;
-                            wallfun(PERPIM, ROAVG[IMM1], TWALLIM, F2(YPLUS_IM, j, k), WBOUND[IMM1], YPLUS_NEW);
+                            wallfun(PERPIM, F3(DPDS_CELL, IMM1, j, k), ROAVG[IMM1], TWALLIM, F2(YPLUS_IM, j, k), WBOUND[IMM1], YPLUS_NEW);
                             F2(YPLUS_IM, j, k) = std::min(R(1000.0), YPLUS_NEW);
                         } else if (YPLUSWALL < R(5.)) {
                             R PERP = F3(VOL, IMM1, j, k) / AREA[IM];

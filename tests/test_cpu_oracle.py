@@ -51,6 +51,29 @@ def test_oracle_float_vs_double_one_step(mods):
         assert rel_linf(of.get(n), od.get(n)) < 1e-4, n
 
 
+def test_oracle_pressure_gradient_wall_functions(mods):
+    """YPLUSWALL < -10 (SET_PWALLGRAD + Shih with the pressure term): REAL*4
+    and REAL*8 agree to 1e-4 over ten steps (two LOSS calls), DPDS_CELL is
+    set on the cells and stays within the DPDS_LIM bound."""
+    case, common_setup, O = mods
+    spec = case.small_stage()
+    spec.ypluswall = -15.0
+    cd = common_setup.build_common(spec)
+    of, od = O.Oracle(cd), O.Oracle(cd, double=True)
+    of.setup_calls()
+    od.setup_calls()
+    for _ in range(10):
+        of.step()
+        od.step()
+    for n in ("RO", "ROE", "ROVX", "XFORCE", "TFORCE"):
+        assert rel_linf(of.get(n), od.get(n)) < 1e-4, n
+    dp = of.get("DPDS_CELL")
+    nr = cd.nrows
+    lim = abs(20.0 * (cd.arrays["PO1"][cd.km // 2 - 1] - 0.5 * (cd.reals["PDOWN_HUB"] + cd.reals["PDOWN_TIP"]) / nr /
+                      (cd.arrays["CHORD"][0] + cd.arrays["CHORD"][nr - 1])))
+    assert np.count_nonzero(dp) > 0 and np.abs(dp).max() <= lim * (1 + 1e-6)
+
+
 def test_oracle_periodic_and_mixing_plane(mods):
     """After a step, non-blade J-planes are periodic (D(1)=D(IM)) and the
     two faces of the mixing plane are pitchwise uniform.  The exit plane

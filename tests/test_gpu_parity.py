@@ -85,6 +85,25 @@ def test_five_steps_with_loss_and_tail(mods, which):
     assert (mg.ivmax, mg.jvmax, mg.kvmax) == (mr.ivmax, mr.jvmax, mr.kvmax)
 
 
+@pytest.mark.parametrize("ypluswall", [-15.0, -10.0])
+def test_pressure_gradient_wall_functions(mods, ypluswall):
+    """YPLUSWALL <= -10: the Shih wall functions with the pressure-gradient
+    term, DPDS_CELL from SET_PWALLGRAD when YPLUSWALL < -10 (at exactly -10
+    the term runs on the stored DPDS_CELL, which WALLFUN raises to 1.0).
+    After SETUP's LOSS every field is within 1e-5, after five steps (LOSS
+    again at step 5) within 1e-4 of the FP32 oracle."""
+    case, common_setup, lib, O = mods
+    spec = case.small_stage()
+    spec.ypluswall = ypluswall
+    cd, gpu, ref = _pair(mods, spec)
+    _compare(gpu, ref, FORCES + ["DPDS_CELL", "YPLUS_K1", "YPLUS_I1"], STEP1_TOL, "setup LOSS")
+    for _ in range(5):
+        gpu.step()
+        ref.step()
+    _compare(gpu, ref, STATE + FORCES + ["DPDS_CELL", "YPLUS_K1", "YPLUS_KM", "YPLUS_I1", "YPLUS_IM"], 1e-4,
+             "step 5")
+
+
 def test_sss_scheme_one_step(mods):
     """ITIMST=-3 (SSS): F2/F3 history terms and SMOOTH_RESID."""
     case = mods[0]
