@@ -15,6 +15,8 @@
  *              MG1 NIB1*(NJB1+1)*NKB1         MG2 NIB2*(NJB2+1)*NKB2
  *              SB  NSBLK
  *       role   GEOM  constant input, must be bound before commit
+ *              OPT   constant input of an option (IF_CUSP=2), must be bound
+ *                    before commit when a row uses that option
  *              STATE evolves in the loop, must be bound, can be read back
  *              OUT   produced by the loop, readable only
  *
@@ -101,6 +103,11 @@
     M_(PDOWN_TIP, MGPU_REQUIRED_REAL)                                     \
     M_(PLATE_LOSS, 0.0f)                                                  \
     M_(THROTTLE_EXIT, 0.0f)                                               \
+    M_(THROTTLE_PRES, 0.0f)                                               \
+    M_(THROTTLE_MAS, 0.0f)                                                \
+    M_(RFTHROTL,  0.0f)                                                   \
+    M_(FLOWIN,    0.0f)                                                   \
+    M_(RFLOW,     0.0f)                                                   \
     M_(VSOUND,    MGPU_REQUIRED_REAL)                                     \
     M_(CONLIM,    0.001f)                                                 \
     M_(VISLAM,    0.0f)                                                   \
@@ -134,6 +141,11 @@
     M_(ROUGH_L,  FLOAT32, ROW, GEOM)                                      \
     M_(ROUGH_U,  FLOAT32, ROW, GEOM)                                      \
     M_(CHORD,    FLOAT32, ROW, GEOM)                                      \
+    M_(NUP_I1,   INT32,   ROW, OPT)                                       \
+    M_(NUP_IM,   INT32,   ROW, OPT)                                       \
+    M_(N_WAKE,   INT32,   ROW, OPT)                                       \
+    M_(SEP_THIK, FLOAT32, ROW, OPT)                                       \
+    M_(SEP_DRAG, FLOAT32, ROW, OPT)                                       \
     /* per streamwise station J */                                       \
     M_(NBLADE,   INT32,   J,   GEOM)                                      \
     M_(IND,      INT32,   J,   GEOM)                                      \
@@ -177,6 +189,7 @@
     M_(FTR,      FLOAT32, IK,  GEOM)                                      \
     /* meridional geometry, /BKGEOM/ /BKAREA/ /BKSTAG/ */                 \
     M_(X,        FLOAT32, JK,  GEOM)                                      \
+    M_(RT_THICK, FLOAT32, JK,  OPT)                                       \
     M_(R,        FLOAT32, JK,  GEOM)                                      \
     M_(ABT,      FLOAT32, JK,  GEOM)                                      \
     M_(WRABT,    FLOAT32, JK,  GEOM)                                      \
@@ -201,6 +214,7 @@
     M_(VOLOR,    FLOAT32, IJK, GEOM)                                      \
     M_(BSTEP,    FLOAT32, IJK, GEOM)                                      \
     M_(DWALLSQ,  FLOAT32, IJK, GEOM)                                      \
+    M_(RTHETA,   FLOAT32, IJK, OPT)                                       \
     /* multigrid block time steps, /BKMGRD/ */                           \
     M_(STEP1,    FLOAT32, MG1, GEOM)                                      \
     M_(STEP2,    FLOAT32, MG2, GEOM)                                      \

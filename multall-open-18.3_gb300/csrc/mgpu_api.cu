@@ -34,7 +34,7 @@ int fail(int code, const std::string &msg) {
     } while (0)
 
 enum Shape { SH_IJK, SH_JK, SH_IK, SH_IJ, SH_J, SH_I, SH_K, SH_ROW, SH_MG1, SH_MG2, SH_SB };
-enum Role { RO_GEOM, RO_STATE, RO_OUT };
+enum Role { RO_GEOM, RO_OPT, RO_STATE, RO_OUT };
 
 struct ArrayInfo {
     const char *name;
@@ -253,11 +253,13 @@ void enqueue_core(const Dev &d, Launch L) {
     launch_flux_energy(d, L);
     launch_tstep(d, L, V_RO, 2);
     launch_bc(d, L);
+    if (d.IN_FLOW != 0) launch_setflo(d, L);
     launch_peff(d, L);
     launch_flux_mom(d, L);
     launch_tstep(d, L, V_ROVX, 3);
     launch_limiters(d, L);
     launch_mixplan(d, L);
+    if (d.any_cusp2) launch_cusp(d, L);
 }
 
 void enqueue_tail(const Dev &d, Launch L) {
@@ -485,7 +487,8 @@ int32_t mgpu_create(int32_t im, int32_t jm, int32_t km, int32_t nrows, mgpu_hand
     if ((rc = dalloc(h, &d.ROLIMIT, nrows))) return bail(rc);
     if ((rc = dalloc(h, &d.BLADE_FLOW, jm))) return bail(rc);
     if ((rc = dalloc(h, &d.DFLAG, (size_t)im * km))) return bail(rc);
-    if ((rc = dalloc(h, &d.BCBUF, (size_t)3 * km))) return bail(rc);
+    if ((rc = dalloc(h, &d.BCBUF, (size_t)4 * km))) return bail(rc);
+    if ((rc = dalloc(h, &d.FLOWJ, jm))) return bail(rc);
     d.nparts = (int)((N + 255) / 256) + 1;
     if ((rc = dalloc(h, &d.part_sum, d.nparts))) return bail(rc);
     if ((rc = dalloc(h, &d.part_key, d.nparts))) return bail(rc);
@@ -530,7 +533,8 @@ int32_t mgpu_set_real(mgpu_handle *h, const char *name, float value) {
 int32_t mgpu_get_real(mgpu_handle *h, const char *name, float *value) {
     if (!h || !name || !value) return fail(MGPU_E_ARG, "null argument");
     if (h->committed && (!strcmp(name, "VISLAM") || !strcmp(name, "FTCOND") || !strcmp(name, "SFT") ||
-                         !strcmp(name, "SFX") || !strcmp(name, "DAMP") || !strcmp(name, "FMIXUP"))) {
+                         !strcmp(name, "SFX") || !strcmp(name, "DAMP") || !strcmp(name, "FMIXUP") ||
+                         !strcmp(name, "PDOWN_HUB") || !strcmp(name, "PDOWN_TIP") || !strcmp(name, "THROTTLE_PRES"))) {
         int rc = read_ctl(h);
         if (rc) return rc;
         const DevCtl &c = *h->h_ctl;
@@ -539,6 +543,9 @@ int32_t mgpu_get_real(mgpu_handle *h, const char *name, float *value) {
         else if (!strcmp(name, "SFT")) *value = c.SFT;
         else if (!strcmp(name, "SFX")) *value = c.SFX;
         else if (!strcmp(name, "DAMP")) *value = c.DAMP;
+        else if (!strcmp(name, "PDOWN_HUB")) *value = c.PDOWN_HUB;
+        else if (!strcmp(name, "PDOWN_TIP")) *value = c.PDOWN_TIP;
+        else if (!strcmp(name, "THROTTLE_PRES")) *value = c.THROTTLE_PRES;
         else *value = c.FMIXUP;
         return 0;
     }
@@ -618,7 +625,7 @@ int32_t mgpu_commit(mgpu_handle *h) {
     if (h->committed) return fail(MGPU_E_STATE, "already committed");
     Dev &d = h->d;
     for (int a = 0; a < kNumArrays; ++a)
-        if (kArrays[a].role != RO_OUT && !h->bound[a])
+        if (kArrays[a].role != RO_OUT && kArrays[a].role != RO_OPT && !h->bound[a])
             return fail(MGPU_E_ARG, std::string("array not bound: ") + kArrays[a].name);
 #define MGPU_CHKI(n, v) if (d.n == MGPU_REQUIRED_INT) return fail(MGPU_E_ARG, "integer not set: " #n);
     MGPU_INT_SCALARS(MGPU_CHKI)
@@ -628,8 +635,8 @@ int32_t mgpu_commit(mgpu_handle *h) {
     if (d.ILOS != 10) return fail(MGPU_E_UNSUPPORTED, "only ILOS=10 (mixing-length LOSS) is covered");
     if (d.IFGAS != 0) return fail(MGPU_E_UNSUPPORTED, "real-gas IFGAS=1 not covered");
     if (d.IFCOOL || d.IFBLEED || d.IFSHROUD) return fail(MGPU_E_UNSUPPORTED, "cooling/bleed/shroud not covered");
-    if (d.IN_FLOW != 0 || d.IF_REPEAT != 0) return fail(MGPU_E_UNSUPPORTED, "IN_FLOW/IF_REPEAT not covered");
-    if (d.PLATE_LOSS > 0.001f || d.THROTTLE_EXIT > 0.001f) return fail(MGPU_E_UNSUPPORTED, "plate loss/throttle not covered");
+    if (d.IF_REPEAT != 0) return fail(MGPU_E_UNSUPPORTED, "IF_REPEAT not covered");
+    if (d.THROTTLE_EXIT > 0.001f && d.THROTTLE_MAS == 0.0f) return fail(MGPU_E_ARG, "THROTTLE_MAS must be set with THROTTLE_EXIT");
     if (d.YPLUSWALL < -10.0f && d.JM > 1700)
         return fail(MGPU_E_UNSUPPORTED, "YPLUSWALL<-10 with JM > 1700 is not covered (SET_PWALLGRAD column buffer)");
     if (d.IPOUT == 3 || d.IPOUT < -1) return fail(MGPU_E_UNSUPPORTED, "IPOUT not covered");
@@ -662,8 +669,25 @@ int32_t mgpu_commit(mgpu_handle *h) {
         (rc = getf("XLLIM_I1", XL[0])) || (rc = getf("XLLIM_IM", XL[1])) || (rc = getf("XLLIM_K1", XL[2])) ||
         (rc = getf("XLLIM_KM", XL[3])) || (rc = getf("XLLIM_DWN", XL[4])) || (rc = getf("XLLIM_UP", XL[5])))
         return rc;
-    for (int nr = 0; nr < d.NROWS; ++nr)
-        if (IF_CUSP[nr] >= 2) return fail(MGPU_E_UNSUPPORTED, "IF_CUSP=2 not covered");
+    d.any_cusp2 = 0;
+    for (int nr = 0; nr < d.NROWS; ++nr) {
+        if (IF_CUSP[nr] > 2) return fail(MGPU_E_UNSUPPORTED, "IF_CUSP above 2 not covered");
+        if (IF_CUSP[nr] == 2) d.any_cusp2 = 1;
+    }
+    if (d.any_cusp2) {
+        for (const char *n : {"NUP_I1", "NUP_IM", "N_WAKE", "SEP_THIK", "SEP_DRAG", "RT_THICK", "RTHETA"})
+            if (!h->bound[find_array(n)]) return fail(MGPU_E_ARG, std::string("IF_CUSP=2 needs ") + n);
+        if (d.IM < 7) return fail(MGPU_E_ARG, "IF_CUSP=2 needs IM >= 7");
+        std::vector<int> NUP1, NUPM, NW;
+        if ((rc = geti("NUP_I1", NUP1)) || (rc = geti("NUP_IM", NUPM)) || (rc = geti("N_WAKE", NW))) return rc;
+        for (int nr = 0; nr < d.NROWS; ++nr) {
+            if (IF_CUSP[nr] != 2) continue;
+            // every forced point stays inside the row, so the rows are independent
+            int js1 = JTE[nr] - NUP1[nr], jsm = JTE[nr] - NUPM[nr];
+            if (js1 < JSTART[nr] + 1 || jsm < JSTART[nr] + 1 || JTE[nr] + NW[nr] > JMIX[nr] || NW[nr] < 0)
+                return fail(MGPU_E_ARG, "IF_CUSP=2: NUP_I1, NUP_IM, N_WAKE reach outside the row");
+        }
+    }
     for (int nr = 0; nr < d.NROWS; ++nr) {
         if (JSTART[nr] < 1 || JMIX[nr] > d.JM || JMIX[nr] - JSTART[nr] < 8)
             return fail(MGPU_E_ARG, "row J ranges (JSTART/JMIX) out of range");
@@ -676,6 +700,7 @@ int32_t mgpu_commit(mgpu_handle *h) {
             return fail(MGPU_E_ARG, "leading/trailing edge indices out of range");
     if (INDMIX[d.JM - 1] != 0) return fail(MGPU_E_ARG, "INDMIX(JM) must be 0");
 
+    d.RFTHROTL1 = 1.0f - d.RFTHROTL;
     // gas constants, SETUP 6459-6468
     d.GA1 = d.GA - 1.0f;
     d.FGA = d.GA1 / d.GA;
@@ -750,6 +775,10 @@ int32_t mgpu_commit(mgpu_handle *h) {
     c.FMIXUP = 1.0f;
     c.VISLAM = d.VISLAM;
     c.FTCOND = d.FTCOND;
+    c.PDOWN_HUB = d.PDOWN_HUB;
+    c.PDOWN_TIP = d.PDOWN_TIP;
+    c.THROTTLE_PRES = d.THROTTLE_PRES;
+    c.CHECK_FLOW_JM = 0.0f;
     c.nstep = d.NSTEP;
     CK(cudaMemcpy(d.ctl, &c, sizeof(c), cudaMemcpyHostToDevice));
     CK(configure_kernels(d));

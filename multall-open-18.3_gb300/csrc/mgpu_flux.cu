@@ -271,13 +271,15 @@ void launch_flux_energy(const Dev &d, Launch L) {
 // ---------------------------------------------------------------------
 __global__ void __launch_bounds__(1024) k_bc_sums(Dev d) {
     pdl_wait();
-    // per warp: the four pitchwise terms of one K line, [4][IMM1]
+    // per warp: the four pitchwise terms of one K line, [4][IMM1], and with
+    // PLATE_LOSS the two ROV_m**2 terms at JM, [2][IM]
     extern __shared__ float bsm[];
-    __shared__ float s_sum[512], s_pd[512], s_r[512];
+    __shared__ float s_sum[512], s_pd[512], s_r[512], s_rov[514];
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const int IMM1 = d.IMM1;
-    float *tt = bsm + (size_t)w * 4 * IMM1;
-    for (int k = w + 1; k <= d.KM; k += nw) {
+    const int IM = d.IM, IMM1 = d.IMM1, KM = d.KM;
+    const bool plate = d.PLATE_LOSS > 0.001f;
+    float *tt = bsm + (size_t)w * (4 * IMM1 + 2 * IM);
+    for (int k = w + 1; k <= KM; k += nw) {
         const float RJM = A2(d.R, d.JM, k);
         for (int i = l + 1; i <= IMM1; i += 32) {
             float fp = A1(d.FP, i);
@@ -289,41 +291,76 @@ __global__ void __launch_bounds__(1024) k_bc_sums(Dev d) {
                                     A3(d.ROVT, i + 1, d.JM, k) * A3(d.VT, i + 1, d.JM, k)) /
                                    RJM;
         }
+        if (plate)
+            for (int i = l + 1; i <= IM; i += 32) {
+                tt[4 * IMM1 + i - 1] = A3(d.ROVX, i, d.JM, k) * A3(d.VX, i, d.JM, k);
+                tt[4 * IMM1 + IM + i - 1] = A3(d.ROVR, i, d.JM, k) * A3(d.VR, i, d.JM, k);
+            }
         __syncwarp();
-        // lanes 0..3 each add one term over I in the reference's order
+        // lanes 0..3 each add one term over I in the reference's order; lane 4
+        // forms ROVMSQ(K) = sum of ROVX*VX + ROVR*VR (4476-4482)
         if (l < 4) {
             const float *t = tt + l * IMM1;
             float sum = 0.0f;
             for (int i = 0; i < IMM1; ++i) sum = sum + t[i];
-            if (l < 3) d.BCBUF[l * d.KM + k - 1] = sum;   // PAVG2, PAVG3, PAVGOUT
+            if (l < 3) d.BCBUF[l * KM + k - 1] = sum;   // PAVG2, PAVG3, PAVGOUT
             else s_sum[k - 1] = sum;
+        } else if (l == 4 && plate) {
+            const float *a = tt + 4 * IMM1, *b = a + IM;
+            float sum = 0.0f;
+            for (int i = 0; i < IM; ++i) {
+                sum = sum + a[i];
+                sum = sum + b[i];
+            }
+            s_rov[k] = sum;
         }
         __syncwarp();
     }
-    if (d.IPOUT > 0) return;
     // the recurrence runs on shared copies of PD and R(JM, K): one thread,
     // no global round trip per K
-    for (int k = threadIdx.x; k < d.KM; k += blockDim.x) {
+    for (int k = threadIdx.x; k < KM; k += blockDim.x) {
         s_pd[k] = d.PD[k];
         s_r[k] = A2(d.R, d.JM, k + 1);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
+        DevCtl *c = d.ctl;
+        // throttle exit condition (4488-4505): the exit pressures follow the
+        // exit mass flow of the last tail
+        const bool throttle = d.THROTTLE_EXIT > 0.001f;
+        float PTHROTTLE = 0.0f, PDMID = 0.0f;
+        if (c->nstep > 100 && throttle) {
+            float FFLOW = c->CHECK_FLOW_JM / d.THROTTLE_MAS;
+            PTHROTTLE = c->THROTTLE_PRES * FFLOW * FFLOW;
+            c->PDOWN_TIP = d.RFTHROTL1 * c->PDOWN_TIP + d.RFTHROTL * PTHROTTLE;
+            c->PDOWN_HUB = d.RFTHROTL1 * c->PDOWN_HUB + d.RFTHROTL * PTHROTTLE;
+            PDMID = PTHROTTLE - s_pd[d.KMID - 1];
+            float RF_P = 0.02f * d.RFTHROTL;
+            c->THROTTLE_PRES = (1.0f - RF_P) * c->THROTTLE_PRES + RF_P * PTHROTTLE;
+        }
+        const float PDOWN_HUB = c->PDOWN_HUB;
         float PDIFF = 0.0f;
-        if (d.IPOUT == -1) PDIFF = d.PDOWN_TIP - s_pd[d.KM - 1];
+        if (d.IPOUT == -1) PDIFF = c->PDOWN_TIP - s_pd[KM - 1];
         float SUMP = 0.0f;
-        for (int k = 1; k <= d.KM; ++k) {
-            s_pd[0] = d.PDOWN_HUB;
-            if (k != 1) {
-                float DP = (s_sum[k - 1] + SUMP) * 0.5f * (s_r[k - 1] - s_r[k - 2]);
-                s_pd[k - 1] = 0.9f * s_pd[k - 1] + 0.1f * (s_pd[k - 2] + DP);
+        for (int k = 1; k <= KM; ++k) {
+            if (d.IPOUT <= 0) {
+                s_pd[0] = PDOWN_HUB;
+                if (k != 1) {
+                    float DP = (s_sum[k - 1] + SUMP) * 0.5f * (s_r[k - 1] - s_r[k - 2]);
+                    s_pd[k - 1] = 0.9f * s_pd[k - 1] + 0.1f * (s_pd[k - 2] + DP);
+                }
+                SUMP = s_sum[k - 1];
+                if (d.IPOUT == -1) s_pd[k - 1] = s_pd[k - 1] + PDIFF;
             }
-            SUMP = s_sum[k - 1];
-            if (d.IPOUT == -1) s_pd[k - 1] = s_pd[k - 1] + PDIFF;
+            if (d.IPOUT >= 1 && throttle) s_pd[k - 1] = s_pd[k - 1] + d.RFTHROTL * PDMID;
+            if (plate) s_pd[k - 1] = s_pd[k - 1] + 0.01f * d.PLATE_LOSS * (s_rov[k] - s_rov[d.KMID]);
+            // the exit update of this K uses PD(K) as it is now; PD(1) is reset
+            // again at the next K
+            d.BCBUF[3 * KM + k - 1] = s_pd[k - 1];
         }
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < d.KM; k += blockDim.x) d.PD[k] = s_pd[k];
+    for (int k = threadIdx.x; k < KM; k += blockDim.x) d.PD[k] = s_pd[k];
 }
 
 __global__ void k_bc_apply(Dev d) {
@@ -394,7 +431,7 @@ __global__ void k_bc_apply(Dev d) {
     // exit: pitchwise pressure variation extrapolated from upstream
     float vr = A3(d.VR, i, d.JM, k), vt = A3(d.VT, i, d.JM, k), vx = A3(d.VX, i, d.JM, k);
     float EKE = 0.5f * (vr * vr + vt * vt + vx * vx);
-    float pe = A1(d.PD, k) + d.FEXTRAP * (A3(d.P, i, d.JMM1, k) - d.BCBUF[2 * d.KM + k - 1]);
+    float pe = d.BCBUF[3 * d.KM + k - 1] + d.FEXTRAP * (A3(d.P, i, d.JMM1, k) - d.BCBUF[2 * d.KM + k - 1]);
     float hoe = 2.0f * A3(d.HO, i, d.JMM1, k) - A3(d.HO, i, d.JM - 2, k);
     float TEXIT = (hoe - EKE) / d.CP;
     float roe_ = pe / d.RGAS / TEXIT;
@@ -404,7 +441,7 @@ __global__ void k_bc_apply(Dev d) {
     A3(d.ROE, i, d.JM, k) = roe_ * (d.CV * TEXIT + EKE);
 }
 
-static size_t bc_sums_smem(const Dev &d) { return (size_t)32 * 4 * d.IMM1 * sizeof(float); }
+static size_t bc_sums_smem(const Dev &d) { return (size_t)32 * (4 * d.IMM1 + 2 * d.IM) * sizeof(float); }
 
 cudaError_t configure_flux_kernels(const Dev &d) {
     size_t b = bc_sums_smem(d);
@@ -417,6 +454,139 @@ void launch_bc(const Dev &d, Launch L) {
     mark(L, "k_bc_sums");
     launchk(L, k_bc_apply, dim3((d.IM * d.KM + 127) / 128), dim3(128), 0, d);
     mark(L, "k_bc_apply");
+}
+
+// ---------------------------------------------------------------------
+// SETFLO (8006-8052), IN_FLOW != 0: relax the mass flow of every J station
+// towards FLOWIN (IN_FLOW = 3) or the mean flow.  k_setflo_flow forms FLOW(J)
+// (one CTA per J; REDUCE_ORDER = 1: one thread in the reference's K, I
+// order, otherwise an FP64 tree of the same terms); k_setflo_apply scales
+// ROVX, ROVR and ROVT of plane J.
+// ---------------------------------------------------------------------
+constexpr int SF_BS = 256;
+
+__global__ void __launch_bounds__(SF_BS) k_setflo_flow(Dev d) {
+    pdl_wait();
+    const int j = blockIdx.x + 1;
+    const int IMM1 = d.IMM1, KMM1 = d.KMM1;
+    const float NBJ = (float)A1(d.NBLADE, j), NB1 = (float)A1(d.NBLADE, 1);
+    if (d.REDUCE_ORDER == 1) {
+        if (threadIdx.x == 0) {
+            float f = 0.0f;
+            for (int k = 1; k <= KMM1; ++k)
+                for (int i = 1; i <= IMM1; ++i) f = f - A3(d.FLOWX, i, j, k) * NBJ / NB1;
+            d.FLOWJ[j - 1] = f;
+        }
+        return;
+    }
+    double s = 0.0;
+    for (int c = threadIdx.x; c < IMM1 * KMM1; c += SF_BS) {
+        int i = c % IMM1 + 1, k = c / IMM1 + 1;
+        s += (double)(A3(d.FLOWX, i, j, k) * NBJ / NB1);
+    }
+    __shared__ double sh[SF_BS / 32];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < SF_BS / 32; ++w) t += sh[w];
+        d.FLOWJ[j - 1] = (float)(-t);
+    }
+}
+
+__global__ void __launch_bounds__(SF_BS) k_setflo_apply(Dev d) {
+    pdl_wait();
+    const int j = blockIdx.x + 1;
+    __shared__ float s_delta;
+    if (threadIdx.x == 0) {
+        float AVFLOW = d.FLOWIN / (float)A1(d.NBLADE, 1);
+        if (d.IN_FLOW != 3) {
+            if (d.REDUCE_ORDER == 1) {
+                float a = 0.0f;
+                for (int jj = 1; jj <= d.JM; ++jj) a = a + d.FLOWJ[jj - 1];
+                AVFLOW = a / (float)d.JM;
+            } else {
+                double a = 0.0;
+                for (int jj = 1; jj <= d.JM; ++jj) a += (double)d.FLOWJ[jj - 1];
+                AVFLOW = (float)(a / (double)d.JM);
+            }
+        }
+        float a = A3(d.ROVX, d.IMID, j, d.KMID), b = A3(d.ROVR, d.IMID, j, d.KMID);
+        float ROVMER = sqrtf(a * a + b * b);
+        float DELTA = (AVFLOW / d.FLOWJ[j - 1] - 1.0f) * ROVMER;
+        s_delta = DELTA * d.RFLOW;
+    }
+    __syncthreads();
+    const float DELTA = s_delta;
+    const int IM = d.IM;
+    for (int t = threadIdx.x; t < IM * d.KM; t += SF_BS) {
+        int i = t % IM + 1, k = t / IM + 1;
+        const int n = ix3(d, i, j, k);
+        float x = d.ROVX[n], r = d.ROVR[n];
+        float RM = sqrtf(x * x + r * r);
+        if (x < 0.0f) RM = -RM;
+        d.ROVX[n] = x + x / RM * DELTA;
+        d.ROVR[n] = r + r / RM * DELTA;
+        float RO_WT = d.ROVT[n] - A2(d.UBLADE, j, k) * d.RO[n];
+        d.ROVT[n] = d.ROVT[n] + RO_WT / RM * DELTA;
+    }
+}
+
+void launch_setflo(const Dev &d, Launch L) {
+    launchk(L, k_setflo_flow, dim3(d.JM), dim3(SF_BS), 0, d);
+    mark(L, "k_setflo_flow");
+    launchk(L, k_setflo_apply, dim3(d.JM), dim3(SF_BS), 0, d);
+    mark(L, "k_setflo_apply");
+}
+
+// ---------------------------------------------------------------------
+// IF_CUSP = 2 (5178-5233): forced separation at the trailing edge of a row.
+// One thread per (row, K) runs the suction-side points (I = 1..6) and then
+// the pressure-side points (I = IM-6..IM), as the reference orders them;
+// the rows' ranges are disjoint (checked at commit).
+// ---------------------------------------------------------------------
+__global__ void k_cusp_sep(Dev d) {
+    pdl_wait();
+    const int nr = blockIdx.x + 1;
+    if (A1(d.IF_CUSP, nr) != 2) return;
+    const int IM = d.IM;
+    const int JTEDGE = A1(d.JTE, nr);
+    const int JSEP_I1 = JTEDGE - A1(d.NUP_I1, nr), JSEP_IM = JTEDGE - A1(d.NUP_IM, nr);
+    const int JTHIK = JSEP_I1 > JSEP_IM ? JSEP_I1 : JSEP_IM;
+    const float FDRAG = A1(d.SEP_DRAG, nr);
+    const int NWKE = A1(d.N_WAKE, nr);
+    for (int k = threadIdx.x + 1; k <= d.KM; k += blockDim.x) {
+        auto force = [&](int i, int j) {
+            const int n = ix3(d, i, j, k);
+            d.ROVX[n] = FDRAG * d.ROVX[n];
+            d.ROVR[n] = FDRAG * d.ROVR[n];
+            float RO_VBLADE = d.RO[n] * A2(d.UBLADE, j, k);
+            float RO_WT = d.ROVT[n] - RO_VBLADE;
+            float RO_VT = FDRAG * RO_WT + RO_VBLADE;
+            d.RORVT[n] = RO_VT * A2(d.R, j, k);
+        };
+        const float THIK_LIM = A1(d.SEP_THIK, nr) * A2(d.RT_THICK, JTHIK, k);
+        const float SSSLOPE = (A3(d.RTHETA, 1, JSEP_I1 + 1, k) - A3(d.RTHETA, 1, JSEP_I1 - 1, k)) /
+                              (A2(d.X, JSEP_I1 + 1, k) - A2(d.X, JSEP_I1 - 1, k));
+        const float PSSLOPE = (A3(d.RTHETA, IM, JSEP_IM + 1, k) - A3(d.RTHETA, IM, JSEP_IM - 1, k)) /
+                              (A2(d.X, JSEP_IM + 1, k) - A2(d.X, JSEP_IM - 1, k));
+        for (int j = JSEP_I1; j <= JTEDGE + NWKE; ++j) {
+            float RTEXTRAP = A3(d.RTHETA, 1, JSEP_I1, k) + SSSLOPE * (A2(d.X, j, k) - A2(d.X, JSEP_I1, k));
+            for (int i = 1; i <= 6; ++i)
+                if ((RTEXTRAP - A3(d.RTHETA, i, j, k)) > THIK_LIM) force(i, j);
+        }
+        for (int j = JSEP_IM; j <= JTEDGE + NWKE; ++j) {
+            float RTEXTRAP = A3(d.RTHETA, IM, JSEP_IM, k) + PSSLOPE * (A2(d.X, j, k) - A2(d.X, JSEP_IM, k));
+            for (int i = IM - 6; i <= IM; ++i)
+                if ((A3(d.RTHETA, i, j, k) - RTEXTRAP) > THIK_LIM) force(i, j);
+        }
+    }
+}
+
+void launch_cusp(const Dev &d, Launch L) {
+    launchk(L, k_cusp_sep, dim3(d.NROWS), dim3(64), 0, d);
+    mark(L, "k_cusp_sep");
 }
 
 // ---------------------------------------------------------------------

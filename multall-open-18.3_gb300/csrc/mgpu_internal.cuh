@@ -52,6 +52,9 @@ struct DevCtl {
     int health;
     double flow_in, flow_out;
     DevMon mon;
+    // exit pressures that the throttle condition moves from step to step
+    // (4488-4505), and CHECK_FLOW(JM) of the last tail
+    float PDOWN_HUB, PDOWN_TIP, THROTTLE_PRES, CHECK_FLOW_JM;
 };
 
 // One conserved variable's TSTEP operands and work arrays.  The five
@@ -85,6 +88,8 @@ struct Dev {
     // gas constants and loop constants (SETUP 6459-6468, LOOP 3677-3709)
     float GA1, FGA, RFGA, RCP, CV, RCV, RGAS;
     float RO_REF, ROLIM, RIJKM, PREFF, RFIN1, RFIN2, TCOOL_MIN;
+    float RFTHROTL1;                   // 1 - RFTHROTL (reader 559)
+    int any_cusp2;                     // some row has IF_CUSP = 2
     // COMMON arrays on the device
 #define MGPU_DEV_A(n, t, s, r) MGPU_T_##t *n;
     MGPU_ARRAYS(MGPU_DEV_A)
@@ -99,7 +104,8 @@ struct Dev {
     float *FILAM, *FITURB, *FIWAKE, *FIUP, *FKLAM, *FKTURB;   // (NROWS, IM|KM)
     float *VLIMIT, *ROLIMIT;           // (NROWS)
     int *DFLAG;                        // (IM*KM) density-limiter column flags
-    float *BCBUF;                      // (3, KM) PAVG2, PAVG3, PAVGOUT of the exit/inlet BCs
+    float *BCBUF;                      // (4, KM) PAVG2, PAVG3, PAVGOUT, and the PD each K's exit update uses
+    float *FLOWJ;                      // (JM) SETFLO's FLOW(J)
     double *BLADE_FLOW;                // (JM)
     // per-block reduction partials of the 5-step tail
     double *part_sum;
@@ -208,6 +214,8 @@ void launch_loss(const Dev &d, Launch L, bool init_call);
 void launch_flux_mass(const Dev &d, Launch L);
 void launch_flux_energy(const Dev &d, Launch L);
 void launch_bc(const Dev &d, Launch L);
+void launch_setflo(const Dev &d, Launch L);       // IN_FLOW != 0
+void launch_cusp(const Dev &d, Launch L);         // IF_CUSP = 2 rows
 void launch_peff(const Dev &d, Launch L);
 void launch_flux_mom(const Dev &d, Launch L);   // XMOM, RVT and RMOM fluxes
 // TSTEP for the nv variables v0 .. v0+nv-1 of d.var

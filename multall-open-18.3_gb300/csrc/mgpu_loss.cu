@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(256) k_pwallgrad_cells(const __grid_constant__
     const int IMM1 = d.IMM1, KMM1 = d.KMM1;
     if (t >= IMM1 * KMM1 * (d.JM - 1)) return;
     const int i = t % IMM1 + 1, q = t / IMM1, k = q % KMM1 + 1, j = q / KMM1 + 2;
-    float PDIV = 0.5f * (d.PDOWN_HUB + d.PDOWN_TIP);
+    float PDIV = 0.5f * (d.ctl->PDOWN_HUB + d.ctl->PDOWN_TIP);
     PDIV = PDIV / (float)d.NROWS;
     PDIV = PDIV / (A1(d.CHORD, 1) + A1(d.CHORD, d.NROWS));
     const float DPDS_LIM = fabsf(20.0f * (A1(d.PO1, d.KMID) - PDIV));
@@ -886,6 +886,7 @@ __global__ void k_tail_final(Dev d, int nparts) {
             }
         }
         c->ECONT = econt;
+        c->CHECK_FLOW_JM = (float)d.BLADE_FLOW[d.JM - 1];   // CHECK_FLOW(JM) for the throttle
         c->JCONT = jc;
         c->flow_in = d.BLADE_FLOW[0];
         c->flow_out = d.BLADE_FLOW[d.JM - 1];

@@ -55,6 +55,13 @@ class RowSpec:
     pdn: float = 0.0
     stage: int = 1          # NSTAGE(NR)
     xllim: tuple = (0.03, 0.03, 0.03, 0.03, 0.03, 0.02)  # XLLIM_I1,IM,K1,KM,DWN,UP
+    # IF_CUSP = 2: forced trailing-edge separation (multall-open-18.3.f:987-1005)
+    if_cusp: int = 0
+    nup_i1: int = 0         # NUP_I1, NUP_IM: points before the TE where it starts
+    nup_im: int = 0
+    n_wake: int = 0         # N_WAKE: points into the wake
+    sep_thik: float = 0.0   # SEP_THIK: fraction of the blade thickness
+    sep_drag: float = 1.0   # SEP_DRAG: momentum factor in the separated region
 
 
 @dataclasses.dataclass
@@ -109,6 +116,14 @@ class CaseSpec:
     nmixup: int = 1000
     nlos: int = 5
     in_vr: int = 0
+    in_flow: int = 0            # IN_FLOW: 0 off, 3 towards FLOWIN, otherwise towards the mean flow
+    flowin: float = 0.0         # FLOWIN (kg/s through all blade passages)
+    rflow: float = 0.0          # RFLOW relaxation
+    plate_loss: float = 0.0     # PLATE_LOSS (exit spanwise loss)
+    throttle_exit: float = 0.0  # THROTTLE_EXIT marker, with THROTTLE_PRES, THROTTLE_MAS, RFTHROTL
+    throttle_pres: float = 0.0
+    throttle_mas: float = 0.0
+    rfthrotl: float = 0.0
 
 
 def geometric_spacing(n_intervals: int, ratio: float, fmax: float) -> np.ndarray:

@@ -528,7 +528,7 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None) -> CommonData:
 
     # ---------------- publish --------------------------------------------
     ints = dict(ITIMST=3, ILOS=10, NLOS=spec.nlos, IBOUND=0, IFMIX=spec.ifmix, IPOUT=spec.ipout,
-                IN_PRESS=0, IN_VTAN=0, IN_VR=spec.in_vr, IN_FLOW=0, IF_REPEAT=0, NRSMTH=0, NSFEXIT=0,
+                IN_PRESS=0, IN_VTAN=0, IN_VR=spec.in_vr, IN_FLOW=spec.in_flow, IF_REPEAT=0, NRSMTH=0, NSFEXIT=0,
                 NSTEPS_MAX=spec.nsteps_max, NCHANGE=spec.nchange, NMIXUP=spec.nmixup, IF_RESTART=0,
                 IR=IR, JR=JR, KR=KR, NIB1=NIB1, NJB1=NJB1, NKB1=NKB1, NIB2=NIB2, NJB2=NJB2,
                 NKB2=NKB2, NSBLK=NSBLK, NSTAGES=NSTAGES, IFGAS=0, IFCOOL=0, IFBLEED=0, IFSHROUD=0)
@@ -540,7 +540,9 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None) -> CommonData:
                  SFEXIT=0.0, RSMTH=0.4, F1=2.0, F2=-1.0, F3=0.0, REYNO=spec.reyno, RF_VIS=spec.rf_vis,
                  FTRANS=spec.ftrans, PRANDTL=spec.prandtl, YPLUSWALL=spec.ypluswall, YPLAM=5.0,
                  YPTURB=25.0, CFWALL=0.0, FACMIXUP=spec.facmixup, PDOWN_HUB=spec.pdown_hub,
-                 PDOWN_TIP=spec.pdown_tip, PLATE_LOSS=0.0, THROTTLE_EXIT=0.0, VSOUND=float(VSOUND),
+                 PDOWN_TIP=spec.pdown_tip, PLATE_LOSS=spec.plate_loss, THROTTLE_EXIT=spec.throttle_exit,
+                 THROTTLE_PRES=spec.throttle_pres, THROTTLE_MAS=spec.throttle_mas, RFTHROTL=spec.rfthrotl,
+                 FLOWIN=spec.flowin, RFLOW=spec.rflow, VSOUND=float(VSOUND),
                  CONLIM=spec.conlim, VISLAM=0.0, FTCOND=0.0)
     if spec.itimst == -3:
         reals.update(F2=-1.65, F3=-0.65)
@@ -549,7 +551,13 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None) -> CommonData:
         JSTART=JSTART, JMIX=JMIX, JLE=JLE, JTE=JTE, JLED=JLED, KTIPS=KTIPS, KTIPE=KTIPE, KS1=KS1, KS2=KS2,
         JTRAN_I1=np.zeros(NROWS, np.int32), JTRAN_IM=np.zeros(NROWS, np.int32),
         JTRAN_K1=np.zeros(NROWS, np.int32), JTRAN_KM=np.zeros(NROWS, np.int32),
-        IF_CUSP=np.zeros(NROWS, np.int32),
+        IF_CUSP=np.array([r.if_cusp for r in spec.rows], np.int32),
+        NUP_I1=np.array([r.nup_i1 for r in spec.rows], np.int32),
+        NUP_IM=np.array([r.nup_im for r in spec.rows], np.int32),
+        N_WAKE=np.array([r.n_wake for r in spec.rows], np.int32),
+        SEP_THIK=np.array([r.sep_thik for r in spec.rows], f32),
+        SEP_DRAG=np.array([r.sep_drag for r in spec.rows], f32),
+        RT_THICK=RT_THICK, RTHETA=RTHETA,
         XLLIM_I1=xl[:, 0], XLLIM_IM=xl[:, 1], XLLIM_K1=xl[:, 2], XLLIM_KM=xl[:, 3], XLLIM_DWN=xl[:, 4],
         XLLIM_UP=xl[:, 5], ROUGH_H=np.zeros(NROWS, f32), ROUGH_T=np.zeros(NROWS, f32),
         ROUGH_L=np.zeros(NROWS, f32), ROUGH_U=np.zeros(NROWS, f32), CHORD=CHORD,

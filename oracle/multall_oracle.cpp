@@ -87,6 +87,7 @@ struct Oracle : OracleBase {
 
     /* COMMON variables the loop derives (SETUP 6459-6468, LOOP 3677-3709) */
     R GA1, FGA, RFGA, RCP, CV, RCV, RGAS;
+    R RFTHROTL1 = R(1);
     R RO_REF, ROMIN, ROLIM, RIJKM, PREFF, RFIN1, RFIN2, TCOOL_MIN;
     R SFT = 0, SFX = 0, DAMP = 0, SFT1, SFTH, SFX1, SFXH, SFX15, SFX14, SFXB, SFXB1, SFXBH, SFXHM1;
     R FMIXUP = 1, ECONT, EAVG, EMAX, VRMS = 0, VMAX = 0, TCOND;
@@ -218,7 +219,8 @@ struct Oracle : OracleBase {
     /* ------------------------------------------------------------------ */
     int commit() override {
         if (IM <= 2 || KM <= 2) return fail(MGPU_E_UNSUPPORTED, "IM=2 (throughflow) or KM=2 (Q3D) not covered");
-#define O_CHK_A(nm, t, s, r) if (!nm##_set && std::string(#r) != "OUT") return fail(MGPU_E_ARG, "array not bound: " #nm);
+#define O_CHK_A(nm, t, s, r) \
+    if (!nm##_set && std::string(#r) != "OUT" && std::string(#r) != "OPT") return fail(MGPU_E_ARG, "array not bound: " #nm);
         MGPU_ARRAYS(O_CHK_A)
 #define O_CHK_I(nm, d) if (nm == MGPU_REQUIRED_INT) return fail(MGPU_E_ARG, "integer not set: " #nm);
         MGPU_INT_SCALARS(O_CHK_I)
@@ -228,11 +230,17 @@ struct Oracle : OracleBase {
         if (ILOS != 10) return fail(MGPU_E_UNSUPPORTED, "only ILOS=10 (mixing-length LOSS) is covered");
         if (IFGAS != 0) return fail(MGPU_E_UNSUPPORTED, "real-gas IFGAS=1 not covered");
         if (IFCOOL || IFBLEED || IFSHROUD) return fail(MGPU_E_UNSUPPORTED, "cooling/bleed/shroud not covered");
-        if (IN_FLOW != 0 || IF_REPEAT != 0) return fail(MGPU_E_UNSUPPORTED, "IN_FLOW/IF_REPEAT not covered");
-        if (PLATE_LOSS > R(0.001) || THROTTLE_EXIT > R(0.001)) return fail(MGPU_E_UNSUPPORTED, "plate loss/throttle not covered");
+        if (IF_REPEAT != 0) return fail(MGPU_E_UNSUPPORTED, "IF_REPEAT not covered");
         if (IPOUT == 3 || IPOUT < -1) return fail(MGPU_E_UNSUPPORTED, "IPOUT not covered");
-        for (int nr = 1; nr <= NROWS; ++nr)
-            if (F1(IF_CUSP, nr) >= 2) return fail(MGPU_E_UNSUPPORTED, "IF_CUSP=2 not covered");
+        if (THROTTLE_EXIT > R(0.001) && THROTTLE_MAS == R(0)) return fail(MGPU_E_ARG, "THROTTLE_MAS must be set with THROTTLE_EXIT");
+        bool cusp2 = false;
+        for (int nr = 1; nr <= NROWS; ++nr) {
+            if (F1(IF_CUSP, nr) > 2) return fail(MGPU_E_UNSUPPORTED, "IF_CUSP above 2 not covered");
+            if (F1(IF_CUSP, nr) == 2) cusp2 = true;
+        }
+        if (cusp2 && !(NUP_I1_set && NUP_IM_set && N_WAKE_set && SEP_THIK_set && SEP_DRAG_set && RT_THICK_set && RTHETA_set))
+            return fail(MGPU_E_ARG, "IF_CUSP=2 needs NUP_I1, NUP_IM, N_WAKE, SEP_THIK, SEP_DRAG, RT_THICK and RTHETA");
+        RFTHROTL1 = R(1.0) - RFTHROTL;
         if (NCHANGE <= 0 || NMIXUP <= 0) return fail(MGPU_E_ARG, "NCHANGE and NMIXUP must be positive");
 
         size_t n3 = (size_t)IM * JM * KM;
@@ -1496,6 +1504,7 @@ struct Oracle : OracleBase {
         energy_fluxes();
         tstep(ROE_v, DROE_v);
         boundary_conditions();
+        if (IN_FLOW != 0) setflo();
         /* PEFF 4321 */
         for (int k = 1; k <= KM; ++k)
             for (int j = 1; j <= JM; ++j) {
@@ -1511,6 +1520,7 @@ struct Oracle : OracleBase {
         tstep(ROVR_v, DROVR_v);
         limiters();
         if (IFMIX > 0 && RFMIX > R(1.0E-3)) new_mixplan();
+        cusp_separation();
 
         int rc = 0;
         if (mon) {
@@ -1637,7 +1647,106 @@ struct Oracle : OracleBase {
     }
 
     /* inlet and exit boundary conditions 4476-4734 (ITIMST<5, IFGAS=0) */
+    /* ================================================================== */
+    /*  SETFLO   multall-open-18.3.f:8006-8052: relax the mass flow of     */
+    /*  every J station towards FLOWIN (IN_FLOW=3) or towards the mean     */
+    /*  flow (other nonzero IN_FLOW)                                        */
+    /* ================================================================== */
+    void setflo() {
+        std::vector<R> FLOW((size_t)JM + 1, R(0));
+        for (int j = 1; j <= JM; ++j) {
+            FLOW[j] = R(0.0);
+            for (int k = 1; k <= KMM1; ++k)
+                for (int i = 1; i <= IMM1; ++i)
+                    FLOW[j] = FLOW[j] - A3(FLOWX, i, j, k) * R(F1(NBLADE, j)) / R(F1(NBLADE, 1));
+        }
+        R AVFLOW = FLOWIN / R(F1(NBLADE, 1));
+        if (IN_FLOW != 3) {
+            AVFLOW = R(0.0);
+            for (int j = 1; j <= JM; ++j) AVFLOW = AVFLOW + FLOW[j];
+            AVFLOW = AVFLOW / R(JM);
+        }
+        for (int j = 1; j <= JM; ++j) {
+            R a = F3(ROVX, IMID, j, KMID), b = F3(ROVR, IMID, j, KMID);
+            R ROVMER = std::sqrt(a * a + b * b);
+            R DELTA = (AVFLOW / FLOW[j] - R(1.0)) * ROVMER;
+            DELTA = DELTA * RFLOW;
+            for (int i = 1; i <= IM; ++i)
+                for (int k = 1; k <= KM; ++k) {
+                    R x = F3(ROVX, i, j, k), r = F3(ROVR, i, j, k);
+                    R RM = std::sqrt(x * x + r * r);
+                    if (x < R(0.0)) RM = -RM;
+                    F3(ROVX, i, j, k) = x + x / RM * DELTA;
+                    F3(ROVR, i, j, k) = r + r / RM * DELTA;
+                    R RO_WT = F3(ROVT, i, j, k) - F2(UBLADE, j, k) * F3(RO, i, j, k);
+                    F3(ROVT, i, j, k) = F3(ROVT, i, j, k) + RO_WT / RM * DELTA;
+                }
+        }
+    }
+
+    /* ================================================================== */
+    /*  IF_CUSP = 2: forced trailing-edge separation, 5178-5233            */
+    /* ================================================================== */
+    void cusp_separation() {
+        for (int nr = 1; nr <= NROWS; ++nr) {
+            if (F1(IF_CUSP, nr) != 2) continue;
+            int JTEDGE = F1(JTE, nr);
+            int JSEP_I1 = JTEDGE - F1(NUP_I1, nr), JSEP_IM = JTEDGE - F1(NUP_IM, nr);
+            int JTHIK = std::max(JSEP_I1, JSEP_IM);
+            R FDRAG = F1(SEP_DRAG, nr);
+            int NWKE = F1(N_WAKE, nr);
+            auto force = [&](int i, int j, int k) {
+                F3(ROVX, i, j, k) = FDRAG * F3(ROVX, i, j, k);
+                F3(ROVR, i, j, k) = FDRAG * F3(ROVR, i, j, k);
+                R RO_VBLADE = F3(RO, i, j, k) * F2(UBLADE, j, k);
+                R RO_WT = F3(ROVT, i, j, k) - RO_VBLADE;
+                R RO_VT = FDRAG * RO_WT + RO_VBLADE;
+                F3(RORVT, i, j, k) = RO_VT * F2(R, j, k);
+            };
+            for (int k = 1; k <= KM; ++k) {
+                R THIK_LIM = F1(SEP_THIK, nr) * F2(RT_THICK, JTHIK, k);
+                R SSSLOPE = (F3(RTHETA, 1, JSEP_I1 + 1, k) - F3(RTHETA, 1, JSEP_I1 - 1, k)) /
+                            (F2(X, JSEP_I1 + 1, k) - F2(X, JSEP_I1 - 1, k));
+                R PSSLOPE = (F3(RTHETA, IM, JSEP_IM + 1, k) - F3(RTHETA, IM, JSEP_IM - 1, k)) /
+                            (F2(X, JSEP_IM + 1, k) - F2(X, JSEP_IM - 1, k));
+                for (int j = JSEP_I1; j <= JTEDGE + NWKE; ++j) {
+                    R RTEXTRAP = F3(RTHETA, 1, JSEP_I1, k) + SSSLOPE * (F2(X, j, k) - F2(X, JSEP_I1, k));
+                    for (int i = 1; i <= 6; ++i)
+                        if ((RTEXTRAP - F3(RTHETA, i, j, k)) > THIK_LIM) force(i, j, k);
+                }
+                for (int j = JSEP_IM; j <= JTEDGE + NWKE; ++j) {
+                    R RTEXTRAP = F3(RTHETA, IM, JSEP_IM, k) + PSSLOPE * (F2(X, j, k) - F2(X, JSEP_IM, k));
+                    for (int i = IM - 6; i <= IM; ++i)
+                        if ((F3(RTHETA, i, j, k) - RTEXTRAP) > THIK_LIM) force(i, j, k);
+                }
+            }
+        }
+    }
+
     void boundary_conditions() {
+        // exit "plate loss" (4476-4484): pitchwise sums of ROV_m**2 at JM.  The
+        // normalising statement after the loop runs once, with K = KM+1, so
+        // the sums themselves are used below
+        std::vector<R> ROVMSQ((size_t)KM + 2, R(0));
+        if (PLATE_LOSS > R(0.001)) {
+            for (int k = 1; k <= KM; ++k) {
+                ROVMSQ[k] = R(0.0);
+                for (int i = 1; i <= IM; ++i)
+                    ROVMSQ[k] = ROVMSQ[k] + F3(ROVX, i, JM, k) * F3(VX, i, JM, k) + F3(ROVR, i, JM, k) * F3(VR, i, JM, k);
+            }
+            ROVMSQ[KM + 1] = R(0.5) * ROVMSQ[KM + 1] / R(IM);
+        }
+        // throttle exit condition (4488-4505)
+        R PTHROTTLE = R(0.0), PDMID = R(0.0);
+        if (NSTEP > 100 && THROTTLE_EXIT > R(0.001)) {
+            R FFLOW = CHECK_FLOW[JM - 1] / THROTTLE_MAS;
+            PTHROTTLE = THROTTLE_PRES * FFLOW * FFLOW;
+            PDOWN_TIP = RFTHROTL1 * PDOWN_TIP + RFTHROTL * PTHROTTLE;
+            PDOWN_HUB = RFTHROTL1 * PDOWN_HUB + RFTHROTL * PTHROTTLE;
+            PDMID = PTHROTTLE - F1(PD, KMID);
+            R RF_P = R(0.02) * RFTHROTL;
+            THROTTLE_PRES = (R(1.) - RF_P) * THROTTLE_PRES + RF_P * PTHROTTLE;
+        }
         R PDIFF = R(0.0);
         if (IPOUT == -1) PDIFF = PDOWN_TIP - F1(PD, KM);
         R SUMP = R(0);
@@ -1660,6 +1769,8 @@ struct Oracle : OracleBase {
                 SUMP = SUM;
                 if (IPOUT == -1) F1(PD, k) = F1(PD, k) + PDIFF;
             }
+            if (IPOUT >= 1 && THROTTLE_EXIT > R(0.001)) F1(PD, k) = F1(PD, k) + RFTHROTL * PDMID;
+            if (PLATE_LOSS > R(0.001)) F1(PD, k) = F1(PD, k) + R(0.01) * PLATE_LOSS * (ROVMSQ[k] - ROVMSQ[KMID]);
             for (int i = 1; i <= IM; ++i) {
                 R RO_STAG = F1(PO1, k) / RGAS / F1(TO1, k);
                 R RO_IN = F3(RO, i, 1, k);

@@ -104,6 +104,59 @@ def test_pressure_gradient_wall_functions(mods, ypluswall):
              "step 5")
 
 
+def _option_spec(case, opt):
+    spec = case.small_stage()
+    if opt == "ipout_minus1":
+        spec.ipout = -1
+    elif opt == "plate_loss":
+        spec.plate_loss = 2.0
+    elif opt == "setflo_mean":
+        spec.in_flow, spec.rflow = 2, 0.05
+    elif opt == "setflo_target":
+        spec.in_flow, spec.rflow, spec.flowin = 3, 0.05, 12.0
+    elif opt == "cusp2":
+        for r in spec.rows:
+            r.if_cusp, r.nup_i1, r.nup_im, r.n_wake, r.sep_thik, r.sep_drag = 2, 3, 3, 2, 0.2, 0.9
+    return spec
+
+
+@pytest.mark.parametrize("opt", ["ipout_minus1", "plate_loss", "setflo_mean", "setflo_target", "cusp2"])
+def test_optional_branches(mods, opt):
+    """The loop's optional branches: IPOUT=-1 (tip-pressure offset, with the
+    K=1 exit update using the offset PD(1) before the next K resets it),
+    the exit plate loss, SETFLO towards the mean flow (IN_FLOW=2) and
+    towards FLOWIN (IN_FLOW=3), and the forced trailing-edge separation of
+    IF_CUSP=2.  One step within 1e-5, five steps within 1e-4."""
+    case = mods[0]
+    cd, gpu, ref = _pair(mods, _option_spec(case, opt))
+    gpu.step()
+    ref.step()
+    _compare(gpu, ref, STATE, STEP1_TOL, f"{opt} step 1")
+    for _ in range(4):
+        gpu.step()
+        ref.step()
+    _compare(gpu, ref, STATE + FORCES, 1e-4, f"{opt} step 5")
+
+
+def test_throttle_exit(mods):
+    """THROTTLE_EXIT: from step 101 the exit pressures follow the exit mass
+    flow of the last tail (4488-4505).  After 120 steps PDOWN_HUB, PDOWN_TIP
+    and THROTTLE_PRES agree with the FP32 oracle to 1e-5 and the flow field
+    to 1e-3."""
+    case = mods[0]
+    spec = case.small_stage()
+    spec.throttle_exit, spec.throttle_pres, spec.throttle_mas, spec.rfthrotl = 1.0, spec.pdown_hub, 14.08, 0.05
+    cd, gpu, ref = _pair(mods, spec)
+    gpu.run(120)
+    for _ in range(120):
+        ref.step()
+    for n in ("PDOWN_HUB", "PDOWN_TIP", "THROTTLE_PRES"):
+        g, r = gpu.get_real(n), ref.get_real(n)
+        assert abs(g - r) <= 1e-5 * abs(r), (n, g, r)
+    assert abs(ref.get_real("PDOWN_HUB") - spec.pdown_hub) > 100.0     # the throttle did move it
+    _compare(gpu, ref, ["RO", "ROVX", "ROE", "P"], 1e-3, "throttle step 120")
+
+
 def test_sss_scheme_one_step(mods):
     """ITIMST=-3 (SSS): F2/F3 history terms and SMOOTH_RESID."""
     case = mods[0]
