@@ -974,10 +974,20 @@ __global__ void __launch_bounds__(MIX_BS) k_mixplan(Dev d) {
             }
         }
         float ROTN = ALPHAA[IM - 1] - ALPHAA[0];
-        float SUMFP = 0.0f;
-        for (int i = 1; i <= IM; ++i) {
-            ALPHAA[i - 1] = ALPHAA[i - 1] - ROTN * (SUMFP - 0.5f);
-            SUMFP = SUMFP + A1(d.FP, i);
+        // periodicity correction (15177-15182); FP64 running sum in the
+        // default precision split, REAL*4 with REDUCE_ORDER = 1
+        if (d.REDUCE_ORDER == 1) {
+            float SUMFP = 0.0f;
+            for (int i = 1; i <= IM; ++i) {
+                ALPHAA[i - 1] = ALPHAA[i - 1] - ROTN * (SUMFP - 0.5f);
+                SUMFP = SUMFP + A1(d.FP, i);
+            }
+        } else {
+            double SUMFP = 0.0;
+            for (int i = 1; i <= IM; ++i) {
+                ALPHAA[i - 1] = (float)((double)ALPHAA[i - 1] - (double)ROTN * (SUMFP - 0.5));
+                SUMFP += (double)A1(d.FP, i);
+            }
         }
     }
     __syncthreads();

@@ -61,6 +61,20 @@ __device__ inline int mp_role(const Dev &d, int j, int *nr) {
     return 0;
 }
 
+// Pitchwise sum of a mixing-plane line in I order: REAL*4 as the reference
+// forms it (REDUCE_ORDER = 1), or accumulated in FP64 and rounded once (the
+// default precision split: FP64 for the mixing-plane circumferential sums).
+__device__ inline float mp_line_sum(const float *row, int n, bool exact32) {
+    if (exact32) {
+        float s = 0.0f;
+        for (int i = 0; i < n; ++i) s = s + row[i];
+        return s;
+    }
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += (double)row[i];
+    return (float)s;
+}
+
 // (i, k) of the points t = start, start + stride, ... of an ni-wide plane,
 // 1-based, advanced without a division per point
 struct Walk2 {
@@ -111,9 +125,7 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_cells(const __grid_constant__ D
         __syncthreads();
         for (int k = threadIdx.x + 1; k <= KMM1; k += TS_BS) {
             const float *row = st + (size_t)(k - 1) * IMM1;
-            float s = 0.0f;
-            for (int i = 0; i < IMM1; ++i) s = s + row[i];
-            lsum[k - 1] = s;
+            lsum[k - 1] = mp_line_sum(row, IMM1, d.REDUCE_ORDER == 1);
         }
     }
     __syncthreads();
@@ -182,8 +194,7 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_cells(const __grid_constant__ D
             bool on = role == 3 ? (FLOWDIRN > 0.0f || lowx) : (FLOWDIRN < 0.0f || lowx);
             if (!on) continue;
             float *row = st + (size_t)(k - 1) * IMM1;
-            float s = 0.0f;
-            for (int i = 0; i < IMM1; ++i) s = s + row[i];
+            float s = mp_line_sum(row, IMM1, d.REDUCE_ORDER == 1);
             for (int i = 0; i < IMM1; ++i) row[i] = s * A1(d.FP, i + 1);
         }
         __syncthreads();
@@ -496,8 +507,7 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_update(const __grid_constant__ 
             bool on = role == 3 ? (FLOWDIRN > 0.0f || lowx) : (FLOWDIRN < 0.0f || lowx);
             if (!on) continue;
             float *row = c + (size_t)(k - 1) * IMM1;
-            float s = 0.0f;
-            for (int i = 0; i < IMM1; ++i) s = s + row[i];
+            float s = mp_line_sum(row, IMM1, d.REDUCE_ORDER == 1);
             s = s / (float)IMM1;
             for (int i = 0; i < IMM1; ++i) row[i] = s;
         }
@@ -805,8 +815,15 @@ __global__ void __launch_bounds__(SV_BS, 4) k_ts_smooth(const __grid_constant__ 
             if (j == A1(d.JMIX, r) || j == A1(d.JMIX, r) + 1) mp = true;
     if (mp) {
         for (int k = threadIdx.x + 1; k <= KM; k += SV_BS) {
-            float s = 0.0f;
-            for (int i = 1; i <= IMM1; ++i) s = s + A1(d.FP, i) * (P(a, i, k) + P(a, i + 1, k));
+            float s;
+            if (d.REDUCE_ORDER == 1) {
+                s = 0.0f;
+                for (int i = 1; i <= IMM1; ++i) s = s + A1(d.FP, i) * (P(a, i, k) + P(a, i + 1, k));
+            } else {
+                double s64 = 0.0;
+                for (int i = 1; i <= IMM1; ++i) s64 += (double)(A1(d.FP, i) * (P(a, i, k) + P(a, i + 1, k)));
+                s = (float)s64;
+            }
             b[k - 1] = 0.5f * s;
         }
         __syncthreads();

@@ -264,6 +264,36 @@ def test_converged_mass_flow_and_efficiency(mods):
     assert abs(ig.eta_tt - ir.eta_tt) <= 1e-4
 
 
+def test_precision_split_against_fp64_oracle(mods):
+    """The reported quantities against the FP64 oracle after 1500 steps of
+    the small stage: the default path (FP32 field arithmetic, FP64 for the
+    multigrid, row-mean, mixing-plane, monitor and integral sums) and the
+    plain FP32 path (REDUCE_ORDER=1) both keep mass flow within 1e-4
+    relative and total-to-total efficiency within 1e-4 absolute."""
+    case, common_setup, lib, O = mods
+    spec = case.small_stage()
+    cd = common_setup.build_common(spec)
+    cd.ints.update(NCHANGE=200, NMIXUP=200)
+    ref64 = O.Oracle(cd, double=True)
+    ref64.setup_calls()
+    n = 1500
+    for _ in range(n):
+        ref64.step()
+    i64 = ref64.integrals()
+    errs = {}
+    for order in (0, 1):
+        cd.ints["REDUCE_ORDER"] = order
+        gpu = lib.Problem(cd)
+        gpu.run(n)
+        ig = gpu.integrals()
+        errs[order] = (abs(ig.mass_flow_in - i64.mass_flow_in) / abs(i64.mass_flow_in), abs(ig.eta_tt - i64.eta_tt))
+        gpu.close()
+    cd.ints["REDUCE_ORDER"] = 0
+    print("mass-flow rel / eta abs error vs FP64 oracle: FP64 sums", errs[0], "plain FP32", errs[1])
+    for order, (em, ee) in errs.items():
+        assert em <= 1e-4 and ee <= 1e-4, (order, em, ee)
+
+
 def test_deterministic(mods):
     """Two runs of the same case are bitwise identical (no float atomics)."""
     case = mods[0]
