@@ -57,6 +57,8 @@ struct mgpu_handle {
     Dev d;
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;     // captures the bodies of conditional graph nodes
+    cudaStream_t aux = nullptr;      // a parallel branch of the step graph (k_bc_sums)
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int device = 0;
     int sm_count = 0;
     bool committed = false;
@@ -246,13 +248,21 @@ __global__ void k_delay(long long cycles) {
 // ROE and resets the momenta at J=1 before their update.  So the step runs
 // two batched TSTEPs, [RO, ROE] and [ROVX, RORVT, ROVR], with the boundary
 // conditions between them; every value is the same as in the serial order.
-void enqueue_core(const Dev &d, Launch L) {
+// join: when the step is captured as a graph, k_bc_sums already runs on a
+// branch forked after k_prim (capture_step) and join marks its end
+void enqueue_core(const Dev &d, Launch L, cudaEvent_t join = nullptr) {
     Launch L0 = L;        // follows the LOSS conditional node: plain stream order
     L0.pdl = false;
     launch_flux_mass(d, L0);
     launch_flux_energy(d, L);
     launch_tstep(d, L, V_RO, 2);
-    launch_bc(d, L);
+    if (join) {
+        cudaStreamWaitEvent(L.s, join, 0);
+        launch_bc_apply(d, L0);
+    } else {
+        launch_bc_sums(d, L);
+        launch_bc_apply(d, L);
+    }
     if (d.IN_FLOW != 0) launch_setflo(d, L);
     launch_peff(d, L);
     launch_flux_mom(d, L);
@@ -325,8 +335,14 @@ int capture_step(mgpu_handle *h) {
     launch_step_begin(dg, L);
     L.pdl = true;          // kernel-to-kernel edges of the step are programmatic
     launch_prim(dg, L);
+    // the exit-pressure sums depend on nothing the next kernels write, so they
+    // run beside LOSS, the mass/energy fluxes and TSTEP(RO, ROE)
+    CK(cudaEventRecord(h->ev_fork, h->stream));
+    CK(cudaStreamWaitEvent(h->aux, h->ev_fork, 0));
+    launch_bc_sums(dg, Launch{h->aux, h->sm_count, nullptr});
+    CK(cudaEventRecord(h->ev_join, h->aux));
     int rc = add_conditional(h, hl, &h->loss_nodes, [&](Launch L2) { launch_loss(dg, L2, false); });
-    if (!rc) enqueue_core(dg, L);
+    if (!rc) enqueue_core(dg, L, h->ev_join);
     if (!rc) rc = add_conditional(h, ht, &h->tail_nodes, [&](Launch L2) { enqueue_tail(dg, L2); });
     return rc;
 }
@@ -438,6 +454,10 @@ int32_t mgpu_create(int32_t im, int32_t jm, int32_t km, int32_t nrows, mgpu_hand
     if (e != cudaSuccess) return bail(fail(MGPU_E_CUDA, cudaGetErrorString(e)));
     e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(fail(MGPU_E_CUDA, cudaGetErrorString(e)));
+    e = cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
+    if (e != cudaSuccess) return bail(fail(MGPU_E_CUDA, cudaGetErrorString(e)));
     // arrays whose size is known now
     for (int a = 0; a < kNumArrays; ++a) {
         Shape s = kArrays[a].shape;
@@ -511,6 +531,9 @@ void mgpu_destroy(mgpu_handle *h) {
     if (h->h_ctl) cudaFreeHost(h->h_ctl);
     if (h->stream) cudaStreamDestroy(h->stream);
     if (h->side) cudaStreamDestroy(h->side);
+    if (h->aux) cudaStreamDestroy(h->aux);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
     delete h;
 }
 

@@ -449,9 +449,12 @@ cudaError_t configure_flux_kernels(const Dev &d) {
                                 (int)(b > 48 * 1024 ? b : 48 * 1024));
 }
 
-void launch_bc(const Dev &d, Launch L) {
+void launch_bc_sums(const Dev &d, Launch L) {
     launchk(L, k_bc_sums, dim3(1), dim3(1024), bc_sums_smem(d), d);
     mark(L, "k_bc_sums");
+}
+
+void launch_bc_apply(const Dev &d, Launch L) {
     launchk(L, k_bc_apply, dim3((d.IM * d.KM + 127) / 128), dim3(128), 0, d);
     mark(L, "k_bc_apply");
 }

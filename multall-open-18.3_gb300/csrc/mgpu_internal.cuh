@@ -213,7 +213,10 @@ void launch_prim(const Dev &d, Launch L);
 void launch_loss(const Dev &d, Launch L, bool init_call);
 void launch_flux_mass(const Dev &d, Launch L);
 void launch_flux_energy(const Dev &d, Launch L);
-void launch_bc(const Dev &d, Launch L);
+// inlet/exit conditions: the pitchwise sums and PD(K) (one CTA), then the
+// boundary states; the sums read only values final before TSTEP(RO, ROE)
+void launch_bc_sums(const Dev &d, Launch L);
+void launch_bc_apply(const Dev &d, Launch L);
 void launch_setflo(const Dev &d, Launch L);       // IN_FLOW != 0
 void launch_cusp(const Dev &d, Launch L);         // IF_CUSP = 2 rows
 void launch_peff(const Dev &d, Launch L);
