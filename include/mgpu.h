@@ -213,6 +213,47 @@ int32_t mgpu_batch_run(mgpu_batch *b, int32_t nsteps, mgpu_monitors *mons);
 /* As mgpu_bench_steps, for the whole batch. */
 int32_t mgpu_batch_bench_steps(mgpu_batch *b, int32_t nsteps, int32_t flush_l2, double *total_ms);
 
+/* ---- discrete adjoint -------------------------------------------------- */
+/* No counterpart in the reference.  Gradients of the efficiency and mass
+ * flow of a converged flow with respect to the geometry arrays, by the
+ * discrete adjoint of one LOOP iteration (multall-open-18.3.f:3759-5240)
+ * with the LOSS body forces and the STEPUP time steps held at their current
+ * values (frozen mixing length; set FROZEN = 1 for a primal that holds them
+ * too).  The converged state U* is a fixed point U* = G(U*, A); the adjoint
+ * lambda = (dG/dU)^T lambda + (dJ/dU)^T is iterated like the flow itself,
+ * and dJ/dA = dJ/dA|_U + lambda^T dG/dA.  Covered: SCREE without residual
+ * smoothing, IPOUT = 0, IN_PRESS = 0, IN_VTAN = 0, IN_VR <= 0, mixing planes
+ * with subsonic relative flow at JMIX+2; other options return
+ * MGPU_E_UNSUPPORTED, as does a linearisation state at which a density or
+ * Mach limiter changes the flow. */
+
+/* Records one step from the current state (the linearisation point),
+ * restores the state, and resets the adjoint to zero. */
+int32_t mgpu_adjoint_prepare(mgpu_handle *h);
+/* Selects the objective: 0 eta_tt, 1 mass flow at the inlet station, 2 at
+ * the exit station (the EFICOOL stations of mgpu_integrals_compute), -1
+ * none (the plain transposed step).  *value = the objective at the
+ * recorded step. */
+int32_t mgpu_adjoint_objective(mgpu_handle *h, int32_t which, double *value);
+/* n adjoint iterations lambda <- (dG/dU)^T lambda + (dJ/dU)^T, one CUDA
+ * graph launch each; *rel_change (or NULL) = |lambda_n - lambda_(n-1)| /
+ * |lambda_n| over the five conserved variables. */
+int32_t mgpu_adjoint_iterate(mgpu_handle *h, int32_t n, double *rel_change);
+/* Iterates until the relative change falls below tol or max_iters
+ * iterations are done; returns 0 if converged, 1 if not. */
+int32_t mgpu_adjoint_solve(mgpu_handle *h, int32_t max_iters, double tol, int32_t *iters, double *rel_change);
+/* One more reverse step that also accumulates dJ/dA for the geometry
+ * arrays AQX, AQR, ABX, ABR, ABT, ASX, ASR and VOLOR. */
+int32_t mgpu_adjoint_gradient(mgpu_handle *h);
+/* The adjoint of a state array by its COMMON name (RO, ROVX, ROVR, RORVT,
+ * ROE, DRO, DROE, DROVX, DROVR, DRORVT, P, HO, ROVT, PEFF, PD), or, with a
+ * "d" prefix (dAQX ...), the geometry gradient of mgpu_adjoint_gradient.
+ * Packed like the COMMON array, FP32. */
+int32_t mgpu_adjoint_get(mgpu_handle *h, const char *name, float *out, int64_t nbytes);
+/* Sets the adjoint of a state array (a user-defined objective's seed, or
+ * a test of the transposed step). */
+int32_t mgpu_adjoint_set(mgpu_handle *h, const char *name, const float *in, int64_t nbytes);
+
 /* ---- instrumentation --------------------------------------------------- */
 /* The reference prints "CPU TIME PER STEP" every 50 steps
  * (multall-open-18.3.f:5404-5414); these are the device-side equivalents. */

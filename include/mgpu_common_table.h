@@ -67,7 +67,11 @@
     /* not a COMMON variable: order of the long reductions on the GPU,   */ \
     /* 0 = FP64 tree sums (default), 1 = the reference's sequential REAL*4 */ \
     /* order for the superblock and row-average sums (parity checks)     */ \
-    M_(REDUCE_ORDER, 0)
+    M_(REDUCE_ORDER, 0)                                                   \
+    /* not a COMMON variable: 1 holds the LOSS body forces and the STEPUP */ \
+    /* time steps at their current values (frozen-turbulence stepping,    */ \
+    /* the primal of the discrete adjoint)                                */ \
+    M_(FROZEN,   0)
 
 /* ----- REAL scalars: /BKGAS/, /BKCNTL/, /BKSMTH/, /BKLOSS/, /BKINPT/ ---- */
 #define MGPU_REAL_SCALARS(M_)                                             \

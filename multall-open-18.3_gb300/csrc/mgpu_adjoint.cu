@@ -1,0 +1,2006 @@
+// mgpu_adjoint.cu -- the discrete adjoint of one time-marching step
+// (multall-open-18.3.f:3759-5240 with LOSS and STEPUP held: frozen body
+// forces and time steps) and its fixed-point solve.
+//
+// The converged flow U* is a fixed point of the step map U -> G(U, A)
+// (A: the geometry arrays).  For an objective J(U, A) the adjoint lambda
+// solves lambda = (dG/dU)^T lambda + (dJ/dU)^T, iterated exactly like the
+// flow itself (the transposed step has the primal's convergence rate), and
+// then dJ/dA = dJ/dA|_U + lambda^T dG/dA.
+//
+// mgpu_adjoint_prepare runs one step from the current state with recording
+// hooks and keeps what the reverse kernels need (the state before the step,
+// the primitive, flux and cell-change arrays of the step, the inlet density
+// and the mixing-plane inputs); the state is then restored.  Every reverse
+// kernel below undoes one forward kernel of the step, in reverse order:
+//   k_mixplan -> k_ts_* (momenta) -> k_flux_mom -> k_peff -> k_bc_apply ->
+//   k_ts_* (RO, ROE) -> k_flux_energy -> k_bc_sums -> k_flux_mass -> k_prim
+// Each takes the adjoints of its forward kernel's outputs and adds the
+// adjoints of its inputs; outputs that the forward kernel overwrote get the
+// adjoint of their old value (zero, or what the kernel read of it).  Where
+// several forward outputs read one input, the reverse scatter uses float
+// atomics; the result is not bitwise reproducible, but its rounding is far
+// below the FP32 adjoint's accuracy.  Branches (limits, the flow-direction
+// tests, |STORE| in the negative feedback) are taken as the recorded step
+// took them.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mgpu_internal.cuh"
+
+namespace mgpu {
+
+// adjoints of one conserved variable's TSTEP operands
+struct AdjVar {
+    float *D, *DIFF;             // the variable and its SCREE history (state)
+    float *XF, *TF, *RF, *SR;    // face fluxes and source
+    float *ST;                   // cell changes after prolongation
+    float *TM;                   // node values before SMOOTH_VAR
+    float *Y;                    // ST * RSTEP: the restriction operand of the transposed prolongation
+    float *P1, *P2;              // per-plane block partials of Y
+    double *psum;                // (JM) per-plane sums of Y
+    double *pblk;                // (JM) per-plane sums of dJ/d(row mean |STORE|)
+    const float *tST;            // recorded STORE after prolongation
+    const float *tBLK;           // (NROWS) recorded row means of |STORE| after the row mixing
+};
+
+struct Adj {
+    AdjVar v[NVAR];
+    // adjoints of the step's node arrays (full size; between steps only the
+    // state parts are nonzero: PEFF, P at J=1, HO at J=JM, ROVT at J=1)
+    float *P, *HO, *VX, *VR, *VT, *ROVT, *PEFF, *FLOWX, *FLOWT, *FLOWR;
+    float *PD, *PDK, *PAVG, *SSUM;   // (KM)
+    // the recorded step: state before it ...
+    const float *tRO, *tROVX, *tROVR, *tRORVT, *tROE, *tPEFF0, *tHOJM, *tROVT1, *tP1;
+    // ... and arrays as the step formed them
+    const float *tVX, *tVR, *tVT, *tROVT, *tP, *tHO, *tPEFF, *tFLOWX, *tFLOWT, *tFLOWR;
+    const float *tBCBUF, *tROIN, *tMIX;
+    const DevCtl *tctl;
+    // geometry adjoints, accumulated when geom != 0
+    float *gAQX, *gAQR, *gABX, *gABR, *gABT, *gASX, *gASR, *gVOLOR;
+    int geom;
+    int *flag;                   // bit 0: supersonic mixing-plane sweep met
+    // objective seeds: node quantities (VX, VT, VR, HO, P) and cell FLOWX on
+    // two J planes
+    const float *seed;
+    int seed_j[2];
+};
+
+namespace {
+
+inline unsigned gridn(size_t n, unsigned b) { return (unsigned)((n + b - 1) / b); }
+
+__device__ __forceinline__ void aadd(float *p, float v) {
+    if (v != 0.0f) atomicAdd(p, v);
+}
+
+// =====================================================================
+// R1: primitive variables (k_prim)
+// =====================================================================
+__global__ void rk_prim(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, (size_t)n, i, j, k);
+    if (j < 2) return;
+    const float RRNOW = 1.0f / A2(d.R, j, k);
+    const float ro = a.tRO[n], RECIP = 1.0f / ro;
+    const float vx = a.tROVX[n] * RECIP, vr = a.tROVR[n] * RECIP;
+    const float rovt = a.tRORVT[n] * RRNOW, vt = rovt * RECIP;
+    float gvx = a.VX[n], gvr = a.VR[n], gvt = a.VT[n], grovt = a.ROVT[n];
+    float gro = 0.0f, groe = 0.0f;
+    if (j <= d.JMM1) {
+        const float EKE = 0.5f * (vr * vr + vt * vt + vx * vx);
+        const float TS = (a.tROE[n] / ro - EKE) / d.CV;
+        const float gP = a.P[n], gHO = a.HO[n];
+        const float gTS = gP * ro * d.RGAS + gHO * d.CP;
+        gro += gP * d.RGAS * TS;
+        const float gEKE = gHO - gTS / d.CV;
+        groe += gTS / d.CV / ro;
+        gro -= gTS / d.CV * a.tROE[n] / (ro * ro);
+        gvr += gEKE * vr;
+        gvt += gEKE * vt;
+        gvx += gEKE * vx;
+        a.P[n] = 0.0f;
+        a.HO[n] = 0.0f;
+    }
+    grovt += gvt * RECIP;
+    float grecip = gvt * rovt + gvx * a.tROVX[n] + gvr * a.tROVR[n];
+    gro -= grecip * RECIP * RECIP;
+    a.v[V_RO].D[n] += gro;
+    a.v[V_ROE].D[n] += groe;
+    a.v[V_ROVX].D[n] += gvx * RECIP;
+    a.v[V_ROVR].D[n] += gvr * RECIP;
+    a.v[V_RORVT].D[n] += grovt * RRNOW;
+    a.VX[n] = 0.0f;
+    a.VR[n] = 0.0f;
+    a.VT[n] = 0.0f;
+    a.ROVT[n] = 0.0f;
+}
+
+// =====================================================================
+// R2: mass fluxes (k_flux_mass)
+// =====================================================================
+// pre-step ROVT: J=1 from the previous inlet condition, J>=2 from k_prim
+__device__ inline float pre_rovt(const Dev &d, const Adj &a, int i, int j, int k) {
+    return j == 1 ? AIK(a.tROVT1, i, k) : A3(a.tROVT, i, j, k);
+}
+
+__device__ inline void rev_flowt_raw(const Dev &d, const Adj &a, int i, int j, int k, float g) {
+    if (g == 0.0f) return;
+    const float c = 0.25f * g;
+    const float abx = A3(d.ABX, i, j, k), abt = A2(d.ABT, j, k), abr = A3(d.ABR, i, j, k);
+    const int jj[4] = {j, j - 1, j - 1, j}, kk[4] = {k, k, k + 1, k + 1};
+    float sx = 0.0f, st = 0.0f, sr = 0.0f;
+    for (int q = 0; q < 4; ++q) {
+        const int m = ix3(d, i, jj[q], kk[q]);
+        aadd(&a.v[V_ROVX].D[m], c * abx);
+        aadd(&a.ROVT[m], c * abt);
+        aadd(&a.v[V_RO].D[m], -c * abt * A2(d.UBLADE, jj[q], kk[q]));
+        aadd(&a.v[V_ROVR].D[m], c * abr);
+        if (a.geom) {
+            sx += a.tROVX[m];
+            st += pre_rovt(d, a, i, jj[q], kk[q]) - A2(d.UBLADE, jj[q], kk[q]) * a.tRO[m];
+            sr += a.tROVR[m];
+        }
+    }
+    if (a.geom) {
+        aadd(&A3(a.gABX, i, j, k), c * sx);
+        aadd(&A2(a.gABT, j, k), c * st);
+        aadd(&A3(a.gABR, i, j, k), c * sr);
+    }
+}
+
+__global__ void rk_flux_mass(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, (size_t)n, i, j, k);
+    if (i < d.IM && k < d.KM) {
+        const float g = a.FLOWX[n];
+        a.FLOWX[n] = 0.0f;
+        if (g != 0.0f) {
+            const float c = 0.25f * g;
+            const int m[4] = {n, ix3(d, i, j, k + 1), ix3(d, i + 1, j, k), ix3(d, i + 1, j, k + 1)};
+            float sx = 0.0f, sr = 0.0f;
+            for (int q = 0; q < 4; ++q) {
+                aadd(&a.v[V_ROVX].D[m[q]], c * d.AQX[n]);
+                aadd(&a.v[V_ROVR].D[m[q]], c * d.AQR[n]);
+                sx += a.tROVX[m[q]];
+                sr += a.tROVR[m[q]];
+            }
+            if (a.geom) {
+                aadd(&a.gAQX[n], c * sx);
+                aadd(&a.gAQR[n], c * sr);
+            }
+        }
+    }
+    if (j >= 2 && k < d.KM) {
+        const float g = a.FLOWT[n];
+        a.FLOWT[n] = 0.0f;
+        if (i == 1 || i == d.IM) {
+            if (A1(d.IND, j) != 1) {
+                rev_flowt_raw(d, a, 1, j, k, 0.5f * g);
+                rev_flowt_raw(d, a, d.IM, j, k, 0.5f * g);
+            } else {
+                const int nr = A1(d.NROW, j);
+                if (!(k >= A1(d.KS1, nr) && k <= A1(d.KS2, nr))) rev_flowt_raw(d, a, i, j, k, g);
+            }
+        } else {
+            rev_flowt_raw(d, a, i, j, k, g);
+        }
+    }
+    if (i < d.IM && j >= 2) {
+        const float g = a.FLOWR[n];
+        a.FLOWR[n] = 0.0f;
+        if (g != 0.0f && k >= 2 && k <= d.KMM1) {
+            const float c = 0.25f * g;
+            const int m[4] = {n, ix3(d, i, j - 1, k), ix3(d, i + 1, j - 1, k), ix3(d, i + 1, j, k)};
+            float sx = 0.0f, sr = 0.0f;
+            for (int q = 0; q < 4; ++q) {
+                aadd(&a.v[V_ROVX].D[m[q]], c * d.ASX[n]);
+                aadd(&a.v[V_ROVR].D[m[q]], c * d.ASR[n]);
+                sx += a.tROVX[m[q]];
+                sr += a.tROVR[m[q]];
+            }
+            if (a.geom) {
+                aadd(&a.gASX[n], c * sx);
+                aadd(&a.gASR[n], c * sr);
+            }
+        }
+    }
+}
+
+// =====================================================================
+// R3: exit pitchwise sums and the radial-equilibrium recurrence (k_bc_sums)
+// IPOUT = 0: PD(1) = PDOWN_HUB, PD(K) = 0.9 PD(K) + 0.1 (PD(K-1) + DP(K))
+// =====================================================================
+__global__ void __launch_bounds__(256) rk_bc_sums(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+    __shared__ float gss[512];
+    const int KM = d.KM, IM = d.IM, IMM1 = d.IMM1;
+    for (int k = threadIdx.x; k < KM; k += blockDim.x) gss[k] = 0.0f;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float gpd[512];
+        for (int k = 0; k < KM; ++k) gpd[k] = a.PD[k] + a.PDK[k];
+        for (int k = KM - 1; k >= 1; --k) {
+            const float g = gpd[k];
+            gpd[k - 1] += 0.1f * g;
+            a.PD[k] = 0.9f * g;
+            const float gdp = 0.1f * g;
+            const float half = 0.5f * (A2(d.R, d.JM, k + 1) - A2(d.R, d.JM, k));
+            gss[k] += gdp * half;
+            gss[k - 1] += gdp * half;
+        }
+        a.PD[0] = 0.0f;
+        for (int k = 0; k < KM; ++k) a.PDK[k] = 0.0f;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < IM * KM; t += blockDim.x) {
+        const int i = t % IM + 1, k = t / IM + 1;
+        const float w = 0.5f * ((i <= IMM1 ? A1(d.FP, i) : 0.0f) + (i >= 2 ? A1(d.FP, i - 1) : 0.0f));
+        const float gp = a.PAVG[k - 1];
+        A3(a.P, i, d.JMM1, k) += gp * w;
+        const float gs = gss[k - 1] * w / A2(d.R, d.JM, k);
+        A3(a.ROVT, i, d.JM, k) += gs * A3(a.tVT, i, d.JM, k);
+        A3(a.VT, i, d.JM, k) += gs * A3(a.tROVT, i, d.JM, k);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < KM; k += blockDim.x) a.PAVG[k] = 0.0f;
+}
+
+// =====================================================================
+// R4: energy fluxes (k_flux_energy); HO(JM) and PEFF as the step began
+// =====================================================================
+__device__ inline float pre_ho(const Dev &d, const Adj &a, int i, int j, int k) {
+    return j == d.JM ? AIK(a.tHOJM, i, k) : A3(a.tHO, i, j, k);
+}
+
+__device__ inline void rev_tflux_energy_raw(const Dev &d, const Adj &a, int i, int j, int k, float g) {
+    if (g == 0.0f) return;
+    const float c = 0.25f * g;
+    const int jj[4] = {j, j - 1, j - 1, j}, kk[4] = {k, k, k + 1, k + 1};
+    float sho = 0.0f;
+    const float ft = A3(a.tFLOWT, i, j, k), wr = A2(d.WRABT, j, k);
+    for (int q = 0; q < 4; ++q) {
+        const int m = ix3(d, i, jj[q], kk[q]);
+        sho += pre_ho(d, a, i, jj[q], kk[q]);
+        aadd(&a.HO[m], c * ft);
+        aadd(&a.PEFF[m], c * wr);
+    }
+    aadd(&A3(a.FLOWT, i, j, k), c * sho);
+}
+
+__global__ void rk_flux_energy(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, (size_t)n, i, j, k);
+    const AdjVar &V = a.v[V_ROE];
+    if (i < d.IM && k < d.KM) {
+        const float g = V.XF[n];
+        V.XF[n] = 0.0f;
+        if (g != 0.0f) {
+            const int m[4] = {n, ix3(d, i, j, k + 1), ix3(d, i + 1, j, k), ix3(d, i + 1, j, k + 1)};
+            const int mj[4] = {j, j, j, j}, mk[4] = {k, k + 1, k, k + 1}, mi[4] = {i, i, i + 1, i + 1};
+            float sho = 0.0f;
+            for (int q = 0; q < 4; ++q) {
+                sho += pre_ho(d, a, mi[q], mj[q], mk[q]);
+                aadd(&a.HO[m[q]], g * a.tFLOWX[n] * 0.25f);
+            }
+            aadd(&a.FLOWX[n], g * sho * 0.25f);
+        }
+    }
+    if (i < d.IM && j >= 2) {
+        const float g = V.RF[n];
+        V.RF[n] = 0.0f;
+        if (g != 0.0f) {
+            const int mi[4] = {i, i, i + 1, i + 1}, mj[4] = {j, j - 1, j - 1, j};
+            float sho = 0.0f;
+            for (int q = 0; q < 4; ++q) {
+                sho += pre_ho(d, a, mi[q], mj[q], k);
+                aadd(&A3(a.HO, mi[q], mj[q], k), 0.25f * g * a.tFLOWR[n]);
+            }
+            aadd(&a.FLOWR[n], 0.25f * g * sho);
+        }
+    }
+    if (j >= 2 && k < d.KM) {
+        const float g = V.TF[n];
+        V.TF[n] = 0.0f;
+        if ((i == 1 || i == d.IM) && A1(d.IND, j) != 1) {
+            rev_tflux_energy_raw(d, a, 1, j, k, 0.5f * g);
+            rev_tflux_energy_raw(d, a, d.IM, j, k, 0.5f * g);
+        } else {
+            rev_tflux_energy_raw(d, a, i, j, k, g);
+        }
+    }
+    V.SR[n] = 0.0f;
+}
+
+// =====================================================================
+// R6: inlet and exit conditions (k_bc_apply), IN_PRESS = 0, IN_VTAN = 0,
+// IN_VR <= 0
+// =====================================================================
+__global__ void rk_bc_apply(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.IM * d.KM) return;
+    const int i = t % d.IM + 1, k = t / d.IM + 1;
+    // ---- inlet ----
+    {
+        const float PO1 = A1(d.PO1, k), TO1 = A1(d.TO1, k);
+        const float RO_STAG = PO1 / d.RGAS / TO1;
+        float RO_IN = a.tROIN[t];
+        const bool c0 = RO_IN > 0.9999f * RO_STAG;
+        if (c0) RO_IN = 0.9999f * RO_STAG;
+        const float PNEW = PO1 * powf(RO_IN / RO_STAG, d.GA);
+        const float p1a = d.RFIN1 * a.tP1[t] + d.RFIN * PNEW;
+        const float plim = A1(d.PLIM, k);
+        const bool c1 = p1a > plim;
+        const float p1b = c1 ? 0.9f * p1a + 0.1f * plim : p1a;
+        const bool c2 = p1b > 0.99999f * PO1;
+        const float p1 = c2 ? PO1 * 0.99999f : p1b;
+        const float TS = TO1 * powf(p1 * A1(d.RPO1, k), d.FGA);
+        const float VABSQ = 2.0f * d.CP * (TO1 - TS);
+        const float VABS = sqrtf(VABSQ);
+        const float VMER = VABS * A1(d.BSCOS, k);
+        const float vt1 = VABS * A1(d.BSSIN, k);
+        const float vr2 = A3(a.tVR, i, 2, k);
+        float VXSQ = VMER * VMER - vr2 * vr2;
+        const bool c3 = VXSQ < 0.0000001f * TO1 * d.CP;
+        if (c3) VXSQ = 0.0000001f * TO1 * d.CP;
+        const float vx1 = sqrtf(VXSQ), vr1 = vr2;
+        const float ro1 = p1 / (d.RGAS * TS);
+        const int n1 = ix3(d, i, 1, k);
+        const float gROE = a.v[V_ROE].D[n1], gROVX = a.v[V_ROVX].D[n1], gRORVT = a.v[V_RORVT].D[n1];
+        const float gROVR = a.v[V_ROVR].D[n1], gRO = a.v[V_RO].D[n1], gROVT = a.ROVT[n1];
+        float gp1 = a.P[n1] + gROE / d.GA1;
+        float gro1 = gROE * 0.5f * VABSQ + gROVX * vx1 + gROVR * vr1 + gRO;
+        float gVABSQ = gROE * 0.5f * ro1;
+        float gvx1 = gROVX * ro1 + a.VX[n1];
+        float gvr1 = gROVR * ro1 + a.VR[n1];
+        const float grovt1 = gRORVT * A2(d.R, 1, k) + gROVT;
+        gro1 += grovt1 * vt1;
+        const float gvt1 = grovt1 * ro1 + a.VT[n1];
+        gp1 += gro1 / (d.RGAS * TS);
+        float gTS = -gro1 * ro1 / TS;
+        float gvr2 = gvr1;
+        if (!c3) {
+            const float gVXSQ = gvx1 * 0.5f / vx1;
+            const float gVMER = gVXSQ * 2.0f * VMER;
+            gvr2 -= gVXSQ * 2.0f * vr2;
+            gVABSQ += (gvt1 * A1(d.BSSIN, k) + gVMER * A1(d.BSCOS, k)) * 0.5f / VABS;
+        } else {
+            gVABSQ += gvt1 * A1(d.BSSIN, k) * 0.5f / VABS;
+        }
+        gTS -= 2.0f * d.CP * gVABSQ;
+        gp1 += gTS * TS * d.FGA / p1;
+        const float gp1b = c2 ? 0.0f : gp1;
+        const float gp1a = c1 ? 0.9f * gp1b : gp1b;
+        const float gPNEW = d.RFIN * gp1a;
+        const float gROIN = c0 ? 0.0f : gPNEW * PNEW * d.GA / RO_IN;
+        a.v[V_RO].D[n1] = gROIN;
+        a.P[n1] = d.RFIN1 * gp1a;
+        A3(a.VR, i, 2, k) += gvr2;
+        a.VX[n1] = 0.0f; a.VR[n1] = 0.0f; a.VT[n1] = 0.0f; a.ROVT[n1] = 0.0f; a.HO[n1] = 0.0f;
+        a.v[V_ROVX].D[n1] = 0.0f; a.v[V_ROVR].D[n1] = 0.0f; a.v[V_RORVT].D[n1] = 0.0f; a.v[V_ROE].D[n1] = 0.0f;
+    }
+    // ---- exit ----
+    {
+        const int ne = ix3(d, i, d.JM, k);
+        const float vr = a.tVR[ne], vt = a.tVT[ne], vx = a.tVX[ne];
+        const float EKE = 0.5f * (vr * vr + vt * vt + vx * vx);
+        const float pe = a.tP[ne], hoe = a.tHO[ne];
+        const float TEXIT = (hoe - EKE) / d.CP;
+        const float roe_ = pe / d.RGAS / TEXIT;
+        const float gP = a.P[ne], gHO = a.HO[ne], gRO = a.v[V_RO].D[ne], gROE = a.v[V_ROE].D[ne];
+        const float groe = gROE * (d.CV * TEXIT + EKE) + gRO;
+        float gTEXIT = gROE * roe_ * d.CV - groe * roe_ / TEXIT;
+        float gEKE = gROE * roe_ - gTEXIT / d.CP;
+        const float ghoe = gTEXIT / d.CP + gHO;
+        const float gpe = groe / (d.RGAS * TEXIT) + gP;
+        A3(a.HO, i, d.JMM1, k) += 2.0f * ghoe;
+        A3(a.HO, i, d.JM - 2, k) -= ghoe;
+        atomicAdd(&a.PDK[k - 1], gpe);
+        A3(a.P, i, d.JMM1, k) += d.FEXTRAP * gpe;
+        atomicAdd(&a.PAVG[k - 1], -d.FEXTRAP * gpe);
+        a.VR[ne] += gEKE * vr;
+        a.VT[ne] += gEKE * vt;
+        a.VX[ne] += gEKE * vx;
+        a.P[ne] = 0.0f; a.HO[ne] = 0.0f; a.v[V_RO].D[ne] = 0.0f; a.v[V_ROE].D[ne] = 0.0f;
+    }
+}
+
+// =====================================================================
+// R7: PEFF = P - PREFF + F_PDOWN (P(J+1) - P)   (k_peff)
+// =====================================================================
+__global__ void rk_peff(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    const float g = a.PEFF[n];
+    a.PEFF[n] = 0.0f;
+    if (d.F_PDOWN == 0.0f) {
+        a.P[n] += g;
+        return;
+    }
+    int i, j, k;
+    node_ijk(d, (size_t)n, i, j, k);
+    if (j == d.JM) {
+        aadd(&a.P[n], g);
+    } else {
+        aadd(&a.P[n], (1.0f - d.F_PDOWN) * g);
+        aadd(&A3(a.P, i, j + 1, k), d.F_PDOWN * g);
+    }
+}
+
+// =====================================================================
+// R8: momentum fluxes (k_flux_mom)
+// =====================================================================
+// the four nodes of a face I = const: (i,j,k), (i,j-1,k), (i,j-1,k+1), (i,j,k+1)
+__device__ inline void iface_nodes(const Dev &d, int i, int j, int k, int m[4]) {
+    m[0] = ix3(d, i, j, k); m[1] = ix3(d, i, j - 1, k); m[2] = ix3(d, i, j - 1, k + 1); m[3] = ix3(d, i, j, k + 1);
+}
+
+__global__ void rk_flux_mom(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, (size_t)n, i, j, k);
+    const int IM = d.IM;
+    const bool hi = i < IM, hj = j >= 2, hk = k < d.KM;
+    const AdjVar &X = a.v[V_ROVX], &T = a.v[V_RORVT], &Rm = a.v[V_ROVR];
+    const float *PE = a.tPEFF, *VX = a.tVX, *VT = a.tVT, *VR = a.tVR, *RV = a.tROVT;
+    const bool edge = (i == 1 || i == IM) && A1(d.IND, j) != 1;
+    // faces K = const
+    if (hi && hk) {
+        const float gx = X.XF[n], gt = T.XF[n], gr = Rm.XF[n];
+        X.XF[n] = 0.0f; T.XF[n] = 0.0f; Rm.XF[n] = 0.0f;
+        X.SR[n] = 0.0f; T.SR[n] = 0.0f;
+        const int m[4] = {n, ix3(d, i, j, k + 1), ix3(d, i + 1, j, k + 1), ix3(d, i + 1, j, k)};
+        const float fx = a.tFLOWX[n];
+        const float AVGR = 0.125f * (A2(d.R, j, k) + A2(d.R, j, k + 1));
+        float sp = 0.0f, svx = 0.0f, svt = 0.0f, svr = 0.0f;
+        for (int q = 0; q < 4; ++q) {
+            sp += PE[m[q]]; svx += VX[m[q]]; svt += VT[m[q]]; svr += VR[m[q]];
+            aadd(&a.PEFF[m[q]], 0.25f * gx * d.AQX[n] + 0.25f * gr * d.AQR[n]);
+            aadd(&a.VX[m[q]], 0.25f * gx * fx);
+            aadd(&a.VT[m[q]], gt * fx * AVGR);
+            aadd(&a.VR[m[q]], 0.25f * gr * fx);
+        }
+        aadd(&a.FLOWX[n], 0.25f * gx * svx + gt * AVGR * svt + 0.25f * gr * svr);
+        if (a.geom) {
+            aadd(&a.gAQX[n], 0.25f * gx * sp);
+            aadd(&a.gAQR[n], 0.25f * gr * sp);
+        }
+    }
+    // faces J = const and the radial source
+    if (hi && hj) {
+        const float gx = X.RF[n], gt = T.RF[n], gr = Rm.RF[n];
+        X.RF[n] = 0.0f; T.RF[n] = 0.0f; Rm.RF[n] = 0.0f;
+        const int m[4] = {n, ix3(d, i, j - 1, k), ix3(d, i + 1, j - 1, k), ix3(d, i + 1, j, k)};
+        const float fr = a.tFLOWR[n];
+        const float AVGR = (A2(d.R, j, k) + A2(d.R, j - 1, k)) * 0.125f;
+        float sp = 0.0f, svx = 0.0f, svt = 0.0f, svr = 0.0f;
+        for (int q = 0; q < 4; ++q) {
+            sp += PE[m[q]]; svx += VX[m[q]]; svt += VT[m[q]]; svr += VR[m[q]];
+            aadd(&a.PEFF[m[q]], 0.25f * gx * d.ASX[n] + 0.25f * gr * d.ASR[n]);
+            aadd(&a.VX[m[q]], 0.25f * gx * fr);
+            aadd(&a.VT[m[q]], gt * fr * AVGR);
+            aadd(&a.VR[m[q]], 0.25f * gr * fr);
+        }
+        aadd(&a.FLOWR[n], 0.25f * gx * svx + gt * svt * AVGR + 0.25f * gr * svr);
+        if (a.geom) {
+            aadd(&a.gASX[n], 0.25f * gx * sp);
+            aadd(&a.gASR[n], 0.25f * gr * sp);
+        }
+        if (hk) {
+            const float gs = Rm.SR[n];
+            Rm.SR[n] = 0.0f;
+            if (gs != 0.0f) {
+                int m8[8];
+                int c = 0;
+                for (int di = 0; di < 2; ++di)
+                    for (int dj = -1; dj <= 0; ++dj)
+                        for (int dk = 0; dk < 2; ++dk) m8[c++] = ix3(d, i + di, j + dj, k + dk);
+                float srv = 0.0f, svt8 = 0.0f, sp8 = 0.0f;
+                for (int q = 0; q < 8; ++q) {
+                    srv += RV[m8[q]];
+                    svt8 += VT[m8[q]];
+                    sp8 += PE[m8[q]];
+                }
+                const float AVGVT8 = 0.125f * svt8;
+                const float vol = d.VOLOR[n];
+                for (int q = 0; q < 8; ++q) {
+                    aadd(&a.ROVT[m8[q]], -gs * vol * AVGVT8);
+                    aadd(&a.VT[m8[q]], -gs * vol * srv * 0.125f);
+                    aadd(&a.PEFF[m8[q]], -gs * vol);
+                }
+                if (a.geom) aadd(&a.gVOLOR[n], -gs * (srv * AVGVT8 + sp8));
+            }
+        } else {
+            Rm.SR[n] = 0.0f;
+        }
+    } else {
+        Rm.SR[n] = 0.0f;
+    }
+    // faces I = const
+    if (hj && hk) {
+        const float gx = X.TF[n], gt = T.TF[n], gr = Rm.TF[n];
+        X.TF[n] = 0.0f; T.TF[n] = 0.0f; Rm.TF[n] = 0.0f;
+        const float FT = a.tFLOWT[n];
+        int m[4], m1[4], mm[4];
+        iface_nodes(d, i, j, k, m);
+        iface_nodes(d, 1, j, k, m1);
+        iface_nodes(d, IM, j, k, mm);
+        const float abx = d.ABX[n], abr = d.ABR[n], abt = A2(d.ABT, j, k);
+        // X momentum
+        if (gx != 0.0f) {
+            if (edge) {
+                float svx = 0.0f, sp = 0.0f;
+                for (int q = 0; q < 4; ++q) {
+                    svx += VX[m1[q]] + VX[mm[q]];
+                    sp += PE[m1[q]] + PE[mm[q]];
+                    aadd(&a.VX[m1[q]], 0.125f * gx * FT);
+                    aadd(&a.VX[mm[q]], 0.125f * gx * FT);
+                    aadd(&a.PEFF[m1[q]], 0.125f * gx * abx);
+                    aadd(&a.PEFF[mm[q]], 0.125f * gx * abx);
+                }
+                aadd(&a.FLOWT[n], 0.125f * gx * svx);
+                if (a.geom) aadd(&a.gABX[n], 0.125f * gx * sp);
+            } else {
+                float svx = 0.0f, sp = 0.0f;
+                for (int q = 0; q < 4; ++q) {
+                    svx += VX[m[q]];
+                    sp += PE[m[q]];
+                    aadd(&a.VX[m[q]], 0.25f * gx * FT);
+                    aadd(&a.PEFF[m[q]], 0.25f * gx * abx);
+                }
+                aadd(&a.FLOWT[n], 0.25f * gx * svx);
+                if (a.geom) aadd(&a.gABX[n], 0.25f * gx * sp);
+            }
+        }
+        // moment of momentum: raw(ii) = (FLOWT(ii) AVGVT(ii) + ABT AVGP(ii)) AVGR
+        if (gt != 0.0f) {
+            const float AVGR = 0.25f * A2(d.RAVG_CELL, j, k);
+            auto rev_rvt = [&](int ii, const int *mq, float g) {
+                const float ft = A3(a.tFLOWT, ii, j, k);
+                float svt = 0.0f, sp = 0.0f;
+                for (int q = 0; q < 4; ++q) {
+                    svt += VT[mq[q]];
+                    sp += PE[mq[q]];
+                    aadd(&a.VT[mq[q]], g * ft * AVGR);
+                    aadd(&a.PEFF[mq[q]], g * abt * AVGR);
+                }
+                aadd(&A3(a.FLOWT, ii, j, k), g * svt * AVGR);
+                if (a.geom) aadd(&A2(a.gABT, j, k), g * sp * AVGR);
+            };
+            if (edge) {
+                rev_rvt(1, m1, 0.5f * gt);
+                rev_rvt(IM, mm, 0.5f * gt);
+            } else {
+                rev_rvt(i, m, gt);
+            }
+        }
+        // radial momentum
+        if (gr != 0.0f) {
+            if (edge) {
+                // 0.5 (0.25 FLOWT(1) AVGVR(1) + 0.25 FLOWT(IM) AVGVR(IM)
+                //      + 0.25 (AVGP(1) + AVGP(IM)) ABR)
+                const float f1 = A3(a.tFLOWT, 1, j, k), fm = A3(a.tFLOWT, IM, j, k);
+                float svr1 = 0.0f, svrm = 0.0f, sp = 0.0f;
+                for (int q = 0; q < 4; ++q) {
+                    svr1 += VR[m1[q]];
+                    svrm += VR[mm[q]];
+                    sp += PE[m1[q]] + PE[mm[q]];
+                    aadd(&a.VR[m1[q]], 0.125f * gr * f1);
+                    aadd(&a.VR[mm[q]], 0.125f * gr * fm);
+                    aadd(&a.PEFF[m1[q]], 0.125f * gr * abr);
+                    aadd(&a.PEFF[mm[q]], 0.125f * gr * abr);
+                }
+                aadd(&A3(a.FLOWT, 1, j, k), 0.125f * gr * svr1);
+                aadd(&A3(a.FLOWT, IM, j, k), 0.125f * gr * svrm);
+                if (a.geom) aadd(&a.gABR[n], 0.125f * gr * sp);
+            } else {
+                float svr = 0.0f, sp = 0.0f;
+                for (int q = 0; q < 4; ++q) {
+                    svr += VR[m[q]];
+                    sp += PE[m[q]];
+                    aadd(&a.VR[m[q]], 0.25f * gr * FT);
+                    aadd(&a.PEFF[m[q]], 0.25f * gr * abr);
+                }
+                aadd(&a.FLOWT[n], 0.25f * gr * svr);
+                if (a.geom) aadd(&a.gABR[n], 0.25f * gr * sp);
+            }
+        }
+    }
+}
+
+// =====================================================================
+// R11: mixing plane (k_mixplan), subsonic relative flow at JP2: the outputs
+// at (I, JP2) depend on the 14 inputs (IMID, JP1) x 5, (I, JP2) x 5 and
+// (I, JP3) x 4, differentiated in forward mode with 14-component duals
+// =====================================================================
+template <int N>
+struct Dual {
+    float v;
+    float g[N];
+    __device__ Dual() : v(0.0f) {
+        for (int q = 0; q < N; ++q) g[q] = 0.0f;
+    }
+    __device__ Dual(float x) : v(x) {
+        for (int q = 0; q < N; ++q) g[q] = 0.0f;
+    }
+};
+template <int N> __device__ inline Dual<N> lin(float v, const Dual<N> &x, float dx) {
+    Dual<N> r(v);
+    for (int q = 0; q < N; ++q) r.g[q] = dx * x.g[q];
+    return r;
+}
+template <int N> __device__ inline Dual<N> lin2(float v, const Dual<N> &x, float dx, const Dual<N> &y, float dy) {
+    Dual<N> r(v);
+    for (int q = 0; q < N; ++q) r.g[q] = dx * x.g[q] + dy * y.g[q];
+    return r;
+}
+template <int N> __device__ inline Dual<N> operator+(const Dual<N> &x, const Dual<N> &y) { return lin2(x.v + y.v, x, 1.0f, y, 1.0f); }
+template <int N> __device__ inline Dual<N> operator-(const Dual<N> &x, const Dual<N> &y) { return lin2(x.v - y.v, x, 1.0f, y, -1.0f); }
+template <int N> __device__ inline Dual<N> operator*(const Dual<N> &x, const Dual<N> &y) { return lin2(x.v * y.v, x, y.v, y, x.v); }
+template <int N> __device__ inline Dual<N> operator/(const Dual<N> &x, const Dual<N> &y) {
+    const float q = x.v / y.v;
+    return lin2(q, x, 1.0f / y.v, y, -q / y.v);
+}
+template <int N> __device__ inline Dual<N> operator*(float c, const Dual<N> &x) { return lin(c * x.v, x, c); }
+template <int N> __device__ inline Dual<N> operator*(const Dual<N> &x, float c) { return lin(c * x.v, x, c); }
+template <int N> __device__ inline Dual<N> operator/(const Dual<N> &x, float c) { return lin(x.v / c, x, 1.0f / c); }
+template <int N> __device__ inline Dual<N> operator-(const Dual<N> &x, float c) { return lin(x.v - c, x, 1.0f); }
+template <int N> __device__ inline Dual<N> operator+(const Dual<N> &x, float c) { return lin(x.v + c, x, 1.0f); }
+template <int N> __device__ inline Dual<N> operator-(float c, const Dual<N> &x) { return lin(c - x.v, x, -1.0f); }
+template <int N> __device__ inline Dual<N> dsqrt(const Dual<N> &x) {
+    const float s = sqrtf(x.v);
+    return lin(s, x, s > 0.0f ? 0.5f / s : 0.0f);
+}
+template <int N> __device__ inline Dual<N> dasin(const Dual<N> &x) { return lin(asinf(x.v), x, rsqrtf(1.0f - x.v * x.v)); }
+template <int N> __device__ inline Dual<N> datan2(const Dual<N> &y, const Dual<N> &x) {
+    const float r2 = x.v * x.v + y.v * y.v;
+    return lin2(atan2f(y.v, x.v), y, x.v / r2, x, -y.v / r2);
+}
+template <int N> __device__ inline Dual<N> dpowc(const Dual<N> &x, float e) {
+    const float p = powf(x.v, e);
+    return lin(p, x, e * p / x.v);
+}
+template <int N> __device__ inline Dual<N> dsin(const Dual<N> &x) { return lin(sinf(x.v), x, cosf(x.v)); }
+template <int N> __device__ inline Dual<N> dcos(const Dual<N> &x) { return lin(cosf(x.v), x, -sinf(x.v)); }
+
+constexpr int MIXN = 14;
+
+__global__ void __launch_bounds__(64) rk_mixplan(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+    typedef Dual<MIXN> D;
+    __shared__ float red[5][64];
+    const int nr = blockIdx.x / d.KM + 1, k = blockIdx.x % d.KM + 1;
+    const int IM = d.IM;
+    const float RFMIX1 = 1.0f - d.RFMIX;
+    const int KSUB = (k == d.KM) ? d.KM - 1 : k;
+    int j = A1(d.JMIX, nr);
+    int JP1, JP2, JP3;
+    float F_ANGLE;
+    if (A3(a.tFLOWX, d.IMID, j, KSUB) < 0.0f) {
+        JP1 = j + 1; JP2 = j + 2; JP3 = j + 3;
+        F_ANGLE = d.FANGLE;
+    } else {
+        j = A1(d.JMIX, nr) + 1;
+        JP1 = j - 1; JP2 = j - 2; JP3 = j - 3;
+        F_ANGLE = 0.0f;
+    }
+    const float F_ANGLE1 = 1.0f - F_ANGLE;
+    const float *rec = a.tMIX + (size_t)blockIdx.x * mix_rec_size(IM);
+    float gacc[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    for (int i = threadIdx.x + 1; i <= IM; i += blockDim.x) {
+        const float *q = rec + 5 + 10 * (i - 1);
+        D x[MIXN];
+        for (int c = 0; c < 5; ++c) x[c] = D(rec[c]);
+        for (int c = 0; c < 5; ++c) x[5 + c] = D(q[c]);
+        for (int c = 0; c < 4; ++c) x[10 + c] = D(q[5 + c]);
+        for (int c = 0; c < MIXN; ++c) x[c].g[c] = 1.0f;
+        const float RJP1 = A2(d.R, JP1, k), UJP1 = A2(d.UBLADE, JP1, k);
+        const D ROMIX = x[0];
+        const D VXMIX = x[1] / ROMIX;
+        const D VRMIX = x[2] / ROMIX;
+        const D VTMIX = x[3] / ROMIX / RJP1;
+        const D ROEMIX = x[4];
+        const D VMSQ = VXMIX * VXMIX + VRMIX * VRMIX;
+        const D VABSQ = VMSQ + VTMIX * VTMIX;
+        const D WTMIX = VTMIX - UJP1;
+        const D WMIXSQ = VMSQ + WTMIX * WTMIX;
+        const D WMIX = dsqrt(WMIXSQ);
+        const D ALPHAMIX = dasin(WTMIX / WMIX);
+        const D GAMAMIX = datan2(VRMIX, VXMIX);
+        const D TMIX = (ROEMIX / ROMIX - 0.5f * VABSQ) / d.CV;
+        const D ROTHALPY = d.CP * TMIX + 0.5f * (WMIXSQ - UJP1 * UJP1);
+        const D PMIX = ROMIX * d.RGAS * TMIX;
+        const float RJP2 = A2(d.R, JP2, k), UNOWJP2 = A2(d.UBLADE, JP2, k);
+        const float RJP3 = A2(d.R, JP3, k), UNOWJP3 = A2(d.UBLADE, JP3, k);
+        const D ROJP2 = x[5];
+        const D XVELJP2 = x[6] / ROJP2;
+        const D RVELJP2 = x[7] / ROJP2;
+        const D TVELJP2 = x[8] / RJP2 / ROJP2;
+        const D WTJP2 = TVELJP2 - UNOWJP2;
+        const D VMSQJP2 = XVELJP2 * XVELJP2 + RVELJP2 * RVELJP2;
+        const D VELSQJP2 = VMSQJP2 + TVELJP2 * TVELJP2;
+        const D WACT_SQ_JP2 = VMSQJP2 + WTJP2 * WTJP2;
+        const D WACT_JP2 = dsqrt(WACT_SQ_JP2);
+        const D T_ACT_JP2 = (x[9] / ROJP2 - 0.5f * VELSQJP2) / d.CV;
+        const D ROJP3 = x[10];
+        const D ROVXJP3 = x[11], ROVRJP3 = x[12];
+        const D ROVTJP3 = x[13] / RJP3;
+        const D ROWTJP3 = ROVTJP3 - UNOWJP3 * ROJP3;
+        const D ROWRELSQJP3 = ROVXJP3 * ROVXJP3 + ROVRJP3 * ROVRJP3 + ROWTJP3 * ROWTJP3;
+        const D ROWRELJP3 = dsqrt(ROWRELSQJP3);
+        const D ALPHAJP3 = dasin(ROWTJP3 / ROWRELJP3);
+        const D GAMAJP3 = datan2(ROVRJP3, ROVXJP3);
+        const D PSTAT = ROJP2 * d.RGAS * T_ACT_JP2;
+        const D TISENT = TMIX * dpowc(PSTAT / PMIX, d.FGA);
+        D WIS_SQ = 2.0f * (ROTHALPY - d.CP * TISENT + 0.5f * UNOWJP2 * UNOWJP2);
+        const D ROISENT = PSTAT / d.RGAS / TISENT;
+        if (WIS_SQ.v < 1.0f) WIS_SQ = D(1.0f);
+        const D WIS = dsqrt(WIS_SQ);
+        const float wm = WACT_JP2.v / sqrtf(d.GA * d.RGAS * T_ACT_JP2.v);
+        if (wm > 1.0f) atomicOr(a.flag, 1);
+        const D ALPHAA = F_ANGLE1 * ALPHAMIX + F_ANGLE * ALPHAJP3;
+        const D GAMA = F_ANGLE1 * GAMAMIX + F_ANGLE * GAMAJP3;
+        const D WT_JP2 = WIS * dsin(ALPHAA);
+        const D VM_JP2 = WIS * dcos(ALPHAA);
+        const D VX_JP2 = VM_JP2 * dcos(GAMA);
+        const D VR_JP2 = VM_JP2 * dsin(GAMA);
+        const D VT_JP2 = WT_JP2 + UNOWJP2;
+        const D V_SQ = VM_JP2 * VM_JP2 + VT_JP2 * VT_JP2;
+        const D ROE_JP2 = ROISENT * (d.CV * TISENT + 0.5f * V_SQ);
+        D out[5];
+        out[0] = RFMIX1 * x[5] + d.RFMIX * ROISENT;
+        out[1] = RFMIX1 * x[6] + d.RFMIX * (ROISENT * VX_JP2);
+        out[2] = RFMIX1 * x[7] + d.RFMIX * (ROISENT * VR_JP2);
+        out[3] = RFMIX1 * x[8] + d.RFMIX * (ROISENT * VT_JP2 * RJP2);
+        out[4] = RFMIX1 * x[9] + d.RFMIX * ROE_JP2;
+        // adjoints: the output order of the state variables is RO, ROVX, ROVR, RORVT, ROE
+        const int n2 = ix3(d, i, JP2, k), n3 = ix3(d, i, JP3, k);
+        float *A[5] = {a.v[V_RO].D, a.v[V_ROVX].D, a.v[V_ROVR].D, a.v[V_RORVT].D, a.v[V_ROE].D};
+        float go[5];
+        for (int c = 0; c < 5; ++c) go[c] = A[c][n2];
+        float gin[MIXN];
+        for (int q = 0; q < MIXN; ++q) {
+            float s = 0.0f;
+            for (int c = 0; c < 5; ++c) s += go[c] * out[c].g[q];
+            gin[q] = s;
+        }
+        for (int c = 0; c < 5; ++c) gacc[c] += gin[c];
+        for (int c = 0; c < 5; ++c) A[c][n2] = gin[5 + c];
+        for (int c = 0; c < 4; ++c) A[c][n3] += gin[10 + c];
+    }
+    for (int c = 0; c < 5; ++c) red[c][threadIdx.x] = gacc[c];
+    __syncthreads();
+    if (threadIdx.x < 5) {
+        float s = 0.0f;
+        for (int t = 0; t < (int)blockDim.x; ++t) s += red[threadIdx.x][t];
+        const int n1 = ix3(d, d.IMID, JP1, k);
+        float *A[5] = {a.v[V_RO].D, a.v[V_ROVX].D, a.v[V_ROVR].D, a.v[V_RORVT].D, a.v[V_ROE].D};
+        atomicAdd(&A[threadIdx.x][n1], s);
+    }
+}
+
+// =====================================================================
+// TSTEP, reversed: rk_ts_smooth (SMOOTH_VAR and the averaging fix-ups) ->
+// rk_ts_gather (corner gather, second mixing-plane average, negative
+// feedback) -> rk_ts_damp (the row-mean term of the negative feedback, the
+// restriction partials) -> rk_ts_cells (prolongation, mixing-plane
+// redistribution, SCREE, flux sum)
+// =====================================================================
+constexpr int RT_BS = 256;
+
+__device__ inline int mp_role_r(const Dev &d, int j, int *nr) {
+    for (int r = 1; r <= d.NRWSM1; ++r) {
+        int jx = A1(d.JMIX, r);
+        if (j == jx) { *nr = r; return 1; }
+        if (j == jx + 1) { *nr = r; return 2; }
+        if (j == jx + 2) { *nr = r; return 3; }
+    }
+    *nr = 0;
+    return 0;
+}
+__device__ inline int stream_case_r(const Dev &d, int j) {
+    int nr = A1(d.NROW, j);
+    int J1 = A1(d.JSTART, nr), J2 = A1(d.JMIX, nr);
+    int sc = 0;
+    if (j >= J1 + 3 && j <= J2 - 3) sc = 1;
+    if (j == J2) sc = 0;
+    if (j == J1) sc = 0;
+    if (j == J1 + 2) sc = 2;
+    if (j == J1 + 1) sc = 3;
+    if (j == J2 - 2) sc = 4;
+    if (j == J2 - 1) sc = 5;
+    return sc;
+}
+__device__ inline int le_case_r(const Dev &d, int j) {
+    int lc = 0;
+    for (int r = 1; r <= d.NROWS; ++r) {
+        int JL = A1(d.JLED, r);
+        if (j == JL - 2 || j == JL - 1) lc = 1;
+        if (j == JL) lc = 2;
+    }
+    return lc;
+}
+// the mixing-plane row of cell plane jc at K is averaged (1750, 1850)
+__device__ inline bool mp_row_on(const Dev &d, const Adj &a, int role, int mnr, int k) {
+    const bool lowx = d.FEXTRAP < 0.001f;
+    const float FLOWDIRN = -A3(a.tFLOWX, d.IMID, A1(d.JMIX, mnr), k);
+    return role == 3 ? (FLOWDIRN > 0.0f || lowx) : (FLOWDIRN < 0.0f || lowx);
+}
+
+__global__ void __launch_bounds__(RT_BS) rk_ts_smooth(const __grid_constant__ Dev d, const __grid_constant__ Adj a, int v0) {
+    extern __shared__ float sm[];
+    const AdjVar &V = a.v[v0 + blockIdx.y];
+    const int IM = d.IM, KM = d.KM, IMM1 = d.IMM1, KMM1 = d.KMM1;
+    const int np = IM * KM;
+    float *A_ = sm, *B_ = sm + np;
+    const int j = blockIdx.x + 1;
+    const DevCtl *c = a.tctl;
+    const size_t ks = (size_t)IM * d.JM;
+#define P(buf, i, k) buf[((i) - 1) + IM * ((k) - 1)]
+    for (int t = threadIdx.x; t < np; t += RT_BS) {
+        const int i = t % IM + 1, k = t / IM + 1;
+        A_[t] = A3(V.D, i, j, k);
+    }
+    __syncthreads();
+    // mixing-plane average of the variable (100)
+    bool mp = false;
+    if (d.IFMIX != 0)
+        for (int r = 1; r <= d.NRWSM1; ++r)
+            if (j == A1(d.JMIX, r) || j == A1(d.JMIX, r) + 1) mp = true;
+    if (mp) {
+        for (int k = threadIdx.x + 1; k <= KM; k += RT_BS) {
+            float s = 0.0f;
+            for (int i = 1; i <= IM; ++i) s += P(A_, i, k);
+            B_[k - 1] = s;
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < np; t += RT_BS) {
+            const int i = t % IM + 1, k = t / IM + 1;
+            A_[t] = 0.5f * B_[k - 1] * ((i <= IMM1 ? A1(d.FP, i) : 0.0f) + (i >= 2 ? A1(d.FP, i - 1) : 0.0f));
+        }
+        __syncthreads();
+    }
+    // tip-gap and periodic averaging of I=1 and I=IM (510, 8000)
+    const bool periodic_j = !(A1(d.IND, j) == 1 || A1(d.INDLE, j) == 1);
+    {
+        int nr = A1(d.NROW, j);
+        int K1 = A1(d.KTIPS, nr), K2 = A1(d.KTIPE, nr);
+        const bool tip = K1 > 0;
+        if (tip) {
+            if (K1 == 1) K2 = K2 - 1;
+            if (K2 == KM) K1 = K1 + 1;
+        }
+        for (int k = threadIdx.x + 1; k <= KM; k += RT_BS) {
+            if (tip && k >= K1 && k <= K2) {
+                float v = 0.5f * (P(A_, 1, k) + P(A_, IM, k));
+                P(A_, 1, k) = v;
+                P(A_, IM, k) = v;
+            }
+            if (periodic_j) {
+                float v = 0.5f * (P(A_, 1, k) + P(A_, IM, k));
+                P(A_, 1, k) = v;
+                P(A_, IM, k) = v;
+            }
+        }
+        __syncthreads();
+    }
+    if (!(d.SFEXIT < 0.0001f) && j >= d.JM + 1 - d.NSFEXIT) {
+        // exit smoothing is rejected when the adjoint is prepared
+    }
+    if (j >= 2 && !(c->SFT < 0.0001f)) {
+        const float SFT = c->SFT, SFT1 = c->SFT1, SFTH = c->SFTH, F4 = d.FAC_4TH;
+        // corners
+        float cv = 0.0f;
+        if (threadIdx.x < 4) {
+            const int ci = (threadIdx.x & 1) ? IM : 1, ck = (threadIdx.x & 2) ? KM : 1;
+            cv = P(A_, ci, ck);
+        }
+        __syncthreads();
+        if (threadIdx.x < 4) {
+            const int ci = (threadIdx.x & 1) ? IM : 1, ck = (threadIdx.x & 2) ? KM : 1;
+            const int ni = ci == 1 ? 2 : IMM1, nk = ck == 1 ? 2 : KMM1;
+            P(A_, ci, ck) = SFT1 * cv;
+            P(A_, ni, ck) += SFTH * cv;
+            P(A_, ci, nk) += SFTH * cv;
+        }
+        __syncthreads();
+        // spanwise pass: A_ = f(B_) -> B_bar
+        for (int t = threadIdx.x; t < np; t += RT_BS) B_[t] = 0.0f;
+        __syncthreads();
+        for (int t = threadIdx.x; t < np; t += RT_BS) {
+            const int i = t % IM + 1, k = t / IM + 1;
+            const float g = A_[t];
+            if (g == 0.0f) continue;
+            float *bi = B_ + (i - 1);     // bi[IM*(kk-1)] = P(B_, i, kk)
+            auto add = [&](int kk, float v) { atomicAdd(&bi[IM * (kk - 1)], v); };
+            add(k, SFT1 * g);
+            if (k == 1) {
+                add(2, SFT * g * (1.0f + 0.5f * A1(d.FKU, 1)));
+                add(3, -SFT * g * 0.5f * A1(d.FKU, 1));
+            } else if (k == KM) {
+                add(KMM1, SFT * g * (1.0f + 0.5f * A1(d.FKU, KM)));
+                add(d.KMM2, -SFT * g * 0.5f * A1(d.FKU, KM));
+            } else {
+                const float fkd = A1(d.FKD, k), fku = A1(d.FKU, k);
+                add(k + 1, SFT * g * fkd);
+                add(k - 1, SFT * g * fku);
+                // SC = FKU(k) curve(k-1) + FKD(k) curve(k+1), curve(kk) = b(kk) - FKD(kk) b(kk+1) - FKU(kk) b(kk-1)
+                const float h = SFT * F4 * g;
+                if (k - 1 != 1 && k - 1 != KM) {
+                    const int kk = k - 1;
+                    add(kk, h * fku);
+                    add(kk + 1, -h * fku * A1(d.FKD, kk));
+                    add(kk - 1, -h * fku * A1(d.FKU, kk));
+                }
+                if (k + 1 != 1 && k + 1 != KM) {
+                    const int kk = k + 1;
+                    add(kk, h * fkd);
+                    add(kk + 1, -h * fkd * A1(d.FKD, kk));
+                    add(kk - 1, -h * fkd * A1(d.FKU, kk));
+                }
+            }
+        }
+        __syncthreads();
+        // pitchwise pass: B_ = f(A_) -> A_bar
+        for (int t = threadIdx.x; t < np; t += RT_BS) A_[t] = 0.0f;
+        __syncthreads();
+        for (int t = threadIdx.x; t < np; t += RT_BS) {
+            const int i = t % IM + 1, k = t / IM + 1;
+            const float g = B_[t];
+            if (g == 0.0f) continue;
+            float *ak = A_ + IM * (k - 1) - 1;     // ak[ii] = P(A_, ii, k)
+            auto add = [&](int ii, float v) { atomicAdd(&ak[ii], v); };
+            // curve(ii) with weight w
+            auto curve = [&](int ii, float w) {
+                if (ii == 1 || ii == IM) {
+                    if (!periodic_j) return;
+                    add(1, w);
+                    add(2, -0.5f * w);
+                    add(IMM1, -0.5f * w);
+                    return;
+                }
+                add(ii, w);
+                add(ii + 1, -w * A1(d.FD, ii));
+                add(ii - 1, -w * A1(d.FU, ii));
+            };
+            add(i, SFT1 * g);
+            const float h = SFT * g;
+            if (i == 1 || i == IM) {
+                if (periodic_j) {
+                    add(2, 0.5f * h);
+                    add(IMM1, 0.5f * h);
+                    curve(2, 0.5f * F4 * h);
+                    curve(IMM1, 0.5f * F4 * h);
+                } else if (i == 1) {
+                    add(2, h * (1.0f + A1(d.FU, 1)));
+                    add(3, -h * A1(d.FU, 1));
+                } else {
+                    add(IMM1, h * (1.0f + A1(d.FU, IM)));
+                    add(d.IMM2, -h * A1(d.FU, IM));
+                }
+            } else {
+                const float fd = A1(d.FD, i), fu = A1(d.FU, i);
+                add(i + 1, h * fd);
+                add(i - 1, h * fu);
+                curve(i - 1, F4 * h * fu);
+                curve(i + 1, F4 * h * fd);
+            }
+        }
+        __syncthreads();
+    }
+    // streamwise and leading-edge smoothing: scatter into TMP's adjoint
+    const bool stream = !(c->SFX < 0.0001f);
+    const int sc = stream ? stream_case_r(d, j) : 0;
+    const int lc = stream ? le_case_r(d, j) : 0;
+    const int nr = A1(d.NROW, j);
+    const int J1 = A1(d.JSTART, nr), J2 = A1(d.JMIX, nr);
+    const float SFX = c->SFX, SFX1 = c->SFX1, SFXB = c->SFXB, SFXB1 = c->SFXB1, SFXBH = c->SFXBH;
+    const float SFXHM1 = c->SFXHM1, SFX14 = c->SFX14, F4 = d.FAC_4TH;
+    int nq = 0, jq[4] = {0, 0, 0, 0};
+    float cq[4] = {0.0f, 0.0f, 0.0f, 0.0f}, c0 = 1.0f;
+    auto addq = [&](int jj, float cc) { jq[nq] = jj; cq[nq] = cc; ++nq; };
+    switch (sc) {
+    case 1:
+        c0 = SFX1 - 0.5f * SFX * F4;
+        addq(j + 1, 0.5f * SFX * (1.0f + F4)); addq(j - 1, 0.5f * SFX * (1.0f + F4));
+        addq(j - 2, -0.25f * SFX * F4); addq(j + 2, -0.25f * SFX * F4);
+        break;
+    case 2: c0 = SFXB1; addq(J1 + 3, SFXBH); addq(J1 + 1, SFXBH); break;
+    case 3: c0 = SFXB1; addq(J1 + 2, 1.25f * SFXB); addq(J1 + 3, 0.5f * SFXB); addq(J1 + 4, -0.75f * SFXB); break;
+    case 4: c0 = SFXB1; addq(J2 - 1, SFXBH); addq(J2 - 3, SFXBH); break;
+    case 5: c0 = SFXB1; addq(J2 - 2, 1.25f * SFXB); addq(J2 - 3, 0.5f * SFXB); addq(J2 - 4, -0.75f * SFXB); break;
+    default: break;
+    }
+    for (int t = threadIdx.x; t < np; t += RT_BS) {
+        const int i = t % IM + 1, k = t / IM + 1;
+        const float g = A_[t];
+        if (g == 0.0f) continue;
+        float *tm = V.TM + (size_t)(i - 1) + ks * (k - 1);     // tm[IM*(jj-1)] = TMP(i, jj, k)
+        if (lc && (i == 1 || i == IM)) {
+            aadd(&tm[(size_t)IM * (j - 1)], SFXHM1 * g);
+            float *tk = V.TM + ks * (k - 1) + (size_t)IM * (j - 1);   // tk[x] = TMP(x+1, j, k)
+            if (lc == 1) {
+                aadd(&tk[1], SFX14 * g);
+                aadd(&tk[IMM1 - 1], SFX14 * g);
+            } else if (i == 1) {
+                aadd(&tk[IM], SFX14 * g);
+                aadd(&tk[IM - 1], SFX14 * g);
+            } else {
+                aadd(&tk[IM + IM - 1], SFX14 * g);
+                aadd(&tk[0], SFX14 * g);
+            }
+            continue;
+        }
+        aadd(&tm[(size_t)IM * (j - 1)], c0 * g);
+        for (int q = 0; q < nq; ++q) aadd(&tm[(size_t)IM * (jq[q] - 1)], cq[q] * g);
+    }
+#undef P
+}
+
+__global__ void __launch_bounds__(RT_BS) rk_ts_gather(const __grid_constant__ Dev d, const __grid_constant__ Adj a, int v0) {
+    extern __shared__ float sm[];
+    __shared__ double shd[RT_BS / 32];
+    const AdjVar &V = a.v[v0 + blockIdx.y];
+    const int IM = d.IM, IMM1 = d.IMM1, KMM1 = d.KMM1;
+    const int j = blockIdx.x + 1;
+    // the variable's own adjoint: D = TMP + gather, so dJ/dD(old) = dJ/dTMP
+    for (int t = threadIdx.x; t < IM * d.KM; t += RT_BS) {
+        const int i = t % IM + 1, k = t / IM + 1;
+        A3(V.D, i, j, k) = A3(V.TM, i, j, k);
+    }
+    if (j < 2) return;
+    const int jc = j;
+    const int nc = IMM1 * KMM1;
+    float *av = sm;
+    const float fdn = A1(d.FACDWN, jc), fup = A1(d.FACUP, jc);
+    for (int c = threadIdx.x; c < nc; c += RT_BS) {
+        const int i = c % IMM1 + 1, k = c / IMM1 + 1;
+        auto tm = [&](int ii, int jj, int kk) { return A3(V.TM, ii, jj, kk); };
+        float s = AIK(d.FBL, i, k) * (fdn * tm(i, jc, k) + fup * tm(i, jc - 1, k));
+        s += AIK(d.FBR, i, k) * (fdn * tm(i + 1, jc, k) + fup * tm(i + 1, jc - 1, k));
+        s += AIK(d.FTL, i, k) * (fdn * tm(i, jc, k + 1) + fup * tm(i, jc - 1, k + 1));
+        s += AIK(d.FTR, i, k) * (fdn * tm(i + 1, jc, k + 1) + fup * tm(i + 1, jc - 1, k + 1));
+        av[c] = s;
+    }
+    __syncthreads();
+    // second mixing-plane average (1850): a row set to its mean
+    int mnr;
+    const int role = mp_role_r(d, jc, &mnr);
+    if (role == 1 || role == 3) {
+        for (int k = threadIdx.x + 1; k <= KMM1; k += RT_BS) {
+            if (!mp_row_on(d, a, role, mnr, k)) continue;
+            float *row = av + (size_t)(k - 1) * IMM1;
+            float s = 0.0f;
+            for (int i = 0; i < IMM1; ++i) s += row[i];
+            s = s / (float)IMM1;
+            for (int i = 0; i < IMM1; ++i) row[i] = s;
+        }
+        __syncthreads();
+    }
+    // negative feedback v = S / (1 + |S| / (blk DAMP)): dv/dS = 1/(1+q)^2,
+    // dv/dblk = S q / (blk (1+q)^2); the blk term is summed per plane
+    const DevCtl *ctl = a.tctl;
+    const int damp_on = ctl->damp_on;
+    const float DAMP = ctl->DAMP;
+    const float blk = damp_on ? V.tBLK[A1(d.NROW, jc) - 1] : 1.0f;
+    double pb = 0.0;
+    for (int c = threadIdx.x; c < nc; c += RT_BS) {
+        const int i = c % IMM1 + 1, k = c / IMM1 + 1;
+        const float g = av[c];
+        float out = g;
+        if (damp_on) {
+            const float S = A3(V.tST, i, jc, k);
+            const float q = fabsf(S) / (blk * DAMP);
+            const float r = 1.0f / (1.0f + q);
+            out = g * r * r;
+            pb += (double)(g * S * q / blk * r * r);
+        }
+        A3(V.ST, i, jc, k) = out;
+    }
+    for (int o = 16; o > 0; o >>= 1) pb += __shfl_down_sync(0xffffffffu, pb, o);
+    if ((threadIdx.x & 31) == 0) shd[threadIdx.x >> 5] = pb;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < RT_BS / 32; ++w) s += shd[w];
+        V.pblk[jc - 1] = s;
+    }
+}
+
+__global__ void __launch_bounds__(RT_BS) rk_ts_damp(const __grid_constant__ Dev d, const __grid_constant__ Adj a, int v0) {
+    __shared__ double shd[RT_BS / 32];
+    __shared__ float gchg[64], gblk[64];
+    const AdjVar &V = a.v[v0 + blockIdx.y];
+    const int IMM1 = d.IMM1, KMM1 = d.KMM1;
+    const int j = blockIdx.x + 2;
+    const int nc = IMM1 * KMM1;
+    const DevCtl *ctl = a.tctl;
+    const int NROWS = d.NROWS;
+    float add = 0.0f;
+    if (ctl->damp_on) {
+        // dJ/dblk per row, then through the row mixing to dJ/dchg
+        if (threadIdx.x < NROWS) {
+            double s = 0.0;
+            for (int jj = 2; jj <= d.JM; ++jj)
+                if (A1(d.NROW, jj) == (int)threadIdx.x + 1) s += V.pblk[jj - 1];
+            gblk[threadIdx.x] = (float)s;
+            gchg[threadIdx.x] = 0.0f;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (NROWS == 1) gchg[0] = gblk[0];
+            if (NROWS == 2) {
+                const float g = gblk[0] + gblk[1];
+                gchg[0] = 0.5f * g;
+                gchg[1] = 0.5f * g;
+            }
+            if (NROWS > 2) {
+                for (int nr = 2; nr <= NROWS - 1; ++nr) {
+                    const float g = gblk[nr - 1];
+                    gchg[nr - 2] += 0.25f * g;
+                    gchg[nr] += 0.25f * g;
+                    gchg[nr - 1] += 0.5f * g;
+                }
+                gchg[NROWS - 2] += 0.5f * gblk[NROWS - 1];
+                gchg[NROWS - 1] += 0.5f * gblk[NROWS - 1];
+                gchg[0] += 0.5f * gblk[0];
+                gchg[1] += 0.5f * gblk[0];
+            }
+        }
+        __syncthreads();
+        for (int nr = 1; nr <= NROWS; ++nr) {
+            const int JST = A1(d.JSTART, nr) + 1, JEN = A1(d.JMIX, nr) - 1;
+            if (j >= JST && j <= JEN) add = gchg[nr - 1] / (float)(IMM1 * KMM1 * (JEN - JST + 1));
+        }
+    }
+    double ps = 0.0;
+    for (int c = threadIdx.x; c < nc; c += RT_BS) {
+        const int i = c % IMM1 + 1, k = c / IMM1 + 1;
+        const int n = ix3(d, i, j, k);
+        float g = V.ST[n];
+        if (add != 0.0f) g += (V.tST[n] < 0.0f ? -add : add);
+        V.ST[n] = g;
+        const float y = g * d.RSTEP[n];
+        V.Y[n] = y;
+        ps += (double)y;
+    }
+    for (int o = 16; o > 0; o >>= 1) ps += __shfl_down_sync(0xffffffffu, ps, o);
+    if ((threadIdx.x & 31) == 0) shd[threadIdx.x >> 5] = ps;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < RT_BS / 32; ++w) s += shd[w];
+        V.psum[j - 1] = s;
+    }
+    // level-1 and level-2 partial sums of Y over this plane
+    const int n1 = d.NIB1 * d.NKB1, n2 = d.NIB2 * d.NKB2;
+    for (int t = threadIdx.x; t < n1 + n2; t += RT_BS) {
+        const bool lv1 = t < n1;
+        const int u = lv1 ? t : t - n1;
+        const int nib = lv1 ? d.NIB1 : d.NIB2;
+        const int ib = u % nib + 1, kb = u / nib + 1;
+        const int i0 = lv1 ? A1(d.IB1_S, ib) : A1(d.IB2_S, ib), i1 = lv1 ? A1(d.IB1_E, ib) : A1(d.IB2_E, ib);
+        const int k0 = lv1 ? A1(d.KB1_S, kb) : A1(d.KB2_S, kb), k1 = lv1 ? A1(d.KB1_E, kb) : A1(d.KB2_E, kb);
+        float s = 0.0f;
+        for (int k = k0; k <= k1; ++k)
+            for (int i = i0; i <= i1; ++i) s += A3(V.Y, i, j, k);
+        if (lv1) V.P1[(size_t)(j - 1) * n1 + u] = s;
+        else V.P2[(size_t)(j - 1) * n2 + u] = s;
+    }
+}
+
+__global__ void __launch_bounds__(RT_BS) rk_ts_cells(const __grid_constant__ Dev d, const __grid_constant__ Adj a, int v0) {
+    extern __shared__ float sm[];
+    __shared__ float s_sb;
+    const AdjVar &V = a.v[v0 + blockIdx.y];
+    const int IM = d.IM, IMM1 = d.IMM1, KMM1 = d.KMM1;
+    const int j = blockIdx.x + 2;
+    const int nc = IMM1 * KMM1;
+    const int n1 = d.NIB1 * d.NKB1, n2 = d.NIB2 * d.NKB2;
+    float *b1 = sm, *b2 = sm + n1, *st = sm + n1 + n2, *rs = st + nc;
+    const int j1 = A1(d.JB1, j), j2 = A1(d.JB2, j), jsb = A1(d.JSBLK, j);
+    const size_t m1 = (size_t)d.NIB1 * (d.NJB1 + 1), m2 = (size_t)d.NIB2 * (d.NJB2 + 1);
+    for (int t = threadIdx.x; t < n1; t += RT_BS) {
+        float s = 0.0f;
+        if (j1 <= d.NJB1)
+            for (int jj = A1(d.JB1_START, j1); jj <= A1(d.JB1_END, j1); ++jj) s += V.P1[(size_t)(jj - 1) * n1 + t];
+        b1[t] = s;
+    }
+    for (int t = threadIdx.x; t < n2; t += RT_BS) {
+        float s = 0.0f;
+        if (j2 <= d.NJB2)
+            for (int jj = A1(d.JB2_START, j2); jj <= A1(d.JB2_END, j2); ++jj) s += V.P2[(size_t)(jj - 1) * n2 + t];
+        b2[t] = s;
+    }
+    if (threadIdx.x < 32) {
+        const int a0 = A1(d.SB_START, jsb), b0 = A1(d.SB_END, jsb);
+        double s = 0.0;
+        for (int jj = a0 + (int)threadIdx.x; jj <= b0; jj += 32) s += V.psum[jj - 1];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) s_sb = (float)s;
+    }
+    __syncthreads();
+    const float SB = s_sb, SSB = A1(d.STEPSBK, jsb);
+    for (int c = threadIdx.x; c < nc; c += RT_BS) {
+        const int i = c % IMM1 + 1, k = c / IMM1 + 1;
+        const int n = ix3(d, i, j, k);
+        const int i1 = A1(d.IB1, i), i2 = A1(d.IB2, i), k1 = A1(d.KB1, k), k2 = A1(d.KB2, k);
+        const size_t s1 = (size_t)(i1 - 1) + (size_t)d.NIB1 * (j1 - 1) + m1 * (k1 - 1);
+        const size_t s2 = (size_t)(i2 - 1) + (size_t)d.NIB2 * (j2 - 1) + m2 * (k2 - 1);
+        st[c] = V.ST[n] * d.STEP[n] + b1[(k1 - 1) * d.NIB1 + (i1 - 1)] * d.STEP1[s1] +
+                b2[(k2 - 1) * d.NIB2 + (i2 - 1)] * d.STEP2[s2] + SB * SSB;
+    }
+    __syncthreads();
+    // mixing-plane pitchwise redistribution (1750): row <- (sum of row) FP(I)
+    int mnr;
+    const int role = mp_role_r(d, j, &mnr);
+    if (role == 1 || role == 3) {
+        for (int k = threadIdx.x + 1; k <= KMM1; k += RT_BS) {
+            if (!mp_row_on(d, a, role, mnr, k)) continue;
+            float *row = st + (size_t)(k - 1) * IMM1;
+            float s = 0.0f;
+            for (int i = 1; i <= IMM1; ++i) s += row[i - 1] * A1(d.FP, i);
+            for (int i = 0; i < IMM1; ++i) row[i] = s;
+        }
+        __syncthreads();
+    }
+    // SCREE: STORE = F1 DELTA + F2 DIFF, DIFF = DELTA + F3 DIFF; then the flux sum
+    const float RATPITCH = (float)A1(d.NBLADE, j - 1) / (float)A1(d.NBLADE, j);
+    const int nr = A1(d.NROW, j);
+    const int kts = A1(d.KTIPS, nr), kte = A1(d.KTIPE, nr);
+    const bool lowx = d.FEXTRAP < 0.001f;
+    const int jmx = role ? A1(d.JMIX, mnr) : 0;
+    const float F1 = d.F1, F2 = d.F2, F3 = d.F3;
+    for (int k = threadIdx.x; k < KMM1; k += RT_BS) rs[k] = 0.0f;
+    __syncthreads();
+    for (int c = threadIdx.x; c < nc; c += RT_BS) {
+        const int i = c % IMM1 + 1, k = c / IMM1 + 1;
+        const int n = ix3(d, i, j, k);
+        const float gdiff = V.DIFF[n];
+        const float gst = st[c];
+        const float gdelta = F1 * gst + gdiff;
+        V.DIFF[n] = F2 * gst + F3 * gdiff;
+        if (gdelta == 0.0f) continue;
+        aadd(&V.XF[n], gdelta);
+        aadd(&A3(V.XF, i, j - 1, k), -RATPITCH * gdelta);
+        aadd(&V.RF[n], gdelta);
+        aadd(&A3(V.RF, i, j, k + 1), -gdelta);
+        const bool gap = kts > 0 && k >= kts && k <= kte - 1;
+        // t0 = TF(i): the tip-gap mean of TF(1) and TF(IM) at i = 1
+        if (gap && i == 1) {
+            aadd(&A3(V.TF, 1, j, k), 0.5f * gdelta);
+            aadd(&A3(V.TF, IM, j, k), 0.5f * gdelta);
+        } else {
+            aadd(&V.TF[n], gdelta);
+        }
+        // t1 = TF(i+1): the mean at i+1 = IM
+        if (gap && i + 1 == IM) {
+            aadd(&A3(V.TF, 1, j, k), -0.5f * gdelta);
+            aadd(&A3(V.TF, IM, j, k), -0.5f * gdelta);
+        } else {
+            aadd(&A3(V.TF, i + 1, j, k), -gdelta);
+        }
+        // source: -src
+        const float gsrc = -gdelta;
+        bool plain = true;
+        if (role && !lowx) {
+            const float FLOWDIRN = -A3(a.tFLOWX, d.IMID, jmx, k);
+            if (role == 1 && FLOWDIRN > 0.0f) {
+                // src = SR - (XF(i,j-1) - lsum FP(i)) FEXTRAP, lsum = sum_i XF(i,j-1)
+                aadd(&A3(V.XF, i, j - 1, k), -gsrc * d.FEXTRAP);
+                atomicAdd(&rs[k - 1], gsrc * d.FEXTRAP * A1(d.FP, i));
+            }
+            if (role == 2) plain = false;
+            if (role == 3 && !(FLOWDIRN > 0.0f)) {
+                aadd(&V.XF[n], gsrc * d.FEXTRAP);
+                atomicAdd(&rs[k - 1], -gsrc * d.FEXTRAP * A1(d.FP, i));
+            }
+        }
+        if (plain) aadd(&V.SR[n], gsrc);
+    }
+    __syncthreads();
+    if (role == 1 || role == 3) {
+        const int jj = role == 1 ? j - 1 : j;
+        for (int c = threadIdx.x; c < nc; c += RT_BS) {
+            const int i = c % IMM1 + 1, k = c / IMM1 + 1;
+            aadd(&A3(V.XF, i, jj, k), rs[k - 1]);
+        }
+    }
+}
+
+// objective seeds added at the start of each reverse step
+__global__ void rk_seed(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+    const int IM = d.IM, KM = d.KM;
+    const int np = IM * KM, nc = d.IMM1 * d.KMM1;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int per = 5 * np + nc;
+    if (t >= 2 * per) return;
+    const int p = t / per, r = t % per;
+    const int j = a.seed_j[p];
+    const float s = a.seed[t];
+    if (s == 0.0f) return;
+    if (r < 5 * np) {
+        const int q = r / np, u = r % np;
+        const int i = u % IM + 1, k = u / IM + 1;
+        float *A[5] = {a.VX, a.VT, a.VR, a.HO, a.P};
+        A3(A[q], i, j, k) += s;
+    } else {
+        const int u = r - 5 * np;
+        const int i = u % d.IMM1 + 1, k = u / d.IMM1 + 1;
+        A3(a.FLOWX, i, j, k) += s;
+    }
+}
+
+// objective seeds of the EFICOOL mass averages on plane j (FP64 weights
+// from the host): dJ/dspo, dJ/dsto, dJ/dbf
+__global__ void rk_seed_plane(const __grid_constant__ Dev d, const __grid_constant__ Adj a, float *seed, int j,
+                              double gspo, double gsto, double gbf, double spo, double sto, double bf) {
+    const int IM = d.IM, KM = d.KM, IMM1 = d.IMM1, KMM1 = d.KMM1;
+    const int np = IM * KM;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const double nb = (double)A1(d.NBLADE, j);
+    const float TO1M = A1(d.TO1, d.KMID), PO1M = A1(d.PO1, d.KMID);
+    auto tmp_of = [&](int n, float *dP, float *dHO, float *dE) {
+        const float vx = a.tVX[n], vt = a.tVT[n], vr = a.tVR[n];
+        const float EKE = 0.5f * (vx * vx + vt * vt + vr * vr);
+        float TS = (a.tHO[n] - EKE) * d.RCP, TSTAG = a.tHO[n] * d.RCP;
+        const bool cT = TSTAG < 0.1f * TO1M, cS = TS < 0.1f * TO1M;
+        if (cT) TSTAG = 0.1f * TO1M;
+        if (cS) TS = 0.1f * TO1M;
+        float PSTAT = a.tP[n];
+        const bool cP = PSTAT < 0.02f * PO1M;
+        if (cP) PSTAT = 0.02f * PO1M;
+        const float rat = powf(TSTAG / TS, d.RFGA);
+        const float TMP = PSTAT * rat / PO1M;
+        *dP = cP ? 0.0f : rat / PO1M;
+        const float dTSTAG = cT ? 0.0f : TMP * d.RFGA / TSTAG * d.RCP;
+        const float dTS = cS ? 0.0f : -TMP * d.RFGA / TS;
+        *dHO = dTSTAG + dTS * d.RCP;
+        *dE = -dTS * d.RCP;   // d/dEKE
+        return TMP;
+    };
+    if (t < np) {
+        // node (i, j, k): the cells of plane j around it weight its TMP, TEMP1 and P
+        const int i = t % IM + 1, k = t / IM + 1;
+        double w = 0.0;
+        for (int kc = k - 1; kc <= k; ++kc)
+            for (int ic = i - 1; ic <= i; ++ic) {
+                if (ic < 1 || ic > IMM1 || kc < 1 || kc > KMM1) continue;
+                w += 0.25 * (-(double)A3(a.tFLOWX, ic, j, kc) * nb) / bf;
+            }
+        const int n = ix3(d, i, j, k);
+        float dP, dHO, dE;
+        tmp_of(n, &dP, &dHO, &dE);
+        const float TSTAG = a.tHO[n] * d.RCP;
+        const float dT1 = (TSTAG < 0.1f * TO1M) ? 0.0f : d.RCP;
+        const double gt = gspo * w, gT1 = gsto * w;
+        const float vx = a.tVX[n], vt = a.tVT[n], vr = a.tVR[n];
+        seed[0 * np + t] = (float)(gt * dE * vx);
+        seed[1 * np + t] = (float)(gt * dE * vt);
+        seed[2 * np + t] = (float)(gt * dE * vr);
+        seed[3 * np + t] = (float)(gt * dHO + gT1 * dT1);
+        seed[4 * np + t] = (float)(gt * dP);
+    } else if (t < np + IMM1 * KMM1) {
+        const int u = t - np;
+        const int i = u % IMM1 + 1, k = u / IMM1 + 1;
+        // spo = sum_c 0.25 DFLOW_c sum TMP / bf, DFLOW_c = -FLOWX_c NB
+        float dP, dHO, dE;
+        double stmp = 0.0, stt = 0.0;
+        const int ii[4] = {i, i + 1, i + 1, i}, kk[4] = {k, k, k + 1, k + 1};
+        for (int q = 0; q < 4; ++q) {
+            const int n = ix3(d, ii[q], j, kk[q]);
+            stmp += (double)tmp_of(n, &dP, &dHO, &dE);
+            float TSTAG = a.tHO[n] * d.RCP;
+            if (TSTAG < 0.1f * TO1M) TSTAG = 0.1f * TO1M;
+            stt += (double)TSTAG;
+        }
+        const double dflow = -nb;   // d DFLOW / d FLOWX
+        const double g = gspo * (0.25 * stmp - spo) / bf * dflow + gsto * (0.25 * stt - sto) / bf * dflow + gbf * dflow;
+        seed[5 * np + u] = (float)g;
+    }
+}
+
+}  // namespace
+
+// =====================================================================
+// host side
+// =====================================================================
+#define ACK(call)                                                                                    \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) return api_fail(MGPU_E_CUDA, (std::string(#call) + ": " + cudaGetErrorString(e_)).c_str()); \
+    } while (0)
+
+// row means of |STORE| after the row mixing, as the negative feedback of the
+// recorded step formed them (1501-1525): one CTA per variable
+__global__ void rk_blk(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+    __shared__ double sh[RT_BS / 32];
+    __shared__ float chg[64];
+    const AdjVar &V = a.v[blockIdx.x];
+    float *blk = const_cast<float *>(V.tBLK);
+    const int IMM1 = d.IMM1, KMM1 = d.KMM1, NROWS = d.NROWS;
+    for (int nr = 1; nr <= NROWS; ++nr) {
+        const int JST = A1(d.JSTART, nr) + 1, JEN = A1(d.JMIX, nr) - 1;
+        const int nc = IMM1 * KMM1 * (JEN - JST + 1);
+        double s = 0.0;
+        for (int c = threadIdx.x; c < nc; c += RT_BS) {
+            const int i = c % IMM1 + 1, r = c / IMM1;
+            const int k = r % KMM1 + 1, j = JST + r / KMM1;
+            s += (double)fabsf(A3(V.tST, i, j, k));
+        }
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w = 0; w < RT_BS / 32; ++w) t += sh[w];
+            chg[nr - 1] = (float)t / (float)nc;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (NROWS == 1) blk[0] = chg[0];
+        if (NROWS == 2) {
+            blk[1] = 0.5f * (chg[0] + chg[1]);
+            blk[0] = blk[1];
+        }
+        if (NROWS > 2) {
+            for (int nr = 2; nr <= NROWS - 1; ++nr) blk[nr - 1] = 0.25f * (chg[nr - 2] + chg[nr]) + 0.5f * chg[nr - 1];
+            blk[NROWS - 1] = 0.5f * (chg[NROWS - 2] + chg[NROWS - 1]);
+            blk[0] = 0.5f * (chg[0] + chg[1]);
+        }
+    }
+}
+
+// sum of squares of the five conserved-variable adjoints and of their change
+__global__ void rk_norms(const __grid_constant__ Dev d, const __grid_constant__ Adj a, const float *prev, double *out) {
+    __shared__ double sh[2][RT_BS / 32];
+    const size_t N = (size_t)d.IM * d.JM * d.KM;
+    double s = 0.0, c = 0.0;
+    for (size_t t = (size_t)blockIdx.x * RT_BS + threadIdx.x; t < 5 * N; t += (size_t)gridDim.x * RT_BS) {
+        const int v = (int)(t / N);
+        const float x = a.v[v].D[t - (size_t)v * N];
+        const float p = prev[t];
+        s += (double)x * x;
+        c += (double)(x - p) * (x - p);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_down_sync(0xffffffffu, s, o);
+        c += __shfl_down_sync(0xffffffffu, c, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sh[0][threadIdx.x >> 5] = s;
+        sh[1][threadIdx.x >> 5] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ts = 0.0, tc = 0.0;
+        for (int w = 0; w < RT_BS / 32; ++w) {
+            ts += sh[0][w];
+            tc += sh[1][w];
+        }
+        atomicAdd(&out[0], ts);
+        atomicAdd(&out[1], tc);
+    }
+}
+
+struct AdjState {
+    mgpu_handle *h = nullptr;
+    Adj a;
+    std::vector<void *> allocs;
+    DevCtl *tctl = nullptr;
+    int *flag = nullptr;
+    float *seed = nullptr;
+    float *prev = nullptr;       // 5 N: the conserved-variable adjoints before the last iteration
+    double *norms = nullptr;
+    std::vector<double> sums;    // (4, JM) EFICOOL sums of the recorded step
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    int objective = -1;
+    double value = 0.0;
+    bool ready = false;
+    int iters = 0;
+};
+
+void adj_destroy(AdjState *s) {
+    if (!s) return;
+    if (s->gexec) cudaGraphExecDestroy(s->gexec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    for (void *p : s->allocs) cudaFree(p);
+    delete s;
+}
+
+namespace {
+
+template <typename T>
+int aalloc(AdjState *s, T **p, size_t count) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, (count ? count : 1) * sizeof(T));
+    if (e != cudaSuccess) return api_fail(MGPU_E_NOMEM, "adjoint device allocation");
+    s->allocs.push_back(q);
+    cudaMemset(q, 0, (count ? count : 1) * sizeof(T));
+    *p = (T *)q;
+    return 0;
+}
+
+size_t smooth_bytes(const Dev &d) { return (size_t)2 * d.IM * d.KM * sizeof(float); }
+size_t gather_bytes(const Dev &d) { return (size_t)d.IMM1 * d.KMM1 * sizeof(float); }
+size_t cells_bytes(const Dev &d) {
+    return ((size_t)d.NIB1 * d.NKB1 + (size_t)d.NIB2 * d.NKB2 + (size_t)d.IMM1 * d.KMM1 + d.KMM1) * sizeof(float);
+}
+
+int configure(const Dev &d) {
+    struct {
+        const void *f;
+        size_t b;
+    } k[] = {{(const void *)rk_ts_smooth, smooth_bytes(d)}, {(const void *)rk_ts_gather, gather_bytes(d)},
+             {(const void *)rk_ts_cells, cells_bytes(d)}};
+    for (auto &x : k) {
+        if (x.b > 200 * 1024) return api_fail(MGPU_E_UNSUPPORTED, "J-plane too large for the adjoint kernels");
+        ACK(cudaFuncSetAttribute(x.f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(x.b > 48 * 1024 ? x.b : 48 * 1024)));
+    }
+    return 0;
+}
+
+void launch_tstep_rev(const Dev &d, const Adj &a, cudaStream_t s, int v0, int nv) {
+    const size_t N = (size_t)d.IM * d.JM * d.KM;
+    for (int v = v0; v < v0 + nv; ++v) cudaMemsetAsync(a.v[v].TM, 0, N * sizeof(float), s);
+    const unsigned ja = (unsigned)d.JM, jp = (unsigned)(d.JM - 1);
+    rk_ts_smooth<<<dim3(ja, nv), RT_BS, smooth_bytes(d), s>>>(d, a, v0);
+    rk_ts_gather<<<dim3(ja, nv), RT_BS, gather_bytes(d), s>>>(d, a, v0);
+    rk_ts_damp<<<dim3(jp, nv), RT_BS, 0, s>>>(d, a, v0);
+    rk_ts_cells<<<dim3(jp, nv), RT_BS, cells_bytes(d), s>>>(d, a, v0);
+}
+
+// one reverse step: the adjoints of the state after a step (plus the
+// objective seeds) -> the adjoints of the state before it
+void enqueue_reverse(const Dev &d, const Adj &a, cudaStream_t s) {
+    const size_t N = (size_t)d.IM * d.JM * d.KM;
+    const unsigned gN = gridn(N, 256);
+    const int per = 5 * d.IM * d.KM + d.IMM1 * d.KMM1;
+    rk_seed<<<gridn((size_t)2 * per, 256), 256, 0, s>>>(d, a);
+    if (d.IFMIX > 0 && d.RFMIX > 1.0e-3f && d.NRWSM1 > 0) rk_mixplan<<<d.NRWSM1 * d.KM, 64, 0, s>>>(d, a);
+    launch_tstep_rev(d, a, s, V_ROVX, 3);
+    rk_flux_mom<<<gN, 256, 0, s>>>(d, a);
+    rk_peff<<<gN, 256, 0, s>>>(d, a);
+    rk_bc_apply<<<gridn((size_t)d.IM * d.KM, 128), 128, 0, s>>>(d, a);
+    launch_tstep_rev(d, a, s, V_RO, 2);
+    rk_flux_energy<<<gN, 256, 0, s>>>(d, a);
+    rk_bc_sums<<<1, 256, 0, s>>>(d, a);
+    rk_flux_mass<<<gN, 256, 0, s>>>(d, a);
+    rk_prim<<<gN, 256, 0, s>>>(d, a);
+}
+
+int unsupported(const Dev &d) {
+    if (d.ITIMST != 3 || d.NRSMTH != 0) return api_fail(MGPU_E_UNSUPPORTED, "adjoint: SCREE without residual smoothing only");
+    if (d.IPOUT != 0) return api_fail(MGPU_E_UNSUPPORTED, "adjoint: IPOUT = 0 only");
+    if (d.IN_PRESS != 0 || d.IN_VTAN != 0 || d.IN_VR > 0)
+        return api_fail(MGPU_E_UNSUPPORTED, "adjoint: IN_PRESS = 0, IN_VTAN = 0 and IN_VR <= 0 only");
+    if (d.IN_FLOW != 0 || d.THROTTLE_EXIT > 0.001f || d.PLATE_LOSS > 0.001f || d.any_cusp2)
+        return api_fail(MGPU_E_UNSUPPORTED, "adjoint: SETFLO, throttle, exit plate loss and IF_CUSP = 2 not differentiated");
+    if (!(d.SFEXIT < 0.0001f) && d.NSFEXIT > 0) return api_fail(MGPU_E_UNSUPPORTED, "adjoint: exit smoothing not differentiated");
+    if (d.KM > 512 || d.NROWS > 64) return api_fail(MGPU_E_UNSUPPORTED, "adjoint: KM <= 512 and NROWS <= 64");
+    return 0;
+}
+
+int allocate(AdjState *s, const Dev &d) {
+    const size_t N = (size_t)d.IM * d.JM * d.KM, np = (size_t)d.IM * d.KM;
+    Adj &a = s->a;
+    memset(&a, 0, sizeof(a));
+    int rc = 0;
+    auto F = [&](float **p, size_t n) { if (!rc) rc = aalloc(s, p, n); };
+    auto Fc = [&](const float **p, size_t n) {
+        float *q = nullptr;
+        if (!rc) rc = aalloc(s, &q, n);
+        *p = q;
+    };
+    for (int v = 0; v < NVAR; ++v) {
+        AdjVar &V = a.v[v];
+        F(&V.D, N); F(&V.DIFF, N); F(&V.SR, N); F(&V.ST, N); F(&V.TM, N); F(&V.Y, N);
+        if (v != V_RO) { F(&V.XF, N); F(&V.TF, N); F(&V.RF, N); }
+        F(&V.P1, (size_t)d.JM * d.NIB1 * d.NKB1);
+        F(&V.P2, (size_t)d.JM * d.NIB2 * d.NKB2);
+        if (!rc) rc = aalloc(s, &V.psum, d.JM);
+        if (!rc) rc = aalloc(s, &V.pblk, d.JM);
+        Fc(&V.tST, N);
+        Fc(&V.tBLK, d.NROWS);
+    }
+    F(&a.P, N); F(&a.HO, N); F(&a.VX, N); F(&a.VR, N); F(&a.VT, N); F(&a.ROVT, N); F(&a.PEFF, N);
+    F(&a.FLOWX, N); F(&a.FLOWT, N); F(&a.FLOWR, N);
+    a.v[V_RO].XF = a.FLOWX; a.v[V_RO].TF = a.FLOWT; a.v[V_RO].RF = a.FLOWR;
+    F(&a.PD, d.KM); F(&a.PDK, d.KM); F(&a.PAVG, d.KM); F(&a.SSUM, d.KM);
+    Fc(&a.tRO, N); Fc(&a.tROVX, N); Fc(&a.tROVR, N); Fc(&a.tRORVT, N); Fc(&a.tROE, N); Fc(&a.tPEFF0, N);
+    Fc(&a.tHOJM, np); Fc(&a.tROVT1, np); Fc(&a.tP1, np);
+    Fc(&a.tVX, N); Fc(&a.tVR, N); Fc(&a.tVT, N); Fc(&a.tROVT, N); Fc(&a.tP, N); Fc(&a.tHO, N); Fc(&a.tPEFF, N);
+    Fc(&a.tFLOWX, N); Fc(&a.tFLOWT, N); Fc(&a.tFLOWR, N);
+    Fc(&a.tBCBUF, (size_t)4 * d.KM); Fc(&a.tROIN, np);
+    Fc(&a.tMIX, (size_t)(d.NRWSM1 > 0 ? d.NRWSM1 : 1) * d.KM * mix_rec_size(d.IM));
+    F(&a.gAQX, N); F(&a.gAQR, N); F(&a.gABX, N); F(&a.gABR, N); F(&a.gASX, N); F(&a.gASR, N); F(&a.gVOLOR, N);
+    F(&a.gABT, (size_t)d.JM * d.KM);
+    if (!rc) rc = aalloc(s, &s->tctl, 1);
+    if (!rc) rc = aalloc(s, &s->flag, 1);
+    const int per = 5 * d.IM * d.KM + d.IMM1 * d.KMM1;
+    F(&s->seed, (size_t)2 * per);
+    F(&s->prev, 5 * N);
+    if (!rc) rc = aalloc(s, &s->norms, 2);
+    a.tctl = s->tctl;
+    a.flag = s->flag;
+    a.seed = s->seed;
+    return rc;
+}
+
+// the adjoint arrays by name: the state adjoints (COMMON names) and PD
+float *state_adj(AdjState *s, const Dev &d, const char *name, size_t *count) {
+    const size_t N = (size_t)d.IM * d.JM * d.KM;
+    Adj &a = s->a;
+    struct {
+        const char *n;
+        float *p;
+    } t[] = {{"RO", a.v[V_RO].D},        {"ROE", a.v[V_ROE].D},     {"ROVX", a.v[V_ROVX].D},
+             {"RORVT", a.v[V_RORVT].D},  {"ROVR", a.v[V_ROVR].D},   {"DRO", a.v[V_RO].DIFF},
+             {"DROE", a.v[V_ROE].DIFF},  {"DROVX", a.v[V_ROVX].DIFF}, {"DRORVT", a.v[V_RORVT].DIFF},
+             {"DROVR", a.v[V_ROVR].DIFF}, {"P", a.P}, {"HO", a.HO}, {"ROVT", a.ROVT}, {"PEFF", a.PEFF},
+             {"VX", a.VX}, {"VR", a.VR}, {"VT", a.VT}};
+    for (auto &e : t)
+        if (!strcmp(name, e.n)) {
+            *count = N;
+            return e.p;
+        }
+    if (!strcmp(name, "PD")) {
+        *count = (size_t)d.KM;
+        return a.PD;
+    }
+    return nullptr;
+}
+
+float *geom_adj(AdjState *s, const Dev &d, const char *name, size_t *count) {
+    const size_t N = (size_t)d.IM * d.JM * d.KM;
+    Adj &a = s->a;
+    struct {
+        const char *n;
+        float *p;
+    } t[] = {{"AQX", a.gAQX}, {"AQR", a.gAQR}, {"ABX", a.gABX}, {"ABR", a.gABR},
+             {"ASX", a.gASX}, {"ASR", a.gASR}, {"VOLOR", a.gVOLOR}};
+    for (auto &e : t)
+        if (!strcmp(name, e.n)) {
+            *count = N;
+            return e.p;
+        }
+    if (!strcmp(name, "ABT")) {
+        *count = (size_t)d.JM * d.KM;
+        return a.gABT;
+    }
+    return nullptr;
+}
+
+int zero_adjoints(AdjState *s, const Dev &d, cudaStream_t st) {
+    const size_t N = (size_t)d.IM * d.JM * d.KM;
+    Adj &a = s->a;
+    for (int v = 0; v < NVAR; ++v) {
+        AdjVar &V = a.v[v];
+        float *z[] = {V.D, V.DIFF, V.SR, V.ST, V.TM, V.Y, V.XF, V.TF, V.RF};
+        for (float *p : z)
+            if (p) ACK(cudaMemsetAsync(p, 0, N * sizeof(float), st));
+    }
+    float *z[] = {a.P, a.HO, a.VX, a.VR, a.VT, a.ROVT, a.PEFF, a.FLOWX, a.FLOWT, a.FLOWR};
+    for (float *p : z) ACK(cudaMemsetAsync(p, 0, N * sizeof(float), st));
+    float *zk[] = {a.PD, a.PDK, a.PAVG, a.SSUM};
+    for (float *p : zk) ACK(cudaMemsetAsync(p, 0, (size_t)d.KM * sizeof(float), st));
+    return 0;
+}
+
+}  // namespace
+}  // namespace mgpu
+
+using namespace mgpu;
+
+extern "C" {
+
+int32_t mgpu_adjoint_prepare(mgpu_handle *h) {
+    HandleView hv = handle_view(h);
+    if (!h || !hv.committed) return api_fail(MGPU_E_STATE, "adjoint before commit");
+    Dev &dh = handle_dev(h);
+    int rc = unsupported(dh);
+    if (rc) return rc;
+    AdjState *&s = handle_adj(h);
+    if (!s) {
+        s = new AdjState();
+        s->h = h;
+        if ((rc = allocate(s, dh)) || (rc = configure(dh))) {
+            adj_destroy(s);
+            s = nullptr;
+            return rc;
+        }
+    }
+    const Dev &d = dh;
+    cudaStream_t st = hv.stream;
+    const size_t N = (size_t)d.IM * d.JM * d.KM, np = (size_t)d.IM * d.KM;
+    const size_t fb = N * sizeof(float);
+    Adj &a = s->a;
+    // the state before the recorded step
+    auto cp = [&](const float *dst, const float *src, size_t n) {
+        return cudaMemcpyAsync((void *)dst, src, n * sizeof(float), cudaMemcpyDeviceToDevice, st);
+    };
+    ACK(cp(a.tRO, d.RO, N)); ACK(cp(a.tROVX, d.ROVX, N)); ACK(cp(a.tROVR, d.ROVR, N));
+    ACK(cp(a.tRORVT, d.RORVT, N)); ACK(cp(a.tROE, d.ROE, N)); ACK(cp(a.tPEFF0, d.PEFF, N));
+    ACK(cudaMemcpy2DAsync((void *)a.tHOJM, (size_t)d.IM * 4, d.HO + (size_t)d.IM * (d.JM - 1), (size_t)d.IM * d.JM * 4,
+                          (size_t)d.IM * 4, d.KM, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpy2DAsync((void *)a.tROVT1, (size_t)d.IM * 4, d.ROVT, (size_t)d.IM * d.JM * 4, (size_t)d.IM * 4, d.KM,
+                          cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpy2DAsync((void *)a.tP1, (size_t)d.IM * 4, d.P, (size_t)d.IM * d.JM * 4, (size_t)d.IM * 4, d.KM,
+                          cudaMemcpyDeviceToDevice, st));
+    // everything else the step changes, restored afterwards
+    float *const keep[] = {d.DRO, d.DROE, d.DROVX, d.DROVR, d.DRORVT, d.P, d.HO, d.T_STATIC, d.VX, d.VR, d.VT,
+                           d.WT, d.ROWT, d.ROVT};
+    const int nkeep = (int)(sizeof(keep) / sizeof(keep[0]));
+    float *save = nullptr, *savepd = nullptr;
+    DevCtl *savectl = nullptr;
+    ACK(cudaMallocAsync((void **)&save, nkeep * fb, st));
+    ACK(cudaMallocAsync((void **)&savepd, (size_t)d.KM * 4, st));
+    ACK(cudaMallocAsync((void **)&savectl, sizeof(DevCtl), st));
+    for (int q = 0; q < nkeep; ++q) ACK(cudaMemcpyAsync(save + (size_t)q * N, keep[q], fb, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(savepd, d.PD, (size_t)d.KM * 4, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(savectl, d.ctl, sizeof(DevCtl), cudaMemcpyDeviceToDevice, st));
+    // the recorded step: LOSS and STEPUP held
+    Dev rec = d;
+    rec.use_cond = 0;
+    rec.FROZEN = 1;
+    rec.ADJ_ROIN = const_cast<float *>(a.tROIN);
+    rec.ADJ_MIX = const_cast<float *>(a.tMIX);
+    rec.ADJ_FLAG = s->flag;
+    ACK(cudaMemsetAsync(s->flag, 0, sizeof(int), st));
+    Launch L{st, handle_sm_count(h)};
+    launch_step_begin(rec, L);
+    launch_prim(rec, L);
+    enqueue_step_core(rec, L);
+    ACK(cudaGetLastError());
+    ACK(cp(a.tVX, d.VX, N)); ACK(cp(a.tVR, d.VR, N)); ACK(cp(a.tVT, d.VT, N)); ACK(cp(a.tROVT, d.ROVT, N));
+    ACK(cp(a.tP, d.P, N)); ACK(cp(a.tHO, d.HO, N)); ACK(cp(a.tPEFF, d.PEFF, N));
+    ACK(cp(a.tFLOWX, d.FLOWX, N)); ACK(cp(a.tFLOWT, d.FLOWT, N)); ACK(cp(a.tFLOWR, d.FLOWR, N));
+    for (int v = 0; v < NVAR; ++v) ACK(cp(a.v[v].tST, d.var[v].ST, N));
+    ACK(cp(a.tBCBUF, d.BCBUF, (size_t)4 * d.KM));
+    ACK(cudaMemcpyAsync(s->tctl, d.ctl, sizeof(DevCtl), cudaMemcpyDeviceToDevice, st));
+    // the EFICOOL sums of the step's arrays (the objectives' forward values)
+    double *dint = handle_int_buf(h);
+    launch_integrals(rec, L, dint);
+    rk_blk<<<NVAR, RT_BS, 0, st>>>(d, a);
+    ACK(cudaGetLastError());
+    s->sums.assign((size_t)4 * d.JM, 0.0);
+    ACK(cudaMemcpyAsync(s->sums.data(), dint, s->sums.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    // restore the state
+    ACK(cudaMemcpyAsync(d.RO, a.tRO, fb, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(d.ROVX, a.tROVX, fb, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(d.ROVR, a.tROVR, fb, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(d.RORVT, a.tRORVT, fb, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(d.ROE, a.tROE, fb, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(d.PEFF, a.tPEFF0, fb, cudaMemcpyDeviceToDevice, st));
+    for (int q = 0; q < nkeep; ++q) ACK(cudaMemcpyAsync(keep[q], save + (size_t)q * N, fb, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(d.PD, savepd, (size_t)d.KM * 4, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(d.ctl, savectl, sizeof(DevCtl), cudaMemcpyDeviceToDevice, st));
+    ACK(cudaFreeAsync(save, st));
+    ACK(cudaFreeAsync(savepd, st));
+    ACK(cudaFreeAsync(savectl, st));
+    int flag = 0;
+    ACK(cudaMemcpyAsync(&flag, s->flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ACK(cudaStreamSynchronize(st));
+    (void)np;
+    if (flag & 3) return api_fail(MGPU_E_UNSUPPORTED, "adjoint: a density or Mach limiter is active at the linearisation state");
+    ACK(cudaMemsetAsync(s->flag, 0, sizeof(int), st));
+    if ((rc = zero_adjoints(s, d, st))) return rc;
+    ACK(cudaMemsetAsync(s->seed, 0, (size_t)2 * (5 * d.IM * d.KM + d.IMM1 * d.KMM1) * sizeof(float), st));
+    s->a.seed_j[0] = 1;
+    s->a.seed_j[1] = 2;
+    s->objective = -1;
+    s->value = 0.0;
+    s->iters = 0;
+    // the reverse step as a CUDA graph
+    if (s->gexec) {
+        cudaGraphExecDestroy(s->gexec);
+        s->gexec = nullptr;
+    }
+    if (s->graph) {
+        cudaGraphDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    ACK(cudaStreamSynchronize(st));
+    s->ready = true;
+    return 0;
+}
+
+namespace {
+int ensure_graph(AdjState *s, const Dev &d, cudaStream_t st) {
+    if (s->gexec) return 0;
+    ACK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    enqueue_reverse(d, s->a, st);
+    cudaGraph_t g = nullptr;
+    ACK(cudaStreamEndCapture(st, &g));
+    s->graph = g;
+    ACK(cudaGraphInstantiate(&s->gexec, g, 0));
+    return 0;
+}
+AdjState *ready_state(mgpu_handle *h) {
+    if (!h) return nullptr;
+    AdjState *s = handle_adj(h);
+    return (s && s->ready) ? s : nullptr;
+}
+}  // namespace
+
+int32_t mgpu_adjoint_objective(mgpu_handle *h, int32_t which, double *value) {
+    AdjState *s = ready_state(h);
+    if (!s) return api_fail(MGPU_E_STATE, "adjoint objective before mgpu_adjoint_prepare");
+    if (which < -1 || which > 2) return api_fail(MGPU_E_ARG, "objective: -1 none, 0 eta_tt, 1 mass flow in, 2 mass flow out");
+    const Dev &d = handle_dev(h);
+    cudaStream_t st = handle_view(h).stream;
+    const int per = 5 * d.IM * d.KM + d.IMM1 * d.KMM1;
+    ACK(cudaMemsetAsync(s->seed, 0, (size_t)2 * per * sizeof(float), st));
+    const int J1 = d.NSTAGES == 1 ? 1 : 2, J2M1 = d.JM - 1;
+    s->a.seed_j[0] = J1;
+    s->a.seed_j[1] = J2M1;
+    const std::vector<double> &v = s->sums;
+    auto bf = [&](int j) { return v[(size_t)(j - 1)]; };
+    auto spo = [&](int j) { return v[(size_t)d.JM + j - 1] / bf(j); };
+    auto sto = [&](int j) { return v[(size_t)2 * d.JM + j - 1] / bf(j); };
+    double J = 0.0, g[2][3] = {{0, 0, 0}, {0, 0, 0}};   // per plane: dJ/dspo, dJ/dsto, dJ/dbf
+    if (which == 1) {
+        J = bf(J1);
+        g[0][2] = 1.0;
+    } else if (which == 2) {
+        J = bf(J2M1);
+        g[1][2] = 1.0;
+    } else if (which == 0) {
+        const double FGA = (double)d.FGA;
+        const double p1 = spo(J1), p2 = spo(J2M1), s1 = sto(J1), s2 = sto(J2M1);
+        const double P = p2 / p1, D = s2 - s1, pf = std::pow(P, FGA), Dis = s1 * (pf - 1.0);
+        const double dPf_dp2 = FGA * std::pow(P, FGA - 1.0) / p1, dPf_dp1 = -FGA * std::pow(P, FGA - 1.0) * p2 / (p1 * p1);
+        if (D < 0.0) {          // turbine: eta = D / Dis
+            J = D / Dis;
+            g[1][1] = 1.0 / Dis;
+            g[0][1] = -1.0 / Dis - D * (pf - 1.0) / (Dis * Dis);
+            g[1][0] = -D / (Dis * Dis) * s1 * dPf_dp2;
+            g[0][0] = -D / (Dis * Dis) * s1 * dPf_dp1;
+        } else if (D > 0.0) {   // compressor: eta = Dis / D
+            J = Dis / D;
+            g[1][1] = -Dis / (D * D);
+            g[0][1] = (pf - 1.0) / D + Dis / (D * D);
+            g[1][0] = s1 * dPf_dp2 / D;
+            g[0][0] = s1 * dPf_dp1 / D;
+        } else {
+            J = 1.0;
+        }
+    }
+    if (which >= 0) {
+        const int js[2] = {J1, J2M1};
+        for (int p = 0; p < 2; ++p) {
+            const int j = js[p];
+            rk_seed_plane<<<gridn((size_t)per, 256), 256, 0, st>>>(d, s->a, s->seed + (size_t)p * per, j, g[p][0], g[p][1],
+                                                                  g[p][2], spo(j), sto(j), bf(j));
+        }
+        ACK(cudaGetLastError());
+    }
+    // the seeds are kernel parameters of the captured graph (seed_j)
+    if (s->gexec) {
+        cudaGraphExecDestroy(s->gexec);
+        s->gexec = nullptr;
+        cudaGraphDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    ACK(cudaStreamSynchronize(st));
+    s->objective = which;
+    s->value = J;
+    if (value) *value = J;
+    return 0;
+}
+
+int32_t mgpu_adjoint_iterate(mgpu_handle *h, int32_t n, double *rel_change) {
+    AdjState *s = ready_state(h);
+    if (!s) return api_fail(MGPU_E_STATE, "adjoint iteration before mgpu_adjoint_prepare");
+    if (n < 1) return api_fail(MGPU_E_ARG, "adjoint iteration count must be positive");
+    const Dev &d = handle_dev(h);
+    cudaStream_t st = handle_view(h).stream;
+    int rc = ensure_graph(s, d, st);
+    if (rc) return rc;
+    const size_t N = (size_t)d.IM * d.JM * d.KM;
+    for (int it = 0; it < n; ++it) {
+        if (it == n - 1 && rel_change) {
+            for (int v = 0; v < NVAR; ++v)
+                ACK(cudaMemcpyAsync(s->prev + (size_t)v * N, s->a.v[v].D, N * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        }
+        ACK(cudaGraphLaunch(s->gexec, st));
+    }
+    s->iters += n;
+    int flag = 0;
+    ACK(cudaMemcpyAsync(&flag, s->flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (rel_change) {
+        ACK(cudaMemsetAsync(s->norms, 0, 2 * sizeof(double), st));
+        rk_norms<<<4 * handle_sm_count(h), RT_BS, 0, st>>>(d, s->a, s->prev, s->norms);
+        double nm[2];
+        ACK(cudaMemcpyAsync(nm, s->norms, sizeof(nm), cudaMemcpyDeviceToHost, st));
+        ACK(cudaStreamSynchronize(st));
+        *rel_change = nm[0] > 0.0 ? std::sqrt(nm[1] / nm[0]) : 0.0;
+    } else {
+        ACK(cudaStreamSynchronize(st));
+    }
+    if (flag & 1) return api_fail(MGPU_E_UNSUPPORTED, "adjoint: supersonic relative flow at a mixing plane (Prandtl-Meyer sweep) is not differentiated");
+    return 0;
+}
+
+int32_t mgpu_adjoint_solve(mgpu_handle *h, int32_t max_iters, double tol, int32_t *iters, double *rel_change) {
+    AdjState *s = ready_state(h);
+    if (!s) return api_fail(MGPU_E_STATE, "adjoint solve before mgpu_adjoint_prepare");
+    if (max_iters < 1 || !(tol > 0.0)) return api_fail(MGPU_E_ARG, "adjoint solve: max_iters >= 1, tol > 0");
+    int done = 0;
+    double rel = 1.0;
+    const int chunk = 50;
+    int rc = 0;
+    while (done < max_iters) {
+        const int n = max_iters - done < chunk ? max_iters - done : chunk;
+        if ((rc = mgpu_adjoint_iterate(h, n, &rel))) break;
+        done += n;
+        if (rel < tol) break;
+    }
+    if (iters) *iters = done;
+    if (rel_change) *rel_change = rel;
+    if (rc) return rc;
+    return rel < tol ? 0 : 1;
+}
+
+int32_t mgpu_adjoint_gradient(mgpu_handle *h) {
+    AdjState *s = ready_state(h);
+    if (!s) return api_fail(MGPU_E_STATE, "adjoint gradient before mgpu_adjoint_prepare");
+    const Dev &d = handle_dev(h);
+    cudaStream_t st = handle_view(h).stream;
+    const size_t N = (size_t)d.IM * d.JM * d.KM;
+    Adj &a = s->a;
+    float *g[] = {a.gAQX, a.gAQR, a.gABX, a.gABR, a.gASX, a.gASR, a.gVOLOR};
+    for (float *p : g) ACK(cudaMemsetAsync(p, 0, N * sizeof(float), st));
+    ACK(cudaMemsetAsync(a.gABT, 0, (size_t)d.JM * d.KM * sizeof(float), st));
+    Adj ag = a;
+    ag.geom = 1;
+    enqueue_reverse(d, ag, st);
+    ACK(cudaGetLastError());
+    ACK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int32_t mgpu_adjoint_get(mgpu_handle *h, const char *name, float *out, int64_t nbytes) {
+    AdjState *s = ready_state(h);
+    if (!s || !name || !out) return api_fail(MGPU_E_STATE, "adjoint get before mgpu_adjoint_prepare");
+    const Dev &d = handle_dev(h);
+    size_t cnt = 0;
+    float *p = state_adj(s, d, name, &cnt);
+    if (!p && !strncmp(name, "d", 1)) p = geom_adj(s, d, name + 1, &cnt);
+    if (!p) return api_fail(MGPU_E_ARG, (std::string("unknown adjoint array ") + name).c_str());
+    if ((int64_t)(cnt * sizeof(float)) != nbytes) return api_fail(MGPU_E_ARG, "adjoint array size mismatch");
+    cudaStream_t st = handle_view(h).stream;
+    ACK(cudaMemcpyAsync(out, p, cnt * sizeof(float), cudaMemcpyDeviceToHost, st));
+    ACK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int32_t mgpu_adjoint_set(mgpu_handle *h, const char *name, const float *in, int64_t nbytes) {
+    AdjState *s = ready_state(h);
+    if (!s || !name || !in) return api_fail(MGPU_E_STATE, "adjoint set before mgpu_adjoint_prepare");
+    const Dev &d = handle_dev(h);
+    size_t cnt = 0;
+    float *p = state_adj(s, d, name, &cnt);
+    if (!p) return api_fail(MGPU_E_ARG, (std::string("unknown adjoint state array ") + name).c_str());
+    if ((int64_t)(cnt * sizeof(float)) != nbytes) return api_fail(MGPU_E_ARG, "adjoint array size mismatch");
+    cudaStream_t st = handle_view(h).stream;
+    ACK(cudaMemcpyAsync(p, in, cnt * sizeof(float), cudaMemcpyHostToDevice, st));
+    ACK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+}  // extern "C"

@@ -74,6 +74,7 @@ struct mgpu_handle {
     void *flush_buf = nullptr;   // > L2, rewritten between timed iterations
     size_t flush_bytes = 0;
     DevCtl *h_ctl = nullptr;     // pinned mirror of the control block
+    AdjState *adj = nullptr;     // discrete adjoint, after mgpu_adjoint_prepare
 };
 
 // A batch: one CUDA graph whose branches are the step graphs of several
@@ -401,6 +402,18 @@ HandleView handle_view(const mgpu_handle *h) { return HandleView{&h->d, h->strea
 
 int api_fail(int code, const char *msg) { return fail(code, msg); }
 
+void enqueue_step_core(const Dev &d, Launch L) { enqueue_core(d, L); }
+AdjState *&handle_adj(mgpu_handle *h) { return h->adj; }
+Dev &handle_dev(mgpu_handle *h) { return h->d; }
+int handle_sm_count(const mgpu_handle *h) { return h->sm_count; }
+double *handle_int_buf(mgpu_handle *h) { return h->d_int; }
+const void *handle_array(const mgpu_handle *h, const char *name, size_t *bytes) {
+    int a = find_array(name);
+    if (a < 0 || !h->dptr[a]) return nullptr;
+    if (bytes) *bytes = h->dbytes[a];
+    return h->dptr[a];
+}
+
 }  // namespace mgpu
 
 extern "C" {
@@ -524,6 +537,7 @@ int32_t mgpu_create(int32_t im, int32_t jm, int32_t km, int32_t nrows, mgpu_hand
 void mgpu_destroy(mgpu_handle *h) {
     if (!h) return;
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->adj) adj_destroy(h->adj);
     if (h->flush_buf) cudaFree(h->flush_buf);
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     if (h->graph) cudaGraphDestroy(h->graph);

@@ -53,7 +53,7 @@ __global__ void k_step_begin(Dev d) {
         c->FMIXUP = FM * FM;
     }
     c->do_tail = (n % 5 == 0) || ifend == 1;
-    c->do_loss = (d.ILOS == 10) && (n % d.NLOS == 0);
+    c->do_loss = (d.ILOS == 10) && (n % d.NLOS == 0) && !d.FROZEN;
     c->damp_on = !(c->DAMP < 2.0f || c->DAMP > 100.0f);
     if (d.use_cond) {
         cudaGraphSetConditional((cudaGraphConditionalHandle)d.cond_loss, c->do_loss ? 1u : 0u);
@@ -372,6 +372,7 @@ __global__ void k_bc_apply(Dev d) {
     // inlet, isentropic from the stagnation state
     float RO_STAG = PO1 / d.RGAS / TO1;
     float RO_IN = A3(d.RO, i, 1, k);
+    if (d.ADJ_ROIN) d.ADJ_ROIN[t] = RO_IN;
     if (RO_IN > 0.9999f * RO_STAG) RO_IN = 0.9999f * RO_STAG;
     float PNEW = PO1 * powf(RO_IN / RO_STAG, d.GA);
     float p1 = A3(d.P, i, 1, k);
@@ -799,7 +800,10 @@ __global__ void k_density_fix(Dev d) {
             if (ro < 0.6f * ROAVG) ro = 0.5f * (ro + 0.6f * ROAVG);
             if (ro > 1.5f * ROAVG) ro = 0.5f * (ro + 1.5f * ROAVG);
             if (ro < ROLIM) ro = 0.5f * (ro + ROLIM);
-            if (ro != r0) A3(RO, i, j, k) = ro;
+            if (ro != r0) {
+                A3(RO, i, j, k) = ro;
+                if (d.ADJ_FLAG) atomicOr(d.ADJ_FLAG, 1);
+            }
             rm2 = rm1;
             rm1 = ro;
             r0 = rp1;
@@ -840,12 +844,14 @@ __global__ void k_mach_limiter(Dev d) {
     if (ro < RO_LIMIT) {
         ro = RO_LIMIT;
         d.RO[n] = ro;
+        if (d.ADJ_FLAG) atomicOr(d.ADJ_FLAG, 2);
     }
     float vx = d.VX[n], vr = d.VR[n], wt = d.WT[n];
     float WRELSQ = vx * vx + vr * vr + wt * wt;
     float WREL = sqrtf(WRELSQ);
     float FACSAFE = V_LIMIT / WREL;
     if (FACSAFE < 1.0f) {
+        if (d.ADJ_FLAG) atomicOr(d.ADJ_FLAG, 2);
         d.ROVX[n] = ro * vx * FACSAFE;
         d.ROVR[n] = ro * vr * FACSAFE;
         float ROVTREL = ro * wt * FACSAFE;
@@ -918,6 +924,23 @@ __global__ void __launch_bounds__(MIX_BS) k_mixplan(Dev d) {
     const float RJP2 = A2(d.R, JP2, k), UNOWJP2 = A2(d.UBLADE, JP2, k);
     const float RJP3 = A2(d.R, JP3, k), UNOWJP3 = A2(d.UBLADE, JP3, k);
     int nmach = 0;
+    if (d.ADJ_MIX) {
+        float *rec = d.ADJ_MIX + (size_t)blockIdx.x * mix_rec_size(IM);
+        if (threadIdx.x == 0) {
+            rec[0] = ROMIX;
+            rec[1] = A3(d.ROVX, d.IMID, JP1, k);
+            rec[2] = A3(d.ROVR, d.IMID, JP1, k);
+            rec[3] = A3(d.RORVT, d.IMID, JP1, k);
+            rec[4] = ROEMIX;
+        }
+        for (int i = threadIdx.x + 1; i <= IM; i += MIX_BS) {
+            float *q = rec + 5 + 10 * (i - 1);
+            q[0] = A3(d.RO, i, JP2, k); q[1] = A3(d.ROVX, i, JP2, k); q[2] = A3(d.ROVR, i, JP2, k);
+            q[3] = A3(d.RORVT, i, JP2, k); q[4] = A3(d.ROE, i, JP2, k);
+            q[5] = A3(d.RO, i, JP3, k); q[6] = A3(d.ROVX, i, JP3, k); q[7] = A3(d.ROVR, i, JP3, k);
+            q[8] = A3(d.RORVT, i, JP3, k); q[9] = A3(d.ROE, i, JP3, k);
+        }
+    }
     for (int i = threadIdx.x + 1; i <= IM; i += MIX_BS) {
         float ROJP2 = A3(d.RO, i, JP2, k);
         float XVELJP2 = A3(d.ROVX, i, JP2, k) / ROJP2;

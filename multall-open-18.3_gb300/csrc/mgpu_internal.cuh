@@ -106,6 +106,12 @@ struct Dev {
     int *DFLAG;                        // (IM*KM) density-limiter column flags
     float *BCBUF;                      // (4, KM) PAVG2, PAVG3, PAVGOUT, and the PD each K's exit update uses
     float *FLOWJ;                      // (JM) SETFLO's FLOW(J)
+    // recording hooks of the adjoint's linearisation step (null otherwise):
+    // RO(I,1,K) as the inlet condition reads it, the mixing-plane inputs of
+    // each (row interface, K), and bit flags for a limiter that changed a value
+    float *ADJ_ROIN;
+    float *ADJ_MIX;
+    int *ADJ_FLAG;
     double *BLADE_FLOW;                // (JM)
     // per-block reduction partials of the 5-step tail
     double *part_sum;
@@ -235,6 +241,14 @@ cudaError_t configure_kernels(const Dev &d);
 cudaError_t configure_loss_kernels(const Dev &d);
 cudaError_t configure_flux_kernels(const Dev &d);
 
+// one LOOP iteration without the LOSS and tail bodies, eager launches on
+// L.s (mgpu_api.cu)
+void enqueue_step_core(const Dev &d, Launch L);
+
+// floats recorded per (row interface, K) by k_mixplan for the adjoint: the
+// five conserved variables at (IMID, JP1), then per I those at JP2 and JP3
+__host__ __device__ inline int mix_rec_size(int im) { return 5 + 10 * im; }
+
 // Read-only view of a handle, for entry points defined outside mgpu_api.cu.
 struct HandleView {
     const Dev *d;
@@ -243,6 +257,14 @@ struct HandleView {
     bool committed;
 };
 HandleView handle_view(const mgpu_handle *h);
+// The discrete adjoint (mgpu_adjoint.cu) keeps its state beside the handle.
+struct AdjState;
+void adj_destroy(AdjState *a);
+AdjState *&handle_adj(mgpu_handle *h);
+Dev &handle_dev(mgpu_handle *h);
+int handle_sm_count(const mgpu_handle *h);
+double *handle_int_buf(mgpu_handle *h);        // (4, JM) FP64 integrals scratch
+const void *handle_array(const mgpu_handle *h, const char *name, size_t *bytes);
 // Records msg for mgpu_last_error() and returns code.
 int api_fail(int code, const char *msg);
 

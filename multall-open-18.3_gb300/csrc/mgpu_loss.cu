@@ -914,7 +914,7 @@ void launch_tail(const Dev &d, Launch L) {
 // ---------------------------------------------------------------------
 __global__ void k_stepup_node(Dev d, int gated) {
     pdl_wait();
-    if (gated && !d.ctl->do_tail) return;
+    if (gated && (!d.ctl->do_tail || d.FROZEN)) return;
     size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t N = (size_t)d.IM * d.JM * d.KM;
     if (n >= N) return;
@@ -949,7 +949,7 @@ __device__ inline float stepup_cell(const Dev &d, int i, int j, int k, float REL
 
 __global__ void k_stepup_cell(Dev d, float RELAX, int gated) {
     pdl_wait();
-    if (gated && !d.ctl->do_tail) return;
+    if (gated && (!d.ctl->do_tail || d.FROZEN)) return;
     size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t N = (size_t)d.IM * d.JM * d.KM;
     if (n >= N) return;
@@ -971,7 +971,7 @@ __global__ void k_stepup_cell(Dev d, float RELAX, int gated) {
 
 __global__ void k_stepup_store(Dev d, int gated) {
     pdl_wait();
-    if (gated && !d.ctl->do_tail) return;
+    if (gated && (!d.ctl->do_tail || d.FROZEN)) return;
     size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t N = (size_t)d.IM * d.JM * d.KM;
     if (n >= N) return;

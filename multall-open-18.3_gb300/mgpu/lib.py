@@ -43,7 +43,9 @@ EXPORTS = ["mgpu_abi_version", "mgpu_last_error", "mgpu_device_count", "mgpu_cre
            "mgpu_commit", "mgpu_stepup", "mgpu_loss_init", "mgpu_step", "mgpu_run", "mgpu_sync",
            "mgpu_integrals_compute", "mgpu_kernels_per_step", "mgpu_bench_steps", "mgpu_profile_steps",
            "mgpu_step_io_bytes", "mgpu_integrals_noalloc", "mgpu_batch_create", "mgpu_batch_destroy",
-           "mgpu_batch_run", "mgpu_batch_bench_steps"]
+           "mgpu_batch_run", "mgpu_batch_bench_steps", "mgpu_adjoint_prepare", "mgpu_adjoint_objective",
+           "mgpu_adjoint_iterate", "mgpu_adjoint_solve", "mgpu_adjoint_gradient", "mgpu_adjoint_get",
+           "mgpu_adjoint_set"]
 
 _lib = None
 
@@ -86,6 +88,14 @@ def load(build: bool = True):
     L.mgpu_batch_destroy.argtypes = [vp]
     L.mgpu_batch_run.argtypes = [vp, i32, ctypes.POINTER(Monitors)]
     L.mgpu_batch_bench_steps.argtypes = [vp, i32, i32, ctypes.POINTER(ctypes.c_double)]
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.mgpu_adjoint_prepare.argtypes = [vp]
+    L.mgpu_adjoint_objective.argtypes = [vp, i32, dp]
+    L.mgpu_adjoint_iterate.argtypes = [vp, i32, dp]
+    L.mgpu_adjoint_solve.argtypes = [vp, i32, ctypes.c_double, ctypes.POINTER(i32), dp]
+    L.mgpu_adjoint_gradient.argtypes = [vp]
+    L.mgpu_adjoint_get.argtypes = [vp, cp, vp, ctypes.c_int64]
+    L.mgpu_adjoint_set.argtypes = [vp, cp, vp, ctypes.c_int64]
     for f in EXPORTS:
         fn = getattr(L, f)
         if f in ("mgpu_destroy", "mgpu_batch_destroy"):
@@ -221,6 +231,52 @@ class Problem:
         n = ctypes.c_int32()
         _chk(load().mgpu_profile_steps(self.h, int(nsteps), arr, 256, ctypes.byref(n)))
         return [(arr[i].name.decode(), arr[i].launches, arr[i].total_ms) for i in range(n.value)]
+
+
+    # ---- discrete adjoint ---------------------------------------------------
+    ADJ_STATE = ["RO", "ROVX", "ROVR", "RORVT", "ROE", "DRO", "DROE", "DROVX", "DROVR", "DRORVT",
+                 "P", "HO", "ROVT", "PEFF", "PD"]
+    ADJ_GEOM = ["AQX", "AQR", "ABX", "ABR", "ABT", "ASX", "ASR", "VOLOR"]
+    OBJECTIVES = {"none": -1, "eta_tt": 0, "mass_flow_in": 1, "mass_flow_out": 2}
+
+    def adjoint_prepare(self):
+        """Records the linearisation step at the current state."""
+        _chk(load().mgpu_adjoint_prepare(self.h))
+
+    def adjoint_objective(self, which: str) -> float:
+        v = ctypes.c_double()
+        _chk(load().mgpu_adjoint_objective(self.h, self.OBJECTIVES[which], ctypes.byref(v)))
+        return v.value
+
+    def adjoint_iterate(self, n: int = 1) -> float:
+        r = ctypes.c_double()
+        _chk(load().mgpu_adjoint_iterate(self.h, int(n), ctypes.byref(r)))
+        return r.value
+
+    def adjoint_solve(self, max_iters: int, tol: float) -> tuple[bool, int, float]:
+        """(converged, iterations, last relative change)."""
+        it, r = ctypes.c_int32(), ctypes.c_double()
+        rc = _chk(load().mgpu_adjoint_solve(self.h, int(max_iters), float(tol), ctypes.byref(it), ctypes.byref(r)))
+        return rc == 0, it.value, r.value
+
+    def adjoint_gradient(self) -> dict:
+        """dJ/dA for the geometry arrays (one more reverse step)."""
+        _chk(load().mgpu_adjoint_gradient(self.h))
+        return {n: self.adjoint_get("d" + n) for n in self.ADJ_GEOM}
+
+    def _adj_shape(self, name: str):
+        base = name[1:] if name.startswith("d") and name[1:] in self.ADJ_GEOM else name
+        ref = self.cd.arrays.get(base)
+        return ref.shape if ref is not None else (self.cd.km, self.cd.jm, self.cd.im)
+
+    def adjoint_get(self, name: str) -> np.ndarray:
+        out = np.zeros(self._adj_shape(name), np.float32)
+        _chk(load().mgpu_adjoint_get(self.h, name.encode(), out.ctypes.data, out.nbytes))
+        return out
+
+    def adjoint_set(self, name: str, a: np.ndarray):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        _chk(load().mgpu_adjoint_set(self.h, name.encode(), a.ctypes.data, a.nbytes))
 
 
 class Batch:

@@ -39,9 +39,23 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <type_traits>
+#include <utility>
 
 #include "../include/mgpu.h"
 #include "../include/mgpu_common_table.h"
+#include "ad_tape.h"
+
+/* math on the REAL type: the std overloads for float and double, the tape's
+   overloads (found by argument-dependent lookup) for adt::AD */
+namespace om {
+#define OM_FN1(f) template <class T> inline T f(const T &x) { using std::f; return f(x); }
+OM_FN1(sqrt) OM_FN1(fabs) OM_FN1(log) OM_FN1(log10) OM_FN1(sin) OM_FN1(cos) OM_FN1(asin)
+#undef OM_FN1
+template <class T> inline T pow(const T &x, const T &y) { using std::pow; return pow(x, y); }
+template <class T> inline T atan2(const T &y, const T &x) { using std::atan2; return atan2(y, x); }
+template <class T> inline bool isfinite(const T &x) { using std::isfinite; return isfinite(x); }
+}  // namespace om
 
 namespace {
 
@@ -67,6 +81,18 @@ struct OracleBase {
     virtual int loss_init() = 0;
     virtual int step(int force_end, mgpu_monitors *mon) = 0;
     virtual int integrals(mgpu_integrals *out) = 0;
+    /* reverse mode (the adt::AD instantiation only): ad_begin makes every
+       REAL array of the COMMON table an independent variable and starts the
+       tape; after a step, ad_seed adds output adjoints to the arrays' current
+       values, ad_reverse sweeps the tape and ad_grad reads the adjoints of
+       the arrays as they were at ad_begin */
+    virtual int set_array_f64(const char *n, const double *p, int64_t cnt) = 0;
+    virtual int ad_begin() { return fail(MGPU_E_STATE, "not a differentiating oracle"); }
+    virtual int ad_zero() { return fail(MGPU_E_STATE, "not a differentiating oracle"); }
+    virtual int ad_seed(const char *, const double *, int64_t) { return fail(MGPU_E_STATE, "not a differentiating oracle"); }
+    virtual int ad_reverse() { return fail(MGPU_E_STATE, "not a differentiating oracle"); }
+    virtual int ad_grad(const char *, double *, int64_t) { return fail(MGPU_E_STATE, "not a differentiating oracle"); }
+    virtual int64_t ad_tape_size() { return 0; }
 };
 
 template <typename R>
@@ -283,7 +309,6 @@ struct Oracle : OracleBase {
         EMAX = R(1.0E06);
         TCOOL_MIN = R(1.0E6);
         IFEND = 0;
-        NSTEP = 0;
         committed = true;
         return 0;
     }
@@ -309,8 +334,8 @@ struct Oracle : OracleBase {
                     R WTREL = F3(WT, i, j, k);
                     R WSQ = VSQ - (vt * vt - WTREL * WTREL);
                     if (WSQ < VLIM) WSQ = VLIM;
-                    R V_SONIC = std::sqrt(GAMNOW * RGAS * TSTATIC);
-                    R VPLUSC = std::sqrt(WSQ) + V_SONIC;
+                    R V_SONIC = om::sqrt(GAMNOW * RGAS * TSTATIC);
+                    R VPLUSC = om::sqrt(WSQ) + V_SONIC;
                     A3(TEMP1, i, j, k) = VSOUND / VPLUSC;
                 }
         for (int i = 1; i <= IMM1; ++i) {
@@ -613,7 +638,7 @@ struct Oracle : OracleBase {
                 int NSUM = IMM1 * KMM1 * JCHANGE;
                 for (int k = 1; k <= KMM1; ++k)
                     for (int j = JST; j <= JEN; ++j)
-                        for (int i = 1; i <= IMM1; ++i) SUMCHG = SUMCHG + std::fabs(A3(STORE, i, j, k));
+                        for (int i = 1; i <= IMM1; ++i) SUMCHG = SUMCHG + om::fabs(A3(STORE, i, j, k));
                 AVG_CHG[nr - 1] = SUMCHG / R(NSUM);
             }
             if (NROWS == 1) AVG_BLK[0] = AVG_CHG[0];
@@ -632,7 +657,7 @@ struct Oracle : OracleBase {
                     int nr = F1(NROW, j);
                     for (int i = 1; i <= IMM1; ++i) {
                         R DELTA = A3(STORE, i, j, k);
-                        R ABSCHG = std::fabs(DELTA);
+                        R ABSCHG = om::fabs(DELTA);
                         R FDAMP = ABSCHG / AVG_BLK[nr - 1];
                         A3(STORE, i, j, k) = DELTA / (R(1.) + FDAMP / DAMP);
                     }
@@ -753,7 +778,7 @@ struct Oracle : OracleBase {
         R t = R(0.5) * (PDOWN_HUB + PDOWN_TIP);
         t = t / R(NROWS);
         t = t / (F1(CHORD, 1) + F1(CHORD, NROWS));
-        R DPDS_LIM = std::fabs(R(20.0) * (F1(PO1, KMID) - t));
+        R DPDS_LIM = om::fabs(R(20.0) * (F1(PO1, KMID) - t));
         for (int j = 2; j <= JM; ++j)
             for (int k = 1; k <= KMM1; ++k)
                 for (int i = 1; i <= IMM1; ++i) {
@@ -765,9 +790,9 @@ struct Oracle : OracleBase {
                                A[ijk(i + 1, j - 1, k + 1)];
                     };
                     R VXCELL = c8(VX_v), VRCELL = c8(VR_v), WTCELL = c8(WT_v);
-                    R WREL_CELL = std::sqrt(VXCELL * VXCELL + VRCELL * VRCELL + WTCELL * WTCELL);
+                    R WREL_CELL = om::sqrt(VXCELL * VXCELL + VRCELL * VRCELL + WTCELL * WTCELL);
                     R DPDS = (DPDX * VXCELL + DPDR * VRCELL + DPDT * WTCELL) / WREL_CELL;
-                    if (std::fabs(DPDS) > DPDS_LIM) DPDS = DPDS_LIM * DPDS / std::fabs(DPDS);
+                    if (om::fabs(DPDS) > DPDS_LIM) DPDS = DPDS_LIM * DPDS / om::fabs(DPDS);
                     F3(DPDS_CELL, i, j, k) = DPDS;
                 }
         std::vector<R> TEMPP((size_t)JM + 8);
@@ -803,9 +828,9 @@ struct Oracle : OracleBase {
         R SGN_DPDS = R(0), VPRES = R(0), VSTAR_P = R(0), FYPLUSP = R(0);
         const bool pres = !(YPLUSWALL > R(-10.0));
         if (pres) {
-            if (std::fabs(DPDS) < R(1.0)) DPDS = R(1.0);
-            SGN_DPDS = std::fabs(DPDS) / DPDS;
-            VPRES = std::pow(VISLAM / DENSITY / DENSITY * std::fabs(DPDS), R(0.33333));
+            if (om::fabs(DPDS) < R(1.0)) DPDS = R(1.0);
+            SGN_DPDS = om::fabs(DPDS) / DPDS;
+            VPRES = om::pow(VISLAM / DENSITY / DENSITY * om::fabs(DPDS), R(0.33333));
             VSTAR_P = YPLUS_OLD * VISLAM / (DENSITY * PERP);
             if (SGN_DPDS < R(0.0) && VPRES > R(0.33) * VSTAR_P) VPRES = R(0.33) * VSTAR_P;
             if (SGN_DPDS > R(0.0) && VPRES > R(2.0) * VSTAR_P) VPRES = R(2.0) * VSTAR_P;
@@ -816,7 +841,7 @@ struct Oracle : OracleBase {
                 FYPLUSP = R(-15.138) + R(8.4688) * P1 - R(0.81976) * P2 + R(3.7292E-2) * P3 - R(6.3866E-4) * P4;
             if (P1 > R(15.0) && P1 <= R(30.0))
                 FYPLUSP = R(11.925) + R(0.934) * P1 - R(2.7805E-2) * P2 + R(4.6262E-4) * P3 - R(3.1442E-6) * P4;
-            if (P1 > R(30.0)) FYPLUSP = R(5) * std::log(P1) + R(8.0);
+            if (P1 > R(30.0)) FYPLUSP = R(5) * om::log(P1) + R(8.0);
         }
         R YP1 = YPLUS_OLD, YP2 = YP1 * YP1, YP3 = YP2 * YP1, YP4 = YP2 * YP2;
         R FYPLUS = R(0);
@@ -825,7 +850,7 @@ struct Oracle : OracleBase {
             FYPLUS = R(-0.872) + R(1.465) * YP1 - R(7.02E-2) * YP2 + R(1.66E-03) * YP3 - R(1.495E-5) * YP4;
         if (YP1 > R(30) && YP1 <= R(140.0))
             FYPLUS = R(8.6) + R(0.1864) * YP1 - R(2.006E-3) * YP2 + R(1.144E-5) * YP3 - R(2.551E-8) * YP4;
-        if (YP1 > R(140.0)) FYPLUS = R(2.439) * std::log(YP1) + R(5.0);
+        if (YP1 > R(140.0)) FYPLUS = R(2.439) * om::log(YP1) + R(5.0);
         R FRACP = pres ? SGN_DPDS * (VPRES / VSTAR_P) * FYPLUSP / FYPLUS : R(0.0);
         R VPLUS = FYPLUS * (R(1.0) + FRACP);
         R VSTAR = WREL_WALL / VPLUS;
@@ -837,7 +862,7 @@ struct Oracle : OracleBase {
      * re/relog/rough as in the reference; returns TWALL for the given
      * density and wall-relative speed used in the final expression. */
     R skin_friction(R RE, R PERP, R ROUGH_IN, R dens, R wb) {
-        R RELOG = R(1.0) / std::log(RE);
+        R RELOG = R(1.0) / om::log(RE);
         R ROUGH = ROUGH_IN;
         R CF;
         if (ROUGH > R(1.0E-7)) {
@@ -858,9 +883,9 @@ struct Oracle : OracleBase {
         if (RE < R(125.)) CF = CFLAM;
         if (ROUGH > R(1.0E-7)) {
             R TW = R(0.5) * CF * dens * wb * wb;
-            R VSTAR = std::sqrt(TW / dens);
+            R VSTAR = om::sqrt(TW / dens);
             R PLUSK = ROUGH * VSTAR * dens / VISLAM;
-            R RELOG10 = std::log10(PERP / ROUGH);
+            R RELOG10 = om::log10(PERP / ROUGH);
             R FUNCN = R(5.75) * RELOG10 + R(8.5);
             R CF_FULL_ROUGH = R(2.0) / (FUNCN * FUNCN);
             if (PLUSK > R(45) && CF > CF_FULL_ROUGH) CF = CF_FULL_ROUGH;
@@ -890,7 +915,7 @@ struct Oracle : OracleBase {
                 if (F1(JTE, 1) > JM) J2 = JM;
                 R XCHORD = F2(SMERID, J2, KMID) - F2(SMERID, J1, KMID);
                 R a = F3(ROVX, IMID, J2, KMID), b = F3(ROVR, IMID, J2, KMID), c = F3(ROWT, IMID, J2, KMID);
-                R ROW2 = std::sqrt(a * a + b * b + c * c);
+                R ROW2 = om::sqrt(a * a + b * b + c * c);
                 VISLAM = XCHORD * ROW2 / REYNO;
             }
             if (REYNO > R(0.0) && REYNO < R(99.99)) VISLAM = REYNO / R(100000.);
@@ -917,7 +942,7 @@ struct Oracle : OracleBase {
             for (int i = 1; i <= IMM1; ++i) {
                 for (int k = 1; k <= KM; ++k) {
                     R asx = F3(ASX, i, j, k), asr = F3(ASR, i, j, k);
-                    AREA[k] = std::sqrt(asx * asx + asr * asr);
+                    AREA[k] = om::sqrt(asx * asx + asr * asr);
                     VXAVG[k] = R(0.25) * (F3(VX, i, j, k) + F3(VX, i, j - 1, k) + F3(VX, i + 1, j, k) + F3(VX, i + 1, j - 1, k));
                     VRAVG[k] = R(0.25) * (F3(VR, i, j, k) + F3(VR, i, j - 1, k) + F3(VR, i + 1, j, k) + F3(VR, i + 1, j - 1, k));
                     VTAVG[k] = R(0.25) * (F3(VT, i, j, k) + F3(VT, i, j - 1, k) + F3(VT, i + 1, j, k) + F3(VT, i + 1, j - 1, k));
@@ -927,13 +952,13 @@ struct Oracle : OracleBase {
                     RAVG[k] = R(0.5) * (F2(R, j, k) + F2(R, j - 1, k));
                     WTAVG[k] = VTAVG[k] - WREL * RAVG[k];
                     R WABSQ = VXAVG[k] * VXAVG[k] + VRAVG[k] * VRAVG[k] + WTAVG[k] * WTAVG[k];
-                    WABS[k] = std::sqrt(WABSQ);
+                    WABS[k] = om::sqrt(WABSQ);
                     WTB[k] = VTAVG[k] - F1(WHUB, j) * RAVG[k];
                     if (k > KMID) WTB[k] = VTAVG[k] - F1(WTIP, j) * RAVG[k];
-                    WBOUND[k] = std::sqrt(VXAVG[k] * VXAVG[k] + VRAVG[k] * VRAVG[k] + WTB[k] * WTB[k]);
+                    WBOUND[k] = om::sqrt(VXAVG[k] * VXAVG[k] + VRAVG[k] * VRAVG[k] + WTB[k] * WTB[k]);
                 }
                 if (REYNO < R(0.0001)) {
-                    VISLAM = (std::fabs(REYNO) / R(100000.0)) * std::pow(TAVG[KMID] / R(288.0), R(0.62));
+                    VISLAM = (om::fabs(REYNO) / R(100000.0)) * om::pow(TAVG[KMID] / R(288.0), R(0.62));
                     TCOND = CP * VISLAM / PRANDTL;
                     FTCOND = TCOND / VISLAM;
                 }
@@ -962,15 +987,15 @@ struct Oracle : OracleBase {
                 } else {
                     TWALLKM = CFWALL * ROAVG[KM] * WBOUND[KM] * WBOUND[KM];
                 }
-                R VSTAR = std::sqrt(TWALLK1 / ROAVG[1]);
+                R VSTAR = om::sqrt(TWALLK1 / ROAVG[1]);
                 for (int k = 1; k <= KMID; ++k) {
-                    R PERP = std::sqrt(F3(DWALLSQ, i, j, k));
+                    R PERP = om::sqrt(F3(DWALLSQ, i, j, k));
                     R YPLSK1 = VSTAR * PERP * ROAVG[1] / VISLAM;
                     F3(Y_PLUS, i, j, k) = std::min(YPLSK1, R(1000.0));
                 }
-                VSTAR = std::sqrt(TWALLKM / ROAVG[KM]);
+                VSTAR = om::sqrt(TWALLKM / ROAVG[KM]);
                 for (int k = KMID + 1; k <= KMM1; ++k) {
-                    R PERP = std::sqrt(F3(DWALLSQ, i, j, k));
+                    R PERP = om::sqrt(F3(DWALLSQ, i, j, k));
                     R YPLS = VSTAR * PERP * ROAVG[KM] / VISLAM;
                     F3(Y_PLUS, i, j, k) = std::min(YPLS, R(1000.0));
                 }
@@ -992,7 +1017,7 @@ struct Oracle : OracleBase {
                     FYPLUS = fyplus_of(F3(Y_PLUS, i, j, k), YPLAM, YPTURB, FYPLUS);
                     R DPERP = F3(VOL, i, j, k) / AREA[k];
                     VLAM[k] = ROWT2(FKLAM, NRW, k, KM) * VISLAM / DPERP;
-                    VTURB[k] = ROWT2(FKTURB, NRW, k, KM) * ROAVG[k] * std::fabs(WABS[k + 1] - WABS[k - 1]) * FMIXUP;
+                    VTURB[k] = ROWT2(FKTURB, NRW, k, KM) * ROAVG[k] * om::fabs(WABS[k + 1] - WABS[k - 1]) * FMIXUP;
                     VTURB[k] = VTURB[k] * FYPLUS;
                 }
                 bool turb = false;
@@ -1050,7 +1075,7 @@ struct Oracle : OracleBase {
                 RAVG[k] = F2(RAVG_CELL, j, k);
                 for (int i = 1; i <= IM; ++i) {
                     R abx = F3(ABX, i, j, k), abr = F3(ABR, i, j, k), abt = F2(ABT, j, k);
-                    AREA[i] = std::sqrt(abx * abx + abr * abr + abt * abt);
+                    AREA[i] = om::sqrt(abx * abx + abr * abr + abt * abt);
                     VXAVG[i] = R(0.25) * (F3(VX, i, j, k) + F3(VX, i, j - 1, k) + F3(VX, i, j - 1, k + 1) + F3(VX, i, j, k + 1));
                     VRAVG[i] = R(0.25) * (F3(VR, i, j, k) + F3(VR, i, j - 1, k) + F3(VR, i, j - 1, k + 1) + F3(VR, i, j, k + 1));
                     VTAVG[i] = R(0.25) * (F3(VT, i, j, k) + F3(VT, i, j - 1, k) + F3(VT, i, j - 1, k + 1) + F3(VT, i, j, k + 1));
@@ -1059,11 +1084,11 @@ struct Oracle : OracleBase {
                     TAVG[i] = R(0.25) * (F3(T_STATIC, i, j, k) + F3(T_STATIC, i, j - 1, k) + F3(T_STATIC, i, j - 1, k + 1) +
                                          F3(T_STATIC, i, j, k + 1));
                     R WABSQ = VXAVG[i] * VXAVG[i] + VRAVG[i] * VRAVG[i] + WTAVG[i] * WTAVG[i];
-                    WABS[i] = std::sqrt(WABSQ);
+                    WABS[i] = om::sqrt(WABSQ);
                     WBOUND[i] = WABS[i];
                 }
                 if (REYNO < R(0.0001)) {
-                    VISLAM = (std::fabs(REYNO) / R(100000.0)) * std::pow(TAVG[IMID] / R(288.0), R(0.62));
+                    VISLAM = (om::fabs(REYNO) / R(100000.0)) * om::pow(TAVG[IMID] / R(288.0), R(0.62));
                     TCOND = CP * VISLAM / PRANDTL;
                     FTCOND = TCOND / VISLAM;
                 }
@@ -1096,15 +1121,15 @@ struct Oracle : OracleBase {
                         } else {
                             TWALLIM = CFWALL * ROAVG[IM] * WABS[IM] * WABS[IM];
                         }
-                        R VSTAR = std::sqrt(TWALLI1 / ROAVG[1]);
+                        R VSTAR = om::sqrt(TWALLI1 / ROAVG[1]);
                         for (int i = 1; i <= IMID; ++i) {
-                            R YPLS = VSTAR * std::sqrt(F3(DWALLSQ, i, j, k)) * ROAVG[1] / VISLAM;
+                            R YPLS = VSTAR * om::sqrt(F3(DWALLSQ, i, j, k)) * ROAVG[1] / VISLAM;
                             R YPLSP = F3(Y_PLUS, i, j, k);
                             F3(Y_PLUS, i, j, k) = std::min(YPLS, YPLSP);
                         }
-                        VSTAR = std::sqrt(TWALLIM / ROAVG[IM]);
+                        VSTAR = om::sqrt(TWALLIM / ROAVG[IM]);
                         for (int i = IMID + 1; i <= IMM1; ++i) {
-                            R YPLS = VSTAR * std::sqrt(F3(DWALLSQ, i, j, k)) * ROAVG[IM] / VISLAM;
+                            R YPLS = VSTAR * om::sqrt(F3(DWALLSQ, i, j, k)) * ROAVG[IM] / VISLAM;
                             R YPLSP = F3(Y_PLUS, i, j, k);
                             F3(Y_PLUS, i, j, k) = std::min(YPLS, YPLSP);
                         }
@@ -1125,7 +1150,7 @@ struct Oracle : OracleBase {
                         FYPLUS = fyplus_of(F3(Y_PLUS, i, j, k), YPLAM, YPTURB, FYPLUS);
                         R DPERP = F3(VOL, i, j, k) / AREA[i];
                         VLAM[i] = ROWT2(FILAM, NRW, i, IM) * VISLAM / DPERP;
-                        VTURB[i] = ROWT2(FITURB, NRW, i, IM) * ROAVG[i] * std::fabs(WABS[i + 1] - WABS[i - 1]) * FMIXUP;
+                        VTURB[i] = ROWT2(FITURB, NRW, i, IM) * ROAVG[i] * om::fabs(WABS[i + 1] - WABS[i - 1]) * FMIXUP;
                         VTURB[i] = VTURB[i] * FYPLUS;
                     }
                     bool turb = false;
@@ -1184,7 +1209,7 @@ struct Oracle : OracleBase {
                             R FBLEND = (FACJ * ROWT2(FIWAKE, NRW, i, IM) + (R(1.) - FACJ) * ROWT2(FITURB, NRW, i, IM)) * FMIXUP;
                             R DPERP = F3(VOL, ISUB, j, k) / AREA[i];
                             VLAM[i] = ROWT2(FILAM, NRW, i, IM) * VISLAM / DPERP;
-                            VTURB[i] = FBLEND * ROAVG[i] * std::fabs(WABS[IP1] - WABS[IM1]);
+                            VTURB[i] = FBLEND * ROAVG[i] * om::fabs(WABS[IP1] - WABS[IM1]);
                             F3(VISC_RAT, i, j, k) = VTURB[i] / VLAM[i];
                             R FM = AREA[i] * (VLAM[i] + VTURB[i]);
                             XSTRES[i] = FM * (VXAVG[IP1] - VXAVG[IM1]);
@@ -1201,7 +1226,7 @@ struct Oracle : OracleBase {
                             int IP1 = (i == IM) ? 2 : i + 1;
                             R DPERP = F3(VOL, ISUB, j, k) / AREA[i];
                             VLAM[i] = ROWT2(FILAM, NRW, i, IM) * VISLAM / DPERP;
-                            VTURB[i] = FMIXUP * ROWT2(FIUP, NRW, i, IM) * ROAVG[i] * std::fabs(WABS[IP1] - WABS[IM1]);
+                            VTURB[i] = FMIXUP * ROWT2(FIUP, NRW, i, IM) * ROAVG[i] * om::fabs(WABS[IP1] - WABS[IM1]);
                             F3(VISC_RAT, i, j, k) = VTURB[i] / VLAM[i];
                             R FM = AREA[i] * (VLAM[i] + VTURB[i]);
                             XSTRES[i] = FM * (VXAVG[IP1] - VXAVG[IM1]);
@@ -1262,7 +1287,7 @@ struct Oracle : OracleBase {
             for (int k = 2; k <= KM; ++k) {
                 R XDIF = F2(X, JMID, k) - F2(X, JMID, k - 1);
                 R RDIF = F2(R, JMID, k) - F2(R, JMID, k - 1);
-                AVGSPAN = AVGSPAN + std::sqrt(XDIF * XDIF + RDIF * RDIF);
+                AVGSPAN = AVGSPAN + om::sqrt(XDIF * XDIF + RDIF * RDIF);
             }
             R AVGPIT = R(2) * R(3.1415926) * F2(R, JMID, KMID) / R(F1(NBLADE, JMID));
             R XLIMH = F1(XLLIM_K1, nrw) * AVGPIT / AVGSPAN;
@@ -1328,9 +1353,9 @@ struct Oracle : OracleBase {
                 R VABSQ = VMSQ + VTMIX * VTMIX;
                 R WTMIX = VTMIX - UJP1;
                 R WMIXSQ = VMSQ + WTMIX * WTMIX;
-                R WMIX = std::sqrt(WMIXSQ);
-                R ALPHAMIX = std::asin(WTMIX / WMIX);
-                R GAMAMIX = std::atan2(VRMIX, VXMIX);
+                R WMIX = om::sqrt(WMIXSQ);
+                R ALPHAMIX = om::asin(WTMIX / WMIX);
+                R GAMAMIX = om::atan2(VRMIX, VXMIX);
                 R TMIX = (ROEMIX / ROMIX - R(0.5) * VABSQ) / CV;
                 R ROTHALPY = CP * TMIX + R(0.5) * (WMIXSQ - UJP1 * UJP1);
                 R GAGAS = GA;
@@ -1346,7 +1371,7 @@ struct Oracle : OracleBase {
                     R VMSQJP2 = XVELJP2 * XVELJP2 + RVELJP2 * RVELJP2;
                     R VELSQJP2 = VMSQJP2 + TVELJP2 * TVELJP2;
                     R WACT_SQ_JP2 = VMSQJP2 + WTJP2 * WTJP2;
-                    R WACT_JP2 = std::sqrt(WACT_SQ_JP2);
+                    R WACT_JP2 = om::sqrt(WACT_SQ_JP2);
                     R RO_ACT_JP2 = ROJP2;
                     R T_ACT_JP2 = (F3(ROE, i, JP2, k) / ROJP2 - R(0.5) * VELSQJP2) / CV;
                     R RJP3 = F2(R, JP3, k), UNOWJP3 = F2(UBLADE, JP3, k);
@@ -1356,21 +1381,21 @@ struct Oracle : OracleBase {
                     R ROWTJP3 = ROVTJP3 - UNOWJP3 * ROJP3;
                     R ROVMSQJP3 = ROVXJP3 * ROVXJP3 + ROVRJP3 * ROVRJP3;
                     R ROWRELSQJP3 = ROVMSQJP3 + ROWTJP3 * ROWTJP3;
-                    R ROWRELJP3 = std::sqrt(ROWRELSQJP3);
-                    R ALPHAJP3 = std::asin(ROWTJP3 / ROWRELJP3);
-                    R GAMAJP3 = std::atan2(ROVRJP3, ROVXJP3);
+                    R ROWRELJP3 = om::sqrt(ROWRELSQJP3);
+                    R ALPHAJP3 = om::asin(ROWTJP3 / ROWRELJP3);
+                    R GAMAJP3 = om::atan2(ROVRJP3, ROVXJP3);
                     R PSTAT = ROJP2 * RGAS * T_ACT_JP2;
-                    R TISENT_JP2 = TMIX * std::pow(PSTAT / PMIX, FGA);
+                    R TISENT_JP2 = TMIX * om::pow(PSTAT / PMIX, FGA);
                     R WIS_SQ_JP2 = R(2) * (ROTHALPY - CP * TISENT_JP2 + R(0.5) * UNOWJP2 * UNOWJP2);
                     R ROISENT_JP2 = PSTAT / RGAS / TISENT_JP2;
                     ROISENT[i] = ROISENT_JP2;
                     PISENT[i] = PSTAT;
                     TISENT[i] = TISENT_JP2;
                     if (WIS_SQ_JP2 < R(1.0)) WIS_SQ_JP2 = R(1.0);
-                    WIS_JP2[i] = std::sqrt(WIS_SQ_JP2);
+                    WIS_JP2[i] = om::sqrt(WIS_SQ_JP2);
                     WREF_JP2[i] = WACT_JP2;
                     ROREF_JP2[i] = RO_ACT_JP2;
-                    WMACH_JP2[i] = WACT_JP2 / std::sqrt(GAGAS * RGAS * T_ACT_JP2);
+                    WMACH_JP2[i] = WACT_JP2 / om::sqrt(GAGAS * RGAS * T_ACT_JP2);
                     if (WMACH_JP2[i] > R(1.0)) NMACH = NMACH + 1;
                     ALPHAA[i] = F_ANGLE1 * ALPHAMIX + F_ANGLE * ALPHAJP3;
                     GAMA[i] = F_ANGLE1 * GAMAMIX + F_ANGLE * GAMAJP3;
@@ -1382,8 +1407,8 @@ struct Oracle : OracleBase {
                         int im1 = i - 1;
                         if (WMACH_JP2[i] > R(1.001) && WMACH_JP2[im1] > R(1.001)) {
                             R DELP = PISENT[i] - PISENT[im1];
-                            R DELTAI = std::sqrt(WMACH_JP2[i] * WMACH_JP2[i] - R(1)) / (ROREF_JP2[i] * WREF_JP2[i] * WREF_JP2[i]);
-                            R DELTAIM1 = std::sqrt(WMACH_JP2[im1] * WMACH_JP2[im1] - R(1)) /
+                            R DELTAI = om::sqrt(WMACH_JP2[i] * WMACH_JP2[i] - R(1)) / (ROREF_JP2[i] * WREF_JP2[i] * WREF_JP2[i]);
+                            R DELTAIM1 = om::sqrt(WMACH_JP2[im1] * WMACH_JP2[im1] - R(1)) /
                                          (ROREF_JP2[im1] * WREF_JP2[im1] * WREF_JP2[im1]);
                             ALPHAA[i] = ALPHAA[im1] + FROTN * DELP * R(0.5) * (DELTAI + DELTAIM1);
                         }
@@ -1392,8 +1417,8 @@ struct Oracle : OracleBase {
                         int ip1 = i + 1;
                         if (WMACH_JP2[i] > R(1.001) && WMACH_JP2[ip1] > R(1.001)) {
                             R DELP = PISENT[i] - PISENT[ip1];
-                            R DELTAI = std::sqrt(WMACH_JP2[i] * WMACH_JP2[i] - R(1)) / (ROREF_JP2[i] * WREF_JP2[i] * WREF_JP2[i]);
-                            R DELTAIP1 = std::sqrt(WMACH_JP2[ip1] * WMACH_JP2[ip1] - R(1)) /
+                            R DELTAI = om::sqrt(WMACH_JP2[i] * WMACH_JP2[i] - R(1)) / (ROREF_JP2[i] * WREF_JP2[i] * WREF_JP2[i]);
+                            R DELTAIP1 = om::sqrt(WMACH_JP2[ip1] * WMACH_JP2[ip1] - R(1)) /
                                          (ROREF_JP2[ip1] * WREF_JP2[ip1] * WREF_JP2[ip1]);
                             ALPHAA[i] = ALPHAA[ip1] + FROTN * DELP * R(0.5) * (DELTAI + DELTAIP1);
                         }
@@ -1407,10 +1432,10 @@ struct Oracle : OracleBase {
                 }
                 for (int i = 1; i <= IM; ++i) {
                     R RO_JP2 = ROISENT[i];
-                    R WT_JP2 = WIS_JP2[i] * std::sin(ALPHAA[i]);
-                    R VM_JP2 = WIS_JP2[i] * std::cos(ALPHAA[i]);
-                    R VX_JP2 = VM_JP2 * std::cos(GAMA[i]);
-                    R VR_JP2 = VM_JP2 * std::sin(GAMA[i]);
+                    R WT_JP2 = WIS_JP2[i] * om::sin(ALPHAA[i]);
+                    R VM_JP2 = WIS_JP2[i] * om::cos(ALPHAA[i]);
+                    R VX_JP2 = VM_JP2 * om::cos(GAMA[i]);
+                    R VR_JP2 = VM_JP2 * om::sin(GAMA[i]);
                     R VT_JP2 = WT_JP2 + UNOWJP2;
                     R V_JP2_SQ = VM_JP2 * VM_JP2 + VT_JP2 * VT_JP2;
                     R ROE_JP2 = ROISENT[i] * (CV * TISENT[i] + R(0.5) * V_JP2_SQ);
@@ -1433,7 +1458,7 @@ struct Oracle : OracleBase {
         NSTEP = NSTEP + 1;
         if (NSTEP == NSTEPS_MAX) IFEND = 1;
         if (EAVG < CONLIM && ECONT < R(0.01)) IFEND = 1;
-        if (std::fabs(EMAX) < R(4) * CONLIM && ECONT < R(0.01)) IFEND = 1;
+        if (om::fabs(EMAX) < R(4) * CONLIM && ECONT < R(0.01)) IFEND = 1;
         if (force_end) IFEND = 1;
 
         if (!(IF_RESTART != 0 && NSTEP > 100)) {
@@ -1484,7 +1509,7 @@ struct Oracle : OracleBase {
                         }
                         VRMS = VRMS + EKE;
                     }
-            VMAX = std::sqrt(VMAX);
+            VMAX = om::sqrt(VMAX);
         }
         /* pressure, stagnation enthalpy, temperature 5900 */
         for (int k = 1; k <= KM; ++k)
@@ -1498,7 +1523,7 @@ struct Oracle : OracleBase {
                     F3(HO, i, j, k) = CP * TSTATIC + EKE;
                     F3(T_STATIC, i, j, k) = TSTATIC;
                 }
-        if (ILOS == 10 && NSTEP % NLOS == 0) loss();
+        if (ILOS == 10 && NSTEP % NLOS == 0 && !FROZEN) loss();
         mass_fluxes();
         tstep(RO_v, DRO_v);
         energy_fluxes();
@@ -1529,12 +1554,12 @@ struct Oracle : OracleBase {
         }
         if (tail) {
             int health = tail_monitors();
-            stepup(0.25);
+            if (!FROZEN) stepup(0.25);
             if (mon) {
                 mon->tail_ran = 1;
                 mon->emax = (float)EMAX; mon->imax = IMAXE; mon->jmax = JMAXE; mon->kmax = KMAXE;
                 mon->eavg = (float)EAVG; mon->econt = (float)ECONT; mon->jcont = JCONT;
-                mon->vref = (float)std::sqrt(VRMS * RIJKM);
+                mon->vref = (float)om::sqrt(VRMS * RIJKM);
                 mon->vmax = (float)VMAX; mon->ivmax = IVMAX; mon->jvmax = JVMAX; mon->kvmax = KVMAX;
                 mon->flow_in = (double)BLADE_FLOW[0];
                 mon->flow_out = (double)BLADE_FLOW[JM - 1];
@@ -1668,13 +1693,13 @@ struct Oracle : OracleBase {
         }
         for (int j = 1; j <= JM; ++j) {
             R a = F3(ROVX, IMID, j, KMID), b = F3(ROVR, IMID, j, KMID);
-            R ROVMER = std::sqrt(a * a + b * b);
+            R ROVMER = om::sqrt(a * a + b * b);
             R DELTA = (AVFLOW / FLOW[j] - R(1.0)) * ROVMER;
             DELTA = DELTA * RFLOW;
             for (int i = 1; i <= IM; ++i)
                 for (int k = 1; k <= KM; ++k) {
                     R x = F3(ROVX, i, j, k), r = F3(ROVR, i, j, k);
-                    R RM = std::sqrt(x * x + r * r);
+                    R RM = om::sqrt(x * x + r * r);
                     if (x < R(0.0)) RM = -RM;
                     F3(ROVX, i, j, k) = x + x / RM * DELTA;
                     F3(ROVR, i, j, k) = r + r / RM * DELTA;
@@ -1775,7 +1800,7 @@ struct Oracle : OracleBase {
                 R RO_STAG = F1(PO1, k) / RGAS / F1(TO1, k);
                 R RO_IN = F3(RO, i, 1, k);
                 if (RO_IN > R(0.9999) * RO_STAG) RO_IN = R(0.9999) * RO_STAG;
-                R PNEW = F1(PO1, k) * std::pow(RO_IN / RO_STAG, GA);
+                R PNEW = F1(PO1, k) * om::pow(RO_IN / RO_STAG, GA);
                 if (IN_PRESS == 0) F3(P, i, 1, k) = RFIN1 * F3(P, i, 1, k) + RFIN * PNEW;
                 if (std::abs(IN_PRESS) == 1)
                     F3(P, i, 1, k) = RFIN1 * F3(P, i, 1, k) + RFIN2 * F3(P, i, 2, k) - RFIN * F3(P, i, 3, k);
@@ -1784,10 +1809,10 @@ struct Oracle : OracleBase {
                     F3(P, i, 1, k) = RFIN1 * F3(P, i, 1, k) + RFIN2 * F3(P, IMID, 2, KMID) - RFIN * F3(P, IMID, 3, KMID);
                 if (F3(P, i, 1, k) > PLIM[k - 1]) F3(P, i, 1, k) = R(0.9) * F3(P, i, 1, k) + R(0.1) * PLIM[k - 1];
                 if (F3(P, i, 1, k) > R(0.99999) * F1(PO1, k)) F3(P, i, 1, k) = F1(PO1, k) * R(0.99999);
-                R TSTATIC = F1(TO1, k) * std::pow(F3(P, i, 1, k) * F1(RPO1, k), FGA);
+                R TSTATIC = F1(TO1, k) * om::pow(F3(P, i, 1, k) * F1(RPO1, k), FGA);
                 R VABSQ = R(2) * CP * (F1(TO1, k) - TSTATIC);
                 F3(T_STATIC, i, 1, k) = TSTATIC;
-                R VABS = std::sqrt(VABSQ);
+                R VABS = om::sqrt(VABSQ);
                 R VMER = R(0);
                 if (IN_VTAN == 0) {
                     VMER = VABS * F1(BSCOS, k);
@@ -1796,21 +1821,21 @@ struct Oracle : OracleBase {
                 if (IN_VTAN == 1) {
                     R VMERSQ = VABSQ - F1(VTIN, k) * F1(VTIN, k);
                     if (VMERSQ < R(0.01)) VMERSQ = R(0.01);
-                    VMER = std::sqrt(VMERSQ);
+                    VMER = om::sqrt(VMERSQ);
                     F3(VT, i, 1, k) = F1(VTIN, k);
                 }
                 if (IN_VTAN == 2) {
                     R WR = F2(UBLADE, 1, k);
                     R VRELSQ = VABSQ - WR * WR * F1(BSCOS, k) * F1(BSCOS, k);
                     if (VRELSQ < R(0.01)) VRELSQ = R(0.01);
-                    R VREL = std::sqrt(VRELSQ) - WR * F1(BSSIN, k);
+                    R VREL = om::sqrt(VRELSQ) - WR * F1(BSSIN, k);
                     VMER = VREL * F1(BSCOS, k);
                     F3(VT, i, 1, k) = VREL * F1(BSSIN, k) + WR;
                 }
                 if (IN_VR > 0) F3(VX, i, 1, k) = VMER * F1(BRCOS, k);
                 R VXSQ = VMER * VMER - F3(VR, i, 2, k) * F3(VR, i, 2, k);
                 if (VXSQ < R(0.0000001) * F1(TO1, k) * CP) VXSQ = R(0.0000001) * F1(TO1, k) * CP;
-                if (IN_VR <= 0) F3(VX, i, 1, k) = std::sqrt(VXSQ);
+                if (IN_VR <= 0) F3(VX, i, 1, k) = om::sqrt(VXSQ);
                 if (IN_VR > 0) F3(VR, i, 1, k) = VMER * F1(BRSIN, k);
                 if (IN_VR <= 0) F3(VR, i, 1, k) = F3(VR, i, 2, k);
                 F3(RO, i, 1, k) = F3(P, i, 1, k) / (RGAS * TSTATIC);
@@ -1964,7 +1989,7 @@ struct Oracle : OracleBase {
         R GM1 = GA - R(1.0);
         R TRATIO = R(1.0) + MACHLIM * MACHLIM * R(0.5) * GM1;
         R RFGM1 = R(1.0) / GM1;
-        R RORATIO = std::pow(TRATIO, RFGM1);
+        R RORATIO = om::pow(TRATIO, RFGM1);
         for (int nr = 1; nr <= NROWS; ++nr) {
             int JREF = F1(JLE, nr);
             R TREFL = F3(T_STATIC, IMID, JREF, KMID);
@@ -1973,8 +1998,8 @@ struct Oracle : OracleBase {
             R TOREL_REF = TREFL + R(0.5) * WREFSQ / CP;
             R TLIMIT = TOREL_REF / TRATIO;
             if (TLIMIT > TCOOL_MIN) TLIMIT = TCOOL_MIN;
-            VLIMIT[nr - 1] = std::sqrt(R(2) * CP * (TOREL_REF - TLIMIT));
-            R ROSTAG_REL = F3(RO, IMID, JREF, KMID) * std::pow(TOREL_REF / TREFL, RFGM1);
+            VLIMIT[nr - 1] = om::sqrt(R(2) * CP * (TOREL_REF - TLIMIT));
+            R ROSTAG_REL = F3(RO, IMID, JREF, KMID) * om::pow(TOREL_REF / TREFL, RFGM1);
             ROLIMIT[nr - 1] = ROSTAG_REL / RORATIO;
         }
         for (int k = 1; k <= KM; ++k)
@@ -1986,7 +2011,7 @@ struct Oracle : OracleBase {
                     R RONOW = F3(RO, i, j, k);
                     R vx = F3(VX, i, j, k), vr = F3(VR, i, j, k), wt = F3(WT, i, j, k);
                     R WRELSQ = vx * vx + vr * vr + wt * wt;
-                    R WREL = std::sqrt(WRELSQ);
+                    R WREL = om::sqrt(WRELSQ);
                     R FACSAFE = V_LIMIT / WREL;
                     if (FACSAFE < R(1.0)) {
                         F3(ROVX, i, j, k) = RONOW * vx * FACSAFE;
@@ -2013,7 +2038,7 @@ struct Oracle : OracleBase {
         ECONT = R(0.0);
         for (int j = 1; j <= JM; ++j) {
             R RATIO = CHECK_FLOW[j - 1] / CHECK_FLOW[0];
-            R EMASS = std::fabs(R(1.) - RATIO);
+            R EMASS = om::fabs(R(1.) - RATIO);
             if (EMASS > ECONT) {
                 ECONT = EMASS;
                 JCONT = j;
@@ -2021,7 +2046,7 @@ struct Oracle : OracleBase {
         }
         EMAX = R(0.0);
         EAVG = R(0.0);
-        R VREF = std::sqrt(VRMS * RIJKM);
+        R VREF = om::sqrt(VRMS * RIJKM);
         R RVEF = R(100.) / VREF;
         for (int k = 1; k <= KM; ++k)
             for (int j = 2; j <= JM; ++j) {
@@ -2031,8 +2056,8 @@ struct Oracle : OracleBase {
                     R VM_END = (XD * F3(ROVX, i, j, k) + RD * F3(ROVR, i, j, k)) / SD / F3(RO, i, j, k);
                     R DVMER = (VM_END - VM_START) * RVEF;
                     A3(STORE, i, j, k) = DVMER;
-                    EAVG = EAVG + std::fabs(DVMER);
-                    if (std::fabs(DVMER) > std::fabs(EMAX)) {
+                    EAVG = EAVG + om::fabs(DVMER);
+                    if (om::fabs(DVMER) > om::fabs(EMAX)) {
                         EMAX = DVMER;
                         IMAXE = i; JMAXE = j; KMAXE = k;
                     }
@@ -2043,14 +2068,94 @@ struct Oracle : OracleBase {
         size_t n3 = (size_t)IM * JM * KM;
         for (size_t q = 0; q < n3; ++q) {
             R ro = RO_v[q];
-            if (!std::isfinite(ro) || !(ro > R(0)) || !std::isfinite(ROE_v[q]) || !std::isfinite(ROVX_v[q]) ||
-                !std::isfinite(ROVR_v[q]) || !std::isfinite(RORVT_v[q]))
+            if (!om::isfinite(ro) || !(ro > R(0)) || !om::isfinite(ROE_v[q]) || !om::isfinite(ROVX_v[q]) ||
+                !om::isfinite(ROVR_v[q]) || !om::isfinite(RORVT_v[q]))
                 ++bad;
         }
         return bad;
     }
 
     /* EFICOOL (IFCOOL=0) with SUMFLX: whole-machine efficiency */
+    /* a REAL array from double values (finite-difference checks) */
+    int set_array_f64(const char *n, const double *p, int64_t cnt) override {
+        std::vector<R> *a = float_array(n);
+        if (!a) return fail(MGPU_E_ARG, std::string("unknown array ") + n);
+        if ((int64_t)a->size() != cnt) return fail(MGPU_E_ARG, std::string("size mismatch for ") + n);
+        for (size_t q = 0; q < a->size(); ++q) (*a)[q] = R(p[q]);
+        return 0;
+    }
+    /* ---- reverse mode ------------------------------------------------ */
+    static constexpr bool is_ad = std::is_same<R, adt::AD>::value;
+    adt::Tape tape_;
+    std::vector<std::pair<std::string, std::vector<int32_t>>> ad_in_;
+#define O_FA_INT32(nm)
+#define O_FA_FLOAT32(nm) if (!strcmp(n, #nm)) return &nm##_v;
+#define O_FA(nm, t, s, r) O_FA_##t(nm)
+    std::vector<R> *float_array(const char *n) {
+        MGPU_ARRAYS(O_FA)
+        return nullptr;
+    }
+    int ad_begin() override {
+        if constexpr (!is_ad) {
+            return fail(MGPU_E_STATE, "not a differentiating oracle");
+        } else {
+            if (!committed) return fail(MGPU_E_STATE, "ad_begin before commit");
+            tape_.clear();
+            ad_in_.clear();
+            adt::tape() = &tape_;
+#define O_REG_INT32(nm)
+#define O_REG_FLOAT32(nm)                                                   \
+    {                                                                       \
+        std::vector<int32_t> ids;                                           \
+        for (auto &x : nm##_v) {                                            \
+            x = adt::independent(x.v);                                      \
+            ids.push_back(x.i);                                             \
+        }                                                                   \
+        ad_in_.emplace_back(#nm, std::move(ids));                           \
+    }
+#define O_REG(nm, t, s, r) O_REG_##t(nm)
+            MGPU_ARRAYS(O_REG)
+            return 0;
+        }
+    }
+    int ad_zero() override {
+        if constexpr (!is_ad) return fail(MGPU_E_STATE, "not a differentiating oracle");
+        adt::tape() = nullptr;
+        tape_.adj.assign(tape_.size(), 0.0);
+        return 0;
+    }
+    int ad_seed(const char *n, const double *w, int64_t cnt) override {
+        if constexpr (!is_ad) {
+            return fail(MGPU_E_STATE, "not a differentiating oracle");
+        } else {
+            std::vector<R> *a = float_array(n);
+            if (!a) return fail(MGPU_E_ARG, std::string("unknown array ") + n);
+            if ((int64_t)a->size() != cnt) return fail(MGPU_E_ARG, std::string("size mismatch for ") + n);
+            if (tape_.adj.size() != tape_.size()) ad_zero();
+            for (size_t q = 0; q < a->size(); ++q)
+                if ((*a)[q].i >= 0) tape_.adj[(size_t)(*a)[q].i] += w[q];
+            return 0;
+        }
+    }
+    int ad_reverse() override {
+        if constexpr (!is_ad) return fail(MGPU_E_STATE, "not a differentiating oracle");
+        if (tape_.adj.size() != tape_.size()) ad_zero();
+        tape_.reverse();
+        return 0;
+    }
+    int ad_grad(const char *n, double *out, int64_t cnt) override {
+        if constexpr (!is_ad) return fail(MGPU_E_STATE, "not a differentiating oracle");
+        for (auto &e : ad_in_)
+            if (e.first == n) {
+                if ((int64_t)e.second.size() != cnt) return fail(MGPU_E_ARG, std::string("size mismatch for ") + n);
+                for (size_t q = 0; q < e.second.size(); ++q)
+                    out[q] = (e.second[q] >= 0 && (size_t)e.second[q] < tape_.adj.size()) ? tape_.adj[(size_t)e.second[q]] : 0.0;
+                return 0;
+            }
+        return fail(MGPU_E_ARG, std::string("array not registered: ") + n);
+    }
+    int64_t ad_tape_size() override { return (int64_t)tape_.size(); }
+
     int integrals(mgpu_integrals *out) override {
         if (!committed) return fail(MGPU_E_STATE, "integrals before commit");
         size_t n3 = (size_t)IM * JM * KM;
@@ -2067,11 +2172,11 @@ struct Oracle : OracleBase {
                     if (TS < R(0.1) * TO1M) TS = R(0.1) * TO1M;
                     R PSTAT = F3(P, i, j, k);
                     if (PSTAT < R(0.02) * PO1M) PSTAT = R(0.02) * PO1M;
-                    R PSTAG = PSTAT * std::pow(TSTAG / TS, RFGA);
+                    R PSTAG = PSTAT * om::pow(TSTAG / TS, RFGA);
                     R TRAT = TS / TO1M, PRAT = PSTAT / PO1M;
                     R ENTRPY = R(0.0);
                     bool skip = (PRAT > R(0.99999) && PRAT < R(1.00001)) || (TRAT > R(0.99999) && TRAT < R(1.00001));
-                    if (!skip) ENTRPY = CP * std::log(TRAT) - RGAS * std::log(PRAT);
+                    if (!skip) ENTRPY = CP * om::log(TRAT) - RGAS * om::log(PRAT);
                     A3(ST2, i, j, k) = TS;
                     A3(T1, i, j, k) = TSTAG;
                     A3(T2, i, j, k) = PSTAG / PO1M;
@@ -2103,8 +2208,8 @@ struct Oracle : OracleBase {
         R TO_IN = STO[J1 - 1], TO_OUT = STO[J2M1 - 1];
         R TORAT = TO_OUT / TO_IN, DELTO = TO_OUT - TO_IN, PORAT = PO2 / POIN, PSRAT = PSOUT / POIN;
         if (PORAT < R(0.01)) PORAT = R(0.01);
-        R TO2IS = std::pow(PORAT, FGA) * TO_IN;
-        R TSTAT2_IS = std::pow(PSRAT, FGA) * TO_IN;
+        R TO2IS = om::pow(PORAT, FGA) * TO_IN;
+        R TSTAT2_IS = om::pow(PSRAT, FGA) * TO_IN;
         R DELTOIS = TO2IS - TO_IN, DELT_TOT_STAT = TSTAT2_IS - TO_IN;
         R ETAIS = R(1.0);
         if (DELTO > R(0.0)) ETAIS = DELTOIS / DELTO;
@@ -2136,6 +2241,7 @@ void *oref_create(int32_t im, int32_t jm, int32_t km, int32_t nrows, int32_t use
         g_err = "bad dimensions";
         return nullptr;
     }
+    if (use_double == 2) return (OracleBase *)new Oracle<adt::AD>(im, jm, km, nrows);
     if (use_double) return (OracleBase *)new Oracle<double>(im, jm, km, nrows);
     return (OracleBase *)new Oracle<float>(im, jm, km, nrows);
 }
@@ -2154,5 +2260,14 @@ int32_t oref_stepup(void *h, double relax) { return ((OracleBase *)h)->stepup(re
 int32_t oref_loss_init(void *h) { return ((OracleBase *)h)->loss_init(); }
 int32_t oref_step(void *h, int32_t force_end, mgpu_monitors *mon) { return ((OracleBase *)h)->step(force_end, mon); }
 int32_t oref_integrals(void *h, mgpu_integrals *out) { return ((OracleBase *)h)->integrals(out); }
+int32_t oref_set_array_f64(void *h, const char *n, const double *p, int64_t cnt) {
+    return ((OracleBase *)h)->set_array_f64(n, p, cnt);
+}
+int32_t oref_ad_begin(void *h) { return ((OracleBase *)h)->ad_begin(); }
+int32_t oref_ad_zero(void *h) { return ((OracleBase *)h)->ad_zero(); }
+int32_t oref_ad_seed(void *h, const char *n, const double *w, int64_t cnt) { return ((OracleBase *)h)->ad_seed(n, w, cnt); }
+int32_t oref_ad_reverse(void *h) { return ((OracleBase *)h)->ad_reverse(); }
+int32_t oref_ad_grad(void *h, const char *n, double *out, int64_t cnt) { return ((OracleBase *)h)->ad_grad(n, out, cnt); }
+int64_t oref_ad_tape_size(void *h) { return ((OracleBase *)h)->ad_tape_size(); }
 
 } /* extern "C" */

@@ -66,9 +66,19 @@ def lib():
         L.oref_loss_init.argtypes = [vp]
         L.oref_step.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(Monitors)]
         L.oref_integrals.argtypes = [vp, ctypes.POINTER(Integrals)]
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.oref_set_array_f64.argtypes = [vp, cp, vp, ctypes.c_int64]
+        L.oref_ad_begin.argtypes = [vp]
+        L.oref_ad_zero.argtypes = [vp]
+        L.oref_ad_seed.argtypes = [vp, cp, vp, ctypes.c_int64]
+        L.oref_ad_reverse.argtypes = [vp]
+        L.oref_ad_grad.argtypes = [vp, cp, vp, ctypes.c_int64]
+        L.oref_ad_tape_size.argtypes = [vp]
+        L.oref_ad_tape_size.restype = ctypes.c_int64
         for f in ("oref_set_int", "oref_set_real", "oref_get_real", "oref_get_int", "oref_set_array",
                   "oref_get_array", "oref_commit", "oref_stepup", "oref_loss_init", "oref_step",
-                  "oref_integrals"):
+                  "oref_integrals", "oref_set_array_f64", "oref_ad_begin", "oref_ad_zero", "oref_ad_seed",
+                  "oref_ad_reverse", "oref_ad_grad"):
             getattr(L, f).restype = ctypes.c_int32
         _lib = L
     return _lib
@@ -79,13 +89,15 @@ class OracleError(RuntimeError):
 
 
 class Oracle:
-    """One oracle problem (float or double arithmetic)."""
+    """One oracle problem: float or double arithmetic, or (ad=True) double
+    arithmetic recorded on a tape for reverse-mode derivatives."""
 
-    def __init__(self, cd, double: bool = False):
+    def __init__(self, cd, double: bool = False, ad: bool = False):
         L = lib()
         self.cd = cd
-        self.double = double
-        self.h = L.oref_create(cd.im, cd.jm, cd.km, cd.nrows, 1 if double else 0)
+        self.double = double or ad
+        self.ad = ad
+        self.h = L.oref_create(cd.im, cd.jm, cd.km, cd.nrows, 2 if ad else (1 if double else 0))
         if not self.h:
             raise OracleError(L.oref_last_error().decode())
         for k, v in cd.ints.items():
@@ -142,3 +154,34 @@ class Oracle:
         o = Integrals()
         self._chk(lib().oref_integrals(self.h, ctypes.byref(o)))
         return o
+
+    def set_f64(self, name: str, values: np.ndarray):
+        """Overwrites a REAL array with double values (finite-difference checks)."""
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        self._chk(lib().oref_set_array_f64(self.h, name.encode(), a.ctypes.data, a.size))
+
+    # ---- reverse mode (ad=True) -------------------------------------------
+    def ad_begin(self):
+        """Makes every REAL COMMON array an independent variable; the next
+        steps are recorded."""
+        self._chk(lib().oref_ad_begin(self.h))
+
+    def ad_reverse(self, seeds: dict) -> None:
+        """Output adjoints {array name: values} on the arrays' current values,
+        then one reverse sweep of the tape."""
+        L = lib()
+        self._chk(L.oref_ad_zero(self.h))
+        for name, w in seeds.items():
+            w = np.ascontiguousarray(w, dtype=np.float64)
+            self._chk(L.oref_ad_seed(self.h, name.encode(), w.ctypes.data, w.size))
+        self._chk(L.oref_ad_reverse(self.h))
+
+    def ad_grad(self, name: str) -> np.ndarray:
+        """Adjoint of an array as it was at ad_begin."""
+        ref = self.cd.arrays[name]
+        out = np.zeros(ref.shape, np.float64)
+        self._chk(lib().oref_ad_grad(self.h, name.encode(), out.ctypes.data, out.size))
+        return out
+
+    def ad_tape_size(self) -> int:
+        return int(lib().oref_ad_tape_size(self.h))
