@@ -44,6 +44,10 @@ WORKLOADS = {
     "nozzle": ("nozzle_row",
                "axial turbine nozzle row 37x97x33, 48 vanes, 3-level multigrid (level 2 off), SCREE, "
                "mixing-length LOSS/5 steps"),
+    "adjoint": ("turbine_stage",
+                "discrete adjoint (frozen mixing length) of the single-stage turbine 65x242x49, SFXIN=SFTIN=0.02: "
+                "gradients of eta_tt and inlet mass flow w.r.t. 30 blade-angle design variables "
+                "(stagger, inlet and exit metal angle at 5 span sections x 2 rows)"),
     "batch64": ("batch_instance",
                 "64 single-stage turbines in one batch graph: I in {33,49,65}, K in {33,49}, J in [97,161], "
                 "exit P/P0 in [0.45,0.70], 7000-10000 rpm (seeded), SCREE, mixing-length LOSS/5 steps"),
@@ -304,6 +308,115 @@ def run_batch(args, rank, world, local_rank):
     return 0
 
 
+# reverse-step kernels: seeds, mixing plane, 2 limiters, 2 x 4 TSTEP kernels,
+# momentum fluxes, PEFF, inlet/exit, energy fluxes, exit sums, mass fluxes, primitives
+ADJ_KERNELS_PER_STEP = 19
+
+
+def run_adjoint(args, rank, world, local_rank):
+    """Config 2: adjoint against finite-difference gradient time.  The time
+    of one primal solve (LOSS on, from the initial guess to the FP32
+    convergence floor), of the adjoint gradient of two objectives with
+    respect to 30 design variables (recording, GMRES on the transposed step,
+    geometry gradients and the chain to the variables), and of one
+    perturbed primal solve, which 60 central differences need each."""
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local_rank)
+        if rank != 0:
+            return 0            # replicas only: one problem per GPU, reported by rank 0
+    import numpy as np
+    from mgpu import case, lib, design
+
+    def make():
+        sp = case.turbine_stage()
+        sp.sfxin = sp.sftin = 0.02
+        return sp
+
+    ds = design.DesignSpace.seeded(make)
+    alpha = ds.alpha0
+    cd = ds.deck(alpha)
+    cd.ints["NSTEPS_MAX"] = 10 ** 9
+    cd.reals["CONLIM"] = 1e-9
+    n_primal, inner, restart, max_steps, n_fd = 16000, 50, 30, 20000, 10000
+    p = lib.Problem(cd)
+    p.run(max(args.warmup, 3))
+    p.close()
+    p = lib.Problem(cd)
+    t0 = time.perf_counter()
+    _, m = p.run(n_primal)
+    t_primal = time.perf_counter() - t0
+    state = {n: p.get(n) for n, a in cd.arrays.items() if a.dtype == np.float32}
+    integ = p.integrals()
+    t0 = time.perf_counter()
+    sens = ds.sensitivities(alpha)
+    g64 = ds.geometry64(alpha)
+    t_sens = time.perf_counter() - t0
+    grads, solves = {}, {}
+    t_adj = 0.0
+    d2h = 0
+    with ClockSampler(0) as clk:
+        for obj in ("eta_tt", "mass_flow_in"):
+            t0 = time.perf_counter()
+            p.adjoint_prepare()
+            val = p.adjoint_objective(obj)
+            ok, steps, res = p.adjoint_solve_krylov(inner=inner, restart=restart, max_steps=max_steps, tol=1e-6)
+            gd = p.adjoint_gradient()
+            t_adj += time.perf_counter() - t0
+            d2h += sum(a.nbytes for a in gd.values())
+            grads[obj] = ds.chain(gd, sens)
+            solves[obj] = {"value": val, "converged": ok, "transposed_steps": steps, "rel_residual": res}
+    # finite differences: restarts of the primal (LOSS on) from the converged
+    # state with the geometry moved by +-h
+    h = 0.2
+    checks = []
+    t_fd_one = None
+    for i in (ds.index(1, "stagger", 2), ds.index(0, "stagger", 0)):
+        js = []
+        for sgn in (1.0, -1.0):
+            a = alpha.copy()
+            a[i] += sgn * h
+            gp = ds.geometry64(a)
+            cdp = design.perturbed_state(cd, state, {n: gp[n] - g64[n] for n in design.GEOM})
+            cdp.ints["NSTEP"] = cd.ints["NCHANGE"] - 1
+            pp = lib.Problem(cdp, setup_calls=False)
+            t0 = time.perf_counter()
+            pp.run(n_fd)
+            dt = time.perf_counter() - t0
+            t_fd_one = dt if t_fd_one is None else min(t_fd_one, dt)
+            r = pp.integrals()
+            js.append((r.eta_tt, r.mass_flow_in))
+            pp.close()
+        checks.append({"variable": ds.names()[i],
+                       "eta_tt": {"adjoint": float(grads["eta_tt"][i]), "fd": (js[0][0] - js[1][0]) / (2 * h)},
+                       "mass_flow_in": {"adjoint": float(grads["mass_flow_in"][i]),
+                                        "fd": (js[0][1] - js[1][1]) / (2 * h)}})
+    t_fd = 2 * ds.size * t_fd_one
+    t_adj_total = t_adj + t_sens
+    steps_total = sum(v["transposed_steps"] for v in solves.values()) + 2 * 2
+    line = {
+        "metric": "FD / adjoint gradient time", "value": t_fd / t_adj_total, "unit": "x", "n_gpus": world,
+        "steps": steps_total, "warmup": max(args.warmup, 3), "ms_per_step": t_adj / max(steps_total, 1) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOADS["adjoint"][1], "nodes": cd.nodes(), "design_variables": ds.size,
+                   "objectives": ["eta_tt", "mass_flow_in"], "primal_steps": n_primal,
+                   "krylov": {"inner": inner, "restart": restart, "max_steps": max_steps},
+                   "fd": {"h_deg": h, "steps_per_solve": n_fd, "solves": 2 * ds.size}},
+        "adjoint_time_s": t_adj_total, "adjoint_device_s": t_adj, "sensitivities_host_s": t_sens,
+        "primal_solve_s": t_primal, "adjoint_over_primal": t_adj_total / t_primal,
+        "fd_gradient_time_s": t_fd, "fd_solve_s": t_fd_one,
+        "primal": {"eavg": float(m.eavg), "eta_tt": integ.eta_tt, "mass_flow_in": integ.mass_flow_in},
+        "solves": solves, "checks": checks,
+        "cpu_baseline": None, "clocks": clk.summary(),
+        "e2e": {"value": t_fd / t_adj_total, "unit": "x", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": d2h / max(steps_total, 1),
+                "how": "mgpu_adjoint_* through the C ABI; geometry gradients read back to the host for the chain"},
+        "gpu_launches": ADJ_KERNELS_PER_STEP * steps_total,
+    }
+    print(json.dumps(line), flush=True)
+    p.close()
+    return 0
+
+
 def run_gpu(args, rank, world, local_rank):
     if world > 1:
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local_rank)
@@ -425,6 +538,8 @@ def main():
         return run_reference(args, rank, world)
     if args.workload == "batch64":
         return run_batch(args, rank, world, local_rank)
+    if args.workload == "adjoint":
+        return run_adjoint(args, rank, world, local_rank)
     return run_gpu(args, rank, world, local_rank)
 
 

@@ -224,8 +224,9 @@ int32_t mgpu_batch_bench_steps(mgpu_batch *b, int32_t nsteps, int32_t flush_l2, 
  * and dJ/dA = dJ/dA|_U + lambda^T dG/dA.  Covered: SCREE without residual
  * smoothing, IPOUT = 0, IN_PRESS = 0, IN_VTAN = 0, IN_VR <= 0, mixing planes
  * with subsonic relative flow at JMIX+2; other options return
- * MGPU_E_UNSUPPORTED, as does a linearisation state at which a density or
- * Mach limiter changes the flow. */
+ * MGPU_E_UNSUPPORTED.  Where the density or Mach limiter acts in the
+ * recorded step it is differentiated with the rows' limits (VLIMIT,
+ * ROLIMIT) held. */
 
 /* Records one step from the current state (the linearisation point),
  * restores the state, and resets the adjoint to zero. */
@@ -242,6 +243,17 @@ int32_t mgpu_adjoint_iterate(mgpu_handle *h, int32_t n, double *rel_change);
 /* Iterates until the relative change falls below tol or max_iters
  * iterations are done; returns 0 if converged, 1 if not. */
 int32_t mgpu_adjoint_solve(mgpu_handle *h, int32_t max_iters, double tol, int32_t *iters, double *rel_change);
+/* The same fixed point by restarted GMRES on the inner-step map,
+ * (I - ((dG/dU)^T)^inner) lambda = sum_{i<inner} ((dG/dU)^T)^i (dJ/dU)^T: the
+ * marching iteration acts as the preconditioner and GMRES removes the few
+ * slow or growing modes that stall it (a frozen step can have a slowly
+ * growing mode; the plain iteration then diverges).  Starts from the current
+ * lambda; restart = basis size (2-200); *steps = transposed steps used in
+ * all; *rel_residual = the preconditioned system's |b - A lambda| / |b|.
+ * Returns 0 if converged, 1 if not.  Holds (restart + 4) packed adjoint
+ * vectors (14 node arrays each) on the device. */
+int32_t mgpu_adjoint_solve_krylov(mgpu_handle *h, int32_t inner, int32_t restart, int32_t max_steps, double tol,
+                                  int32_t *steps, double *rel_residual);
 /* One more reverse step that also accumulates dJ/dA for the geometry
  * arrays AQX, AQR, ABX, ABR, ABT, ASX, ASR and VOLOR. */
 int32_t mgpu_adjoint_gradient(mgpu_handle *h);

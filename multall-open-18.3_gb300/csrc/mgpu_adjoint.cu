@@ -57,6 +57,11 @@ struct Adj {
     // ... and arrays as the step formed them
     const float *tVX, *tVR, *tVT, *tROVT, *tP, *tHO, *tPEFF, *tFLOWX, *tFLOWT, *tFLOWR;
     const float *tBCBUF, *tROIN, *tMIX;
+    // limiters: RO as each found it, WT of the step, the rows' limits, and
+    // the density limiter's linear coefficients lim(J) = C0 RO(J) + CA ROAVG
+    const float *tROL, *tROM, *tWT, *tVLIM, *tROLIM, *tDC0, *tDCA;
+    const int *tDCOL;
+    float *WT;                   // adjoint of WT (k_flux_mass), read by the Mach limiter
     const DevCtl *tctl;
     // geometry adjoints, accumulated when geom != 0
     float *gAQX, *gAQR, *gABX, *gABR, *gABT, *gASX, *gASR, *gVOLOR;
@@ -65,6 +70,7 @@ struct Adj {
     // objective seeds: node quantities (VX, VT, VR, HO, P) and cell FLOWX on
     // two J planes
     const float *seed;
+    const int *seed_on;          // 0: the plain transposed step (Krylov products)
     int seed_j[2];
 };
 
@@ -192,6 +198,16 @@ __global__ void rk_flux_mass(const __grid_constant__ Dev d, const __grid_constan
             }
         } else {
             rev_flowt_raw(d, a, i, j, k, g);
+        }
+    }
+    {
+        // WT = (ROVT - U RO) / RO
+        const float gw = a.WT[n];
+        if (gw != 0.0f) {
+            a.WT[n] = 0.0f;
+            const float ro = a.tRO[n];
+            aadd(&a.ROVT[n], gw / ro);
+            aadd(&a.v[V_RO].D[n], -gw * pre_rovt(d, a, i, j, k) / (ro * ro));
         }
     }
     if (i < d.IM && j >= 2) {
@@ -792,6 +808,90 @@ __global__ void __launch_bounds__(64) rk_mixplan(const __grid_constant__ Dev d, 
 }
 
 // =====================================================================
+// R10: the density limiter (k_density_fix) and the Mach limiter
+// (k_mach_limiter), with the limits VLIMIT/ROLIMIT of each row held at the
+// recorded step's values.  Where the density limiter acts,
+// lim(J) = C0(J) RO(J) + CA(J) ROAVG(J), ROAVG = (lim(J-2) + lim(J-1) +
+// RO(J+1) + RO(J+2)) / 4, J walked upwards; the coefficients come from a
+// replay of the recorded column (rk_density_prep).
+// =====================================================================
+__global__ void rk_density_prep(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.IM * d.KM) return;
+    const int i = t % d.IM + 1, k = t / d.IM + 1;
+    float *C0 = const_cast<float *>(a.tDC0), *CA = const_cast<float *>(a.tDCA);
+    int any = 0;
+    const float *RO = a.tROL;
+    float rm2 = A3(RO, i, 1, k), rm1 = A3(RO, i, 2, k), r0 = A3(RO, i, 3, k), rp1 = A3(RO, i, 4, k);
+    for (int j = 3; j <= d.JM - 3; ++j) {
+        const float rp2 = A3(RO, i, j + 2, k);
+        const float ROAVG = 0.25f * (rm2 + rm1 + rp1 + rp2);
+        float ro = r0, c0 = 1.0f, ca = 0.0f;
+        if (ro < 0.6f * ROAVG) { ro = 0.5f * (ro + 0.6f * ROAVG); c0 *= 0.5f; ca = 0.5f * ca + 0.3f; }
+        if (ro > 1.5f * ROAVG) { ro = 0.5f * (ro + 1.5f * ROAVG); c0 *= 0.5f; ca = 0.5f * ca + 0.75f; }
+        if (ro < d.ROLIM) { ro = 0.5f * (ro + d.ROLIM); c0 *= 0.5f; ca *= 0.5f; }
+        if (c0 != 1.0f) any = 1;
+        A3(C0, i, j, k) = c0;
+        A3(CA, i, j, k) = ca;
+        rm2 = rm1;
+        rm1 = ro;
+        r0 = rp1;
+        rp1 = rp2;
+    }
+    const_cast<int *>(a.tDCOL)[t] = any;
+}
+
+__global__ void rk_density(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.IM * d.KM || !a.tDCOL[t]) return;
+    const int i = t % d.IM + 1, k = t / d.IM + 1;
+    float *aRO = a.v[V_RO].D;
+    for (int j = d.JM - 3; j >= 3; --j) {
+        const float g = A3(aRO, i, j, k);
+        A3(aRO, i, j, k) = A3(a.tDC0, i, j, k) * g;
+        const float q = 0.25f * A3(a.tDCA, i, j, k) * g;
+        if (q == 0.0f) continue;
+        A3(aRO, i, j - 1, k) += q;
+        A3(aRO, i, j - 2, k) += q;
+        A3(aRO, i, j + 1, k) += q;
+        A3(aRO, i, j + 2, k) += q;
+    }
+}
+
+__global__ void rk_mach(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, (size_t)n, i, j, k);
+    const int nr = A1(d.NROW, j);
+    const float VL = a.tVLIM[nr - 1], ROL = a.tROLIM[nr - 1];
+    const float ro_in = a.tROM[n];
+    const bool clamp = ro_in < ROL;
+    const float ro = clamp ? ROL : ro_in;
+    const float vx = a.tVX[n], vr = a.tVR[n], wt = a.tWT[n];
+    const float WRELSQ = vx * vx + vr * vr + wt * wt;
+    const float F = VL / sqrtf(WRELSQ);
+    float *aRO = a.v[V_RO].D;
+    if (F < 1.0f) {
+        const float gX = a.v[V_ROVX].D[n], gR = a.v[V_ROVR].D[n], gT = a.v[V_RORVT].D[n];
+        const float gROVT = a.ROVT[n] + gT * A2(d.R, j, k);
+        const float gro = aRO[n] + (gX * vx + gR * vr + gROVT * wt) * F + gROVT * A2(d.UBLADE, j, k);
+        const float gF = (gX * vx + gR * vr + gROVT * wt) * ro;
+        a.VX[n] += gX * ro * F - gF * F * vx / WRELSQ;
+        a.VR[n] += gR * ro * F - gF * F * vr / WRELSQ;
+        a.WT[n] += gROVT * ro * F - gF * F * wt / WRELSQ;
+        a.v[V_ROVX].D[n] = 0.0f;
+        a.v[V_ROVR].D[n] = 0.0f;
+        a.v[V_RORVT].D[n] = 0.0f;
+        a.ROVT[n] = 0.0f;
+        aRO[n] = clamp ? 0.0f : gro;
+    } else if (clamp) {
+        aRO[n] = 0.0f;
+    }
+}
+
+// =====================================================================
 // TSTEP, reversed: rk_ts_smooth (SMOOTH_VAR and the averaging fix-ups) ->
 // rk_ts_gather (corner gather, second mixing-plane average, negative
 // feedback) -> rk_ts_damp (the row-mean term of the negative feedback, the
@@ -1326,7 +1426,7 @@ __global__ void rk_seed(const __grid_constant__ Dev d, const __grid_constant__ A
     const int np = IM * KM, nc = d.IMM1 * d.KMM1;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int per = 5 * np + nc;
-    if (t >= 2 * per) return;
+    if (t >= 2 * per || !*a.seed_on) return;
     const int p = t / per, r = t % per;
     const int j = a.seed_j[p];
     const float s = a.seed[t];
@@ -1496,6 +1596,43 @@ __global__ void rk_norms(const __grid_constant__ Dev d, const __grid_constant__ 
     }
 }
 
+// Krylov vector kernels over packed adjoint vectors of length len
+// out[i] += V_i . w for i < nv (grid.y = i), FP64
+__global__ void rk_kdots(const float *V, int nv, const float *w, size_t len, double *out) {
+    __shared__ double sh[RT_BS / 32];
+    const int i = blockIdx.y;
+    const float *v = V + (size_t)i * len;
+    double s = 0.0;
+    for (size_t t = (size_t)blockIdx.x * RT_BS + threadIdx.x; t < len; t += (size_t)gridDim.x * RT_BS)
+        s += (double)v[t] * (double)w[t];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < RT_BS / 32; ++q) t += sh[q];
+        atomicAdd(&out[i], t);
+    }
+}
+// w += sign * sum_i c_i V_i
+__global__ void rk_kcomb(const float *V, int nv, const double *c, float sign, float *w, size_t len) {
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < len; t += (size_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int i = 0; i < nv; ++i) s += c[i] * (double)V[(size_t)i * len + t];
+        w[t] = (float)((double)w[t] + (double)sign * s);
+    }
+}
+// y = a x
+__global__ void rk_kscale(float a_, const float *x, float *y, size_t len) {
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < len; t += (size_t)gridDim.x * blockDim.x)
+        y[t] = a_ * x[t];
+}
+// y = a x + b y
+__global__ void rk_kaxpby(float a_, const float *x, float b_, float *y, size_t len) {
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < len; t += (size_t)gridDim.x * blockDim.x)
+        y[t] = a_ * x[t] + b_ * y[t];
+}
+
 struct AdjState {
     mgpu_handle *h = nullptr;
     Adj a;
@@ -1512,6 +1649,15 @@ struct AdjState {
     double value = 0.0;
     bool ready = false;
     int iters = 0;
+    int limiters = 0;            // bit 0: density, bit 1: Mach limiter active in the recorded step
+    int *seed_on = nullptr;
+    // restarted GMRES on (I - (dG/dU)^T) lambda = (dJ/dU)^T over the packed
+    // state adjoint (the arrays of state_segments())
+    float *kv = nullptr;         // (m + 1) basis vectors
+    float *kw = nullptr, *kb = nullptr, *kx = nullptr;
+    double *kdot = nullptr;      // (m + 2) FP64 dot products
+    int kcap = 0;
+    size_t klen = 0;
 };
 
 void adj_destroy(AdjState *s) {
@@ -1519,6 +1665,9 @@ void adj_destroy(AdjState *s) {
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
     if (s->graph) cudaGraphDestroy(s->graph);
     for (void *p : s->allocs) cudaFree(p);
+    void *kb[] = {s->kv, s->kw, s->kb, s->kx, s->kdot};
+    for (void *p : kb)
+        if (p) cudaFree(p);
     delete s;
 }
 
@@ -1572,6 +1721,8 @@ void enqueue_reverse(const Dev &d, const Adj &a, cudaStream_t s) {
     const int per = 5 * d.IM * d.KM + d.IMM1 * d.KMM1;
     rk_seed<<<gridn((size_t)2 * per, 256), 256, 0, s>>>(d, a);
     if (d.IFMIX > 0 && d.RFMIX > 1.0e-3f && d.NRWSM1 > 0) rk_mixplan<<<d.NRWSM1 * d.KM, 64, 0, s>>>(d, a);
+    rk_mach<<<gN, 256, 0, s>>>(d, a);
+    rk_density<<<gridn((size_t)d.IM * d.KM, 128), 128, 0, s>>>(d, a);
     launch_tstep_rev(d, a, s, V_ROVX, 3);
     rk_flux_mom<<<gN, 256, 0, s>>>(d, a);
     rk_peff<<<gN, 256, 0, s>>>(d, a);
@@ -1626,6 +1777,14 @@ int allocate(AdjState *s, const Dev &d) {
     Fc(&a.tVX, N); Fc(&a.tVR, N); Fc(&a.tVT, N); Fc(&a.tROVT, N); Fc(&a.tP, N); Fc(&a.tHO, N); Fc(&a.tPEFF, N);
     Fc(&a.tFLOWX, N); Fc(&a.tFLOWT, N); Fc(&a.tFLOWR, N);
     Fc(&a.tBCBUF, (size_t)4 * d.KM); Fc(&a.tROIN, np);
+    Fc(&a.tROL, N); Fc(&a.tROM, N); Fc(&a.tWT, N); Fc(&a.tDC0, N); Fc(&a.tDCA, N);
+    Fc(&a.tVLIM, d.NROWS); Fc(&a.tROLIM, d.NROWS);
+    {
+        int *q = nullptr;
+        if (!rc) rc = aalloc(s, &q, np);
+        a.tDCOL = q;
+    }
+    F(&a.WT, N);
     Fc(&a.tMIX, (size_t)(d.NRWSM1 > 0 ? d.NRWSM1 : 1) * d.KM * mix_rec_size(d.IM));
     F(&a.gAQX, N); F(&a.gAQR, N); F(&a.gABX, N); F(&a.gABR, N); F(&a.gASX, N); F(&a.gASR, N); F(&a.gVOLOR, N);
     F(&a.gABT, (size_t)d.JM * d.KM);
@@ -1635,6 +1794,8 @@ int allocate(AdjState *s, const Dev &d) {
     F(&s->seed, (size_t)2 * per);
     F(&s->prev, 5 * N);
     if (!rc) rc = aalloc(s, &s->norms, 2);
+    if (!rc) rc = aalloc(s, &s->seed_on, 1);
+    a.seed_on = s->seed_on;
     a.tctl = s->tctl;
     a.flag = s->flag;
     a.seed = s->seed;
@@ -1685,6 +1846,43 @@ float *geom_adj(AdjState *s, const Dev &d, const char *name, size_t *count) {
     return nullptr;
 }
 
+// the state adjoint as segments of a packed vector
+struct Seg {
+    float *p;
+    size_t n;
+};
+std::vector<Seg> state_segments(AdjState *s, const Dev &d) {
+    const size_t N = (size_t)d.IM * d.JM * d.KM;
+    Adj &a = s->a;
+    std::vector<Seg> v;
+    for (int q = 0; q < NVAR; ++q) v.push_back({a.v[q].D, N});
+    for (int q = 0; q < NVAR; ++q) v.push_back({a.v[q].DIFF, N});
+    v.push_back({a.PEFF, N});
+    v.push_back({a.P, N});
+    v.push_back({a.HO, N});
+    v.push_back({a.ROVT, N});
+    v.push_back({a.PD, (size_t)d.KM});
+    return v;
+}
+
+int pack(AdjState *s, const Dev &d, float *dst, cudaStream_t st) {
+    size_t o = 0;
+    for (const Seg &g : state_segments(s, d)) {
+        ACK(cudaMemcpyAsync(dst + o, g.p, g.n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        o += g.n;
+    }
+    return 0;
+}
+
+int unpack(AdjState *s, const Dev &d, const float *src, cudaStream_t st) {
+    size_t o = 0;
+    for (const Seg &g : state_segments(s, d)) {
+        ACK(cudaMemcpyAsync(g.p, src + o, g.n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        o += g.n;
+    }
+    return 0;
+}
+
 int zero_adjoints(AdjState *s, const Dev &d, cudaStream_t st) {
     const size_t N = (size_t)d.IM * d.JM * d.KM;
     Adj &a = s->a;
@@ -1694,7 +1892,7 @@ int zero_adjoints(AdjState *s, const Dev &d, cudaStream_t st) {
         for (float *p : z)
             if (p) ACK(cudaMemsetAsync(p, 0, N * sizeof(float), st));
     }
-    float *z[] = {a.P, a.HO, a.VX, a.VR, a.VT, a.ROVT, a.PEFF, a.FLOWX, a.FLOWT, a.FLOWR};
+    float *z[] = {a.P, a.HO, a.VX, a.VR, a.VT, a.ROVT, a.PEFF, a.FLOWX, a.FLOWT, a.FLOWR, a.WT};
     for (float *p : z) ACK(cudaMemsetAsync(p, 0, N * sizeof(float), st));
     float *zk[] = {a.PD, a.PDK, a.PAVG, a.SSUM};
     for (float *p : zk) ACK(cudaMemsetAsync(p, 0, (size_t)d.KM * sizeof(float), st));
@@ -1760,6 +1958,8 @@ int32_t mgpu_adjoint_prepare(mgpu_handle *h) {
     rec.ADJ_ROIN = const_cast<float *>(a.tROIN);
     rec.ADJ_MIX = const_cast<float *>(a.tMIX);
     rec.ADJ_FLAG = s->flag;
+    rec.ADJ_RO_LIM = const_cast<float *>(a.tROL);
+    rec.ADJ_RO_MACH = const_cast<float *>(a.tROM);
     ACK(cudaMemsetAsync(s->flag, 0, sizeof(int), st));
     Launch L{st, handle_sm_count(h)};
     launch_step_begin(rec, L);
@@ -1771,11 +1971,15 @@ int32_t mgpu_adjoint_prepare(mgpu_handle *h) {
     ACK(cp(a.tFLOWX, d.FLOWX, N)); ACK(cp(a.tFLOWT, d.FLOWT, N)); ACK(cp(a.tFLOWR, d.FLOWR, N));
     for (int v = 0; v < NVAR; ++v) ACK(cp(a.v[v].tST, d.var[v].ST, N));
     ACK(cp(a.tBCBUF, d.BCBUF, (size_t)4 * d.KM));
+    ACK(cp(a.tWT, d.WT, N));
+    ACK(cp(a.tVLIM, d.VLIMIT, (size_t)d.NROWS));
+    ACK(cp(a.tROLIM, d.ROLIMIT, (size_t)d.NROWS));
     ACK(cudaMemcpyAsync(s->tctl, d.ctl, sizeof(DevCtl), cudaMemcpyDeviceToDevice, st));
     // the EFICOOL sums of the step's arrays (the objectives' forward values)
     double *dint = handle_int_buf(h);
     launch_integrals(rec, L, dint);
     rk_blk<<<NVAR, RT_BS, 0, st>>>(d, a);
+    rk_density_prep<<<gridn(np, 128), 128, 0, st>>>(d, a);
     ACK(cudaGetLastError());
     s->sums.assign((size_t)4 * d.JM, 0.0);
     ACK(cudaMemcpyAsync(s->sums.data(), dint, s->sums.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1795,8 +1999,7 @@ int32_t mgpu_adjoint_prepare(mgpu_handle *h) {
     int flag = 0;
     ACK(cudaMemcpyAsync(&flag, s->flag, sizeof(int), cudaMemcpyDeviceToHost, st));
     ACK(cudaStreamSynchronize(st));
-    (void)np;
-    if (flag & 3) return api_fail(MGPU_E_UNSUPPORTED, "adjoint: a density or Mach limiter is active at the linearisation state");
+    s->limiters = flag & 3;
     ACK(cudaMemsetAsync(s->flag, 0, sizeof(int), st));
     if ((rc = zero_adjoints(s, d, st))) return rc;
     ACK(cudaMemsetAsync(s->seed, 0, (size_t)2 * (5 * d.IM * d.KM + d.IMM1 * d.KMM1) * sizeof(float), st));
@@ -1813,6 +2016,10 @@ int32_t mgpu_adjoint_prepare(mgpu_handle *h) {
     if (s->graph) {
         cudaGraphDestroy(s->graph);
         s->graph = nullptr;
+    }
+    {
+        const int one = 1;
+        ACK(cudaMemcpyAsync(s->seed_on, &one, sizeof(int), cudaMemcpyHostToDevice, st));
     }
     ACK(cudaStreamSynchronize(st));
     s->ready = true;
@@ -1953,6 +2160,142 @@ int32_t mgpu_adjoint_solve(mgpu_handle *h, int32_t max_iters, double tol, int32_
     if (iters) *iters = done;
     if (rel_change) *rel_change = rel;
     if (rc) return rc;
+    return rel < tol ? 0 : 1;
+}
+
+int32_t mgpu_adjoint_solve_krylov(mgpu_handle *h, int32_t inner, int32_t restart, int32_t max_steps, double tol,
+                                  int32_t *steps, double *rel_residual) {
+    AdjState *s = ready_state(h);
+    if (!s) return api_fail(MGPU_E_STATE, "adjoint solve before mgpu_adjoint_prepare");
+    if (inner < 1 || restart < 2 || restart > 200 || max_steps < 1 || !(tol > 0.0))
+        return api_fail(MGPU_E_ARG, "Krylov solve: inner >= 1, 2 <= restart <= 200, max_steps >= 1, tol > 0");
+    const Dev &d = handle_dev(h);
+    cudaStream_t st = handle_view(h).stream;
+    int rc = ensure_graph(s, d, st);
+    if (rc) return rc;
+    size_t len = 0;
+    for (const Seg &g : state_segments(s, d)) len += g.n;
+    if (s->kcap < restart + 1 || s->klen != len) {
+        if (s->kv) cudaFree(s->kv);
+        if (s->kw) cudaFree(s->kw);
+        if (s->kb) cudaFree(s->kb);
+        if (s->kx) cudaFree(s->kx);
+        if (s->kdot) cudaFree(s->kdot);
+        s->kv = s->kw = s->kb = s->kx = nullptr;
+        s->kdot = nullptr;
+        ACK(cudaMalloc(&s->kv, (size_t)(restart + 1) * len * sizeof(float)));
+        ACK(cudaMalloc(&s->kw, len * sizeof(float)));
+        ACK(cudaMalloc(&s->kb, len * sizeof(float)));
+        ACK(cudaMalloc(&s->kx, len * sizeof(float)));
+        ACK(cudaMalloc(&s->kdot, (size_t)(restart + 2) * sizeof(double)));
+        s->kcap = restart + 1;
+        s->klen = len;
+    }
+    const int sm = handle_sm_count(h);
+    const unsigned gb = (unsigned)(4 * sm);
+    auto seeds = [&](int on) { return cudaMemsetAsync(s->seed_on, on ? 1 : 0, sizeof(int), st); };
+    auto dots = [&](const float *V, int nv, const float *w, std::vector<double> &out) -> int {
+        ACK(cudaMemsetAsync(s->kdot, 0, (size_t)nv * sizeof(double), st));
+        rk_kdots<<<dim3(gb, nv), RT_BS, 0, st>>>(V, nv, w, len, s->kdot);
+        out.assign((size_t)nv, 0.0);
+        ACK(cudaMemcpyAsync(out.data(), s->kdot, (size_t)nv * sizeof(double), cudaMemcpyDeviceToHost, st));
+        ACK(cudaStreamSynchronize(st));
+        return 0;
+    };
+    auto comb = [&](const float *V, const std::vector<double> &c, float sign, float *w) -> int {
+        ACK(cudaMemcpyAsync(s->kdot, c.data(), c.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        rk_kcomb<<<gb, RT_BS, 0, st>>>(V, (int)c.size(), s->kdot, sign, w, len);
+        return 0;
+    };
+    // The operator is the inner-step map: out = x - ((dG/dU)^T)^inner x, and
+    // the right-hand side b = sum_{i < inner} ((dG/dU)^T)^i (dJ/dU)^T, the
+    // inner steps from lambda = 0; the fixed point is the adjoint's.
+    int nprod = 0;
+    auto apply = [&](const float *x, float *out) -> int {
+        int r = unpack(s, d, x, st);
+        if (r) return r;
+        ACK(seeds(0));
+        for (int q = 0; q < inner; ++q) ACK(cudaGraphLaunch(s->gexec, st));
+        r = pack(s, d, out, st);
+        if (r) return r;
+        rk_kaxpby<<<gb, RT_BS, 0, st>>>(1.0f, x, -1.0f, out, len);
+        nprod += inner;
+        return 0;
+    };
+    if ((rc = pack(s, d, s->kx, st))) return rc;          // initial guess: the current adjoint
+    ACK(cudaMemsetAsync(s->kw, 0, len * sizeof(float), st));
+    if ((rc = unpack(s, d, s->kw, st))) return rc;
+    ACK(seeds(1));
+    for (int q = 0; q < inner; ++q) ACK(cudaGraphLaunch(s->gexec, st));
+    nprod += inner;
+    if ((rc = pack(s, d, s->kb, st))) return rc;
+    std::vector<double> dd;
+    if ((rc = dots(s->kb, 1, s->kb, dd))) return rc;
+    const double bnorm = std::sqrt(dd[0]);
+    double rel = 0.0;
+    const int m = restart;
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
+    bool done = bnorm == 0.0;
+    while (!done && nprod < max_steps) {
+        // r = b - A x into v_0
+        float *v0 = s->kv;
+        if ((rc = apply(s->kx, v0))) return rc;
+        rk_kaxpby<<<gb, RT_BS, 0, st>>>(1.0f, s->kb, -1.0f, v0, len);
+        if ((rc = dots(v0, 1, v0, dd))) return rc;
+        const double beta = std::sqrt(dd[0]);
+        rel = beta / bnorm;
+        if (rel < tol) break;
+        rk_kscale<<<gb, RT_BS, 0, st>>>((float)(1.0 / beta), v0, v0, len);
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        int jdone = 0;
+        for (int j = 0; j < m && nprod < max_steps; ++j) {
+            float *vj = s->kv + (size_t)j * len, *w = s->kw;
+            if ((rc = apply(vj, w))) return rc;
+            std::vector<double> h1, h2;
+            if ((rc = dots(s->kv, j + 1, w, h1))) return rc;     // classical Gram-Schmidt, twice
+            if ((rc = comb(s->kv, h1, -1.0f, w))) return rc;
+            if ((rc = dots(s->kv, j + 1, w, h2))) return rc;
+            if ((rc = comb(s->kv, h2, -1.0f, w))) return rc;
+            if ((rc = dots(w, 1, w, dd))) return rc;
+            const double hn = std::sqrt(dd[0]);
+            for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = h1[i] + h2[i];
+            H[(size_t)(j + 1) * m + j] = hn;
+            if (hn > 0.0) rk_kscale<<<gb, RT_BS, 0, st>>>((float)(1.0 / hn), w, s->kv + (size_t)(j + 1) * len, len);
+            // Givens rotations of the Hessenberg column
+            for (int i = 0; i < j; ++i) {
+                const double a0 = H[(size_t)i * m + j], a1 = H[(size_t)(i + 1) * m + j];
+                H[(size_t)i * m + j] = cs[i] * a0 + sn[i] * a1;
+                H[(size_t)(i + 1) * m + j] = -sn[i] * a0 + cs[i] * a1;
+            }
+            const double a0 = H[(size_t)j * m + j], a1 = H[(size_t)(j + 1) * m + j];
+            const double r_ = std::sqrt(a0 * a0 + a1 * a1);
+            cs[j] = r_ > 0.0 ? a0 / r_ : 1.0;
+            sn[j] = r_ > 0.0 ? a1 / r_ : 0.0;
+            H[(size_t)j * m + j] = r_;
+            H[(size_t)(j + 1) * m + j] = 0.0;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            jdone = j + 1;
+            rel = std::fabs(g[j + 1]) / bnorm;
+            if (rel < tol || hn == 0.0) break;
+        }
+        // x += V y, H y = g
+        for (int i = jdone - 1; i >= 0; --i) {
+            double t = g[i];
+            for (int k = i + 1; k < jdone; ++k) t -= H[(size_t)i * m + k] * y[k];
+            y[i] = t / H[(size_t)i * m + i];
+        }
+        std::vector<double> yy(y.begin(), y.begin() + jdone);
+        if ((rc = comb(s->kv, yy, 1.0f, s->kx))) return rc;
+        if (rel < tol) done = true;
+    }
+    if ((rc = unpack(s, d, s->kx, st))) return rc;
+    ACK(seeds(1));
+    ACK(cudaStreamSynchronize(st));
+    s->iters += nprod;
+    if (steps) *steps = nprod;
+    if (rel_residual) *rel_residual = rel;
     return rel < tol ? 0 : 1;
 }
 

@@ -774,6 +774,7 @@ __global__ void k_density_detect(Dev d) {
     size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t N = (size_t)d.IM * d.JM * d.KM;
     if (n >= N) return;
+    if (d.ADJ_RO_LIM) d.ADJ_RO_LIM[n] = d.RO[n];
     int i, j, k;
     node_ijk(d, n, i, j, k);
     if (j < 3 || j > d.JM - 3) return;
@@ -841,6 +842,7 @@ __global__ void k_mach_limiter(Dev d) {
     int nr = A1(d.NROW, j);
     float V_LIMIT = A1(d.VLIMIT, nr), RO_LIMIT = A1(d.ROLIMIT, nr);
     float ro = d.RO[n];
+    if (d.ADJ_RO_MACH) d.ADJ_RO_MACH[n] = ro;
     if (ro < RO_LIMIT) {
         ro = RO_LIMIT;
         d.RO[n] = ro;

@@ -112,6 +112,8 @@ struct Dev {
     float *ADJ_ROIN;
     float *ADJ_MIX;
     int *ADJ_FLAG;
+    float *ADJ_RO_LIM;     // RO as the density limiter finds it
+    float *ADJ_RO_MACH;    // RO as the Mach limiter finds it
     double *BLADE_FLOW;                // (JM)
     // per-block reduction partials of the 5-step tail
     double *part_sum;

@@ -62,6 +62,12 @@ class RowSpec:
     n_wake: int = 0         # N_WAKE: points into the wake
     sep_thik: float = 0.0   # SEP_THIK: fraction of the blade thickness
     sep_drag: float = 1.0   # SEP_DRAG: momentum factor in the separated region
+    # design offsets (degrees) at the nsect span sections, interpolated across
+    # the span like the noise: inlet and exit metal angle (pivot at the
+    # leading edge) and stagger (all metal angles, pivot at mid-chord)
+    d_in: tuple = ()
+    d_out: tuple = ()
+    d_stag: tuple = ()
 
 
 @dataclasses.dataclass
@@ -212,7 +218,7 @@ class CaseGeometry:
     fthick: np.ndarray     # FTHICK(NR,K)  (NROWS, KM)
 
 
-def build_geometry(spec: CaseSpec) -> CaseGeometry:
+def build_geometry(spec: CaseSpec, dtype=f32) -> CaseGeometry:
     im, km = spec.im, spec.km
     rng = np.random.default_rng(spec.seed)
     nrows = len(spec.rows)
@@ -247,15 +253,30 @@ def build_geometry(spec: CaseSpec) -> CaseGeometry:
         sec_span = np.linspace(0.0, 1.0, row.nsect)
         n_in = rng.normal(0.0, row.noise_deg, row.nsect)
         n_out = rng.normal(0.0, row.noise_deg, row.nsect)
+        zero = np.zeros(row.nsect)
+        d_in = np.asarray(row.d_in, np.float64) if len(row.d_in) else zero
+        d_out = np.asarray(row.d_out, np.float64) if len(row.d_out) else zero
+        d_stag = np.asarray(row.d_stag, np.float64) if len(row.d_stag) else zero
+        jmid = (row.jle + row.jte) // 2 - 1
+
+        def camber(ch):
+            # r*theta of the camber line: integrate tan(chi) dx (trapezoids)
+            tanc = np.tan(ch)
+            rt = np.concatenate([[0.0], np.cumsum(0.5 * (tanc[1:] + tanc[:-1]) * np.diff(xr))])
+            return rt - rt[row.jle - 1]
+
         for k in range(km):
-            chi1 = math.radians(row.chi_in + np.interp(frs[k], sec_span, n_in))
-            chi2 = math.radians(row.chi_out + np.interp(frs[k], sec_span, n_out))
+            chi1 = math.radians(row.chi_in + np.interp(frs[k], sec_span, n_in + d_in))
+            chi2 = math.radians(row.chi_out + np.interp(frs[k], sec_span, n_out + d_out))
+            stag = math.radians(float(np.interp(frs[k], sec_span, d_stag)))
             s = np.clip((xr - x_le) / (x_te - x_le), 0.0, 1.0)
             chi = chi1 + (chi2 - chi1) * s
-            # r*theta of the camber line: integrate tan(chi) dx (trapezoids)
-            tanc = np.tan(chi)
-            rtc = np.concatenate([[0.0], np.cumsum(0.5 * (tanc[1:] + tanc[:-1]) * np.diff(xr))])
-            rtc -= rtc[row.jle - 1]
+            rtc = camber(chi)
+            if stag != 0.0:
+                # the section turned by the stagger offset about its mid-chord point
+                rts = camber(chi + stag)
+                rtc = rts - (rts[jmid] - rtc[jmid])
+                chi = chi + stag
             t = np.zeros_like(xr)
             on = (np.arange(row.jm) >= row.jle - 1) & (np.arange(row.jm) <= row.jte - 1)
             t[on] = row.chord * thickness(s[on], row) / np.cos(chi[on])
@@ -282,8 +303,8 @@ def build_geometry(spec: CaseSpec) -> CaseGeometry:
     r = rh + frs[:, None] * (rc - rh)
     rt_upp = rt_c + 0.5 * thick
     return CaseGeometry(spec=spec, im=im, jm=jm, km=km,
-                        x=x.astype(f32), r=r.astype(f32), rt_upp=rt_upp.astype(f32),
-                        rt_thick=thick.astype(f32), fp=fp, fr=fr,
+                        x=x.astype(dtype), r=r.astype(dtype), rt_upp=rt_upp.astype(dtype),
+                        rt_thick=thick.astype(dtype), fp=fp, fr=fr,
                         row_first_j=first_j, ktips=ktips, ktipe=ktipe,
                         fthick=fthick.astype(f32))
 

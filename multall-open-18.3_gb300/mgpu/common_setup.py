@@ -46,9 +46,13 @@ def _intp(n, xs, ys, x):
     return float(np.interp(x, xs[:n], ys[:n]))
 
 
-def build_common(spec: CaseSpec, geo: CaseGeometry | None = None) -> CommonData:
+def build_common(spec: CaseSpec, geo: CaseGeometry | None = None, metrics64: bool = False,
+                 metrics_only: bool = False) -> CommonData:
+    """The COMMON state SETUP leaves for the loop.  metrics64: also keep the
+    face areas and volumes computed in double precision in cd.geom64;
+    metrics_only: stop there (cd holds only geom64)."""
     if geo is None:
-        geo = build_geometry(spec)
+        geo = build_geometry(spec, dtype=np.float64 if metrics64 else f32)
     IM, JM, KM = geo.im, geo.jm, geo.km
     NROWS = len(spec.rows)
     IMM1, JMM1, KMM1, IMM2, KMM2 = IM - 1, JM - 1, KM - 1, IM - 2, KM - 2
@@ -198,101 +202,102 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None) -> CommonData:
     FACUP[1] = 2.0
     FACDWN[JM - 1] = 2.0
 
-    X = geo.x.astype(f32)            # (KM, JM)
-    R = geo.r.astype(f32)
-    RT_UPP = geo.rt_upp.astype(f32).copy()
-    RT_THICK = geo.rt_thick.astype(f32).copy()
+    dt = np.float64 if metrics64 else f32
+    X = geo.x.astype(dt)            # (KM, JM)
+    R = geo.r.astype(dt)
+    RT_UPP = geo.rt_upp.astype(dt).copy()
+    RT_THICK = geo.rt_thick.astype(dt).copy()
     # align the blades circumferentially across mixing planes, 3022
-    SHIFT = f32(0.0)
+    SHIFT = dt(0.0)
     for J in range(3, JM + 1):
         if INDMIX[J - 1] == 1:
-            SHIFT = f32((RT_UPP[KMID - 1, J - 2] - RT_UPP[KMID - 1, J - 1]) / R[KMID - 1, J - 1])
-        RT_UPP[:, J - 1] = (RT_UPP[:, J - 1] + SHIFT * R[:, J - 1]).astype(f32)
+            SHIFT = dt((RT_UPP[KMID - 1, J - 2] - RT_UPP[KMID - 1, J - 1]) / R[KMID - 1, J - 1])
+        RT_UPP[:, J - 1] = (RT_UPP[:, J - 1] + SHIFT * R[:, J - 1]).astype(dt)
     # pinched-tip thickness scaling, 2506
     for J in range(1, JM + 1):
         nr = NROW[J]
-        rtmid = RT_UPP[:, J - 1] - f32(0.5) * RT_THICK[:, J - 1]
+        rtmid = RT_UPP[:, J - 1] - dt(0.5) * RT_THICK[:, J - 1]
         thick = geo.fthick[nr - 1] * RT_THICK[:, J - 1]
-        RT_UPP[:, J - 1] = (rtmid + f32(0.5) * thick).astype(f32)
-        RT_THICK[:, J - 1] = thick.astype(f32)
-    CP, GA = f32(spec.cp), f32(spec.ga)
-    GA1 = f32(GA - f32(1.0))
-    FGA = f32(GA1 / GA)
-    RFGA = f32(f32(1.0) / FGA)
-    CV = f32(CP / GA)
-    RGAS = f32(CP - CV)
+        RT_UPP[:, J - 1] = (rtmid + dt(0.5) * thick).astype(dt)
+        RT_THICK[:, J - 1] = thick.astype(dt)
+    CP, GA = dt(spec.cp), dt(spec.ga)
+    GA1 = dt(GA - dt(1.0))
+    FGA = dt(GA1 / GA)
+    RFGA = dt(dt(1.0) / FGA)
+    CV = dt(CP / GA)
+    RGAS = dt(CP - CV)
 
     # theta / r*theta of the grid nodes, 3000
-    NB = NBLADE[1:JM + 1].astype(f32)                     # per J
-    PITCH = (f32(2.0) * PI / NB).astype(f32)              # (JM,)
-    GAP = (PITCH[None, :] * R - RT_THICK).astype(f32)     # (KM, JM)
-    RTHETA = np.zeros((KM, JM, IM), f32)
+    NB = NBLADE[1:JM + 1].astype(dt)                     # per J
+    PITCH = (dt(2.0) * dt(PI) / NB).astype(dt)              # (JM,)
+    GAP = (PITCH[None, :] * R - RT_THICK).astype(dt)     # (KM, JM)
+    RTHETA = np.zeros((KM, JM, IM), dt)
     RTHETA[:, :, 0] = RT_UPP
     for i in range(2, IM + 1):
-        RTHETA[:, :, i - 1] = RTHETA[:, :, i - 2] + FP[i - 2] * GAP
-    THETA = (RTHETA / R[:, :, None]).astype(f32)
+        RTHETA[:, :, i - 1] = RTHETA[:, :, i - 2] + dt(FP[i - 2]) * GAP
+    THETA = (RTHETA / R[:, :, None]).astype(dt)
     # meridional distances 3530
-    SMERID = np.zeros((KM, JM), f32)
-    DR = np.zeros((KM, JM), f32)
-    DX = np.zeros((KM, JM), f32)
-    DS = np.zeros((KM, JM), f32)
+    SMERID = np.zeros((KM, JM), dt)
+    DR = np.zeros((KM, JM), dt)
+    DX = np.zeros((KM, JM), dt)
+    DS = np.zeros((KM, JM), dt)
     DR[:, 1:] = R[:, 1:] - R[:, :-1]
     DX[:, 1:] = X[:, 1:] - X[:, :-1]
     DS[:, 1:] = np.sqrt(DR[:, 1:] * DR[:, 1:] + DX[:, 1:] * DX[:, 1:])
     for J in range(2, JM + 1):
         SMERID[:, J - 1] = SMERID[:, J - 2] + DS[:, J - 1]
-    DSMIN = f32(DS[:, 1:].min())
+    DSMIN = dt(DS[:, 1:].min())
     DX[:, 0] = DX[:, 1]
     DS[:, 0] = DS[:, 1]
     DR[:, 0] = DR[:, 1]
-    CHORD = np.zeros(NROWS, f32)
+    CHORD = np.zeros(NROWS, dt)
     for nr in range(1, NROWS + 1):
         jl, jt = JLE[nr - 1], JTE[nr - 1]
         sch = SMERID[KMID - 1, jt - 1] - SMERID[KMID - 1, jl - 1]
         tch = RTHETA[KMID - 1, jl - 1, 0] - RTHETA[KMID - 1, jt - 1, 0]
         CHORD[nr - 1] = np.sqrt(sch * sch + tch * tch)
-    RAVG_CELL = np.zeros((KM, JM), f32)
-    RAVG_CELL[:KMM1, 1:] = f32(0.25) * (R[:KMM1, 1:] + R[:KMM1, :-1] + R[1:, :-1] + R[1:, 1:])
-    UBLADE = (WRAD[1:JM + 1][None, :] * R).astype(f32)
+    RAVG_CELL = np.zeros((KM, JM), dt)
+    RAVG_CELL[:KMM1, 1:] = dt(0.25) * (R[:KMM1, 1:] + R[:KMM1, :-1] + R[1:, :-1] + R[1:, 1:])
+    UBLADE = (WRAD[1:JM + 1][None, :].astype(dt) * R).astype(dt)
     # theta extrapolated onto the upstream side of each mixing plane, 3025
-    TEMP1 = np.zeros((KM, JM, IM), f32)
-    TEMP2 = np.zeros((KM, JM, IM), f32)
+    TEMP1 = np.zeros((KM, JM, IM), dt)
+    TEMP2 = np.zeros((KM, JM, IM), dt)
     for J in range(1, JM + 1):
         if INDMIX[J] != 1:
             continue
-        fac = (DS[:, J] / DS[:, J + 1]).astype(f32)          # DS(J+1)/DS(J+2)
+        fac = (DS[:, J] / DS[:, J + 1]).astype(dt)          # DS(J+1)/DS(J+2)
         TEMP1[:, J - 1, :] = THETA[:, J, :] + fac[:, None] * (THETA[:, J, :] - THETA[:, J + 1, :])
         TEMP2[:, J - 1, :] = R[:, J - 1][:, None] * TEMP1[:, J - 1, :]
 
     # ---------------- face areas and volumes, 3030-4045 -------------------
-    AQX = np.zeros((KM, JM, IM), f32)
-    AQR = np.zeros((KM, JM, IM), f32)
+    AQX = np.zeros((KM, JM, IM), dt)
+    AQR = np.zeros((KM, JM, IM), dt)
     X1 = (X[1:, :] - X[:-1, :])[:, :, None]
     R1 = (R[1:, :] - R[:-1, :])[:, :, None]
     Rk = R[:-1, :][:, :, None]
     Rkp = R[1:, :][:, :, None]
     T1 = Rkp * (THETA[1:, :, 1:] - THETA[:-1, :, :-1])
     T2 = Rkp * (THETA[1:, :, :-1] - THETA[:-1, :, :-1]) - Rk * (THETA[:-1, :, 1:] - THETA[:-1, :, :-1])
-    AQX[:KMM1, :, :IMM1] = f32(-0.5) * (R1 * T1 - R1 * T2)
-    AQR[:KMM1, :, :IMM1] = f32(-0.5) * (X1 * T2 - X1 * T1)
-    AQTOT = np.sqrt(AQX * AQX + AQR * AQR).astype(f32)
+    AQX[:KMM1, :, :IMM1] = dt(-0.5) * (R1 * T1 - R1 * T2)
+    AQR[:KMM1, :, :IMM1] = dt(-0.5) * (X1 * T2 - X1 * T1)
+    AQTOT = np.sqrt(AQX * AQX + AQR * AQR).astype(dt)
     AQX[KM - 1, :, :IMM1] = AQX[KMM1 - 1, :, :IMM1]
     AQR[KM - 1, :, :IMM1] = AQR[KMM1 - 1, :, :IMM1]
     AQX[:, :, IM - 1] = AQX[:, :, IMM1 - 1]
     AQR[:, :, IM - 1] = AQR[:, :, IMM1 - 1]
 
-    ABT = np.zeros((KM, JM), f32)
-    WRABT = np.zeros((KM, JM), f32)
-    ABX = np.zeros((KM, JM, IM), f32)
-    ABR = np.zeros((KM, JM, IM), f32)
-    ABTOT = np.zeros((KM, JM, IM), f32)
-    VOL = np.zeros((KM, JM, IM), f32)
+    ABT = np.zeros((KM, JM), dt)
+    WRABT = np.zeros((KM, JM), dt)
+    ABX = np.zeros((KM, JM, IM), dt)
+    ABR = np.zeros((KM, JM, IM), dt)
+    ABTOT = np.zeros((KM, JM, IM), dt)
+    VOL = np.zeros((KM, JM, IM), dt)
     bx1 = X[1:, :-1] - X[:-1, 1:]          # X(J-1,K+1)-X(J,K), (KMM1, JMM1) over J=2..JM
     bx2 = X[1:, 1:] - X[:-1, :-1]          # X(J,K+1)-X(J-1,K)
     br1 = R[1:, :-1] - R[:-1, 1:]
     br2 = R[1:, 1:] - R[:-1, :-1]
-    ABT[:KMM1, 1:] = f32(-0.5) * (bx1 * br2 - bx2 * br1)
-    WRABT[:KMM1, 1:] = (WRAD[2:JM + 1][None, :] * f32(0.25) *
+    ABT[:KMM1, 1:] = dt(-0.5) * (bx1 * br2 - bx2 * br1)
+    WRABT[:KMM1, 1:] = (WRAD[2:JM + 1][None, :].astype(dt) * dt(0.25) *
                         (R[:-1, 1:] + R[:-1, :-1] + R[1:, :-1] + R[1:, 1:]) * ABT[:KMM1, 1:])
     mixprev = np.array([INDMIX[J - 1] == 1 for J in range(2, JM + 1)])      # INDMIX(J-1), J=2..JM
     THm = np.where(mixprev[None, :, None], TEMP1[:, :-1, :], THETA[:, :-1, :])   # theta at J-1 (KM, JMM1, IM)
@@ -303,16 +308,16 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None) -> CommonData:
     th_jk = THETA[:-1, 1:, :]
     T1 = Rjm1_kp * (THm[1:, :, :] - th_jk)
     T2 = Rj_kp * (THETA[1:, 1:, :] - th_jk) - Rjm1_k * (THm[:-1, :, :] - th_jk)
-    ABX[:KMM1, 1:, :] = f32(-0.5) * (br1[:, :, None] * T2 - br2[:, :, None] * T1)
-    ABR[:KMM1, 1:, :] = f32(-0.5) * (bx2[:, :, None] * T1 - bx1[:, :, None] * T2)
+    ABX[:KMM1, 1:, :] = dt(-0.5) * (br1[:, :, None] * T2 - br2[:, :, None] * T1)
+    ABR[:KMM1, 1:, :] = dt(-0.5) * (bx2[:, :, None] * T1 - bx1[:, :, None] * T2)
     ABTOT[:KMM1, 1:, :] = np.sqrt(ABX[:KMM1, 1:, :] ** 2 + ABR[:KMM1, 1:, :] ** 2 +
                                   ABT[:KMM1, 1:, None] ** 2)
-    VOL[:KMM1, 1:, :IMM1] = ABT[:KMM1, 1:, None] * f32(0.25) * (
+    VOL[:KMM1, 1:, :IMM1] = ABT[:KMM1, 1:, None] * dt(0.25) * (
         RTHETA[:-1, 1:, 1:] + RTm[:-1, :, 1:] + RTm[1:, :, 1:] + RTHETA[1:, 1:, 1:]
         - RTHETA[:-1, 1:, :-1] - RTm[:-1, :, :-1] - RTm[1:, :, :-1] - RTHETA[1:, 1:, :-1])
 
-    ASX = np.zeros((KM, JM, IM), f32)
-    ASR = np.zeros((KM, JM, IM), f32)
+    ASX = np.zeros((KM, JM, IM), dt)
+    ASR = np.zeros((KM, JM, IM), dt)
     sx1 = (X[:, :-1] - X[:, 1:])[:, :, None]           # X(J-1,K)-X(J,K)
     sr1 = (R[:, :-1] - R[:, 1:])[:, :, None]
     Rjm1 = R[:, :-1][:, :, None]
@@ -320,13 +325,26 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None) -> CommonData:
     th = THETA[:, 1:, :-1]                              # THETA(I,J,K)
     T1 = Rjm1 * (THm[:, :, :-1] - th) - Rj * (THETA[:, 1:, 1:] - th)
     T2 = Rjm1 * (THm[:, :, 1:] - th)
-    ASX[:, 1:, :IMM1] = f32(0.5) * (sr1 * T2 - sr1 * T1)
-    ASR[:, 1:, :IMM1] = f32(0.5) * (sx1 * T1 - sx1 * T2)
+    ASX[:, 1:, :IMM1] = dt(0.5) * (sr1 * T2 - sr1 * T1)
+    ASR[:, 1:, :IMM1] = dt(0.5) * (sx1 * T1 - sx1 * T2)
 
-    VOLOR = np.zeros((KM, JM, IM), f32)
+    VOLOR = np.zeros((KM, JM, IM), dt)
     RAREA = (ABR[:KMM1, 1:, :IMM1] - ABR[:KMM1, 1:, 1:] + AQR[:KMM1, 1:, :IMM1] - AQR[:KMM1, :-1, :IMM1]
              + ASR[:KMM1, 1:, :IMM1] - ASR[1:, 1:, :IMM1])
-    VOLOR[:KMM1, 1:, :IMM1] = f32(-0.125) * RAREA
+    VOLOR[:KMM1, 1:, :IMM1] = dt(-0.125) * RAREA
+    if metrics64:
+        # the face areas and volumes in double precision (geometry
+        # sensitivities); the deck itself continues in REAL*4
+        cd.geom64 = dict(AQX=AQX.copy(), AQR=AQR.copy(), ABX=ABX.copy(), ABR=ABR.copy(), ABT=ABT.copy(),
+                         ASX=ASX.copy(), ASR=ASR.copy(), VOLOR=VOLOR.copy(), VOL=VOL.copy())
+        if metrics_only:
+            return cd
+        (X, R, RT_UPP, RT_THICK, RTHETA, THETA, SMERID, DR, DX, DS, RAVG_CELL, UBLADE, AQX, AQR, AQTOT, ABT, WRABT,
+         ABX, ABR, ABTOT, VOL, ASX, ASR, VOLOR, CHORD, GA1, FGA, RFGA, CV, RGAS, CP, GA, DSMIN) = (
+            np.asarray(v).astype(f32) if isinstance(v, np.ndarray) else f32(v)
+            for v in (X, R, RT_UPP, RT_THICK, RTHETA, THETA, SMERID, DR, DX, DS, RAVG_CELL, UBLADE, AQX, AQR,
+                      AQTOT, ABT, WRABT, ABX, ABR, ABTOT, VOL, ASX, ASR, VOLOR, CHORD, GA1, FGA, RFGA, CV, RGAS,
+                      CP, GA, DSMIN))
 
     # ---------------- initial guess, 3211-3500 -----------------------------
     PD = np.zeros(KM, f32)

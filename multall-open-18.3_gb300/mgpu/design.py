@@ -1,0 +1,107 @@
+"""Blade-angle design variables and the chain from the adjoint's geometry
+gradients to them.
+
+The design variables are offsets, in degrees, of the stagger and of the
+inlet and exit metal angles at `nsect` equispaced span sections of every
+blade row (30 for the two-row stage at 5 sections), applied on top of
+seeded base offsets drawn uniformly in +-1 degree.  They change the blade
+surfaces, hence the node angles THETA and through them the face areas and
+volumes that the time step reads: AQX, AQR, ABX, ABR, ASX, ASR, VOLOR (ABT,
+a meridional area, does not depend on them).
+
+mgpu_adjoint_gradient returns dJ/dA for those arrays.  The derivatives
+dA/d(alpha) of the host-side geometry generator are central differences of
+the double-precision metrics (`build_common(..., metrics64=True)`), and
+dJ/d(alpha_i) = sum over A of dJ/dA . dA/d(alpha_i).  Everything the
+frozen step holds fixed (time steps, body forces, smoothing and corner
+weights) is held at the base deck's values in the finite-difference checks
+as well.
+"""
+from __future__ import annotations
+
+import copy
+import dataclasses
+from typing import Callable, Dict, List
+
+import numpy as np
+
+from . import case as _case
+from . import common_setup as _cs
+
+KINDS = ("stagger", "inlet", "exit")
+GEOM = ("AQX", "AQR", "ABX", "ABR", "ABT", "ASX", "ASR", "VOLOR")
+
+
+@dataclasses.dataclass
+class DesignSpace:
+    make_spec: Callable[[], _case.CaseSpec]
+    alpha0: np.ndarray            # base offsets, degrees
+    nrows: int
+    nsect: int
+
+    @classmethod
+    def seeded(cls, make_spec, seed: int = 2, nsect: int = 5) -> "DesignSpace":
+        spec = make_spec()
+        nrows = len(spec.rows)
+        rng = np.random.default_rng(seed)
+        alpha0 = rng.uniform(-1.0, 1.0, nrows * len(KINDS) * nsect)
+        return cls(make_spec=make_spec, alpha0=alpha0, nrows=nrows, nsect=nsect)
+
+    @property
+    def size(self) -> int:
+        return self.nrows * len(KINDS) * self.nsect
+
+    def index(self, row: int, kind: str, sect: int) -> int:
+        return (row * len(KINDS) + KINDS.index(kind)) * self.nsect + sect
+
+    def names(self) -> List[str]:
+        return [f"row{r + 1}_{k}_s{s + 1}" for r in range(self.nrows) for k in KINDS for s in range(self.nsect)]
+
+    def spec(self, alpha: np.ndarray) -> _case.CaseSpec:
+        spec = self.make_spec()
+        a = np.asarray(alpha, np.float64).reshape(self.nrows, len(KINDS), self.nsect)
+        for r, row in enumerate(spec.rows):
+            row.nsect = self.nsect
+            row.d_stag = tuple(a[r, 0])
+            row.d_in = tuple(a[r, 1])
+            row.d_out = tuple(a[r, 2])
+        return spec
+
+    def deck(self, alpha: np.ndarray) -> _cs.CommonData:
+        """The REAL*4 COMMON deck of the design alpha."""
+        return _cs.build_common(self.spec(alpha))
+
+    def geometry64(self, alpha: np.ndarray) -> Dict[str, np.ndarray]:
+        return _cs.build_common(self.spec(alpha), metrics64=True, metrics_only=True).geom64
+
+    def sensitivities(self, alpha: np.ndarray, h: float = 1e-3) -> List[Dict[str, np.ndarray]]:
+        """dA/d(alpha_i) per design variable (per degree), central differences
+        of the double-precision metrics."""
+        out = []
+        for i in range(self.size):
+            e = np.zeros(self.size)
+            e[i] = h
+            gp, gm = self.geometry64(alpha + e), self.geometry64(alpha - e)
+            out.append({n: (gp[n] - gm[n]) / (2.0 * h) for n in GEOM})
+        return out
+
+    @staticmethod
+    def chain(dJdA: Dict[str, np.ndarray], sens: List[Dict[str, np.ndarray]]) -> np.ndarray:
+        """dJ/d(alpha) from the geometry gradients."""
+        return np.array([sum(float(np.sum(dJdA[n].astype(np.float64) * s[n])) for n in GEOM) for s in sens])
+
+
+def perturbed_state(base: _cs.CommonData, state: Dict[str, np.ndarray], delta64: Dict[str, np.ndarray]):
+    """The finite-difference check's restart: the converged state and every
+    frozen array of `state` (arrays read back from the converged problem),
+    with the face areas and volumes moved by the double-precision geometry
+    change delta64 (rounded to REAL*4 once, on the sum)."""
+    cd = copy.copy(base)
+    cd.arrays = dict(base.arrays)
+    cd.ints = dict(base.ints)
+    cd.reals = dict(base.reals)
+    for n, a in state.items():
+        cd.arrays[n] = a
+    for n in GEOM:
+        cd.arrays[n] = (state.get(n, base.arrays[n]).astype(np.float64) + delta64[n]).astype(np.float32)
+    return cd

@@ -45,7 +45,7 @@ EXPORTS = ["mgpu_abi_version", "mgpu_last_error", "mgpu_device_count", "mgpu_cre
            "mgpu_step_io_bytes", "mgpu_integrals_noalloc", "mgpu_batch_create", "mgpu_batch_destroy",
            "mgpu_batch_run", "mgpu_batch_bench_steps", "mgpu_adjoint_prepare", "mgpu_adjoint_objective",
            "mgpu_adjoint_iterate", "mgpu_adjoint_solve", "mgpu_adjoint_gradient", "mgpu_adjoint_get",
-           "mgpu_adjoint_set"]
+           "mgpu_adjoint_set", "mgpu_adjoint_solve_krylov"]
 
 _lib = None
 
@@ -94,6 +94,7 @@ def load(build: bool = True):
     L.mgpu_adjoint_iterate.argtypes = [vp, i32, dp]
     L.mgpu_adjoint_solve.argtypes = [vp, i32, ctypes.c_double, ctypes.POINTER(i32), dp]
     L.mgpu_adjoint_gradient.argtypes = [vp]
+    L.mgpu_adjoint_solve_krylov.argtypes = [vp, i32, i32, i32, ctypes.c_double, ctypes.POINTER(i32), dp]
     L.mgpu_adjoint_get.argtypes = [vp, cp, vp, ctypes.c_int64]
     L.mgpu_adjoint_set.argtypes = [vp, cp, vp, ctypes.c_int64]
     for f in EXPORTS:
@@ -257,6 +258,14 @@ class Problem:
         """(converged, iterations, last relative change)."""
         it, r = ctypes.c_int32(), ctypes.c_double()
         rc = _chk(load().mgpu_adjoint_solve(self.h, int(max_iters), float(tol), ctypes.byref(it), ctypes.byref(r)))
+        return rc == 0, it.value, r.value
+
+    def adjoint_solve_krylov(self, inner: int = 40, restart: int = 30, max_steps: int = 20000, tol: float = 1e-6):
+        """(converged, transposed steps used, relative residual) of GMRES on
+        the inner-step map."""
+        it, r = ctypes.c_int32(), ctypes.c_double()
+        rc = _chk(load().mgpu_adjoint_solve_krylov(self.h, int(inner), int(restart), int(max_steps), float(tol),
+                                                   ctypes.byref(it), ctypes.byref(r)))
         return rc == 0, it.value, r.value
 
     def adjoint_gradient(self) -> dict:

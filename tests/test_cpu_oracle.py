@@ -224,3 +224,34 @@ def test_oracle_reverse_mode_matches_finite_differences(mods):
         out.append({n: od.get(n) for n in names})
     lhs = sum(float(np.sum(w[n] * (out[0][n] - out[1][n]))) for n in names) / (2 * eps)
     assert abs(lhs - rhs) <= 1e-7 * abs(rhs), (lhs, rhs)
+
+
+def test_design_space_and_geometry_sensitivities(mods):
+    """The 30 blade-angle design variables of the adjoint configuration:
+    the double-precision metrics agree with the REAL*4 deck, a zero offset
+    leaves the deck bitwise unchanged, every variable moves the blade-wise
+    areas of its own row only, and the chain rule is linear."""
+    case, common_setup, O = mods
+    from mgpu import design
+    ds = design.DesignSpace.seeded(case.small_stage)
+    assert ds.size == 30 and len(ds.names()) == 30
+    base = common_setup.build_common(case.small_stage())
+    zero = common_setup.build_common(ds.spec(np.zeros(ds.size)))
+    for n in ("AQX", "ABX", "VOLOR", "RO", "STEP"):
+        assert np.array_equal(base.arrays[n], zero.arrays[n]), n
+    cd = ds.deck(ds.alpha0)
+    g64 = ds.geometry64(ds.alpha0)
+    for n in ("AQX", "ABX", "ABR", "VOLOR"):
+        scale = np.abs(g64[n]).max()
+        assert np.abs(cd.arrays[n] - g64[n]).max() <= 1e-5 * scale, n
+    sens = ds.sensitivities(ds.alpha0)
+    j_row2 = int(cd.arrays["JSTART"][1])
+    i_row1 = ds.index(0, "stagger", 2)
+    own = np.abs(sens[i_row1]["ABX"][:, :j_row2 - 2, :]).max()
+    assert own > 0.0
+    assert np.abs(sens[i_row1]["ABX"][:, j_row2 + 1:, :]).max() <= 1e-9 * own
+    rng = np.random.default_rng(0)
+    g1 = {n: rng.standard_normal(g64[n].shape) for n in design.GEOM}
+    g2 = {n: 2.0 * g1[n] for n in design.GEOM}
+    c1, c2 = ds.chain(g1, sens), ds.chain(g2, sens)
+    assert np.allclose(c2, 2.0 * c1)

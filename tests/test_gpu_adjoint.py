@@ -81,3 +81,90 @@ def test_transposed_step_matches_oracle_reverse(mods, which):
         worst[n] = rel_linf(got, ref)
     bad = {n: e for n, e in worst.items() if e > 1e-3}
     assert not bad, f"{which}: {bad} (all: {worst})"
+
+
+def _restart(cd, state, frozen=1):
+    """The converged problem restarted with LOSS and STEPUP held: NSTEP set
+    so that the first step re-forms the final smoothing ramp values."""
+    import copy
+    c = copy.copy(cd)
+    c.arrays, c.ints, c.reals = dict(cd.arrays), dict(cd.ints), dict(cd.reals)
+    c.arrays.update(state)
+    c.ints["NSTEP"] = cd.ints["NCHANGE"] - 1
+    c.ints["FROZEN"] = frozen
+    return c
+
+
+def _state(p, cd):
+    return {n: p.get(n) for n, a in cd.arrays.items() if a.dtype == np.float32}
+
+
+@pytest.fixture(scope="module")
+def converged_small_stage(mods):
+    """The small stage with SFXIN = SFTIN = 0.02 converged with LOSS (EAVG at
+    its FP32 floor, ~6e-6), then 2000 frozen steps."""
+    case, common_setup, lib, O = mods
+    from mgpu import design
+
+    def make():
+        sp = case.small_stage()
+        sp.sfxin = sp.sftin = 0.02
+        return sp
+
+    ds = design.DesignSpace.seeded(make)
+    cd = ds.deck(ds.alpha0)
+    cd.ints["NSTEPS_MAX"] = 10 ** 9
+    cd.reals["CONLIM"] = 1e-9
+    p = lib.Problem(cd)
+    p.run(3000)
+    st = _state(p, cd)
+    p.close()
+    cdf = _restart(cd, st)
+    pf = lib.Problem(cdf, setup_calls=False)
+    _, m = pf.run(2000)
+    assert m.eavg < 2e-5
+    return ds, cdf, pf, _state(pf, cdf)
+
+
+def test_adjoint_gradient_matches_frozen_finite_differences(mods, converged_small_stage):
+    """dJ/d(alpha) of eta_tt and of the inlet mass flow from the adjoint
+    (fixed-point iteration) against central differences of the frozen
+    primal restarted from the converged state with the perturbed geometry
+    (h = 0.2 degree, 3000 steps), for a stagger and an exit-angle variable
+    of each row: within 3 % (the finite differences' own noise), and the
+    GMRES solve gives the same gradient within 1 %."""
+    case, common_setup, lib, O = mods
+    from mgpu import design
+    ds, cdf, pf, stf = converged_small_stage
+    alpha = ds.alpha0
+    sens = ds.sensitivities(alpha)
+    g64 = ds.geometry64(alpha)
+    grads, kgrads = {}, {}
+    for obj in ("eta_tt", "mass_flow_in"):
+        pf.adjoint_prepare()
+        pf.adjoint_objective(obj)
+        for _ in range(8):
+            pf.adjoint_iterate(1000)
+        grads[obj] = ds.chain(pf.adjoint_gradient(), sens)
+        pf.adjoint_prepare()
+        pf.adjoint_objective(obj)
+        ok, steps, res = pf.adjoint_solve_krylov(inner=50, restart=30, max_steps=6000, tol=1e-6)
+        kgrads[obj] = ds.chain(pf.adjoint_gradient(), sens)
+    h = 0.2
+    for i in (ds.index(0, "stagger", 0), ds.index(0, "exit", 2), ds.index(1, "stagger", 2), ds.index(1, "exit", 2)):
+        js = []
+        for sgn in (1.0, -1.0):
+            a = alpha.copy()
+            a[i] += sgn * h
+            gp = ds.geometry64(a)
+            cdp = design.perturbed_state(cdf, stf, {n: gp[n] - g64[n] for n in design.GEOM})
+            pp = lib.Problem(cdp, setup_calls=False)
+            pp.run(3000)
+            r = pp.integrals()
+            js.append((r.eta_tt, r.mass_flow_in))
+            pp.close()
+        fd = {"eta_tt": (js[0][0] - js[1][0]) / (2 * h), "mass_flow_in": (js[0][1] - js[1][1]) / (2 * h)}
+        for obj in fd:
+            adj = grads[obj][i]
+            assert abs(adj - fd[obj]) <= 0.03 * abs(fd[obj]), (ds.names()[i], obj, adj, fd[obj])
+            assert abs(kgrads[obj][i] - adj) <= 0.01 * abs(adj), (ds.names()[i], obj, kgrads[obj][i], adj)
