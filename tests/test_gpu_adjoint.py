@@ -168,3 +168,27 @@ def test_adjoint_gradient_matches_frozen_finite_differences(mods, converged_smal
             adj = grads[obj][i]
             assert abs(adj - fd[obj]) <= 0.03 * abs(fd[obj]), (ds.names()[i], obj, adj, fd[obj])
             assert abs(kgrads[obj][i] - adj) <= 0.01 * abs(adj), (ds.names()[i], obj, kgrads[obj][i], adj)
+
+
+def test_autograd_wrapper_returns_the_adjoint_gradient(mods):
+    """The torch.autograd.Function of the check harness: backward() delivers
+    the adjoint gradient of the objective the forward pass computed."""
+    torch = pytest.importorskip("torch")
+    case = mods[0]
+    from mgpu import design
+    from mgpu.autograd import AdjointObjective, DesignSolve
+
+    def make():
+        sp = case.small_stage()
+        sp.sfxin = sp.sftin = 0.02
+        return sp
+
+    ds = design.DesignSpace.seeded(make)
+    solver = DesignSolve(ds, steps=3000, adjoint_iters=8000)
+    alpha = torch.tensor(ds.alpha0, dtype=torch.float64, requires_grad=True)
+    eta = AdjointObjective.apply(alpha, solver, "eta_tt")
+    eta.backward()
+    value, grad = solver.last
+    assert abs(float(eta) - value) < 1e-12
+    assert np.allclose(alpha.grad.numpy(), grad)
+    assert np.abs(grad).max() > 0.0
