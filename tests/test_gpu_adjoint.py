@@ -55,10 +55,19 @@ def _stepped(mods, spec, nsteps=30):
     return cd
 
 
-@pytest.mark.parametrize("which", ["small_nozzle", "small_stage"])
+def _medium_stage(case):
+    """33 x 122 x 25: the stage's multigrid blocks (3 and 9), leading-edge
+    smoothing and a multi-point tip gap, small enough for the oracle's tape."""
+    spec = case.turbine_stage(im=33, jm_row=61, km=25, seed=5)
+    spec.name = "medium_stage_33x122x25"
+    return spec
+
+
+@pytest.mark.parametrize("which", ["small_nozzle", "small_stage", "medium_stage"])
 def test_transposed_step_matches_oracle_reverse(mods, which):
     case, common_setup, lib, O = mods
-    cd = _stepped(mods, getattr(case, which)())
+    spec = _medium_stage(case) if which == "medium_stage" else getattr(case, which)()
+    cd = _stepped(mods, spec, nsteps=30 if which != "medium_stage" else 20)
     rng = np.random.default_rng(7)
     seeds = {}
     for n in ADJ_STATE:
