@@ -66,8 +66,9 @@ B_ALG_STEP = 132
 #   smooth  TMP read; D written
 KERNEL_BYTES = {
     "k_prim": (48, 1), "k_flux_mass": (60, 1), "k_flux_energy": (40, 1),
-    # momentum fluxes: 18 arrays read (PEFF, V*, ROVT, FLOW*, 6 areas, VOLOR, 3 forces), 12 written
-    "k_flux_mom": (120, 1), "k_peff": (8, 1), "k_density_detect": (4, 1),
+    # momentum fluxes: 19 arrays read (P, V*, ROVT, FLOW*, 6 areas, VOLOR, 3 forces, RO for the
+    # density-limiter flags), 13 written (9 fluxes, 3 sources, PEFF)
+    "k_flux_mom": (128, 1),
     "k_mach_limiter": (24, 1),
     "k_ts_cells": (28, 5), "k_ts_prolong": (16, 5), "k_ts_update": (12, 5), "k_ts_smooth": (8, 5),
     "k_loss_kfaces": (72, 0.2), "k_loss_ifaces": (84, 0.2),
@@ -476,6 +477,24 @@ def run_gpu(args, rank, world, local_rank):
            "steps": ne, "how": "per step mgpu_step() (graph launch, control word in, monitors out, sync); "
                                "flow state uploaded before and downloaded after from pageable host buffers"}
 
+    # the plain FP32 path: the same workload with the long sums formed in the
+    # reference's sequential REAL*4 order (REDUCE_ORDER=1, the parity mode)
+    plain = None
+    if os.environ.get("MGPU_BENCH_PLAIN", "1") != "0":
+        cdp = build_case()
+        cdp.ints["REDUCE_ORDER"] = 1
+        pp = lib.Problem(cdp)
+        pp.run(max(args.warmup, 3))
+        npl = max(10, min(60, args.steps // 10))
+        ms_pl = pp.bench_steps(npl, flush_l2=True)
+        pp.close()
+        v_pl = N * npl / (ms_pl / 1e3) / 1e9
+        plain = {"value": v_pl, "unit": METRIC, "steps": npl, "ms_per_step": ms_pl / npl,
+                 "chosen_over_plain": value / world / v_pl,
+                 "how": "REDUCE_ORDER=1: multigrid, row-mean, mixing-plane and monitor sums in the reference's "
+                        "sequential REAL*4 order; accuracy of both paths against the FP64 oracle is checked in "
+                        "tests/test_gpu_parity.py (small stage, 1500 steps)"}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         rate, n, dt = cpu_oracle_rate(cd, float(os.environ.get("MGPU_CPU_SECONDS", "15")), 10 ** 6)
@@ -498,6 +517,7 @@ def run_gpu(args, rank, world, local_rank):
                          "share_of_step": dom_ms / total_prof,
                          "step": {"alg_bytes_per_node_iter": B_ALG_STEP,
                                   "achieved": value / world * B_ALG_STEP, "frac": value / world * B_ALG_STEP / peak}},
+            "plain_fp32": plain,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "e2e": e2e,

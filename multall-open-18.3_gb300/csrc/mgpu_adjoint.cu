@@ -13,7 +13,7 @@
 // the primitive, flux and cell-change arrays of the step, the inlet density
 // and the mixing-plane inputs); the state is then restored.  Every reverse
 // kernel below undoes one forward kernel of the step, in reverse order:
-//   k_mixplan -> k_ts_* (momenta) -> k_flux_mom -> k_peff -> k_bc_apply ->
+//   k_mixplan -> k_ts_* (momenta) -> k_flux_mom (fluxes, then PEFF) -> k_bc_apply ->
 //   k_ts_* (RO, ROE) -> k_flux_energy -> k_bc_sums -> k_flux_mass -> k_prim
 // Each takes the adjoints of its forward kernel's outputs and adds the
 // adjoints of its inputs; outputs that the forward kernel overwrote get the
@@ -432,7 +432,7 @@ __global__ void rk_bc_apply(const __grid_constant__ Dev d, const __grid_constant
 }
 
 // =====================================================================
-// R7: PEFF = P - PREFF + F_PDOWN (P(J+1) - P)   (k_peff)
+// R7: PEFF = P - PREFF + F_PDOWN (P(J+1) - P)   (formed in k_flux_mom)
 // =====================================================================
 __global__ void rk_peff(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;

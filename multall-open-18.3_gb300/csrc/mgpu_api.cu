@@ -265,8 +265,7 @@ void enqueue_core(const Dev &d, Launch L, cudaEvent_t join = nullptr) {
         launch_bc_apply(d, L);
     }
     if (d.IN_FLOW != 0) launch_setflo(d, L);
-    launch_peff(d, L);
-    launch_flux_mom(d, L);
+    launch_flux_mom(d, L);          // also PEFF and the density limiter's column flags
     launch_tstep(d, L, V_ROVX, 3);
     launch_limiters(d, L);
     launch_mixplan(d, L);

@@ -594,42 +594,35 @@ void launch_cusp(const Dev &d, Launch L) {
 }
 
 // ---------------------------------------------------------------------
-// PEFF = P - PREFF + F_PDOWN*(P(J+1)-P(J))  (4321)
-// ---------------------------------------------------------------------
-__global__ void k_peff(Dev d) {
-    pdl_wait();
-    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t N = (size_t)d.IM * d.JM * d.KM;
-    if (n >= N) return;
-    int i, j, k;
-    node_ijk(d, n, i, j, k);
-    int jp1 = (j == d.JM) ? d.JM : j + 1;
-    float p = d.P[n];
-    d.PEFF[n] = p - d.PREFF + d.F_PDOWN * (A3(d.P, i, jp1, k) - p);
-}
-
-void launch_peff(const Dev &d, Launch L) {
-    size_t N = (size_t)d.IM * d.JM * d.KM;
-    launchk(L, k_peff, dim3(grid_for(N, 256)), dim3(256), 0, d);
-    mark(L, "k_peff");
-}
-
-// ---------------------------------------------------------------------
 // raw TFLUX of the moment-of-momentum (6200-6230) and radial-momentum
 // (6300-6330) equations at one I, used for the periodic balances at I=1
 // and I=IM (902, 6260)
 // ---------------------------------------------------------------------
+__device__ inline bool density_triggers(float ro, float ROAVG, float ROLIM) {
+    return ro < 0.6f * ROAVG || ro > 1.5f * ROAVG || ro < ROLIM;
+}
+
+// PEFF = P - PREFF + F_PDOWN*(P(J+1) - P) (4321) of node (i, j, k), formed
+// where it is read; the expression and its order are those of the
+// reference's PEFF loop
+__device__ __forceinline__ float peff_of(const Dev &d, const float *P, int o, int j) {
+    const float p = P[o];
+    const float pj1 = (d.F_PDOWN != 0.0f && j < d.JM) ? P[o + d.IM] : p;
+    return p - d.PREFF + d.F_PDOWN * (pj1 - p);
+}
+__device__ __forceinline__ float peff_at(const Dev &d, int i, int j, int k) { return peff_of(d, d.P, ix3(d, i, j, k), j); }
+
 __device__ inline float tflux_rvt_raw(const Dev &d, int i, int j, int k, float AVGR) {
-    const float *PE = d.PEFF, *VT = d.VT;
+    const float *VT = d.VT;
     float AVGVT = A3(VT, i, j, k) + A3(VT, i, j - 1, k) + A3(VT, i, j - 1, k + 1) + A3(VT, i, j, k + 1);
-    float AVGP = A3(PE, i, j, k) + A3(PE, i, j - 1, k) + A3(PE, i, j - 1, k + 1) + A3(PE, i, j, k + 1);
+    float AVGP = peff_at(d, i, j, k) + peff_at(d, i, j - 1, k) + peff_at(d, i, j - 1, k + 1) + peff_at(d, i, j, k + 1);
     return (A3(d.FLOWT, i, j, k) * AVGVT + A2(d.ABT, j, k) * AVGP) * AVGR;
 }
 
 __device__ inline float tflux_rmom_raw(const Dev &d, int i, int j, int k, float *avgp4) {
-    const float *PE = d.PEFF, *VR = d.VR;
+    const float *VR = d.VR;
     float AVGVR = A3(VR, i, j, k) + A3(VR, i, j - 1, k) + A3(VR, i, j - 1, k + 1) + A3(VR, i, j, k + 1);
-    float AVGP = A3(PE, i, j, k) + A3(PE, i, j - 1, k) + A3(PE, i, j - 1, k + 1) + A3(PE, i, j, k + 1);
+    float AVGP = peff_at(d, i, j, k) + peff_at(d, i, j - 1, k) + peff_at(d, i, j - 1, k + 1) + peff_at(d, i, j, k + 1);
     *avgp4 = AVGP;
     return 0.25f * (A3(d.FLOWT, i, j, k) * AVGVR + AVGP * A3(d.ABR, i, j, k));
 }
@@ -651,7 +644,7 @@ __global__ void __launch_bounds__(256, 4) k_flux_mom(Dev d) {
     node_ijk(d, (size_t)n, i, j, k);
     const int IM = d.IM, sJ = d.IM, sK = d.IM * d.JM;
     const bool hi = i < IM, hj = j >= 2, hk = k < d.KM;
-    const float *__restrict__ PE = d.PEFF;
+    const float *__restrict__ PP = d.P;
     const float *__restrict__ VX = d.VX;
     const float *__restrict__ VT = d.VT;
     const float *__restrict__ VR = d.VR;
@@ -666,7 +659,7 @@ __global__ void __launch_bounds__(256, 4) k_flux_mom(Dev d) {
             for (int dk = 0; dk < 2; ++dk) {
                 if ((di && !hi) || (dj && !hj) || (dk && !hk)) continue;
                 const int o = n + di + dj * sJ + dk * sK;
-                pe[di][dj + 1][dk] = PE[o];
+                pe[di][dj + 1][dk] = peff_of(d, PP, o, j + dj);
                 vt[di][dj + 1][dk] = VT[o];
                 if (!(di && dj && dk)) {
                     vx[di][dj + 1][dk] = VX[o];
@@ -675,6 +668,7 @@ __global__ void __launch_bounds__(256, 4) k_flux_mom(Dev d) {
                 if (hi && hj && hk) rv[di][dj + 1][dk] = RV[o];
             }
 #define C(a, di, dj, dk) a[di][(dj) + 1][dk]
+    d.PEFF[n] = C(pe, 0, 0, 0);    // PEFF of this step, read by the next step's energy fluxes
     const VarSet &VXm = d.var[V_ROVX], &VTm = d.var[V_RORVT], &VRm = d.var[V_ROVR];
     const bool edge = (i == 1 || i == IM) && A1(d.IND, j) != 1;
     // faces K = const (XFLUX) and the axial / tangential sources
@@ -715,8 +709,9 @@ __global__ void __launch_bounds__(256, 4) k_flux_mom(Dev d) {
         const float FT = d.FLOWT[n];
         float AVGP = C(pe, 0, 0, 0) + C(pe, 0, -1, 0) + C(pe, 0, -1, 1) + C(pe, 0, 0, 1);
         if (edge) {
-            float AVGPCUSP = A3(PE, 1, j, k) + A3(PE, 1, j - 1, k) + A3(PE, 1, j, k + 1) + A3(PE, 1, j - 1, k + 1) +
-                             A3(PE, IM, j, k) + A3(PE, IM, j - 1, k) + A3(PE, IM, j, k + 1) + A3(PE, IM, j - 1, k + 1);
+            float AVGPCUSP = peff_at(d, 1, j, k) + peff_at(d, 1, j - 1, k) + peff_at(d, 1, j, k + 1) +
+                             peff_at(d, 1, j - 1, k + 1) + peff_at(d, IM, j, k) + peff_at(d, IM, j - 1, k) +
+                             peff_at(d, IM, j, k + 1) + peff_at(d, IM, j - 1, k + 1);
             float AVGVXCUSP = A3(VX, 1, j, k) + A3(VX, 1, j - 1, k) + A3(VX, 1, j, k + 1) + A3(VX, 1, j - 1, k + 1) +
                               A3(VX, IM, j, k) + A3(VX, IM, j - 1, k) + A3(VX, IM, j, k + 1) + A3(VX, IM, j - 1, k + 1);
             VXm.TF[n] = 0.125f * (FT * AVGVXCUSP + AVGPCUSP * d.ABX[n]);
@@ -739,8 +734,10 @@ __global__ void __launch_bounds__(256, 4) k_flux_mom(Dev d) {
             float ap1, apm;
             float t1raw = tflux_rmom_raw(d, 1, j, k, &ap1);
             float tmraw = tflux_rmom_raw(d, IM, j, k, &apm);
-            float AVGP1 = 0.25f * (A3(PE, 1, j, k) + A3(PE, 1, j - 1, k) + A3(PE, 1, j, k + 1) + A3(PE, 1, j - 1, k + 1));
-            float AVGPM = 0.25f * (A3(PE, IM, j, k) + A3(PE, IM, j - 1, k) + A3(PE, IM, j, k + 1) + A3(PE, IM, j - 1, k + 1));
+            float AVGP1 = 0.25f * (peff_at(d, 1, j, k) + peff_at(d, 1, j - 1, k) + peff_at(d, 1, j, k + 1) +
+                                   peff_at(d, 1, j - 1, k + 1));
+            float AVGPM = 0.25f * (peff_at(d, IM, j, k) + peff_at(d, IM, j - 1, k) + peff_at(d, IM, j, k + 1) +
+                                   peff_at(d, IM, j - 1, k + 1));
             float T1 = t1raw - AVGP1 * A3(d.ABR, 1, j, k);
             float T2 = tmraw - AVGPM * A3(d.ABR, IM, j, k);
             tr = 0.5f * ((T1 + T2) + (AVGP1 + AVGPM) * d.ABR[n]);
@@ -748,6 +745,15 @@ __global__ void __launch_bounds__(256, 4) k_flux_mom(Dev d) {
         VRm.TF[n] = tr;
     }
 #undef C
+    // the density limiter's column flags (7200): RO is final here (after
+    // TSTEP(RO) and the inlet/exit conditions) and TSTEP of the momenta
+    // does not change it
+    if (d.ADJ_RO_LIM) d.ADJ_RO_LIM[n] = d.RO[n];
+    if (j >= 3 && j <= d.JM - 3) {
+        const float *RO = d.RO;
+        const float ROAVG = 0.25f * (RO[n - 2 * sJ] + RO[n - sJ] + RO[n + sJ] + RO[n + 2 * sJ]);
+        if (density_triggers(RO[n], ROAVG, d.ROLIM)) d.DFLAG[(size_t)(k - 1) * d.IM + (i - 1)] = 1;
+    }
 }
 
 void launch_flux_mom(const Dev &d, Launch L) {
@@ -760,29 +766,11 @@ void launch_flux_mom(const Dev &d, Launch L) {
 // density limiter (7200).  The reference walks J in place, so RO(J-1) and
 // RO(J-2) are already limited when RO(J) is tested.  A column's result
 // differs from its input only if some J triggers a limit on the unmodified
-// values (the first trigger is the same in both), so k_density_detect flags
-// those columns in parallel and k_density_fix replays the sequential walk
-// on flagged columns only.  The thread owning (IMID,KMID) then sets the
+// values (the first trigger is the same in both), so k_flux_mom flags those
+// columns in parallel and k_density_fix replays the sequential walk on
+// flagged columns only.  The thread owning (IMID,KMID) then sets the
 // per-row Mach limits VLIMIT/ROLIMIT (7250) from its final densities.
 // ---------------------------------------------------------------------
-__device__ inline bool density_triggers(float ro, float ROAVG, float ROLIM) {
-    return ro < 0.6f * ROAVG || ro > 1.5f * ROAVG || ro < ROLIM;
-}
-
-__global__ void k_density_detect(Dev d) {
-    pdl_wait();
-    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t N = (size_t)d.IM * d.JM * d.KM;
-    if (n >= N) return;
-    if (d.ADJ_RO_LIM) d.ADJ_RO_LIM[n] = d.RO[n];
-    int i, j, k;
-    node_ijk(d, n, i, j, k);
-    if (j < 3 || j > d.JM - 3) return;
-    const float *RO = d.RO;
-    float ROAVG = 0.25f * (A3(RO, i, j - 2, k) + A3(RO, i, j - 1, k) + A3(RO, i, j + 1, k) + A3(RO, i, j + 2, k));
-    if (density_triggers(RO[n], ROAVG, d.ROLIM)) d.DFLAG[(size_t)(k - 1) * d.IM + (i - 1)] = 1;
-}
-
 __global__ void k_density_fix(Dev d) {
     pdl_wait();
     int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -865,9 +853,6 @@ __global__ void k_mach_limiter(Dev d) {
 }
 
 void launch_limiters(const Dev &d, Launch L) {
-    size_t Nn = (size_t)d.IM * d.JM * d.KM;
-    launchk(L, k_density_detect, dim3(grid_for(Nn, 256)), dim3(256), 0, d);
-    mark(L, "k_density_detect");
     int lines = d.IM * d.KM;
     launchk(L, k_density_fix, dim3((lines + 127) / 128), dim3(128), 0, d);
     mark(L, "k_density_fix");
