@@ -250,6 +250,7 @@ def run_batch(args, rank, world, local_rank):
     from mgpu import lib
     nodes = sum(cd.nodes() for cd in cds)
     probs = [lib.Problem(cd) for cd in cds]
+    tuned = [p.autotune()[0] for p in probs]
     batch = lib.Batch(probs)
     batch.run(max(args.warmup, 3))
     dist_barrier(dist)
@@ -286,6 +287,7 @@ def run_batch(args, rank, world, local_rank):
             "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOADS["batch64"][1], "instances": BATCH, "nodes": nodes,
+                       "autotune": {"tstep_threads_per_cta": {str(b): tuned.count(b) for b in (128, 256, 512)}},
                        "l2": "flushed between timed steps", "parallelism": f"replicas: one batch per GPU x{world}",
                        "reductions": "FP64 tree sums (REDUCE_ORDER=0)"},
             "roofline": {"bound": "hbm", "kernel": None, "peak": peak, "unit": "GB/s", "peak_source": peak_kind,
@@ -343,6 +345,7 @@ def run_adjoint(args, rank, world, local_rank):
     p.run(max(args.warmup, 3))
     p.close()
     p = lib.Problem(cd)
+    p.autotune()
     t0 = time.perf_counter()
     _, m = p.run(n_primal)
     t_primal = time.perf_counter() - t0
@@ -430,6 +433,8 @@ def run_gpu(args, rank, world, local_rank):
     kps = prob.kernels_per_step()
     kps_loss, kps_tail = prob.kernels_per_step(loss=True) - kps, prob.kernels_per_step(tail=True) - kps
     prob.run(max(args.warmup, 3))
+    tuned, tune_ms = prob.autotune()        # threads per J-plane CTA of the TSTEP kernels
+    prob.run(3)
     dist_barrier(dist)
     with ClockSampler(0) as clk:
         t_wall0 = time.perf_counter()
@@ -508,7 +513,9 @@ def run_gpu(args, rank, world, local_rank):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOADS[ARGS_WORKLOAD][1], "nodes": N, "l2": "flushed between timed steps",
                        "parallelism": f"replicas: one instance per GPU x{world}",
-                       "reductions": "FP64 tree sums (REDUCE_ORDER=0)"},
+                       "reductions": "FP64 tree sums (REDUCE_ORDER=0)",
+                       "autotune": {"tstep_threads_per_cta": tuned,
+                                    "tstep_pass_ms": dict(zip(("128", "256", "512"), tune_ms))}},
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "alg_bytes_per_launch": alg_step / launches_step,

@@ -71,7 +71,10 @@
     /* not a COMMON variable: 1 holds the LOSS body forces and the STEPUP */ \
     /* time steps at their current values (frozen-turbulence stepping,    */ \
     /* the primal of the discrete adjoint)                                */ \
-    M_(FROZEN,   0)
+    M_(FROZEN,   0)                                                       \
+    /* not a COMMON variable: threads per J-plane CTA of TSTEP, 128, 256  */ \
+    /* or 512 (0: 256 until mgpu_autotune chooses)                        */ \
+    M_(TS_THREADS, 0)
 
 /* ----- REAL scalars: /BKGAS/, /BKCNTL/, /BKSMTH/, /BKLOSS/, /BKINPT/ ---- */
 #define MGPU_REAL_SCALARS(M_)                                             \

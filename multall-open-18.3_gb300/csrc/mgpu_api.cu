@@ -450,6 +450,7 @@ int32_t mgpu_create(int32_t im, int32_t jm, int32_t km, int32_t nrows, mgpu_hand
     d.IMID = (int)(0.5f * im);
     d.KMID = (int)(0.5f * km);
     d.NRWSM1 = nrows - 1;
+    d.ts_bs = 256;
 #define MGPU_DEF_I(n, v) d.n = v;
     MGPU_INT_SCALARS(MGPU_DEF_I)
 #define MGPU_DEF_R(n, v) d.n = v;
@@ -802,6 +803,9 @@ int32_t mgpu_commit(mgpu_handle *h) {
             return rc;
     }
     if (d.REDUCE_ORDER != 0 && d.REDUCE_ORDER != 1) return fail(MGPU_E_ARG, "REDUCE_ORDER must be 0 or 1");
+    if (d.TS_THREADS != 0 && d.TS_THREADS != 128 && d.TS_THREADS != 256 && d.TS_THREADS != 512)
+        return fail(MGPU_E_ARG, "TS_THREADS must be 0, 128, 256 or 512");
+    d.ts_bs = d.TS_THREADS ? d.TS_THREADS : 256;
     // the control block
     DevCtl c;
     memset(&c, 0, sizeof(c));
@@ -930,6 +934,72 @@ int32_t mgpu_integrals_compute(mgpu_handle *h, mgpu_integrals *out) {
     out->to_ratio = TORAT;
     out->j1 = J1;
     out->j2m1 = J2M1;
+    return 0;
+}
+
+int32_t mgpu_autotune(mgpu_handle *h, int32_t *chosen, double *ms) {
+    if (!h || !h->committed) return fail(MGPU_E_STATE, "autotune before commit");
+    Dev &d = h->d;
+    const size_t N = (size_t)d.IM * d.JM * d.KM, fb = N * sizeof(float);
+    // the candidates run TSTEP on the handle's arrays; the variables and their
+    // histories are put back after each
+    float *save = nullptr;
+    CK(cudaMallocAsync((void **)&save, 2 * NVAR * fb, h->stream));
+    for (int v = 0; v < NVAR; ++v) {
+        CK(cudaMemcpyAsync(save + (size_t)(2 * v) * N, d.var[v].D, fb, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(save + (size_t)(2 * v + 1) * N, d.var[v].DIFF, fb, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    const int cand[3] = {128, 256, 512};
+    double t[3] = {0.0, 0.0, 0.0};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    int best = 1;
+    for (int c = 0; c < 3; ++c) {
+        Dev dt = d;
+        dt.ts_bs = cand[c];
+        dt.use_cond = 0;
+        Launch L{h->stream, h->sm_count};
+        for (int r = 0; r < 2; ++r) {
+            launch_tstep(dt, L, V_RO, 2);
+            launch_tstep(dt, L, V_ROVX, 3);
+        }
+        CK(cudaEventRecord(e0, h->stream));
+        const int reps = 10;
+        for (int r = 0; r < reps; ++r) {
+            launch_tstep(dt, L, V_RO, 2);
+            launch_tstep(dt, L, V_ROVX, 3);
+        }
+        CK(cudaEventRecord(e1, h->stream));
+        CK(cudaGetLastError());
+        CK(cudaEventSynchronize(e1));
+        float f = 0.0f;
+        CK(cudaEventElapsedTime(&f, e0, e1));
+        t[c] = (double)f / reps;
+        for (int v = 0; v < NVAR; ++v) {
+            CK(cudaMemcpyAsync(d.var[v].D, save + (size_t)(2 * v) * N, fb, cudaMemcpyDeviceToDevice, h->stream));
+            CK(cudaMemcpyAsync(d.var[v].DIFF, save + (size_t)(2 * v + 1) * N, fb, cudaMemcpyDeviceToDevice, h->stream));
+        }
+        if (t[c] < t[best]) best = c;
+    }
+    CK(cudaFreeAsync(save, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (d.ts_bs != cand[best]) {
+        d.ts_bs = cand[best];
+        if (h->gexec) {
+            cudaGraphExecDestroy(h->gexec);
+            h->gexec = nullptr;
+        }
+        if (h->graph) {
+            cudaGraphDestroy(h->graph);
+            h->graph = nullptr;
+        }
+    }
+    if (chosen) *chosen = cand[best];
+    if (ms)
+        for (int c = 0; c < 3; ++c) ms[c] = t[c];
     return 0;
 }
 

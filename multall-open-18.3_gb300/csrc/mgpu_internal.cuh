@@ -130,6 +130,7 @@ struct Dev {
     // the step-control kernel when the step runs from the CUDA graph)
     int use_cond;
     unsigned long long cond_loss, cond_tail;
+    int ts_bs;                         // threads per J-plane CTA of TSTEP: 128, 256 or 512 (mgpu_autotune)
 };
 
 // Element offsets in 32-bit int: mgpu_create keeps IM*JM*KM below 2^30,

@@ -27,10 +27,11 @@ namespace mgpu {
 
 static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
 
-constexpr int TS_BS = 256;      // threads per J-plane CTA; 4 CTAs resident per SM
+// Threads per J-plane CTA: 128, 256 (the default) or 512, chosen per
+// problem by mgpu_autotune (Dev::ts_bs); each size keeps 1024 threads of
+// 64 registers resident per SM.
 constexpr int TS_U = 3;          // cells per thread whose loads are issued together
 constexpr int TS_UG = 4;         // the same for the damping and gather phases of update
-constexpr int SV_BS = 256;
 constexpr int SV_U = 3;          // points per thread whose streamwise loads are issued together
 
 template <int BS>
@@ -99,12 +100,13 @@ struct Walk2 {
 // cells: 5503-5510 (tip gap), 5516-5555 (MP extrapolation), 1000 (flux
 // sum), 1750 (MP redistribution) and the multigrid partial sums
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(TS_BS, 4) k_ts_cells(const __grid_constant__ Dev d, int v0) {
+template <int BS>
+__global__ void __launch_bounds__(BS, 1024 / BS) k_ts_cells(const __grid_constant__ Dev d, int v0) {
     pdl_wait();
     extern __shared__ float sm[];
     const VarSet &V = d.var[v0 + blockIdx.y];
     float *__restrict__ DIFF = V.DIFF;
-    __shared__ double shd[TS_BS / 32];
+    __shared__ double shd[BS / 32];
     const int j = blockIdx.x + 2;
     const int IM = d.IM, IMM1 = d.IMM1, KMM1 = d.KMM1;
     const int nc = IMM1 * KMM1;
@@ -118,12 +120,12 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_cells(const __grid_constant__ D
         // stage the XFLUX plane in shared memory (coalesced), then add each
         // I-line in the reference's order
         int jj = role == 1 ? j - 1 : j;
-        for (int c = threadIdx.x; c < nc; c += TS_BS) {
+        for (int c = threadIdx.x; c < nc; c += BS) {
             int i = c % IMM1 + 1, k = c / IMM1 + 1;
             st[c] = A3(V.XF, i, jj, k);
         }
         __syncthreads();
-        for (int k = threadIdx.x + 1; k <= KMM1; k += TS_BS) {
+        for (int k = threadIdx.x + 1; k <= KMM1; k += BS) {
             const float *row = st + (size_t)(k - 1) * IMM1;
             lsum[k - 1] = mp_line_sum(row, IMM1, d.REDUCE_ORDER == 1);
         }
@@ -140,8 +142,8 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_cells(const __grid_constant__ D
     // each thread first loads the operands of its TS_U cells, then computes:
     // the loads of all cells are in flight together
     const size_t ks = (size_t)IM * d.JM, pj = (size_t)IM * (j - 1);
-    Walk2 w(IMM1, threadIdx.x, TS_BS);
-    for (int c0 = threadIdx.x; c0 < nc; c0 += TS_U * TS_BS) {
+    Walk2 w(IMM1, threadIdx.x, BS);
+    for (int c0 = threadIdx.x; c0 < nc; c0 += TS_U * BS) {
         float xf[TS_U], xm[TS_U], rf[TS_U], rk[TS_U], ta[TS_U], tb1[TS_U], sr[TS_U], df[TS_U];
         int ci[TS_U], ck[TS_U];
 #pragma unroll
@@ -149,7 +151,7 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_cells(const __grid_constant__ D
             ci[u] = w.i;
             ck[u] = w.k;
             w.next();
-            if (c0 + u * TS_BS < nc) {
+            if (c0 + u * BS < nc) {
                 const size_t n = pj + (size_t)(ci[u] - 1) + ks * (ck[u] - 1);
                 xf[u] = XF[n];
                 xm[u] = XF[n - IM];
@@ -163,7 +165,7 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_cells(const __grid_constant__ D
         }
 #pragma unroll
         for (int u = 0; u < TS_U; ++u) {
-            const int c = c0 + u * TS_BS;
+            const int c = c0 + u * BS;
             if (c >= nc) break;
             const int i = ci[u], k = ck[u];
             const size_t n = pj + (size_t)(i - 1) + ks * (k - 1);
@@ -189,7 +191,7 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_cells(const __grid_constant__ D
     }
     __syncthreads();
     if (role == 1 || role == 3) {
-        for (int k = threadIdx.x + 1; k <= KMM1; k += TS_BS) {
+        for (int k = threadIdx.x + 1; k <= KMM1; k += BS) {
             float FLOWDIRN = -A3(d.FLOWX, d.IMID, jmx, k);
             bool on = role == 3 ? (FLOWDIRN > 0.0f || lowx) : (FLOWDIRN < 0.0f || lowx);
             if (!on) continue;
@@ -200,17 +202,17 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_cells(const __grid_constant__ D
         __syncthreads();
     }
     double ps = 0.0;
-    for (int c = threadIdx.x; c < nc; c += TS_BS) {
+    for (int c = threadIdx.x; c < nc; c += BS) {
         int i = c % IMM1 + 1, k = c / IMM1 + 1;
         float v = st[c];
         A3(V.ST, i, j, k) = v;
         ps += (double)v;
     }
-    ps = block_sum<TS_BS>(ps, shd);
+    ps = block_sum<BS>(ps, shd);
     if (threadIdx.x == 0) V.psum[j - 1] = ps;
     // level-1 and level-2 partial sums of this plane
     const int n1 = d.NIB1 * d.NKB1, n2 = d.NIB2 * d.NKB2;
-    for (int t = threadIdx.x; t < n1 + n2; t += TS_BS) {
+    for (int t = threadIdx.x; t < n1 + n2; t += BS) {
         const bool lv1 = t < n1;
         int u = lv1 ? t : t - n1;
         int nib = lv1 ? d.NIB1 : d.NIB2;
@@ -267,11 +269,12 @@ __global__ void k_ts_restrict_seq(const __grid_constant__ Dev d, int v0) {
 // ---------------------------------------------------------------------
 // prolong: 1500, with the block sums assembled from the plane partials
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(TS_BS, 4) k_ts_prolong(const __grid_constant__ Dev d, int v0, int want_abs) {
+template <int BS>
+__global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_constant__ Dev d, int v0, int want_abs) {
     pdl_wait();
     extern __shared__ float sm[];
     const VarSet &V = d.var[v0 + blockIdx.y];
-    __shared__ double shd[TS_BS / 32];
+    __shared__ double shd[BS / 32];
     __shared__ float s_sb;
     const int j = blockIdx.x + 2;
     const int IMM1 = d.IMM1, KMM1 = d.KMM1;
@@ -285,12 +288,12 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_prolong(const __grid_constant__
     // sums so their latency overlaps the assembly below
     float pst[TS_U], pstp[TS_U], prs[TS_U], ps1[TS_U], ps2[TS_U];
     int pb1[TS_U], pb2[TS_U];
-    Walk2 w(IMM1, threadIdx.x, TS_BS);
+    Walk2 w(IMM1, threadIdx.x, BS);
 #pragma unroll
     for (int u = 0; u < TS_U; ++u) {
         const int i = w.i, k = w.k;
         w.next();
-        if (threadIdx.x + u * TS_BS < nc) {
+        if (threadIdx.x + u * BS < nc) {
             const size_t n = pj + (size_t)(i - 1) + ks * (k - 1);
             const int i1 = A1(d.IB1, i), i2 = A1(d.IB2, i), k1 = A1(d.KB1, k), k2 = A1(d.KB2, k);
             pst[u] = V.ST[n];
@@ -303,23 +306,23 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_prolong(const __grid_constant__
         }
     }
     if (d.REDUCE_ORDER == 1) {
-        for (int t = threadIdx.x; t < n1; t += TS_BS) {
+        for (int t = threadIdx.x; t < n1; t += BS) {
             int ib = t % d.NIB1 + 1, kb = t / d.NIB1 + 1;
             b1[t] = V.B1CHG[(size_t)(ib - 1) + (size_t)d.NIB1 * (j1 - 1) + m1 * (kb - 1)];
         }
-        for (int t = threadIdx.x; t < n2; t += TS_BS) {
+        for (int t = threadIdx.x; t < n2; t += BS) {
             int ib = t % d.NIB2 + 1, kb = t / d.NIB2 + 1;
             b2[t] = V.B2CHG[(size_t)(ib - 1) + (size_t)d.NIB2 * (j2 - 1) + m2 * (kb - 1)];
         }
         if (threadIdx.x == 0) s_sb = A1(V.SBSUM, jsb);
     } else {
-        for (int t = threadIdx.x; t < n1; t += TS_BS) {
+        for (int t = threadIdx.x; t < n1; t += BS) {
             float s = 0.0f;
             if (j1 <= d.NJB1)
                 for (int jj = A1(d.JB1_START, j1); jj <= A1(d.JB1_END, j1); ++jj) s = s + V.P1[(size_t)(jj - 1) * n1 + t];
             b1[t] = s;
         }
-        for (int t = threadIdx.x; t < n2; t += TS_BS) {
+        for (int t = threadIdx.x; t < n2; t += BS) {
             float s = 0.0f;
             if (j2 <= d.NJB2)
                 for (int jj = A1(d.JB2_START, j2); jj <= A1(d.JB2_END, j2); ++jj) s = s + V.P2[(size_t)(jj - 1) * n2 + t];
@@ -336,19 +339,19 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_prolong(const __grid_constant__
     __syncthreads();
     const float SBCHG = s_sb, SSB = A1(d.STEPSBK, jsb);
     double sabs = 0.0;
-    w = Walk2(IMM1, threadIdx.x, TS_BS);
+    w = Walk2(IMM1, threadIdx.x, BS);
 #pragma unroll
     for (int u = 0; u < TS_U; ++u) {
         const int i = w.i, k = w.k;
         w.next();
-        if (threadIdx.x + u * TS_BS < nc) {
+        if (threadIdx.x + u * BS < nc) {
             const size_t n = pj + (size_t)(i - 1) + ks * (k - 1);
             float DELTA = pst[u] * pstp[u] + (b1[pb1[u]] * ps1[u] + b2[pb2[u]] * ps2[u] + SBCHG * SSB) * prs[u];
             V.ST[n] = DELTA;
             sabs += (double)fabsf(DELTA);
         }
     }
-    for (int c = threadIdx.x + TS_U * TS_BS; c < nc; c += TS_BS, w.next()) {
+    for (int c = threadIdx.x + TS_U * BS; c < nc; c += BS, w.next()) {
         const int i = w.i, k = w.k;
         const int i1 = A1(d.IB1, i), i2 = A1(d.IB2, i), k1 = A1(d.KB1, k), k2 = A1(d.KB2, k);
         const size_t s1 = (size_t)(i1 - 1) + (size_t)d.NIB1 * (j1 - 1) + m1 * (k1 - 1);
@@ -360,24 +363,25 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_prolong(const __grid_constant__
         sabs += (double)fabsf(DELTA);
     }
     if (want_abs) {
-        sabs = block_sum<TS_BS>(sabs, shd);
+        sabs = block_sum<BS>(sabs, shd);
         if (threadIdx.x == 0) V.pabs[j - 1] = sabs;
     }
 }
 
 // per-J-plane sum of |STORE| (after residual smoothing)
-__global__ void __launch_bounds__(TS_BS, 4) k_ts_plane_abs(const __grid_constant__ Dev d, int v0) {
+template <int BS>
+__global__ void __launch_bounds__(BS, 1024 / BS) k_ts_plane_abs(const __grid_constant__ Dev d, int v0) {
     pdl_wait();
-    __shared__ double shd[TS_BS / 32];
+    __shared__ double shd[BS / 32];
     const VarSet &V = d.var[v0 + blockIdx.y];
     int j = blockIdx.x + 2;
     int nc = d.IMM1 * d.KMM1;
     double s = 0.0;
-    for (int c = threadIdx.x; c < nc; c += TS_BS) {
+    for (int c = threadIdx.x; c < nc; c += BS) {
         int i = c % d.IMM1 + 1, k = c / d.IMM1 + 1;
         s += (double)fabsf(A3(V.ST, i, j, k));
     }
-    s = block_sum<TS_BS>(s, shd);
+    s = block_sum<BS>(s, shd);
     if (threadIdx.x == 0) V.pabs[j - 1] = s;
 }
 
@@ -416,7 +420,8 @@ __global__ void k_ts_avgblk_seq(const __grid_constant__ Dev d, int v0) {
 // ---------------------------------------------------------------------
 // update: negative feedback, second MP average, corner gather -> TMP
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(TS_BS, 4) k_ts_update(const __grid_constant__ Dev d, int v0) {
+template <int BS>
+__global__ void __launch_bounds__(BS, 1024 / BS) k_ts_update(const __grid_constant__ Dev d, int v0) {
     pdl_wait();
     extern __shared__ float sm[];
     const VarSet &V = d.var[v0 + blockIdx.y];
@@ -432,10 +437,10 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_update(const __grid_constant__ 
     const float DAMP = ctl->DAMP;
     if (damp_on) {
         if (d.REDUCE_ORDER == 1) {
-            for (int r = threadIdx.x; r < d.NROWS; r += TS_BS) s_blk[r] = V.AVG_BLK[r];
+            for (int r = threadIdx.x; r < d.NROWS; r += BS) s_blk[r] = V.AVG_BLK[r];
         } else {
             int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-            for (int nr = w + 1; nr <= d.NROWS; nr += TS_BS / 32) {
+            for (int nr = w + 1; nr <= d.NROWS; nr += BS / 32) {
                 int JST = A1(d.JSTART, nr) + 1, JEN = A1(d.JMIX, nr) - 1;
                 double s = 0.0;
                 for (int jj = JST + l; jj <= JEN; jj += 32) s += V.pabs[jj - 1];
@@ -468,17 +473,17 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_update(const __grid_constant__ 
         const float blk = damp_on ? s_blk[A1(d.NROW, jc) - 1] : 1.0f;
         const float *__restrict__ stp = V.ST + (size_t)IM * (jc - 1);     // plane jc, (i, k) at i-1 + IM*JM*(k-1)
         const size_t kstride = (size_t)IM * d.JM;
-        Walk2 w(IMM1, threadIdx.x, TS_BS);
-        for (int t0 = threadIdx.x; t0 < nc; t0 += TS_UG * TS_BS) {
+        Walk2 w(IMM1, threadIdx.x, BS);
+        for (int t0 = threadIdx.x; t0 < nc; t0 += TS_UG * BS) {
             float sv[TS_UG];
 #pragma unroll
             for (int u = 0; u < TS_UG; ++u) {
-                if (t0 + u * TS_BS < nc) sv[u] = stp[(size_t)(w.i - 1) + kstride * (w.k - 1)];
+                if (t0 + u * BS < nc) sv[u] = stp[(size_t)(w.i - 1) + kstride * (w.k - 1)];
                 w.next();
             }
 #pragma unroll
             for (int u = 0; u < TS_UG; ++u) {
-                const int t = t0 + u * TS_BS;
+                const int t = t0 + u * BS;
                 if (t >= nc) break;
                 float v = sv[u];
                 if (damp_on) {
@@ -502,7 +507,7 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_update(const __grid_constant__ 
         any = true;
         float *c = h ? cB : cA;
         int jmx = A1(d.JMIX, mnr);
-        for (int k = threadIdx.x + 1; k <= KMM1; k += TS_BS) {
+        for (int k = threadIdx.x + 1; k <= KMM1; k += BS) {
             float FLOWDIRN = -A3(d.FLOWX, d.IMID, jmx, k);
             bool on = role == 3 ? (FLOWDIRN > 0.0f || lowx) : (FLOWDIRN < 0.0f || lowx);
             if (!on) continue;
@@ -523,8 +528,8 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_update(const __grid_constant__ 
     const float *__restrict__ FTL = d.FTL;
     const float *__restrict__ FTR = d.FTR;
     const size_t nbase = (size_t)IM * (j - 1), kstride = (size_t)IM * d.JM;
-    Walk2 w(IM, threadIdx.x, TS_BS);
-    for (int t0 = threadIdx.x; t0 < np; t0 += TS_UG * TS_BS) {
+    Walk2 w(IM, threadIdx.x, BS);
+    for (int t0 = threadIdx.x; t0 < np; t0 += TS_UG * BS) {
         // loads of TS_UG nodes first: the node value and, for interior nodes,
         // the four corner weights
         float dv[TS_UG], wtr[TS_UG], wtl[TS_UG], wbr[TS_UG], wbl[TS_UG];
@@ -535,7 +540,7 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_update(const __grid_constant__ 
             ni[u] = i;
             nk[u] = k;
             w.next();
-            if (t0 + u * TS_BS < np) {
+            if (t0 + u * BS < np) {
                 dv[u] = D[nbase + (size_t)(i - 1) + kstride * (k - 1)];
                 if (hA && hB && i >= 2 && i <= IMM1 && k >= 2 && k <= KMM1) {
                     wtr[u] = FTR[(i - 2) + IM * (k - 2)];
@@ -547,7 +552,7 @@ __global__ void __launch_bounds__(TS_BS, 4) k_ts_update(const __grid_constant__ 
         }
 #pragma unroll
         for (int u = 0; u < TS_UG; ++u) {
-            if (t0 + u * TS_BS >= np) break;
+            if (t0 + u * BS >= np) break;
             const int i = ni[u], k = nk[u];
             const size_t n = nbase + (size_t)(i - 1) + kstride * (k - 1);
             float v = dv[u];
@@ -617,7 +622,8 @@ __device__ inline int le_case(const Dev &d, int j) {
     return lc;
 }
 
-__global__ void __launch_bounds__(SV_BS, 4) k_ts_smooth(const __grid_constant__ Dev d, int v0) {
+template <int BS>
+__global__ void __launch_bounds__(BS, 1024 / BS) k_ts_smooth(const __grid_constant__ Dev d, int v0) {
     pdl_wait();
     extern __shared__ float sm[];
     const VarSet &V = d.var[v0 + blockIdx.y];
@@ -630,11 +636,11 @@ __global__ void __launch_bounds__(SV_BS, 4) k_ts_smooth(const __grid_constant__ 
     const int j = blockIdx.x + 1;
     const DevCtl *c = d.ctl;
     const bool stream = !(c->SFX < 0.0001f);
-    for (int t = threadIdx.x; t < IM; t += SV_BS) {
+    for (int t = threadIdx.x; t < IM; t += BS) {
         cFD[t] = d.FD[t];
         cFU[t] = d.FU[t];
     }
-    for (int t = threadIdx.x; t < KM; t += SV_BS) {
+    for (int t = threadIdx.x; t < KM; t += BS) {
         cFKD[t] = d.FKD[t];
         cFKU[t] = d.FKU[t];
     }
@@ -656,8 +662,8 @@ __global__ void __launch_bounds__(SV_BS, 4) k_ts_smooth(const __grid_constant__ 
         if (sc == 3) { add(J1 + 2); add(J1 + 3); add(J1 + 4); }
         if (sc == 4) { add(J2 - 1); add(J2 - 3); }
         if (sc == 5) { add(J2 - 2); add(J2 - 3); add(J2 - 4); }
-        Walk2 w(IM, threadIdx.x, SV_BS);
-        for (int t0 = threadIdx.x; t0 < np; t0 += SV_U * SV_BS) {
+        Walk2 w(IM, threadIdx.x, BS);
+        for (int t0 = threadIdx.x; t0 < np; t0 += SV_U * BS) {
             float d0[SV_U], x[SV_U][4];
             int pi[SV_U], pk[SV_U];
 #pragma unroll
@@ -665,7 +671,7 @@ __global__ void __launch_bounds__(SV_BS, 4) k_ts_smooth(const __grid_constant__ 
                 pi[u] = w.i;
                 pk[u] = w.k;
                 w.next();
-                if (t0 + u * SV_BS < np) {
+                if (t0 + u * BS < np) {
                     const float *p = Sj + (size_t)(pi[u] - 1) + ks * (pk[u] - 1);
                     d0[u] = p[0];
 #pragma unroll
@@ -675,7 +681,7 @@ __global__ void __launch_bounds__(SV_BS, 4) k_ts_smooth(const __grid_constant__ 
             }
 #pragma unroll
             for (int u = 0; u < SV_U; ++u) {
-                const int t = t0 + u * SV_BS;
+                const int t = t0 + u * BS;
                 if (t >= np) break;
                 const int i = pi[u], k = pk[u];
                 const float dd = d0[u];
@@ -706,8 +712,8 @@ __global__ void __launch_bounds__(SV_BS, 4) k_ts_smooth(const __grid_constant__ 
     const bool periodic_j = !(A1(d.IND, j) == 1 || A1(d.INDLE, j) == 1);
     if (j >= 2 && !(c->SFT < 0.0001f)) {
         const float SFT = c->SFT, SFT1 = c->SFT1, F4 = d.FAC_4TH;
-        Walk2 w(IM, threadIdx.x, SV_BS);
-        for (int t = threadIdx.x; t < np; t += SV_BS, w.next()) {
+        Walk2 w(IM, threadIdx.x, BS);
+        for (int t = threadIdx.x; t < np; t += BS, w.next()) {
             const int i = w.i, k = w.k;
             const float *ak = a + IM * (k - 1) - 1;     // ak[i] = P(a, i, k)
             auto curve = [&](int ii) -> float {
@@ -736,8 +742,8 @@ __global__ void __launch_bounds__(SV_BS, 4) k_ts_smooth(const __grid_constant__ 
             b[t] = SFT1 * ak[i] + SFT * (AVG + F4 * SC);
         }
         __syncthreads();
-        w = Walk2(IM, threadIdx.x, SV_BS);
-        for (int t = threadIdx.x; t < np; t += SV_BS, w.next()) {
+        w = Walk2(IM, threadIdx.x, BS);
+        for (int t = threadIdx.x; t < np; t += BS, w.next()) {
             const int i = w.i, k = w.k;
             const float *bi = b + (i - 1) - IM;         // bi[IM * kk] = P(b, i, kk)
             auto curvek = [&](int kk) -> float {
@@ -776,13 +782,13 @@ __global__ void __launch_bounds__(SV_BS, 4) k_ts_smooth(const __grid_constant__ 
     }
     if (!(d.SFEXIT < 0.0001f) && j >= d.JM + 1 - d.NSFEXIT) {
         const float SE = d.SFEXIT, SE1 = 1.0f - SE, SEH = 0.5f * SE;
-        for (int k = threadIdx.x + 1; k <= KM; k += SV_BS) {
+        for (int k = threadIdx.x + 1; k <= KM; k += BS) {
             for (int i = 2; i <= IMM1; ++i) P(a, i, k) = SE1 * P(a, i, k) + SEH * (P(a, i + 1, k) + P(a, i - 1, k));
             P(a, 1, k) = P(a, 1, k) + SE * (2.0f * P(a, 2, k) - P(a, 3, k) - P(a, 1, k));
             P(a, IM, k) = P(a, IM, k) + SE * (2.0f * P(a, IMM1, k) - P(a, d.IMM2, k) - P(a, IM, k));
         }
         __syncthreads();
-        for (int i = threadIdx.x + 1; i <= IM; i += SV_BS) {
+        for (int i = threadIdx.x + 1; i <= IM; i += BS) {
             for (int k = 2; k <= KMM1; ++k) P(a, i, k) = SE1 * P(a, i, k) + SEH * (P(a, i, k - 1) + P(a, i, k + 1));
             P(a, i, 1) = P(a, i, 1) + SE * (2.0f * P(a, i, 2) - P(a, i, 3) - P(a, i, 1));
             P(a, i, KM) = P(a, i, KM) + SE * (2.0f * P(a, i, KMM1) - P(a, i, d.KMM2) - P(a, i, KM));
@@ -796,7 +802,7 @@ __global__ void __launch_bounds__(SV_BS, 4) k_ts_smooth(const __grid_constant__ 
         if (K1 == 1) K2 = K2 - 1;
         if (K2 == KM) K1 = K1 + 1;
     }
-    for (int k = threadIdx.x + 1; k <= KM; k += SV_BS) {
+    for (int k = threadIdx.x + 1; k <= KM; k += BS) {
         if (periodic_j) {
             float v = 0.5f * (P(a, 1, k) + P(a, IM, k));
             P(a, 1, k) = v;
@@ -814,7 +820,7 @@ __global__ void __launch_bounds__(SV_BS, 4) k_ts_smooth(const __grid_constant__ 
         for (int r = 1; r <= d.NRWSM1; ++r)
             if (j == A1(d.JMIX, r) || j == A1(d.JMIX, r) + 1) mp = true;
     if (mp) {
-        for (int k = threadIdx.x + 1; k <= KM; k += SV_BS) {
+        for (int k = threadIdx.x + 1; k <= KM; k += BS) {
             float s;
             if (d.REDUCE_ORDER == 1) {
                 s = 0.0f;
@@ -827,13 +833,13 @@ __global__ void __launch_bounds__(SV_BS, 4) k_ts_smooth(const __grid_constant__ 
             b[k - 1] = 0.5f * s;
         }
         __syncthreads();
-        for (int t = threadIdx.x; t < np; t += SV_BS) a[t] = b[t / IM];
+        for (int t = threadIdx.x; t < np; t += BS) a[t] = b[t / IM];
         __syncthreads();
     }
 #undef P
     float *Dj = D + (size_t)IM * (j - 1);
-    Walk2 w(IM, threadIdx.x, SV_BS);
-    for (int t = threadIdx.x; t < np; t += SV_BS, w.next()) Dj[(size_t)(w.i - 1) + ks * (w.k - 1)] = a[t];
+    Walk2 w(IM, threadIdx.x, BS);
+    for (int t = threadIdx.x; t < np; t += BS, w.next()) Dj[(size_t)(w.i - 1) + ks * (w.k - 1)] = a[t];
 }
 
 // ---------------------------------------------------------------------
@@ -892,37 +898,46 @@ static size_t prolong_smem(const Dev &d) { return ((size_t)d.NIB1 * d.NKB1 + (si
 static size_t update_smem(const Dev &d) { return (size_t)2 * d.IMM1 * d.KMM1 * sizeof(float); }
 static size_t smooth_smem(const Dev &d) { return ((size_t)2 * d.IM * d.KM + 2 * d.IM + 2 * d.KM) * sizeof(float); }
 
-cudaError_t configure_kernels(const Dev &d) {
+template <int BS>
+static cudaError_t configure_bs(const Dev &d) {
     struct {
         const void *f;
         size_t bytes;
-    } k[] = {{(const void *)k_ts_cells, cells_smem(d)},
-             {(const void *)k_ts_prolong, prolong_smem(d)},
-             {(const void *)k_ts_update, update_smem(d)},
-             {(const void *)k_ts_smooth, smooth_smem(d)}};
+    } k[] = {{(const void *)k_ts_cells<BS>, cells_smem(d)},
+             {(const void *)k_ts_prolong<BS>, prolong_smem(d)},
+             {(const void *)k_ts_update<BS>, update_smem(d)},
+             {(const void *)k_ts_smooth<BS>, smooth_smem(d)}};
     for (auto &x : k) {
         if (x.bytes > 200 * 1024) return cudaErrorInvalidValue;
         int want = (int)(x.bytes > 48 * 1024 ? x.bytes : 48 * 1024);
         cudaError_t e = cudaFuncSetAttribute(x.f, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
         if (e != cudaSuccess) return e;
     }
-    cudaError_t e = configure_loss_kernels(d);
+    return cudaSuccess;
+}
+
+cudaError_t configure_kernels(const Dev &d) {
+    cudaError_t e = configure_bs<128>(d);
+    if (e == cudaSuccess) e = configure_bs<256>(d);
+    if (e == cudaSuccess) e = configure_bs<512>(d);
+    if (e == cudaSuccess) e = configure_loss_kernels(d);
     return e != cudaSuccess ? e : configure_flux_kernels(d);
 }
 
-void launch_tstep(const Dev &d, Launch L, int v0, int nv) {
+template <int BS>
+static void launch_tstep_bs(const Dev &d, Launch L, int v0, int nv) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
     unsigned gN = grid_for(N, 256);
     const bool seq = d.REDUCE_ORDER == 1;
     const unsigned jp = (unsigned)(d.JM - 1), ja = (unsigned)d.JM, vy = (unsigned)nv;
-    launchk(L, k_ts_cells, dim3(jp, vy), dim3(TS_BS), cells_smem(d), d, v0);
+    launchk(L, k_ts_cells<BS>, dim3(jp, vy), dim3(BS), cells_smem(d), d, v0);
     mark(L, "k_ts_cells");
     if (seq) {
         int nb = d.NIB1 * (d.NJB1 + 1) * d.NKB1 + d.NIB2 * (d.NJB2 + 1) * d.NKB2 + d.NSBLK;
         launchk(L, k_ts_restrict_seq, dim3(grid_for(nb, 64), vy), dim3(64), 0, d, v0);
         mark(L, "k_ts_restrict_seq");
     }
-    launchk(L, k_ts_prolong, dim3(jp, vy), dim3(TS_BS), prolong_smem(d), d, v0, (d.NRSMTH == 0 && !seq) ? 1 : 0);
+    launchk(L, k_ts_prolong<BS>, dim3(jp, vy), dim3(BS), prolong_smem(d), d, v0, (d.NRSMTH == 0 && !seq) ? 1 : 0);
     mark(L, "k_ts_prolong");
     if (d.NRSMTH > 0) {
         for (int it = 0; it < d.NRSMTH; ++it) {
@@ -936,7 +951,7 @@ void launch_tstep(const Dev &d, Launch L, int v0, int nv) {
             mark(L, "k_copy_tm_st");
         }
         if (!seq) {
-            launchk(L, k_ts_plane_abs, dim3(jp, vy), dim3(TS_BS), 0, d, v0);
+            launchk(L, k_ts_plane_abs<BS>, dim3(jp, vy), dim3(BS), 0, d, v0);
             mark(L, "k_ts_plane_abs");
         }
     }
@@ -944,10 +959,16 @@ void launch_tstep(const Dev &d, Launch L, int v0, int nv) {
         launchk(L, k_ts_avgblk_seq, dim3(1, vy), dim3(32), 0, d, v0);
         mark(L, "k_ts_avgblk_seq");
     }
-    launchk(L, k_ts_update, dim3(ja, vy), dim3(TS_BS), update_smem(d), d, v0);
+    launchk(L, k_ts_update<BS>, dim3(ja, vy), dim3(BS), update_smem(d), d, v0);
     mark(L, "k_ts_update");
-    launchk(L, k_ts_smooth, dim3(ja, vy), dim3(SV_BS), smooth_smem(d), d, v0);
+    launchk(L, k_ts_smooth<BS>, dim3(ja, vy), dim3(BS), smooth_smem(d), d, v0);
     mark(L, "k_ts_smooth");
+}
+
+void launch_tstep(const Dev &d, Launch L, int v0, int nv) {
+    if (d.ts_bs == 128) launch_tstep_bs<128>(d, L, v0, nv);
+    else if (d.ts_bs == 512) launch_tstep_bs<512>(d, L, v0, nv);
+    else launch_tstep_bs<256>(d, L, v0, nv);
 }
 
 }  // namespace mgpu

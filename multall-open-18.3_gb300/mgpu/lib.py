@@ -45,7 +45,7 @@ EXPORTS = ["mgpu_abi_version", "mgpu_last_error", "mgpu_device_count", "mgpu_cre
            "mgpu_step_io_bytes", "mgpu_integrals_noalloc", "mgpu_batch_create", "mgpu_batch_destroy",
            "mgpu_batch_run", "mgpu_batch_bench_steps", "mgpu_adjoint_prepare", "mgpu_adjoint_objective",
            "mgpu_adjoint_iterate", "mgpu_adjoint_solve", "mgpu_adjoint_gradient", "mgpu_adjoint_get",
-           "mgpu_adjoint_set", "mgpu_adjoint_solve_krylov"]
+           "mgpu_adjoint_set", "mgpu_adjoint_solve_krylov", "mgpu_autotune"]
 
 _lib = None
 
@@ -94,6 +94,7 @@ def load(build: bool = True):
     L.mgpu_adjoint_iterate.argtypes = [vp, i32, dp]
     L.mgpu_adjoint_solve.argtypes = [vp, i32, ctypes.c_double, ctypes.POINTER(i32), dp]
     L.mgpu_adjoint_gradient.argtypes = [vp]
+    L.mgpu_autotune.argtypes = [vp, ctypes.POINTER(i32), dp]
     L.mgpu_adjoint_solve_krylov.argtypes = [vp, i32, i32, i32, ctypes.c_double, ctypes.POINTER(i32), dp]
     L.mgpu_adjoint_get.argtypes = [vp, cp, vp, ctypes.c_int64]
     L.mgpu_adjoint_set.argtypes = [vp, cp, vp, ctypes.c_int64]
@@ -219,6 +220,13 @@ class Problem:
     def kernels_per_step(self, loss: bool = False, tail: bool = False) -> int:
         """Kernel launches of one step (LOSS and tail steps launch more)."""
         return _chk(load().mgpu_kernels_per_step(self.h, (1 if loss else 0) | (2 if tail else 0)))
+
+    def autotune(self) -> tuple[int, list]:
+        """(threads per J-plane CTA chosen, [ms per TSTEP pass for 128, 256, 512])."""
+        c = ctypes.c_int32()
+        ms = (ctypes.c_double * 3)()
+        _chk(load().mgpu_autotune(self.h, ctypes.byref(c), ms))
+        return c.value, list(ms)
 
     def bench_steps(self, nsteps: int, flush_l2: bool = True) -> float:
         """Sum of the device times (ms) of nsteps iterations."""

@@ -355,3 +355,28 @@ def test_api_errors(mods):
     with pytest.raises(lib.MgpuError) as e:
         gpu.set("AQX", cd.arrays["AQX"])      # geometry is fixed after commit
     assert e.value.code == -2
+
+
+@pytest.mark.parametrize("bs", [128, 512])
+def test_tstep_cta_sizes_match_oracle(mods, bs):
+    """Every CTA size the autotuner can choose gives the oracle's step: the
+    small stage after one step within 1e-5 and after five steps (LOSS and
+    tail) within 1e-4, with TSTEP set to each size through TS_THREADS."""
+    case, common_setup, lib, O = mods
+    cd = common_setup.build_common(case.small_stage())
+    probe = lib.Problem(cd)
+    chosen, ms = probe.autotune()
+    assert chosen in (128, 256, 512) and all(m > 0 for m in ms)
+    probe.close()
+    cd.ints["TS_THREADS"] = bs
+    gpu = lib.Problem(cd)
+    ref = O.Oracle(cd)
+    ref.setup_calls()
+    for n in range(5):
+        gpu.step()
+        ref.step()
+        if n == 0:
+            for name in ("RO", "ROE", "ROVX", "RORVT", "ROVR"):
+                assert rel_linf(gpu.get(name), ref.get(name)) <= 1e-5, (bs, name)
+    for name in ("RO", "ROE", "ROVX", "RORVT", "ROVR"):
+        assert rel_linf(gpu.get(name), ref.get(name)) <= 1e-4, (bs, name)
