@@ -341,6 +341,18 @@ def run_adjoint(args, rank, world, local_rank):
     cd.ints["NSTEPS_MAX"] = 10 ** 9
     cd.reals["CONLIM"] = 1e-9
     n_primal, inner, restart, max_steps, n_fd = 16000, 50, 30, 20000, 10000
+    if os.environ.get("MGPU_ADJ_PROFILE") == "1":
+        # a short run for kernel profiles: 200 primal steps, then 20 transposed
+        # steps with an objective and the geometry pass, no solve and no FD
+        p = lib.Problem(cd)
+        p.run(200)
+        p.adjoint_prepare()
+        p.adjoint_objective("eta_tt")
+        rel = p.adjoint_iterate(20)
+        p.adjoint_gradient()
+        print(json.dumps({"workload": "adjoint profile run", "transposed_steps": 21, "rel_change": rel}), flush=True)
+        p.close()
+        return 0
     p = lib.Problem(cd)
     p.run(max(args.warmup, 3))
     p.close()
@@ -433,8 +445,10 @@ def run_gpu(args, rank, world, local_rank):
     kps = prob.kernels_per_step()
     kps_loss, kps_tail = prob.kernels_per_step(loss=True) - kps, prob.kernels_per_step(tail=True) - kps
     prob.run(max(args.warmup, 3))
-    tuned, tune_ms = prob.autotune()        # threads per J-plane CTA of the TSTEP kernels
-    prob.run(3)
+    tuned, tune_ms = 256, [None, None, None]
+    if os.environ.get("MGPU_AUTOTUNE", "1") != "0":
+        tuned, tune_ms = prob.autotune()    # threads per J-plane CTA of the TSTEP kernels
+        prob.run(3)
     dist_barrier(dist)
     with ClockSampler(0) as clk:
         t_wall0 = time.perf_counter()

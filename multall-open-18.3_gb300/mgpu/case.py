@@ -360,11 +360,16 @@ def turbine_stage(im=65, jm_row=121, km=49, seed=1, pexit=0.85e5, rpm=9000.0) ->
                     nchange=1000, conlim=0.00001)
 
 
-def compressor_4stage(im=73, jm_row=89, km=57, seed=4) -> CaseSpec:
+def compressor_4stage(im=73, jm_row=89, km=57, seed=4, pr_row=1.10, chi_rotor=(-66.0, -54.0),
+                      chi_stator=(39.0, 8.0)) -> CaseSpec:
     """Four-stage axial compressor, 8 rows (36,52,40,56,44,60,48,64 blades),
     12000 rpm, hub 0.25 m, casing tapering 0.40 -> 0.33 m, P0 1.013e5 Pa,
     T0 288.15 K; double-circular-arc sections with t/c 0.08 and +-0.3 deg
-    noise; 73 x 752 x 57 with mixing planes between all rows."""
+    noise; 73 x 752 x 57 with mixing planes between all rows.  The metal
+    angles follow the mean-radius velocity triangles at 12000 rpm (blade
+    speed ~390 m/s, axial velocity ~160 m/s: relative inflow ~-68 deg, de
+    Haller ratio ~0.72; stator inflow ~39 deg), and the exit static pressure
+    is the inlet's times pr_row per row (2.14 over the 8 rows)."""
     counts = [36, 52, 40, 56, 44, 60, 48, 64]
     rows = []
     npts = []
@@ -379,10 +384,11 @@ def compressor_4stage(im=73, jm_row=89, km=57, seed=4) -> CaseSpec:
         lead = n - jm_row if nr == 0 else 0
         jle = lead + int(round(jm_row * 0.25))
         jte = lead + int(round(jm_row * 0.75))
-        p_in, p_out = p, p * 1.12
+        p_in, p_out = p, p * pr_row
         rows.append(RowSpec(nblade=nb, jm=n, jle=jle, jte=jte,
                             rpm=12000.0 if rotor else 0.0, rpm_hub=12000.0 if rotor else 0.0,
-                            chi_in=(-55.0 if rotor else 40.0), chi_out=(-30.0 if rotor else 5.0),
+                            chi_in=(chi_rotor[0] if rotor else chi_stator[0]),
+                            chi_out=(chi_rotor[1] if rotor else chi_stator[1]),
                             tmax=0.08, xtmax=0.5, tle=0.01, tte=0.01, chord=0.03,
                             up_len=0.012 + (0.03 if nr == 0 else 0.0),
                             dn_len=0.012 + (0.03 if nr == 7 else 0.0),
