@@ -1698,7 +1698,7 @@ int configure(const Dev &d) {
              {(const void *)rk_ts_cells, cells_bytes(d)}};
     for (auto &x : k) {
         if (x.b > 200 * 1024) return api_fail(MGPU_E_UNSUPPORTED, "J-plane too large for the adjoint kernels");
-        ACK(cudaFuncSetAttribute(x.f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(x.b > 48 * 1024 ? x.b : 48 * 1024)));
+        ACK(raise_smem(x.f, x.b));
     }
     return 0;
 }

@@ -445,9 +445,7 @@ __global__ void k_bc_apply(Dev d) {
 static size_t bc_sums_smem(const Dev &d) { return (size_t)32 * (4 * d.IMM1 + 2 * d.IM) * sizeof(float); }
 
 cudaError_t configure_flux_kernels(const Dev &d) {
-    size_t b = bc_sums_smem(d);
-    return cudaFuncSetAttribute((const void *)k_bc_sums, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(b > 48 * 1024 ? b : 48 * 1024));
+    return raise_smem((const void *)k_bc_sums, bc_sums_smem(d));
 }
 
 void launch_bc_sums(const Dev &d, Launch L) {

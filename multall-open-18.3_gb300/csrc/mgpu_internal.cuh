@@ -239,6 +239,19 @@ void launch_tail(const Dev &d, Launch L);
 void launch_stepup(const Dev &d, Launch L, float relax, bool gated);
 void launch_integrals(const Dev &d, Launch L, double *out8);
 
+// Raises a kernel's dynamic shared-memory limit to `bytes` (at least the
+// 48 KB default) and never lowers it: the limit belongs to the function, not
+// to a handle, so handles of different sizes (a batch) must not shrink one
+// another's.
+inline cudaError_t raise_smem(const void *f, size_t bytes) {
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, f);
+    if (e != cudaSuccess) return e;
+    const int want = (int)(bytes > 48 * 1024 ? bytes : 48 * 1024);
+    if (a.maxDynamicSharedSizeBytes >= want) return cudaSuccess;
+    return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
+}
+
 // sets per-kernel attributes (dynamic shared memory of the J-plane kernels
 // and of the LOSS kernels)
 cudaError_t configure_kernels(const Dev &d);

@@ -661,16 +661,13 @@ cudaError_t configure_loss_kernels(const Dev &d) {
     size_t kb = loss_kfaces_smem(d), ib = loss_ifaces_smem(d), pb = pwallgrad_smem(d);
     if (d.YPLUSWALL < -10.0f) {
         if (pb > 220 * 1024) return cudaErrorInvalidValue;
-        cudaError_t e = cudaFuncSetAttribute((const void *)k_pwallgrad_smooth, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)(pb > 48 * 1024 ? pb : 48 * 1024));
+        cudaError_t e = raise_smem((const void *)k_pwallgrad_smooth, pb);
         if (e != cudaSuccess) return e;
     }
     if (kb > 220 * 1024 || ib > 220 * 1024) return cudaErrorInvalidValue;   // KM <= 160: kb <= 201 KB
-    cudaError_t e = cudaFuncSetAttribute((const void *)k_loss_kfaces, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(kb > 48 * 1024 ? kb : 48 * 1024));
+    cudaError_t e = raise_smem((const void *)k_loss_kfaces, kb);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute((const void *)k_loss_ifaces, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(ib > 48 * 1024 ? ib : 48 * 1024));
+    return raise_smem((const void *)k_loss_ifaces, ib);
 }
 
 void launch_loss(const Dev &d, Launch L, bool init_call) {

@@ -909,8 +909,7 @@ static cudaError_t configure_bs(const Dev &d) {
              {(const void *)k_ts_smooth<BS>, smooth_smem(d)}};
     for (auto &x : k) {
         if (x.bytes > 200 * 1024) return cudaErrorInvalidValue;
-        int want = (int)(x.bytes > 48 * 1024 ? x.bytes : 48 * 1024);
-        cudaError_t e = cudaFuncSetAttribute(x.f, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
+        cudaError_t e = raise_smem(x.f, x.bytes);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;

@@ -380,3 +380,25 @@ def test_tstep_cta_sizes_match_oracle(mods, bs):
                 assert rel_linf(gpu.get(name), ref.get(name)) <= 1e-5, (bs, name)
     for name in ("RO", "ROE", "ROVX", "RORVT", "ROVR"):
         assert rel_linf(gpu.get(name), ref.get(name)) <= 1e-4, (bs, name)
+
+
+def test_handles_of_different_sizes_keep_their_launch_limits(mods):
+    """A kernel's dynamic shared-memory limit is per function, not per
+    handle: committing a small problem after a large one must not lower the
+    limit the large one needs (k_bc_sums takes 49 KB at IM = 65).  Both
+    step, alone and in one batch, with the large one's values the same
+    either way."""
+    case, common_setup, lib, O = mods
+    big = common_setup.build_common(case.turbine_stage(im=65, jm_row=30, km=9, seed=6))
+    small = common_setup.build_common(case.turbine_stage(im=33, jm_row=30, km=9, seed=7))
+    pb = lib.Problem(big)
+    ps = lib.Problem(small)
+    pb.run(6)
+    ps.run(6)
+    alone = pb.get("RO").copy()
+    pb2 = lib.Problem(big)
+    ps2 = lib.Problem(small)
+    b = lib.Batch([pb2, ps2])
+    b.run(6)
+    assert np.array_equal(pb2.get("RO"), alone)
+    b.close()
