@@ -23,6 +23,11 @@
 // below the FP32 adjoint's accuracy.  Branches (limits, the flow-direction
 // tests, |STORE| in the negative feedback) are taken as the recorded step
 // took them.
+//
+// The per-node reverse kernels take Dev and Adj by value and inline their
+// helpers, so every member read stays a constant-bank parameter load; only
+// the J-plane kernels, which index a.v by blockIdx.y, take them as
+// __grid_constant__.
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -62,6 +67,7 @@ struct Adj {
     const float *tROL, *tROM, *tWT, *tVLIM, *tROLIM, *tDC0, *tDCA;
     const int *tDCOL;
     float *WT;                   // adjoint of WT (k_flux_mass), read by the Mach limiter
+    float *cf;                   // per-face coefficients of the flux reverses (MOM_NCOEF x N)
     const DevCtl *tctl;
     // geometry adjoints, accumulated when geom != 0
     float *gAQX, *gAQR, *gABX, *gABR, *gABT, *gASX, *gASR, *gVOLOR;
@@ -85,7 +91,7 @@ __device__ __forceinline__ void aadd(float *p, float v) {
 // =====================================================================
 // R1: primitive variables (k_prim)
 // =====================================================================
-__global__ void rk_prim(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+__global__ void rk_prim(const Dev d, const Adj a) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = d.IM * d.JM * d.KM;
     if (n >= N) return;
@@ -131,11 +137,11 @@ __global__ void rk_prim(const __grid_constant__ Dev d, const __grid_constant__ A
 // R2: mass fluxes (k_flux_mass)
 // =====================================================================
 // pre-step ROVT: J=1 from the previous inlet condition, J>=2 from k_prim
-__device__ inline float pre_rovt(const Dev &d, const Adj &a, int i, int j, int k) {
+__device__ __forceinline__ float pre_rovt(const Dev &d, const Adj &a, int i, int j, int k) {
     return j == 1 ? AIK(a.tROVT1, i, k) : A3(a.tROVT, i, j, k);
 }
 
-__device__ inline void rev_flowt_raw(const Dev &d, const Adj &a, int i, int j, int k, float g) {
+__device__ __forceinline__ void rev_flowt_raw(const Dev &d, const Adj &a, int i, int j, int k, float g) {
     if (g == 0.0f) return;
     const float c = 0.25f * g;
     const float abx = A3(d.ABX, i, j, k), abt = A2(d.ABT, j, k), abr = A3(d.ABR, i, j, k);
@@ -160,82 +166,139 @@ __device__ inline void rev_flowt_raw(const Dev &d, const Adj &a, int i, int j, i
     }
 }
 
-__global__ void rk_flux_mass(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+// Two passes like rk_flux_mom.  Coefficients cf[q * N + owner]: FLOWX q = 0, 1
+// (ROVX, ROVR on the owner's K-face nodes), FLOWT q = 2..4 (ROVX; ROVT and
+// -U RO from ABT; ROVR on its I-face nodes), FLOWR q = 5, 6 (ROVX, ROVR on
+// its J-face nodes).  The periodic edge faces scatter with atomics.
+__global__ void rk_flux_mass_coef(const Dev d, const Adj a) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = d.IM * d.JM * d.KM;
     if (n >= N) return;
     int i, j, k;
     node_ijk(d, (size_t)n, i, j, k);
+    float c[7] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     if (i < d.IM && k < d.KM) {
         const float g = a.FLOWX[n];
         a.FLOWX[n] = 0.0f;
         if (g != 0.0f) {
-            const float c = 0.25f * g;
-            const int m[4] = {n, ix3(d, i, j, k + 1), ix3(d, i + 1, j, k), ix3(d, i + 1, j, k + 1)};
-            float sx = 0.0f, sr = 0.0f;
-            for (int q = 0; q < 4; ++q) {
-                aadd(&a.v[V_ROVX].D[m[q]], c * d.AQX[n]);
-                aadd(&a.v[V_ROVR].D[m[q]], c * d.AQR[n]);
-                sx += a.tROVX[m[q]];
-                sr += a.tROVR[m[q]];
-            }
+            c[0] = 0.25f * g * d.AQX[n];
+            c[1] = 0.25f * g * d.AQR[n];
             if (a.geom) {
-                aadd(&a.gAQX[n], c * sx);
-                aadd(&a.gAQR[n], c * sr);
+                const int m[4] = {n, ix3(d, i, j, k + 1), ix3(d, i + 1, j, k), ix3(d, i + 1, j, k + 1)};
+                float sx = 0.0f, sr = 0.0f;
+                for (int q = 0; q < 4; ++q) {
+                    sx += a.tROVX[m[q]];
+                    sr += a.tROVR[m[q]];
+                }
+                aadd(&a.gAQX[n], 0.25f * g * sx);
+                aadd(&a.gAQR[n], 0.25f * g * sr);
             }
         }
     }
     if (j >= 2 && k < d.KM) {
         const float g = a.FLOWT[n];
         a.FLOWT[n] = 0.0f;
-        if (i == 1 || i == d.IM) {
-            if (A1(d.IND, j) != 1) {
-                rev_flowt_raw(d, a, 1, j, k, 0.5f * g);
-                rev_flowt_raw(d, a, d.IM, j, k, 0.5f * g);
-            } else {
-                const int nr = A1(d.NROW, j);
-                if (!(k >= A1(d.KS1, nr) && k <= A1(d.KS2, nr))) rev_flowt_raw(d, a, i, j, k, g);
-            }
+        const bool end = i == 1 || i == d.IM;
+        if (end && A1(d.IND, j) != 1) {
+            rev_flowt_raw(d, a, 1, j, k, 0.5f * g);
+            rev_flowt_raw(d, a, d.IM, j, k, 0.5f * g);
         } else {
-            rev_flowt_raw(d, a, i, j, k, g);
-        }
-    }
-    {
-        // WT = (ROVT - U RO) / RO
-        const float gw = a.WT[n];
-        if (gw != 0.0f) {
-            a.WT[n] = 0.0f;
-            const float ro = a.tRO[n];
-            aadd(&a.ROVT[n], gw / ro);
-            aadd(&a.v[V_RO].D[n], -gw * pre_rovt(d, a, i, j, k) / (ro * ro));
+            bool on = true;
+            if (end) {
+                const int nr = A1(d.NROW, j);
+                if (k >= A1(d.KS1, nr) && k <= A1(d.KS2, nr)) on = false;
+            }
+            if (on && g != 0.0f) {
+                c[2] = 0.25f * g * d.ABX[n];
+                c[3] = 0.25f * g * A2(d.ABT, j, k);
+                c[4] = 0.25f * g * d.ABR[n];
+                if (a.geom) {
+                    const int jj[4] = {j, j - 1, j - 1, j}, kk[4] = {k, k, k + 1, k + 1};
+                    float sx = 0.0f, st = 0.0f, sr = 0.0f;
+                    for (int q = 0; q < 4; ++q) {
+                        const int m = ix3(d, i, jj[q], kk[q]);
+                        sx += a.tROVX[m];
+                        st += pre_rovt(d, a, i, jj[q], kk[q]) - A2(d.UBLADE, jj[q], kk[q]) * a.tRO[m];
+                        sr += a.tROVR[m];
+                    }
+                    aadd(&a.gABX[n], 0.25f * g * sx);
+                    aadd(&A2(a.gABT, j, k), 0.25f * g * st);
+                    aadd(&a.gABR[n], 0.25f * g * sr);
+                }
+            }
         }
     }
     if (i < d.IM && j >= 2) {
         const float g = a.FLOWR[n];
         a.FLOWR[n] = 0.0f;
         if (g != 0.0f && k >= 2 && k <= d.KMM1) {
-            const float c = 0.25f * g;
-            const int m[4] = {n, ix3(d, i, j - 1, k), ix3(d, i + 1, j - 1, k), ix3(d, i + 1, j, k)};
-            float sx = 0.0f, sr = 0.0f;
-            for (int q = 0; q < 4; ++q) {
-                aadd(&a.v[V_ROVX].D[m[q]], c * d.ASX[n]);
-                aadd(&a.v[V_ROVR].D[m[q]], c * d.ASR[n]);
-                sx += a.tROVX[m[q]];
-                sr += a.tROVR[m[q]];
-            }
+            c[5] = 0.25f * g * d.ASX[n];
+            c[6] = 0.25f * g * d.ASR[n];
             if (a.geom) {
-                aadd(&a.gASX[n], c * sx);
-                aadd(&a.gASR[n], c * sr);
+                const int m[4] = {n, ix3(d, i, j - 1, k), ix3(d, i + 1, j - 1, k), ix3(d, i + 1, j, k)};
+                float sx = 0.0f, sr = 0.0f;
+                for (int q = 0; q < 4; ++q) {
+                    sx += a.tROVX[m[q]];
+                    sr += a.tROVR[m[q]];
+                }
+                aadd(&a.gASX[n], 0.25f * g * sx);
+                aadd(&a.gASR[n], 0.25f * g * sr);
             }
         }
     }
+    for (int q = 0; q < 7; ++q) a.cf[(size_t)q * N + n] = c[q];
+}
+
+__global__ void rk_flux_mass_gather(const Dev d, const Adj a) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, (size_t)n, i, j, k);
+    const float *cf = a.cf;
+    auto C = [&](int q, int o) { return cf[(size_t)q * N + o]; };
+    float gX = 0.0f, gR = 0.0f, gT = 0.0f;
+    for (int di = 0; di < 2; ++di)
+        for (int dk = 0; dk < 2; ++dk) {
+            const int ii = i - di, kk = k - dk;
+            if (ii < 1 || kk < 1) continue;
+            const int o = ix3(d, ii, j, kk);
+            gX += C(0, o); gR += C(1, o);
+        }
+    for (int dj = 0; dj < 2; ++dj)
+        for (int dk = 0; dk < 2; ++dk) {
+            const int jj = j + dj, kk = k - dk;
+            if (jj > d.JM || kk < 1) continue;
+            const int o = ix3(d, i, jj, kk);
+            gX += C(2, o); gT += C(3, o); gR += C(4, o);
+        }
+    for (int di = 0; di < 2; ++di)
+        for (int dj = 0; dj < 2; ++dj) {
+            const int ii = i - di, jj = j + dj;
+            if (ii < 1 || jj > d.JM) continue;
+            const int o = ix3(d, ii, jj, k);
+            gX += C(5, o); gR += C(6, o);
+        }
+    float gRO = -gT * A2(d.UBLADE, j, k), gRV = gT;
+    // WT = (ROVT - U RO) / RO of this node
+    const float gw = a.WT[n];
+    if (gw != 0.0f) {
+        a.WT[n] = 0.0f;
+        const float ro = a.tRO[n];
+        gRV += gw / ro;
+        gRO -= gw * pre_rovt(d, a, i, j, k) / (ro * ro);
+    }
+    a.v[V_ROVX].D[n] += gX;
+    a.v[V_ROVR].D[n] += gR;
+    a.ROVT[n] += gRV;
+    a.v[V_RO].D[n] += gRO;
 }
 
 // =====================================================================
 // R3: exit pitchwise sums and the radial-equilibrium recurrence (k_bc_sums)
 // IPOUT = 0: PD(1) = PDOWN_HUB, PD(K) = 0.9 PD(K) + 0.1 (PD(K-1) + DP(K))
 // =====================================================================
-__global__ void __launch_bounds__(256) rk_bc_sums(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+__global__ void __launch_bounds__(256) rk_bc_sums(const Dev d, const Adj a) {
     __shared__ float gss[512];
     const int KM = d.KM, IM = d.IM, IMM1 = d.IMM1;
     for (int k = threadIdx.x; k < KM; k += blockDim.x) gss[k] = 0.0f;
@@ -272,11 +335,11 @@ __global__ void __launch_bounds__(256) rk_bc_sums(const __grid_constant__ Dev d,
 // =====================================================================
 // R4: energy fluxes (k_flux_energy); HO(JM) and PEFF as the step began
 // =====================================================================
-__device__ inline float pre_ho(const Dev &d, const Adj &a, int i, int j, int k) {
+__device__ __forceinline__ float pre_ho(const Dev &d, const Adj &a, int i, int j, int k) {
     return j == d.JM ? AIK(a.tHOJM, i, k) : A3(a.tHO, i, j, k);
 }
 
-__device__ inline void rev_tflux_energy_raw(const Dev &d, const Adj &a, int i, int j, int k, float g) {
+__device__ __forceinline__ void rev_tflux_energy_raw(const Dev &d, const Adj &a, int i, int j, int k, float g) {
     if (g == 0.0f) return;
     const float c = 0.25f * g;
     const int jj[4] = {j, j - 1, j - 1, j}, kk[4] = {k, k, k + 1, k + 1};
@@ -291,25 +354,26 @@ __device__ inline void rev_tflux_energy_raw(const Dev &d, const Adj &a, int i, i
     aadd(&A3(a.FLOWT, i, j, k), c * sho);
 }
 
-__global__ void rk_flux_energy(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+// Two passes.  Coefficients cf[q * N + owner]: XFLUX q = 0 (HO on the K-face
+// nodes), RFLUX q = 1 (HO on the J-face nodes), TFLUX q = 2, 3 (HO, PEFF on the
+// I-face nodes); the periodic edge faces scatter with atomics.
+__global__ void rk_flux_energy_coef(const Dev d, const Adj a) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = d.IM * d.JM * d.KM;
     if (n >= N) return;
     int i, j, k;
     node_ijk(d, (size_t)n, i, j, k);
     const AdjVar &V = a.v[V_ROE];
+    float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     if (i < d.IM && k < d.KM) {
         const float g = V.XF[n];
         V.XF[n] = 0.0f;
         if (g != 0.0f) {
-            const int m[4] = {n, ix3(d, i, j, k + 1), ix3(d, i + 1, j, k), ix3(d, i + 1, j, k + 1)};
-            const int mj[4] = {j, j, j, j}, mk[4] = {k, k + 1, k, k + 1}, mi[4] = {i, i, i + 1, i + 1};
+            const int mi[4] = {i, i, i + 1, i + 1}, mk[4] = {k, k + 1, k, k + 1};
             float sho = 0.0f;
-            for (int q = 0; q < 4; ++q) {
-                sho += pre_ho(d, a, mi[q], mj[q], mk[q]);
-                aadd(&a.HO[m[q]], g * a.tFLOWX[n] * 0.25f);
-            }
-            aadd(&a.FLOWX[n], g * sho * 0.25f);
+            for (int q = 0; q < 4; ++q) sho += pre_ho(d, a, mi[q], j, mk[q]);
+            c[0] = g * a.tFLOWX[n] * 0.25f;
+            a.FLOWX[n] += g * sho * 0.25f;
         }
     }
     if (i < d.IM && j >= 2) {
@@ -318,11 +382,9 @@ __global__ void rk_flux_energy(const __grid_constant__ Dev d, const __grid_const
         if (g != 0.0f) {
             const int mi[4] = {i, i, i + 1, i + 1}, mj[4] = {j, j - 1, j - 1, j};
             float sho = 0.0f;
-            for (int q = 0; q < 4; ++q) {
-                sho += pre_ho(d, a, mi[q], mj[q], k);
-                aadd(&A3(a.HO, mi[q], mj[q], k), 0.25f * g * a.tFLOWR[n]);
-            }
-            aadd(&a.FLOWR[n], 0.25f * g * sho);
+            for (int q = 0; q < 4; ++q) sho += pre_ho(d, a, mi[q], mj[q], k);
+            c[1] = 0.25f * g * a.tFLOWR[n];
+            a.FLOWR[n] += 0.25f * g * sho;
         }
     }
     if (j >= 2 && k < d.KM) {
@@ -331,18 +393,57 @@ __global__ void rk_flux_energy(const __grid_constant__ Dev d, const __grid_const
         if ((i == 1 || i == d.IM) && A1(d.IND, j) != 1) {
             rev_tflux_energy_raw(d, a, 1, j, k, 0.5f * g);
             rev_tflux_energy_raw(d, a, d.IM, j, k, 0.5f * g);
-        } else {
-            rev_tflux_energy_raw(d, a, i, j, k, g);
+        } else if (g != 0.0f) {
+            const int jj[4] = {j, j - 1, j - 1, j}, kk[4] = {k, k, k + 1, k + 1};
+            float sho = 0.0f;
+            for (int q = 0; q < 4; ++q) sho += pre_ho(d, a, i, jj[q], kk[q]);
+            c[2] = 0.25f * g * a.tFLOWT[n];
+            c[3] = 0.25f * g * A2(d.WRABT, j, k);
+            a.FLOWT[n] += 0.25f * g * sho;
         }
     }
     V.SR[n] = 0.0f;
+    for (int q = 0; q < 4; ++q) a.cf[(size_t)q * N + n] = c[q];
+}
+
+__global__ void rk_flux_energy_gather(const Dev d, const Adj a) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, (size_t)n, i, j, k);
+    const float *cf = a.cf;
+    auto C = [&](int q, int o) { return cf[(size_t)q * N + o]; };
+    float gH = 0.0f, gP = 0.0f;
+    for (int di = 0; di < 2; ++di)
+        for (int dk = 0; dk < 2; ++dk) {
+            const int ii = i - di, kk = k - dk;
+            if (ii < 1 || kk < 1) continue;
+            gH += C(0, ix3(d, ii, j, kk));
+        }
+    for (int di = 0; di < 2; ++di)
+        for (int dj = 0; dj < 2; ++dj) {
+            const int ii = i - di, jj = j + dj;
+            if (ii < 1 || jj > d.JM) continue;
+            gH += C(1, ix3(d, ii, jj, k));
+        }
+    for (int dj = 0; dj < 2; ++dj)
+        for (int dk = 0; dk < 2; ++dk) {
+            const int jj = j + dj, kk = k - dk;
+            if (jj > d.JM || kk < 1) continue;
+            const int o = ix3(d, i, jj, kk);
+            gH += C(2, o);
+            gP += C(3, o);
+        }
+    a.HO[n] += gH;
+    a.PEFF[n] += gP;
 }
 
 // =====================================================================
 // R6: inlet and exit conditions (k_bc_apply), IN_PRESS = 0, IN_VTAN = 0,
 // IN_VR <= 0
 // =====================================================================
-__global__ void rk_bc_apply(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+__global__ void rk_bc_apply(const Dev d, const Adj a) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= d.IM * d.KM) return;
     const int i = t % d.IM + 1, k = t / d.IM + 1;
@@ -434,7 +535,7 @@ __global__ void rk_bc_apply(const __grid_constant__ Dev d, const __grid_constant
 // =====================================================================
 // R7: PEFF = P - PREFF + F_PDOWN (P(J+1) - P)   (formed in k_flux_mom)
 // =====================================================================
-__global__ void rk_peff(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+__global__ void rk_peff(const Dev d, const Adj a) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = d.IM * d.JM * d.KM;
     if (n >= N) return;
@@ -458,11 +559,22 @@ __global__ void rk_peff(const __grid_constant__ Dev d, const __grid_constant__ A
 // R8: momentum fluxes (k_flux_mom)
 // =====================================================================
 // the four nodes of a face I = const: (i,j,k), (i,j-1,k), (i,j-1,k+1), (i,j,k+1)
-__device__ inline void iface_nodes(const Dev &d, int i, int j, int k, int m[4]) {
+__device__ __forceinline__ void iface_nodes(const Dev &d, int i, int j, int k, int m[4]) {
     m[0] = ix3(d, i, j, k); m[1] = ix3(d, i, j - 1, k); m[2] = ix3(d, i, j - 1, k + 1); m[3] = ix3(d, i, j, k + 1);
 }
 
-__global__ void rk_flux_mom(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+// Two passes.  rk_flux_mom_coef: each face owner turns its flux adjoints into
+// one coefficient per (face, input array) -- every node of a face gets the
+// same one -- and adds its own FLOWX/FLOWR/FLOWT and geometry adjoints.
+// rk_flux_mom_gather: each node sums the coefficients of the faces and cells
+// it belongs to.  Only the periodic edge faces (I = 1, IM with IND != 1),
+// which reach both edge columns, scatter with atomics.
+// Coefficients, cf[q * N + owner]: K faces q = 0..3 (PEFF, VX, VT, VR), J faces
+// 4..7 (same), radial source 8..10 (ROVT, VT, PEFF), I faces 11..14 (VX, PEFF,
+// VT, VR).
+constexpr int MOM_NCOEF = 15;
+
+__global__ void rk_flux_mom_coef(const Dev d, const Adj a) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = d.IM * d.JM * d.KM;
     if (n >= N) return;
@@ -472,6 +584,9 @@ __global__ void rk_flux_mom(const __grid_constant__ Dev d, const __grid_constant
     const bool hi = i < IM, hj = j >= 2, hk = k < d.KM;
     const AdjVar &X = a.v[V_ROVX], &T = a.v[V_RORVT], &Rm = a.v[V_ROVR];
     const float *PE = a.tPEFF, *VX = a.tVX, *VT = a.tVT, *VR = a.tVR, *RV = a.tROVT;
+    float *cf = a.cf;
+    float c[MOM_NCOEF];
+    for (int q = 0; q < MOM_NCOEF; ++q) c[q] = 0.0f;
     const bool edge = (i == 1 || i == IM) && A1(d.IND, j) != 1;
     // faces K = const
     if (hi && hk) {
@@ -484,18 +599,20 @@ __global__ void rk_flux_mom(const __grid_constant__ Dev d, const __grid_constant
         float sp = 0.0f, svx = 0.0f, svt = 0.0f, svr = 0.0f;
         for (int q = 0; q < 4; ++q) {
             sp += PE[m[q]]; svx += VX[m[q]]; svt += VT[m[q]]; svr += VR[m[q]];
-            aadd(&a.PEFF[m[q]], 0.25f * gx * d.AQX[n] + 0.25f * gr * d.AQR[n]);
-            aadd(&a.VX[m[q]], 0.25f * gx * fx);
-            aadd(&a.VT[m[q]], gt * fx * AVGR);
-            aadd(&a.VR[m[q]], 0.25f * gr * fx);
         }
-        aadd(&a.FLOWX[n], 0.25f * gx * svx + gt * AVGR * svt + 0.25f * gr * svr);
+        c[0] = 0.25f * gx * d.AQX[n] + 0.25f * gr * d.AQR[n];
+        c[1] = 0.25f * gx * fx;
+        c[2] = gt * fx * AVGR;
+        c[3] = 0.25f * gr * fx;
+        a.FLOWX[n] += 0.25f * gx * svx + gt * AVGR * svt + 0.25f * gr * svr;
         if (a.geom) {
-            aadd(&a.gAQX[n], 0.25f * gx * sp);
-            aadd(&a.gAQR[n], 0.25f * gr * sp);
+            a.gAQX[n] += 0.25f * gx * sp;
+            a.gAQR[n] += 0.25f * gr * sp;
         }
     }
     // faces J = const and the radial source
+    const float gsr = Rm.SR[n];
+    Rm.SR[n] = 0.0f;
     if (hi && hj) {
         const float gx = X.RF[n], gt = T.RF[n], gr = Rm.RF[n];
         X.RF[n] = 0.0f; T.RF[n] = 0.0f; Rm.RF[n] = 0.0f;
@@ -505,45 +622,36 @@ __global__ void rk_flux_mom(const __grid_constant__ Dev d, const __grid_constant
         float sp = 0.0f, svx = 0.0f, svt = 0.0f, svr = 0.0f;
         for (int q = 0; q < 4; ++q) {
             sp += PE[m[q]]; svx += VX[m[q]]; svt += VT[m[q]]; svr += VR[m[q]];
-            aadd(&a.PEFF[m[q]], 0.25f * gx * d.ASX[n] + 0.25f * gr * d.ASR[n]);
-            aadd(&a.VX[m[q]], 0.25f * gx * fr);
-            aadd(&a.VT[m[q]], gt * fr * AVGR);
-            aadd(&a.VR[m[q]], 0.25f * gr * fr);
         }
-        aadd(&a.FLOWR[n], 0.25f * gx * svx + gt * svt * AVGR + 0.25f * gr * svr);
+        c[4] = 0.25f * gx * d.ASX[n] + 0.25f * gr * d.ASR[n];
+        c[5] = 0.25f * gx * fr;
+        c[6] = gt * fr * AVGR;
+        c[7] = 0.25f * gr * fr;
+        a.FLOWR[n] += 0.25f * gx * svx + gt * svt * AVGR + 0.25f * gr * svr;
         if (a.geom) {
-            aadd(&a.gASX[n], 0.25f * gx * sp);
-            aadd(&a.gASR[n], 0.25f * gr * sp);
+            a.gASX[n] += 0.25f * gx * sp;
+            a.gASR[n] += 0.25f * gr * sp;
         }
         if (hk) {
-            const float gs = Rm.SR[n];
-            Rm.SR[n] = 0.0f;
+            const float gs = gsr;
             if (gs != 0.0f) {
-                int m8[8];
-                int c = 0;
+                float srv = 0.0f, svt8 = 0.0f, sp8 = 0.0f;
                 for (int di = 0; di < 2; ++di)
                     for (int dj = -1; dj <= 0; ++dj)
-                        for (int dk = 0; dk < 2; ++dk) m8[c++] = ix3(d, i + di, j + dj, k + dk);
-                float srv = 0.0f, svt8 = 0.0f, sp8 = 0.0f;
-                for (int q = 0; q < 8; ++q) {
-                    srv += RV[m8[q]];
-                    svt8 += VT[m8[q]];
-                    sp8 += PE[m8[q]];
-                }
+                        for (int dk = 0; dk < 2; ++dk) {
+                            const int o = ix3(d, i + di, j + dj, k + dk);
+                            srv += RV[o];
+                            svt8 += VT[o];
+                            sp8 += PE[o];
+                        }
                 const float AVGVT8 = 0.125f * svt8;
                 const float vol = d.VOLOR[n];
-                for (int q = 0; q < 8; ++q) {
-                    aadd(&a.ROVT[m8[q]], -gs * vol * AVGVT8);
-                    aadd(&a.VT[m8[q]], -gs * vol * srv * 0.125f);
-                    aadd(&a.PEFF[m8[q]], -gs * vol);
-                }
-                if (a.geom) aadd(&a.gVOLOR[n], -gs * (srv * AVGVT8 + sp8));
+                c[8] = -gs * vol * AVGVT8;
+                c[9] = -gs * vol * srv * 0.125f;
+                c[10] = -gs * vol;
+                if (a.geom) a.gVOLOR[n] += -gs * (srv * AVGVT8 + sp8);
             }
-        } else {
-            Rm.SR[n] = 0.0f;
         }
-    } else {
-        Rm.SR[n] = 0.0f;
     }
     // faces I = const
     if (hj && hk) {
@@ -552,12 +660,27 @@ __global__ void rk_flux_mom(const __grid_constant__ Dev d, const __grid_constant
         const float FT = a.tFLOWT[n];
         int m[4], m1[4], mm[4];
         iface_nodes(d, i, j, k, m);
-        iface_nodes(d, 1, j, k, m1);
-        iface_nodes(d, IM, j, k, mm);
         const float abx = d.ABX[n], abr = d.ABR[n], abt = A2(d.ABT, j, k);
-        // X momentum
-        if (gx != 0.0f) {
-            if (edge) {
+        const float AVGR = 0.25f * A2(d.RAVG_CELL, j, k);
+        if (!edge) {
+            float svx = 0.0f, svt = 0.0f, svr = 0.0f, sp = 0.0f;
+            for (int q = 0; q < 4; ++q) {
+                svx += VX[m[q]]; svt += VT[m[q]]; svr += VR[m[q]]; sp += PE[m[q]];
+            }
+            c[11] = 0.25f * gx * FT;
+            c[12] = 0.25f * gx * abx + gt * abt * AVGR + 0.25f * gr * abr;
+            c[13] = gt * FT * AVGR;
+            c[14] = 0.25f * gr * FT;
+            a.FLOWT[n] += 0.25f * gx * svx + gt * svt * AVGR + 0.25f * gr * svr;
+            if (a.geom) {
+                a.gABX[n] += 0.25f * gx * sp;
+                a.gABR[n] += 0.25f * gr * sp;
+                aadd(&A2(a.gABT, j, k), gt * sp * AVGR);
+            }
+        } else {
+            iface_nodes(d, 1, j, k, m1);
+            iface_nodes(d, IM, j, k, mm);
+            if (gx != 0.0f) {
                 float svx = 0.0f, sp = 0.0f;
                 for (int q = 0; q < 4; ++q) {
                     svx += VX[m1[q]] + VX[mm[q]];
@@ -569,45 +692,24 @@ __global__ void rk_flux_mom(const __grid_constant__ Dev d, const __grid_constant
                 }
                 aadd(&a.FLOWT[n], 0.125f * gx * svx);
                 if (a.geom) aadd(&a.gABX[n], 0.125f * gx * sp);
-            } else {
-                float svx = 0.0f, sp = 0.0f;
-                for (int q = 0; q < 4; ++q) {
-                    svx += VX[m[q]];
-                    sp += PE[m[q]];
-                    aadd(&a.VX[m[q]], 0.25f * gx * FT);
-                    aadd(&a.PEFF[m[q]], 0.25f * gx * abx);
-                }
-                aadd(&a.FLOWT[n], 0.25f * gx * svx);
-                if (a.geom) aadd(&a.gABX[n], 0.25f * gx * sp);
             }
-        }
-        // moment of momentum: raw(ii) = (FLOWT(ii) AVGVT(ii) + ABT AVGP(ii)) AVGR
-        if (gt != 0.0f) {
-            const float AVGR = 0.25f * A2(d.RAVG_CELL, j, k);
-            auto rev_rvt = [&](int ii, const int *mq, float g) {
-                const float ft = A3(a.tFLOWT, ii, j, k);
-                float svt = 0.0f, sp = 0.0f;
-                for (int q = 0; q < 4; ++q) {
-                    svt += VT[mq[q]];
-                    sp += PE[mq[q]];
-                    aadd(&a.VT[mq[q]], g * ft * AVGR);
-                    aadd(&a.PEFF[mq[q]], g * abt * AVGR);
-                }
-                aadd(&A3(a.FLOWT, ii, j, k), g * svt * AVGR);
-                if (a.geom) aadd(&A2(a.gABT, j, k), g * sp * AVGR);
-            };
-            if (edge) {
+            if (gt != 0.0f) {
+                auto rev_rvt = [&](int ii, const int *mq, float g) {
+                    const float ft = A3(a.tFLOWT, ii, j, k);
+                    float svt = 0.0f, sp = 0.0f;
+                    for (int q = 0; q < 4; ++q) {
+                        svt += VT[mq[q]];
+                        sp += PE[mq[q]];
+                        aadd(&a.VT[mq[q]], g * ft * AVGR);
+                        aadd(&a.PEFF[mq[q]], g * abt * AVGR);
+                    }
+                    aadd(&A3(a.FLOWT, ii, j, k), g * svt * AVGR);
+                    if (a.geom) aadd(&A2(a.gABT, j, k), g * sp * AVGR);
+                };
                 rev_rvt(1, m1, 0.5f * gt);
                 rev_rvt(IM, mm, 0.5f * gt);
-            } else {
-                rev_rvt(i, m, gt);
             }
-        }
-        // radial momentum
-        if (gr != 0.0f) {
-            if (edge) {
-                // 0.5 (0.25 FLOWT(1) AVGVR(1) + 0.25 FLOWT(IM) AVGVR(IM)
-                //      + 0.25 (AVGP(1) + AVGP(IM)) ABR)
+            if (gr != 0.0f) {
                 const float f1 = A3(a.tFLOWT, 1, j, k), fm = A3(a.tFLOWT, IM, j, k);
                 float svr1 = 0.0f, svrm = 0.0f, sp = 0.0f;
                 for (int q = 0; q < 4; ++q) {
@@ -622,19 +724,53 @@ __global__ void rk_flux_mom(const __grid_constant__ Dev d, const __grid_constant
                 aadd(&A3(a.FLOWT, 1, j, k), 0.125f * gr * svr1);
                 aadd(&A3(a.FLOWT, IM, j, k), 0.125f * gr * svrm);
                 if (a.geom) aadd(&a.gABR[n], 0.125f * gr * sp);
-            } else {
-                float svr = 0.0f, sp = 0.0f;
-                for (int q = 0; q < 4; ++q) {
-                    svr += VR[m[q]];
-                    sp += PE[m[q]];
-                    aadd(&a.VR[m[q]], 0.25f * gr * FT);
-                    aadd(&a.PEFF[m[q]], 0.25f * gr * abr);
-                }
-                aadd(&a.FLOWT[n], 0.25f * gr * svr);
-                if (a.geom) aadd(&a.gABR[n], 0.25f * gr * sp);
             }
         }
     }
+    for (int q = 0; q < MOM_NCOEF; ++q) cf[(size_t)q * N + n] = c[q];
+}
+
+__global__ void rk_flux_mom_gather(const Dev d, const Adj a) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, (size_t)n, i, j, k);
+    const float *cf = a.cf;
+    auto C = [&](int q, int o) { return cf[(size_t)q * N + o]; };
+    float gP = 0.0f, gVX = 0.0f, gVT = 0.0f, gVR = 0.0f, gRV = 0.0f;
+    for (int di = 0; di < 2; ++di)
+        for (int dk = 0; dk < 2; ++dk) {
+            const int ii = i - di, kk = k - dk;
+            if (ii < 1 || kk < 1) continue;
+            const int o = ix3(d, ii, j, kk);       // K face of owner (ii, j, kk)
+            gP += C(0, o); gVX += C(1, o); gVT += C(2, o); gVR += C(3, o);
+        }
+    for (int di = 0; di < 2; ++di)
+        for (int dj = 0; dj < 2; ++dj) {
+            const int ii = i - di, jj = j + dj;
+            if (ii < 1 || jj > d.JM) continue;
+            const int o = ix3(d, ii, jj, k);       // J face of owner (ii, jj, k)
+            gP += C(4, o); gVX += C(5, o); gVT += C(6, o); gVR += C(7, o);
+            for (int dk = 0; dk < 2; ++dk) {
+                const int kk = k - dk;
+                if (kk < 1) continue;
+                const int o2 = ix3(d, ii, jj, kk); // radial-source cell of owner (ii, jj, kk)
+                gRV += C(8, o2); gVT += C(9, o2); gP += C(10, o2);
+            }
+        }
+    for (int dj = 0; dj < 2; ++dj)
+        for (int dk = 0; dk < 2; ++dk) {
+            const int jj = j + dj, kk = k - dk;
+            if (jj > d.JM || kk < 1) continue;
+            const int o = ix3(d, i, jj, kk);       // I face of owner (i, jj, kk)
+            gVX += C(11, o); gP += C(12, o); gVT += C(13, o); gVR += C(14, o);
+        }
+    a.PEFF[n] += gP;
+    a.VX[n] += gVX;
+    a.VT[n] += gVT;
+    a.VR[n] += gVR;
+    a.ROVT[n] += gRV;
 }
 
 // =====================================================================
@@ -694,7 +830,7 @@ template <int N> __device__ inline Dual<N> dcos(const Dual<N> &x) { return lin(c
 
 constexpr int MIXN = 14;
 
-__global__ void __launch_bounds__(64) rk_mixplan(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+__global__ void __launch_bounds__(64) rk_mixplan(const Dev d, const Adj a) {
     typedef Dual<MIXN> D;
     __shared__ float red[5][64];
     const int nr = blockIdx.x / d.KM + 1, k = blockIdx.x % d.KM + 1;
@@ -815,7 +951,7 @@ __global__ void __launch_bounds__(64) rk_mixplan(const __grid_constant__ Dev d, 
 // RO(J+1) + RO(J+2)) / 4, J walked upwards; the coefficients come from a
 // replay of the recorded column (rk_density_prep).
 // =====================================================================
-__global__ void rk_density_prep(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+__global__ void rk_density_prep(const Dev d, const Adj a) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= d.IM * d.KM) return;
     const int i = t % d.IM + 1, k = t / d.IM + 1;
@@ -841,7 +977,7 @@ __global__ void rk_density_prep(const __grid_constant__ Dev d, const __grid_cons
     const_cast<int *>(a.tDCOL)[t] = any;
 }
 
-__global__ void rk_density(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+__global__ void rk_density(const Dev d, const Adj a) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= d.IM * d.KM || !a.tDCOL[t]) return;
     const int i = t % d.IM + 1, k = t / d.IM + 1;
@@ -858,7 +994,7 @@ __global__ void rk_density(const __grid_constant__ Dev d, const __grid_constant_
     }
 }
 
-__global__ void rk_mach(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+__global__ void rk_mach(const Dev d, const Adj a) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = d.IM * d.JM * d.KM;
     if (n >= N) return;
@@ -1421,7 +1557,7 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_cells(const __grid_constant__ Dev
 }
 
 // objective seeds added at the start of each reverse step
-__global__ void rk_seed(const __grid_constant__ Dev d, const __grid_constant__ Adj a) {
+__global__ void rk_seed(const Dev d, const Adj a) {
     const int IM = d.IM, KM = d.KM;
     const int np = IM * KM, nc = d.IMM1 * d.KMM1;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1445,7 +1581,7 @@ __global__ void rk_seed(const __grid_constant__ Dev d, const __grid_constant__ A
 
 // objective seeds of the EFICOOL mass averages on plane j (FP64 weights
 // from the host): dJ/dspo, dJ/dsto, dJ/dbf
-__global__ void rk_seed_plane(const __grid_constant__ Dev d, const __grid_constant__ Adj a, float *seed, int j,
+__global__ void rk_seed_plane(const Dev d, const Adj a, float *seed, int j,
                               double gspo, double gsto, double gbf, double spo, double sto, double bf) {
     const int IM = d.IM, KM = d.KM, IMM1 = d.IMM1, KMM1 = d.KMM1;
     const int np = IM * KM;
@@ -1724,13 +1860,16 @@ void enqueue_reverse(const Dev &d, const Adj &a, cudaStream_t s) {
     rk_mach<<<gN, 256, 0, s>>>(d, a);
     rk_density<<<gridn((size_t)d.IM * d.KM, 128), 128, 0, s>>>(d, a);
     launch_tstep_rev(d, a, s, V_ROVX, 3);
-    rk_flux_mom<<<gN, 256, 0, s>>>(d, a);
+    rk_flux_mom_coef<<<gN, 256, 0, s>>>(d, a);
+    rk_flux_mom_gather<<<gN, 256, 0, s>>>(d, a);
     rk_peff<<<gN, 256, 0, s>>>(d, a);
     rk_bc_apply<<<gridn((size_t)d.IM * d.KM, 128), 128, 0, s>>>(d, a);
     launch_tstep_rev(d, a, s, V_RO, 2);
-    rk_flux_energy<<<gN, 256, 0, s>>>(d, a);
+    rk_flux_energy_coef<<<gN, 256, 0, s>>>(d, a);
+    rk_flux_energy_gather<<<gN, 256, 0, s>>>(d, a);
     rk_bc_sums<<<1, 256, 0, s>>>(d, a);
-    rk_flux_mass<<<gN, 256, 0, s>>>(d, a);
+    rk_flux_mass_coef<<<gN, 256, 0, s>>>(d, a);
+    rk_flux_mass_gather<<<gN, 256, 0, s>>>(d, a);
     rk_prim<<<gN, 256, 0, s>>>(d, a);
 }
 
@@ -1785,6 +1924,7 @@ int allocate(AdjState *s, const Dev &d) {
         a.tDCOL = q;
     }
     F(&a.WT, N);
+    F(&a.cf, (size_t)15 * N);
     Fc(&a.tMIX, (size_t)(d.NRWSM1 > 0 ? d.NRWSM1 : 1) * d.KM * mix_rec_size(d.IM));
     F(&a.gAQX, N); F(&a.gAQR, N); F(&a.gABX, N); F(&a.gABR, N); F(&a.gASX, N); F(&a.gASR, N); F(&a.gVOLOR, N);
     F(&a.gABT, (size_t)d.JM * d.KM);
