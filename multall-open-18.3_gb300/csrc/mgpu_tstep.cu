@@ -266,6 +266,22 @@ __global__ void k_ts_restrict_seq(const __grid_constant__ Dev d, int v0) {
     (lv1 ? V.B1CHG : V.B2CHG)[u] = s;
 }
 
+// Sum over the J planes a..e of one block's per-plane partial sums, added in
+// J order in REAL*4; the loads of three planes (a level-1 block, a third of a
+// level-2 block) are issued before their adds.
+__device__ __forceinline__ float plane_partials_sum(const float *__restrict__ P, int n, int t, int a, int e) {
+    float s = 0.0f;
+    int jj = a;
+    for (; jj + 2 <= e; jj += 3) {
+        const float x0 = P[(size_t)(jj - 1) * n + t], x1 = P[(size_t)jj * n + t], x2 = P[(size_t)(jj + 1) * n + t];
+        s = s + x0;
+        s = s + x1;
+        s = s + x2;
+    }
+    for (; jj <= e; ++jj) s = s + P[(size_t)(jj - 1) * n + t];
+    return s;
+}
+
 // ---------------------------------------------------------------------
 // prolong: 1500, with the block sums assembled from the plane partials
 // ---------------------------------------------------------------------
@@ -316,18 +332,12 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
         }
         if (threadIdx.x == 0) s_sb = A1(V.SBSUM, jsb);
     } else {
-        for (int t = threadIdx.x; t < n1; t += BS) {
-            float s = 0.0f;
-            if (j1 <= d.NJB1)
-                for (int jj = A1(d.JB1_START, j1); jj <= A1(d.JB1_END, j1); ++jj) s = s + V.P1[(size_t)(jj - 1) * n1 + t];
-            b1[t] = s;
-        }
-        for (int t = threadIdx.x; t < n2; t += BS) {
-            float s = 0.0f;
-            if (j2 <= d.NJB2)
-                for (int jj = A1(d.JB2_START, j2); jj <= A1(d.JB2_END, j2); ++jj) s = s + V.P2[(size_t)(jj - 1) * n2 + t];
-            b2[t] = s;
-        }
+        // the J planes of this plane's level-1 and level-2 blocks (empty past
+        // the last block); each sum adds the planes' partials in J order
+        const int a1 = j1 <= d.NJB1 ? A1(d.JB1_START, j1) : 1, e1 = j1 <= d.NJB1 ? A1(d.JB1_END, j1) : 0;
+        const int a2 = j2 <= d.NJB2 ? A1(d.JB2_START, j2) : 1, e2 = j2 <= d.NJB2 ? A1(d.JB2_END, j2) : 0;
+        for (int t = threadIdx.x; t < n1; t += BS) b1[t] = plane_partials_sum(V.P1, n1, t, a1, e1);
+        for (int t = threadIdx.x; t < n2; t += BS) b2[t] = plane_partials_sum(V.P2, n2, t, a2, e2);
         if (threadIdx.x < 32) {
             int a = A1(d.SB_START, jsb), b = A1(d.SB_END, jsb);
             double s = 0.0;
