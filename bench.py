@@ -311,9 +311,17 @@ def run_batch(args, rank, world, local_rank):
     return 0
 
 
-# reverse-step kernels: seeds, mixing plane, 2 limiters, 2 x 4 TSTEP kernels,
-# momentum fluxes, PEFF, inlet/exit, energy fluxes, exit sums, mass fluxes, primitives
-ADJ_KERNELS_PER_STEP = 19
+# reverse-step kernels: seeds, mixing plane (when there is one), 2 limiters,
+# 2 x 4 TSTEP kernels, momentum, energy and mass fluxes (a coefficient and a
+# gather pass each), inlet/exit, exit sums, primitives; PEFF's own reverse
+# only when F_PDOWN != 0
+def adj_kernels_per_step(cd) -> int:
+    n = 20
+    if cd.ints.get("IFMIX", 0) > 0 and cd.reals.get("RFMIX", 0.0) > 1e-3 and cd.nrows > 1:
+        n += 1
+    if cd.reals.get("F_PDOWN", 0.0) != 0.0:
+        n += 1
+    return n
 
 
 def run_adjoint(args, rank, world, local_rank):
@@ -430,7 +438,7 @@ def run_adjoint(args, rank, world, local_rank):
         "e2e": {"value": t_fd / t_adj_total, "unit": "x", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": d2h / max(steps_total, 1),
                 "how": "mgpu_adjoint_* through the C ABI; geometry gradients read back to the host for the chain"},
-        "gpu_launches": ADJ_KERNELS_PER_STEP * steps_total,
+        "gpu_launches": adj_kernels_per_step(cd) * steps_total,
     }
     print(json.dumps(line), flush=True)
     p.close()

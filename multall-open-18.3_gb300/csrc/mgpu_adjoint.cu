@@ -116,8 +116,6 @@ __global__ void rk_prim(const Dev d, const Adj a) {
         gvr += gEKE * vr;
         gvt += gEKE * vt;
         gvx += gEKE * vx;
-        a.P[n] = 0.0f;
-        a.HO[n] = 0.0f;
     }
     grovt += gvt * RECIP;
     float grecip = gvt * rovt + gvx * a.tROVX[n] + gvr * a.tROVR[n];
@@ -127,6 +125,11 @@ __global__ void rk_prim(const Dev d, const Adj a) {
     a.v[V_ROVX].D[n] += gvx * RECIP;
     a.v[V_ROVR].D[n] += gvr * RECIP;
     a.v[V_RORVT].D[n] += grovt * RRNOW;
+    // cleared after the stores that use them (stores keep their order)
+    if (j <= d.JMM1) {
+        a.P[n] = 0.0f;
+        a.HO[n] = 0.0f;
+    }
     a.VX[n] = 0.0f;
     a.VR[n] = 0.0f;
     a.VT[n] = 0.0f;
@@ -176,74 +179,65 @@ __global__ void rk_flux_mass_coef(const Dev d, const Adj a) {
     if (n >= N) return;
     int i, j, k;
     node_ijk(d, (size_t)n, i, j, k);
-    float c[7] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    if (i < d.IM && k < d.KM) {
-        const float g = a.FLOWX[n];
-        a.FLOWX[n] = 0.0f;
-        if (g != 0.0f) {
-            c[0] = 0.25f * g * d.AQX[n];
-            c[1] = 0.25f * g * d.AQR[n];
-            if (a.geom) {
-                const int m[4] = {n, ix3(d, i, j, k + 1), ix3(d, i + 1, j, k), ix3(d, i + 1, j, k + 1)};
-                float sx = 0.0f, sr = 0.0f;
-                for (int q = 0; q < 4; ++q) {
-                    sx += a.tROVX[m[q]];
-                    sr += a.tROVR[m[q]];
-                }
-                aadd(&a.gAQX[n], 0.25f * g * sx);
-                aadd(&a.gAQR[n], 0.25f * g * sr);
-            }
-        }
+    const bool fx = i < d.IM && k < d.KM, ft = j >= 2 && k < d.KM, fr = i < d.IM && j >= 2;
+    const bool end = i == 1 || i == d.IM;
+    const bool edge = ft && end && A1(d.IND, j) != 1;
+    bool on = ft && !edge;
+    if (on && end) {
+        const int nr = A1(d.NROW, j);
+        if (k >= A1(d.KS1, nr) && k <= A1(d.KS2, nr)) on = false;
     }
-    if (j >= 2 && k < d.KM) {
-        const float g = a.FLOWT[n];
-        a.FLOWT[n] = 0.0f;
-        const bool end = i == 1 || i == d.IM;
-        if (end && A1(d.IND, j) != 1) {
-            rev_flowt_raw(d, a, 1, j, k, 0.5f * g);
-            rev_flowt_raw(d, a, d.IM, j, k, 0.5f * g);
-        } else {
-            bool on = true;
-            if (end) {
-                const int nr = A1(d.NROW, j);
-                if (k >= A1(d.KS1, nr) && k <= A1(d.KS2, nr)) on = false;
-            }
-            if (on && g != 0.0f) {
-                c[2] = 0.25f * g * d.ABX[n];
-                c[3] = 0.25f * g * A2(d.ABT, j, k);
-                c[4] = 0.25f * g * d.ABR[n];
-                if (a.geom) {
-                    const int jj[4] = {j, j - 1, j - 1, j}, kk[4] = {k, k, k + 1, k + 1};
-                    float sx = 0.0f, st = 0.0f, sr = 0.0f;
-                    for (int q = 0; q < 4; ++q) {
-                        const int m = ix3(d, i, jj[q], kk[q]);
-                        sx += a.tROVX[m];
-                        st += pre_rovt(d, a, i, jj[q], kk[q]) - A2(d.UBLADE, jj[q], kk[q]) * a.tRO[m];
-                        sr += a.tROVR[m];
-                    }
-                    aadd(&a.gABX[n], 0.25f * g * sx);
-                    aadd(&A2(a.gABT, j, k), 0.25f * g * st);
-                    aadd(&a.gABR[n], 0.25f * g * sr);
-                }
-            }
-        }
+    const bool rs = fr && k >= 2 && k <= d.KMM1;
+    // every load before any store
+    const float gx = fx ? a.FLOWX[n] : 0.0f, gt = ft ? a.FLOWT[n] : 0.0f, gr = rs ? a.FLOWR[n] : 0.0f;
+    const float aqx = fx ? d.AQX[n] : 0.0f, aqr = fx ? d.AQR[n] : 0.0f;
+    const float abx = on ? d.ABX[n] : 0.0f, abt = on ? A2(d.ABT, j, k) : 0.0f, abr = on ? d.ABR[n] : 0.0f;
+    const float asx = rs ? d.ASX[n] : 0.0f, asr = rs ? d.ASR[n] : 0.0f;
+    float c[7];
+    c[0] = 0.25f * gx * aqx;
+    c[1] = 0.25f * gx * aqr;
+    c[2] = 0.25f * gt * abx;
+    c[3] = 0.25f * gt * abt;
+    c[4] = 0.25f * gt * abr;
+    c[5] = 0.25f * gr * asx;
+    c[6] = 0.25f * gr * asr;
+    if (edge) {
+        rev_flowt_raw(d, a, 1, j, k, 0.5f * gt);
+        rev_flowt_raw(d, a, d.IM, j, k, 0.5f * gt);
     }
-    if (i < d.IM && j >= 2) {
-        const float g = a.FLOWR[n];
-        a.FLOWR[n] = 0.0f;
-        if (g != 0.0f && k >= 2 && k <= d.KMM1) {
-            c[5] = 0.25f * g * d.ASX[n];
-            c[6] = 0.25f * g * d.ASR[n];
-            if (a.geom) {
-                const int m[4] = {n, ix3(d, i, j - 1, k), ix3(d, i + 1, j - 1, k), ix3(d, i + 1, j, k)};
-                float sx = 0.0f, sr = 0.0f;
-                for (int q = 0; q < 4; ++q) {
-                    sx += a.tROVX[m[q]];
-                    sr += a.tROVR[m[q]];
-                }
-                aadd(&a.gASX[n], 0.25f * g * sx);
-                aadd(&a.gASR[n], 0.25f * g * sr);
+    if (a.geom) {
+        if (fx && gx != 0.0f) {
+            const int m[4] = {n, ix3(d, i, j, k + 1), ix3(d, i + 1, j, k), ix3(d, i + 1, j, k + 1)};
+            float sx = 0.0f, sr = 0.0f;
+            for (int q = 0; q < 4; ++q) {
+                sx += a.tROVX[m[q]];
+                sr += a.tROVR[m[q]];
             }
+            aadd(&a.gAQX[n], 0.25f * gx * sx);
+            aadd(&a.gAQR[n], 0.25f * gx * sr);
+        }
+        if (on && gt != 0.0f) {
+            const int jj[4] = {j, j - 1, j - 1, j}, kk[4] = {k, k, k + 1, k + 1};
+            float sx = 0.0f, st = 0.0f, sr = 0.0f;
+            for (int q = 0; q < 4; ++q) {
+                const int m = ix3(d, i, jj[q], kk[q]);
+                sx += a.tROVX[m];
+                st += pre_rovt(d, a, i, jj[q], kk[q]) - A2(d.UBLADE, jj[q], kk[q]) * a.tRO[m];
+                sr += a.tROVR[m];
+            }
+            aadd(&a.gABX[n], 0.25f * gt * sx);
+            aadd(&A2(a.gABT, j, k), 0.25f * gt * st);
+            aadd(&a.gABR[n], 0.25f * gt * sr);
+        }
+        if (rs && gr != 0.0f) {
+            const int m[4] = {n, ix3(d, i, j - 1, k), ix3(d, i + 1, j - 1, k), ix3(d, i + 1, j, k)};
+            float sx = 0.0f, sr = 0.0f;
+            for (int q = 0; q < 4; ++q) {
+                sx += a.tROVX[m[q]];
+                sr += a.tROVR[m[q]];
+            }
+            aadd(&a.gASX[n], 0.25f * gr * sx);
+            aadd(&a.gASR[n], 0.25f * gr * sr);
         }
     }
     for (int q = 0; q < 7; ++q) a.cf[(size_t)q * N + n] = c[q];
@@ -292,6 +286,9 @@ __global__ void rk_flux_mass_gather(const Dev d, const Adj a) {
     a.v[V_ROVR].D[n] += gR;
     a.ROVT[n] += gRV;
     a.v[V_RO].D[n] += gRO;
+    // the face-flux adjoints rk_flux_mass_coef consumed (cleared here, not
+    // there: see rk_flux_mom_gather)
+    a.FLOWX[n] = 0.0f; a.FLOWT[n] = 0.0f; a.FLOWR[n] = 0.0f;
 }
 
 // =====================================================================
@@ -364,45 +361,33 @@ __global__ void rk_flux_energy_coef(const Dev d, const Adj a) {
     int i, j, k;
     node_ijk(d, (size_t)n, i, j, k);
     const AdjVar &V = a.v[V_ROE];
-    float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    if (i < d.IM && k < d.KM) {
-        const float g = V.XF[n];
-        V.XF[n] = 0.0f;
-        if (g != 0.0f) {
-            const int mi[4] = {i, i, i + 1, i + 1}, mk[4] = {k, k + 1, k, k + 1};
-            float sho = 0.0f;
-            for (int q = 0; q < 4; ++q) sho += pre_ho(d, a, mi[q], j, mk[q]);
-            c[0] = g * a.tFLOWX[n] * 0.25f;
-            a.FLOWX[n] += g * sho * 0.25f;
-        }
+    const bool fx = i < d.IM && k < d.KM, fr = i < d.IM && j >= 2, ft = j >= 2 && k < d.KM;
+    const bool edge = ft && (i == 1 || i == d.IM) && A1(d.IND, j) != 1;
+    const bool fi = ft && !edge;
+    // every load before any store
+    const float gx = fx ? V.XF[n] : 0.0f, gr = fr ? V.RF[n] : 0.0f, gt = ft ? V.TF[n] : 0.0f;
+    const float FX = fx ? a.tFLOWX[n] : 0.0f, FR = fr ? a.tFLOWR[n] : 0.0f, FT = fi ? a.tFLOWT[n] : 0.0f;
+    const float WR = fi ? A2(d.WRABT, j, k) : 0.0f;
+    const float h000 = pre_ho(d, a, i, j, k);
+    const float h001 = (fx || fi) ? pre_ho(d, a, i, j, k + 1) : 0.0f;
+    const float h100 = (fx || fr) ? pre_ho(d, a, i + 1, j, k) : 0.0f;
+    const float h101 = fx ? pre_ho(d, a, i + 1, j, k + 1) : 0.0f;
+    const float h0m0 = (fr || fi) ? pre_ho(d, a, i, j - 1, k) : 0.0f;
+    const float h1m0 = fr ? pre_ho(d, a, i + 1, j - 1, k) : 0.0f;
+    const float h0m1 = fi ? pre_ho(d, a, i, j - 1, k + 1) : 0.0f;
+    const float ax = fx ? a.FLOWX[n] : 0.0f, ar = fr ? a.FLOWR[n] : 0.0f, at = fi ? a.FLOWT[n] : 0.0f;
+    float c[4];
+    c[0] = gx * FX * 0.25f;
+    c[1] = 0.25f * gr * FR;
+    c[2] = 0.25f * gt * FT;
+    c[3] = 0.25f * gt * WR;
+    if (edge) {
+        rev_tflux_energy_raw(d, a, 1, j, k, 0.5f * gt);
+        rev_tflux_energy_raw(d, a, d.IM, j, k, 0.5f * gt);
     }
-    if (i < d.IM && j >= 2) {
-        const float g = V.RF[n];
-        V.RF[n] = 0.0f;
-        if (g != 0.0f) {
-            const int mi[4] = {i, i, i + 1, i + 1}, mj[4] = {j, j - 1, j - 1, j};
-            float sho = 0.0f;
-            for (int q = 0; q < 4; ++q) sho += pre_ho(d, a, mi[q], mj[q], k);
-            c[1] = 0.25f * g * a.tFLOWR[n];
-            a.FLOWR[n] += 0.25f * g * sho;
-        }
-    }
-    if (j >= 2 && k < d.KM) {
-        const float g = V.TF[n];
-        V.TF[n] = 0.0f;
-        if ((i == 1 || i == d.IM) && A1(d.IND, j) != 1) {
-            rev_tflux_energy_raw(d, a, 1, j, k, 0.5f * g);
-            rev_tflux_energy_raw(d, a, d.IM, j, k, 0.5f * g);
-        } else if (g != 0.0f) {
-            const int jj[4] = {j, j - 1, j - 1, j}, kk[4] = {k, k, k + 1, k + 1};
-            float sho = 0.0f;
-            for (int q = 0; q < 4; ++q) sho += pre_ho(d, a, i, jj[q], kk[q]);
-            c[2] = 0.25f * g * a.tFLOWT[n];
-            c[3] = 0.25f * g * A2(d.WRABT, j, k);
-            a.FLOWT[n] += 0.25f * g * sho;
-        }
-    }
-    V.SR[n] = 0.0f;
+    if (fx) a.FLOWX[n] = ax + gx * (((h000 + h001) + h100) + h101) * 0.25f;
+    if (fr) a.FLOWR[n] = ar + 0.25f * gr * (((h000 + h0m0) + h1m0) + h100);
+    if (fi) a.FLOWT[n] = at + 0.25f * gt * (((h000 + h0m0) + h0m1) + h001);
     for (int q = 0; q < 4; ++q) a.cf[(size_t)q * N + n] = c[q];
 }
 
@@ -437,6 +422,9 @@ __global__ void rk_flux_energy_gather(const Dev d, const Adj a) {
         }
     a.HO[n] += gH;
     a.PEFF[n] += gP;
+    const AdjVar &V = a.v[V_ROE];
+    // the ROE flux adjoints rk_flux_energy_coef consumed (see rk_flux_mom_gather)
+    V.XF[n] = 0.0f; V.RF[n] = 0.0f; V.TF[n] = 0.0f; V.SR[n] = 0.0f;
 }
 
 // =====================================================================
@@ -533,18 +521,16 @@ __global__ void rk_bc_apply(const Dev d, const Adj a) {
 }
 
 // =====================================================================
-// R7: PEFF = P - PREFF + F_PDOWN (P(J+1) - P)   (formed in k_flux_mom)
+// R7: PEFF = P - PREFF + F_PDOWN (P(J+1) - P)   (formed in k_flux_mom).
+// Launched only for F_PDOWN != 0; with F_PDOWN = 0 rk_flux_mom_gather
+// passes the adjoint to P itself.  The clearing store follows the atomics
+// that use g, so it never meets the load of the same address in flight.
 // =====================================================================
 __global__ void rk_peff(const Dev d, const Adj a) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = d.IM * d.JM * d.KM;
     if (n >= N) return;
     const float g = a.PEFF[n];
-    a.PEFF[n] = 0.0f;
-    if (d.F_PDOWN == 0.0f) {
-        a.P[n] += g;
-        return;
-    }
     int i, j, k;
     node_ijk(d, (size_t)n, i, j, k);
     if (j == d.JM) {
@@ -553,6 +539,7 @@ __global__ void rk_peff(const Dev d, const Adj a) {
         aadd(&a.P[n], (1.0f - d.F_PDOWN) * g);
         aadd(&A3(a.P, i, j + 1, k), d.F_PDOWN * g);
     }
+    a.PEFF[n] = 0.0f;
 }
 
 // =====================================================================
@@ -561,6 +548,65 @@ __global__ void rk_peff(const Dev d, const Adj a) {
 // the four nodes of a face I = const: (i,j,k), (i,j-1,k), (i,j-1,k+1), (i,j,k+1)
 __device__ __forceinline__ void iface_nodes(const Dev &d, int i, int j, int k, int m[4]) {
     m[0] = ix3(d, i, j, k); m[1] = ix3(d, i, j - 1, k); m[2] = ix3(d, i, j - 1, k + 1); m[3] = ix3(d, i, j, k + 1);
+}
+
+// The periodic edge faces I = 1 and IM (IND != 1) of the momentum fluxes:
+// both edge columns share one face, so the face's adjoints reach the nodes
+// of both columns, with atomics.
+__device__ __forceinline__ void rev_mom_iface_edge(const Dev &d, const Adj &a, int i, int j, int k, float gx,
+                                                   float gt, float gr, float abx, float abt, float abr, float AVGR) {
+    const int IM = d.IM;
+    const float *PE = a.tPEFF, *VX = a.tVX, *VT = a.tVT, *VR = a.tVR;
+    const int n = ix3(d, i, j, k);
+    const float FT = a.tFLOWT[n];
+    int m1[4], mm[4];
+    iface_nodes(d, 1, j, k, m1);
+    iface_nodes(d, IM, j, k, mm);
+    if (gx != 0.0f) {
+        float svx = 0.0f, sp = 0.0f;
+        for (int q = 0; q < 4; ++q) {
+            svx += VX[m1[q]] + VX[mm[q]];
+            sp += PE[m1[q]] + PE[mm[q]];
+            aadd(&a.VX[m1[q]], 0.125f * gx * FT);
+            aadd(&a.VX[mm[q]], 0.125f * gx * FT);
+            aadd(&a.PEFF[m1[q]], 0.125f * gx * abx);
+            aadd(&a.PEFF[mm[q]], 0.125f * gx * abx);
+        }
+        aadd(&a.FLOWT[n], 0.125f * gx * svx);
+        if (a.geom) aadd(&a.gABX[n], 0.125f * gx * sp);
+    }
+    if (gt != 0.0f) {
+        auto rev_rvt = [&](int ii, const int *mq, float g) {
+            const float ft = A3(a.tFLOWT, ii, j, k);
+            float svt = 0.0f, sp = 0.0f;
+            for (int q = 0; q < 4; ++q) {
+                svt += VT[mq[q]];
+                sp += PE[mq[q]];
+                aadd(&a.VT[mq[q]], g * ft * AVGR);
+                aadd(&a.PEFF[mq[q]], g * abt * AVGR);
+            }
+            aadd(&A3(a.FLOWT, ii, j, k), g * svt * AVGR);
+            if (a.geom) aadd(&A2(a.gABT, j, k), g * sp * AVGR);
+        };
+        rev_rvt(1, m1, 0.5f * gt);
+        rev_rvt(IM, mm, 0.5f * gt);
+    }
+    if (gr != 0.0f) {
+        const float f1 = A3(a.tFLOWT, 1, j, k), fm = A3(a.tFLOWT, IM, j, k);
+        float svr1 = 0.0f, svrm = 0.0f, sp = 0.0f;
+        for (int q = 0; q < 4; ++q) {
+            svr1 += VR[m1[q]];
+            svrm += VR[mm[q]];
+            sp += PE[m1[q]] + PE[mm[q]];
+            aadd(&a.VR[m1[q]], 0.125f * gr * f1);
+            aadd(&a.VR[mm[q]], 0.125f * gr * fm);
+            aadd(&a.PEFF[m1[q]], 0.125f * gr * abr);
+            aadd(&a.PEFF[mm[q]], 0.125f * gr * abr);
+        }
+        aadd(&A3(a.FLOWT, 1, j, k), 0.125f * gr * svr1);
+        aadd(&A3(a.FLOWT, IM, j, k), 0.125f * gr * svrm);
+        if (a.geom) aadd(&a.gABR[n], 0.125f * gr * sp);
+    }
 }
 
 // Two passes.  rk_flux_mom_coef: each face owner turns its flux adjoints into
@@ -572,6 +618,13 @@ __device__ __forceinline__ void iface_nodes(const Dev &d, int i, int j, int k, i
 // Coefficients, cf[q * N + owner]: K faces q = 0..3 (PEFF, VX, VT, VR), J faces
 // 4..7 (same), radial source 8..10 (ROVT, VT, PEFF), I faces 11..14 (VX, PEFF,
 // VT, VR).
+// The coefficient passes issue every load before their first store and
+// branch on no loaded value, and they clear none of the adjoints they read:
+// the gathers clear them.  Clearing in place (a store of a constant right
+// after the load of the same address) made these passes 6-12 times slower
+// than their gathers, with the warps stalled on long-scoreboard waits at a
+// small fraction of the memory bandwidth; moving the clears took the whole
+// transposed step of the 65 x 242 x 49 stage from 0.86 to 0.60 ms.
 constexpr int MOM_NCOEF = 15;
 
 __global__ void rk_flux_mom_coef(const Dev d, const Adj a) {
@@ -582,152 +635,123 @@ __global__ void rk_flux_mom_coef(const Dev d, const Adj a) {
     node_ijk(d, (size_t)n, i, j, k);
     const int IM = d.IM;
     const bool hi = i < IM, hj = j >= 2, hk = k < d.KM;
+    const bool fk = hi && hk, fj = hi && hj, fs = fj && hk, ft = hj && hk;
     const AdjVar &X = a.v[V_ROVX], &T = a.v[V_RORVT], &Rm = a.v[V_ROVR];
     const float *PE = a.tPEFF, *VX = a.tVX, *VT = a.tVT, *VR = a.tVR, *RV = a.tROVT;
-    float *cf = a.cf;
+    const bool edge = ft && (i == 1 || i == IM) && A1(d.IND, j) != 1;
+    const bool fi = ft && !edge;
+    // every load before any store: the flux adjoints, then the recorded
+    // values on the cube (i..i+1, j-1..j, k..k+1); index [di][dj + 1][dk]
+    const float gxk = fk ? X.XF[n] : 0.0f, gtk = fk ? T.XF[n] : 0.0f, grk = fk ? Rm.XF[n] : 0.0f;
+    const float gxj = fj ? X.RF[n] : 0.0f, gtj = fj ? T.RF[n] : 0.0f, grj = fj ? Rm.RF[n] : 0.0f;
+    const float gxi = ft ? X.TF[n] : 0.0f, gti = ft ? T.TF[n] : 0.0f, gri = ft ? Rm.TF[n] : 0.0f;
+    const float gs = fs ? Rm.SR[n] : 0.0f;
+    float pe[2][2][2], vx[2][2][2], vt[2][2][2], vr[2][2][2], rv[2][2][2];
+#pragma unroll
+    for (int di = 0; di < 2; ++di)
+#pragma unroll
+        for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+            for (int dk = 0; dk < 2; ++dk) {
+                const bool ok = (di == 0 || hi) && (dj == 1 || hj) && (dk == 0 || hk);
+                const int o = ok ? ix3(d, i + di, j + dj - 1, k + dk) : n;
+                pe[di][dj][dk] = ok ? PE[o] : 0.0f;
+                vx[di][dj][dk] = ok ? VX[o] : 0.0f;
+                vt[di][dj][dk] = ok ? VT[o] : 0.0f;
+                vr[di][dj][dk] = ok ? VR[o] : 0.0f;
+                rv[di][dj][dk] = (ok && fs) ? RV[o] : 0.0f;
+            }
+    const float fxw = fk ? a.tFLOWX[n] : 0.0f, frw = fj ? a.tFLOWR[n] : 0.0f, FT = fi ? a.tFLOWT[n] : 0.0f;
+    const float rjk = A2(d.R, j, k);
+    const float rk1 = fk ? A2(d.R, j, k + 1) : 0.0f, rj1 = fj ? A2(d.R, j - 1, k) : 0.0f;
+    const float aqx = fk ? d.AQX[n] : 0.0f, aqr = fk ? d.AQR[n] : 0.0f;
+    const float asx = fj ? d.ASX[n] : 0.0f, asr = fj ? d.ASR[n] : 0.0f;
+    const float vol = fs ? d.VOLOR[n] : 0.0f;
+    const float abx = ft ? d.ABX[n] : 0.0f, abr = ft ? d.ABR[n] : 0.0f, abt = ft ? A2(d.ABT, j, k) : 0.0f;
+    const float ravg = ft ? A2(d.RAVG_CELL, j, k) : 0.0f;
+    const float ofx = fk ? a.FLOWX[n] : 0.0f, ofr = fj ? a.FLOWR[n] : 0.0f, oft = fi ? a.FLOWT[n] : 0.0f;
     float c[MOM_NCOEF];
-    for (int q = 0; q < MOM_NCOEF; ++q) c[q] = 0.0f;
-    const bool edge = (i == 1 || i == IM) && A1(d.IND, j) != 1;
-    // faces K = const
-    if (hi && hk) {
-        const float gx = X.XF[n], gt = T.XF[n], gr = Rm.XF[n];
-        X.XF[n] = 0.0f; T.XF[n] = 0.0f; Rm.XF[n] = 0.0f;
-        X.SR[n] = 0.0f; T.SR[n] = 0.0f;
-        const int m[4] = {n, ix3(d, i, j, k + 1), ix3(d, i + 1, j, k + 1), ix3(d, i + 1, j, k)};
-        const float fx = a.tFLOWX[n];
-        const float AVGR = 0.125f * (A2(d.R, j, k) + A2(d.R, j, k + 1));
-        float sp = 0.0f, svx = 0.0f, svt = 0.0f, svr = 0.0f;
-        for (int q = 0; q < 4; ++q) {
-            sp += PE[m[q]]; svx += VX[m[q]]; svt += VT[m[q]]; svr += VR[m[q]];
-        }
-        c[0] = 0.25f * gx * d.AQX[n] + 0.25f * gr * d.AQR[n];
-        c[1] = 0.25f * gx * fx;
-        c[2] = gt * fx * AVGR;
-        c[3] = 0.25f * gr * fx;
-        a.FLOWX[n] += 0.25f * gx * svx + gt * AVGR * svt + 0.25f * gr * svr;
-        if (a.geom) {
-            a.gAQX[n] += 0.25f * gx * sp;
-            a.gAQR[n] += 0.25f * gr * sp;
-        }
-    }
-    // faces J = const and the radial source
-    const float gsr = Rm.SR[n];
-    Rm.SR[n] = 0.0f;
-    if (hi && hj) {
-        const float gx = X.RF[n], gt = T.RF[n], gr = Rm.RF[n];
-        X.RF[n] = 0.0f; T.RF[n] = 0.0f; Rm.RF[n] = 0.0f;
-        const int m[4] = {n, ix3(d, i, j - 1, k), ix3(d, i + 1, j - 1, k), ix3(d, i + 1, j, k)};
-        const float fr = a.tFLOWR[n];
-        const float AVGR = (A2(d.R, j, k) + A2(d.R, j - 1, k)) * 0.125f;
-        float sp = 0.0f, svx = 0.0f, svt = 0.0f, svr = 0.0f;
-        for (int q = 0; q < 4; ++q) {
-            sp += PE[m[q]]; svx += VX[m[q]]; svt += VT[m[q]]; svr += VR[m[q]];
-        }
-        c[4] = 0.25f * gx * d.ASX[n] + 0.25f * gr * d.ASR[n];
-        c[5] = 0.25f * gx * fr;
-        c[6] = gt * fr * AVGR;
-        c[7] = 0.25f * gr * fr;
-        a.FLOWR[n] += 0.25f * gx * svx + gt * svt * AVGR + 0.25f * gr * svr;
-        if (a.geom) {
-            a.gASX[n] += 0.25f * gx * sp;
-            a.gASR[n] += 0.25f * gr * sp;
-        }
-        if (hk) {
-            const float gs = gsr;
-            if (gs != 0.0f) {
-                float srv = 0.0f, svt8 = 0.0f, sp8 = 0.0f;
-                for (int di = 0; di < 2; ++di)
-                    for (int dj = -1; dj <= 0; ++dj)
-                        for (int dk = 0; dk < 2; ++dk) {
-                            const int o = ix3(d, i + di, j + dj, k + dk);
-                            srv += RV[o];
-                            svt8 += VT[o];
-                            sp8 += PE[o];
-                        }
-                const float AVGVT8 = 0.125f * svt8;
-                const float vol = d.VOLOR[n];
-                c[8] = -gs * vol * AVGVT8;
-                c[9] = -gs * vol * srv * 0.125f;
-                c[10] = -gs * vol;
-                if (a.geom) a.gVOLOR[n] += -gs * (srv * AVGVT8 + sp8);
-            }
-        }
-    }
-    // faces I = const
-    if (hj && hk) {
-        const float gx = X.TF[n], gt = T.TF[n], gr = Rm.TF[n];
-        X.TF[n] = 0.0f; T.TF[n] = 0.0f; Rm.TF[n] = 0.0f;
-        const float FT = a.tFLOWT[n];
-        int m[4], m1[4], mm[4];
-        iface_nodes(d, i, j, k, m);
-        const float abx = d.ABX[n], abr = d.ABR[n], abt = A2(d.ABT, j, k);
-        const float AVGR = 0.25f * A2(d.RAVG_CELL, j, k);
-        if (!edge) {
-            float svx = 0.0f, svt = 0.0f, svr = 0.0f, sp = 0.0f;
-            for (int q = 0; q < 4; ++q) {
-                svx += VX[m[q]]; svt += VT[m[q]]; svr += VR[m[q]]; sp += PE[m[q]];
-            }
-            c[11] = 0.25f * gx * FT;
-            c[12] = 0.25f * gx * abx + gt * abt * AVGR + 0.25f * gr * abr;
-            c[13] = gt * FT * AVGR;
-            c[14] = 0.25f * gr * FT;
-            a.FLOWT[n] += 0.25f * gx * svx + gt * svt * AVGR + 0.25f * gr * svr;
+    // faces K = const: nodes (i,j,k), (i,j,k+1), (i+1,j,k+1), (i+1,j,k)
+    {
+        const float sp = ((pe[0][1][0] + pe[0][1][1]) + pe[1][1][1]) + pe[1][1][0];
+        const float svx = ((vx[0][1][0] + vx[0][1][1]) + vx[1][1][1]) + vx[1][1][0];
+        const float svt = ((vt[0][1][0] + vt[0][1][1]) + vt[1][1][1]) + vt[1][1][0];
+        const float svr = ((vr[0][1][0] + vr[0][1][1]) + vr[1][1][1]) + vr[1][1][0];
+        const float AVGR = 0.125f * (rjk + rk1);
+        c[0] = 0.25f * gxk * aqx + 0.25f * grk * aqr;
+        c[1] = 0.25f * gxk * fxw;
+        c[2] = gtk * fxw * AVGR;
+        c[3] = 0.25f * grk * fxw;
+        if (fk) {
+            a.FLOWX[n] = ofx + (0.25f * gxk * svx + gtk * AVGR * svt + 0.25f * grk * svr);
             if (a.geom) {
-                a.gABX[n] += 0.25f * gx * sp;
-                a.gABR[n] += 0.25f * gr * sp;
-                aadd(&A2(a.gABT, j, k), gt * sp * AVGR);
+                a.gAQX[n] += 0.25f * gxk * sp;
+                a.gAQR[n] += 0.25f * grk * sp;
+            }
+        }
+    }
+    // faces J = const: nodes (i,j,k), (i,j-1,k), (i+1,j-1,k), (i+1,j,k)
+    {
+        const float sp = ((pe[0][1][0] + pe[0][0][0]) + pe[1][0][0]) + pe[1][1][0];
+        const float svx = ((vx[0][1][0] + vx[0][0][0]) + vx[1][0][0]) + vx[1][1][0];
+        const float svt = ((vt[0][1][0] + vt[0][0][0]) + vt[1][0][0]) + vt[1][1][0];
+        const float svr = ((vr[0][1][0] + vr[0][0][0]) + vr[1][0][0]) + vr[1][1][0];
+        const float AVGR = (rjk + rj1) * 0.125f;
+        c[4] = 0.25f * gxj * asx + 0.25f * grj * asr;
+        c[5] = 0.25f * gxj * frw;
+        c[6] = gtj * frw * AVGR;
+        c[7] = 0.25f * grj * frw;
+        if (fj) {
+            a.FLOWR[n] = ofr + (0.25f * gxj * svx + gtj * svt * AVGR + 0.25f * grj * svr);
+            if (a.geom) {
+                a.gASX[n] += 0.25f * gxj * sp;
+                a.gASR[n] += 0.25f * grj * sp;
+            }
+        }
+    }
+    // radial source: the cell cube, summed in (di, dj, dk) order
+    {
+        float srv = 0.0f, svt8 = 0.0f, sp8 = 0.0f;
+#pragma unroll
+        for (int di = 0; di < 2; ++di)
+#pragma unroll
+            for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+                for (int dk = 0; dk < 2; ++dk) {
+                    srv += rv[di][dj][dk];
+                    svt8 += vt[di][dj][dk];
+                    sp8 += pe[di][dj][dk];
+                }
+        const float AVGVT8 = 0.125f * svt8;
+        c[8] = -gs * vol * AVGVT8;
+        c[9] = -gs * vol * srv * 0.125f;
+        c[10] = -gs * vol;
+        if (fs && a.geom && gs != 0.0f) a.gVOLOR[n] += -gs * (srv * AVGVT8 + sp8);
+    }
+    // faces I = const: nodes (i,j,k), (i,j-1,k), (i,j-1,k+1), (i,j,k+1)
+    {
+        const float AVGR = 0.25f * ravg;
+        const float svx = ((vx[0][1][0] + vx[0][0][0]) + vx[0][0][1]) + vx[0][1][1];
+        const float svt = ((vt[0][1][0] + vt[0][0][0]) + vt[0][0][1]) + vt[0][1][1];
+        const float svr = ((vr[0][1][0] + vr[0][0][0]) + vr[0][0][1]) + vr[0][1][1];
+        const float sp = ((pe[0][1][0] + pe[0][0][0]) + pe[0][0][1]) + pe[0][1][1];
+        c[11] = 0.25f * gxi * FT;
+        c[12] = 0.25f * gxi * abx + gti * abt * AVGR + 0.25f * gri * abr;
+        c[13] = gti * FT * AVGR;
+        c[14] = 0.25f * gri * FT;
+        if (fi) {
+            a.FLOWT[n] = oft + (0.25f * gxi * svx + gti * svt * AVGR + 0.25f * gri * svr);
+            if (a.geom) {
+                a.gABX[n] += 0.25f * gxi * sp;
+                a.gABR[n] += 0.25f * gri * sp;
+                aadd(&A2(a.gABT, j, k), gti * sp * AVGR);
             }
         } else {
-            iface_nodes(d, 1, j, k, m1);
-            iface_nodes(d, IM, j, k, mm);
-            if (gx != 0.0f) {
-                float svx = 0.0f, sp = 0.0f;
-                for (int q = 0; q < 4; ++q) {
-                    svx += VX[m1[q]] + VX[mm[q]];
-                    sp += PE[m1[q]] + PE[mm[q]];
-                    aadd(&a.VX[m1[q]], 0.125f * gx * FT);
-                    aadd(&a.VX[mm[q]], 0.125f * gx * FT);
-                    aadd(&a.PEFF[m1[q]], 0.125f * gx * abx);
-                    aadd(&a.PEFF[mm[q]], 0.125f * gx * abx);
-                }
-                aadd(&a.FLOWT[n], 0.125f * gx * svx);
-                if (a.geom) aadd(&a.gABX[n], 0.125f * gx * sp);
-            }
-            if (gt != 0.0f) {
-                auto rev_rvt = [&](int ii, const int *mq, float g) {
-                    const float ft = A3(a.tFLOWT, ii, j, k);
-                    float svt = 0.0f, sp = 0.0f;
-                    for (int q = 0; q < 4; ++q) {
-                        svt += VT[mq[q]];
-                        sp += PE[mq[q]];
-                        aadd(&a.VT[mq[q]], g * ft * AVGR);
-                        aadd(&a.PEFF[mq[q]], g * abt * AVGR);
-                    }
-                    aadd(&A3(a.FLOWT, ii, j, k), g * svt * AVGR);
-                    if (a.geom) aadd(&A2(a.gABT, j, k), g * sp * AVGR);
-                };
-                rev_rvt(1, m1, 0.5f * gt);
-                rev_rvt(IM, mm, 0.5f * gt);
-            }
-            if (gr != 0.0f) {
-                const float f1 = A3(a.tFLOWT, 1, j, k), fm = A3(a.tFLOWT, IM, j, k);
-                float svr1 = 0.0f, svrm = 0.0f, sp = 0.0f;
-                for (int q = 0; q < 4; ++q) {
-                    svr1 += VR[m1[q]];
-                    svrm += VR[mm[q]];
-                    sp += PE[m1[q]] + PE[mm[q]];
-                    aadd(&a.VR[m1[q]], 0.125f * gr * f1);
-                    aadd(&a.VR[mm[q]], 0.125f * gr * fm);
-                    aadd(&a.PEFF[m1[q]], 0.125f * gr * abr);
-                    aadd(&a.PEFF[mm[q]], 0.125f * gr * abr);
-                }
-                aadd(&A3(a.FLOWT, 1, j, k), 0.125f * gr * svr1);
-                aadd(&A3(a.FLOWT, IM, j, k), 0.125f * gr * svrm);
-                if (a.geom) aadd(&a.gABR[n], 0.125f * gr * sp);
-            }
+            c[11] = c[12] = c[13] = c[14] = 0.0f;
         }
+        if (edge) rev_mom_iface_edge(d, a, i, j, k, gxi, gti, gri, abx, abt, abr, AVGR);
     }
-    for (int q = 0; q < MOM_NCOEF; ++q) cf[(size_t)q * N + n] = c[q];
+    for (int q = 0; q < MOM_NCOEF; ++q) a.cf[(size_t)q * N + n] = c[q];
 }
 
 __global__ void rk_flux_mom_gather(const Dev d, const Adj a) {
@@ -766,11 +790,24 @@ __global__ void rk_flux_mom_gather(const Dev d, const Adj a) {
             const int o = ix3(d, i, jj, kk);       // I face of owner (i, jj, kk)
             gVX += C(11, o); gP += C(12, o); gVT += C(13, o); gVR += C(14, o);
         }
-    a.PEFF[n] += gP;
+    const bool peff_here = d.F_PDOWN == 0.0f;
+    if (peff_here)
+        a.P[n] += a.PEFF[n] + gP;   // PEFF = P - PREFF: its whole adjoint is P's
+    else
+        a.PEFF[n] += gP;            // rk_peff distributes it over P(J) and P(J+1)
     a.VX[n] += gVX;
     a.VT[n] += gVT;
     a.VR[n] += gVR;
     a.ROVT[n] += gRV;
+    // clear the adjoints that rk_flux_mom_coef consumed.  Stored here, and
+    // not where they were read: a store of a constant to an address whose
+    // load is still in flight stalls that kernel's warps for a long time.
+    if (peff_here) a.PEFF[n] = 0.0f;
+    const AdjVar *W = &a.v[V_ROVX];
+    for (int v = 0; v < 3; ++v) {
+        const AdjVar &V = W[v];
+        V.XF[n] = 0.0f; V.RF[n] = 0.0f; V.TF[n] = 0.0f; V.SR[n] = 0.0f;
+    }
 }
 
 // =====================================================================
@@ -1734,13 +1771,19 @@ __global__ void rk_norms(const __grid_constant__ Dev d, const __grid_constant__ 
 
 // Krylov vector kernels over packed adjoint vectors of length len
 // out[i] += V_i . w for i < nv (grid.y = i), FP64
+// Dot products <V_i, w>.  Each thread sums its strided elements in FP32 (a
+// few dozen terms), and the partial sums are added across threads in FP64.
+// FP64 arithmetic is a small fraction of the FP32 rate on this GPU, so a
+// conversion and an FP64 multiply-add per element would cost more than the
+// memory traffic.
 __global__ void rk_kdots(const float *V, int nv, const float *w, size_t len, double *out) {
     __shared__ double sh[RT_BS / 32];
     const int i = blockIdx.y;
     const float *v = V + (size_t)i * len;
-    double s = 0.0;
+    float sf = 0.0f;
     for (size_t t = (size_t)blockIdx.x * RT_BS + threadIdx.x; t < len; t += (size_t)gridDim.x * RT_BS)
-        s += (double)v[t] * (double)w[t];
+        sf += v[t] * w[t];
+    double s = (double)sf;
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
     __syncthreads();
@@ -1750,12 +1793,16 @@ __global__ void rk_kdots(const float *V, int nv, const float *w, size_t len, dou
         atomicAdd(&out[i], t);
     }
 }
-// w += sign * sum_i c_i V_i
+// w += sign * sum_i c_i V_i, in FP32 (the basis vectors are FP32)
+constexpr int KMAX = 256;
 __global__ void rk_kcomb(const float *V, int nv, const double *c, float sign, float *w, size_t len) {
+    __shared__ float cs[KMAX];
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) cs[i] = sign * (float)c[i];
+    __syncthreads();
     for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < len; t += (size_t)gridDim.x * blockDim.x) {
-        double s = 0.0;
-        for (int i = 0; i < nv; ++i) s += c[i] * (double)V[(size_t)i * len + t];
-        w[t] = (float)((double)w[t] + (double)sign * s);
+        float s = 0.0f;
+        for (int i = 0; i < nv; ++i) s += cs[i] * V[(size_t)i * len + t];
+        w[t] += s;
     }
 }
 // y = a x
@@ -1862,7 +1909,7 @@ void enqueue_reverse(const Dev &d, const Adj &a, cudaStream_t s) {
     launch_tstep_rev(d, a, s, V_ROVX, 3);
     rk_flux_mom_coef<<<gN, 256, 0, s>>>(d, a);
     rk_flux_mom_gather<<<gN, 256, 0, s>>>(d, a);
-    rk_peff<<<gN, 256, 0, s>>>(d, a);
+    if (d.F_PDOWN != 0.0f) rk_peff<<<gN, 256, 0, s>>>(d, a);
     rk_bc_apply<<<gridn((size_t)d.IM * d.KM, 128), 128, 0, s>>>(d, a);
     launch_tstep_rev(d, a, s, V_RO, 2);
     rk_flux_energy_coef<<<gN, 256, 0, s>>>(d, a);
