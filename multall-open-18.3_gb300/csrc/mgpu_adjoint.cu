@@ -1368,7 +1368,7 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_gather(const __grid_constant__ De
     const int damp_on = ctl->damp_on;
     const float DAMP = ctl->DAMP;
     const float blk = damp_on ? V.tBLK[A1(d.NROW, jc) - 1] : 1.0f;
-    double pb = 0.0;
+    float pbf = 0.0f;             // FP32 per thread, FP64 across threads
     for (int c = threadIdx.x; c < nc; c += RT_BS) {
         const int i = c % IMM1 + 1, k = c / IMM1 + 1;
         const float g = av[c];
@@ -1378,10 +1378,11 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_gather(const __grid_constant__ De
             const float q = fabsf(S) / (blk * DAMP);
             const float r = 1.0f / (1.0f + q);
             out = g * r * r;
-            pb += (double)(g * S * q / blk * r * r);
+            pbf += g * S * q / blk * r * r;
         }
         A3(V.ST, i, jc, k) = out;
     }
+    double pb = (double)pbf;
     for (int o = 16; o > 0; o >>= 1) pb += __shfl_down_sync(0xffffffffu, pb, o);
     if ((threadIdx.x & 31) == 0) shd[threadIdx.x >> 5] = pb;
     __syncthreads();
@@ -1438,7 +1439,7 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_damp(const __grid_constant__ Dev 
             if (j >= JST && j <= JEN) add = gchg[nr - 1] / (float)(IMM1 * KMM1 * (JEN - JST + 1));
         }
     }
-    double ps = 0.0;
+    float psf = 0.0f;             // FP32 per thread, FP64 across threads
     for (int c = threadIdx.x; c < nc; c += RT_BS) {
         const int i = c % IMM1 + 1, k = c / IMM1 + 1;
         const int n = ix3(d, i, j, k);
@@ -1447,8 +1448,9 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_damp(const __grid_constant__ Dev 
         V.ST[n] = g;
         const float y = g * d.RSTEP[n];
         V.Y[n] = y;
-        ps += (double)y;
+        psf += y;
     }
+    double ps = (double)psf;
     for (int o = 16; o > 0; o >>= 1) ps += __shfl_down_sync(0xffffffffu, ps, o);
     if ((threadIdx.x & 31) == 0) shd[threadIdx.x >> 5] = ps;
     __syncthreads();

@@ -201,14 +201,17 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_cells(const __grid_constan
         }
         __syncthreads();
     }
-    double ps = 0.0;
+    // plane sum: a thread's dozen cells in FP32, the threads' partials in
+    // FP64 (FP64 arithmetic is slow on this GPU: one FP64 add per cell
+    // kept its pipe a third busy)
+    float psf = 0.0f;
     for (int c = threadIdx.x; c < nc; c += BS) {
         int i = c % IMM1 + 1, k = c / IMM1 + 1;
         float v = st[c];
         A3(V.ST, i, j, k) = v;
-        ps += (double)v;
+        psf += v;
     }
-    ps = block_sum<BS>(ps, shd);
+    const double ps = block_sum<BS>((double)psf, shd);
     if (threadIdx.x == 0) V.psum[j - 1] = ps;
     // level-1 and level-2 partial sums of this plane
     const int n1 = d.NIB1 * d.NKB1, n2 = d.NIB2 * d.NKB2;
@@ -348,7 +351,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
     }
     __syncthreads();
     const float SBCHG = s_sb, SSB = A1(d.STEPSBK, jsb);
-    double sabs = 0.0;
+    float sabs = 0.0f;            // FP32 per thread, FP64 across threads (as in k_ts_cells)
     w = Walk2(IMM1, threadIdx.x, BS);
 #pragma unroll
     for (int u = 0; u < TS_U; ++u) {
@@ -358,7 +361,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
             const size_t n = pj + (size_t)(i - 1) + ks * (k - 1);
             float DELTA = pst[u] * pstp[u] + (b1[pb1[u]] * ps1[u] + b2[pb2[u]] * ps2[u] + SBCHG * SSB) * prs[u];
             V.ST[n] = DELTA;
-            sabs += (double)fabsf(DELTA);
+            sabs += fabsf(DELTA);
         }
     }
     for (int c = threadIdx.x + TS_U * BS; c < nc; c += BS, w.next()) {
@@ -370,11 +373,11 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
         float B1 = b1[(k1 - 1) * d.NIB1 + (i1 - 1)], B2 = b2[(k2 - 1) * d.NIB2 + (i2 - 1)];
         float DELTA = V.ST[n] * d.STEP[n] + (B1 * d.STEP1[s1] + B2 * d.STEP2[s2] + SBCHG * SSB) * d.RSTEP[n];
         V.ST[n] = DELTA;
-        sabs += (double)fabsf(DELTA);
+        sabs += fabsf(DELTA);
     }
     if (want_abs) {
-        sabs = block_sum<BS>(sabs, shd);
-        if (threadIdx.x == 0) V.pabs[j - 1] = sabs;
+        const double t = block_sum<BS>((double)sabs, shd);
+        if (threadIdx.x == 0) V.pabs[j - 1] = t;
     }
 }
 
@@ -386,12 +389,12 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_plane_abs(const __grid_con
     const VarSet &V = d.var[v0 + blockIdx.y];
     int j = blockIdx.x + 2;
     int nc = d.IMM1 * d.KMM1;
-    double s = 0.0;
+    float sf = 0.0f;
     for (int c = threadIdx.x; c < nc; c += BS) {
         int i = c % d.IMM1 + 1, k = c / d.IMM1 + 1;
-        s += (double)fabsf(A3(V.ST, i, j, k));
+        sf += fabsf(A3(V.ST, i, j, k));
     }
-    s = block_sum<BS>(s, shd);
+    const double s = block_sum<BS>((double)sf, shd);
     if (threadIdx.x == 0) V.pabs[j - 1] = s;
 }
 
