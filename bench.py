@@ -287,7 +287,9 @@ def run_batch(args, rank, world, local_rank):
             "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOADS["batch64"][1], "instances": BATCH, "nodes": nodes,
-                       "autotune": {"tstep_threads_per_cta": {str(b): tuned.count(b) for b in (128, 256, 512)}},
+                       "autotune": {"tstep_threads_per_cta": {
+                           p: {str(b): [t[q] for t in tuned].count(b) for b in (128, 192, 256, 512)}
+                           for q, p in enumerate(("ro_roe_pass", "momentum_pass"))}},
                        "l2": "flushed between timed steps", "parallelism": f"replicas: one batch per GPU x{world}",
                        "reductions": "FP64 tree sums (REDUCE_ORDER=0)"},
             "roofline": {"bound": "hbm", "kernel": None, "peak": peak, "unit": "GB/s", "peak_source": peak_kind,
@@ -457,7 +459,7 @@ def run_gpu(args, rank, world, local_rank):
     kps = prob.kernels_per_step()
     kps_loss, kps_tail = prob.kernels_per_step(loss=True) - kps, prob.kernels_per_step(tail=True) - kps
     prob.run(max(args.warmup, 3))
-    tuned, tune_ms = 256, [None, None, None]
+    tuned, tune_ms = (256, 256), None
     if os.environ.get("MGPU_AUTOTUNE", "1") != "0":
         tuned, tune_ms = prob.autotune()    # threads per J-plane CTA of the TSTEP kernels
         prob.run(3)
@@ -540,8 +542,9 @@ def run_gpu(args, rank, world, local_rank):
             "config": {"workload": WORKLOADS[ARGS_WORKLOAD][1], "nodes": N, "l2": "flushed between timed steps",
                        "parallelism": f"replicas: one instance per GPU x{world}",
                        "reductions": "FP64 tree sums (REDUCE_ORDER=0)",
-                       "autotune": {"tstep_threads_per_cta": tuned,
-                                    "tstep_pass_ms": dict(zip(("128", "256", "512"), tune_ms))}},
+                       "autotune": {"tstep_threads_per_cta": {"ro_roe_pass": tuned[0], "momentum_pass": tuned[1]},
+                                    "tstep_pass_ms": None if tune_ms is None else
+                                    {p: dict(zip(("128", "192", "256", "512"), v)) for p, v in tune_ms.items()}}},
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "alg_bytes_per_launch": alg_step / launches_step,

@@ -274,14 +274,17 @@ int32_t mgpu_adjoint_set(mgpu_handle *h, const char *name, const float *in, int6
  * which = 0 a plain step, 1 a LOSS step, 2 a tail step (every 5th), 3 a step
  * that is both. */
 int32_t mgpu_kernels_per_step(mgpu_handle *h, int32_t which);
-/* The autotuner: times TSTEP (the five variables, both launches) with 128,
- * 256 and 512 threads per J-plane CTA on the handle's current arrays,
- * restores them, and keeps the fastest for the handle's step graph.
- * *chosen = the threads per CTA; ms (3 entries, or NULL) = the time of one
- * TSTEP pass per candidate.  The default without tuning is 256.  The
- * candidates differ in the association of two FP64 per-plane sums, so a
- * tuned handle is deterministic for its choice; two choices can differ in
- * the last bit of a value.  A member of a batch keeps its own choice. */
+/* The autotuner: times each of the two TSTEP launches of a step (RO and
+ * ROE; the three momenta) with 128, 192, 256 and 512 threads per J-plane CTA
+ * on the handle's current arrays, restores them, and keeps the fastest size
+ * of each launch for the handle's step graph.  chosen (2 entries, or NULL)
+ * = the threads per CTA of the RO/ROE launch and of the momentum launch;
+ * ms (8 entries, or NULL) = the time of one launch per candidate, the RO/ROE
+ * launch's four first.  The default without tuning is 256 for both.  The
+ * candidates differ in the association of per-plane sums (FP32 within a
+ * thread, FP64 across threads), so a tuned handle is deterministic for its
+ * choice; two choices can differ in the last bits of a value.  A member of
+ * a batch keeps its own choice. */
 int32_t mgpu_autotune(mgpu_handle *h, int32_t *chosen, double *ms);
 /* Runs nsteps iterations, each bracketed by CUDA events on the handle's
  * stream; with flush_l2=1 a buffer larger than L2 is rewritten between the

@@ -450,7 +450,7 @@ int32_t mgpu_create(int32_t im, int32_t jm, int32_t km, int32_t nrows, mgpu_hand
     d.IMID = (int)(0.5f * im);
     d.KMID = (int)(0.5f * km);
     d.NRWSM1 = nrows - 1;
-    d.ts_bs = 256;
+    d.ts_bs[0] = d.ts_bs[1] = 256;
 #define MGPU_DEF_I(n, v) d.n = v;
     MGPU_INT_SCALARS(MGPU_DEF_I)
 #define MGPU_DEF_R(n, v) d.n = v;
@@ -803,9 +803,10 @@ int32_t mgpu_commit(mgpu_handle *h) {
             return rc;
     }
     if (d.REDUCE_ORDER != 0 && d.REDUCE_ORDER != 1) return fail(MGPU_E_ARG, "REDUCE_ORDER must be 0 or 1");
-    if (d.TS_THREADS != 0 && d.TS_THREADS != 128 && d.TS_THREADS != 256 && d.TS_THREADS != 512)
-        return fail(MGPU_E_ARG, "TS_THREADS must be 0, 128, 256 or 512");
-    d.ts_bs = d.TS_THREADS ? d.TS_THREADS : 256;
+    if (d.TS_THREADS != 0 && d.TS_THREADS != 128 && d.TS_THREADS != 192 && d.TS_THREADS != 256 &&
+        d.TS_THREADS != 512)
+        return fail(MGPU_E_ARG, "TS_THREADS must be 0, 128, 192, 256 or 512");
+    d.ts_bs[0] = d.ts_bs[1] = d.TS_THREADS ? d.TS_THREADS : 256;
     // the control block
     DevCtl c;
     memset(&c, 0, sizeof(c));
@@ -949,45 +950,62 @@ int32_t mgpu_autotune(mgpu_handle *h, int32_t *chosen, double *ms) {
         CK(cudaMemcpyAsync(save + (size_t)(2 * v) * N, d.var[v].D, fb, cudaMemcpyDeviceToDevice, h->stream));
         CK(cudaMemcpyAsync(save + (size_t)(2 * v + 1) * N, d.var[v].DIFF, fb, cudaMemcpyDeviceToDevice, h->stream));
     }
-    const int cand[3] = {128, 256, 512};
-    double t[3] = {0.0, 0.0, 0.0};
+    constexpr int NC = 4;
+    const int cand[NC] = {128, 192, 256, 512};
+    // each timed pass starts from a cold L2, as it does inside a step (the
+    // passes run back to back would find their arrays in L2)
+    if (!h->flush_buf) {
+        int l2 = 0;
+        CK(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, h->device));
+        h->flush_bytes = (size_t)(l2 > 0 ? l2 : 128 << 20) * 2;
+        CK(cudaMalloc(&h->flush_buf, h->flush_bytes));
+    }
+    double t[2][NC] = {};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    int best = 1;
-    for (int c = 0; c < 3; ++c) {
-        Dev dt = d;
-        dt.ts_bs = cand[c];
-        dt.use_cond = 0;
-        Launch L{h->stream, h->sm_count};
-        for (int r = 0; r < 2; ++r) {
-            launch_tstep(dt, L, V_RO, 2);
-            launch_tstep(dt, L, V_ROVX, 3);
+    int best[2] = {2, 2};
+    // each pass on its own: the pass of RO and ROE (2 x (JM-1) CTAs) and the
+    // pass of the momenta (3 x (JM-1)) fill the SMs differently
+    for (int p = 0; p < 2; ++p) {
+        const int v0 = p ? V_ROVX : V_RO, nv = p ? 3 : 2;
+        for (int c = 0; c < NC; ++c) {
+            Dev dt = d;
+            dt.ts_bs[p] = cand[c];
+            dt.use_cond = 0;
+            Launch L{h->stream, h->sm_count};
+            for (int r = 0; r < 2; ++r) launch_tstep(dt, L, v0, nv);
+            const int reps = 10;
+            double sum = 0.0;
+            for (int r = 0; r < reps; ++r) {
+                CK(cudaMemsetAsync(h->flush_buf, r & 0xff, h->flush_bytes, h->stream));
+                CK(cudaEventRecord(e0, h->stream));
+                launch_tstep(dt, L, v0, nv);
+                CK(cudaEventRecord(e1, h->stream));
+                CK(cudaGetLastError());
+                CK(cudaEventSynchronize(e1));
+                float f = 0.0f;
+                CK(cudaEventElapsedTime(&f, e0, e1));
+                sum += (double)f;
+            }
+            t[p][c] = sum / reps;
+            for (int v = v0; v < v0 + nv; ++v) {
+                CK(cudaMemcpyAsync(d.var[v].D, save + (size_t)(2 * v) * N, fb, cudaMemcpyDeviceToDevice, h->stream));
+                CK(cudaMemcpyAsync(d.var[v].DIFF, save + (size_t)(2 * v + 1) * N, fb, cudaMemcpyDeviceToDevice,
+                                   h->stream));
+            }
         }
-        CK(cudaEventRecord(e0, h->stream));
-        const int reps = 10;
-        for (int r = 0; r < reps; ++r) {
-            launch_tstep(dt, L, V_RO, 2);
-            launch_tstep(dt, L, V_ROVX, 3);
-        }
-        CK(cudaEventRecord(e1, h->stream));
-        CK(cudaGetLastError());
-        CK(cudaEventSynchronize(e1));
-        float f = 0.0f;
-        CK(cudaEventElapsedTime(&f, e0, e1));
-        t[c] = (double)f / reps;
-        for (int v = 0; v < NVAR; ++v) {
-            CK(cudaMemcpyAsync(d.var[v].D, save + (size_t)(2 * v) * N, fb, cudaMemcpyDeviceToDevice, h->stream));
-            CK(cudaMemcpyAsync(d.var[v].DIFF, save + (size_t)(2 * v + 1) * N, fb, cudaMemcpyDeviceToDevice, h->stream));
-        }
-        if (t[c] < t[best]) best = c;
+        // the fastest candidate, once all are timed
+        for (int c = 0; c < NC; ++c)
+            if (t[p][c] < t[p][best[p]]) best[p] = c;
     }
     CK(cudaFreeAsync(save, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (d.ts_bs != cand[best]) {
-        d.ts_bs = cand[best];
+    if (d.ts_bs[0] != cand[best[0]] || d.ts_bs[1] != cand[best[1]]) {
+        d.ts_bs[0] = cand[best[0]];
+        d.ts_bs[1] = cand[best[1]];
         if (h->gexec) {
             cudaGraphExecDestroy(h->gexec);
             h->gexec = nullptr;
@@ -997,9 +1015,13 @@ int32_t mgpu_autotune(mgpu_handle *h, int32_t *chosen, double *ms) {
             h->graph = nullptr;
         }
     }
-    if (chosen) *chosen = cand[best];
+    if (chosen) {
+        chosen[0] = cand[best[0]];
+        chosen[1] = cand[best[1]];
+    }
     if (ms)
-        for (int c = 0; c < 3; ++c) ms[c] = t[c];
+        for (int p = 0; p < 2; ++p)
+            for (int c = 0; c < NC; ++c) ms[p * NC + c] = t[p][c];
     return 0;
 }
 

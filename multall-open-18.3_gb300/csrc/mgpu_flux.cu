@@ -121,26 +121,29 @@ __global__ void __launch_bounds__(PRIM_BS) k_prim(Dev d) {
         int i, j, k;
         node_ijk(d, n, i, j, k);
         if (j >= 2) {
-            float RRNOW = 1.0f / A2(d.R, j, k);
-            float RECIP = 1.0f / d.RO[n];
-            float vx = d.ROVX[n] * RECIP;
-            float vr = d.ROVR[n] * RECIP;
-            float rovt = d.RORVT[n] * RRNOW;
+            // every load before the first store (a store through one Dev
+            // pointer keeps later loads through another behind it)
+            const bool thermo = j <= d.JMM1;
+            const float rr = A2(d.R, j, k), RONOW = d.RO[n], rovx = d.ROVX[n], rovr = d.ROVR[n];
+            const float rorvt = d.RORVT[n], roe = thermo ? d.ROE[n] : 0.0f, wt = do_tail ? d.WT[n] : 0.0f;
+            float RRNOW = 1.0f / rr;
+            float RECIP = 1.0f / RONOW;
+            float vx = rovx * RECIP;
+            float vr = rovr * RECIP;
+            float rovt = rorvt * RRNOW;
             float vt = rovt * RECIP;
             d.VX[n] = vx;
             d.VR[n] = vr;
             d.ROVT[n] = rovt;
             d.VT[n] = vt;
             if (do_tail) {
-                float wt = d.WT[n];
                 float EKE = vr * vr + wt * wt + vx * vx;
                 eke_s = (double)EKE;
                 key = max_key(EKE, n);
             }
-            if (j <= d.JMM1) {
-                float RONOW = d.RO[n];
+            if (thermo) {
                 float EKE = 0.5f * (vr * vr + vt * vt + vx * vx);
-                float TSTATIC = (d.ROE[n] / RONOW - EKE) / d.CV;
+                float TSTATIC = (roe / RONOW - EKE) / d.CV;
                 d.P[n] = RONOW * d.RGAS * TSTATIC;
                 d.HO[n] = d.CP * TSTATIC + EKE;
                 d.T_STATIC[n] = TSTATIC;
@@ -177,19 +180,20 @@ __global__ void k_flux_mass(Dev d) {
     if (n >= N) return;
     int i, j, k;
     node_ijk(d, n, i, j, k);
-    if (i < d.IM && k < d.KM) {
+    // results are kept in registers and stored at the end, so that no store
+    // orders the loads of a later section behind it
+    const bool hx = i < d.IM && k < d.KM, ht = j >= 2 && k < d.KM, hr = i < d.IM && j >= 2;
+    float fx = 0.0f, ft = 0.0f, fr = 0.0f;
+    if (hx) {
         float AVGRVX = A3(d.ROVX, i, j, k) + A3(d.ROVX, i, j, k + 1) + A3(d.ROVX, i + 1, j, k) + A3(d.ROVX, i + 1, j, k + 1);
         float AVGRVR = A3(d.ROVR, i, j, k) + A3(d.ROVR, i, j, k + 1) + A3(d.ROVR, i + 1, j, k) + A3(d.ROVR, i + 1, j, k + 1);
-        float fx = 0.25f * (AVGRVX * A3(d.AQX, i, j, k) + AVGRVR * A3(d.AQR, i, j, k));
-        d.FLOWX[n] = fx;
+        fx = 0.25f * (AVGRVX * A3(d.AQX, i, j, k) + AVGRVR * A3(d.AQR, i, j, k));
     }
-    {
-        float rowt = d.ROVT[n] - A2(d.UBLADE, j, k) * d.RO[n];
-        d.ROWT[n] = rowt;
-        d.WT[n] = rowt / d.RO[n];
-    }
-    if (j >= 2 && k < d.KM) {
-        float ft = flowt_raw(d, i, j, k);
+    const float ro = d.RO[n];
+    const float rowt = d.ROVT[n] - A2(d.UBLADE, j, k) * ro;
+    const float wt = rowt / ro;
+    if (ht) {
+        ft = flowt_raw(d, i, j, k);
         if (i == 1 || i == d.IM) {
             if (A1(d.IND, j) != 1) {
                 float f1 = (i == 1) ? ft : flowt_raw(d, 1, j, k);
@@ -200,17 +204,19 @@ __global__ void k_flux_mass(Dev d) {
                 if (k >= A1(d.KS1, nr) && k <= A1(d.KS2, nr)) ft = 0.0f;
             }
         }
-        d.FLOWT[n] = ft;
     }
-    if (i < d.IM && j >= 2) {
-        float fr = 0.0f;
+    if (hr) {
         if (k >= 2 && k <= d.KMM1) {
             float AVGRVX = A3(d.ROVX, i, j, k) + A3(d.ROVX, i, j - 1, k) + A3(d.ROVX, i + 1, j - 1, k) + A3(d.ROVX, i + 1, j, k);
             float AVGRVR = A3(d.ROVR, i, j, k) + A3(d.ROVR, i, j - 1, k) + A3(d.ROVR, i + 1, j - 1, k) + A3(d.ROVR, i + 1, j, k);
             fr = 0.25f * (AVGRVX * A3(d.ASX, i, j, k) + AVGRVR * A3(d.ASR, i, j, k));
         }
-        d.FLOWR[n] = fr;
     }
+    if (hx) d.FLOWX[n] = fx;
+    d.ROWT[n] = rowt;
+    d.WT[n] = wt;
+    if (ht) d.FLOWT[n] = ft;
+    if (hr) d.FLOWR[n] = fr;
 }
 
 void launch_flux_mass(const Dev &d, Launch L) {
@@ -236,24 +242,30 @@ __global__ void k_flux_energy(Dev d) {
     int i, j, k;
     node_ijk(d, n, i, j, k);
     const VarSet &V = d.var[V_ROE];
-    if (i < d.IM && k < d.KM) {
+    // results in registers, stored at the end (as in k_flux_mass)
+    const bool hx = i < d.IM && k < d.KM, hs = hx && j >= 2, hr = i < d.IM && j >= 2, ht = j >= 2 && k < d.KM;
+    float xf = 0.0f, src = 0.0f, rf = 0.0f, tf = 0.0f;
+    if (hx) {
         float AVGHO = A3(d.HO, i, j, k) + A3(d.HO, i, j, k + 1) + A3(d.HO, i + 1, j, k) + A3(d.HO, i + 1, j, k + 1);
-        V.XF[n] = d.FLOWX[n] * AVGHO * 0.25f;
-        if (j >= 2) V.SR[n] = d.QSOURCE[n];
+        xf = d.FLOWX[n] * AVGHO * 0.25f;
+        if (hs) src = d.QSOURCE[n];
     }
-    if (i < d.IM && j >= 2) {
+    if (hr) {
         float AVGHO = 0.25f * (A3(d.HO, i, j, k) + A3(d.HO, i, j - 1, k) + A3(d.HO, i + 1, j - 1, k) + A3(d.HO, i + 1, j, k));
-        V.RF[n] = d.FLOWR[n] * AVGHO;
+        rf = d.FLOWR[n] * AVGHO;
     }
-    if (j >= 2 && k < d.KM) {
-        float tf = tflux_energy_raw(d, i, j, k);
+    if (ht) {
+        tf = tflux_energy_raw(d, i, j, k);
         if ((i == 1 || i == d.IM) && A1(d.IND, j) != 1) {
             float t1 = (i == 1) ? tf : tflux_energy_raw(d, 1, j, k);
             float tm = (i == d.IM) ? tf : tflux_energy_raw(d, d.IM, j, k);
             tf = 0.5f * (t1 + tm);
         }
-        V.TF[n] = tf;
     }
+    if (hx) V.XF[n] = xf;
+    if (hs) V.SR[n] = src;
+    if (hr) V.RF[n] = rf;
+    if (ht) V.TF[n] = tf;
 }
 
 void launch_flux_energy(const Dev &d, Launch L) {
@@ -633,7 +645,7 @@ __device__ inline float tflux_rmom_raw(const Dev &d, int i, int j, int k, float 
 // reference's expression.  The balances at I=1 and I=IM, which also need the
 // other end's column, keep the direct loads of the helpers above.
 
-__global__ void __launch_bounds__(256, 4) k_flux_mom(Dev d) {
+__global__ void __launch_bounds__(256, 3) k_flux_mom(Dev d) {
     pdl_wait();
     const int n = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int N = d.IM * d.JM * d.KM;
@@ -666,32 +678,49 @@ __global__ void __launch_bounds__(256, 4) k_flux_mom(Dev d) {
                 if (hi && hj && hk) rv[di][dj + 1][dk] = RV[o];
             }
 #define C(a, di, dj, dk) a[di][(dj) + 1][dk]
+    // every per-node operand is loaded before the first store, so that the
+    // loads are in flight together (the stores below may not be reordered
+    // ahead of loads through other Dev pointers)
+    const bool fK = hi && hk, fJ = hi && hj, fI = hj && hk, fS = fJ && hk;
+    const float xforce = fK ? d.XFORCE[n] : 0.0f, tforce = fK ? d.TFORCE[n] : 0.0f;
+    const float aqx = fK ? d.AQX[n] : 0.0f, aqr = fK ? d.AQR[n] : 0.0f, flowx = fK ? d.FLOWX[n] : 0.0f;
+    const float rjk = A2(d.R, j, k);
+    const float rk1 = fK ? A2(d.R, j, k + 1) : 0.0f, rj1 = fJ ? A2(d.R, j - 1, k) : 0.0f;
+    const float asx = fJ ? d.ASX[n] : 0.0f, asr = fJ ? d.ASR[n] : 0.0f, flowr = fJ ? d.FLOWR[n] : 0.0f;
+    const float rforce = fS ? d.RFORCE[n] : 0.0f, volor = fS ? d.VOLOR[n] : 0.0f;
+    const float FT = fI ? d.FLOWT[n] : 0.0f, abx = fI ? d.ABX[n] : 0.0f, abr = fI ? d.ABR[n] : 0.0f;
+    const float abt = fI ? A2(d.ABT, j, k) : 0.0f, ravg = fI ? A2(d.RAVG_CELL, j, k) : 0.0f;
+    const bool edge = (i == 1 || i == IM) && A1(d.IND, j) != 1;
+    const float *RO = d.RO;
+    const bool dens = j >= 3 && j <= d.JM - 3;
+    const float ro0 = RO[n];
+    const float rom2 = dens ? RO[n - 2 * sJ] : 0.0f, rom1 = dens ? RO[n - sJ] : 0.0f;
+    const float rop1 = dens ? RO[n + sJ] : 0.0f, rop2 = dens ? RO[n + 2 * sJ] : 0.0f;
     d.PEFF[n] = C(pe, 0, 0, 0);    // PEFF of this step, read by the next step's energy fluxes
     const VarSet &VXm = d.var[V_ROVX], &VTm = d.var[V_RORVT], &VRm = d.var[V_ROVR];
-    const bool edge = (i == 1 || i == IM) && A1(d.IND, j) != 1;
     // faces K = const (XFLUX) and the axial / tangential sources
-    if (hi && hk) {
-        VXm.SR[n] = d.XFORCE[n];
+    if (fK) {
+        VXm.SR[n] = xforce;
         float AVGP = C(pe, 0, 0, 0) + C(pe, 0, 0, 1) + C(pe, 1, 0, 1) + C(pe, 1, 0, 0);
         float AVGVX = C(vx, 0, 0, 0) + C(vx, 0, 0, 1) + C(vx, 1, 0, 1) + C(vx, 1, 0, 0);
-        VXm.XF[n] = 0.25f * (AVGP * d.AQX[n] + d.FLOWX[n] * AVGVX);
-        float AVGR = 0.125f * (A2(d.R, j, k) + A2(d.R, j, k + 1));
+        VXm.XF[n] = 0.25f * (AVGP * aqx + flowx * AVGVX);
+        float AVGR = 0.125f * (rjk + rk1);
         float AVGVT = C(vt, 0, 0, 0) + C(vt, 0, 0, 1) + C(vt, 1, 0, 0) + C(vt, 1, 0, 1);
-        VTm.SR[n] = d.TFORCE[n];
-        VTm.XF[n] = d.FLOWX[n] * AVGR * AVGVT;
+        VTm.SR[n] = tforce;
+        VTm.XF[n] = flowx * AVGR * AVGVT;
         float AVGVR = C(vr, 0, 0, 0) + C(vr, 0, 0, 1) + C(vr, 1, 0, 0) + C(vr, 1, 0, 1);
-        VRm.XF[n] = 0.25f * (d.FLOWX[n] * AVGVR + d.AQR[n] * AVGP);
+        VRm.XF[n] = 0.25f * (flowx * AVGVR + aqr * AVGP);
     }
     // faces J = const (RFLUX) and the radial source
-    if (hi && hj) {
+    if (fJ) {
         float AVGP = C(pe, 0, 0, 0) + C(pe, 0, -1, 0) + C(pe, 1, -1, 0) + C(pe, 1, 0, 0);
         float AVGVX = C(vx, 0, 0, 0) + C(vx, 0, -1, 0) + C(vx, 1, -1, 0) + C(vx, 1, 0, 0);
-        VXm.RF[n] = 0.25f * (AVGP * d.ASX[n] + d.FLOWR[n] * AVGVX);
-        float AVGR = (A2(d.R, j, k) + A2(d.R, j - 1, k)) * 0.125f;
+        VXm.RF[n] = 0.25f * (AVGP * asx + flowr * AVGVX);
+        float AVGR = (rjk + rj1) * 0.125f;
         float AVGVT = C(vt, 0, 0, 0) + C(vt, 0, -1, 0) + C(vt, 1, -1, 0) + C(vt, 1, 0, 0);
-        VTm.RF[n] = d.FLOWR[n] * AVGVT * AVGR;
+        VTm.RF[n] = flowr * AVGVT * AVGR;
         float AVGVR = C(vr, 0, 0, 0) + C(vr, 0, -1, 0) + C(vr, 1, -1, 0) + C(vr, 1, 0, 0);
-        VRm.RF[n] = 0.25f * (d.FLOWR[n] * AVGVR + d.ASR[n] * AVGP);
+        VRm.RF[n] = 0.25f * (flowr * AVGVR + asr * AVGP);
         if (hk) {
             float AVGRVT = C(rv, 0, 0, 0) + C(rv, 0, 0, 1) + C(rv, 0, -1, 0) + C(rv, 0, -1, 1) + C(rv, 1, 0, 0) +
                            C(rv, 1, 0, 1) + C(rv, 1, -1, 0) + C(rv, 1, -1, 1);
@@ -699,12 +728,11 @@ __global__ void __launch_bounds__(256, 4) k_flux_mom(Dev d) {
                                      C(vt, 1, -1, 0) + C(vt, 1, -1, 1) + C(vt, 1, 0, 1));
             float AVGP8 = C(pe, 0, 0, 0) + C(pe, 0, -1, 0) + C(pe, 0, -1, 1) + C(pe, 0, 0, 1) + C(pe, 1, 0, 0) +
                           C(pe, 1, -1, 0) + C(pe, 1, -1, 1) + C(pe, 1, 0, 1);
-            VRm.SR[n] = d.RFORCE[n] - (AVGRVT * AVGVT8 + AVGP8) * d.VOLOR[n];
+            VRm.SR[n] = rforce - (AVGRVT * AVGVT8 + AVGP8) * volor;
         }
     }
     // faces I = const (TFLUX)
-    if (hj && hk) {
-        const float FT = d.FLOWT[n];
+    if (fI) {
         float AVGP = C(pe, 0, 0, 0) + C(pe, 0, -1, 0) + C(pe, 0, -1, 1) + C(pe, 0, 0, 1);
         if (edge) {
             float AVGPCUSP = peff_at(d, 1, j, k) + peff_at(d, 1, j - 1, k) + peff_at(d, 1, j, k + 1) +
@@ -712,14 +740,14 @@ __global__ void __launch_bounds__(256, 4) k_flux_mom(Dev d) {
                              peff_at(d, IM, j, k + 1) + peff_at(d, IM, j - 1, k + 1);
             float AVGVXCUSP = A3(VX, 1, j, k) + A3(VX, 1, j - 1, k) + A3(VX, 1, j, k + 1) + A3(VX, 1, j - 1, k + 1) +
                               A3(VX, IM, j, k) + A3(VX, IM, j - 1, k) + A3(VX, IM, j, k + 1) + A3(VX, IM, j - 1, k + 1);
-            VXm.TF[n] = 0.125f * (FT * AVGVXCUSP + AVGPCUSP * d.ABX[n]);
+            VXm.TF[n] = 0.125f * (FT * AVGVXCUSP + AVGPCUSP * abx);
         } else {
             float AVGVX = C(vx, 0, 0, 0) + C(vx, 0, -1, 0) + C(vx, 0, -1, 1) + C(vx, 0, 0, 1);
-            VXm.TF[n] = 0.25f * (FT * AVGVX + d.ABX[n] * AVGP);
+            VXm.TF[n] = 0.25f * (FT * AVGVX + abx * AVGP);
         }
-        const float AVGR = 0.25f * A2(d.RAVG_CELL, j, k);
+        const float AVGR = 0.25f * ravg;
         float AVGVT = C(vt, 0, 0, 0) + C(vt, 0, -1, 0) + C(vt, 0, -1, 1) + C(vt, 0, 0, 1);
-        float tf = (FT * AVGVT + A2(d.ABT, j, k) * AVGP) * AVGR;
+        float tf = (FT * AVGVT + abt * AVGP) * AVGR;
         if (edge) {
             float t1 = (i == 1) ? tf : tflux_rvt_raw(d, 1, j, k, AVGR);
             float tm = (i == IM) ? tf : tflux_rvt_raw(d, IM, j, k, AVGR);
@@ -727,7 +755,7 @@ __global__ void __launch_bounds__(256, 4) k_flux_mom(Dev d) {
         }
         VTm.TF[n] = tf;
         float AVGVR = C(vr, 0, 0, 0) + C(vr, 0, -1, 0) + C(vr, 0, -1, 1) + C(vr, 0, 0, 1);
-        float tr = 0.25f * (FT * AVGVR + AVGP * d.ABR[n]);
+        float tr = 0.25f * (FT * AVGVR + AVGP * abr);
         if (edge) {
             float ap1, apm;
             float t1raw = tflux_rmom_raw(d, 1, j, k, &ap1);
@@ -738,7 +766,7 @@ __global__ void __launch_bounds__(256, 4) k_flux_mom(Dev d) {
                                    peff_at(d, IM, j - 1, k + 1));
             float T1 = t1raw - AVGP1 * A3(d.ABR, 1, j, k);
             float T2 = tmraw - AVGPM * A3(d.ABR, IM, j, k);
-            tr = 0.5f * ((T1 + T2) + (AVGP1 + AVGPM) * d.ABR[n]);
+            tr = 0.5f * ((T1 + T2) + (AVGP1 + AVGPM) * abr);
         }
         VRm.TF[n] = tr;
     }
@@ -746,11 +774,10 @@ __global__ void __launch_bounds__(256, 4) k_flux_mom(Dev d) {
     // the density limiter's column flags (7200): RO is final here (after
     // TSTEP(RO) and the inlet/exit conditions) and TSTEP of the momenta
     // does not change it
-    if (d.ADJ_RO_LIM) d.ADJ_RO_LIM[n] = d.RO[n];
-    if (j >= 3 && j <= d.JM - 3) {
-        const float *RO = d.RO;
-        const float ROAVG = 0.25f * (RO[n - 2 * sJ] + RO[n - sJ] + RO[n + sJ] + RO[n + 2 * sJ]);
-        if (density_triggers(RO[n], ROAVG, d.ROLIM)) d.DFLAG[(size_t)(k - 1) * d.IM + (i - 1)] = 1;
+    if (d.ADJ_RO_LIM) d.ADJ_RO_LIM[n] = ro0;
+    if (dens) {
+        const float ROAVG = 0.25f * (rom2 + rom1 + rop1 + rop2);
+        if (density_triggers(ro0, ROAVG, d.ROLIM)) d.DFLAG[(size_t)(k - 1) * d.IM + (i - 1)] = 1;
     }
 }
 

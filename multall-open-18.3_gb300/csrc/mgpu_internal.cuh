@@ -130,7 +130,8 @@ struct Dev {
     // the step-control kernel when the step runs from the CUDA graph)
     int use_cond;
     unsigned long long cond_loss, cond_tail;
-    int ts_bs;                         // threads per J-plane CTA of TSTEP: 128, 256 or 512 (mgpu_autotune)
+    int ts_bs[2];                      // threads per J-plane CTA of TSTEP (128, 192, 256 or 512; mgpu_autotune)
+                                       // for the pass of 2 variables (RO, ROE) and the pass of 3 (momenta)
 };
 
 // Element offsets in 32-bit int: mgpu_create keeps IM*JM*KM below 2^30,

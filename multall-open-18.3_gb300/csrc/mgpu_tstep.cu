@@ -27,9 +27,11 @@ namespace mgpu {
 
 static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
 
-// Threads per J-plane CTA: 128, 256 (the default) or 512, chosen per
-// problem by mgpu_autotune (Dev::ts_bs); each size keeps 1024 threads of
-// 64 registers resident per SM.
+// Threads per J-plane CTA: 128, 192, 256 (the default) or 512, chosen per
+// problem and pass by mgpu_autotune (Dev::ts_bs); each size keeps 1024
+// threads of 64 registers resident per SM (960 for 192: five CTAs).  A pass
+// of 3 x 241 CTAs fills five 192-thread slots per SM in one wave, where four
+// 256-thread slots take 1.2 waves.
 constexpr int TS_U = 3;          // cells per thread whose loads are issued together
 constexpr int TS_UG = 4;         // the same for the damping and gather phases of update
 constexpr int SV_U = 3;          // points per thread whose streamwise loads are issued together
@@ -364,16 +366,35 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
             sabs += fabsf(DELTA);
         }
     }
-    for (int c = threadIdx.x + TS_U * BS; c < nc; c += BS, w.next()) {
-        const int i = w.i, k = w.k;
-        const int i1 = A1(d.IB1, i), i2 = A1(d.IB2, i), k1 = A1(d.KB1, k), k2 = A1(d.KB2, k);
-        const size_t s1 = (size_t)(i1 - 1) + (size_t)d.NIB1 * (j1 - 1) + m1 * (k1 - 1);
-        const size_t s2 = (size_t)(i2 - 1) + (size_t)d.NIB2 * (j2 - 1) + m2 * (k2 - 1);
-        const size_t n = pj + (size_t)(i - 1) + ks * (k - 1);
-        float B1 = b1[(k1 - 1) * d.NIB1 + (i1 - 1)], B2 = b2[(k2 - 1) * d.NIB2 + (i2 - 1)];
-        float DELTA = V.ST[n] * d.STEP[n] + (B1 * d.STEP1[s1] + B2 * d.STEP2[s2] + SBCHG * SSB) * d.RSTEP[n];
-        V.ST[n] = DELTA;
-        sabs += fabsf(DELTA);
+    // the remaining cells, TS_U at a time: their loads are issued together,
+    // before the stores of the group (a store of ST keeps later loads behind it)
+    for (int c0 = threadIdx.x + TS_U * BS; c0 < nc; c0 += TS_U * BS) {
+        int cn[TS_U];
+#pragma unroll
+        for (int u = 0; u < TS_U; ++u) {
+            const int i = w.i, k = w.k;
+            w.next();
+            cn[u] = -1;
+            if (c0 + u * BS < nc) {
+                const size_t n = pj + (size_t)(i - 1) + ks * (k - 1);
+                const int i1 = A1(d.IB1, i), i2 = A1(d.IB2, i), k1 = A1(d.KB1, k), k2 = A1(d.KB2, k);
+                cn[u] = (int)n;
+                pst[u] = V.ST[n];
+                pstp[u] = d.STEP[n];
+                prs[u] = d.RSTEP[n];
+                ps1[u] = d.STEP1[(size_t)(i1 - 1) + (size_t)d.NIB1 * (j1 - 1) + m1 * (k1 - 1)];
+                ps2[u] = d.STEP2[(size_t)(i2 - 1) + (size_t)d.NIB2 * (j2 - 1) + m2 * (k2 - 1)];
+                pb1[u] = (k1 - 1) * d.NIB1 + (i1 - 1);
+                pb2[u] = (k2 - 1) * d.NIB2 + (i2 - 1);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < TS_U; ++u) {
+            if (cn[u] < 0) continue;
+            float DELTA = pst[u] * pstp[u] + (b1[pb1[u]] * ps1[u] + b2[pb2[u]] * ps2[u] + SBCHG * SSB) * prs[u];
+            V.ST[cn[u]] = DELTA;
+            sabs += fabsf(DELTA);
+        }
     }
     if (want_abs) {
         const double t = block_sum<BS>((double)sabs, shd);
@@ -931,6 +952,7 @@ static cudaError_t configure_bs(const Dev &d) {
 cudaError_t configure_kernels(const Dev &d) {
     cudaError_t e = configure_bs<128>(d);
     if (e == cudaSuccess) e = configure_bs<256>(d);
+    if (e == cudaSuccess) e = configure_bs<192>(d);
     if (e == cudaSuccess) e = configure_bs<512>(d);
     if (e == cudaSuccess) e = configure_loss_kernels(d);
     return e != cudaSuccess ? e : configure_flux_kernels(d);
@@ -978,8 +1000,10 @@ static void launch_tstep_bs(const Dev &d, Launch L, int v0, int nv) {
 }
 
 void launch_tstep(const Dev &d, Launch L, int v0, int nv) {
-    if (d.ts_bs == 128) launch_tstep_bs<128>(d, L, v0, nv);
-    else if (d.ts_bs == 512) launch_tstep_bs<512>(d, L, v0, nv);
+    const int bs = d.ts_bs[nv >= 3 ? 1 : 0];
+    if (bs == 128) launch_tstep_bs<128>(d, L, v0, nv);
+    else if (bs == 192) launch_tstep_bs<192>(d, L, v0, nv);
+    else if (bs == 512) launch_tstep_bs<512>(d, L, v0, nv);
     else launch_tstep_bs<256>(d, L, v0, nv);
 }
 

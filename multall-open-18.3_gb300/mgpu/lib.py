@@ -221,12 +221,16 @@ class Problem:
         """Kernel launches of one step (LOSS and tail steps launch more)."""
         return _chk(load().mgpu_kernels_per_step(self.h, (1 if loss else 0) | (2 if tail else 0)))
 
-    def autotune(self) -> tuple[int, list]:
-        """(threads per J-plane CTA chosen, [ms per TSTEP pass for 128, 256, 512])."""
-        c = ctypes.c_int32()
-        ms = (ctypes.c_double * 3)()
-        _chk(load().mgpu_autotune(self.h, ctypes.byref(c), ms))
-        return c.value, list(ms)
+    TUNE_CANDIDATES = (128, 192, 256, 512)
+
+    def autotune(self) -> tuple[tuple, dict]:
+        """((threads per J-plane CTA chosen for the RO/ROE pass, for the
+        momentum pass), {"2": [ms per pass of 2 variables for 128, 192, 256,
+        512], "3": [the same for the pass of 3]})."""
+        c = (ctypes.c_int32 * 2)()
+        ms = (ctypes.c_double * 8)()
+        _chk(load().mgpu_autotune(self.h, c, ms))
+        return (c[0], c[1]), {"2": list(ms[:4]), "3": list(ms[4:])}
 
     def bench_steps(self, nsteps: int, flush_l2: bool = True) -> float:
         """Sum of the device times (ms) of nsteps iterations."""

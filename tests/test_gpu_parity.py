@@ -357,7 +357,7 @@ def test_api_errors(mods):
     assert e.value.code == -2
 
 
-@pytest.mark.parametrize("bs", [128, 512])
+@pytest.mark.parametrize("bs", [128, 192, 512])
 def test_tstep_cta_sizes_match_oracle(mods, bs):
     """Every CTA size the autotuner can choose gives the oracle's step: the
     small stage after one step within 1e-5 and after five steps (LOSS and
@@ -366,7 +366,8 @@ def test_tstep_cta_sizes_match_oracle(mods, bs):
     cd = common_setup.build_common(case.small_stage())
     probe = lib.Problem(cd)
     chosen, ms = probe.autotune()
-    assert chosen in (128, 256, 512) and all(m > 0 for m in ms)
+    assert all(c in (128, 192, 256, 512) for c in chosen)
+    assert all(m > 0 for p in ("2", "3") for m in ms[p])
     probe.close()
     cd.ints["TS_THREADS"] = bs
     gpu = lib.Problem(cd)
