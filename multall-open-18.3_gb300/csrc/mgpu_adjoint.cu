@@ -1072,6 +1072,11 @@ __global__ void rk_mach(const Dev d, const Adj a) {
 // redistribution, SCREE, flux sum)
 // =====================================================================
 constexpr int RT_BS = 256;
+// Cells (or nodes) per thread whose loads the J-plane reverse kernels issue
+// together before the group's stores: a store keeps every later load of the
+// thread behind it, so a one-at-a-time loop costs a memory round trip per
+// cell.
+constexpr int RT_U = 4;
 
 __device__ inline int mp_role_r(const Dev &d, int j, int *nr) {
     for (int r = 1; r <= d.NRWSM1; ++r) {
@@ -1329,9 +1334,24 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_gather(const __grid_constant__ De
     const int IM = d.IM, IMM1 = d.IMM1, KMM1 = d.KMM1;
     const int j = blockIdx.x + 1;
     // the variable's own adjoint: D = TMP + gather, so dJ/dD(old) = dJ/dTMP
-    for (int t = threadIdx.x; t < IM * d.KM; t += RT_BS) {
-        const int i = t % IM + 1, k = t / IM + 1;
-        A3(V.D, i, j, k) = A3(V.TM, i, j, k);
+    {
+        const int np = IM * d.KM;
+        for (int t0 = threadIdx.x; t0 < np; t0 += RT_U * RT_BS) {
+            float v[RT_U];
+            int o[RT_U];
+#pragma unroll
+            for (int u = 0; u < RT_U; ++u) {
+                const int t = t0 + u * RT_BS;
+                o[u] = -1;
+                if (t < np) {
+                    o[u] = ix3(d, t % IM + 1, j, t / IM + 1);
+                    v[u] = V.TM[o[u]];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < RT_U; ++u)
+                if (o[u] >= 0) V.D[o[u]] = v[u];
+        }
     }
     if (j < 2) return;
     const int jc = j;
@@ -1369,18 +1389,32 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_gather(const __grid_constant__ De
     const float DAMP = ctl->DAMP;
     const float blk = damp_on ? V.tBLK[A1(d.NROW, jc) - 1] : 1.0f;
     float pbf = 0.0f;             // FP32 per thread, FP64 across threads
-    for (int c = threadIdx.x; c < nc; c += RT_BS) {
-        const int i = c % IMM1 + 1, k = c / IMM1 + 1;
-        const float g = av[c];
-        float out = g;
-        if (damp_on) {
-            const float S = A3(V.tST, i, jc, k);
-            const float q = fabsf(S) / (blk * DAMP);
-            const float r = 1.0f / (1.0f + q);
-            out = g * r * r;
-            pbf += g * S * q / blk * r * r;
+    for (int c0 = threadIdx.x; c0 < nc; c0 += RT_U * RT_BS) {
+        float S[RT_U];
+        int o[RT_U];
+#pragma unroll
+        for (int u = 0; u < RT_U; ++u) {
+            const int c = c0 + u * RT_BS;
+            o[u] = -1;
+            S[u] = 0.0f;
+            if (c < nc) {
+                o[u] = ix3(d, c % IMM1 + 1, jc, c / IMM1 + 1);
+                if (damp_on) S[u] = V.tST[o[u]];
+            }
         }
-        A3(V.ST, i, jc, k) = out;
+#pragma unroll
+        for (int u = 0; u < RT_U; ++u) {
+            if (o[u] < 0) continue;
+            const float g = av[c0 + u * RT_BS];
+            float out = g;
+            if (damp_on) {
+                const float q = fabsf(S[u]) / (blk * DAMP);
+                const float r = 1.0f / (1.0f + q);
+                out = g * r * r;
+                pbf += g * S[u] * q / blk * r * r;
+            }
+            V.ST[o[u]] = out;
+        }
     }
     double pb = (double)pbf;
     for (int o = 16; o > 0; o >>= 1) pb += __shfl_down_sync(0xffffffffu, pb, o);
@@ -1440,15 +1474,31 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_damp(const __grid_constant__ Dev 
         }
     }
     float psf = 0.0f;             // FP32 per thread, FP64 across threads
-    for (int c = threadIdx.x; c < nc; c += RT_BS) {
-        const int i = c % IMM1 + 1, k = c / IMM1 + 1;
-        const int n = ix3(d, i, j, k);
-        float g = V.ST[n];
-        if (add != 0.0f) g += (V.tST[n] < 0.0f ? -add : add);
-        V.ST[n] = g;
-        const float y = g * d.RSTEP[n];
-        V.Y[n] = y;
-        psf += y;
+    for (int c0 = threadIdx.x; c0 < nc; c0 += RT_U * RT_BS) {
+        float g[RT_U], ts[RT_U], rsp[RT_U];
+        int o[RT_U];
+#pragma unroll
+        for (int u = 0; u < RT_U; ++u) {
+            const int c = c0 + u * RT_BS;
+            o[u] = -1;
+            if (c < nc) {
+                const int n = ix3(d, c % IMM1 + 1, j, c / IMM1 + 1);
+                o[u] = n;
+                g[u] = V.ST[n];
+                ts[u] = add != 0.0f ? V.tST[n] : 0.0f;
+                rsp[u] = d.RSTEP[n];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < RT_U; ++u) {
+            if (o[u] < 0) continue;
+            float gg = g[u];
+            if (add != 0.0f) gg += (ts[u] < 0.0f ? -add : add);
+            V.ST[o[u]] = gg;
+            const float y = gg * rsp[u];
+            V.Y[o[u]] = y;
+            psf += y;
+        }
     }
     double ps = (double)psf;
     for (int o = 16; o > 0; o >>= 1) ps += __shfl_down_sync(0xffffffffu, ps, o);
@@ -1540,14 +1590,13 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_cells(const __grid_constant__ Dev
     const float F1 = d.F1, F2 = d.F2, F3 = d.F3;
     for (int k = threadIdx.x; k < KMM1; k += RT_BS) rs[k] = 0.0f;
     __syncthreads();
-    for (int c = threadIdx.x; c < nc; c += RT_BS) {
-        const int i = c % IMM1 + 1, k = c / IMM1 + 1;
-        const int n = ix3(d, i, j, k);
-        const float gdiff = V.DIFF[n];
+    // the cell body; gdiff is the cell's DIFF adjoint, loaded with those of
+    // the other cells of its group
+    auto cell = [&](int c, int i, int k, int n, float gdiff) {
         const float gst = st[c];
         const float gdelta = F1 * gst + gdiff;
         V.DIFF[n] = F2 * gst + F3 * gdiff;
-        if (gdelta == 0.0f) continue;
+        if (gdelta == 0.0f) return;
         aadd(&V.XF[n], gdelta);
         aadd(&A3(V.XF, i, j - 1, k), -RATPITCH * gdelta);
         aadd(&V.RF[n], gdelta);
@@ -1584,6 +1633,24 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_cells(const __grid_constant__ Dev
             }
         }
         if (plain) aadd(&V.SR[n], gsrc);
+    };
+    for (int c0 = threadIdx.x; c0 < nc; c0 += RT_U * RT_BS) {
+        float gd[RT_U];
+        int o[RT_U];
+#pragma unroll
+        for (int u = 0; u < RT_U; ++u) {
+            const int c = c0 + u * RT_BS;
+            o[u] = -1;
+            if (c < nc) {
+                o[u] = ix3(d, c % IMM1 + 1, j, c / IMM1 + 1);
+                gd[u] = V.DIFF[o[u]];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < RT_U; ++u) {
+            const int c = c0 + u * RT_BS;
+            if (o[u] >= 0) cell(c, c % IMM1 + 1, c / IMM1 + 1, o[u], gd[u]);
+        }
     }
     __syncthreads();
     if (role == 1 || role == 3) {

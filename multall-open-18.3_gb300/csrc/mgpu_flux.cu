@@ -855,13 +855,13 @@ __global__ void k_mach_limiter(Dev d) {
     int nr = A1(d.NROW, j);
     float V_LIMIT = A1(d.VLIMIT, nr), RO_LIMIT = A1(d.ROLIMIT, nr);
     float ro = d.RO[n];
+    const float vx = d.VX[n], vr = d.VR[n], wt = d.WT[n];   // loaded before any store
     if (d.ADJ_RO_MACH) d.ADJ_RO_MACH[n] = ro;
     if (ro < RO_LIMIT) {
         ro = RO_LIMIT;
         d.RO[n] = ro;
         if (d.ADJ_FLAG) atomicOr(d.ADJ_FLAG, 2);
     }
-    float vx = d.VX[n], vr = d.VR[n], wt = d.WT[n];
     float WRELSQ = vx * vx + vr * vr + wt * wt;
     float WREL = sqrtf(WRELSQ);
     float FACSAFE = V_LIMIT / WREL;
