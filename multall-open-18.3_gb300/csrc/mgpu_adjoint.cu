@@ -84,6 +84,14 @@ namespace {
 
 inline unsigned gridn(size_t n, unsigned b) { return (unsigned)((n + b - 1) / b); }
 
+// threads of the J-plane reverse kernels
+constexpr int RT_BS = 256;
+// Cells (or nodes) per thread whose loads the J-plane reverse kernels issue
+// together before the group's stores: a store keeps every later load of the
+// thread behind it, so a one-at-a-time loop costs a memory round trip per
+// cell.
+constexpr int RT_U = 4;
+
 __device__ __forceinline__ void aadd(float *p, float v) {
     if (v != 0.0f) atomicAdd(p, v);
 }
@@ -295,35 +303,67 @@ __global__ void rk_flux_mass_gather(const Dev d, const Adj a) {
 // R3: exit pitchwise sums and the radial-equilibrium recurrence (k_bc_sums)
 // IPOUT = 0: PD(1) = PDOWN_HUB, PD(K) = 0.9 PD(K) + 0.1 (PD(K-1) + DP(K))
 // =====================================================================
-__global__ void __launch_bounds__(256) rk_bc_sums(const Dev d, const Adj a) {
-    __shared__ float gss[512];
+// One CTA of RBC_BS threads.  The recurrence runs on one thread over
+// shared copies of PD's adjoint and R(JM, K), which all threads load first;
+// the pitchwise part issues the loads of its RT_U points before their
+// read-modify-writes.
+constexpr int RBC_BS = 1024;
+__global__ void __launch_bounds__(RBC_BS) rk_bc_sums(const Dev d, const Adj a) {
+    __shared__ float gss[512], sr[512], gpd[512];
     const int KM = d.KM, IM = d.IM, IMM1 = d.IMM1;
-    for (int k = threadIdx.x; k < KM; k += blockDim.x) gss[k] = 0.0f;
+    for (int k = threadIdx.x; k < KM; k += blockDim.x) {
+        gss[k] = 0.0f;
+        sr[k] = A2(d.R, d.JM, k + 1);
+        gpd[k] = a.PD[k] + a.PDK[k];
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-        float gpd[512];
-        for (int k = 0; k < KM; ++k) gpd[k] = a.PD[k] + a.PDK[k];
         for (int k = KM - 1; k >= 1; --k) {
             const float g = gpd[k];
             gpd[k - 1] += 0.1f * g;
-            a.PD[k] = 0.9f * g;
+            gpd[k] = 0.9f * g;
             const float gdp = 0.1f * g;
-            const float half = 0.5f * (A2(d.R, d.JM, k + 1) - A2(d.R, d.JM, k));
+            const float half = 0.5f * (sr[k] - sr[k - 1]);
             gss[k] += gdp * half;
             gss[k - 1] += gdp * half;
         }
-        a.PD[0] = 0.0f;
-        for (int k = 0; k < KM; ++k) a.PDK[k] = 0.0f;
+        gpd[0] = 0.0f;
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < IM * KM; t += blockDim.x) {
-        const int i = t % IM + 1, k = t / IM + 1;
-        const float w = 0.5f * ((i <= IMM1 ? A1(d.FP, i) : 0.0f) + (i >= 2 ? A1(d.FP, i - 1) : 0.0f));
-        const float gp = a.PAVG[k - 1];
-        A3(a.P, i, d.JMM1, k) += gp * w;
-        const float gs = gss[k - 1] * w / A2(d.R, d.JM, k);
-        A3(a.ROVT, i, d.JM, k) += gs * A3(a.tVT, i, d.JM, k);
-        A3(a.VT, i, d.JM, k) += gs * A3(a.tROVT, i, d.JM, k);
+    for (int k = threadIdx.x; k < KM; k += blockDim.x) {
+        a.PD[k] = gpd[k];
+        a.PDK[k] = 0.0f;
+    }
+    const int np = IM * KM;
+    for (int t0 = threadIdx.x; t0 < np; t0 += RT_U * RBC_BS) {
+        float gP[RT_U], gR[RT_U], gV[RT_U], tvt[RT_U], trv[RT_U], w[RT_U], gpv[RT_U], rr[RT_U];
+        int kk[RT_U];
+#pragma unroll
+        for (int u = 0; u < RT_U; ++u) {
+            const int t = t0 + u * RBC_BS;
+            kk[u] = -1;
+            if (t < np) {
+                const int i = t % IM + 1, k = t / IM + 1;
+                kk[u] = k;
+                w[u] = 0.5f * ((i <= IMM1 ? A1(d.FP, i) : 0.0f) + (i >= 2 ? A1(d.FP, i - 1) : 0.0f));
+                gpv[u] = a.PAVG[k - 1];
+                rr[u] = A2(d.R, d.JM, k);
+                gP[u] = A3(a.P, i, d.JMM1, k);
+                gR[u] = A3(a.ROVT, i, d.JM, k);
+                gV[u] = A3(a.VT, i, d.JM, k);
+                tvt[u] = A3(a.tVT, i, d.JM, k);
+                trv[u] = A3(a.tROVT, i, d.JM, k);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < RT_U; ++u) {
+            if (kk[u] < 0) continue;
+            const int t = t0 + u * RBC_BS, i = t % IM + 1, k = kk[u];
+            A3(a.P, i, d.JMM1, k) = gP[u] + gpv[u] * w[u];
+            const float gs = gss[k - 1] * w[u] / rr[u];
+            A3(a.ROVT, i, d.JM, k) = gR[u] + gs * tvt[u];
+            A3(a.VT, i, d.JM, k) = gV[u] + gs * trv[u];
+        }
     }
     __syncthreads();
     for (int k = threadIdx.x; k < KM; k += blockDim.x) a.PAVG[k] = 0.0f;
@@ -435,6 +475,11 @@ __global__ void rk_bc_apply(const Dev d, const Adj a) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= d.IM * d.KM) return;
     const int i = t % d.IM + 1, k = t / d.IM + 1;
+    // the exit's operands are loaded first: the inlet's stores below (other
+    // addresses) would otherwise keep these loads behind them
+    const int ne = ix3(d, i, d.JM, k);
+    const float evr = a.tVR[ne], evt = a.tVT[ne], evx = a.tVX[ne], epe = a.tP[ne], ehoe = a.tHO[ne];
+    const float eP = a.P[ne], eHO = a.HO[ne], eRO = a.v[V_RO].D[ne], eROE = a.v[V_ROE].D[ne];
     // ---- inlet ----
     {
         const float PO1 = A1(d.PO1, k), TO1 = A1(d.TO1, k);
@@ -496,13 +541,12 @@ __global__ void rk_bc_apply(const Dev d, const Adj a) {
     }
     // ---- exit ----
     {
-        const int ne = ix3(d, i, d.JM, k);
-        const float vr = a.tVR[ne], vt = a.tVT[ne], vx = a.tVX[ne];
+        const float vr = evr, vt = evt, vx = evx;
         const float EKE = 0.5f * (vr * vr + vt * vt + vx * vx);
-        const float pe = a.tP[ne], hoe = a.tHO[ne];
+        const float pe = epe, hoe = ehoe;
         const float TEXIT = (hoe - EKE) / d.CP;
         const float roe_ = pe / d.RGAS / TEXIT;
-        const float gP = a.P[ne], gHO = a.HO[ne], gRO = a.v[V_RO].D[ne], gROE = a.v[V_ROE].D[ne];
+        const float gP = eP, gHO = eHO, gRO = eRO, gROE = eROE;
         const float groe = gROE * (d.CV * TEXIT + EKE) + gRO;
         float gTEXIT = gROE * roe_ * d.CV - groe * roe_ / TEXIT;
         float gEKE = gROE * roe_ - gTEXIT / d.CP;
@@ -1071,12 +1115,6 @@ __global__ void rk_mach(const Dev d, const Adj a) {
 // restriction partials) -> rk_ts_cells (prolongation, mixing-plane
 // redistribution, SCREE, flux sum)
 // =====================================================================
-constexpr int RT_BS = 256;
-// Cells (or nodes) per thread whose loads the J-plane reverse kernels issue
-// together before the group's stores: a store keeps every later load of the
-// thread behind it, so a one-at-a-time loop costs a memory round trip per
-// cell.
-constexpr int RT_U = 4;
 
 __device__ inline int mp_role_r(const Dev &d, int j, int *nr) {
     for (int r = 1; r <= d.NRWSM1; ++r) {
@@ -1439,12 +1477,20 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_damp(const __grid_constant__ Dev 
     float add = 0.0f;
     if (ctl->damp_on) {
         // dJ/dblk per row, then through the row mixing to dJ/dchg
-        if (threadIdx.x < NROWS) {
-            double s = 0.0;
-            for (int jj = 2; jj <= d.JM; ++jj)
-                if (A1(d.NROW, jj) == (int)threadIdx.x + 1) s += V.pblk[jj - 1];
-            gblk[threadIdx.x] = (float)s;
-            gchg[threadIdx.x] = 0.0f;
+        // one warp per row, its lanes over the J planes (a serial walk over
+        // all planes by one thread per row was a chain of dependent loads)
+        {
+            const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+            for (int nr = w + 1; nr <= NROWS; nr += RT_BS / 32) {
+                double s = 0.0;
+                for (int jj = 2 + l; jj <= d.JM; jj += 32)
+                    if (A1(d.NROW, jj) == nr) s += V.pblk[jj - 1];
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+                if (l == 0) {
+                    gblk[nr - 1] = (float)s;
+                    gchg[nr - 1] = 0.0f;
+                }
+            }
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -1983,7 +2029,7 @@ void enqueue_reverse(const Dev &d, const Adj &a, cudaStream_t s) {
     launch_tstep_rev(d, a, s, V_RO, 2);
     rk_flux_energy_coef<<<gN, 256, 0, s>>>(d, a);
     rk_flux_energy_gather<<<gN, 256, 0, s>>>(d, a);
-    rk_bc_sums<<<1, 256, 0, s>>>(d, a);
+    rk_bc_sums<<<1, RBC_BS, 0, s>>>(d, a);
     rk_flux_mass_coef<<<gN, 256, 0, s>>>(d, a);
     rk_flux_mass_gather<<<gN, 256, 0, s>>>(d, a);
     rk_prim<<<gN, 256, 0, s>>>(d, a);

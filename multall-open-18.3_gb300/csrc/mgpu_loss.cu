@@ -975,8 +975,9 @@ __global__ void k_stepup_store(Dev d, int gated) {
     int i, j, k;
     node_ijk(d, n, i, j, k);
     if (i >= d.IM || j < 2 || k >= d.KM) return;
-    d.STEP[n] = d.TMP[n];
-    d.RSTEP[n] = d.STORE[n];
+    const float step = d.TMP[n], rstep = d.STORE[n];   // both loads before the stores
+    d.STEP[n] = step;
+    d.RSTEP[n] = rstep;
 }
 
 void launch_stepup(const Dev &d, Launch L, float relax, bool gated) {

@@ -21,6 +21,8 @@ from __future__ import annotations
 
 import copy
 import dataclasses
+import os
+from concurrent.futures import ThreadPoolExecutor
 from typing import Callable, Dict, List
 
 import numpy as np
@@ -74,16 +76,23 @@ class DesignSpace:
     def geometry64(self, alpha: np.ndarray) -> Dict[str, np.ndarray]:
         return _cs.build_common(self.spec(alpha), metrics64=True, metrics_only=True).geom64
 
-    def sensitivities(self, alpha: np.ndarray, h: float = 1e-3) -> List[Dict[str, np.ndarray]]:
+    def sensitivities(self, alpha: np.ndarray, h: float = 1e-3, threads: int | None = None) -> List[Dict[str, np.ndarray]]:
         """dA/d(alpha_i) per design variable (per degree), central differences
-        of the double-precision metrics."""
-        out = []
-        for i in range(self.size):
+        of the double-precision metrics.  The 2 x size geometry evaluations
+        are independent and spend their time in NumPy array operations, which
+        release the GIL, so they run on a thread pool."""
+        def one(i):
             e = np.zeros(self.size)
             e[i] = h
             gp, gm = self.geometry64(alpha + e), self.geometry64(alpha - e)
-            out.append({n: (gp[n] - gm[n]) / (2.0 * h) for n in GEOM})
-        return out
+            return {n: (gp[n] - gm[n]) / (2.0 * h) for n in GEOM}
+        first = one(0)
+        big = first["VOLOR"].size > 100_000      # small grids: the pool costs more than it saves
+        nt = threads if threads is not None else (min(16, os.cpu_count() or 1) if big else 1)
+        if nt <= 1:
+            return [first] + [one(i) for i in range(1, self.size)]
+        with ThreadPoolExecutor(nt) as ex:
+            return [first] + list(ex.map(one, range(1, self.size)))
 
     @staticmethod
     def chain(dJdA: Dict[str, np.ndarray], sens: List[Dict[str, np.ndarray]]) -> np.ndarray:
