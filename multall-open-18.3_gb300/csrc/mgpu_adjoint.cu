@@ -1160,7 +1160,7 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_smooth(const __grid_constant__ De
     const AdjVar &V = a.v[v0 + blockIdx.y];
     const int IM = d.IM, KM = d.KM, IMM1 = d.IMM1, KMM1 = d.KMM1;
     const int np = IM * KM;
-    float *A_ = sm, *B_ = sm + np;
+    float *A_ = sm, *B_ = sm + np, *C_ = sm + 2 * np;
     const int j = blockIdx.x + 1;
     const DevCtl *c = a.tctl;
     const size_t ks = (size_t)IM * d.JM;
@@ -1232,87 +1232,85 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_smooth(const __grid_constant__ De
             P(A_, ci, nk) += SFTH * cv;
         }
         __syncthreads();
-        // spanwise pass: A_ = f(B_) -> B_bar
-        for (int t = threadIdx.x; t < np; t += RT_BS) B_[t] = 0.0f;
-        __syncthreads();
+        // The spanwise pass (b -> a, per I column) and the pitchwise pass
+        // (a -> b, per K line) reversed in gather form: each point sums the
+        // terms of the outputs that read it, so no shared-memory atomics.
+        // Curvatures first: c(m) = x(m) - FD(m) x(m+1) - FU(m) x(m-1) for an
+        // interior m, read by the smoothed values at m-1 and m+1.
+        const float h = SFT * F4;
+        // spanwise: A_ = adjoint of its output; B_ = curvature adjoints
         for (int t = threadIdx.x; t < np; t += RT_BS) {
             const int i = t % IM + 1, k = t / IM + 1;
-            const float g = A_[t];
-            if (g == 0.0f) continue;
-            float *bi = B_ + (i - 1);     // bi[IM*(kk-1)] = P(B_, i, kk)
-            auto add = [&](int kk, float v) { atomicAdd(&bi[IM * (kk - 1)], v); };
-            add(k, SFT1 * g);
-            if (k == 1) {
-                add(2, SFT * g * (1.0f + 0.5f * A1(d.FKU, 1)));
-                add(3, -SFT * g * 0.5f * A1(d.FKU, 1));
-            } else if (k == KM) {
-                add(KMM1, SFT * g * (1.0f + 0.5f * A1(d.FKU, KM)));
-                add(d.KMM2, -SFT * g * 0.5f * A1(d.FKU, KM));
-            } else {
-                const float fkd = A1(d.FKD, k), fku = A1(d.FKU, k);
-                add(k + 1, SFT * g * fkd);
-                add(k - 1, SFT * g * fku);
-                // SC = FKU(k) curve(k-1) + FKD(k) curve(k+1), curve(kk) = b(kk) - FKD(kk) b(kk+1) - FKU(kk) b(kk-1)
-                const float h = SFT * F4 * g;
-                if (k - 1 != 1 && k - 1 != KM) {
-                    const int kk = k - 1;
-                    add(kk, h * fku);
-                    add(kk + 1, -h * fku * A1(d.FKD, kk));
-                    add(kk - 1, -h * fku * A1(d.FKU, kk));
-                }
-                if (k + 1 != 1 && k + 1 != KM) {
-                    const int kk = k + 1;
-                    add(kk, h * fkd);
-                    add(kk + 1, -h * fkd * A1(d.FKD, kk));
-                    add(kk - 1, -h * fkd * A1(d.FKU, kk));
-                }
+            float cb = 0.0f;
+            if (k >= 2 && k <= KMM1) {
+                if (k + 1 <= KMM1) cb += A1(d.FKU, k + 1) * P(A_, i, k + 1);
+                if (k - 1 >= 2) cb += A1(d.FKD, k - 1) * P(A_, i, k - 1);
             }
+            B_[t] = h * cb;
         }
         __syncthreads();
-        // pitchwise pass: B_ = f(A_) -> A_bar
-        for (int t = threadIdx.x; t < np; t += RT_BS) A_[t] = 0.0f;
+        // C_ = adjoint of the pitchwise output
+        for (int t = threadIdx.x; t < np; t += RT_BS) {
+            const int i = t % IM + 1, k = t / IM + 1;
+            float g = SFT1 * P(A_, i, k);
+            if (k - 1 >= 2 && k - 1 <= KMM1) g += SFT * A1(d.FKD, k - 1) * P(A_, i, k - 1);
+            if (k + 1 >= 2 && k + 1 <= KMM1) g += SFT * A1(d.FKU, k + 1) * P(A_, i, k + 1);
+            if (k == 2) g += SFT * P(A_, i, 1) * (1.0f + 0.5f * A1(d.FKU, 1));
+            if (k == 3) g -= SFT * P(A_, i, 1) * 0.5f * A1(d.FKU, 1);
+            if (k == KMM1) g += SFT * P(A_, i, KM) * (1.0f + 0.5f * A1(d.FKU, KM));
+            if (k == d.KMM2) g -= SFT * P(A_, i, KM) * 0.5f * A1(d.FKU, KM);
+            if (k >= 2 && k <= KMM1) g += P(B_, i, k);
+            if (k - 1 >= 2 && k - 1 <= KMM1) g -= A1(d.FKD, k - 1) * P(B_, i, k - 1);
+            if (k + 1 >= 2 && k + 1 <= KMM1) g -= A1(d.FKU, k + 1) * P(B_, i, k + 1);
+            C_[t] = g;
+        }
+        __syncthreads();
+        // pitchwise: C_ = adjoint of its output; B_ = curvature adjoints, the
+        // end curvature c(1) = c(IM) = a(1) - (a(2) + a(IMM1))/2 of a periodic
+        // plane at I = 1 and IM
+        for (int t = threadIdx.x; t < np; t += RT_BS) {
+            const int i = t % IM + 1, k = t / IM + 1;
+            float cb = 0.0f;
+            if (i >= 2 && i <= IMM1) {
+                if (i + 1 <= IMM1) cb += A1(d.FU, i + 1) * P(C_, i + 1, k);
+                if (i - 1 >= 2) cb += A1(d.FD, i - 1) * P(C_, i - 1, k);
+            } else if (periodic_j) {
+                if (i == 1 && IMM1 >= 2) cb += A1(d.FU, 2) * P(C_, 2, k);
+                if (i == IM && IMM1 >= 2) cb += A1(d.FD, IMM1) * P(C_, IMM1, k);
+            }
+            if (periodic_j) {
+                const float e = 0.5f * (P(C_, 1, k) + P(C_, IM, k));
+                if (i == 2) cb += e;
+                if (i == IMM1) cb += e;
+            }
+            B_[t] = h * cb;
+        }
         __syncthreads();
         for (int t = threadIdx.x; t < np; t += RT_BS) {
             const int i = t % IM + 1, k = t / IM + 1;
-            const float g = B_[t];
-            if (g == 0.0f) continue;
-            float *ak = A_ + IM * (k - 1) - 1;     // ak[ii] = P(A_, ii, k)
-            auto add = [&](int ii, float v) { atomicAdd(&ak[ii], v); };
-            // curve(ii) with weight w
-            auto curve = [&](int ii, float w) {
-                if (ii == 1 || ii == IM) {
-                    if (!periodic_j) return;
-                    add(1, w);
-                    add(2, -0.5f * w);
-                    add(IMM1, -0.5f * w);
-                    return;
-                }
-                add(ii, w);
-                add(ii + 1, -w * A1(d.FD, ii));
-                add(ii - 1, -w * A1(d.FU, ii));
-            };
-            add(i, SFT1 * g);
-            const float h = SFT * g;
-            if (i == 1 || i == IM) {
-                if (periodic_j) {
-                    add(2, 0.5f * h);
-                    add(IMM1, 0.5f * h);
-                    curve(2, 0.5f * F4 * h);
-                    curve(IMM1, 0.5f * F4 * h);
-                } else if (i == 1) {
-                    add(2, h * (1.0f + A1(d.FU, 1)));
-                    add(3, -h * A1(d.FU, 1));
-                } else {
-                    add(IMM1, h * (1.0f + A1(d.FU, IM)));
-                    add(d.IMM2, -h * A1(d.FU, IM));
-                }
+            float g = SFT1 * P(C_, i, k);
+            if (i - 1 >= 2 && i - 1 <= IMM1) g += SFT * A1(d.FD, i - 1) * P(C_, i - 1, k);
+            if (i + 1 >= 2 && i + 1 <= IMM1) g += SFT * A1(d.FU, i + 1) * P(C_, i + 1, k);
+            if (periodic_j) {
+                const float e = 0.5f * SFT * (P(C_, 1, k) + P(C_, IM, k));
+                if (i == 2) g += e;
+                if (i == IMM1) g += e;
             } else {
-                const float fd = A1(d.FD, i), fu = A1(d.FU, i);
-                add(i + 1, h * fd);
-                add(i - 1, h * fu);
-                curve(i - 1, F4 * h * fu);
-                curve(i + 1, F4 * h * fd);
+                if (i == 2) g += SFT * P(C_, 1, k) * (1.0f + A1(d.FU, 1));
+                if (i == 3) g -= SFT * P(C_, 1, k) * A1(d.FU, 1);
+                if (i == IMM1) g += SFT * P(C_, IM, k) * (1.0f + A1(d.FU, IM));
+                if (i == d.IMM2) g -= SFT * P(C_, IM, k) * A1(d.FU, IM);
             }
+            if (i >= 2 && i <= IMM1) g += P(B_, i, k);
+            if (i - 1 >= 2 && i - 1 <= IMM1) g -= A1(d.FD, i - 1) * P(B_, i - 1, k);
+            if (i + 1 >= 2 && i + 1 <= IMM1) g -= A1(d.FU, i + 1) * P(B_, i + 1, k);
+            if (periodic_j) {
+                const float e = P(B_, 1, k) + P(B_, IM, k);
+                if (i == 1) g += e;
+                if (i == 2) g -= 0.5f * e;
+                if (i == IMM1) g -= 0.5f * e;
+            }
+            A_[t] = g;
         }
         __syncthreads();
     }
@@ -1982,7 +1980,7 @@ int aalloc(AdjState *s, T **p, size_t count) {
     return 0;
 }
 
-size_t smooth_bytes(const Dev &d) { return (size_t)2 * d.IM * d.KM * sizeof(float); }
+size_t smooth_bytes(const Dev &d) { return (size_t)3 * d.IM * d.KM * sizeof(float); }
 size_t gather_bytes(const Dev &d) { return (size_t)d.IMM1 * d.KMM1 * sizeof(float); }
 size_t cells_bytes(const Dev &d) {
     return ((size_t)d.NIB1 * d.NKB1 + (size_t)d.NIB2 * d.NKB2 + (size_t)d.IMM1 * d.KMM1 + d.KMM1) * sizeof(float);
