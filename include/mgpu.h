@@ -156,6 +156,25 @@ int32_t mgpu_sync(mgpu_handle *h);
  * on the device with FP64 accumulation. */
 int32_t mgpu_integrals_compute(mgpu_handle *h, mgpu_integrals *out);
 
+/* ---- restart / plotting file ------------------------------------------- */
+/* Writes the combined restart/plotting file "flow_out" from the device
+ * state, as OUTPUT writes it (multall-open-18.3.f:5942-5978): the records
+ * NSTEP, RO, ROVX, ROVR, ROVT, ROE, ROSUB, DPDS_CELL*1.0E-6 and PEFF+PREFF
+ * (PREFF = (P(IMID,1,KMID) + P(IMID,JM,KMID))/2 of the current pressures)
+ * in gfortran's sequential unformatted layout (each record between two
+ * 4-byte byte counts).  rosub: the caller's packed ROSUB, which LOOP does
+ * not change for ITIMST = 3, or NULL to write RO in its place.  Valid after
+ * mgpu_commit. */
+int32_t mgpu_write_flow_out(mgpu_handle *h, const char *path, const float *rosub);
+/* Reads a flow_out file as SETUP's IF_RESTART branch does
+ * (multall-open-18.3.f:6920-6992): sets RO, ROVX, ROVR, ROVT and ROE from it
+ * and forms RORVT, VX, VR, VT, T_STATIC, HO, P, PEFF = P and, for IPOUT 0 or
+ * -1, the exit pressures PD.  Valid after the COMMON arrays are bound and
+ * before mgpu_commit, whose LOOP prologue (PREFF, ROLIM, PLIM) then starts
+ * from the restarted flow.  *nstep (may be NULL) receives the file's NSTEP;
+ * like LOOP, the step counter itself starts again from the bound NSTEP. */
+int32_t mgpu_read_flow_out(mgpu_handle *h, const char *path, int32_t *nstep);
+
 /* The same integrals as mgpu_integrals_compute, through a path that
  * allocates nothing.  This entry point has no counterpart in the reference
  * (whose efficiency summary is plain Fortran over COMMON arrays).

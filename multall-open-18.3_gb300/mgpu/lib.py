@@ -45,7 +45,8 @@ EXPORTS = ["mgpu_abi_version", "mgpu_last_error", "mgpu_device_count", "mgpu_cre
            "mgpu_step_io_bytes", "mgpu_integrals_noalloc", "mgpu_batch_create", "mgpu_batch_destroy",
            "mgpu_batch_run", "mgpu_batch_bench_steps", "mgpu_adjoint_prepare", "mgpu_adjoint_objective",
            "mgpu_adjoint_iterate", "mgpu_adjoint_solve", "mgpu_adjoint_gradient", "mgpu_adjoint_get",
-           "mgpu_adjoint_set", "mgpu_adjoint_solve_krylov", "mgpu_autotune"]
+           "mgpu_adjoint_set", "mgpu_adjoint_solve_krylov", "mgpu_autotune", "mgpu_write_flow_out",
+           "mgpu_read_flow_out"]
 
 _lib = None
 
@@ -95,6 +96,8 @@ def load(build: bool = True):
     L.mgpu_adjoint_solve.argtypes = [vp, i32, ctypes.c_double, ctypes.POINTER(i32), dp]
     L.mgpu_adjoint_gradient.argtypes = [vp]
     L.mgpu_autotune.argtypes = [vp, ctypes.POINTER(i32), dp]
+    L.mgpu_write_flow_out.argtypes = [vp, cp, vp]
+    L.mgpu_read_flow_out.argtypes = [vp, cp, ctypes.POINTER(i32)]
     L.mgpu_adjoint_solve_krylov.argtypes = [vp, i32, i32, i32, ctypes.c_double, ctypes.POINTER(i32), dp]
     L.mgpu_adjoint_get.argtypes = [vp, cp, vp, ctypes.c_int64]
     L.mgpu_adjoint_set.argtypes = [vp, cp, vp, ctypes.c_int64]
@@ -136,7 +139,9 @@ def _chk(rc: int) -> int:
 class Problem:
     """One flow problem resident on the current GPU."""
 
-    def __init__(self, cd, setup_calls: bool = True):
+    def __init__(self, cd, setup_calls: bool = True, restart: str | None = None):
+        """restart: a flow_out file read after the COMMON data are bound and
+        before the commit, as SETUP reads it with IF_RESTART = 1."""
         L = load()
         n = L.mgpu_device_count()
         if n <= 0:
@@ -152,9 +157,20 @@ class Problem:
         for k, a in cd.arrays.items():
             a = np.ascontiguousarray(a)
             _chk(L.mgpu_set_array(self.h, k.encode(), a.ctypes.data, a.nbytes))
+        self.restart_nstep = None
+        if restart is not None:
+            ns = ctypes.c_int32()
+            _chk(L.mgpu_read_flow_out(self.h, os.fsencode(restart), ctypes.byref(ns)))
+            self.restart_nstep = ns.value
         _chk(L.mgpu_commit(self.h))
         if setup_calls:
             self.setup_calls()
+
+    def write_flow_out(self, path: str, rosub: np.ndarray | None = None):
+        """The restart/plotting file flow_out of the current state."""
+        if rosub is not None:
+            rosub = np.ascontiguousarray(rosub, np.float32)
+        _chk(load().mgpu_write_flow_out(self.h, os.fsencode(path), None if rosub is None else rosub.ctypes.data))
 
     def setup_calls(self):
         """STEPUP(1.0) and the first LOSS, as SETUP makes them."""

@@ -93,7 +93,23 @@ struct OracleBase {
     virtual int ad_reverse() { return fail(MGPU_E_STATE, "not a differentiating oracle"); }
     virtual int ad_grad(const char *, double *, int64_t) { return fail(MGPU_E_STATE, "not a differentiating oracle"); }
     virtual int64_t ad_tape_size() { return 0; }
+    /* the restart/plotting file flow_out (OUTPUT 5942-5978; SETUP's
+       IF_RESTART branch 6920-6992) */
+    virtual int write_flow_out(const char *, const float *) { return fail(MGPU_E_STATE, "flow_out needs a REAL oracle"); }
+    virtual int read_flow_out(const char *, int *) { return fail(MGPU_E_STATE, "flow_out needs a REAL oracle"); }
 };
+
+/* gfortran's sequential unformatted records: the payload between two copies
+   of its byte count (4-byte integers) */
+bool fo_put(FILE *f, const void *p, uint32_t n) {
+    return fwrite(&n, 4, 1, f) == 1 && (n == 0 || fwrite(p, 1, n, f) == n) && fwrite(&n, 4, 1, f) == 1;
+}
+bool fo_get(FILE *f, void *p, uint32_t n) {
+    uint32_t a = 0, b = 0;
+    if (fread(&a, 4, 1, f) != 1 || a != n) return false;
+    if (p ? fread(p, 1, n, f) != n : fseek(f, (long)n, SEEK_CUR) != 0) return false;
+    return fread(&b, 4, 1, f) == 1 && b == n;
+}
 
 template <typename R>
 struct Oracle : OracleBase {
@@ -240,6 +256,87 @@ struct Oracle : OracleBase {
         if (!strcmp(n, "STORE")) return take(STORE, SH_IJK, p, nb, as_double, n, false);
         if (!strcmp(n, "FLOWX")) return take(FLOWX, SH_IJK, p, nb, as_double, n, false);
         return fail(MGPU_E_ARG, std::string("unknown array ") + n);
+    }
+
+    /* ---- flow_out: REAL*4 records for float, REAL*8 for double (the
+       -fdefault-real-8 build) ------------------------------------------ */
+    static constexpr bool kPlainReal = std::is_same<R, float>::value || std::is_same<R, double>::value;
+    int write_flow_out(const char *path, const float *rosub) override {
+        if constexpr (!kPlainReal) {
+            return fail(MGPU_E_STATE, "flow_out needs a REAL oracle");
+        } else {
+            if (!committed) return fail(MGPU_E_STATE, "write_flow_out before commit");
+            const size_t N = (size_t)IM * JM * KM;
+            /* OUTPUT's own PREFF (5950) */
+            const R PRF = R(0.5) * (F3(P, IMID, 1, KMID) + F3(P, IMID, JM, KMID));
+            const R E6 = std::is_same<R, float>::value ? R(1.0e-6f) : R(1.0e-6);
+            std::vector<R> dp(N), pe(N), rs(N);
+            for (size_t n = 0; n < N; ++n) {
+                dp[n] = DPDS_CELL_v[n] * E6;
+                pe[n] = PEFF_v[n] + PRF;
+                rs[n] = rosub ? R(rosub[n]) : RO_v[n];
+            }
+            FILE *f = fopen(path, "wb");
+            if (!f) return fail(MGPU_E_ARG, std::string("cannot open for writing: ") + path);
+            const uint32_t rb = (uint32_t)(N * sizeof(R));
+            int32_t ns = NSTEP;
+            bool ok = fo_put(f, &ns, 4);
+            const std::vector<R> *recs[] = {&RO_v, &ROVX_v, &ROVR_v, &ROVT_v, &ROE_v, &rs, &dp, &pe};
+            for (auto *r : recs) ok = ok && fo_put(f, r->data(), rb);
+            ok = fclose(f) == 0 && ok;
+            return ok ? 0 : fail(MGPU_E_ARG, std::string("write failed: ") + path);
+        }
+    }
+    int read_flow_out(const char *path, int *nstep) override {
+        if constexpr (!kPlainReal) {
+            return fail(MGPU_E_STATE, "flow_out needs a REAL oracle");
+        } else {
+            if (committed) return fail(MGPU_E_STATE, "read_flow_out after commit (SETUP reads the restart file)");
+            const size_t N = (size_t)IM * JM * KM;
+            const uint32_t rb = (uint32_t)(N * sizeof(R));
+            std::vector<R> ro(N), rovx(N), rovr(N), rovt(N), roe(N);
+            int32_t ns = 0;
+            FILE *f = fopen(path, "rb");
+            if (!f) return fail(MGPU_E_ARG, std::string("cannot open: ") + path);
+            const bool ok = fo_get(f, &ns, 4) && fo_get(f, ro.data(), rb) && fo_get(f, rovx.data(), rb) &&
+                            fo_get(f, rovr.data(), rb) && fo_get(f, rovt.data(), rb) && fo_get(f, roe.data(), rb) &&
+                            fo_get(f, nullptr, rb) && fo_get(f, nullptr, rb);
+            fclose(f);
+            if (!ok) return fail(MGPU_E_ARG, std::string("not a flow_out file of this grid: ") + path);
+            if (!R_v.size() || !FP_v.size() || !PD_v.size()) return fail(MGPU_E_ARG, "bind R, FP and PD before the restart");
+            const R CVr = CP / GA, RGASr = CP - CVr;   /* SETUP 6459-6468 */
+            RO_v = ro; ROVX_v = rovx; ROVR_v = rovr; ROVT_v = rovt; ROE_v = roe;
+            for (std::vector<R> *v : {&VX_v, &VR_v, &VT_v, &RORVT_v, &T_STATIC_v, &HO_v, &P_v, &PEFF_v}) v->assign(N, R(0));
+            /* 3900, IFGAS = 0, ITIMST < 5 */
+            for (int k = 1; k <= KM; ++k)
+                for (int j = 1; j <= JM; ++j)
+                    for (int i = 1; i <= IM; ++i) {
+                        F3(VX, i, j, k) = F3(ROVX, i, j, k) / F3(RO, i, j, k);
+                        F3(VR, i, j, k) = F3(ROVR, i, j, k) / F3(RO, i, j, k);
+                        F3(VT, i, j, k) = F3(ROVT, i, j, k) / F3(RO, i, j, k);
+                        F3(RORVT, i, j, k) = F3(ROVT, i, j, k) * F2(R, j, k);
+                        const R EKE = R(0.5) * (F3(VX, i, j, k) * F3(VX, i, j, k) + F3(VR, i, j, k) * F3(VR, i, j, k) +
+                                                F3(VT, i, j, k) * F3(VT, i, j, k));
+                        const R TSTATIC = (F3(ROE, i, j, k) / F3(RO, i, j, k) - EKE) / CVr;
+                        F3(T_STATIC, i, j, k) = TSTATIC;
+                        F3(HO, i, j, k) = CP * TSTATIC + EKE;
+                        F3(P, i, j, k) = F3(RO, i, j, k) * RGASr * TSTATIC;
+                        F3(PEFF, i, j, k) = F3(P, i, j, k);
+                    }
+            /* 3902-3903 */
+            if (IPOUT <= 0) {
+                std::vector<R> PDOWN(KM + 1, R(0));
+                for (int k = 1; k <= KM; ++k)
+                    for (int i = 1; i <= IMM1; ++i)
+                        PDOWN[k] = PDOWN[k] + FP_v[i - 1] * R(0.5) * (F3(P, i, JM, k) + F3(P, i + 1, JM, k));
+                const R PDIFF = IPOUT == 0 ? PD_v[0] - PDOWN[1] : PD_v[KM - 1] - PDOWN[KM];
+                for (int k = 1; k <= KM; ++k) PD_v[k - 1] = PDOWN[k] + PDIFF;
+            }
+            RO_set = ROVX_set = ROVR_set = ROVT_set = ROE_set = true;
+            VX_set = VR_set = VT_set = RORVT_set = T_STATIC_set = HO_set = P_set = PEFF_set = true;
+            if (nstep) *nstep = ns;
+            return 0;
+        }
     }
 
     /* ------------------------------------------------------------------ */
@@ -2269,5 +2366,11 @@ int32_t oref_ad_seed(void *h, const char *n, const double *w, int64_t cnt) { ret
 int32_t oref_ad_reverse(void *h) { return ((OracleBase *)h)->ad_reverse(); }
 int32_t oref_ad_grad(void *h, const char *n, double *out, int64_t cnt) { return ((OracleBase *)h)->ad_grad(n, out, cnt); }
 int64_t oref_ad_tape_size(void *h) { return ((OracleBase *)h)->ad_tape_size(); }
+int32_t oref_write_flow_out(void *h, const char *path, const float *rosub) {
+    return ((OracleBase *)h)->write_flow_out(path, rosub);
+}
+int32_t oref_read_flow_out(void *h, const char *path, int32_t *nstep) {
+    return ((OracleBase *)h)->read_flow_out(path, nstep);
+}
 
 } /* extern "C" */

@@ -75,10 +75,12 @@ def lib():
         L.oref_ad_grad.argtypes = [vp, cp, vp, ctypes.c_int64]
         L.oref_ad_tape_size.argtypes = [vp]
         L.oref_ad_tape_size.restype = ctypes.c_int64
+        L.oref_write_flow_out.argtypes = [vp, cp, vp]
+        L.oref_read_flow_out.argtypes = [vp, cp, ctypes.POINTER(ctypes.c_int32)]
         for f in ("oref_set_int", "oref_set_real", "oref_get_real", "oref_get_int", "oref_set_array",
                   "oref_get_array", "oref_commit", "oref_stepup", "oref_loss_init", "oref_step",
                   "oref_integrals", "oref_set_array_f64", "oref_ad_begin", "oref_ad_zero", "oref_ad_seed",
-                  "oref_ad_reverse", "oref_ad_grad"):
+                  "oref_ad_reverse", "oref_ad_grad", "oref_write_flow_out", "oref_read_flow_out"):
             getattr(L, f).restype = ctypes.c_int32
         _lib = L
     return _lib
@@ -92,7 +94,9 @@ class Oracle:
     """One oracle problem: float or double arithmetic, or (ad=True) double
     arithmetic recorded on a tape for reverse-mode derivatives."""
 
-    def __init__(self, cd, double: bool = False, ad: bool = False):
+    def __init__(self, cd, double: bool = False, ad: bool = False, restart: str | None = None):
+        """restart: a flow_out file read before the commit, as SETUP reads it
+        with IF_RESTART = 1 (multall-open-18.3.f:6920-6992)."""
         L = lib()
         self.cd = cd
         self.double = double or ad
@@ -107,7 +111,18 @@ class Oracle:
         for k, a in cd.arrays.items():
             a = np.ascontiguousarray(a)
             self._chk(L.oref_set_array(self.h, k.encode(), a.ctypes.data, a.nbytes))
+        self.restart_nstep = None
+        if restart is not None:
+            ns = ctypes.c_int32()
+            self._chk(L.oref_read_flow_out(self.h, os.fsencode(restart), ctypes.byref(ns)))
+            self.restart_nstep = ns.value
         self._chk(L.oref_commit(self.h))
+
+    def write_flow_out(self, path: str, rosub: np.ndarray | None = None):
+        """OUTPUT's restart/plotting file flow_out (5942-5978) of the state."""
+        if rosub is not None:
+            rosub = np.ascontiguousarray(rosub, np.float32)
+        self._chk(lib().oref_write_flow_out(self.h, os.fsencode(path), None if rosub is None else rosub.ctypes.data))
 
     def _chk(self, rc):
         if rc != 0:

@@ -15,3 +15,21 @@ def rel_linf(a: np.ndarray, b: np.ndarray) -> float:
     if scale == 0.0:
         return float(np.max(np.abs(a - b)))
     return float(np.max(np.abs(a - b)) / scale)
+
+
+def read_flow_out(path: str, n: int, dtype=np.float32):
+    """(NSTEP, [8 arrays]) of a flow_out file: gfortran sequential unformatted
+    records, each payload between two 4-byte byte counts."""
+    raw = open(path, "rb").read()
+    pos, recs = 0, []
+    while pos < len(raw):
+        m = int(np.frombuffer(raw, np.int32, 1, pos)[0])
+        body = raw[pos + 4: pos + 4 + m]
+        assert int(np.frombuffer(raw, np.int32, 1, pos + 4 + m)[0]) == m, "record markers differ"
+        recs.append(body)
+        pos += m + 8
+    assert len(recs) == 9 and len(recs[0]) == 4, [len(r) for r in recs]
+    nstep = int(np.frombuffer(recs[0], np.int32)[0])
+    arrays = [np.frombuffer(r, dtype).copy() for r in recs[1:]]
+    assert all(a.size == n for a in arrays)
+    return nstep, arrays

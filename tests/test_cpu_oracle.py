@@ -255,3 +255,66 @@ def test_design_space_and_geometry_sensitivities(mods):
     g2 = {n: 2.0 * g1[n] for n in design.GEOM}
     c1, c2 = ds.chain(g1, sens), ds.chain(g2, sens)
     assert np.allclose(c2, 2.0 * c1)
+
+
+def test_flow_out_and_restart_follow_the_reference(mods, tmp_path):
+    """OUTPUT's flow_out (multall-open-18.3.f:5942-5978) from the FP32
+    oracle: nine gfortran records holding NSTEP and the eight fields, with
+    DPDS_CELL*1.0E-6 and PEFF+PREFF formed in REAL*4.  Read back as SETUP's
+    IF_RESTART branch does (6920-6992): the secondary variables, PEFF = P and
+    the shifted exit pressures PD, checked bitwise against the same REAL*4
+    expressions in NumPy, and LOOP's prologue (PREFF) taken from the
+    restarted pressures."""
+    from helpers import read_flow_out
+    case, common_setup, O = mods
+    cd = common_setup.build_common(case.small_stage())
+    ref = O.Oracle(cd)
+    ref.setup_calls()
+    for _ in range(3):
+        ref.step()
+    f = str(tmp_path / "flow_out")
+    ref.write_flow_out(f)
+    N = cd.nodes()
+    nstep, (ro, rovx, rovr, rovt, roe, rosub, dpds, peff) = read_flow_out(f, N)
+    g = lambda n: ref.get(n, double=False).ravel()
+    assert nstep == 3
+    for a, n in ((ro, "RO"), (rovx, "ROVX"), (rovr, "ROVR"), (rovt, "ROVT"), (roe, "ROE")):
+        assert np.array_equal(a, g(n)), n
+    assert np.array_equal(rosub, g("RO"))
+    assert np.array_equal(dpds, g("DPDS_CELL") * np.float32(1.0e-6))
+    P = g("P").reshape(cd.km, cd.jm, cd.im)
+    imid, kmid = int(0.5 * cd.im), int(0.5 * cd.km)
+    preff = np.float32(0.5) * (P[kmid - 1, 0, imid - 1] + P[kmid - 1, cd.jm - 1, imid - 1])
+    assert np.array_equal(peff, g("PEFF") + preff)
+
+    rs = O.Oracle(cd, restart=f)
+    assert rs.restart_nstep == 3
+    f32 = np.float32
+    cp, ga = f32(cd.reals["CP"]), f32(cd.reals["GA"])
+    cv = cp / ga
+    rgas = cp - cv
+    vx, vr, vt = rovx / ro, rovr / ro, rovt / ro
+    eke = f32(0.5) * (vx * vx + vr * vr + vt * vt)
+    ts = (roe / ro - eke) / cv
+    p = ro * rgas * ts
+    r = cd.arrays["R"].reshape(cd.km, cd.jm)[:, :, None]
+    want = {"VX": vx, "VR": vr, "VT": vt, "T_STATIC": ts, "HO": cp * ts + eke, "P": p, "PEFF": p,
+            "RORVT": (rovt.reshape(cd.km, cd.jm, cd.im) * r).ravel()}
+    for n, w in want.items():
+        assert np.array_equal(rs.get(n, double=False).ravel(), w), n
+    # the exit pressures: PDOWN(K) in the reference's order, shifted by PD(1)
+    pk = p.reshape(cd.km, cd.jm, cd.im)[:, cd.jm - 1, :]
+    fp = cd.arrays["FP"].ravel()
+    pdown = np.zeros(cd.km, np.float32)
+    for k in range(cd.km):
+        s = f32(0.0)
+        for i in range(cd.im - 1):
+            s = f32(s + fp[i] * f32(0.5) * (pk[k, i] + pk[k, i + 1]))
+        pdown[k] = s
+    assert cd.ints["IPOUT"] == 0
+    pd = pdown + (cd.arrays["PD"].ravel()[0] - pdown[0])
+    assert np.array_equal(rs.get("PD", double=False).ravel(), pd)
+    pr = p.reshape(cd.km, cd.jm, cd.im)
+    assert rs.get_real("PREFF") == float(f32(0.5) * (pr[kmid - 1, 0, imid - 1] + pr[kmid - 1, cd.jm - 1, imid - 1]))
+    rs.setup_calls()
+    rs.step()

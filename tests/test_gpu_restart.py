@@ -1,0 +1,98 @@
+"""The restart/plotting file flow_out through the C ABI: the file the GPU
+writes (OUTPUT, multall-open-18.3.f:5942-5978) against the FP32 oracle's,
+and a restart from a file (SETUP's IF_RESTART branch, 6920-6992) against
+the oracle's restart from the same file."""
+import copy
+
+import numpy as np
+import pytest
+
+from helpers import STATE, read_flow_out, rel_linf
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["RO", "ROVX", "ROVR", "ROVT", "ROE", "ROSUB", "DPDS_CELL*1e-6", "PEFF+PREFF"]
+
+
+@pytest.fixture(scope="module")
+def mods():
+    from mgpu import case, common_setup, lib
+    import oracle as O
+    lib.load()
+    return case, common_setup, lib, O
+
+
+def _restart_deck(cd):
+    c = copy.copy(cd)
+    c.ints = dict(cd.ints)
+    c.ints["IF_RESTART"] = 1
+    return c
+
+
+def test_flow_out_matches_oracle(mods, tmp_path):
+    """After three steps the GPU's flow_out has the oracle's record layout,
+    the GPU's own arrays exactly, and the oracle's values within 1e-5 (the
+    conserved variables) and 1e-4 (the LOSS wall term and PEFF)."""
+    case, common_setup, lib, O = mods
+    cd = common_setup.build_common(case.small_stage())
+    gpu = lib.Problem(cd)
+    ref = O.Oracle(cd)
+    ref.setup_calls()
+    for _ in range(3):
+        gpu.step()
+        ref.step()
+    fg, fr = str(tmp_path / "gpu_flow_out"), str(tmp_path / "ref_flow_out")
+    gpu.write_flow_out(fg)
+    ref.write_flow_out(fr)
+    N = cd.nodes()
+    ng, ag = read_flow_out(fg, N)
+    nr, ar = read_flow_out(fr, N)
+    assert ng == nr == 3
+    for a, n in zip(ag[:5], ("RO", "ROVX", "ROVR", "ROVT", "ROE")):
+        assert np.array_equal(a, gpu.get(n).ravel()), n
+    for a, b, n in zip(ag, ar, FIELDS):
+        tol = 1e-4 if n in ("DPDS_CELL*1e-6", "PEFF+PREFF") else 1e-5
+        assert rel_linf(a, b) <= tol, (n, rel_linf(a, b))
+
+
+def test_restart_matches_oracle_restart(mods, tmp_path):
+    """A restart from the oracle's file: the secondary variables, PEFF = P,
+    the exit pressures PD and LOOP's PREFF are the oracle's bit for bit;
+    five steps later every field is within 1e-4."""
+    case, common_setup, lib, O = mods
+    cd = common_setup.build_common(case.small_stage())
+    ref = O.Oracle(cd)
+    ref.setup_calls()
+    for _ in range(3):
+        ref.step()
+    f = str(tmp_path / "flow_out")
+    ref.write_flow_out(f)
+    cdr = _restart_deck(cd)
+    gpu = lib.Problem(cdr, restart=f)
+    ref2 = O.Oracle(cdr, restart=f)
+    ref2.setup_calls()
+    assert gpu.restart_nstep == ref2.restart_nstep == 3
+    for n in ("RO", "ROVX", "ROVR", "ROVT", "ROE", "RORVT", "VX", "VR", "VT", "T_STATIC", "HO", "P", "PEFF", "PD"):
+        assert np.array_equal(gpu.get(n).ravel(), ref2.get(n, double=False).ravel()), n
+    assert gpu.get_real("PREFF") == ref2.get_real("PREFF")
+    for _ in range(5):
+        gpu.step()
+        ref2.step()
+    for n in STATE:
+        assert rel_linf(gpu.get(n), ref2.get(n)) <= 1e-4, (n, rel_linf(gpu.get(n), ref2.get(n)))
+
+
+def test_gpu_checkpoint_round_trip(mods, tmp_path):
+    """The GPU's own checkpoint: a new handle restarted from it holds the
+    writer's conserved variables exactly."""
+    case, common_setup, lib, O = mods
+    cd = common_setup.build_common(case.small_nozzle())
+    gpu = lib.Problem(cd)
+    gpu.run(7)
+    f = str(tmp_path / "flow_out")
+    gpu.write_flow_out(f)
+    back = lib.Problem(_restart_deck(cd), restart=f)
+    assert back.restart_nstep == 7
+    for n in ("RO", "ROVX", "ROVR", "ROVT", "ROE"):
+        assert np.array_equal(back.get(n), gpu.get(n)), n
+    back.run(3)
