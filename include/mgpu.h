@@ -89,6 +89,20 @@ typedef struct mgpu_integrals {
     int32_t j1, j2m1;      /* stations used                                 */
 } mgpu_integrals;
 
+/* One row of EFICOOL's stage table (multall-open-18.3.f:11253-11420,
+ * IFCOOL = 0): the mass-averaged performance between the stations j1 and
+ * j2m1 and, for a stage, the reactions at hub, mid-span and tip from the
+ * pitchwise static pressures at j1, jmix and j2m1. */
+typedef struct mgpu_stage {
+    int32_t j1, j2m1, jmix;   /* stations (J1, J2M1, JMIX_STAGE)             */
+    int32_t has_reaction;     /* 0 for the whole machine                      */
+    double mass_flow_in;      /* BLADE_FLOW(J1)                               */
+    double mass_flow_out;     /* BLADE_FLOW(J2M1)                             */
+    double po_ratio, to_ratio, delta_to;   /* PORAT, TORAT, DELTO             */
+    double eta_tt, eta_ts, eta_poly;       /* ETAIS, ETATS, EPOLY             */
+    double reac_hub, reac_mid, reac_tip;   /* REAC_HUB, REAC_MID, REAC_TIP    */
+} mgpu_stage;
+
 /* ---- library information --------------------------------------------- */
 int32_t mgpu_abi_version(void);
 /* Copies the text of the last error raised on the calling thread. */
@@ -155,6 +169,15 @@ int32_t mgpu_sync(mgpu_handle *h);
 /* EFICOOL's mass averages and efficiencies on the current state, computed
  * on the device with FP64 accumulation. */
 int32_t mgpu_integrals_compute(mgpu_handle *h, mgpu_integrals *out);
+
+/* EFICOOL's table for stage nstg = 1..NSTAGES, or with nstg = NSTAGES+1 for
+ * the whole machine (multi-stage machines only, as EFICOOL prints it).  The
+ * stage of each row comes from the integer row array NSTAGE (bound like the
+ * COMMON arrays); the stations follow the reader's JSTG_START/JSTG_END
+ * (1522-1536).  The mass averages are the FP64 sums of
+ * mgpu_integrals_compute; the pitchwise pressures of the reactions are
+ * summed in REAL*4 in the reference's order. */
+int32_t mgpu_stage_performance(mgpu_handle *h, int32_t nstg, mgpu_stage *out);
 
 /* ---- restart / plotting file ------------------------------------------- */
 /* Writes the combined restart/plotting file "flow_out" from the device

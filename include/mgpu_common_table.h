@@ -153,6 +153,7 @@
     M_(N_WAKE,   INT32,   ROW, OPT)                                       \
     M_(SEP_THIK, FLOAT32, ROW, OPT)                                       \
     M_(SEP_DRAG, FLOAT32, ROW, OPT)                                       \
+    M_(NSTAGE,   INT32,   ROW, OPT)     /* stage of each row (EFICOOL) */ \
     /* per streamwise station J */                                       \
     M_(NBLADE,   INT32,   J,   GEOM)                                      \
     M_(IND,      INT32,   J,   GEOM)                                      \

@@ -938,6 +938,117 @@ int32_t mgpu_integrals_compute(mgpu_handle *h, mgpu_integrals *out) {
     return 0;
 }
 
+int32_t mgpu_stage_performance(mgpu_handle *h, int32_t nstg, mgpu_stage *out) {
+    if (!h || !h->committed || !out) return fail(MGPU_E_STATE, "stage performance before commit");
+    const Dev &d = h->d;
+    const int NSTAGES = d.NSTAGES, NROWS = d.NROWS;
+    const int NSTGP1 = NSTAGES == 1 ? 1 : NSTAGES + 1;
+    if (nstg < 1 || nstg > NSTGP1) return fail(MGPU_E_ARG, "stage number out of range");
+    const int an = find_array("NSTAGE");
+    if (!h->bound[an]) return fail(MGPU_E_STATE, "bind the row array NSTAGE for the stage table");
+    std::vector<int> NSTAGE, JSTART, JMIX, NROW;
+    std::vector<float> P, FP, PO1;
+    auto geti = [&](const char *n, std::vector<int> &v) {
+        int a = find_array(n);
+        return download(h, v, (const int *)h->dptr[a], shape_count(h, kArrays[a].shape));
+    };
+    auto getf = [&](const char *n, std::vector<float> &v) {
+        int a = find_array(n);
+        return download(h, v, (const float *)h->dptr[a], shape_count(h, kArrays[a].shape));
+    };
+    int rc = 0;
+    if ((rc = geti("NSTAGE", NSTAGE)) || (rc = geti("JSTART", JSTART)) || (rc = geti("JMIX", JMIX)) ||
+        (rc = geti("NROW", NROW)) || (rc = getf("P", P)) || (rc = getf("FP", FP)) || (rc = getf("PO1", PO1)))
+        return rc;
+    // the stages' stations, as the reader sets them (1522-1536)
+    std::vector<int> JSTG_START(NSTAGES + 2, 0), JSTG_END(NSTAGES + 2, 0);
+    JSTG_START[1] = 1;
+    for (int n = 1; n <= NROWS; ++n) {
+        const int s0 = NSTAGE[n - 1], s1 = n < NROWS ? NSTAGE[n] : NSTAGES + 1;
+        if (s0 < 1 || s0 > NSTAGES) return fail(MGPU_E_ARG, "NSTAGE out of 1..NSTAGES");
+        if (s0 != s1) {
+            JSTG_END[s0] = JMIX[n - 1];
+            if (s1 <= NSTAGES) JSTG_START[s1] = JSTART[n];
+        }
+    }
+    // 11269-11293
+    int J1, J2, J2M1, JMS;
+    const bool whole = NSTGP1 > 1 && nstg == NSTGP1;
+    if (!whole) {
+        J1 = JSTG_START[nstg];
+        J2 = JSTG_END[nstg] + 1;
+        J2M1 = nstg == NSTAGES ? d.JM - 1 : J2;
+        JMS = JMIX[NROW[J1] - 1];          // NROW(J1+1)
+    } else {
+        J1 = 2;
+        J2 = d.JM;
+        J2M1 = d.JM - 1;
+        JMS = (J1 + J2) / 2;
+    }
+    if (J1 < 1 || J2M1 > d.JM || J1 >= J2M1) return fail(MGPU_E_ARG, "stage stations out of range");
+    Launch L{h->stream, h->sm_count};
+    launch_integrals(d, L, h->d_int);
+    CK(cudaGetLastError());
+    std::vector<double> v((size_t)4 * d.JM);
+    CK(cudaMemcpyAsync(v.data(), h->d_int, v.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    auto bf = [&](int j) { return v[(size_t)(j - 1)]; };
+    auto spo = [&](int j) { return v[(size_t)d.JM + j - 1] / bf(j); };
+    auto sto = [&](int j) { return v[(size_t)2 * d.JM + j - 1] / bf(j); };
+    auto sps = [&](int j) { return v[(size_t)3 * d.JM + j - 1] / bf(j); };
+    const double PO1M = PO1[d.KMID - 1], FGA = (double)d.FGA;
+    out->j1 = J1;
+    out->j2m1 = J2M1;
+    out->jmix = JMS;
+    out->has_reaction = !whole;
+    out->reac_hub = out->reac_mid = out->reac_tip = 0.0;
+    if (!whole) {
+        // pitchwise static pressures, REAL*4 in I order (11300-11349)
+        const int KMID2 = d.KM / 2;
+        auto pline = [&](int j, int k) {
+            float s = 0.0f;
+            for (int i = 1; i <= d.IMM1; ++i) {
+                const size_t a = (size_t)(i - 1) + (size_t)d.IM * ((size_t)(j - 1) + (size_t)d.JM * (size_t)(k - 1));
+                s = s + 0.5f * (P[a] + P[a + 1]) * FP[i - 1];
+            }
+            return s;
+        };
+        const int ks[3] = {1, KMID2, d.KM};
+        float rr[3];
+        const float pmid_in = pline(J1, KMID2), pmid_out = pline(J2M1, KMID2);
+        for (int q = 0; q < 3; ++q) {
+            const float pin = pline(J1, ks[q]), pm = pline(JMS, ks[q]), po = pline(J2M1, ks[q]);
+            rr[q] = (pm - po) / (pin - po);
+            if (pmid_out > pmid_in) rr[q] = 1.0f - rr[q];    // a compressor
+        }
+        out->reac_hub = rr[0];
+        out->reac_mid = rr[1];
+        out->reac_tip = rr[2];
+    }
+    // 11366-11394
+    const double POIN = spo(J1) * PO1M, PO2 = spo(J2M1) * PO1M, PSOUT = sps(J2M1);
+    const double TO_IN = sto(J1), TO_OUT = sto(J2M1);
+    const double TORAT = TO_OUT / TO_IN, DELTO = TO_OUT - TO_IN, PSRAT = PSOUT / POIN;
+    double PORAT = PO2 / POIN;
+    if (PORAT < 0.01) PORAT = 0.01;
+    const double TO2IS = pow(PORAT, FGA) * TO_IN, TSTAT2_IS = pow(PSRAT, FGA) * TO_IN;
+    const double DELTOIS = TO2IS - TO_IN, DELT_TOT_STAT = TSTAT2_IS - TO_IN;
+    double ETAIS = 1.0, ETATS = 1.0;
+    if (DELTO > 0.0) { ETAIS = DELTOIS / DELTO; ETATS = DELT_TOT_STAT / DELTO; }
+    if (DELTO < 0.0) { ETAIS = DELTO / DELTOIS; ETATS = DELTO / DELT_TOT_STAT; }
+    double EPOLY = log(TORAT) / log(PORAT) / FGA;
+    if (TORAT > 1.0) EPOLY = 1.0 / EPOLY;
+    out->mass_flow_in = bf(J1);
+    out->mass_flow_out = bf(J2M1);
+    out->po_ratio = PORAT;
+    out->to_ratio = TORAT;
+    out->delta_to = DELTO;
+    out->eta_tt = ETAIS;
+    out->eta_ts = ETATS;
+    out->eta_poly = EPOLY;
+    return 0;
+}
+
 int32_t mgpu_autotune(mgpu_handle *h, int32_t *chosen, double *ms) {
     if (!h || !h->committed) return fail(MGPU_E_STATE, "autotune before commit");
     Dev &d = h->d;

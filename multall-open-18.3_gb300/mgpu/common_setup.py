@@ -573,6 +573,7 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None, metrics64: boo
         NUP_I1=np.array([r.nup_i1 for r in spec.rows], np.int32),
         NUP_IM=np.array([r.nup_im for r in spec.rows], np.int32),
         N_WAKE=np.array([r.n_wake for r in spec.rows], np.int32),
+        NSTAGE=np.array([r.stage for r in spec.rows], np.int32),
         SEP_THIK=np.array([r.sep_thik for r in spec.rows], f32),
         SEP_DRAG=np.array([r.sep_drag for r in spec.rows], f32),
         RT_THICK=RT_THICK, RTHETA=RTHETA,

@@ -27,6 +27,16 @@ class Monitors(ctypes.Structure):
                 ("kvmax", ctypes.c_int32), ("flow_in", ctypes.c_double), ("flow_out", ctypes.c_double)]
 
 
+class Stage(ctypes.Structure):
+    """One row of EFICOOL's stage table (mgpu_stage)."""
+    _fields_ = [("j1", ctypes.c_int32), ("j2m1", ctypes.c_int32), ("jmix", ctypes.c_int32),
+                ("has_reaction", ctypes.c_int32), ("mass_flow_in", ctypes.c_double),
+                ("mass_flow_out", ctypes.c_double), ("po_ratio", ctypes.c_double), ("to_ratio", ctypes.c_double),
+                ("delta_to", ctypes.c_double), ("eta_tt", ctypes.c_double), ("eta_ts", ctypes.c_double),
+                ("eta_poly", ctypes.c_double), ("reac_hub", ctypes.c_double), ("reac_mid", ctypes.c_double),
+                ("reac_tip", ctypes.c_double)]
+
+
 class Integrals(ctypes.Structure):
     _fields_ = [("mass_flow_in", ctypes.c_double), ("mass_flow_out", ctypes.c_double),
                 ("eta_tt", ctypes.c_double), ("eta_ts", ctypes.c_double), ("po_ratio", ctypes.c_double),
@@ -46,7 +56,7 @@ EXPORTS = ["mgpu_abi_version", "mgpu_last_error", "mgpu_device_count", "mgpu_cre
            "mgpu_batch_run", "mgpu_batch_bench_steps", "mgpu_adjoint_prepare", "mgpu_adjoint_objective",
            "mgpu_adjoint_iterate", "mgpu_adjoint_solve", "mgpu_adjoint_gradient", "mgpu_adjoint_get",
            "mgpu_adjoint_set", "mgpu_adjoint_solve_krylov", "mgpu_autotune", "mgpu_write_flow_out",
-           "mgpu_read_flow_out"]
+           "mgpu_read_flow_out", "mgpu_stage_performance"]
 
 _lib = None
 
@@ -97,6 +107,7 @@ def load(build: bool = True):
     L.mgpu_adjoint_gradient.argtypes = [vp]
     L.mgpu_autotune.argtypes = [vp, ctypes.POINTER(i32), dp]
     L.mgpu_write_flow_out.argtypes = [vp, cp, vp]
+    L.mgpu_stage_performance.argtypes = [vp, i32, ctypes.POINTER(Stage)]
     L.mgpu_read_flow_out.argtypes = [vp, cp, ctypes.POINTER(i32)]
     L.mgpu_adjoint_solve_krylov.argtypes = [vp, i32, i32, i32, ctypes.c_double, ctypes.POINTER(i32), dp]
     L.mgpu_adjoint_get.argtypes = [vp, cp, vp, ctypes.c_int64]
@@ -165,6 +176,12 @@ class Problem:
         _chk(L.mgpu_commit(self.h))
         if setup_calls:
             self.setup_calls()
+
+    def stage(self, nstg: int) -> Stage:
+        """EFICOOL's table for stage nstg (NSTAGES+1: the whole machine)."""
+        o = Stage()
+        _chk(load().mgpu_stage_performance(self.h, int(nstg), ctypes.byref(o)))
+        return o
 
     def write_flow_out(self, path: str, rosub: np.ndarray | None = None):
         """The restart/plotting file flow_out of the current state."""

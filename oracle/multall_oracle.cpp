@@ -81,6 +81,7 @@ struct OracleBase {
     virtual int loss_init() = 0;
     virtual int step(int force_end, mgpu_monitors *mon) = 0;
     virtual int integrals(mgpu_integrals *out) = 0;
+    virtual int stage_performance(int nstg, mgpu_stage *out) = 0;
     /* reverse mode (the adt::AD instantiation only): ad_begin makes every
        REAL array of the COMMON table an independent variable and starts the
        tape; after a step, ad_seed adds output adjoints to the arrays' current
@@ -2253,8 +2254,8 @@ struct Oracle : OracleBase {
     }
     int64_t ad_tape_size() override { return (int64_t)tape_.size(); }
 
-    int integrals(mgpu_integrals *out) override {
-        if (!committed) return fail(MGPU_E_STATE, "integrals before commit");
+    /* EFICOOL's mass averages per J station (10662-10849, IFCOOL = 0) */
+    void per_j_sums(std::vector<R> &BF, std::vector<R> &SPO, std::vector<R> &STO, std::vector<R> &SPS) {
         size_t n3 = (size_t)IM * JM * KM;
         std::vector<R> ST2(n3), T1(n3), T2(n3), T3(n3), T4(n3);
         R TO1M = F1(TO1, KMID), PO1M = F1(PO1, KMID);
@@ -2280,7 +2281,7 @@ struct Oracle : OracleBase {
                     A3(T3, i, j, k) = F3(RORVT, i, j, k) / F3(RO, i, j, k);
                     A3(T4, i, j, k) = ENTRPY;
                 }
-        std::vector<R> BF(JM), SPO(JM), STO(JM), SPS(JM);
+        BF.assign(JM, R(0)); SPO.assign(JM, R(0)); STO.assign(JM, R(0)); SPS.assign(JM, R(0));
         for (int j = 1; j <= JM; ++j) {
             R bf = 0, spo = 0, sto = 0, sps = 0;
             for (int k = 1; k <= KMM1; ++k)
@@ -2297,6 +2298,79 @@ struct Oracle : OracleBase {
             STO[j - 1] = sto / bf;
             SPS[j - 1] = sps / bf;
         }
+    }
+
+    /* EFICOOL's stage table (11253-11420, IFCOOL = 0) with the stations of
+       the reader's JSTG_START / JSTG_END (1522-1536) */
+    int stage_performance(int nstg, mgpu_stage *out) override {
+        if (!committed) return fail(MGPU_E_STATE, "stage performance before commit");
+        if (!NSTAGE_set) return fail(MGPU_E_STATE, "bind the row array NSTAGE for the stage table");
+        const int NSTGP1 = NSTAGES == 1 ? 1 : NSTAGES + 1;
+        if (nstg < 1 || nstg > NSTGP1) return fail(MGPU_E_ARG, "stage number out of range");
+        std::vector<int> JSTG_START(NSTAGES + 2, 0), JSTG_END(NSTAGES + 2, 0);
+        JSTG_START[1] = 1;
+        for (int n = 1; n <= NROWS; ++n) {
+            const int s0 = NSTAGE_v[n - 1], s1 = n < NROWS ? NSTAGE_v[n] : NSTAGES + 1;
+            if (s0 != s1) {
+                JSTG_END[s0] = JMIX_v[n - 1];
+                if (s1 <= NSTAGES) JSTG_START[s1] = JSTART_v[n];
+            }
+        }
+        const bool whole = NSTGP1 > 1 && nstg == NSTGP1;
+        int J1, J2, J2M1, JMS;
+        if (!whole) {
+            J1 = JSTG_START[nstg];
+            J2 = JSTG_END[nstg] + 1;
+            J2M1 = nstg == NSTAGES ? JM - 1 : J2;
+            JMS = JMIX_v[NROW_v[J1] - 1];
+        } else {
+            J1 = 2; J2 = JM; J2M1 = JM - 1; JMS = (J1 + J2) / 2;
+        }
+        out->j1 = J1; out->j2m1 = J2M1; out->jmix = JMS; out->has_reaction = !whole;
+        out->reac_hub = out->reac_mid = out->reac_tip = 0.0;
+        if (!whole) {
+            const int KM2 = KM / 2;
+            auto pline = [&](int j, int k) {
+                R s = R(0);
+                for (int i = 1; i <= IMM1; ++i) s = s + R(0.5) * (F3(P, i, j, k) + F3(P, i + 1, j, k)) * F1(FP, i);
+                return s;
+            };
+            const int ks[3] = {1, KM2, KM};
+            const R pmi = pline(J1, KM2), pmo = pline(J2M1, KM2);
+            double rr[3];
+            for (int q = 0; q < 3; ++q) {
+                R r = (pline(JMS, ks[q]) - pline(J2M1, ks[q])) / (pline(J1, ks[q]) - pline(J2M1, ks[q]));
+                if (pmo > pmi) r = R(1.0) - r;
+                rr[q] = (double)r;
+            }
+            out->reac_hub = rr[0]; out->reac_mid = rr[1]; out->reac_tip = rr[2];
+        }
+        std::vector<R> BF, SPO, STO, SPS;
+        per_j_sums(BF, SPO, STO, SPS);
+        const R PO1M = F1(PO1, KMID);
+        R POIN = SPO[J1 - 1] * PO1M, PO2 = SPO[J2M1 - 1] * PO1M, PSOUT = SPS[J2M1 - 1];
+        R TO_IN = STO[J1 - 1], TO_OUT = STO[J2M1 - 1];
+        R TORAT = TO_OUT / TO_IN, DELTO = TO_OUT - TO_IN, PORAT = PO2 / POIN, PSRAT = PSOUT / POIN;
+        if (PORAT < R(0.01)) PORAT = R(0.01);
+        R TO2IS = om::pow(PORAT, FGA) * TO_IN, TSTAT2_IS = om::pow(PSRAT, FGA) * TO_IN;
+        R DELTOIS = TO2IS - TO_IN, DELT_TOT_STAT = TSTAT2_IS - TO_IN;
+        R ETAIS = R(1.0), ETATS = R(1.0);
+        if (DELTO > R(0.0)) { ETAIS = DELTOIS / DELTO; ETATS = DELT_TOT_STAT / DELTO; }
+        if (DELTO < R(0.0)) { ETAIS = DELTO / DELTOIS; ETATS = DELTO / DELT_TOT_STAT; }
+        R EPOLY = om::log(TORAT) / om::log(PORAT) / FGA;
+        if (TORAT > R(1.0)) EPOLY = R(1.0) / EPOLY;
+        out->mass_flow_in = (double)BF[J1 - 1];
+        out->mass_flow_out = (double)BF[J2M1 - 1];
+        out->po_ratio = (double)PORAT; out->to_ratio = (double)TORAT; out->delta_to = (double)DELTO;
+        out->eta_tt = (double)ETAIS; out->eta_ts = (double)ETATS; out->eta_poly = (double)EPOLY;
+        return 0;
+    }
+
+    int integrals(mgpu_integrals *out) override {
+        if (!committed) return fail(MGPU_E_STATE, "integrals before commit");
+        std::vector<R> BF, SPO, STO, SPS;
+        per_j_sums(BF, SPO, STO, SPS);
+        R PO1M = F1(PO1, KMID);
         int J1, J2M1;
         if (NSTAGES == 1) { J1 = 1; J2M1 = JM - 1; }
         else { J1 = 2; J2M1 = JM - 1; }
@@ -2357,6 +2431,9 @@ int32_t oref_stepup(void *h, double relax) { return ((OracleBase *)h)->stepup(re
 int32_t oref_loss_init(void *h) { return ((OracleBase *)h)->loss_init(); }
 int32_t oref_step(void *h, int32_t force_end, mgpu_monitors *mon) { return ((OracleBase *)h)->step(force_end, mon); }
 int32_t oref_integrals(void *h, mgpu_integrals *out) { return ((OracleBase *)h)->integrals(out); }
+int32_t oref_stage_performance(void *h, int32_t nstg, mgpu_stage *out) {
+    return ((OracleBase *)h)->stage_performance(nstg, out);
+}
 int32_t oref_set_array_f64(void *h, const char *n, const double *p, int64_t cnt) {
     return ((OracleBase *)h)->set_array_f64(n, p, cnt);
 }

@@ -28,6 +28,16 @@ class Monitors(ctypes.Structure):
                 ("kvmax", ctypes.c_int32), ("flow_in", ctypes.c_double), ("flow_out", ctypes.c_double)]
 
 
+class Stage(ctypes.Structure):
+    """One row of EFICOOL's stage table (mgpu_stage)."""
+    _fields_ = [("j1", ctypes.c_int32), ("j2m1", ctypes.c_int32), ("jmix", ctypes.c_int32),
+                ("has_reaction", ctypes.c_int32), ("mass_flow_in", ctypes.c_double),
+                ("mass_flow_out", ctypes.c_double), ("po_ratio", ctypes.c_double), ("to_ratio", ctypes.c_double),
+                ("delta_to", ctypes.c_double), ("eta_tt", ctypes.c_double), ("eta_ts", ctypes.c_double),
+                ("eta_poly", ctypes.c_double), ("reac_hub", ctypes.c_double), ("reac_mid", ctypes.c_double),
+                ("reac_tip", ctypes.c_double)]
+
+
 class Integrals(ctypes.Structure):
     _fields_ = [("mass_flow_in", ctypes.c_double), ("mass_flow_out", ctypes.c_double),
                 ("eta_tt", ctypes.c_double), ("eta_ts", ctypes.c_double), ("po_ratio", ctypes.c_double),
@@ -76,11 +86,13 @@ def lib():
         L.oref_ad_tape_size.argtypes = [vp]
         L.oref_ad_tape_size.restype = ctypes.c_int64
         L.oref_write_flow_out.argtypes = [vp, cp, vp]
+        L.oref_stage_performance.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(Stage)]
         L.oref_read_flow_out.argtypes = [vp, cp, ctypes.POINTER(ctypes.c_int32)]
         for f in ("oref_set_int", "oref_set_real", "oref_get_real", "oref_get_int", "oref_set_array",
                   "oref_get_array", "oref_commit", "oref_stepup", "oref_loss_init", "oref_step",
                   "oref_integrals", "oref_set_array_f64", "oref_ad_begin", "oref_ad_zero", "oref_ad_seed",
-                  "oref_ad_reverse", "oref_ad_grad", "oref_write_flow_out", "oref_read_flow_out"):
+                  "oref_ad_reverse", "oref_ad_grad", "oref_write_flow_out", "oref_read_flow_out",
+                  "oref_stage_performance"):
             getattr(L, f).restype = ctypes.c_int32
         _lib = L
     return _lib
@@ -117,6 +129,12 @@ class Oracle:
             self._chk(L.oref_read_flow_out(self.h, os.fsencode(restart), ctypes.byref(ns)))
             self.restart_nstep = ns.value
         self._chk(L.oref_commit(self.h))
+
+    def stage(self, nstg: int) -> "Stage":
+        """EFICOOL's table for stage nstg (NSTAGES+1: the whole machine)."""
+        o = Stage()
+        self._chk(lib().oref_stage_performance(self.h, int(nstg), ctypes.byref(o)))
+        return o
 
     def write_flow_out(self, path: str, rosub: np.ndarray | None = None):
         """OUTPUT's restart/plotting file flow_out (5942-5978) of the state."""

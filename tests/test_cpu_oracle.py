@@ -318,3 +318,37 @@ def test_flow_out_and_restart_follow_the_reference(mods, tmp_path):
     assert rs.get_real("PREFF") == float(f32(0.5) * (pr[kmid - 1, 0, imid - 1] + pr[kmid - 1, cd.jm - 1, imid - 1]))
     rs.setup_calls()
     rs.step()
+
+
+def test_stage_table_stations_and_whole_machine(mods):
+    """EFICOOL's stage table on a 4-stage compressor: the stations follow the
+    reader's JSTG_START / JSTG_END (multall-open-18.3.f:1522-1536) and the
+    stage loop (11269-11293); the whole-machine row is the integrals' one."""
+    case, common_setup, O = mods
+    cd = common_setup.build_common(case.compressor_4stage(im=9, jm_row=25, km=7))
+    ns = cd.ints["NSTAGES"]
+    nstage, jstart, jmix = (cd.arrays[n].ravel() for n in ("NSTAGE", "JSTART", "JMIX"))
+    nrow = cd.arrays["NROW"].ravel()
+    js, je = {1: 1}, {}
+    for n in range(len(nstage)):
+        s0 = int(nstage[n])
+        s1 = int(nstage[n + 1]) if n + 1 < len(nstage) else ns + 1
+        if s0 != s1:
+            je[s0] = int(jmix[n])
+            if s1 <= ns:
+                js[s1] = int(jstart[n + 1])
+    ref = O.Oracle(cd)
+    ref.setup_calls()
+    for _ in range(10):
+        ref.step()
+    for s in range(1, ns + 1):
+        st = ref.stage(s)
+        j2 = je[s] + 1
+        assert (st.j1, st.j2m1, st.jmix, st.has_reaction) == (
+            js[s], cd.jm - 1 if s == ns else j2, int(jmix[nrow[js[s]] - 1]), 1), s
+    whole, ig = ref.stage(ns + 1), ref.integrals()
+    assert (whole.j1, whole.j2m1, whole.has_reaction) == (ig.j1, ig.j2m1, 0) == (2, cd.jm - 1, 0)
+    for f in ("mass_flow_in", "mass_flow_out", "eta_tt", "eta_ts", "po_ratio", "to_ratio"):
+        assert getattr(whole, f) == getattr(ig, f), f
+    with pytest.raises(O.OracleError):
+        ref.stage(ns + 2)

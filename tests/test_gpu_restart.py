@@ -1,7 +1,8 @@
-"""The restart/plotting file flow_out through the C ABI: the file the GPU
-writes (OUTPUT, multall-open-18.3.f:5942-5978) against the FP32 oracle's,
-and a restart from a file (SETUP's IF_RESTART branch, 6920-6992) against
-the oracle's restart from the same file."""
+"""The restart/plotting file flow_out and EFICOOL's stage table through the C
+ABI.  flow_out: the file the GPU writes (OUTPUT, multall-open-18.3.f:
+5942-5978) against the FP32 oracle's, and a restart from a file (SETUP's
+IF_RESTART branch, 6920-6992) against the oracle's restart from the same
+file.  The stage table (11253-11420) against the oracle's."""
 import copy
 
 import numpy as np
@@ -96,3 +97,25 @@ def test_gpu_checkpoint_round_trip(mods, tmp_path):
     for n in ("RO", "ROVX", "ROVR", "ROVT", "ROE"):
         assert np.array_equal(back.get(n), gpu.get(n)), n
     back.run(3)
+
+
+def test_stage_table_matches_oracle(mods):
+    """EFICOOL's stage table of a 4-stage compressor after 30 steps: the
+    stations are the oracle's, the mass flows and ratios agree to 1e-4
+    relative (FP64 per-J sums on the GPU, REAL*4 in the oracle), the
+    efficiencies and reactions to 1e-3."""
+    case, common_setup, lib, O = mods
+    cd = common_setup.build_common(case.compressor_4stage(im=9, jm_row=25, km=7))
+    gpu = lib.Problem(cd)
+    ref = O.Oracle(cd)
+    ref.setup_calls()
+    for _ in range(30):
+        gpu.step()
+        ref.step()
+    for s in range(1, cd.ints["NSTAGES"] + 2):
+        g, r = gpu.stage(s), ref.stage(s)
+        assert (g.j1, g.j2m1, g.jmix, g.has_reaction) == (r.j1, r.j2m1, r.jmix, r.has_reaction), s
+        for f in ("mass_flow_in", "mass_flow_out", "po_ratio", "to_ratio"):
+            assert abs(getattr(g, f) - getattr(r, f)) <= 1e-4 * abs(getattr(r, f)), (s, f)
+        for f in ("eta_tt", "eta_ts", "eta_poly", "reac_hub", "reac_mid", "reac_tip"):
+            assert abs(getattr(g, f) - getattr(r, f)) <= 1e-3, (s, f, getattr(g, f), getattr(r, f))
