@@ -357,7 +357,10 @@ def run_adjoint(args, rank, world, local_rank):
     cd = ds.deck(alpha)
     cd.ints["NSTEPS_MAX"] = 10 ** 9
     cd.reals["CONLIM"] = 1e-9
-    n_primal, inner, restart, max_steps, n_fd = 16000, 50, 30, 20000, 10000
+    # GMRES stops at tol, at max_steps, or when a restart cycle lowers the
+    # residual by less than 1 % (stagnation: on this frozen-turbulence stage
+    # the residual levels off at 0.09 for eta_tt and 0.20 for the mass flow)
+    n_primal, inner, restart, max_steps, stall, n_fd = 16000, 50, 30, 30000, 0.01, 10000
     if os.environ.get("MGPU_ADJ_PROFILE") == "1":
         # a short run for kernel profiles: 200 primal steps, then 20 transposed
         # steps with an objective and the geometry pass, no solve and no FD
@@ -396,7 +399,8 @@ def run_adjoint(args, rank, world, local_rank):
             t0 = time.perf_counter()
             p.adjoint_prepare()
             val = p.adjoint_objective(obj)
-            ok, steps, res = p.adjoint_solve_krylov(inner=inner, restart=restart, max_steps=max_steps, tol=1e-6)
+            ok, steps, res = p.adjoint_solve_krylov(inner=inner, restart=restart, max_steps=max_steps, tol=1e-6,
+                                                    stall=stall)
             gd = p.adjoint_gradient()
             t_adj += time.perf_counter() - t0
             d2h += sum(a.nbytes for a in gd.values())
@@ -436,7 +440,7 @@ def run_adjoint(args, rank, world, local_rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOADS["adjoint"][1], "nodes": cd.nodes(), "design_variables": ds.size,
                    "objectives": ["eta_tt", "mass_flow_in"], "primal_steps": n_primal,
-                   "krylov": {"inner": inner, "restart": restart, "max_steps": max_steps},
+                   "krylov": {"inner": inner, "restart": restart, "max_steps": max_steps, "stall": stall},
                    "fd": {"h_deg": h, "steps_per_solve": n_fd, "solves": 2 * ds.size}},
         "adjoint_time_s": t_adj_total, "adjoint_device_s": t_adj, "sensitivities_host_s": t_sens,
         "primal_solve_s": t_primal, "adjoint_over_primal": t_adj_total / t_primal,

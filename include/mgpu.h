@@ -292,10 +292,12 @@ int32_t mgpu_adjoint_solve(mgpu_handle *h, int32_t max_iters, double tol, int32_
  * growing mode; the plain iteration then diverges).  Starts from the current
  * lambda; restart = basis size (2-200); *steps = transposed steps used in
  * all; *rel_residual = the preconditioned system's |b - A lambda| / |b|.
+ * stall > 0 also ends the solve when a restart cycle lowers the residual by
+ * less than that fraction of it (stagnation); 0 runs to tol or max_steps.
  * Returns 0 if converged, 1 if not.  Holds (restart + 4) packed adjoint
  * vectors (14 node arrays each) on the device. */
 int32_t mgpu_adjoint_solve_krylov(mgpu_handle *h, int32_t inner, int32_t restart, int32_t max_steps, double tol,
-                                  int32_t *steps, double *rel_residual);
+                                  double stall, int32_t *steps, double *rel_residual);
 /* One more reverse step that also accumulates dJ/dA for the geometry
  * arrays AQX, AQR, ABX, ABR, ABT, ASX, ASR and VOLOR. */
 int32_t mgpu_adjoint_gradient(mgpu_handle *h);

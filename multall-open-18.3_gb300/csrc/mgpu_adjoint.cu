@@ -2464,11 +2464,12 @@ int32_t mgpu_adjoint_solve(mgpu_handle *h, int32_t max_iters, double tol, int32_
 }
 
 int32_t mgpu_adjoint_solve_krylov(mgpu_handle *h, int32_t inner, int32_t restart, int32_t max_steps, double tol,
-                                  int32_t *steps, double *rel_residual) {
+                                  double stall, int32_t *steps, double *rel_residual) {
     AdjState *s = ready_state(h);
     if (!s) return api_fail(MGPU_E_STATE, "adjoint solve before mgpu_adjoint_prepare");
-    if (inner < 1 || restart < 2 || restart > 200 || max_steps < 1 || !(tol > 0.0))
-        return api_fail(MGPU_E_ARG, "Krylov solve: inner >= 1, 2 <= restart <= 200, max_steps >= 1, tol > 0");
+    if (inner < 1 || restart < 2 || restart > 200 || max_steps < 1 || !(tol > 0.0) || !(stall >= 0.0 && stall < 1.0))
+        return api_fail(MGPU_E_ARG,
+                        "Krylov solve: inner >= 1, 2 <= restart <= 200, max_steps >= 1, tol > 0, 0 <= stall < 1");
     const Dev &d = handle_dev(h);
     cudaStream_t st = handle_view(h).stream;
     int rc = ensure_graph(s, d, st);
@@ -2536,6 +2537,7 @@ int32_t mgpu_adjoint_solve_krylov(mgpu_handle *h, int32_t inner, int32_t restart
     const int m = restart;
     std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
     bool done = bnorm == 0.0;
+    double cycle_rel = -1.0;     // residual estimate at the end of the last restart cycle
     while (!done && nprod < max_steps) {
         // r = b - A x into v_0
         float *v0 = s->kv;
@@ -2589,6 +2591,9 @@ int32_t mgpu_adjoint_solve_krylov(mgpu_handle *h, int32_t inner, int32_t restart
         std::vector<double> yy(y.begin(), y.begin() + jdone);
         if ((rc = comb(s->kv, yy, 1.0f, s->kx))) return rc;
         if (rel < tol) done = true;
+        // stagnation: this cycle lowered the residual by less than stall of it
+        if (stall > 0.0 && cycle_rel > 0.0 && cycle_rel - rel < stall * cycle_rel) done = true;
+        cycle_rel = rel;
     }
     if ((rc = unpack(s, d, s->kx, st))) return rc;
     ACK(seeds(1));

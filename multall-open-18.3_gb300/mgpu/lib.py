@@ -109,7 +109,8 @@ def load(build: bool = True):
     L.mgpu_write_flow_out.argtypes = [vp, cp, vp]
     L.mgpu_stage_performance.argtypes = [vp, i32, ctypes.POINTER(Stage)]
     L.mgpu_read_flow_out.argtypes = [vp, cp, ctypes.POINTER(i32)]
-    L.mgpu_adjoint_solve_krylov.argtypes = [vp, i32, i32, i32, ctypes.c_double, ctypes.POINTER(i32), dp]
+    L.mgpu_adjoint_solve_krylov.argtypes = [vp, i32, i32, i32, ctypes.c_double, ctypes.c_double,
+                                            ctypes.POINTER(i32), dp]
     L.mgpu_adjoint_get.argtypes = [vp, cp, vp, ctypes.c_int64]
     L.mgpu_adjoint_set.argtypes = [vp, cp, vp, ctypes.c_int64]
     for f in EXPORTS:
@@ -305,12 +306,14 @@ class Problem:
         rc = _chk(load().mgpu_adjoint_solve(self.h, int(max_iters), float(tol), ctypes.byref(it), ctypes.byref(r)))
         return rc == 0, it.value, r.value
 
-    def adjoint_solve_krylov(self, inner: int = 40, restart: int = 30, max_steps: int = 20000, tol: float = 1e-6):
+    def adjoint_solve_krylov(self, inner: int = 40, restart: int = 30, max_steps: int = 20000, tol: float = 1e-6,
+                             stall: float = 0.0):
         """(converged, transposed steps used, relative residual) of GMRES on
-        the inner-step map."""
+        the inner-step map; stall > 0 stops when a restart cycle lowers the
+        residual by less than that fraction."""
         it, r = ctypes.c_int32(), ctypes.c_double()
         rc = _chk(load().mgpu_adjoint_solve_krylov(self.h, int(inner), int(restart), int(max_steps), float(tol),
-                                                   ctypes.byref(it), ctypes.byref(r)))
+                                                   float(stall), ctypes.byref(it), ctypes.byref(r)))
         return rc == 0, it.value, r.value
 
     def adjoint_gradient(self) -> dict:
