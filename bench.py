@@ -387,10 +387,12 @@ def run_adjoint(args, rank, world, local_rank):
     t_primal = time.perf_counter() - t0
     state = {n: p.get(n) for n, a in cd.arrays.items() if a.dtype == np.float32}
     integ = p.integrals()
+    # dTHETA/d(alpha) of the generator; the device turns dJ/dA into dJ/dTHETA
+    # (transposed SETUP metrics), so the host differences the node angles only
     t0 = time.perf_counter()
-    sens = ds.sensitivities(alpha)
-    g64 = ds.geometry64(alpha)
+    sens = ds.theta_sensitivities(alpha)
     t_sens = time.perf_counter() - t0
+    g64 = ds.geometry64(alpha)
     grads, solves = {}, {}
     t_adj = 0.0
     d2h = 0
@@ -401,10 +403,11 @@ def run_adjoint(args, rank, world, local_rank):
             val = p.adjoint_objective(obj)
             ok, steps, res = p.adjoint_solve_krylov(inner=inner, restart=restart, max_steps=max_steps, tol=1e-6,
                                                     stall=stall)
-            gd = p.adjoint_gradient()
+            p.adjoint_gradient(read=False)
+            gth = p.adjoint_gradient_theta()
             t_adj += time.perf_counter() - t0
-            d2h += sum(a.nbytes for a in gd.values())
-            grads[obj] = ds.chain(gd, sens)
+            d2h += gth.nbytes
+            grads[obj] = ds.chain_theta(gth, sens)
             solves[obj] = {"value": val, "converged": ok, "transposed_steps": steps, "rel_residual": res}
     # finite differences: restarts of the primal (LOSS on) from the converged
     # state with the geometry moved by +-h
@@ -450,7 +453,7 @@ def run_adjoint(args, rank, world, local_rank):
         "cpu_baseline": None, "clocks": clk.summary(),
         "e2e": {"value": t_fd / t_adj_total, "unit": "x", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": d2h / max(steps_total, 1),
-                "how": "mgpu_adjoint_* through the C ABI; geometry gradients read back to the host for the chain"},
+                "how": "mgpu_adjoint_* through the C ABI; dJ/dTHETA read back to the host for the chain"},
         "gpu_launches": adj_kernels_per_step(cd) * steps_total,
     }
     print(json.dumps(line), flush=True)

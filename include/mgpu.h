@@ -301,6 +301,13 @@ int32_t mgpu_adjoint_solve_krylov(mgpu_handle *h, int32_t inner, int32_t restart
 /* One more reverse step that also accumulates dJ/dA for the geometry
  * arrays AQX, AQR, ABX, ABR, ABT, ASX, ASR and VOLOR. */
 int32_t mgpu_adjoint_gradient(mgpu_handle *h);
+/* dJ/dTHETA (IM*JM*KM values, per radian) from the geometry gradient of the
+ * last mgpu_adjoint_gradient.  SETUP's face areas and volumes (3030-4045)
+ * are linear in the node angles THETA for fixed X and R, so this is the
+ * transposed metric map applied to dJ/d(AQX, AQR, ABX, ABR, ASX, ASR,
+ * VOLOR), through the extrapolation of THETA onto the mixing planes
+ * (3025).  Computed on the device. */
+int32_t mgpu_adjoint_gradient_theta(mgpu_handle *h, float *djdtheta, int64_t nbytes);
 /* The adjoint of a state array by its COMMON name (RO, ROVX, ROVR, RORVT,
  * ROE, DRO, DROE, DROVX, DROVR, DRORVT, P, HO, ROVT, PEFF, PD), or, with a
  * "d" prefix (dAQX ...), the geometry gradient of mgpu_adjoint_gradient.

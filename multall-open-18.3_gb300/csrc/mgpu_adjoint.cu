@@ -1929,6 +1929,94 @@ __global__ void rk_kaxpby(float a_, const float *x, float b_, float *y, size_t l
         y[t] = a_ * x[t] + b_ * y[t];
 }
 
+// =====================================================================
+// SETUP's face areas and volumes (3030-4045) transposed: with the node
+// coordinates X, R fixed they are linear in THETA, so dJ/dTHETA is the
+// transposed map applied to dJ/d(AQX, AQR, ABX, ABR, ASX, ASR, VOLOR).
+// One thread per node owns the faces whose corner (I, J, K) it is and
+// scatters its THETA terms with atomics (once per gradient, not per step).
+// On the planes after a mixing plane the areas read the downstream THETA
+// extrapolated onto the mixing plane (3025):
+//   TH(JMIX) = TH(JMIX+1) + DS(JMIX+1)/DS(JMIX+2) (TH(JMIX+1) - TH(JMIX+2)).
+// =====================================================================
+__device__ __forceinline__ void th_add(const Dev &d, float *gth, int i, int j, int k, float g) {
+    if (g != 0.0f) atomicAdd(&gth[ix3(d, i, j, k)], g);
+}
+// an adjoint of THETA at plane jm = J-1 as the areas of plane J read it
+__device__ __forceinline__ void thm_add(const Dev &d, float *gth, int i, int jm, int k, float g) {
+    if (g == 0.0f) return;
+    if (A1(d.INDMIX, jm) == 1) {
+        const float fac = A2(d.DS, jm + 1, k) / A2(d.DS, jm + 2, k);
+        th_add(d, gth, i, jm + 1, k, (1.0f + fac) * g);
+        th_add(d, gth, i, jm + 2, k, -fac * g);
+    } else {
+        th_add(d, gth, i, jm, k, g);
+    }
+}
+
+__global__ void rk_metrics(const Dev d, const Adj a, float *gth) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = d.IM * d.JM * d.KM;
+    if (n >= N) return;
+    int i, j, k;
+    node_ijk(d, (size_t)n, i, j, k);
+    const int IM = d.IM, KM = d.KM, IMM1 = d.IMM1, KMM1 = d.KMM1, JM = d.JM;
+    // VOLOR = -RAREA/8, RAREA = ABR(i) - ABR(i+1) + AQR(j) - AQR(j-1) + ASR(k) - ASR(k+1)
+    auto gv = [&](int ii, int jj, int kk) -> float {
+        if (ii < 1 || ii > IMM1 || jj < 2 || jj > JM || kk < 1 || kk > KMM1) return 0.0f;
+        return A3(a.gVOLOR, ii, jj, kk);
+    };
+    // faces K = const, i <= IMM1, k <= KMM1 (AQX, AQR; K = KM and I = IM copy them)
+    if (i <= IMM1 && k <= KMM1) {
+        float gx = A3(a.gAQX, i, j, k), gr = A3(a.gAQR, i, j, k);
+        if (k == KMM1) { gx += A3(a.gAQX, i, j, KM); gr += A3(a.gAQR, i, j, KM); }
+        if (i == IMM1) { gx += A3(a.gAQX, IM, j, k); gr += A3(a.gAQR, IM, j, k); }
+        if (i == IMM1 && k == KMM1) { gx += A3(a.gAQX, IM, j, KM); gr += A3(a.gAQR, IM, j, KM); }
+        gr += -0.125f * gv(i, j, k) + 0.125f * gv(i, j + 1, k);
+        const float R1 = A2(d.R, j, k + 1) - A2(d.R, j, k), X1 = A2(d.X, j, k + 1) - A2(d.X, j, k);
+        // AQX = -(R1 T1 - R1 T2)/2, AQR = -(X1 T2 - X1 T1)/2
+        const float gT1 = -0.5f * R1 * gx + 0.5f * X1 * gr, gT2 = 0.5f * R1 * gx - 0.5f * X1 * gr;
+        const float rk1 = A2(d.R, j, k + 1), rk = A2(d.R, j, k);
+        // T1 = R(j,k+1) (TH(i+1,j,k+1) - TH(i,j,k))
+        // T2 = R(j,k+1) (TH(i,j,k+1) - TH(i,j,k)) - R(j,k) (TH(i+1,j,k) - TH(i,j,k))
+        th_add(d, gth, i + 1, j, k + 1, rk1 * gT1);
+        th_add(d, gth, i, j, k + 1, rk1 * gT2);
+        th_add(d, gth, i + 1, j, k, -rk * gT2);
+        th_add(d, gth, i, j, k, -rk1 * gT1 + (rk - rk1) * gT2);
+    }
+    // faces I = const, j >= 2, k <= KMM1 (ABX, ABR)
+    if (j >= 2 && k <= KMM1) {
+        const float gx = A3(a.gABX, i, j, k);
+        const float gr = A3(a.gABR, i, j, k) - 0.125f * gv(i, j, k) + 0.125f * gv(i - 1, j, k);
+        const float bx1 = A2(d.X, j - 1, k + 1) - A2(d.X, j, k), bx2 = A2(d.X, j, k + 1) - A2(d.X, j - 1, k);
+        const float br1 = A2(d.R, j - 1, k + 1) - A2(d.R, j, k), br2 = A2(d.R, j, k + 1) - A2(d.R, j - 1, k);
+        // ABX = -(br1 T2 - br2 T1)/2, ABR = -(bx2 T1 - bx1 T2)/2
+        const float gT1 = 0.5f * br2 * gx - 0.5f * bx2 * gr, gT2 = -0.5f * br1 * gx + 0.5f * bx1 * gr;
+        const float rm1kp = A2(d.R, j - 1, k + 1), rjkp = A2(d.R, j, k + 1), rm1k = A2(d.R, j - 1, k);
+        // T1 = R(j-1,k+1) (THm(i,j-1,k+1) - TH(i,j,k))
+        // T2 = R(j,k+1) (TH(i,j,k+1) - TH(i,j,k)) - R(j-1,k) (THm(i,j-1,k) - TH(i,j,k))
+        thm_add(d, gth, i, j - 1, k + 1, rm1kp * gT1);
+        th_add(d, gth, i, j, k + 1, rjkp * gT2);
+        thm_add(d, gth, i, j - 1, k, -rm1k * gT2);
+        th_add(d, gth, i, j, k, -rm1kp * gT1 + (rm1k - rjkp) * gT2);
+    }
+    // faces J = const, j >= 2, i <= IMM1 (ASX, ASR)
+    if (j >= 2 && i <= IMM1) {
+        const float gx = A3(a.gASX, i, j, k);
+        const float gr = A3(a.gASR, i, j, k) - 0.125f * gv(i, j, k) + 0.125f * gv(i, j, k - 1);
+        const float sx1 = A2(d.X, j - 1, k) - A2(d.X, j, k), sr1 = A2(d.R, j - 1, k) - A2(d.R, j, k);
+        // ASX = (sr1 T2 - sr1 T1)/2, ASR = (sx1 T1 - sx1 T2)/2
+        const float gT1 = -0.5f * sr1 * gx + 0.5f * sx1 * gr, gT2 = 0.5f * sr1 * gx - 0.5f * sx1 * gr;
+        const float rm1 = A2(d.R, j - 1, k), rj = A2(d.R, j, k);
+        // T1 = R(j-1,k) (THm(i,j-1,k) - TH(i,j,k)) - R(j,k) (TH(i+1,j,k) - TH(i,j,k))
+        // T2 = R(j-1,k) (THm(i+1,j-1,k) - TH(i,j,k))
+        thm_add(d, gth, i, j - 1, k, rm1 * gT1);
+        th_add(d, gth, i + 1, j, k, -rj * gT1);
+        thm_add(d, gth, i + 1, j - 1, k, rm1 * gT2);
+        th_add(d, gth, i, j, k, (rj - rm1) * gT1 - rm1 * gT2);
+    }
+}
+
 struct AdjState {
     mgpu_handle *h = nullptr;
     Adj a;
@@ -2618,6 +2706,24 @@ int32_t mgpu_adjoint_gradient(mgpu_handle *h) {
     ag.geom = 1;
     enqueue_reverse(d, ag, st);
     ACK(cudaGetLastError());
+    ACK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int32_t mgpu_adjoint_gradient_theta(mgpu_handle *h, float *djdtheta, int64_t nbytes) {
+    AdjState *s = ready_state(h);
+    if (!s || !djdtheta) return api_fail(MGPU_E_STATE, "adjoint THETA gradient before mgpu_adjoint_prepare");
+    const Dev &d = handle_dev(h);
+    const size_t N = (size_t)d.IM * d.JM * d.KM;
+    if ((int64_t)(N * sizeof(float)) != nbytes) return api_fail(MGPU_E_ARG, "THETA gradient size mismatch");
+    cudaStream_t st = handle_view(h).stream;
+    float *gth = nullptr;
+    ACK(cudaMallocAsync((void **)&gth, N * sizeof(float), st));
+    ACK(cudaMemsetAsync(gth, 0, N * sizeof(float), st));
+    rk_metrics<<<gridn(N, 256), 256, 0, st>>>(d, s->a, gth);
+    ACK(cudaGetLastError());
+    ACK(cudaMemcpyAsync(djdtheta, gth, N * sizeof(float), cudaMemcpyDeviceToHost, st));
+    ACK(cudaFreeAsync(gth, st));
     ACK(cudaStreamSynchronize(st));
     return 0;
 }

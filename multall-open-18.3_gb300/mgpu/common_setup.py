@@ -47,10 +47,11 @@ def _intp(n, xs, ys, x):
 
 
 def build_common(spec: CaseSpec, geo: CaseGeometry | None = None, metrics64: bool = False,
-                 metrics_only: bool = False) -> CommonData:
+                 metrics_only: bool = False, theta_only: bool = False) -> CommonData:
     """The COMMON state SETUP leaves for the loop.  metrics64: also keep the
     face areas and volumes computed in double precision in cd.geom64;
-    metrics_only: stop there (cd holds only geom64)."""
+    metrics_only: stop there (cd holds only geom64); theta_only: stop once
+    the node angles THETA (KM, JM, IM) are formed (cd.theta)."""
     if geo is None:
         geo = build_geometry(spec, dtype=np.float64 if metrics64 else f32)
     IM, JM, KM = geo.im, geo.jm, geo.km
@@ -236,6 +237,10 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None, metrics64: boo
     for i in range(2, IM + 1):
         RTHETA[:, :, i - 1] = RTHETA[:, :, i - 2] + dt(FP[i - 2]) * GAP
     THETA = (RTHETA / R[:, :, None]).astype(dt)
+    if theta_only:
+        # the node angles alone (design sensitivities through dJ/dTHETA)
+        cd.theta = THETA
+        return cd
     # meridional distances 3530
     SMERID = np.zeros((KM, JM), dt)
     DR = np.zeros((KM, JM), dt)

@@ -76,6 +76,31 @@ class DesignSpace:
     def geometry64(self, alpha: np.ndarray) -> Dict[str, np.ndarray]:
         return _cs.build_common(self.spec(alpha), metrics64=True, metrics_only=True).geom64
 
+    def theta64(self, alpha: np.ndarray) -> np.ndarray:
+        """The node angles THETA (KM, JM, IM) of the design, double precision."""
+        return _cs.build_common(self.spec(alpha), metrics64=True, theta_only=True).theta
+
+    def theta_sensitivities(self, alpha: np.ndarray, h: float = 1e-3) -> np.ndarray:
+        """dTHETA/d(alpha_i) (size, KM, JM, IM), per degree: central
+        differences of the generator's node angles, without the metrics
+        (on a thread pool for large grids, as sensitivities)."""
+        def one(i):
+            e = np.zeros(self.size)
+            e[i] = h
+            return (self.theta64(alpha + e) - self.theta64(alpha - e)) / (2.0 * h)
+        first = one(0)
+        nt = min(16, os.cpu_count() or 1) if first.size > 100_000 else 1
+        if nt <= 1:
+            return np.stack([first] + [one(i) for i in range(1, self.size)])
+        with ThreadPoolExecutor(nt) as ex:
+            return np.stack([first] + list(ex.map(one, range(1, self.size))))
+
+    @staticmethod
+    def chain_theta(djdtheta: np.ndarray, sens: np.ndarray) -> np.ndarray:
+        """dJ/d(alpha) from dJ/dTHETA (mgpu_adjoint_gradient_theta)."""
+        g = djdtheta.astype(np.float64).ravel()
+        return sens.reshape(sens.shape[0], -1) @ g
+
     def sensitivities(self, alpha: np.ndarray, h: float = 1e-3, threads: int | None = None) -> List[Dict[str, np.ndarray]]:
         """dA/d(alpha_i) per design variable (per degree), central differences
         of the double-precision metrics.  The 2 x size geometry evaluations

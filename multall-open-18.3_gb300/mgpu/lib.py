@@ -56,7 +56,7 @@ EXPORTS = ["mgpu_abi_version", "mgpu_last_error", "mgpu_device_count", "mgpu_cre
            "mgpu_batch_run", "mgpu_batch_bench_steps", "mgpu_adjoint_prepare", "mgpu_adjoint_objective",
            "mgpu_adjoint_iterate", "mgpu_adjoint_solve", "mgpu_adjoint_gradient", "mgpu_adjoint_get",
            "mgpu_adjoint_set", "mgpu_adjoint_solve_krylov", "mgpu_autotune", "mgpu_write_flow_out",
-           "mgpu_read_flow_out", "mgpu_stage_performance"]
+           "mgpu_read_flow_out", "mgpu_stage_performance", "mgpu_adjoint_gradient_theta"]
 
 _lib = None
 
@@ -108,6 +108,7 @@ def load(build: bool = True):
     L.mgpu_autotune.argtypes = [vp, ctypes.POINTER(i32), dp]
     L.mgpu_write_flow_out.argtypes = [vp, cp, vp]
     L.mgpu_stage_performance.argtypes = [vp, i32, ctypes.POINTER(Stage)]
+    L.mgpu_adjoint_gradient_theta.argtypes = [vp, vp, ctypes.c_int64]
     L.mgpu_read_flow_out.argtypes = [vp, cp, ctypes.POINTER(i32)]
     L.mgpu_adjoint_solve_krylov.argtypes = [vp, i32, i32, i32, ctypes.c_double, ctypes.c_double,
                                             ctypes.POINTER(i32), dp]
@@ -316,9 +317,18 @@ class Problem:
                                                    float(stall), ctypes.byref(it), ctypes.byref(r)))
         return rc == 0, it.value, r.value
 
-    def adjoint_gradient(self) -> dict:
-        """dJ/dA for the geometry arrays (one more reverse step)."""
+    def adjoint_gradient_theta(self) -> np.ndarray:
+        """dJ/dTHETA (KM, JM, IM) on the device from the last adjoint_gradient."""
+        out = np.zeros((self.cd.km, self.cd.jm, self.cd.im), np.float32)
+        _chk(load().mgpu_adjoint_gradient_theta(self.h, out.ctypes.data, out.nbytes))
+        return out
+
+    def adjoint_gradient(self, read: bool = True) -> dict | None:
+        """dJ/dA for the geometry arrays (one more reverse step); read=False
+        leaves them on the device (for adjoint_gradient_theta)."""
         _chk(load().mgpu_adjoint_gradient(self.h))
+        if not read:
+            return None
         return {n: self.adjoint_get("d" + n) for n in self.ADJ_GEOM}
 
     def _adj_shape(self, name: str):

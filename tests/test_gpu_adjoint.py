@@ -201,3 +201,24 @@ def test_autograd_wrapper_returns_the_adjoint_gradient(mods):
     assert abs(float(eta) - value) < 1e-12
     assert np.allclose(alpha.grad.numpy(), grad)
     assert np.abs(grad).max() > 0.0
+
+
+def test_theta_gradient_matches_metric_chain(mods):
+    """dJ/dTHETA from the transposed SETUP metrics on the device, chained
+    with the generator's dTHETA/d(alpha), gives the design gradient that
+    dJ/dA chained with the metrics' dA/d(alpha) gives (small stage, with a
+    mixing plane and a tip gap)."""
+    case, common_setup, lib, O = mods
+    from mgpu import design
+    ds = design.DesignSpace.seeded(case.small_stage)
+    alpha = ds.alpha0
+    p = lib.Problem(ds.deck(alpha))
+    p.run(60)
+    p.adjoint_prepare()
+    p.adjoint_objective("eta_tt")
+    p.adjoint_iterate(20)
+    ga = ds.chain(p.adjoint_gradient(), ds.sensitivities(alpha))
+    gt = ds.chain_theta(p.adjoint_gradient_theta(), ds.theta_sensitivities(alpha))
+    scale = float(np.max(np.abs(ga)))
+    assert scale > 0.0
+    assert float(np.max(np.abs(gt - ga))) <= 1e-3 * scale, (ga, gt)
