@@ -197,6 +197,11 @@ int32_t mgpu_write_flow_out(mgpu_handle *h, const char *path, const float *rosub
  * from the restarted flow.  *nstep (may be NULL) receives the file's NSTEP;
  * like LOOP, the step counter itself starts again from the bound NSTEP. */
 int32_t mgpu_read_flow_out(mgpu_handle *h, const char *path, int32_t *nstep);
+/* Writes the plotting file "grid_out" as SETUP writes it (6585-6597): the
+ * records NSTEPS_MAX; IM, JM, KM; CP, GA; INDLETE(J) (1 on the leading- and
+ * trailing-edge planes, 6307-6309); WRAD(J); NBLADE(J); then for each J and
+ * K (K fastest) X, R and RTHETA(1..IM), from the bound COMMON data. */
+int32_t mgpu_write_grid_out(mgpu_handle *h, const char *path);
 
 /* The same integrals as mgpu_integrals_compute, through a path that
  * allocates nothing.  This entry point has no counterpart in the reference

@@ -99,6 +99,54 @@ int32_t mgpu_write_flow_out(mgpu_handle *h, const char *path, const float *rosub
     return 0;
 }
 
+int32_t mgpu_write_grid_out(mgpu_handle *h, const char *path) {
+    if (!h || !path) return api_fail(MGPU_E_ARG, "null argument to mgpu_write_grid_out");
+    const HandleView hv = handle_view(h);
+    const Dims g = dims_of(hv);
+    const size_t njk = (size_t)g.JM * g.KM;
+    int32_t nrows = hv.d->NROWS, nsmax = 0;
+    float CP = 0.0f, GA = 0.0f;
+    std::vector<float> X(njk), R(njk), RT(g.N), WRAD(g.JM);
+    std::vector<int32_t> INDLE(g.JM), NBLADE(g.JM), JTE(nrows);
+    int rc = 0;
+    if ((rc = mgpu_get_int(h, "NSTEPS_MAX", &nsmax)) || (rc = mgpu_get_real(h, "CP", &CP)) ||
+        (rc = mgpu_get_real(h, "GA", &GA)) || (rc = mgpu_get_array(h, "X", X.data(), (int64_t)njk * 4)) ||
+        (rc = mgpu_get_array(h, "R", R.data(), (int64_t)njk * 4)) ||
+        (rc = mgpu_get_array(h, "RTHETA", RT.data(), (int64_t)g.N * 4)) ||
+        (rc = mgpu_get_array(h, "WRAD", WRAD.data(), (int64_t)g.JM * 4)) ||
+        (rc = mgpu_get_array(h, "INDLE", INDLE.data(), (int64_t)g.JM * 4)) ||
+        (rc = mgpu_get_array(h, "NBLADE", NBLADE.data(), (int64_t)g.JM * 4)) ||
+        (rc = mgpu_get_array(h, "JTE", JTE.data(), (int64_t)nrows * 4)))
+        return rc;
+    // INDLETE (6307-6309): 1 on the leading- and trailing-edge planes
+    std::vector<int32_t> INDLETE(g.JM, 0);
+    for (int j = 1; j <= g.JM; ++j)
+        if (INDLE[j - 1] == 1) INDLETE[j - 1] = 1;
+    for (int nr = 0; nr < nrows; ++nr)
+        if (JTE[nr] >= 1 && JTE[nr] <= g.JM) INDLETE[JTE[nr] - 1] = 1;
+    FileCloser fc;
+    fc.f = fopen(path, "wb");
+    if (!fc.f) return api_fail(MGPU_E_ARG, (std::string("cannot open for writing: ") + path).c_str());
+    // 6587-6597
+    const int32_t dims[3] = {g.IM, g.JM, g.KM};
+    const float gas[2] = {CP, GA};
+    const uint32_t nj = (uint32_t)g.JM * 4;
+    bool ok = put_record(fc.f, &nsmax, 4) && put_record(fc.f, dims, 12) && put_record(fc.f, gas, 8) &&
+              put_record(fc.f, INDLETE.data(), nj) && put_record(fc.f, WRAD.data(), nj) &&
+              put_record(fc.f, NBLADE.data(), nj);
+    std::vector<float> rec((size_t)g.IM + 2);
+    for (int j = 1; j <= g.JM && ok; ++j)
+        for (int k = 1; k <= g.KM && ok; ++k) {
+            const size_t jk = (size_t)(j - 1) + (size_t)g.JM * (size_t)(k - 1);
+            rec[0] = X[jk];
+            rec[1] = R[jk];
+            for (int i = 1; i <= g.IM; ++i) rec[(size_t)i + 1] = RT[(size_t)(i - 1) + (size_t)g.IM * jk];
+            ok = put_record(fc.f, rec.data(), (uint32_t)rec.size() * 4);
+        }
+    if (!ok || fflush(fc.f) != 0) return api_fail(MGPU_E_ARG, (std::string("write failed: ") + path).c_str());
+    return 0;
+}
+
 int32_t mgpu_read_flow_out(mgpu_handle *h, const char *path, int32_t *nstep) {
     if (!h || !path) return api_fail(MGPU_E_ARG, "null argument to mgpu_read_flow_out");
     const HandleView hv = handle_view(h);

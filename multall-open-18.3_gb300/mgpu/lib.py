@@ -56,7 +56,8 @@ EXPORTS = ["mgpu_abi_version", "mgpu_last_error", "mgpu_device_count", "mgpu_cre
            "mgpu_batch_run", "mgpu_batch_bench_steps", "mgpu_adjoint_prepare", "mgpu_adjoint_objective",
            "mgpu_adjoint_iterate", "mgpu_adjoint_solve", "mgpu_adjoint_gradient", "mgpu_adjoint_get",
            "mgpu_adjoint_set", "mgpu_adjoint_solve_krylov", "mgpu_autotune", "mgpu_write_flow_out",
-           "mgpu_read_flow_out", "mgpu_stage_performance", "mgpu_adjoint_gradient_theta"]
+           "mgpu_read_flow_out", "mgpu_stage_performance", "mgpu_adjoint_gradient_theta",
+           "mgpu_write_grid_out"]
 
 _lib = None
 
@@ -107,6 +108,7 @@ def load(build: bool = True):
     L.mgpu_adjoint_gradient.argtypes = [vp]
     L.mgpu_autotune.argtypes = [vp, ctypes.POINTER(i32), dp]
     L.mgpu_write_flow_out.argtypes = [vp, cp, vp]
+    L.mgpu_write_grid_out.argtypes = [vp, cp]
     L.mgpu_stage_performance.argtypes = [vp, i32, ctypes.POINTER(Stage)]
     L.mgpu_adjoint_gradient_theta.argtypes = [vp, vp, ctypes.c_int64]
     L.mgpu_read_flow_out.argtypes = [vp, cp, ctypes.POINTER(i32)]
@@ -190,6 +192,10 @@ class Problem:
         if rosub is not None:
             rosub = np.ascontiguousarray(rosub, np.float32)
         _chk(load().mgpu_write_flow_out(self.h, os.fsencode(path), None if rosub is None else rosub.ctypes.data))
+
+    def write_grid_out(self, path: str):
+        """SETUP's plotting file grid_out of the bound geometry."""
+        _chk(load().mgpu_write_grid_out(self.h, os.fsencode(path)))
 
     def setup_calls(self):
         """STEPUP(1.0) and the first LOSS, as SETUP makes them."""

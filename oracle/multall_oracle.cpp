@@ -98,6 +98,7 @@ struct OracleBase {
        IF_RESTART branch 6920-6992) */
     virtual int write_flow_out(const char *, const float *) { return fail(MGPU_E_STATE, "flow_out needs a REAL oracle"); }
     virtual int read_flow_out(const char *, int *) { return fail(MGPU_E_STATE, "flow_out needs a REAL oracle"); }
+    virtual int write_grid_out(const char *) { return fail(MGPU_E_STATE, "grid_out needs a REAL oracle"); }
 };
 
 /* gfortran's sequential unformatted records: the payload between two copies
@@ -288,6 +289,37 @@ struct Oracle : OracleBase {
             return ok ? 0 : fail(MGPU_E_ARG, std::string("write failed: ") + path);
         }
     }
+    /* SETUP's plotting file grid_out (6585-6597) */
+    int write_grid_out(const char *path) override {
+        if constexpr (!kPlainReal) {
+            return fail(MGPU_E_STATE, "grid_out needs a REAL oracle");
+        } else {
+            std::vector<int32_t> INDLETE(JM, 0);     /* 6307-6309 */
+            for (int j = 1; j <= JM; ++j)
+                if (INDLE_v[j - 1] == 1) INDLETE[j - 1] = 1;
+            for (int nr = 0; nr < NROWS; ++nr)
+                if (JTE_v[nr] >= 1 && JTE_v[nr] <= JM) INDLETE[JTE_v[nr] - 1] = 1;
+            FILE *f = fopen(path, "wb");
+            if (!f) return fail(MGPU_E_ARG, std::string("cannot open for writing: ") + path);
+            const int32_t ns = NSTEPS_MAX, dims[3] = {IM, JM, KM};
+            const R gas[2] = {CP, GA};
+            const std::vector<int32_t> nb(NBLADE_v.begin(), NBLADE_v.end());
+            bool ok = fo_put(f, &ns, 4) && fo_put(f, dims, 12) && fo_put(f, gas, 2 * sizeof(R)) &&
+                      fo_put(f, INDLETE.data(), (uint32_t)JM * 4) && fo_put(f, WRAD_v.data(), (uint32_t)(JM * sizeof(R))) &&
+                      fo_put(f, nb.data(), (uint32_t)JM * 4);
+            std::vector<R> rec((size_t)IM + 2);
+            for (int j = 1; j <= JM && ok; ++j)
+                for (int k = 1; k <= KM && ok; ++k) {
+                    rec[0] = F2(X, j, k);
+                    rec[1] = F2(R, j, k);
+                    for (int i = 1; i <= IM; ++i) rec[(size_t)i + 1] = F3(RTHETA, i, j, k);
+                    ok = fo_put(f, rec.data(), (uint32_t)(rec.size() * sizeof(R)));
+                }
+            ok = fclose(f) == 0 && ok;
+            return ok ? 0 : fail(MGPU_E_ARG, std::string("write failed: ") + path);
+        }
+    }
+
     int read_flow_out(const char *path, int *nstep) override {
         if constexpr (!kPlainReal) {
             return fail(MGPU_E_STATE, "flow_out needs a REAL oracle");
@@ -2446,6 +2478,7 @@ int64_t oref_ad_tape_size(void *h) { return ((OracleBase *)h)->ad_tape_size(); }
 int32_t oref_write_flow_out(void *h, const char *path, const float *rosub) {
     return ((OracleBase *)h)->write_flow_out(path, rosub);
 }
+int32_t oref_write_grid_out(void *h, const char *path) { return ((OracleBase *)h)->write_grid_out(path); }
 int32_t oref_read_flow_out(void *h, const char *path, int32_t *nstep) {
     return ((OracleBase *)h)->read_flow_out(path, nstep);
 }

@@ -87,12 +87,13 @@ def lib():
         L.oref_ad_tape_size.restype = ctypes.c_int64
         L.oref_write_flow_out.argtypes = [vp, cp, vp]
         L.oref_stage_performance.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(Stage)]
+        L.oref_write_grid_out.argtypes = [vp, cp]
         L.oref_read_flow_out.argtypes = [vp, cp, ctypes.POINTER(ctypes.c_int32)]
         for f in ("oref_set_int", "oref_set_real", "oref_get_real", "oref_get_int", "oref_set_array",
                   "oref_get_array", "oref_commit", "oref_stepup", "oref_loss_init", "oref_step",
                   "oref_integrals", "oref_set_array_f64", "oref_ad_begin", "oref_ad_zero", "oref_ad_seed",
                   "oref_ad_reverse", "oref_ad_grad", "oref_write_flow_out", "oref_read_flow_out",
-                  "oref_stage_performance"):
+                  "oref_stage_performance", "oref_write_grid_out"):
             getattr(L, f).restype = ctypes.c_int32
         _lib = L
     return _lib
@@ -135,6 +136,10 @@ class Oracle:
         o = Stage()
         self._chk(lib().oref_stage_performance(self.h, int(nstg), ctypes.byref(o)))
         return o
+
+    def write_grid_out(self, path: str):
+        """SETUP's plotting file grid_out (6585-6597) of the bound geometry."""
+        self._chk(lib().oref_write_grid_out(self.h, os.fsencode(path)))
 
     def write_flow_out(self, path: str, rosub: np.ndarray | None = None):
         """OUTPUT's restart/plotting file flow_out (5942-5978) of the state."""

@@ -352,3 +352,39 @@ def test_stage_table_stations_and_whole_machine(mods):
         assert getattr(whole, f) == getattr(ig, f), f
     with pytest.raises(O.OracleError):
         ref.stage(ns + 2)
+
+
+def test_grid_out_follows_setup(mods, tmp_path):
+    """SETUP's plotting file grid_out (multall-open-18.3.f:6585-6597) from the
+    FP32 oracle: NSTEPS_MAX; IM, JM, KM; CP, GA; INDLETE; WRAD; NBLADE; then
+    X, R and RTHETA(1..IM) per (J, K) with K fastest, each a gfortran record."""
+    case, common_setup, O = mods
+    cd = common_setup.build_common(case.small_stage())
+    ref = O.Oracle(cd)
+    f = str(tmp_path / "grid_out")
+    ref.write_grid_out(f)
+    raw = open(f, "rb").read()
+    recs, pos = [], 0
+    while pos < len(raw):
+        m = int(np.frombuffer(raw, np.int32, 1, pos)[0])
+        assert int(np.frombuffer(raw, np.int32, 1, pos + 4 + m)[0]) == m
+        recs.append(raw[pos + 4: pos + 4 + m])
+        pos += m + 8
+    im, jm, km = cd.im, cd.jm, cd.km
+    assert len(recs) == 6 + jm * km
+    assert np.frombuffer(recs[0], np.int32)[0] == cd.ints["NSTEPS_MAX"]
+    assert list(np.frombuffer(recs[1], np.int32)) == [im, jm, km]
+    assert np.array_equal(np.frombuffer(recs[2], np.float32), np.float32([cd.reals["CP"], cd.reals["GA"]]))
+    indlete = np.zeros(jm, np.int32)
+    indlete[cd.arrays["INDLE"].ravel() == 1] = 1
+    indlete[cd.arrays["JTE"].ravel() - 1] = 1
+    assert np.array_equal(np.frombuffer(recs[3], np.int32), indlete)
+    assert np.array_equal(np.frombuffer(recs[4], np.float32), cd.arrays["WRAD"].ravel())
+    assert np.array_equal(np.frombuffer(recs[5], np.int32), cd.arrays["NBLADE"].ravel())
+    X = cd.arrays["X"].reshape(km, jm)
+    R = cd.arrays["R"].reshape(km, jm)
+    RT = cd.arrays["RTHETA"].reshape(km, jm, im)
+    for j in (0, jm // 2, jm - 1):
+        for k in (0, km - 1):
+            rec = np.frombuffer(recs[6 + j * km + k], np.float32)
+            assert rec[0] == X[k, j] and rec[1] == R[k, j] and np.array_equal(rec[2:], RT[k, j])

@@ -119,3 +119,16 @@ def test_stage_table_matches_oracle(mods):
             assert abs(getattr(g, f) - getattr(r, f)) <= 1e-4 * abs(getattr(r, f)), (s, f)
         for f in ("eta_tt", "eta_ts", "eta_poly", "reac_hub", "reac_mid", "reac_tip"):
             assert abs(getattr(g, f) - getattr(r, f)) <= 1e-3, (s, f, getattr(g, f), getattr(r, f))
+
+
+def test_grid_out_matches_oracle(mods, tmp_path):
+    """grid_out holds only bound constants, so the GPU's file is the
+    oracle's byte for byte."""
+    case, common_setup, lib, O = mods
+    cd = common_setup.build_common(case.small_stage())
+    gpu = lib.Problem(cd, setup_calls=False)
+    ref = O.Oracle(cd)
+    fg, fr = str(tmp_path / "gpu_grid_out"), str(tmp_path / "ref_grid_out")
+    gpu.write_grid_out(fg)
+    ref.write_grid_out(fr)
+    assert open(fg, "rb").read() == open(fr, "rb").read()
