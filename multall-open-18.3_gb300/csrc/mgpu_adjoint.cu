@@ -1394,14 +1394,35 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_gather(const __grid_constant__ De
     const int nc = IMM1 * KMM1;
     float *av = sm;
     const float fdn = A1(d.FACDWN, jc), fup = A1(d.FACUP, jc);
-    for (int c = threadIdx.x; c < nc; c += RT_BS) {
-        const int i = c % IMM1 + 1, k = c / IMM1 + 1;
-        auto tm = [&](int ii, int jj, int kk) { return A3(V.TM, ii, jj, kk); };
-        float s = AIK(d.FBL, i, k) * (fdn * tm(i, jc, k) + fup * tm(i, jc - 1, k));
-        s += AIK(d.FBR, i, k) * (fdn * tm(i + 1, jc, k) + fup * tm(i + 1, jc - 1, k));
-        s += AIK(d.FTL, i, k) * (fdn * tm(i, jc, k + 1) + fup * tm(i, jc - 1, k + 1));
-        s += AIK(d.FTR, i, k) * (fdn * tm(i + 1, jc, k + 1) + fup * tm(i + 1, jc - 1, k + 1));
-        av[c] = s;
+    // RT_U cells at a time, their loads issued together
+    for (int c0 = threadIdx.x; c0 < nc; c0 += RT_U * RT_BS) {
+        float tA[RT_U][4], tB[RT_U][4], wt[RT_U][4];
+#pragma unroll
+        for (int u = 0; u < RT_U; ++u) {
+            const int c = c0 + u * RT_BS;
+            if (c >= nc) continue;
+            const int i = c % IMM1 + 1, k = c / IMM1 + 1;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int ii = i + (q & 1), kk = k + (q >> 1);   // (i,k) (i+1,k) (i,k+1) (i+1,k+1)
+                tA[u][q] = A3(V.TM, ii, jc, kk);
+                tB[u][q] = A3(V.TM, ii, jc - 1, kk);
+            }
+            wt[u][0] = AIK(d.FBL, i, k);
+            wt[u][1] = AIK(d.FBR, i, k);
+            wt[u][2] = AIK(d.FTL, i, k);
+            wt[u][3] = AIK(d.FTR, i, k);
+        }
+#pragma unroll
+        for (int u = 0; u < RT_U; ++u) {
+            const int c = c0 + u * RT_BS;
+            if (c >= nc) continue;
+            float s = wt[u][0] * (fdn * tA[u][0] + fup * tB[u][0]);
+            s += wt[u][1] * (fdn * tA[u][1] + fup * tB[u][1]);
+            s += wt[u][2] * (fdn * tA[u][2] + fup * tB[u][2]);
+            s += wt[u][3] * (fdn * tA[u][3] + fup * tB[u][3]);
+            av[c] = s;
+        }
     }
     __syncthreads();
     // second mixing-plane average (1850): a row set to its mean
@@ -1602,14 +1623,37 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_cells(const __grid_constant__ Dev
     }
     __syncthreads();
     const float SB = s_sb, SSB = A1(d.STEPSBK, jsb);
-    for (int c = threadIdx.x; c < nc; c += RT_BS) {
-        const int i = c % IMM1 + 1, k = c / IMM1 + 1;
-        const int n = ix3(d, i, j, k);
-        const int i1 = A1(d.IB1, i), i2 = A1(d.IB2, i), k1 = A1(d.KB1, k), k2 = A1(d.KB2, k);
-        const size_t s1 = (size_t)(i1 - 1) + (size_t)d.NIB1 * (j1 - 1) + m1 * (k1 - 1);
-        const size_t s2 = (size_t)(i2 - 1) + (size_t)d.NIB2 * (j2 - 1) + m2 * (k2 - 1);
-        st[c] = V.ST[n] * d.STEP[n] + b1[(k1 - 1) * d.NIB1 + (i1 - 1)] * d.STEP1[s1] +
-                b2[(k2 - 1) * d.NIB2 + (i2 - 1)] * d.STEP2[s2] + SB * SSB;
+    // RT_U cells at a time: their block indices, then their operands, are
+    // loaded together
+    for (int c0 = threadIdx.x; c0 < nc; c0 += RT_U * RT_BS) {
+        int i1[RT_U], i2[RT_U], k1[RT_U], k2[RT_U], nn[RT_U];
+        float vs[RT_U], vp[RT_U], v1[RT_U], v2[RT_U];
+#pragma unroll
+        for (int u = 0; u < RT_U; ++u) {
+            const int c = c0 + u * RT_BS;
+            if (c >= nc) continue;
+            const int i = c % IMM1 + 1, k = c / IMM1 + 1;
+            nn[u] = ix3(d, i, j, k);
+            i1[u] = A1(d.IB1, i); i2[u] = A1(d.IB2, i); k1[u] = A1(d.KB1, k); k2[u] = A1(d.KB2, k);
+        }
+#pragma unroll
+        for (int u = 0; u < RT_U; ++u) {
+            const int c = c0 + u * RT_BS;
+            if (c >= nc) continue;
+            const size_t s1 = (size_t)(i1[u] - 1) + (size_t)d.NIB1 * (j1 - 1) + m1 * (k1[u] - 1);
+            const size_t s2 = (size_t)(i2[u] - 1) + (size_t)d.NIB2 * (j2 - 1) + m2 * (k2[u] - 1);
+            vs[u] = V.ST[nn[u]];
+            vp[u] = d.STEP[nn[u]];
+            v1[u] = d.STEP1[s1];
+            v2[u] = d.STEP2[s2];
+        }
+#pragma unroll
+        for (int u = 0; u < RT_U; ++u) {
+            const int c = c0 + u * RT_BS;
+            if (c >= nc) continue;
+            st[c] = vs[u] * vp[u] + b1[(k1[u] - 1) * d.NIB1 + (i1[u] - 1)] * v1[u] +
+                    b2[(k2[u] - 1) * d.NIB2 + (i2[u] - 1)] * v2[u] + SB * SSB;
+        }
     }
     __syncthreads();
     // mixing-plane pitchwise redistribution (1750): row <- (sum of row) FP(I)
