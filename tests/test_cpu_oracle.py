@@ -388,3 +388,16 @@ def test_grid_out_follows_setup(mods, tmp_path):
         for k in (0, km - 1):
             rec = np.frombuffer(recs[6 + j * km + k], np.float32)
             assert rec[0] == X[k, j] and rec[1] == R[k, j] and np.array_equal(rec[2:], RT[k, j])
+
+
+def test_flow_out_of_another_grid_is_refused(mods, tmp_path):
+    """A restart file of another grid is refused (the record lengths do not
+    match), before anything of the new problem is changed."""
+    case, common_setup, O = mods
+    cd = common_setup.build_common(case.small_stage())
+    ref = O.Oracle(cd)
+    f = str(tmp_path / "flow_out")
+    ref.write_flow_out(f)
+    other = common_setup.build_common(case.small_nozzle())
+    with pytest.raises(O.OracleError, match="not a flow_out file of this grid"):
+        O.Oracle(other, restart=f)

@@ -132,3 +132,14 @@ def test_grid_out_matches_oracle(mods, tmp_path):
     gpu.write_grid_out(fg)
     ref.write_grid_out(fr)
     assert open(fg, "rb").read() == open(fr, "rb").read()
+
+
+def test_flow_out_of_another_grid_is_refused(mods, tmp_path):
+    case, common_setup, lib, O = mods
+    cd = common_setup.build_common(case.small_stage())
+    ref = O.Oracle(cd)
+    f = str(tmp_path / "flow_out")
+    ref.write_flow_out(f)
+    other = common_setup.build_common(case.small_nozzle())
+    with pytest.raises(lib.MgpuError):
+        lib.Problem(other, restart=f)
