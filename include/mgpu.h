@@ -156,10 +156,13 @@ int32_t mgpu_loss_init(mgpu_handle *h);
  * mon may be NULL.  Returns MGPU_E_NONFINITE if the tail's health check
  * finds a NaN/Inf or a non-positive density. */
 int32_t mgpu_step(mgpu_handle *h, int32_t force_end, mgpu_monitors *mon);
-/* nsteps LOOP iterations launched back to back (CUDA graph replay), no
- * host synchronisation in between; mon receives the last tail's values.
- * Stops early, returning 1, if the reference's convergence test
- * (multall-open-18.3.f:3762-3764) is met at a tail. */
+/* Up to nsteps LOOP iterations (CUDA graph replay); mon receives the last
+ * tail's values.  The steps between two tails are launched back to back and
+ * the control block is read once per tail.  Returns 1 right after the final
+ * step (IFEND: the convergence test of multall-open-18.3.f:3762-3764 met at
+ * a tail, or NSTEP reaching NSTEPS_MAX), where LOOP stops (5444-5451), and
+ * at once, without stepping, on a handle whose final step has run; 0 when
+ * all nsteps ran without reaching it. */
 int32_t mgpu_run(mgpu_handle *h, int32_t nsteps, mgpu_monitors *mon);
 /* Bytes one mgpu_step() call moves between host and device: the
  * end-of-run flag it sends and the control block (monitors) it reads back. */

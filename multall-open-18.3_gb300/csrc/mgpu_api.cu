@@ -865,19 +865,32 @@ int32_t mgpu_run(mgpu_handle *h, int32_t nsteps, mgpu_monitors *mon) {
     if (nsteps < 0) return fail(MGPU_E_ARG, "negative step count");
     int rc = build_graph(h);
     if (rc) return rc;
-    const int chunk = 50;
+    // The end test at the top of step n (3762-3764) reads NSTEP and the
+    // monitors EMAX, EAVG and ECONT, which only a tail (every fifth step, or
+    // the final one) rewrites.  So no step after a tail up to and including
+    // the next tail can be the final one unless that tail met the test or
+    // NSTEPS_MAX falls among them: such a run of steps is launched back to
+    // back, then the control block is read, and the run stops right after
+    // the final step, where LOOP stops (5444-5451).
+    if ((rc = read_ctl(h))) return rc;
     int done = 0;
-    while (done < nsteps) {
-        int n = nsteps - done < chunk ? nsteps - done : chunk;
+    for (;;) {
+        const DevCtl &c = *h->h_ctl;
+        if (mon) fill_monitors(c, mon);
+        if (done > 0 && c.health) return fail(MGPU_E_NONFINITE, "non-finite or non-positive density in the flow field");
+        if (c.ifend) return 1;
+        if (done >= nsteps) return 0;
+        const int n0 = c.nstep;
+        int n = 1;                              // a met test makes the next step the final one
+        if (!c.converged) {
+            n = (n0 / 5 + 1) * 5 - n0;          // up to the next tail
+            if (h->d.NSTEPS_MAX > n0 && h->d.NSTEPS_MAX - n0 < n) n = h->d.NSTEPS_MAX - n0;
+        }
+        if (n > nsteps - done) n = nsteps - done;
         for (int s = 0; s < n; ++s) CK(cudaGraphLaunch(h->gexec, h->stream));
         done += n;
         if ((rc = read_ctl(h))) return rc;
-        const DevCtl &c = *h->h_ctl;
-        if (mon) fill_monitors(c, mon);
-        if (c.health) return fail(MGPU_E_NONFINITE, "non-finite or non-positive density in the flow field");
-        if (c.converged || c.ifend) return 1;
     }
-    return 0;
 }
 
 int32_t mgpu_step_io_bytes(int32_t *h2d, int32_t *d2h) {

@@ -294,6 +294,31 @@ def test_precision_split_against_fp64_oracle(mods):
         assert em <= 1e-4 and ee <= 1e-4, (order, em, ee)
 
 
+@pytest.mark.parametrize("limit", ["nsteps_max", "conlim"])
+def test_run_stops_after_the_final_step(mods, limit):
+    """mgpu_run stops right after the step on which IFEND is set, where LOOP
+    stops: NSTEP reaching NSTEPS_MAX (12, between two tails) or the
+    convergence test met at a tail (CONLIM=1e3, so ECONT < 0.01 decides; the
+    oracle's ECONT is 0.0104 at the tail of step 340 and 0.0096 at 345, so
+    step 346 is the final one).  The state is the oracle's after the same
+    final step, and a further run returns at once without stepping."""
+    case = mods[0]
+    over, final, tol = ({"NSTEPS_MAX": 12}, 12, 1e-4) if limit == "nsteps_max" else ({"CONLIM": 1e3}, 346, 1e-3)
+    cd, gpu, ref = _pair(mods, case.small_stage(), **over)
+    rc, mg = gpu.run(1000)
+    for _ in range(1000):
+        mr = ref.step()
+        if mr.ifend:
+            break
+    assert mr.nstep == final and mr.tail_ran == 1
+    assert rc == 1 and mg.ifend == 1 and mg.tail_ran == 1 and mg.nstep == final
+    _compare(gpu, ref, STATE, tol, f"final step {final}")
+    ro = gpu.get("RO")
+    rc2, m2 = gpu.run(10)
+    assert rc2 == 1 and m2.nstep == final
+    assert np.array_equal(gpu.get("RO"), ro)
+
+
 def test_deterministic(mods):
     """Two runs of the same case are bitwise identical (no float atomics)."""
     case = mods[0]
