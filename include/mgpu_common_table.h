@@ -106,6 +106,8 @@
     M_(YPTURB,    25.0f)                                                  \
     M_(CFWALL,    0.0f)                                                   \
     M_(FACMIXUP,  2.0f)                                                   \
+    M_(VORT_MAX,  0.0f)                                                   \
+    M_(TURBVIS_LIM, 3000.0f)                                              \
     M_(PDOWN_HUB, MGPU_REQUIRED_REAL)                                     \
     M_(PDOWN_TIP, MGPU_REQUIRED_REAL)                                     \
     M_(PLATE_LOSS, 0.0f)                                                  \
@@ -222,6 +224,10 @@
     M_(VOLOR,    FLOAT32, IJK, GEOM)                                      \
     M_(BSTEP,    FLOAT32, IJK, GEOM)                                      \
     M_(DWALLSQ,  FLOAT32, IJK, GEOM)                                      \
+    /* NEW_LOSS (ILOS 100-199) mixing lengths, SET_XLENGTH 12476-12492 */ \
+    M_(XLENGTH,  FLOAT32, IJK, OPT)                                       \
+    M_(FST_RAT,  FLOAT32, IJK, OPT)                                       \
+    M_(ROAVG_CELL, FLOAT32, IJK, OPT)                                     \
     M_(RTHETA,   FLOAT32, IJK, OPT)                                       \
     /* multigrid block time steps, /BKMGRD/ */                           \
     M_(STEP1,    FLOAT32, MG1, GEOM)                                      \
@@ -256,6 +262,7 @@
     M_(RSTEP,    FLOAT32, IJK, STATE)                                     \
     M_(Y_PLUS,   FLOAT32, IJK, STATE)                                     \
     M_(DPDS_CELL,FLOAT32, IJK, STATE)                                     \
-    M_(VISC_RAT, FLOAT32, IJK, OUT)
+    M_(VISC_RAT, FLOAT32, IJK, OUT)                                       \
+    M_(VISC_LAM, FLOAT32, IJK, OUT)
 
 #endif /* MGPU_COMMON_TABLE_H_ */

@@ -257,6 +257,7 @@ void enqueue_core(const Dev &d, Launch L, cudaEvent_t join = nullptr) {
     launch_flux_mass(d, L0);
     launch_flux_energy(d, L);
     launch_tstep(d, L, V_RO, 2);
+    if (d.ILOS >= 100) launch_roavg_cell(d, L);     // 4255-4267, after TSTEP(RO)
     if (join) {
         cudaStreamWaitEvent(L.s, join, 0);
         launch_bc_apply(d, L0);
@@ -669,7 +670,14 @@ int32_t mgpu_commit(mgpu_handle *h) {
 #define MGPU_CHKR(n, v) if (d.n == MGPU_REQUIRED_REAL) return fail(MGPU_E_ARG, "real not set: " #n);
     MGPU_REAL_SCALARS(MGPU_CHKR)
     if (d.ITIMST != 3) return fail(MGPU_E_UNSUPPORTED, "ITIMST other than 3 (incompressible 5/6) not covered");
-    if (d.ILOS != 10) return fail(MGPU_E_UNSUPPORTED, "only ILOS=10 (mixing-length LOSS) is covered");
+    const bool new_loss = d.ILOS >= 100 && d.ILOS < 200;
+    if (d.ILOS != 10 && !new_loss)
+        return fail(MGPU_E_UNSUPPORTED, "only ILOS=10 (LOSS) and ILOS 100-199 (NEW_LOSS) are covered");
+    if (new_loss) {
+        for (const char *n : {"XLENGTH", "FST_RAT", "ROAVG_CELL"})
+            if (!h->bound[find_array(n)]) return fail(MGPU_E_ARG, std::string("ILOS 100-199 needs ") + n);
+        if (!(d.VORT_MAX > 0.0f)) return fail(MGPU_E_ARG, "ILOS 100-199 needs VORT_MAX > 0 (SETUP 7322-7328)");
+    }
     if (d.IFGAS != 0) return fail(MGPU_E_UNSUPPORTED, "real-gas IFGAS=1 not covered");
     if (d.IFCOOL || d.IFBLEED || d.IFSHROUD) return fail(MGPU_E_UNSUPPORTED, "cooling/bleed/shroud not covered");
     if (d.IF_REPEAT != 0) return fail(MGPU_E_UNSUPPORTED, "IF_REPEAT not covered");
@@ -706,6 +714,7 @@ int32_t mgpu_commit(mgpu_handle *h) {
         (rc = getf("XLLIM_I1", XL[0])) || (rc = getf("XLLIM_IM", XL[1])) || (rc = getf("XLLIM_K1", XL[2])) ||
         (rc = getf("XLLIM_KM", XL[3])) || (rc = getf("XLLIM_DWN", XL[4])) || (rc = getf("XLLIM_UP", XL[5])))
         return rc;
+    if (new_loss && !d.NLS && (rc = dalloc(h, &d.NLS, new_loss_work_floats(d)))) return rc;
     d.any_cusp2 = 0;
     for (int nr = 0; nr < d.NROWS; ++nr) {
         if (IF_CUSP[nr] > 2) return fail(MGPU_E_UNSUPPORTED, "IF_CUSP above 2 not covered");

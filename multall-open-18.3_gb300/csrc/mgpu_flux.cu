@@ -53,7 +53,7 @@ __global__ void k_step_begin(Dev d) {
         c->FMIXUP = FM * FM;
     }
     c->do_tail = (n % 5 == 0) || ifend == 1;
-    c->do_loss = (d.ILOS == 10) && (n % d.NLOS == 0) && !d.FROZEN;
+    c->do_loss = (d.ILOS == 10 || (d.ILOS >= 100 && d.ILOS < 200)) && (n % d.NLOS == 0) && !d.FROZEN;
     c->damp_on = !(c->DAMP < 2.0f || c->DAMP > 100.0f);
     if (d.use_cond) {
         cudaGraphSetConditional((cudaGraphConditionalHandle)d.cond_loss, c->do_loss ? 1u : 0u);

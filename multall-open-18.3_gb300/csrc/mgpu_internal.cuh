@@ -106,6 +106,7 @@ struct Dev {
     int *DFLAG;                        // (IM*KM) density-limiter column flags
     float *BCBUF;                      // (4, KM) PAVG2, PAVG3, PAVGOUT, and the PD each K's exit update uses
     float *FLOWJ;                      // (JM) SETFLO's FLOW(J)
+    float *NLS;                        // NEW_LOSS work: 9 strain-rate arrays, then the wall-face terms
     // recording hooks of the adjoint's linearisation step (null otherwise):
     // RO(I,1,K) as the inlet condition reads it, the mixing-plane inputs of
     // each (row interface, K), and bit flags for a limiter that changed a value
@@ -226,6 +227,9 @@ inline void mark(const Launch &L, const char *name) {
 void launch_step_begin(const Dev &d, Launch L);
 void launch_prim(const Dev &d, Launch L);
 void launch_loss(const Dev &d, Launch L, bool init_call);
+void launch_new_loss(const Dev &d, Launch L, bool init_call);
+void launch_roavg_cell(const Dev &d, Launch L);
+size_t new_loss_work_floats(const Dev &d);
 void launch_flux_mass(const Dev &d, Launch L);
 void launch_flux_energy(const Dev &d, Launch L);
 // inlet/exit conditions: the pitchwise sums and PD(K) (one CTA), then the

@@ -671,6 +671,10 @@ cudaError_t configure_loss_kernels(const Dev &d) {
 }
 
 void launch_loss(const Dev &d, Launch L, bool init_call) {
+    if (d.ILOS >= 100) {
+        launch_new_loss(d, L, init_call);
+        return;
+    }
     launchk(L, k_loss_prologue, dim3(1), dim3(1), 0, d, init_call ? 1 : 0);
     mark(L, "k_loss_prologue");
     if (d.YPLUSWALL < -10.0f) {
@@ -1050,6 +1054,483 @@ void launch_integrals(const Dev &d, Launch L, double *out) {
     mark(L, "k_int_node");
     launchk(L, k_int_sum, dim3(d.JM), dim3(TAIL_BS), 0, d, out);
     mark(L, "k_int_sum");
+}
+
+// ---------------------------------------------------------------------
+// NEW_LOSS (ILOS 100-199, 12522-13462): the eddy viscosity of a mixing
+// length and the vorticity of the relative velocity, the full viscous
+// stress tensor and heat flux from GRADVEL (13468-13508) in every cell,
+// transition, the wall shear stress on the blade surfaces and endwalls (log
+// law with roughness, or the Shih wall functions), and the stresses summed
+// over the I and K faces into the body forces.  The reference scatters each
+// face's stress into its two cells; here every cell gathers its faces in
+// the order the reference adds them, so each force is the same FP32 sum.
+//   k_loss_prologue (as LOSS)            VISLAM, FTCOND (12545-12568)
+//   k_nl_cells        one thread a cell  strain rates, VISC_RAT, VISC_LAM (DO 150)
+//   k_nl_transition   one CTA a J plane  laminar lines (DO 160)
+//   k_pwallgrad_*     YPLUSWALL < -10    DPDS_CELL
+//   k_nl_walls        one thread a wall face: shear stress and wall forces
+//   k_nl_forces       one thread a cell  face sums, Y_PLUS, relaxation (DO 500)
+// Work (d.NLS): the nine strain rates TXR TXX TXT TRR TRT TTT QXX QRR QTT
+// (N each), then per wall face XF RF TF ES VSTAR 0.25*ROAVG for the I=1 and
+// I=IM blade surfaces ((JM,KM) each) and the hub and casing ((IM,JM) each).
+// ---------------------------------------------------------------------
+size_t new_loss_work_floats(const Dev &d) {
+    return (size_t)9 * d.IM * d.JM * d.KM + (size_t)12 * d.JM * d.KM + (size_t)12 * d.IM * d.JM;
+}
+
+// the log-law skin friction of NEW_LOSS with roughness (12879-12925 and its
+// three copies), written on the sums of four corner values RO4 and W4
+__device__ inline float nl_twall(float RE, float DPERP, float ROUGH, float RO4, float W4, float VISLAM) {
+    const float RELOG = 1.0f / logf(RE);
+    float CF;
+    if (ROUGH > 1.0E-7f) {
+        if (ROUGH > DPERP) ROUGH = DPERP;
+        float REK = RE * ROUGH / DPERP;
+        REK = REK - 80.0f;
+        if (REK < 0.0f) REK = 0.0f;
+        const float REKSQ = REK * REK;
+        const float A1c = -.00178493f + .0000814923f * REK + .000000150445f * REKSQ;
+        const float A2c = .029072f - .001584f * REK - .00000225194f * REKSQ;
+        const float A3c = .270313f + .0091409f * REK + .00000451537f * REKSQ + .00000000464767f * REKSQ * REK;
+        CF = A1c + A2c * RELOG + A3c * RELOG * RELOG;
+    } else {
+        CF = -0.00178493f + 0.029072f * RELOG + 0.270313f * RELOG * RELOG;
+    }
+    const float CFLAM = 2.0f / RE;
+    CF = fmaxf(CF, CFLAM);
+    if (RE < 125.0f) CF = CFLAM;
+    if (ROUGH > 1.0E-7f) {
+        const float TW = CF * RO4 * W4 * W4 / 128.0f;
+        const float VSTAR = sqrtf(TW / (RO4 / 4.0f));
+        const float PLUSK = ROUGH * VSTAR * RO4 / VISLAM / 4.0f;
+        const float RELOG10 = log10f(DPERP / ROUGH);
+        const float FUNCN = 5.75f * RELOG10 + 8.5f;
+        const float CF_FULL_ROUGH = 2.0f / (FUNCN * FUNCN);
+        if (PLUSK > 45.0f && CF > CF_FULL_ROUGH) CF = CF_FULL_ROUGH;
+    }
+    return CF * RO4 * W4 * W4 / 128.0f;
+}
+
+// the cell (i, j, k), i fastest, of thread t; false past the last cell
+__device__ inline bool nl_cell(const Dev &d, int t, int &i, int &j, int &k) {
+    const int IMM1 = d.IMM1, JC = d.JM - 1;
+    if (t >= IMM1 * JC * d.KMM1) return false;
+    i = t % IMM1 + 1;
+    const int q = t / IMM1;
+    j = q % JC + 2;
+    k = q / JC + 1;
+    return true;
+}
+
+// cell-average density for NEW_LOSS, every step after TSTEP(RO) (4255-4267)
+__global__ void __launch_bounds__(256) k_roavg_cell(const __grid_constant__ Dev d) {
+    pdl_wait();
+    int i, j, k;
+    if (!nl_cell(d, blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
+    const int sJ = d.IM, sK = d.IM * d.JM, n = ix3(d, i, j, k);
+    const float *A = d.RO;
+    d.ROAVG_CELL[n] = 0.125f * (A[n] + A[n + 1] + A[n + 1 + sK] + A[n + sK] + A[n - sJ] + A[n + 1 - sJ] +
+                                A[n + 1 - sJ + sK] + A[n - sJ + sK]);
+}
+
+void launch_roavg_cell(const Dev &d, Launch L) {
+    const int nc = d.IMM1 * d.KMM1 * (d.JM - 1);
+    launchk(L, k_roavg_cell, dim3((nc + 255) / 256), dim3(256), 0, d);
+    mark(L, "k_roavg_cell");
+}
+
+// DO 150: strain rates, vorticity, the eddy viscosity and its ratio
+__global__ void __launch_bounds__(256) k_nl_cells(const __grid_constant__ Dev d, int init_call) {
+    pdl_wait();
+    const DevCtl *c = d.ctl;
+    if (!init_call && !c->do_loss) return;
+    int i, j, k;
+    if (!nl_cell(d, blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
+    const int sJ = d.IM, sK = d.IM * d.JM, n = ix3(d, i, j, k);
+    const int o000 = n, o100 = n + 1, o0m0 = n - sJ, o1m0 = n + 1 - sJ;
+    const int o001 = n + sK, o101 = n + 1 + sK, o0m1 = n - sJ + sK, o1m1 = n + 1 - sJ + sK;
+    const float FMIXUP = init_call ? 1.0f : c->FMIXUP;
+    float VISLAM = c->VISLAM;
+    auto avg8 = [&](const float *A) {
+        return 0.125f * (A[o000] + A[o100] + A[o101] + A[o001] + A[o0m0] + A[o1m0] + A[o1m1] + A[o0m1]);
+    };
+    const float WTAVG = avg8(d.WT);
+    const float ROAVG = d.ROAVG_CELL[n];
+    const float TSAVG = avg8(d.T_STATIC);
+    const float RAVG = A2(d.RAVG_CELL, j, k);
+    const float RVOL = 0.25f / d.VOL[n];
+    const float aqx0 = d.AQX[n], aqx1 = d.AQX[n - sJ], abx0 = d.ABX[n], abx1 = d.ABX[n + 1], asx0 = d.ASX[n],
+                asx1 = d.ASX[n + sK];
+    const float aqr0 = d.AQR[n], aqr1 = d.AQR[n - sJ], abr0 = d.ABR[n], abr1 = d.ABR[n + 1], asr0 = d.ASR[n],
+                asr1 = d.ASR[n + sK];
+    const float abt = A2(d.ABT, j, k);
+    auto grad = [&](const float *V, float &dx, float &dr, float &dt) {
+        const float VAVGJ1 = V[o0m0] + V[o1m0] + V[o1m1] + V[o0m1];
+        const float VAVGJ2 = V[o000] + V[o100] + V[o101] + V[o001];
+        const float VAVGI1 = V[o000] + V[o0m0] + V[o0m1] + V[o001];
+        const float VAVGI2 = V[o100] + V[o1m0] + V[o1m1] + V[o101];
+        const float VAVGK1 = V[o000] + V[o100] + V[o1m0] + V[o0m0];
+        const float VAVGK2 = V[o001] + V[o101] + V[o1m1] + V[o0m1];
+        const float VAVGCELL = 0.125f * (VAVGJ1 + VAVGJ2);
+        dx = -((VAVGJ2 * aqx0 - VAVGJ1 * aqx1 + VAVGI1 * abx0 - VAVGI2 * abx1 + VAVGK1 * asx0 - VAVGK2 * asx1) * RVOL);
+        dr = -((VAVGJ2 * aqr0 - VAVGJ1 * aqr1 + VAVGI1 * abr0 - VAVGI2 * abr1 + VAVGK1 * asr0 - VAVGK2 * asr1) * RVOL) -
+             VAVGCELL / RAVG;
+        dt = -((VAVGI1 - VAVGI2) * abt * RVOL);
+    };
+    float DVXDX, DVXDR, DVXDT, DVRDX, DVRDR, DVRDT, DWTDX, DWTDR, DWTDT, DTDX, DTDR, DTDT;
+    grad(d.VX, DVXDX, DVXDR, DVXDT);
+    grad(d.VR, DVRDX, DVRDR, DVRDT);
+    grad(d.WT, DWTDX, DWTDR, DWTDT);
+    grad(d.T_STATIC, DTDX, DTDR, DTDT);
+    const float XLEN = d.XLENGTH[n], FST = d.FST_RAT[n], YP = d.Y_PLUS[n];
+    const size_t N = (size_t)d.IM * d.JM * d.KM;
+    float *W = d.NLS;
+    W[n] = DVXDR + DVRDX;                      // TXR
+    W[N + n] = DVXDX;                          // TXX
+    W[2 * N + n] = DWTDX + DVXDT;              // TXT
+    W[3 * N + n] = DVRDR;                      // TRR
+    W[4 * N + n] = DWTDR + DVRDT - WTAVG / RAVG;   // TRT
+    W[5 * N + n] = DWTDT;                      // TTT
+    W[6 * N + n] = DTDX;                       // QXX
+    W[7 * N + n] = DTDR;                       // QRR
+    W[8 * N + n] = DTDT;                       // QTT
+    const float VORTX = DVRDT - DWTDR - WTAVG / RAVG;
+    const float VORTR = DWTDX - DVXDT;
+    const float VORTT = DVXDR - DVRDX;
+    float VORT = sqrtf(VORTX * VORTX + VORTR * VORTR + VORTT * VORTT);
+    if (VORT > d.VORT_MAX) VORT = d.VORT_MAX;
+    float TURBVIS_WALL = ROAVG * XLEN * VORT * FMIXUP;
+    TURBVIS_WALL = TURBVIS_WALL * fyplus_of(YP, d.YPLAM, d.YPTURB, 0.0f);
+    if (d.REYNO < 0.0001f) VISLAM = (fabsf(d.REYNO) / 100000.0f) * powf(TSAVG / 288.0f, 0.62f);
+    float VISTOT = VISLAM * (1.0f + FST) + TURBVIS_WALL;
+    const float VISLIM = d.TURBVIS_LIM * VISLAM;
+    if (VISTOT > VISLIM) VISTOT = VISLIM;
+    d.VISC_RAT[n] = VISTOT / VISLAM;
+    d.VISC_LAM[n] = VISLAM;
+}
+
+// DO 160: a line whose largest viscosity ratio stays at or below FTRANS, or
+// that lies upstream of its transition point, is laminar.  The hub and
+// casing lines of every I come first, then the I=1 and I=IM lines of every
+// K, as the reference orders them within a J plane.
+__global__ void __launch_bounds__(128) k_nl_transition(const __grid_constant__ Dev d, int init_call) {
+    pdl_wait();
+    if (!init_call && !d.ctl->do_loss) return;
+    const int j = blockIdx.x + 2;
+    const int NRW = A1(d.NROW, j);
+    const int JROW = j - A1(d.JSTART, NRW) + 1;
+    const int KMID = d.KMID, IMID = d.IMID, KMM1 = d.KMM1, IMM1 = d.IMM1;
+    float *VRAT = d.VISC_RAT;
+    auto line = [&](bool upstream, int n0, int stride, int cnt) {
+        bool lam = upstream;
+        if (!lam) {
+            float RMAX = 0.0f;
+            for (int q = 0; q < cnt; ++q) {
+                const float r = VRAT[n0 + q * stride];
+                if (!(r < RMAX)) RMAX = r;
+            }
+            lam = !(RMAX > d.FTRANS);
+        }
+        if (lam)
+            for (int q = 0; q < cnt; ++q) VRAT[n0 + q * stride] = 1.0f;
+    };
+    const int sK = d.IM * d.JM;
+    for (int i = threadIdx.x + 1; i <= IMM1; i += blockDim.x) {
+        line(JROW < A1(d.JTRAN_K1, NRW), ix3(d, i, j, 1), sK, KMID);
+        line(JROW < A1(d.JTRAN_KM, NRW), ix3(d, i, j, KMID), sK, KMM1 - KMID + 1);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x + 1; k <= KMM1; k += blockDim.x) {
+        line(JROW < A1(d.JTRAN_I1, NRW), ix3(d, 1, j, k), 1, IMID);
+        line(JROW < A1(d.JTRAN_IM, NRW), ix3(d, IMID, j, k), 1, IMM1 - IMID + 1);
+    }
+    // the COMMON VISLAM leaves NEW_LOSS as the last cell's laminar viscosity
+    if (blockIdx.x == 0 && threadIdx.x == 0 && d.REYNO < 0.0001f) d.ctl->VISLAM = A3(d.VISC_LAM, IMM1, d.JM, KMM1);
+}
+
+// the wall shear stress of one wall face and its force on the wall cell:
+// the I=1 and I=IM blade surfaces of every (J,K) outside a tip gap
+// (12825-13052), the hub and casing of every (I,J) (13168-13390)
+__global__ void __launch_bounds__(256) k_nl_walls(const __grid_constant__ Dev d, int init_call) {
+    pdl_wait();
+    const DevCtl *c = d.ctl;
+    if (!init_call && !c->do_loss) return;
+    const int nb = (d.JM - 1) * d.KMM1, ne = (d.JM - 1) * d.IMM1;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * nb + 2 * ne) return;
+    const float VISLAM = c->VISLAM;
+    const float VISLAM16 = VISLAM * 16.0f;
+    const size_t N = (size_t)d.IM * d.JM * d.KM, SB = (size_t)d.JM * d.KM, SE = (size_t)d.IM * d.JM;
+    float *WB = d.NLS + 9 * N, *WE = WB + 12 * SB;
+    const int sJ = d.IM, sK = d.IM * d.JM;
+    if (t < 2 * nb) {
+        const int side = t / nb, r = t % nb;
+        const int j = r % (d.JM - 1) + 2, k = r / (d.JM - 1) + 1;
+        const int NRW = A1(d.NROW, j);
+        if (A1(d.IND, j) == 0) return;
+        if (A1(d.KTIPS, NRW) > 0 && k >= A1(d.KTIPS, NRW) && k < A1(d.KTIPE, NRW)) return;
+        const int iw = side == 0 ? 2 : d.IMM1;       // node line of the averages
+        const int ic = side == 0 ? 1 : d.IMM1;       // wall cell
+        const int ia = side == 0 ? 1 : d.IM;         // wall face
+        const int a = ix3(d, iw, j, k);
+        auto s4 = [&](const float *A) { return A[a] + A[a - sJ] + A[a - sJ + sK] + A[a + sK]; };
+        const float VXAVG = s4(d.VX), VRAVG = s4(d.VR), WTAVG = s4(d.WT), ROAVG = s4(d.RO);
+        const float WAVG = sqrtf(WTAVG * WTAVG + VXAVG * VXAVG + VRAVG * VRAVG);
+        const int fa = ix3(d, ia, j, k);
+        const float abt = A2(d.ABT, j, k);
+        const float AREA = sqrtf(d.ABX[fa] * d.ABX[fa] + d.ABR[fa] * d.ABR[fa] + abt * abt);
+        const int nc = ix3(d, ic, j, k);
+        const float DPERP = d.VOL[nc] / AREA;
+        float TW;
+        if (d.YPLUSWALL < -0.001f) {
+            float &yp = side == 0 ? A2(d.YPLUS_I1, j, k) : A2(d.YPLUS_IM, j, k);
+            float YN;
+            wallfun(DPERP, d.DPDS_CELL[nc], 0.25f * ROAVG, TW, yp, 0.25f * WAVG, YN, VISLAM, d.YPLUSWALL);
+            yp = fminf(1000.0f, YN);
+        } else {
+            const float RE = DPERP * ROAVG * WAVG / VISLAM16;
+            TW = nl_twall(RE, DPERP, side == 0 ? A1(d.ROUGH_L, NRW) : A1(d.ROUGH_U, NRW), ROAVG, WAVG, VISLAM);
+        }
+        const float DEN = 0.25f * ROAVG;
+        const float FMULT = -TW * AREA / WAVG;
+        const float TF = FMULT * WTAVG;
+        const size_t o = (size_t)ix2(d, j, k);
+        float *w = WB + (size_t)side * 6 * SB;
+        w[o] = FMULT * VXAVG;
+        w[SB + o] = FMULT * VRAVG;
+        w[2 * SB + o] = TF;
+        w[3 * SB + o] = TF * A1(d.WRAD, j) * A2(d.RAVG_CELL, j, k);
+        w[4 * SB + o] = sqrtf(TW / DEN);
+        w[5 * SB + o] = DEN;
+        return;
+    }
+    t -= 2 * nb;
+    const int side = t / ne, r = t % ne;
+    const int i = r % d.IMM1 + 1, j = r / d.IMM1 + 2;
+    const int NRW = A1(d.NROW, j);
+    const int kn = side == 0 ? 2 : d.KMM1;           // node line of the averages
+    const int kc = side == 0 ? 1 : d.KMM1;           // wall cell
+    const int ka = side == 0 ? 1 : d.KM;             // wall face
+    const int a = ix3(d, i, j, kn);
+    auto s4 = [&](const float *A) { return A[a] + A[a + 1] + A[a + 1 - sJ] + A[a - sJ]; };
+    const float VXAVG = s4(d.VX), VRAVG = s4(d.VR), VTAVG = s4(d.VT), ROAVG = s4(d.RO);
+    const float RAVG = A2(d.R, j, kn) + A2(d.R, j, kn) + A2(d.R, j - 1, kn) + A2(d.R, j - 1, kn);
+    const float WW = side == 0 ? A1(d.WHUB, j) : A1(d.WTIP, j);
+    const float WTAVG = VTAVG - WW * RAVG;
+    const float WAVG = sqrtf(VXAVG * VXAVG + VRAVG * VRAVG + WTAVG * WTAVG);
+    const int fa = ix3(d, i, j, ka);
+    const float AREA = sqrtf(d.ASX[fa] * d.ASX[fa] + d.ASR[fa] * d.ASR[fa]);
+    const int nc = ix3(d, i, j, kc);
+    const float DPERP = d.VOL[nc] / AREA;
+    float TW;
+    if (d.YPLUSWALL < -0.001f) {
+        float &yp = side == 0 ? AIJ(d.YPLUS_K1, i, j) : AIJ(d.YPLUS_KM, i, j);
+        float YN;
+        wallfun(DPERP, d.DPDS_CELL[nc], 0.25f * ROAVG, TW, yp, 0.25f * WAVG, YN, VISLAM, d.YPLUSWALL);
+        yp = fminf(1000.0f, YN);
+    } else {
+        const float RE = DPERP * ROAVG * WAVG / VISLAM16;
+        TW = nl_twall(RE, DPERP, side == 0 ? A1(d.ROUGH_H, NRW) : A1(d.ROUGH_T, NRW), ROAVG, WAVG, VISLAM);
+    }
+    const float DEN = 0.25f * ROAVG;
+    float FMULT = -TW * AREA / WAVG;
+    if (side == 0 ? (d.IBOUND == 1 || d.IBOUND > 2) : (d.IBOUND >= 2)) FMULT = 0.0f;
+    const float TF = FMULT * WTAVG;
+    const size_t o = (size_t)ixij(d, i, j);
+    float *w = WE + (size_t)side * 6 * SE;
+    w[o] = FMULT * VXAVG;
+    w[SE + o] = FMULT * VRAVG;
+    w[2 * SE + o] = TF;
+    w[3 * SE + o] = TF * 0.25f * WW * RAVG;
+    w[4 * SE + o] = sqrtf(TW / DEN);
+    w[5 * SE + o] = DEN;
+}
+
+struct NlStress {
+    float txr, txx, txt, trr, trt, ttt, qxx, qrr, qtt;
+};
+
+// DO 190 for one cell: the strain rates times the final viscosity
+__device__ inline NlStress nl_stress(const Dev &d, const float *W, size_t N, int m) {
+    const float VIS = d.VISC_RAT[m] * d.VISC_LAM[m];
+    const float TH = d.CP * VIS / d.PRANDTL;
+    const float VIS2 = 2.0f * VIS;
+    NlStress s;
+    s.txr = VIS * W[m];
+    s.txx = VIS2 * W[N + m];
+    s.txt = VIS * W[2 * N + m];
+    s.trr = VIS2 * W[3 * N + m];
+    s.trt = VIS * W[4 * N + m];
+    s.ttt = VIS2 * W[5 * N + m];
+    s.qxx = -TH * W[6 * N + m];
+    s.qrr = -TH * W[7 * N + m];
+    s.qtt = -TH * W[8 * N + m];
+    return s;
+}
+
+// Each cell's forces: the blade-wall and periodic terms, its I faces, the
+// endwall terms and its K faces, in the reference's order of addition; then
+// Y_PLUS from the wall shear stresses, and the relaxation into XFORCE,
+// RFORCE, TFORCE and QSOURCE (DO 500).
+__global__ void __launch_bounds__(256) k_nl_forces(const __grid_constant__ Dev d, int init_call) {
+    pdl_wait();
+    const DevCtl *c = d.ctl;
+    if (!init_call && !c->do_loss) return;
+    int i, j, k;
+    if (!nl_cell(d, blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
+    const float VISLAM = c->VISLAM;
+    const float RF_VIS = init_call ? 1.0f : d.RF_VIS;
+    const size_t N = (size_t)d.IM * d.JM * d.KM, SB = (size_t)d.JM * d.KM, SE = (size_t)d.IM * d.JM;
+    const float *W = d.NLS, *WB = W + 9 * N, *WE = WB + 12 * SB;
+    const int sJ = d.IM, sK = d.IM * d.JM, n = ix3(d, i, j, k);
+    const int IMM1 = d.IMM1, KMM1 = d.KMM1;
+    const int NRW = A1(d.NROW, j), IND = A1(d.IND, j);
+    const int KTS = A1(d.KTIPS, NRW), KTE = A1(d.KTIPE, NRW);
+    const bool blade = IND != 0 && !(KTS > 0 && k >= KTS && k < KTE);
+    // 13063: (IND(J).EQ.1).AND.(K.LT.KTIPS).OR.(K.GT.KTIPE) skips the periodic face
+    const bool periodic = !((IND == 1 && k < KTS) || k > KTE);
+    const float xf0 = d.XFORCE[n], rf0 = d.RFORCE[n], tf0 = d.TFORCE[n], qs0 = d.QSOURCE[n];
+    const float ravg = A2(d.RAVG_CELL, j, k), dw = sqrtf(d.DWALLSQ[n]), yp0 = d.Y_PLUS[n];
+    auto wb = [&](int side, int f) { return WB[((size_t)side * 6 + f) * SB + (size_t)ix2(d, j, k)]; };
+    auto we = [&](int side, int f) { return WE[((size_t)side * 6 + f) * SE + (size_t)ixij(d, i, j)]; };
+    auto iface = [&](int I, int cI, int cmI, float &XF, float &RF, float &TF, float &Q, float &WV) {
+        const NlStress a = nl_stress(d, W, N, ix3(d, cI, j, k)), b = nl_stress(d, W, N, ix3(d, cmI, j, k));
+        const int f = ix3(d, I, j, k);
+        const float abr = d.ABR[f], abx = d.ABX[f], abt = A2(d.ABT, j, k);
+        XF = 0.5f * ((a.txr + b.txr) * abr + (a.txt + b.txt) * abt + (a.txx + b.txx) * abx);
+        RF = 0.5f * ((a.trr + b.trr) * abr + (a.trt + b.trt) * abt + (a.txr + b.txr) * abx);
+        TF = 0.5f * ((a.trt + b.trt) * abr + (a.ttt + b.ttt) * abt + (a.txt + b.txt) * abx);
+        Q = 0.5f * ((a.qxx + b.qxx) * abx + (a.qrr + b.qrr) * abr + (a.qtt + b.qtt) * abt);
+        const float vx = d.VX[f] + d.VX[f - sJ] + d.VX[f - sJ + sK] + d.VX[f + sK];
+        const float vr = d.VR[f] + d.VR[f - sJ] + d.VR[f - sJ + sK] + d.VR[f + sK];
+        const float vt = d.VT[f] + d.VT[f - sJ] + d.VT[f - sJ + sK] + d.VT[f + sK];
+        WV = -0.25f * (XF * vx + RF * vr + TF * vt);
+    };
+    auto kface = [&](int K, float &XF, float &RF, float &TF, float &Q, float &WV) {
+        const NlStress a = nl_stress(d, W, N, ix3(d, i, j, K)), b = nl_stress(d, W, N, ix3(d, i, j, K - 1));
+        const int f = ix3(d, i, j, K);
+        const float asr = d.ASR[f], asx = d.ASX[f];
+        XF = 0.5f * ((a.txr + b.txr) * asr + (a.txx + b.txx) * asx);
+        RF = 0.5f * ((a.trr + b.trr) * asr + (a.txr + b.txr) * asx);
+        TF = 0.5f * ((a.trt + b.trt) * asr + (a.txt + b.txt) * asx);
+        Q = 0.5f * ((a.qxx + b.qxx) * asx + (a.qrr + b.qrr) * asr);
+        const float vx = d.VX[f] + d.VX[f + 1] + d.VX[f + 1 - sJ] + d.VX[f - sJ];
+        const float vr = d.VR[f] + d.VR[f + 1] + d.VR[f + 1 - sJ] + d.VR[f - sJ];
+        const float vt = d.VT[f] + d.VT[f + 1] + d.VT[f + 1 - sJ] + d.VT[f - sJ];
+        WV = -0.25f * (XF * vx + RF * vr + TF * vt);
+    };
+    float fx = 0.0f, fr = 0.0f, ft = 0.0f, es = 0.0f;
+    float XF, RF, TF, Q, WV;
+    if (i == 1 || i == IMM1) {
+        // FORCE*(1) and FORCE*(IM-1) after the blade-wall terms, then the
+        // periodic face and the average of the two cells
+        float p1[4] = {0.0f, 0.0f, 0.0f, 0.0f}, pm[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (blade)
+            for (int f = 0; f < 4; ++f) {
+                p1[f] = 0.0f + wb(0, f);
+                pm[f] = 0.0f + wb(1, f);
+            }
+        if (periodic) {
+            iface(1, 1, IMM1, XF, RF, TF, Q, WV);
+            const float fl[3] = {XF, RF, TF};
+            for (int f = 0; f < 3; ++f) {
+                pm[f] = pm[f] + fl[f];
+                p1[f] = p1[f] - fl[f];
+                const float avg = 0.5f * (p1[f] + pm[f]);
+                p1[f] = avg;
+                pm[f] = avg;
+            }
+            p1[3] = p1[3] + Q + WV;
+            pm[3] = pm[3] - Q - WV;
+            const float avg = 0.5f * (p1[3] + pm[3]);
+            p1[3] = avg;
+            pm[3] = avg;
+        }
+        const float *p = i == 1 ? p1 : pm;
+        fx = p[0];
+        fr = p[1];
+        ft = p[2];
+        es = p[3];
+    }
+    if (i >= 2) {
+        iface(i, i, i - 1, XF, RF, TF, Q, WV);
+        fx = fx - XF;
+        fr = fr - RF;
+        ft = ft - TF;
+        es = es + Q + WV;
+    }
+    if (i + 1 <= IMM1) {
+        iface(i + 1, i + 1, i, XF, RF, TF, Q, WV);
+        fx = fx + XF;
+        fr = fr + RF;
+        ft = ft + TF;
+        es = es - Q - WV;
+    }
+    if (k == 1) {
+        fx = fx + we(0, 0);
+        fr = fr + we(0, 1);
+        ft = ft + we(0, 2);
+        es = es + we(0, 3);
+    }
+    if (k == KMM1) {
+        fx = fx + we(1, 0);
+        fr = fr + we(1, 1);
+        ft = ft + we(1, 2);
+        es = es + we(1, 3);
+    }
+    if (k >= 2) {
+        kface(k, XF, RF, TF, Q, WV);
+        fx = fx - XF;
+        fr = fr - RF;
+        ft = ft - TF;
+        es = es + Q + WV;
+    }
+    if (k + 1 <= KMM1) {
+        kface(k + 1, XF, RF, TF, Q, WV);
+        fx = fx + XF;
+        fr = fr + RF;
+        ft = ft + TF;
+        es = es - Q - WV;
+    }
+    // Y_PLUS: the blade surface of the cell's half pitch, then the lower of
+    // that and the hub or casing value (12965-12970, 13036-13040, 13249-13257, 13365-13373)
+    float yp = yp0;
+    if (blade) {
+        const int side = i <= d.IMID ? 0 : 1;
+        yp = fminf(1000.0f, wb(side, 4) * dw * wb(side, 5) / VISLAM);
+    }
+    if (k <= d.KMID && (d.IBOUND == 0 || d.IBOUND == 2)) yp = fminf(we(0, 4) * dw * we(0, 5) / VISLAM, yp);
+    if (k > d.KMID && d.IBOUND <= 1) yp = fminf(we(1, 4) * dw * we(1, 5) / VISLAM, yp);
+    d.Y_PLUS[n] = yp;
+    const float RF_VIS1 = 1.0f - RF_VIS;
+    d.XFORCE[n] = RF_VIS1 * xf0 - RF_VIS * fx;
+    d.TFORCE[n] = RF_VIS1 * tf0 - RF_VIS * ft * ravg;
+    d.RFORCE[n] = RF_VIS1 * rf0 - RF_VIS * fr;
+    d.QSOURCE[n] = RF_VIS1 * qs0 - RF_VIS * es;
+}
+
+void launch_new_loss(const Dev &d, Launch L, bool init_call) {
+    const int ic = init_call ? 1 : 0;
+    launchk(L, k_loss_prologue, dim3(1), dim3(1), 0, d, ic);
+    mark(L, "k_loss_prologue");
+    const int nc = d.IMM1 * d.KMM1 * (d.JM - 1);
+    launchk(L, k_nl_cells, dim3((nc + 255) / 256), dim3(256), 0, d, ic);
+    mark(L, "k_nl_cells");
+    launchk(L, k_nl_transition, dim3(d.JM - 1), dim3(128), 0, d, ic);
+    mark(L, "k_nl_transition");
+    if (d.YPLUSWALL < -10.0f) {
+        launchk(L, k_pwallgrad_cells, dim3((nc + 255) / 256), dim3(256), 0, d, ic);
+        mark(L, "k_pwallgrad_cells");
+        launchk(L, k_pwallgrad_smooth, dim3((unsigned)((d.IMM1 + 31) / 32), (unsigned)d.KMM1), dim3(32),
+                pwallgrad_smem(d), d, ic);
+        mark(L, "k_pwallgrad_smooth");
+    }
+    const int nw = 2 * (d.JM - 1) * d.KMM1 + 2 * (d.JM - 1) * d.IMM1;
+    launchk(L, k_nl_walls, dim3((nw + 255) / 256), dim3(256), 0, d, ic);
+    mark(L, "k_nl_walls");
+    launchk(L, k_nl_forces, dim3((nc + 255) / 256), dim3(256), 0, d, ic);
+    mark(L, "k_nl_forces");
 }
 
 }  // namespace mgpu

@@ -55,6 +55,8 @@ class RowSpec:
     pdn: float = 0.0
     stage: int = 1          # NSTAGE(NR)
     xllim: tuple = (0.03, 0.03, 0.03, 0.03, 0.03, 0.02)  # XLLIM_I1,IM,K1,KM,DWN,UP
+    xllim_new: tuple = (0.03, 0.03, 0.03, 0.03)  # ILOS >= 100: XLLIM_IN,LE,TE,DN
+    fsturb: float = 1.0     # ILOS >= 100: FSTURB, free-stream turbulent viscosity ratio
     # IF_CUSP = 2: forced trailing-edge separation (multall-open-18.3.f:987-1005)
     if_cusp: int = 0
     nup_i1: int = 0         # NUP_I1, NUP_IM: points before the TE where it starts
@@ -121,6 +123,8 @@ class CaseSpec:
     facmixup: float = 2.0
     nmixup: int = 1000
     nlos: int = 5
+    ilos: int = 10              # 10: LOSS; 100-199: NEW_LOSS
+    turbvis_lim: float = 3000.0
     in_vr: int = 0
     in_flow: int = 0            # IN_FLOW: 0 off, 3 towards FLOWIN, otherwise towards the mean flow
     flowin: float = 0.0         # FLOWIN (kg/s through all blade passages)

@@ -546,11 +546,22 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None, metrics64: boo
             volb = 0.0
 
     # ---------------- wall distance (SET_XLENGTH, 12194-12517) -------------
-    DWALLSQ = wall_distance_sq(IM, JM, KM, X, R, THETA, ASX, ASR, ABX, ABR, ABT, JSTART, JMIX, JLE, JTE,
-                               NROW, NBLADE, IMID, spec)
+    DWALLSQ, DIST = wall_distance_sq(IM, JM, KM, X, R, THETA, ASX, ASR, ABX, ABR, ABT, JSTART, JMIX, JLE, JTE,
+                                     NROW, NBLADE, IMID, spec, with_dist=True)
+    new_loss = {}
+    if 100 <= spec.ilos < 200:
+        new_loss = mixing_lengths(spec, IM, JM, KM, DIST, SMERID, JSTART, JMIX, JLE, JTE, NROW, IMID, KMID)
+        # cell-average density: the initial guess's node values (6796) until
+        # the first step forms it (4255-4267)
+        new_loss["ROAVG_CELL"] = RO.copy()
+        # vorticity limit (7322-7328)
+        DR1, DX1 = R[KM - 1, 0] - R[0, 0], X[KM - 1, 0] - X[0, 0]
+        DRM, DXM = R[KM - 1, JM - 1] - R[0, JM - 1], X[KM - 1, JM - 1] - X[0, JM - 1]
+        AVGSPAN = f32(0.5) * (np.sqrt(f32(DX1 * DX1 + DR1 * DR1)) + np.sqrt(f32(DXM * DXM + DRM * DRM)))
+        new_loss_vort = float(f32(5000.0) * VM1[KMID - 1] / AVGSPAN)
 
     # ---------------- publish --------------------------------------------
-    ints = dict(ITIMST=3, ILOS=10, NLOS=spec.nlos, IBOUND=0, IFMIX=spec.ifmix, IPOUT=spec.ipout,
+    ints = dict(ITIMST=3, ILOS=spec.ilos, NLOS=spec.nlos, IBOUND=0, IFMIX=spec.ifmix, IPOUT=spec.ipout,
                 IN_PRESS=0, IN_VTAN=0, IN_VR=spec.in_vr, IN_FLOW=spec.in_flow, IF_REPEAT=0, NRSMTH=0, NSFEXIT=0,
                 NSTEPS_MAX=spec.nsteps_max, NCHANGE=spec.nchange, NMIXUP=spec.nmixup, IF_RESTART=0,
                 IR=IR, JR=JR, KR=KR, NIB1=NIB1, NJB1=NJB1, NKB1=NKB1, NIB2=NIB2, NJB2=NJB2,
@@ -569,6 +580,9 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None, metrics64: boo
                  CONLIM=spec.conlim, VISLAM=0.0, FTCOND=0.0)
     if spec.itimst == -3:
         reals.update(F2=-1.65, F3=-0.65)
+    reals["TURBVIS_LIM"] = spec.turbvis_lim
+    if new_loss:
+        reals["VORT_MAX"] = new_loss_vort
     xl = np.array([r.xllim for r in spec.rows], np.float32)
     arr = dict(
         JSTART=JSTART, JMIX=JMIX, JLE=JLE, JTE=JTE, JLED=JLED, KTIPS=KTIPS, KTIPE=KTIPE, KS1=KS1, KS2=KS2,
@@ -601,6 +615,7 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None, metrics64: boo
         RFORCE=zeros3.copy(), TFORCE=zeros3.copy(), QSOURCE=zeros3.copy(), STEP=STEP, RSTEP=RSTEP,
         Y_PLUS=np.full((KM, JM, IM), 25.0, f32), DPDS_CELL=zeros3.copy(),
     )
+    arr.update(new_loss)
     cd.ints = ints
     cd.reals = reals
     for k, v in arr.items():
@@ -612,7 +627,7 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None, metrics64: boo
 
 
 def wall_distance_sq(IM, JM, KM, X, R, THETA, ASX, ASR, ABX, ABR, ABT, JSTART, JMIX, JLE, JTE, NROW,
-                     NBLADE, IMID, spec, ibound=0):
+                     NBLADE, IMID, spec, ibound=0, with_dist=False):
     """DWALLSQ(I,J,K): the squared cell-average distance to the nearest
     solid wall, as SET_XLENGTH computes it (multall-open-18.3.f:12194-12517)."""
     JRANGE, KRANGE = 20, 5
@@ -699,4 +714,48 @@ def wall_distance_sq(IM, JM, KM, X, R, THETA, ASX, ASR, ABX, ABR, ABT, JSTART, J
     avg = f32(0.125) * (DIST[:-1, 1:, :-1] + DIST[1:, 1:, :-1] + DIST[:-1, :-1, :-1] + DIST[1:, :-1, :-1]
                         + DIST[:-1, 1:, 1:] + DIST[1:, 1:, 1:] + DIST[:-1, :-1, 1:] + DIST[1:, :-1, 1:])
     DW[:KMM1, 1:, :IMM1] = avg * avg
-    return DW
+    return (DW, DIST) if with_dist else DW
+
+
+def mixing_lengths(spec, IM, JM, KM, DIST, SMERID, JSTART, JMIX, JLE, JTE, NROW, IMID, KMID):
+    """XLENGTH and FST_RAT of NEW_LOSS from the node wall distances DIST_MIN
+    (SET_XLENGTH, multall-open-18.3.f:12423-12492): the mixing-length limit
+    XLIMIT(J) interpolated along the meridional distance from XLLIM_IN, _LE,
+    _TE and _DN of the row, the blend of the linear and constant regions, and
+    the cell averages, 0.41**2 times the squared mean length."""
+    KMM1, IMM1 = KM - 1, IM - 1
+    XLIMIT = np.zeros(JM + 1, f32)
+    for J in range(1, JM + 1):
+        nr = NROW[J]
+        xin, xle, xte, xdn = (f32(v) for v in spec.rows[nr - 1].xllim_new)
+        sm = lambda jj: SMERID[KMID - 1, jj - 1]
+        js, jl, jt, jx = JSTART[nr - 1], JLE[nr - 1], JTE[nr - 1], JMIX[nr - 1]
+        if J <= jl:
+            XLLIM = xin + (sm(J) - sm(js)) / (sm(jl) - sm(js)) * (xle - xin)
+        if jl < J <= jt:
+            XLLIM = xle + (sm(J) - sm(jl)) / (sm(jt) - sm(jl)) * (xte - xle)
+        if J > jt:
+            XLLIM = xte + (sm(J) - sm(jt)) / (sm(jx) - sm(jt)) * (xdn - xte)
+        XLIMIT[J] = f32(2.0) * DIST[KMID - 1, J - 1, IMID - 1] * f32(XLLIM)
+    DBLEND = f32(0.6666666)
+    EXPON = DBLEND / (f32(1.0) - DBLEND)
+    FBLEND = (f32(1.0) - DBLEND) * DBLEND ** EXPON
+    XL = XLIMIT[1:][None, :, None]
+    RATIO = DIST / XL
+    with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
+        STORE = np.where(RATIO > DBLEND, XL * (f32(1.0) - FBLEND * RATIO ** (-EXPON)), DIST).astype(f32)
+    TEMP3 = ((STORE / XL) ** 4).astype(f32)
+
+    def avg8(A):
+        return f32(0.125) * (A[:-1, 1:, :-1] + A[1:, 1:, :-1] + A[:-1, :-1, :-1] + A[1:, :-1, :-1]
+                             + A[:-1, 1:, 1:] + A[1:, 1:, 1:] + A[:-1, :-1, 1:] + A[1:, :-1, 1:])
+    XLENGTH = np.zeros((KM, JM, IM), f32)
+    FST_RAT = np.zeros((KM, JM, IM), f32)
+    ax = avg8(STORE)
+    XLENGTH[:KMM1, 1:, :IMM1] = f32(0.41) * f32(0.41) * ax * ax
+    fs = np.array([f32(spec.rows[NROW[J] - 1].fsturb) for J in range(2, JM + 1)], f32)
+    FST_RAT[:KMM1, 1:, :IMM1] = avg8(TEMP3) * fs[None, :, None]
+    first = np.array([J == JSTART[NROW[J] - 1] for J in range(2, JM + 1)])
+    XLENGTH[:KMM1, 1:, :IMM1][:, first, :] = 0.0
+    FST_RAT[:KMM1, 1:, :IMM1][:, first, :] = 0.0
+    return dict(XLENGTH=XLENGTH, FST_RAT=FST_RAT)

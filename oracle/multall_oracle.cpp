@@ -12,6 +12,7 @@
  *   SMOOTH_VAR      15352-15594
  *   SMOOTH_RESID    14833-14917
  *   LOSS            8058-9066   (ILOS=10)
+ *   NEW_LOSS        12522-13508 (ILOS 100-199) and the cell-average density 4255-4267
  *   WALLFUN         15980-16047
  *   NEW_MIXPLAN     14922-15251
  *   STEPUP          7916-8002
@@ -383,7 +384,11 @@ struct Oracle : OracleBase {
 #define O_CHK_R(nm, d) if ((float)nm == MGPU_REQUIRED_REAL) return fail(MGPU_E_ARG, "real not set: " #nm);
         MGPU_REAL_SCALARS(O_CHK_R)
         if (ITIMST != 3) return fail(MGPU_E_UNSUPPORTED, "ITIMST other than 3 (incompressible 5/6) not covered");
-        if (ILOS != 10) return fail(MGPU_E_UNSUPPORTED, "only ILOS=10 (mixing-length LOSS) is covered");
+        if (ILOS != 10 && !(ILOS >= 100 && ILOS < 200))
+            return fail(MGPU_E_UNSUPPORTED, "only ILOS=10 (LOSS) and ILOS 100-199 (NEW_LOSS) are covered");
+        if (ILOS >= 100 && !(VORT_MAX > R(0))) return fail(MGPU_E_ARG, "ILOS 100-199 needs VORT_MAX > 0 (SETUP 7322-7328)");
+        if (ILOS >= 100 && !(XLENGTH_set && FST_RAT_set && ROAVG_CELL_set))
+            return fail(MGPU_E_ARG, "ILOS 100-199 needs XLENGTH, FST_RAT and ROAVG_CELL");
         if (IFGAS != 0) return fail(MGPU_E_UNSUPPORTED, "real-gas IFGAS=1 not covered");
         if (IFCOOL || IFBLEED || IFSHROUD) return fail(MGPU_E_UNSUPPORTED, "cooling/bleed/shroud not covered");
         if (IF_REPEAT != 0) return fail(MGPU_E_UNSUPPORTED, "IF_REPEAT not covered");
@@ -404,6 +409,7 @@ struct Oracle : OracleBase {
         SOURCE.assign(n3, R(0)); FLOWX.assign(n3, R(0)); FLOWT.assign(n3, R(0));
         FLOWR.assign(n3, R(0)); STORE.assign(n3, R(0)); TEMP1.assign(n3, R(0));
         VISC_RAT_v.assign(n3, R(0));
+        VISC_LAM_v.assign(n3, R(0));
         PLIM.assign(KM, R(0)); VLIMIT.assign(NROWS, R(0)); ROLIMIT.assign(NROWS, R(0));
         AVG_CHG.assign(NROWS, R(0)); AVG_BLK.assign(NROWS, R(0));
         BLADE_FLOW.assign(JM, R(0)); CHECK_FLOW.assign(JM, R(0));
@@ -1435,6 +1441,329 @@ struct Oracle : OracleBase {
         }
     }
 
+
+    /* ================================================================== */
+    /*  NEW_LOSS (ILOS 100-199)  multall-open-18.3.f:12522-13462, with      */
+    /*  GRADVEL 13468-13508 and the cell-average density 4255-4267          */
+    /* ================================================================== */
+    void roavg_cell() {
+        for (int k = 1; k <= KMM1; ++k)
+            for (int j = 2; j <= JM; ++j)
+                for (int i = 1; i <= IMM1; ++i)
+                    F3(ROAVG_CELL, i, j, k) =
+                        R(0.125) * (F3(RO, i, j, k) + F3(RO, i + 1, j, k) + F3(RO, i + 1, j, k + 1) + F3(RO, i, j, k + 1) +
+                                    F3(RO, i, j - 1, k) + F3(RO, i + 1, j - 1, k) + F3(RO, i + 1, j - 1, k + 1) +
+                                    F3(RO, i, j - 1, k + 1));
+    }
+
+    // NEW_LOSS's log-law skin friction on the sums of four corner values
+    // (12879-12925 and its three copies)
+    R nl_twall(R RE, R DPERP, R ROUGH, R RO4, R W4) {
+        R RELOG = R(1.) / om::log(RE);
+        R CF;
+        if (ROUGH > R(1.0E-7)) {
+            if (ROUGH > DPERP) ROUGH = DPERP;
+            R REK = RE * ROUGH / DPERP;
+            REK = REK - R(80.0);
+            if (REK < R(0.0)) REK = R(0.0);
+            R REKSQ = REK * REK;
+            R A1 = R(-.00178493) + R(.0000814923) * REK + R(.000000150445) * REKSQ;
+            R A2 = R(.029072) - R(.001584) * REK - R(.00000225194) * REKSQ;
+            R A3c = R(.270313) + R(.0091409) * REK + R(.00000451537) * REKSQ + R(.00000000464767) * REKSQ * REK;
+            CF = A1 + A2 * RELOG + A3c * RELOG * RELOG;
+        } else {
+            CF = R(-0.00178493) + R(0.029072) * RELOG + R(0.270313) * RELOG * RELOG;
+        }
+        R CFLAM = R(2.0) / RE;
+        CF = std::max(CF, CFLAM);
+        if (RE < R(125.)) CF = CFLAM;
+        if (ROUGH > R(1.0E-7)) {
+            R TW = CF * RO4 * W4 * W4 / R(128);
+            R VSTAR = om::sqrt(TW / (RO4 / R(4)));
+            R PLUSK = ROUGH * VSTAR * RO4 / VISLAM / R(4);
+            R RELOG10 = om::log10(DPERP / ROUGH);
+            R FUNCN = R(5.75) * RELOG10 + R(8.5);
+            R CF_FULL_ROUGH = R(2.0) / (FUNCN * FUNCN);
+            if (PLUSK > R(45) && CF > CF_FULL_ROUGH) CF = CF_FULL_ROUGH;
+        }
+        return CF * RO4 * W4 * W4 / R(128);
+    }
+
+    void new_loss() {
+        if (NSTEP == 1 || NSTEP < NSTEPS_MAX / 4) {
+            if (REYNO > R(100.)) {
+                int J1 = F1(JLE, 1), J2 = F1(JTE, 1);
+                if (F1(JLE, 1) > JM) J1 = 1;
+                if (F1(JTE, 1) > JM) J2 = JM;
+                R XCHORD = F2(SMERID, J2, KMID) - F2(SMERID, J1, KMID);
+                R a = F3(ROVX, IMID, J2, KMID), b = F3(ROVR, IMID, J2, KMID), c = F3(ROWT, IMID, J2, KMID);
+                VISLAM = XCHORD * om::sqrt(a * a + b * b + c * c) / REYNO;
+            }
+            if (REYNO > R(0.0) && REYNO < R(99.99)) VISLAM = REYNO / R(100000.);
+            if (REYNO < R(0.0)) VISLAM = -REYNO * R(1.0E-5);
+            TCOND = CP * VISLAM / PRANDTL;
+            FTCOND = TCOND / VISLAM;
+        }
+        const size_t N = (size_t)IM * JM * KM;
+        std::vector<R> FX(N, R(0)), FRr(N, R(0)), FT(N, R(0)), ES(N, R(0));
+        std::vector<R> TXR(N), TXX(N), TXT(N), TRR(N), TRT(N), TTT(N), QXX(N), QRR(N), QTT(N);
+        R FYPLUS = R(0);
+        /* ---- DO 150: strain rates and the eddy viscosity of every cell ---- */
+        for (int k = 1; k <= KMM1; ++k)
+            for (int j = 2; j <= JM; ++j)
+                for (int i = 1; i <= IMM1; ++i) {
+                    auto avg8 = [&](const std::vector<R> &A) {
+                        return R(0.125) * (A3(A, i, j, k) + A3(A, i + 1, j, k) + A3(A, i + 1, j, k + 1) + A3(A, i, j, k + 1) +
+                                           A3(A, i, j - 1, k) + A3(A, i + 1, j - 1, k) + A3(A, i + 1, j - 1, k + 1) +
+                                           A3(A, i, j - 1, k + 1));
+                    };
+                    R WTAVG = avg8(WT_v), ROAVG = F3(ROAVG_CELL, i, j, k), TSAVG = avg8(T_STATIC_v);
+                    R RAVG = F2(RAVG_CELL, j, k);
+                    R DVXDX, DVXDR, DVXDT, DVRDX, DVRDR, DVRDT, DWTDX, DWTDR, DWTDT, DTDX, DTDR, DTDT;
+                    gradvel(i, j, k, VX_v, DVXDX, DVXDR, DVXDT);
+                    gradvel(i, j, k, VR_v, DVRDX, DVRDR, DVRDT);
+                    gradvel(i, j, k, WT_v, DWTDX, DWTDR, DWTDT);
+                    gradvel(i, j, k, T_STATIC_v, DTDX, DTDR, DTDT);
+                    size_t n = ijk(i, j, k);
+                    TXR[n] = DVXDR + DVRDX;
+                    TXX[n] = DVXDX;
+                    TXT[n] = DWTDX + DVXDT;
+                    TRR[n] = DVRDR;
+                    TRT[n] = DWTDR + DVRDT - WTAVG / RAVG;
+                    TTT[n] = DWTDT;
+                    QXX[n] = DTDX;
+                    QRR[n] = DTDR;
+                    QTT[n] = DTDT;
+                    R VORTX = DVRDT - DWTDR - WTAVG / RAVG, VORTR = DWTDX - DVXDT, VORTT = DVXDR - DVRDX;
+                    R VORT = om::sqrt(VORTX * VORTX + VORTR * VORTR + VORTT * VORTT);
+                    if (VORT > VORT_MAX) VORT = VORT_MAX;
+                    R TURBVIS_WALL = ROAVG * F3(XLENGTH, i, j, k) * VORT * FMIXUP;
+                    FYPLUS = fyplus_of(F3(Y_PLUS, i, j, k), YPLAM, YPTURB, FYPLUS);
+                    TURBVIS_WALL = TURBVIS_WALL * FYPLUS;
+                    if (REYNO < R(0.0001)) VISLAM = (om::fabs(REYNO) / R(100000.0)) * om::pow(TSAVG / R(288.0), R(0.62));
+                    R VISTOT = VISLAM * (R(1) + F3(FST_RAT, i, j, k)) + TURBVIS_WALL;
+                    R VISLIM = TURBVIS_LIM * VISLAM;
+                    if (VISTOT > VISLIM) VISTOT = VISLIM;
+                    F3(VISC_RAT, i, j, k) = VISTOT / VISLAM;
+                    F3(VISC_LAM, i, j, k) = VISLAM;
+                }
+        /* ---- DO 160: transition ---- */
+        for (int j = 2; j <= JM; ++j) {
+            int NRW = F1(NROW, j);
+            int JROW = j - F1(JSTART, NRW) + 1;
+            auto line = [&](bool upstream, int i0, int i1, int k0, int k1) {
+                bool lam = upstream;
+                if (!lam) {
+                    R RMAX = R(0.0);
+                    for (int k = k0; k <= k1; ++k)
+                        for (int i = i0; i <= i1; ++i)
+                            if (!(F3(VISC_RAT, i, j, k) < RMAX)) RMAX = F3(VISC_RAT, i, j, k);
+                    lam = !(RMAX > FTRANS);
+                }
+                if (lam)
+                    for (int k = k0; k <= k1; ++k)
+                        for (int i = i0; i <= i1; ++i) F3(VISC_RAT, i, j, k) = R(1.0);
+            };
+            for (int i = 1; i <= IMM1; ++i) {
+                line(JROW < F1(JTRAN_K1, NRW), i, i, 1, KMID);
+                line(JROW < F1(JTRAN_KM, NRW), i, i, KMID, KMM1);
+            }
+            for (int k = 1; k <= KMM1; ++k) {
+                line(JROW < F1(JTRAN_I1, NRW), 1, IMID, k, k);
+                line(JROW < F1(JTRAN_IM, NRW), IMID, IMM1, k, k);
+            }
+        }
+        /* ---- DO 190: stresses and heat flows ---- */
+        for (int k = 1; k <= KMM1; ++k)
+            for (int j = 2; j <= JM; ++j)
+                for (int i = 1; i <= IMM1; ++i) {
+                    size_t n = ijk(i, j, k);
+                    VISLAM = F3(VISC_LAM, i, j, k);
+                    R VISTOT = F3(VISC_RAT, i, j, k) * VISLAM;
+                    R THCOND = CP * VISTOT / PRANDTL;
+                    R VISTOT2 = R(2.0) * VISTOT;
+                    TXR[n] = VISTOT * TXR[n];
+                    TXX[n] = VISTOT2 * TXX[n];
+                    TXT[n] = VISTOT * TXT[n];
+                    TRR[n] = VISTOT2 * TRR[n];
+                    TRT[n] = VISTOT * TRT[n];
+                    TTT[n] = VISTOT2 * TTT[n];
+                    QXX[n] = -THCOND * QXX[n];
+                    QRR[n] = -THCOND * QRR[n];
+                    QTT[n] = -THCOND * QTT[n];
+                }
+        /* TRX = TXR, TTX = TXT, TTR = TRT */
+        if (YPLUSWALL < R(-10.0)) set_pwallgrad();
+        const R VISLAM16 = VISLAM * R(16.0);
+        auto iface = [&](int I, int IM1, int j, int k, R &XFOR, R &RFOR, R &TFOR, R &QFLOW, R &WVISC) {
+            size_t a = ijk(I, j, k), b = ijk(IM1, j, k);
+            R abr = F3(ABR, I, j, k), abt = F2(ABT, j, k), abx = F3(ABX, I, j, k);
+            XFOR = R(0.5) * ((TXR[a] + TXR[b]) * abr + (TXT[a] + TXT[b]) * abt + (TXX[a] + TXX[b]) * abx);
+            RFOR = R(0.5) * ((TRR[a] + TRR[b]) * abr + (TRT[a] + TRT[b]) * abt + (TXR[a] + TXR[b]) * abx);
+            TFOR = R(0.5) * ((TRT[a] + TRT[b]) * abr + (TTT[a] + TTT[b]) * abt + (TXT[a] + TXT[b]) * abx);
+            QFLOW = R(0.5) * ((QXX[a] + QXX[b]) * abx + (QRR[a] + QRR[b]) * abr + (QTT[a] + QTT[b]) * abt);
+            R VXAVG = F3(VX, I, j, k) + F3(VX, I, j - 1, k) + F3(VX, I, j - 1, k + 1) + F3(VX, I, j, k + 1);
+            R VRAVG = F3(VR, I, j, k) + F3(VR, I, j - 1, k) + F3(VR, I, j - 1, k + 1) + F3(VR, I, j, k + 1);
+            R VTAVG = F3(VT, I, j, k) + F3(VT, I, j - 1, k) + F3(VT, I, j - 1, k + 1) + F3(VT, I, j, k + 1);
+            WVISC = R(-0.25) * (XFOR * VXAVG + RFOR * VRAVG + TFOR * VTAVG);
+        };
+        /* ---- DO 200: blade surfaces, the periodic face and the I faces ---- */
+        for (int k = 1; k <= KMM1; ++k)
+            for (int j = 2; j <= JM; ++j) {
+                int NRW = F1(NROW, j);
+                bool wall = F1(IND, j) != 0 &&
+                            !(F1(KTIPS, NRW) > 0 && k >= F1(KTIPS, NRW) && k < F1(KTIPE, NRW));
+                if (wall) {
+                    for (int side = 0; side < 2; ++side) {
+                        int iw = side == 0 ? 2 : IMM1, ic = side == 0 ? 1 : IMM1, ia = side == 0 ? 1 : IM;
+                        auto s4 = [&](const std::vector<R> &A) {
+                            return A3(A, iw, j, k) + A3(A, iw, j - 1, k) + A3(A, iw, j - 1, k + 1) + A3(A, iw, j, k + 1);
+                        };
+                        R VXA = s4(VX_v), VRA = s4(VR_v), WTA = s4(WT_v), ROA = s4(RO_v);
+                        R WAVG = om::sqrt(WTA * WTA + VXA * VXA + VRA * VRA);
+                        R bx = F3(ABX, ia, j, k), br = F3(ABR, ia, j, k), bt = F2(ABT, j, k);
+                        R AREA = om::sqrt(bx * bx + br * br + bt * bt);
+                        R DPERP = F3(VOL, ic, j, k) / AREA;
+                        R TW;
+                        if (YPLUSWALL < R(-0.001)) {
+                            R &yp = side == 0 ? F2(YPLUS_I1, j, k) : F2(YPLUS_IM, j, k);
+                            R YN;
+                            wallfun(DPERP, F3(DPDS_CELL, ic, j, k), R(0.25) * ROA, TW, yp, R(0.25) * WAVG, YN);
+                            yp = std::min(R(1000.0), YN);
+                        } else {
+                            R RE = DPERP * ROA * WAVG / VISLAM16;
+                            TW = nl_twall(RE, DPERP, side == 0 ? F1(ROUGH_L, NRW) : F1(ROUGH_U, NRW), ROA, WAVG);
+                        }
+                        int i0 = side == 0 ? 1 : IMID + 1, i1 = side == 0 ? IMID : IMM1;
+                        for (int i = i0; i <= i1; ++i) {
+                            R VSTAR = om::sqrt(TW / (R(0.25) * ROA));
+                            R YPLS = VSTAR * om::sqrt(F3(DWALLSQ, i, j, k)) * (R(0.25) * ROA) / VISLAM;
+                            F3(Y_PLUS, i, j, k) = std::min(R(1000.0), YPLS);
+                        }
+                        R FMULT = -TW * AREA / WAVG;
+                        R TFc = FMULT * WTA;
+                        size_t c = ijk(ic, j, k);
+                        FX[c] = FX[c] + FMULT * VXA;
+                        FRr[c] = FRr[c] + FMULT * VRA;
+                        FT[c] = FT[c] + TFc;
+                        ES[c] = ES[c] + TFc * F1(WRAD, j) * F2(RAVG_CELL, j, k);
+                    }
+                }
+                bool skip = (F1(IND, j) == 1 && k < F1(KTIPS, NRW)) || k > F1(KTIPE, NRW);
+                R XFOR, RFOR, TFOR, QFLOW, WVISC;
+                if (!skip) {
+                    iface(1, IMM1, j, k, XFOR, RFOR, TFOR, QFLOW, WVISC);
+                    size_t a = ijk(1, j, k), b = ijk(IMM1, j, k);
+                    std::vector<R> *FF[3] = {&FX, &FRr, &FT};
+                    R fl[3] = {XFOR, RFOR, TFOR};
+                    for (int f = 0; f < 3; ++f) {
+                        std::vector<R> &A = *FF[f];
+                        A[b] = A[b] + fl[f];
+                        A[a] = A[a] - fl[f];
+                        R AVG = R(0.5) * (A[a] + A[b]);
+                        A[a] = AVG;
+                        A[b] = AVG;
+                    }
+                    ES[a] = ES[a] + QFLOW + WVISC;
+                    ES[b] = ES[b] - QFLOW - WVISC;
+                    R AVG = R(0.5) * (ES[a] + ES[b]);
+                    ES[a] = AVG;
+                    ES[b] = AVG;
+                }
+                for (int I = 2; I <= IMM1; ++I) {
+                    iface(I, I - 1, j, k, XFOR, RFOR, TFOR, QFLOW, WVISC);
+                    size_t a = ijk(I, j, k), b = ijk(I - 1, j, k);
+                    FX[b] = FX[b] + XFOR;
+                    FX[a] = FX[a] - XFOR;
+                    FRr[b] = FRr[b] + RFOR;
+                    FRr[a] = FRr[a] - RFOR;
+                    FT[b] = FT[b] + TFOR;
+                    FT[a] = FT[a] - TFOR;
+                    ES[a] = ES[a] + QFLOW + WVISC;
+                    ES[b] = ES[b] - QFLOW - WVISC;
+                }
+            }
+        /* ---- DO 400: hub and casing, then the K faces ---- */
+        for (int j = 2; j <= JM; ++j) {
+            int NRW = F1(NROW, j);
+            for (int i = 1; i <= IMM1; ++i) {
+                for (int side = 0; side < 2; ++side) {
+                    int kn = side == 0 ? 2 : KMM1, kc = side == 0 ? 1 : KMM1, ka = side == 0 ? 1 : KM;
+                    auto s4 = [&](const std::vector<R> &A) {
+                        return A3(A, i, j, kn) + A3(A, i + 1, j, kn) + A3(A, i + 1, j - 1, kn) + A3(A, i, j - 1, kn);
+                    };
+                    R VXA = s4(VX_v), VRA = s4(VR_v), VTA = s4(VT_v), ROA = s4(RO_v);
+                    R RAVG = F2(R, j, kn) + F2(R, j, kn) + F2(R, j - 1, kn) + F2(R, j - 1, kn);
+                    R WW = side == 0 ? F1(WHUB, j) : F1(WTIP, j);
+                    R WTA = VTA - WW * RAVG;
+                    R WAVG = om::sqrt(VXA * VXA + VRA * VRA + WTA * WTA);
+                    R sx = F3(ASX, i, j, ka), sr = F3(ASR, i, j, ka);
+                    R AREA = om::sqrt(sx * sx + sr * sr);
+                    R DPERP = F3(VOL, i, j, kc) / AREA;
+                    R TW;
+                    if (YPLUSWALL < R(-0.001)) {
+                        R &yp = side == 0 ? FIJ(YPLUS_K1, i, j) : FIJ(YPLUS_KM, i, j);
+                        R YN;
+                        wallfun(DPERP, F3(DPDS_CELL, i, j, kc), R(0.25) * ROA, TW, yp, R(0.25) * WAVG, YN);
+                        yp = std::min(R(1000.0), YN);
+                    } else {
+                        R RE = DPERP * ROA * WAVG / VISLAM16;
+                        TW = nl_twall(RE, DPERP, side == 0 ? F1(ROUGH_H, NRW) : F1(ROUGH_T, NRW), ROA, WAVG);
+                    }
+                    bool yset = side == 0 ? (IBOUND == 0 || IBOUND == 2) : (IBOUND <= 1);
+                    if (yset) {
+                        int k0 = side == 0 ? 1 : KMID + 1, k1 = side == 0 ? KMID : KMM1;
+                        for (int k = k0; k <= k1; ++k) {
+                            R VSTAR = om::sqrt(TW / (R(0.25) * ROA));
+                            R YPLS = VSTAR * om::sqrt(F3(DWALLSQ, i, j, k)) * (R(0.25) * ROA) / VISLAM;
+                            R YPLSP = F3(Y_PLUS, i, j, k);
+                            F3(Y_PLUS, i, j, k) = std::min(YPLS, YPLSP);
+                        }
+                    }
+                    R FMULT = -TW * AREA / WAVG;
+                    if (side == 0 ? (IBOUND == 1 || IBOUND > 2) : (IBOUND >= 2)) FMULT = R(0.0);
+                    R TFc = FMULT * WTA;
+                    size_t c = ijk(i, j, kc);
+                    FX[c] = FX[c] + FMULT * VXA;
+                    FRr[c] = FRr[c] + FMULT * VRA;
+                    FT[c] = FT[c] + TFc;
+                    ES[c] = ES[c] + TFc * R(0.25) * WW * RAVG;
+                }
+                for (int K = 2; K <= KMM1; ++K) {
+                    size_t a = ijk(i, j, K), b = ijk(i, j, K - 1);
+                    R sr = F3(ASR, i, j, K), sx = F3(ASX, i, j, K);
+                    R XFOR = R(0.5) * ((TXR[a] + TXR[b]) * sr + (TXX[a] + TXX[b]) * sx);
+                    R RFOR = R(0.5) * ((TRR[a] + TRR[b]) * sr + (TXR[a] + TXR[b]) * sx);
+                    R TFOR = R(0.5) * ((TRT[a] + TRT[b]) * sr + (TXT[a] + TXT[b]) * sx);
+                    R QFLOW = R(0.5) * ((QXX[a] + QXX[b]) * sx + (QRR[a] + QRR[b]) * sr);
+                    R VXAVG = F3(VX, i, j, K) + F3(VX, i + 1, j, K) + F3(VX, i + 1, j - 1, K) + F3(VX, i, j - 1, K);
+                    R VRAVG = F3(VR, i, j, K) + F3(VR, i + 1, j, K) + F3(VR, i + 1, j - 1, K) + F3(VR, i, j - 1, K);
+                    R VTAVG = F3(VT, i, j, K) + F3(VT, i + 1, j, K) + F3(VT, i + 1, j - 1, K) + F3(VT, i, j - 1, K);
+                    R WVISC = R(-0.25) * (XFOR * VXAVG + RFOR * VRAVG + TFOR * VTAVG);
+                    FX[b] = FX[b] + XFOR;
+                    FX[a] = FX[a] - XFOR;
+                    FRr[b] = FRr[b] + RFOR;
+                    FRr[a] = FRr[a] - RFOR;
+                    FT[b] = FT[b] + TFOR;
+                    FT[a] = FT[a] - TFOR;
+                    ES[a] = ES[a] + QFLOW + WVISC;
+                    ES[b] = ES[b] - QFLOW - WVISC;
+                }
+            }
+        }
+        /* ---- DO 500 ---- */
+        R RF_VIS1 = R(1.0) - RF_VIS;
+        for (int k = 1; k <= KMM1; ++k)
+            for (int j = 2; j <= JM; ++j)
+                for (int i = 1; i <= IMM1; ++i) {
+                    size_t n = ijk(i, j, k);
+                    F3(XFORCE, i, j, k) = RF_VIS1 * F3(XFORCE, i, j, k) - RF_VIS * FX[n];
+                    F3(TFORCE, i, j, k) = RF_VIS1 * F3(TFORCE, i, j, k) - RF_VIS * FT[n] * F2(RAVG_CELL, j, k);
+                    F3(RFORCE, i, j, k) = RF_VIS1 * F3(RFORCE, i, j, k) - RF_VIS * FRr[n];
+                    F3(QSOURCE, i, j, k) = RF_VIS1 * F3(QSOURCE, i, j, k) - RF_VIS * ES[n];
+                }
+    }
+
     int loss_init() override {
         if (!committed) return fail(MGPU_E_STATE, "loss_init before commit");
         R save_rf = RF_VIS, save_fm = FMIXUP;
@@ -1442,7 +1771,8 @@ struct Oracle : OracleBase {
         RF_VIS = R(1.0);
         FMIXUP = R(1.0);
         NSTEP = 1;
-        loss();
+        if (ILOS >= 100) new_loss();
+        else loss();
         RF_VIS = save_rf;
         FMIXUP = save_fm;
         NSTEP = save_n;
@@ -1654,8 +1984,10 @@ struct Oracle : OracleBase {
                     F3(T_STATIC, i, j, k) = TSTATIC;
                 }
         if (ILOS == 10 && NSTEP % NLOS == 0 && !FROZEN) loss();
+        if (ILOS >= 100 && ILOS < 200 && NSTEP % NLOS == 0 && !FROZEN) new_loss();
         mass_fluxes();
         tstep(RO_v, DRO_v);
+        if (ILOS >= 100) roavg_cell();
         energy_fluxes();
         tstep(ROE_v, DROE_v);
         boundary_conditions();

@@ -401,3 +401,30 @@ def test_flow_out_of_another_grid_is_refused(mods, tmp_path):
     other = common_setup.build_common(case.small_nozzle())
     with pytest.raises(O.OracleError, match="not a flow_out file of this grid"):
         O.Oracle(other, restart=f)
+
+
+def test_new_loss_oracle_float_vs_double(mods):
+    """NEW_LOSS (ILOS=100) in the oracle: the mixing lengths SETUP derives
+    are zero on the first cell of each row and FST_RAT stays within FSTURB;
+    after SETUP's call and ten steps (NEW_LOSS on steps 5 and 10) the FP32
+    restatement agrees with the FP64 one to 1e-4 on the state, forces and
+    viscosity ratios."""
+    case, common_setup, O = mods[0], mods[1], mods[2]
+    spec = case.small_stage()
+    spec.ilos = 100
+    cd = common_setup.build_common(spec)
+    JS = cd.arrays["JSTART"]
+    for j0 in JS[1:]:
+        assert not cd.arrays["XLENGTH"][:-1, j0 - 1, :-1].any()
+    assert cd.arrays["FST_RAT"].max() <= 1.0 and cd.arrays["XLENGTH"].max() > 0.0
+    assert cd.reals["VORT_MAX"] > 0.0
+    of, od = O.Oracle(cd), O.Oracle(cd, double=True)
+    of.setup_calls()
+    od.setup_calls()
+    for n in ("XFORCE", "QSOURCE", "VISC_RAT", "Y_PLUS"):
+        assert rel_linf(of.get(n, double=False), od.get(n)) <= 1e-5, n
+    for _ in range(10):
+        of.step()
+        od.step()
+    for n in ("RO", "ROVX", "ROE", "XFORCE", "RFORCE", "TFORCE", "QSOURCE", "VISC_RAT", "ROAVG_CELL"):
+        assert rel_linf(of.get(n, double=False), od.get(n)) <= 1e-4, n

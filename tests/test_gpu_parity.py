@@ -428,3 +428,79 @@ def test_handles_of_different_sizes_keep_their_launch_limits(mods):
     b.run(6)
     assert np.array_equal(pb2.get("RO"), alone)
     b.close()
+
+
+def _new_loss_spec(case, opt):
+    spec = case.small_stage()
+    spec.ilos = 100
+    if opt == "wall_functions":
+        spec.ypluswall = -15.0
+    elif opt == "reyno_temperature":
+        spec.reyno = -4.0
+    elif opt == "no_tip_gap":
+        for r in spec.rows:
+            r.tip_gap = 0.0
+    return spec
+
+
+NEW_LOSS_OPTS = ["log_law", "wall_functions", "reyno_temperature", "rough_transition", "ibound1", "no_tip_gap"]
+
+
+def _new_loss_pair(mods, opt):
+    case, common_setup, lib, O = mods
+    cd = common_setup.build_common(_new_loss_spec(case, opt))
+    if opt == "rough_transition":
+        nr = cd.arrays["ROUGH_H"].size
+        for n, v in (("ROUGH_H", 2e-5), ("ROUGH_T", 1e-5), ("ROUGH_L", 3e-5), ("ROUGH_U", 5e-6)):
+            cd.arrays[n] = np.full(nr, v, np.float32)
+        for n, v in (("JTRAN_I1", 8), ("JTRAN_IM", 12), ("JTRAN_K1", 4), ("JTRAN_KM", 20)):
+            cd.arrays[n] = np.full(nr, v, np.int32)
+        cd.reals["FTRANS"] = 2.0
+    elif opt == "ibound1":
+        cd.ints["IBOUND"] = 1
+    gpu = lib.Problem(cd)
+    ref = O.Oracle(cd)
+    ref.setup_calls()
+    return cd, gpu, ref
+
+
+@pytest.mark.parametrize("opt", NEW_LOSS_OPTS)
+def test_new_loss_setup_call(mods, opt):
+    """NEW_LOSS (ILOS=100) as SETUP calls it: the eddy viscosity, the wall
+    shear stresses (log law with roughness, or the Shih wall functions with
+    the pressure-gradient term), transition, the stresses summed over the I
+    and K faces, and the relaxed body forces, within 1e-5 of the FP32 oracle."""
+    cd, gpu, ref = _new_loss_pair(mods, opt)
+    _compare(gpu, ref, FORCES + ["VISC_RAT", "VISC_LAM", "ROAVG_CELL"], STEP1_TOL, f"NEW_LOSS setup ({opt})")
+    if opt == "wall_functions":
+        _compare(gpu, ref, ["YPLUS_I1", "YPLUS_IM", "YPLUS_K1", "YPLUS_KM", "DPDS_CELL"], STEP1_TOL, "wall functions")
+    if opt == "rough_transition":
+        v = gpu.get("VISC_RAT")
+        assert np.count_nonzero(v == 1.0) > 0          # some lines were made laminar
+    assert np.abs(gpu.get("XFORCE")).max() > 0.0
+
+
+@pytest.mark.parametrize("opt", NEW_LOSS_OPTS)
+def test_new_loss_ten_steps(mods, opt):
+    """Ten steps with NEW_LOSS on steps 5 and 10 and the cell-average
+    density formed after TSTEP(RO) on every step: state, forces, viscosity
+    ratios and ROAVG_CELL within 1e-4 of the FP32 oracle."""
+    cd, gpu, ref = _new_loss_pair(mods, opt)
+    for _ in range(10):
+        mg = gpu.step()
+        ref.step()
+    assert mg.tail_ran == 1
+    _compare(gpu, ref, STATE + FORCES + ["VISC_RAT", "VISC_LAM", "ROAVG_CELL"], 1e-4, f"NEW_LOSS step 10 ({opt})")
+
+
+def test_new_loss_long_run(mods):
+    """300 steps of the small stage under NEW_LOSS through the graph
+    (mgpu_run): the flow field within 1e-3 and the mass flow within 1e-4 of
+    the FP32 oracle."""
+    cd, gpu, ref = _new_loss_pair(mods, "log_law")
+    gpu.run(300)
+    for _ in range(300):
+        mr = ref.step()
+    _compare(gpu, ref, ["RO", "ROVX", "ROE", "P", "VISC_RAT"], 1e-3, "NEW_LOSS step 300")
+    ig, ir = gpu.integrals(), ref.integrals()
+    assert abs(ig.mass_flow_in - ir.mass_flow_in) <= 1e-4 * abs(ir.mass_flow_in)
