@@ -504,3 +504,23 @@ def test_new_loss_long_run(mods):
     _compare(gpu, ref, ["RO", "ROVX", "ROE", "P", "VISC_RAT"], 1e-3, "NEW_LOSS step 300")
     ig, ir = gpu.integrals(), ref.integrals()
     assert abs(ig.mass_flow_in - ir.mass_flow_in) <= 1e-4 * abs(ir.mass_flow_in)
+
+
+def test_new_loss_stage_config_setup_call(mods):
+    """NEW_LOSS at the single-stage turbine's full size, 65 x 242 x 49, with
+    the long sums in the reference's sequential REAL*4 order (REDUCE_ORDER=1,
+    as the other full-size parity tests): SETUP's call and then one step
+    within 1e-5 of the FP32 oracle."""
+    case, common_setup, lib, O = mods
+    spec = case.turbine_stage()
+    spec.ilos = 100
+    cd = common_setup.build_common(spec)
+    cd.ints["REDUCE_ORDER"] = 1
+    gpu = lib.Problem(cd)
+    ref = O.Oracle(cd)
+    ref.setup_calls()
+    _compare(gpu, ref, FORCES + ["VISC_RAT", "VISC_LAM"], STEP1_TOL, "stage NEW_LOSS setup")
+    gpu.step()
+    ref.step()
+    _compare(gpu, ref, STATE + ["ROAVG_CELL"], STEP1_TOL, "stage NEW_LOSS step 1")
+    gpu.close()
