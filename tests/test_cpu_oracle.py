@@ -428,3 +428,24 @@ def test_new_loss_oracle_float_vs_double(mods):
         od.step()
     for n in ("RO", "ROVX", "ROE", "XFORCE", "RFORCE", "TFORCE", "QSOURCE", "VISC_RAT", "ROAVG_CELL"):
         assert rel_linf(of.get(n, double=False), od.get(n)) <= 1e-4, n
+
+
+def test_new_loss_inputs_are_required(mods):
+    """ILOS 100-199 needs the SETUP-made mixing lengths and VORT_MAX, and
+    ILOS 200 (Spalart-Allmaras) is refused as not covered, as mgpu_commit
+    does."""
+    case, common_setup, O = mods[0], mods[1], mods[2]
+    spec = case.small_nozzle()
+    spec.ilos = 100
+    cd = common_setup.build_common(spec)
+    bad = common_setup.build_common(spec)
+    del bad.arrays["XLENGTH"]
+    with pytest.raises(O.OracleError, match="XLENGTH"):
+        O.Oracle(bad)
+    bad = common_setup.build_common(spec)
+    bad.reals["VORT_MAX"] = 0.0
+    with pytest.raises(O.OracleError, match="VORT_MAX"):
+        O.Oracle(bad)
+    cd.ints["ILOS"] = 200
+    with pytest.raises(O.OracleError, match="ILOS"):
+        O.Oracle(cd)
