@@ -1,6 +1,7 @@
-"""Generates the regression fixture small_stage_10steps.npz: the FP32
-oracle's state after SETUP's calls and 10 LOOP iterations on the seeded
-small stage case.  The reference ships no outputs, so this fixture pins the
+"""Generates the regression fixtures small_stage_10steps.npz and
+small_stage_newloss_10steps.npz: the FP32 oracle's state after SETUP's calls
+and 10 LOOP iterations on the seeded small stage case, with LOSS (ILOS=10)
+and with NEW_LOSS (ILOS=100).  The reference ships no outputs, so this fixture pins the
 oracle against itself (a guard against accidental changes), not against the
 reference.  Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -18,14 +19,22 @@ from mgpu import case, common_setup  # noqa: E402
 import oracle as O  # noqa: E402
 
 
-def main():
-    cd = common_setup.build_common(case.small_stage())
-    o = O.Oracle(cd)
+def run(ilos, names, fname):
+    spec = case.small_stage()
+    spec.ilos = ilos
+    o = O.Oracle(common_setup.build_common(spec))
     o.setup_calls()
     for _ in range(10):
         o.step()
-    out = {n: o.get(n, double=False) for n in ("RO", "ROVX", "ROVR", "RORVT", "ROE", "XFORCE", "STEP")}
-    np.savez_compressed(os.path.join(HERE, "small_stage_10steps.npz"), **out)
+    np.savez_compressed(os.path.join(HERE, fname), **{n: o.get(n, double=False) for n in names})
+
+
+def main():
+    run(10, ("RO", "ROVX", "ROVR", "RORVT", "ROE", "XFORCE", "STEP"), "small_stage_10steps.npz")
+    run(100, NEW_LOSS_FIELDS, "small_stage_newloss_10steps.npz")
+
+
+NEW_LOSS_FIELDS = ("RO", "ROVX", "ROE", "XFORCE", "TFORCE", "QSOURCE", "VISC_RAT", "Y_PLUS")
 
 
 if __name__ == "__main__":

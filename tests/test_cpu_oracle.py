@@ -140,6 +140,21 @@ def test_golden_regression(mods):
         assert np.array_equal(o.get(n, double=False), g[n]), n
 
 
+def test_golden_regression_new_loss(mods):
+    """The same guard for NEW_LOSS (ILOS=100): ten steps of the small stage
+    reproduce tests/golden/small_stage_newloss_10steps.npz bit for bit."""
+    case, common_setup, O = mods
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "small_stage_newloss_10steps.npz"))
+    spec = case.small_stage()
+    spec.ilos = 100
+    o = O.Oracle(common_setup.build_common(spec))
+    o.setup_calls()
+    for _ in range(10):
+        o.step()
+    for n in g.files:
+        assert np.array_equal(o.get(n, double=False), g[n]), n
+
+
 def test_abi_library_exports_every_declared_symbol():
     """libmgpu.so loads without a GPU and exports each function
     include/mgpu.h declares."""
