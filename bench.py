@@ -48,6 +48,10 @@ WORKLOADS = {
                 "discrete adjoint (frozen mixing length) of the single-stage turbine 65x242x49, SFXIN=SFTIN=0.02: "
                 "gradients of eta_tt and inlet mass flow w.r.t. 30 blade-angle design variables "
                 "(stagger, inlet and exit metal angle at 5 span sections x 2 rows)"),
+    "converge": ("turbine_stage",
+                 "single-stage axial turbine 65x242x49 as the headline workload with SFXIN=SFTIN=0.02, marched "
+                 "from SETUP's initial guess to the reference's end test (EAVG or |EMAX| below CONLIM=1e-5 with "
+                 "ECONT < 1%): default precision split against the plain FP32 path"),
     "batch64": ("batch_instance",
                 "64 single-stage turbines in one batch graph: I in {33,49,65}, K in {33,49}, J in [97,161], "
                 "exit P/P0 in [0.45,0.70], 7000-10000 rpm (seeded), SCREE, mixing-length LOSS/5 steps"),
@@ -65,12 +69,15 @@ B_ALG_STEP = 132
 #   update  STORE, D read; TMP written
 #   smooth  TMP read; D written
 KERNEL_BYTES = {
-    "k_prim": (48, 1), "k_flux_mass": (60, 1), "k_flux_energy": (40, 1),
+    # mass and energy fluxes: ROVX, ROVR, RO, ROVT, 6 areas, HO, PEFF, QSOURCE read (13 arrays); FLOWX, FLOWT,
+    # FLOWR, ROWT, WT and ROE's XFLUX, TFLUX, RFLUX, SOURCE written (9)
+    "k_prim": (48, 1), "k_flux_mass_energy": (88, 1),
     # momentum fluxes: 19 arrays read (P, V*, ROVT, FLOW*, 6 areas, VOLOR, 3 forces, RO for the
     # density-limiter flags), 13 written (9 fluxes, 3 sources, PEFF)
     "k_flux_mom": (128, 1),
     "k_mach_limiter": (24, 1),
-    "k_ts_cells": (28, 5), "k_ts_prolong": (16, 5), "k_ts_update": (12, 5), "k_ts_smooth": (8, 5),
+    "k_ts_cells": (28, 5), "k_ts_prolong": (16, 5), "k_ts_update": (12, 5), "k_ts_update_pair": (12, 5),
+    "k_ts_smooth": (8, 5),
     "k_loss_kfaces": (72, 0.2), "k_loss_ifaces": (84, 0.2),
 }
 PROFILE_STEPS = 10
@@ -108,6 +115,70 @@ def ncu_traffic_per_launch():
             except ValueError:
                 pass
     return out
+
+
+class NvmlSampler:
+    """SM clock and clock-event reasons read through NVML (the driver's
+    libnvidia-ml, bound with ctypes) every ~2 ms on a thread, so that a timed
+    region of a few milliseconds still holds samples.  Reads only."""
+    SM_CLOCK = 1
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown", 0x4: "sw_power_cap"}
+
+    def __init__(self, gpu_index=0):
+        import ctypes
+        self.ct = ctypes
+        self.nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.nv.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        if self.nv.nvmlDeviceGetHandleByIndex_v2(gpu_index, ctypes.byref(self.h)) != 0:
+            raise OSError("no NVML device")
+        try:
+            self.reasons_fn = self.nv.nvmlDeviceGetCurrentClocksEventReasons
+        except AttributeError:
+            self.reasons_fn = self.nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint()
+        self.nv.nvmlDeviceGetMaxClockInfo(self.h, self.SM_CLOCK, ctypes.byref(mx))
+        self.max_mhz = float(mx.value)
+        self.rows = []
+        self.stop = threading.Event()
+
+    def _read(self):
+        ct = self.ct
+        mhz, rs = ct.c_uint(), ct.c_ulonglong()
+        while not self.stop.is_set():
+            if self.nv.nvmlDeviceGetClockInfo(self.h, self.SM_CLOCK, ct.byref(mhz)) == 0:
+                r = rs.value if self.reasons_fn(self.h, ct.byref(rs)) == 0 else 0
+                self.rows.append((float(mhz.value), int(r)))
+            time.sleep(0.002)
+
+    def __enter__(self):
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=2)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": [], "samples": 0, "source": "nvml"}
+        reasons = set()
+        for _, r in self.rows:
+            for bit, name in self.REASONS.items():
+                if r & bit:
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(m for m, _ in self.rows), "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(reasons), "samples": len(self.rows), "source": "nvml, every ~2 ms"}
+
+
+def clock_sampler(gpu_index=0):
+    """NVML sampler when the driver's library loads, else nvidia-smi."""
+    try:
+        return NvmlSampler(gpu_index)
+    except (OSError, AttributeError):
+        return ClockSampler(gpu_index)
 
 
 class ClockSampler:
@@ -162,6 +233,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def pinned_like(a):
+    """A page-locked host copy of a (torch's pinned allocator), as a numpy
+    view; a plain copy when pinning is unavailable."""
+    try:
+        import torch
+        t = torch.empty(a.shape, dtype=getattr(torch, a.dtype.name), pin_memory=True)
+        out = t.numpy()            # shares t's storage and keeps it alive
+        out[...] = a
+        return out
+    except Exception:
+        return a.copy()
+
+
 def dist_setup(world, rank):
     if world <= 1:
         return None
@@ -169,6 +253,24 @@ def dist_setup(world, rank):
     os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
     dist.init_process_group("gloo", rank=rank, world_size=world)
     return dist
+
+
+def replica_setup(world, rank, local_rank):
+    """One process per GPU: rank r sees only GPU local_rank, and the ranks
+    join one gloo group for the host-side barrier and the max-over-ranks
+    time (there is no data-path collective: each rank marches its own
+    instance)."""
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local_rank)
+    return dist_setup(world, rank)
+
+
+def replica_value(dist, world, nodes_per_rank, steps, ms_local):
+    """(slowest rank's ms, whole-job Gnode-iter/s): every rank marched
+    nodes_per_rank nodes for `steps` steps; the job took the slowest rank's
+    time."""
+    ms_max = dist_max(dist, ms_local)
+    return ms_max, nodes_per_rank * steps * world / (ms_max / 1e3) / 1e9
 
 
 def dist_max(dist, x):
@@ -193,22 +295,63 @@ def build_case():
     return common_setup.build_common(spec)
 
 
-def cpu_oracle_rate(cd, seconds, max_steps):
-    """Serial CPU oracle (FP32) on the workload: (Gnode-iter/s, steps, s)."""
+def host_cpu():
+    """nproc and the CPU model of the host the CPU baseline runs on."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.TimeoutExpired):
+        pass
+    if model is None and os.path.exists("/proc/cpuinfo"):
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    return {"nproc": os.cpu_count(), "model": model}
+
+
+def cpu_oracle_rate(cd, seconds, max_steps, warmup=1):
+    """Serial CPU oracle (FP32) on the workload, the process pinned to one
+    core for the timed steps (as `taskset -c <core>` would): a dict with
+    Gnode-iter/s, steps, seconds, the core, the host and the reference's own
+    figure, CPU time per point per step (multall-open-18.3.f:5404-5414)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
     o = O.Oracle(cd)
     o.setup_calls()
-    o.step()                                  # warm-up step
-    t0 = time.perf_counter()
-    n = 0
-    while n < max_steps and (n == 0 or time.perf_counter() - t0 < seconds):
+    for _ in range(warmup):
         o.step()
-        n += 1
-    dt = time.perf_counter() - t0
+    old = os.sched_getaffinity(0) if hasattr(os, "sched_getaffinity") else None
+    core = min(old) if old else None
+    if core is not None:
+        os.sched_setaffinity(0, {core})
+    try:
+        t0 = time.perf_counter()
+        n = 0
+        while n < max_steps and (n == 0 or time.perf_counter() - t0 < seconds):
+            o.step()
+            n += 1
+        dt = time.perf_counter() - t0
+    finally:
+        if old is not None:
+            os.sched_setaffinity(0, old)
     o.close()
-    return cd.nodes() * n / dt / 1e9, n, dt
+    return {"rate": cd.nodes() * n / dt / 1e9, "steps": n, "seconds": dt, "warmup": warmup, "core": core,
+            "host": host_cpu(), "cpu_time_per_point_per_step_s": dt / n / cd.nodes()}
+
+
+def cpu_baseline_entry(r, what):
+    return {"value": r["rate"], "unit": METRIC, "cores": 1, "kind": "port",
+            "pinned_core": r["core"], "host": r["host"],
+            "cpu_time_per_point_per_step_s": r["cpu_time_per_point_per_step_s"],
+            "sample": f"{r['steps']} LOOP iterations of {what} after {r['warmup']} warm-up, serial C++ "
+                      f"restatement of LOOP (oracle) built -O2 -ffp-contract=off, one thread pinned to core "
+                      f"{r['core']}, {r['seconds']:.1f} s"}
 
 
 def run_reference(args, rank, world):
@@ -216,16 +359,15 @@ def run_reference(args, rank, world):
         return 0
     cd = build_case()
     budget = float(os.environ.get("MGPU_REF_SECONDS", "120"))
-    rate, n, dt = cpu_oracle_rate(cd, budget, max(1, args.steps))
+    r = cpu_oracle_rate(cd, budget, max(1, args.steps), warmup=max(1, min(args.warmup, 3)))
+    rate, n, dt = r["rate"], r["steps"], r["seconds"]
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": METRIC, "n_gpus": args.gpus,
-        "steps": n, "warmup": 1, "ms_per_step": dt / n * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "steps": n, "warmup": r["warmup"], "ms_per_step": dt / n * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOADS[ARGS_WORKLOAD][1], "nodes": cd.nodes(),
-                   "parallelism": "serial CPU (the reference is serial)"},
-        "cpu_baseline": {"value": rate, "unit": METRIC, "cores": 1, "kind": "port",
-                         "sample": f"{n} LOOP iterations of the workload after 1 warm-up, serial C++ restatement "
-                                   f"(oracle) built -O2 -ffp-contract=off, {dt:.1f} s"},
+                   "parallelism": "serial CPU: the reference is a serial program, so one thread is all it uses"},
+        "cpu_baseline": cpu_baseline_entry(r, "the workload"),
         "e2e": {"value": rate, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -261,7 +403,7 @@ def run_batch(args, rank, world, local_rank):
     batch = lib.Batch(probs)
     batch.run(max(args.warmup, 3))
     dist_barrier(dist)
-    with ClockSampler(0) as clk:
+    with clock_sampler(0) as clk:
         ms = batch.bench_steps(args.steps, flush_l2=True)
     dist_barrier(dist)
     ms_max = dist_max(dist, ms)
@@ -396,7 +538,7 @@ def run_adjoint(args, rank, world, local_rank):
     grads, solves = {}, {}
     t_adj = 0.0
     d2h = 0
-    with ClockSampler(0) as clk:
+    with clock_sampler(0) as clk:
         for obj in ("eta_tt", "mass_flow_in"):
             t0 = time.perf_counter()
             p.adjoint_prepare()
@@ -461,10 +603,88 @@ def run_adjoint(args, rank, world, local_rank):
     return 0
 
 
-def run_gpu(args, rank, world, local_rank):
+CONVERGE_SMOOTHING = 0.02      # SFXIN = SFTIN: with the default 0.005 the stage does not settle
+CONVERGE_MAXSTEPS = 40000
+
+
+def run_converge(args, rank, world, local_rank):
+    """Time to convergence on the stage: each path from SETUP's initial guess
+    to the reference's end test (multall-open-18.3.f:3762-3764) through
+    mgpu_run, with mass flow and efficiency at the stop compared with the
+    FP64 oracle's converged values (tests/golden/stage_converged_fp64.json,
+    made by tests/golden/make_converged_fp64.py).  The paths: the default
+    precision split (FP64 long sums) and the plain FP32 path (REDUCE_ORDER=2,
+    the same trees with FP32 adds)."""
     if world > 1:
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local_rank)
-    dist = dist_setup(world, rank)
+        if rank != 0:
+            return 0            # replicas only: one problem per GPU, reported by rank 0
+    from mgpu import case, common_setup, lib
+    fx_path = os.path.join(ROOT, "tests", "golden", "stage_converged_fp64.json")
+    fx = json.load(open(fx_path)) if os.path.exists(fx_path) else None
+
+    def spec():
+        sp = case.turbine_stage()
+        sp.sfxin = sp.sftin = CONVERGE_SMOOTHING
+        return sp
+
+    # warm-up: one short run builds the library's graph and loads the kernels
+    w = lib.Problem(common_setup.build_common(spec()))
+    w.run(max(args.warmup, 3))
+    w.close()
+    res = {}
+    state_names = ["RO", "ROVX", "ROVR", "RORVT", "ROE"]
+    with clock_sampler(0) as clk:
+        for name, order in (("chosen", 0), ("plain_fp32", 2)):
+            cd = common_setup.build_common(spec())
+            cd.ints["NSTEPS_MAX"] = CONVERGE_MAXSTEPS
+            cd.ints["REDUCE_ORDER"] = order
+            p = lib.Problem(cd)
+            tuned, _ = p.autotune()       # restores the state it times on
+            p.run(0)                      # builds the step graph outside the timed region
+            p.sync()
+            t0 = time.perf_counter()
+            rc, m = p.run(CONVERGE_MAXSTEPS)
+            out = {n: p.get(n) for n in state_names}
+            t = time.perf_counter() - t0
+            it = p.integrals()
+            r = {"seconds": t, "steps": int(m.nstep), "stopped_by_end_test": bool(rc == 1 and m.nstep < CONVERGE_MAXSTEPS),
+                 "eavg": float(m.eavg), "emax": float(m.emax), "econt": float(m.econt),
+                 "eta_tt": it.eta_tt, "mass_flow_in": it.mass_flow_in, "tstep_threads_per_cta": list(tuned),
+                 "state_bytes_downloaded": int(sum(a.nbytes for a in out.values()))}
+            if fx is not None:
+                r["eta_err_vs_fp64"] = abs(it.eta_tt - fx["eta_tt"])
+                r["mass_flow_rel_err_vs_fp64"] = abs(it.mass_flow_in - fx["mass_flow_in"]) / abs(fx["mass_flow_in"])
+                r["meets_1e-4"] = r["eta_err_vs_fp64"] <= 1e-4 and r["mass_flow_rel_err_vs_fp64"] <= 1e-4
+            res[name] = r
+            p.close()
+    c, pl = res["chosen"], res["plain_fp32"]
+    nodes = 65 * 242 * 49
+    kps = 18
+    line = {
+        "metric": "time to convergence", "value": c["seconds"], "unit": "s", "n_gpus": world, "steps": c["steps"],
+        "warmup": max(args.warmup, 3), "ms_per_step": c["seconds"] / max(c["steps"], 1) * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOADS["converge"][1], "nodes": nodes, "max_steps": CONVERGE_MAXSTEPS,
+                   "l2": "inputs (216 MB working set) larger than L2, no flush inside a run",
+                   "fp64_oracle": None if fx is None else {k: fx[k] for k in ("nstep", "eta_tt", "mass_flow_in",
+                                                                               "eavg", "stopped_by_end_test")}},
+        "chosen": c, "plain_fp32": pl,
+        "plain_over_chosen_time": pl["seconds"] / c["seconds"],
+        "gnode_iter_per_s": nodes * c["steps"] / c["seconds"] / 1e9,
+        "cpu_baseline": None, "clocks": clk.summary(),
+        "e2e": {"value": c["seconds"], "unit": "s", "h2d_bytes_per_step": 4,
+                "d2h_bytes_per_step": (c["state_bytes_downloaded"] + 200 * c["steps"] / 5) / max(c["steps"], 1),
+                "how": "mgpu_run through the C ABI (control block read back every fifth step), the flow state "
+                       "downloaded at the end"},
+        "gpu_launches": kps * c["steps"] + 10 * (c["steps"] // 5),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args, rank, world, local_rank):
+    dist = replica_setup(world, rank, local_rank)
     from mgpu import lib
     import numpy as np
     cd = build_case()
@@ -478,13 +698,12 @@ def run_gpu(args, rank, world, local_rank):
         tuned, tune_ms = prob.autotune()    # threads per J-plane CTA of the TSTEP kernels
         prob.run(3)
     dist_barrier(dist)
-    with ClockSampler(0) as clk:
+    with clock_sampler(0) as clk:
         t_wall0 = time.perf_counter()
         ms = prob.bench_steps(args.steps, flush_l2=True)
         t_wall1 = time.perf_counter()
     dist_barrier(dist)
-    ms_max = dist_max(dist, ms)
-    value = N * args.steps * world / (ms_max / 1e3) / 1e9
+    ms_max, value = replica_value(dist, world, N, args.steps, ms)
     ms_per_step = ms_max / args.steps
 
     # per-kernel device times (events around each launch, no graph); LOSS
@@ -502,18 +721,23 @@ def run_gpu(args, rank, world, local_rank):
     traffic = ncu_traffic_per_launch().get(dom_name)
     total_prof = sum(p[2] for p in prof)
 
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI, as a Fortran LOOP replacement drives it:
+    # the flow state (the COMMON arrays RO, ROVX, ROVR, RORVT, ROE) uploaded
+    # from pinned host buffers, then every one of the K steps through
+    # mgpu_step() (control word in, monitors out, synchronous), then the
+    # state downloaded into the pinned buffers, all inside the wall clock
     state = ["RO", "ROVX", "ROVR", "RORVT", "ROE"]
-    host = {n: prob.get(n) for n in state}
+    host = {n: pinned_like(prob.get(n)) for n in state}
     h2d_step, d2h_step = lib.step_io_bytes()
-    ne = max(1, args.steps // 2)
+    ne = max(1, args.steps)
     dist_barrier(dist)
     t0 = time.perf_counter()
     for n in state:
         prob.set(n, host[n])
     for _ in range(ne):
         prob.step()
-    out = {n: prob.get(n) for n in state}
+    for n in state:
+        prob.get_into(n, host[n])
     t1 = time.perf_counter()
     dist_barrier(dist)
     e2e_s = dist_max(dist, t1 - t0)
@@ -521,33 +745,47 @@ def run_gpu(args, rank, world, local_rank):
     e2e = {"value": N * ne * world / e2e_s / 1e9, "unit": METRIC,
            "h2d_bytes_per_step": (state_bytes + h2d_step * ne) / ne,
            "d2h_bytes_per_step": (state_bytes + d2h_step * ne) / ne,
-           "steps": ne, "how": "per step mgpu_step() (graph launch, control word in, monitors out, sync); "
-                               "flow state uploaded before and downloaded after from pageable host buffers"}
+           "steps": ne, "wall_s": e2e_s,
+           "how": f"the flow state ({state_bytes} B) uploaded from pinned host buffers, then {ne} x mgpu_step() "
+                  f"(graph launch, {h2d_step} B control word in, {d2h_step} B monitors out, synchronous), then "
+                  f"the state downloaded; bytes per step include the state copies spread over the {ne} steps"}
 
-    # the plain FP32 path: the same workload with the long sums formed in the
-    # reference's sequential REAL*4 order (REDUCE_ORDER=1, the parity mode)
-    plain = None
+    # the plain FP32 path (REDUCE_ORDER=2: the same parallel trees with FP32
+    # adds) and the reference-order path (REDUCE_ORDER=1: the long sums
+    # formed by single threads in the reference's sequential REAL*4 order,
+    # the parity mode), each on the same workload with the same CTA sizes
+    plain = ref_order = None
     if os.environ.get("MGPU_BENCH_PLAIN", "1") != "0":
-        cdp = build_case()
-        cdp.ints["REDUCE_ORDER"] = 1
-        pp = lib.Problem(cdp)
-        pp.run(max(args.warmup, 3))
-        npl = max(10, min(60, args.steps // 10))
-        ms_pl = pp.bench_steps(npl, flush_l2=True)
-        pp.close()
-        v_pl = N * npl / (ms_pl / 1e3) / 1e9
-        plain = {"value": v_pl, "unit": METRIC, "steps": npl, "ms_per_step": ms_pl / npl,
-                 "chosen_over_plain": value / world / v_pl,
-                 "how": "REDUCE_ORDER=1: multigrid, row-mean, mixing-plane and monitor sums in the reference's "
-                        "sequential REAL*4 order; accuracy of both paths against the FP64 oracle is checked in "
-                        "tests/test_gpu_parity.py (small stage, 1500 steps)"}
+        for order in (2, 1):
+            cdp = build_case()
+            cdp.ints["REDUCE_ORDER"] = order
+            cdp.ints["TS_THREADS"] = 0
+            pp = lib.Problem(cdp)
+            pp.run(max(args.warmup, 3))
+            if order == 2:
+                pp.autotune()
+                pp.run(3)
+            npl = max(20, min(200, args.steps)) if order == 2 else 10
+            ms_pl = pp.bench_steps(npl, flush_l2=True)
+            pp.close()
+            v_pl = N * npl / (ms_pl / 1e3) / 1e9
+            entry = {"value": v_pl, "unit": METRIC, "steps": npl, "ms_per_step": ms_pl / npl,
+                     "chosen_over_this": value / world / v_pl}
+            if order == 2:
+                entry["how"] = ("REDUCE_ORDER=2: the default path's parallel reduction trees (multigrid superblock, "
+                                "row-mean, monitor sums) with FP32 adds, mixing-plane line sums in REAL*4; "
+                                "time to convergence and errors against the FP64 oracle: bench.py --workload "
+                                "converge")
+                plain = entry
+            else:
+                entry["how"] = ("REDUCE_ORDER=1: the long sums formed by single threads in the reference's "
+                                "sequential REAL*4 order (the parity mode)")
+                ref_order = entry
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        rate, n, dt = cpu_oracle_rate(cd, float(os.environ.get("MGPU_CPU_SECONDS", "15")), 10 ** 6)
-        cpu = {"value": rate, "unit": METRIC, "cores": 1, "kind": "port",
-               "sample": f"{n} LOOP iterations of the same workload after 1 warm-up, serial C++ restatement of "
-                         f"LOOP (oracle), {dt:.1f} s"}
+        r = cpu_oracle_rate(cd, float(os.environ.get("MGPU_CPU_SECONDS", "15")), 10 ** 6)
+        cpu = cpu_baseline_entry(r, "the same workload")
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
@@ -568,6 +806,7 @@ def run_gpu(args, rank, world, local_rank):
                          "step": {"alg_bytes_per_node_iter": B_ALG_STEP,
                                   "achieved": value / world * B_ALG_STEP, "frac": value / world * B_ALG_STEP / peak}},
             "plain_fp32": plain,
+            "reference_order": ref_order,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "e2e": e2e,
@@ -610,6 +849,8 @@ def main():
         return run_batch(args, rank, world, local_rank)
     if args.workload == "adjoint":
         return run_adjoint(args, rank, world, local_rank)
+    if args.workload == "converge":
+        return run_converge(args, rank, world, local_rank)
     return run_gpu(args, rank, world, local_rank)
 
 

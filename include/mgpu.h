@@ -230,10 +230,13 @@ int32_t mgpu_write_grid_out(mgpu_handle *h, const char *path);
  *    it has written earlier in the same call.
  *  - The first call on each device looks up the scratch's device address
  *    (with the handle's device current, which it must be: otherwise
- *    MGPU_E_STATE); under CUDA's lazy module loading that lookup also loads
- *    the library module holding the scratch.  Make that first call before
- *    any stream capture begins;
- *    a call with out == NULL performs only this set-up and returns 0.
+ *    MGPU_E_STATE) and loads this path's two kernels, so that under CUDA's
+ *    lazy module loading no later call loads a module (which could take
+ *    device memory).  A call with out == NULL performs only this set-up
+ *    and returns 0; make it once per device before marching begins.
+ *  - Every call with out != NULL synchronises the handle's stream and
+ *    copies its results to the host, so it must not be made while that
+ *    stream is capturing.
  *  - Calls whose executions overlap in time on the same device (two host
  *    threads, or two handles on one device) share the one scratch array and
  *    race: serialise them.  The call returns only after its results are on

@@ -66,7 +66,8 @@
     M_(NSTEP,    0)                                                       \
     /* not a COMMON variable: order of the long reductions on the GPU,   */ \
     /* 0 = FP64 tree sums (default), 1 = the reference's sequential REAL*4 */ \
-    /* order for the superblock and row-average sums (parity checks)     */ \
+    /* order for the superblock and row-average sums (parity checks),    */ \
+    /* 2 = the trees of 0 with FP32 adds (the plain FP32 path)           */ \
     M_(REDUCE_ORDER, 0)                                                   \
     /* not a COMMON variable: 1 holds the LOSS body forces and the STEPUP */ \
     /* time steps at their current values (frozen-turbulence stepping,    */ \
@@ -74,7 +75,11 @@
     M_(FROZEN,   0)                                                       \
     /* not a COMMON variable: threads per J-plane CTA of TSTEP, 128, 256  */ \
     /* or 512 (0: 256 until mgpu_autotune chooses)                        */ \
-    M_(TS_THREADS, 0)
+    M_(TS_THREADS, 0)                                                     \
+    /* not a COMMON variable: 1 (default) runs TSTEP's damping and corner */ \
+    /* gather over pairs of J-planes (one CTA of twice the threads per    */ \
+    /* pair), 0 one CTA per J-plane; the results are bitwise the same     */ \
+    M_(TS_PAIR, 1)
 
 /* ----- REAL scalars: /BKGAS/, /BKCNTL/, /BKSMTH/, /BKLOSS/, /BKINPT/ ---- */
 #define MGPU_REAL_SCALARS(M_)                                             \

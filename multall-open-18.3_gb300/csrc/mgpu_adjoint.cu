@@ -14,7 +14,7 @@
 // and the mixing-plane inputs); the state is then restored.  Every reverse
 // kernel below undoes one forward kernel of the step, in reverse order:
 //   k_mixplan -> k_ts_* (momenta) -> k_flux_mom (fluxes, then PEFF) -> k_bc_apply ->
-//   k_ts_* (RO, ROE) -> k_flux_energy -> k_bc_sums -> k_flux_mass -> k_prim
+//   k_ts_* (RO, ROE) -> energy fluxes -> k_bc_sums -> mass fluxes -> k_prim
 // Each takes the adjoints of its forward kernel's outputs and adds the
 // adjoints of its inputs; outputs that the forward kernel overwrote get the
 // adjoint of their old value (zero, or what the kernel read of it).  Where
@@ -66,7 +66,7 @@ struct Adj {
     // the density limiter's linear coefficients lim(J) = C0 RO(J) + CA ROAVG
     const float *tROL, *tROM, *tWT, *tVLIM, *tROLIM, *tDC0, *tDCA;
     const int *tDCOL;
-    float *WT;                   // adjoint of WT (k_flux_mass), read by the Mach limiter
+    float *WT;                   // adjoint of WT (k_flux_mass_energy), read by the Mach limiter
     float *cf;                   // per-face coefficients of the flux reverses (MOM_NCOEF x N)
     const DevCtl *tctl;
     // geometry adjoints, accumulated when geom != 0
@@ -145,7 +145,7 @@ __global__ void rk_prim(const Dev d, const Adj a) {
 }
 
 // =====================================================================
-// R2: mass fluxes (k_flux_mass)
+// R2: mass fluxes (the mass part of k_flux_mass_energy)
 // =====================================================================
 // pre-step ROVT: J=1 from the previous inlet condition, J>=2 from k_prim
 __device__ __forceinline__ float pre_rovt(const Dev &d, const Adj &a, int i, int j, int k) {
@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(RBC_BS) rk_bc_sums(const Dev d, const Adj a) {
 }
 
 // =====================================================================
-// R4: energy fluxes (k_flux_energy); HO(JM) and PEFF as the step began
+// R4: energy fluxes (the energy part of k_flux_mass_energy); HO(JM) and PEFF as the step began
 // =====================================================================
 __device__ __forceinline__ float pre_ho(const Dev &d, const Adj &a, int i, int j, int k) {
     return j == d.JM ? AIK(a.tHOJM, i, k) : A3(a.tHO, i, j, k);

@@ -254,8 +254,7 @@ __global__ void k_delay(long long cycles) {
 void enqueue_core(const Dev &d, Launch L, cudaEvent_t join = nullptr) {
     Launch L0 = L;        // follows the LOSS conditional node: plain stream order
     L0.pdl = false;
-    launch_flux_mass(d, L0);
-    launch_flux_energy(d, L);
+    launch_flux_mass_energy(d, L0);
     launch_tstep(d, L, V_RO, 2);
     if (d.ILOS >= 100) launch_roavg_cell(d, L);     // 4255-4267, after TSTEP(RO)
     if (join) {
@@ -799,6 +798,19 @@ int32_t mgpu_commit(mgpu_handle *h) {
         if ((rc = dalloc(h, x.ds, x.n)) || (rc = dalloc(h, x.de, x.n))) return rc;
         if ((rc = upload(h, *x.ds, s)) || (rc = upload(h, *x.de, e))) return rc;
     }
+    // level-2 blocks nested in level-1 blocks (IRBB, KRBB multiples of IR,
+    // KR): the cells kernel then forms the level-2 partials from the level-1 ones
+    {
+        auto nested = [&](const std::vector<int> &m1, const std::vector<int> &m2, int n) {
+            for (int x = 1; x <= n; ++x) {
+                const bool start2 = x == 1 || m2[x - 1] != m2[x - 2], end2 = x == n || m2[x - 1] != m2[x];
+                const bool start1 = x == 1 || m1[x - 1] != m1[x - 2], end1 = x == n || m1[x - 1] != m1[x];
+                if ((start2 && !start1) || (end2 && !end1)) return false;
+            }
+            return true;
+        };
+        d.mg_nested = nested(IB1, IB2, d.IMM1) && nested(KB1, KB2, d.KMM1) ? 1 : 0;
+    }
     for (int j = 2; j <= d.JM; ++j) {
         if (JB1[j - 1] < 1 || JB1[j - 1] > d.NJB1 + 1 || JB2[j - 1] < 1 || JB2[j - 1] > d.NJB2 + 1 ||
             JSBLK[j - 1] < 1 || JSBLK[j - 1] > d.NSBLK)
@@ -811,10 +823,11 @@ int32_t mgpu_commit(mgpu_handle *h) {
             (rc = dalloc(h, &V.P2, (size_t)d.JM * d.NIB2 * d.NKB2)))
             return rc;
     }
-    if (d.REDUCE_ORDER != 0 && d.REDUCE_ORDER != 1) return fail(MGPU_E_ARG, "REDUCE_ORDER must be 0 or 1");
+    if (d.REDUCE_ORDER < 0 || d.REDUCE_ORDER > 2) return fail(MGPU_E_ARG, "REDUCE_ORDER must be 0, 1 or 2");
     if (d.TS_THREADS != 0 && d.TS_THREADS != 128 && d.TS_THREADS != 192 && d.TS_THREADS != 256 &&
         d.TS_THREADS != 512)
         return fail(MGPU_E_ARG, "TS_THREADS must be 0, 128, 192, 256 or 512");
+    if (d.TS_PAIR != 0 && d.TS_PAIR != 1) return fail(MGPU_E_ARG, "TS_PAIR must be 0 or 1");
     d.ts_bs[0] = d.ts_bs[1] = d.TS_THREADS ? d.TS_THREADS : 256;
     // the control block
     DevCtl c;
@@ -886,7 +899,10 @@ int32_t mgpu_run(mgpu_handle *h, int32_t nsteps, mgpu_monitors *mon) {
     for (;;) {
         const DevCtl &c = *h->h_ctl;
         if (mon) fill_monitors(c, mon);
-        if (done > 0 && c.health) return fail(MGPU_E_NONFINITE, "non-finite or non-positive density in the flow field");
+        // a field already flagged by the last tail (of this call, or of an
+        // earlier mgpu_step / mgpu_run) is not marched further
+        if ((done > 0 || c.nstep > 0) && c.health)
+            return fail(MGPU_E_NONFINITE, "non-finite or non-positive density in the flow field");
         if (c.ifend) return 1;
         if (done >= nsteps) return 0;
         const int n0 = c.nstep;

@@ -78,12 +78,12 @@ void launch_step_begin(const Dev &d, Launch L) {
 // also the sum and the maximum of |W|^2 (5910, uses the previous WT).
 // ---------------------------------------------------------------------
 template <int BS>
-__device__ inline void block_reduce_sum_key(double s, unsigned long long key, double *out_s,
+__device__ inline void block_reduce_sum_key(int order, double s, unsigned long long key, double *out_s,
                                             unsigned long long *out_k) {
     __shared__ double ss[BS / 32];
     __shared__ unsigned long long sk[BS / 32];
     for (int o = 16; o > 0; o >>= 1) {
-        s += __shfl_down_sync(0xffffffffu, s, o);
+        s = racc(order, s, __shfl_down_sync(0xffffffffu, s, o));
         unsigned long long ok = __shfl_down_sync(0xffffffffu, key, o);
         key = ok > key ? ok : key;
     }
@@ -97,7 +97,7 @@ __device__ inline void block_reduce_sum_key(double s, unsigned long long key, do
         s = l < BS / 32 ? ss[l] : 0.0;
         key = l < BS / 32 ? sk[l] : 0ull;
         for (int o = 16; o > 0; o >>= 1) {
-            s += __shfl_down_sync(0xffffffffu, s, o);
+            s = racc(order, s, __shfl_down_sync(0xffffffffu, s, o));
             unsigned long long ok = __shfl_down_sync(0xffffffffu, key, o);
             key = ok > key ? ok : key;
         }
@@ -150,7 +150,8 @@ __global__ void __launch_bounds__(PRIM_BS) k_prim(Dev d) {
             }
         }
     }
-    if (do_tail) block_reduce_sum_key<PRIM_BS>(eke_s, key, &d.part_sum[blockIdx.x], &d.part_key[blockIdx.x]);
+    if (do_tail)
+        block_reduce_sum_key<PRIM_BS>(d.REDUCE_ORDER, eke_s, key, &d.part_sum[blockIdx.x], &d.part_key[blockIdx.x]);
 }
 
 void launch_prim(const Dev &d, Launch L) {
@@ -173,17 +174,28 @@ __device__ inline float flowt_raw(const Dev &d, int i, int j, int k) {
     return (AVGRVX * A3(d.ABX, i, j, k) + AVGRVT * A2(d.ABT, j, k) + AVGRVR * A3(d.ABR, i, j, k)) * 0.25f;
 }
 
-__global__ void k_flux_mass(Dev d) {
+// energy flux of the blade-wise face (I, J, K) whose mass flux is flowt
+__device__ inline float tflux_energy_at(const Dev &d, float flowt, int i, int j, int k) {
+    float AVGHO = A3(d.HO, i, j, k) + A3(d.HO, i, j - 1, k) + A3(d.HO, i, j - 1, k + 1) + A3(d.HO, i, j, k + 1);
+    float AVGPB = A3(d.PEFF, i, j, k) + A3(d.PEFF, i, j - 1, k) + A3(d.PEFF, i, j - 1, k + 1) + A3(d.PEFF, i, j, k + 1);
+    return (flowt * AVGHO + A2(d.WRABT, j, k) * AVGPB) * 0.25f;
+}
+
+__global__ void k_flux_mass_energy(Dev d) {
     pdl_wait();
-    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t N = (size_t)d.IM * d.JM * d.KM;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = d.IM * d.JM * d.KM;
     if (n >= N) return;
     int i, j, k;
-    node_ijk(d, n, i, j, k);
+    node_ijk(d, (size_t)n, i, j, k);
+    const VarSet &V = d.var[V_ROE];
     // results are kept in registers and stored at the end, so that no store
     // orders the loads of a later section behind it
     const bool hx = i < d.IM && k < d.KM, ht = j >= 2 && k < d.KM, hr = i < d.IM && j >= 2;
+    const bool hs = hx && j >= 2;
     float fx = 0.0f, ft = 0.0f, fr = 0.0f;
+    float xf = 0.0f, src = 0.0f, rf = 0.0f, tf = 0.0f;
+    // mass fluxes (5020-5045)
     if (hx) {
         float AVGRVX = A3(d.ROVX, i, j, k) + A3(d.ROVX, i, j, k + 1) + A3(d.ROVX, i + 1, j, k) + A3(d.ROVX, i + 1, j, k + 1);
         float AVGRVR = A3(d.ROVR, i, j, k) + A3(d.ROVR, i, j, k + 1) + A3(d.ROVR, i + 1, j, k) + A3(d.ROVR, i + 1, j, k + 1);
@@ -192,6 +204,7 @@ __global__ void k_flux_mass(Dev d) {
     const float ro = d.RO[n];
     const float rowt = d.ROVT[n] - A2(d.UBLADE, j, k) * ro;
     const float wt = rowt / ro;
+    bool tbal = false;          // periodic I = 1 / IM face: FLOWT there is the balanced value ft at both
     if (ht) {
         ft = flowt_raw(d, i, j, k);
         if (i == 1 || i == d.IM) {
@@ -199,6 +212,7 @@ __global__ void k_flux_mass(Dev d) {
                 float f1 = (i == 1) ? ft : flowt_raw(d, 1, j, k);
                 float fm = (i == d.IM) ? ft : flowt_raw(d, d.IM, j, k);
                 ft = 0.5f * (f1 + fm);
+                tbal = true;
             } else {
                 int nr = A1(d.NROW, j);
                 if (k >= A1(d.KS1, nr) && k <= A1(d.KS2, nr)) ft = 0.0f;
@@ -212,67 +226,43 @@ __global__ void k_flux_mass(Dev d) {
             fr = 0.25f * (AVGRVX * A3(d.ASX, i, j, k) + AVGRVR * A3(d.ASR, i, j, k));
         }
     }
+    // energy fluxes (5501-5503) from this node's mass fluxes, and their
+    // periodic balance (900): with IND(J) != 1 the mass flux of both edge
+    // faces is the balanced ft, so the two edge energy fluxes are formed here
+    if (hx) {
+        float AVGHO = A3(d.HO, i, j, k) + A3(d.HO, i, j, k + 1) + A3(d.HO, i + 1, j, k) + A3(d.HO, i + 1, j, k + 1);
+        xf = fx * AVGHO * 0.25f;
+        if (hs) src = d.QSOURCE[n];
+    }
+    if (hr) {
+        float AVGHO = 0.25f * (A3(d.HO, i, j, k) + A3(d.HO, i, j - 1, k) + A3(d.HO, i + 1, j - 1, k) + A3(d.HO, i + 1, j, k));
+        rf = fr * AVGHO;
+    }
+    if (ht) {
+        tf = tflux_energy_at(d, ft, i, j, k);
+        if (tbal) {
+            float t1 = (i == 1) ? tf : tflux_energy_at(d, ft, 1, j, k);
+            float tm = (i == d.IM) ? tf : tflux_energy_at(d, ft, d.IM, j, k);
+            tf = 0.5f * (t1 + tm);
+        }
+    }
     if (hx) d.FLOWX[n] = fx;
     d.ROWT[n] = rowt;
     d.WT[n] = wt;
     if (ht) d.FLOWT[n] = ft;
     if (hr) d.FLOWR[n] = fr;
-}
-
-void launch_flux_mass(const Dev &d, Launch L) {
-    size_t N = (size_t)d.IM * d.JM * d.KM;
-    launchk(L, k_flux_mass, dim3(grid_for(N, 256)), dim3(256), 0, d);
-    mark(L, "k_flux_mass");
-}
-
-// ---------------------------------------------------------------------
-// energy fluxes (5501-5503) and their periodic balance (900)
-// ---------------------------------------------------------------------
-__device__ inline float tflux_energy_raw(const Dev &d, int i, int j, int k) {
-    float AVGHO = A3(d.HO, i, j, k) + A3(d.HO, i, j - 1, k) + A3(d.HO, i, j - 1, k + 1) + A3(d.HO, i, j, k + 1);
-    float AVGPB = A3(d.PEFF, i, j, k) + A3(d.PEFF, i, j - 1, k) + A3(d.PEFF, i, j - 1, k + 1) + A3(d.PEFF, i, j, k + 1);
-    return (A3(d.FLOWT, i, j, k) * AVGHO + A2(d.WRABT, j, k) * AVGPB) * 0.25f;
-}
-
-__global__ void k_flux_energy(Dev d) {
-    pdl_wait();
-    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t N = (size_t)d.IM * d.JM * d.KM;
-    if (n >= N) return;
-    int i, j, k;
-    node_ijk(d, n, i, j, k);
-    const VarSet &V = d.var[V_ROE];
-    // results in registers, stored at the end (as in k_flux_mass)
-    const bool hx = i < d.IM && k < d.KM, hs = hx && j >= 2, hr = i < d.IM && j >= 2, ht = j >= 2 && k < d.KM;
-    float xf = 0.0f, src = 0.0f, rf = 0.0f, tf = 0.0f;
-    if (hx) {
-        float AVGHO = A3(d.HO, i, j, k) + A3(d.HO, i, j, k + 1) + A3(d.HO, i + 1, j, k) + A3(d.HO, i + 1, j, k + 1);
-        xf = d.FLOWX[n] * AVGHO * 0.25f;
-        if (hs) src = d.QSOURCE[n];
-    }
-    if (hr) {
-        float AVGHO = 0.25f * (A3(d.HO, i, j, k) + A3(d.HO, i, j - 1, k) + A3(d.HO, i + 1, j - 1, k) + A3(d.HO, i + 1, j, k));
-        rf = d.FLOWR[n] * AVGHO;
-    }
-    if (ht) {
-        tf = tflux_energy_raw(d, i, j, k);
-        if ((i == 1 || i == d.IM) && A1(d.IND, j) != 1) {
-            float t1 = (i == 1) ? tf : tflux_energy_raw(d, 1, j, k);
-            float tm = (i == d.IM) ? tf : tflux_energy_raw(d, d.IM, j, k);
-            tf = 0.5f * (t1 + tm);
-        }
-    }
     if (hx) V.XF[n] = xf;
     if (hs) V.SR[n] = src;
     if (hr) V.RF[n] = rf;
     if (ht) V.TF[n] = tf;
 }
 
-void launch_flux_energy(const Dev &d, Launch L) {
+void launch_flux_mass_energy(const Dev &d, Launch L) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
-    launchk(L, k_flux_energy, dim3(grid_for(N, 256)), dim3(256), 0, d);
-    mark(L, "k_flux_energy");
+    launchk(L, k_flux_mass_energy, dim3(grid_for(N, 256)), dim3(256), 0, d);
+    mark(L, "k_flux_mass_energy");
 }
+
 
 // ---------------------------------------------------------------------
 // inlet and exit boundary conditions (4476-4734).  k_bc_sums: one warp per
@@ -493,18 +483,19 @@ __global__ void __launch_bounds__(SF_BS) k_setflo_flow(Dev d) {
         }
         return;
     }
+    const int ro = d.REDUCE_ORDER;
     double s = 0.0;
     for (int c = threadIdx.x; c < IMM1 * KMM1; c += SF_BS) {
         int i = c % IMM1 + 1, k = c / IMM1 + 1;
-        s += (double)(A3(d.FLOWX, i, j, k) * NBJ / NB1);
+        s = racc(ro, s, (double)(A3(d.FLOWX, i, j, k) * NBJ / NB1));
     }
     __shared__ double sh[SF_BS / 32];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    for (int o = 16; o > 0; o >>= 1) s = racc(ro, s, __shfl_down_sync(0xffffffffu, s, o));
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
     __syncthreads();
     if (threadIdx.x == 0) {
         double t = 0.0;
-        for (int w = 0; w < SF_BS / 32; ++w) t += sh[w];
+        for (int w = 0; w < SF_BS / 32; ++w) t = racc(ro, t, sh[w]);
         d.FLOWJ[j - 1] = (float)(-t);
     }
 }
@@ -522,8 +513,8 @@ __global__ void __launch_bounds__(SF_BS) k_setflo_apply(Dev d) {
                 AVFLOW = a / (float)d.JM;
             } else {
                 double a = 0.0;
-                for (int jj = 1; jj <= d.JM; ++jj) a += (double)d.FLOWJ[jj - 1];
-                AVFLOW = (float)(a / (double)d.JM);
+                for (int jj = 1; jj <= d.JM; ++jj) a = racc(d.REDUCE_ORDER, a, (double)d.FLOWJ[jj - 1]);
+                AVFLOW = d.REDUCE_ORDER == 2 ? (float)a / (float)d.JM : (float)(a / (double)d.JM);
             }
         }
         float a = A3(d.ROVX, d.IMID, j, d.KMID), b = A3(d.ROVR, d.IMID, j, d.KMID);
@@ -1013,8 +1004,8 @@ __global__ void __launch_bounds__(MIX_BS) k_mixplan(Dev d) {
         }
         float ROTN = ALPHAA[IM - 1] - ALPHAA[0];
         // periodicity correction (15177-15182); FP64 running sum in the
-        // default precision split, REAL*4 with REDUCE_ORDER = 1
-        if (d.REDUCE_ORDER == 1) {
+        // default precision split, REAL*4 with REDUCE_ORDER 1 and 2
+        if (d.REDUCE_ORDER != 0) {
             float SUMFP = 0.0f;
             for (int i = 1; i <= IM; ++i) {
                 ALPHAA[i - 1] = ALPHAA[i - 1] - ROTN * (SUMFP - 0.5f);

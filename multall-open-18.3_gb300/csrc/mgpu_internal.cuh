@@ -126,6 +126,7 @@ struct Dev {
     int *IB1_S, *IB1_E, *IB2_S, *IB2_E;                 // (NIBn) I extent of each block
     int *KB1_S, *KB1_E, *KB2_S, *KB2_E;                 // (NKBn) K extent of each block
     int *SB_START, *SB_END;                             // (NSBLK)
+    int mg_nested;                     // every level-2 block is a union of level-1 blocks (in I and in K)
     DevCtl *ctl;
     // graph conditionals selecting the LOSS and 5-step tail bodies (set by
     // the step-control kernel when the step runs from the CUDA graph)
@@ -160,6 +161,16 @@ __device__ inline void node_ijk(const Dev &d, size_t n, int &i, int &j, int &k) 
     i = (int)(u - q * im) + 1;
     j = (int)(q - q2 * jm) + 1;
     k = (int)q2 + 1;
+}
+
+// One addition of a long parallel reduction (the tree sums of the multigrid
+// levels, row means, monitors and mixing-plane averages).  REDUCE_ORDER 0,
+// the default precision split, adds in FP64.  REDUCE_ORDER 2, the plain FP32
+// path, rounds every partial sum to REAL*4: the same tree, with FP32 adds
+// (a float sum of two floats, held exactly in a double).  REDUCE_ORDER 1
+// forms these sums elsewhere, sequentially in the reference's order.
+__device__ __forceinline__ double racc(int order, double s, double x) {
+    return order == 2 ? (double)((float)s + (float)x) : s + x;
 }
 
 // Order-preserving key for "largest value, earliest index wins": the value
@@ -230,8 +241,8 @@ void launch_loss(const Dev &d, Launch L, bool init_call);
 void launch_new_loss(const Dev &d, Launch L, bool init_call);
 void launch_roavg_cell(const Dev &d, Launch L);
 size_t new_loss_work_floats(const Dev &d);
-void launch_flux_mass(const Dev &d, Launch L);
-void launch_flux_energy(const Dev &d, Launch L);
+// mass fluxes FLOWX/FLOWT/FLOWR, ROWT, WT and the energy fluxes of ROE
+void launch_flux_mass_energy(const Dev &d, Launch L);
 // inlet/exit conditions: the pitchwise sums and PD(K) (one CTA), then the
 // boundary states; the sums read only values final before TSTEP(RO, ROE)
 void launch_bc_sums(const Dev &d, Launch L);

@@ -704,19 +704,20 @@ __global__ void __launch_bounds__(TAIL_BS) k_tail_flow(Dev d) {
     if (!d.ctl->do_tail) return;
     int j = blockIdx.x + 1;
     int ncell = d.IMM1 * d.KMM1;
+    const int ro = d.REDUCE_ORDER;
     double s = 0.0;
     for (int c = threadIdx.x; c < ncell; c += TAIL_BS) {
         int i = c % d.IMM1 + 1, k = c / d.IMM1 + 1;
-        s -= (double)A3(d.FLOWX, i, j, k);
+        s = racc(ro, s, -(double)A3(d.FLOWX, i, j, k));
     }
     __shared__ double sh[TAIL_BS / 32];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    for (int o = 16; o > 0; o >>= 1) s = racc(ro, s, __shfl_down_sync(0xffffffffu, s, o));
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
     __syncthreads();
     if (threadIdx.x == 0) {
         double t = 0.0;
-        for (int w = 0; w < TAIL_BS / 32; ++w) t += sh[w];
-        d.BLADE_FLOW[j - 1] = t * (double)A1(d.NBLADE, j);
+        for (int w = 0; w < TAIL_BS / 32; ++w) t = racc(ro, t, sh[w]);
+        d.BLADE_FLOW[j - 1] = ro == 2 ? (double)((float)t * (float)A1(d.NBLADE, j)) : t * (double)A1(d.NBLADE, j);
     }
 }
 
@@ -725,17 +726,18 @@ __global__ void k_tail_vref(Dev d, int nparts) {
     pdl_wait();
     DevCtl *c = d.ctl;
     if (!c->do_tail) return;
+    const int ro = d.REDUCE_ORDER;
     double s = 0.0;
     unsigned long long key = 0ull;
     for (int p = threadIdx.x; p < nparts; p += blockDim.x) {
-        s += d.part_sum[p];
+        s = racc(ro, s, d.part_sum[p]);
         unsigned long long k2 = d.part_key[p];
         key = k2 > key ? k2 : key;
     }
     __shared__ double ss[32];
     __shared__ unsigned long long sk[32];
     for (int o = 16; o > 0; o >>= 1) {
-        s += __shfl_down_sync(0xffffffffu, s, o);
+        s = racc(ro, s, __shfl_down_sync(0xffffffffu, s, o));
         unsigned long long ok = __shfl_down_sync(0xffffffffu, key, o);
         key = ok > key ? ok : key;
     }
@@ -748,7 +750,7 @@ __global__ void k_tail_vref(Dev d, int nparts) {
         double t = 0.0;
         unsigned long long kk = 0ull;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-            t += ss[w];
+            t = racc(ro, t, ss[w]);
             kk = sk[w] > kk ? sk[w] : kk;
         }
         c->mon.vrms = t;
@@ -797,8 +799,9 @@ __global__ void __launch_bounds__(TAIL_BS) k_tail_dvm(Dev d) {
     __shared__ double ss[TAIL_BS / 32];
     __shared__ unsigned long long sk[TAIL_BS / 32];
     __shared__ int sc[TAIL_BS / 32];
+    const int ro = d.REDUCE_ORDER;
     for (int o = 16; o > 0; o >>= 1) {
-        s += __shfl_down_sync(0xffffffffu, s, o);
+        s = racc(ro, s, __shfl_down_sync(0xffffffffu, s, o));
         unsigned long long ok = __shfl_down_sync(0xffffffffu, key, o);
         key = ok > key ? ok : key;
         bad += __shfl_down_sync(0xffffffffu, bad, o);
@@ -815,7 +818,7 @@ __global__ void __launch_bounds__(TAIL_BS) k_tail_dvm(Dev d) {
         unsigned long long kk = 0ull;
         int cnt = 0;
         for (int q = 0; q < TAIL_BS / 32; ++q) {
-            t += ss[q];
+            t = racc(ro, t, ss[q]);
             kk = sk[q] > kk ? sk[q] : kk;
             cnt += sc[q];
         }
@@ -829,11 +832,12 @@ __global__ void k_tail_final(Dev d, int nparts) {
     pdl_wait();
     DevCtl *c = d.ctl;
     if (!c->do_tail) return;
+    const int ro = d.REDUCE_ORDER;
     double s = 0.0;
     unsigned long long key = 0ull;
     int bad = 0;
     for (int p = threadIdx.x; p < nparts; p += blockDim.x) {
-        s += d.part_sum[p];
+        s = racc(ro, s, d.part_sum[p]);
         unsigned long long k2 = d.part_key[p];
         key = k2 > key ? k2 : key;
         bad += d.part_cnt[p];
@@ -842,7 +846,7 @@ __global__ void k_tail_final(Dev d, int nparts) {
     __shared__ unsigned long long sk[32];
     __shared__ int sc[32];
     for (int o = 16; o > 0; o >>= 1) {
-        s += __shfl_down_sync(0xffffffffu, s, o);
+        s = racc(ro, s, __shfl_down_sync(0xffffffffu, s, o));
         unsigned long long ok = __shfl_down_sync(0xffffffffu, key, o);
         key = ok > key ? ok : key;
         bad += __shfl_down_sync(0xffffffffu, bad, o);
@@ -858,7 +862,7 @@ __global__ void k_tail_final(Dev d, int nparts) {
         unsigned long long kk = 0ull;
         int cnt = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-            t += ss[w];
+            t = racc(ro, t, ss[w]);
             kk = sk[w] > kk ? sk[w] : kk;
             cnt += sc[w];
         }

@@ -122,7 +122,8 @@ __global__ void k_int_eta(Dev d, double *sums) {
 }
 
 // Looks up (once per device, with that device current) the address of the
-// static scratch.
+// static scratch, and loads the two kernels of this path, so that no later
+// call loads a module.
 int scratch_for_device(int dev, double **p) {
     char msg[160];
     if (dev < 0 || dev >= NA_MAX_DEVICES) {
@@ -135,6 +136,15 @@ int scratch_for_device(int dev, double **p) {
         cudaError_t e = cudaGetSymbolAddress(&a, g_int_scratch);
         if (e != cudaSuccess || a == nullptr) {
             snprintf(msg, sizeof msg, "mgpu_integrals_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+            return api_fail(MGPU_E_CUDA, msg);
+        }
+        // load both kernels now: under lazy module loading a kernel is
+        // otherwise loaded at its first launch, which may take device memory
+        cudaFuncAttributes fa;
+        e = cudaFuncGetAttributes(&fa, k_int_sum_direct);
+        if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_int_eta);
+        if (e != cudaSuccess) {
+            snprintf(msg, sizeof msg, "mgpu_integrals_noalloc: loading the kernels: %s", cudaGetErrorString(e));
             return api_fail(MGPU_E_CUDA, msg);
         }
         g_scratch_addr[dev] = (double *)a;

@@ -20,7 +20,9 @@
 //            pitchwise, spanwise, corners, exit smoothing, periodic,
 //            tip-gap and mixing-plane averaging in shared memory -> D
 // With REDUCE_ORDER=1 the level sums and the row mean are instead formed by
-// single threads in the reference's sequential REAL*4 order (parity checks).
+// single threads in the reference's sequential REAL*4 order (parity checks);
+// with REDUCE_ORDER=2 (the plain FP32 path) they are the default path's
+// trees with FP32 adds.
 #include "mgpu_internal.cuh"
 
 namespace mgpu {
@@ -37,15 +39,15 @@ constexpr int TS_UG = 4;         // the same for the damping and gather phases o
 constexpr int SV_U = 3;          // points per thread whose streamwise loads are issued together
 
 template <int BS>
-__device__ inline double block_sum(double v, double *sh) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+__device__ inline double block_sum(int order, double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v = racc(order, v, __shfl_down_sync(0xffffffffu, v, o));
     int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     if (l == 0) sh[w] = v;
     __syncthreads();
     double r = 0.0;
     if (w == 0) {
         r = l < BS / 32 ? sh[l] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+        for (int o = 16; o > 0; o >>= 1) r = racc(order, r, __shfl_down_sync(0xffffffffu, r, o));
     }
     __syncthreads();
     return r;
@@ -65,8 +67,9 @@ __device__ inline int mp_role(const Dev &d, int j, int *nr) {
 }
 
 // Pitchwise sum of a mixing-plane line in I order: REAL*4 as the reference
-// forms it (REDUCE_ORDER = 1), or accumulated in FP64 and rounded once (the
-// default precision split: FP64 for the mixing-plane circumferential sums).
+// forms it (REDUCE_ORDER 1, and the plain FP32 path, 2), or accumulated in
+// FP64 and rounded once (the default precision split: FP64 for the
+// mixing-plane circumferential sums).
 __device__ inline float mp_line_sum(const float *row, int n, bool exact32) {
     if (exact32) {
         float s = 0.0f;
@@ -129,7 +132,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_cells(const __grid_constan
         __syncthreads();
         for (int k = threadIdx.x + 1; k <= KMM1; k += BS) {
             const float *row = st + (size_t)(k - 1) * IMM1;
-            lsum[k - 1] = mp_line_sum(row, IMM1, d.REDUCE_ORDER == 1);
+            lsum[k - 1] = mp_line_sum(row, IMM1, d.REDUCE_ORDER != 0);
         }
     }
     __syncthreads();
@@ -198,7 +201,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_cells(const __grid_constan
             bool on = role == 3 ? (FLOWDIRN > 0.0f || lowx) : (FLOWDIRN < 0.0f || lowx);
             if (!on) continue;
             float *row = st + (size_t)(k - 1) * IMM1;
-            float s = mp_line_sum(row, IMM1, d.REDUCE_ORDER == 1);
+            float s = mp_line_sum(row, IMM1, d.REDUCE_ORDER != 0);
             for (int i = 0; i < IMM1; ++i) row[i] = s * A1(d.FP, i + 1);
         }
         __syncthreads();
@@ -213,10 +216,37 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_cells(const __grid_constan
         A3(V.ST, i, j, k) = v;
         psf += v;
     }
-    const double ps = block_sum<BS>((double)psf, shd);
+    const double ps = block_sum<BS>(d.REDUCE_ORDER, (double)psf, shd);
     if (threadIdx.x == 0) V.psum[j - 1] = ps;
     // level-1 and level-2 partial sums of this plane
     const int n1 = d.NIB1 * d.NKB1, n2 = d.NIB2 * d.NKB2;
+    if (d.mg_nested) {
+        // every level-2 block is a union of level-1 blocks: the level-1
+        // partials first (in shared memory), then each level-2 partial as the
+        // sum of its level-1 partials (a 9-term chain for 3 x 3 blocks of
+        // 3 x 3 cells, where the direct sum is an 81-term chain)
+        float *p1 = lsum + KMM1;
+        for (int u = threadIdx.x; u < n1; u += BS) {
+            const int ib = u % d.NIB1 + 1, kb = u / d.NIB1 + 1;
+            const int i0 = A1(d.IB1_S, ib), i1 = A1(d.IB1_E, ib), k0 = A1(d.KB1_S, kb), k1 = A1(d.KB1_E, kb);
+            float s = 0.0f;
+            for (int k = k0; k <= k1; ++k)
+                for (int i = i0; i <= i1; ++i) s = s + st[(k - 1) * IMM1 + (i - 1)];
+            p1[u] = s;
+            V.P1[(size_t)(j - 1) * n1 + u] = s;
+        }
+        __syncthreads();
+        for (int u = threadIdx.x; u < n2; u += BS) {
+            const int ib = u % d.NIB2 + 1, kb = u / d.NIB2 + 1;
+            const int a0 = A1(d.IB1, A1(d.IB2_S, ib)), a1 = A1(d.IB1, A1(d.IB2_E, ib));
+            const int c0 = A1(d.KB1, A1(d.KB2_S, kb)), c1 = A1(d.KB1, A1(d.KB2_E, kb));
+            float s = 0.0f;
+            for (int kb1 = c0; kb1 <= c1; ++kb1)
+                for (int ib1 = a0; ib1 <= a1; ++ib1) s = s + p1[(kb1 - 1) * d.NIB1 + (ib1 - 1)];
+            V.P2[(size_t)(j - 1) * n2 + u] = s;
+        }
+        return;
+    }
     for (int t = threadIdx.x; t < n1 + n2; t += BS) {
         const bool lv1 = t < n1;
         int u = lv1 ? t : t - n1;
@@ -345,9 +375,10 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
         for (int t = threadIdx.x; t < n2; t += BS) b2[t] = plane_partials_sum(V.P2, n2, t, a2, e2);
         if (threadIdx.x < 32) {
             int a = A1(d.SB_START, jsb), b = A1(d.SB_END, jsb);
+            const int ro = d.REDUCE_ORDER;
             double s = 0.0;
-            for (int jj = a + (int)threadIdx.x; jj <= b; jj += 32) s += V.psum[jj - 1];
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            for (int jj = a + (int)threadIdx.x; jj <= b; jj += 32) s = racc(ro, s, V.psum[jj - 1]);
+            for (int o = 16; o > 0; o >>= 1) s = racc(ro, s, __shfl_down_sync(0xffffffffu, s, o));
             if (threadIdx.x == 0) s_sb = (float)s;
         }
     }
@@ -397,7 +428,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
         }
     }
     if (want_abs) {
-        const double t = block_sum<BS>((double)sabs, shd);
+        const double t = block_sum<BS>(d.REDUCE_ORDER, (double)sabs, shd);
         if (threadIdx.x == 0) V.pabs[j - 1] = t;
     }
 }
@@ -415,7 +446,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_plane_abs(const __grid_con
         int i = c % d.IMM1 + 1, k = c / d.IMM1 + 1;
         sf += fabsf(A3(V.ST, i, j, k));
     }
-    const double s = block_sum<BS>((double)sf, shd);
+    const double s = block_sum<BS>(d.REDUCE_ORDER, (double)sf, shd);
     if (threadIdx.x == 0) V.pabs[j - 1] = s;
 }
 
@@ -476,9 +507,10 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_update(const __grid_consta
             int w = threadIdx.x >> 5, l = threadIdx.x & 31;
             for (int nr = w + 1; nr <= d.NROWS; nr += BS / 32) {
                 int JST = A1(d.JSTART, nr) + 1, JEN = A1(d.JMIX, nr) - 1;
+                const int ro = d.REDUCE_ORDER;
                 double s = 0.0;
-                for (int jj = JST + l; jj <= JEN; jj += 32) s += V.pabs[jj - 1];
-                for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+                for (int jj = JST + l; jj <= JEN; jj += 32) s = racc(ro, s, V.pabs[jj - 1]);
+                for (int o = 16; o > 0; o >>= 1) s = racc(ro, s, __shfl_down_sync(0xffffffffu, s, o));
                 if (l == 0) chg[nr - 1] = (float)s / (float)(IMM1 * KMM1 * (JEN - JST + 1));
             }
             __syncthreads();
@@ -546,7 +578,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_update(const __grid_consta
             bool on = role == 3 ? (FLOWDIRN > 0.0f || lowx) : (FLOWDIRN < 0.0f || lowx);
             if (!on) continue;
             float *row = c + (size_t)(k - 1) * IMM1;
-            float s = mp_line_sum(row, IMM1, d.REDUCE_ORDER == 1);
+            float s = mp_line_sum(row, IMM1, d.REDUCE_ORDER != 0);
             s = s / (float)IMM1;
             for (int i = 0; i < IMM1; ++i) row[i] = s;
         }
@@ -619,6 +651,213 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_update(const __grid_consta
                 }
             }
             V.TM[n] = v;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// update over a pair of node planes: the same result as k_ts_update for
+// node planes j0 and j0+1, from one CTA of PBS threads.  The CTA damps the
+// three cell planes j0, j0+1, j0+2 once each (k_ts_update damps every cell
+// plane in the two CTAs that read it: 2 dampings per cell plane, here 1.5),
+// and each thread gathers the same (i, k) on both node planes, so the four
+// corner weights, the index arithmetic and the reads of the middle cell
+// plane serve both planes.  Every value is formed by the same expressions
+// in the same order as in k_ts_update.
+// ---------------------------------------------------------------------
+template <int PBS>
+__global__ void __launch_bounds__(PBS, 1024 / PBS) k_ts_update_pair(const __grid_constant__ Dev d, int v0) {
+    pdl_wait();
+    extern __shared__ float sm[];
+    const VarSet &V = d.var[v0 + blockIdx.y];
+    const float *__restrict__ D = V.D;
+    float *__restrict__ TM = V.TM;
+    __shared__ float s_blk[64];
+    __shared__ float chg[64];
+    const int j0 = 2 * blockIdx.x + 1;
+    const int IM = d.IM, JM = d.JM, IMM1 = d.IMM1, KM = d.KM, KMM1 = d.KMM1;
+    const int nc = IMM1 * KMM1;
+    const bool two = j0 + 1 <= JM;              // the second node plane exists
+    const DevCtl *ctl = d.ctl;
+    const int damp_on = ctl->damp_on;
+    const float DAMP = ctl->DAMP;
+    if (damp_on) {
+        if (d.REDUCE_ORDER == 1) {
+            for (int r = threadIdx.x; r < d.NROWS; r += PBS) s_blk[r] = V.AVG_BLK[r];
+        } else {
+            const int ro = d.REDUCE_ORDER;
+            int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+            for (int nr = w + 1; nr <= d.NROWS; nr += PBS / 32) {
+                int JST = A1(d.JSTART, nr) + 1, JEN = A1(d.JMIX, nr) - 1;
+                double s = 0.0;
+                for (int jj = JST + l; jj <= JEN; jj += 32) s = racc(ro, s, V.pabs[jj - 1]);
+                for (int o = 16; o > 0; o >>= 1) s = racc(ro, s, __shfl_down_sync(0xffffffffu, s, o));
+                if (l == 0) chg[nr - 1] = (float)s / (float)(IMM1 * KMM1 * (JEN - JST + 1));
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int NROWS = d.NROWS;
+                if (NROWS == 1) s_blk[0] = chg[0];
+                if (NROWS == 2) {
+                    s_blk[1] = 0.5f * (chg[0] + chg[1]);
+                    s_blk[0] = s_blk[1];
+                }
+                if (NROWS > 2) {
+                    for (int nr = 2; nr <= NROWS - 1; ++nr)
+                        s_blk[nr - 1] = 0.25f * (chg[nr - 2] + chg[nr]) + 0.5f * chg[nr - 1];
+                    s_blk[NROWS - 1] = 0.5f * (chg[NROWS - 2] + chg[NROWS - 1]);
+                    s_blk[0] = 0.5f * (chg[0] + chg[1]);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    // damped cell changes of the cell planes j0, j0+1, j0+2 (those in 2..JM)
+    const int ks = IM * JM;
+    for (int h = 0; h < 3; ++h) {
+        const int jc = j0 + h;
+        if (jc < 2 || jc > JM) continue;
+        float *c = sm + h * nc;
+        const float blk = damp_on ? s_blk[A1(d.NROW, jc) - 1] : 1.0f;
+        const float *__restrict__ stp = V.ST + IM * (jc - 1);
+        Walk2 w(IMM1, threadIdx.x, PBS);
+        for (int t0 = threadIdx.x; t0 < nc; t0 += TS_UG * PBS) {
+            float sv[TS_UG];
+#pragma unroll
+            for (int u = 0; u < TS_UG; ++u) {
+                if (t0 + u * PBS < nc) sv[u] = stp[(w.i - 1) + ks * (w.k - 1)];
+                w.next();
+            }
+#pragma unroll
+            for (int u = 0; u < TS_UG; ++u) {
+                const int t = t0 + u * PBS;
+                if (t >= nc) break;
+                float v = sv[u];
+                if (damp_on) {
+                    float FDAMP = fabsf(v) / blk;
+                    v = v / (1.0f + FDAMP / DAMP);
+                }
+                c[t] = v;
+            }
+        }
+    }
+    __syncthreads();
+    // second pitchwise average on the mixing-plane cells (1850)
+    const bool lowx = d.FEXTRAP < 0.001f;
+    bool any = false;
+    for (int h = 0; h < 3; ++h) {
+        const int jc = j0 + h;
+        if (jc < 2 || jc > JM) continue;
+        int mnr;
+        const int role = mp_role(d, jc, &mnr);
+        if (role != 1 && role != 3) continue;
+        any = true;
+        float *c = sm + h * nc;
+        const int jmx = A1(d.JMIX, mnr);
+        for (int k = threadIdx.x + 1; k <= KMM1; k += PBS) {
+            float FLOWDIRN = -A3(d.FLOWX, d.IMID, jmx, k);
+            bool on = role == 3 ? (FLOWDIRN > 0.0f || lowx) : (FLOWDIRN < 0.0f || lowx);
+            if (!on) continue;
+            float *row = c + (k - 1) * IMM1;
+            float s = mp_line_sum(row, IMM1, d.REDUCE_ORDER != 0);
+            s = s / (float)IMM1;
+            for (int i = 0; i < IMM1; ++i) row[i] = s;
+        }
+    }
+    if (any) __syncthreads();
+    // gather (1100) on both node planes
+    const float *c0 = sm, *c1 = sm + nc, *c2 = sm + 2 * nc;
+    const float fdn0 = A1(d.FACDWN, j0), fup0 = two ? A1(d.FACUP, j0 + 1) : 0.0f;
+    const float fdn1 = two ? A1(d.FACDWN, j0 + 1) : 0.0f;
+    const float fup1 = j0 + 2 <= JM ? A1(d.FACUP, j0 + 2) : 0.0f;
+    const bool hA0 = j0 >= 2, hB0 = two;         // cell planes of node plane j0
+    const bool hB1 = j0 + 2 <= JM;               // node plane j0 + 1 always has its cell plane j0 + 1
+    const float *__restrict__ FBL = d.FBL;
+    const float *__restrict__ FBR = d.FBR;
+    const float *__restrict__ FTL = d.FTL;
+    const float *__restrict__ FTR = d.FTR;
+    const int nb0 = IM * (j0 - 1);
+    const int np = IM * KM;
+    // the general form of one node: cells (kc, h, ic) in the reference's order
+    auto edge = [&](int i, int k, float v, const float *cA, const float *cB, bool hA, bool hB, float fdn,
+                    float fup) -> float {
+        for (int kc = k - 1; kc <= k; ++kc) {
+            if (kc < 1 || kc > KMM1) continue;
+            for (int h = 0; h < 2; ++h) {
+                if (!(h ? hB : hA)) continue;
+                const float *c = h ? cB : cA;
+                float fac = h ? fup : fdn;
+                for (int ic = i - 1; ic <= i; ++ic) {
+                    if (ic < 1 || ic > IMM1) continue;
+                    float wt;
+                    if (ic == i) wt = (kc == k) ? AIK(FBL, ic, kc) : AIK(FTL, ic, kc);
+                    else wt = (kc == k) ? AIK(FBR, ic, kc) : AIK(FTR, ic, kc);
+                    v = v + c[(kc - 1) * IMM1 + (ic - 1)] * wt * fac;
+                }
+            }
+        }
+        return v;
+    };
+    Walk2 w(IM, threadIdx.x, PBS);
+    for (int t0 = threadIdx.x; t0 < np; t0 += TS_UG * PBS) {
+        float dv0[TS_UG], dv1[TS_UG], wtr[TS_UG], wtl[TS_UG], wbr[TS_UG], wbl[TS_UG];
+        int ni[TS_UG], nk[TS_UG];
+#pragma unroll
+        for (int u = 0; u < TS_UG; ++u) {
+            const int i = w.i, k = w.k;
+            ni[u] = i;
+            nk[u] = k;
+            w.next();
+            if (t0 + u * PBS < np) {
+                const int n = nb0 + (i - 1) + ks * (k - 1);
+                dv0[u] = D[n];
+                if (two) dv1[u] = D[n + IM];
+                if (i >= 2 && i <= IMM1 && k >= 2 && k <= KMM1) {
+                    wtr[u] = FTR[(i - 2) + IM * (k - 2)];
+                    wtl[u] = FTL[(i - 1) + IM * (k - 2)];
+                    wbr[u] = FBR[(i - 2) + IM * (k - 1)];
+                    wbl[u] = FBL[(i - 1) + IM * (k - 1)];
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < TS_UG; ++u) {
+            if (t0 + u * PBS >= np) break;
+            const int i = ni[u], k = nk[u];
+            const int n = nb0 + (i - 1) + ks * (k - 1);
+            const bool inner = i >= 2 && i <= IMM1 && k >= 2 && k <= KMM1;
+            const int lo = (i - 2) + IMM1 * (k - 2), hi = lo + IMM1;
+            // node plane j0: cell planes j0 (c0) and j0 + 1 (c1)
+            float v = dv0[u];
+            if (inner && hA0 && hB0) {
+                v = v + c0[lo] * wtr[u] * fdn0;
+                v = v + c0[lo + 1] * wtl[u] * fdn0;
+                v = v + c1[lo] * wtr[u] * fup0;
+                v = v + c1[lo + 1] * wtl[u] * fup0;
+                v = v + c0[hi] * wbr[u] * fdn0;
+                v = v + c0[hi + 1] * wbl[u] * fdn0;
+                v = v + c1[hi] * wbr[u] * fup0;
+                v = v + c1[hi + 1] * wbl[u] * fup0;
+            } else {
+                v = edge(i, k, v, c0, c1, hA0, hB0, fdn0, fup0);
+            }
+            TM[n] = v;
+            if (!two) continue;
+            // node plane j0 + 1: cell planes j0 + 1 (c1) and j0 + 2 (c2)
+            v = dv1[u];
+            if (inner && hB1) {
+                v = v + c1[lo] * wtr[u] * fdn1;
+                v = v + c1[lo + 1] * wtl[u] * fdn1;
+                v = v + c2[lo] * wtr[u] * fup1;
+                v = v + c2[lo + 1] * wtl[u] * fup1;
+                v = v + c1[hi] * wbr[u] * fdn1;
+                v = v + c1[hi + 1] * wbl[u] * fdn1;
+                v = v + c2[hi] * wbr[u] * fup1;
+                v = v + c2[hi + 1] * wbl[u] * fup1;
+            } else {
+                v = edge(i, k, v, c1, c2, true, hB1, fdn1, fup1);
+            }
+            TM[n + IM] = v;
         }
     }
 }
@@ -856,7 +1095,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_smooth(const __grid_consta
     if (mp) {
         for (int k = threadIdx.x + 1; k <= KM; k += BS) {
             float s;
-            if (d.REDUCE_ORDER == 1) {
+            if (d.REDUCE_ORDER != 0) {
                 s = 0.0f;
                 for (int i = 1; i <= IMM1; ++i) s = s + A1(d.FP, i) * (P(a, i, k) + P(a, i + 1, k));
             } else {
@@ -927,9 +1166,12 @@ __global__ void k_copy_tm_st(const __grid_constant__ Dev d, int v0, size_t n) {
     if (t < n) V.ST[t] = V.TM[t];
 }
 
-static size_t cells_smem(const Dev &d) { return ((size_t)d.IMM1 * d.KMM1 + d.KMM1) * sizeof(float); }
+static size_t cells_smem(const Dev &d) {
+    return ((size_t)d.IMM1 * d.KMM1 + d.KMM1 + (size_t)d.NIB1 * d.NKB1) * sizeof(float);
+}
 static size_t prolong_smem(const Dev &d) { return ((size_t)d.NIB1 * d.NKB1 + (size_t)d.NIB2 * d.NKB2) * sizeof(float); }
 static size_t update_smem(const Dev &d) { return (size_t)2 * d.IMM1 * d.KMM1 * sizeof(float); }
+static size_t update_pair_smem(const Dev &d) { return (size_t)3 * d.IMM1 * d.KMM1 * sizeof(float); }
 static size_t smooth_smem(const Dev &d) { return ((size_t)2 * d.IM * d.KM + 2 * d.IM + 2 * d.KM) * sizeof(float); }
 
 template <int BS>
@@ -940,6 +1182,7 @@ static cudaError_t configure_bs(const Dev &d) {
     } k[] = {{(const void *)k_ts_cells<BS>, cells_smem(d)},
              {(const void *)k_ts_prolong<BS>, prolong_smem(d)},
              {(const void *)k_ts_update<BS>, update_smem(d)},
+             {(const void *)k_ts_update_pair<2 * BS>, update_pair_smem(d)},
              {(const void *)k_ts_smooth<BS>, smooth_smem(d)}};
     for (auto &x : k) {
         if (x.bytes > 200 * 1024) return cudaErrorInvalidValue;
@@ -993,8 +1236,13 @@ static void launch_tstep_bs(const Dev &d, Launch L, int v0, int nv) {
         launchk(L, k_ts_avgblk_seq, dim3(1, vy), dim3(32), 0, d, v0);
         mark(L, "k_ts_avgblk_seq");
     }
-    launchk(L, k_ts_update<BS>, dim3(ja, vy), dim3(BS), update_smem(d), d, v0);
-    mark(L, "k_ts_update");
+    if (d.TS_PAIR) {
+        launchk(L, k_ts_update_pair<2 * BS>, dim3((ja + 1) / 2, vy), dim3(2 * BS), update_pair_smem(d), d, v0);
+        mark(L, "k_ts_update_pair");
+    } else {
+        launchk(L, k_ts_update<BS>, dim3(ja, vy), dim3(BS), update_smem(d), d, v0);
+        mark(L, "k_ts_update");
+    }
     launchk(L, k_ts_smooth<BS>, dim3(ja, vy), dim3(BS), smooth_smem(d), d, v0);
     mark(L, "k_ts_smooth");
 }

@@ -237,6 +237,14 @@ class Problem:
         _chk(load().mgpu_get_array(self.h, name.encode(), out.ctypes.data, out.nbytes))
         return out
 
+    def get_into(self, name: str, out: np.ndarray) -> np.ndarray:
+        """Copies a COMMON array into a caller's contiguous buffer (e.g. pinned
+        host memory), without allocating."""
+        if not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("get_into needs a contiguous buffer")
+        _chk(load().mgpu_get_array(self.h, name.encode(), out.ctypes.data, out.nbytes))
+        return out
+
     def set(self, name: str, a: np.ndarray):
         a = np.ascontiguousarray(a)
         _chk(load().mgpu_set_array(self.h, name.encode(), a.ctypes.data, a.nbytes))

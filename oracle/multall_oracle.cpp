@@ -204,7 +204,16 @@ struct Oracle : OracleBase {
         if (!strcmp(n, "FMIXUP")) { *v = (double)FMIXUP; return 0; }
         return fail(MGPU_E_ARG, std::string("unknown real scalar ") + n);
     }
+    /* branch counters of the last step, for tests that must show a branch
+       ran before they compare it: density-limiter changes (7200), Mach-
+       limiter changes (7100: RO raised to RO_LIMIT or FACSAFE < 1), and
+       NEW_MIXPLAN Prandtl-Meyer sweep updates (15151-15173) */
+    int cnt_dens = 0, cnt_mach = 0, cnt_pm = 0;
+
     int get_int(const char *n, int *v) override {
+        if (!strcmp(n, "ORACLE_NDENS")) { *v = cnt_dens; return 0; }
+        if (!strcmp(n, "ORACLE_NMACH")) { *v = cnt_mach; return 0; }
+        if (!strcmp(n, "ORACLE_NPM")) { *v = cnt_pm; return 0; }
 #define O_GI(nm, d) if (!strcmp(n, #nm)) { *v = nm; return 0; }
         MGPU_INT_SCALARS(O_GI)
         return fail(MGPU_E_ARG, std::string("unknown integer scalar ") + n);
@@ -1871,6 +1880,7 @@ struct Oracle : OracleBase {
                             R DELTAIM1 = om::sqrt(WMACH_JP2[im1] * WMACH_JP2[im1] - R(1)) /
                                          (ROREF_JP2[im1] * WREF_JP2[im1] * WREF_JP2[im1]);
                             ALPHAA[i] = ALPHAA[im1] + FROTN * DELP * R(0.5) * (DELTAI + DELTAIM1);
+                            ++cnt_pm;
                         }
                     }
                     for (int i = IMID - 1; i >= 1; --i) {
@@ -1881,6 +1891,7 @@ struct Oracle : OracleBase {
                             R DELTAIP1 = om::sqrt(WMACH_JP2[ip1] * WMACH_JP2[ip1] - R(1)) /
                                          (ROREF_JP2[ip1] * WREF_JP2[ip1] * WREF_JP2[ip1]);
                             ALPHAA[i] = ALPHAA[ip1] + FROTN * DELP * R(0.5) * (DELTAI + DELTAIP1);
+                            ++cnt_pm;
                         }
                     }
                     R ROTN = ALPHAA[IM] - ALPHAA[1];
@@ -1914,6 +1925,7 @@ struct Oracle : OracleBase {
     /* ================================================================== */
     int step(int force_end, mgpu_monitors *mon) override {
         if (!committed) return fail(MGPU_E_STATE, "step before commit");
+        cnt_dens = cnt_mach = cnt_pm = 0;
         IFPRINT = 0;
         NSTEP = NSTEP + 1;
         if (NSTEP == NSTEPS_MAX) IFEND = 1;
@@ -2444,9 +2456,11 @@ struct Oracle : OracleBase {
             for (int j = 3; j <= JM - 3; ++j)
                 for (int i = 1; i <= IM; ++i) {
                     R ROAVG = R(0.25) * (F3(RO, i, j - 2, k) + F3(RO, i, j - 1, k) + F3(RO, i, j + 1, k) + F3(RO, i, j + 2, k));
+                    const R before = F3(RO, i, j, k);
                     if (F3(RO, i, j, k) < R(0.6) * ROAVG) F3(RO, i, j, k) = R(0.5) * (F3(RO, i, j, k) + R(0.6) * ROAVG);
                     if (F3(RO, i, j, k) > R(1.5) * ROAVG) F3(RO, i, j, k) = R(0.5) * (F3(RO, i, j, k) + R(1.5) * ROAVG);
                     if (F3(RO, i, j, k) < ROLIM) F3(RO, i, j, k) = R(0.5) * (F3(RO, i, j, k) + ROLIM);
+                    if (!(F3(RO, i, j, k) == before)) ++cnt_dens;
                 }
         R GM1 = GA - R(1.0);
         R TRATIO = R(1.0) + MACHLIM * MACHLIM * R(0.5) * GM1;
@@ -2469,13 +2483,17 @@ struct Oracle : OracleBase {
                 int nr = F1(NROW, j);
                 R V_LIMIT = VLIMIT[nr - 1], RO_LIMIT = ROLIMIT[nr - 1];
                 for (int i = 1; i <= IM; ++i) {
-                    if (F3(RO, i, j, k) < RO_LIMIT) F3(RO, i, j, k) = RO_LIMIT;
+                    if (F3(RO, i, j, k) < RO_LIMIT) {
+                        F3(RO, i, j, k) = RO_LIMIT;
+                        ++cnt_mach;
+                    }
                     R RONOW = F3(RO, i, j, k);
                     R vx = F3(VX, i, j, k), vr = F3(VR, i, j, k), wt = F3(WT, i, j, k);
                     R WRELSQ = vx * vx + vr * vr + wt * wt;
                     R WREL = om::sqrt(WRELSQ);
                     R FACSAFE = V_LIMIT / WREL;
                     if (FACSAFE < R(1.0)) {
+                        ++cnt_mach;
                         F3(ROVX, i, j, k) = RONOW * vx * FACSAFE;
                         F3(ROVR, i, j, k) = RONOW * vr * FACSAFE;
                         R ROVTREL = RONOW * wt * FACSAFE;

@@ -183,6 +183,14 @@ class Oracle:
         self._chk(lib().oref_get_array(self.h, name.encode(), out.ctypes.data, out.nbytes, 1 if double else 0))
         return out
 
+    def get_int(self, name: str) -> int:
+        """An integer scalar, or one of the oracle's branch counters of the
+        last step: ORACLE_NDENS (density-limiter changes), ORACLE_NMACH
+        (Mach-limiter changes), ORACLE_NPM (Prandtl-Meyer sweep updates)."""
+        v = ctypes.c_int32()
+        self._chk(lib().oref_get_int(self.h, name.encode(), ctypes.byref(v)))
+        return v.value
+
     def get_real(self, name: str) -> float:
         v = ctypes.c_double()
         self._chk(lib().oref_get_real(self.h, name.encode(), ctypes.byref(v)))

@@ -464,3 +464,64 @@ def test_new_loss_inputs_are_required(mods):
     cd.ints["ILOS"] = 200
     with pytest.raises(O.OracleError, match="ILOS"):
         O.Oracle(cd)
+
+
+@pytest.mark.parametrize("branch", ["density_limiter", "mach_limiter", "supersonic_mixing_plane"])
+def test_branch_cases_make_the_oracle_take_each_branch(mods, branch):
+    """The inputs of the GPU branch tests make the oracle take the density
+    limiter, the Mach limiter and the Prandtl-Meyer sweep on step 1."""
+    from helpers import BRANCH_CASES
+    case, common_setup, O = mods
+    make, counter = BRANCH_CASES[branch]
+    o = O.Oracle(make(case, common_setup))
+    o.setup_calls()
+    o.step()
+    assert o.get_int(counter) > 0
+    assert O.Oracle(common_setup.build_common(case.small_stage())).get_int(counter) == 0
+    o.close()
+
+
+def test_gloo_two_ranks_run_the_bench_replica_logic():
+    """bench.py's multi-rank path on two gloo ranks with the GPU calls
+    stubbed: each rank sees only its own GPU (CUDA_VISIBLE_DEVICES = its
+    local rank), marches its own instance (here the CPU oracle, timed on the
+    host), and both report the slowest rank's time and the whole-job
+    throughput; the reference arm does no work on rank 1."""
+    import torch.multiprocessing as mp
+    mp.spawn(_bench_rank_main, args=(2,), nprocs=2, join=True)
+
+
+def _bench_rank_main(rank, world):
+    import os
+    import sys
+    import time
+    here = os.path.dirname(os.path.abspath(__file__))
+    for p in ("..", os.path.join("..", "multall-open-18.3_gb300"), os.path.join("..", "oracle")):
+        sys.path.insert(0, os.path.join(here, p))
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank), MASTER_ADDR="127.0.0.1",
+                      MASTER_PORT="29547")
+    import torch
+    import bench
+    from mgpu import case, common_setup
+    import oracle as O
+    dist = bench.replica_setup(world, rank, rank)
+    assert os.environ["CUDA_VISIBLE_DEVICES"] == str(rank)
+    cd = common_setup.build_common(case.small_stage(seed=20 + rank))
+    o = O.Oracle(cd)
+    o.setup_calls()
+    bench.dist_barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(2 + 3 * rank):          # rank 1 is the slow one
+        o.step()
+    ms = (time.perf_counter() - t0) * 1e3
+    ms_max, value = bench.replica_value(dist, world, cd.nodes(), 5, ms)
+    both = [torch.zeros(2, dtype=torch.float64) for _ in range(world)]
+    dist.all_gather(both, torch.tensor([ms, ms_max], dtype=torch.float64))
+    assert all(abs(b[1].item() - max(x[0].item() for x in both)) < 1e-9 for b in both)
+    assert abs(value - cd.nodes() * 5 * world / (ms_max / 1e3) / 1e9) < 1e-12
+    if rank == 1:
+        class A:
+            steps, warmup, gpus = 1, 1, world
+        assert bench.run_reference(A, rank, world) == 0
+    o.close()
+    dist.destroy_process_group()

@@ -61,9 +61,12 @@ def test_setup_calls_match(mods, which):
 
 
 @pytest.mark.parametrize("which", ["small_nozzle", "small_stage"])
-def test_one_step(mods, which):
+@pytest.mark.parametrize("order", [0, 2])
+def test_one_step(mods, which, order):
+    """One step against the FP32 oracle, on the default precision split
+    (REDUCE_ORDER 0) and on the plain FP32 path (2)."""
     case = mods[0]
-    cd, gpu, ref = _pair(mods, getattr(case, which)())
+    cd, gpu, ref = _pair(mods, getattr(case, which)(), REDUCE_ORDER=order)
     gpu.step()
     ref.step()
     _compare(gpu, ref, STATE, STEP1_TOL, "step 1")
@@ -267,9 +270,11 @@ def test_converged_mass_flow_and_efficiency(mods):
 def test_precision_split_against_fp64_oracle(mods):
     """The reported quantities against the FP64 oracle after 1500 steps of
     the small stage: the default path (FP32 field arithmetic, FP64 for the
-    multigrid, row-mean, mixing-plane, monitor and integral sums) and the
-    plain FP32 path (REDUCE_ORDER=1) both keep mass flow within 1e-4
-    relative and total-to-total efficiency within 1e-4 absolute."""
+    multigrid, row-mean, mixing-plane, monitor and integral sums), the
+    reference-order path (REDUCE_ORDER=1: the long sums sequential in
+    REAL*4) and the plain FP32 path (REDUCE_ORDER=2: the default path's
+    parallel trees with FP32 adds) all keep mass flow within 1e-4 relative
+    and total-to-total efficiency within 1e-4 absolute."""
     case, common_setup, lib, O = mods
     spec = case.small_stage()
     cd = common_setup.build_common(spec)
@@ -281,7 +286,7 @@ def test_precision_split_against_fp64_oracle(mods):
         ref64.step()
     i64 = ref64.integrals()
     errs = {}
-    for order in (0, 1):
+    for order in (0, 1, 2):
         cd.ints["REDUCE_ORDER"] = order
         gpu = lib.Problem(cd)
         gpu.run(n)
@@ -289,7 +294,8 @@ def test_precision_split_against_fp64_oracle(mods):
         errs[order] = (abs(ig.mass_flow_in - i64.mass_flow_in) / abs(i64.mass_flow_in), abs(ig.eta_tt - i64.eta_tt))
         gpu.close()
     cd.ints["REDUCE_ORDER"] = 0
-    print("mass-flow rel / eta abs error vs FP64 oracle: FP64 sums", errs[0], "plain FP32", errs[1])
+    print("mass-flow rel / eta abs error vs FP64 oracle: FP64 sums", errs[0], "reference order", errs[1],
+          "plain FP32", errs[2])
     for order, (em, ee) in errs.items():
         assert em <= 1e-4 and ee <= 1e-4, (order, em, ee)
 
@@ -327,6 +333,28 @@ def test_deterministic(mods):
         cd, gpu, ref = _pair(mods, case.small_stage())
         gpu.run(20)
         outs.append([gpu.get(n) for n in ("RO", "ROE", "ROVX")])
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("which", ["small_stage", "small_nozzle"])
+@pytest.mark.parametrize("bs", [128, 192, 256, 512])
+def test_pair_update_matches_single_plane_update(mods, which, bs):
+    """TSTEP's damping and corner gather over pairs of J-planes (TS_PAIR=1,
+    the default) give bitwise the state of the one-CTA-per-plane kernel
+    (TS_PAIR=0) after 12 steps, at every CTA size.  The nozzle's JM = 29 is
+    odd, so its last pair holds a single plane."""
+    case, common_setup, lib, O = mods
+    spec = getattr(case, which)()
+    outs = []
+    for pair in (0, 1):
+        cd = common_setup.build_common(spec)
+        cd.ints["TS_PAIR"] = pair
+        cd.ints["TS_THREADS"] = bs
+        gpu = lib.Problem(cd)
+        gpu.run(12)
+        outs.append([gpu.get(n) for n in ("RO", "ROE", "ROVX", "RORVT", "ROVR", "DRO", "DROE")])
+        gpu.close()
     for a, b in zip(*outs):
         assert np.array_equal(a, b)
 
@@ -380,6 +408,11 @@ def test_api_errors(mods):
     with pytest.raises(lib.MgpuError) as e:
         gpu.set("AQX", cd.arrays["AQX"])      # geometry is fixed after commit
     assert e.value.code == -2
+    gpu.close()
+    cd.ints["REDUCE_ORDER"] = 3                # 0, 1 and 2 are the only orders
+    with pytest.raises(lib.MgpuError) as e:
+        lib.Problem(cd)
+    assert e.value.code == -1
 
 
 @pytest.mark.parametrize("bs", [128, 192, 512])
