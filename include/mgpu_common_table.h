@@ -125,7 +125,16 @@
     M_(VSOUND,    MGPU_REQUIRED_REAL)                                     \
     M_(CONLIM,    0.001f)                                                 \
     M_(VISLAM,    0.0f)                                                   \
-    M_(FTCOND,    0.0f)
+    M_(FTCOND,    0.0f)                                                   \
+    /* Spalart-Allmaras (ILOS >= 200) source-term factors, reader 631-652 */ \
+    M_(FAC_STMIX, 0.0f)                                                   \
+    M_(FAC_ST0,   1.0f)                                                   \
+    M_(FAC_ST1,   1.0f)                                                   \
+    M_(FAC_ST2,   1.0f)                                                   \
+    M_(FAC_ST3,   1.0f)                                                   \
+    M_(FAC_SFVIS, 2.0f)                                                   \
+    M_(FAC_VORT,  0.0f)                                                   \
+    M_(FAC_PGRAD, 0.0f)
 
 /* ----- arrays ------------------------------------------------------------ */
 #define MGPU_ARRAYS(M_)                                                   \
@@ -161,6 +170,10 @@
     M_(SEP_THIK, FLOAT32, ROW, OPT)                                       \
     M_(SEP_DRAG, FLOAT32, ROW, OPT)                                       \
     M_(NSTAGE,   INT32,   ROW, OPT)     /* stage of each row (EFICOOL) */ \
+    /* Spalart-Allmaras: free-stream turbulence and mixing-plane decay   */ \
+    /* of the transported viscosity (reader 2070-2073)                   */ \
+    M_(FSTURB,   FLOAT32, ROW, OPT)                                       \
+    M_(TURBVIS_DAMP, FLOAT32, ROW, OPT)                                   \
     /* per streamwise station J */                                       \
     M_(NBLADE,   INT32,   J,   GEOM)                                      \
     M_(IND,      INT32,   J,   GEOM)                                      \
@@ -268,6 +281,14 @@
     M_(Y_PLUS,   FLOAT32, IJK, STATE)                                     \
     M_(DPDS_CELL,FLOAT32, IJK, STATE)                                     \
     M_(VISC_RAT, FLOAT32, IJK, OUT)                                       \
-    M_(VISC_LAM, FLOAT32, IJK, OUT)
+    M_(VISC_LAM, FLOAT32, IJK, OUT)                                       \
+    /* Spalart-Allmaras (ILOS >= 200): the transported (cell-centred)    */ \
+    /* turbulent viscosity, its SCREE history, its kinematic value and    */ \
+    /* its relaxed source term, /BKNEWLOS/                                */ \
+    M_(TRANS_DYN_VIS, FLOAT32, IJK, OPT)                                  \
+    M_(DEL_DYNVIS, FLOAT32, IJK, OPT)                                     \
+    M_(TRANS_KVIS, FLOAT32, IJK, OPT)                                     \
+    M_(T_SOURCE, FLOAT32, IJK, OPT)                                       \
+    M_(VISC_TURB, FLOAT32, IJK, OUT)
 
 #endif /* MGPU_COMMON_TABLE_H_ */

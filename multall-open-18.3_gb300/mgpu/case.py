@@ -57,6 +57,7 @@ class RowSpec:
     xllim: tuple = (0.03, 0.03, 0.03, 0.03, 0.03, 0.02)  # XLLIM_I1,IM,K1,KM,DWN,UP
     xllim_new: tuple = (0.03, 0.03, 0.03, 0.03)  # ILOS >= 100: XLLIM_IN,LE,TE,DN
     fsturb: float = 1.0     # ILOS >= 100: FSTURB, free-stream turbulent viscosity ratio
+    turbvis_damp: float = 0.5   # ILOS >= 200: TURBVIS_DAMP, decay of the transported viscosity across a mixing plane
     # IF_CUSP = 2: forced trailing-edge separation (multall-open-18.3.f:987-1005)
     if_cusp: int = 0
     nup_i1: int = 0         # NUP_I1, NUP_IM: points before the TE where it starts
@@ -123,7 +124,14 @@ class CaseSpec:
     facmixup: float = 2.0
     nmixup: int = 1000
     nlos: int = 5
-    ilos: int = 10              # 10: LOSS; 100-199: NEW_LOSS
+    ilos: int = 10              # 10: LOSS; 100-199: NEW_LOSS; 200-299: Spalart-Allmaras (SPAL_LOSS)
+    # Spalart-Allmaras source-term factors FAC_STMIX, FAC_ST0..3, FAC_SFVIS,
+    # FAC_VORT, FAC_PGRAD (the reader's defaults, 631-639)
+    fac_stmix: float = 0.0
+    fac_st: tuple = (1.0, 1.0, 1.0, 1.0)
+    fac_sfvis: float = 2.0
+    fac_vort: float = 0.0
+    fac_pgrad: float = 0.0
     turbvis_lim: float = 3000.0
     in_vr: int = 0
     in_flow: int = 0            # IN_FLOW: 0 off, 3 towards FLOWIN, otherwise towards the mean flow

@@ -549,7 +549,7 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None, metrics64: boo
     DWALLSQ, DIST = wall_distance_sq(IM, JM, KM, X, R, THETA, ASX, ASR, ABX, ABR, ABT, JSTART, JMIX, JLE, JTE,
                                      NROW, NBLADE, IMID, spec, with_dist=True)
     new_loss = {}
-    if 100 <= spec.ilos < 200:
+    if spec.ilos >= 100:
         new_loss = mixing_lengths(spec, IM, JM, KM, DIST, SMERID, JSTART, JMIX, JLE, JTE, NROW, IMID, KMID)
         # cell-average density: the initial guess's node values (6796) until
         # the first step forms it (4255-4267)
@@ -583,6 +583,13 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None, metrics64: boo
     reals["TURBVIS_LIM"] = spec.turbvis_lim
     if new_loss:
         reals["VORT_MAX"] = new_loss_vort
+    if spec.ilos >= 200:
+        # the Spalart-Allmaras cards (reader 631-652, 2070-2073)
+        reals.update(FAC_STMIX=spec.fac_stmix, FAC_ST0=spec.fac_st[0], FAC_ST1=spec.fac_st[1],
+                     FAC_ST2=spec.fac_st[2], FAC_ST3=spec.fac_st[3], FAC_SFVIS=spec.fac_sfvis,
+                     FAC_VORT=spec.fac_vort, FAC_PGRAD=spec.fac_pgrad)
+        new_loss["FSTURB"] = np.array([r.fsturb for r in spec.rows], f32)
+        new_loss["TURBVIS_DAMP"] = np.array([r.turbvis_damp for r in spec.rows], f32)
     xl = np.array([r.xllim for r in spec.rows], np.float32)
     arr = dict(
         JSTART=JSTART, JMIX=JMIX, JLE=JLE, JTE=JTE, JLED=JLED, KTIPS=KTIPS, KTIPE=KTIPE, KS1=KS1, KS2=KS2,

@@ -120,6 +120,10 @@ inline AD exp(const AD &x) {
 inline AD sin(const AD &x) { return rec1(std::sin(x.v), x, std::cos(x.v)); }
 inline AD cos(const AD &x) { return rec1(std::cos(x.v), x, -std::sin(x.v)); }
 inline AD asin(const AD &x) { return rec1(std::asin(x.v), x, 1.0 / std::sqrt(1.0 - x.v * x.v)); }
+inline AD tanh(const AD &x) {
+    double t = std::tanh(x.v);
+    return rec1(t, x, 1.0 - t * t);
+}
 inline AD atan2(const AD &y, const AD &x) {
     double r2 = x.v * x.v + y.v * y.v;
     return rec2(std::atan2(y.v, x.v), y, x.v / r2, x, -y.v / r2);

@@ -13,6 +13,9 @@
  *   SMOOTH_RESID    14833-14917
  *   LOSS            8058-9066   (ILOS=10)
  *   NEW_LOSS        12522-13508 (ILOS 100-199) and the cell-average density 4255-4267
+ *   SPAL_LOSS       13586-14832 (ILOS 200-299), GRADCELL 13516-13585, the
+ *                   transported viscosity's fluxes 4279-4347, TSTEP's
+ *                   NCALL = 2 branch 5736-5777 and its inlet value 4679-4689
  *   WALLFUN         15980-16047
  *   NEW_MIXPLAN     14922-15251
  *   STEPUP          7916-8002
@@ -51,7 +54,7 @@
    overloads (found by argument-dependent lookup) for adt::AD */
 namespace om {
 #define OM_FN1(f) template <class T> inline T f(const T &x) { using std::f; return f(x); }
-OM_FN1(sqrt) OM_FN1(fabs) OM_FN1(log) OM_FN1(log10) OM_FN1(sin) OM_FN1(cos) OM_FN1(asin)
+OM_FN1(sqrt) OM_FN1(fabs) OM_FN1(log) OM_FN1(log10) OM_FN1(sin) OM_FN1(cos) OM_FN1(asin) OM_FN1(tanh)
 #undef OM_FN1
 template <class T> inline T pow(const T &x, const T &y) { using std::pow; return pow(x, y); }
 template <class T> inline T atan2(const T &y, const T &x) { using std::atan2; return atan2(y, x); }
@@ -283,8 +286,10 @@ struct Oracle : OracleBase {
             const R PRF = R(0.5) * (F3(P, IMID, 1, KMID) + F3(P, IMID, JM, KMID));
             const R E6 = std::is_same<R, float>::value ? R(1.0e-6f) : R(1.0e-6);
             std::vector<R> dp(N), pe(N), rs(N);
+            /* the seventh array: the transported viscosity with the S-A model,
+               else DPDS_CELL * 1e-6 for plotting (5966-5972) */
             for (size_t n = 0; n < N; ++n) {
-                dp[n] = DPDS_CELL_v[n] * E6;
+                dp[n] = ILOS >= 200 ? TRANS_DYN_VIS_v[n] : DPDS_CELL_v[n] * E6;
                 pe[n] = PEFF_v[n] + PRF;
                 rs[n] = rosub ? R(rosub[n]) : RO_v[n];
             }
@@ -337,18 +342,22 @@ struct Oracle : OracleBase {
             if (committed) return fail(MGPU_E_STATE, "read_flow_out after commit (SETUP reads the restart file)");
             const size_t N = (size_t)IM * JM * KM;
             const uint32_t rb = (uint32_t)(N * sizeof(R));
-            std::vector<R> ro(N), rovx(N), rovr(N), rovt(N), roe(N);
+            std::vector<R> ro(N), rovx(N), rovr(N), rovt(N), roe(N), tdv(N);
             int32_t ns = 0;
             FILE *f = fopen(path, "rb");
             if (!f) return fail(MGPU_E_ARG, std::string("cannot open: ") + path);
+            /* the seventh array is read into TRANS_DYN_VIS whatever the model
+               (6934) */
             const bool ok = fo_get(f, &ns, 4) && fo_get(f, ro.data(), rb) && fo_get(f, rovx.data(), rb) &&
                             fo_get(f, rovr.data(), rb) && fo_get(f, rovt.data(), rb) && fo_get(f, roe.data(), rb) &&
-                            fo_get(f, nullptr, rb) && fo_get(f, nullptr, rb);
+                            fo_get(f, nullptr, rb) && fo_get(f, tdv.data(), rb);
             fclose(f);
             if (!ok) return fail(MGPU_E_ARG, std::string("not a flow_out file of this grid: ") + path);
             if (!R_v.size() || !FP_v.size() || !PD_v.size()) return fail(MGPU_E_ARG, "bind R, FP and PD before the restart");
             const R CVr = CP / GA, RGASr = CP - CVr;   /* SETUP 6459-6468 */
             RO_v = ro; ROVX_v = rovx; ROVR_v = rovr; ROVT_v = rovt; ROE_v = roe;
+            TRANS_DYN_VIS_v = tdv;
+            TRANS_DYN_VIS_set = true;
             for (std::vector<R> *v : {&VX_v, &VR_v, &VT_v, &RORVT_v, &T_STATIC_v, &HO_v, &P_v, &PEFF_v}) v->assign(N, R(0));
             /* 3900, IFGAS = 0, ITIMST < 5 */
             for (int k = 1; k <= KM; ++k)
@@ -393,11 +402,11 @@ struct Oracle : OracleBase {
 #define O_CHK_R(nm, d) if ((float)nm == MGPU_REQUIRED_REAL) return fail(MGPU_E_ARG, "real not set: " #nm);
         MGPU_REAL_SCALARS(O_CHK_R)
         if (ITIMST != 3) return fail(MGPU_E_UNSUPPORTED, "ITIMST other than 3 (incompressible 5/6) not covered");
-        if (ILOS != 10 && !(ILOS >= 100 && ILOS < 200))
-            return fail(MGPU_E_UNSUPPORTED, "only ILOS=10 (LOSS) and ILOS 100-199 (NEW_LOSS) are covered");
-        if (ILOS >= 100 && !(VORT_MAX > R(0))) return fail(MGPU_E_ARG, "ILOS 100-199 needs VORT_MAX > 0 (SETUP 7322-7328)");
+        if (ILOS != 10 && !(ILOS >= 100 && ILOS < 300))
+            return fail(MGPU_E_UNSUPPORTED, "only ILOS=10 (LOSS), 100-199 (NEW_LOSS) and 200-299 (SPAL_LOSS) are covered");
+        if (ILOS >= 100 && !(VORT_MAX > R(0))) return fail(MGPU_E_ARG, "ILOS >= 100 needs VORT_MAX > 0 (SETUP 7322-7328)");
         if (ILOS >= 100 && !(XLENGTH_set && FST_RAT_set && ROAVG_CELL_set))
-            return fail(MGPU_E_ARG, "ILOS 100-199 needs XLENGTH, FST_RAT and ROAVG_CELL");
+            return fail(MGPU_E_ARG, "ILOS >= 100 needs XLENGTH, FST_RAT and ROAVG_CELL");
         if (IFGAS != 0) return fail(MGPU_E_UNSUPPORTED, "real-gas IFGAS=1 not covered");
         if (IFCOOL || IFBLEED || IFSHROUD) return fail(MGPU_E_UNSUPPORTED, "cooling/bleed/shroud not covered");
         if (IF_REPEAT != 0) return fail(MGPU_E_UNSUPPORTED, "IF_REPEAT not covered");
@@ -419,6 +428,15 @@ struct Oracle : OracleBase {
         FLOWR.assign(n3, R(0)); STORE.assign(n3, R(0)); TEMP1.assign(n3, R(0));
         VISC_RAT_v.assign(n3, R(0));
         VISC_LAM_v.assign(n3, R(0));
+        VISC_TURB_v.assign(n3, R(0));
+        /* Spalart-Allmaras state: zero unless bound (SETUP 6905-6908), the
+           reader's defaults FSTURB = 1, TURBVIS_DAMP = 0.5 (2052-2053) */
+        if (!TRANS_DYN_VIS_set) TRANS_DYN_VIS_v.assign(n3, R(0));
+        if (!DEL_DYNVIS_set) DEL_DYNVIS_v.assign(n3, R(0));
+        if (!TRANS_KVIS_set) TRANS_KVIS_v.assign(n3, R(0));
+        if (!T_SOURCE_set) T_SOURCE_v.assign(n3, R(0));
+        if (!FSTURB_set) FSTURB_v.assign(NROWS, R(1.0));
+        if (!TURBVIS_DAMP_set) TURBVIS_DAMP_v.assign(NROWS, R(0.5));
         PLIM.assign(KM, R(0)); VLIMIT.assign(NROWS, R(0)); ROLIMIT.assign(NROWS, R(0));
         AVG_CHG.assign(NROWS, R(0)); AVG_BLK.assign(NROWS, R(0));
         BLADE_FLOW.assign(JM, R(0)); CHECK_FLOW.assign(JM, R(0));
@@ -663,7 +681,7 @@ struct Oracle : OracleBase {
     /* ================================================================== */
     /*  TSTEP(D, DIFF, NCALL)   multall-open-18.3.f:5470-5932               */
     /* ================================================================== */
-    void tstep(std::vector<R> &D, std::vector<R> &DIFF) {
+    void tstep(std::vector<R> &D, std::vector<R> &DIFF, int NCALL = 1) {
         std::fill(B1CHG.begin(), B1CHG.end(), R(0.0));
         std::fill(B2CHG.begin(), B2CHG.end(), R(0.0));
         std::fill(SBCHG.begin(), SBCHG.end(), R(0.0));
@@ -808,6 +826,26 @@ struct Oracle : OracleBase {
                     }
                 }
         }
+        if (NCALL == 2) {
+            /* the cell-centred transported viscosity (5736-5777): the change
+               is added to the cell, the row's last plane is carried across
+               the mixing plane with the decay TURBVIS_DAMP, then one
+               residual-smoothing pass */
+            for (int k = 1; k <= KMM1; ++k)
+                for (int j = 2; j <= JM; ++j)
+                    for (int i = 1; i <= IMM1; ++i) A3(D, i, j, k) = A3(D, i, j, k) + A3(STORE, i, j, k);
+            for (int nr = 1; nr <= NROWS - 1; ++nr) {
+                int j = F1(JMIX, nr);
+                R FMULT = F1(TURBVIS_DAMP, nr);
+                for (int k = 1; k <= KMM1; ++k) {
+                    R AVG = R(0.0);
+                    for (int i = 1; i <= IMM1; ++i) AVG = AVG + F1(FP, i) * A3(D, i, j, k);
+                    for (int jav = j + 1; jav <= j + 2; ++jav)
+                        for (int i = 1; i <= IMM1; ++i) A3(D, i, jav, k) = FMULT * AVG;
+                }
+            }
+            smooth_resid(D, FAC_SFVIS * SFT, 1);
+        } else {
         /* second mixing-plane pitchwise average 1850 */
         for (int nr = 1; nr <= NRWSM1; ++nr) {
             int j = F1(JMIX, nr);
@@ -844,8 +882,9 @@ struct Oracle : OracleBase {
                     A3(D, i + 1, j - 1, k + 1) = A3(D, i + 1, j - 1, k + 1) + ADD * FIK(FTR, i, k) * fup;
                 }
         smooth_var(D);
+        }
         /* periodic boundaries 8000 */
-        int ILAST = IM;
+        int ILAST = NCALL == 2 ? IMM1 : IM;
         for (int j = 1; j <= JM; ++j) {
             if (F1(IND, j) == 1 || F1(INDLE, j) == 1) continue;
             for (int k = 1; k <= KM; ++k) {
@@ -1514,7 +1553,6 @@ struct Oracle : OracleBase {
             FTCOND = TCOND / VISLAM;
         }
         const size_t N = (size_t)IM * JM * KM;
-        std::vector<R> FX(N, R(0)), FRr(N, R(0)), FT(N, R(0)), ES(N, R(0));
         std::vector<R> TXR(N), TXX(N), TXT(N), TRR(N), TRT(N), TTT(N), QXX(N), QRR(N), QTT(N);
         R FYPLUS = R(0);
         /* ---- DO 150: strain rates and the eddy viscosity of every cell ---- */
@@ -1601,6 +1639,18 @@ struct Oracle : OracleBase {
                     QRR[n] = -THCOND * QRR[n];
                     QTT[n] = -THCOND * QTT[n];
                 }
+        viscous_walls_and_forces(TXR, TXX, TXT, TRR, TRT, TTT, QXX, QRR, QTT, false);
+    }
+
+    /* The wall shear stresses, the I- and K-face stresses and the body-force
+       update that NEW_LOSS (12975-13462) and SPAL_LOSS (14160-14832) share;
+       they differ only in SPAL_LOSS setting Y_PLUS up to I = IM on the
+       I = IM side (14236) where NEW_LOSS stops at IMM1 (12742). */
+    void viscous_walls_and_forces(std::vector<R> &TXR, std::vector<R> &TXX, std::vector<R> &TXT, std::vector<R> &TRR,
+                                  std::vector<R> &TRT, std::vector<R> &TTT, std::vector<R> &QXX, std::vector<R> &QRR,
+                                  std::vector<R> &QTT, bool sa) {
+        const size_t N = (size_t)IM * JM * KM;
+        std::vector<R> FX(N, R(0)), FRr(N, R(0)), FT(N, R(0)), ES(N, R(0));
         /* TRX = TXR, TTX = TXT, TTR = TRT */
         if (YPLUSWALL < R(-10.0)) set_pwallgrad();
         const R VISLAM16 = VISLAM * R(16.0);
@@ -1643,7 +1693,7 @@ struct Oracle : OracleBase {
                             R RE = DPERP * ROA * WAVG / VISLAM16;
                             TW = nl_twall(RE, DPERP, side == 0 ? F1(ROUGH_L, NRW) : F1(ROUGH_U, NRW), ROA, WAVG);
                         }
-                        int i0 = side == 0 ? 1 : IMID + 1, i1 = side == 0 ? IMID : IMM1;
+                        int i0 = side == 0 ? 1 : IMID + 1, i1 = side == 0 ? IMID : (sa ? IM : IMM1);
                         for (int i = i0; i <= i1; ++i) {
                             R VSTAR = om::sqrt(TW / (R(0.25) * ROA));
                             R YPLS = VSTAR * om::sqrt(F3(DWALLSQ, i, j, k)) * (R(0.25) * ROA) / VISLAM;
@@ -1773,6 +1823,380 @@ struct Oracle : OracleBase {
                 }
     }
 
+    /* ================================================================== */
+    /*  SPAL_LOSS (ILOS >= 200)  multall-open-18.3.f:13586-14832, with      */
+    /*  GRADCELL 13516-13585; the wall shear and face stresses are         */
+    /*  NEW_LOSS's (viscous_walls_and_forces)                              */
+    /* ================================================================== */
+    /* cell gradient of a cell-centred quantity by Gauss' theorem
+       (13516-13585).  Cells past J = JM read the never-written COMMON slots
+       of V, which hold zero. */
+    void gradcell(int i, int j, int k, const std::vector<R> &V, R &DVDX, R &DVDR, R &DVDT) {
+        int ip1 = i + 1, jp1 = j + 1, kp1 = k + 1, im1 = i - 1, jm1 = j - 1, km1 = k - 1;
+        if (i == 1) im1 = IMM1;
+        if (i == IMM1) ip1 = 1;
+        if (k == 1) km1 = 1;
+        if (k == KMM1) kp1 = KMM1;
+        auto v = [&](int a, int b, int c) -> R { return b > JM ? R(0) : V[ijk(a, b, c)]; };
+        R RVOL = R(0.5) / F3(VOL, i, j, k);
+        R VAVGJ1 = v(i, j, k) + v(i, jm1, k);
+        R VAVGJ2 = v(i, j, k) + v(i, jp1, k);
+        R VAVGI1 = v(i, j, k) + v(im1, j, k);
+        R VAVGI2 = v(i, j, k) + v(ip1, j, k);
+        R VAVGK1 = v(i, j, k) + v(i, j, km1);
+        R VAVGK2 = v(i, j, k) + v(i, j, kp1);
+        if (F1(IND, j) == 1) {
+            if (i == 1) VAVGI1 = R(0.0);
+            if (i == IMM1) VAVGI2 = R(0.0);
+        }
+        if (k == 1 && (IBOUND == 0 || IBOUND == 2)) VAVGK1 = R(0.0);
+        if (k == KMM1 && IBOUND <= 1) VAVGK2 = R(0.0);
+        DVDX = -(VAVGJ2 * F3(AQX, i, j, k) - VAVGJ1 * F3(AQX, i, jm1, k) + VAVGI1 * F3(ABX, i, j, k) -
+                 VAVGI2 * F3(ABX, ip1, j, k) + VAVGK1 * F3(ASX, i, j, k) - VAVGK2 * F3(ASX, i, j, kp1)) *
+               RVOL;
+        DVDR = -(VAVGJ2 * F3(AQR, i, j, k) - VAVGJ1 * F3(AQR, i, jm1, k) + VAVGI1 * F3(ABR, i, j, k) -
+                 VAVGI2 * F3(ABR, ip1, j, k) + VAVGK1 * F3(ASR, i, j, k) - VAVGK2 * F3(ASR, i, j, kp1)) *
+                   RVOL -
+               v(i, j, k) / F2(RAVG_CELL, j, k);
+        DVDT = -(VAVGI1 - VAVGI2) * F2(ABT, j, k) * RVOL;
+    }
+
+    /* the free-stream transported viscosity (13832-13838, 4681-4684) */
+    R sa_transvis_in(R vislam) const {
+        R fs = F1(FSTURB, 1);
+        if (fs < R(1.0)) return R(4.35) * vislam * om::pow(fs, R(0.25));
+        return vislam * (R(3.5) + fs * R(0.85));
+    }
+
+    std::vector<R> ABS_VORT_w, TRANS_VORT_w, DYN_VIS_ML_w, GRAD_TVIS_w, TVISGRADX_w, TVISGRADR_w, TVISGRADT_w;
+    std::vector<R> REYNOLDS_w;
+
+    void spal_loss() {
+        const int NDAMP = 100000;
+        if (NSTEP == 1 || NSTEP < NSTEPS_MAX / 4) {
+            if (REYNO > R(100.)) {
+                int J1 = F1(JLE, 1), J2 = F1(JTE, 1);
+                if (F1(JLE, 1) > JM) J1 = 1;
+                if (F1(JTE, 1) > JM) J2 = JM;
+                R XCHORD = F2(SMERID, J2, KMID) - F2(SMERID, J1, KMID);
+                R a = F3(ROVX, IMID, J2, KMID), b = F3(ROVR, IMID, J2, KMID), c = F3(ROWT, IMID, J2, KMID);
+                VISLAM = XCHORD * om::sqrt(a * a + b * b + c * c) / REYNO;
+            }
+            if (REYNO > R(0.0) && REYNO < R(99.99)) VISLAM = REYNO / R(100000.);
+            if (REYNO < R(0.0)) VISLAM = -REYNO * R(1.0E-5);
+            TCOND = CP * VISLAM / PRANDTL;
+            FTCOND = TCOND / VISLAM;
+        }
+        const size_t N = (size_t)IM * JM * KM;
+        std::vector<R> TXR(N), TXX(N), TXT(N), TRR(N), TRT(N), TTT(N), QXX(N), QRR(N), QTT(N);
+        if (ABS_VORT_w.size() != N) {
+            ABS_VORT_w.assign(N, R(0)); TRANS_VORT_w.assign(N, R(0)); DYN_VIS_ML_w.assign(N, R(0));
+            GRAD_TVIS_w.assign(N, R(0)); TVISGRADX_w.assign(N, R(0)); TVISGRADR_w.assign(N, R(0));
+            TVISGRADT_w.assign(N, R(0));
+            REYNOLDS_w.assign(NROWS, R(0));
+        }
+        if (FAC_PGRAD > R(0.001)) set_pwallgrad();
+        R VORTICITY_FAC = R(0), PGRAD_FAC = R(0);   /* scalars: the last cell's values are used below */
+        /* ---- DO 1000: strain rates, vorticity and the S-A viscosity ---- */
+        for (int k = 1; k <= KMM1; ++k)
+            for (int j = 2; j <= JM; ++j) {
+                int NRW = F1(NROW, j), JTEDGE = F1(JTE, NRW);
+                for (int i = 1; i <= IMM1; ++i) {
+                    auto avg8 = [&](const std::vector<R> &A) {
+                        return R(0.125) * (A3(A, i, j, k) + A3(A, i + 1, j, k) + A3(A, i + 1, j, k + 1) + A3(A, i, j, k + 1) +
+                                           A3(A, i, j - 1, k) + A3(A, i + 1, j - 1, k) + A3(A, i + 1, j - 1, k + 1) +
+                                           A3(A, i, j - 1, k + 1));
+                    };
+                    auto sum8 = [&](const std::vector<R> &A) {
+                        return A3(A, i, j, k) + A3(A, i + 1, j, k) + A3(A, i + 1, j, k + 1) + A3(A, i, j, k + 1) +
+                               A3(A, i, j - 1, k) + A3(A, i + 1, j - 1, k) + A3(A, i + 1, j - 1, k + 1) + A3(A, i, j - 1, k + 1);
+                    };
+                    R WTAVG = avg8(WT_v), ROAVG = F3(ROAVG_CELL, i, j, k), TSAVG = avg8(T_STATIC_v);
+                    R RAVG = F2(RAVG_CELL, j, k);
+                    R DVXDX, DVXDR, DVXDT, DVRDX, DVRDR, DVRDT, DWTDX, DWTDR, DWTDT, DTDX, DTDR, DTDT;
+                    gradvel(i, j, k, VX_v, DVXDX, DVXDR, DVXDT);
+                    gradvel(i, j, k, VR_v, DVRDX, DVRDR, DVRDT);
+                    gradvel(i, j, k, WT_v, DWTDX, DWTDR, DWTDT);
+                    gradvel(i, j, k, T_STATIC_v, DTDX, DTDR, DTDT);
+                    size_t n = ijk(i, j, k);
+                    TXR[n] = DVXDR + DVRDX;
+                    TXX[n] = DVXDX;
+                    TXT[n] = DWTDX + DVXDT;
+                    TRR[n] = DVRDR;
+                    TRT[n] = DWTDR + DVRDT - WTAVG / RAVG;
+                    TTT[n] = DWTDT;
+                    QXX[n] = DTDX;
+                    QRR[n] = DTDR;
+                    QTT[n] = DTDT;
+                    R VORTX = DVRDT - DWTDR - WTAVG / RAVG, VORTR = DWTDX - DVXDT, VORTT = DVXDR - DVRDX;
+                    R VORT = om::sqrt(VORTX * VORTX + VORTR * VORTR + VORTT * VORTT);
+                    if (j == F1(JSTART, NRW)) VORT = R(0.0);
+                    if (VORT > VORT_MAX) VORT = VORT_MAX;
+                    if (F1(INDMIX, j) == 1) VORT = A3(ABS_VORT_w, i, j - 1, k);
+                    A3(ABS_VORT_w, i, j, k) = VORT;
+                    R WREL = R(0), VXAVG = R(0), VRAVG = R(0);
+                    if (FAC_VORT > R(0.001) || FAC_PGRAD > R(0.001)) {
+                        WTAVG = sum8(WT_v);
+                        VXAVG = sum8(VX_v);
+                        VRAVG = sum8(VR_v);
+                        WREL = om::sqrt(VXAVG * VXAVG + VRAVG * VRAVG + WTAVG * WTAVG);
+                    }
+                    if (FAC_VORT > R(0.001)) {
+                        R HELICITY = (VXAVG * VORTX + VRAVG * VORTR + WTAVG * VORTT) / (WREL * VORT);
+                        VORTICITY_FAC = R(1.0) + FAC_VORT * om::tanh(R(3.0) * HELICITY * HELICITY);
+                    }
+                    if (FAC_PGRAD > R(0.001)) {
+                        R a = F3(VX, IMID, j, k), b = F3(VR, IMID, j, k), c = F3(WT, IMID, j, k);
+                        R WLIM = R(0.1) * om::sqrt(a * a + b * b + c * c);
+                        if (WREL < WLIM) WREL = WLIM;
+                        WREL = R(0.125) * WREL;
+                        R PGRAD = F3(DPDS_CELL, i, j, k);
+                        if (PGRAD < R(0.0)) PGRAD = R(0.0);
+                        R PTERM = PGRAD * VISLAM / (ROAVG * ROAVG * WREL * WREL * WREL);
+                        PTERM = PTERM * REYNOLDS_w[NRW - 1];
+                        PGRAD_FAC = R(1.0) + FAC_PGRAD * om::tanh(PTERM * PTERM);
+                    }
+                    R TURBVIS_WALL = ROAVG * F3(XLENGTH, i, j, k) * VORT * FMIXUP;
+                    if (REYNO < R(0.0001)) VISLAM = (om::fabs(REYNO) / R(100000.0)) * om::pow(TSAVG / R(288.0), R(0.62));
+                    if (i == IMID && k == KMID && j == JTEDGE) {
+                        R vx = F3(VX, i, j, k), vr = F3(VR, i, j, k), wt = F3(WT, i, j, k);
+                        R WABS = om::sqrt(vx * vx + vr * vr + wt * wt);
+                        R ROVEXIT = F3(RO, i, j, k) * WABS;
+                        REYNOLDS_w[NRW - 1] = F1(CHORD, NRW) * ROVEXIT / VISLAM;
+                    }
+                    R VISTOT = VISLAM * (R(1) + F3(FST_RAT, i, j, k)) + TURBVIS_WALL;
+                    R VISLIM = TURBVIS_LIM * VISLAM;
+                    if (VISTOT > VISLIM) VISTOT = VISLIM;
+                    R VISKLAM = VISLAM / ROAVG;
+                    A3(DYN_VIS_ML_w, i, j, k) = VISTOT - VISLAM;
+                    if (IF_RESTART == 0 && NSTEP == 1) F3(TRANS_DYN_VIS, i, j, k) = sa_transvis_in(VISLAM);
+                    if (NSTEP == 1) F3(TRANS_KVIS, i, j, k) = F3(TRANS_DYN_VIS, i, j, k) / ROAVG;
+                    R TRANSKVIS = F3(TRANS_KVIS, i, j, k);
+                    R XI = TRANSKVIS / VISKLAM;
+                    if (XI < R(1.1)) XI = R(1.1);
+                    if (XI > TURBVIS_LIM) XI = TURBVIS_LIM;
+                    R XI3 = XI * XI * XI;
+                    R FV1 = XI3 / (XI3 + R(357.9));
+                    R TRANSVISLIM = VISLIM / ROAVG / FV1;
+                    if (TRANSKVIS > TRANSVISLIM) TRANSKVIS = TRANSVISLIM;
+                    R VISTRU = TRANSKVIS * FV1 * ROAVG;
+                    A3(TRANS_VORT_w, i, j, k) = A3(ABS_VORT_w, i, j, k);
+                    VISTOT = VISTRU + VISLAM;
+                    VISLIM = TURBVIS_LIM * VISLAM;
+                    if (VISTOT > VISLIM) VISTOT = VISLIM;
+                    F3(VISC_RAT, i, j, k) = VISTOT / VISLAM;
+                    F3(VISC_LAM, i, j, k) = VISLAM;
+                    F3(VISC_TURB, i, j, k) = VISTOT - VISLAM;
+                }
+            }
+        /* ---- DO 1500: gradient of the kinematic transported viscosity ---- */
+        for (int k = 1; k <= KMM1; ++k)
+            for (int j = 2; j <= JMM1; ++j) {
+                int NRW = F1(NROW, j);
+                for (int i = 1; i <= IMM1; ++i) {
+                    R DX_, DR_, DT_;
+                    gradcell(i, j, k, TRANS_KVIS_v, DX_, DR_, DT_);
+                    A3(GRAD_TVIS_w, i, j, k) = DX_ * DX_ + DR_ * DR_ + DT_ * DT_;
+                    R VISCEFF = F3(TRANS_KVIS, i, j, k) + F3(VISC_LAM, i, j, k);
+                    A3(TVISGRADX_w, i, j, k) = VISCEFF * DX_;
+                    A3(TVISGRADR_w, i, j, k) = VISCEFF * DR_;
+                    A3(TVISGRADT_w, i, j, k) = VISCEFF * DT_;
+                    if (j == F1(JSTART, NRW) || j == F1(JSTART, NRW) - 1) {
+                        A3(GRAD_TVIS_w, i, j, k) = R(0.0);
+                        A3(TVISGRADX_w, i, j, k) = R(0.0);
+                        A3(TVISGRADR_w, i, j, k) = R(0.0);
+                        A3(TVISGRADT_w, i, j, k) = R(0.0);
+                    }
+                }
+            }
+        /* ---- DO 1600: the source terms ---- */
+        const R CW2 = R(0.3), SIGMA = R(0.6667), CB2 = R(0.622), CB1 = R(0.1355);
+        const R CW1 = R(0.80607) + R(2.433);
+        const R FST0 = FAC_ST0 * CB1, FST1 = FAC_ST1 / SIGMA, FST2 = FAC_ST2 * CB2 / SIGMA, FST3 = FAC_ST3 * CW1;
+        const R FSTMIX = FAC_STMIX / R(NDAMP);
+        const R RF_VIS1 = R(1.0) - RF_VIS;
+        R FYPLUS = R(0);
+        for (int k = 1; k <= KMM1; ++k)
+            for (int j = 2; j <= JM; ++j)
+                for (int i = 1; i <= IMM1; ++i) {
+                    FYPLUS = fyplus_of(F3(Y_PLUS, i, j, k), YPLAM, YPTURB, FYPLUS);
+                    R TVISDDX, TVISDDR, TVISDDT, d1, d2;
+                    gradcell(i, j, k, TVISGRADX_w, TVISDDX, d1, d2);
+                    gradcell(i, j, k, TVISGRADR_w, d1, TVISDDR, d2);
+                    gradcell(i, j, k, TVISGRADT_w, d1, d2, TVISDDT);
+                    R ROAVG = F3(ROAVG_CELL, i, j, k);
+                    R TVIS = F3(TRANS_KVIS, i, j, k);
+                    R ST0 = FST0 * A3(TRANS_VORT_w, i, j, k) * TVIS;
+                    if (FAC_VORT > R(0.001)) ST0 = ST0 * VORTICITY_FAC;
+                    if (FAC_PGRAD > R(0.001)) ST0 = ST0 * PGRAD_FAC;
+                    ST0 = ST0 * FYPLUS;
+                    R ST1 = FST1 * (TVISDDX + TVISDDR + TVISDDT);
+                    R ST2 = FST2 * A3(GRAD_TVIS_w, i, j, k);
+                    R TAU = R(5.9488) * TVIS / A3(TRANS_VORT_w, i, j, k) / F3(DWALLSQ, i, j, k);
+                    if (TAU > R(1.2)) TAU = R(1.2);
+                    if (TAU < R(0.001)) TAU = R(0.001);
+                    R G = TAU + CW2 * (TAU * TAU * TAU * TAU * TAU * TAU - TAU);
+                    R G6CW6 = G * G * G * G * G * G / R(64.0);
+                    R FW = G * om::pow((R(1) + R(0.015625)) / (R(1) + G6CW6), R(0.166667));
+                    R ST3 = FST3 * FW * TVIS * TVIS / F3(DWALLSQ, i, j, k);
+                    R ST_MIXL = FSTMIX * (A3(DYN_VIS_ML_w, i, j, k) - F3(VISC_TURB, i, j, k)) / F3(STEP, i, j, k);
+                    F3(T_SOURCE, i, j, k) = RF_VIS1 * F3(T_SOURCE, i, j, k) +
+                                            RF_VIS * (ROAVG * (ST0 + ST1 + ST2 - ST3) * F3(VOL, i, j, k) + ST_MIXL);
+                    if (j > 2 && F1(INDMIX, j - 1) == 1) F3(T_SOURCE, i, j, k) = R(0.0);
+                    if (j > 2 && F1(INDMIX, j - 2) == 1) F3(T_SOURCE, i, j, k) = R(0.0);
+                }
+        /* ---- DO 160: laminar regions pull the source towards a profile ---- */
+        const int IEND1 = IMID / 2, IENDM = IMM1 - IEND1, KEND1 = KMID / 2, KENDM = KMM1 - KEND1;
+        auto damp_to = [&](int i, int j, int k, R TVSPEC) {
+            F3(T_SOURCE, i, j, k) = F3(T_SOURCE, i, j, k) - (F3(VISC_TURB, i, j, k) - TVSPEC) / F3(STEP, i, j, k) / R(NDAMP);
+        };
+        for (int j = 2; j <= JM; ++j) {
+            int NRW = F1(NROW, j), J1 = F1(JSTART, NRW), JROW = j - J1 + 1;
+            int JTRHUB = F1(JTRAN_K1, NRW), JTRTIP = F1(JTRAN_KM, NRW), JTRLOW = F1(JTRAN_I1, NRW),
+                JTRUP = F1(JTRAN_IM, NRW), JLEROW = F1(JLE, NRW);
+            for (int i = 1; i <= IMM1; ++i) {
+                /* hub */
+                if (!(JTRHUB <= 1 && FTRANS < R(0.1))) {
+                    bool lam = JROW < JTRHUB;
+                    if (!lam) {
+                        R RMAX = R(0.0);
+                        for (int k = 1; k <= KEND1; ++k)
+                            if (!(F3(VISC_RAT, i, j, k) < RMAX)) RMAX = F3(VISC_RAT, i, j, k);
+                        lam = !(RMAX > FTRANS);
+                    }
+                    if (lam) {
+                        R TVEDGE = F3(VISC_TURB, i, j, KEND1);
+                        for (int k = 1; k <= KEND1; ++k) {
+                            R FK = R(KEND1 + 1 - k) / R(KEND1);
+                            FK = FK * FK * (R(3) - R(2) * FK);
+                            damp_to(i, j, k, FK * TVEDGE);
+                        }
+                    }
+                }
+                /* casing */
+                if (!(JTRTIP <= 1 && FTRANS < R(0.1))) {
+                    bool lam = JROW < JTRTIP;
+                    if (!lam) {
+                        R RMAX = R(0.0);
+                        for (int k = KENDM; k <= KMM1; ++k)
+                            if (!(F3(VISC_RAT, i, j, k) < RMAX)) RMAX = F3(VISC_RAT, i, j, k);
+                        lam = !(RMAX > FTRANS);
+                    }
+                    if (lam) {
+                        R TVEDGE = F3(VISC_TURB, i, j, KENDM);
+                        for (int k = KENDM; k <= KMM1; ++k) {
+                            R FK = R(k + 1 - KENDM) / R(KM - KENDM);
+                            FK = FK * FK * (R(3) - R(2) * FK);
+                            damp_to(i, j, k, FK * TVEDGE);
+                        }
+                    }
+                }
+            }
+            for (int k = 1; k <= KMM1; ++k) {
+                /* I = 1 surface */
+                if (!(JTRLOW <= 1 && FTRANS < R(0.1)) && !(j <= JLEROW)) {
+                    bool lam = JROW < JTRLOW || j < JLEROW;
+                    if (!lam) {
+                        R RMAX = R(0.0);
+                        for (int i = 1; i <= IEND1; ++i)
+                            if (!(F3(VISC_RAT, i, j, k) < RMAX)) RMAX = F3(VISC_RAT, i, j, k);
+                        lam = !(RMAX > FTRANS);
+                    }
+                    if (lam) {
+                        R TVEDGE = F3(VISC_TURB, IEND1, j, k);
+                        for (int i = 1; i <= IEND1; ++i) {
+                            R FI = R(IEND1 + 1 - i) / R(IEND1);
+                            FI = FI * FI * (R(3) - R(2) * FI);
+                            damp_to(i, j, k, FI * TVEDGE);
+                        }
+                    }
+                }
+                /* I = IM surface */
+                if (!(JTRUP <= 1 && FTRANS < R(0.1)) && !(j <= JLEROW)) {
+                    bool lam = JROW < JTRUP;
+                    if (!lam) {
+                        R RMAX = R(0.0);
+                        for (int i = IENDM; i <= IMM1; ++i)
+                            if (!(F3(VISC_RAT, i, j, k) < RMAX)) RMAX = F3(VISC_RAT, i, j, k);
+                        lam = !(RMAX > FTRANS);
+                    }
+                    if (lam) {
+                        R TVEDGE = F3(VISC_TURB, IENDM, j, k);
+                        for (int i = IENDM; i <= IMM1; ++i) {
+                            R FI = R(i + 1 - IENDM) / R(IM - IENDM);
+                            FI = FI * FI * (R(3) - R(2) * FI);
+                            damp_to(i, j, k, FI * TVEDGE);
+                        }
+                    }
+                }
+            }
+        }
+        /* ---- DO 190: stresses and heat flows with the final viscosity ---- */
+        for (int k = 1; k <= KMM1; ++k)
+            for (int j = 2; j <= JM; ++j)
+                for (int i = 1; i <= IMM1; ++i) {
+                    size_t n = ijk(i, j, k);
+                    VISLAM = F3(VISC_LAM, i, j, k);
+                    R VISTOT = F3(VISC_RAT, i, j, k) * VISLAM;
+                    R THCOND = CP * VISTOT / PRANDTL;
+                    R VISTOT2 = R(2.0) * VISTOT;
+                    TXR[n] = VISTOT * TXR[n];
+                    TXX[n] = VISTOT2 * TXX[n];
+                    TXT[n] = VISTOT * TXT[n];
+                    TRR[n] = VISTOT2 * TRR[n];
+                    TRT[n] = VISTOT * TRT[n];
+                    TTT[n] = VISTOT2 * TTT[n];
+                    QXX[n] = -THCOND * QXX[n];
+                    QRR[n] = -THCOND * QRR[n];
+                    QTT[n] = -THCOND * QTT[n];
+                }
+        viscous_walls_and_forces(TXR, TXX, TXT, TRR, TRT, TTT, QXX, QRR, QTT, true);
+    }
+
+    /* the transported viscosity's fluxes and source (LOOP 4279-4330), its
+       TSTEP (NCALL = 2) and the floor and kinematic value after it
+       (4340-4347) */
+    void sa_transport() {
+        for (int k = 1; k <= KMM1; ++k)
+            for (int j = 1; j <= JM; ++j) {
+                int JP1 = j + 1;
+                if (j == JM) JP1 = JM;
+                if (j == 1) JP1 = 1;
+                if (F1(INDMIX, j) == 1) JP1 = j;
+                for (int i = 1; i <= IMM1; ++i)
+                    A3(XFLUX, i, j, k) = A3(FLOWX, i, j, k) * (F3(TRANS_KVIS, i, j, k) + F3(TRANS_KVIS, i, JP1, k));
+            }
+        for (int k = 1; k <= KMM1; ++k)
+            for (int j = 2; j <= JM; ++j)
+                for (int i = 1; i <= IMM1; ++i) A3(SOURCE, i, j, k) = R(-2.0) * F3(T_SOURCE, i, j, k);
+        for (int k = 1; k <= KMM1; ++k)
+            for (int j = 2; j <= JM; ++j)
+                for (int i = 2; i <= IMM1; ++i)
+                    A3(TFLUX, i, j, k) = A3(FLOWT, i, j, k) * (F3(TRANS_KVIS, i - 1, j, k) + F3(TRANS_KVIS, i, j, k));
+        for (int k = 1; k <= KMM1; ++k)
+            for (int j = 2; j <= JM; ++j) {
+                A3(TFLUX, 1, j, k) = A3(FLOWT, 1, j, k) * (F3(TRANS_KVIS, IMM1, j, k) + F3(TRANS_KVIS, 1, j, k));
+                A3(TFLUX, IM, j, k) = A3(TFLUX, 1, j, k);
+            }
+        for (int k = 2; k <= KMM1; ++k)
+            for (int j = 2; j <= JM; ++j)
+                for (int i = 1; i <= IMM1; ++i)
+                    A3(RFLUX, i, j, k) = A3(FLOWR, i, j, k) * (F3(TRANS_KVIS, i, j, k - 1) + F3(TRANS_KVIS, i, j, k));
+        for (int j = 2; j <= JM; ++j)
+            for (int i = 1; i <= IMM1; ++i) {
+                A3(RFLUX, i, j, 1) = R(0.0);
+                A3(RFLUX, i, j, KM) = R(0.0);
+            }
+        tstep(TRANS_DYN_VIS_v, DEL_DYNVIS_v, 2);
+        R TRANSVISMIN = R(0.1) * F3(VISC_LAM, IMID, 2, KMID);
+        for (int k = 1; k <= KMM1; ++k)
+            for (int j = 2; j <= JM; ++j)
+                for (int i = 1; i <= IMM1; ++i) {
+                    if (F3(TRANS_DYN_VIS, i, j, k) < TRANSVISMIN) F3(TRANS_DYN_VIS, i, j, k) = TRANSVISMIN;
+                    F3(TRANS_KVIS, i, j, k) = F3(TRANS_DYN_VIS, i, j, k) / F3(ROAVG_CELL, i, j, k);
+                }
+    }
+
     int loss_init() override {
         if (!committed) return fail(MGPU_E_STATE, "loss_init before commit");
         R save_rf = RF_VIS, save_fm = FMIXUP;
@@ -1780,7 +2204,8 @@ struct Oracle : OracleBase {
         RF_VIS = R(1.0);
         FMIXUP = R(1.0);
         NSTEP = 1;
-        if (ILOS >= 100) new_loss();
+        if (ILOS >= 200) spal_loss();
+        else if (ILOS >= 100) new_loss();
         else loss();
         RF_VIS = save_rf;
         FMIXUP = save_fm;
@@ -1997,9 +2422,11 @@ struct Oracle : OracleBase {
                 }
         if (ILOS == 10 && NSTEP % NLOS == 0 && !FROZEN) loss();
         if (ILOS >= 100 && ILOS < 200 && NSTEP % NLOS == 0 && !FROZEN) new_loss();
+        if (ILOS >= 200 && NSTEP % NLOS == 0 && !FROZEN) spal_loss();
         mass_fluxes();
         tstep(RO_v, DRO_v);
         if (ILOS >= 100) roavg_cell();
+        if (ILOS >= 200) sa_transport();
         energy_fluxes();
         tstep(ROE_v, DROE_v);
         boundary_conditions();
@@ -2319,6 +2746,14 @@ struct Oracle : OracleBase {
                 F3(ROVX, i, 1, k) = F3(RO, i, 1, k) * F3(VX, i, 1, k);
                 F3(ROE, i, 1, k) = F3(P, i, 1, k) / GA1 + F3(RO, i, 1, k) * R(0.5) * VABSQ;
                 F3(HO, i, 1, k) = CP * F1(TO1, k);
+                if (ILOS >= 200) {
+                    /* the transported viscosity at inlet (4679-4689); RO(IMID,1,KMID)
+                       is the value this K, I loop has reached */
+                    F3(TRANS_DYN_VIS, i, 1, k) = sa_transvis_in(F3(VISC_LAM, i, 2, k));
+                    F3(TRANS_DYN_VIS, i, 2, k) = F3(TRANS_DYN_VIS, i, 1, k);
+                    F3(TRANS_KVIS, i, 1, k) = F3(TRANS_DYN_VIS, i, 1, k) / F3(RO, IMID, 1, KMID);
+                    F3(TRANS_KVIS, i, 2, k) = F3(TRANS_KVIS, i, 1, k);
+                }
                 /* exit */
                 R vr = F3(VR, i, JM, k), vt = F3(VT, i, JM, k), vx = F3(VX, i, JM, k);
                 R EKE = R(.5) * (vr * vr + vt * vt + vx * vx);

@@ -25,7 +25,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 from mgpu import case, common_setup  # noqa: E402
 import oracle as O  # noqa: E402
 
-MAXSTEPS = 30000
+MAXSTEPS = 20000
 SMOOTHING = 0.02
 
 

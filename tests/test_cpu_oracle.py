@@ -446,9 +446,8 @@ def test_new_loss_oracle_float_vs_double(mods):
 
 
 def test_new_loss_inputs_are_required(mods):
-    """ILOS 100-199 needs the SETUP-made mixing lengths and VORT_MAX, and
-    ILOS 200 (Spalart-Allmaras) is refused as not covered, as mgpu_commit
-    does."""
+    """ILOS 100-299 needs the SETUP-made mixing lengths and VORT_MAX, and
+    ILOS 300 and above is refused as not covered, as mgpu_commit does."""
     case, common_setup, O = mods[0], mods[1], mods[2]
     spec = case.small_nozzle()
     spec.ilos = 100
@@ -461,7 +460,7 @@ def test_new_loss_inputs_are_required(mods):
     bad.reals["VORT_MAX"] = 0.0
     with pytest.raises(O.OracleError, match="VORT_MAX"):
         O.Oracle(bad)
-    cd.ints["ILOS"] = 200
+    cd.ints["ILOS"] = 300
     with pytest.raises(O.OracleError, match="ILOS"):
         O.Oracle(cd)
 
@@ -525,3 +524,47 @@ def _bench_rank_main(rank, world):
         assert bench.run_reference(A, rank, world) == 0
     o.close()
     dist.destroy_process_group()
+
+
+def test_sa_oracle_float_vs_double(mods):
+    """The Spalart-Allmaras restatement (SPAL_LOSS, the transported viscosity
+    and TSTEP's NCALL = 2 branch): the FP32 instance stays within 1e-4 of the
+    FP64 one over 20 steps (SPAL_LOSS on steps 5, 10, 15, 20), and the
+    transported viscosity of every cell is positive."""
+    case, common_setup, O = mods
+    sp = case.small_stage()
+    sp.ilos = 200
+    cd = common_setup.build_common(sp)
+    outs = []
+    for dbl in (False, True):
+        o = O.Oracle(cd, double=dbl)
+        o.setup_calls()
+        for _ in range(20):
+            o.step()
+        outs.append({n: o.get(n) for n in ("RO", "ROVX", "ROE", "TRANS_DYN_VIS", "T_SOURCE", "XFORCE")})
+        tdv = o.get("TRANS_DYN_VIS")[:-1, 1:, :-1]          # the cells
+        assert tdv.min() > 0.0
+        o.close()
+    for n in outs[0]:
+        assert rel_linf(outs[0][n], outs[1][n]) <= 1e-4, n
+
+
+def test_sa_oracle_flow_out_round_trip(mods, tmp_path):
+    """With ILOS >= 200 the oracle's flow_out carries TRANS_DYN_VIS as its
+    seventh array and a restart reads it back (5966-5972, 6934)."""
+    case, common_setup, O = mods
+    sp = case.small_stage()
+    sp.ilos = 200
+    cd = common_setup.build_common(sp)
+    o = O.Oracle(cd)
+    o.setup_calls()
+    for _ in range(6):
+        o.step()
+    path = str(tmp_path / "flow_out")
+    o.write_flow_out(path)
+    tdv = o.get("TRANS_DYN_VIS", double=False)
+    cd.ints["IF_RESTART"] = 1
+    o2 = O.Oracle(cd, restart=path)
+    assert np.array_equal(o2.get("TRANS_DYN_VIS", double=False), tdv)
+    o.close()
+    o2.close()
