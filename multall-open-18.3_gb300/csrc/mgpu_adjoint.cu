@@ -2174,6 +2174,7 @@ int unsupported(const Dev &d) {
         return api_fail(MGPU_E_UNSUPPORTED, "adjoint: SETFLO, throttle, exit plate loss and IF_CUSP = 2 not differentiated");
     if (!(d.SFEXIT < 0.0001f) && d.NSFEXIT > 0) return api_fail(MGPU_E_UNSUPPORTED, "adjoint: exit smoothing not differentiated");
     if (d.KM > 512 || d.NROWS > 64) return api_fail(MGPU_E_UNSUPPORTED, "adjoint: KM <= 512 and NROWS <= 64");
+    if (d.ILOS >= 200) return api_fail(MGPU_E_UNSUPPORTED, "adjoint: the Spalart-Allmaras model is not differentiated");
     return 0;
 }
 

@@ -257,6 +257,7 @@ void enqueue_core(const Dev &d, Launch L, cudaEvent_t join = nullptr) {
     launch_flux_mass_energy(d, L0);
     launch_tstep(d, L, V_RO, 2);
     if (d.ILOS >= 100) launch_roavg_cell(d, L);     // 4255-4267, after TSTEP(RO)
+    if (d.ILOS >= 200) launch_sa_transport(d, L);   // 4279-4347, after the cell-average density
     if (join) {
         cudaStreamWaitEvent(L.s, join, 0);
         launch_bc_apply(d, L0);
@@ -264,6 +265,7 @@ void enqueue_core(const Dev &d, Launch L, cudaEvent_t join = nullptr) {
         launch_bc_sums(d, L);
         launch_bc_apply(d, L);
     }
+    if (d.ILOS >= 200) launch_sa_inlet(d, L);       // 4679-4689
     if (d.IN_FLOW != 0) launch_setflo(d, L);
     launch_flux_mom(d, L);          // also PEFF and the density limiter's column flags
     launch_tstep(d, L, V_ROVX, 3);
@@ -669,13 +671,17 @@ int32_t mgpu_commit(mgpu_handle *h) {
 #define MGPU_CHKR(n, v) if (d.n == MGPU_REQUIRED_REAL) return fail(MGPU_E_ARG, "real not set: " #n);
     MGPU_REAL_SCALARS(MGPU_CHKR)
     if (d.ITIMST != 3) return fail(MGPU_E_UNSUPPORTED, "ITIMST other than 3 (incompressible 5/6) not covered");
-    const bool new_loss = d.ILOS >= 100 && d.ILOS < 200;
+    // new_loss: NEW_LOSS (ILOS 100-199) or SPAL_LOSS (200-299), which share
+    // the per-cell strain-rate work, the mixing lengths and the wall terms
+    const bool new_loss = d.ILOS >= 100 && d.ILOS < 300;
+    const bool sa = d.ILOS >= 200 && d.ILOS < 300;
     if (d.ILOS != 10 && !new_loss)
-        return fail(MGPU_E_UNSUPPORTED, "only ILOS=10 (LOSS) and ILOS 100-199 (NEW_LOSS) are covered");
+        return fail(MGPU_E_UNSUPPORTED,
+                    "only ILOS=10 (LOSS), 100-199 (NEW_LOSS) and 200-299 (Spalart-Allmaras, SPAL_LOSS) are covered");
     if (new_loss) {
         for (const char *n : {"XLENGTH", "FST_RAT", "ROAVG_CELL"})
-            if (!h->bound[find_array(n)]) return fail(MGPU_E_ARG, std::string("ILOS 100-199 needs ") + n);
-        if (!(d.VORT_MAX > 0.0f)) return fail(MGPU_E_ARG, "ILOS 100-199 needs VORT_MAX > 0 (SETUP 7322-7328)");
+            if (!h->bound[find_array(n)]) return fail(MGPU_E_ARG, std::string("ILOS >= 100 needs ") + n);
+        if (!(d.VORT_MAX > 0.0f)) return fail(MGPU_E_ARG, "ILOS >= 100 needs VORT_MAX > 0 (SETUP 7322-7328)");
     }
     if (d.IFGAS != 0) return fail(MGPU_E_UNSUPPORTED, "real-gas IFGAS=1 not covered");
     if (d.IFCOOL || d.IFBLEED || d.IFSHROUD) return fail(MGPU_E_UNSUPPORTED, "cooling/bleed/shroud not covered");
@@ -714,6 +720,28 @@ int32_t mgpu_commit(mgpu_handle *h) {
         (rc = getf("XLLIM_KM", XL[3])) || (rc = getf("XLLIM_DWN", XL[4])) || (rc = getf("XLLIM_UP", XL[5])))
         return rc;
     if (new_loss && !d.NLS && (rc = dalloc(h, &d.NLS, new_loss_work_floats(d)))) return rc;
+    if (sa) {
+        // the reader's defaults FSTURB = 1, TURBVIS_DAMP = 0.5 (2052-2053)
+        if (!h->bound[find_array("FSTURB")] && (rc = upload(h, d.FSTURB, std::vector<float>(d.NROWS, 1.0f))))
+            return rc;
+        if (!h->bound[find_array("TURBVIS_DAMP")] &&
+            (rc = upload(h, d.TURBVIS_DAMP, std::vector<float>(d.NROWS, 0.5f))))
+            return rc;
+        if (!d.SAW && (rc = dalloc(h, &d.SAW, sa_work_floats(d)))) return rc;
+        // the sixth TSTEP variable: TRANS_DYN_VIS with its history DEL_DYNVIS
+        VarSet &V = d.var[V_SA];
+        const size_t N = (size_t)d.IM * d.JM * d.KM;
+        V.D = d.TRANS_DYN_VIS;
+        V.DIFF = d.DEL_DYNVIS;
+        if (!V.XF) {
+            float **fl[] = {&V.XF, &V.TF, &V.RF, &V.SR, &V.ST, &V.TM};
+            for (float **w : fl)
+                if ((rc = dalloc(h, w, N))) return rc;
+            if ((rc = dalloc(h, &V.psum, d.JM)) || (rc = dalloc(h, &V.pabs, d.JM)) ||
+                (rc = dalloc(h, &V.AVG_BLK, d.NROWS)))
+                return rc;
+        }
+    }
     d.any_cusp2 = 0;
     for (int nr = 0; nr < d.NROWS; ++nr) {
         if (IF_CUSP[nr] > 2) return fail(MGPU_E_UNSUPPORTED, "IF_CUSP above 2 not covered");
@@ -816,7 +844,7 @@ int32_t mgpu_commit(mgpu_handle *h) {
             JSBLK[j - 1] < 1 || JSBLK[j - 1] > d.NSBLK)
             return fail(MGPU_E_ARG, "multigrid J map out of range");
     }
-    for (int v = 0; v < NVAR; ++v) {
+    for (int v = 0; v < (sa ? NVAR + 1 : NVAR); ++v) {
         VarSet &V = d.var[v];
         if ((rc = dalloc(h, &V.B1CHG, shape_count(h, SH_MG1))) || (rc = dalloc(h, &V.B2CHG, shape_count(h, SH_MG2))) ||
             (rc = dalloc(h, &V.SBSUM, d.NSBLK)) || (rc = dalloc(h, &V.P1, (size_t)d.JM * d.NIB1 * d.NKB1)) ||

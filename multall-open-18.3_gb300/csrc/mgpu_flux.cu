@@ -53,7 +53,7 @@ __global__ void k_step_begin(Dev d) {
         c->FMIXUP = FM * FM;
     }
     c->do_tail = (n % 5 == 0) || ifend == 1;
-    c->do_loss = (d.ILOS == 10 || (d.ILOS >= 100 && d.ILOS < 200)) && (n % d.NLOS == 0) && !d.FROZEN;
+    c->do_loss = (d.ILOS == 10 || (d.ILOS >= 100 && d.ILOS < 300)) && (n % d.NLOS == 0) && !d.FROZEN;
     c->damp_on = !(c->DAMP < 2.0f || c->DAMP > 100.0f);
     if (d.use_cond) {
         cudaGraphSetConditional((cudaGraphConditionalHandle)d.cond_loss, c->do_loss ? 1u : 0u);
@@ -375,6 +375,10 @@ __global__ void k_bc_apply(Dev d) {
     float RO_STAG = PO1 / d.RGAS / TO1;
     float RO_IN = A3(d.RO, i, 1, k);
     if (d.ADJ_ROIN) d.ADJ_ROIN[t] = RO_IN;
+    // the Spalart-Allmaras inlet value divides by RO(IMID,1,KMID) as the
+    // reference's K, I loop finds it: the inlet points before (IMID, KMID)
+    // see this value from before the update (k_sa_inlet)
+    if (d.SAW && i == d.IMID && k == d.KMID) d.SAW[sa_work_node_floats(d) + 64 + 2] = RO_IN;
     if (RO_IN > 0.9999f * RO_STAG) RO_IN = 0.9999f * RO_STAG;
     float PNEW = PO1 * powf(RO_IN / RO_STAG, d.GA);
     float p1 = A3(d.P, i, 1, k);

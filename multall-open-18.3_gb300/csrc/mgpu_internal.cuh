@@ -75,6 +75,9 @@ struct VarSet {
 };
 constexpr int NVAR = 5;
 enum { V_RO = 0, V_ROE = 1, V_ROVX = 2, V_RORVT = 3, V_ROVR = 4 };
+// the Spalart-Allmaras transported viscosity (ILOS >= 200): a sixth TSTEP
+// variable, cell-centred, after the five conserved ones
+constexpr int V_SA = 5;
 
 struct Dev {
     // dimensions
@@ -99,7 +102,7 @@ struct Dev {
     // is the all-zero ZERO array.
     float *FLOWX, *FLOWT, *FLOWR, *ZERO;
     float *STORE, *TMP, *TEMP1;
-    VarSet var[NVAR];
+    VarSet var[NVAR + 1];
     float *PLIM;                       // (KM)
     float *FILAM, *FITURB, *FIWAKE, *FIUP, *FKLAM, *FKTURB;   // (NROWS, IM|KM)
     float *VLIMIT, *ROLIMIT;           // (NROWS)
@@ -107,6 +110,9 @@ struct Dev {
     float *BCBUF;                      // (4, KM) PAVG2, PAVG3, PAVGOUT, and the PD each K's exit update uses
     float *FLOWJ;                      // (JM) SETFLO's FLOW(J)
     float *NLS;                        // NEW_LOSS work: 9 strain-rate arrays, then the wall-face terms
+    // Spalart-Allmaras work (ILOS >= 200): ABS_VORT, DYN_VIS_ML, GRAD_TVIS,
+    // TVISGRADX/R/T (node arrays), then REYNOLDS(NROWS) and three scalars
+    float *SAW;
     // recording hooks of the adjoint's linearisation step (null otherwise):
     // RO(I,1,K) as the inlet condition reads it, the mixing-plane inputs of
     // each (row interface, K), and bit flags for a limiter that changed a value
@@ -239,6 +245,12 @@ void launch_step_begin(const Dev &d, Launch L);
 void launch_prim(const Dev &d, Launch L);
 void launch_loss(const Dev &d, Launch L, bool init_call);
 void launch_new_loss(const Dev &d, Launch L, bool init_call);
+// pieces NEW_LOSS and SPAL_LOSS share: the laminar viscosity for the first
+// quarter of the steps, SET_PWALLGRAD, and the wall shear stresses, face
+// stresses and force update (mgpu_loss.cu)
+void launch_loss_prologue(const Dev &d, Launch L, bool init_call);
+void launch_pwallgrad(const Dev &d, Launch L, bool init_call);
+void launch_viscous_walls_and_forces(const Dev &d, Launch L, bool init_call);
 void launch_roavg_cell(const Dev &d, Launch L);
 size_t new_loss_work_floats(const Dev &d);
 // mass fluxes FLOWX/FLOWT/FLOWR, ROWT, WT and the energy fluxes of ROE
@@ -256,6 +268,21 @@ void launch_flux_mom(const Dev &d, Launch L);
 void launch_tstep(const Dev &d, Launch L, int v0, int nv);
 void launch_limiters(const Dev &d, Launch L);
 void launch_mixplan(const Dev &d, Launch L);
+// node arrays at the start of the Spalart-Allmaras work buffer (SAW); then
+// REYNOLDS(1..64) and the scalars VORTICITY_FAC, PGRAD_FAC and the inlet
+// density RO(IMID,1,KMID) before the inlet condition
+__host__ __device__ inline size_t sa_work_node_floats(const Dev &d) { return (size_t)6 * d.IM * d.JM * d.KM; }
+// Spalart-Allmaras (mgpu_sa.cu): the transported viscosity's step after
+// TSTEP(RO) and the cell-average density, its inlet value after the inlet
+// condition, and SPAL_LOSS
+void launch_sa_transport(const Dev &d, Launch L);
+void launch_sa_inlet(const Dev &d, Launch L);
+void launch_spal_loss(const Dev &d, Launch L, bool init_call);
+size_t sa_work_floats(const Dev &d);
+// TSTEP's flux sum, SCREE, multigrid and residual smoothing of STORE for the
+// nv variables from v0 (the stages TSTEP shares with the transported
+// viscosity), mgpu_tstep.cu
+void launch_tstep_cells_prolong(const Dev &d, Launch L, int v0, int nv);
 void launch_tail(const Dev &d, Launch L);
 void launch_stepup(const Dev &d, Launch L, float relax, bool gated);
 void launch_integrals(const Dev &d, Launch L, double *out8);

@@ -6,7 +6,8 @@
 // The file is what gfortran writes for WRITE(7) on a sequential unformatted
 // unit: each record is its payload between two copies of its length in
 // bytes, as 4-byte little-endian integers.  Records: NSTEP (INTEGER), then
-// RO, ROVX, ROVR, ROVT, ROE, ROSUB, DPDS_CELL*1.0E-6 and PEFF+PREFF, each
+// RO, ROVX, ROVR, ROVT, ROE, ROSUB, DPDS_CELL*1.0E-6 (TRANS_DYN_VIS with the
+// Spalart-Allmaras model) and PEFF+PREFF, each
 // IM*JM*KM REAL*4 values in Fortran order (I fastest).
 //
 // Both directions run on the host.  Writing reads the arrays back from the
@@ -83,8 +84,12 @@ int32_t mgpu_write_flow_out(mgpu_handle *h, const char *path, const float *rosub
         return v[(size_t)(i - 1) + (size_t)g.IM * ((size_t)(j - 1) + (size_t)g.JM * (size_t)(k - 1))];
     };
     const float PREFF = 0.5f * (at(p, IMID, 1, KMID) + at(p, IMID, g.JM, KMID));
+    // the seventh array is the transported viscosity with the Spalart-
+    // Allmaras model, else DPDS_CELL * 1.0E-6 for plotting (5966-5972)
+    const bool sa = hv.d->ILOS >= 200;
+    if (sa && (rc = mgpu_get_array(h, "TRANS_DYN_VIS", dpds.data(), nb))) return rc;
     for (size_t n = 0; n < N; ++n) {
-        dpds[n] = dpds[n] * 1.0e-6f;
+        if (!sa) dpds[n] = dpds[n] * 1.0e-6f;
         peff[n] = peff[n] + PREFF;
     }
     FileCloser fc;
@@ -156,18 +161,18 @@ int32_t mgpu_read_flow_out(mgpu_handle *h, const char *path, int32_t *nstep) {
     const size_t N = g.N;
     const int64_t nb = (int64_t)(N * sizeof(float));
     const uint32_t rb = (uint32_t)nb;
-    std::vector<float> ro(N), rovx(N), rovr(N), rovt(N), roe(N);
+    std::vector<float> ro(N), rovx(N), rovr(N), rovt(N), roe(N), tdv(N);
     int32_t ns = 0;
     {
         FileCloser fc;
         fc.f = fopen(path, "rb");
         if (!fc.f) return api_fail(MGPU_E_ARG, (std::string("cannot open: ") + path).c_str());
-        // 6927-6934: NSTEP, the five variables, ROSUB and TRANS_DYN_VIS
-        // (neither is used by the covered schemes)
+        // 6927-6934: NSTEP, the five variables, ROSUB (unused by the
+        // covered schemes) and TRANS_DYN_VIS, read whatever the model
         const bool ok = get_record(fc.f, &ns, 4) && get_record(fc.f, ro.data(), rb) &&
                         get_record(fc.f, rovx.data(), rb) && get_record(fc.f, rovr.data(), rb) &&
                         get_record(fc.f, rovt.data(), rb) && get_record(fc.f, roe.data(), rb) &&
-                        get_record(fc.f, nullptr, rb) && get_record(fc.f, nullptr, rb);
+                        get_record(fc.f, nullptr, rb) && get_record(fc.f, tdv.data(), rb);
         if (!ok)
             return api_fail(MGPU_E_ARG, (std::string("not a flow_out file of this grid: ") + path).c_str());
     }
@@ -219,7 +224,8 @@ int32_t mgpu_read_flow_out(mgpu_handle *h, const char *path, int32_t *nstep) {
         const std::vector<float> *v;
     } up[] = {{"RO", &ro}, {"ROVX", &rovx}, {"ROVR", &rovr}, {"ROVT", &rovt}, {"ROE", &roe},
               {"RORVT", &rorvt}, {"VX", &vx}, {"VR", &vr}, {"VT", &vt}, {"T_STATIC", &ts},
-              {"HO", &ho}, {"P", &p}, {"PEFF", &p}};     // PEFF = P here (6977)
+              {"HO", &ho}, {"P", &p}, {"PEFF", &p},      // PEFF = P here (6977)
+              {"TRANS_DYN_VIS", &tdv}};
     for (auto &u : up)
         if ((rc = mgpu_set_array(h, u.name, u.v->data(), nb))) return rc;
     if ((rc = mgpu_set_array(h, "PD", PD.data(), (int64_t)PD.size() * 4))) return rc;

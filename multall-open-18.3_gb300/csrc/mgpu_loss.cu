@@ -671,6 +671,10 @@ cudaError_t configure_loss_kernels(const Dev &d) {
 }
 
 void launch_loss(const Dev &d, Launch L, bool init_call) {
+    if (d.ILOS >= 200) {
+        launch_spal_loss(d, L, init_call);
+        return;
+    }
     if (d.ILOS >= 100) {
         launch_new_loss(d, L, init_call);
         return;
@@ -1301,6 +1305,11 @@ __global__ void __launch_bounds__(256) k_nl_walls(const __grid_constant__ Dev d,
         const float TF = FMULT * WTAVG;
         const size_t o = (size_t)ix2(d, j, k);
         float *w = WB + (size_t)side * 6 * SB;
+        // SPAL_LOSS sets Y_PLUS on the I = IM side up to I = IM itself (14236)
+        if (d.ILOS >= 200 && side == 1) {
+            const int m = ix3(d, d.IM, j, k);
+            d.Y_PLUS[m] = fminf(1000.0f, sqrtf(TW / DEN) * sqrtf(d.DWALLSQ[m]) * DEN / VISLAM);
+        }
         w[o] = FMULT * VXAVG;
         w[SB + o] = FMULT * VRAVG;
         w[2 * SB + o] = TF;
@@ -1514,27 +1523,41 @@ __global__ void __launch_bounds__(256) k_nl_forces(const __grid_constant__ Dev d
     d.QSOURCE[n] = RF_VIS1 * qs0 - RF_VIS * es;
 }
 
-void launch_new_loss(const Dev &d, Launch L, bool init_call) {
-    const int ic = init_call ? 1 : 0;
-    launchk(L, k_loss_prologue, dim3(1), dim3(1), 0, d, ic);
+void launch_loss_prologue(const Dev &d, Launch L, bool init_call) {
+    launchk(L, k_loss_prologue, dim3(1), dim3(1), 0, d, init_call ? 1 : 0);
     mark(L, "k_loss_prologue");
+}
+
+void launch_pwallgrad(const Dev &d, Launch L, bool init_call) {
+    const int ic = init_call ? 1 : 0;
     const int nc = d.IMM1 * d.KMM1 * (d.JM - 1);
-    launchk(L, k_nl_cells, dim3((nc + 255) / 256), dim3(256), 0, d, ic);
-    mark(L, "k_nl_cells");
-    launchk(L, k_nl_transition, dim3(d.JM - 1), dim3(128), 0, d, ic);
-    mark(L, "k_nl_transition");
-    if (d.YPLUSWALL < -10.0f) {
-        launchk(L, k_pwallgrad_cells, dim3((nc + 255) / 256), dim3(256), 0, d, ic);
-        mark(L, "k_pwallgrad_cells");
-        launchk(L, k_pwallgrad_smooth, dim3((unsigned)((d.IMM1 + 31) / 32), (unsigned)d.KMM1), dim3(32),
-                pwallgrad_smem(d), d, ic);
-        mark(L, "k_pwallgrad_smooth");
-    }
+    launchk(L, k_pwallgrad_cells, dim3((nc + 255) / 256), dim3(256), 0, d, ic);
+    mark(L, "k_pwallgrad_cells");
+    launchk(L, k_pwallgrad_smooth, dim3((unsigned)((d.IMM1 + 31) / 32), (unsigned)d.KMM1), dim3(32),
+            pwallgrad_smem(d), d, ic);
+    mark(L, "k_pwallgrad_smooth");
+}
+
+void launch_viscous_walls_and_forces(const Dev &d, Launch L, bool init_call) {
+    const int ic = init_call ? 1 : 0;
+    const int nc = d.IMM1 * d.KMM1 * (d.JM - 1);
     const int nw = 2 * (d.JM - 1) * d.KMM1 + 2 * (d.JM - 1) * d.IMM1;
     launchk(L, k_nl_walls, dim3((nw + 255) / 256), dim3(256), 0, d, ic);
     mark(L, "k_nl_walls");
     launchk(L, k_nl_forces, dim3((nc + 255) / 256), dim3(256), 0, d, ic);
     mark(L, "k_nl_forces");
+}
+
+void launch_new_loss(const Dev &d, Launch L, bool init_call) {
+    const int ic = init_call ? 1 : 0;
+    launch_loss_prologue(d, L, init_call);
+    const int nc = d.IMM1 * d.KMM1 * (d.JM - 1);
+    launchk(L, k_nl_cells, dim3((nc + 255) / 256), dim3(256), 0, d, ic);
+    mark(L, "k_nl_cells");
+    launchk(L, k_nl_transition, dim3(d.JM - 1), dim3(128), 0, d, ic);
+    mark(L, "k_nl_transition");
+    if (d.YPLUSWALL < -10.0f) launch_pwallgrad(d, L, init_call);
+    launch_viscous_walls_and_forces(d, L, init_call);
 }
 
 }  // namespace mgpu

@@ -1201,12 +1201,16 @@ cudaError_t configure_kernels(const Dev &d) {
     return e != cudaSuccess ? e : configure_flux_kernels(d);
 }
 
+// TSTEP up to the negative feedback's row means: flux sum, SCREE and the
+// mixing-plane redistribution (cells), the multigrid block sums and the
+// time step (prolong), SMOOTH_RESID of STORE, and |STORE| per plane (or,
+// with REDUCE_ORDER=1, the row means in the reference's order)
 template <int BS>
-static void launch_tstep_bs(const Dev &d, Launch L, int v0, int nv) {
+static void launch_tstep_front(const Dev &d, Launch L, int v0, int nv) {
     size_t N = (size_t)d.IM * d.JM * d.KM;
     unsigned gN = grid_for(N, 256);
     const bool seq = d.REDUCE_ORDER == 1;
-    const unsigned jp = (unsigned)(d.JM - 1), ja = (unsigned)d.JM, vy = (unsigned)nv;
+    const unsigned jp = (unsigned)(d.JM - 1), vy = (unsigned)nv;
     launchk(L, k_ts_cells<BS>, dim3(jp, vy), dim3(BS), cells_smem(d), d, v0);
     mark(L, "k_ts_cells");
     if (seq) {
@@ -1236,6 +1240,12 @@ static void launch_tstep_bs(const Dev &d, Launch L, int v0, int nv) {
         launchk(L, k_ts_avgblk_seq, dim3(1, vy), dim3(32), 0, d, v0);
         mark(L, "k_ts_avgblk_seq");
     }
+}
+
+template <int BS>
+static void launch_tstep_bs(const Dev &d, Launch L, int v0, int nv) {
+    launch_tstep_front<BS>(d, L, v0, nv);
+    const unsigned ja = (unsigned)d.JM, vy = (unsigned)nv;
     if (d.TS_PAIR) {
         launchk(L, k_ts_update_pair<2 * BS>, dim3((ja + 1) / 2, vy), dim3(2 * BS), update_pair_smem(d), d, v0);
         mark(L, "k_ts_update_pair");
@@ -1245,6 +1255,14 @@ static void launch_tstep_bs(const Dev &d, Launch L, int v0, int nv) {
     }
     launchk(L, k_ts_smooth<BS>, dim3(ja, vy), dim3(BS), smooth_smem(d), d, v0);
     mark(L, "k_ts_smooth");
+}
+
+void launch_tstep_cells_prolong(const Dev &d, Launch L, int v0, int nv) {
+    const int bs = d.ts_bs[0];
+    if (bs == 128) launch_tstep_front<128>(d, L, v0, nv);
+    else if (bs == 192) launch_tstep_front<192>(d, L, v0, nv);
+    else if (bs == 512) launch_tstep_front<512>(d, L, v0, nv);
+    else launch_tstep_front<256>(d, L, v0, nv);
 }
 
 void launch_tstep(const Dev &d, Launch L, int v0, int nv) {
