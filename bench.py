@@ -605,16 +605,23 @@ def run_adjoint(args, rank, world, local_rank):
 
 CONVERGE_SMOOTHING = 0.02      # SFXIN = SFTIN: with the default 0.005 the stage does not settle
 CONVERGE_MAXSTEPS = 40000
+CONVERGE_CHUNK = 500
 
 
 def run_converge(args, rank, world, local_rank):
-    """Time to convergence on the stage: each path from SETUP's initial guess
-    to the reference's end test (multall-open-18.3.f:3762-3764) through
-    mgpu_run, with mass flow and efficiency at the stop compared with the
-    FP64 oracle's converged values (tests/golden/stage_converged_fp64.json,
-    made by tests/golden/make_converged_fp64.py).  The paths: the default
-    precision split (FP64 long sums) and the plain FP32 path (REDUCE_ORDER=2,
-    the same trees with FP32 adds)."""
+    """Time to convergence on the stage, each path from SETUP's initial guess
+    through mgpu_run in chunks of CONVERGE_CHUNK steps.  After each chunk the
+    monitors of the last tail and the integrals are read, and two times are
+    recorded: when the EAVG clause of the reference's end test holds (EAVG <
+    CONLIM, multall-open-18.3.f:3763), and when mass flow and total-to-total
+    efficiency first sit within 1e-4 (relative, absolute) of the FP64
+    oracle's converged values (tests/golden/stage_converged_fp64.json, made
+    by tests/golden/make_converged_fp64.py).  The time to convergence is the
+    later of the two.  The full end test also asks ECONT < 1 %; on this
+    synthetic stage the continuity error settles at 1.2 % one plane ahead
+    of the stator trailing edge, in the oracle as on the GPU, so it never
+    holds and is reported, not waited for.  Paths: the default precision
+    split (FP64 long sums) and the plain FP32 path (REDUCE_ORDER=2)."""
     if world > 1:
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local_rank)
         if rank != 0:
@@ -633,51 +640,70 @@ def run_converge(args, rank, world, local_rank):
     w.run(max(args.warmup, 3))
     w.close()
     res = {}
-    state_names = ["RO", "ROVX", "ROVR", "RORVT", "ROE"]
+    conlim = None
     with clock_sampler(0) as clk:
         for name, order in (("chosen", 0), ("plain_fp32", 2)):
             cd = common_setup.build_common(spec())
-            cd.ints["NSTEPS_MAX"] = CONVERGE_MAXSTEPS
+            conlim = cd.reals["CONLIM"]
+            cd.ints["NSTEPS_MAX"] = 10 ** 9
             cd.ints["REDUCE_ORDER"] = order
             p = lib.Problem(cd)
             tuned, _ = p.autotune()       # restores the state it times on
             p.run(0)                      # builds the step graph outside the timed region
             p.sync()
+            t_eavg = t_close = None
+            s_eavg = s_close = None
+            hist = []
             t0 = time.perf_counter()
-            rc, m = p.run(CONVERGE_MAXSTEPS)
-            out = {n: p.get(n) for n in state_names}
-            t = time.perf_counter() - t0
-            it = p.integrals()
-            r = {"seconds": t, "steps": int(m.nstep), "stopped_by_end_test": bool(rc == 1 and m.nstep < CONVERGE_MAXSTEPS),
-                 "eavg": float(m.eavg), "emax": float(m.emax), "econt": float(m.econt),
-                 "eta_tt": it.eta_tt, "mass_flow_in": it.mass_flow_in, "tstep_threads_per_cta": list(tuned),
-                 "state_bytes_downloaded": int(sum(a.nbytes for a in out.values()))}
+            steps = 0
+            while steps < CONVERGE_MAXSTEPS:
+                _, m = p.run(CONVERGE_CHUNK)
+                steps += CONVERGE_CHUNK
+                it = p.integrals()
+                t = time.perf_counter() - t0
+                e_eta = abs(it.eta_tt - fx["eta_tt"]) if fx else None
+                e_m = abs(it.mass_flow_in - fx["mass_flow_in"]) / abs(fx["mass_flow_in"]) if fx else None
+                hist.append([steps, round(t, 4), float(m.eavg), float(m.econt), it.eta_tt, it.mass_flow_in])
+                if t_eavg is None and m.eavg < conlim:
+                    t_eavg, s_eavg = t, steps
+                if fx and t_close is None and e_eta <= 1e-4 and e_m <= 1e-4:
+                    t_close, s_close = t, steps
+                if t_eavg is not None and (fx is None or t_close is not None):
+                    break
+            r = {"steps_to_eavg_below_conlim": s_eavg, "seconds_to_eavg_below_conlim": t_eavg,
+                 "steps_to_within_1e-4_of_fp64": s_close, "seconds_to_within_1e-4_of_fp64": t_close,
+                 "converged_seconds": None if (t_eavg is None or (fx and t_close is None)) else
+                 max(t_eavg, t_close or 0.0),
+                 "final": {"steps": steps, "eavg": float(m.eavg), "emax": float(m.emax), "econt": float(m.econt),
+                           "jcont": int(m.jcont), "eta_tt": it.eta_tt, "mass_flow_in": it.mass_flow_in},
+                 "tstep_threads_per_cta": list(tuned), "history": hist}
             if fx is not None:
-                r["eta_err_vs_fp64"] = abs(it.eta_tt - fx["eta_tt"])
-                r["mass_flow_rel_err_vs_fp64"] = abs(it.mass_flow_in - fx["mass_flow_in"]) / abs(fx["mass_flow_in"])
-                r["meets_1e-4"] = r["eta_err_vs_fp64"] <= 1e-4 and r["mass_flow_rel_err_vs_fp64"] <= 1e-4
+                r["final"]["eta_err_vs_fp64"] = abs(it.eta_tt - fx["eta_tt"])
+                r["final"]["mass_flow_rel_err_vs_fp64"] = abs(it.mass_flow_in - fx["mass_flow_in"]) / abs(
+                    fx["mass_flow_in"])
             res[name] = r
             p.close()
     c, pl = res["chosen"], res["plain_fp32"]
     nodes = 65 * 242 * 49
-    kps = 18
+    value = c["converged_seconds"]
+    steps = c["final"]["steps"]
     line = {
-        "metric": "time to convergence", "value": c["seconds"], "unit": "s", "n_gpus": world, "steps": c["steps"],
-        "warmup": max(args.warmup, 3), "ms_per_step": c["seconds"] / max(c["steps"], 1) * 1e3,
+        "metric": "time to convergence", "value": value, "unit": "s", "n_gpus": world, "steps": steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": c["history"][-1][1] / steps * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOADS["converge"][1], "nodes": nodes, "max_steps": CONVERGE_MAXSTEPS,
+        "config": {"workload": WORKLOADS["converge"][1], "nodes": nodes, "chunk_steps": CONVERGE_CHUNK,
+                   "conlim": conlim, "max_steps": CONVERGE_MAXSTEPS,
                    "l2": "inputs (216 MB working set) larger than L2, no flush inside a run",
-                   "fp64_oracle": None if fx is None else {k: fx[k] for k in ("nstep", "eta_tt", "mass_flow_in",
-                                                                               "eavg", "stopped_by_end_test")}},
+                   "fp64_oracle": None if fx is None else {k: fx.get(k) for k in ("nstep", "eta_tt", "mass_flow_in",
+                                                                                  "eavg", "econt")}},
         "chosen": c, "plain_fp32": pl,
-        "plain_over_chosen_time": pl["seconds"] / c["seconds"],
-        "gnode_iter_per_s": nodes * c["steps"] / c["seconds"] / 1e9,
+        "plain_over_chosen_time": (pl["converged_seconds"] / value) if (value and pl["converged_seconds"]) else None,
         "cpu_baseline": None, "clocks": clk.summary(),
-        "e2e": {"value": c["seconds"], "unit": "s", "h2d_bytes_per_step": 4,
-                "d2h_bytes_per_step": (c["state_bytes_downloaded"] + 200 * c["steps"] / 5) / max(c["steps"], 1),
-                "how": "mgpu_run through the C ABI (control block read back every fifth step), the flow state "
-                       "downloaded at the end"},
-        "gpu_launches": kps * c["steps"] + 10 * (c["steps"] // 5),
+        "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 4,
+                "d2h_bytes_per_step": (200 * steps / 5 + 64 * steps / CONVERGE_CHUNK) / max(steps, 1),
+                "how": "mgpu_run through the C ABI in chunks (control block read back every fifth step), "
+                       "mgpu_integrals_compute after each chunk"},
+        "gpu_launches": 17 * steps + 10 * (steps // 5),
     }
     print(json.dumps(line), flush=True)
     return 0
