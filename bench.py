@@ -41,6 +41,10 @@ WORKLOADS = {
     "compressor": ("compressor_4stage",
                    "4-stage axial compressor 73x752x57, 8 rows (36..64 blades) 12000 rpm, mixing planes "
                    "between all rows, 3-level multigrid, SCREE, mixing-length LOSS/5 steps"),
+    "deck_stage": ("deck:Single-stage-turbine-17.1",
+                   "the reference's own single-stage turbine test deck (Single-stage-turbine-17.1.dat) 46x282x46, "
+                   "nozzle 71 vanes + rotor 83 blades 3000 rpm, mixing plane, 3-level multigrid, SCREE, "
+                   "mixing-length LOSS/5 steps, read by mgpu.deck (tests/golden/decks)"),
     "nozzle": ("nozzle_row",
                "axial turbine nozzle row 37x97x33, 48 vanes, 3-level multigrid (level 2 off), SCREE, "
                "mixing-length LOSS/5 steps"),
@@ -101,17 +105,18 @@ def load_peaks():
 
 
 def ncu_traffic_per_launch():
-    """Per-kernel DRAM bytes per launch from the committed ncu summary of
-    this workload (profiles/ncu_stage_traffic.md), if present."""
+    """Per-kernel (DRAM bytes per launch, threads per CTA) from the committed
+    ncu summary of the stage workload (profiles/ncu_stage_traffic.md), if
+    present: one-kernel captures of an untuned run, not of this run."""
     p = os.path.join(ROOT, "profiles", "ncu_stage_traffic.md")
     out = {}
     if not os.path.exists(p):
         return out
     for line in open(p):
         cols = [c.strip() for c in line.strip().strip("|").split("|")]
-        if len(cols) >= 3 and cols[0].startswith("k_"):
+        if len(cols) >= 6 and cols[0].startswith("k_"):
             try:
-                out[cols[0]] = float(cols[2])
+                out[cols[0]] = (float(cols[2]), cols[5])
             except ValueError:
                 pass
     return out
@@ -291,7 +296,12 @@ def build_case():
     from mgpu import case, common_setup
     if ARGS_WORKLOAD == "batch64":          # one member stands for the batch on the CPU
         return common_setup.build_common(case.batch_instance(0))
-    spec = getattr(case, WORKLOADS[ARGS_WORKLOAD][0])()
+    src = WORKLOADS[ARGS_WORKLOAD][0]
+    if src.startswith("deck:"):             # a reference deck, as the reader left it
+        from mgpu import deck
+        spec, geo = deck.load_fixture(os.path.join(ROOT, "tests", "golden", "decks", src[5:] + ".npz"))
+        return common_setup.build_common(spec, geo)
+    spec = getattr(case, src)()
     return common_setup.build_common(spec)
 
 
@@ -744,7 +754,14 @@ def run_gpu(args, rank, world, local_rank):
     launches_step = dom_launches / PROFILE_STEPS
     achieved = alg_step / step_s / 1e9
     peak, peak_kind = load_peaks()
-    traffic = ncu_traffic_per_launch().get(dom_name)
+    # DRAM traffic of the dominant kernel: measured by ncu on the stage
+    # workload only, in its own capture (profiles/ncu_stage_traffic.md)
+    traffic = traffic_source = None
+    if ARGS_WORKLOAD == "stage" and dom_name in ncu_traffic_per_launch():
+        traffic, cta = ncu_traffic_per_launch()[dom_name]
+        traffic_source = (f"profile: profiles/ncu_stage_traffic.md, ncu dram__bytes_read.sum+dram__bytes_write.sum "
+                          f"of a one-kernel capture (-c 4, cold L2) of an untuned run at {cta} threads per CTA, "
+                          f"not of this run")
     total_prof = sum(p[2] for p in prof)
 
     # end to end through the C ABI, as a Fortran LOOP replacement drives it:
@@ -824,7 +841,8 @@ def run_gpu(args, rank, world, local_rank):
                                     "tstep_pass_ms": None if tune_ms is None else
                                     {p: dict(zip(("128", "192", "256", "512"), v)) for p, v in tune_ms.items()}}},
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_source,
+                         "peak_source": peak_kind,
                          "alg_bytes_per_launch": alg_step / launches_step,
                          "avg_launch_ms": step_s * 1e3 / launches_step,
                          "alg_bytes_per_node_unit": bpn, "units_per_step": units,

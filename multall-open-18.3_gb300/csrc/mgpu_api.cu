@@ -343,7 +343,8 @@ int capture_step(mgpu_handle *h) {
     CK(cudaStreamWaitEvent(h->aux, h->ev_fork, 0));
     launch_bc_sums(dg, Launch{h->aux, h->sm_count, nullptr});
     CK(cudaEventRecord(h->ev_join, h->aux));
-    int rc = add_conditional(h, hl, &h->loss_nodes, [&](Launch L2) { launch_loss(dg, L2, false); });
+    // an inviscid problem (ILOS = 0) has no LOSS node
+    int rc = dg.ILOS == 0 ? 0 : add_conditional(h, hl, &h->loss_nodes, [&](Launch L2) { launch_loss(dg, L2, false); });
     if (!rc) enqueue_core(dg, L, h->ev_join);
     if (!rc) rc = add_conditional(h, ht, &h->tail_nodes, [&](Launch L2) { enqueue_tail(dg, L2); });
     return rc;
@@ -675,9 +676,9 @@ int32_t mgpu_commit(mgpu_handle *h) {
     // the per-cell strain-rate work, the mixing lengths and the wall terms
     const bool new_loss = d.ILOS >= 100 && d.ILOS < 300;
     const bool sa = d.ILOS >= 200 && d.ILOS < 300;
-    if (d.ILOS != 10 && !new_loss)
-        return fail(MGPU_E_UNSUPPORTED,
-                    "only ILOS=10 (LOSS), 100-199 (NEW_LOSS) and 200-299 (Spalart-Allmaras, SPAL_LOSS) are covered");
+    if (d.ILOS != 0 && d.ILOS != 10 && !new_loss)
+        return fail(MGPU_E_UNSUPPORTED, "only ILOS=0 (inviscid), 10 (LOSS), 100-199 (NEW_LOSS) and 200-299 "
+                                        "(Spalart-Allmaras, SPAL_LOSS) are covered");
     if (new_loss) {
         for (const char *n : {"XLENGTH", "FST_RAT", "ROAVG_CELL"})
             if (!h->bound[find_array(n)]) return fail(MGPU_E_ARG, std::string("ILOS >= 100 needs ") + n);

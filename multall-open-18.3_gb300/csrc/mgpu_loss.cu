@@ -671,6 +671,7 @@ cudaError_t configure_loss_kernels(const Dev &d) {
 }
 
 void launch_loss(const Dev &d, Launch L, bool init_call) {
+    if (d.ILOS == 0) return;            // inviscid: no loss routine is called (3935-3942, 7354-7356)
     if (d.ILOS >= 200) {
         launch_spal_loss(d, L, init_call);
         return;

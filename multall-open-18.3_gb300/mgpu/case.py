@@ -71,6 +71,11 @@ class RowSpec:
     d_in: tuple = ()
     d_out: tuple = ()
     d_stag: tuple = ()
+    # JROTHS, JROTHE, JROTTS, JROTTE, row-relative (reader 940-960); None:
+    # the hub rotates with the row over its whole length, the casing not
+    jrot: Optional[tuple] = None
+    jtran: tuple = (0, 0, 0, 0)     # JTRAN_I1, JTRAN_IM, JTRAN_K1, JTRAN_KM
+    rough: tuple = (0.0, 0.0, 0.0, 0.0)   # ROUGH_H, ROUGH_T, ROUGH_L, ROUGH_U (m)
 
 
 @dataclasses.dataclass
@@ -142,6 +147,18 @@ class CaseSpec:
     throttle_pres: float = 0.0
     throttle_mas: float = 0.0
     rfthrotl: float = 0.0
+    # inlet data on the KM grid points as INPINT leaves it (PO1, TO1, VTIN,
+    # VM1, BS, BR); None: uniform po1 / to1, no swirl or pitch, and VM1 from
+    # the isentropic expansion to the first row's upstream pressure guess
+    inlet: Optional[dict] = None
+    ibound: int = 0
+    in_vtan: int = 0
+    in_press: int = 0
+    f_pdown: float = 0.0
+    sfexit: float = 0.0
+    nsfexit: int = 0
+    yplam: float = 5.0
+    ypturb: float = 25.0
 
 
 def geometric_spacing(n_intervals: int, ratio: float, fmax: float) -> np.ndarray:

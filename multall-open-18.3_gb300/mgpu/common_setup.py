@@ -100,8 +100,9 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None, metrics64: boo
         else:
             KS1[nr - 1], KS2[nr - 1] = 1, kt - 1
             KTIPE[nr - 1] = KM
-        # hub rotating over the whole row, casing stationary
-        JROTHS, JROTHE, JROTTS, JROTTE = 1, JMROW, JMROW, JMROW
+        # the rotating parts of the hub and casing (reader 940-960); by
+        # default the hub rotates over the whole row, the casing not
+        JROTHS, JROTHE, JROTTS, JROTTE = row.jrot if row.jrot is not None else (1, JMROW, JMROW, JMROW)
         JMIDRW = int(0.5 * (JLEROW + JTEROW))
         JROW = 0
         for J in range(J1, J2 + 1):
@@ -137,16 +138,21 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None, metrics64: boo
     NSTAGES = spec.rows[-1].stage
 
     # ---------------- inlet boundary data on the KM grid points ----------
-    PO1 = np.full(KM, f32(spec.po1), f32)
-    TO1 = np.full(KM, f32(spec.to1), f32)
-    VTIN = np.zeros(KM, f32)
-    BS = np.zeros(KM, f32)
-    BR = np.zeros(KM, f32)
-    # VM1: the inlet meridional speed of the initial guess, isentropic from
-    # P0 to the first row's upstream pressure guess
-    pr = spec.rows[0].pup / spec.po1
-    vm1 = math.sqrt(max(2.0 * spec.cp * spec.to1 * (1.0 - pr ** ((spec.ga - 1) / spec.ga)), 1.0))
-    VM1 = np.full(KM, f32(vm1), f32)
+    if spec.inlet is not None:
+        # a deck's inlet cards as INPINT interpolated them (9073-9199)
+        PO1, TO1, VTIN, VM1, BS, BR = (np.asarray(spec.inlet[n], f32).copy()
+                                       for n in ("PO1", "TO1", "VTIN", "VM1", "BS", "BR"))
+    else:
+        PO1 = np.full(KM, f32(spec.po1), f32)
+        TO1 = np.full(KM, f32(spec.to1), f32)
+        VTIN = np.zeros(KM, f32)
+        BS = np.zeros(KM, f32)
+        BR = np.zeros(KM, f32)
+        # VM1: the inlet meridional speed of the initial guess, isentropic from
+        # P0 to the first row's upstream pressure guess
+        pr = spec.rows[0].pup / spec.po1
+        vm1 = math.sqrt(max(2.0 * spec.cp * spec.to1 * (1.0 - pr ** ((spec.ga - 1) / spec.ga)), 1.0))
+        VM1 = np.full(KM, f32(vm1), f32)
 
     # ---------------- SETUP (multall-open-18.3.f:6280-7487) ---------------
     BSSIN = np.sin(BS * DEGRAD).astype(f32)
@@ -561,19 +567,22 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None, metrics64: boo
         new_loss_vort = float(f32(5000.0) * VM1[KMID - 1] / AVGSPAN)
 
     # ---------------- publish --------------------------------------------
-    ints = dict(ITIMST=3, ILOS=spec.ilos, NLOS=spec.nlos, IBOUND=0, IFMIX=spec.ifmix, IPOUT=spec.ipout,
-                IN_PRESS=0, IN_VTAN=0, IN_VR=spec.in_vr, IN_FLOW=spec.in_flow, IF_REPEAT=0, NRSMTH=0, NSFEXIT=0,
+    # the wall shear stress of the YPLUSWALL model (reader 2083-2088)
+    cfwall = float(f32(1.0) / (f32(spec.ypluswall) * f32(spec.ypluswall))) if spec.ypluswall > 5.0 else 0.0
+    ints = dict(ITIMST=3, ILOS=spec.ilos, NLOS=spec.nlos, IBOUND=spec.ibound, IFMIX=spec.ifmix, IPOUT=spec.ipout,
+                IN_PRESS=spec.in_press, IN_VTAN=spec.in_vtan, IN_VR=spec.in_vr, IN_FLOW=spec.in_flow, IF_REPEAT=0,
+                NRSMTH=0, NSFEXIT=spec.nsfexit,
                 NSTEPS_MAX=spec.nsteps_max, NCHANGE=spec.nchange, NMIXUP=spec.nmixup, IF_RESTART=0,
                 IR=IR, JR=JR, KR=KR, NIB1=NIB1, NJB1=NJB1, NKB1=NKB1, NIB2=NIB2, NJB2=NJB2,
                 NKB2=NKB2, NSBLK=NSBLK, NSTAGES=NSTAGES, IFGAS=0, IFCOOL=0, IFBLEED=0, IFSHROUD=0)
     if spec.itimst == -3:
         ints["NRSMTH"] = 1
     reals = dict(CP=spec.cp, GA=spec.ga, CFL=spec.cfl, DAMPIN=spec.dampin, MACHLIM=spec.machlim,
-                 F_PDOWN=0.0, SFXIN=spec.sfxin, SFTIN=spec.sftin, FAC_4TH=spec.fac_4th, RFIN=spec.rfin,
+                 F_PDOWN=spec.f_pdown, SFXIN=spec.sfxin, SFTIN=spec.sftin, FAC_4TH=spec.fac_4th, RFIN=spec.rfin,
                  FEXTRAP=spec.fextrap, RFMIX=spec.rfmix, FSMTHB=spec.fsmthb, FANGLE=spec.fangle,
-                 SFEXIT=0.0, RSMTH=0.4, F1=2.0, F2=-1.0, F3=0.0, REYNO=spec.reyno, RF_VIS=spec.rf_vis,
-                 FTRANS=spec.ftrans, PRANDTL=spec.prandtl, YPLUSWALL=spec.ypluswall, YPLAM=5.0,
-                 YPTURB=25.0, CFWALL=0.0, FACMIXUP=spec.facmixup, PDOWN_HUB=spec.pdown_hub,
+                 SFEXIT=spec.sfexit, RSMTH=0.4, F1=2.0, F2=-1.0, F3=0.0, REYNO=spec.reyno, RF_VIS=spec.rf_vis,
+                 FTRANS=spec.ftrans, PRANDTL=spec.prandtl, YPLUSWALL=spec.ypluswall, YPLAM=spec.yplam,
+                 YPTURB=spec.ypturb, CFWALL=cfwall, FACMIXUP=spec.facmixup, PDOWN_HUB=spec.pdown_hub,
                  PDOWN_TIP=spec.pdown_tip, PLATE_LOSS=spec.plate_loss, THROTTLE_EXIT=spec.throttle_exit,
                  THROTTLE_PRES=spec.throttle_pres, THROTTLE_MAS=spec.throttle_mas, RFTHROTL=spec.rfthrotl,
                  FLOWIN=spec.flowin, RFLOW=spec.rflow, VSOUND=float(VSOUND),
@@ -593,8 +602,10 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None, metrics64: boo
     xl = np.array([r.xllim for r in spec.rows], np.float32)
     arr = dict(
         JSTART=JSTART, JMIX=JMIX, JLE=JLE, JTE=JTE, JLED=JLED, KTIPS=KTIPS, KTIPE=KTIPE, KS1=KS1, KS2=KS2,
-        JTRAN_I1=np.zeros(NROWS, np.int32), JTRAN_IM=np.zeros(NROWS, np.int32),
-        JTRAN_K1=np.zeros(NROWS, np.int32), JTRAN_KM=np.zeros(NROWS, np.int32),
+        JTRAN_I1=np.array([r.jtran[0] for r in spec.rows], np.int32),
+        JTRAN_IM=np.array([r.jtran[1] for r in spec.rows], np.int32),
+        JTRAN_K1=np.array([r.jtran[2] for r in spec.rows], np.int32),
+        JTRAN_KM=np.array([r.jtran[3] for r in spec.rows], np.int32),
         IF_CUSP=np.array([r.if_cusp for r in spec.rows], np.int32),
         NUP_I1=np.array([r.nup_i1 for r in spec.rows], np.int32),
         NUP_IM=np.array([r.nup_im for r in spec.rows], np.int32),
@@ -604,8 +615,9 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None, metrics64: boo
         SEP_DRAG=np.array([r.sep_drag for r in spec.rows], f32),
         RT_THICK=RT_THICK, RTHETA=RTHETA,
         XLLIM_I1=xl[:, 0], XLLIM_IM=xl[:, 1], XLLIM_K1=xl[:, 2], XLLIM_KM=xl[:, 3], XLLIM_DWN=xl[:, 4],
-        XLLIM_UP=xl[:, 5], ROUGH_H=np.zeros(NROWS, f32), ROUGH_T=np.zeros(NROWS, f32),
-        ROUGH_L=np.zeros(NROWS, f32), ROUGH_U=np.zeros(NROWS, f32), CHORD=CHORD,
+        XLLIM_UP=xl[:, 5], ROUGH_H=np.array([r.rough[0] for r in spec.rows], f32),
+        ROUGH_T=np.array([r.rough[1] for r in spec.rows], f32), ROUGH_L=np.array([r.rough[2] for r in spec.rows], f32),
+        ROUGH_U=np.array([r.rough[3] for r in spec.rows], f32), CHORD=CHORD,
         NBLADE=NBLADE[1:], IND=IND[1:], INDLE=INDLE[1:], INDMIX=INDMIX[1:JM + 1], NROW=NROW[1:],
         JB1=JB1[1:], JB2=JB2[1:], JSBLK=JSBLK[1:], WRAD=WRAD[1:], WHUB=WHUB[1:], WTIP=WTIP[1:],
         FACUP=FACUP, FACDWN=FACDWN, FP=FP, FU=FU, FD=FD, IB1=IB1, IB2=IB2, FR=FR, FKU=FKU, FKD=FKD,

@@ -402,8 +402,9 @@ struct Oracle : OracleBase {
 #define O_CHK_R(nm, d) if ((float)nm == MGPU_REQUIRED_REAL) return fail(MGPU_E_ARG, "real not set: " #nm);
         MGPU_REAL_SCALARS(O_CHK_R)
         if (ITIMST != 3) return fail(MGPU_E_UNSUPPORTED, "ITIMST other than 3 (incompressible 5/6) not covered");
-        if (ILOS != 10 && !(ILOS >= 100 && ILOS < 300))
-            return fail(MGPU_E_UNSUPPORTED, "only ILOS=10 (LOSS), 100-199 (NEW_LOSS) and 200-299 (SPAL_LOSS) are covered");
+        if (ILOS != 0 && ILOS != 10 && !(ILOS >= 100 && ILOS < 300))
+            return fail(MGPU_E_UNSUPPORTED,
+                        "only ILOS=0 (inviscid), 10 (LOSS), 100-199 (NEW_LOSS) and 200-299 (SPAL_LOSS) are covered");
         if (ILOS >= 100 && !(VORT_MAX > R(0))) return fail(MGPU_E_ARG, "ILOS >= 100 needs VORT_MAX > 0 (SETUP 7322-7328)");
         if (ILOS >= 100 && !(XLENGTH_set && FST_RAT_set && ROAVG_CELL_set))
             return fail(MGPU_E_ARG, "ILOS >= 100 needs XLENGTH, FST_RAT and ROAVG_CELL");
@@ -2204,9 +2205,10 @@ struct Oracle : OracleBase {
         RF_VIS = R(1.0);
         FMIXUP = R(1.0);
         NSTEP = 1;
+        // SETUP 7354-7356: no loss routine for an inviscid problem (ILOS = 0)
         if (ILOS >= 200) spal_loss();
         else if (ILOS >= 100) new_loss();
-        else loss();
+        else if (ILOS == 10) loss();
         RF_VIS = save_rf;
         FMIXUP = save_fm;
         NSTEP = save_n;

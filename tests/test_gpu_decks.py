@@ -1,0 +1,96 @@
+"""GPU parity on the reference's own input decks (tests/golden/decks: the
+decks of Multall-open-18.3/multall-test-cases read by mgpu.deck), called
+through the C ABI and compared with the FP32 oracle on the same COMMON
+state.
+
+Bars: SETUP's calls into the path (STEPUP and the first loss call) and one
+step within 1e-5 L-infinity relative, with the long sums in the reference's
+sequential REAL*4 order (REDUCE_ORDER=1, the parity mode at full size);
+five steps (a LOSS step and the first convergence tail) within 1e-4; on the
+single-stage turbine also 200 steps within 1e-3, and the default precision
+split after 200 steps within 1e-3 as well.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from helpers import FORCES, STATE, rel_linf
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "decks", "*.npz")))
+NAMES = [os.path.basename(p)[:-4] for p in FIXTURES]
+SA_FIELDS = ["TRANS_DYN_VIS", "TRANS_KVIS"]
+
+
+@pytest.fixture(scope="module")
+def mods():
+    from mgpu import common_setup, deck, lib
+    import oracle as O
+    lib.load()
+    return common_setup, deck, lib, O
+
+
+def _pair(mods, name, **ints):
+    common_setup, deck, lib, O = mods
+    spec, geo = deck.load_fixture(os.path.join(HERE, "golden", "decks", name + ".npz"))
+    cd = common_setup.build_common(spec, geo)
+    cd.ints.update(ints)
+    gpu = lib.Problem(cd)
+    ref = O.Oracle(cd)
+    ref.setup_calls()
+    return spec, cd, gpu, ref
+
+
+def _fields(spec):
+    return STATE + (SA_FIELDS if 200 <= spec.ilos < 300 else [])
+
+
+def _compare(gpu, ref, names, tol, label):
+    worst = {n: rel_linf(gpu.get(n), ref.get(n, double=False)) for n in names}
+    bad = {k: v for k, v in worst.items() if not v <= tol}
+    assert not bad, f"{label}: fields above {tol}: {bad}"
+    return worst
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_deck_setup_calls_and_one_step(mods, name):
+    spec, cd, gpu, ref = _pair(mods, name, REDUCE_ORDER=1)
+    forces = FORCES if spec.ilos != 0 else []
+    _compare(gpu, ref, ["STEP"] + forces, 1e-5, f"{name} SETUP calls")
+    gpu.step()
+    ref.step()
+    _compare(gpu, ref, _fields(spec), 1e-5, f"{name} step 1")
+    gpu.close()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_deck_five_steps(mods, name):
+    spec, cd, gpu, ref = _pair(mods, name, REDUCE_ORDER=1)
+    for _ in range(5):
+        mg = gpu.step()
+        mr = ref.step()
+    _compare(gpu, ref, _fields(spec) + (FORCES if spec.ilos != 0 else []), 1e-4, f"{name} five steps")
+    assert abs(mg.eavg - mr.eavg) <= 1e-4 * abs(mr.eavg) + 1e-12
+    gpu.close()
+
+
+def test_single_stage_turbine_deck_200_steps(mods):
+    """The reference's single-stage turbine, 200 steps: within 1e-3 of the
+    oracle in the parity mode, and the default precision split likewise,
+    with the inlet and exit mass flows within 1e-3 of the oracle's."""
+    for order in (1, 0):
+        spec, cd, gpu, ref = _pair(mods, "Single-stage-turbine-17.1", REDUCE_ORDER=order)
+        gpu.run(200)
+        for _ in range(200):
+            ref.step()
+        _compare(gpu, ref, ["RO", "ROVX", "ROVR", "RORVT", "ROE", "XFORCE"], 1e-3,
+                 f"single-stage turbine deck, 200 steps, REDUCE_ORDER={order}")
+        ig, ir = gpu.integrals(), ref.integrals()
+        assert abs(ig.mass_flow_in - ir.mass_flow_in) <= 1e-3 * abs(ir.mass_flow_in)
+        assert abs(ig.mass_flow_out - ir.mass_flow_out) <= 1e-3 * abs(ir.mass_flow_out)
+        assert np.isfinite(ig.eta_tt)
+        gpu.close()
