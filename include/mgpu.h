@@ -206,6 +206,24 @@ int32_t mgpu_read_flow_out(mgpu_handle *h, const char *path, int32_t *nstep);
  * K (K fastest) X, R and RTHETA(1..IM), from the bound COMMON data. */
 int32_t mgpu_write_grid_out(mgpu_handle *h, const char *path);
 
+/* ---- SETUP's metrics on the device ------------------------------------ */
+/* Forms THETA = RTHETA/R, the theta extrapolated onto the upstream side of
+ * each mixing plane, and SETUP's face areas and volumes (multall-open-
+ * 18.3.f:6490-6502, 6570-6578, 6605-6711): AQX, AQR, ABT, WRABT, ABX, ABR,
+ * VOL, ASX, ASR and VOLOR, from the bound X, R, RTHETA, INDMIX and WRAD, in
+ * REAL*4 in SETUP's order of operations, and binds them.  Replaces SETUP's
+ * metric loops for a caller that binds the grid instead of the areas.
+ * Valid before mgpu_commit (the geometry is fixed after it). */
+int32_t mgpu_setup_metrics(mgpu_handle *h);
+/* The same metrics in double precision from double X, R (JM*KM each) and
+ * RTHETA (IM*JM*KM), with the handle's INDMIX and WRAD; the handle is not
+ * changed.  out receives AQX, AQR, ABX, ABR, VOL, ASX, ASR, VOLOR (IM*JM*KM
+ * each) then ABT, WRABT (JM*KM each); n_out is its length in doubles.  For
+ * geometry sensitivities, where REAL*4 metrics would bury a small change of
+ * the grid in rounding.  Valid once INDMIX and WRAD are bound. */
+int32_t mgpu_setup_metrics64(mgpu_handle *h, const double *x, const double *r, const double *rtheta, double *out,
+                             int64_t n_out);
+
 /* The same integrals as mgpu_integrals_compute, through a path that
  * allocates nothing.  This entry point has no counterpart in the reference
  * (whose efficiency summary is plain Fortran over COMMON arrays).

@@ -327,7 +327,9 @@ int capture_step(mgpu_handle *h) {
     cudaGraph_t cg = nullptr;
     CK(cudaStreamGetCaptureInfo(h->stream, &st, nullptr, &cg, nullptr, nullptr, nullptr));
     cudaGraphConditionalHandle hl = 0, ht = 0;
-    CK(cudaGraphConditionalHandleCreate(&hl, cg, 0, cudaGraphCondAssignDefault));
+    // every handle of a graph belongs to one conditional node: an inviscid
+    // problem (ILOS = 0), which has no LOSS node, creates no LOSS handle
+    if (h->d.ILOS != 0) CK(cudaGraphConditionalHandleCreate(&hl, cg, 0, cudaGraphCondAssignDefault));
     CK(cudaGraphConditionalHandleCreate(&ht, cg, 0, cudaGraphCondAssignDefault));
     Dev dg = h->d;
     dg.use_cond = 1;
@@ -657,6 +659,59 @@ int32_t mgpu_get_array(mgpu_handle *h, const char *name, void *host, int64_t nby
     if ((size_t)nbytes != want) return fail(MGPU_E_ARG, std::string("size mismatch for ") + name);
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaMemcpy(host, src, want, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int32_t mgpu_setup_metrics(mgpu_handle *h) {
+    if (!h) return fail(MGPU_E_ARG, "null handle");
+    if (h->committed) return fail(MGPU_E_STATE, "setup_metrics after commit: the geometry is fixed by then");
+    for (const char *n : {"X", "R", "RTHETA", "INDMIX", "WRAD"})
+        if (!h->bound[find_array(n)]) return fail(MGPU_E_STATE, std::string("setup_metrics needs ") + n);
+    const Dev &d = h->d;
+    const size_t N = (size_t)d.IM * d.JM * d.KM;
+    float *work = nullptr;
+    CK(cudaMalloc(&work, 3 * N * sizeof(float)));
+    auto P = [&](const char *n) { return (float *)h->dptr[find_array(n)]; };
+    MetricArgs<float> a{P("X"), P("R"), P("RTHETA"), (const int *)h->dptr[find_array("INDMIX")], P("WRAD"),
+                        work, work + N, work + 2 * N, P("AQX"), P("AQR"), P("ABX"), P("ABR"), P("VOL"), P("ASX"),
+                        P("ASR"), P("VOLOR"), P("ABT"), P("WRABT")};
+    cudaError_t e = launch_setup_metrics(d.IM, d.JM, d.KM, a, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(work);
+    if (e != cudaSuccess) return fail(MGPU_E_CUDA, std::string("setup_metrics: ") + cudaGetErrorString(e));
+    for (const char *n : {"AQX", "AQR", "ABX", "ABR", "VOL", "ASX", "ASR", "VOLOR", "ABT", "WRABT"})
+        h->bound[find_array(n)] = true;
+    return 0;
+}
+
+int32_t mgpu_setup_metrics64(mgpu_handle *h, const double *x, const double *r, const double *rtheta, double *out,
+                             int64_t n_out) {
+    if (!h || !x || !r || !rtheta || !out) return fail(MGPU_E_ARG, "null argument");
+    for (const char *n : {"INDMIX", "WRAD"})
+        if (!h->bound[find_array(n)]) return fail(MGPU_E_STATE, std::string("setup_metrics64 needs ") + n);
+    const Dev &d = h->d;
+    const size_t N = (size_t)d.IM * d.JM * d.KM, JK = (size_t)d.JM * d.KM;
+    if (n_out != (int64_t)(8 * N + 2 * JK))
+        return fail(MGPU_E_ARG, "setup_metrics64: out holds 8*IM*JM*KM + 2*JM*KM doubles");
+    double *buf = nullptr;
+    const size_t total = 2 * JK + N + 3 * N + 8 * N + 2 * JK;
+    CK(cudaMalloc(&buf, total * sizeof(double)));
+    double *dx = buf, *dr = dx + JK, *drt = dr + JK, *work = drt + N, *o = work + 3 * N;
+    cudaError_t e = cudaMemcpyAsync(dx, x, JK * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dr, r, JK * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(drt, rtheta, N * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(o, 0, (8 * N + 2 * JK) * sizeof(double), h->stream);
+    if (e == cudaSuccess) {
+        MetricArgs<double> a{dx, dr, drt, (const int *)h->dptr[find_array("INDMIX")],
+                             (const float *)h->dptr[find_array("WRAD")], work, work + N, work + 2 * N,
+                             o, o + N, o + 2 * N, o + 3 * N, o + 4 * N, o + 5 * N, o + 6 * N, o + 7 * N,
+                             o + 8 * N, o + 8 * N + JK};
+        e = launch_setup_metrics(d.IM, d.JM, d.KM, a, h->stream);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, o, (8 * N + 2 * JK) * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(buf);
+    if (e != cudaSuccess) return fail(MGPU_E_CUDA, std::string("setup_metrics64: ") + cudaGetErrorString(e));
     return 0;
 }
 

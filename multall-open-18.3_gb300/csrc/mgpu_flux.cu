@@ -56,7 +56,7 @@ __global__ void k_step_begin(Dev d) {
     c->do_loss = (d.ILOS == 10 || (d.ILOS >= 100 && d.ILOS < 300)) && (n % d.NLOS == 0) && !d.FROZEN;
     c->damp_on = !(c->DAMP < 2.0f || c->DAMP > 100.0f);
     if (d.use_cond) {
-        cudaGraphSetConditional((cudaGraphConditionalHandle)d.cond_loss, c->do_loss ? 1u : 0u);
+        if (d.ILOS != 0) cudaGraphSetConditional((cudaGraphConditionalHandle)d.cond_loss, c->do_loss ? 1u : 0u);
         cudaGraphSetConditional((cudaGraphConditionalHandle)d.cond_tail, c->do_tail ? 1u : 0u);
     }
     if (c->do_tail) {

@@ -314,6 +314,21 @@ void enqueue_step_core(const Dev &d, Launch L);
 // five conserved variables at (IMID, JP1), then per I those at JP2 and JP3
 __host__ __device__ inline int mix_rec_size(int im) { return 5 + 10 * im; }
 
+// SETUP's face areas and volumes (mgpu_metrics.cu), in float or double:
+// from X, R (J,K), RTHETA (I,J,K), INDMIX and WRAD (J) to the face areas,
+// volumes, ABT and WRABT; THETA, TEMP1 and TEMP2 are work arrays of IJK size.
+template <typename T>
+struct MetricArgs {
+    const T *X, *R, *RTHETA;
+    const int *INDMIX;
+    const float *WRAD;
+    T *THETA, *TEMP1, *TEMP2;
+    T *AQX, *AQR, *ABX, *ABR, *VOL, *ASX, *ASR, *VOLOR;
+    T *ABT, *WRABT;
+};
+template <typename T>
+cudaError_t launch_setup_metrics(int IM, int JM, int KM, const MetricArgs<T> &a, cudaStream_t s);
+
 // Read-only view of a handle, for entry points defined outside mgpu_api.cu.
 struct HandleView {
     const Dev *d;

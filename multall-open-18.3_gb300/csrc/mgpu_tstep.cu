@@ -66,18 +66,25 @@ __device__ inline int mp_role(const Dev &d, int j, int *nr) {
     return 0;
 }
 
-// Pitchwise sum of a mixing-plane line in I order: REAL*4 as the reference
-// forms it (REDUCE_ORDER 1, and the plain FP32 path, 2), or accumulated in
-// FP64 and rounded once (the default precision split: FP64 for the
-// mixing-plane circumferential sums).
-__device__ inline float mp_line_sum(const float *row, int n, bool exact32) {
-    if (exact32) {
-        float s = 0.0f;
-        for (int i = 0; i < n; ++i) s = s + row[i];
-        return s;
-    }
+// Pitchwise sum of a mixing-plane line in I order, REAL*4 as the reference
+// forms it (REDUCE_ORDER 1, and the plain FP32 path, 2).
+__device__ inline float mp_line_sum(const float *row, int n) {
+    float s = 0.0f;
+    for (int i = 0; i < n; ++i) s = s + row[i];
+    return s;
+}
+
+// The default precision split's form of the same sum: accumulated in FP64
+// and rounded once, by one warp (every lane calls it, with the same n).
+// Each lane adds every 32nd term, then a shuffle tree; every lane gets the
+// total.  A thread-serial FP64 chain over an I-line is long on this GPU,
+// whose FP64 adds are few per clock: the warp form shortens the chain from
+// n terms to n/32 + 5.
+template <class F>
+__device__ inline float warp_sum64(int n, F term) {
     double s = 0.0;
-    for (int i = 0; i < n; ++i) s += (double)row[i];
+    for (int i = (int)(threadIdx.x & 31); i < n; i += 32) s += (double)term(i);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     return (float)s;
 }
 
@@ -125,14 +132,20 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_cells(const __grid_constan
         // stage the XFLUX plane in shared memory (coalesced), then add each
         // I-line in the reference's order
         int jj = role == 1 ? j - 1 : j;
-        for (int c = threadIdx.x; c < nc; c += BS) {
-            int i = c % IMM1 + 1, k = c / IMM1 + 1;
-            st[c] = A3(V.XF, i, jj, k);
-        }
+        Walk2 wx(IMM1, threadIdx.x, BS);
+        for (int c = threadIdx.x; c < nc; c += BS, wx.next()) st[c] = A3(V.XF, wx.i, jj, wx.k);
         __syncthreads();
-        for (int k = threadIdx.x + 1; k <= KMM1; k += BS) {
-            const float *row = st + (size_t)(k - 1) * IMM1;
-            lsum[k - 1] = mp_line_sum(row, IMM1, d.REDUCE_ORDER != 0);
+        if (d.REDUCE_ORDER != 0) {
+            for (int k = threadIdx.x + 1; k <= KMM1; k += BS) {
+                const float *row = st + (size_t)(k - 1) * IMM1;
+                lsum[k - 1] = mp_line_sum(row, IMM1);
+            }
+        } else {
+            for (int k = (int)(threadIdx.x >> 5) + 1; k <= KMM1; k += BS / 32) {
+                const float *row = st + (size_t)(k - 1) * IMM1;
+                float s = warp_sum64(IMM1, [&](int i) { return row[i]; });
+                if ((threadIdx.x & 31) == 0) lsum[k - 1] = s;
+            }
         }
     }
     __syncthreads();
@@ -145,8 +158,9 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_cells(const __grid_constan
     const float *__restrict__ TF = V.TF;
     const float *__restrict__ SR = V.SR;
     // each thread first loads the operands of its TS_U cells, then computes:
-    // the loads of all cells are in flight together
-    const size_t ks = (size_t)IM * d.JM, pj = (size_t)IM * (j - 1);
+    // the loads of all cells are in flight together.  Offsets are 32-bit
+    // (a node array holds fewer than 2^31 points: commit limits IM, KM and JM)
+    const int ks = IM * d.JM, pj = IM * (j - 1);
     Walk2 w(IMM1, threadIdx.x, BS);
     for (int c0 = threadIdx.x; c0 < nc; c0 += TS_U * BS) {
         float xf[TS_U], xm[TS_U], rf[TS_U], rk[TS_U], ta[TS_U], tb1[TS_U], sr[TS_U], df[TS_U];
@@ -157,7 +171,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_cells(const __grid_constan
             ck[u] = w.k;
             w.next();
             if (c0 + u * BS < nc) {
-                const size_t n = pj + (size_t)(ci[u] - 1) + ks * (ck[u] - 1);
+                const int n = pj + (ci[u] - 1) + ks * (ck[u] - 1);
                 xf[u] = XF[n];
                 xm[u] = XF[n - IM];
                 rf[u] = RF[n];
@@ -173,7 +187,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_cells(const __grid_constan
             const int c = c0 + u * BS;
             if (c >= nc) break;
             const int i = ci[u], k = ck[u];
-            const size_t n = pj + (size_t)(i - 1) + ks * (k - 1);
+            const int n = pj + (i - 1) + ks * (k - 1);
             float t0 = ta[u], t1 = tb1[u];
             if (kts > 0 && k >= kts && k <= kte - 1) {
                 if (i == 1 || i + 1 == IM) {
@@ -196,13 +210,22 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_cells(const __grid_constan
     }
     __syncthreads();
     if (role == 1 || role == 3) {
-        for (int k = threadIdx.x + 1; k <= KMM1; k += BS) {
+        const bool lane_par = d.REDUCE_ORDER == 0;
+        const int k0 = lane_par ? (int)(threadIdx.x >> 5) + 1 : (int)threadIdx.x + 1;
+        const int kstep = lane_par ? BS / 32 : BS;
+        for (int k = k0; k <= KMM1; k += kstep) {
             float FLOWDIRN = -A3(d.FLOWX, d.IMID, jmx, k);
             bool on = role == 3 ? (FLOWDIRN > 0.0f || lowx) : (FLOWDIRN < 0.0f || lowx);
             if (!on) continue;
             float *row = st + (size_t)(k - 1) * IMM1;
-            float s = mp_line_sum(row, IMM1, d.REDUCE_ORDER != 0);
-            for (int i = 0; i < IMM1; ++i) row[i] = s * A1(d.FP, i + 1);
+            if (lane_par) {
+                float s = warp_sum64(IMM1, [&](int i) { return row[i]; });
+                __syncwarp();
+                for (int i = (int)(threadIdx.x & 31); i < IMM1; i += 32) row[i] = s * A1(d.FP, i + 1);
+            } else {
+                float s = mp_line_sum(row, IMM1);
+                for (int i = 0; i < IMM1; ++i) row[i] = s * A1(d.FP, i + 1);
+            }
         }
         __syncthreads();
     }
@@ -210,11 +233,14 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_cells(const __grid_constan
     // FP64 (FP64 arithmetic is slow on this GPU: one FP64 add per cell
     // kept its pipe a third busy)
     float psf = 0.0f;
-    for (int c = threadIdx.x; c < nc; c += BS) {
-        int i = c % IMM1 + 1, k = c / IMM1 + 1;
-        float v = st[c];
-        A3(V.ST, i, j, k) = v;
-        psf += v;
+    {
+        float *__restrict__ STj = V.ST + pj;
+        Walk2 wp(IMM1, threadIdx.x, BS);
+        for (int c = threadIdx.x; c < nc; c += BS, wp.next()) {
+            float v = st[c];
+            STj[(wp.i - 1) + ks * (wp.k - 1)] = v;
+            psf += v;
+        }
     }
     const double ps = block_sum<BS>(d.REDUCE_ORDER, (double)psf, shd);
     if (threadIdx.x == 0) V.psum[j - 1] = ps;
@@ -333,8 +359,8 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
     float *b1 = sm, *b2 = sm + n1;
     const int j1 = A1(d.JB1, j), j2 = A1(d.JB2, j), jsb = A1(d.JSBLK, j);
     const int nc = IMM1 * KMM1;
-    const size_t ks = (size_t)d.IM * d.JM, pj = (size_t)d.IM * (j - 1);
-    const size_t m1 = (size_t)d.NIB1 * (d.NJB1 + 1), m2 = (size_t)d.NIB2 * (d.NJB2 + 1);
+    const int ks = d.IM * d.JM, pj = d.IM * (j - 1);
+    const int m1 = d.NIB1 * (d.NJB1 + 1), m2 = d.NIB2 * (d.NJB2 + 1);
     // operands of this thread's first TS_U cells, loaded before the block
     // sums so their latency overlaps the assembly below
     float pst[TS_U], pstp[TS_U], prs[TS_U], ps1[TS_U], ps2[TS_U];
@@ -345,13 +371,13 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
         const int i = w.i, k = w.k;
         w.next();
         if (threadIdx.x + u * BS < nc) {
-            const size_t n = pj + (size_t)(i - 1) + ks * (k - 1);
+            const int n = pj + (i - 1) + ks * (k - 1);
             const int i1 = A1(d.IB1, i), i2 = A1(d.IB2, i), k1 = A1(d.KB1, k), k2 = A1(d.KB2, k);
             pst[u] = V.ST[n];
             pstp[u] = d.STEP[n];
             prs[u] = d.RSTEP[n];
-            ps1[u] = d.STEP1[(size_t)(i1 - 1) + (size_t)d.NIB1 * (j1 - 1) + m1 * (k1 - 1)];
-            ps2[u] = d.STEP2[(size_t)(i2 - 1) + (size_t)d.NIB2 * (j2 - 1) + m2 * (k2 - 1)];
+            ps1[u] = d.STEP1[(i1 - 1) + d.NIB1 * (j1 - 1) + m1 * (k1 - 1)];
+            ps2[u] = d.STEP2[(i2 - 1) + d.NIB2 * (j2 - 1) + m2 * (k2 - 1)];
             pb1[u] = (k1 - 1) * d.NIB1 + (i1 - 1);
             pb2[u] = (k2 - 1) * d.NIB2 + (i2 - 1);
         }
@@ -359,11 +385,11 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
     if (d.REDUCE_ORDER == 1) {
         for (int t = threadIdx.x; t < n1; t += BS) {
             int ib = t % d.NIB1 + 1, kb = t / d.NIB1 + 1;
-            b1[t] = V.B1CHG[(size_t)(ib - 1) + (size_t)d.NIB1 * (j1 - 1) + m1 * (kb - 1)];
+            b1[t] = V.B1CHG[(ib - 1) + d.NIB1 * (j1 - 1) + m1 * (kb - 1)];
         }
         for (int t = threadIdx.x; t < n2; t += BS) {
             int ib = t % d.NIB2 + 1, kb = t / d.NIB2 + 1;
-            b2[t] = V.B2CHG[(size_t)(ib - 1) + (size_t)d.NIB2 * (j2 - 1) + m2 * (kb - 1)];
+            b2[t] = V.B2CHG[(ib - 1) + d.NIB2 * (j2 - 1) + m2 * (kb - 1)];
         }
         if (threadIdx.x == 0) s_sb = A1(V.SBSUM, jsb);
     } else {
@@ -391,7 +417,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
         const int i = w.i, k = w.k;
         w.next();
         if (threadIdx.x + u * BS < nc) {
-            const size_t n = pj + (size_t)(i - 1) + ks * (k - 1);
+            const int n = pj + (i - 1) + ks * (k - 1);
             float DELTA = pst[u] * pstp[u] + (b1[pb1[u]] * ps1[u] + b2[pb2[u]] * ps2[u] + SBCHG * SSB) * prs[u];
             V.ST[n] = DELTA;
             sabs += fabsf(DELTA);
@@ -407,14 +433,14 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
             w.next();
             cn[u] = -1;
             if (c0 + u * BS < nc) {
-                const size_t n = pj + (size_t)(i - 1) + ks * (k - 1);
+                const int n = pj + (i - 1) + ks * (k - 1);
                 const int i1 = A1(d.IB1, i), i2 = A1(d.IB2, i), k1 = A1(d.KB1, k), k2 = A1(d.KB2, k);
-                cn[u] = (int)n;
+                cn[u] = n;
                 pst[u] = V.ST[n];
                 pstp[u] = d.STEP[n];
                 prs[u] = d.RSTEP[n];
-                ps1[u] = d.STEP1[(size_t)(i1 - 1) + (size_t)d.NIB1 * (j1 - 1) + m1 * (k1 - 1)];
-                ps2[u] = d.STEP2[(size_t)(i2 - 1) + (size_t)d.NIB2 * (j2 - 1) + m2 * (k2 - 1)];
+                ps1[u] = d.STEP1[(i1 - 1) + d.NIB1 * (j1 - 1) + m1 * (k1 - 1)];
+                ps2[u] = d.STEP2[(i2 - 1) + d.NIB2 * (j2 - 1) + m2 * (k2 - 1)];
                 pb1[u] = (k1 - 1) * d.NIB1 + (i1 - 1);
                 pb2[u] = (k2 - 1) * d.NIB2 + (i2 - 1);
             }
@@ -573,14 +599,22 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_update(const __grid_consta
         any = true;
         float *c = h ? cB : cA;
         int jmx = A1(d.JMIX, mnr);
-        for (int k = threadIdx.x + 1; k <= KMM1; k += BS) {
+        const bool lane_par = d.REDUCE_ORDER == 0;
+        const int k0 = lane_par ? (int)(threadIdx.x >> 5) + 1 : (int)threadIdx.x + 1;
+        const int kstep = lane_par ? BS / 32 : BS;
+        for (int k = k0; k <= KMM1; k += kstep) {
             float FLOWDIRN = -A3(d.FLOWX, d.IMID, jmx, k);
             bool on = role == 3 ? (FLOWDIRN > 0.0f || lowx) : (FLOWDIRN < 0.0f || lowx);
             if (!on) continue;
             float *row = c + (size_t)(k - 1) * IMM1;
-            float s = mp_line_sum(row, IMM1, d.REDUCE_ORDER != 0);
-            s = s / (float)IMM1;
-            for (int i = 0; i < IMM1; ++i) row[i] = s;
+            if (lane_par) {
+                float s = warp_sum64(IMM1, [&](int i) { return row[i]; }) / (float)IMM1;
+                __syncwarp();
+                for (int i = (int)(threadIdx.x & 31); i < IMM1; i += 32) row[i] = s;
+            } else {
+                float s = mp_line_sum(row, IMM1) / (float)IMM1;
+                for (int i = 0; i < IMM1; ++i) row[i] = s;
+            }
         }
     }
     if (any) __syncthreads();
@@ -754,14 +788,22 @@ __global__ void __launch_bounds__(PBS, 1024 / PBS) k_ts_update_pair(const __grid
         any = true;
         float *c = sm + h * nc;
         const int jmx = A1(d.JMIX, mnr);
-        for (int k = threadIdx.x + 1; k <= KMM1; k += PBS) {
+        const bool lane_par = d.REDUCE_ORDER == 0;
+        const int k0 = lane_par ? (int)(threadIdx.x >> 5) + 1 : (int)threadIdx.x + 1;
+        const int kstep = lane_par ? PBS / 32 : PBS;
+        for (int k = k0; k <= KMM1; k += kstep) {
             float FLOWDIRN = -A3(d.FLOWX, d.IMID, jmx, k);
             bool on = role == 3 ? (FLOWDIRN > 0.0f || lowx) : (FLOWDIRN < 0.0f || lowx);
             if (!on) continue;
             float *row = c + (k - 1) * IMM1;
-            float s = mp_line_sum(row, IMM1, d.REDUCE_ORDER != 0);
-            s = s / (float)IMM1;
-            for (int i = 0; i < IMM1; ++i) row[i] = s;
+            if (lane_par) {
+                float s = warp_sum64(IMM1, [&](int i) { return row[i]; }) / (float)IMM1;
+                __syncwarp();
+                for (int i = (int)(threadIdx.x & 31); i < IMM1; i += 32) row[i] = s;
+            } else {
+                float s = mp_line_sum(row, IMM1) / (float)IMM1;
+                for (int i = 0; i < IMM1; ++i) row[i] = s;
+            }
         }
     }
     if (any) __syncthreads();
@@ -917,8 +959,8 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_smooth(const __grid_consta
         cFKD[t] = d.FKD[t];
         cFKU[t] = d.FKU[t];
     }
-    const size_t ks = (size_t)IM * d.JM;                     // K stride of a node array
-    const float *__restrict__ Sj = S + (size_t)IM * (j - 1);  // plane j: (i, k) at i-1 + ks*(k-1)
+    const int ks = IM * d.JM;                        // K stride of a node array
+    const float *__restrict__ Sj = S + IM * (j - 1);  // plane j: (i, k) at i-1 + ks*(k-1)
     {
         const int sc = stream ? stream_case(d, j) : 0;
         const int lc = stream ? le_case(d, j) : 0;
@@ -945,7 +987,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_smooth(const __grid_consta
                 pk[u] = w.k;
                 w.next();
                 if (t0 + u * BS < np) {
-                    const float *p = Sj + (size_t)(pi[u] - 1) + ks * (pk[u] - 1);
+                    const float *p = Sj + (pi[u] - 1) + ks * (pk[u] - 1);
                     d0[u] = p[0];
 #pragma unroll
                     for (int q = 0; q < 4; ++q)
@@ -1093,26 +1135,26 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_smooth(const __grid_consta
         for (int r = 1; r <= d.NRWSM1; ++r)
             if (j == A1(d.JMIX, r) || j == A1(d.JMIX, r) + 1) mp = true;
     if (mp) {
-        for (int k = threadIdx.x + 1; k <= KM; k += BS) {
-            float s;
-            if (d.REDUCE_ORDER != 0) {
-                s = 0.0f;
+        if (d.REDUCE_ORDER != 0) {
+            for (int k = threadIdx.x + 1; k <= KM; k += BS) {
+                float s = 0.0f;
                 for (int i = 1; i <= IMM1; ++i) s = s + A1(d.FP, i) * (P(a, i, k) + P(a, i + 1, k));
-            } else {
-                double s64 = 0.0;
-                for (int i = 1; i <= IMM1; ++i) s64 += (double)(A1(d.FP, i) * (P(a, i, k) + P(a, i + 1, k)));
-                s = (float)s64;
+                b[k - 1] = 0.5f * s;
             }
-            b[k - 1] = 0.5f * s;
+        } else {
+            for (int k = (int)(threadIdx.x >> 5) + 1; k <= KM; k += BS / 32) {
+                float s = warp_sum64(IMM1, [&](int i) { return A1(d.FP, i + 1) * (P(a, i + 1, k) + P(a, i + 2, k)); });
+                if ((threadIdx.x & 31) == 0) b[k - 1] = 0.5f * s;
+            }
         }
         __syncthreads();
         for (int t = threadIdx.x; t < np; t += BS) a[t] = b[t / IM];
         __syncthreads();
     }
 #undef P
-    float *Dj = D + (size_t)IM * (j - 1);
+    float *Dj = D + IM * (j - 1);
     Walk2 w(IM, threadIdx.x, BS);
-    for (int t = threadIdx.x; t < np; t += BS, w.next()) Dj[(size_t)(w.i - 1) + ks * (w.k - 1)] = a[t];
+    for (int t = threadIdx.x; t < np; t += BS, w.next()) Dj[(w.i - 1) + ks * (w.k - 1)] = a[t];
 }
 
 // ---------------------------------------------------------------------

@@ -23,7 +23,7 @@ CSRC = os.path.join(ROOT, "csrc")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libmgpu.so")
 SOURCES = ["mgpu_api.cu", "mgpu_flux.cu", "mgpu_tstep.cu", "mgpu_loss.cu", "mgpu_noalloc.cu", "mgpu_adjoint.cu",
-           "mgpu_io.cu", "mgpu_sa.cu"]
+           "mgpu_io.cu", "mgpu_sa.cu", "mgpu_metrics.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
          "-Xptxas", "-O3"]

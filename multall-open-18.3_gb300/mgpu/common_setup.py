@@ -346,7 +346,8 @@ def build_common(spec: CaseSpec, geo: CaseGeometry | None = None, metrics64: boo
     if metrics64:
         # the face areas and volumes in double precision (geometry
         # sensitivities); the deck itself continues in REAL*4
-        cd.geom64 = dict(AQX=AQX.copy(), AQR=AQR.copy(), ABX=ABX.copy(), ABR=ABR.copy(), ABT=ABT.copy(),
+        cd.geom64 = dict(X=X.copy(), R=R.copy(), RTHETA=RTHETA.copy(), WRABT=WRABT.copy(),
+                         AQX=AQX.copy(), AQR=AQR.copy(), ABX=ABX.copy(), ABR=ABR.copy(), ABT=ABT.copy(),
                          ASX=ASX.copy(), ASR=ASR.copy(), VOLOR=VOLOR.copy(), VOL=VOL.copy())
         if metrics_only:
             return cd

@@ -57,7 +57,10 @@ EXPORTS = ["mgpu_abi_version", "mgpu_last_error", "mgpu_device_count", "mgpu_cre
            "mgpu_adjoint_iterate", "mgpu_adjoint_solve", "mgpu_adjoint_gradient", "mgpu_adjoint_get",
            "mgpu_adjoint_set", "mgpu_adjoint_solve_krylov", "mgpu_autotune", "mgpu_write_flow_out",
            "mgpu_read_flow_out", "mgpu_stage_performance", "mgpu_adjoint_gradient_theta",
-           "mgpu_write_grid_out"]
+           "mgpu_write_grid_out", "mgpu_setup_metrics", "mgpu_setup_metrics64"]
+
+# SETUP's metric arrays, which mgpu_setup_metrics forms on the device
+METRIC_ARRAYS = ("AQX", "AQR", "ABX", "ABR", "VOL", "ASX", "ASR", "VOLOR", "ABT", "WRABT")
 
 _lib = None
 
@@ -116,6 +119,8 @@ def load(build: bool = True):
                                             ctypes.POINTER(i32), dp]
     L.mgpu_adjoint_get.argtypes = [vp, cp, vp, ctypes.c_int64]
     L.mgpu_adjoint_set.argtypes = [vp, cp, vp, ctypes.c_int64]
+    L.mgpu_setup_metrics.argtypes = [vp]
+    L.mgpu_setup_metrics64.argtypes = [vp, vp, vp, vp, vp, ctypes.c_int64]
     for f in EXPORTS:
         fn = getattr(L, f)
         if f in ("mgpu_destroy", "mgpu_batch_destroy"):
@@ -154,9 +159,11 @@ def _chk(rc: int) -> int:
 class Problem:
     """One flow problem resident on the current GPU."""
 
-    def __init__(self, cd, setup_calls: bool = True, restart: str | None = None):
+    def __init__(self, cd, setup_calls: bool = True, restart: str | None = None, device_metrics: bool = False):
         """restart: a flow_out file read after the COMMON data are bound and
-        before the commit, as SETUP reads it with IF_RESTART = 1."""
+        before the commit, as SETUP reads it with IF_RESTART = 1.
+        device_metrics: the face areas and volumes are not bound from cd but
+        formed on the device from X, R and RTHETA (mgpu_setup_metrics)."""
         L = load()
         n = L.mgpu_device_count()
         if n <= 0:
@@ -170,8 +177,12 @@ class Problem:
         for k, v in cd.reals.items():
             _chk(L.mgpu_set_real(self.h, k.encode(), float(v)))
         for k, a in cd.arrays.items():
+            if device_metrics and k in METRIC_ARRAYS:
+                continue
             a = np.ascontiguousarray(a)
             _chk(L.mgpu_set_array(self.h, k.encode(), a.ctypes.data, a.nbytes))
+        if device_metrics:
+            _chk(L.mgpu_setup_metrics(self.h))
         self.restart_nstep = None
         if restart is not None:
             ns = ctypes.c_int32()
@@ -201,6 +212,21 @@ class Problem:
         """STEPUP(1.0) and the first LOSS, as SETUP makes them."""
         _chk(load().mgpu_stepup(self.h, 1.0))
         _chk(load().mgpu_loss_init(self.h))
+
+    def metrics64(self, x: np.ndarray, r: np.ndarray, rtheta: np.ndarray) -> dict:
+        """SETUP's metrics in double precision on the device from double X,
+        R (KM, JM) and RTHETA (KM, JM, IM), with this handle's INDMIX and
+        WRAD: {name: array} in the COMMON shapes."""
+        IM, JM, KM = self.cd.im, self.cd.jm, self.cd.km
+        x, r, rt = (np.ascontiguousarray(a, np.float64) for a in (x, r, rtheta))
+        N, JK = IM * JM * KM, JM * KM
+        out = np.zeros(8 * N + 2 * JK, np.float64)
+        _chk(load().mgpu_setup_metrics64(self.h, x.ctypes.data, r.ctypes.data, rt.ctypes.data, out.ctypes.data,
+                                         out.size))
+        res = {n: out[q * N:(q + 1) * N].reshape(KM, JM, IM) for q, n in enumerate(METRIC_ARRAYS[:8])}
+        res["ABT"] = out[8 * N:8 * N + JK].reshape(KM, JM)
+        res["WRABT"] = out[8 * N + JK:].reshape(KM, JM)
+        return res
 
     def close(self):
         if getattr(self, "h", None):

@@ -162,7 +162,7 @@ def test_abi_library_exports_every_declared_symbol():
     path = build.build()
     L = ctypes.CDLL(path)
     hdr = open(os.path.join(os.path.dirname(__file__), "..", "include", "mgpu.h")).read()
-    declared = set(re.findall(r"\b(mgpu_[a-z_]+)\s*\(", hdr))
+    declared = set(re.findall(r"\b(mgpu_[a-z0-9_]+)\s*\(", hdr))
     assert declared == set(lib.EXPORTS)
     for name in declared:
         assert hasattr(L, name), name

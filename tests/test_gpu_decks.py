@@ -22,7 +22,9 @@ pytestmark = pytest.mark.gpu
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "decks", "*.npz")))
-NAMES = [os.path.basename(p)[:-4] for p in FIXTURES]
+# decks the library refuses at mgpu_create, and why
+REFUSED = {"Staggered-wedge-exact-17.1": "KM = 3: the library takes KM >= 5"}
+NAMES = [os.path.basename(p)[:-4] for p in FIXTURES if os.path.basename(p)[:-4] not in REFUSED]
 SA_FIELDS = ["TRANS_DYN_VIS", "TRANS_KVIS"]
 
 
@@ -76,6 +78,17 @@ def test_deck_five_steps(mods, name):
     _compare(gpu, ref, _fields(spec) + (FORCES if spec.ilos != 0 else []), 1e-4, f"{name} five steps")
     assert abs(mg.eavg - mr.eavg) <= 1e-4 * abs(mr.eavg) + 1e-12
     gpu.close()
+
+
+@pytest.mark.parametrize("name", sorted(REFUSED))
+def test_deck_outside_the_library_is_refused(mods, name):
+    """A deck the library does not cover fails at mgpu_create with an
+    argument error, before any device work."""
+    common_setup, deck, lib, O = mods
+    spec, geo = deck.load_fixture(os.path.join(HERE, "golden", "decks", name + ".npz"))
+    cd = common_setup.build_common(spec, geo)
+    with pytest.raises(lib.MgpuError, match="dimensions out of range"):
+        lib.Problem(cd)
 
 
 def test_single_stage_turbine_deck_200_steps(mods):
