@@ -45,7 +45,7 @@ struct AdjVar {
     float *TM;                   // node values before SMOOTH_VAR
     float *Y;                    // ST * RSTEP: the restriction operand of the transposed prolongation
     float *P1, *P2;              // per-plane block partials of Y
-    double *psum;                // (JM) per-plane sums of Y
+    df *psum;                    // (JM) per-plane sums of Y (double-float)
     double *pblk;                // (JM) per-plane sums of dJ/d(row mean |STORE|)
     const float *tST;            // recorded STORE after prolongation
     const float *tBLK;           // (NROWS) recorded row means of |STORE| after the row mixing
@@ -1565,13 +1565,14 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_damp(const __grid_constant__ Dev 
             psf += y;
         }
     }
-    double ps = (double)psf;
-    for (int o = 16; o > 0; o >>= 1) ps += __shfl_down_sync(0xffffffffu, ps, o);
-    if ((threadIdx.x & 31) == 0) shd[threadIdx.x >> 5] = ps;
+    __shared__ df shdf[RT_BS / 32];
+    df ps = df_of(psf);
+    for (int o = 16; o > 0; o >>= 1) ps = df_add(ps, df_shfl_down(ps, o));
+    if ((threadIdx.x & 31) == 0) shdf[threadIdx.x >> 5] = ps;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int w = 0; w < RT_BS / 32; ++w) s += shd[w];
+        df s = df_of(0.0f);
+        for (int w = 0; w < RT_BS / 32; ++w) s = df_add(s, shdf[w]);
         V.psum[j - 1] = s;
     }
     // level-1 and level-2 partial sums of Y over this plane
@@ -1616,10 +1617,10 @@ __global__ void __launch_bounds__(RT_BS) rk_ts_cells(const __grid_constant__ Dev
     }
     if (threadIdx.x < 32) {
         const int a0 = A1(d.SB_START, jsb), b0 = A1(d.SB_END, jsb);
-        double s = 0.0;
-        for (int jj = a0 + (int)threadIdx.x; jj <= b0; jj += 32) s += V.psum[jj - 1];
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if (threadIdx.x == 0) s_sb = (float)s;
+        df s = df_of(0.0f);
+        for (int jj = a0 + (int)threadIdx.x; jj <= b0; jj += 32) s = df_add(s, V.psum[jj - 1]);
+        for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_down(s, o));
+        if (threadIdx.x == 0) s_sb = df_val(s);
     }
     __syncthreads();
     const float SB = s_sb, SSB = A1(d.STEPSBK, jsb);

@@ -57,6 +57,11 @@ struct DevCtl {
     float PDOWN_HUB, PDOWN_TIP, THROTTLE_PRES, CHECK_FLOW_JM;
 };
 
+// A double-float value hi + lo (its arithmetic is below, beside racc).
+struct df {
+    float hi, lo;
+};
+
 // One conserved variable's TSTEP operands and work arrays.  The five
 // variables (RO, ROE, ROVX, RORVT, ROVR) each have their own face fluxes and
 // cell-change arrays, so the TSTEP kernels can update several variables in
@@ -67,7 +72,7 @@ struct VarSet {
     float *XF, *TF, *RF, *SR;    // XFLUX, TFLUX, RFLUX, SOURCE of this variable
     float *ST;                   // STORE: cell changes
     float *TM;                   // TMP: node values before SMOOTH_VAR
-    double *psum, *pabs;         // (JM) per-J-plane sums of STORE and |STORE|
+    df *psum, *pabs;             // (JM) per-J-plane sums of STORE and |STORE| (double-float)
     float *P1, *P2;              // (JM, NIB1*NKB1) / (JM, NIB2*NKB2) per-plane block partials
     float *B1CHG, *B2CHG;        // MG1 / MG2 block sums, reference order
     float *SBSUM;                // (NSBLK) superblock sums, reference order
@@ -179,6 +184,43 @@ __device__ __forceinline__ double racc(int order, double s, double x) {
     return order == 2 ? (double)((float)s + (float)x) : s + x;
 }
 
+// A double-float: the unevaluated sum hi + lo of two FP32 values with |lo|
+// at most half an ulp of hi, a 48-bit significand.  The TSTEP kernels'
+// long sums of the default precision split accumulate in it rather than in
+// FP64: GB300 issues very few FP64 instructions per clock, and the FP64 tree
+// sums that every CTA forms in its prologue or epilogue queued behind one
+// another on each SM's FP64 pipe.  An addition is two of Knuth's TwoSum and
+// two of Dekker's Fast2Sum (the accurate double-double addition), all in
+// FP32; these error-free transformations need every sum rounded on its own,
+// which the library's --fmad=false build guarantees (they hold no products).
+__device__ __forceinline__ df df_of(float x) { return df{x, 0.0f}; }
+__device__ __forceinline__ float df_val(df a) { return a.hi + a.lo; }
+__device__ __forceinline__ df df_add(df a, df b) {
+    float s = a.hi + b.hi;
+    float bv = s - a.hi;
+    float e = (a.hi - (s - bv)) + (b.hi - bv);          // a.hi + b.hi = s + e exactly
+    float t = a.lo + b.lo;
+    float tv = t - a.lo;
+    float f = (a.lo - (t - tv)) + (b.lo - tv);          // a.lo + b.lo = t + f exactly
+    e = e + t;
+    float s2 = s + e;
+    e = e - (s2 - s);
+    e = e + f;
+    float s3 = s2 + e;
+    return df{s3, e - (s3 - s2)};
+}
+__device__ __forceinline__ df df_shfl_down(df v, int o) {
+    return df{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+}
+__device__ __forceinline__ df df_shfl_xor(df v, int o) {
+    return df{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
+// One addition of a long sum: double-float for REDUCE_ORDER 0, FP32 (every
+// partial sum rounded to REAL*4) for REDUCE_ORDER 2, the plain FP32 path.
+__device__ __forceinline__ df dacc(int order, df s, df x) {
+    return order == 2 ? df{s.hi + x.hi, 0.0f} : df_add(s, x);
+}
+
 // Order-preserving key for "largest value, earliest index wins": the value
 // must be >= 0 (squares, absolute values); NaN counts as smallest.
 __device__ inline unsigned long long max_key(float v, size_t lin) {
@@ -264,6 +306,8 @@ void launch_cusp(const Dev &d, Launch L);         // IF_CUSP = 2 rows
 // XMOM, RVT and RMOM fluxes; also PEFF (4321) and the density limiter's
 // column flags
 void launch_flux_mom(const Dev &d, Launch L);
+void launch_flux_mom_interior(const Dev &d, Launch L);
+void launch_flux_mom_rest(const Dev &d, Launch L);
 // TSTEP for the nv variables v0 .. v0+nv-1 of d.var
 void launch_tstep(const Dev &d, Launch L, int v0, int nv);
 void launch_limiters(const Dev &d, Launch L);

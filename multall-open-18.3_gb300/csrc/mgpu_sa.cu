@@ -471,10 +471,10 @@ __global__ void __launch_bounds__(SA_BS) k_sa_update(const __grid_constant__ Dev
             const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
             for (int nr = w + 1; nr <= d.NROWS; nr += SA_BS / 32) {
                 const int JST = A1(d.JSTART, nr) + 1, JEN = A1(d.JMIX, nr) - 1;
-                double s = 0.0;
-                for (int jj = JST + l; jj <= JEN; jj += 32) s = racc(ro, s, V.pabs[jj - 1]);
-                for (int o = 16; o > 0; o >>= 1) s = racc(ro, s, __shfl_down_sync(0xffffffffu, s, o));
-                if (l == 0) chg[nr - 1] = (float)s / (float)(IMM1 * KMM1 * (JEN - JST + 1));
+                df s = df_of(0.0f);
+                for (int jj = JST + l; jj <= JEN; jj += 32) s = dacc(ro, s, V.pabs[jj - 1]);
+                for (int o = 16; o > 0; o >>= 1) s = dacc(ro, s, df_shfl_down(s, o));
+                if (l == 0) chg[nr - 1] = df_val(s) / (float)(IMM1 * KMM1 * (JEN - JST + 1));
             }
             __syncthreads();
             if (threadIdx.x == 0) {

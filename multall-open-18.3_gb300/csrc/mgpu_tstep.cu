@@ -38,16 +38,17 @@ constexpr int TS_U = 3;          // cells per thread whose loads are issued toge
 constexpr int TS_UG = 4;         // the same for the damping and gather phases of update
 constexpr int SV_U = 3;          // points per thread whose streamwise loads are issued together
 
+// CTA sum of one double-float per thread (thread 0 receives it)
 template <int BS>
-__device__ inline double block_sum(int order, double v, double *sh) {
-    for (int o = 16; o > 0; o >>= 1) v = racc(order, v, __shfl_down_sync(0xffffffffu, v, o));
+__device__ inline df block_sum(int order, df v, df *sh) {
+    for (int o = 16; o > 0; o >>= 1) v = dacc(order, v, df_shfl_down(v, o));
     int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     if (l == 0) sh[w] = v;
     __syncthreads();
-    double r = 0.0;
+    df r = df_of(0.0f);
     if (w == 0) {
-        r = l < BS / 32 ? sh[l] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) r = racc(order, r, __shfl_down_sync(0xffffffffu, r, o));
+        r = l < BS / 32 ? sh[l] : df_of(0.0f);
+        for (int o = 16; o > 0; o >>= 1) r = dacc(order, r, df_shfl_down(r, o));
     }
     __syncthreads();
     return r;
@@ -74,18 +75,16 @@ __device__ inline float mp_line_sum(const float *row, int n) {
     return s;
 }
 
-// The default precision split's form of the same sum: accumulated in FP64
-// and rounded once, by one warp (every lane calls it, with the same n).
-// Each lane adds every 32nd term, then a shuffle tree; every lane gets the
-// total.  A thread-serial FP64 chain over an I-line is long on this GPU,
-// whose FP64 adds are few per clock: the warp form shortens the chain from
-// n terms to n/32 + 5.
+// The default precision split's form of the same sum: accumulated in
+// double-float and rounded once, by one warp (every lane calls it, with the
+// same n).  Each lane adds every 32nd term, then a shuffle tree; every lane
+// gets the total.
 template <class F>
 __device__ inline float warp_sum64(int n, F term) {
-    double s = 0.0;
-    for (int i = (int)(threadIdx.x & 31); i < n; i += 32) s += (double)term(i);
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    return (float)s;
+    df s = df_of(0.0f);
+    for (int i = (int)(threadIdx.x & 31); i < n; i += 32) s = df_add(s, df_of(term(i)));
+    for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_xor(s, o));
+    return df_val(s);
 }
 
 // (i, k) of the points t = start, start + stride, ... of an ni-wide plane,
@@ -118,7 +117,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_cells(const __grid_constan
     extern __shared__ float sm[];
     const VarSet &V = d.var[v0 + blockIdx.y];
     float *__restrict__ DIFF = V.DIFF;
-    __shared__ double shd[BS / 32];
+    __shared__ df shd[BS / 32];
     const int j = blockIdx.x + 2;
     const int IM = d.IM, IMM1 = d.IMM1, KMM1 = d.KMM1;
     const int nc = IMM1 * KMM1;
@@ -230,8 +229,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_cells(const __grid_constan
         __syncthreads();
     }
     // plane sum: a thread's dozen cells in FP32, the threads' partials in
-    // FP64 (FP64 arithmetic is slow on this GPU: one FP64 add per cell
-    // kept its pipe a third busy)
+    // double-float
     float psf = 0.0f;
     {
         float *__restrict__ STj = V.ST + pj;
@@ -242,7 +240,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_cells(const __grid_constan
             psf += v;
         }
     }
-    const double ps = block_sum<BS>(d.REDUCE_ORDER, (double)psf, shd);
+    const df ps = block_sum<BS>(d.REDUCE_ORDER, df_of(psf), shd);
     if (threadIdx.x == 0) V.psum[j - 1] = ps;
     // level-1 and level-2 partial sums of this plane
     const int n1 = d.NIB1 * d.NKB1, n2 = d.NIB2 * d.NKB2;
@@ -351,7 +349,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
     pdl_wait();
     extern __shared__ float sm[];
     const VarSet &V = d.var[v0 + blockIdx.y];
-    __shared__ double shd[BS / 32];
+    __shared__ df shd[BS / 32];
     __shared__ float s_sb;
     const int j = blockIdx.x + 2;
     const int IMM1 = d.IMM1, KMM1 = d.KMM1;
@@ -402,15 +400,15 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
         if (threadIdx.x < 32) {
             int a = A1(d.SB_START, jsb), b = A1(d.SB_END, jsb);
             const int ro = d.REDUCE_ORDER;
-            double s = 0.0;
-            for (int jj = a + (int)threadIdx.x; jj <= b; jj += 32) s = racc(ro, s, V.psum[jj - 1]);
-            for (int o = 16; o > 0; o >>= 1) s = racc(ro, s, __shfl_down_sync(0xffffffffu, s, o));
-            if (threadIdx.x == 0) s_sb = (float)s;
+            df s = df_of(0.0f);
+            for (int jj = a + (int)threadIdx.x; jj <= b; jj += 32) s = dacc(ro, s, V.psum[jj - 1]);
+            for (int o = 16; o > 0; o >>= 1) s = dacc(ro, s, df_shfl_down(s, o));
+            if (threadIdx.x == 0) s_sb = df_val(s);
         }
     }
     __syncthreads();
     const float SBCHG = s_sb, SSB = A1(d.STEPSBK, jsb);
-    float sabs = 0.0f;            // FP32 per thread, FP64 across threads (as in k_ts_cells)
+    float sabs = 0.0f;            // FP32 per thread, double-float across threads (as in k_ts_cells)
     w = Walk2(IMM1, threadIdx.x, BS);
 #pragma unroll
     for (int u = 0; u < TS_U; ++u) {
@@ -454,7 +452,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
         }
     }
     if (want_abs) {
-        const double t = block_sum<BS>(d.REDUCE_ORDER, (double)sabs, shd);
+        const df t = block_sum<BS>(d.REDUCE_ORDER, df_of(sabs), shd);
         if (threadIdx.x == 0) V.pabs[j - 1] = t;
     }
 }
@@ -463,7 +461,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
 template <int BS>
 __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_plane_abs(const __grid_constant__ Dev d, int v0) {
     pdl_wait();
-    __shared__ double shd[BS / 32];
+    __shared__ df shd[BS / 32];
     const VarSet &V = d.var[v0 + blockIdx.y];
     int j = blockIdx.x + 2;
     int nc = d.IMM1 * d.KMM1;
@@ -472,7 +470,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_plane_abs(const __grid_con
         int i = c % d.IMM1 + 1, k = c / d.IMM1 + 1;
         sf += fabsf(A3(V.ST, i, j, k));
     }
-    const double s = block_sum<BS>(d.REDUCE_ORDER, (double)sf, shd);
+    const df s = block_sum<BS>(d.REDUCE_ORDER, df_of(sf), shd);
     if (threadIdx.x == 0) V.pabs[j - 1] = s;
 }
 
@@ -534,10 +532,10 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_update(const __grid_consta
             for (int nr = w + 1; nr <= d.NROWS; nr += BS / 32) {
                 int JST = A1(d.JSTART, nr) + 1, JEN = A1(d.JMIX, nr) - 1;
                 const int ro = d.REDUCE_ORDER;
-                double s = 0.0;
-                for (int jj = JST + l; jj <= JEN; jj += 32) s = racc(ro, s, V.pabs[jj - 1]);
-                for (int o = 16; o > 0; o >>= 1) s = racc(ro, s, __shfl_down_sync(0xffffffffu, s, o));
-                if (l == 0) chg[nr - 1] = (float)s / (float)(IMM1 * KMM1 * (JEN - JST + 1));
+                df s = df_of(0.0f);
+                for (int jj = JST + l; jj <= JEN; jj += 32) s = dacc(ro, s, V.pabs[jj - 1]);
+                for (int o = 16; o > 0; o >>= 1) s = dacc(ro, s, df_shfl_down(s, o));
+                if (l == 0) chg[nr - 1] = df_val(s) / (float)(IMM1 * KMM1 * (JEN - JST + 1));
             }
             __syncthreads();
             if (threadIdx.x == 0) {
@@ -723,10 +721,10 @@ __global__ void __launch_bounds__(PBS, 1024 / PBS) k_ts_update_pair(const __grid
             int w = threadIdx.x >> 5, l = threadIdx.x & 31;
             for (int nr = w + 1; nr <= d.NROWS; nr += PBS / 32) {
                 int JST = A1(d.JSTART, nr) + 1, JEN = A1(d.JMIX, nr) - 1;
-                double s = 0.0;
-                for (int jj = JST + l; jj <= JEN; jj += 32) s = racc(ro, s, V.pabs[jj - 1]);
-                for (int o = 16; o > 0; o >>= 1) s = racc(ro, s, __shfl_down_sync(0xffffffffu, s, o));
-                if (l == 0) chg[nr - 1] = (float)s / (float)(IMM1 * KMM1 * (JEN - JST + 1));
+                df s = df_of(0.0f);
+                for (int jj = JST + l; jj <= JEN; jj += 32) s = dacc(ro, s, V.pabs[jj - 1]);
+                for (int o = 16; o > 0; o >>= 1) s = dacc(ro, s, df_shfl_down(s, o));
+                if (l == 0) chg[nr - 1] = df_val(s) / (float)(IMM1 * KMM1 * (JEN - JST + 1));
             }
             __syncthreads();
             if (threadIdx.x == 0) {

@@ -76,7 +76,9 @@ def test_deck_five_steps(mods, name):
         mg = gpu.step()
         mr = ref.step()
     _compare(gpu, ref, _fields(spec) + (FORCES if spec.ilos != 0 else []), 1e-4, f"{name} five steps")
-    assert abs(mg.eavg - mr.eavg) <= 1e-4 * abs(mr.eavg) + 1e-12
+    # EAVG sums |change| over every node: the library adds it in FP64 trees,
+    # the oracle in sequential REAL*4, whose rounding alone is ~sqrt(N) ulp
+    assert abs(mg.eavg - mr.eavg) <= 1e-3 * abs(mr.eavg) + 1e-12
     gpu.close()
 
 
