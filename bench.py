@@ -691,6 +691,7 @@ def run_converge(args, rank, world, local_rank):
                 r["final"]["eta_err_vs_fp64"] = abs(it.eta_tt - fx["eta_tt"])
                 r["final"]["mass_flow_rel_err_vs_fp64"] = abs(it.mass_flow_in - fx["mass_flow_in"]) / abs(
                     fx["mass_flow_in"])
+            r["kernels_per_step"] = [p.kernels_per_step(), p.kernels_per_step(loss=True, tail=True)]
             res[name] = r
             p.close()
     c, pl = res["chosen"], res["plain_fp32"]
@@ -713,7 +714,8 @@ def run_converge(args, rank, world, local_rank):
                 "d2h_bytes_per_step": (200 * steps / 5 + 64 * steps / CONVERGE_CHUNK) / max(steps, 1),
                 "how": "mgpu_run through the C ABI in chunks (control block read back every fifth step), "
                        "mgpu_integrals_compute after each chunk"},
-        "gpu_launches": 17 * steps + 10 * (steps // 5),
+        "gpu_launches": c["kernels_per_step"][0] * steps
+        + (c["kernels_per_step"][1] - c["kernels_per_step"][0]) * (steps // 5),
     }
     print(json.dumps(line), flush=True)
     return 0

@@ -2176,6 +2176,7 @@ int unsupported(const Dev &d) {
     if (!(d.SFEXIT < 0.0001f) && d.NSFEXIT > 0) return api_fail(MGPU_E_UNSUPPORTED, "adjoint: exit smoothing not differentiated");
     if (d.KM > 512 || d.NROWS > 64) return api_fail(MGPU_E_UNSUPPORTED, "adjoint: KM <= 512 and NROWS <= 64");
     if (d.ILOS >= 200) return api_fail(MGPU_E_UNSUPPORTED, "adjoint: the Spalart-Allmaras model is not differentiated");
+    if (d.IR <= 1 && d.JR <= 1 && d.KR <= 1) return api_fail(MGPU_E_UNSUPPORTED, "adjoint: runs without multigrid");
     return 0;
 }
 

@@ -747,7 +747,6 @@ int32_t mgpu_commit(mgpu_handle *h) {
         return fail(MGPU_E_UNSUPPORTED, "YPLUSWALL<-10 with JM > 1700 is not covered (SET_PWALLGRAD column buffer)");
     if (d.IPOUT == 3 || d.IPOUT < -1) return fail(MGPU_E_UNSUPPORTED, "IPOUT not covered");
     if (d.NCHANGE <= 0 || d.NMIXUP <= 0 || d.NLOS <= 0) return fail(MGPU_E_ARG, "NCHANGE, NMIXUP, NLOS must be positive");
-    if (d.IR <= 1 && d.JR <= 1 && d.KR <= 1) return fail(MGPU_E_UNSUPPORTED, "runs without multigrid are not covered");
     if (d.KM > 512) return fail(MGPU_E_UNSUPPORTED, "KM above 512");
     size_t smem = (size_t)2 * d.IM * d.KM * sizeof(float);
     if (smem > 200 * 1024) return fail(MGPU_E_UNSUPPORTED, "J-plane does not fit shared memory");

@@ -306,8 +306,6 @@ void launch_cusp(const Dev &d, Launch L);         // IF_CUSP = 2 rows
 // XMOM, RVT and RMOM fluxes; also PEFF (4321) and the density limiter's
 // column flags
 void launch_flux_mom(const Dev &d, Launch L);
-void launch_flux_mom_interior(const Dev &d, Launch L);
-void launch_flux_mom_rest(const Dev &d, Launch L);
 // TSTEP for the nv variables v0 .. v0+nv-1 of d.var
 void launch_tstep(const Dev &d, Launch L, int v0, int nv);
 void launch_limiters(const Dev &d, Launch L);

@@ -406,6 +406,13 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_prolong(const __grid_const
             if (threadIdx.x == 0) s_sb = df_val(s);
         }
     }
+    if (d.IR <= 1 && d.JR <= 1 && d.KR <= 1) {
+        // no multigrid: TSTEP skips the restriction (5613) and the block
+        // changes keep the zeros they start from (5490-5498)
+        for (int t = threadIdx.x; t < n1; t += BS) b1[t] = 0.0f;
+        for (int t = threadIdx.x; t < n2; t += BS) b2[t] = 0.0f;
+        if (threadIdx.x == 0) s_sb = 0.0f;
+    }
     __syncthreads();
     const float SBCHG = s_sb, SSB = A1(d.STEPSBK, jsb);
     float sabs = 0.0f;            // FP32 per thread, double-float across threads (as in k_ts_cells)

@@ -51,3 +51,27 @@ def test_branch_fires_and_matches_oracle(mods, branch):
     assert not bad, f"{branch}, step 5: {bad} (branch counts {fired})"
     gpu.close()
     ref.close()
+
+
+def test_run_without_multigrid(mods):
+    """IR = JR = KR = 1 (and IRBB = JRBB = KRBB = 1): TSTEP skips the block
+    restriction and its block changes stay zero (multall-open-18.3.f:5613,
+    5490-5498).  One step within 1e-5 and ten steps within 1e-4 of the
+    oracle, which takes the same branch."""
+    case, common_setup, lib, O = mods
+    spec = case.small_stage()
+    spec.ir = spec.jr = spec.kr = 1
+    spec.irbb = spec.jrbb = spec.krbb = 1
+    cd = common_setup.build_common(spec)
+    gpu = lib.Problem(cd)
+    ref = O.Oracle(cd)
+    ref.setup_calls()
+    gpu.step()
+    ref.step()
+    for n in STATE:
+        assert rel_linf(gpu.get(n), ref.get(n, double=False)) <= 1e-5, n
+    for _ in range(9):
+        gpu.step()
+        ref.step()
+    for n in ["RO", "ROVX", "ROVR", "RORVT", "ROE"]:
+        assert rel_linf(gpu.get(n), ref.get(n, double=False)) <= 1e-4, n
