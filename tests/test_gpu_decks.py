@@ -109,3 +109,46 @@ def test_single_stage_turbine_deck_200_steps(mods):
         assert abs(ig.mass_flow_out - ir.mass_flow_out) <= 1e-3 * abs(ir.mass_flow_out)
         assert np.isfinite(ig.eta_tt)
         gpu.close()
+
+
+def test_single_stage_turbine_deck_at_convergence(mods):
+    """The reference's single-stage turbine deck on the library's default
+    precision split against the FP64 oracle (tests/golden/
+    deck_converged_fp64.json): the deck's own end test (EAVG < CONLIM = 1e-3
+    with ECONT < 1 %) is met within 1 % of the oracle's step, and after the
+    deck's NSTEPS_MAX steps the mass flows are within 1e-4 relative and the
+    total-to-total efficiency within 1e-4 of the oracle's."""
+    import json
+    fx_path = os.path.join(HERE, "golden", "deck_converged_fp64.json")
+    if not os.path.exists(fx_path):
+        pytest.skip("no FP64 fixture")
+    fx = json.load(open(fx_path))
+    common_setup, deck, lib, O = mods
+    spec, geo = deck.load_fixture(os.path.join(HERE, "golden", "decks", "Single-stage-turbine-17.1.npz"))
+    # the deck as it stands: mgpu_run stops right after the end test's step
+    cd = common_setup.build_common(spec, geo)
+    cd.ints["NSTEPS_MAX"] = 10 ** 9
+    gpu = lib.Problem(cd)
+    n = 0
+    while True:
+        rc, m = gpu.run(500)
+        if rc == 1:
+            break
+        n += 500
+        assert n < 4 * fx["end_test_step"], "the end test never held"
+    stop = m.nstep - 1                 # the step whose tail met the test
+    assert abs(stop - fx["end_test_step"]) <= max(10, 0.01 * fx["end_test_step"]), (stop, fx["end_test_step"])
+    gpu.close()
+    # marched on to NSTEPS_MAX
+    cd.reals["CONLIM"] = 0.0
+    gpu = lib.Problem(cd)
+    n = 0
+    while n < fx["nstep"]:
+        k = min(500, fx["nstep"] - n)
+        gpu.run(k)
+        n += k
+    it = gpu.integrals()
+    assert abs(it.mass_flow_in - fx["mass_flow_in"]) <= 1e-4 * abs(fx["mass_flow_in"])
+    assert abs(it.mass_flow_out - fx["mass_flow_out"]) <= 1e-4 * abs(fx["mass_flow_out"])
+    assert abs(it.eta_tt - fx["eta_tt"]) <= 1e-4
+    gpu.close()
