@@ -20,9 +20,10 @@ from mgpu import deck  # noqa: E402
 # one deck per kind of input the path accepts: the mixing-length model on a
 # stage (the reference's single-stage turbine), NEW_LOSS and Spalart-Allmaras
 # on a transonic rotor with a tip gap, inviscid flow, a radial compressor,
-# a transonic fan and a linear cascade
+# a transonic fan, a linear cascade and a twelve-row compressor
 DECKS = [
     "Single-stage-turbine-17.1",
+    "Six-stage-compr-17.1",
     "r37+samods-17.5",
     "Rotor-37-17.1",
     "Shock-test-17.1",
