@@ -215,6 +215,19 @@ int32_t mgpu_write_grid_out(mgpu_handle *h, const char *path);
  * metric loops for a caller that binds the grid instead of the areas.
  * Valid before mgpu_commit (the geometry is fixed after it). */
 int32_t mgpu_setup_metrics(mgpu_handle *h);
+/* SETUP's grid from a deck's blade sections, then its metrics: NEW_INTPOL
+ * (multall-open-18.3.f:7493-7613) onto the KM stream surfaces with the
+ * tip-gap grid, the alignment of the rows at mid-span (6442-6448), the
+ * pinched-tip thickness (6452-6459) and RTHETA (6490-6501), in REAL*4 in
+ * SETUP's order of operations; binds X, R, RT_THICK and RTHETA and then
+ * does what mgpu_setup_metrics does.  sections: XSURF, RSURF, RT_UPP and
+ * RT_THICK of the nsecs input sections as the reader leaves them, each
+ * (nsecs, JM) with J fastest; fthick: FTHICK (NROWS, KM) with K fastest;
+ * fractip: FRACTIP1, FRACTIP2 per row.  Needs FR and FP (normalised), NROW,
+ * NBLADE, INDMIX, JSTART, JLE, JTE, JMIX, KTIPS, KTIPE, KS1, KS2 and WRAD
+ * bound.  Valid before mgpu_commit. */
+int32_t mgpu_setup_geometry(mgpu_handle *h, int32_t nsecs, const float *sections, const float *fthick,
+                            const float *fractip);
 /* The same metrics in double precision from double X, R (JM*KM each) and
  * RTHETA (IM*JM*KM), with the handle's INDMIX and WRAD; the handle is not
  * changed.  out receives AQX, AQR, ABX, ABR, VOL, ASX, ASR, VOLOR (IM*JM*KM

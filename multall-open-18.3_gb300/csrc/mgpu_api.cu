@@ -684,6 +684,40 @@ int32_t mgpu_setup_metrics(mgpu_handle *h) {
     return 0;
 }
 
+int32_t mgpu_setup_geometry(mgpu_handle *h, int32_t nsecs, const float *sections, const float *fthick,
+                            const float *fractip) {
+    if (!h || !sections || !fthick || !fractip) return fail(MGPU_E_ARG, "null argument");
+    if (h->committed) return fail(MGPU_E_STATE, "setup_geometry after commit: the geometry is fixed by then");
+    if (nsecs < 2 || nsecs > 32) return fail(MGPU_E_ARG, "setup_geometry: 2 to 32 blade sections");
+    for (const char *n : {"FR", "FP", "NROW", "NBLADE", "INDMIX", "JSTART", "JLE", "JTE", "JMIX", "KTIPS", "KTIPE", "KS1",
+                          "KS2", "WRAD"})
+        if (!h->bound[find_array(n)]) return fail(MGPU_E_STATE, std::string("setup_geometry needs ") + n);
+    const Dev &d = h->d;
+    const size_t JK = (size_t)d.JM * d.KM, ns = (size_t)nsecs;
+    const size_t n_sec = 4 * ns * d.JM, n_fth = (size_t)d.NROWS * d.KM, n_frt = 2 * (size_t)d.NROWS;
+    float *buf = nullptr;
+    const size_t total = n_sec + n_fth + n_frt + ns * d.JM + d.JM + JK;
+    CK(cudaMalloc(&buf, total * sizeof(float)));
+    float *dsec = buf, *dfth = dsec + n_sec, *dfrt = dfth + n_fth, *dsm = dfrt + n_frt, *dsh = dsm + ns * d.JM,
+          *drtu = dsh + d.JM;
+    cudaError_t e = cudaMemcpyAsync(dsec, sections, n_sec * sizeof(float), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dfth, fthick, n_fth * sizeof(float), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dfrt, fractip, n_frt * sizeof(float), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) {
+        auto F = [&](const char *n) { return (float *)h->dptr[find_array(n)]; };
+        auto I = [&](const char *n) { return (const int *)h->dptr[find_array(n)]; };
+        GeoArgs g{d.IM, d.JM, d.KM, nsecs, d.KMID, dsec, F("FR"), F("FP"), I("NROW"), I("NBLADE"), I("INDMIX"),
+                  I("JSTART"), I("JLE"), I("JTE"), I("JMIX"), I("KTIPS"), I("KTIPE"), I("KS1"), I("KS2"), dfrt, dfth,
+                  dsm, dsh, F("X"), F("R"), drtu, F("RT_THICK"), F("RTHETA")};
+        e = launch_setup_geometry(g, h->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(buf);
+    if (e != cudaSuccess) return fail(MGPU_E_CUDA, std::string("setup_geometry: ") + cudaGetErrorString(e));
+    for (const char *n : {"X", "R", "RT_THICK", "RTHETA"}) h->bound[find_array(n)] = true;
+    return mgpu_setup_metrics(h);
+}
+
 int32_t mgpu_setup_metrics64(mgpu_handle *h, const double *x, const double *r, const double *rtheta, double *out,
                              int64_t n_out) {
     if (!h || !x || !r || !rtheta || !out) return fail(MGPU_E_ARG, "null argument");

@@ -371,6 +371,20 @@ struct MetricArgs {
 template <typename T>
 cudaError_t launch_setup_metrics(int IM, int JM, int KM, const MetricArgs<T> &a, cudaStream_t s);
 
+// SETUP's grid from a deck's NS blade sections (mgpu_metrics.cu).
+struct GeoArgs {
+    int IM, JM, KM, NS, KMID;
+    const float *sec;                 // (4, NS, JM): XSURF, RSURF, RT_UPP, RT_THICK
+    const float *FR, *FP;             // normalised spacings
+    const int *NROW, *NBLADE, *INDMIX;
+    const int *JSTART, *JLE, *JTE, *JMIX, *KTIPS, *KTIPE, *KS1, *KS2;
+    const float *FRACTIP, *FTHICK;    // (NROWS, 2), (NROWS, KM)
+    float *SMERID, *SH;               // work: (NS, JM), (JM)
+    float *X, *R, *RTU, *RTT;         // (J, K)
+    float *RTHETA;                    // (I, J, K)
+};
+cudaError_t launch_setup_geometry(const GeoArgs &g, cudaStream_t s);
+
 // Read-only view of a handle, for entry points defined outside mgpu_api.cu.
 struct HandleView {
     const Dev *d;

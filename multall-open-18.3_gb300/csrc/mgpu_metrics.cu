@@ -151,7 +151,174 @@ __global__ void k_met_volor(Geo<T> g) {
     }
 }
 
+// ---------------------------------------------------------------------
+// SETUP's grid from a deck's blade sections: NEW_INTPOL (7493-7613), the
+// circumferential alignment of the rows at mid-span (6442-6448), the
+// pinched-tip thickness (6452-6459) and RTHETA (6490-6501), in REAL*4 in
+// the reference's order of operations.
+// ---------------------------------------------------------------------
+constexpr int MAX_SECS = 32;
+
+// INTP (7801-7872): Lagrange interpolation through four neighbouring table
+// points (all n when n < 4); xn, yn 0-based here
+__device__ float intp_dev(int n, const float *xn, const float *yn, float x) {
+    const float span = xn[n - 1] - xn[0];
+    int L = 1, nm = n;
+    if (n >= 4) {
+        nm = 4;
+        for (;;) {
+            if ((span > 0.0f && x < xn[L - 1]) || (span < 0.0f && x > xn[L - 1])) {
+                L = L > 2 ? (L != n ? L - 2 : n - 3) : 1;
+                break;
+            }
+            if (L == n) {
+                L = n - 3;
+                break;
+            }
+            ++L;
+        }
+    }
+    float y = 0.0f;
+    for (int l1 = 1; l1 <= nm; ++l1) {
+        float co = 1.0f;
+        for (int l2 = 1; l2 <= nm; ++l2) {
+            float temp = 1.0f;
+            if (l1 != l2) temp = (x - xn[L + l2 - 2]) / (xn[L + l1 - 2] - xn[L + l2 - 2]);
+            co = co * temp;
+        }
+        y = y + co * yn[L + l1 - 2];
+    }
+    return y;
+}
+
+// SMERID of each input section (7500-7506), one thread per section
+__global__ void k_geo_smerid(GeoArgs g) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.NS) return;
+    const float *xs = g.sec + (size_t)s * g.JM, *rs = g.sec + (size_t)(g.NS + s) * g.JM;
+    float *sm = g.SMERID + (size_t)s * g.JM;
+    sm[0] = 0.0f;
+    for (int j = 2; j <= g.JM; ++j) {
+        const float xd = xs[j - 1] - xs[j - 2], rd = rs[j - 1] - rs[j - 2];
+        sm[j - 1] = sm[j - 2] + sqrtf(xd * xd + rd * rd);
+    }
+}
+
+// NEW_INTPOL, one thread per J: the KM stream surfaces of plane J
+__global__ void k_geo_intpol(GeoArgs g) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (j > g.JM) return;
+    const int JM = g.JM, NS = g.NS;
+    const int nr = g.NROW[j - 1];
+    const int j1 = g.JSTART[nr - 1], jl = g.JLE[nr - 1], jt = g.JTE[nr - 1], je = g.JMIX[nr - 1];
+    const int kts = g.KTIPS[nr - 1], kte = g.KTIPE[nr - 1], ks1 = g.KS1[nr - 1], ks2 = g.KS2[nr - 1];
+    // the tip-gap grid (FRMOD, 7519-7560): FAC, TIPGAP, TIPSPACE and SUMFR
+    // are DOUBLE PRECISION there
+    double fac = 1.0, tipgap = 0.0, tipspace = 0.0, sumfr = 0.0;
+    const bool tip = kts > 0;
+    if (tip) {
+        const int ktip = kts == 1 ? 1 : NS;
+        const float *sm = g.SMERID + (size_t)(ktip - 1) * JM;
+        const float f1 = g.FRACTIP[2 * (nr - 1)], f2 = g.FRACTIP[2 * (nr - 1) + 1];
+        if (j >= j1 && j < jl) {
+            fac = (double)((sm[j - 1] - sm[j1 - 1]) / (sm[jl - 1] - sm[j1 - 1]));
+            tipgap = (double)f1;
+        }
+        if (j >= jl && j <= jt) {
+            fac = 1.0;
+            const float frac = (sm[j - 1] - sm[jl - 1]) / (sm[jt - 1] - sm[jl - 1]);
+            tipgap = (double)(f1 + frac * (f2 - f1));
+        }
+        if (j > jt && j <= je) {
+            fac = (double)((sm[je - 1] - sm[j - 1]) / (sm[je - 1] - sm[jt - 1]));
+            tipgap = (double)f2;
+        }
+        for (int k = kts; k <= kte - 1; ++k) sumfr = sumfr + (double)g.FR[k - 1];
+        tipspace = tipgap / (double)(kte - kts);
+    }
+    float xi[MAX_SECS], yi[MAX_SECS], ru[MAX_SECS], rt[MAX_SECS], qod[MAX_SECS];
+    for (int s = 0; s < NS; ++s) {
+        xi[s] = g.sec[(size_t)s * JM + (j - 1)];
+        yi[s] = g.sec[(size_t)(NS + s) * JM + (j - 1)];
+        ru[s] = g.sec[(size_t)(2 * NS + s) * JM + (j - 1)];
+        rt[s] = g.sec[(size_t)(3 * NS + s) * JM + (j - 1)];
+        if (s == 0) {
+            qod[0] = 0.0f;
+        } else {
+            const float rd = yi[s] - yi[s - 1], xd = xi[s] - xi[s - 1];
+            qod[s] = qod[s - 1] + sqrtf(xd * xd + rd * rd);
+        }
+    }
+    const float qospan = qod[NS - 1];
+    float xarg = 0.0f;
+    for (int k = 1; k <= g.KM; ++k) {
+        const int o = (j - 1) + JM * (k - 1);
+        g.X[o] = intp_dev(NS, qod, xi, xarg);
+        g.R[o] = intp_dev(NS, qod, yi, xarg);
+        g.RTU[o] = intp_dev(NS, qod, ru, xarg);
+        g.RTT[o] = intp_dev(NS, qod, rt, xarg);
+        float frmod = g.FR[k - 1];
+        if (tip && k >= kts && k <= kte - 1) frmod = (float)(tipspace * fac + (1.0 - fac) * (double)g.FR[k - 1]);
+        if (tip && k >= ks1 && k <= ks2)
+            frmod = (float)((double)g.FR[k - 1] * ((1.0 - tipgap) / (1.0 - sumfr) * fac + (1.0 - fac)));
+        xarg = xarg + frmod * qospan;
+    }
+}
+
+// the alignment shifts along J (6442-6448): each plane after a mixing plane
+// is turned so that its mid-span I = 1 line continues the previous plane's;
+// sequential in J, one thread
+__global__ void k_geo_shift(GeoArgs g) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const int JM = g.JM, km = g.KMID;
+    float SHIFT = 0.0f, prev = g.RTU[1 + JM * (km - 1)];    // RT_UPP(2, KMID), not moved
+    g.SH[0] = g.SH[1] = 0.0f;
+    for (int j = 3; j <= JM; ++j) {
+        const float rtu = g.RTU[(j - 1) + JM * (km - 1)], r = g.R[(j - 1) + JM * (km - 1)];
+        if (g.INDMIX[j - 2] == 1) SHIFT = (prev - rtu) / r;
+        g.SH[j - 1] = SHIFT;
+        prev = rtu + SHIFT * r;
+    }
+}
+
+// the shift and the pinched-tip thickness of node line (J, K), then its
+// RTHETA(I) (6490-6501)
+__global__ void k_geo_rtheta(GeoArgs g) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.JM * g.KM) return;
+    const int j = t % g.JM + 1, k = t / g.JM + 1;
+    const float R = g.R[t];
+    float rtu = g.RTU[t], rtt = g.RTT[t];
+    if (j >= 3) rtu = rtu + g.SH[j - 1] * R;
+    const int nr = g.NROW[j - 1];
+    const float RTMID = rtu - 0.5f * rtt;
+    const float THICK = g.FTHICK[(size_t)(nr - 1) * g.KM + (k - 1)] * rtt;
+    rtu = RTMID + 0.5f * THICK;
+    rtt = THICK;
+    g.RTU[t] = rtu;
+    g.RTT[t] = rtt;
+    const float PI = 3.14159265f;
+    const float PITCH = 2.0f * PI / (float)g.NBLADE[j - 1];
+    const float GAP = PITCH * R - rtt;
+    float *rth = g.RTHETA + (size_t)(j - 1) * g.IM + (size_t)(k - 1) * g.IM * g.JM;
+    float v = rtu;
+    rth[0] = v;
+    for (int i = 2; i <= g.IM; ++i) {
+        v = v + g.FP[i - 2] * GAP;
+        rth[i - 1] = v;
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_setup_geometry(const GeoArgs &g, cudaStream_t s) {
+    if (g.NS < 2 || g.NS > MAX_SECS) return cudaErrorInvalidValue;
+    k_geo_smerid<<<1, 32, 0, s>>>(g);
+    k_geo_intpol<<<(g.JM + 127) / 128, 128, 0, s>>>(g);
+    k_geo_shift<<<1, 1, 0, s>>>(g);
+    k_geo_rtheta<<<(g.JM * g.KM + 255) / 256, 256, 0, s>>>(g);
+    return cudaGetLastError();
+}
 
 template <typename T>
 cudaError_t launch_setup_metrics(int IM, int JM, int KM, const MetricArgs<T> &a, cudaStream_t s) {

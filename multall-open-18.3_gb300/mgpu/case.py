@@ -245,6 +245,11 @@ class CaseGeometry:
     ktips: List[int]
     ktipe: List[int]
     fthick: np.ndarray     # FTHICK(NR,K)  (NROWS, KM)
+    # a deck's NSECS_IN blade sections before NEW_INTPOL, XSURF, RSURF,
+    # RT_UPP, RT_THICK (4, NSECS_IN, JM), and FRACTIP1/2 (NROWS, 2); None
+    # for the generated cases
+    sections: Optional[np.ndarray] = None
+    fractip: Optional[np.ndarray] = None
 
 
 def build_geometry(spec: CaseSpec, dtype=f32) -> CaseGeometry:

@@ -849,6 +849,11 @@ def read_deck(text: str, name: str = "deck") -> tuple[CaseSpec, CaseGeometry]:
         for n in range(nrows):
             rough[n] = tuple(float(f32(v * f32(1.0e-6))) for v in c.reals(4))
 
+    # the sections NEW_INTPOL starts from (the device form of it takes these)
+    sections = np.stack([g.xs[1:jm + 1, 1:nsecs_in + 1].T, g.rs[1:jm + 1, 1:nsecs_in + 1].T,
+                         g.rtu[1:jm + 1, 1:nsecs_in + 1].T, g.rtt[1:jm + 1, 1:nsecs_in + 1].T]).astype(f32)
+    fractip = np.array([[rw.fractip[0], rw.fractip[1]] for rw in rows], f32)
+
     # ------------------ NEW_INTPOL, 7493-7613 ------------------------------
     frn = fr.copy()
     s = f32(0.0)
@@ -953,7 +958,7 @@ def read_deck(text: str, name: str = "deck") -> tuple[CaseSpec, CaseGeometry]:
     geo = CaseGeometry(spec=spec, im=im, jm=jm, km=km, x=X, r=R, rt_upp=RTU, rt_thick=RTT,
                        fp=fp[1:im + 1].copy(), fr=fr[1:km + 1].copy(), row_first_j=list(jstart),
                        ktips=[rw.ktips for rw in rows], ktipe=[rw.ktipe for rw in rows],
-                       fthick=np.stack([rw.fthick for rw in rows]).astype(f32))
+                       fthick=np.stack([rw.fthick for rw in rows]).astype(f32), sections=sections, fractip=fractip)
     return spec, geo
 
 
@@ -981,6 +986,9 @@ def save_fixture(path: str, spec: CaseSpec, geo: CaseGeometry, source: str = "")
     meta = dict(spec=sd, rows=rows, im=geo.im, jm=geo.jm, km=geo.km, row_first_j=geo.row_first_j,
                 ktips=geo.ktips, ktipe=geo.ktipe, source=source)
     arrays = {k: np.asarray(getattr(geo, k), f32) for k in _GEO_ARRAYS}
+    if geo.sections is not None:
+        arrays["sections"] = np.asarray(geo.sections, f32)
+        arrays["fractip"] = np.asarray(geo.fractip, f32)
     for k, v in (spec.inlet or {}).items():
         arrays["inlet_" + k] = np.asarray(v, f32)
     np.savez_compressed(path, meta=np.array(json.dumps(meta, default=float)), **arrays)
@@ -999,5 +1007,7 @@ def load_fixture(path: str) -> tuple[CaseSpec, CaseGeometry]:
     spec = CaseSpec(rows=rows, hub=None, casing=None, inlet=inlet, **sd)
     geo = CaseGeometry(spec=spec, im=meta["im"], jm=meta["jm"], km=meta["km"],
                        **{k: z[k] for k in _GEO_ARRAYS}, row_first_j=meta["row_first_j"],
-                       ktips=meta["ktips"], ktipe=meta["ktipe"])
+                       ktips=meta["ktips"], ktipe=meta["ktipe"],
+                       sections=z["sections"] if "sections" in z.files else None,
+                       fractip=z["fractip"] if "fractip" in z.files else None)
     return spec, geo

@@ -57,7 +57,7 @@ EXPORTS = ["mgpu_abi_version", "mgpu_last_error", "mgpu_device_count", "mgpu_cre
            "mgpu_adjoint_iterate", "mgpu_adjoint_solve", "mgpu_adjoint_gradient", "mgpu_adjoint_get",
            "mgpu_adjoint_set", "mgpu_adjoint_solve_krylov", "mgpu_autotune", "mgpu_write_flow_out",
            "mgpu_read_flow_out", "mgpu_stage_performance", "mgpu_adjoint_gradient_theta",
-           "mgpu_write_grid_out", "mgpu_setup_metrics", "mgpu_setup_metrics64"]
+           "mgpu_write_grid_out", "mgpu_setup_metrics", "mgpu_setup_metrics64", "mgpu_setup_geometry"]
 
 # SETUP's metric arrays, which mgpu_setup_metrics forms on the device
 METRIC_ARRAYS = ("AQX", "AQR", "ABX", "ABR", "VOL", "ASX", "ASR", "VOLOR", "ABT", "WRABT")
@@ -120,6 +120,7 @@ def load(build: bool = True):
     L.mgpu_adjoint_get.argtypes = [vp, cp, vp, ctypes.c_int64]
     L.mgpu_adjoint_set.argtypes = [vp, cp, vp, ctypes.c_int64]
     L.mgpu_setup_metrics.argtypes = [vp]
+    L.mgpu_setup_geometry.argtypes = [vp, i32, vp, vp, vp]
     L.mgpu_setup_metrics64.argtypes = [vp, vp, vp, vp, vp, ctypes.c_int64]
     for f in EXPORTS:
         fn = getattr(L, f)
@@ -159,11 +160,15 @@ def _chk(rc: int) -> int:
 class Problem:
     """One flow problem resident on the current GPU."""
 
-    def __init__(self, cd, setup_calls: bool = True, restart: str | None = None, device_metrics: bool = False):
+    def __init__(self, cd, setup_calls: bool = True, restart: str | None = None, device_metrics: bool = False,
+                 device_geometry=None):
         """restart: a flow_out file read after the COMMON data are bound and
         before the commit, as SETUP reads it with IF_RESTART = 1.
         device_metrics: the face areas and volumes are not bound from cd but
-        formed on the device from X, R and RTHETA (mgpu_setup_metrics)."""
+        formed on the device from X, R and RTHETA (mgpu_setup_metrics).
+        device_geometry: a deck's CaseGeometry whose blade sections give the
+        grid and its metrics on the device (mgpu_setup_geometry) in place of
+        cd's X, R, RT_THICK, RTHETA and metric arrays."""
         L = load()
         n = L.mgpu_device_count()
         if n <= 0:
@@ -176,12 +181,21 @@ class Problem:
             _chk(L.mgpu_set_int(self.h, k.encode(), int(v)))
         for k, v in cd.reals.items():
             _chk(L.mgpu_set_real(self.h, k.encode(), float(v)))
+        skip = set(METRIC_ARRAYS) if (device_metrics or device_geometry is not None) else set()
+        if device_geometry is not None:
+            skip |= {"X", "R", "RT_THICK", "RTHETA"}
         for k, a in cd.arrays.items():
-            if device_metrics and k in METRIC_ARRAYS:
+            if k in skip:
                 continue
             a = np.ascontiguousarray(a)
             _chk(L.mgpu_set_array(self.h, k.encode(), a.ctypes.data, a.nbytes))
-        if device_metrics:
+        if device_geometry is not None:
+            g = device_geometry
+            sec = np.ascontiguousarray(g.sections, np.float32)
+            fth = np.ascontiguousarray(g.fthick, np.float32)
+            frt = np.ascontiguousarray(g.fractip, np.float32)
+            _chk(L.mgpu_setup_geometry(self.h, sec.shape[1], sec.ctypes.data, fth.ctypes.data, frt.ctypes.data))
+        elif device_metrics:
             _chk(L.mgpu_setup_metrics(self.h))
         self.restart_nstep = None
         if restart is not None:

@@ -74,3 +74,24 @@ def test_device_metrics64_match_setup64(mods, which):
         err = np.max(np.abs(out[n] - ref)) / scale
         assert err <= 1e-12, (n, err)
     gpu.close()
+
+
+DECKS = ["Single-stage-turbine-17.1", "r37+samods-17.5", "Rotor-37-17.1", "Six-stage-compr-17.1",
+         "centrif-compr-17.1", "Transonic-fan-rotor-17.1", "Harrison-cascade-17.1", "Shock-test-17.1"]
+
+
+@pytest.mark.parametrize("name", DECKS)
+def test_device_geometry_from_deck_sections_equals_setup(mods, name):
+    """The reference's decks: NEW_INTPOL (tip-gap grid included), the
+    alignment at mid-span, the pinched-tip thickness, RTHETA and the metrics
+    formed on the device from the reader's blade sections equal the host
+    restatement (the deck reader's NEW_INTPOL and mgpu/common_setup.py) bit
+    for bit."""
+    case, common_setup, deck, lib = mods
+    spec, geo = deck.load_fixture(os.path.join(HERE, "golden", "decks", name + ".npz"))
+    cd = common_setup.build_common(spec, geo)
+    gpu = lib.Problem(cd, setup_calls=False, device_geometry=geo)
+    for n in ("X", "R", "RT_THICK", "RTHETA") + lib.METRIC_ARRAYS:
+        g, h = gpu.get(n), cd.arrays[n]
+        assert np.array_equal(g, h), (n, float(np.max(np.abs(g.astype(np.float64) - h))))
+    gpu.close()
