@@ -58,7 +58,9 @@ struct mgpu_handle {
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;     // captures the bodies of conditional graph nodes
     cudaStream_t aux = nullptr;      // a parallel branch of the step graph (k_bc_sums)
+    cudaStream_t aux2 = nullptr;     // another (the Spalart-Allmaras transport)
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_sa0 = nullptr, ev_sa1 = nullptr, ev_sa2 = nullptr;
     int device = 0;
     int sm_count = 0;
     bool committed = false;
@@ -251,13 +253,32 @@ __global__ void k_delay(long long cycles) {
 // conditions between them; every value is the same as in the serial order.
 // join: when the step is captured as a graph, k_bc_sums already runs on a
 // branch forked after k_prim (capture_step) and join marks its end
-void enqueue_core(const Dev &d, Launch L, cudaEvent_t join = nullptr) {
+// A second parallel branch of the step graph for the Spalart-Allmaras
+// model: the transported viscosity's fluxes and TSTEP read the mass fluxes,
+// the cell-average density and the model's own arrays, none of which the
+// inlet/exit conditions, the momentum fluxes or TSTEP of the momenta write,
+// and these read nothing it writes.  Its inlet value (4679-4689) follows the
+// conditions; the limiters, which may change the density it reads there,
+// wait for it.
+struct SaBranch {
+    cudaStream_t s = nullptr;
+    cudaEvent_t start = nullptr, bc = nullptr, done = nullptr;
+};
+
+void enqueue_core(const Dev &d, Launch L, cudaEvent_t join = nullptr, const SaBranch *sa = nullptr) {
     Launch L0 = L;        // follows the LOSS conditional node: plain stream order
     L0.pdl = false;
     launch_flux_mass_energy(d, L0);
     launch_tstep(d, L, V_RO, 2);
     if (d.ILOS >= 100) launch_roavg_cell(d, L);     // 4255-4267, after TSTEP(RO)
-    if (d.ILOS >= 200) launch_sa_transport(d, L);   // 4279-4347, after the cell-average density
+    const bool sab = sa && sa->s && d.ILOS >= 200;
+    if (sab) {
+        cudaEventRecord(sa->start, L.s);
+        cudaStreamWaitEvent(sa->s, sa->start, 0);
+        launch_sa_transport(d, Launch{sa->s, L.sm_count, nullptr});   // 4279-4347
+    } else if (d.ILOS >= 200) {
+        launch_sa_transport(d, L);                  // 4279-4347, after the cell-average density
+    }
     if (join) {
         cudaStreamWaitEvent(L.s, join, 0);
         launch_bc_apply(d, L0);
@@ -265,11 +286,23 @@ void enqueue_core(const Dev &d, Launch L, cudaEvent_t join = nullptr) {
         launch_bc_sums(d, L);
         launch_bc_apply(d, L);
     }
-    if (d.ILOS >= 200) launch_sa_inlet(d, L);       // 4679-4689
+    if (sab) {
+        cudaEventRecord(sa->bc, L.s);
+        cudaStreamWaitEvent(sa->s, sa->bc, 0);
+        launch_sa_inlet(d, Launch{sa->s, L.sm_count, nullptr});       // 4679-4689
+        cudaEventRecord(sa->done, sa->s);
+    } else if (d.ILOS >= 200) {
+        launch_sa_inlet(d, L);
+    }
     if (d.IN_FLOW != 0) launch_setflo(d, L);
     launch_flux_mom(d, L);          // also PEFF and the density limiter's column flags
     launch_tstep(d, L, V_ROVX, 3);
-    launch_limiters(d, L);
+    if (sab) {
+        cudaStreamWaitEvent(L.s, sa->done, 0);
+        launch_limiters(d, L0);
+    } else {
+        launch_limiters(d, L);
+    }
     launch_mixplan(d, L);
     if (d.any_cusp2) launch_cusp(d, L);
 }
@@ -347,7 +380,8 @@ int capture_step(mgpu_handle *h) {
     CK(cudaEventRecord(h->ev_join, h->aux));
     // an inviscid problem (ILOS = 0) has no LOSS node
     int rc = dg.ILOS == 0 ? 0 : add_conditional(h, hl, &h->loss_nodes, [&](Launch L2) { launch_loss(dg, L2, false); });
-    if (!rc) enqueue_core(dg, L, h->ev_join);
+    SaBranch sab{h->aux2, h->ev_sa0, h->ev_sa1, h->ev_sa2};
+    if (!rc) enqueue_core(dg, L, h->ev_join, &sab);
     if (!rc) rc = add_conditional(h, ht, &h->tail_nodes, [&](Launch L2) { enqueue_tail(dg, L2); });
     return rc;
 }
@@ -475,6 +509,10 @@ int32_t mgpu_create(int32_t im, int32_t jm, int32_t km, int32_t nrows, mgpu_hand
     e = cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->aux2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_sa0, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_sa1, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_sa2, cudaEventDisableTiming);
     if (e != cudaSuccess) return bail(fail(MGPU_E_CUDA, cudaGetErrorString(e)));
     // arrays whose size is known now
     for (int a = 0; a < kNumArrays; ++a) {
@@ -551,8 +589,11 @@ void mgpu_destroy(mgpu_handle *h) {
     if (h->stream) cudaStreamDestroy(h->stream);
     if (h->side) cudaStreamDestroy(h->side);
     if (h->aux) cudaStreamDestroy(h->aux);
+    if (h->aux2) cudaStreamDestroy(h->aux2);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
+    for (cudaEvent_t ev : {h->ev_sa0, h->ev_sa1, h->ev_sa2})
+        if (ev) cudaEventDestroy(ev);
     delete h;
 }
 
