@@ -82,6 +82,21 @@ def test_deck_five_steps(mods, name):
     gpu.close()
 
 
+@pytest.mark.parametrize("name", ["Rotor-37-17.1", "r37+samods-17.5"])
+def test_rotor37_decks_200_steps(mods, name):
+    """NASA rotor 37 with NEW_LOSS and with the Spalart-Allmaras model (the
+    reference's decks, tip gap, 13 input sections for the S-A deck): 200
+    steps within 1e-3 of the oracle in the parity mode, the transported
+    viscosity included."""
+    spec, cd, gpu, ref = _pair(mods, name, REDUCE_ORDER=1)
+    gpu.run(200)
+    for _ in range(200):
+        ref.step()
+    names = ["RO", "ROVX", "ROVR", "RORVT", "ROE", "XFORCE"] + (["TRANS_DYN_VIS"] if spec.ilos >= 200 else [])
+    _compare(gpu, ref, names, 1e-3, f"{name}, 200 steps")
+    gpu.close()
+
+
 @pytest.mark.parametrize("name", sorted(REFUSED))
 def test_deck_outside_the_library_is_refused(mods, name):
     """A deck the library does not cover fails at mgpu_create with an
