@@ -825,26 +825,11 @@ __global__ void __launch_bounds__(PBS, 1024 / PBS) k_ts_update_pair(const __grid
     const float *__restrict__ FTR = d.FTR;
     const int nb0 = IM * (j0 - 1);
     const int np = IM * KM;
-    // the general form of one node: cells (kc, h, ic) in the reference's order
-    auto edge = [&](int i, int k, float v, const float *cA, const float *cB, bool hA, bool hB, float fdn,
-                    float fup) -> float {
-        for (int kc = k - 1; kc <= k; ++kc) {
-            if (kc < 1 || kc > KMM1) continue;
-            for (int h = 0; h < 2; ++h) {
-                if (!(h ? hB : hA)) continue;
-                const float *c = h ? cB : cA;
-                float fac = h ? fup : fdn;
-                for (int ic = i - 1; ic <= i; ++ic) {
-                    if (ic < 1 || ic > IMM1) continue;
-                    float wt;
-                    if (ic == i) wt = (kc == k) ? AIK(FBL, ic, kc) : AIK(FTL, ic, kc);
-                    else wt = (kc == k) ? AIK(FBR, ic, kc) : AIK(FTR, ic, kc);
-                    v = v + c[(kc - 1) * IMM1 + (ic - 1)] * wt * fac;
-                }
-            }
-        }
-        return v;
-    };
+    // one node of a node plane from its <= 8 cells (kc, h, ic), cA the cell
+    // plane before it and cB the one after, added in the reference's order
+    // (kc outer, then the plane, then ic); a cell outside the grid is
+    // skipped, so the boundary nodes take the same predicated path as the
+    // inner ones instead of a branch of their own
     Walk2 w(IM, threadIdx.x, PBS);
     for (int t0 = threadIdx.x; t0 < np; t0 += TS_UG * PBS) {
         float dv0[TS_UG], dv1[TS_UG], wtr[TS_UG], wtl[TS_UG], wbr[TS_UG], wbl[TS_UG];
@@ -859,12 +844,11 @@ __global__ void __launch_bounds__(PBS, 1024 / PBS) k_ts_update_pair(const __grid
                 const int n = nb0 + (i - 1) + ks * (k - 1);
                 dv0[u] = D[n];
                 if (two) dv1[u] = D[n + IM];
-                if (i >= 2 && i <= IMM1 && k >= 2 && k <= KMM1) {
-                    wtr[u] = FTR[(i - 2) + IM * (k - 2)];
-                    wtl[u] = FTL[(i - 1) + IM * (k - 2)];
-                    wbr[u] = FBR[(i - 2) + IM * (k - 1)];
-                    wbl[u] = FBL[(i - 1) + IM * (k - 1)];
-                }
+                const bool hL = i >= 2, hR = i <= IMM1, hD = k >= 2, hU = k <= KMM1;
+                wtr[u] = (hL && hD) ? FTR[(i - 2) + IM * (k - 2)] : 0.0f;
+                wtl[u] = (hR && hD) ? FTL[(i - 1) + IM * (k - 2)] : 0.0f;
+                wbr[u] = (hL && hU) ? FBR[(i - 2) + IM * (k - 1)] : 0.0f;
+                wbl[u] = (hR && hU) ? FBL[(i - 1) + IM * (k - 1)] : 0.0f;
             }
         }
 #pragma unroll
@@ -872,39 +856,29 @@ __global__ void __launch_bounds__(PBS, 1024 / PBS) k_ts_update_pair(const __grid
             if (t0 + u * PBS >= np) break;
             const int i = ni[u], k = nk[u];
             const int n = nb0 + (i - 1) + ks * (k - 1);
-            const bool inner = i >= 2 && i <= IMM1 && k >= 2 && k <= KMM1;
-            const int lo = (i - 2) + IMM1 * (k - 2), hi = lo + IMM1;
+            const bool hL = i >= 2, hR = i <= IMM1, hD = k >= 2, hU = k <= KMM1;
+            const int lo = (i - 2) + IMM1 * (k - 2), hi = lo + IMM1;    // cells (i-1, k-1) and (i-1, k)
+            auto gather = [&](float v, const float *cA, const float *cB, bool hA, bool hB, float fdn,
+                              float fup) -> float {
+                if (hD) {
+                    if (hA && hL) v = v + cA[lo] * wtr[u] * fdn;
+                    if (hA && hR) v = v + cA[lo + 1] * wtl[u] * fdn;
+                    if (hB && hL) v = v + cB[lo] * wtr[u] * fup;
+                    if (hB && hR) v = v + cB[lo + 1] * wtl[u] * fup;
+                }
+                if (hU) {
+                    if (hA && hL) v = v + cA[hi] * wbr[u] * fdn;
+                    if (hA && hR) v = v + cA[hi + 1] * wbl[u] * fdn;
+                    if (hB && hL) v = v + cB[hi] * wbr[u] * fup;
+                    if (hB && hR) v = v + cB[hi + 1] * wbl[u] * fup;
+                }
+                return v;
+            };
             // node plane j0: cell planes j0 (c0) and j0 + 1 (c1)
-            float v = dv0[u];
-            if (inner && hA0 && hB0) {
-                v = v + c0[lo] * wtr[u] * fdn0;
-                v = v + c0[lo + 1] * wtl[u] * fdn0;
-                v = v + c1[lo] * wtr[u] * fup0;
-                v = v + c1[lo + 1] * wtl[u] * fup0;
-                v = v + c0[hi] * wbr[u] * fdn0;
-                v = v + c0[hi + 1] * wbl[u] * fdn0;
-                v = v + c1[hi] * wbr[u] * fup0;
-                v = v + c1[hi + 1] * wbl[u] * fup0;
-            } else {
-                v = edge(i, k, v, c0, c1, hA0, hB0, fdn0, fup0);
-            }
-            TM[n] = v;
+            TM[n] = gather(dv0[u], c0, c1, hA0, hB0, fdn0, fup0);
             if (!two) continue;
             // node plane j0 + 1: cell planes j0 + 1 (c1) and j0 + 2 (c2)
-            v = dv1[u];
-            if (inner && hB1) {
-                v = v + c1[lo] * wtr[u] * fdn1;
-                v = v + c1[lo + 1] * wtl[u] * fdn1;
-                v = v + c2[lo] * wtr[u] * fup1;
-                v = v + c2[lo + 1] * wtl[u] * fup1;
-                v = v + c1[hi] * wbr[u] * fdn1;
-                v = v + c1[hi + 1] * wbl[u] * fdn1;
-                v = v + c2[hi] * wbr[u] * fup1;
-                v = v + c2[hi + 1] * wbl[u] * fup1;
-            } else {
-                v = edge(i, k, v, c1, c2, true, hB1, fdn1, fup1);
-            }
-            TM[n + IM] = v;
+            TM[n + IM] = gather(dv1[u], c1, c2, true, hB1, fdn1, fup1);
         }
     }
 }
