@@ -1006,34 +1006,40 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_smooth(const __grid_consta
     const bool periodic_j = !(A1(d.IND, j) == 1 || A1(d.INDLE, j) == 1);
     if (j >= 2 && !(c->SFT < 0.0001f)) {
         const float SFT = c->SFT, SFT1 = c->SFT1, F4 = d.FAC_4TH;
-        Walk2 w(IM, threadIdx.x, BS);
-        for (int t = threadIdx.x; t < np; t += BS, w.next()) {
-            const int i = w.i, k = w.k;
+        // the points I = 2..IMM1 first, every lane on the same path: the
+        // curvature at I = 1 and IM, which the points I = 2 and IMM1 take, is
+        // one value per line (the reference's CURVE there is the I = 1 value,
+        // or 0 off the periodic planes) and is selected, not branched to
+        const int ni = IM - 2;
+        Walk2 w(ni, threadIdx.x, BS);
+        for (int t = threadIdx.x; t < ni * KM; t += BS, w.next()) {
+            const int i = w.i + 1, k = w.k;
             const float *ak = a + IM * (k - 1) - 1;     // ak[i] = P(a, i, k)
-            auto curve = [&](int ii) -> float {
-                if (ii == 1 || ii == IM) {
-                    if (!periodic_j) return 0.0f;
-                    float avg1 = 0.5f * (ak[2] + ak[IMM1]);
-                    return ak[1] - avg1;
-                }
-                float avg = cFD[ii - 1] * ak[ii + 1] + cFU[ii - 1] * ak[ii - 1];
-                return ak[ii] - avg;
-            };
+            const float cper = periodic_j ? ak[1] - 0.5f * (ak[2] + ak[IMM1]) : 0.0f;
+            const int im = i - 1 > 1 ? i - 1 : 2, ip = i + 1 < IM ? i + 1 : IMM1;   // in range
+            const float gm = ak[im] - (cFD[im - 1] * ak[im + 1] + cFU[im - 1] * ak[im - 1]);
+            const float gp = ak[ip] - (cFD[ip - 1] * ak[ip + 1] + cFU[ip - 1] * ak[ip - 1]);
+            const float cm = i - 1 == 1 ? cper : gm, cp = i + 1 == IM ? cper : gp;
+            const float AVG = cFD[i - 1] * ak[i + 1] + cFU[i - 1] * ak[i - 1];
+            const float SC = cFU[i - 1] * cm + cFD[i - 1] * cp;
+            b[(i - 1) + IM * (k - 1)] = SFT1 * ak[i] + SFT * (AVG + F4 * SC);
+        }
+        // then the points I = 1 and IM of every line
+        for (int t = threadIdx.x; t < 2 * KM; t += BS) {
+            const int i = (t & 1) ? IM : 1, k = (t >> 1) + 1;
+            const float *ak = a + IM * (k - 1) - 1;
             float AVG, SC;
-            if (i == 1 || i == IM) {
-                if (periodic_j) {
-                    AVG = 0.5f * (ak[2] + ak[IMM1]);
-                    SC = 0.5f * (curve(2) + curve(IMM1));
-                } else {
-                    if (i == 1) AVG = ak[2] + cFU[0] * (ak[2] - ak[3]);
-                    else AVG = ak[IMM1] + cFU[IM - 1] * (ak[IMM1] - ak[d.IMM2]);
-                    SC = 0.0f;
-                }
+            if (periodic_j) {
+                AVG = 0.5f * (ak[2] + ak[IMM1]);
+                const float c2 = ak[2] - (cFD[1] * ak[3] + cFU[1] * ak[1]);
+                const float cm1 = ak[IMM1] - (cFD[IMM1 - 1] * ak[IM] + cFU[IMM1 - 1] * ak[d.IMM2]);
+                SC = 0.5f * (c2 + cm1);
             } else {
-                AVG = cFD[i - 1] * ak[i + 1] + cFU[i - 1] * ak[i - 1];
-                SC = cFU[i - 1] * curve(i - 1) + cFD[i - 1] * curve(i + 1);
+                if (i == 1) AVG = ak[2] + cFU[0] * (ak[2] - ak[3]);
+                else AVG = ak[IMM1] + cFU[IM - 1] * (ak[IMM1] - ak[d.IMM2]);
+                SC = 0.0f;
             }
-            b[t] = SFT1 * ak[i] + SFT * (AVG + F4 * SC);
+            b[(i - 1) + IM * (k - 1)] = SFT1 * ak[i] + SFT * (AVG + F4 * SC);
         }
         __syncthreads();
         w = Walk2(IM, threadIdx.x, BS);
