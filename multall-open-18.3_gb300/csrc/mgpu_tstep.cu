@@ -37,6 +37,7 @@ static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n
 constexpr int TS_U = 3;          // cells per thread whose loads are issued together
 constexpr int TS_UG = 4;         // the same for the damping and gather phases of update
 constexpr int SV_U = 3;          // points per thread whose streamwise loads are issued together
+constexpr int SM_SEG = 8;        // points per thread of one pitchwise or spanwise smoothing segment
 
 // CTA sum of one double-float per thread (thread 0 receives it)
 template <int BS>
@@ -925,8 +926,12 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_smooth(const __grid_consta
     float *__restrict__ D = V.D;
     const int IM = d.IM, KM = d.KM, IMM1 = d.IMM1, KMM1 = d.KMM1;
     const int np = IM * KM;
-    float *a = sm, *b = sm + np;
-    float *cFD = b + np, *cFU = cFD + IM, *cFKD = cFU + IM, *cFKU = cFKD + KM;   // FD, FU, FKD, FKU
+    // the plane buffers hold (i, k) at (i-1) + IMP*(k-1); the odd row pitch
+    // keeps the pitchwise pass, whose lanes step from one K line to the
+    // next, free of bank conflicts
+    const int IMP = IM | 1;
+    float *a = sm, *b = sm + IMP * KM;
+    float *cFD = b + IMP * KM, *cFU = cFD + IM, *cFKD = cFU + IM, *cFKU = cFKD + KM;   // FD, FU, FKD, FKU
     const int j = blockIdx.x + 1;
     const DevCtl *c = d.ctl;
     const bool stream = !(c->SFX < 0.0001f);
@@ -997,37 +1002,54 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_smooth(const __grid_consta
                     else if (i == 1) v = SFXHM1 * dd + SFX14 * (pkk[IM + 0] + pkk[IM - 1]);
                     else v = SFXHM1 * dd + SFX14 * (pkk[IM + IM - 1] + pkk[0]);
                 }
-                a[t] = v;
+                a[(i - 1) + IMP * (k - 1)] = v;
             }
         }
     }
     __syncthreads();
-#define P(buf, i, k) buf[((i) - 1) + IM * ((k) - 1)]
+#define P(buf, i, k) buf[((i) - 1) + IMP * ((k) - 1)]
     const bool periodic_j = !(A1(d.IND, j) == 1 || A1(d.INDLE, j) == 1);
     if (j >= 2 && !(c->SFT < 0.0001f)) {
         const float SFT = c->SFT, SFT1 = c->SFT1, F4 = d.FAC_4TH;
-        // the points I = 2..IMM1 first, every lane on the same path: the
-        // curvature at I = 1 and IM, which the points I = 2 and IMM1 take, is
-        // one value per line (the reference's CURVE there is the I = 1 value,
-        // or 0 off the periodic planes) and is selected, not branched to
-        const int ni = IM - 2;
-        Walk2 w(ni, threadIdx.x, BS);
-        for (int t = threadIdx.x; t < ni * KM; t += BS, w.next()) {
-            const int i = w.i + 1, k = w.k;
-            const float *ak = a + IM * (k - 1) - 1;     // ak[i] = P(a, i, k)
+        // the points I = 2..IMM1 first, in segments of SM_SEG points of one K
+        // line per thread, the lanes on successive K lines: each point's
+        // curvature is formed once and the segment's values stay in
+        // registers.  The curvature at I = 1 and IM, which the points I = 2
+        // and IMM1 take, is one value per line (the reference's CURVE there
+        // is the I = 1 value, or 0 off the periodic planes)
+        const int nsi = (IM - 2 + SM_SEG - 1) / SM_SEG;
+        Walk2 w(KM, threadIdx.x, BS);
+        for (int t = threadIdx.x; t < nsi * KM; t += BS, w.next()) {
+            const int k = w.i, i0 = 2 + SM_SEG * (w.k - 1);
+            const int len = min(SM_SEG, IMM1 - i0 + 1);
+            const float *ak = a + IMP * (k - 1) - 1;     // ak[i] = P(a, i, k)
+            float x[SM_SEG + 4];                          // x[q] = P(a, i0 - 2 + q, k)
+#pragma unroll
+            for (int q = 0; q < SM_SEG + 4; ++q) {
+                const int ii = i0 - 2 + q;
+                x[q] = (q < len + 4 && ii >= 1 && ii <= IM) ? ak[ii] : 0.0f;
+            }
             const float cper = periodic_j ? ak[1] - 0.5f * (ak[2] + ak[IMM1]) : 0.0f;
-            const int im = i - 1 > 1 ? i - 1 : 2, ip = i + 1 < IM ? i + 1 : IMM1;   // in range
-            const float gm = ak[im] - (cFD[im - 1] * ak[im + 1] + cFU[im - 1] * ak[im - 1]);
-            const float gp = ak[ip] - (cFD[ip - 1] * ak[ip + 1] + cFU[ip - 1] * ak[ip - 1]);
-            const float cm = i - 1 == 1 ? cper : gm, cp = i + 1 == IM ? cper : gp;
-            const float AVG = cFD[i - 1] * ak[i + 1] + cFU[i - 1] * ak[i - 1];
-            const float SC = cFU[i - 1] * cm + cFD[i - 1] * cp;
-            b[(i - 1) + IM * (k - 1)] = SFT1 * ak[i] + SFT * (AVG + F4 * SC);
+            float g[SM_SEG + 2];                          // g[q]: the curvature at I = i0 - 1 + q
+#pragma unroll
+            for (int q = 0; q < SM_SEG + 2; ++q) {
+                const int ii = i0 - 1 + q;
+                g[q] = (ii == 1 || ii >= IM) ? cper : x[q + 1] - (cFD[ii - 1] * x[q + 2] + cFU[ii - 1] * x[q]);
+            }
+            float *bk = b + IMP * (k - 1) - 1;
+#pragma unroll
+            for (int q = 0; q < SM_SEG; ++q) {
+                if (q >= len) break;
+                const int ii = i0 + q;
+                const float AVG = cFD[ii - 1] * x[q + 3] + cFU[ii - 1] * x[q + 1];
+                const float SC = cFU[ii - 1] * g[q] + cFD[ii - 1] * g[q + 2];
+                bk[ii] = SFT1 * x[q + 2] + SFT * (AVG + F4 * SC);
+            }
         }
         // then the points I = 1 and IM of every line
         for (int t = threadIdx.x; t < 2 * KM; t += BS) {
             const int i = (t & 1) ? IM : 1, k = (t >> 1) + 1;
-            const float *ak = a + IM * (k - 1) - 1;
+            const float *ak = a + IMP * (k - 1) - 1;
             float AVG, SC;
             if (periodic_j) {
                 AVG = 0.5f * (ak[2] + ak[IMM1]);
@@ -1039,30 +1061,46 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_smooth(const __grid_consta
                 else AVG = ak[IMM1] + cFU[IM - 1] * (ak[IMM1] - ak[d.IMM2]);
                 SC = 0.0f;
             }
-            b[(i - 1) + IM * (k - 1)] = SFT1 * ak[i] + SFT * (AVG + F4 * SC);
+            P(b, i, k) = SFT1 * ak[i] + SFT * (AVG + F4 * SC);
         }
         __syncthreads();
+        // spanwise: segments of SM_SEG points of one I line per thread, the
+        // lanes on successive I lines
+        const int nsk = (KM + SM_SEG - 1) / SM_SEG;
         w = Walk2(IM, threadIdx.x, BS);
-        for (int t = threadIdx.x; t < np; t += BS, w.next()) {
-            const int i = w.i, k = w.k;
-            const float *bi = b + (i - 1) - IM;         // bi[IM * kk] = P(b, i, kk)
-            auto curvek = [&](int kk) -> float {
-                if (kk == 1 || kk == KM) return 0.0f;
-                float avg = cFKD[kk - 1] * bi[IM * (kk + 1)] + cFKU[kk - 1] * bi[IM * (kk - 1)];
-                return bi[IM * kk] - avg;
-            };
-            float AVG, SC;
-            if (k == 1) {
-                AVG = bi[IM * 2] + 0.5f * cFKU[0] * (bi[IM * 2] - bi[IM * 3]);
-                SC = 0.0f;
-            } else if (k == KM) {
-                AVG = bi[IM * KMM1] + 0.5f * cFKU[KM - 1] * (bi[IM * KMM1] - bi[IM * d.KMM2]);
-                SC = 0.0f;
-            } else {
-                AVG = cFKD[k - 1] * bi[IM * (k + 1)] + cFKU[k - 1] * bi[IM * (k - 1)];
-                SC = cFKU[k - 1] * curvek(k - 1) + cFKD[k - 1] * curvek(k + 1);
+        for (int t = threadIdx.x; t < nsk * IM; t += BS, w.next()) {
+            const int i = w.i, k0 = 1 + SM_SEG * (w.k - 1);
+            const int len = min(SM_SEG, KM - k0 + 1);
+            const float *bi = b + (i - 1) - IMP;          // bi[IMP * kk] = P(b, i, kk)
+            float y[SM_SEG + 4];                          // y[q] = P(b, i, k0 - 2 + q)
+#pragma unroll
+            for (int q = 0; q < SM_SEG + 4; ++q) {
+                const int kk = k0 - 2 + q;
+                y[q] = (q < len + 4 && kk >= 1 && kk <= KM) ? bi[IMP * kk] : 0.0f;
             }
-            a[t] = SFT1 * bi[IM * k] + SFT * (AVG + F4 * SC);
+            float h[SM_SEG + 2];                          // h[q]: the curvature at K = k0 - 1 + q
+#pragma unroll
+            for (int q = 0; q < SM_SEG + 2; ++q) {
+                const int kk = k0 - 1 + q;
+                h[q] = (kk <= 1 || kk >= KM) ? 0.0f : y[q + 1] - (cFKD[kk - 1] * y[q + 2] + cFKU[kk - 1] * y[q]);
+            }
+#pragma unroll
+            for (int q = 0; q < SM_SEG; ++q) {
+                if (q >= len) break;
+                const int kk = k0 + q;
+                float AVG, SC;
+                if (kk == 1) {
+                    AVG = y[q + 3] + 0.5f * cFKU[0] * (y[q + 3] - y[q + 4]);
+                    SC = 0.0f;
+                } else if (kk == KM) {
+                    AVG = y[q + 1] + 0.5f * cFKU[KM - 1] * (y[q + 1] - y[q]);
+                    SC = 0.0f;
+                } else {
+                    AVG = cFKD[kk - 1] * y[q + 3] + cFKU[kk - 1] * y[q + 1];
+                    SC = cFKU[kk - 1] * h[q] + cFKD[kk - 1] * h[q + 2];
+                }
+                P(a, i, kk) = SFT1 * y[q + 2] + SFT * (AVG + F4 * SC);
+            }
         }
         __syncthreads();
         float cv = 0.0f;
@@ -1133,13 +1171,14 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_ts_smooth(const __grid_consta
             }
         }
         __syncthreads();
-        for (int t = threadIdx.x; t < np; t += BS) a[t] = b[t / IM];
+        Walk2 w(IM, threadIdx.x, BS);
+        for (int t = threadIdx.x; t < np; t += BS, w.next()) P(a, w.i, w.k) = b[w.k - 1];
         __syncthreads();
     }
 #undef P
     float *Dj = D + IM * (j - 1);
     Walk2 w(IM, threadIdx.x, BS);
-    for (int t = threadIdx.x; t < np; t += BS, w.next()) Dj[(w.i - 1) + ks * (w.k - 1)] = a[t];
+    for (int t = threadIdx.x; t < np; t += BS, w.next()) Dj[(w.i - 1) + ks * (w.k - 1)] = a[(w.i - 1) + IMP * (w.k - 1)];
 }
 
 // ---------------------------------------------------------------------
@@ -1199,7 +1238,7 @@ static size_t cells_smem(const Dev &d) {
 static size_t prolong_smem(const Dev &d) { return ((size_t)d.NIB1 * d.NKB1 + (size_t)d.NIB2 * d.NKB2) * sizeof(float); }
 static size_t update_smem(const Dev &d) { return (size_t)2 * d.IMM1 * d.KMM1 * sizeof(float); }
 static size_t update_pair_smem(const Dev &d) { return (size_t)3 * d.IMM1 * d.KMM1 * sizeof(float); }
-static size_t smooth_smem(const Dev &d) { return ((size_t)2 * d.IM * d.KM + 2 * d.IM + 2 * d.KM) * sizeof(float); }
+static size_t smooth_smem(const Dev &d) { return ((size_t)2 * (d.IM | 1) * d.KM + 2 * d.IM + 2 * d.KM) * sizeof(float); }
 
 template <int BS>
 static cudaError_t configure_bs(const Dev &d) {
