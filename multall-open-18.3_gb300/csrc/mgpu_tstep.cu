@@ -38,6 +38,7 @@ constexpr int TS_U = 3;          // cells per thread whose loads are issued toge
 constexpr int TS_UG = 4;         // the same for the damping and gather phases of update
 constexpr int SV_U = 3;          // points per thread whose streamwise loads are issued together
 constexpr int SM_SEG = 8;        // points per thread of one pitchwise or spanwise smoothing segment
+constexpr int UG_SEG = 3;        // nodes per thread of one K column in the pair update's gather
 
 // CTA sum of one double-float per thread (thread 0 receives it)
 template <int BS>
@@ -829,57 +830,95 @@ __global__ void __launch_bounds__(PBS, 1024 / PBS) k_ts_update_pair(const __grid
     // one node of a node plane from its <= 8 cells (kc, h, ic), cA the cell
     // plane before it and cB the one after, added in the reference's order
     // (kc outer, then the plane, then ic); a cell outside the grid is
-    // skipped, so the boundary nodes take the same predicated path as the
-    // inner ones instead of a branch of their own
+    // skipped.  One thread per column of UG_SEG nodes along K at one I, the
+    // lanes on successive I: walking up the column, the cells above a node
+    // are the cells below the next one, so each cell value is read from
+    // shared memory once per column and the boundary nodes take the same
+    // predicated path as the inner ones
+    const bool pv0 = hA0, pv1 = two, pv2 = hB1;  // cell planes j0, j0 + 1, j0 + 2 present
+    const int nsk = (KM + UG_SEG - 1) / UG_SEG;
     Walk2 w(IM, threadIdx.x, PBS);
-    for (int t0 = threadIdx.x; t0 < np; t0 += TS_UG * PBS) {
-        float dv0[TS_UG], dv1[TS_UG], wtr[TS_UG], wtl[TS_UG], wbr[TS_UG], wbl[TS_UG];
-        int ni[TS_UG], nk[TS_UG];
+    for (int t = threadIdx.x; t < IM * nsk; t += PBS, w.next()) {
+        const int i = w.i, k0 = 1 + UG_SEG * (w.k - 1);
+        const int len = min(UG_SEG, KM - k0 + 1);
+        const bool hL = i >= 2, hR = i <= IMM1;
+        // the global operands of the column's nodes, loaded together
+        float dv0[UG_SEG], dv1[UG_SEG], wtr[UG_SEG], wtl[UG_SEG], wbr[UG_SEG], wbl[UG_SEG];
 #pragma unroll
-        for (int u = 0; u < TS_UG; ++u) {
-            const int i = w.i, k = w.k;
-            ni[u] = i;
-            nk[u] = k;
-            w.next();
-            if (t0 + u * PBS < np) {
-                const int n = nb0 + (i - 1) + ks * (k - 1);
-                dv0[u] = D[n];
-                if (two) dv1[u] = D[n + IM];
-                const bool hL = i >= 2, hR = i <= IMM1, hD = k >= 2, hU = k <= KMM1;
-                wtr[u] = (hL && hD) ? FTR[(i - 2) + IM * (k - 2)] : 0.0f;
-                wtl[u] = (hR && hD) ? FTL[(i - 1) + IM * (k - 2)] : 0.0f;
-                wbr[u] = (hL && hU) ? FBR[(i - 2) + IM * (k - 1)] : 0.0f;
-                wbl[u] = (hR && hU) ? FBL[(i - 1) + IM * (k - 1)] : 0.0f;
-            }
+        for (int q = 0; q < UG_SEG; ++q) {
+            if (q >= len) break;
+            const int k = k0 + q;
+            const int n = nb0 + (i - 1) + ks * (k - 1);
+            const bool hD = k >= 2, hU = k <= KMM1;
+            dv0[q] = D[n];
+            dv1[q] = two ? D[n + IM] : 0.0f;
+            wtr[q] = (hL && hD) ? FTR[(i - 2) + IM * (k - 2)] : 0.0f;
+            wtl[q] = (hR && hD) ? FTL[(i - 1) + IM * (k - 2)] : 0.0f;
+            wbr[q] = (hL && hU) ? FBR[(i - 2) + IM * (k - 1)] : 0.0f;
+            wbl[q] = (hR && hU) ? FBL[(i - 1) + IM * (k - 1)] : 0.0f;
+        }
+        // cells (i-1, r) and (i, r) of the three cell planes, r = the cell
+        // row below the node (dn) and above it (up)
+        float dn0l = 0.0f, dn0r = 0.0f, dn1l = 0.0f, dn1r = 0.0f, dn2l = 0.0f, dn2r = 0.0f;
+        const int cl = i - 2;                       // cell (i-1, r) at cl + IMM1*(r-1)
+        if (k0 >= 2) {
+            const int o = cl + IMM1 * (k0 - 2);
+            if (pv0 && hL) dn0l = c0[o];
+            if (pv0 && hR) dn0r = c0[o + 1];
+            if (pv1 && hL) dn1l = c1[o];
+            if (pv1 && hR) dn1r = c1[o + 1];
+            if (pv2 && hL) dn2l = c2[o];
+            if (pv2 && hR) dn2r = c2[o + 1];
         }
 #pragma unroll
-        for (int u = 0; u < TS_UG; ++u) {
-            if (t0 + u * PBS >= np) break;
-            const int i = ni[u], k = nk[u];
+        for (int q = 0; q < UG_SEG; ++q) {
+            if (q >= len) break;
+            const int k = k0 + q;
+            const bool hD = k >= 2, hU = k <= KMM1;
+            float up0l = 0.0f, up0r = 0.0f, up1l = 0.0f, up1r = 0.0f, up2l = 0.0f, up2r = 0.0f;
+            if (hU) {
+                const int o = cl + IMM1 * (k - 1);
+                if (pv0 && hL) up0l = c0[o];
+                if (pv0 && hR) up0r = c0[o + 1];
+                if (pv1 && hL) up1l = c1[o];
+                if (pv1 && hR) up1r = c1[o + 1];
+                if (pv2 && hL) up2l = c2[o];
+                if (pv2 && hR) up2r = c2[o + 1];
+            }
             const int n = nb0 + (i - 1) + ks * (k - 1);
-            const bool hL = i >= 2, hR = i <= IMM1, hD = k >= 2, hU = k <= KMM1;
-            const int lo = (i - 2) + IMM1 * (k - 2), hi = lo + IMM1;    // cells (i-1, k-1) and (i-1, k)
-            auto gather = [&](float v, const float *cA, const float *cB, bool hA, bool hB, float fdn,
-                              float fup) -> float {
+            // node plane j0: cell planes j0 and j0 + 1
+            float v = dv0[q];
+            if (hD) {
+                if (hA0 && hL) v = v + dn0l * wtr[q] * fdn0;
+                if (hA0 && hR) v = v + dn0r * wtl[q] * fdn0;
+                if (hB0 && hL) v = v + dn1l * wtr[q] * fup0;
+                if (hB0 && hR) v = v + dn1r * wtl[q] * fup0;
+            }
+            if (hU) {
+                if (hA0 && hL) v = v + up0l * wbr[q] * fdn0;
+                if (hA0 && hR) v = v + up0r * wbl[q] * fdn0;
+                if (hB0 && hL) v = v + up1l * wbr[q] * fup0;
+                if (hB0 && hR) v = v + up1r * wbl[q] * fup0;
+            }
+            TM[n] = v;
+            if (two) {
+                // node plane j0 + 1: cell planes j0 + 1 and j0 + 2
+                float v1 = dv1[q];
                 if (hD) {
-                    if (hA && hL) v = v + cA[lo] * wtr[u] * fdn;
-                    if (hA && hR) v = v + cA[lo + 1] * wtl[u] * fdn;
-                    if (hB && hL) v = v + cB[lo] * wtr[u] * fup;
-                    if (hB && hR) v = v + cB[lo + 1] * wtl[u] * fup;
+                    if (hL) v1 = v1 + dn1l * wtr[q] * fdn1;
+                    if (hR) v1 = v1 + dn1r * wtl[q] * fdn1;
+                    if (hB1 && hL) v1 = v1 + dn2l * wtr[q] * fup1;
+                    if (hB1 && hR) v1 = v1 + dn2r * wtl[q] * fup1;
                 }
                 if (hU) {
-                    if (hA && hL) v = v + cA[hi] * wbr[u] * fdn;
-                    if (hA && hR) v = v + cA[hi + 1] * wbl[u] * fdn;
-                    if (hB && hL) v = v + cB[hi] * wbr[u] * fup;
-                    if (hB && hR) v = v + cB[hi + 1] * wbl[u] * fup;
+                    if (hL) v1 = v1 + up1l * wbr[q] * fdn1;
+                    if (hR) v1 = v1 + up1r * wbl[q] * fdn1;
+                    if (hB1 && hL) v1 = v1 + up2l * wbr[q] * fup1;
+                    if (hB1 && hR) v1 = v1 + up2r * wbl[q] * fup1;
                 }
-                return v;
-            };
-            // node plane j0: cell planes j0 (c0) and j0 + 1 (c1)
-            TM[n] = gather(dv0[u], c0, c1, hA0, hB0, fdn0, fup0);
-            if (!two) continue;
-            // node plane j0 + 1: cell planes j0 + 1 (c1) and j0 + 2 (c2)
-            TM[n + IM] = gather(dv1[u], c1, c2, true, hB1, fdn1, fup1);
+                TM[n + IM] = v1;
+            }
+            dn0l = up0l; dn0r = up0r; dn1l = up1l; dn1r = up1r; dn2l = up2l; dn2r = up2r;
         }
     }
 }
