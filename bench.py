@@ -61,6 +61,11 @@ WORKLOADS = {
                 "exit P/P0 in [0.45,0.70], 7000-10000 rpm (seeded), SCREE, mixing-length LOSS/5 steps"),
 }
 BATCH = 64
+# The default precision split (REDUCE_ORDER=0), as the JSON line names it
+REDUCTIONS = ("precision split (REDUCE_ORDER=0): FP32 field arithmetic; the long sums (multigrid blocks, row means, "
+              "mixing-plane averages, monitors) formed wide and rounded once: double-float FP32 pairs in the "
+              "TSTEP kernels, FP64 elsewhere")
+
 # Compulsory traffic of one LOOP iteration per node (FP32), every array read
 # once and written once: 5 state arrays r+w (40 B), 5 SCREE histories r+w
 # (40 B), 9 geometry arrays r (36 B), 4 body forces r (16 B).
@@ -450,7 +455,7 @@ def run_batch(args, rank, world, local_rank):
                            p: {str(b): [t[q] for t in tuned].count(b) for b in (128, 192, 256, 512)}
                            for q, p in enumerate(("ro_roe_pass", "momentum_pass"))}},
                        "l2": "flushed between timed steps", "parallelism": f"replicas: one batch per GPU x{world}",
-                       "reductions": "FP64 tree sums (REDUCE_ORDER=0)"},
+                       "reductions": REDUCTIONS},
             "roofline": {"bound": "hbm", "kernel": None, "peak": peak, "unit": "GB/s", "peak_source": peak_kind,
                          "step": {"alg_bytes_per_node_iter": B_ALG_STEP, "achieved": value / world * B_ALG_STEP,
                                   "frac": value / world * B_ALG_STEP / peak}},
@@ -838,7 +843,7 @@ def run_gpu(args, rank, world, local_rank):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOADS[ARGS_WORKLOAD][1], "nodes": N, "l2": "flushed between timed steps",
                        "parallelism": f"replicas: one instance per GPU x{world}",
-                       "reductions": "FP64 tree sums (REDUCE_ORDER=0)",
+                       "reductions": REDUCTIONS,
                        "autotune": {"tstep_threads_per_cta": {"ro_roe_pass": tuned[0], "momentum_pass": tuned[1]},
                                     "tstep_pass_ms": None if tune_ms is None else
                                     {p: dict(zip(("128", "192", "256", "512"), v)) for p, v in tune_ms.items()}}},
