@@ -791,6 +791,8 @@ void launch_flux_mom(const Dev &d, Launch L) {
 // flagged columns only.  The thread owning (IMID,KMID) then sets the
 // per-row Mach limits VLIMIT/ROLIMIT (7250) from its final densities.
 // ---------------------------------------------------------------------
+constexpr int DF_AHEAD = 16;     // J values a flagged column loads together in k_density_fix
+
 __global__ void k_density_fix(Dev d) {
     pdl_wait();
     int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -800,23 +802,39 @@ __global__ void k_density_fix(Dev d) {
     if (d.DFLAG[t]) {
         d.DFLAG[t] = 0;
         float ROLIM = d.ROLIM;
-        float rm2 = A3(RO, i, 1, k), rm1 = A3(RO, i, 2, k), r0 = A3(RO, i, 3, k);
-        float rp1 = A3(RO, i, 4, k);
-        for (int j = 3; j <= d.JM - 3; ++j) {
-            float rp2 = A3(RO, i, j + 2, k);
-            float ROAVG = 0.25f * (rm2 + rm1 + rp1 + rp2);
-            float ro = r0;
-            if (ro < 0.6f * ROAVG) ro = 0.5f * (ro + 0.6f * ROAVG);
-            if (ro > 1.5f * ROAVG) ro = 0.5f * (ro + 1.5f * ROAVG);
-            if (ro < ROLIM) ro = 0.5f * (ro + ROLIM);
-            if (ro != r0) {
-                A3(RO, i, j, k) = ro;
-                if (d.ADJ_FLAG) atomicOr(d.ADJ_FLAG, 1);
+        const int JM = d.JM, sJ = d.IM;
+        float *col = RO + (i - 1) + (size_t)sJ * JM * (k - 1);     // col[sJ * (j - 1)] = RO(i, j, k)
+        float rm2 = col[0], rm1 = col[sJ], r0 = col[2 * sJ];
+        float rp1 = col[3 * sJ];
+        // the walk reads RO(J+2) before any write reaches it, so the
+        // values ahead are loaded DF_AHEAD at a time: one memory latency
+        // per batch instead of one per J
+        for (int jb = 3; jb <= JM - 3; jb += DF_AHEAD) {
+            float ahead[DF_AHEAD];
+#pragma unroll
+            for (int q = 0; q < DF_AHEAD; ++q) {
+                const int jj = jb + 2 + q;
+                ahead[q] = jj <= JM ? col[sJ * (jj - 1)] : 0.0f;
             }
-            rm2 = rm1;
-            rm1 = ro;
-            r0 = rp1;
-            rp1 = rp2;
+#pragma unroll
+            for (int q = 0; q < DF_AHEAD; ++q) {
+                const int j = jb + q;
+                if (j > JM - 3) break;
+                float rp2 = ahead[q];
+                float ROAVG = 0.25f * (rm2 + rm1 + rp1 + rp2);
+                float ro = r0;
+                if (ro < 0.6f * ROAVG) ro = 0.5f * (ro + 0.6f * ROAVG);
+                if (ro > 1.5f * ROAVG) ro = 0.5f * (ro + 1.5f * ROAVG);
+                if (ro < ROLIM) ro = 0.5f * (ro + ROLIM);
+                if (ro != r0) {
+                    col[sJ * (j - 1)] = ro;
+                    if (d.ADJ_FLAG) atomicOr(d.ADJ_FLAG, 1);
+                }
+                rm2 = rm1;
+                rm1 = ro;
+                r0 = rp1;
+                rp1 = rp2;
+            }
         }
     }
     if (i == d.IMID && k == d.KMID) {
