@@ -222,7 +222,26 @@ class StagenInput:
     fac_scale: float
     rows: List[RowInput] = field(default_factory=list)
     pressures: tuple = ()                    # PUPHUB, PUPTIP, PDHUB, PDTIP
+    controls: Optional[dict] = None          # the IFDEF != 0 control block, by Stagen name
     inlet: Optional[dict] = None             # FSPAN, POIN, TOIN, VTIN, VMIN, B1IN, BRIN (1-based tables)
+
+
+# the IFDEF != 0 control block (Stagen-18.1.f:145-160), card by card
+_CONTROL_CARDS = (
+    ("ii", ("NMAX", "NCHANGE")),
+    ("i" * 14, ("IN_VTAN", "IN_PRESS", "INPUT", "IN_VR", "ITIMST", "ISMTH", "IPOUT", "IN_FLOW", "ILOS", "NLOS",
+                "IF_RESTART", "IOUTST", "IBOUND", "ISHIFT")),
+    ("i" * 11, ("IR", "JR", "KR", "IRBB", "JRBB", "KRBB", "NSBUP", "NSBON", "NSBDN", "IFMIX", "NEWGRID")),
+    ("iiii", ("JTRANS", "JTRANP", "JTRANH", "JTRANT")),
+    ("iiiiii", ("IF_CUSP", "ICUSP", "LCUSP", "LCUSPUP", "IFANGLES", "IF_DESIGN")),
+    ("r" * 7, ("CP", "GA", "CFL", "SFT", "SFX", "FAC_4TH", "MACHLIM")),
+    ("r" * 7, ("DAMP", "FBLK1", "FBLK2", "FBLK3", "SFEX", "CLIM", "RFIN")),
+    ("irrrrii", ("IFMIX", "RFMIX", "FSMTHB", "FEXTRAP", "FANGLE", "NEXTRAP_LE", "NEXTRAP_TE")),
+    ("r" * 10, ("FSTURB", "TURBVIS_DAMP", "TURBVIS_LIM", "REYNO", "PRANDTL", "RF_VIS", "FTRANS", "YPLUSWALL",
+                "YPLAM", "YPTURB")),
+    ("r" * 8, ("FAC_STMIX", "FAC_ST0", "FAC_ST1", "FAC_ST2", "FAC_ST3", "FAC_SFVIS", "FAC_VORT", "FAC_PGRAD")),
+    ("r" * 7, ("FRACPB", "FRACPW", "FRACPUP", "FRACPIN", "FRACPLE", "FRACPTE", "FRACPDWN")),
+)
 
 
 def _tab(vals) -> np.ndarray:
@@ -243,14 +262,20 @@ def read_stagen(text: str) -> StagenInput:
         fprat, fpmax = c.reals(2)
         frrat, frmax = c.reals(2)
         ifdef = c.ints(1)[0]
+        controls = None
         if ifdef != 0:
-            raise StagenError("IFDEF != 0 (the control-variable block) is not read")
+            # the control block (145-160); every card is one list-directed READ
+            controls = {}
+            for kinds, names in _CONTROL_CARDS:
+                for name, v in zip(names, c.mixed(kinds)):
+                    controls[name] = v
         nrows, nosect = c.ints(2)
         if km == 2 or im == 2:
             raise StagenError("quasi-3D (KM = 2) and throughflow (IM = 2) inputs are not generated")
         fac_scale = c.reals(1)[0]
         inp = StagenInput(float(rgas), float(gamma), im, km, fprat, fpmax, frrat, frmax, ifdef, nrows, nosect,
                           fac_scale)
+        inp.controls = controls
         for _ in range(nrows):
             c.skip()
             title = c.line().strip()
@@ -989,16 +1014,22 @@ def _ld(*items) -> str:
 
 def write_deck(inp: StagenInput, **overrides) -> str:
     """The MULTALL deck Stagen writes to stage_new.dat for this input
-    (IFDEF = 0: the control variables take Stagen's defaults, or those
-    given as keyword overrides by their Stagen names)."""
-    d = dict(DEFAULTS)
+    (IFDEF = 0: the control variables take Stagen's defaults; IFDEF != 0:
+    those of the input's control block, every variable it does not set
+    zero as in the reference, which then skips its defaults; keyword
+    overrides by Stagen name go on top)."""
+    if inp.controls is None:
+        d = dict(DEFAULTS)
+    else:
+        d = {k: 0 for k in DEFAULTS}
+        d.update({k: v for k, v in inp.controls.items() if k in d or k in ("CP", "GA")})
     for k, v in overrides.items():
         if k not in d:
             raise StagenError(f"unknown control variable {k}")
         d[k] = v
     im, km = inp.im, inp.km
-    gam = f32(inp.gamma)
-    cp = f32(f32(f32(inp.rgas) * gam) / f32(gam - f32(1.0)))
+    gam = f32(d.get("GA", inp.gamma))
+    cp = f32(d["CP"]) if "CP" in d else f32(f32(f32(inp.rgas) * gam) / f32(gam - f32(1.0)))
     fp = pitch_spacing(im, inp.fprat, inp.fpmax)
     fr = pitch_spacing(km, inp.frrat, inp.frmax)
     L: List[str] = []

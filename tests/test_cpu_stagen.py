@@ -102,9 +102,114 @@ def test_interpolation_helpers():
     assert list(sp) == pytest.approx([1.0, 1.25, 1.5, 1.5, 1.5, 1.5, 1.25, 1.0])
 
 
+# a one-row vane of this test's own, with Stagen's control-variable block
+# (IFDEF = 1), in Stagen's input layout
+SYNTHETIC_IFDEF = """287.5  1.4               RGAS, GAMMA
+ 37  37                  IM, KM
+ 1.25  20.0              FPRAT, FPMAX
+ 1.25  20.0              FRRAT, FRMAX
+ 1                       IFDEF
+ 4000  500               NMAX, NCHANGE
+ 0 0 2 1 3 0 1 0 10 5 0 1 0 2
+ 3 3 3 9 9 9 1 3 1 1 0
+ 0 0 0 0
+ 0 0 3 0 0 0
+ 1005.0 1.4 0.45 0.006 0.006 0.8 2.0
+ 10.0 0.4 0.2 0.1 0.0 0.001 0.5
+ 1 0.025 1.0 0.8 0.8 10 10
+ 1.0 0.5 1000.0 800000.0 1.0 0.5 0.0001 0.0 5.0 25.0
+ 0.0 1.0 1.0 1.0 1.0 2.0 0.0 0.0
+ 0.05 0.05 0.03 0.02 0.03 0.03 0.04
+ 1  2                    NROWS, NOSECT
+ 1.0                     scale
+blank
+ VANE ROW
+blank
+ 20  60  20
+ 0.0    1.0
+ 0.5    1.2
+ 1.001  1.0
+ 50
+ 0.0  100000.  100000.  90000.  90000.
+ 0  0  10  70  10  70  0.0  0.0
+blank
+ HUB SECTION
+blank
+ 1
+ 5  200  2
+ 0.0    0.0
+ 0.25  10.0
+ 0.5   25.0
+ 0.75  40.0
+ 1.0   55.0
+ 0.02  0.01  0.10  0.40  0.05  0.02  2.0
+ 0.0  0.0  1.0
+ 0.0  0.5  0.5
+ 0.5  0.5  0.0  55.0
+blank
+ 2
+ -0.1  0.2
+  0.5  0.5
+ 0.0  0.05  0.5  0.5
+ 0.0  0.0  0  0  0
+ 1.0  0
+blank
+ TIP SECTION
+blank
+ 1
+ 5  200  2
+ 0.0    0.0
+ 0.25  12.0
+ 0.5   28.0
+ 0.75  44.0
+ 1.0   60.0
+ 0.02  0.01  0.08  0.40  0.05  0.02  2.0
+ 0.0  0.0  1.0
+ 0.0  0.5  0.5
+ 0.5  0.5  0.0  60.0
+blank
+ 2
+ -0.1  0.2
+  0.6  0.6
+ 0.0  0.05  0.6  0.6
+ 1.0  0.0  0  0  0
+ 1.0  0
+blank
+ 95000.  95000.  90000.  90000.
+blank
+ 2
+ 0.0  1.0
+ 100000.  100000.
+ 300.  300.
+ 0.0  0.0
+ 100.  100.
+ 0.0  0.0
+ 0.0  0.0
+"""
+
+
+def test_control_block_input():
+    """IFDEF != 0: the control cards are read by name, the deck carries
+    them, and the variables the block does not set are zero (Stagen skips
+    its defaults then)."""
+    from mgpu import deck, stagen
+    inp = stagen.read_stagen(SYNTHETIC_IFDEF)
+    assert inp.controls["NMAX"] == 4000 and inp.controls["ILOS"] == 10
+    assert inp.controls["CFL"] == pytest.approx(0.45) and inp.controls["TURBVIS_LIM"] == pytest.approx(1000.0)
+    g = stagen.generate_row(inp.rows[0], inp.km)
+    assert (g.jm, g.jle, g.jte) == (101, 21, 81)
+    assert np.all(np.isfinite(np.concatenate(g.x + g.y + g.tk + g.r)))
+    assert g.tk[0].max() == pytest.approx(0.05 * 0.10, rel=0.01)    # TKMAX of the axial chord x its length
+    text = stagen.write_deck(inp)
+    spec, geo = deck.read_deck(text)
+    assert spec.nsteps_max == 4000 and spec.cfl == pytest.approx(0.45) and spec.cp == pytest.approx(1005.0)
+    assert geo.jm == 101 and spec.ilos == 10
+    assert "FACTOR TO INCREASE" in text and text.rstrip().endswith("0")   # FACMIXUP, NMIXUP left at zero
+
+
 def test_unsupported_inputs_are_refused():
     from mgpu import stagen
     with pytest.raises(stagen.StagenError):
         stagen.read_stagen("287.5 1.4\n37 2\n1.2 5\n1.2 5\n0\n1 2\n1.0\n")
     with pytest.raises(stagen.StagenError):
-        stagen.read_stagen("287.5 1.4\n37 37\n1.2 5\n1.2 5\n1\n")
+        stagen.read_stagen("287.5 1.4\n37 37\n1.2 5\n1.2 5\n1\n")      # the control block ends early
