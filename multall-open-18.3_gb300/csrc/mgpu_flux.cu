@@ -791,7 +791,7 @@ void launch_flux_mom(const Dev &d, Launch L) {
 // flagged columns only.  The thread owning (IMID,KMID) then sets the
 // per-row Mach limits VLIMIT/ROLIMIT (7250) from its final densities.
 // ---------------------------------------------------------------------
-constexpr int DF_AHEAD = 16;     // J values a flagged column loads together in k_density_fix
+constexpr int DF_AHEAD = 64;     // J values a flagged column loads together in k_density_fix
 
 __global__ void k_density_fix(Dev d) {
     pdl_wait();
