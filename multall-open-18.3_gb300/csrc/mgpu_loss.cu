@@ -774,33 +774,43 @@ __global__ void k_tail_vref(Dev d, int nparts) {
     }
 }
 
+// Each thread of k_tail_dvm takes TAIL_NPT nodes (TAIL_BS apart, so the
+// loads stay coalesced) and adds their |DVMER| in FP32 before the FP64 tree:
+// GB300 issues few FP64 instructions per clock, and a tree per node kept
+// the kernel on the FP64 pipe.
+constexpr int TAIL_NPT = 8;
+
 __global__ void __launch_bounds__(TAIL_BS) k_tail_dvm(Dev d) {
     pdl_wait();
     const DevCtl *c = d.ctl;
     if (!c->do_tail) return;
-    size_t n = (size_t)blockIdx.x * TAIL_BS + threadIdx.x;
-    size_t N = (size_t)d.IM * d.JM * d.KM;
-    double s = 0.0;
+    const int N = d.IM * d.JM * d.KM;                   // below 2^31: commit limits the node count
+    const float RVEF = 100.0f / c->VREF;
+    float sf = 0.0f;
     unsigned long long key = 0ull;
     int bad = 0;
-    if (n < N) {
-        int i, j, k;
-        node_ijk(d, n, i, j, k);
+#pragma unroll 2
+    for (int u = 0; u < TAIL_NPT; ++u) {
+        const int n = ((int)blockIdx.x * TAIL_NPT + u) * TAIL_BS + (int)threadIdx.x;
+        if (n >= N) break;
+        const int jk = n / d.IM;                         // (j-1) + JM*(k-1)
+        const bool jin = jk % d.JM != 0;                 // j >= 2
         float ro = d.RO[n];
         if (!isfinite(ro) || !(ro > 0.0f) || !isfinite(d.ROE[n]) || !isfinite(d.ROVX[n]) || !isfinite(d.ROVR[n]) ||
             !isfinite(d.RORVT[n]))
-            bad = 1;
-        if (j >= 2) {
-            float RVEF = 100.0f / c->VREF;
-            float XD = A2(d.DX, j, k), RD = A2(d.DR, j, k), SD = A2(d.DS, j, k);
+            bad += 1;
+        if (jin) {
+            float XD = d.DX[jk], RD = d.DR[jk], SD = d.DS[jk];
             float VM_START = (XD * d.VX[n] + RD * d.VR[n]) / SD;
             float VM_END = (XD * d.ROVX[n] + RD * d.ROVR[n]) / SD / ro;
             float DVMER = (VM_END - VM_START) * RVEF;
             d.STORE[n] = DVMER;
-            s = (double)fabsf(DVMER);
-            key = max_key(fabsf(DVMER), n);
+            sf += fabsf(DVMER);
+            const unsigned long long kn = max_key(fabsf(DVMER), (size_t)n);
+            key = kn > key ? kn : key;
         }
     }
+    double s = (double)sf;
     __shared__ double ss[TAIL_BS / 32];
     __shared__ unsigned long long sk[TAIL_BS / 32];
     __shared__ int sc[TAIL_BS / 32];
@@ -847,28 +857,44 @@ __global__ void k_tail_final(Dev d, int nparts) {
         key = k2 > key ? k2 : key;
         bad += d.part_cnt[p];
     }
+    // the continuity error ECONT = max over J of |1 - FLOW(J)/FLOW(1)| and
+    // the first J that reaches it, one J per thread as a (value, J) key
+    unsigned long long ek = 0ull;
+    const float cf1f = (float)d.BLADE_FLOW[0];
+    for (int j = threadIdx.x + 1; j <= d.JM; j += blockDim.x) {
+        float RATIO = (float)d.BLADE_FLOW[j - 1] / cf1f;
+        float EMASS = fabsf(1.0f - RATIO);
+        if (EMASS > 0.0f) {
+            const unsigned long long kj = max_key(EMASS, (size_t)(j - 1));
+            ek = kj > ek ? kj : ek;
+        }
+    }
     __shared__ double ss[32];
-    __shared__ unsigned long long sk[32];
+    __shared__ unsigned long long sk[32], se[32];
     __shared__ int sc[32];
     for (int o = 16; o > 0; o >>= 1) {
         s = racc(ro, s, __shfl_down_sync(0xffffffffu, s, o));
         unsigned long long ok = __shfl_down_sync(0xffffffffu, key, o);
         key = ok > key ? ok : key;
+        unsigned long long oe = __shfl_down_sync(0xffffffffu, ek, o);
+        ek = oe > ek ? oe : ek;
         bad += __shfl_down_sync(0xffffffffu, bad, o);
     }
     if ((threadIdx.x & 31) == 0) {
         ss[threadIdx.x >> 5] = s;
         sk[threadIdx.x >> 5] = key;
+        se[threadIdx.x >> 5] = ek;
         sc[threadIdx.x >> 5] = bad;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         double t = 0.0;
-        unsigned long long kk = 0ull;
+        unsigned long long kk = 0ull, ke = 0ull;
         int cnt = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
             t = racc(ro, t, ss[w]);
             kk = sk[w] > kk ? sk[w] : kk;
+            ke = se[w] > ke ? se[w] : ke;
             cnt += sc[w];
         }
         c->mon.eavg_sum = t;
@@ -883,17 +909,13 @@ __global__ void k_tail_final(Dev d, int nparts) {
             c->EMAX = 0.0f;
         }
         c->health = cnt;
-        // continuity error ECONT and its station
-        double cf1 = d.BLADE_FLOW[0];
+        // continuity error ECONT and its station (the reference's J loop
+        // keeps the first J of the largest value; none above 0 keeps JCONT)
         float econt = 0.0f;
         int jc = c->JCONT;
-        for (int j = 1; j <= d.JM; ++j) {
-            float RATIO = (float)d.BLADE_FLOW[j - 1] / (float)cf1;
-            float EMASS = fabsf(1.0f - RATIO);
-            if (EMASS > econt) {
-                econt = EMASS;
-                jc = j;
-            }
+        if (ke) {
+            econt = __uint_as_float((unsigned)(ke >> 32));
+            jc = (int)(0xFFFFFFFFu - (unsigned)(ke & 0xFFFFFFFFull)) + 1;
         }
         c->ECONT = econt;
         c->CHECK_FLOW_JM = (float)d.BLADE_FLOW[d.JM - 1];   // CHECK_FLOW(JM) for the throttle
@@ -912,7 +934,7 @@ void launch_tail(const Dev &d, Launch L) {
     int prim_parts = (int)grid_for(N, 256);
     launchk(L, k_tail_vref, dim3(1), dim3(1024), 0, d, prim_parts);
     mark(L, "k_tail_vref");
-    int parts = (int)grid_for(N, TAIL_BS);
+    int parts = (int)grid_for(N, (size_t)TAIL_BS * TAIL_NPT);
     launchk(L, k_tail_dvm, dim3(parts), dim3(TAIL_BS), 0, d);
     mark(L, "k_tail_dvm");
     launchk(L, k_tail_final, dim3(1), dim3(1024), 0, d, parts);
