@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(32) k_pwallgrad_smooth(const __grid_constant__
 // transition scans run one thread per column in the reference's order.
 // ---------------------------------------------------------------------
 constexpr int LK_W = 8;            // warps per CTA (K stride)
-constexpr int LK_NARR = 10;        // [K][32] arrays in shared memory (+ RAVG per K)
+constexpr int LK_NARR = 8;         // [K][32] arrays in shared memory (+ RAVG per K): 4 CTAs per SM at KM = 49
 
 __global__ void __launch_bounds__(32 * LK_W) k_loss_kfaces(const __grid_constant__ Dev d, int init_call) {
     pdl_wait();
@@ -236,8 +236,8 @@ __global__ void __launch_bounds__(32 * LK_W) k_loss_kfaces(const __grid_constant
     const bool col = i <= d.IMM1;
     // [K][32] arrays, row k-1
     float *AREA = lsm, *VXAVG = AREA + KM * 32, *VRAVG = VXAVG + KM * 32, *VTAVG = VRAVG + KM * 32;
-    float *ROAVG = VTAVG + KM * 32, *TAVG = ROAVG + KM * 32, *WABS = TAVG + KM * 32, *YP = WABS + KM * 32;
-    float *VLAM = YP + KM * 32, *VTURB = VLAM + KM * 32, *RAVGK = VTURB + KM * 32;   // RAVGK: [K] only
+    float *ROAVG = VTAVG + KM * 32, *TAVG = ROAVG + KM * 32;
+    float *VLAM = TAVG + KM * 32, *VTURB = VLAM + KM * 32, *RAVGK = VTURB + KM * 32;   // RAVGK: [K] only
     __shared__ float s_vis[32], s_ftc[32], s_tw1[32], s_twm[32];
     __shared__ float s_w1[32][4], s_wm[32][4];     // wall-face xs, rs, ts, wv at K=1 and K=KM
 #define LK(a, k) a[((k) - 1) * 32 + tx]
@@ -261,9 +261,6 @@ __global__ void __launch_bounds__(32 * LK_W) k_loss_kfaces(const __grid_constant
         LK(ROAVG, k) = 0.25f * (A3(d.RO, i, j, k) + A3(d.RO, i, j - 1, k) + A3(d.RO, i + 1, j, k) + A3(d.RO, i + 1, j - 1, k));
         LK(TAVG, k) = 0.25f * (A3(d.T_STATIC, i, j, k) + A3(d.T_STATIC, i, j - 1, k) + A3(d.T_STATIC, i + 1, j, k) +
                                A3(d.T_STATIC, i + 1, j - 1, k));
-        float WTAVG = vt - WREL * RAVG;
-        float WABSQ = vx * vx + vr * vr + WTAVG * WTAVG;
-        LK(WABS, k) = sqrtf(WABSQ);
     }
     __syncthreads();
     // 2. viscosity and wall shear stresses, one thread per column
@@ -339,21 +336,28 @@ __global__ void __launch_bounds__(32 * LK_W) k_loss_kfaces(const __grid_constant
             float y = k <= KMID ? VS1 * PERP * LK(ROAVG, 1) / VISLAM : VSM * PERP * LK(ROAVG, KM) / VISLAM;
             y = fminf(y, 1000.0f);
             A3(d.Y_PLUS, i, j, k) = y;
-            LK(YP, k) = y;
         }
     }
     __syncthreads();
-    // 4. laminar and mixing-length viscosities of the interior faces
+    // 4. laminar and mixing-length viscosities of the interior faces.  The
+    //    relative speed of the faces is formed again here, and Y_PLUS is read
+    //    back from this CTA's own stores of step 3 (visible after the
+    //    barrier): two K-arrays fewer in shared memory lets four CTAs share
+    //    an SM
+    auto wabs = [&](int kq) {
+        float WTAVG = LK(VTAVG, kq) - WREL * RAVGK[kq - 1];
+        return sqrtf(LK(VXAVG, kq) * LK(VXAVG, kq) + LK(VRAVG, kq) * LK(VRAVG, kq) + WTAVG * WTAVG);
+    };
     if (col) {
         const float VISLAM = s_vis[tx];
         for (int k = ty + 2; k <= KMM1; k += LK_W) {
             // FYPLUS keeps its previous value where Y_PLUS is NaN
             int kk = k;
-            while (kk >= 2 && isnan(LK(YP, kk))) --kk;
-            float FYPLUS = kk >= 2 ? fyplus_of(LK(YP, kk), d.YPLAM, d.YPTURB, 0.0f) : 0.0f;
+            while (kk >= 2 && isnan(A3(d.Y_PLUS, i, j, kk))) --kk;
+            float FYPLUS = kk >= 2 ? fyplus_of(A3(d.Y_PLUS, i, j, kk), d.YPLAM, d.YPTURB, 0.0f) : 0.0f;
             float DPERP = A3(d.VOL, i, j, k) / LK(AREA, k);
             LK(VLAM, k) = d.FKLAM[(size_t)(NRW - 1) * KM + k - 1] * VISLAM / DPERP;
-            float vt = d.FKTURB[(size_t)(NRW - 1) * KM + k - 1] * LK(ROAVG, k) * fabsf(LK(WABS, k + 1) - LK(WABS, k - 1)) *
+            float vt = d.FKTURB[(size_t)(NRW - 1) * KM + k - 1] * LK(ROAVG, k) * fabsf(wabs(k + 1) - wabs(k - 1)) *
                        FMIXUP;
             LK(VTURB, k) = vt * FYPLUS;
         }
@@ -420,7 +424,7 @@ __global__ void __launch_bounds__(32 * LK_W) k_loss_kfaces(const __grid_constant
 // LOSS DO 100 (8566-9044).  One warp per (J,K) line; the lanes cover I (coalesced), the
 // line's arrays sit in this warp's slice of shared memory.
 // ---------------------------------------------------------------------
-constexpr int LI_W = 4;            // warps (lines) per CTA
+constexpr int LI_W = 4;            // warps (lines) per CTA; 64 registers: 8 CTAs per SM
 constexpr int LI_NARR = 16;        // per-line arrays of IM+1 floats
 
 // Transition test of one wall's mixing-length viscosity (LOSS 8481-8510,
@@ -453,7 +457,7 @@ __device__ inline bool transition_warp(const float *vt, const float *vl, int a, 
     return any;
 }
 
-__global__ void __launch_bounds__(32 * LI_W) k_loss_ifaces(const __grid_constant__ Dev d, int init_call) {
+__global__ void __launch_bounds__(32 * LI_W, 8) k_loss_ifaces(const __grid_constant__ Dev d, int init_call) {
     pdl_wait();
     const DevCtl *c = d.ctl;
     if (!init_call && !c->do_loss) return;
