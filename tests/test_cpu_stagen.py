@@ -213,3 +213,71 @@ def test_unsupported_inputs_are_refused():
         stagen.read_stagen("287.5 1.4\n37 2\n1.2 5\n1.2 5\n0\n1 2\n1.0\n")
     with pytest.raises(stagen.StagenError):
         stagen.read_stagen("287.5 1.4\n37 37\n1.2 5\n1.2 5\n1\n")      # the control block ends early
+
+
+def _turbine_section():
+    from mgpu import stagen
+    inp = _input("stagen-single-stg-turbine")
+    return inp, inp.rows[0], inp.rows[0].sections[0]
+
+
+def test_coordinate_input_reproduces_the_generated_section():
+    """INTYPE 0 (blade coordinates read in) fed with the surface points an
+    INTYPE 1 section generates gives the same section on the grid: the
+    rescaling to unit axial chord is the only step between them."""
+    import copy
+    from mgpu import stagen
+    inp, row, s1 = _turbine_section()
+    nin, xs, ys, _ = stagen._generated_surface(s1)
+    s0 = copy.copy(s1)
+    s0.intype = 0
+    s0.xyin = (xs[:nin + 1].copy(), ys[:nin + 1].copy(), 0, 0)
+    r1 = copy.copy(row)
+    r1.sections = [s1]
+    r0 = copy.copy(row)
+    r0.sections = [s0]
+    g1 = stagen.generate_row(r1, inp.km)
+    g0 = stagen.generate_row(r0, inp.km)
+    chord = float(g1.x[0][g1.jte - 1] - g1.x[0][g1.jle - 1])
+    for key in ("x", "y", "tk", "r"):
+        a, b = getattr(g0, key)[0], getattr(g1, key)[0]
+        assert np.max(np.abs(a - b)) <= 1e-4 * chord, key
+
+
+@pytest.mark.parametrize("intype", [2, 3])
+def test_thickness_and_surface_slope_inputs(intype):
+    """INTYPE 2 (camber slopes with thicknesses above and below) and INTYPE 3
+    (the two surface slopes), on a turbine vane: a closed section whose
+    tangential thickness peaks at TKMAX of the meridional chord (FTKSCALE = 1
+    scales it there) and vanishes off the blade."""
+    import copy
+    from mgpu import stagen
+    f32 = np.float32
+    inp, row, s1 = _turbine_section()
+    s = copy.copy(s1)
+    s.intype = intype
+    npin = len(s1.fracx) - 1
+    x = s1.fracx[1:]
+    half = f32(0.5) * np.sin(np.pi * x).astype(f32) * f32(0.1)       # a thickness shape; rescaled to TKMAX
+    if intype == 2:
+        s.tkh = stagen._tab(half)
+        s.tkl = stagen._tab(half)
+    else:
+        slope = s1.slope[1:]
+        dt = np.gradient(half.astype(np.float64), x.astype(np.float64)).astype(f32)
+        s.slpup = stagen._tab(slope + dt)
+        s.slplow = stagen._tab(slope - dt)
+        s.slope = np.zeros(npin + 1, f32)
+    s.fchord = (f32(0.0), f32(0.0), f32(1.0))
+    r = copy.copy(row)
+    r.sections = [s]
+    g = stagen.generate_row(r, inp.km)
+    tk = g.tk[0]
+    assert np.all(np.isfinite(np.concatenate([g.x[0], g.y[0], tk, g.r[0]])))
+    chord = float(g.x[0][g.jte - 1] - g.x[0][g.jle - 1])
+    # the 4-point interpolation onto the grid may undershoot zero at the
+    # rounded trailing edge by a few millionths of the chord, as Stagen's does
+    assert np.all(tk >= -1e-4 * chord)
+    assert np.all(tk[:g.jle - 1] == 0.0) and np.all(tk[g.jte + 1:] == 0.0)
+    tkmax = float(s.thick[2])
+    assert tk.max() == pytest.approx(tkmax * chord, rel=0.05)
