@@ -51,7 +51,7 @@ extern "C" {
 #define MGPU_E_ARG          -1  /* bad argument, unknown name, size mismatch   */
 #define MGPU_E_STATE        -2  /* call out of order (e.g. step before commit) */
 #define MGPU_E_CUDA         -3  /* CUDA runtime error                          */
-#define MGPU_E_UNSUPPORTED  -4  /* an input option this build does not cover   */
+#define MGPU_E_UNSUPPORTED  -4  /* an input option the library does not cover */
 #define MGPU_E_NONFINITE    -5  /* health check: NaN/Inf or RO <= 0 found      */
 #define MGPU_E_NOMEM        -6  /* device allocation failed                    */
 

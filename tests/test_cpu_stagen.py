@@ -281,3 +281,21 @@ def test_thickness_and_surface_slope_inputs(intype):
     assert np.all(tk[:g.jle - 1] == 0.0) and np.all(tk[g.jte + 1:] == 0.0)
     tkmax = float(s.thick[2])
     assert tk.max() == pytest.approx(tkmax * chord, rel=0.05)
+
+
+@pytest.mark.parametrize("name", ["stagen-single-stg-turbine", "stagen-18.1-intype=4-test"])
+def test_written_deck_steps_in_the_oracle(name):
+    """Stagen input -> deck -> the test-side SETUP -> five oracle steps: a
+    finite, positive density field and a falling residual."""
+    import oracle as O
+    from mgpu import common_setup, deck, stagen
+    inp = _input(name)
+    spec, geo = deck.read_deck(stagen.write_deck(inp))
+    cd = common_setup.build_common(spec, geo)
+    ref = O.Oracle(cd)
+    ref.setup_calls()
+    for _ in range(5):
+        m = ref.step()
+    ro = ref.get("RO", double=False)
+    assert np.all(np.isfinite(ro)) and ro.min() > 0.0
+    assert np.isfinite(m.eavg) and m.eavg > 0.0
