@@ -717,7 +717,7 @@ def _expansion(r, npts, up: bool):
     rat = f32(1.2)
     if r < npts:
         rat = f32(0.9)
-    for _ in range(49):
+    for _ in range(50):
         rhs = f32(f32(rat - f32(1.0)) * r)
         if r >= npts:
             rat = f32(f32(0.5) * f32(rat + f32(np.power(f32(rhs + f32(1.0)), f32(f32(1.0) / f32(npts))))))

@@ -14,13 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = os.path.join(HERE, "golden", "stagen")
 
 # the decks print F10.6: half a unit in the sixth decimal, plus the float32
-# rounding of values up to ~4 and of the REAL*4 transcendentals
-TOL = 2.5e-6
-# the centrifugal compressor's deck differs from this Stagen in the far
-# upstream point and the exit radius of its first row (a radial stream
-# surface extrapolated by the 4-point Lagrange INTP); every other value is
-# within TOL
-TOL_BY_INPUT = {"stagen-centrif-compr": 2e-4}
+# rounding of values up to ~2 and of the REAL*4 transcendentals
+TOL = 1.5e-6
 
 INPUTS = sorted(f[:-5] for f in os.listdir(GOLD) if f.endswith(".json")) if os.path.isdir(GOLD) else []
 PAIRED = [n for n in INPUTS if os.path.exists(os.path.join(GOLD, n + "_deck.npz"))]
@@ -36,7 +31,7 @@ def test_generated_sections_equal_the_reference_decks(name):
     from mgpu import stagen
     inp = _input(name)
     ref = np.load(os.path.join(GOLD, name + "_deck.npz"))
-    tol = TOL_BY_INPUT.get(name, TOL)
+    tol = TOL
     worst = 0.0
     n = 0
     for nr, row in enumerate(inp.rows, start=1):
