@@ -1279,3 +1279,33 @@ def input_from_dict(d: dict) -> StagenInput:
             row.sections.append(s)
         inp.rows.append(row)
     return inp
+
+
+def case_from_input(inp: StagenInput, **overrides):
+    """(CaseSpec, CaseGeometry) of the machine: the deck Stagen writes for
+    the input, read as MULTALL reads it (mgpu.deck)."""
+    from . import deck as _deck
+    return _deck.read_deck(write_deck(inp, **overrides))
+
+
+def main(argv=None) -> int:
+    """As the reference's program runs: read a Stagen input file and write
+    the new-format deck (stage_new.dat by default)."""
+    import argparse
+    ap = argparse.ArgumentParser(description="Stagen: blade-design input -> MULTALL deck")
+    ap.add_argument("input", help="Stagen input file (e.g. stagen.dat)")
+    ap.add_argument("-o", "--output", default="stage_new.dat", help="deck to write")
+    args = ap.parse_args(argv)
+    with open(args.input) as f:
+        inp = read_stagen(f.read())
+    text = write_deck(inp)
+    with open(args.output, "w") as f:
+        f.write(text)
+    jms = [r.nintup + r.ninton + 1 + r.nintdn for r in inp.rows]
+    print(f"{args.output}: {inp.nrows} rows, IM = {inp.im}, JM = {sum(jms)}, KM = {inp.km}")
+    return 0
+
+
+if __name__ == "__main__":
+    import sys
+    sys.exit(main())

@@ -294,3 +294,15 @@ def test_written_deck_steps_in_the_oracle(name):
     ro = ref.get("RO", double=False)
     assert np.all(np.isfinite(ro)) and ro.min() > 0.0
     assert np.isfinite(m.eavg) and m.eavg > 0.0
+
+
+def test_command_line_writes_the_deck(tmp_path):
+    """python -m mgpu.stagen input -o deck: the deck write_deck gives."""
+    from mgpu import stagen
+    src = tmp_path / "stagen.dat"
+    src.write_text(SYNTHETIC_IFDEF)
+    out = tmp_path / "stage_new.dat"
+    assert stagen.main([str(src), "-o", str(out)]) == 0
+    assert out.read_text() == stagen.write_deck(stagen.read_stagen(SYNTHETIC_IFDEF))
+    spec, geo = stagen.case_from_input(stagen.read_stagen(SYNTHETIC_IFDEF))
+    assert geo.jm == 101
